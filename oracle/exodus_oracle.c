@@ -1,0 +1,1352 @@
+/*
+ * CPU restatement of sif's exodus void-finder path (see exodus_oracle.h).
+ * TEST INFRASTRUCTURE ONLY: the parity checker and the timed CPU baseline.
+ *
+ * Compiled with -ffp-contract=off: every float expression below is evaluated
+ * in the written order with one rounding per operation, which is what the
+ * reference computes in a strict IEEE build. Where the reference's order of
+ * evaluation is part of the answer (the filter table, the distance, the skip
+ * and crossing tests) the expression is written in that order and cited.
+ */
+#include "exodus_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "fftw_shim/fftw3.h"
+
+#ifdef _OPENMP
+#  include <omp.h>
+#endif
+
+#define PI_F ((float)3.14159265358979323846)
+
+/* ------------------------------------------------------------------------ */
+/* Box folding and the chain mesh                                           */
+/* ------------------------------------------------------------------------ */
+
+/* sif__box_fold, src/structures/field_internal.h:58-64. */
+static inline float box_fold(float v, float box) {
+  if (v >= box)
+    v -= box;
+  else if (v < 0)
+    v += box;
+  return v >= box ? 0.0f : v;
+}
+
+/* chain_mesh_flat_idx, src/structures/chain_mesh.c:316-331. */
+static inline uint64_t mesh_cell_of(
+  float x, float y, float z, float inv_l, uint32_t n, float box) {
+  int32_t ix = (int32_t)(box_fold(x, box) * inv_l);
+  int32_t iy = (int32_t)(box_fold(y, box) * inv_l);
+  int32_t iz = (int32_t)(box_fold(z, box) * inv_l);
+  const int32_t hi = (int32_t)n - 1;
+  ix = ix < 0 ? 0 : (ix > hi ? hi : ix);
+  iy = iy < 0 ? 0 : (iy > hi ? hi : iy);
+  iz = iz < 0 ? 0 : (iz > hi ? hi : iz);
+  return (uint64_t)ix * n * n + (uint64_t)iy * n + (uint64_t)iz;
+}
+
+/* The mesh of chain_mesh_create + chain_mesh_canonicalise
+ * (src/structures/chain_mesh.c:680-832, 420-542): counts per cell, offsets,
+ * and each cell in ascending source index -- which a stable counting sort
+ * gives directly. The box check of chain_mesh_new (field.c:889-935) is the
+ * caller's; coordinates are folded as the scatter folds them. */
+int orc_chain_mesh(const float* x, const float* y, const float* z, uint64_t n,
+  uint32_t n_cells, float box, float* ox, float* oy, float* oz,
+  uint64_t* offsets, uint64_t* orig) {
+  if (n_cells == 0 || !(box > 0.0f))
+    return -2;
+  const uint64_t total = (uint64_t)n_cells * n_cells * n_cells;
+  const float cell_length = box / (float)n_cells;
+  const float inv_l = 1.0f / cell_length;
+  uint64_t* cell = malloc(n * sizeof(uint64_t));
+  if (!cell)
+    return -1;
+  memset(offsets, 0, (total + 1) * sizeof(uint64_t));
+  for (uint64_t i = 0; i < n; i++) {
+    cell[i] = mesh_cell_of(x[i], y[i], z[i], inv_l, n_cells, box);
+    offsets[cell[i] + 1]++;
+  }
+  for (uint64_t c = 0; c < total; c++)
+    offsets[c + 1] += offsets[c];
+  uint64_t* cursor = malloc(total * sizeof(uint64_t));
+  if (!cursor) {
+    free(cell);
+    return -1;
+  }
+  memcpy(cursor, offsets, total * sizeof(uint64_t));
+  for (uint64_t i = 0; i < n; i++) {
+    const uint64_t pos = cursor[cell[i]]++;
+    ox[pos] = box_fold(x[i], box);
+    oy[pos] = box_fold(y[i], box);
+    oz[pos] = box_fold(z[i], box);
+    if (orig)
+      orig[pos] = i;
+  }
+  free(cursor);
+  free(cell);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* CIC and the density contrast                                             */
+/* ------------------------------------------------------------------------ */
+
+/* The CIC deposit of grid_compute_cic (src/structures/grid.c:455-746) in
+ * double: base cell (uint32)(fold(x) * N/L) with the >= N fallback to 0,
+ * weights (1 - t, t), periodic upper neighbours, divided by the cell volume.
+ */
+void orc_cic_f64(const float* x, const float* y, const float* z, uint64_t n,
+  uint32_t N, float box, double* out) {
+  const uint64_t total = (uint64_t)N * N * N;
+  memset(out, 0, total * sizeof(double));
+  const double idx = (double)N / (double)box;
+  for (uint64_t p = 0; p < n; p++) {
+    const double u[3] = {(double)box_fold(x[p], box) * idx,
+      (double)box_fold(y[p], box) * idx, (double)box_fold(z[p], box) * idx};
+    uint32_t i0[3], i1[3];
+    double w0[3], w1[3];
+    for (int a = 0; a < 3; a++) {
+      const uint32_t raw = (uint32_t)u[a];
+      i0[a] = raw >= N ? 0u : raw;
+      i1[a] = i0[a] + 1 == N ? 0u : i0[a] + 1;
+      const double t = u[a] - (double)raw;
+      w0[a] = 1.0 - t;
+      w1[a] = t;
+    }
+    for (int a = 0; a < 2; a++)
+      for (int b = 0; b < 2; b++)
+        for (int c = 0; c < 2; c++) {
+          const uint64_t cell =
+            ((uint64_t)(a ? i1[0] : i0[0]) * N + (b ? i1[1] : i0[1])) * N +
+            (c ? i1[2] : i0[2]);
+          out[cell] += (a ? w1[0] : w0[0]) * (b ? w1[1] : w0[1]) *
+                       (c ? w1[2] : w0[2]);
+        }
+  }
+  const double cl = (double)box / (double)N;
+  const double inv_vol = 1.0 / (cl * cl * cl);
+  for (uint64_t i = 0; i < total; i++)
+    out[i] *= inv_vol;
+}
+
+/* sif_grid_to_density_contrast, src/structures/grid.c:1177-1244: the mean in
+ * 64 fixed blocks of double, then v * (float)(1/mean) - 1 in float. */
+int orc_density_contrast(float* v, uint64_t n) {
+  const int blocks = 64;
+  const uint64_t block = (n + blocks - 1) / blocks;
+  double total = 0.0;
+  for (int b = 0; b < blocks; b++) {
+    const uint64_t s = (uint64_t)b * block;
+    const uint64_t e = s + block < n ? s + block : n;
+    double sum = 0.0;
+    for (uint64_t i = s; i < e; i++)
+      sum += (double)v[i];
+    total += sum;
+  }
+  const double mean = total / (double)n;
+  if (!(mean > 0.0))
+    return -3;
+  const float inv = (float)(1.0 / mean);
+  for (uint64_t i = 0; i < n; i++)
+    v[i] = v[i] * inv - 1.0f;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Smoothing                                                                */
+/* ------------------------------------------------------------------------ */
+
+struct orc_spectrum {
+  uint32_t n;
+  float box;
+  int mode;
+  fftw_complex* spec; /* n * n * (n/2+1) */
+  double* window;     /* per-axis factor, or NULL */
+};
+
+/* x = pi k / N for index i (src/math/fft.c:939-943), with the reference's
+ * float pi in the float mode. */
+static double axis_x(uint32_t i, uint32_t n, int mode) {
+  const uint32_t h = n >> 1;
+  const int32_t k = i > h ? (int32_t)i - (int32_t)n : (int32_t)i;
+  const double pi = mode ? (double)PI_F : M_PI;
+  return pi * (double)k / (double)n;
+}
+
+orc_spectrum_t* orc_spectrum_new(
+  const float* delta, uint32_t n, float box, int window_mode, int mode) {
+  orc_spectrum_t* s = calloc(1, sizeof(*s));
+  s->n = n;
+  s->box = box;
+  s->mode = mode;
+  const uint64_t total = (uint64_t)n * n * n;
+  const uint64_t modes = (uint64_t)n * n * (n / 2 + 1);
+  double* in = malloc(total * sizeof(double));
+  for (uint64_t i = 0; i < total; i++)
+    in[i] = (double)delta[i];
+  s->spec = fftw_malloc(modes * sizeof(fftw_complex));
+  fftw_plan p = fftw_plan_dft_r2c_3d(n, n, n, in, s->spec, FFTW_ESTIMATE);
+  fftw_execute(p);
+  fftw_destroy_plan(p);
+  free(in);
+  if (mode) {
+    /* The forward transform of a float grid comes back in float. */
+    for (uint64_t i = 0; i < modes; i++) {
+      s->spec[i][0] = (double)(float)s->spec[i][0];
+      s->spec[i][1] = (double)(float)s->spec[i][1];
+    }
+  }
+  if (window_mode) {
+    /* fft_build_window_axis, src/math/fft.c:958-975, order 2 (CIC):
+     * W = sinc^2, factor 1/W (full) or W/S with S = 1 - 2 sin^2/3. */
+    s->window = malloc(n * sizeof(double));
+    for (uint32_t i = 0; i < n; i++) {
+      const double x = axis_x(i, n, mode);
+      const double sc = (x < 1e-9 && x > -1e-9) ? 1.0 : sin(x) / x;
+      double w = 1.0;
+      w *= sc;
+      w *= sc;
+      if (window_mode == 2) {
+        const double s2 = sin(x) * sin(x);
+        s->window[i] = w / (1.0 - 2.0 * s2 / 3.0);
+      } else {
+        s->window[i] = 1.0 / w;
+      }
+    }
+  }
+  return s;
+}
+
+/* fft_build_filter_lut + sif__fft_apply_filter_smoothed + the backward
+ * transform's 1/N^3 (src/math/fft.c:521-568, 703-788, 820-888). */
+void orc_spectrum_smooth(orc_spectrum_t* s, int filter, float r, float sigma,
+  float* out_f, double* out_d) {
+  const uint32_t n = s->n;
+  const uint32_t h = n >> 1;
+  const uint32_t zd = n / 2 + 1;
+  const uint32_t max_k2 = 3 * h * h;
+  const uint64_t modes = (uint64_t)n * n * zd;
+  const uint64_t total = (uint64_t)n * n * n;
+  double* lut = malloc(((size_t)max_k2 + 1) * sizeof(double));
+  if (s->mode) {
+    const float factor = (float)((double)r * 2.0 * (double)PI_F / (double)s->box);
+    const float factor2 = factor * factor;
+    const float gfactor = (float)((double)sigma * 2.0 * (double)PI_F / (double)s->box);
+    const float gfactor2 = gfactor * gfactor;
+    for (uint32_t k2 = 0; k2 <= max_k2; k2++) {
+      float v;
+      if (k2 == 0) {
+        v = 1.0f;
+      } else if (filter == 1) {
+        const float kr = factor * sqrtf((float)k2);
+        v = kr > 1e-4f ? 3.0f * (sinf(kr) - kr * cosf(kr)) / (kr * kr * kr) : 1.0f;
+      } else {
+        v = expf(-0.5f * factor2 * (float)k2);
+      }
+      if (sigma > 0.0f && k2 > 0)
+        v *= expf(-0.5f * gfactor2 * (float)k2);
+      lut[k2] = v;
+    }
+  } else {
+    const double factor = (double)r * 2.0 * M_PI / (double)s->box;
+    const double gfactor = (double)sigma * 2.0 * M_PI / (double)s->box;
+    for (uint32_t k2 = 0; k2 <= max_k2; k2++) {
+      double v;
+      if (k2 == 0) {
+        v = 1.0;
+      } else if (filter == 1) {
+        const double kr = factor * sqrt((double)k2);
+        v = kr > 1e-4 ? 3.0 * (sin(kr) - kr * cos(kr)) / (kr * kr * kr) : 1.0;
+      } else {
+        v = exp(-0.5 * factor * factor * (double)k2);
+      }
+      if (sigma > 0.0f && k2 > 0)
+        v *= exp(-0.5 * gfactor * gfactor * (double)k2);
+      lut[k2] = v;
+    }
+  }
+  fftw_complex* work = fftw_malloc(modes * sizeof(fftw_complex));
+  const double* win = s->window;
+#pragma omp parallel for schedule(static)
+  for (uint32_t ix = 0; ix < n; ix++) {
+    const int32_t kx = ix > h ? (int32_t)ix - (int32_t)n : (int32_t)ix;
+    const uint32_t kx2 = (uint32_t)(kx * kx);
+    const double cx = win ? win[ix] : 1.0;
+    for (uint32_t iy = 0; iy < n; iy++) {
+      const int32_t ky = iy > h ? (int32_t)iy - (int32_t)n : (int32_t)iy;
+      const uint32_t kxy2 = kx2 + (uint32_t)(ky * ky);
+      const double cxy = cx * (win ? win[iy] : 1.0);
+      for (uint32_t iz = 0; iz < zd; iz++) {
+        const uint32_t k2 = kxy2 + iz * iz;
+        const uint64_t i = ((uint64_t)ix * n + iy) * zd + iz;
+        double sm;
+        if (s->mode) {
+          float smf = (float)lut[k2];
+          if (win)
+            smf = (float)((double)smf * cxy * win[iz]);
+          work[i][0] = (double)((float)s->spec[i][0] * smf);
+          work[i][1] = (double)((float)s->spec[i][1] * smf);
+          continue;
+        }
+        sm = lut[k2];
+        if (win)
+          sm = sm * cxy * win[iz];
+        work[i][0] = s->spec[i][0] * sm;
+        work[i][1] = s->spec[i][1] * sm;
+      }
+    }
+  }
+  free(lut);
+  double* real = malloc(total * sizeof(double));
+  fftw_plan p = fftw_plan_dft_c2r_3d(n, n, n, work, real, FFTW_ESTIMATE);
+  fftw_execute(p);
+  fftw_destroy_plan(p);
+  fftw_free(work);
+  const double norm = 1.0 / (double)total;
+  const float normf = 1.0f / (float)total;
+  for (uint64_t i = 0; i < total; i++) {
+    if (out_d)
+      out_d[i] = real[i] * norm;
+    if (out_f)
+      out_f[i] = s->mode ? (float)real[i] * normf : (float)(real[i] * norm);
+  }
+  free(real);
+}
+
+void orc_spectrum_free(orc_spectrum_t* s) {
+  if (!s)
+    return;
+  fftw_free(s->spec);
+  free(s->window);
+  free(s);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Candidate order                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* The reference sorts candidates with a three-way (Dijkstra) quicksort whose
+ * pivot is the middle element of the range (include/sif/utils/sort.h:56-98),
+ * and its parallel form reproduces the serial permutation (108-145). Equal
+ * depths are common, and their order is part of the answer, so the same
+ * partition steps are taken here: scan left to right; a smaller key moves to
+ * the low end, a larger one is exchanged with the high end and re-examined,
+ * an equal one stays. Ranges are kept on an explicit stack; the two sides of a
+ * partition are disjoint, so the order they are processed in is immaterial. */
+void orc_sort_candidates(orc_candidate_t* a, uint64_t count) {
+  if (count < 2)
+    return;
+  int64_t* stack = malloc(sizeof(int64_t) * 2 * 128);
+  size_t cap = 128, top = 0;
+  stack[top * 2] = 0;
+  stack[top * 2 + 1] = (int64_t)count - 1;
+  top++;
+  while (top > 0) {
+    top--;
+    const int64_t lo = stack[top * 2], hi = stack[top * 2 + 1];
+    if (lo >= hi)
+      continue;
+    const float pivot = a[lo + (hi - lo) / 2].delta;
+    int64_t lt = lo, i = lo, gt = hi;
+    while (i <= gt) {
+      const float v = a[i].delta;
+      if (v < pivot) {
+        const orc_candidate_t t = a[lt];
+        a[lt] = a[i];
+        a[i] = t;
+        lt++;
+        i++;
+      } else if (pivot < v) {
+        const orc_candidate_t t = a[i];
+        a[i] = a[gt];
+        a[gt] = t;
+        gt--;
+      } else {
+        i++;
+      }
+    }
+    if (top + 2 > cap) {
+      cap *= 2;
+      stack = realloc(stack, sizeof(int64_t) * 2 * cap);
+    }
+    stack[top * 2] = lo;
+    stack[top * 2 + 1] = lt - 1;
+    top++;
+    stack[top * 2] = gt + 1;
+    stack[top * 2 + 1] = hi;
+    top++;
+  }
+  free(stack);
+}
+
+/* ------------------------------------------------------------------------ */
+/* The rescaling                                                            */
+/* ------------------------------------------------------------------------ */
+
+#define CELL_CORE   1
+#define CELL_STRADDLE 2
+#define CELL_EDGE   3
+#define CELL_SHELL  4
+
+/* sif__exodus_template_build, src/finder/exodus_rescale.c:175-283. */
+int orc_template_build(orc_template_t* t, uint32_t mesh_n, float cell_length,
+  float rmin, float r_search) {
+  memset(t, 0, sizeof(*t));
+  const int32_t cr = (int32_t)(r_search / cell_length) + 1;
+  if (cr >= (int32_t)mesh_n)
+    return -3;
+  const uint64_t max = (uint64_t)(2 * cr + 1) * (2 * cr + 1) * (2 * cr + 1);
+  t->dx = malloc(max * sizeof(int32_t));
+  t->dy = malloc(max * sizeof(int32_t));
+  t->dz = malloc(max * sizeof(int32_t));
+  t->type = malloc(max);
+  t->min_d2 = malloc(max * sizeof(float));
+  t->max_d2 = malloc(max * sizeof(float));
+  const float rs2 = r_search * r_search;
+  const float rc2 = rmin * rmin;
+  for (int32_t dx = -cr; dx <= cr; dx++)
+    for (int32_t dy = -cr; dy <= cr; dy++)
+      for (int32_t dz = -cr; dz <= cr; dz++) {
+        const float mnx = dx == 0 ? 0.0f : (fabsf((float)dx) - 1.0f) * cell_length;
+        const float mny = dy == 0 ? 0.0f : (fabsf((float)dy) - 1.0f) * cell_length;
+        const float mnz = dz == 0 ? 0.0f : (fabsf((float)dz) - 1.0f) * cell_length;
+        const float mn = mnx * mnx + mny * mny + mnz * mnz;
+        if (mn > rs2)
+          continue;
+        const float mxx = (fabsf((float)dx) + 1.0f) * cell_length;
+        const float mxy = (fabsf((float)dy) + 1.0f) * cell_length;
+        const float mxz = (fabsf((float)dz) + 1.0f) * cell_length;
+        const float mx = mxx * mxx + mxy * mxy + mxz * mxz;
+        const uint32_t k = t->count++;
+        t->dx[k] = dx;
+        t->dy[k] = dy;
+        t->dz[k] = dz;
+        t->min_d2[k] = mn;
+        t->max_d2[k] = mx;
+        if (mx <= rc2)
+          t->type[k] = CELL_CORE;
+        else if (mn > rc2)
+          t->type[k] = mx <= rs2 ? CELL_SHELL : CELL_EDGE;
+        else
+          t->type[k] = CELL_STRADDLE;
+      }
+  return 0;
+}
+
+void orc_template_free(orc_template_t* t) {
+  free(t->dx);
+  free(t->dy);
+  free(t->dz);
+  free(t->type);
+  free(t->min_d2);
+  free(t->max_d2);
+  memset(t, 0, sizeof(*t));
+}
+
+typedef struct {
+  const orc_mesh_t* m;
+  const orc_template_t* t;
+  float cx, cy, cz;
+  int32_t ix, iy, iz;
+} query_t;
+
+/* query_cell, src/finder/exodus_rescale.c:295-342: the wrapped cell and the
+ * periodic image of the centre its particles are measured against. */
+static inline int query_cell(const query_t* q, uint32_t i, uint64_t* s,
+  uint64_t* e, float* ex, float* ey, float* ez) {
+  const int32_t N = (int32_t)q->m->n_cells;
+  const float L = q->m->box_length;
+  int32_t ix = q->ix + q->t->dx[i];
+  float cx = q->cx;
+  if (ix < 0) {
+    ix += N;
+    cx += L;
+  } else if (ix >= N) {
+    ix -= N;
+    cx -= L;
+  }
+  int32_t iy = q->iy + q->t->dy[i];
+  float cy = q->cy;
+  if (iy < 0) {
+    iy += N;
+    cy += L;
+  } else if (iy >= N) {
+    iy -= N;
+    cy -= L;
+  }
+  int32_t iz = q->iz + q->t->dz[i];
+  float cz = q->cz;
+  if (iz < 0) {
+    iz += N;
+    cz += L;
+  } else if (iz >= N) {
+    iz -= N;
+    cz -= L;
+  }
+  const uint64_t flat = (uint64_t)ix * N * N + (uint64_t)iy * N + (uint64_t)iz;
+  *s = q->m->offsets[flat];
+  *e = q->m->offsets[flat + 1];
+  *ex = cx;
+  *ey = cy;
+  *ez = cz;
+  return *e > *s;
+}
+
+/* dist2, src/finder/exodus_rescale.c:349-355. */
+static inline float dist2(float px, float py, float pz, float cx, float cy, float cz) {
+  const float dx = px - cx;
+  const float dy = py - cy;
+  const float dz = pz - cz;
+  return dx * dx + dy * dy + dz * dz;
+}
+
+/* bin_of, src/finder/exodus_rescale.c:360-369. */
+static inline uint32_t bin_of(float d2, float rc2, float inv_w, uint32_t nb) {
+  const int32_t b = (int32_t)((d2 - rc2) * inv_w);
+  if (b < 0)
+    return 0;
+  if ((uint32_t)b >= nb)
+    return nb - 1;
+  return (uint32_t)b;
+}
+
+static int cmp_float(const void* a, const void* b) {
+  const float x = *(const float*)a, y = *(const float*)b;
+  return (x > y) - (x < y);
+}
+
+/* resolve_bin, src/finder/exodus_rescale.c:391-507 (unweighted). The
+ * collected distances are equal values wherever they tie, so any ascending
+ * sort gives the reference's sequence. */
+static int resolve(const query_t* q, uint32_t blo, uint32_t bhi, float lo,
+  float hi, float rc2, float rs2, float inv_w, uint32_t nb, uint64_t cur_n,
+  float K2, float* out, float** buf, uint64_t* cap) {
+  const orc_template_t* t = q->t;
+  uint64_t count = 0;
+  for (uint32_t i = 0; i < t->count; i++) {
+    const uint8_t type = t->type[i];
+    if (type == CELL_CORE || t->max_d2[i] < lo || t->min_d2[i] > hi)
+      continue;
+    uint64_t s, e;
+    float ex, ey, ez;
+    if (!query_cell(q, i, &s, &e, &ex, &ey, &ez))
+      continue;
+    if (count + (e - s) > *cap) {
+      while (count + (e - s) > *cap)
+        *cap *= 2;
+      *buf = realloc(*buf, *cap * sizeof(float));
+    }
+    for (uint64_t p = s; p < e; p++) {
+      const float d2 = dist2(q->m->x[p], q->m->y[p], q->m->z[p], ex, ey, ez);
+      if (type != CELL_SHELL && !(d2 > rc2 && d2 <= rs2))
+        continue;
+      const uint32_t bi = bin_of(d2, rc2, inv_w, nb);
+      if (bi < blo || bi > bhi)
+        continue;
+      (*buf)[count++] = d2;
+    }
+  }
+  if (count > 1)
+    qsort(*buf, count, sizeof(float), cmp_float);
+  for (int64_t k = (int64_t)count - 1; k >= 0; k--) {
+    const float d2 = (*buf)[k];
+    if (d2 == 0.0f) {
+      cur_n--;
+      continue;
+    }
+    const uint64_t n_in = cur_n - 1;
+    const float d2c = d2 * d2 * d2;
+    const float rn = (float)n_in;
+    if (rn * rn <= K2 * d2c) {
+      *out = sqrtf(d2);
+      return 1;
+    }
+    cur_n--;
+  }
+  return 0;
+}
+
+/* find_exact_radius_impl, src/finder/exodus_rescale.c:642-1012, unweighted
+ * (mass_factor = vol_factor). */
+float orc_find_radius(const orc_mesh_t* m, const orc_template_t* t, float cx,
+  float cy, float cz, float r_search, float threshold, float vol_factor,
+  float rmin, uint32_t window, uint8_t* reason, uint64_t* span_sum,
+  uint64_t* span_count) {
+  *reason = ORC_RESCALE_OK;
+  const float inv_l = 1.0f / m->cell_length;
+  const query_t q = {m, t, cx, cy, cz, (int32_t)(cx * inv_l),
+    (int32_t)(cy * inv_l), (int32_t)(cz * inv_l)};
+  const float rs2 = r_search * r_search;
+  const float rc2 = rmin * rmin;
+
+  const float span = rs2 - rc2;
+  uint32_t nb = 2048u;
+  {
+    const float expected_shell =
+      vol_factor * (r_search * r_search * r_search - rmin * rmin * rmin);
+    const float want = expected_shell / 16.0f;
+    if (!(want >= 64.0f))
+      nb = 64u;
+    else if (want < 2048.0f)
+      nb = (uint32_t)want;
+  }
+  if (!(span > 0.0f)) {
+    *reason = ORC_RESCALE_DEGENERATE;
+    return -1.0f;
+  }
+
+  /* The early refusal, 738-782. */
+  {
+    const float expected = vol_factor * r_search * r_search * r_search;
+    uint64_t within = 0;
+    for (uint32_t i = 0; i < t->count; i++) {
+      const uint8_t type = t->type[i];
+      uint64_t s, e;
+      float ex, ey, ez;
+      if (!query_cell(&q, i, &s, &e, &ex, &ey, &ez))
+        continue;
+      if (type == CELL_CORE || type == CELL_SHELL) {
+        within += e - s;
+        continue;
+      }
+      for (uint64_t p = s; p < e; p++)
+        within += dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez) <= rs2;
+    }
+    if (within == 0) {
+      *reason = ORC_RESCALE_EMPTY;
+      return -1.0f;
+    }
+    if (((float)within / expected) - 1.0f <= threshold) {
+      *reason = ORC_RESCALE_BEYOND_SEARCH;
+      return -1.0f;
+    }
+  }
+
+  const float inv_w = (float)nb / span;
+  const float bin_w = span / (float)nb;
+  uint32_t* bins = calloc(nb, sizeof(uint32_t));
+  uint64_t n_core = 0, n_shell = 0;
+  for (uint32_t i = 0; i < t->count; i++) {
+    const uint8_t type = t->type[i];
+    uint64_t s, e;
+    float ex, ey, ez;
+    if (!query_cell(&q, i, &s, &e, &ex, &ey, &ez))
+      continue;
+    if (type == CELL_CORE) {
+      n_core += e - s;
+    } else if (type == CELL_SHELL) {
+      for (uint64_t p = s; p < e; p++)
+        bins[bin_of(dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez), rc2, inv_w, nb)]++;
+      n_shell += e - s;
+    } else {
+      for (uint64_t p = s; p < e; p++) {
+        const float d2 = dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez);
+        n_core += d2 <= rc2;
+        if (d2 > rc2 && d2 <= rs2) {
+          bins[bin_of(d2, rc2, inv_w, nb)]++;
+          n_shell++;
+        }
+      }
+    }
+  }
+
+  const uint64_t total = n_core + n_shell;
+  if (total == 0) {
+    free(bins);
+    *reason = ORC_RESCALE_EMPTY;
+    return -1.0f;
+  }
+  {
+    const float expected = vol_factor * r_search * r_search * r_search;
+    if (((float)total / expected) - 1.0f <= threshold) {
+      free(bins);
+      *reason = ORC_RESCALE_BEYOND_SEARCH;
+      return -1.0f;
+    }
+  }
+
+  const float K = (threshold + 1.0f) * vol_factor;
+  const float K2 = K * K;
+  uint64_t above = 0;
+  int32_t b_first = -1;
+  uint64_t cap = 4096;
+  float* buf = malloc(cap * sizeof(float));
+  float result = -1.0f;
+  *reason = ORC_RESCALE_BELOW_RUNG;
+  for (int32_t b = (int32_t)nb - 1; b >= 0; b--) {
+    const uint32_t count = bins[b];
+    if (count == 0)
+      continue;
+    float hi = rc2 + (float)(b + 1) * bin_w;
+    if (b == (int32_t)nb - 1)
+      hi = rs2 * (1.0f + 1e-6f);
+    const float n_in_min = (float)(total - above - count);
+    if (n_in_min * n_in_min > K2 * hi * hi * hi) {
+      above += count;
+      continue;
+    }
+    if (b_first < 0)
+      b_first = b;
+    int32_t b_lo = b - (int32_t)(window - 1);
+    if (b_lo < 0)
+      b_lo = 0;
+    uint64_t wcount = 0;
+    for (int32_t bb = b_lo; bb <= b; bb++)
+      wcount += bins[bb];
+    const float win_lo = rc2 + (float)b_lo * bin_w;
+    float r = -1.0f;
+    if (resolve(&q, (uint32_t)b_lo, (uint32_t)b, win_lo, hi, rc2, rs2, inv_w, nb,
+          total - above, K2, &r, &buf, &cap)) {
+      const int32_t b_found = (int32_t)bin_of(r * r, rc2, inv_w, nb);
+      int32_t reached = b_first - b_found + 1;
+      if (reached < 1)
+        reached = 1;
+      if (span_sum)
+        *span_sum += (uint64_t)reached;
+      if (span_count)
+        (*span_count)++;
+      result = r;
+      *reason = ORC_RESCALE_OK;
+      break;
+    }
+    above += wcount;
+    b = b_lo;
+  }
+  free(buf);
+  free(bins);
+  return result;
+}
+
+static int cmp_double(const void* a, const void* b) {
+  const double x = *(const double*)a, y = *(const double*)b;
+  return (x > y) - (x < y);
+}
+
+/* The radius by definition, over every particle in the box: the outermost
+ * distance d in (rung, r_search] at which the particles strictly inside are at
+ * most (1 + threshold) times the mean count of a sphere of radius d; -1 when
+ * none qualifies. The definition tests/test_finders.c:419-459 checks the
+ * finder against; nothing here shares code with the histogram walk. */
+double orc_brute_force_radius(const float* x, const float* y, const float* z,
+  uint64_t n, float box, double cx, double cy, double cz, double rung,
+  double r_search, double threshold) {
+  const double L = (double)box, half = 0.5 * L;
+  uint64_t n_core = 0, n_shell = 0;
+  double* d = malloc((n ? n : 1) * sizeof(double));
+  for (uint64_t p = 0; p < n; p++) {
+    double dx = fabs((double)x[p] - cx), dy = fabs((double)y[p] - cy),
+           dz = fabs((double)z[p] - cz);
+    dx = dx > half ? L - dx : dx;
+    dy = dy > half ? L - dy : dy;
+    dz = dz > half ? L - dz : dz;
+    const double r = sqrt(dx * dx + dy * dy + dz * dz);
+    if (r <= rung)
+      n_core++;
+    else if (r <= r_search)
+      d[n_shell++] = r;
+  }
+  qsort(d, n_shell, sizeof(double), cmp_double);
+  const double k = (1.0 + threshold) * (double)n / (L * L * L) * 4.0 / 3.0 * M_PI;
+  double out = -1.0;
+  for (uint64_t i = n_shell; i-- > 0;) {
+    if ((double)(n_core + i) <= k * d[i] * d[i] * d[i]) {
+      out = d[i];
+      break;
+    }
+  }
+  free(d);
+  return out;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Overlap tests, the mask, the void index                                  */
+/* ------------------------------------------------------------------------ */
+
+/* sif__wrap_pbc, src/finder/utils.h:25-31, for any n. */
+static inline uint32_t wrap_pbc(int32_t v, uint32_t n) {
+  int32_t w = v % (int32_t)n;
+  return (uint32_t)(w < 0 ? w + (int32_t)n : w);
+}
+
+static inline int mask_get(const uint64_t* words, uint64_t i) {
+  return (words[i >> 6] >> (i & 63)) & 1u;
+}
+
+static inline void mask_set(uint64_t* words, uint64_t i) {
+  words[i >> 6] |= 1ull << (i & 63);
+}
+
+/* sif__overlap_quick, src/finder/utils.c:819-848: the six axis poles. */
+static int overlap_quick(const uint64_t* mask, uint32_t n, uint32_t ix,
+  uint32_t iy, uint32_t iz, uint32_t r) {
+  const uint64_t nn = n;
+  if (mask_get(mask, ((uint64_t)wrap_pbc((int32_t)(ix + r), n) * nn + iy) * nn + iz))
+    return 1;
+  if (mask_get(mask, ((uint64_t)wrap_pbc((int32_t)ix - (int32_t)r, n) * nn + iy) * nn + iz))
+    return 1;
+  if (mask_get(mask, ((uint64_t)ix * nn + wrap_pbc((int32_t)(iy + r), n)) * nn + iz))
+    return 1;
+  if (mask_get(mask, ((uint64_t)ix * nn + wrap_pbc((int32_t)iy - (int32_t)r, n)) * nn + iz))
+    return 1;
+  if (mask_get(mask, ((uint64_t)ix * nn + iy) * nn + wrap_pbc((int32_t)(iz + r), n)))
+    return 1;
+  if (mask_get(mask, ((uint64_t)ix * nn + iy) * nn + wrap_pbc((int32_t)iz - (int32_t)r, n)))
+    return 1;
+  return 0;
+}
+
+/* The accepted voids and their 32^3 periodic cell index
+ * (src/structures/cell_linked_list.c, VOID_CLL_CELLS exodus_finder.c:219). */
+#define VOID_CELLS 32
+typedef struct {
+  float *cx, *cy, *cz, *r;
+  uint64_t n, cap;
+  int32_t head[VOID_CELLS * VOID_CELLS * VOID_CELLS];
+  int32_t* next;
+  float inv_cell; /* (float)32 / box */
+} voids_t;
+
+static uint32_t void_axis(const voids_t* v, float c) {
+  int32_t i = (int32_t)floorf(c * v->inv_cell);
+  i %= VOID_CELLS;
+  if (i < 0)
+    i += VOID_CELLS;
+  return (uint32_t)i;
+}
+
+static void voids_init(voids_t* v, float box) {
+  memset(v, 0, sizeof(*v));
+  memset(v->head, 0xFF, sizeof(v->head));
+  v->inv_cell = (float)VOID_CELLS / box;
+}
+
+static void voids_add(voids_t* v, float cx, float cy, float cz, float r) {
+  if (v->n == v->cap) {
+    v->cap = v->cap ? 2 * v->cap : 1024;
+    v->cx = realloc(v->cx, v->cap * sizeof(float));
+    v->cy = realloc(v->cy, v->cap * sizeof(float));
+    v->cz = realloc(v->cz, v->cap * sizeof(float));
+    v->r = realloc(v->r, v->cap * sizeof(float));
+    v->next = realloc(v->next, v->cap * sizeof(int32_t));
+  }
+  const uint64_t i = v->n++;
+  v->cx[i] = cx;
+  v->cy[i] = cy;
+  v->cz[i] = cz;
+  v->r[i] = r;
+  const uint64_t cell = ((uint64_t)void_axis(v, cx) * VOID_CELLS + void_axis(v, cy)) *
+                          VOID_CELLS +
+                        void_axis(v, cz);
+  v->next[i] = v->head[cell];
+  v->head[cell] = (int32_t)i;
+}
+
+static void voids_free(voids_t* v) {
+  free(v->cx);
+  free(v->cy);
+  free(v->cz);
+  free(v->r);
+  free(v->next);
+}
+
+/* sif__overlap_exact, src/finder/utils.c:850-960. */
+static int overlap_exact(const voids_t* v, float cx, float cy, float cz,
+  float r, float max_r, float box, float f, float scale) {
+  const float half = box * 0.5f;
+  const float search = scale * (r + max_r - f * (r < max_r ? r : max_r));
+  const float inv = v->inv_cell;
+  const int32_t x0 = (int32_t)floorf((cx - search) * inv);
+  const int32_t x1 = (int32_t)floorf((cx + search) * inv);
+  const int32_t y0 = (int32_t)floorf((cy - search) * inv);
+  const int32_t y1 = (int32_t)floorf((cy + search) * inv);
+  const int32_t z0 = (int32_t)floorf((cz - search) * inv);
+  const int32_t z1 = (int32_t)floorf((cz + search) * inv);
+  const int interior = (cx - search >= 0.0f) && (cx + search < box) &&
+                       (cy - search >= 0.0f) && (cy + search < box) &&
+                       (cz - search >= 0.0f) && (cz + search < box);
+  for (int32_t ix = x0; ix <= x1; ix++) {
+    const uint32_t wx = (uint32_t)ix & (VOID_CELLS - 1);
+    for (int32_t iy = y0; iy <= y1; iy++) {
+      const uint32_t wy = (uint32_t)iy & (VOID_CELLS - 1);
+      for (int32_t iz = z0; iz <= z1; iz++) {
+        const uint32_t wz = (uint32_t)iz & (VOID_CELLS - 1);
+        int32_t j = v->head[(wx * VOID_CELLS + wy) * VOID_CELLS + wz];
+        while (j != -1) {
+          const float rj = v->r[j];
+          const float mn = r < rj ? r : rj;
+          const float tot = scale * (r + rj - f * mn);
+          const float tot2 = tot * tot;
+          if (interior) {
+            const float dx = cx - v->cx[j];
+            const float dy = cy - v->cy[j];
+            const float dz = cz - v->cz[j];
+            if (dx * dx + dy * dy + dz * dz < tot2)
+              return 1;
+          } else {
+            float dx = fabsf(cx - v->cx[j]);
+            dx = dx > half ? box - dx : dx;
+            const float dx2 = dx * dx;
+            if (dx2 < tot2) {
+              float dy = fabsf(cy - v->cy[j]);
+              dy = dy > half ? box - dy : dy;
+              const float dy2 = dy * dy;
+              if (dx2 + dy2 < tot2) {
+                float dz = fabsf(cz - v->cz[j]);
+                dz = dz > half ? box - dz : dz;
+                if (dx2 + dy2 + dz * dz < tot2)
+                  return 1;
+              }
+            }
+          }
+          j = v->next[j];
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* paint_sphere with set = 1, src/finder/utils.c:965-1027. */
+static void mark_sphere(uint64_t* mask, float cx, float cy, float cz, float r,
+  uint32_t n, float cell_length) {
+  const float r2 = r * r;
+  const float inv = 1.0f / cell_length;
+  const float box = (float)n * cell_length;
+  const float half = box * 0.5f;
+  const int32_t cr = (int32_t)(r * inv) + 1;
+  const int32_t ci = (int32_t)(cx * inv), cj = (int32_t)(cy * inv),
+                ck = (int32_t)(cz * inv);
+  for (int32_t dx = -cr; dx <= cr; dx++) {
+    const int32_t gx = ci + dx;
+    float ddx = fabsf((float)gx * cell_length - cx);
+    ddx = ddx > half ? box - ddx : ddx;
+    const float dx2 = ddx * ddx;
+    if (dx2 > r2)
+      continue;
+    const uint32_t wx = wrap_pbc(gx, n);
+    for (int32_t dy = -cr; dy <= cr; dy++) {
+      const int32_t gy = cj + dy;
+      float ddy = fabsf((float)gy * cell_length - cy);
+      ddy = ddy > half ? box - ddy : ddy;
+      const float dxy2 = dx2 + ddy * ddy;
+      if (dxy2 > r2)
+        continue;
+      const uint32_t wy = wrap_pbc(gy, n);
+      for (int32_t dz = -cr; dz <= cr; dz++) {
+        const int32_t gz = ck + dz;
+        float ddz = fabsf((float)gz * cell_length - cz);
+        ddz = ddz > half ? box - ddz : ddz;
+        if (dxy2 + ddz * ddz <= r2)
+          mask_set(mask, ((uint64_t)wx * n + wy) * n + wrap_pbc(gz, n));
+      }
+    }
+  }
+}
+
+/* collision_radius, src/finder/exodus_finder.c:780-845 (no displacement). */
+#define COLLISION_SLACK 1e-5
+static double collision_radius(const voids_t* v, float max_acc, float scale_f,
+  float cx, float cy, float cz, float r_hi, float min_rj, float f, float box) {
+  const double L = (double)box, half = 0.5 * L, ff = (double)f,
+               scale = (double)scale_f;
+  const float reach = scale_f * (r_hi + max_acc);
+  const float x[3] = {cx, cy, cz};
+  int32_t lo[3], hi[3];
+  for (int a = 0; a < 3; a++) {
+    lo[a] = (int32_t)floorf((x[a] - reach) * v->inv_cell);
+    hi[a] = (int32_t)floorf((x[a] + reach) * v->inv_cell);
+    if (hi[a] - lo[a] >= VOID_CELLS) {
+      lo[a] = 0;
+      hi[a] = VOID_CELLS - 1;
+    }
+  }
+  double best = INFINITY;
+  for (int32_t a = lo[0]; a <= hi[0]; a++) {
+    const int32_t wa = ((a % VOID_CELLS) + VOID_CELLS) % VOID_CELLS;
+    for (int32_t b = lo[1]; b <= hi[1]; b++) {
+      const int32_t wb = ((b % VOID_CELLS) + VOID_CELLS) % VOID_CELLS;
+      for (int32_t c = lo[2]; c <= hi[2]; c++) {
+        const int32_t wc = ((c % VOID_CELLS) + VOID_CELLS) % VOID_CELLS;
+        for (int32_t i = v->head[(wa * VOID_CELLS + wb) * VOID_CELLS + wc]; i != -1;
+             i = v->next[i]) {
+          const double rj = (double)v->r[i];
+          if (v->r[i] < min_rj)
+            continue;
+          double dx = fabs((double)cx - (double)v->cx[i]);
+          double dy = fabs((double)cy - (double)v->cy[i]);
+          double dz = fabs((double)cz - (double)v->cz[i]);
+          dx = dx > half ? L - dx : dx;
+          dy = dy > half ? L - dy : dy;
+          dz = dz > half ? L - dz : dz;
+          const double D = (sqrt(dx * dx + dy * dy + dz * dz) +
+                             COLLISION_SLACK * (L + (double)r_hi + rj)) /
+                           scale;
+          double rs;
+          if (D <= rj)
+            rs = 0.0;
+          else if (D <= (2.0 - ff) * rj)
+            rs = (D - rj) / (1.0 - ff);
+          else
+            rs = D - (1.0 - ff) * rj;
+          if (rs < best)
+            best = rs;
+        }
+      }
+    }
+  }
+  return best;
+}
+
+/* sif__exodus_witness, src/finder/exodus_rescale.c:1074-1167 (closed = 0). */
+#define WITNESS_SLACK 1e-5f
+static int witness(const orc_mesh_t* m, const orc_template_t* t, float cx,
+  float cy, float cz, float rho2, float r_search, float threshold,
+  float vol_factor) {
+  const float inv_l = 1.0f / m->cell_length;
+  const query_t q = {m, t, cx, cy, cz, (int32_t)(cx * inv_l),
+    (int32_t)(cy * inv_l), (int32_t)(cz * inv_l)};
+  const float rs2 = r_search * r_search;
+  if (!(rho2 < rs2))
+    return 0;
+  const float K = (threshold + 1.0f) * vol_factor;
+  const float K2 = K * K;
+  const float bound = K2 * (rho2 * rho2 * rho2) * (1.0f - WITNESS_SLACK);
+  const double n_cap = sqrt((double)bound) + 2.0;
+  const float whole_in = rho2 * (1.0f - WITNESS_SLACK);
+  const float whole_out = rho2 * (1.0f + WITNESS_SLACK);
+  uint64_t n = 0;
+  int beyond = 0;
+  for (uint32_t i = 0; i < t->count; i++) {
+    const uint8_t type = t->type[i];
+    if (beyond && t->min_d2[i] > whole_out)
+      continue;
+    uint64_t s, e;
+    float ex, ey, ez;
+    if (!query_cell(&q, i, &s, &e, &ex, &ey, &ez))
+      continue;
+    if (type == CELL_CORE || t->max_d2[i] <= whole_in) {
+      n += e - s;
+    } else if (type == CELL_SHELL && t->min_d2[i] > whole_out) {
+      beyond = 1;
+    } else {
+      for (uint64_t p = s; p < e; p++) {
+        const float d2 = dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez);
+        if (d2 <= rho2)
+          n++;
+        else if (type == CELL_SHELL || d2 <= rs2)
+          beyond = 1;
+      }
+    }
+    if ((double)n > n_cap)
+      return 0;
+  }
+  const float rn = (float)n;
+  if (!beyond || !(rn * rn <= bound))
+    return 0;
+  return 1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The run                                                                  */
+/* ------------------------------------------------------------------------ */
+
+#define BATCH_MAX 4096u
+#define BATCH_PER_THREAD 8u
+#define BATCH_FLOOR 32u
+#define RESOLVE_INITIAL 8u
+
+#define ST_PROXY 1
+#define ST_MESH 2
+#define ST_RESCALE 3
+#define ST_ACCEPTED 4
+#define ST_WITNESS 5
+
+typedef struct {
+  uint8_t status;
+  float r;
+  float cx, cy, cz;
+  uint32_t ix, iy, iz;
+} result_t;
+
+static int cmp_desc(const void* a, const void* b) {
+  const float x = *(const float*)a, y = *(const float*)b;
+  return (x < y) - (x > y);
+}
+
+/* The rung loop of sif__exodus_run (src/finder/exodus_finder.c:1585-2492)
+ * for a box, unweighted, SIF_FINDER_SEEDS_CELLS on their nodes: per rung the
+ * top-hat smoothing, the scan and sort, the reach, the template, the
+ * pre-filter at the rung, then speculative batches -- phase 0 (masked skip),
+ * phase 1 (pole probe, exact overlap, collision witness, rescaling; in
+ * parallel), phase 2 (the sequential commit with its re-checks at the
+ * rescaled radius) -- and the batch and window retuning between them. */
+int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in,
+  uint32_t n_radii, const orc_exodus_params_t* p, orc_catalogue_t* out,
+  orc_rung_stats_t* stats_out) {
+  memset(out, 0, sizeof(*out));
+  const uint32_t N = p->grid_n;
+  const float box = p->box_length;
+  const float cell = box / (float)N;
+  const uint64_t total = (uint64_t)N * N * N;
+  const float threshold = p->threshold, f = p->overlap_fraction;
+  const uint32_t opt = p->options;
+  if (!(threshold > -1.0f && threshold < 0.0f) || !(f >= 0.0f && f <= 1.0f) ||
+      n_radii == 0 || mesh->box_length != box)
+    return -2;
+  if (opt & ((1u << 9) | (3u << 19) | (1u << 21) | (1u << 22)))
+    return -5; /* minima, refinement, extended reach, displacement */
+
+  float* radii = malloc(n_radii * sizeof(float));
+  memcpy(radii, radii_in, n_radii * sizeof(float));
+  qsort(radii, n_radii, sizeof(float), cmp_desc);
+
+  const float scale = (opt & (1u << 18)) ? (float)cbrt(1.0 + (double)threshold) : 1.0f;
+  static const float factors[4] = {1.5f, 1.25f, 1.75f, 2.0f};
+  const float search_factor = factors[(opt >> 12) & 3u];
+  const int window_mode = (opt & (1u << 14)) ? 0 : ((opt & (1u << 8)) ? 2 : 1);
+
+  orc_spectrum_t* spec = NULL;
+  if (!p->inject)
+    spec = orc_spectrum_new(delta, N, box, window_mode, p->smoothing_mode);
+
+  const float box_volume = box * box * box;
+  const float mean_density = (float)mesh->n_particles / box_volume;
+  const float vol_factor = (4.0f / 3.0f) * PI_F * mean_density;
+
+  int n_threads = p->n_threads > 0 ? p->n_threads : 1;
+  uint64_t* mask = calloc((total + 63) / 64, sizeof(uint64_t));
+  float* field = malloc(total * sizeof(float));
+  voids_t V;
+  voids_init(&V, box);
+  float max_acc = 0.0f;
+  orc_candidate_t* cand = NULL;
+  uint64_t cand_cap = 0;
+  result_t* res = malloc(2 * BATCH_MAX * sizeof(result_t));
+  uint64_t* bidx = malloc(2 * BATCH_MAX * sizeof(uint64_t));
+  int status = 0;
+
+  for (uint32_t ri = 0; ri < n_radii && status == 0; ri++) {
+    const float radius = radii[ri];
+    orc_rung_stats_t st;
+    memset(&st, 0, sizeof(st));
+    if (p->inject)
+      memcpy(field, p->inject + (uint64_t)ri * total, total * sizeof(float));
+    else
+      orc_spectrum_smooth(spec, 1, radius, 0.0f, field, NULL);
+
+    /* The scan, src/finder/utils.c:130-213: flat order, then the sort. */
+    uint64_t nc = 0;
+    for (uint64_t i = 0; i < total; i++)
+      nc += field[i] <= threshold && !mask_get(mask, i);
+    if (nc > cand_cap) {
+      cand_cap = nc;
+      cand = realloc(cand, cand_cap * sizeof(orc_candidate_t));
+    }
+    nc = 0;
+    for (uint64_t i = 0; i < total; i++)
+      if (field[i] <= threshold && !mask_get(mask, i)) {
+        cand[nc].delta = field[i];
+        cand[nc].refined = 0;
+        cand[nc].flat = i;
+        nc++;
+      }
+    orc_sort_candidates(cand, nc);
+    st.n_candidates = nc;
+
+    const float rmin = 1.0f * radius;
+    float r_search = radius + fmaxf((search_factor - 1.0f) * radius, 3.0f * cell);
+    if (ri > 0 && radii[ri - 1] > r_search)
+      r_search = radii[ri - 1];
+    orc_template_t tpl;
+    if (orc_template_build(&tpl, mesh->n_cells, mesh->cell_length, rmin, r_search)) {
+      status = -3;
+      break;
+    }
+    const int32_t proxy_pole = (int32_t)(scale * radius * (1.0f - f) / cell) - 1;
+    const float rc2 = rmin * rmin;
+
+    /* prefilter_cells, src/finder/exodus_finder.c:871-944 (order kept). */
+    {
+      uint64_t w = 0;
+      for (uint64_t k = 0; k < nc; k++) {
+        const uint64_t flat = cand[k].flat;
+        if (mask_get(mask, flat)) {
+          st.rejected_masked++;
+          continue;
+        }
+        const uint32_t ix = (uint32_t)(flat / ((uint64_t)N * N)),
+                       iy = (uint32_t)((flat / N) % N), iz = (uint32_t)(flat % N);
+        if (proxy_pole > 0 && overlap_quick(mask, N, ix, iy, iz, (uint32_t)proxy_pole)) {
+          st.rejected_proxy++;
+          continue;
+        }
+        if (overlap_exact(&V, (float)ix * cell, (float)iy * cell, (float)iz * cell,
+              radius, max_acc, box, f, scale)) {
+          st.rejected_overlap++;
+          continue;
+        }
+        cand[w++] = cand[k];
+      }
+      nc = w;
+    }
+
+    uint64_t floor_ = (uint64_t)BATCH_PER_THREAD * (uint64_t)n_threads;
+    if (floor_ < BATCH_FLOOR)
+      floor_ = BATCH_FLOOR;
+    if (floor_ > BATCH_MAX)
+      floor_ = BATCH_MAX;
+    uint64_t batch_cap = floor_;
+    uint32_t window = p->window > 0 ? (uint32_t)p->window : RESOLVE_INITIAL;
+
+    uint64_t k = 0;
+    while (k < nc && status == 0) {
+      uint64_t nb = 0;
+      while (k < nc && nb < batch_cap) {
+        if (mask_get(mask, cand[k].flat))
+          st.rejected_masked++;
+        else
+          bidx[nb++] = k;
+        k++;
+      }
+      if (nb == 0)
+        break;
+      uint64_t span_sum = 0, span_count = 0;
+      const float max_acc_frozen = max_acc;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(n_threads) \
+  reduction(+ : span_sum, span_count)
+      for (uint64_t b = 0; b < nb; b++) {
+        const uint64_t flat = cand[bidx[b]].flat;
+        result_t* r = &res[b];
+        r->ix = (uint32_t)(flat / ((uint64_t)N * N));
+        r->iy = (uint32_t)((flat / N) % N);
+        r->iz = (uint32_t)(flat % N);
+        if (proxy_pole > 0 &&
+            overlap_quick(mask, N, r->ix, r->iy, r->iz, (uint32_t)proxy_pole)) {
+          r->status = ST_PROXY;
+          continue;
+        }
+        r->cx = (float)r->ix * cell;
+        r->cy = (float)r->iy * cell;
+        r->cz = (float)r->iz * cell;
+        if (overlap_exact(&V, r->cx, r->cy, r->cz, radius, max_acc_frozen, box, f,
+              scale)) {
+          r->status = ST_MESH;
+          continue;
+        }
+        const double rho = collision_radius(&V, max_acc_frozen, scale, r->cx, r->cy,
+          r->cz, r_search, 0.0f, f, box);
+        if (rho < (double)r_search) {
+          float rho2 = (float)(rho * rho * (1.0 + COLLISION_SLACK));
+          if (rho2 < rc2)
+            rho2 = rc2;
+          if (witness(mesh, &tpl, r->cx, r->cy, r->cz, rho2, r_search, threshold,
+                vol_factor)) {
+            r->status = ST_WITNESS;
+            continue;
+          }
+        }
+        uint8_t reason;
+        uint64_t ss = 0, sc = 0;
+        r->r = orc_find_radius(mesh, &tpl, r->cx, r->cy, r->cz, r_search, threshold,
+          vol_factor, rmin, window, &reason, &ss, &sc);
+        span_sum += ss;
+        span_count += sc;
+        r->status = r->r < 0.0f ? ST_RESCALE : ST_ACCEPTED;
+      }
+
+      const uint64_t acc_before = st.accepted;
+      for (uint64_t b = 0; b < nb; b++) {
+        const result_t* r = &res[b];
+        if (r->status == ST_PROXY) {
+          st.rejected_proxy++;
+          continue;
+        }
+        if (r->status == ST_MESH) {
+          st.rejected_overlap++;
+          continue;
+        }
+        if (r->status == ST_RESCALE) {
+          st.rejected_rescale++;
+          st.n_rescaled++;
+          continue;
+        }
+        if (r->status == ST_WITNESS) {
+          st.rejected_witness++;
+          continue;
+        }
+        st.n_rescaled++;
+        if (mask_get(mask, cand[bidx[b]].flat)) {
+          st.rejected_masked++;
+          continue;
+        }
+        const int32_t exact_pole = (int32_t)(scale * r->r * (1.0f - f) / cell) - 1;
+        if (exact_pole > 0 &&
+            overlap_quick(mask, N, r->ix, r->iy, r->iz, (uint32_t)exact_pole)) {
+          st.rejected_proxy_recheck++;
+          continue;
+        }
+        if (overlap_exact(&V, r->cx, r->cy, r->cz, r->r, max_acc, box, f, scale)) {
+          st.rejected_exact++;
+          continue;
+        }
+        voids_add(&V, r->cx, r->cy, r->cz, r->r);
+        mark_sphere(mask, r->cx, r->cy, r->cz, scale * r->r, N, cell);
+        if (r->r > max_acc)
+          max_acc = r->r;
+        st.accepted++;
+      }
+
+      const uint64_t n_acc = st.accepted - acc_before;
+      if (n_acc == 0) {
+        batch_cap += floor_;
+        if (batch_cap > BATCH_MAX)
+          batch_cap = BATCH_MAX;
+      } else {
+        batch_cap /= (n_acc + 1);
+        if (batch_cap < floor_)
+          batch_cap = floor_;
+      }
+      if (p->window <= 0 && span_count > 0) {
+        uint64_t w = (span_sum * 2u + span_count - 1) / span_count;
+        if (w < 1)
+          w = 1;
+        if (w > 64)
+          w = 64;
+        window = (uint32_t)w;
+      }
+    }
+    orc_template_free(&tpl);
+    if (stats_out)
+      stats_out[ri] = st;
+  }
+
+  free(bidx);
+  free(res);
+  free(cand);
+  free(field);
+  free(mask);
+  free(radii);
+  orc_spectrum_free(spec);
+  if (status == 0) {
+    out->n_voids = V.n;
+    out->cx = V.cx;
+    out->cy = V.cy;
+    out->cz = V.cz;
+    out->r = V.r;
+    free(V.next);
+  } else {
+    voids_free(&V);
+  }
+  return status;
+}
+
+void orc_catalogue_free(orc_catalogue_t* c) {
+  free(c->cx);
+  free(c->cy);
+  free(c->cz);
+  free(c->r);
+  memset(c, 0, sizeof(*c));
+}

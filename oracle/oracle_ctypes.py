@@ -1,0 +1,220 @@
+"""ctypes wrapper of liboracle.so, this project's C restatement of sif's exodus
+path (exodus_oracle.c). TEST INFRASTRUCTURE ONLY: imported by tests/, by
+__graft_entry__.smoke() and by bench.py's CPU-baseline leg, as the checker;
+never by the product path.
+
+``build()`` compiles it with the Makefile beside this file (gcc + OpenMP),
+which works on both the x86 build machine and the Arm GPU machines.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+_lib = None
+
+
+def build(quiet=True):
+    out = subprocess.run(["make", "-s", "-C", HERE, "oracle"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+
+
+class Mesh(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("offsets", C.c_void_p), ("n_particles", C.c_uint64),
+                ("n_cells", C.c_uint32), ("box_length", C.c_float),
+                ("cell_length", C.c_float)]
+
+
+class Template(C.Structure):
+    _fields_ = [("dx", C.c_void_p), ("dy", C.c_void_p), ("dz", C.c_void_p),
+                ("type", C.c_void_p), ("min_d2", C.c_void_p), ("max_d2", C.c_void_p),
+                ("count", C.c_uint32)]
+
+
+class RungStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "n_candidates", "rejected_masked", "rejected_proxy", "rejected_overlap",
+        "rejected_rescale", "rejected_proxy_recheck", "rejected_exact",
+        "rejected_witness", "accepted", "n_rescaled")]
+
+
+class Params(C.Structure):
+    _fields_ = [("grid_n", C.c_uint32), ("box_length", C.c_float),
+                ("threshold", C.c_float), ("overlap_fraction", C.c_float),
+                ("options", C.c_uint32), ("n_threads", C.c_int), ("window", C.c_int),
+                ("smoothing_mode", C.c_int), ("inject", C.c_void_p)]
+
+
+class Catalogue(C.Structure):
+    _fields_ = [("cx", C.POINTER(C.c_float)), ("cy", C.POINTER(C.c_float)),
+                ("cz", C.POINTER(C.c_float)), ("r", C.POINTER(C.c_float)),
+                ("n_voids", C.c_uint64)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        vp, u64, u32, f32 = C.c_void_p, C.c_uint64, C.c_uint32, C.c_float
+        L.orc_chain_mesh.argtypes = [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]
+        L.orc_cic_f64.argtypes = [vp, vp, vp, u64, u32, f32, vp]
+        L.orc_density_contrast.argtypes = [vp, u64]
+        L.orc_spectrum_new.argtypes = [vp, u32, f32, C.c_int, C.c_int]
+        L.orc_spectrum_new.restype = vp
+        L.orc_spectrum_smooth.argtypes = [vp, C.c_int, f32, f32, vp, vp]
+        L.orc_spectrum_free.argtypes = [vp]
+        L.orc_sort_candidates.argtypes = [vp, u64]
+        L.orc_template_build.argtypes = [C.POINTER(Template), u32, f32, f32, f32]
+        L.orc_template_free.argtypes = [C.POINTER(Template)]
+        L.orc_find_radius.argtypes = [C.POINTER(Mesh), C.POINTER(Template), f32, f32, f32,
+                                      f32, f32, f32, f32, u32, C.POINTER(C.c_uint8),
+                                      C.POINTER(u64), C.POINTER(u64)]
+        L.orc_find_radius.restype = f32
+        L.orc_brute_force_radius.argtypes = [vp, vp, vp, u64, f32, C.c_double, C.c_double,
+                                             C.c_double, C.c_double, C.c_double, C.c_double]
+        L.orc_brute_force_radius.restype = C.c_double
+        L.orc_exodus.argtypes = [vp, C.POINTER(Mesh), vp, u32, C.POINTER(Params),
+                                 C.POINTER(Catalogue), vp]
+        L.orc_catalogue_free.argtypes = [C.POINTER(Catalogue)]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+CANDIDATE_DTYPE = np.dtype([("delta", np.float32), ("refined", np.uint32), ("flat", np.uint64)])
+
+
+class OracleMesh:
+    """A chain mesh built by the oracle; keeps its arrays alive."""
+
+    def __init__(self, x, y, z, n_cells, box):
+        n = len(x)
+        self.x = np.empty(n, np.float32)
+        self.y = np.empty(n, np.float32)
+        self.z = np.empty(n, np.float32)
+        self.offsets = np.empty(n_cells ** 3 + 1, np.uint64)
+        self.orig = np.empty(n, np.uint64)
+        xs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
+        st = lib().orc_chain_mesh(_p(xs[0]), _p(xs[1]), _p(xs[2]), n, n_cells, box,
+                                  _p(self.x), _p(self.y), _p(self.z), _p(self.offsets),
+                                  _p(self.orig))
+        if st != 0:
+            raise ValueError(f"orc_chain_mesh: {st}")
+        self.n_cells = n_cells
+        self.box = np.float32(box)
+        self.cell_length = np.float32(np.float32(box) / np.float32(n_cells))
+        self.struct = Mesh(_p(self.x), _p(self.y), _p(self.z), _p(self.offsets), n,
+                           n_cells, float(self.box), float(self.cell_length))
+
+    @classmethod
+    def from_arrays(cls, x, y, z, offsets, n_cells, box):
+        self = cls.__new__(cls)
+        self.x, self.y, self.z = (np.ascontiguousarray(a, np.float32) for a in (x, y, z))
+        self.offsets = np.ascontiguousarray(offsets, np.uint64)
+        self.orig = None
+        self.n_cells = n_cells
+        self.box = np.float32(box)
+        self.cell_length = np.float32(np.float32(box) / np.float32(n_cells))
+        self.struct = Mesh(_p(self.x), _p(self.y), _p(self.z), _p(self.offsets), len(self.x),
+                           n_cells, float(self.box), float(self.cell_length))
+        return self
+
+
+def cic_f64(x, y, z, n_grid, box):
+    out = np.empty(n_grid ** 3, np.float64)
+    xs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
+    lib().orc_cic_f64(_p(xs[0]), _p(xs[1]), _p(xs[2]), len(xs[0]), n_grid, box, _p(out))
+    return out
+
+
+def density_contrast(v):
+    v = np.ascontiguousarray(v, dtype=np.float32).copy()
+    st = lib().orc_density_contrast(_p(v), v.size)
+    if st != 0:
+        raise ValueError(f"orc_density_contrast: {st}")
+    return v
+
+
+def smooth(delta, n_grid, box, radii, filter=1, sigma=0.0, window_mode=1, mode=0,
+           want="f32"):
+    """Per-radius smoothed fields, (len(radii), n^3), float32 or float64."""
+    d = np.ascontiguousarray(delta, dtype=np.float32)
+    s = lib().orc_spectrum_new(_p(d), n_grid, box, window_mode, mode)
+    try:
+        out = np.empty((len(radii), n_grid ** 3), np.float64 if want == "f64" else np.float32)
+        for i, r in enumerate(radii):
+            row = out[i]
+            if want == "f64":
+                lib().orc_spectrum_smooth(s, filter, float(r), float(sigma), None, _p(row))
+            else:
+                lib().orc_spectrum_smooth(s, filter, float(r), float(sigma), _p(row), None)
+        return out
+    finally:
+        lib().orc_spectrum_free(s)
+
+
+def sort_candidates(records):
+    a = np.ascontiguousarray(records, dtype=CANDIDATE_DTYPE).copy()
+    lib().orc_sort_candidates(_p(a), len(a))
+    return a
+
+
+def find_radius(mesh, cx, cy, cz, radius, r_search, threshold, vol_factor, window=8):
+    t = Template()
+    st = lib().orc_template_build(C.byref(t), mesh.n_cells, float(mesh.cell_length),
+                                  float(radius), float(r_search))
+    if st != 0:
+        raise ValueError("template wider than the mesh")
+    try:
+        reason = C.c_uint8(0)
+        ss, sc = C.c_uint64(0), C.c_uint64(0)
+        r = lib().orc_find_radius(C.byref(mesh.struct), C.byref(t), cx, cy, cz, r_search,
+                                  threshold, vol_factor, radius, window, C.byref(reason),
+                                  C.byref(ss), C.byref(sc))
+        return r, reason.value
+    finally:
+        lib().orc_template_free(C.byref(t))
+
+
+def brute_force_radius(x, y, z, box, c, rung, r_search, threshold):
+    xs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
+    return lib().orc_brute_force_radius(_p(xs[0]), _p(xs[1]), _p(xs[2]), len(xs[0]), box,
+                                        float(c[0]), float(c[1]), float(c[2]), rung,
+                                        r_search, threshold)
+
+
+def exodus(delta, mesh, radii, n_grid, box, threshold, overlap=0.0, options=0, n_threads=1,
+           window=0, smoothing_mode=1, inject=None, with_stats=False):
+    """The oracle finder; returns (cx, cy, cz, r) float32 arrays."""
+    d = np.ascontiguousarray(delta, dtype=np.float32)
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    inj = None
+    if inject is not None:
+        inj = np.ascontiguousarray(inject, dtype=np.float32)
+        assert inj.shape == (len(radii), n_grid ** 3)
+    p = Params(n_grid, box, threshold, overlap, options, n_threads, window, smoothing_mode,
+               _p(inj) if inj is not None else None)
+    cat = Catalogue()
+    stats = (RungStats * len(radii))()
+    st = lib().orc_exodus(_p(d), C.byref(mesh.struct), _p(radii), len(radii), C.byref(p),
+                          C.byref(cat), stats)
+    if st != 0:
+        raise ValueError(f"orc_exodus: {st}")
+    n = cat.n_voids
+    out = tuple(np.ctypeslib.as_array(getattr(cat, k), shape=(n,)).copy() if n else
+                np.zeros(0, np.float32) for k in ("cx", "cy", "cz", "r"))
+    lib().orc_catalogue_free(C.byref(cat))
+    if with_stats:
+        return out, [{k: getattr(s, k) for k, _ in RungStats._fields_} for s in stats]
+    return out
