@@ -1,0 +1,327 @@
+/*
+ * sif_gb300.h -- the C ABI of the GB300 exodus library (libsif_gb300.so).
+ *
+ * Part 1 is sif's own C API for the exodus path: the same symbol names, the
+ * same struct layouts and the same status conventions as the reference's
+ * headers (single-precision build, sif_real = float), so that pysif, the
+ * sif-exodus CLI and C callers link against this library unchanged. Each
+ * declaration names the reference declaration it replaces. The work runs on
+ * one GPU; the structs stay in host memory, and every call copies what it
+ * needs to the device and its result back.
+ *
+ * Part 2 is additive: entry points that take device pointers, for callers
+ * that keep particles and grids resident in GPU memory, plus the stage-level
+ * calls the parity tests use. They have no counterpart in the reference.
+ */
+#ifndef SIF_GB300_H
+#define SIF_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* Part 1: sif's API                                                       */
+/* ---------------------------------------------------------------------- */
+
+/* include/sif/core/macros.h:42, 468-506 */
+typedef uint32_t sif_option;
+typedef float sif_real;
+
+/* include/sif/core/macros.h:690-707 */
+#define SIF_OK                0
+#define SIF_ERR_ALLOC         (-1)
+#define SIF_ERR_INVALID       (-2)
+#define SIF_ERR_RANGE         (-3)
+#define SIF_ERR_IO            (-4)
+#define SIF_ERR_UNSUPPORTED   (-5)
+#define SIF_ERR_UNINITIALISED (-6)
+
+/* include/sif/core/macros.h:73-292 (the finder and mesh options) */
+#define SIF_FINDER_ALIASING_WINDOW    (1u << 8)
+#define SIF_FINDER_SEEDS_CELLS        (0u << 9)
+#define SIF_FINDER_SEEDS_MINIMA       (1u << 9)
+#define SIF_FINDER_NO_CHECKPOINT      (1u << 11)
+#define SIF_FINDER_SEARCH_1_50        (0u << 12)
+#define SIF_FINDER_SEARCH_1_25        (1u << 12)
+#define SIF_FINDER_SEARCH_1_75        (2u << 12)
+#define SIF_FINDER_SEARCH_2_00        (3u << 12)
+#define SIF_FINDER_KEEP_CIC_WINDOW    (1u << 14)
+#define SIF_FINDER_CONSUME_GRID       (1u << 15)
+#define SIF_MESH_DROP_INDICES         (1u << 16)
+#define SIF_MESH_NO_CANONICAL         (1u << 17)
+#define SIF_FINDER_LAGRANGIAN_OVERLAP (1u << 18)
+#define SIF_FINDER_REFINE_NONE        (0u << 19)
+#define SIF_FINDER_REFINE_GAUSSIAN    (1u << 19)
+#define SIF_FINDER_REFINE_TRACERS     (2u << 19)
+#define SIF_FINDER_REFINE_HILL        (3u << 19)
+#define SIF_FINDER_EXTEND_REACH       (1u << 21)
+#define SIF_FINDER_DISPLACE           (1u << 22)
+
+/* include/sif/core/macros.h:772-777 */
+#define SIF_LOG_LEVEL_TRACE   0
+#define SIF_LOG_LEVEL_DEBUG   1
+#define SIF_LOG_LEVEL_INFO    2
+#define SIF_LOG_LEVEL_WARNING 3
+#define SIF_LOG_LEVEL_ERROR   4
+#define SIF_LOG_LEVEL_NONE    5
+
+/* include/sif/core/system.h:44-100 */
+typedef struct {
+  bool skip_tuning;
+} sif_fft_config_t;
+typedef struct {
+  uint32_t n_threads;
+} sif_omp_config_t;
+typedef struct {
+  const char* key;
+  const char* value;
+} sif_setting_t;
+typedef struct {
+  sif_fft_config_t* fft_config;
+  sif_omp_config_t* omp_config;
+  uint8_t log_level;
+  const sif_setting_t* settings;
+  size_t n_settings;
+} sif_config_t;
+
+/* include/sif/structures/field.h:90-133 */
+typedef enum { SIF_COORDINATES_CARTESIAN = 0, SIF_COORDINATES_SKY } sif_coordinates_t;
+typedef struct {
+  sif_real* _position_block;
+  sif_real* _velocity_block;
+  sif_real* x;
+  sif_real* y;
+  sif_real* z;
+  sif_real* vx;
+  sif_real* vy;
+  sif_real* vz;
+  sif_real* weights;
+  uint64_t* original_indices;
+  sif_real min_p[3];
+  sif_real max_p[3];
+  sif_real centre[3];
+  sif_real half_span;
+  uint32_t state_flags;
+  uint64_t n_particles;
+  sif_coordinates_t units;
+} sif_field_t;
+
+/* include/sif/structures/grid.h:32-128 */
+typedef enum {
+  SIF_GRID_EMPTY = 0,
+  SIF_GRID_DENSITY,
+  SIF_GRID_DENSITY_CONTRAST
+} sif_grid_content_t;
+typedef enum {
+  SIF_ASSIGNMENT_UNKNOWN = 0,
+  SIF_ASSIGNMENT_NGP = 1,
+  SIF_ASSIGNMENT_CIC = 2,
+  SIF_ASSIGNMENT_TSC = 3,
+  SIF_ASSIGNMENT_PCS = 4
+} sif_assignment_t;
+typedef struct {
+  sif_real* values;
+  sif_grid_content_t content;
+  sif_assignment_t assignment;
+  uint32_t interlaced;
+  uint32_t n_cells;
+  uint64_t total_cells;
+  sif_real box_length;
+  sif_real cell_length;
+  uint32_t p2_mask;
+  uint32_t p2_shift;
+} sif_grid_t;
+
+/* include/sif/structures/chain_mesh.h:40-108 */
+typedef struct {
+  uint32_t n_cells;
+  uint64_t total_cells;
+  sif_real box_length;
+  sif_real cell_length;
+  sif_real* _position_block;
+  sif_real* _velocity_block;
+  sif_real* x;
+  sif_real* y;
+  sif_real* z;
+  sif_real* vx;
+  sif_real* vy;
+  sif_real* vz;
+  sif_real* weights;
+  double total_weight;
+  sif_real* cell_weights;
+  uint64_t* original_indices;
+  uint64_t n_particles;
+  uint64_t* cell_offsets;
+} sif_chain_mesh_t;
+
+/* include/sif/structures/catalogue.h:38-93 */
+typedef struct {
+  sif_real* _block;
+  sif_real* cx;
+  sif_real* cy;
+  sif_real* cz;
+  sif_real* radii;
+  sif_real* _footprint_block;
+  sif_real* footprint;
+  sif_real* footprint_shell;
+  sif_coordinates_t units;
+  void* _meta;
+  uint32_t _n_meta;
+  uint64_t n_voids;
+  uint64_t capacity;
+} sif_catalogue_t;
+
+/* include/sif/finder/exodus_finder.h:40-106 */
+typedef struct {
+  const char* checkpoint;
+  const sif_catalogue_t* prior;
+  int keep_checkpoint;
+  int save_memory;
+} sif_finder_exodus_extras_t;
+
+/* include/sif/finder/exodus_finder.h:124-133 */
+typedef enum {
+  SIF_EXODUS_EXCURSION_SET = 0,
+  SIF_EXODUS_EXCURSION_PEAK,
+  SIF_EXODUS_LAGRANGIAN_OVERLAP,
+  SIF__EXODUS_N_VARIANTS
+} sif_exodus_variant_t;
+
+/* include/sif/finder/exodus_finder.h:689-695 */
+typedef enum { SIF_FINDER_UNITS_PHYSICAL = 0, SIF_FINDER_UNITS_MPS } sif_finder_units_t;
+
+/* include/sif/core/system.h:118 -- selects the GPU (CUDA_VISIBLE_DEVICES /
+ * device 0) and sizes the host team that replays the candidate order. */
+int sif_system_init(sif_config_t* config);
+/* include/sif/core/system.h:127 */
+void sif_system_finalise(void);
+/* include/sif/utils/logger.h:330 */
+const char* sif_error_message(void);
+/* include/sif/utils/logger.h:346 */
+int sif_error_status(void);
+
+/* include/sif/structures/field.h:146, 165, 202 */
+sif_field_t* sif_field_alloc(uint64_t n_particles);
+void sif_field_free(sif_field_t* field);
+int sif_field_assign_positions(sif_field_t* field, const sif_real* x, const sif_real* y,
+                               const sif_real* z);
+
+/* include/sif/structures/grid.h:140, 147, 212, 233 */
+sif_grid_t* sif_grid_alloc(uint32_t n_cells, sif_real box_length);
+void sif_grid_free(sif_grid_t* grid);
+int sif_grid_assign_cic(sif_grid_t* grid, const sif_field_t* field);
+int sif_grid_to_density_contrast(sif_grid_t* grid);
+
+/* include/sif/structures/chain_mesh.h:141, 175, 182 */
+sif_chain_mesh_t* sif_chain_mesh_alloc(uint32_t n_cells, sif_real box_length,
+                                       const sif_field_t* field, sif_option opt);
+sif_chain_mesh_t* sif_chain_mesh_alloc_consume(uint32_t n_cells, sif_real box_length,
+                                               sif_field_t* field, sif_option opt);
+void sif_chain_mesh_free(sif_chain_mesh_t* mesh);
+
+/* include/sif/structures/catalogue.h:116 */
+void sif_catalogue_free(sif_catalogue_t* catalogue);
+
+/* include/sif/finder/exodus_finder.h:147, 155, 163 */
+int sif_finder_exodus_preset(sif_exodus_variant_t variant, sif_real* overlap_fraction,
+                             sif_option* opt);
+const char* sif_finder_exodus_variant_name(sif_exodus_variant_t variant);
+int sif_finder_exodus_variant_from_name(const char* name, sif_exodus_variant_t* variant);
+
+/* include/sif/finder/exodus_finder.h:177-180 */
+sif_catalogue_t* sif_finder_exodus(sif_grid_t* grid, const sif_chain_mesh_t* mesh,
+                                   const sif_real* radii, uint32_t n_radii, sif_real threshold,
+                                   sif_exodus_variant_t variant,
+                                   const sif_finder_exodus_extras_t* extras);
+/* include/sif/finder/exodus_finder.h:290-293 */
+sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t* mesh,
+                                       const sif_real* radii, uint32_t n_radii,
+                                       sif_real threshold, sif_real overlap_fraction,
+                                       sif_option opt, const sif_finder_exodus_extras_t* extras);
+
+/* include/sif/finder/exodus_finder.h:721-723 */
+uint32_t sif_finder_grid_cells_from_size(uint64_t n_particles, sif_real box_length,
+                                         sif_real cell_size, sif_finder_units_t units,
+                                         sif_real volume);
+
+/* ---------------------------------------------------------------------- */
+/* Part 2: device-resident entry points (no counterpart in the reference)  */
+/* ---------------------------------------------------------------------- */
+
+/* Per-rung counts of the last sifg_exodus_device / sifg_box_device run. */
+typedef struct {
+  float radius;
+  float r_search;
+  uint64_t n_candidates;
+  uint64_t n_survivors;
+  uint64_t n_accepted;
+  uint64_t rounds;
+  uint64_t n_rescale_fail;
+  uint64_t n_overflow;
+} sifg_rung_stat_t;
+
+/* Kernel timings of the last run, CUDA events on the launching stream. */
+typedef struct {
+  double wall_ms;
+  double growth_ms;
+  int growth_launches;
+  double filter_ms;
+  int filter_launches;
+  double cic_ms;
+  int cic_launches;
+  double mesh_ms;
+  int mesh_launches;
+} sifg_timings_t;
+
+/* The CIC density (per unit volume, float) of n device-resident particles
+ * on an n_grid^3 device grid. */
+int sifg_cic_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
+                    float box, float* grid);
+/* Density to density contrast in place; *mean_out (may be NULL) receives
+ * the mean density. */
+int sifg_contrast_device(float* grid, uint64_t total_cells, double* mean_out);
+/* A chain mesh of device particles into device arrays: positions (n each),
+ * offsets (n_cells^3 + 1, uint32), source indices (n, uint32; may be NULL). */
+int sifg_mesh_device(const float* x, const float* y, const float* z, uint64_t n,
+                     uint32_t n_cells, float box, float* mx, float* my, float* mz,
+                     uint32_t* offsets, uint32_t* orig);
+/* The density contrast on the device smoothed at radius r (filter 1
+ * top-hat, 2 Gaussian; window_mode 0 none, 1 CIC, 2 aliasing-aware) into a
+ * device grid. */
+int sifg_smooth_device(const float* delta, uint32_t n_grid, float box, float r, int filter,
+                       int window_mode, float* out);
+/* The exodus finder on a device density contrast and a device mesh. radii in
+ * host memory. inject: NULL, or n_radii device grids that replace the
+ * smoothing, largest radius first. The catalogue is written to the host
+ * arrays (capacity entries each); *n_voids receives the count (which may
+ * exceed capacity: then only capacity are written). */
+int sifg_exodus_device(const float* delta, uint32_t n_grid, float box, const float* mx,
+                       const float* my, const float* mz, const uint32_t* offsets,
+                       uint64_t n_particles, uint32_t mesh_cells, const float* radii,
+                       uint32_t n_radii, float threshold, float overlap, uint32_t opt,
+                       const float* inject, float* cx, float* cy, float* cz, float* r,
+                       uint64_t capacity, uint64_t* n_voids);
+/* The whole box path on device particles: CIC, contrast, mesh, exodus. */
+int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
+                    float box, uint32_t mesh_cells, const float* radii, uint32_t n_radii,
+                    float threshold, float overlap, uint32_t opt, float* cx, float* cy,
+                    float* cz, float* r, uint64_t capacity, uint64_t* n_voids);
+/* Statistics and timings of the last run (up to max_rungs entries). */
+uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs);
+void sifg_last_timings(sifg_timings_t* out);
+/* The resolve window (bins per pass) the sphere growth uses; default 8. */
+void sifg_set_window(int bins);
+/* The replay of the reference's candidate order on host data, for tests:
+ * rank[k] = sorted position of delta[k]. */
+void sifg_candidate_ranks(const float* delta, uint32_t m, uint32_t* rank);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIF_GB300_H */

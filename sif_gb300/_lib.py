@@ -1,0 +1,89 @@
+"""Loads libsif_gb300.so (built in-tree by sif_gb300/build.py) and declares
+its C signatures (include/sif_gb300.h). There is no fallback: a missing
+library is an ImportError-like failure the caller sees.
+"""
+import ctypes as C
+import os
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsif_gb300.so")
+
+_lib = None
+
+
+class RungStat(C.Structure):
+    _fields_ = [("radius", C.c_float), ("r_search", C.c_float),
+                ("n_candidates", C.c_uint64), ("n_survivors", C.c_uint64),
+                ("n_accepted", C.c_uint64), ("rounds", C.c_uint64),
+                ("n_rescale_fail", C.c_uint64), ("n_overflow", C.c_uint64)]
+
+
+class Timings(C.Structure):
+    _fields_ = [("wall_ms", C.c_double), ("growth_ms", C.c_double), ("growth_launches", C.c_int),
+                ("filter_ms", C.c_double), ("filter_launches", C.c_int),
+                ("cic_ms", C.c_double), ("cic_launches", C.c_int),
+                ("mesh_ms", C.c_double), ("mesh_launches", C.c_int)]
+
+
+EXPORTED = [
+    # sif's API
+    "sif_system_init", "sif_system_finalise", "sif_error_message", "sif_error_status",
+    "sif_field_alloc", "sif_field_free", "sif_field_assign_positions",
+    "sif_grid_alloc", "sif_grid_free", "sif_grid_assign_cic", "sif_grid_to_density_contrast",
+    "sif_chain_mesh_alloc", "sif_chain_mesh_alloc_consume", "sif_chain_mesh_free",
+    "sif_catalogue_free", "sif_finder_exodus_preset", "sif_finder_exodus_variant_name",
+    "sif_finder_exodus_variant_from_name", "sif_finder_exodus", "sif_finder_exodus_raw",
+    "sif_finder_grid_cells_from_size",
+    # device-resident additions
+    "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
+    "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
+    "sifg_set_window", "sifg_candidate_ranks",
+]
+
+
+def load():
+    """The library, loaded once; raises OSError when it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OSError(f"{LIB_PATH} is not built; run sif_gb300/build.py "
+                      "(or __graft_entry__.build())")
+    lib = C.CDLL(LIB_PATH)
+    abi.bind_sif_api(lib)
+    vp, u32, u64, f32, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_int
+    sigs = {
+        "sifg_cic_device": (i32, [vp, vp, vp, u64, u32, f32, vp]),
+        "sifg_contrast_device": (i32, [vp, u64, C.POINTER(C.c_double)]),
+        "sifg_mesh_device": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]),
+        "sifg_smooth_device": (i32, [vp, u32, f32, f32, i32, i32, vp]),
+        "sifg_exodus_device": (i32, [vp, u32, f32, vp, vp, vp, vp, u64, u32, vp, u32, f32, f32,
+                                     u32, vp, vp, vp, vp, vp, u64, C.POINTER(u64)]),
+        "sifg_box_device": (i32, [vp, vp, vp, u64, u32, f32, u32, vp, u32, f32, f32, u32,
+                                  vp, vp, vp, vp, u64, C.POINTER(u64)]),
+        "sifg_last_rung_stats": (u32, [C.POINTER(RungStat), u32]),
+        "sifg_last_timings": (None, [C.POINTER(Timings)]),
+        "sifg_set_window": (None, [i32]),
+        "sifg_candidate_ranks": (None, [vp, u32, vp]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def status_error(lib, status, what):
+    """The exception pysif raises for a sif status (python/src/py_common.h)."""
+    msg = lib.sif_error_message()
+    text = f"{what}: {msg.decode() if msg else status}"
+    if status == abi.SIF_ERR_UNINITIALISED:
+        return RuntimeError(text)
+    if status == abi.SIF_ERR_ALLOC:
+        return MemoryError(text)
+    if status == abi.SIF_ERR_UNSUPPORTED:
+        return NotImplementedError(text)
+    return ValueError(text)

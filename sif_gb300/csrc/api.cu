@@ -1,0 +1,901 @@
+// sif's C API for the exodus path over the GPU engine, and the additive
+// device-resident entry points (include/sif_gb300.h).
+//
+// The structs are the reference's and live in host memory; each call copies
+// what it needs to the GPU and its results back, and checks its arguments as
+// the reference does, with the same statuses (include/sif/core/macros.h:
+// 690-707) and an error message for sif_error_message().
+#include <cuda_runtime.h>
+#include <omp.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sif_gb300.h"
+#include "engine.cuh"
+
+namespace sifg {
+
+namespace {
+std::mutex g_mu;
+std::unique_ptr<Engine> g_engine;
+bool g_init = false;
+int g_log_level = SIF_LOG_LEVEL_INFO;
+int g_status = SIF_OK;
+std::string g_message;
+std::vector<RungStat> g_stats;
+sifg_timings_t g_timings{};
+int g_window = 8;
+
+void log_msg(int level, const char* tag, const std::string& msg) {
+  if (level < g_log_level) return;
+  static const char* names[] = {"TRACE", "DEBUG", "INFO", "WARNING", "ERROR"};
+  fprintf(stderr, "[%s] %s: %s\n", names[level < 5 ? level : 4], tag, msg.c_str());
+}
+
+std::string fmt(const char* f, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, f);
+  vsnprintf(buf, sizeof buf, f, ap);
+  va_end(ap);
+  return buf;
+}
+}  // namespace
+
+void set_error(int status, const std::string& msg) {
+  g_status = status;
+  g_message = msg;
+  log_msg(SIF_LOG_LEVEL_ERROR, "gb300", msg);
+}
+
+static int fail(int status, const std::string& msg) {
+  set_error(status, msg);
+  return status;
+}
+
+// Maps a CUDA failure to a status; a missing or lost device is an error the
+// caller sees, never a silent fallback.
+static int cuda_fail(const CudaError& e) {
+  return fail(e.code == cudaErrorMemoryAllocation ? SIF_ERR_ALLOC : SIF_ERR_INVALID,
+              fmt("CUDA: %s (%s)", cudaGetErrorString(e.code), e.where));
+}
+
+static Engine* engine() {
+  if (!g_init || !g_engine) {
+    set_error(SIF_ERR_UNINITIALISED, "sif_system_init() has not been called");
+    return nullptr;
+  }
+  SIFG_CUDA(cudaSetDevice(g_engine->device()));
+  return g_engine.get();
+}
+
+// --- device scratch for the C API's copies -------------------------------
+
+struct ApiBufs {
+  DevBuf px, py, pz, grid, mx, my, mz, offs, orig, bad;
+};
+static ApiBufs& bufs() {
+  static ApiBufs b;
+  return b;
+}
+
+// sif__field_check_in_box (src/structures/field.c:889-935): every coordinate
+// in [0, L), or within 4 float epsilons of L of a face (folded later).
+__global__ void box_check_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                 const float* __restrict__ z, uint64_t n, float box, double tol,
+                                 unsigned long long* __restrict__ out) {
+  unsigned long long bad = 0, edge = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const float v[3] = {x[i], y[i], z[i]};
+    bool inside = true, accepted = true;
+    for (int a = 0; a < 3; a++) {
+      inside = inside && v[a] >= 0.0f && v[a] < box;
+      const double d = (double)v[a];
+      accepted = accepted && d >= -tol && d <= (double)box + tol;
+    }
+    if (!inside) {
+      if (accepted)
+        edge++;
+      else
+        bad++;
+    }
+  }
+  for (int d = 16; d > 0; d >>= 1) {
+    bad += __shfl_down_sync(0xffffffffu, bad, d);
+    edge += __shfl_down_sync(0xffffffffu, edge, d);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (bad) atomicAdd(out, bad);
+    if (edge) atomicAdd(out + 1, edge);
+  }
+}
+
+static int check_in_box(const float* dx, const float* dy, const float* dz, uint64_t n, float box,
+                        const char* name, cudaStream_t st) {
+  unsigned long long* d = (unsigned long long*)bufs().bad.ensure(16);
+  SIFG_CUDA(cudaMemsetAsync(d, 0, 16, st));
+  const double tol = (double)box * 4.0 * (double)FLT_EPSILON;
+  box_check_kernel<<<grid_for(n, 256), 256, 0, st>>>(dx, dy, dz, n, box, tol, d);
+  SIFG_LAUNCH_CHECK();
+  unsigned long long h[2];
+  SIFG_CUDA(cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, st));
+  SIFG_CUDA(cudaStreamSynchronize(st));
+  if (h[0])
+    return fail(SIF_ERR_RANGE,
+                fmt("%s: %llu of %llu particles outside the box [0, %g)", name, h[0],
+                    (unsigned long long)n, (double)box));
+  return SIF_OK;
+}
+
+static int check_field(const sif_field_t* field, const char* tag) {
+  if (!field) return fail(SIF_ERR_INVALID, fmt("%s: field: NULL", tag));
+  if (field->n_particles == 0) return fail(SIF_ERR_INVALID, fmt("%s: field: no particles", tag));
+  if (!field->x || !field->y || !field->z)
+    return fail(SIF_ERR_INVALID, fmt("%s: field: no positions", tag));
+  if (field->units != SIF_COORDINATES_CARTESIAN)
+    return fail(SIF_ERR_INVALID, fmt("%s: field: sky coordinates (expected Cartesian)", tag));
+  return SIF_OK;
+}
+
+static void upload_positions(const sif_field_t* f, cudaStream_t st) {
+  const size_t b = f->n_particles * sizeof(float);
+  SIFG_CUDA(cudaMemcpyAsync(bufs().px.ensure(b), f->x, b, cudaMemcpyHostToDevice, st));
+  SIFG_CUDA(cudaMemcpyAsync(bufs().py.ensure(b), f->y, b, cudaMemcpyHostToDevice, st));
+  SIFG_CUDA(cudaMemcpyAsync(bufs().pz.ensure(b), f->z, b, cudaMemcpyHostToDevice, st));
+}
+
+static sif_catalogue_t* make_catalogue(const HostCatalogue& c) {
+  const uint64_t n = c.cx.size();
+  sif_catalogue_t* cat = (sif_catalogue_t*)calloc(1, sizeof(sif_catalogue_t));
+  if (!cat) return nullptr;
+  const uint64_t cap = n ? n : 1;
+  cat->_block = (float*)malloc(4 * cap * sizeof(float));
+  if (!cat->_block) {
+    free(cat);
+    return nullptr;
+  }
+  cat->cx = cat->_block;
+  cat->cy = cat->_block + cap;
+  cat->cz = cat->_block + 2 * cap;
+  cat->radii = cat->_block + 3 * cap;
+  if (n) {
+    memcpy(cat->cx, c.cx.data(), n * 4);
+    memcpy(cat->cy, c.cy.data(), n * 4);
+    memcpy(cat->cz, c.cz.data(), n * 4);
+    memcpy(cat->radii, c.r.data(), n * 4);
+  }
+  cat->units = SIF_COORDINATES_CARTESIAN;
+  cat->n_voids = n;
+  cat->capacity = cap;
+  return cat;
+}
+
+static void record_timings(RunTimings& t) {
+  g_timings.wall_ms = t.wall_ms;
+  g_timings.growth_ms = t.growth.total_ms();
+  g_timings.growth_launches = t.growth.launches();
+  g_timings.filter_ms = t.filter.total_ms();
+  g_timings.filter_launches = t.filter.launches();
+  g_timings.cic_ms = t.cic.total_ms();
+  g_timings.cic_launches = t.cic.launches();
+  g_timings.mesh_ms = t.mesh.total_ms();
+  g_timings.mesh_launches = t.mesh.launches();
+}
+
+}  // namespace sifg
+
+using namespace sifg;
+
+#define API_GUARD_BEGIN try {
+#define API_GUARD_END(ret)                                                              \
+  }                                                                                     \
+  catch (const CudaError& e) {                                                          \
+    cuda_fail(e);                                                                       \
+    return ret;                                                                         \
+  }                                                                                     \
+  catch (const std::bad_alloc&) {                                                       \
+    fail(SIF_ERR_ALLOC, "out of host memory");                                          \
+    return ret;                                                                         \
+  }
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// System
+// ---------------------------------------------------------------------------
+
+int sif_system_init(sif_config_t* config) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (config) g_log_level = config->log_level;
+  if (g_init) return SIF_OK;
+  API_GUARD_BEGIN
+  int n_dev = 0;
+  const cudaError_t e = cudaGetDeviceCount(&n_dev);
+  if (e != cudaSuccess || n_dev == 0)
+    return fail(SIF_ERR_UNSUPPORTED,
+                fmt("no CUDA device (%s): this library runs the exodus path on a GPU only",
+                    e != cudaSuccess ? cudaGetErrorString(e) : "none found"));
+  g_engine.reset(new Engine(0));
+  g_engine->host_threads =
+      (config && config->omp_config && config->omp_config->n_threads) ? (int)config->omp_config->n_threads
+                                                                      : omp_get_max_threads();
+  g_init = true;
+  g_status = SIF_OK;
+  g_message.clear();
+  return SIF_OK;
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+void sif_system_finalise(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_engine.reset();
+  g_init = false;
+  g_log_level = SIF_LOG_LEVEL_INFO;
+}
+
+const char* sif_error_message(void) { return g_message.c_str(); }
+int sif_error_status(void) { return g_status; }
+
+// ---------------------------------------------------------------------------
+// Field, grid, catalogue (host structs; src/structures/field.c, grid.c:64-108,
+// catalogue.c)
+// ---------------------------------------------------------------------------
+
+sif_field_t* sif_field_alloc(uint64_t n_particles) {
+  sif_field_t* f = (sif_field_t*)calloc(1, sizeof(sif_field_t));
+  if (!f) {
+    fail(SIF_ERR_ALLOC, "field: cannot allocate");
+    return nullptr;
+  }
+  f->n_particles = n_particles;
+  f->units = SIF_COORDINATES_CARTESIAN;
+  return f;
+}
+
+void sif_field_free(sif_field_t* f) {
+  if (!f) return;
+  free(f->_position_block);
+  free(f->_velocity_block);
+  free(f->weights);
+  free(f->original_indices);
+  free(f);
+}
+
+int sif_field_assign_positions(sif_field_t* f, const sif_real* x, const sif_real* y,
+                               const sif_real* z) {
+  if (!f || !x || !y || !z) return fail(SIF_ERR_INVALID, "field: NULL argument");
+  const uint64_t n = f->n_particles;
+  if (!f->_position_block) {
+    f->_position_block = (float*)malloc(3 * (n ? n : 1) * sizeof(float));
+    if (!f->_position_block) return fail(SIF_ERR_ALLOC, "field: cannot allocate positions");
+    f->x = f->_position_block;
+    f->y = f->_position_block + n;
+    f->z = f->_position_block + 2 * n;
+  }
+  memcpy(f->x, x, n * sizeof(float));
+  memcpy(f->y, y, n * sizeof(float));
+  memcpy(f->z, z, n * sizeof(float));
+  free(f->original_indices);
+  f->original_indices = nullptr;
+  f->state_flags = 0;
+  return SIF_OK;
+}
+
+sif_grid_t* sif_grid_alloc(uint32_t n_cells, sif_real box_length) {
+  if (n_cells == 0) {
+    fail(SIF_ERR_INVALID, "n_cells: 0 (expected > 0)");
+    return nullptr;
+  }
+  if (!(box_length > 0.0f)) {
+    fail(SIF_ERR_INVALID, fmt("box_length: %g (expected > 0)", (double)box_length));
+    return nullptr;
+  }
+  sif_grid_t* g = (sif_grid_t*)calloc(1, sizeof(sif_grid_t));
+  if (!g) {
+    fail(SIF_ERR_ALLOC, "grid: cannot allocate");
+    return nullptr;
+  }
+  g->n_cells = n_cells;
+  g->total_cells = (uint64_t)n_cells * n_cells * n_cells;
+  g->box_length = box_length;
+  g->cell_length = box_length / (float)n_cells;
+  g->p2_mask = ((n_cells & (n_cells - 1)) == 0) ? (n_cells - 1) : 0;
+  g->p2_shift = g->p2_mask ? (uint32_t)__builtin_ctz(n_cells) : 0;
+  g->content = SIF_GRID_EMPTY;
+  g->assignment = SIF_ASSIGNMENT_UNKNOWN;
+  g->values = (float*)calloc(g->total_cells, sizeof(float));
+  if (!g->values) {
+    free(g);
+    fail(SIF_ERR_ALLOC, fmt("grid: cannot allocate %u^3 cells", n_cells));
+    return nullptr;
+  }
+  return g;
+}
+
+void sif_grid_free(sif_grid_t* g) {
+  if (!g) return;
+  free(g->values);
+  free(g);
+}
+
+void sif_catalogue_free(sif_catalogue_t* c) {
+  if (!c) return;
+  free(c->_block);
+  free(c->_footprint_block);
+  free(c);
+}
+
+// sif_grid_assign with SIF_ASSIGNMENT_CIC (src/structures/grid.c:1042-1175).
+int sif_grid_assign_cic(sif_grid_t* grid, const sif_field_t* field) {
+  if (!grid || !grid->values) return fail(SIF_ERR_INVALID, grid ? "grid: no cell values" : "grid: NULL");
+  if (grid->n_cells < 4)
+    return fail(SIF_ERR_INVALID,
+                fmt("n_cells: %u (expected at least 4 to assign onto)", grid->n_cells));
+  int st = check_field(field, "grid");
+  if (st != SIF_OK) return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  cudaStream_t s = e->stream();
+  upload_positions(field, s);
+  st = check_in_box(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(),
+                    field->n_particles, grid->box_length, "field", s);
+  if (st != SIF_OK) return st;
+  float* dg = (float*)bufs().grid.ensure(grid->total_cells * sizeof(float));
+  e->scratch.ensure(cic_scratch_bytes(field->n_particles, grid->n_cells));
+  cic_deposit(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(),
+              field->n_particles, grid->n_cells, grid->box_length, dg, e->scratch.ptr, s, nullptr);
+  SIFG_CUDA(cudaMemcpyAsync(grid->values, dg, grid->total_cells * sizeof(float),
+                            cudaMemcpyDeviceToHost, s));
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  grid->content = SIF_GRID_DENSITY;
+  grid->assignment = SIF_ASSIGNMENT_CIC;
+  grid->interlaced = 0;
+  return SIF_OK;
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+// src/structures/grid.c:1177-1244.
+int sif_grid_to_density_contrast(sif_grid_t* grid) {
+  if (!grid || !grid->values) return fail(SIF_ERR_INVALID, grid ? "grid: no cell values" : "grid: NULL");
+  if (grid->content == SIF_GRID_DENSITY_CONTRAST)
+    return fail(SIF_ERR_INVALID,
+                "grid: already a density contrast (converting again would divide by a mean of about 0)");
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  cudaStream_t s = e->stream();
+  const size_t b = grid->total_cells * sizeof(float);
+  float* dg = (float*)bufs().grid.ensure(b);
+  SIFG_CUDA(cudaMemcpyAsync(dg, grid->values, b, cudaMemcpyHostToDevice, s));
+  double* scratch = (double*)e->scratch.ensure(density_contrast_scratch_bytes());
+  density_contrast(dg, grid->total_cells, scratch, s);
+  const double mean = read_mean(scratch);
+  if (!(mean > 0.0))
+    return fail(SIF_ERR_RANGE, fmt("grid: mean density %g (expected > 0)", mean));
+  SIFG_CUDA(cudaMemcpyAsync(grid->values, dg, b, cudaMemcpyDeviceToHost, s));
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  grid->content = SIF_GRID_DENSITY_CONTRAST;
+  return SIF_OK;
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+// sif_chain_mesh_alloc / _consume (src/structures/chain_mesh.c:49-215).
+static sif_chain_mesh_t* mesh_alloc(uint32_t n_cells, sif_real box, sif_field_t* field,
+                                    sif_option opt, bool consume) {
+  if (check_field(field, "mesh") != SIF_OK) return nullptr;
+  if (n_cells == 0) {
+    fail(SIF_ERR_INVALID, "n_cells: 0 (expected > 0)");
+    return nullptr;
+  }
+  if (!(box > 0.0f)) {
+    fail(SIF_ERR_INVALID, fmt("box_length: %g (expected > 0)", (double)box));
+    return nullptr;
+  }
+  if (field->weights || field->vx) {
+    fail(SIF_ERR_UNSUPPORTED, "mesh: weighted or velocity-carrying fields are not supported on the GPU");
+    return nullptr;
+  }
+  const uint64_t n = field->n_particles;
+  if (n >= 0xffffffffull) {
+    fail(SIF_ERR_RANGE, "mesh: 2^32 particles or more");
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return nullptr;
+  cudaStream_t s = e->stream();
+  upload_positions(field, s);
+  if (check_in_box(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(), n, box,
+                   "field", s) != SIF_OK)
+    return nullptr;
+  DeviceMesh m;
+  m.n_cells = n_cells;
+  m.box_length = box;
+  m.cell_length = box / (float)n_cells;
+  const uint64_t cells = (uint64_t)n_cells * n_cells * n_cells;
+  m.x = (float*)bufs().mx.ensure(n * 4);
+  m.y = (float*)bufs().my.ensure(n * 4);
+  m.z = (float*)bufs().mz.ensure(n * 4);
+  m.offsets = (uint32_t*)bufs().offs.ensure((cells + 1) * 4);
+  const bool keep_idx = !(opt & SIF_MESH_DROP_INDICES);
+  m.orig = keep_idx ? (uint32_t*)bufs().orig.ensure(n * 4) : nullptr;
+  e->scratch.ensure(mesh_scratch_bytes(n, n_cells));
+  mesh_build(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(), n, m,
+             e->scratch.ptr, s, nullptr);
+
+  sif_chain_mesh_t* mesh = (sif_chain_mesh_t*)calloc(1, sizeof(sif_chain_mesh_t));
+  mesh->n_cells = n_cells;
+  mesh->total_cells = cells;
+  mesh->box_length = box;
+  mesh->cell_length = m.cell_length;
+  mesh->n_particles = n;
+  mesh->total_weight = (double)n;
+  mesh->_position_block = (float*)malloc(3 * (n ? n : 1) * sizeof(float));
+  mesh->x = mesh->_position_block;
+  mesh->y = mesh->_position_block + n;
+  mesh->z = mesh->_position_block + 2 * n;
+  mesh->cell_offsets = (uint64_t*)malloc((cells + 1) * sizeof(uint64_t));
+  std::vector<uint32_t> offs32(cells + 1);
+  SIFG_CUDA(cudaMemcpyAsync(mesh->x, m.x, n * 4, cudaMemcpyDeviceToHost, s));
+  SIFG_CUDA(cudaMemcpyAsync(mesh->y, m.y, n * 4, cudaMemcpyDeviceToHost, s));
+  SIFG_CUDA(cudaMemcpyAsync(mesh->z, m.z, n * 4, cudaMemcpyDeviceToHost, s));
+  SIFG_CUDA(cudaMemcpyAsync(offs32.data(), m.offsets, (cells + 1) * 4, cudaMemcpyDeviceToHost, s));
+  std::vector<uint32_t> orig32;
+  if (keep_idx) {
+    orig32.resize(n);
+    SIFG_CUDA(cudaMemcpyAsync(orig32.data(), m.orig, n * 4, cudaMemcpyDeviceToHost, s));
+  }
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  for (uint64_t c = 0; c <= cells; c++) mesh->cell_offsets[c] = offs32[c];
+  if (keep_idx) {
+    mesh->original_indices = (uint64_t*)malloc(n * sizeof(uint64_t));
+    for (uint64_t i = 0; i < n; i++) mesh->original_indices[i] = orig32[i];
+  }
+  if (consume) {
+    free(field->_position_block);
+    field->_position_block = nullptr;
+    field->x = field->y = field->z = nullptr;
+    field->n_particles = 0;
+  }
+  return mesh;
+  API_GUARD_END(nullptr)
+}
+
+sif_chain_mesh_t* sif_chain_mesh_alloc(uint32_t n_cells, sif_real box_length,
+                                       const sif_field_t* field, sif_option opt) {
+  return mesh_alloc(n_cells, box_length, const_cast<sif_field_t*>(field), opt, false);
+}
+
+sif_chain_mesh_t* sif_chain_mesh_alloc_consume(uint32_t n_cells, sif_real box_length,
+                                               sif_field_t* field, sif_option opt) {
+  return mesh_alloc(n_cells, box_length, field, opt, true);
+}
+
+void sif_chain_mesh_free(sif_chain_mesh_t* m) {
+  if (!m) return;
+  free(m->_position_block);
+  free(m->_velocity_block);
+  free(m->weights);
+  free(m->cell_weights);
+  free(m->original_indices);
+  free(m->cell_offsets);
+  free(m);
+}
+
+// ---------------------------------------------------------------------------
+// Variants (src/finder/exodus_finder.c:1199-1254)
+// ---------------------------------------------------------------------------
+
+static const struct {
+  const char* name;
+  float overlap;
+  uint32_t options;
+} kVariants[SIF__EXODUS_N_VARIANTS] = {
+    {"excursion-set", 0.0f, SIF_FINDER_SEEDS_CELLS},
+    {"excursion-peak", 1.0f, SIF_FINDER_SEEDS_MINIMA | SIF_FINDER_EXTEND_REACH | SIF_FINDER_DISPLACE},
+    {"lagrangian-overlap", 0.0f, SIF_FINDER_SEEDS_CELLS | SIF_FINDER_LAGRANGIAN_OVERLAP},
+};
+
+int sif_finder_exodus_preset(sif_exodus_variant_t variant, sif_real* overlap, sif_option* opt) {
+  if ((unsigned)variant >= (unsigned)SIF__EXODUS_N_VARIANTS)
+    return fail(SIF_ERR_INVALID, fmt("variant: %d (expected 0 to %d)", (int)variant,
+                                     SIF__EXODUS_N_VARIANTS - 1));
+  if (overlap) *overlap = kVariants[variant].overlap;
+  if (opt) *opt = kVariants[variant].options;
+  return SIF_OK;
+}
+
+const char* sif_finder_exodus_variant_name(sif_exodus_variant_t variant) {
+  return (unsigned)variant < (unsigned)SIF__EXODUS_N_VARIANTS ? kVariants[variant].name : nullptr;
+}
+
+int sif_finder_exodus_variant_from_name(const char* name, sif_exodus_variant_t* variant) {
+  for (int v = 0; name && v < SIF__EXODUS_N_VARIANTS; v++) {
+    if (strcmp(name, kVariants[v].name) == 0) {
+      if (variant) *variant = (sif_exodus_variant_t)v;
+      return SIF_OK;
+    }
+  }
+  return fail(SIF_ERR_INVALID,
+              fmt("variant: \"%s\" (expected excursion-set, excursion-peak or lagrangian-overlap)",
+                  name ? name : "(null)"));
+}
+
+// ---------------------------------------------------------------------------
+// The finder
+// ---------------------------------------------------------------------------
+
+// sif__finder_check_args, src/finder/utils.c:33-57.
+static int check_args(const sif_real* radii, uint32_t n_radii, sif_real threshold, sif_real f) {
+  if (!radii || n_radii == 0) return fail(SIF_ERR_INVALID, "radii: none given");
+  for (uint32_t i = 0; i < n_radii; i++)
+    if (!(radii[i] > 0.0f) || !std::isfinite(radii[i]))
+      return fail(SIF_ERR_INVALID,
+                  fmt("radii[%u] = %g: not a positive radius", i, (double)radii[i]));
+  if (!(threshold > -1.0f && threshold < 0.0f))
+    return fail(SIF_ERR_INVALID,
+                fmt("threshold %g: not a density contrast in (-1, 0)", (double)threshold));
+  if (!(f >= 0.0f && f <= 1.0f))
+    return fail(SIF_ERR_INVALID, fmt("overlap_fraction %g: not in [0, 1]", (double)f));
+  return SIF_OK;
+}
+
+sif_catalogue_t* sif_finder_exodus(sif_grid_t* grid, const sif_chain_mesh_t* mesh,
+                                   const sif_real* radii, uint32_t n_radii, sif_real threshold,
+                                   sif_exodus_variant_t variant,
+                                   const sif_finder_exodus_extras_t* extras) {
+  sif_real f;
+  sif_option opt;
+  if (sif_finder_exodus_preset(variant, &f, &opt) != SIF_OK) return nullptr;
+  return sif_finder_exodus_raw(grid, mesh, radii, n_radii, threshold, f, opt, extras);
+}
+
+// sif_finder_exodus_raw, src/finder/exodus_finder.c:1272-1345.
+sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t* mesh,
+                                       const sif_real* radii, uint32_t n_radii,
+                                       sif_real threshold, sif_real f, sif_option opt,
+                                       const sif_finder_exodus_extras_t* extras) {
+  if (!grid || !grid->values || !mesh) {
+    fail(SIF_ERR_INVALID, !grid ? "grid: NULL" : (!grid->values ? "grid: no values" : "mesh: NULL"));
+    return nullptr;
+  }
+  if (check_args(radii, n_radii, threshold, f) != SIF_OK) return nullptr;
+  if (grid->content == SIF_GRID_DENSITY)
+    log_msg(SIF_LOG_LEVEL_WARNING, "finder.exodus",
+            "this grid holds a density, not a density contrast; call "
+            "sif_grid_to_density_contrast first");
+  if (!mesh->x || mesh->n_particles == 0) {
+    fail(SIF_ERR_INVALID, "mesh: no particles");
+    return nullptr;
+  }
+  if (mesh->box_length != grid->box_length) {
+    fail(SIF_ERR_INVALID, fmt("mesh: box of %g, grid: box of %g (must match)",
+                              (double)mesh->box_length, (double)grid->box_length));
+    return nullptr;
+  }
+  if (mesh->weights) {
+    fail(SIF_ERR_UNSUPPORTED, "mesh: weighted meshes are not supported by the GPU finder");
+    return nullptr;
+  }
+  if (extras) {
+    if (extras->checkpoint && (opt & SIF_FINDER_NO_CHECKPOINT)) {
+      fail(SIF_ERR_INVALID, fmt("checkpoint: %s, with SIF_FINDER_NO_CHECKPOINT set", extras->checkpoint));
+      return nullptr;
+    }
+    if (extras->checkpoint || (extras->prior && extras->prior->n_voids) || extras->save_memory) {
+      fail(SIF_ERR_UNSUPPORTED,
+           "extras: checkpoints, prior catalogues and save_memory are not supported by the GPU finder");
+      return nullptr;
+    }
+  }
+  if (mesh->n_particles >= 0xffffffffull) {
+    fail(SIF_ERR_RANGE, "mesh: 2^32 particles or more");
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return nullptr;
+  cudaStream_t s = e->stream();
+  const uint64_t n = mesh->n_particles;
+  const uint64_t mcells = mesh->total_cells;
+  const size_t gb = grid->total_cells * sizeof(float);
+  float* dg = (float*)bufs().grid.ensure(gb);
+  SIFG_CUDA(cudaMemcpyAsync(dg, grid->values, gb, cudaMemcpyHostToDevice, s));
+  DeviceMesh m;
+  m.n_cells = mesh->n_cells;
+  m.box_length = mesh->box_length;
+  m.cell_length = mesh->cell_length;
+  m.n_particles = n;
+  m.x = (float*)bufs().mx.ensure(n * 4);
+  m.y = (float*)bufs().my.ensure(n * 4);
+  m.z = (float*)bufs().mz.ensure(n * 4);
+  SIFG_CUDA(cudaMemcpyAsync(m.x, mesh->x, n * 4, cudaMemcpyHostToDevice, s));
+  SIFG_CUDA(cudaMemcpyAsync(m.y, mesh->y, n * 4, cudaMemcpyHostToDevice, s));
+  SIFG_CUDA(cudaMemcpyAsync(m.z, mesh->z, n * 4, cudaMemcpyHostToDevice, s));
+  std::vector<uint32_t> offs32(mcells + 1);
+  for (uint64_t c = 0; c <= mcells; c++) offs32[c] = (uint32_t)mesh->cell_offsets[c];
+  m.offsets = (uint32_t*)bufs().offs.ensure((mcells + 1) * 4);
+  SIFG_CUDA(cudaMemcpyAsync(m.offsets, offs32.data(), (mcells + 1) * 4, cudaMemcpyHostToDevice, s));
+
+  RunParams p;
+  p.grid_n = grid->n_cells;
+  p.box = grid->box_length;
+  p.threshold = threshold;
+  p.overlap = f;
+  p.options = opt;
+  p.radii.assign(radii, radii + n_radii);
+  p.window = g_window;
+  float* consume = nullptr;
+  if (opt & SIF_FINDER_CONSUME_GRID) consume = (float*)bufs().px.ensure(gb);
+  p.consume_out = consume;
+  HostCatalogue cat;
+  RunTimings tm;
+  g_stats.clear();
+  const int st = e->exodus(dg, m, p, cat, &g_stats, &tm);
+  record_timings(tm);
+  if (st != SIF_OK) return nullptr;
+  // The grid handed back: untouched, which restores it exactly; under
+  // SIF_FINDER_CONSUME_GRID it holds the last rung's smoothing, as the
+  // reference leaves it (exodus_finder.c:2426-2453).
+  if (consume) {
+    SIFG_CUDA(cudaMemcpyAsync(grid->values, consume, gb, cudaMemcpyDeviceToHost, s));
+    SIFG_CUDA(cudaStreamSynchronize(s));
+  }
+  sif_catalogue_t* out = make_catalogue(cat);
+  if (!out) fail(SIF_ERR_ALLOC, "catalogue: cannot allocate");
+  return out;
+  API_GUARD_END(nullptr)
+}
+
+// sif_finder_grid_cells_from_size, src/finder/exodus_finder.c:2494-2560.
+uint32_t sif_finder_grid_cells_from_size(uint64_t n_particles, sif_real box_length,
+                                         sif_real cell_size, sif_finder_units_t units,
+                                         sif_real volume) {
+  if (!(box_length > 0.0f) || !std::isfinite(box_length) || !(cell_size > 0.0f) ||
+      !std::isfinite(cell_size)) {
+    fail(SIF_ERR_INVALID, "grid cells: box and cell size must be positive and finite");
+    return 0;
+  }
+  double cell = (double)cell_size;
+  if (units == SIF_FINDER_UNITS_MPS) {
+    if (n_particles == 0 || !(volume >= 0.0f)) {
+      fail(SIF_ERR_INVALID, "grid cells: no tracers to take a mean separation from");
+      return 0;
+    }
+    const double vol = volume > 0.0f ? (double)volume
+                                     : (double)box_length * box_length * box_length;
+    cell *= std::cbrt(vol / (double)n_particles);
+  }
+  const double ratio = (double)box_length / cell;
+  const double nearest = std::round(ratio);
+  const double n = std::fabs(ratio - nearest) <= 1e-5 * nearest ? nearest : std::ceil(ratio);
+  if (!(n >= 1.0) || n > 4294967295.0) {
+    fail(SIF_ERR_RANGE, "grid cells: count does not fit in 32 bits");
+    return 0;
+  }
+  return (uint32_t)n;
+}
+
+// ---------------------------------------------------------------------------
+// Part 2: device-resident entry points
+// ---------------------------------------------------------------------------
+
+int sifg_cic_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
+                    float box, float* grid) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  if (n_grid < 4) return fail(SIF_ERR_INVALID, "n_grid: expected at least 4");
+  cudaStream_t s = e->stream();
+  const int st = check_in_box(x, y, z, n, box, "field", s);
+  if (st != SIF_OK) return st;
+  e->scratch.ensure(cic_scratch_bytes(n, n_grid));
+  RunTimings tm;
+  cic_deposit(x, y, z, n, n_grid, box, grid, e->scratch.ptr, s, &tm.cic);
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  g_timings.cic_ms = tm.cic.total_ms();
+  g_timings.cic_launches = tm.cic.launches();
+  return SIF_OK;
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+int sifg_contrast_device(float* grid, uint64_t total_cells, double* mean_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  cudaStream_t s = e->stream();
+  double* scratch = (double*)e->scratch.ensure(density_contrast_scratch_bytes());
+  density_contrast(grid, total_cells, scratch, s);
+  const double mean = read_mean(scratch);
+  if (mean_out) *mean_out = mean;
+  if (!(mean > 0.0)) return fail(SIF_ERR_RANGE, fmt("grid: mean density %g (expected > 0)", mean));
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  return SIF_OK;
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+int sifg_mesh_device(const float* x, const float* y, const float* z, uint64_t n,
+                     uint32_t n_cells, float box, float* mx, float* my, float* mz,
+                     uint32_t* offsets, uint32_t* orig) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  if (n_cells == 0 || !(box > 0.0f)) return fail(SIF_ERR_INVALID, "mesh: bad geometry");
+  cudaStream_t s = e->stream();
+  const int st = check_in_box(x, y, z, n, box, "field", s);
+  if (st != SIF_OK) return st;
+  DeviceMesh m;
+  m.n_cells = n_cells;
+  m.box_length = box;
+  m.cell_length = box / (float)n_cells;
+  m.x = mx;
+  m.y = my;
+  m.z = mz;
+  m.offsets = offsets;
+  m.orig = orig;
+  e->scratch.ensure(mesh_scratch_bytes(n, n_cells));
+  RunTimings tm;
+  mesh_build(x, y, z, n, m, e->scratch.ptr, s, &tm.mesh);
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  g_timings.mesh_ms = tm.mesh.total_ms();
+  g_timings.mesh_launches = tm.mesh.launches();
+  return SIF_OK;
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+int sifg_smooth_device(const float* delta, uint32_t n_grid, float box, float r, int filter,
+                       int window_mode, float* out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  cudaStream_t s = e->stream();
+  e->smoother.setup(n_grid, box, window_mode, s);
+  e->smoother.forward(delta);
+  RunTimings tm;
+  e->smoother.smooth(filter, r, 0.0f, out, &tm.filter);
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  g_timings.filter_ms = tm.filter.total_ms();
+  g_timings.filter_launches = tm.filter.launches();
+  return SIF_OK;
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+static int run_device(Engine* e, const float* delta, uint32_t n_grid, float box, DeviceMesh& m,
+                      const float* radii, uint32_t n_radii, float threshold, float overlap,
+                      uint32_t opt, const float* inject, float* cx, float* cy, float* cz, float* r,
+                      uint64_t capacity, uint64_t* n_voids, RunTimings& tm) {
+  if (check_args(radii, n_radii, threshold, overlap) != SIF_OK) return g_status;
+  RunParams p;
+  p.grid_n = n_grid;
+  p.box = box;
+  p.threshold = threshold;
+  p.overlap = overlap;
+  p.options = opt;
+  p.radii.assign(radii, radii + n_radii);
+  p.window = g_window;
+  p.inject = inject;
+  p.inject_on_device = true;
+  HostCatalogue cat;
+  g_stats.clear();
+  const int st = e->exodus(delta, m, p, cat, &g_stats, &tm);
+  if (st != SIF_OK) return st;
+  const uint64_t nv = cat.cx.size();
+  if (n_voids) *n_voids = nv;
+  const uint64_t w = nv < capacity ? nv : capacity;
+  if (w) {
+    memcpy(cx, cat.cx.data(), w * 4);
+    memcpy(cy, cat.cy.data(), w * 4);
+    memcpy(cz, cat.cz.data(), w * 4);
+    memcpy(r, cat.r.data(), w * 4);
+  }
+  return SIF_OK;
+}
+
+int sifg_exodus_device(const float* delta, uint32_t n_grid, float box, const float* mx,
+                       const float* my, const float* mz, const uint32_t* offsets,
+                       uint64_t n_particles, uint32_t mesh_cells, const float* radii,
+                       uint32_t n_radii, float threshold, float overlap, uint32_t opt,
+                       const float* inject, float* cx, float* cy, float* cz, float* r,
+                       uint64_t capacity, uint64_t* n_voids) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  DeviceMesh m;
+  m.n_cells = mesh_cells;
+  m.box_length = box;
+  m.cell_length = box / (float)mesh_cells;
+  m.n_particles = n_particles;
+  m.x = const_cast<float*>(mx);
+  m.y = const_cast<float*>(my);
+  m.z = const_cast<float*>(mz);
+  m.offsets = const_cast<uint32_t*>(offsets);
+  RunTimings tm;
+  const int st = run_device(e, delta, n_grid, box, m, radii, n_radii, threshold, overlap, opt,
+                            inject, cx, cy, cz, r, capacity, n_voids, tm);
+  record_timings(tm);
+  return st;
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
+                    float box, uint32_t mesh_cells, const float* radii, uint32_t n_radii,
+                    float threshold, float overlap, uint32_t opt, float* cx, float* cy,
+                    float* cz, float* r, uint64_t capacity, uint64_t* n_voids) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  if (n_grid < 4 || mesh_cells == 0) return fail(SIF_ERR_INVALID, "grid or mesh: bad size");
+  cudaStream_t s = e->stream();
+  const auto t0 = std::chrono::steady_clock::now();
+  int st = check_in_box(x, y, z, n, box, "field", s);
+  if (st != SIF_OK) return st;
+  const uint64_t cells = (uint64_t)n_grid * n_grid * n_grid;
+  const uint64_t mcells = (uint64_t)mesh_cells * mesh_cells * mesh_cells;
+  float* dg = (float*)bufs().grid.ensure(cells * 4);
+  RunTimings tm;
+  e->scratch.ensure(std::max(cic_scratch_bytes(n, n_grid), mesh_scratch_bytes(n, mesh_cells)));
+  cic_deposit(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic);
+  double* cscratch = (double*)bufs().bad.ensure(density_contrast_scratch_bytes() + 64);
+  density_contrast(dg, cells, cscratch, s);
+  DeviceMesh m;
+  m.n_cells = mesh_cells;
+  m.box_length = box;
+  m.cell_length = box / (float)mesh_cells;
+  m.x = (float*)bufs().mx.ensure(n * 4);
+  m.y = (float*)bufs().my.ensure(n * 4);
+  m.z = (float*)bufs().mz.ensure(n * 4);
+  m.offsets = (uint32_t*)bufs().offs.ensure((mcells + 1) * 4);
+  m.orig = nullptr;
+  mesh_build(x, y, z, n, m, e->scratch.ptr, s, &tm.mesh);
+  st = run_device(e, dg, n_grid, box, m, radii, n_radii, threshold, overlap, opt, nullptr, cx, cy,
+                  cz, r, capacity, n_voids, tm);
+  tm.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  record_timings(tm);
+  return st;
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
+  const uint32_t n = (uint32_t)g_stats.size();
+  for (uint32_t i = 0; i < n && i < max_rungs; i++) {
+    const RungStat& s = g_stats[i];
+    out[i] = sifg_rung_stat_t{s.radius, s.r_search, s.n_candidates, s.n_survivors, s.n_accepted,
+                              s.rounds, s.n_rescale_fail, s.n_overflow};
+  }
+  return n;
+}
+
+void sifg_last_timings(sifg_timings_t* out) {
+  if (out) *out = g_timings;
+}
+
+void sifg_set_window(int bins) { g_window = bins < 1 ? 1 : (bins > 64 ? 64 : bins); }
+
+void sifg_candidate_ranks(const float* delta, uint32_t m, uint32_t* rank) {
+  candidate_ranks(delta, m, rank, 0);
+}
+
+}  // extern "C"

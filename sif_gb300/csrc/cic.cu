@@ -1,0 +1,375 @@
+// CIC deposit of particles onto the density grid, and the density contrast.
+//
+// Replaces grid_compute_cic / grid_cic_deposit_tile (src/structures/grid.c:
+// 455-746) and sif_grid_to_density_contrast (grid.c:1177-1244).
+//
+// The reference sums float weights in a fixed slab/chunk order so its grid is
+// deterministic. Here every corner weight is quantised to 2^-24 of a particle
+// and summed as int64, so the sum is exact and independent of the order the
+// GPU happens to add in. The eight quantised weights of a particle sum to
+// exactly 2^24: each corner is rounded, and what rounding left over goes to
+// the particle's largest corner.
+//
+// Layout of the work:
+//   1. tile_count:   each particle's tile (16^3 base cells), histogram with
+//                    warp-aggregated atomics;
+//   2. exclusive scan of the tile counts;
+//   3. tile_scatter: positions copied into tile order (one atomic per group
+//                    of lanes bound for the same tile);
+//   4. tile_deposit: one CTA per tile accumulates a 17^3 int64 tile in shared
+//                    memory, lanes bound for the same cell first reduced
+//                    across the warp; the 15^3 cells no other tile touches
+//                    are written straight to the grid as float density, the
+//                    faces shared with neighbouring tiles go to int64 face
+//                    buffers with global atomics;
+//   5. face_fixup:   the face buffers converted to float density.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace sifg {
+
+constexpr int TB = kCicTile;  // base cells per tile side
+constexpr int TS = TB + 1;    // tile extent including the upper neighbours
+constexpr double kQ = 16777216.0;  // 2^24 quanta per particle
+
+struct CicGeom {
+  uint32_t n;       // grid cells per side
+  uint32_t nt;      // tiles per side
+  float box;
+  float idx;        // (float)n / box, as the reference computes it
+};
+
+// The reference's base cell along one axis (grid.c:585-620): u = fold(v) * idx,
+// raw = (uint32)u, cell = raw >= n ? 0 : raw, t = u - raw.
+__device__ __forceinline__ void cic_axis(float v, const CicGeom& g, uint32_t& cell, float& t) {
+  const float u = fmul(box_fold(v, g.box), g.idx);
+  const uint32_t raw = (uint32_t)u;
+  cell = raw >= g.n ? 0u : raw;
+  t = fsub(u, (float)raw);
+}
+
+__device__ __forceinline__ uint32_t tile_of(float x, float y, float z, const CicGeom& g) {
+  uint32_t cx, cy, cz;
+  float t;
+  cic_axis(x, g, cx, t);
+  cic_axis(y, g, cy, t);
+  cic_axis(z, g, cz, t);
+  return ((cx / TB) * g.nt + cy / TB) * g.nt + cz / TB;
+}
+
+__global__ void tile_count_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                  const float* __restrict__ z, uint64_t n, CicGeom g,
+                                  uint32_t* __restrict__ counts) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint64_t p = base + threadIdx.x;
+    const bool valid = p < n;
+    const uint32_t tile = valid ? tile_of(x[p], y[p], z[p], g) : 0xffffffffu;
+    const unsigned peers = __match_any_sync(0xffffffffu, tile);
+    if (valid && (threadIdx.x & 31u) == (unsigned)(__ffs(peers) - 1))
+      atomicAdd(counts + tile, (uint32_t)__popc(peers));
+  }
+}
+
+__global__ void tile_scatter_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                    const float* __restrict__ z, uint64_t n, CicGeom g,
+                                    uint32_t* __restrict__ cursor, float* __restrict__ sx,
+                                    float* __restrict__ sy, float* __restrict__ sz) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint64_t p = base + threadIdx.x;
+    const bool valid = p < n;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    uint32_t tile = 0xffffffffu;
+    if (valid) {
+      px = x[p];
+      py = y[p];
+      pz = z[p];
+      tile = tile_of(px, py, pz, g);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, tile);
+    const unsigned leader = __ffs(peers) - 1;
+    uint32_t slot0 = 0;
+    if (valid && lane == leader) slot0 = atomicAdd(cursor + tile, (uint32_t)__popc(peers));
+    slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+    if (valid) {
+      const uint32_t slot = slot0 + __popc(peers & ((1u << lane) - 1u));
+      sx[slot] = px;
+      sy[slot] = py;
+      sz[slot] = pz;
+    }
+  }
+}
+
+// Face buffers: cells on a tile boundary in x (x % TB == 0), else in y, else
+// in z, each laid out densely over its own boundary planes.
+struct FaceBufs {
+  unsigned long long* fx;  // [nt][n][n]
+  unsigned long long* fy;  // [n][nt][n]
+  unsigned long long* fz;  // [n][n][nt]
+};
+
+__device__ __forceinline__ unsigned long long* face_slot(const FaceBufs& f, uint32_t gx,
+                                                        uint32_t gy, uint32_t gz,
+                                                        const CicGeom& g) {
+  const uint64_t n = g.n, nt = g.nt;
+  if (gx % TB == 0) return f.fx + ((uint64_t)(gx / TB) * n + gy) * n + gz;
+  if (gy % TB == 0) return f.fy + ((uint64_t)gx * nt + gy / TB) * n + gz;
+  return f.fz + ((uint64_t)gx * n + gy) * nt + gz / TB;
+}
+
+__global__ void __launch_bounds__(256) tile_deposit_kernel(
+    const float* __restrict__ sx, const float* __restrict__ sy, const float* __restrict__ sz,
+    const uint32_t* __restrict__ offsets, CicGeom g, float inv_cell_vol,
+    float* __restrict__ grid, FaceBufs faces) {
+  extern __shared__ unsigned long long acc[];  // TS^3
+  const uint32_t nt = g.nt;
+  const uint32_t n_tiles = nt * nt * nt;
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const uint32_t tx = tile / (nt * nt), ty = (tile / nt) % nt, tz = tile % nt;
+    const uint32_t ox = tx * TB, oy = ty * TB, oz = tz * TB;
+    for (int i = threadIdx.x; i < TS * TS * TS; i += blockDim.x) acc[i] = 0ull;
+    __syncthreads();
+
+    const uint32_t s = offsets[tile], e = offsets[tile + 1];
+    for (uint32_t base = s; base < e; base += blockDim.x) {
+      const uint32_t p = base + threadIdx.x;
+      const bool valid = p < e;
+      uint32_t cell = 0xffffffffu;
+      unsigned long long q[8];
+      if (valid) {
+        uint32_t cx, cy, cz;
+        float tx_, ty_, tz_;
+        cic_axis(sx[p], g, cx, tx_);
+        cic_axis(sy[p], g, cy, ty_);
+        cic_axis(sz[p], g, cz, tz_);
+        const float wx0 = fsub(1.0f, tx_), wy0 = fsub(1.0f, ty_), wz0 = fsub(1.0f, tz_);
+        // The reference's eight products (grid.c:627-650): (x,y) pairs times z.
+        const float w00 = fmul(wx0, wy0), w01 = fmul(wx0, ty_);
+        const float w10 = fmul(tx_, wy0), w11 = fmul(tx_, ty_);
+        const float w[8] = {fmul(w00, wz0), fmul(w00, tz_), fmul(w01, wz0), fmul(w01, tz_),
+                            fmul(w10, wz0), fmul(w10, tz_), fmul(w11, wz0), fmul(w11, tz_)};
+        long long sum = 0;
+        int big = 0;
+        for (int k = 0; k < 8; k++) {
+          const long long qk = __double2ll_rn((double)w[k] * kQ);
+          q[k] = (unsigned long long)qk;
+          sum += qk;
+          if (w[k] > w[big]) big = k;
+        }
+        q[big] += (unsigned long long)((long long)kQ - sum);
+        cell = ((cx - ox) * TS + (cy - oy)) * TS + (cz - oz);
+      }
+      // Lanes bound for the same base cell add their eight corners together
+      // first (a corner's quanta, at most 2^24 + 4, sum over a warp within 32
+      // bits); then one shared atomic per corner per group.
+      const unsigned peers = __match_any_sync(0xffffffffu, cell);
+      const bool leader = lane == (unsigned)(__ffs(peers) - 1);
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const unsigned v = __reduce_add_sync(peers, valid ? (unsigned)q[k] : 0u);
+        if (valid && leader) {
+          const uint32_t c =
+              cell + (uint32_t)(((k >> 2) & 1) * TS * TS + ((k >> 1) & 1) * TS + (k & 1));
+          atomicAdd(acc + c, (unsigned long long)v);
+        }
+      }
+    }
+    __syncthreads();
+
+    // Flush. Cells 1..TB-1 of this tile (within the grid) are touched by no
+    // other tile; the rest are shared with a neighbour.
+    const uint32_t ex = min((uint32_t)TB, g.n - ox), ey = min((uint32_t)TB, g.n - oy),
+                   ez = min((uint32_t)TB, g.n - oz);
+    for (int i = threadIdx.x; i < TS * TS * TS; i += blockDim.x) {
+      const uint32_t a = i / (TS * TS), b = (i / TS) % TS, c = i % TS;
+      if (a > ex || b > ey || c > ez) continue;
+      const unsigned long long v = acc[i];
+      const uint32_t gx = ox + a == g.n ? 0u : ox + a;
+      const uint32_t gy = oy + b == g.n ? 0u : oy + b;
+      const uint32_t gz = oz + c == g.n ? 0u : oz + c;
+      const bool interior = a >= 1 && a < ex && b >= 1 && b < ey && c >= 1 && c < ez;
+      if (interior) {
+        grid[((uint64_t)gx * g.n + gy) * g.n + gz] =
+            fmul((float)((double)v * (1.0 / kQ)), inv_cell_vol);
+      } else if (v != 0ull) {
+        atomicAdd(face_slot(faces, gx, gy, gz, g), v);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void face_fixup_kernel(CicGeom g, float inv_cell_vol, float* __restrict__ grid,
+                                  FaceBufs faces) {
+  const uint64_t n = g.n, nt = g.nt;
+  const uint64_t nfx = nt * n * n;
+  const uint64_t total = 3 * nfx;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    const uint64_t which = i / nfx, j = i % nfx;
+    uint64_t gx, gy, gz;
+    unsigned long long v;
+    if (which == 0) {
+      gx = (j / (n * n)) * TB;
+      gy = (j / n) % n;
+      gz = j % n;
+      if (gx >= n) continue;
+      v = faces.fx[j];
+    } else if (which == 1) {
+      gx = j / (nt * n);
+      gy = ((j / n) % nt) * TB;
+      gz = j % n;
+      if (gy >= n || gx % TB == 0) continue;
+      v = faces.fy[j];
+    } else {
+      gx = j / (n * nt);
+      gy = (j / nt) % n;
+      gz = (j % nt) * TB;
+      if (gz >= n || gx % TB == 0 || gy % TB == 0) continue;
+      v = faces.fz[j];
+    }
+    grid[(gx * n + gy) * n + gz] = fmul((float)((double)v * (1.0 / kQ)), inv_cell_vol);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Density contrast: the mean in double over fixed blocks (a fixed launch, so
+// the summation order and the result never change), then v * inv - 1.
+// ---------------------------------------------------------------------------
+constexpr int kMeanBlocks = 1024;
+constexpr int kMeanThreads = 256;
+
+__global__ void __launch_bounds__(kMeanThreads) mean_partial_kernel(const float* __restrict__ v,
+                                                                    uint64_t n,
+                                                                    double* __restrict__ partial) {
+  __shared__ double s[kMeanThreads];
+  const uint64_t chunk = (n + kMeanBlocks - 1) / kMeanBlocks;
+  const uint64_t lo = (uint64_t)blockIdx.x * chunk;
+  const uint64_t hi = lo + chunk < n ? lo + chunk : n;
+  double acc = 0.0;
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += kMeanThreads) acc += (double)v[i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kMeanThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+}
+
+__global__ void mean_final_kernel(const double* __restrict__ partial, uint64_t n,
+                                  double* __restrict__ mean_out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double t = 0.0;
+    for (int b = 0; b < kMeanBlocks; b++) t += partial[b];
+    mean_out[0] = t / (double)n;
+  }
+}
+
+__global__ void contrast_kernel(float* __restrict__ v, uint64_t n,
+                                const double* __restrict__ mean) {
+  const double m = mean[0];
+  const float inv = (float)(1.0 / m);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    v[i] = fsub(fmul(v[i], inv), 1.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+static CicGeom make_geom(uint32_t n, float box) {
+  CicGeom g;
+  g.n = n;
+  g.nt = (n + TB - 1) / TB;
+  g.box = box;
+  g.idx = (float)n / box;
+  return g;
+}
+
+size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n) {
+  const uint64_t nt = (n + TB - 1) / TB;
+  const uint64_t tiles = nt * nt * nt;
+  const uint64_t face = 3 * nt * (uint64_t)n * n * sizeof(unsigned long long);
+  return 3 * n_particles * sizeof(float) + (2 * tiles + 2) * sizeof(uint32_t) + face + 16 * 256;
+}
+
+void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_particles,
+                 uint32_t n, float box, float* grid, void* scratch, cudaStream_t st,
+                 KernelTimer* timer) {
+  const CicGeom g = make_geom(n, box);
+  const uint64_t nt = g.nt, tiles = nt * nt * nt;
+  char* p = (char*)scratch;
+  auto take = [&](size_t bytes) {
+    char* r = p;
+    p += (bytes + 255) & ~(size_t)255;
+    return (void*)r;
+  };
+  float* sx = (float*)take(n_particles * sizeof(float));
+  float* sy = (float*)take(n_particles * sizeof(float));
+  float* sz = (float*)take(n_particles * sizeof(float));
+  uint32_t* counts = (uint32_t*)take((tiles + 1) * sizeof(uint32_t));
+  uint32_t* cursor = (uint32_t*)take((tiles + 1) * sizeof(uint32_t));
+  const size_t face_elems = nt * (uint64_t)n * n;
+  FaceBufs faces;
+  faces.fx = (unsigned long long*)take(face_elems * 8);
+  faces.fy = (unsigned long long*)take(face_elems * 8);
+  faces.fz = (unsigned long long*)take(face_elems * 8);
+
+  SIFG_CUDA(cudaMemsetAsync(counts, 0, (tiles + 1) * sizeof(uint32_t), st));
+  SIFG_CUDA(cudaMemsetAsync(faces.fx, 0, face_elems * 8, st));
+  SIFG_CUDA(cudaMemsetAsync(faces.fy, 0, face_elems * 8, st));
+  SIFG_CUDA(cudaMemsetAsync(faces.fz, 0, face_elems * 8, st));
+  const unsigned blk = 256;
+  const unsigned grd = grid_for(n_particles, blk, 152u * 16u);
+  tile_count_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, counts);
+  SIFG_LAUNCH_CHECK();
+  exclusive_scan_u32(counts, (uint32_t)(tiles + 1), st);
+  SIFG_CUDA(cudaMemcpyAsync(cursor, counts, (tiles + 1) * sizeof(uint32_t),
+                            cudaMemcpyDeviceToDevice, st));
+  tile_scatter_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, cursor, sx, sy, sz);
+  SIFG_LAUNCH_CHECK();
+  const float cl = box / (float)n;
+  const float inv_cell_vol = 1.0f / (float)(cl * cl * cl);
+  const size_t smem = (size_t)TS * TS * TS * sizeof(unsigned long long);
+  static bool attr = false;
+  if (!attr) {
+    SIFG_CUDA(cudaFuncSetAttribute(tile_deposit_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  const unsigned dgrid = (unsigned)(tiles < 152u * 5u ? tiles : 152u * 5u);
+  if (timer) timer->begin(st);
+  tile_deposit_kernel<<<dgrid, 256, smem, st>>>(sx, sy, sz, counts, g, inv_cell_vol, grid,
+                                                faces);
+  SIFG_LAUNCH_CHECK();
+  if (timer) timer->end(st);
+  face_fixup_kernel<<<grid_for(3 * face_elems, 256), 256, 0, st>>>(g, inv_cell_vol, grid, faces);
+  SIFG_LAUNCH_CHECK();
+}
+
+void density_contrast(float* v, uint64_t n, double* d_scratch, cudaStream_t st) {
+  // d_scratch: kMeanBlocks + 1 doubles.
+  mean_partial_kernel<<<kMeanBlocks, kMeanThreads, 0, st>>>(v, n, d_scratch);
+  SIFG_LAUNCH_CHECK();
+  mean_final_kernel<<<1, 32, 0, st>>>(d_scratch, n, d_scratch + kMeanBlocks);
+  SIFG_LAUNCH_CHECK();
+  contrast_kernel<<<grid_for(n, 256), 256, 0, st>>>(v, n, d_scratch + kMeanBlocks);
+  SIFG_LAUNCH_CHECK();
+}
+
+size_t density_contrast_scratch_bytes() { return (kMeanBlocks + 1) * sizeof(double); }
+
+double read_mean(const double* d_scratch) {
+  double m = 0.0;
+  SIFG_CUDA(cudaMemcpy(&m, d_scratch + kMeanBlocks, sizeof(double), cudaMemcpyDeviceToHost));
+  return m;
+}
+
+}  // namespace sifg

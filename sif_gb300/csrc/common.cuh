@@ -1,0 +1,95 @@
+// Shared definitions of the GB300 exodus library: error plumbing, the
+// strict single-precision helpers the bit-exact kernels are written with, and
+// small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+
+namespace sifg {
+
+// sif's status codes (include/sif/core/macros.h:690-707).
+constexpr int kOk = 0;
+constexpr int kErrAlloc = -1;
+constexpr int kErrInvalid = -2;
+constexpr int kErrRange = -3;
+constexpr int kErrUnsupported = -5;
+constexpr int kErrUninitialised = -6;
+
+// Records a status and message for sif_error_status()/sif_error_message().
+void set_error(int status, const std::string& msg);
+
+struct CudaError {
+  cudaError_t code;
+  const char* where;
+};
+
+#define SIFG_CUDA(call)                                                      \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess) throw ::sifg::CudaError{e_, #call};               \
+  } while (0)
+
+#define SIFG_LAUNCH_CHECK() SIFG_CUDA(cudaGetLastError())
+
+inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap = 152u * 32u) {
+  uint64_t g = (n + block - 1) / block;
+  if (g > cap) g = cap;
+  if (g == 0) g = 1;
+  return (unsigned)g;
+}
+
+// ---------------------------------------------------------------------------
+// Strict IEEE single precision. The reference computes its distances, bins
+// and density tests in float with one rounding per operation; the _rn
+// intrinsics are never contracted into fused multiply-adds, so these give
+// the same bits as the strict CPU build.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// dist2 of src/finder/exodus_rescale.c:349-355: ((dx*dx + dy*dy) + dz*dz).
+__device__ __forceinline__ float dist2(float px, float py, float pz, float cx, float cy,
+                                       float cz) {
+  const float dx = fsub(px, cx), dy = fsub(py, cy), dz = fsub(pz, cz);
+  return fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
+}
+
+// bin_of of src/finder/exodus_rescale.c:360-369: truncation toward zero.
+__device__ __forceinline__ uint32_t bin_of(float d2, float rc2, float inv_w, uint32_t nb) {
+  const int32_t b = __float2int_rz(fmul(fsub(d2, rc2), inv_w));
+  if (b < 0) return 0;
+  if ((uint32_t)b >= nb) return nb - 1;
+  return (uint32_t)b;
+}
+
+// sif__box_fold, src/structures/field_internal.h:58-64.
+__host__ __device__ __forceinline__ float box_fold(float v, float box) {
+  if (v >= box)
+    v -= box;
+  else if (v < 0.0f)
+    v += box;
+  return v >= box ? 0.0f : v;
+}
+
+__device__ __forceinline__ uint32_t wrap_pbc(int32_t v, uint32_t n) {
+  int32_t w = v % (int32_t)n;
+  return (uint32_t)(w < 0 ? w + (int32_t)n : w);
+}
+
+__device__ __forceinline__ bool mask_get(const uint32_t* m, uint64_t i) {
+  return (__ldg(m + (i >> 5)) >> (i & 31)) & 1u;
+}
+
+// The mask is also read with plain loads by kernels that run after writers
+// in the same stream; __ldg is only used where the mask is read-only for the
+// whole kernel.
+__device__ __forceinline__ bool mask_get_rw(const uint32_t* m, uint64_t i) {
+  return (m[i >> 5] >> (i & 31)) & 1u;
+}
+
+}  // namespace sifg

@@ -1,0 +1,471 @@
+// The exodus run on one GPU: the rung loop of sif__exodus_run
+// (src/finder/exodus_finder.c:1585-2492) for a periodic box, unweighted,
+// SIF_FINDER_SEEDS_CELLS on their nodes.
+//
+// Per rung, on one stream:
+//   smooth (filter + C2R)  ->  candidate count  ->  [host: M]  ->  candidate
+//   write  ->  copy to the host  ->  pre-filter  ->  sphere growth of every
+//   survivor  ->  commit rounds  ->  append in rank order  ->  void index.
+// While the GPU runs the pre-filter and the sphere growth, the host replays
+// the reference's quicksort over the candidates (the depth order, ties
+// included, is part of what the reference's catalogue is) and uploads each
+// candidate's rank; the commit rounds are the first kernels that need it.
+//
+// The commit is the reference's sequential greedy pass, decided in rounds:
+// a survivor is decided once every survivor ranked before it that could
+// interact with it has been. Its tests -- node masked, pole masked at the
+// rescaled radius, exact overlap -- are the reference's, against every void
+// accepted before it; a failed test stays failed as the catalogue grows, so
+// a survivor that fails against the current state is rejected at once.
+#include <cuda_runtime.h>
+#include <omp.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "engine.cuh"
+
+namespace sifg {
+
+static constexpr float kPiF = (float)3.14159265358979323846;
+static constexpr uint32_t kOptSeedsMinima = 1u << 9;
+static constexpr uint32_t kOptKeepWindow = 1u << 14;
+static constexpr uint32_t kOptAliasing = 1u << 8;
+static constexpr uint32_t kOptLagrangian = 1u << 18;
+static constexpr uint32_t kOptRefineMask = 3u << 19;
+static constexpr uint32_t kOptExtendReach = 1u << 21;
+static constexpr uint32_t kOptDisplace = 1u << 22;
+static constexpr uint32_t kGrowCap = 1u << 15;  // overflow window, floats per CTA
+
+Engine::Engine(int device) : device_(device) {
+  SIFG_CUDA(cudaSetDevice(device));
+  SIFG_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+  SIFG_CUDA(cudaEventCreateWithFlags(&ev_cand_, cudaEventDisableTiming));
+  SIFG_CUDA(cudaMallocHost(&h_counters_, 16 * sizeof(uint32_t)));
+}
+
+Engine::~Engine() {
+  cudaFreeHost(h_delta_);
+  cudaFreeHost(h_flat_);
+  cudaFreeHost(h_rank_);
+  cudaFreeHost(h_counters_);
+  if (ev_cand_) cudaEventDestroy(ev_cand_);
+  if (st_) cudaStreamDestroy(st_);
+}
+
+void Engine::ensure_host(size_t m) {
+  if (m <= h_cap_) return;
+  cudaFreeHost(h_delta_);
+  cudaFreeHost(h_flat_);
+  cudaFreeHost(h_rank_);
+  const size_t cap = m + m / 4 + 1024;
+  SIFG_CUDA(cudaMallocHost(&h_delta_, cap * sizeof(float)));
+  SIFG_CUDA(cudaMallocHost(&h_flat_, cap * sizeof(uint32_t)));
+  SIFG_CUDA(cudaMallocHost(&h_rank_, cap * sizeof(uint32_t)));
+  h_cap_ = cap;
+}
+
+// ---------------------------------------------------------------------------
+// The candidate order
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct Rec {
+  float d;
+  uint32_t i;
+};
+
+// One three-way partition as the reference performs it: the pivot is the
+// middle element's key; scanning from the left, a smaller key is exchanged to
+// the low end, a larger one with the high end (and examined again), an equal
+// one is passed over.
+inline void partition3(Rec* a, int64_t lo, int64_t hi, int64_t* lt_out, int64_t* gt_out) {
+  const float pivot = a[lo + (hi - lo) / 2].d;
+  int64_t lt = lo, i = lo, gt = hi;
+  while (i <= gt) {
+    const float v = a[i].d;
+    if (v < pivot) {
+      std::swap(a[lt], a[i]);
+      lt++;
+      i++;
+    } else if (pivot < v) {
+      std::swap(a[i], a[gt]);
+      gt--;
+    } else {
+      i++;
+    }
+  }
+  *lt_out = lt;
+  *gt_out = gt;
+}
+
+void qsort_serial(Rec* a, int64_t lo, int64_t hi) {
+  std::vector<std::pair<int64_t, int64_t>> stack;
+  stack.emplace_back(lo, hi);
+  while (!stack.empty()) {
+    const auto [l, h] = stack.back();
+    stack.pop_back();
+    if (l >= h) continue;
+    int64_t lt, gt;
+    partition3(a, l, h, &lt, &gt);
+    stack.emplace_back(l, lt - 1);
+    stack.emplace_back(gt + 1, h);
+  }
+}
+
+constexpr int64_t kTaskCutoff = 65536;  // SIF_QUICKSORT_TASK_CUTOFF, sort.h:104
+
+void qsort_tasks(Rec* a, int64_t lo, int64_t hi) {
+  if (hi - lo < kTaskCutoff) {
+    qsort_serial(a, lo, hi);
+    return;
+  }
+  int64_t lt, gt;
+  partition3(a, lo, hi, &lt, &gt);
+#pragma omp task untied
+  qsort_tasks(a, lo, lt - 1);
+  qsort_tasks(a, gt + 1, hi);
+}
+
+}  // namespace
+
+void candidate_ranks(const float* delta, uint32_t m, uint32_t* rank, int threads) {
+  std::vector<Rec> a(m);
+  for (uint32_t k = 0; k < m; k++) a[k] = Rec{delta[k], k};
+  if (m > (uint32_t)kTaskCutoff && threads != 1) {
+    const int t = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel num_threads(t)
+#pragma omp single nowait
+    qsort_tasks(a.data(), 0, (int64_t)m - 1);
+  } else if (m > 1) {
+    qsort_serial(a.data(), 0, (int64_t)m - 1);
+  }
+  for (uint32_t k = 0; k < m; k++) rank[a[k].i] = k;
+}
+
+// ---------------------------------------------------------------------------
+// The template
+// ---------------------------------------------------------------------------
+
+int build_template(HostTemplate& t, uint32_t mesh_n, float cell_length, float rmin,
+                   float r_search) {
+  t = HostTemplate();
+  const int32_t cr = (int32_t)(r_search / cell_length) + 1;
+  if (cr >= (int32_t)mesh_n) return kErrRange;
+  const float rs2 = r_search * r_search;
+  const float rc2 = rmin * rmin;
+  for (int32_t dx = -cr; dx <= cr; dx++)
+    for (int32_t dy = -cr; dy <= cr; dy++)
+      for (int32_t dz = -cr; dz <= cr; dz++) {
+        const float mnx = dx == 0 ? 0.0f : (std::fabs((float)dx) - 1.0f) * cell_length;
+        const float mny = dy == 0 ? 0.0f : (std::fabs((float)dy) - 1.0f) * cell_length;
+        const float mnz = dz == 0 ? 0.0f : (std::fabs((float)dz) - 1.0f) * cell_length;
+        const float mn = mnx * mnx + mny * mny + mnz * mnz;
+        if (mn > rs2) continue;
+        const float mxx = (std::fabs((float)dx) + 1.0f) * cell_length;
+        const float mxy = (std::fabs((float)dy) + 1.0f) * cell_length;
+        const float mxz = (std::fabs((float)dz) + 1.0f) * cell_length;
+        const float mx = mxx * mxx + mxy * mxy + mxz * mxz;
+        t.dx.push_back(dx);
+        t.dy.push_back(dy);
+        t.dz.push_back(dz);
+        t.min_d2.push_back(mn);
+        t.max_d2.push_back(mx);
+        uint8_t type;
+        if (mx <= rc2)
+          type = kCellCore;
+        else if (mn > rc2)
+          type = mx <= rs2 ? kCellShell : kCellEdge;
+        else
+          type = kCellStraddle;
+        t.type.push_back(type);
+      }
+  return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// The run
+// ---------------------------------------------------------------------------
+
+template <class T>
+static T* grow_to(DevBuf& b, size_t n) {
+  return (T*)b.ensure(n * sizeof(T));
+}
+
+int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams& p,
+                   HostCatalogue& out, std::vector<RungStat>* stats, RunTimings* tm) {
+  const auto t_start = std::chrono::steady_clock::now();
+  const uint32_t N = p.grid_n;
+  const uint64_t cells = (uint64_t)N * N * N;
+  const float box = p.box;
+  const float cell = box / (float)N;
+  const float threshold = p.threshold, f = p.overlap;
+  const uint32_t opt = p.options;
+  if (opt & (kOptSeedsMinima | kOptRefineMask | kOptExtendReach | kOptDisplace)) {
+    set_error(kErrUnsupported,
+              "options: minima seeds, centre refinement, extended reach and displacement are not "
+              "supported by the GPU finder");
+    return kErrUnsupported;
+  }
+  if (cells >= (1ull << 32)) {
+    set_error(kErrRange, "grid: more than 2^32 cells");
+    return kErrRange;
+  }
+  const float scale = (opt & kOptLagrangian) ? (float)std::cbrt(1.0 + (double)threshold) : 1.0f;
+  static const float factors[4] = {1.5f, 1.25f, 1.75f, 2.0f};
+  const float search_factor = factors[(opt >> 12) & 3u];
+  const int window_mode = (opt & kOptKeepWindow) ? 0 : ((opt & kOptAliasing) ? 2 : 1);
+
+  std::vector<float> radii = p.radii;
+  std::sort(radii.begin(), radii.end(), [](float a, float b) { return a > b; });
+
+  float* field = grow_to<float>(field_, cells);
+  uint32_t* mask = grow_to<uint32_t>(mask_, (cells + 31) / 32);
+  SIFG_CUDA(cudaMemsetAsync(mask, 0, ((cells + 31) / 32) * sizeof(uint32_t), st_));
+  if (!p.inject) {
+    smoother.setup(N, box, window_mode, st_);
+    smoother.forward(d_delta);
+  }
+
+  // Loop invariants, exodus_finder.c:1629-1632.
+  const float box_volume = box * box * box;
+  const float mean_density = (float)mesh.n_particles / box_volume;
+  const float vol_factor = (4.0f / 3.0f) * kPiF * mean_density;
+
+  uint32_t n_voids = 0;
+  size_t cat_cap = 0;
+  auto ensure_cat = [&](size_t want) {
+    if (want <= cat_cap) return;
+    size_t cap = std::max<size_t>(want + want / 2, 1 << 16);
+    DevBuf* bufs[4] = {&cat_x_, &cat_y_, &cat_z_, &cat_r_};
+    for (DevBuf* b : bufs) {
+      void* fresh = nullptr;
+      SIFG_CUDA(cudaMalloc(&fresh, cap * sizeof(float)));
+      if (n_voids)
+        SIFG_CUDA(cudaMemcpyAsync(fresh, b->ptr, n_voids * sizeof(float), cudaMemcpyDeviceToDevice, st_));
+      SIFG_CUDA(cudaStreamSynchronize(st_));
+      b->release();
+      b->ptr = fresh;
+      b->bytes = cap * sizeof(float);
+    }
+    vids_.ensure(cap * sizeof(uint32_t));
+    vcell_.ensure(cap * sizeof(uint32_t));
+    cat_cap = cap;
+  };
+  ensure_cat(1 << 16);
+  const uint32_t vcells = kVoidCells * kVoidCells * kVoidCells;
+  uint32_t* vstart = grow_to<uint32_t>(vstart_, vcells + 1);
+  build_void_index(cat_x_.as<float>(), cat_y_.as<float>(), cat_z_.as<float>(), 0, box, vstart,
+                   vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
+  float max_r = 0.0f;
+  float* gbuf = grow_to<float>(gbuf_, (size_t)growth_grid() * kGrowCap);
+  uint32_t* dcount = grow_to<uint32_t>(dcount_, 16);
+  uint32_t* counters = grow_to<uint32_t>(counters_, 16);
+  const uint32_t nb_scan = scan_blocks(cells);
+  uint32_t* blocks = grow_to<uint32_t>(blocks_, (size_t)std::max<uint64_t>(nb_scan + 1, 1024));
+
+  MeshView mv{mesh.x, mesh.y, mesh.z, mesh.offsets, (int32_t)mesh.n_cells, mesh.box_length,
+              1.0f / mesh.cell_length};
+
+  for (uint32_t ri = 0; ri < radii.size(); ri++) {
+    RungStat rs;
+    const float radius = radii[ri];
+    rs.radius = radius;
+
+    // 1. The rung's field.
+    if (p.inject) {
+      SIFG_CUDA(cudaMemcpyAsync(field, p.inject + (uint64_t)ri * cells, cells * sizeof(float),
+                                p.inject_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                st_));
+    } else {
+      smoother.smooth(kFilterTopHat, radius, 0.0f, field, tm ? &tm->filter : nullptr);
+    }
+
+    // 2. Candidates, in flat order.
+    scan_count_pass(field, mask, cells, threshold, blocks, dcount, st_);
+    SIFG_CUDA(cudaMemcpyAsync(h_counters_, dcount, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaStreamSynchronize(st_));
+    const uint32_t m = h_counters_[0];
+    rs.n_candidates = m;
+
+    // The reach and the rescaling's constants (exodus_finder.c:1771-1817,
+    // exodus_rescale.c:681-720, 894-908).
+    const float rmin = 1.0f * radius;
+    float r_search = radius + std::fmax((search_factor - 1.0f) * radius, 3.0f * cell);
+    if (ri > 0 && radii[ri - 1] > r_search) r_search = radii[ri - 1];
+    rs.r_search = r_search;
+    if (m == 0) {
+      if (stats) stats->push_back(rs);
+      continue;
+    }
+
+    float* cdelta = grow_to<float>(cand_delta_, m);
+    uint32_t* cflat = grow_to<uint32_t>(cand_flat_, m);
+    scan_write_pass(field, mask, cells, threshold, blocks, cdelta, cflat, st_);
+    ensure_host(m);
+    SIFG_CUDA(cudaMemcpyAsync(h_delta_, cdelta, m * sizeof(float), cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaEventRecord(ev_cand_, st_));
+
+    RungConsts rc;
+    rc.radius = radius;
+    rc.r_search = r_search;
+    rc.rmin = rmin;
+    rc.rs2 = r_search * r_search;
+    rc.rc2 = rmin * rmin;
+    const float span = rc.rs2 - rc.rc2;
+    uint32_t nb = 2048u;
+    {
+      const float expected_shell =
+          vol_factor * (r_search * r_search * r_search - rmin * rmin * rmin);
+      const float want = expected_shell / 16.0f;
+      if (!(want >= 64.0f))
+        nb = 64u;
+      else if (want < 2048.0f)
+        nb = (uint32_t)want;
+    }
+    rc.nb = nb;
+    rc.inv_w = (float)nb / span;
+    rc.bin_w = span / (float)nb;
+    const float K = (threshold + 1.0f) * vol_factor;
+    rc.K2 = K * K;
+    rc.expected = vol_factor * r_search * r_search * r_search;
+    rc.threshold = threshold;
+    rc.proxy_pole = (int32_t)(scale * radius * (1.0f - f) / cell) - 1;
+    rc.scale = scale;
+    rc.f = f;
+    rc.cell = cell;
+    rc.grid_n = N;
+    rc.box = box;
+    rc.gbox = (float)N * cell;
+    rc.window = (uint32_t)std::max(1, p.window);
+
+    HostTemplate ht;
+    if (build_template(ht, mesh.n_cells, mesh.cell_length, rmin, r_search) != kOk) {
+      set_error(kErrRange, "search sphere of " + std::to_string(r_search) +
+                               " wider than the mesh; use a finer mesh or smaller radii");
+      return kErrRange;
+    }
+    const uint32_t tcount = (uint32_t)ht.type.size();
+    int32_t* tdx = grow_to<int32_t>(tdx_, tcount);
+    int32_t* tdy = grow_to<int32_t>(tdy_, tcount);
+    int32_t* tdz = grow_to<int32_t>(tdz_, tcount);
+    uint8_t* ttype = grow_to<uint8_t>(ttype_, tcount);
+    float* tmin = grow_to<float>(tmin_, tcount);
+    float* tmax = grow_to<float>(tmax_, tcount);
+    SIFG_CUDA(cudaMemcpyAsync(tdx, ht.dx.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
+    SIFG_CUDA(cudaMemcpyAsync(tdy, ht.dy.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
+    SIFG_CUDA(cudaMemcpyAsync(tdz, ht.dz.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
+    SIFG_CUDA(cudaMemcpyAsync(ttype, ht.type.data(), tcount, cudaMemcpyHostToDevice, st_));
+    SIFG_CUDA(cudaMemcpyAsync(tmin, ht.min_d2.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
+    SIFG_CUDA(cudaMemcpyAsync(tmax, ht.max_d2.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
+    TemplateView tv{tdx, tdy, tdz, ttype, tmin, tmax, tcount};
+
+    // 3. Pre-filter at the rung, against the catalogue as the rung begins.
+    VoidView vv{cat_x_.as<float>(), cat_y_.as<float>(), cat_z_.as<float>(), cat_r_.as<float>(),
+                vstart, vids_.as<uint32_t>(), (float)kVoidCells / box, max_r, n_voids};
+    uint8_t* alive = grow_to<uint8_t>(alive_, m);
+    uint32_t* scand = grow_to<uint32_t>(surv_cand_, m);
+    uint32_t* sflat = grow_to<uint32_t>(surv_flat_, m);
+    float* scx = grow_to<float>(scx_, m);
+    float* scy = grow_to<float>(scy_, m);
+    float* scz = grow_to<float>(scz_, m);
+    float* sr = grow_to<float>(sr_, m);
+    uint8_t* sreason = grow_to<uint8_t>(sreason_, m);
+    uint32_t* blocks2 = grow_to<uint32_t>(rank_slots_, (size_t)m + 2048);
+    prefilter(cflat, m, mask, vv, rc, alive, blocks2, scand, sflat, scx, scy, scz, dcount + 1, st_);
+    Survivors sv{scand, sflat, scx, scy, scz, sr, sreason, dcount + 1};
+
+    // 4. Sphere growth of every survivor.
+    if (!(span > 0.0f)) {
+      // RESCALE_DEGENERATE for every candidate: no annulus.
+      std::vector<float> neg(m, -1.0f);
+      SIFG_CUDA(cudaMemcpyAsync(sr, neg.data(), m * sizeof(float), cudaMemcpyHostToDevice, st_));
+      SIFG_CUDA(cudaMemsetAsync(sreason, kRescaleDegenerate, m, st_));
+    } else {
+      grow(mv, tv, rc, sv, m, gbuf, kGrowCap, st_, tm ? &tm->growth : nullptr);
+    }
+
+    // 5. The order, on the host while the GPU grows spheres.
+    SIFG_CUDA(cudaEventSynchronize(ev_cand_));
+    candidate_ranks(h_delta_, m, h_rank_, host_threads);
+    uint32_t* rank = grow_to<uint32_t>(rank_, m);
+    SIFG_CUDA(cudaMemcpyAsync(rank, h_rank_, m * sizeof(uint32_t), cudaMemcpyHostToDevice, st_));
+
+    // 6. The commit, in rounds.
+    const float reach = 2.0f * scale * r_search + 2.0f * cell;
+    int32_t ng = (int32_t)std::floor(box / reach);
+    if (ng < 3) ng = 1;
+    if (ng > 256) ng = 256;
+    const uint32_t sg_cells = (uint32_t)(ng * ng * ng);
+    uint32_t* sg_start = grow_to<uint32_t>(sgrid_start_, sg_cells + 1);
+    uint32_t* sg_ids = grow_to<uint32_t>(sgrid_ids_, m);
+    uint32_t* sg_cell = grow_to<uint32_t>(sgrid_cellof_, m);
+    build_survivor_grid(scx, scy, scz, dcount + 1, m, ng, box, sg_start, sg_ids, sg_cell, st_);
+    SurvivorGrid sg{sg_start, sg_ids, ng, (float)ng / box};
+    uint8_t* sa = grow_to<uint8_t>(state_a_, m);
+    uint8_t* sb = grow_to<uint8_t>(state_b_, m);
+    uint32_t* acc = grow_to<uint32_t>(acc_, m);
+    SIFG_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(uint32_t), st_));
+    commit_init(sv, sa, counters, m, st_);
+    uint64_t rounds = 0;
+    for (;;) {
+      SIFG_CUDA(cudaMemcpyAsync(counters + 2, counters, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st_));
+      SIFG_CUDA(cudaMemsetAsync(counters + 1, 0, sizeof(uint32_t), st_));
+      commit_round(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters, m, st_);
+      paint_new(sv, acc, counters, mask, rc, m, st_);
+      std::swap(sa, sb);
+      rounds++;
+      SIFG_CUDA(cudaMemcpyAsync(h_counters_, counters, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
+      SIFG_CUDA(cudaMemcpyAsync(h_counters_ + 8, dcount + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
+      SIFG_CUDA(cudaStreamSynchronize(st_));
+      if (h_counters_[1] == 0) break;
+      if (rounds > (uint64_t)m + 2) {
+        set_error(kErrInvalid, "commit: no progress");
+        return kErrInvalid;
+      }
+    }
+    const uint32_t n_acc = h_counters_[0];
+    rs.n_survivors = h_counters_[8];
+    rs.n_accepted = n_acc;
+    rs.rounds = rounds;
+    rs.n_rescale_fail = h_counters_[4];
+    rs.n_overflow = h_counters_[5];
+    if (n_acc) {
+      float rmax;
+      std::memcpy(&rmax, &h_counters_[3], sizeof(float));
+      if (rmax > max_r) max_r = rmax;
+      ensure_cat(n_voids + n_acc);
+      append_accepted(sv, rank, acc, counters, m, blocks2, cat_x_.as<float>(), cat_y_.as<float>(),
+                      cat_z_.as<float>(), cat_r_.as<float>(), n_voids, m, st_);
+      n_voids += n_acc;
+      build_void_index(cat_x_.as<float>(), cat_y_.as<float>(), cat_z_.as<float>(), n_voids, box,
+                       vstart, vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
+    }
+    if (stats) stats->push_back(rs);
+  }
+
+  if (p.consume_out) {
+    SIFG_CUDA(cudaMemcpyAsync(p.consume_out, field, cells * sizeof(float), cudaMemcpyDeviceToDevice, st_));
+  }
+  const size_t base = out.cx.size();
+  out.cx.resize(base + n_voids);
+  out.cy.resize(base + n_voids);
+  out.cz.resize(base + n_voids);
+  out.r.resize(base + n_voids);
+  if (n_voids) {
+    SIFG_CUDA(cudaMemcpyAsync(out.cx.data() + base, cat_x_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaMemcpyAsync(out.cy.data() + base, cat_y_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaMemcpyAsync(out.cz.data() + base, cat_z_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaMemcpyAsync(out.r.data() + base, cat_r_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
+  }
+  SIFG_CUDA(cudaStreamSynchronize(st_));
+  if (tm)
+    tm->wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start)
+                       .count();
+  return kOk;
+}
+
+}  // namespace sifg

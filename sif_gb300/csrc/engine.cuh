@@ -1,0 +1,100 @@
+// The exodus run on one GPU (engine.cu): the rung loop around the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "finder.cuh"
+#include "kernels.cuh"
+#include "smooth.cuh"
+
+namespace sifg {
+
+struct RunParams {
+  uint32_t grid_n = 0;
+  float box = 0.f;
+  float threshold = -0.8f;
+  float overlap = 0.f;
+  uint32_t options = 0;
+  std::vector<float> radii;  // any order
+  int window = 8;            // bins resolved per pass
+  // Fields that replace the smoothing, rung by rung (largest radius first),
+  // n_radii * grid_n^3 floats; host or device memory as inject_on_device says.
+  const float* inject = nullptr;
+  bool inject_on_device = false;
+  // Where the last rung's field goes under SIF_FINDER_CONSUME_GRID (device).
+  float* consume_out = nullptr;
+};
+
+struct RungStat {
+  float radius = 0.f, r_search = 0.f;
+  uint64_t n_candidates = 0, n_survivors = 0, n_accepted = 0, rounds = 0;
+  uint64_t n_rescale_fail = 0, n_overflow = 0;
+};
+
+struct RunTimings {
+  KernelTimer growth, filter, cic, mesh;
+  double wall_ms = 0.0;
+  void reset() {
+    growth.reset();
+    filter.reset();
+    cic.reset();
+    mesh.reset();
+    wall_ms = 0.0;
+  }
+};
+
+struct HostCatalogue {
+  std::vector<float> cx, cy, cz, r;
+};
+
+class Engine {
+ public:
+  explicit Engine(int device);
+  ~Engine();
+
+  cudaStream_t stream() const { return st_; }
+  int device() const { return device_; }
+
+  // The finder on a density contrast on the device and a device mesh.
+  // Returns a sif status; the catalogue is appended to `out`.
+  int exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams& p, HostCatalogue& out,
+             std::vector<RungStat>* stats, RunTimings* timings);
+
+  DevBuf scratch;  // shared scratch for CIC / mesh builds
+  Smoother smoother;
+  int host_threads = 0;
+
+ private:
+  int device_;
+  cudaStream_t st_ = 0;
+  DevBuf field_, mask_, cand_delta_, cand_flat_, blocks_, rank_, rank_slots_, alive_;
+  DevBuf surv_cand_, surv_flat_, scx_, scy_, scz_, sr_, sreason_, state_a_, state_b_, acc_;
+  DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
+  DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
+  DevBuf tdx_, tdy_, tdz_, ttype_, tmin_, tmax_, gbuf_;
+  float* h_delta_ = nullptr;
+  uint32_t* h_flat_ = nullptr;
+  uint32_t* h_rank_ = nullptr;
+  uint32_t* h_counters_ = nullptr;
+  size_t h_cap_ = 0;
+  cudaEvent_t ev_cand_ = nullptr;
+  void ensure_host(size_t m);
+};
+
+// The reference's candidate order (include/sif/utils/sort.h:56-145 over
+// src/finder/utils.c:24): rank[k] is the position of candidate k, given in
+// flat order, once sorted by depth with the three-way quicksort.
+void candidate_ranks(const float* delta, uint32_t m, uint32_t* rank, int threads);
+
+// Template of the rescaling (src/finder/exodus_rescale.c:175-283).
+struct HostTemplate {
+  std::vector<int32_t> dx, dy, dz;
+  std::vector<uint8_t> type;
+  std::vector<float> min_d2, max_d2;
+};
+int build_template(HostTemplate& t, uint32_t mesh_n, float cell_length, float rmin, float r_search);
+
+}  // namespace sifg

@@ -1,0 +1,884 @@
+// The per-rung finder stages of the exodus path on the GPU.
+//
+// scan_candidates  sif__finder_scan_candidates (src/finder/utils.c:130-213),
+//                  the flat-order compaction; the depth order itself is
+//                  the host's replay of the reference's quicksort.
+// prefilter        prefilter_cells (src/finder/exodus_finder.c:871-944):
+//                  mask bit, pole probe and exact overlap at the rung radius,
+//                  against the catalogue as the rung begins.
+// grow             sif__exodus_find_radius (src/finder/exodus_rescale.c:
+//                  642-1027): early refusal, d^2 histogram in shared memory,
+//                  bin walk, exact resolution of a window of bins.
+// commit_round     the sequential commit of exodus_finder.c:2181-2329 as
+//                  rounds: a survivor is decided once every survivor ranked
+//                  before it that it could interact with is decided.
+// paint_new        sif__mark_sphere (src/finder/utils.c:965-1033).
+//
+// Every float expression that decides a candidate is written with _rn
+// intrinsics in the reference's order, so it rounds as the strict CPU build.
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include "common.cuh"
+#include "finder.cuh"
+
+namespace sifg {
+
+// ---------------------------------------------------------------------------
+// Candidate scan
+// ---------------------------------------------------------------------------
+constexpr int kScanT = 256;
+constexpr int kScanRounds = 16;
+constexpr uint64_t kScanChunk = (uint64_t)kScanT * kScanRounds;
+
+uint32_t scan_blocks(uint64_t n_cells) { return (uint32_t)((n_cells + kScanChunk - 1) / kScanChunk); }
+
+__device__ __forceinline__ bool is_candidate(const float* f, const uint32_t* mask, uint64_t i,
+                                             uint64_t n, float thr) {
+  return i < n && f[i] <= thr && !mask_get(mask, i);
+}
+
+__global__ void __launch_bounds__(kScanT) scan_count_kernel(const float* __restrict__ f,
+                                                            const uint32_t* __restrict__ mask,
+                                                            uint64_t n, float thr,
+                                                            uint32_t* __restrict__ counts) {
+  __shared__ uint32_t ws[kScanT / 32];
+  const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
+  uint32_t c = 0;
+  for (int j = 0; j < kScanRounds; j++) c += is_candidate(f, mask, base + j * kScanT + threadIdx.x, n, thr);
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < kScanT / 32; w++) t += ws[w];
+    counts[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kScanT) scan_write_kernel(
+    const float* __restrict__ f, const uint32_t* __restrict__ mask, uint64_t n, float thr,
+    const uint32_t* __restrict__ offsets, float* __restrict__ cdelta, uint32_t* __restrict__ cflat) {
+  __shared__ uint32_t wsum[kScanT / 32];
+  const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t out = offsets[blockIdx.x];
+  for (int j = 0; j < kScanRounds; j++) {
+    const uint64_t i = base + j * kScanT + threadIdx.x;
+    const bool p = is_candidate(f, mask, i, n, thr);
+    const unsigned bal = __ballot_sync(0xffffffffu, p);
+    if (lane == 0) wsum[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < kScanT / 32; w++) {
+      const uint32_t v = wsum[w];
+      before += (w < (int)warp) ? v : 0u;
+      total += v;
+    }
+    if (p) {
+      const uint32_t pos = out + before + __popc(bal & ((1u << lane) - 1u));
+      cdelta[pos] = f[i];
+      cflat[pos] = (uint32_t)i;
+    }
+    out += total;
+    __syncthreads();
+  }
+}
+
+__global__ void store_total_kernel(const uint32_t* __restrict__ offsets, uint32_t nb,
+                                   uint32_t* __restrict__ d_count) {
+  d_count[0] = offsets[nb];
+}
+
+void scan_count_pass(const float* field, const uint32_t* mask, uint64_t n_cells, float threshold,
+                     uint32_t* block_counts, uint32_t* d_count, cudaStream_t st) {
+  const uint32_t nb = scan_blocks(n_cells);
+  scan_count_kernel<<<nb, kScanT, 0, st>>>(field, mask, n_cells, threshold, block_counts);
+  SIFG_LAUNCH_CHECK();
+  SIFG_CUDA(cudaMemsetAsync(block_counts + nb, 0, sizeof(uint32_t), st));
+  exclusive_scan_u32(block_counts, nb + 1, st);
+  store_total_kernel<<<1, 1, 0, st>>>(block_counts, nb, d_count);
+  SIFG_LAUNCH_CHECK();
+}
+
+void scan_write_pass(const float* field, const uint32_t* mask, uint64_t n_cells, float threshold,
+                     const uint32_t* block_counts, float* cand_delta, uint32_t* cand_flat,
+                     cudaStream_t st) {
+  scan_write_kernel<<<scan_blocks(n_cells), kScanT, 0, st>>>(field, mask, n_cells, threshold,
+                                                             block_counts, cand_delta, cand_flat);
+  SIFG_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Overlap tests
+// ---------------------------------------------------------------------------
+
+// sif__overlap_quick, src/finder/utils.c:819-848.
+__device__ bool overlap_quick(const uint32_t* mask, uint32_t n, uint32_t ix, uint32_t iy,
+                              uint32_t iz, uint32_t r) {
+  const uint64_t nn = n;
+  if (mask_get_rw(mask, ((uint64_t)wrap_pbc((int32_t)(ix + r), n) * nn + iy) * nn + iz)) return true;
+  if (mask_get_rw(mask, ((uint64_t)wrap_pbc((int32_t)ix - (int32_t)r, n) * nn + iy) * nn + iz)) return true;
+  if (mask_get_rw(mask, ((uint64_t)ix * nn + wrap_pbc((int32_t)(iy + r), n)) * nn + iz)) return true;
+  if (mask_get_rw(mask, ((uint64_t)ix * nn + wrap_pbc((int32_t)iy - (int32_t)r, n)) * nn + iz)) return true;
+  if (mask_get_rw(mask, ((uint64_t)ix * nn + iy) * nn + wrap_pbc((int32_t)(iz + r), n))) return true;
+  if (mask_get_rw(mask, ((uint64_t)ix * nn + iy) * nn + wrap_pbc((int32_t)iz - (int32_t)r, n))) return true;
+  return false;
+}
+
+// The pair test of sif__overlap_exact (src/finder/utils.c:904-955): the
+// interior form when the query's search box lies inside the box, the
+// minimum-image form otherwise.
+__device__ __forceinline__ bool collide(float cx, float cy, float cz, float r, float vx, float vy,
+                                        float vz, float rj, float f, float scale, float box,
+                                        float half, bool interior) {
+  const float mn = r < rj ? r : rj;
+  const float tot = fmul(scale, fsub(fadd(r, rj), fmul(f, mn)));
+  const float tot2 = fmul(tot, tot);
+  if (interior) {
+    const float dx = fsub(cx, vx), dy = fsub(cy, vy), dz = fsub(cz, vz);
+    return fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)) < tot2;
+  }
+  float dx = fabsf(fsub(cx, vx));
+  dx = dx > half ? fsub(box, dx) : dx;
+  const float dx2 = fmul(dx, dx);
+  if (dx2 >= tot2) return false;
+  float dy = fabsf(fsub(cy, vy));
+  dy = dy > half ? fsub(box, dy) : dy;
+  const float dy2 = fmul(dy, dy);
+  const float dxy2 = fadd(dx2, dy2);
+  if (dxy2 >= tot2) return false;
+  float dz = fabsf(fsub(cz, vz));
+  dz = dz > half ? fsub(box, dz) : dz;
+  return fadd(dxy2, fmul(dz, dz)) < tot2;
+}
+
+__device__ __forceinline__ float search_radius(float r, float max_r, float f, float scale) {
+  const float mn = r < max_r ? r : max_r;
+  return fmul(scale, fsub(fadd(r, max_r), fmul(f, mn)));
+}
+
+__device__ __forceinline__ bool is_interior(float cx, float cy, float cz, float s, float box) {
+  return fsub(cx, s) >= 0.0f && fadd(cx, s) < box && fsub(cy, s) >= 0.0f && fadd(cy, s) < box &&
+         fsub(cz, s) >= 0.0f && fadd(cz, s) < box;
+}
+
+// sif__overlap_exact (src/finder/utils.c:850-960) over the void index.
+__device__ bool overlap_exact(const VoidView& v, float cx, float cy, float cz, float r, float f,
+                              float scale, float box) {
+  if (v.n == 0) return false;
+  const float half = fmul(box, 0.5f);
+  const float s = search_radius(r, v.max_r, f, scale);
+  const int32_t x0 = (int32_t)floorf(fmul(fsub(cx, s), v.inv_cell));
+  const int32_t x1 = (int32_t)floorf(fmul(fadd(cx, s), v.inv_cell));
+  const int32_t y0 = (int32_t)floorf(fmul(fsub(cy, s), v.inv_cell));
+  const int32_t y1 = (int32_t)floorf(fmul(fadd(cy, s), v.inv_cell));
+  const int32_t z0 = (int32_t)floorf(fmul(fsub(cz, s), v.inv_cell));
+  const int32_t z1 = (int32_t)floorf(fmul(fadd(cz, s), v.inv_cell));
+  const bool interior = is_interior(cx, cy, cz, s, box);
+  for (int32_t ix = x0; ix <= x1; ix++) {
+    const uint32_t wx = (uint32_t)ix & (kVoidCells - 1);
+    for (int32_t iy = y0; iy <= y1; iy++) {
+      const uint32_t wy = (uint32_t)iy & (kVoidCells - 1);
+      for (int32_t iz = z0; iz <= z1; iz++) {
+        const uint32_t wz = (uint32_t)iz & (kVoidCells - 1);
+        const uint32_t c = (wx * kVoidCells + wy) * kVoidCells + wz;
+        for (uint32_t k = v.start[c]; k < v.start[c + 1]; k++) {
+          const uint32_t j = v.ids[k];
+          if (collide(cx, cy, cz, r, v.cx[j], v.cy[j], v.cz[j], v.r[j], f, scale, box, half,
+                      interior))
+            return true;
+        }
+      }
+    }
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Pre-filter
+// ---------------------------------------------------------------------------
+
+__global__ void prefilter_kernel(const uint32_t* __restrict__ cflat, uint32_t m,
+                                 const uint32_t* __restrict__ mask, VoidView voids, RungConsts rc,
+                                 uint8_t* __restrict__ alive) {
+  const uint32_t n = rc.grid_n;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const uint32_t flat = cflat[k];
+    uint8_t ok = 1;
+    if (mask_get_rw(mask, flat)) {
+      ok = 0;
+    } else {
+      const uint32_t ix = flat / (n * n), iy = (flat / n) % n, iz = flat % n;
+      if (rc.proxy_pole > 0 && overlap_quick(mask, n, ix, iy, iz, (uint32_t)rc.proxy_pole)) {
+        ok = 0;
+      } else {
+        const float cx = fmul((float)ix, rc.cell), cy = fmul((float)iy, rc.cell),
+                    cz = fmul((float)iz, rc.cell);
+        if (overlap_exact(voids, cx, cy, cz, rc.radius, rc.f, rc.scale, rc.box)) ok = 0;
+      }
+    }
+    alive[k] = ok;
+  }
+}
+
+constexpr int kCompactT = 256;
+constexpr int kCompactRounds = 8;
+constexpr uint32_t kCompactChunk = kCompactT * kCompactRounds;
+
+__global__ void __launch_bounds__(kCompactT) flag_count_kernel(const uint8_t* __restrict__ flags,
+                                                               uint32_t m,
+                                                               uint32_t* __restrict__ counts) {
+  __shared__ uint32_t ws[kCompactT / 32];
+  const uint32_t base = blockIdx.x * kCompactChunk;
+  uint32_t c = 0;
+  for (int j = 0; j < kCompactRounds; j++) {
+    const uint32_t i = base + j * kCompactT + threadIdx.x;
+    c += (i < m && flags[i]) ? 1u : 0u;
+  }
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < kCompactT / 32; w++) t += ws[w];
+    counts[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kCompactT) survivor_write_kernel(
+    const uint8_t* __restrict__ flags, uint32_t m, const uint32_t* __restrict__ offsets,
+    const uint32_t* __restrict__ cflat, RungConsts rc, uint32_t* __restrict__ surv_cand,
+    uint32_t* __restrict__ sflat, float* __restrict__ scx, float* __restrict__ scy,
+    float* __restrict__ scz) {
+  __shared__ uint32_t wsum[kCompactT / 32];
+  const uint32_t base = blockIdx.x * kCompactChunk;
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t out = offsets[blockIdx.x];
+  const uint32_t n = rc.grid_n;
+  for (int j = 0; j < kCompactRounds; j++) {
+    const uint32_t i = base + j * kCompactT + threadIdx.x;
+    const bool p = i < m && flags[i];
+    const unsigned bal = __ballot_sync(0xffffffffu, p);
+    if (lane == 0) wsum[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < kCompactT / 32; w++) {
+      const uint32_t v = wsum[w];
+      before += (w < (int)warp) ? v : 0u;
+      total += v;
+    }
+    if (p) {
+      const uint32_t pos = out + before + __popc(bal & ((1u << lane) - 1u));
+      const uint32_t flat = cflat[i];
+      surv_cand[pos] = i;
+      sflat[pos] = flat;
+      // candidate_centre (exodus_finder.c:366-388) on its node.
+      scx[pos] = fmul((float)(flat / (n * n)), rc.cell);
+      scy[pos] = fmul((float)((flat / n) % n), rc.cell);
+      scz[pos] = fmul((float)(flat % n), rc.cell);
+    }
+    out += total;
+    __syncthreads();
+  }
+}
+
+void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, VoidView voids,
+               RungConsts rc, uint8_t* alive, uint32_t* block_counts, uint32_t* surv_cand,
+               uint32_t* surv_flat, float* scx, float* scy, float* scz, uint32_t* d_surv_count,
+               cudaStream_t st) {
+  if (m == 0) {
+    SIFG_CUDA(cudaMemsetAsync(d_surv_count, 0, sizeof(uint32_t), st));
+    return;
+  }
+  prefilter_kernel<<<grid_for(m, 128), 128, 0, st>>>(cand_flat, m, mask, voids, rc, alive);
+  SIFG_LAUNCH_CHECK();
+  const uint32_t nb = (m + kCompactChunk - 1) / kCompactChunk;
+  flag_count_kernel<<<nb, kCompactT, 0, st>>>(alive, m, block_counts);
+  SIFG_LAUNCH_CHECK();
+  SIFG_CUDA(cudaMemsetAsync(block_counts + nb, 0, sizeof(uint32_t), st));
+  exclusive_scan_u32(block_counts, nb + 1, st);
+  store_total_kernel<<<1, 1, 0, st>>>(block_counts, nb, d_surv_count);
+  SIFG_LAUNCH_CHECK();
+  survivor_write_kernel<<<nb, kCompactT, 0, st>>>(alive, m, block_counts, cand_flat, rc,
+                                                  surv_cand, surv_flat, scx, scy, scz);
+  SIFG_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Sphere growth
+// ---------------------------------------------------------------------------
+constexpr int kGrowT = 256;
+constexpr int kGrowWarps = kGrowT / 32;
+constexpr uint32_t kMaxBins = 2048;
+constexpr uint32_t kSmemBuf = 4096;
+
+unsigned growth_grid() { return 152u * 4u; }
+
+struct CellRange {
+  uint32_t s, e;
+  float ex, ey, ez;
+};
+
+// query_cell, src/finder/exodus_rescale.c:295-342.
+__device__ __forceinline__ CellRange query_cell(const MeshView& m, const TemplateView& t,
+                                                uint32_t i, int32_t ci, int32_t cj, int32_t ck,
+                                                float cx, float cy, float cz) {
+  const int32_t N = m.n;
+  int32_t ix = ci + __ldg(t.dx + i), iy = cj + __ldg(t.dy + i), iz = ck + __ldg(t.dz + i);
+  CellRange r;
+  r.ex = cx;
+  r.ey = cy;
+  r.ez = cz;
+  if (ix < 0) { ix += N; r.ex = fadd(cx, m.box); } else if (ix >= N) { ix -= N; r.ex = fsub(cx, m.box); }
+  if (iy < 0) { iy += N; r.ey = fadd(cy, m.box); } else if (iy >= N) { iy -= N; r.ey = fsub(cy, m.box); }
+  if (iz < 0) { iz += N; r.ez = fadd(cz, m.box); } else if (iz >= N) { iz -= N; r.ez = fsub(cz, m.box); }
+  const uint64_t flat = ((uint64_t)ix * N + iy) * N + iz;
+  r.s = __ldg(m.offsets + flat);
+  r.e = __ldg(m.offsets + flat + 1);
+  return r;
+}
+
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v,
+                                                            unsigned long long* red) {
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned long long t = 0;
+  for (int w = 0; w < kGrowWarps; w++) t += red[w];
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ int block_max_int(int v, int* red) {
+  for (int d = 16; d > 0; d >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, d));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int t = red[0];
+  for (int w = 1; w < kGrowWarps; w++) t = max(t, red[w]);
+  __syncthreads();
+  return t;
+}
+
+// Top edge of bin b (exodus_rescale.c:905-913).
+__device__ __forceinline__ float bin_hi(const RungConsts& rc, int32_t b) {
+  if (b == (int32_t)rc.nb - 1) return fmul(rc.rs2, 1.0f + 1e-6f);
+  return fadd(rc.rc2, fmul((float)(b + 1), rc.bin_w));
+}
+
+// Ascending bitonic sort of buf[0, p), p a power of two.
+__device__ void bitonic_sort(float* buf, uint32_t p) {
+  for (uint32_t k = 2; k <= p; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < p; i += kGrowT) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const float a = buf[i], b = buf[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            buf[i] = b;
+            buf[l] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateView tpl,
+                                                        RungConsts rc, Survivors sv,
+                                                        float* __restrict__ gbuf, uint32_t gcap) {
+  __shared__ uint32_t bins[kMaxBins];
+  __shared__ unsigned long long below[kMaxBins];  // particles inside bin b's lower edge
+  __shared__ float sbuf[kSmemBuf];
+  __shared__ unsigned long long red64[kGrowWarps];
+  __shared__ int redi[kGrowWarps];
+  __shared__ uint32_t collected;
+
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t n_surv = *sv.count;
+  float* my_gbuf = gbuf + (uint64_t)blockIdx.x * gcap;
+
+  for (uint32_t s = blockIdx.x; s < n_surv; s += gridDim.x) {
+    const float cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
+    const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
+                  ck = (int32_t)fmul(cz, mesh.inv_l);
+    uint8_t reason = kRescaleOk;
+    float radius = -1.0f;
+
+    // 1. The early refusal (exodus_rescale.c:738-782): whole core and shell
+    //    cells by their counts, the rest particle by particle.
+    unsigned long long within = 0;
+    for (uint32_t i = warp; i < tpl.count; i += kGrowWarps) {
+      const CellRange c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
+      const uint8_t type = __ldg(tpl.type + i);
+      if (type == kCellCore || type == kCellShell) {
+        if (lane == 0) within += c.e - c.s;
+      } else {
+        for (uint32_t p = c.s + lane; p < c.e; p += 32)
+          within += dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez) <= rc.rs2;
+      }
+    }
+    within = block_sum_u64(within, red64);
+    if (within == 0) {
+      reason = kRescaleEmpty;
+    } else if (fsub(__fdiv_rn(__ull2float_rn(within), rc.expected), 1.0f) <= rc.threshold) {
+      reason = kRescaleBeyondSearch;
+    }
+
+    if (reason == kRescaleOk) {
+      // 2. The d^2 histogram (exodus_rescale.c:794-865).
+      for (uint32_t b = threadIdx.x; b < rc.nb; b += kGrowT) bins[b] = 0;
+      __syncthreads();
+      unsigned long long n_core = 0, n_shell = 0;
+      for (uint32_t i = warp; i < tpl.count; i += kGrowWarps) {
+        const CellRange c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
+        const uint8_t type = __ldg(tpl.type + i);
+        if (type == kCellCore) {
+          if (lane == 0) n_core += c.e - c.s;
+        } else if (type == kCellShell) {
+          for (uint32_t p = c.s + lane; p < c.e; p += 32) {
+            const float d2 = dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez);
+            atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
+          }
+          if (lane == 0) n_shell += c.e - c.s;
+        } else {
+          for (uint32_t p = c.s + lane; p < c.e; p += 32) {
+            const float d2 = dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez);
+            if (d2 <= rc.rc2) {
+              n_core++;
+            } else if (d2 <= rc.rs2) {
+              atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
+              n_shell++;
+            }
+          }
+        }
+      }
+      n_core = block_sum_u64(n_core, red64);
+      n_shell = block_sum_u64(n_shell, red64);
+      const unsigned long long total = n_core + n_shell;
+      if (total == 0) {
+        reason = kRescaleEmpty;
+      } else if (fsub(__fdiv_rn(__ull2float_rn(total), rc.expected), 1.0f) <= rc.threshold) {
+        reason = kRescaleBeyondSearch;
+      }
+      if (reason == kRescaleOk) {
+        // below[b] = core + bins < b: the interior count of bin b's skip test.
+        if (warp == 0) {
+          unsigned long long carry = n_core;
+          for (uint32_t b0 = 0; b0 < rc.nb; b0 += 32) {
+            const uint32_t b = b0 + lane;
+            const unsigned long long v = b < rc.nb ? bins[b] : 0ull;
+            unsigned long long x = v;
+            for (int d = 1; d < 32; d <<= 1) {
+              const unsigned long long y = __shfl_up_sync(0xffffffffu, x, d);
+              if (lane >= (unsigned)d) x += y;
+            }
+            if (b < rc.nb) below[b] = carry + x - v;
+            carry += __shfl_sync(0xffffffffu, x, 31);
+          }
+        }
+        __syncthreads();
+
+        // 3. The walk (exodus_rescale.c:914-1007): the highest bin not ruled
+        //    out by its skip test, resolved with the bins below it.
+        int32_t cursor = (int32_t)rc.nb - 1;
+        reason = kRescaleBelowRung;
+        while (cursor >= 0) {
+          int best = -1;
+          for (int32_t b = threadIdx.x; b <= cursor; b += kGrowT) {
+            const uint32_t cnt = bins[b];
+            if (cnt == 0) continue;
+            const float hi = bin_hi(rc, b);
+            const float nm = __ull2float_rn(below[b]);
+            if (!(fmul(nm, nm) > fmul(fmul(fmul(rc.K2, hi), hi), hi))) best = max(best, b);
+          }
+          best = block_max_int(best, redi);
+          if (best < 0) break;
+          const int32_t b_hi = best;
+          int32_t b_lo = b_hi - (int32_t)rc.window + 1;
+          if (b_lo < 0) b_lo = 0;
+          const unsigned long long top = below[b_hi] + bins[b_hi];
+          while (b_lo < b_hi && top - below[b_lo] > kSmemBuf) b_lo++;
+          const uint32_t want = (uint32_t)(top - below[b_lo]);
+          float* buf = sbuf;
+          uint32_t cap = kSmemBuf;
+          if (want > kSmemBuf) {
+            buf = my_gbuf;
+            cap = gcap;
+          }
+          if (want > cap) {
+            reason = kRescaleOverflow;
+            break;
+          }
+          const float lo = fadd(rc.rc2, fmul((float)b_lo, rc.bin_w));
+          const float hi = bin_hi(rc, b_hi);
+          if (threadIdx.x == 0) collected = 0;
+          __syncthreads();
+          for (uint32_t i = warp; i < tpl.count; i += kGrowWarps) {
+            const uint8_t type = __ldg(tpl.type + i);
+            if (type == kCellCore || __ldg(tpl.max_d2 + i) < lo || __ldg(tpl.min_d2 + i) > hi) continue;
+            const CellRange c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
+            for (uint32_t p = c.s + lane; p < c.e; p += 32) {
+              const float d2 = dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez);
+              if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) continue;
+              const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
+              if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) continue;
+              const uint32_t slot = atomicAdd(&collected, 1u);
+              if (slot < cap) buf[slot] = d2;
+            }
+          }
+          __syncthreads();
+          const uint32_t m = collected < cap ? collected : cap;
+          uint32_t p2 = 1;
+          while (p2 < m) p2 <<= 1;
+          for (uint32_t i = m + threadIdx.x; i < p2; i += kGrowT) buf[i] = CUDART_INF_F;
+          __syncthreads();
+          bitonic_sort(buf, p2);
+          // Outside-in: the k-th smallest encloses top - m + k particles.
+          int found = -1;
+          for (uint32_t k = threadIdx.x; k < m; k += kGrowT) {
+            const float d2 = buf[k];
+            if (d2 == 0.0f) continue;
+            const float rn = __ull2float_rn(top - m + k);
+            const float d2c = fmul(fmul(d2, d2), d2);
+            if (fmul(rn, rn) <= fmul(rc.K2, d2c)) found = max(found, (int)k);
+          }
+          found = block_max_int(found, redi);
+          if (found >= 0) {
+            radius = __fsqrt_rn(buf[found]);
+            reason = kRescaleOk;
+            break;
+          }
+          cursor = b_lo - 1;
+          __syncthreads();
+        }
+      }
+    }
+    if (threadIdx.x == 0) {
+      sv.r[s] = reason == kRescaleOk ? radius : -1.0f;
+      sv.reason[s] = reason;
+    }
+    __syncthreads();
+  }
+}
+
+void grow(MeshView mesh, TemplateView tpl, RungConsts rc, Survivors s, uint32_t max_survivors,
+          float* gbuf, uint32_t gcap, cudaStream_t st, KernelTimer* timer) {
+  if (max_survivors == 0) return;
+  const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
+  if (timer) timer->begin(st);
+  growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap);
+  SIFG_LAUNCH_CHECK();
+  if (timer) timer->end(st);
+}
+
+// ---------------------------------------------------------------------------
+// Survivor hash
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int32_t hash_axis(float c, float inv, int32_t ng) {
+  int32_t i = (int32_t)fmul(c, inv);
+  return i < 0 ? 0 : (i >= ng ? ng - 1 : i);
+}
+
+__global__ void sgrid_count_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                   const float* __restrict__ z, const uint32_t* __restrict__ cnt,
+                                   int32_t ng, float inv, uint32_t* __restrict__ counts,
+                                   uint32_t* __restrict__ cell_of) {
+  const uint32_t n = *cnt;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t c = ((uint32_t)hash_axis(x[i], inv, ng) * ng + hash_axis(y[i], inv, ng)) * ng +
+                       hash_axis(z[i], inv, ng);
+    cell_of[i] = c;
+    atomicAdd(counts + c, 1u);
+  }
+}
+
+__global__ void scatter_ids_kernel(const uint32_t* __restrict__ cell_of, const uint32_t* __restrict__ cnt,
+                                   uint32_t fixed_n, uint32_t* __restrict__ cursor,
+                                   uint32_t* __restrict__ ids) {
+  const uint32_t n = cnt ? *cnt : fixed_n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    ids[atomicAdd(cursor + cell_of[i], 1u)] = i;
+}
+
+void build_survivor_grid(const float* scx, const float* scy, const float* scz,
+                         const uint32_t* d_count, uint32_t max_survivors, int32_t ng, float box,
+                         uint32_t* start, uint32_t* ids, uint32_t* cell_of, cudaStream_t st) {
+  const uint32_t cells = (uint32_t)(ng * ng * ng);
+  SIFG_CUDA(cudaMemsetAsync(start, 0, (cells + 1) * sizeof(uint32_t), st));
+  if (max_survivors == 0) return;
+  const float inv = (float)ng / box;
+  sgrid_count_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(scx, scy, scz, d_count, ng, inv,
+                                                                   start, cell_of);
+  SIFG_LAUNCH_CHECK();
+  exclusive_scan_u32(start, cells + 1, st);
+  static DevBuf cursor;
+  uint32_t* cur = (uint32_t*)cursor.ensure((cells + 1) * sizeof(uint32_t));
+  SIFG_CUDA(cudaMemcpyAsync(cur, start, (cells + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+  scatter_ids_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(cell_of, d_count, 0, cur, ids);
+  SIFG_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Commit rounds
+// ---------------------------------------------------------------------------
+
+// Two survivors can interact -- one's acceptance change the other's fate --
+// only if their centres are closer than the largest distance any of the
+// commit's tests reaches: the mask and pole probes reach scale * (r_i + r_j)
+// plus a cell, the overlap scale * (r_i + r_j); two cells of slack cover
+// every rounding.
+__device__ __forceinline__ bool interacts(float ax, float ay, float az, float ar, float bx,
+                                          float by, float bz, float br, const RungConsts& rc) {
+  const float half = 0.5f * rc.box;
+  float dx = fabsf(ax - bx), dy = fabsf(ay - by), dz = fabsf(az - bz);
+  dx = dx > half ? rc.box - dx : dx;
+  dy = dy > half ? rc.box - dy : dy;
+  dz = dz > half ? rc.box - dz : dz;
+  const float reach = rc.scale * (ar + br) + 2.0f * rc.cell;
+  return dx * dx + dy * dy + dz * dz < reach * reach;
+}
+
+__global__ void commit_round_kernel(Survivors sv, const uint32_t* __restrict__ rank,
+                                    SurvivorGrid g, VoidView voids, const uint32_t* __restrict__ mask,
+                                    RungConsts rc, const uint8_t* __restrict__ st_in,
+                                    uint8_t* __restrict__ st_out, uint32_t* __restrict__ acc,
+                                    uint32_t* __restrict__ counters) {
+  const uint32_t n = *sv.count;
+  const uint32_t nn = rc.grid_n;
+  const float half = fmul(rc.box, 0.5f);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint8_t s0 = st_in[i];
+    if (s0 != kUndecided) {
+      st_out[i] = s0;
+      continue;
+    }
+    const float cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i], r = sv.r[i];
+    const uint32_t node = sv.flat[i];
+    const uint32_t ix = node / (nn * nn), iy = (node / nn) % nn, iz = node % nn;
+    // The commit's re-checks (exodus_finder.c:2286-2317), against every void
+    // accepted so far: the node's mask bit, the poles at the rescaled radius,
+    // the exact overlap.
+    bool reject = mask_get_rw(mask, node);
+    if (!reject) {
+      const int32_t pole = (int32_t)(__fdiv_rn(fmul(fmul(rc.scale, r), fsub(1.0f, rc.f)), rc.cell)) - 1;
+      if (pole > 0 && overlap_quick(mask, nn, ix, iy, iz, (uint32_t)pole)) reject = true;
+    }
+    if (!reject && overlap_exact(voids, cx, cy, cz, r, rc.f, rc.scale, rc.box)) reject = true;
+    // Voids accepted this rung, from the survivor hash.
+    bool ready = true;
+    if (!reject) {
+      const uint32_t my_rank = rank[sv.cand[i]];
+      const bool interior_all = false;
+      const int32_t ng = g.ng;
+      const int32_t hx = hash_axis(cx, g.inv_cell, ng), hy = hash_axis(cy, g.inv_cell, ng),
+                    hz = hash_axis(cz, g.inv_cell, ng);
+      const int32_t span = ng >= 3 ? 1 : 0;  // a hash coarser than 3 cells is one cell
+      for (int32_t ax = -span; ax <= span && !reject; ax++)
+        for (int32_t ay = -span; ay <= span && !reject; ay++)
+          for (int32_t az = -span; az <= span && !reject; az++) {
+            const uint32_t c = (uint32_t)(((hx + ax + ng) % ng) * ng + (hy + ay + ng) % ng) * ng +
+                               (uint32_t)((hz + az + ng) % ng);
+            const uint32_t e = g.start[c + 1];
+            for (uint32_t k = g.start[c]; k < e; k++) {
+              const uint32_t j = g.ids[k];
+              if (j == i) continue;
+              const uint8_t sj = st_in[j];
+              if (sj == kRejected) continue;
+              const float jx = sv.cx[j], jy = sv.cy[j], jz = sv.cz[j], rj = sv.r[j];
+              if (sj == kAccepted) {
+                // A same-rung void: the exact pair test (its search box is
+                // the reference's at the rung's largest radius; the minimum
+                // image form agrees with the interior one wherever it
+                // applies, since neither reaches half the box).
+                if (collide(cx, cy, cz, r, jx, jy, jz, rj, rc.f, rc.scale, rc.box, half,
+                            interior_all)) {
+                  reject = true;
+                  break;
+                }
+              } else if (ready && rank[sv.cand[j]] < my_rank &&
+                         interacts(cx, cy, cz, r, jx, jy, jz, rj, rc)) {
+                ready = false;
+              }
+            }
+          }
+    }
+    uint8_t out = kUndecided;
+    if (reject) {
+      out = kRejected;
+    } else if (ready) {
+      out = kAccepted;
+      acc[atomicAdd(counters, 1u)] = i;
+      atomicMax((int*)(counters + 3), __float_as_int(r));  // r > 0: int order is float order
+    } else {
+      atomicAdd(counters + 1, 1u);
+    }
+    st_out[i] = out;
+  }
+}
+
+__global__ void commit_init_kernel(Survivors sv, uint8_t* __restrict__ state,
+                                   uint32_t* __restrict__ counters) {
+  const uint32_t n = *sv.count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const bool ok = sv.r[i] >= 0.0f;
+    state[i] = ok ? kUndecided : kRejected;
+    if (!ok) atomicAdd(counters + 4, 1u);
+    if (sv.reason[i] == kRescaleOverflow) atomicAdd(counters + 5, 1u);
+  }
+}
+
+void commit_init(Survivors s, uint8_t* state, uint32_t* counters, uint32_t max_survivors,
+                 cudaStream_t st) {
+  if (max_survivors == 0) return;
+  commit_init_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(s, state, counters);
+  SIFG_LAUNCH_CHECK();
+}
+
+void commit_round(Survivors s, const uint32_t* rank, SurvivorGrid g, VoidView voids,
+                  const uint32_t* mask, RungConsts rc, const uint8_t* state_in, uint8_t* state_out,
+                  uint32_t* acc, uint32_t* counters, uint32_t max_survivors, cudaStream_t st) {
+  commit_round_kernel<<<grid_for(max_survivors, 128), 128, 0, st>>>(s, rank, g, voids, mask, rc,
+                                                                     state_in, state_out, acc,
+                                                                     counters);
+  SIFG_LAUNCH_CHECK();
+}
+
+// paint_sphere with set = 1 (src/finder/utils.c:965-1027), one warp per void:
+// every node whose centre lies within scale * r, measured as the reference
+// measures it.
+__global__ void paint_kernel(Survivors sv, const uint32_t* __restrict__ acc,
+                             const uint32_t* __restrict__ counters, uint32_t* __restrict__ mask,
+                             RungConsts rc) {
+  const uint32_t lo = counters[2], hi = counters[0];
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  const uint32_t n = rc.grid_n;
+  for (uint32_t a = lo + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); a < hi; a += warps) {
+    const uint32_t i = acc[a];
+    const float cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i];
+    const float rt = fmul(rc.scale, sv.r[i]);
+    const float r2 = fmul(rt, rt);
+    const float inv = __fdiv_rn(1.0f, rc.cell);
+    const float half = fmul(rc.gbox, 0.5f);
+    const int32_t cr = (int32_t)fmul(rt, inv) + 1;
+    const int32_t ci = (int32_t)fmul(cx, inv), cj = (int32_t)fmul(cy, inv), ck = (int32_t)fmul(cz, inv);
+    const int32_t side = 2 * cr + 1;
+    for (int32_t q = lane; q < side * side; q += 32) {
+      const int32_t gx = ci + q / side - cr, gy = cj + q % side - cr;
+      float ddx = fabsf(fsub(fmul((float)gx, rc.cell), cx));
+      ddx = ddx > half ? fsub(rc.gbox, ddx) : ddx;
+      const float dx2 = fmul(ddx, ddx);
+      if (dx2 > r2) continue;
+      float ddy = fabsf(fsub(fmul((float)gy, rc.cell), cy));
+      ddy = ddy > half ? fsub(rc.gbox, ddy) : ddy;
+      const float dxy2 = fadd(dx2, fmul(ddy, ddy));
+      if (dxy2 > r2) continue;
+      const uint64_t row = ((uint64_t)wrap_pbc(gx, n) * n + wrap_pbc(gy, n)) * n;
+      for (int32_t dz = -cr; dz <= cr; dz++) {
+        const int32_t gz = ck + dz;
+        float ddz = fabsf(fsub(fmul((float)gz, rc.cell), cz));
+        ddz = ddz > half ? fsub(rc.gbox, ddz) : ddz;
+        if (fadd(dxy2, fmul(ddz, ddz)) <= r2) {
+          const uint64_t cell = row + wrap_pbc(gz, n);
+          atomicOr(mask + (cell >> 5), 1u << (cell & 31));
+        }
+      }
+    }
+  }
+}
+
+void paint_new(Survivors s, const uint32_t* acc, const uint32_t* counters, uint32_t* mask,
+               RungConsts rc, uint32_t max_survivors, cudaStream_t st) {
+  const uint32_t warps = max_survivors < 152u * 16u ? (max_survivors ? max_survivors : 1) : 152u * 16u;
+  paint_kernel<<<(warps + 3) / 4, 128, 0, st>>>(s, acc, counters, mask, rc);
+  SIFG_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Appending the rung's voids in rank order
+// ---------------------------------------------------------------------------
+
+__global__ void mark_ranks_kernel(Survivors sv, const uint32_t* __restrict__ rank,
+                                  const uint32_t* __restrict__ acc, const uint32_t* __restrict__ counters,
+                                  uint32_t* __restrict__ slots) {
+  const uint32_t n = counters[0];
+  for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x)
+    slots[rank[sv.cand[acc[a]]]] = 1;
+}
+
+__global__ void write_voids_kernel(Survivors sv, const uint32_t* __restrict__ rank,
+                                   const uint32_t* __restrict__ acc,
+                                   const uint32_t* __restrict__ counters,
+                                   const uint32_t* __restrict__ pos, float* __restrict__ cx,
+                                   float* __restrict__ cy, float* __restrict__ cz,
+                                   float* __restrict__ cr, uint32_t base) {
+  const uint32_t n = counters[0];
+  for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+    const uint32_t i = acc[a];
+    const uint32_t o = base + pos[rank[sv.cand[i]]];
+    cx[o] = sv.cx[i];
+    cy[o] = sv.cy[i];
+    cz[o] = sv.cz[i];
+    cr[o] = sv.r[i];
+  }
+}
+
+void append_accepted(Survivors s, const uint32_t* rank, const uint32_t* acc,
+                     const uint32_t* counters, uint32_t m_candidates, uint32_t* rank_slots,
+                     float* cat_x, float* cat_y, float* cat_z, float* cat_r, uint32_t n_voids,
+                     uint32_t max_survivors, cudaStream_t st) {
+  SIFG_CUDA(cudaMemsetAsync(rank_slots, 0, (m_candidates + 1) * sizeof(uint32_t), st));
+  mark_ranks_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(s, rank, acc, counters, rank_slots);
+  SIFG_LAUNCH_CHECK();
+  exclusive_scan_u32(rank_slots, m_candidates + 1, st);
+  write_voids_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(s, rank, acc, counters, rank_slots,
+                                                                   cat_x, cat_y, cat_z, cat_r, n_voids);
+  SIFG_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Void index
+// ---------------------------------------------------------------------------
+
+// cll_axis_index, src/structures/cell_linked_list.c:40-58 (periodic).
+__device__ __forceinline__ uint32_t void_axis(float c, float inv) {
+  int32_t i = (int32_t)floorf(fmul(c, inv));
+  i %= (int32_t)kVoidCells;
+  if (i < 0) i += kVoidCells;
+  return (uint32_t)i;
+}
+
+__global__ void void_count_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                  const float* __restrict__ z, uint32_t n, float inv,
+                                  uint32_t* __restrict__ counts, uint32_t* __restrict__ cell_of) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t c = (void_axis(x[i], inv) * kVoidCells + void_axis(y[i], inv)) * kVoidCells +
+                       void_axis(z[i], inv);
+    cell_of[i] = c;
+    atomicAdd(counts + c, 1u);
+  }
+}
+
+void build_void_index(const float* cx, const float* cy, const float* cz, uint32_t n, float box,
+                      uint32_t* start, uint32_t* ids, uint32_t* cell_of, cudaStream_t st) {
+  const uint32_t cells = kVoidCells * kVoidCells * kVoidCells;
+  SIFG_CUDA(cudaMemsetAsync(start, 0, (cells + 1) * sizeof(uint32_t), st));
+  if (n == 0) return;
+  const float inv = (float)kVoidCells / box;
+  void_count_kernel<<<grid_for(n, 256), 256, 0, st>>>(cx, cy, cz, n, inv, start, cell_of);
+  SIFG_LAUNCH_CHECK();
+  exclusive_scan_u32(start, cells + 1, st);
+  static DevBuf cursor;
+  uint32_t* cur = (uint32_t*)cursor.ensure((cells + 1) * sizeof(uint32_t));
+  SIFG_CUDA(cudaMemcpyAsync(cur, start, (cells + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+  scatter_ids_kernel<<<grid_for(n, 256), 256, 0, st>>>(cell_of, nullptr, n, cur, ids);
+  SIFG_LAUNCH_CHECK();
+}
+
+}  // namespace sifg

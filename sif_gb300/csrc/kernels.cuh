@@ -1,0 +1,66 @@
+// Host-side entry points of the kernel modules, and the small helpers they
+// share (device buffers, the event timer). Internal to the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace sifg {
+
+constexpr int kCicTile = 16;  // CIC tile side, in grid cells
+
+// Times a kernel with events on the stream it is launched on; accumulates.
+struct KernelTimer {
+  std::vector<cudaEvent_t> starts, stops;
+  int open = -1;
+  void begin(cudaStream_t st);
+  void end(cudaStream_t st);
+  double total_ms();  // synchronises; sums every begin/end pair recorded
+  int launches() const { return (int)stops.size(); }
+  void reset();
+  ~KernelTimer();
+};
+
+// A device allocation that grows on demand and is freed with its owner.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  void* ensure(size_t want);
+  void release();
+  ~DevBuf() { release(); }
+  template <class T>
+  T* as() const { return (T*)ptr; }
+};
+
+// --- scan.cu ---
+// In-place exclusive prefix sum of n uint32 values (n < 2^31).
+void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st);
+
+// --- cic.cu ---
+size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n);
+void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_particles,
+                 uint32_t n, float box, float* grid, void* scratch, cudaStream_t st,
+                 KernelTimer* timer);
+size_t density_contrast_scratch_bytes();
+void density_contrast(float* v, uint64_t n, double* d_scratch, cudaStream_t st);
+double read_mean(const double* d_scratch);
+
+// --- mesh.cu ---
+struct DeviceMesh {
+  uint32_t n_cells = 0;
+  float box_length = 0.f, cell_length = 0.f;
+  uint64_t n_particles = 0;
+  float *x = nullptr, *y = nullptr, *z = nullptr;
+  uint32_t* offsets = nullptr;  // n_cells^3 + 1
+  uint32_t* orig = nullptr;     // source index of each entry
+};
+size_t mesh_scratch_bytes(uint64_t n_particles, uint32_t n_cells);
+// Builds into caller buffers (x, y, z, offsets, orig sized for the mesh).
+void mesh_build(const float* x, const float* y, const float* z, uint64_t n_particles,
+                DeviceMesh& m, void* scratch, cudaStream_t st, KernelTimer* timer);
+
+}  // namespace sifg

@@ -1,0 +1,161 @@
+// Chain-mesh build: the particles grouped by mesh cell, cells in flat order,
+// each cell's particles in source order.
+//
+// Replaces chain_mesh_create + chain_mesh_canonicalise
+// (src/structures/chain_mesh.c:680-832, 420-542). The cell of a particle is
+// the reference's: (int32)(fold(x) * (1/cell_length)) clamped into the mesh
+// (chain_mesh.c:316-331), so the mesh is the reference's bit for bit.
+//
+//   1. cell_count:  per-cell counts, warp-aggregated atomics;
+//   2. exclusive scan into the cell offsets;
+//   3. cell_scatter: (source index, x, y, z) into each cell's range, in the
+//      order the atomics hand out slots;
+//   4. cell_canon:  per cell, each entry's rank among the cell's source
+//      indices (a count over the cell, with every lane reading the same
+//      shared word at once), and the entry written to that rank -- the
+//      canonical order, which no atomic race can change.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace sifg {
+
+struct MeshGeom {
+  uint32_t n;
+  float box;
+  float inv_l;  // 1.0f / cell_length
+};
+
+__device__ __forceinline__ uint32_t mesh_cell(float x, float y, float z, const MeshGeom& g) {
+  int32_t ix = (int32_t)fmul(box_fold(x, g.box), g.inv_l);
+  int32_t iy = (int32_t)fmul(box_fold(y, g.box), g.inv_l);
+  int32_t iz = (int32_t)fmul(box_fold(z, g.box), g.inv_l);
+  const int32_t hi = (int32_t)g.n - 1;
+  ix = ix < 0 ? 0 : (ix > hi ? hi : ix);
+  iy = iy < 0 ? 0 : (iy > hi ? hi : iy);
+  iz = iz < 0 ? 0 : (iz > hi ? hi : iz);
+  return ((uint32_t)ix * g.n + (uint32_t)iy) * g.n + (uint32_t)iz;
+}
+
+__global__ void cell_count_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                  const float* __restrict__ z, uint64_t n, MeshGeom g,
+                                  uint32_t* __restrict__ counts) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint64_t p = base + threadIdx.x;
+    const bool valid = p < n;
+    const uint32_t c = valid ? mesh_cell(x[p], y[p], z[p], g) : 0xffffffffu;
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    if (valid && (threadIdx.x & 31u) == (unsigned)(__ffs(peers) - 1))
+      atomicAdd(counts + c, (uint32_t)__popc(peers));
+  }
+}
+
+__global__ void cell_scatter_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                    const float* __restrict__ z, uint64_t n, MeshGeom g,
+                                    uint32_t* __restrict__ cursor, uint4* __restrict__ tmp) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint64_t p = base + threadIdx.x;
+    const bool valid = p < n;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    uint32_t c = 0xffffffffu;
+    if (valid) {
+      px = box_fold(x[p], g.box);
+      py = box_fold(y[p], g.box);
+      pz = box_fold(z[p], g.box);
+      c = mesh_cell(x[p], y[p], z[p], g);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    const unsigned leader = __ffs(peers) - 1;
+    uint32_t slot0 = 0;
+    if (valid && lane == leader) slot0 = atomicAdd(cursor + c, (uint32_t)__popc(peers));
+    slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+    if (valid) {
+      const uint32_t slot = slot0 + __popc(peers & ((1u << lane) - 1u));
+      tmp[slot] = make_uint4((uint32_t)p, __float_as_uint(px), __float_as_uint(py),
+                             __float_as_uint(pz));
+    }
+  }
+}
+
+constexpr int kCanonThreads = 128;
+constexpr int kCanonSmem = 2048;  // entries a CTA ranks in shared memory
+
+// One warp per cell. A cell of up to kCanonSmem/4 entries per warp is ranked
+// from shared memory; a larger one is ranked straight from global memory.
+__global__ void __launch_bounds__(kCanonThreads) cell_canon_kernel(
+    const uint4* __restrict__ tmp, const uint32_t* __restrict__ offsets, uint32_t n_cells_total,
+    float* __restrict__ ox, float* __restrict__ oy, float* __restrict__ oz,
+    uint32_t* __restrict__ orig) {
+  __shared__ uint32_t keys[kCanonSmem];
+  const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const unsigned warps = kCanonThreads / 32;
+  const uint32_t per_warp = kCanonSmem / warps;
+  uint32_t* wk = keys + warp * per_warp;
+  for (uint32_t cell = blockIdx.x * warps + warp; cell < n_cells_total;
+       cell += gridDim.x * warps) {
+    const uint32_t s = offsets[cell], e = offsets[cell + 1], cnt = e - s;
+    if (cnt == 0) continue;
+    const bool in_smem = cnt <= per_warp;
+    if (in_smem) {
+      for (uint32_t i = lane; i < cnt; i += 32) wk[i] = tmp[s + i].x;
+      __syncwarp();
+    }
+    for (uint32_t i = lane; i < cnt + (32 - cnt % 32) % 32; i += 32) {
+      const bool mine = i < cnt;
+      const uint4 v = mine ? tmp[s + i] : make_uint4(0, 0, 0, 0);
+      uint32_t rank = 0;
+      if (in_smem) {
+        for (uint32_t j = 0; j < cnt; j++) rank += wk[j] < v.x;
+      } else {
+        for (uint32_t j = 0; j < cnt; j++) rank += tmp[s + j].x < v.x;
+      }
+      if (mine) {
+        const uint32_t dst = s + rank;
+        ox[dst] = __uint_as_float(v.y);
+        oy[dst] = __uint_as_float(v.z);
+        oz[dst] = __uint_as_float(v.w);
+        if (orig) orig[dst] = v.x;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+size_t mesh_scratch_bytes(uint64_t n_particles, uint32_t n_cells) {
+  const uint64_t cells = (uint64_t)n_cells * n_cells * n_cells;
+  return n_particles * sizeof(uint4) + (cells + 1) * sizeof(uint32_t) + 1024;
+}
+
+void mesh_build(const float* x, const float* y, const float* z, uint64_t n_particles,
+                DeviceMesh& m, void* scratch, cudaStream_t st, KernelTimer* timer) {
+  MeshGeom g;
+  g.n = m.n_cells;
+  g.box = m.box_length;
+  g.inv_l = 1.0f / m.cell_length;
+  const uint64_t cells = (uint64_t)m.n_cells * m.n_cells * m.n_cells;
+  uint4* tmp = (uint4*)scratch;
+  uint32_t* cursor =
+      (uint32_t*)((char*)scratch + ((n_particles * sizeof(uint4) + 255) & ~(size_t)255));
+  SIFG_CUDA(cudaMemsetAsync(m.offsets, 0, (cells + 1) * sizeof(uint32_t), st));
+  const unsigned grd = grid_for(n_particles, 256, 152u * 16u);
+  if (timer) timer->begin(st);
+  cell_count_kernel<<<grd, 256, 0, st>>>(x, y, z, n_particles, g, m.offsets);
+  SIFG_LAUNCH_CHECK();
+  exclusive_scan_u32(m.offsets, (uint32_t)(cells + 1), st);
+  SIFG_CUDA(cudaMemcpyAsync(cursor, m.offsets, cells * sizeof(uint32_t),
+                            cudaMemcpyDeviceToDevice, st));
+  cell_scatter_kernel<<<grd, 256, 0, st>>>(x, y, z, n_particles, g, cursor, tmp);
+  SIFG_LAUNCH_CHECK();
+  const unsigned cgrid = grid_for(cells, kCanonThreads / 32 * 1, 152u * 16u);
+  cell_canon_kernel<<<cgrid, kCanonThreads, 0, st>>>(tmp, m.offsets, (uint32_t)cells, m.x, m.y,
+                                                     m.z, m.orig);
+  SIFG_LAUNCH_CHECK();
+  if (timer) timer->end(st);
+  m.n_particles = n_particles;
+}
+
+}  // namespace sifg

@@ -1,0 +1,164 @@
+// Exclusive prefix sums, and the small host helpers of kernels.cuh.
+//
+// The scan is the usual three phases: every CTA reduces its chunk, one CTA
+// scans the chunk totals, every CTA rescans its chunk from its total.
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace sifg {
+
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr uint32_t kScanChunk = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums,
+                                                         uint32_t& total) {
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= (unsigned)d) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    uint32_t w = lane < (unsigned)nw ? warp_sums[lane] : 0u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, d);
+      if (lane >= (unsigned)d) w += y;
+    }
+    if (lane < (unsigned)nw) warp_sums[lane] = w;
+  }
+  __syncthreads();
+  total = warp_sums[(blockDim.x >> 5) - 1];
+  const uint32_t before = warp ? warp_sums[warp - 1] : 0u;
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const uint32_t* __restrict__ d,
+                                                                   uint32_t n,
+                                                                   uint32_t* __restrict__ sums) {
+  __shared__ uint32_t ws[32];
+  const uint32_t base = blockIdx.x * kScanChunk;
+  uint32_t acc = 0;
+  for (int k = 0; k < kScanItems; k++) {
+    const uint32_t i = base + k * kScanThreads + threadIdx.x;
+    if (i < n) acc += d[i];
+  }
+  uint32_t total;
+  block_exclusive_scan(acc, ws, total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_sums_kernel(uint32_t* __restrict__ sums,
+                                                                 uint32_t m) {
+  __shared__ uint32_t ws[32];
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < m; base += kScanThreads) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < m ? sums[i] : 0u;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan(v, ws, total);
+    if (i < m) sums[i] = carry + ex;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(uint32_t* __restrict__ d,
+                                                                  uint32_t n,
+                                                                  const uint32_t* __restrict__ sums) {
+  __shared__ uint32_t ws[32];
+  const uint32_t base = blockIdx.x * kScanChunk;
+  // Each thread owns kScanItems consecutive entries.
+  const uint32_t first = base + threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t acc = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    const uint32_t i = first + k;
+    v[k] = i < n ? d[i] : 0u;
+    acc += v[k];
+  }
+  uint32_t total;
+  uint32_t run = block_exclusive_scan(acc, ws, total) + sums[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    const uint32_t i = first + k;
+    if (i < n) d[i] = run;
+    run += v[k];
+  }
+}
+
+void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st) {
+  if (n == 0) return;
+  const uint32_t blocks = (n + kScanChunk - 1) / kScanChunk;
+  static DevBuf sums;  // chunk totals; small
+  uint32_t* s = (uint32_t*)sums.ensure((size_t)blocks * sizeof(uint32_t));
+  scan_reduce_kernel<<<blocks, kScanThreads, 0, st>>>(data, n, s);
+  SIFG_LAUNCH_CHECK();
+  scan_sums_kernel<<<1, kScanThreads, 0, st>>>(s, blocks);
+  SIFG_LAUNCH_CHECK();
+  scan_apply_kernel<<<blocks, kScanThreads, 0, st>>>(data, n, s);
+  SIFG_LAUNCH_CHECK();
+}
+
+// --- helpers ---
+
+void* DevBuf::ensure(size_t want) {
+  if (want <= bytes && ptr) return ptr;
+  release();
+  size_t b = want < 256 ? 256 : want;
+  SIFG_CUDA(cudaMalloc(&ptr, b));
+  bytes = b;
+  return ptr;
+}
+
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+void KernelTimer::begin(cudaStream_t st) {
+  cudaEvent_t e;
+  SIFG_CUDA(cudaEventCreate(&e));
+  SIFG_CUDA(cudaEventRecord(e, st));
+  starts.push_back(e);
+  open = (int)starts.size() - 1;
+}
+
+void KernelTimer::end(cudaStream_t st) {
+  cudaEvent_t e;
+  SIFG_CUDA(cudaEventCreate(&e));
+  SIFG_CUDA(cudaEventRecord(e, st));
+  stops.push_back(e);
+  open = -1;
+}
+
+double KernelTimer::total_ms() {
+  double t = 0.0;
+  for (size_t i = 0; i < stops.size() && i < starts.size(); i++) {
+    SIFG_CUDA(cudaEventSynchronize(stops[i]));
+    float ms = 0.f;
+    SIFG_CUDA(cudaEventElapsedTime(&ms, starts[i], stops[i]));
+    t += ms;
+  }
+  return t;
+}
+
+void KernelTimer::reset() {
+  for (auto e : starts) cudaEventDestroy(e);
+  for (auto e : stops) cudaEventDestroy(e);
+  starts.clear();
+  stops.clear();
+  open = -1;
+}
+
+KernelTimer::~KernelTimer() { reset(); }
+
+}  // namespace sifg

@@ -1,0 +1,148 @@
+// The per-rung smoothing: cuFFT R2C of the density contrast once, then per
+// radius one fused filter kernel and a cuFFT C2R.
+//
+// Replaces sif__fft_grid_forward, fft_build_filter_lut,
+// sif__fft_apply_filter_smoothed and sif__fft_grid_backward
+// (src/math/fft.c:790-818, 521-568, 703-788, 820-888) and the window setup of
+// sif__finder_deconvolve_window (src/finder/utils.c:75-110,
+// src/math/fft.c:958-1046). cuFFT stands in for FFTW's planes and pencils.
+//
+// The filter kernel multiplies each mode by W(k R) (top-hat
+// 3(sin x - x cos x)/x^3, or Gaussian exp(-x^2/2)), by the CIC window
+// correction 1/sinc^2 per axis (or the aliasing-aware W/S), and by the C2R's
+// 1/N^3, reading the spectrum once and writing the transform's input once.
+// The radial factor comes from a table indexed by the integer |k|^2, built in
+// double by a small kernel, as the reference tabulates it. The unfiltered
+// pass (the grid handed back at the end of a run) applies no window, as the
+// reference's SIF__FILTER_NONE copies the spectrum untouched.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "smooth.cuh"
+
+namespace sifg {
+
+#define SIFG_CUFFT(call)                                                        \
+  do {                                                                          \
+    cufftResult r_ = (call);                                                    \
+    if (r_ != CUFFT_SUCCESS) throw ::sifg::CudaError{cudaErrorUnknown, #call};  \
+  } while (0)
+
+__global__ void filter_kernel(const float2* __restrict__ spec, float2* __restrict__ out,
+                              uint32_t n, const float* __restrict__ lut,
+                              const float* __restrict__ win, float norm) {
+  const uint32_t zd = n / 2 + 1;
+  const uint32_t h = n >> 1;
+  const uint64_t total = (uint64_t)n * n * zd;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    const uint32_t iz = (uint32_t)(i % zd);
+    const uint64_t row = i / zd;
+    const uint32_t iy = (uint32_t)(row % n), ix = (uint32_t)(row / n);
+    const int32_t kx = ix > h ? (int32_t)ix - (int32_t)n : (int32_t)ix;
+    const int32_t ky = iy > h ? (int32_t)iy - (int32_t)n : (int32_t)iy;
+    const uint32_t k2 = (uint32_t)(kx * kx + ky * ky) + iz * iz;
+    float s = __ldg(lut + k2) * norm;
+    if (win) s = s * __ldg(win + ix) * __ldg(win + iy) * __ldg(win + iz);
+    const float2 v = spec[i];
+    out[i] = make_float2(v.x * s, v.y * s);
+  }
+}
+
+// fft_build_filter_lut, src/math/fft.c:521-568: the radial factor by integer
+// |k|^2, computed in double.
+__global__ void lut_kernel(float* __restrict__ lut, uint32_t max_k2, int filter, double factor,
+                           double gfactor) {
+  for (uint32_t k2 = blockIdx.x * blockDim.x + threadIdx.x; k2 <= max_k2;
+       k2 += gridDim.x * blockDim.x) {
+    double v;
+    if (k2 == 0) {
+      v = 1.0;
+    } else if (filter == kFilterTopHat) {
+      const double kr = factor * sqrt((double)k2);
+      v = kr > 1e-4 ? 3.0 * (sin(kr) - kr * cos(kr)) / (kr * kr * kr) : 1.0;
+    } else if (filter == kFilterGaussian) {
+      v = exp(-0.5 * factor * factor * (double)k2);
+    } else {
+      v = 1.0;
+    }
+    if (gfactor > 0.0 && k2 > 0) v *= exp(-0.5 * gfactor * gfactor * (double)k2);
+    lut[k2] = (float)v;
+  }
+}
+
+Smoother::~Smoother() { release(); }
+
+void Smoother::release() {
+  if (plan_r2c) cufftDestroy(plan_r2c);
+  if (plan_c2r) cufftDestroy(plan_c2r);
+  plan_r2c = plan_c2r = 0;
+  n = 0;
+}
+
+void Smoother::setup(uint32_t n_, float box_, int window_mode_, cudaStream_t st) {
+  if (n_ != n || st != stream) {
+    release();
+    n = n_;
+    stream = st;
+    SIFG_CUFFT(cufftPlan3d(&plan_r2c, (int)n, (int)n, (int)n, CUFFT_R2C));
+    SIFG_CUFFT(cufftPlan3d(&plan_c2r, (int)n, (int)n, (int)n, CUFFT_C2R));
+    SIFG_CUFFT(cufftSetStream(plan_r2c, st));
+    SIFG_CUFFT(cufftSetStream(plan_c2r, st));
+  }
+  box = box_;
+  window_mode = window_mode_;
+  const uint64_t modes = (uint64_t)n * n * (n / 2 + 1);
+  spectrum.ensure(modes * sizeof(float2));
+  work.ensure(modes * sizeof(float2));
+  const uint32_t h = n >> 1;
+  const uint32_t max_k2 = 3 * h * h;
+  lut.ensure(((size_t)max_k2 + 1) * sizeof(float));
+  win.ensure((size_t)n * sizeof(float));
+  if (window_mode) {
+    // fft_build_window_axis, src/math/fft.c:958-975, CIC (order 2): 1/W full,
+    // W/S aliasing-aware, W = sinc^2(pi k / N), S = 1 - 2 sin^2/3.
+    std::vector<float> w(n);
+    for (uint32_t i = 0; i < n; i++) {
+      const int32_t k = i > h ? (int32_t)i - (int32_t)n : (int32_t)i;
+      const double x = M_PI * (double)k / (double)n;
+      const double s = (x < 1e-9 && x > -1e-9) ? 1.0 : std::sin(x) / x;
+      const double W = s * s;
+      w[i] = (float)(window_mode == 2 ? W / (1.0 - 2.0 * std::sin(x) * std::sin(x) / 3.0)
+                                      : 1.0 / W);
+    }
+    SIFG_CUDA(cudaMemcpyAsync(win.ptr, w.data(), n * sizeof(float), cudaMemcpyHostToDevice, st));
+    SIFG_CUDA(cudaStreamSynchronize(st));
+  }
+}
+
+void Smoother::forward(const float* grid) {
+  SIFG_CUFFT(cufftExecR2C(plan_r2c, (cufftReal*)grid, (cufftComplex*)spectrum.ptr));
+}
+
+void Smoother::smooth(int filter, float r, float sigma, float* out, KernelTimer* timer) {
+  const uint32_t h = n >> 1;
+  const uint32_t max_k2 = 3 * h * h;
+  const double factor = (double)r * 2.0 * M_PI / (double)box;
+  const double gfactor = sigma > 0.0f ? (double)sigma * 2.0 * M_PI / (double)box : 0.0;
+  lut_kernel<<<grid_for((uint64_t)max_k2 + 1, 256), 256, 0, stream>>>(lut.as<float>(), max_k2,
+                                                                        filter, factor, gfactor);
+  SIFG_LAUNCH_CHECK();
+  const uint64_t modes = (uint64_t)n * n * (n / 2 + 1);
+  const float norm = (float)(1.0 / ((double)n * n * n));
+  if (timer) timer->begin(stream);
+  filter_kernel<<<grid_for(modes, 256, 152u * 8u), 256, 0, stream>>>(
+      spectrum.as<float2>(), work.as<float2>(), n, lut.as<float>(),
+      (window_mode && filter != kFilterNone) ? win.as<float>() : nullptr, norm);
+  SIFG_LAUNCH_CHECK();
+  if (timer) timer->end(stream);
+  SIFG_CUFFT(cufftExecC2R(plan_c2r, (cufftComplex*)work.ptr, (cufftReal*)out));
+}
+
+void Smoother::restore(float* out) { smooth(kFilterNone, 0.f, 0.f, out, nullptr); }
+
+}  // namespace sifg

@@ -1,0 +1,116 @@
+"""Device-resident entry points over torch CUDA tensors.
+
+torch only allocates and holds the device memory here; every stage is a call
+into libsif_gb300.so (include/sif_gb300.h, part 2) with raw device pointers.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib, abi
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    assert t.is_cuda and t.is_contiguous(), "expected a contiguous CUDA tensor"
+    return C.c_void_p(t.data_ptr())
+
+
+def _check(status, what):
+    if status != abi.SIF_OK:
+        raise _lib.status_error(_lib.load(), status, what)
+
+
+def cic(x, y, z, n_grid, box):
+    import torch
+
+    grid = torch.empty(n_grid ** 3, dtype=torch.float32, device=x.device)
+    _check(_lib.load().sifg_cic_device(_ptr(x), _ptr(y), _ptr(z), x.numel(), n_grid, box,
+                                       _ptr(grid)), "cic")
+    return grid
+
+
+def density_contrast(grid):
+    mean = C.c_double(0.0)
+    _check(_lib.load().sifg_contrast_device(_ptr(grid), grid.numel(), C.byref(mean)), "contrast")
+    return mean.value
+
+
+def chain_mesh(x, y, z, n_cells, box, with_indices=True):
+    import torch
+
+    n = x.numel()
+    dev = x.device
+    mx = torch.empty(n, dtype=torch.float32, device=dev)
+    my = torch.empty_like(mx)
+    mz = torch.empty_like(mx)
+    offs = torch.empty(n_cells ** 3 + 1, dtype=torch.int32, device=dev)
+    orig = torch.empty(n, dtype=torch.int32, device=dev) if with_indices else None
+    _check(_lib.load().sifg_mesh_device(_ptr(x), _ptr(y), _ptr(z), n, n_cells, box, _ptr(mx),
+                                        _ptr(my), _ptr(mz), _ptr(offs), _ptr(orig)), "chain_mesh")
+    return mx, my, mz, offs, orig
+
+
+def smooth(delta, n_grid, box, radius, filter="top-hat", window="full"):
+    import torch
+
+    out = torch.empty(n_grid ** 3, dtype=torch.float32, device=delta.device)
+    f = {"top-hat": 1, "gaussian": 2}[filter]
+    w = {"none": 0, "full": 1, "aliasing": 2}[window]
+    _check(_lib.load().sifg_smooth_device(_ptr(delta), n_grid, box, radius, f, w, _ptr(out)),
+           "smooth")
+    return out
+
+
+def _catalogue_arrays(cap):
+    return [np.empty(cap, np.float32) for _ in range(4)]
+
+
+def exodus(delta, n_grid, box, mesh, mesh_cells, radii, threshold, overlap=0.0, options=0,
+           inject=None, capacity=1 << 22):
+    """The finder on device data. mesh = (mx, my, mz, offsets, ...)."""
+    lib = _lib.load()
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    cols = _catalogue_arrays(capacity)
+    n = C.c_uint64(0)
+    mx, my, mz, offs = mesh[:4]
+    st = lib.sifg_exodus_device(_ptr(delta), n_grid, box, _ptr(mx), _ptr(my), _ptr(mz),
+                                _ptr(offs), mx.numel(), mesh_cells,
+                                radii.ctypes.data_as(C.c_void_p), len(radii), threshold, overlap,
+                                options, _ptr(inject), *[c.ctypes.data_as(C.c_void_p) for c in cols],
+                                capacity, C.byref(n))
+    _check(st, "exodus")
+    return tuple(c[: n.value].copy() for c in cols)
+
+
+def box(x, y, z, n_grid, box_length, mesh_cells, radii, threshold, overlap=0.0, options=0,
+        capacity=1 << 22):
+    """The whole path on device particles: CIC, contrast, mesh, finder."""
+    lib = _lib.load()
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    cols = _catalogue_arrays(capacity)
+    n = C.c_uint64(0)
+    st = lib.sifg_box_device(_ptr(x), _ptr(y), _ptr(z), x.numel(), n_grid, box_length, mesh_cells,
+                             radii.ctypes.data_as(C.c_void_p), len(radii), threshold, overlap,
+                             options, *[c.ctypes.data_as(C.c_void_p) for c in cols], capacity,
+                             C.byref(n))
+    _check(st, "box")
+    return tuple(c[: n.value].copy() for c in cols)
+
+
+def last_rung_stats():
+    lib = _lib.load()
+    arr = (_lib.RungStat * 256)()
+    k = lib.sifg_last_rung_stats(arr, 256)
+    return [{f: getattr(arr[i], f) for f, _ in _lib.RungStat._fields_} for i in range(min(k, 256))]
+
+
+def last_timings():
+    t = _lib.Timings()
+    _lib.load().sifg_last_timings(C.byref(t))
+    return {f: getattr(t, f) for f, _ in _lib.Timings._fields_}
+
+
+def set_window(bins):
+    _lib.load().sifg_set_window(int(bins))

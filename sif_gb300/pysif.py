@@ -1,0 +1,192 @@
+"""The pysif interface for the exodus path, over the GB300 library.
+
+Mirrors the names and argument meanings of pysif (python/pysif/__init__.pyi,
+finders.pyi:37-140; python/src/finders/py_finders.c:362-477;
+python/src/structures/py_grid.c:49-122) so scripts written against pysif's
+exodus path run unchanged: ``system_init``, ``Field``, ``Grid.assign_cic``,
+``Grid.to_density_contrast``, ``ChainMesh``, ``finders.exodus`` and
+``finders.exodus_raw``. Each call goes through sif's C API as the GB300
+library exports it; the work runs on the GPU.
+"""
+import ctypes as C
+import types
+
+import numpy as np
+
+from . import _lib, abi
+
+
+def _P(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _check(status, what):
+    if status != abi.SIF_OK:
+        raise _lib.status_error(_lib.load(), status, what)
+
+
+def system_init(n_threads=0, log_level="warning", skip_tuning=True):
+    """pysif.system_init: selects the GPU; n_threads sizes the host team."""
+    lib = _lib.load()
+    levels = {"trace": 0, "debug": 1, "info": 2, "warning": 3, "error": 4, "none": 5}
+    fft = abi.sif_fft_config_t(skip_tuning=skip_tuning)
+    omp = abi.sif_omp_config_t(n_threads=n_threads)
+    cfg = abi.sif_config_t(C.pointer(fft), C.pointer(omp), levels[log_level], None, 0)
+    _check(lib.sif_system_init(C.byref(cfg)), "system_init")
+
+
+def system_finalise():
+    _lib.load().sif_system_finalise()
+
+
+class Field:
+    """Particle positions (float32, in [0, box))."""
+
+    def __init__(self, x, y, z):
+        lib = _lib.load()
+        x, y, z = (np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z))
+        if not (len(x) == len(y) == len(z)):
+            raise ValueError("positions: x, y and z differ in length")
+        self._ptr = lib.sif_field_alloc(len(x))
+        if not self._ptr:
+            raise MemoryError("field")
+        _check(lib.sif_field_assign_positions(self._ptr, _P(x), _P(y), _P(z)), "Field")
+
+    @property
+    def n_particles(self):
+        return self._ptr.contents.n_particles if self._ptr else 0
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            _lib.load().sif_field_free(self._ptr)
+            self._ptr = None
+
+
+class Grid:
+    """A cubic grid of n_cells^3 float32 cells over [0, box)^3."""
+
+    def __init__(self, n_cells, box_length):
+        lib = _lib.load()
+        self._ptr = lib.sif_grid_alloc(n_cells, box_length)
+        if not self._ptr:
+            raise _lib.status_error(lib, lib.sif_error_status(), "Grid")
+
+    @property
+    def n_cells(self):
+        return self._ptr.contents.n_cells
+
+    @property
+    def box_length(self):
+        return self._ptr.contents.box_length
+
+    @property
+    def values(self):
+        """A view of the cells, (n, n, n), x slowest."""
+        g = self._ptr.contents
+        return np.ctypeslib.as_array(g.values, shape=(g.n_cells,) * 3)
+
+    def assign_cic(self, field):
+        _check(_lib.load().sif_grid_assign_cic(self._ptr, field._ptr), "assign_cic")
+
+    def to_density_contrast(self):
+        _check(_lib.load().sif_grid_to_density_contrast(self._ptr), "to_density_contrast")
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            _lib.load().sif_grid_free(self._ptr)
+            self._ptr = None
+
+
+class ChainMesh:
+    """Particles grouped by cell (sif_chain_mesh_alloc)."""
+
+    def __init__(self, n_cells, box_length, field, drop_indices=False, consume=False):
+        lib = _lib.load()
+        opt = abi.SIF_MESH_DROP_INDICES if drop_indices else 0
+        fn = lib.sif_chain_mesh_alloc_consume if consume else lib.sif_chain_mesh_alloc
+        self._ptr = fn(n_cells, box_length, field._ptr, opt)
+        if not self._ptr:
+            raise _lib.status_error(lib, lib.sif_error_status(), "ChainMesh")
+
+    def arrays(self):
+        m = self._ptr.contents
+        n = m.n_particles
+
+        def col(p):
+            return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+        offs = np.ctypeslib.as_array(m.cell_offsets, shape=(m.total_cells + 1,)).copy()
+        idx = np.ctypeslib.as_array(m.original_indices, shape=(n,)).copy() \
+            if m.original_indices else None
+        return col(m.x), col(m.y), col(m.z), offs, idx
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            _lib.load().sif_chain_mesh_free(self._ptr)
+            self._ptr = None
+
+
+class Catalogue:
+    """Void centres and radii (float32 arrays)."""
+
+    def __init__(self, cx, cy, cz, radii):
+        self.cx, self.cy, self.cz, self.radii = cx, cy, cz, radii
+
+    def __len__(self):
+        return len(self.radii)
+
+    def as_tuple(self):
+        return self.cx, self.cy, self.cz, self.radii
+
+
+def _take_catalogue(lib, ptr, what):
+    if not ptr:
+        raise _lib.status_error(lib, lib.sif_error_status(), what)
+    cat = ptr.contents
+    n = cat.n_voids
+    cols = [np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0, np.float32)
+            for p in (cat.cx, cat.cy, cat.cz, cat.radii)]
+    lib.sif_catalogue_free(ptr)
+    return Catalogue(*cols)
+
+
+_VARIANTS = {"excursion-set": 0, "excursion-peak": 1, "lagrangian-overlap": 2}
+_SEARCH = {1.5: abi.SIF_FINDER_SEARCH_1_50, 1.25: abi.SIF_FINDER_SEARCH_1_25,
+           1.75: abi.SIF_FINDER_SEARCH_1_75, 2.0: abi.SIF_FINDER_SEARCH_2_00}
+
+
+def _exodus(grid, mesh, radii, threshold, variant="excursion-set", *, checkpoint=None,
+            prior=None, keep_checkpoint=False, save_memory=False):
+    """finders.exodus (python/pysif/finders.pyi:37-140)."""
+    lib = _lib.load()
+    if variant not in _VARIANTS:
+        raise ValueError(f"variant: {variant!r}")
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    extras = None
+    if checkpoint or prior is not None or save_memory:
+        raise NotImplementedError("checkpoints, prior catalogues and save_memory")
+    ptr = lib.sif_finder_exodus(grid._ptr, mesh._ptr, _P(radii), len(radii), threshold,
+                                _VARIANTS[variant], extras)
+    return _take_catalogue(lib, ptr, "exodus")
+
+
+def _exodus_raw(grid, mesh, radii, threshold, overlap_fraction=0.0, *, overlap_type="eulerian",
+                search_factor=1.5, deconvolution="full", consume_grid=False, checkpoint=False):
+    """finders.exodus_raw, for the options the GPU finder runs."""
+    lib = _lib.load()
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    opt = _SEARCH[float(search_factor)] | abi.SIF_FINDER_NO_CHECKPOINT
+    if overlap_type == "lagrangian":
+        opt |= abi.SIF_FINDER_LAGRANGIAN_OVERLAP
+    if deconvolution == "none":
+        opt |= abi.SIF_FINDER_KEEP_CIC_WINDOW
+    elif deconvolution == "aliasing":
+        opt |= abi.SIF_FINDER_ALIASING_WINDOW
+    if consume_grid:
+        opt |= abi.SIF_FINDER_CONSUME_GRID
+    ptr = lib.sif_finder_exodus_raw(grid._ptr, mesh._ptr, _P(radii), len(radii), threshold,
+                                    overlap_fraction, opt, None)
+    return _take_catalogue(lib, ptr, "exodus_raw")
+
+
+finders = types.SimpleNamespace(exodus=_exodus, exodus_raw=_exodus_raw)
