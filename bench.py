@@ -1,0 +1,380 @@
+"""Benchmark of the exodus box path on GB300: Mparticles/s at 512^3.
+
+One step is the whole path over one box: CIC deposit, density contrast,
+chain-mesh build, and the finder over the 19-rung ladder (per rung: filter +
+C2R, candidate scan, pre-filter, sphere growth, commit), ending with the
+catalogue on the host.
+
+- ``value``: the step on particles already resident in HBM
+  (sifg_box_device), timed with CUDA events on the library's own stream.
+- ``e2e``: the same step through sif's C API with host buffers
+  (sif_grid_assign_cic, sif_grid_to_density_contrast, sif_chain_mesh_alloc,
+  sif_finder_exodus_raw), every host<->device copy inside the timed region.
+- ``cpu_baseline``: the CPU restatement of the reference's path (oracle/)
+  with all host cores, on a bounded sample of the same recipe.
+
+``--impl reference`` times that CPU path alone (the reference arm).
+Under torchrun every rank runs its own replica (the path does not shard).
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "exodus Mparticles/s at 512^3"
+UNIT = "Mparticles/s"
+
+# The 512^3 workload: Zel'dovich lattice, box 1000 Mpc/h, rms displacement 5,
+# seed 1002; grid 512^3; mesh cells of 8 Mpc/h; ladder(4, 24, 0.10);
+# threshold -0.8; excursion-set variant.
+WORKLOAD = dict(name="B", n=512, box=1000.0, rms=5.0, seed=1002, grid=512, mesh=125, r0=4.0,
+                threshold=-0.8)
+# The CPU sample: the same recipe (density, grid spacing, mesh cell, ladder,
+# displacement) on a periodic box of 1/64 the volume.
+CPU_SAMPLE = dict(n=128, box=250.0, rms=5.0, seed=1102, grid=128, mesh=31, r0=4.0,
+                  threshold=-0.8)
+
+
+def radii_of(w):
+    from sif_gb300 import synth
+
+    return synth.ladder(w["r0"], 6.0 * w["r0"], 0.10).astype(np.float32)
+
+
+def small_workload():
+    return dict(name="A-small", n=128, box=500.0, rms=4.0, seed=1001, grid=128, mesh=50, r0=5.0,
+                threshold=-0.8)
+
+
+# --------------------------------------------------------------------------
+# clocks
+# --------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# the GPU arm
+# --------------------------------------------------------------------------
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def gpu_arm(args, rank, world):
+    import torch
+
+    from sif_gb300 import abi, build, device, pysif, synth
+
+    build.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    pysif.system_init(log_level="error")
+    w = small_workload() if args.small else WORKLOAD
+    radii = radii_of(w)
+    x, y, z = synth.zeldovich(w["n"], w["box"], w["rms"], w["seed"], backend="torch")
+    n = len(x)
+    xs = [torch.from_numpy(a).cuda() for a in (x, y, z)]
+    torch.cuda.synchronize()
+    stream = device.stream()
+
+    def step():
+        return device.box(*xs, w["grid"], w["box"], w["mesh"], radii, w["threshold"])
+
+    for _ in range(args.warmup):
+        cat = step()
+    n_voids = len(cat[0])
+    launches0 = device.launch_count()
+    timings = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+            timings.append(device.last_timings())
+        end.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+    ms = start.elapsed_time(end) / args.steps
+    launches = (device.launch_count() - launches0) // args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms / 1e3) / 1e6
+
+    # Roofline of the dominant kernel of the step, from the last step's events.
+    tm = timings[-1]
+    peak, peak_kind = peaks()
+    kernels = {
+        "growth_kernel": (tm["growth_ms"], tm["growth_launches"],
+                          12.0 * tm["growth_particles"] + 16.0 * tm["growth_cells"]),
+        "tile_deposit_kernel": (tm["cic_ms"], tm["cic_launches"],
+                                12.0 * n + 4.0 * w["grid"] ** 3),
+        "filter_kernel": (tm["filter_ms"], tm["filter_launches"],
+                          tm["filter_launches"] * 16.0 * w["grid"] ** 2 * (w["grid"] // 2 + 1)),
+    }
+    dom = max(kernels, key=lambda k: kernels[k][0])
+    rooflines = {}
+    for k, (kms, kl, kbytes) in kernels.items():
+        if kl == 0 or kms <= 0:
+            continue
+        per_launch = kbytes / kl
+        achieved = per_launch / (kms / kl / 1e3) / 1e9
+        traffic = profiled_traffic(k)
+        rooflines[k] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                        "unit": "GB/s", "frac": round(achieved / peak, 4),
+                        "traffic": traffic, "ms_per_launch": round(kms / kl, 4),
+                        "launches_per_step": kl,
+                        "algorithmic_bytes_per_launch": per_launch,
+                        "peak_kind": peak_kind}
+
+    # e2e: sif's C API on host buffers.
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_run(args, w, x, y, z, radii)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_run(seconds=args.cpu_seconds)
+
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic Zel'dovich lattice (seeded), no dataset",
+        "config": {"workload": ("512^3 particles, box 1000 Mpc/h, grid 512^3, mesh 125^3 (8 Mpc/h),"
+                                " ladder(4, 24, 0.10) 19 rungs, threshold -0.8, excursion-set")
+                   if not args.small else "128^3 particles, box 500, grid 128^3, mesh 50^3",
+                   "n_particles": n, "n_voids": n_voids, "l2": "inputs larger than L2 (1.6 GB of particles)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "window_bins": 8},
+        "roofline": dict(rooflines.get(dom, {}), kernel=dom),
+        "rooflines": rooflines,
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "stages_ms_last_step": {"growth": round(tm["growth_ms"], 3), "cic_deposit": round(tm["cic_ms"], 3),
+                                "mesh": round(tm["mesh_ms"], 3), "filter": round(tm["filter_ms"], 3),
+                                "wall": round(tm["wall_ms"], 3)},
+        "rungs_last_step": device.last_rung_stats() if args.verbose else None,
+    }
+    return line
+
+
+def e2e_run(args, w, x, y, z, radii):
+    from sif_gb300 import _lib, abi
+
+    lib = _lib.load()
+    n = len(x)
+    P = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    field = lib.sif_field_alloc(n)
+    assert lib.sif_field_assign_positions(field, P(x), P(y), P(z)) == 0
+    grid = lib.sif_grid_alloc(w["grid"], w["box"])
+    r = np.ascontiguousarray(radii, np.float32)
+    opt = abi.SIF_FINDER_NO_CHECKPOINT
+
+    def step():
+        grid.contents.content = abi.SIF_GRID_EMPTY
+        assert lib.sif_grid_assign_cic(grid, field) == 0
+        assert lib.sif_grid_to_density_contrast(grid) == 0
+        mesh = lib.sif_chain_mesh_alloc(w["mesh"], w["box"], field, abi.SIF_MESH_DROP_INDICES)
+        assert mesh
+        cat = lib.sif_finder_exodus_raw(grid, mesh, P(r), len(r), w["threshold"], 0.0, opt, None)
+        assert cat
+        nv = cat.contents.n_voids
+        lib.sif_catalogue_free(cat)
+        lib.sif_chain_mesh_free(mesh)
+        return nv
+
+    steps = max(1, min(args.steps, args.e2e_steps))
+    for _ in range(max(1, min(args.warmup, 2))):
+        nv = step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        nv = step()
+    dt = (time.perf_counter() - t0) / steps
+    lib.sif_grid_free(grid)
+    lib.sif_field_free(field)
+    nc, mc = w["grid"] ** 3, w["mesh"] ** 3 + 1
+    h2d = 2 * 12 * n + 4 * nc + 4 * nc + 12 * n + 4 * mc
+    d2h = 4 * nc + 4 * nc + 12 * n + 4 * mc + 16 * nv
+    return {"value": round(n / dt / 1e6, 2), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": round(dt * 1e3, 2), "steps": steps}
+
+
+# --------------------------------------------------------------------------
+# the CPU path (the oracle port of the reference)
+# --------------------------------------------------------------------------
+
+def cpu_pipeline(O, x, y, z, w, radii, threads):
+    """The whole path through the CPU restatement: CIC, contrast, mesh,
+    finder (its own smoothing)."""
+    d = O.density_contrast(O.cic_f64(x, y, z, w["grid"], w["box"]).astype(np.float32))
+    m = O.OracleMesh(x, y, z, w["mesh"], w["box"])
+    return O.exodus(d, m, radii, w["grid"], w["box"], w["threshold"], n_threads=threads)
+
+
+def cpu_run(seconds=20.0, steps=None, warmup=1):
+    import oracle_ctypes as O
+
+    from sif_gb300 import synth
+
+    O.build()
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    w = CPU_SAMPLE
+    radii = radii_of(w)
+    x, y, z = synth.zeldovich(w["n"], w["box"], w["rms"], w["seed"])
+    for _ in range(warmup):
+        cpu_pipeline(O, x, y, z, w, radii, threads)
+    times = []
+    t_start = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        cpu_pipeline(O, x, y, z, w, radii, threads)
+        times.append(time.perf_counter() - t0)
+        if steps is not None and len(times) >= steps:
+            break
+        if steps is None and time.perf_counter() - t_start >= seconds:
+            break
+    dt = statistics.median(times)
+    sample = (f"the same recipe on a {w['n']}^3-particle periodic box of {w['box']} Mpc/h (1/64 "
+              f"of the volume: same density, grid spacing, mesh cell, ladder), whole path, "
+              f"median of {len(times)} runs")
+    return {"value": round(len(x) / dt / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": sample, "ms_per_step": round(dt * 1e3, 1)}
+
+
+def reference_arm(args):
+    cpu = cpu_run(steps=args.steps, warmup=args.warmup)
+    return {
+        "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cpu["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic Zel'dovich lattice (seeded), no dataset",
+        "config": {"workload": "512^3 recipe, timed on " + cpu["sample"]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--small", action="store_true", help="a 128^3 box, for quick checks")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--verbose", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(reference_arm(args)))
+        return 0
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    line = gpu_arm(args, rank, world)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

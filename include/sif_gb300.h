@@ -276,6 +276,10 @@ typedef struct {
   int cic_launches;
   double mesh_ms;
   int mesh_launches;
+  /* What the sphere growth gathered: particle positions read (12 bytes
+   * each) and template cells visited (16 bytes each). */
+  uint64_t growth_particles;
+  uint64_t growth_cells;
 } sifg_timings_t;
 
 /* The CIC density (per unit volume, float) of n device-resident particles
@@ -314,6 +318,12 @@ int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, 
 /* Statistics and timings of the last run (up to max_rungs entries). */
 uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs);
 void sifg_last_timings(sifg_timings_t* out);
+/* Kernels of this library launched so far in the process (cuFFT's own are
+ * not counted). */
+uint64_t sifg_launch_count(void);
+/* The CUDA stream every call above runs on (a cudaStream_t), for callers
+ * that time or order work against it; 0 before sif_system_init(). */
+uint64_t sifg_stream(void);
 /* The resolve window (bins per pass) the sphere growth uses; default 8. */
 void sifg_set_window(int bins);
 /* The replay of the reference's candidate order on host data, for tests:

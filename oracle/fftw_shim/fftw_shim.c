@@ -244,20 +244,25 @@ static void pass_axis(cplx* a, const int* shape, int r, int ax, const engine_t* 
   size_t outer = 1;
   for (int d = 0; d < ax; d++)
     outer *= (size_t)shape[d];
-  cplx* line = malloc(sizeof(cplx) * len);
-  cplx* work = malloc(sizeof(cplx) * engine_work(e));
-  for (size_t o = 0; o < outer; o++) {
-    for (size_t s = 0; s < stride; s++) {
-      cplx* base = a + o * len * stride + s;
-      for (size_t j = 0; j < len; j++)
-        line[j] = base[j * stride];
-      engine_run(e, line, work);
-      for (size_t j = 0; j < len; j++)
-        base[j * stride] = line[j];
+  /* Every line is independent: a team shares them when OpenMP is on. */
+#pragma omp parallel
+  {
+    cplx* line = malloc(sizeof(cplx) * len);
+    cplx* work = malloc(sizeof(cplx) * engine_work(e));
+#pragma omp for schedule(static) collapse(2)
+    for (size_t o = 0; o < outer; o++) {
+      for (size_t s = 0; s < stride; s++) {
+        cplx* base = a + o * len * stride + s;
+        for (size_t j = 0; j < len; j++)
+          line[j] = base[j * stride];
+        engine_run(e, line, work);
+        for (size_t j = 0; j < len; j++)
+          base[j * stride] = line[j];
+      }
     }
+    free(line);
+    free(work);
   }
-  free(line);
-  free(work);
 }
 
 static void exec_r2c(const struct shim_fft_plan* p, const void* in, void* out) {
@@ -273,20 +278,24 @@ static void exec_r2c(const struct shim_fft_plan* p, const void* in, void* out) {
   shape[r - 1] = half;
 
   cplx* spec = malloc(sizeof(cplx) * rows * (size_t)half);
-  cplx* line = malloc(sizeof(cplx) * (size_t)nl);
-  cplx* work = malloc(sizeof(cplx) * engine_work(p->eng[r - 1]));
-  for (size_t row = 0; row < rows; row++) {
-    for (int j = 0; j < nl; j++) {
-      const size_t i = row * (size_t)nl + (size_t)j;
-      line[j].re = p->is_float ? (double)((const float*)in)[i]
-                               : ((const double*)in)[i];
-      line[j].im = 0.0;
+#pragma omp parallel
+  {
+    cplx* line = malloc(sizeof(cplx) * (size_t)nl);
+    cplx* work = malloc(sizeof(cplx) * engine_work(p->eng[r - 1]));
+#pragma omp for schedule(static)
+    for (size_t row = 0; row < rows; row++) {
+      for (int j = 0; j < nl; j++) {
+        const size_t i = row * (size_t)nl + (size_t)j;
+        line[j].re = p->is_float ? (double)((const float*)in)[i]
+                                 : ((const double*)in)[i];
+        line[j].im = 0.0;
+      }
+      engine_run(p->eng[r - 1], line, work);
+      memcpy(spec + row * (size_t)half, line, sizeof(cplx) * (size_t)half);
     }
-    engine_run(p->eng[r - 1], line, work);
-    memcpy(spec + row * (size_t)half, line, sizeof(cplx) * (size_t)half);
+    free(line);
+    free(work);
   }
-  free(line);
-  free(work);
   for (int ax = r - 2; ax >= 0; ax--)
     pass_axis(spec, shape, r, ax, p->eng[ax]);
   for (size_t i = 0; i < rows * (size_t)half; i++)
@@ -312,8 +321,11 @@ static void exec_c2r(const struct shim_fft_plan* p, const void* in, void* out) {
   for (int ax = 0; ax <= r - 2; ax++)
     pass_axis(spec, shape, r, ax, p->eng[ax]);
 
+#pragma omp parallel
+  {
   cplx* line = malloc(sizeof(cplx) * (size_t)nl);
   cplx* work = malloc(sizeof(cplx) * engine_work(p->eng[r - 1]));
+#pragma omp for schedule(static)
   for (size_t row = 0; row < rows; row++) {
     const cplx* s = spec + row * (size_t)half;
     /* The Hermitian completion; the imaginary parts of the self-conjugate
@@ -335,6 +347,7 @@ static void exec_c2r(const struct shim_fft_plan* p, const void* in, void* out) {
   }
   free(line);
   free(work);
+  }
   free(spec);
 }
 

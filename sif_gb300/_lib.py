@@ -24,7 +24,8 @@ class Timings(C.Structure):
     _fields_ = [("wall_ms", C.c_double), ("growth_ms", C.c_double), ("growth_launches", C.c_int),
                 ("filter_ms", C.c_double), ("filter_launches", C.c_int),
                 ("cic_ms", C.c_double), ("cic_launches", C.c_int),
-                ("mesh_ms", C.c_double), ("mesh_launches", C.c_int)]
+                ("mesh_ms", C.c_double), ("mesh_launches", C.c_int),
+                ("growth_particles", C.c_uint64), ("growth_cells", C.c_uint64)]
 
 
 EXPORTED = [
@@ -39,7 +40,7 @@ EXPORTED = [
     # device-resident additions
     "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
     "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
-    "sifg_set_window", "sifg_candidate_ranks",
+    "sifg_set_window", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
 ]
 
 
@@ -66,6 +67,8 @@ def load():
         "sifg_last_rung_stats": (u32, [C.POINTER(RungStat), u32]),
         "sifg_last_timings": (None, [C.POINTER(Timings)]),
         "sifg_set_window": (None, [i32]),
+        "sifg_stream": (u64, []),
+        "sifg_launch_count": (u64, []),
         "sifg_candidate_ranks": (None, [vp, u32, vp]),
     }
     for name, (res, args) in sigs.items():

@@ -192,6 +192,8 @@ static void record_timings(RunTimings& t) {
   g_timings.cic_launches = t.cic.launches();
   g_timings.mesh_ms = t.mesh.total_ms();
   g_timings.mesh_launches = t.mesh.launches();
+  g_timings.growth_particles = t.growth_particles;
+  g_timings.growth_cells = t.growth_cells;
 }
 
 }  // namespace sifg
@@ -890,6 +892,19 @@ uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
 
 void sifg_last_timings(sifg_timings_t* out) {
   if (out) *out = g_timings;
+}
+
+uint64_t sifg_launch_count(void) { return g_kernel_launches.load(); }
+
+uint64_t sifg_stream(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  try {
+    Engine* e = engine();
+    return e ? (uint64_t)(uintptr_t)e->stream() : 0;
+  } catch (const CudaError& err) {
+    cuda_fail(err);
+    return 0;
+  }
 }
 
 void sifg_set_window(int bins) { g_window = bins < 1 ? 1 : (bins > 64 ? 64 : bins); }

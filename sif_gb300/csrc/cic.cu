@@ -38,16 +38,34 @@ struct CicGeom {
   uint32_t n;       // grid cells per side
   uint32_t nt;      // tiles per side
   float box;
-  float idx;        // (float)n / box, as the reference computes it
+  float idx_hi;     // n / box in double, as a pair of floats
+  float idx_lo;
 };
 
-// The reference's base cell along one axis (grid.c:585-620): u = fold(v) * idx,
-// raw = (uint32)u, cell = raw >= n ? 0 : raw, t = u - raw.
+// A coordinate in cell units, u = fold(v) * n / box, and its base cell and
+// fraction (grid.c:585-620: cell = floor(u), wrapped into [0, n); t = u -
+// floor(u)). The reference rounds u to a float, which moves t by up to an
+// ulp of u -- 1e-5 of a cell at u ~ 128; here the product is kept exact as
+// hi + lo (lo from the fused multiply-add's residual), so t is good to an ulp
+// of 1 and the deposit's error is the 2^-24 quantum.
 __device__ __forceinline__ void cic_axis(float v, const CicGeom& g, uint32_t& cell, float& t) {
-  const float u = fmul(box_fold(v, g.box), g.idx);
-  const uint32_t raw = (uint32_t)u;
-  cell = raw >= g.n ? 0u : raw;
-  t = fsub(u, (float)raw);
+  const float x = box_fold(v, g.box);
+  const float hi = fmul(x, g.idx_hi);
+  const float lo = fadd(__fmaf_rn(x, g.idx_hi, -hi), fmul(x, g.idx_lo));
+  float r = floorf(hi);
+  float f = fadd(fsub(hi, r), lo);
+  if (f < 0.0f) {
+    r -= 1.0f;
+    f = fadd(f, 1.0f);
+  } else if (f >= 1.0f) {
+    r += 1.0f;
+    f = fsub(f, 1.0f);
+  }
+  int32_t c = (int32_t)r;
+  if (c < 0) c += (int32_t)g.n;
+  if (c >= (int32_t)g.n) c -= (int32_t)g.n;
+  cell = (uint32_t)c;
+  t = f;
 }
 
 __device__ __forceinline__ uint32_t tile_of(float x, float y, float z, const CicGeom& g) {
@@ -289,7 +307,9 @@ static CicGeom make_geom(uint32_t n, float box) {
   g.n = n;
   g.nt = (n + TB - 1) / TB;
   g.box = box;
-  g.idx = (float)n / box;
+  const double idx = (double)n / (double)box;
+  g.idx_hi = (float)idx;
+  g.idx_lo = (float)(idx - (double)g.idx_hi);
   return g;
 }
 

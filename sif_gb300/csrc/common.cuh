@@ -7,9 +7,14 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
 #include <string>
 
 namespace sifg {
+
+// Kernels this library has launched (every launch site checks itself with
+// SIFG_LAUNCH_CHECK, which counts it); read by sifg_launch_count().
+extern std::atomic<uint64_t> g_kernel_launches;
 
 // sif's status codes (include/sif/core/macros.h:690-707).
 constexpr int kOk = 0;
@@ -33,7 +38,11 @@ struct CudaError {
     if (e_ != cudaSuccess) throw ::sifg::CudaError{e_, #call};               \
   } while (0)
 
-#define SIFG_LAUNCH_CHECK() SIFG_CUDA(cudaGetLastError())
+#define SIFG_LAUNCH_CHECK()                                                  \
+  do {                                                                       \
+    ::sifg::g_kernel_launches.fetch_add(1, std::memory_order_relaxed);       \
+    SIFG_CUDA(cudaGetLastError());                                           \
+  } while (0)
 
 inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap = 152u * 32u) {
   uint64_t g = (n + block - 1) / block;

@@ -37,7 +37,9 @@ struct RungStat {
 struct RunTimings {
   KernelTimer growth, filter, cic, mesh;
   double wall_ms = 0.0;
+  uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the sphere growth
   void reset() {
+    growth_particles = growth_cells = 0;
     growth.reset();
     filter.reset();
     cic.reset();
@@ -74,7 +76,7 @@ class Engine {
   DevBuf surv_cand_, surv_flat_, scx_, scy_, scz_, sr_, sreason_, state_a_, state_b_, acc_;
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
-  DevBuf tdx_, tdy_, tdz_, ttype_, tmin_, tmax_, gbuf_;
+  DevBuf tdx_, tdy_, tdz_, ttype_, tmin_, tmax_, gbuf_, traffic_;
   float* h_delta_ = nullptr;
   uint32_t* h_flat_ = nullptr;
   uint32_t* h_rank_ = nullptr;

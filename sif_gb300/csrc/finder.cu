@@ -388,9 +388,14 @@ __device__ void bitonic_sort(float* buf, uint32_t p) {
   }
 }
 
+// traffic[0] counts the particles whose positions a pass read (12 bytes
+// each), traffic[1] the template cells a pass visited (a range lookup, 8
+// bytes, plus the template entry, 8 bytes): the gathered bytes of the
+// sphere growth.
 __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateView tpl,
                                                         RungConsts rc, Survivors sv,
-                                                        float* __restrict__ gbuf, uint32_t gcap) {
+                                                        float* __restrict__ gbuf, uint32_t gcap,
+                                                        unsigned long long* __restrict__ traffic) {
   __shared__ uint32_t bins[kMaxBins];
   __shared__ unsigned long long below[kMaxBins];  // particles inside bin b's lower edge
   __shared__ float sbuf[kSmemBuf];
@@ -411,13 +416,15 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
 
     // 1. The early refusal (exodus_rescale.c:738-782): whole core and shell
     //    cells by their counts, the rest particle by particle.
-    unsigned long long within = 0;
+    unsigned long long within = 0, read = 0, visited = 0;
     for (uint32_t i = warp; i < tpl.count; i += kGrowWarps) {
       const CellRange c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
       const uint8_t type = __ldg(tpl.type + i);
+      if (lane == 0) visited++;
       if (type == kCellCore || type == kCellShell) {
         if (lane == 0) within += c.e - c.s;
       } else {
+        if (lane == 0) read += c.e - c.s;
         for (uint32_t p = c.s + lane; p < c.e; p += 32)
           within += dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez) <= rc.rs2;
       }
@@ -437,6 +444,10 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
       for (uint32_t i = warp; i < tpl.count; i += kGrowWarps) {
         const CellRange c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
         const uint8_t type = __ldg(tpl.type + i);
+        if (lane == 0) {
+          visited++;
+          if (type != kCellCore) read += c.e - c.s;
+        }
         if (type == kCellCore) {
           if (lane == 0) n_core += c.e - c.s;
         } else if (type == kCellShell) {
@@ -522,6 +533,10 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
             const uint8_t type = __ldg(tpl.type + i);
             if (type == kCellCore || __ldg(tpl.max_d2 + i) < lo || __ldg(tpl.min_d2 + i) > hi) continue;
             const CellRange c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
+            if (lane == 0) {
+              visited++;
+              read += c.e - c.s;
+            }
             for (uint32_t p = c.s + lane; p < c.e; p += 32) {
               const float d2 = dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez);
               if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) continue;
@@ -558,6 +573,14 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
         }
       }
     }
+    if (traffic) {
+      read = block_sum_u64(read, red64);
+      visited = block_sum_u64(visited, red64);
+      if (threadIdx.x == 0) {
+        atomicAdd(traffic, read);
+        atomicAdd(traffic + 1, visited);
+      }
+    }
     if (threadIdx.x == 0) {
       sv.r[s] = reason == kRescaleOk ? radius : -1.0f;
       sv.reason[s] = reason;
@@ -567,11 +590,12 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
 }
 
 void grow(MeshView mesh, TemplateView tpl, RungConsts rc, Survivors s, uint32_t max_survivors,
-          float* gbuf, uint32_t gcap, cudaStream_t st, KernelTimer* timer) {
+          float* gbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
+          KernelTimer* timer) {
   if (max_survivors == 0) return;
   const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
   if (timer) timer->begin(st);
-  growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap);
+  growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(st);
 }

@@ -123,8 +123,11 @@ void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, Void
 // Sphere growth of every survivor. gbuf: a global overflow scratch of
 // grid * gcap floats.
 unsigned growth_grid();
+// traffic (may be NULL): two counters the kernel adds to -- particles read
+// and template cells visited.
 void grow(MeshView mesh, TemplateView tpl, RungConsts rc, Survivors s, uint32_t max_survivors,
-          float* gbuf, uint32_t gcap, cudaStream_t st, KernelTimer* timer);
+          float* gbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
+          KernelTimer* timer);
 
 // The survivor hash for the commit.
 void build_survivor_grid(const float* scx, const float* scy, const float* scz,

@@ -8,6 +8,8 @@
 
 namespace sifg {
 
+std::atomic<uint64_t> g_kernel_launches{0};
+
 constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr uint32_t kScanChunk = kScanThreads * kScanItems;

@@ -112,5 +112,16 @@ def last_timings():
     return {f: getattr(t, f) for f, _ in _lib.Timings._fields_}
 
 
+def stream():
+    """The library's CUDA stream as a torch stream, for events on it."""
+    import torch
+
+    return torch.cuda.ExternalStream(_lib.load().sifg_stream())
+
+
+def launch_count():
+    return int(_lib.load().sifg_launch_count())
+
+
 def set_window(bins):
     _lib.load().sifg_set_window(int(bins))

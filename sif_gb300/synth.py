@@ -106,7 +106,8 @@ def zeldovich(n, box, rms_disp, seed, backend="numpy", device="cuda"):
     amp[0, 0, 0] = 0.0
     delta_k = white * amp
     del white, amp
-    psi = [np.fft.irfftn(1j * (kc / k2) * delta_k, s=(n, n, n)) for kc in (kx, ky, kzz)]
+    psi = [np.fft.irfftn(1j * (kc / k2) * delta_k, s=(n, n, n), axes=(0, 1, 2))
+           for kc in (kx, ky, kzz)]
     rms = math.sqrt(sum(float((c * c).mean()) for c in psi))
     scale = rms_disp / rms
     q = (np.arange(n, dtype=np.float64) + 0.5) * (box / n)

@@ -1,0 +1,53 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+    config.addinivalue_line("markers", "slow: a full-size workload")
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    import oracle_ctypes as O
+
+    O.build()
+    return O
+
+
+@pytest.fixture(scope="session")
+def golden_box32():
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32.npz")))
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    """The built GB300 library, initialised on the GPU."""
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from sif_gb300 import build, pysif
+
+    build.build()
+    pysif.system_init(log_level="error")
+    return pysif
+
+
+def same_bits(a, b):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def same_catalogue(c1, c2):
+    return all(same_bits(a, b) for a, b in zip(c1, c2))

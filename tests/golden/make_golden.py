@@ -1,0 +1,75 @@
+"""Generates the golden vectors under tests/golden/ from the reference itself.
+
+Run in a checkout where the reference sif is compiled (``make -C oracle ref``,
+which needs the reference sources); the GPU machines only read the .npz
+files this writes.
+
+golden_box32.npz -- a 32^3 Zel'dovich box (side 128, rms displacement 4,
+  seed 11), ladder(8, 24, 0.1), threshold -0.7, a mesh of 8^3 cells:
+  the positions; the reference's CIC density and density contrast
+  (sif_grid_assign_cic, sif_grid_to_density_contrast); its chain mesh
+  (positions, offsets, source indices); the 12 per-rung smoothed fields its
+  own run produced (captured from sif__fft_grid_backward); and its catalogue
+  for several option sets, each run on exactly those fields.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from sif_gb300 import abi, synth  # noqa: E402
+
+import ref_ctypes as R  # noqa: E402
+
+# Option sets the catalogue is recorded for: (name, overlap_fraction, options).
+OPTION_SETS = [
+    ("default", 0.0, 0),
+    ("search_2_00", 0.0, abi.SIF_FINDER_SEARCH_2_00),
+    ("search_1_25", 0.0, abi.SIF_FINDER_SEARCH_1_25),
+    ("lagrangian", 0.0, abi.SIF_FINDER_LAGRANGIAN_OVERLAP),
+    ("overlap_0_5", 0.5, 0),
+]
+
+BOX32 = dict(n=32, box=128.0, rms_disp=4.0, seed=11, r0=8.0, threshold=-0.7, mesh=8)
+
+
+def make_box32(path):
+    p = BOX32
+    x, y, z = synth.zeldovich(p["n"], p["box"], p["rms_disp"], p["seed"])
+    radii = synth.ladder(p["r0"], 3 * p["r0"], 0.1).astype(np.float32)
+    lib = R.load("strict", 4, abi.SIF_LOG_LEVEL_ERROR)
+    f = R.RefField(lib, x, y, z)
+    g = R.RefGrid(lib, p["n"], p["box"])
+    g.assign_cic(f)
+    density = g.values()
+    g.to_contrast()
+    delta = g.values()
+    m = R.RefMesh(lib, p["mesh"], p["box"], f)
+    mx, my, mz, offs, idx = m.arrays()
+    fields = np.zeros((len(radii), p["n"] ** 3), np.float32)
+    cat = R.exodus_raw(lib, g, m, radii, p["threshold"], capture=fields)
+    out = dict(x=x, y=y, z=z, radii=radii, density=density, delta=delta, mesh_x=mx, mesh_y=my,
+               mesh_z=mz, mesh_offsets=offs, mesh_index=idx, fields=fields,
+               params=np.array([p["n"], p["box"], p["rms_disp"], p["seed"], p["r0"],
+                                p["threshold"], p["mesh"]], np.float64))
+    for name, overlap, opt in OPTION_SETS:
+        c = R.exodus_raw(lib, g, m, radii, p["threshold"], overlap, opt, inject=fields)
+        for k, col in zip(("cx", "cy", "cz", "r"), c):
+            out[f"cat_{name}_{k}"] = col
+        out[f"cat_{name}_opt"] = np.array([overlap, opt], np.float64)
+    # The default run on its own fields is the run that captured them.
+    assert all(np.array_equal(a, out[f"cat_default_{k}"]) for a, k in zip(cat, "cx cy cz r".split()))
+    m.free()
+    g.free()
+    f.free()
+    np.savez_compressed(path, **out)
+    print(f"{path}: {len(cat[0])} voids over {len(radii)} rungs")
+
+
+if __name__ == "__main__":
+    make_box32(os.path.join(HERE, "golden_box32.npz"))

@@ -1,0 +1,101 @@
+"""The C ABI: the library builds, loads, and exports every entry point
+include/sif_gb300.h declares; the host-side logic that needs no GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sif_gb300 import _lib, build
+
+    build.build()
+    return _lib.load()
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "sif_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b((?:sif|sifg)_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_reference_entry_points():
+    names = _declared()
+    for n in ["sif_grid_assign_cic", "sif_grid_to_density_contrast", "sif_chain_mesh_alloc",
+              "sif_chain_mesh_alloc_consume", "sif_finder_exodus", "sif_finder_exodus_raw",
+              "sif_system_init", "sif_error_message"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from sif_gb300 import _lib
+
+    for name in _declared():
+        assert hasattr(lib, name), name
+    assert set(_declared()) == set(_lib.EXPORTED)
+
+
+def test_struct_sizes_match_the_reference_layout():
+    from sif_gb300 import abi
+
+    # LP64 sizes of the reference's structs (float build), as its own headers
+    # compile them.
+    assert C.sizeof(abi.sif_grid_t) == 48
+    assert C.sizeof(abi.sif_chain_mesh_t) == 136
+    assert C.sizeof(abi.sif_catalogue_t) == 104
+    assert C.sizeof(abi.sif_field_t) == 144
+    assert C.sizeof(abi.sif_finder_exodus_extras_t) == 24
+    assert C.sizeof(abi.sif_config_t) == 40
+    assert abi.sif_chain_mesh_t.cell_offsets.offset == 128
+    assert abi.sif_catalogue_t.n_voids.offset == 88
+
+
+def test_host_rank_replay_matches_oracle_sort(lib, oracle):
+    rng = np.random.default_rng(9)
+    for m in [0, 1, 7, 4096, 70000, 200000]:
+        d = (rng.integers(0, 64, m) * np.float32(-0.002) - np.float32(0.8)).astype(np.float32)
+        rank = np.empty(m, np.uint32)
+        if m:
+            lib.sifg_candidate_ranks(d.ctypes.data, m, rank.ctypes.data)
+        rec = np.zeros(m, oracle.CANDIDATE_DTYPE)
+        rec["delta"] = d
+        rec["flat"] = np.arange(m)
+        s = oracle.sort_candidates(rec)
+        want = np.empty(m, np.int64)
+        want[s["flat"].astype(np.int64)] = np.arange(m)
+        assert np.array_equal(rank.astype(np.int64), want)
+
+
+def test_variants_and_argument_errors_without_a_gpu(lib):
+    from sif_gb300 import abi
+
+    ov = C.c_float(-1)
+    opt = C.c_uint32(0)
+    assert lib.sif_finder_exodus_preset(1, C.byref(ov), C.byref(opt)) == 0
+    assert ov.value == 1.0 and opt.value == (abi.SIF_FINDER_SEEDS_MINIMA |
+                                             abi.SIF_FINDER_EXTEND_REACH | abi.SIF_FINDER_DISPLACE)
+    assert lib.sif_finder_exodus_preset(7, None, None) == abi.SIF_ERR_INVALID
+    assert lib.sif_finder_exodus_variant_name(2) == b"lagrangian-overlap"
+    v = C.c_int(-1)
+    assert lib.sif_finder_exodus_variant_from_name(b"excursion-peak", C.byref(v)) == 0 and v.value == 1
+    assert lib.sif_finder_grid_cells_from_size(0, 256.0, 1.0, 0, 0.0) == 256
+    g = lib.sif_grid_alloc(0, 100.0)
+    assert not g and lib.sif_error_status() == abi.SIF_ERR_INVALID
+
+
+def test_init_without_a_gpu_fails_loudly(lib):
+    """No silent CPU path: without a CUDA device the library refuses."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from sif_gb300 import abi
+
+    cfg = abi.sif_config_t(None, None, abi.SIF_LOG_LEVEL_NONE, None, 0)
+    assert lib.sif_system_init(C.byref(cfg)) == abi.SIF_ERR_UNSUPPORTED
+    assert b"GPU" in lib.sif_error_message()

@@ -1,0 +1,268 @@
+"""Parity of the GPU path with the oracle and the reference's golden vectors.
+
+Every stage is called through the C ABI (libsif_gb300.so), on device data
+for the stage tests and through sif's own API for the end-to-end ones.
+Bars: the chain mesh and the catalogue bit for bit (integer and index work,
+and the finder's float tests replayed op for op); the CIC grid and the
+smoothed field against FP64 within 1e-6 relative L2 (the tolerance the
+workloads state), 1e-5 max-norm over the field rms.
+"""
+import numpy as np
+import pytest
+
+from conftest import same_bits, same_catalogue
+from sif_gb300 import abi, synth
+
+pytestmark = pytest.mark.gpu
+
+FIELD_L2_TOL = 1e-6
+FIELD_MAX_TOL = 1e-5
+
+
+def _cuda(*arrays):
+    import torch
+
+    return [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrays]
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    rms = np.sqrt((b * b).mean())
+    return np.sqrt(((a - b) ** 2).mean()) / rms, np.abs(a - b).max() / rms
+
+
+@pytest.fixture(scope="module")
+def dev(gpu_lib):
+    from sif_gb300 import device
+
+    return device
+
+
+def test_cic_against_fp64(dev, oracle):
+    x, y, z = synth.zeldovich(64, 250.0, 4.0, 5)
+    g = dev.cic(*_cuda(x, y, z), 64, 250.0).cpu().numpy()
+    want = oracle.cic_f64(x, y, z, 64, 250.0)
+    l2, mx = _rel(g, want)
+    assert l2 <= FIELD_L2_TOL and mx <= FIELD_MAX_TOL, (l2, mx)
+    cl = 250.0 / 64
+    assert abs(g.astype(np.float64).sum() * cl ** 3 - len(x)) <= 1e-5 * len(x)
+
+
+def test_cic_is_independent_of_particle_order(dev):
+    x, y, z = synth.zeldovich(48, 200.0, 4.0, 6)
+    perm = np.random.default_rng(1).permutation(len(x))
+    a = dev.cic(*_cuda(x, y, z), 48, 200.0).cpu().numpy()
+    b = dev.cic(*_cuda(x[perm], y[perm], z[perm]), 48, 200.0).cpu().numpy()
+    assert same_bits(a, b)
+
+
+@pytest.mark.parametrize("n_grid", [37, 64, 100])
+def test_cic_non_tile_multiple_grids(dev, oracle, n_grid):
+    x, y, z = synth.zeldovich(40, 180.0, 4.0, n_grid)
+    g = dev.cic(*_cuda(x, y, z), n_grid, 180.0).cpu().numpy()
+    l2, mx = _rel(g, oracle.cic_f64(x, y, z, n_grid, 180.0))
+    assert l2 <= FIELD_L2_TOL and mx <= FIELD_MAX_TOL, (l2, mx)
+
+
+def test_cic_edge_coordinates(dev, oracle):
+    """Coordinates on and within rounding of the faces fold as the
+    reference's do (src/structures/field_internal.h:58-64)."""
+    box = np.float32(100.0)
+    v = np.array([0.0, np.nextafter(box, 0), 99.99999, 50.0, 0.0, 1e-30], np.float32)
+    x, y, z = v, v[::-1].copy(), np.roll(v, 2)
+    g = dev.cic(*_cuda(x, y, z), 16, 100.0).cpu().numpy()
+    l2, mx = _rel(g, oracle.cic_f64(x, y, z, 16, 100.0))
+    assert mx <= 1e-5
+
+
+def test_contrast_matches_oracle(dev, oracle, golden_box32):
+    import torch
+
+    d = torch.from_numpy(golden_box32["density"].copy()).cuda()
+    dev.density_contrast(d)
+    assert same_bits(d.cpu().numpy(), golden_box32["delta"])
+
+
+def test_mesh_matches_reference_golden(dev, golden_box32):
+    g = golden_box32
+    mx, my, mz, offs, orig = dev.chain_mesh(*_cuda(g["x"], g["y"], g["z"]), int(g["params"][6]),
+                                            float(g["params"][1]))
+    assert same_bits(mx.cpu().numpy(), g["mesh_x"])
+    assert same_bits(my.cpu().numpy(), g["mesh_y"])
+    assert same_bits(mz.cpu().numpy(), g["mesh_z"])
+    assert np.array_equal(offs.cpu().numpy().astype(np.uint64), g["mesh_offsets"])
+    assert np.array_equal(orig.cpu().numpy().astype(np.uint64), g["mesh_index"])
+
+
+@pytest.mark.parametrize("n_cells", [7, 25, 64])
+def test_mesh_matches_oracle(dev, oracle, n_cells):
+    x, y, z = synth.zeldovich(50, 300.0, 6.0, n_cells)
+    # Clustered duplicates exercise the large-cell path of the canonical sort.
+    x[:3000] = x[0]
+    y[:3000] = y[0]
+    z[:3000] = z[0]
+    mx, my, mz, offs, orig = dev.chain_mesh(*_cuda(x, y, z), n_cells, 300.0)
+    m = oracle.OracleMesh(x, y, z, n_cells, 300.0)
+    assert same_bits(mx.cpu().numpy(), m.x) and same_bits(mz.cpu().numpy(), m.z)
+    assert np.array_equal(offs.cpu().numpy().astype(np.uint64), m.offsets)
+    assert np.array_equal(orig.cpu().numpy().astype(np.uint64), m.orig)
+
+
+@pytest.mark.parametrize("window", ["full", "aliasing", "none"])
+def test_smoothing_against_fp64(dev, oracle, golden_box32, window):
+    g = golden_box32
+    n, box = int(g["params"][0]), float(g["params"][1])
+    (delta,) = _cuda(g["delta"])
+    radii = np.sort(g["radii"])[::-1]
+    mode = {"none": 0, "full": 1, "aliasing": 2}[window]
+    want = oracle.smooth(g["delta"], n, box, radii, window_mode=mode, mode=0, want="f64")
+    for i, r in enumerate(radii):
+        got = dev.smooth(delta, n, box, float(r), window=window).cpu().numpy()
+        l2, mx = _rel(got, want[i])
+        assert l2 <= FIELD_L2_TOL and mx <= FIELD_MAX_TOL, (r, l2, mx)
+
+
+def test_gaussian_smoothing_against_fp64(dev, oracle, golden_box32):
+    g = golden_box32
+    n, box = int(g["params"][0]), float(g["params"][1])
+    (delta,) = _cuda(g["delta"])
+    want = oracle.smooth(g["delta"], n, box, [6.0], filter=2, mode=0, want="f64")[0]
+    got = dev.smooth(delta, n, box, 6.0, filter="gaussian").cpu().numpy()
+    l2, mx = _rel(got, want)
+    assert l2 <= FIELD_L2_TOL and mx <= FIELD_MAX_TOL
+
+
+def _golden_mesh(g):
+    return _cuda(g["mesh_x"], g["mesh_y"], g["mesh_z"], g["mesh_offsets"].astype(np.int32))
+
+
+@pytest.mark.parametrize("name", ["default", "search_2_00", "search_1_25", "lagrangian",
+                                  "overlap_0_5"])
+def test_catalogue_matches_reference_golden(dev, golden_box32, name):
+    """The reference's own catalogue, on the fields its own run smoothed."""
+    g = golden_box32
+    n, box, thr, n_mesh = int(g["params"][0]), float(g["params"][1]), float(g["params"][5]), int(g["params"][6])
+    overlap, opt = g[f"cat_{name}_opt"]
+    delta, fields = _cuda(g["delta"], g["fields"].reshape(-1))
+    cat = dev.exodus(delta, n, box, _golden_mesh(g), n_mesh, g["radii"], thr, float(overlap),
+                     int(opt), inject=fields)
+    want = tuple(g[f"cat_{name}_{k}"] for k in ("cx", "cy", "cz", "r"))
+    assert len(cat[0]) == len(want[0])
+    assert same_catalogue(cat, want)
+
+
+@pytest.mark.parametrize("window", [1, 5, 64])
+def test_catalogue_independent_of_resolve_window(dev, golden_box32, window):
+    g = golden_box32
+    n, box, thr = int(g["params"][0]), float(g["params"][1]), float(g["params"][5])
+    delta, fields = _cuda(g["delta"], g["fields"].reshape(-1))
+    dev.set_window(window)
+    try:
+        cat = dev.exodus(delta, n, box, _golden_mesh(g), int(g["params"][6]), g["radii"], thr,
+                         inject=fields)
+    finally:
+        dev.set_window(8)
+    want = tuple(g[f"cat_default_{k}"] for k in ("cx", "cy", "cz", "r"))
+    assert same_catalogue(cat, want)
+
+
+BOXES = [
+    # n, box, rms, seed, grid, mesh, r0, threshold, options, overlap
+    (64, 250.0, 4.0, 31, 64, 25, 5.0, -0.8, 0, 0.0),
+    (60, 240.0, 5.0, 32, 60, 20, 6.0, -0.75, abi.SIF_FINDER_SEARCH_2_00, 0.0),
+    (72, 300.0, 5.0, 33, 96, 24, 6.5, -0.7, abi.SIF_FINDER_LAGRANGIAN_OVERLAP, 0.0),
+    (64, 200.0, 3.0, 34, 64, 16, 4.0, -0.8, abi.SIF_FINDER_SEARCH_1_75, 0.25),
+]
+
+
+@pytest.mark.parametrize("case", BOXES, ids=[f"box{i}" for i in range(len(BOXES))])
+def test_catalogue_matches_oracle_on_shared_fields(dev, oracle, case):
+    """The GPU's own smoothed fields, handed to the oracle: every candidate,
+    radius and commit decision must then agree bit for bit."""
+    import torch
+
+    n, box, rms, seed, ng, nm, r0, thr, opt, ov = case
+    x, y, z = synth.zeldovich(n, box, rms, seed)
+    xs = _cuda(x, y, z)
+    grid = dev.cic(*xs, ng, box)
+    dev.density_contrast(grid)
+    mesh = dev.chain_mesh(*xs, nm, box)
+    radii = synth.ladder(r0, 4 * r0, 0.1).astype(np.float32)
+    fields = torch.stack([dev.smooth(grid, ng, box, float(r)) for r in np.sort(radii)[::-1]])
+    got = dev.exodus(grid, ng, box, mesh, nm, radii, thr, ov, opt, inject=fields.reshape(-1))
+    m = oracle.OracleMesh(x, y, z, nm, box)
+    want = oracle.exodus(grid.cpu().numpy(), m, radii, ng, box, thr, ov, opt, n_threads=4,
+                         inject=fields.cpu().numpy())
+    assert len(want[0]) > 10
+    assert len(got[0]) == len(want[0]) and same_catalogue(got, want)
+    # The GPU's own run (smoothing inside the finder) is the same run.
+    own = dev.exodus(grid, ng, box, mesh, nm, radii, thr, ov, opt)
+    assert same_catalogue(own, want)
+
+
+def test_four_holes_and_brute_force_radii(gpu_lib, oracle):
+    """tests/test_finders.c:117-164, 433-538 on the GPU path, through sif's
+    C API: the four evacuated holes, and each radius equal to the O(N)
+    brute-force radius in double to 1e-5."""
+    from test_oracle import _check_holes, _holes_field
+
+    pysif = gpu_lib
+    x, y, z, holes = _holes_field()
+    f = pysif.Field(x, y, z)
+    g = pysif.Grid(32, 200.0)
+    g.assign_cic(f)
+    g.to_density_contrast()
+    m = pysif.ChainMesh(8, 200.0, f, drop_indices=True)
+    radii = np.array([30, 25, 20, 16, 13, 10], np.float32)
+    before = g.values.copy()
+    cat = pysif.finders.exodus(g, m, radii, -0.7)
+    _check_holes(cat.as_tuple(), holes, 200.0 / 32)
+    assert same_bits(g.values, before)  # restored exactly
+    for rung, factor in [(16.0, 1.5), (20.0, 2.0), (13.0, 1.25)]:
+        c = pysif.finders.exodus_raw(g, m, [rung], -0.7, search_factor=factor)
+        assert len(c) > 0
+        r_search = rung + max((factor - 1.0) * rung, 3.0 * 200.0 / 32)
+        for i in range(len(c)):
+            want = oracle.brute_force_radius(x, y, z, 200.0, (c.cx[i], c.cy[i], c.cz[i]), rung,
+                                             r_search, -0.7)
+            assert want > 0 and abs(c.radii[i] - want) <= 1e-5 * want
+
+
+def test_c_api_end_to_end_and_errors(gpu_lib, oracle):
+    pysif = gpu_lib
+    x, y, z = synth.zeldovich(48, 220.0, 5.0, 41)
+    f = pysif.Field(x, y, z)
+    g = pysif.Grid(48, 220.0)
+    g.assign_cic(f)
+    l2, mx = _rel(g.values.reshape(-1), oracle.cic_f64(x, y, z, 48, 220.0))
+    assert l2 <= FIELD_L2_TOL
+    g.to_density_contrast()
+    with pytest.raises(ValueError):
+        g.to_density_contrast()  # already a contrast
+    m = pysif.ChainMesh(11, 220.0, f)
+    om = oracle.OracleMesh(x, y, z, 11, 220.0)
+    mx_, my_, mz_, offs, idx = m.arrays()
+    assert same_bits(mx_, om.x) and np.array_equal(offs, om.offsets) and np.array_equal(idx, om.orig)
+    radii = synth.ladder(7.0, 21.0, 0.1)
+    cat = pysif.finders.exodus(g, m, radii, -0.75)
+    assert len(cat) > 0
+    with pytest.raises(ValueError):
+        pysif.finders.exodus(g, m, radii, 0.5)  # threshold out of (-1, 0)
+    with pytest.raises(ValueError):
+        pysif.finders.exodus(g, m, [-1.0], -0.7)
+    with pytest.raises(NotImplementedError):
+        pysif.finders.exodus(g, m, radii, -0.7, variant="excursion-peak")
+    wrong = pysif.Grid(48, 221.0)
+    with pytest.raises(ValueError):
+        pysif.finders.exodus(wrong, m, radii, -0.7)
+    bad = pysif.Field(np.array([1.0, 300.0], np.float32), np.zeros(2, np.float32),
+                      np.zeros(2, np.float32))
+    with pytest.raises(ValueError):
+        pysif.Grid(8, 220.0).assign_cic(bad)  # a particle outside the box
+    # CONSUME_GRID leaves the last rung's smoothing in the grid.
+    g2 = pysif.Grid(48, 220.0)
+    g2.assign_cic(f)
+    g2.to_density_contrast()
+    pysif.finders.exodus_raw(g2, m, radii, -0.75, consume_grid=True)
+    assert not same_bits(g2.values, g.values)

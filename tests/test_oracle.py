@@ -1,0 +1,176 @@
+"""The oracle (this project's C restatement of sif's exodus path), pinned
+against the reference: against the committed golden vectors everywhere, and
+against the reference library itself where it is compiled (oracle/_ref)."""
+import numpy as np
+import pytest
+
+from conftest import same_bits, same_catalogue
+from sif_gb300 import abi, synth
+
+
+def test_ladder_matches_sif_exodus_helper():
+    r = synth.ladder(5.0, 30.0, 0.10)
+    assert len(r) == 19
+    assert r[0] == 5.0 and abs(r[-1] - 5.0 * 1.1 ** 18) < 1e-12
+    assert len(synth.workload_radii("B")) == 19
+
+
+def test_oracle_mesh_matches_golden(oracle, golden_box32):
+    g = golden_box32
+    n_mesh = int(g["params"][6])
+    m = oracle.OracleMesh(g["x"], g["y"], g["z"], n_mesh, float(g["params"][1]))
+    assert same_bits(m.x, g["mesh_x"]) and same_bits(m.y, g["mesh_y"]) and same_bits(m.z, g["mesh_z"])
+    assert np.array_equal(m.offsets, g["mesh_offsets"])
+    assert np.array_equal(m.orig, g["mesh_index"])
+
+
+def test_oracle_contrast_matches_golden(oracle, golden_box32):
+    d = oracle.density_contrast(golden_box32["density"])
+    assert same_bits(d, golden_box32["delta"])
+
+
+def test_oracle_cic_f64_close_to_reference_float_cic(oracle, golden_box32):
+    g = golden_box32
+    n, box = int(g["params"][0]), float(g["params"][1])
+    f64 = oracle.cic_f64(g["x"], g["y"], g["z"], n, box)
+    ref = g["density"].astype(np.float64)
+    # The reference accumulates in float: agreement to float rounding.
+    assert np.abs(f64 - ref).max() <= 1e-4 * np.abs(f64).max()
+    cl = box / n
+    assert abs(f64.sum() * cl ** 3 - len(g["x"])) < 1e-6 * len(g["x"])
+
+
+@pytest.mark.parametrize("name", ["default", "search_2_00", "search_1_25", "lagrangian",
+                                  "overlap_0_5"])
+def test_oracle_catalogue_matches_golden(oracle, golden_box32, name):
+    g = golden_box32
+    n, box, thr, n_mesh = int(g["params"][0]), float(g["params"][1]), float(g["params"][5]), int(g["params"][6])
+    overlap, opt = g[f"cat_{name}_opt"]
+    m = oracle.OracleMesh(g["x"], g["y"], g["z"], n_mesh, box)
+    cat = oracle.exodus(g["delta"], m, g["radii"], n, box, thr, float(overlap), int(opt),
+                        n_threads=2, inject=g["fields"])
+    want = tuple(g[f"cat_{name}_{k}"] for k in ("cx", "cy", "cz", "r"))
+    assert len(cat[0]) == len(want[0])
+    assert same_catalogue(cat, want)
+
+
+@pytest.mark.parametrize("window", [1, 3, 64])
+def test_oracle_catalogue_window_invariant(oracle, golden_box32, window):
+    """The resolve window changes how bins are grouped, never the answer
+    (src/finder/exodus_rescale.c:382-386)."""
+    g = golden_box32
+    n, box, thr = int(g["params"][0]), float(g["params"][1]), float(g["params"][5])
+    m = oracle.OracleMesh(g["x"], g["y"], g["z"], int(g["params"][6]), box)
+    cat = oracle.exodus(g["delta"], m, g["radii"], n, box, thr, window=window, inject=g["fields"])
+    want = tuple(g[f"cat_default_{k}"] for k in ("cx", "cy", "cz", "r"))
+    assert same_catalogue(cat, want)
+
+
+def test_oracle_sort_is_three_way_quicksort_with_ties(oracle):
+    rng = np.random.default_rng(3)
+    d = (rng.integers(0, 40, 5000) * -0.003 - 0.7).astype(np.float32)
+    rec = np.zeros(len(d), oracle.CANDIDATE_DTYPE)
+    rec["delta"] = d
+    rec["flat"] = np.arange(len(d))
+    s = oracle.sort_candidates(rec)
+    assert np.all(np.diff(s["delta"]) >= 0)
+    assert sorted(s["flat"].tolist()) == list(range(len(d)))
+    # Ties are not in input order: the permutation is the quicksort's own.
+    ties = [s["flat"][s["delta"] == v] for v in np.unique(d)]
+    assert any(np.any(np.diff(t.astype(np.int64)) < 0) for t in ties)
+
+
+def _holes_field():
+    """The reference test fixture of tests/test_finders.c:57-115: 60000
+    uniform particles in a box of 200 with four spheres evacuated to 3%, from
+    the MMIX linear congruential generator seeded 0x243F6A8885A308D3."""
+    holes = [(50.0, 50.0, 50.0, 26.0), (150.0, 140.0, 60.0, 21.0), (70.0, 160.0, 150.0, 18.0),
+             (160.0, 40.0, 170.0, 15.0)]
+    mask64 = (1 << 64) - 1
+    state = 0x243F6A8885A308D3
+
+    def uni():
+        nonlocal state
+        state = (state * 6364136223846793005 + 1442695040888963407) & mask64
+        return ((state >> 11) & 0x1FFFFFFFFFFFFF) / float(0x20000000000000)
+
+    out = []
+    while len(out) < 60000:
+        p = (uni() * 200.0, uni() * 200.0, uni() * 200.0)
+        inside = any((p[0] - h[0]) ** 2 + (p[1] - h[1]) ** 2 + (p[2] - h[2]) ** 2 < h[3] ** 2
+                     for h in holes)
+        if inside and uni() > 0.03:
+            continue
+        out.append(p)
+    a = np.array(out, np.float32)
+    return a[:, 0].copy(), a[:, 1].copy(), a[:, 2].copy(), holes
+
+
+@pytest.fixture(scope="session")
+def holes_field():
+    return _holes_field()
+
+
+def _check_holes(cat, holes, cell):
+    cx, cy, cz, r = cat
+    assert len(r) == 4
+    matched = set()
+    for i in range(4):
+        d = [np.sqrt((cx[i] - h[0]) ** 2 + (cy[i] - h[1]) ** 2 + (cz[i] - h[2]) ** 2) for h in holes]
+        j = int(np.argmin(d))
+        assert d[j] <= 2 * cell
+        assert j not in matched
+        matched.add(j)
+        assert 0.9 * holes[j][3] <= r[i] <= 1.5 * holes[j][3]
+
+
+def test_oracle_four_holes_and_brute_force_radius(oracle, holes_field):
+    """tests/test_finders.c:117-164 and 419-538: the four holes recovered,
+    and every radius equal to the brute-force radius to 1e-5."""
+    x, y, z, holes = holes_field
+    n, box = 32, 200.0
+    d = oracle.density_contrast(oracle.cic_f64(x, y, z, n, box).astype(np.float32))
+    radii = np.array([30, 25, 20, 16, 13, 10], np.float32)
+    m = oracle.OracleMesh(x, y, z, 8, box)
+    cat = oracle.exodus(d, m, radii, n, box, -0.7, n_threads=4)
+    _check_holes(cat, holes, box / n)
+    # One rung at a time, so each void's search range is known.
+    m2 = oracle.OracleMesh(x, y, z, 8, box)
+    for rung, opt, factor in [(16.0, 0, 1.5), (20.0, abi.SIF_FINDER_SEARCH_2_00, 2.0),
+                              (13.0, abi.SIF_FINDER_SEARCH_1_25, 1.25)]:
+        c = oracle.exodus(d, m2, np.array([rung], np.float32), n, box, -0.7, options=opt)
+        assert len(c[0]) > 0
+        r_search = rung + max((factor - 1.0) * rung, 3.0 * box / n)
+        for i in range(len(c[0])):
+            want = oracle.brute_force_radius(x, y, z, box, (c[0][i], c[1][i], c[2][i]), rung,
+                                             r_search, -0.7)
+            assert want > 0 and abs(c[3][i] - want) <= 1e-5 * want
+
+
+@pytest.mark.skipif("not __import__('ref_ctypes').available()")
+def test_oracle_matches_reference_library_on_zeldovich(oracle):
+    """Against the reference compiled from its own sources: its own CIC,
+    contrast and smoothing, captured and injected into the oracle."""
+    import ref_ctypes as R
+
+    x, y, z = synth.zeldovich(48, 200.0, 5.0, 21)
+    radii = synth.ladder(8.0, 24.0, 0.1).astype(np.float32)
+    lib = R.load("strict", 4, abi.SIF_LOG_LEVEL_ERROR)
+    f = R.RefField(lib, x, y, z)
+    g = R.RefGrid(lib, 48, 200.0)
+    g.assign_cic(f)
+    g.to_contrast()
+    delta = g.values()
+    rm = R.RefMesh(lib, 12, 200.0, f)
+    fields = np.zeros((len(radii), 48 ** 3), np.float32)
+    want = R.exodus_raw(lib, g, rm, radii, -0.75, capture=fields)
+    m = oracle.OracleMesh(x, y, z, 12, 200.0)
+    got = oracle.exodus(delta, m, radii, 48, 200.0, -0.75, n_threads=3, inject=fields)
+    assert len(want[0]) > 5 and same_catalogue(got, want)
+    # The oracle's own float smoothing reproduces the reference's to rounding.
+    own = oracle.smooth(delta, 48, 200.0, np.sort(radii)[::-1], mode=1)
+    rms = np.sqrt((fields ** 2).mean())
+    assert np.abs(own - fields).max() <= 1e-5 * rms
+    rm.free()
+    g.free()
+    f.free()
