@@ -32,7 +32,6 @@ namespace sifg {
 
 constexpr int TB = kCicTile;  // base cells per tile side
 constexpr int TS = TB + 1;    // tile extent including the upper neighbours
-constexpr double kQ = 16777216.0;  // 2^24 quanta per particle
 
 struct CicGeom {
   uint32_t n;       // grid cells per side
@@ -171,15 +170,17 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
         const float w10 = fmul(tx_, wy0), w11 = fmul(tx_, ty_);
         const float w[8] = {fmul(w00, wz0), fmul(w00, tz_), fmul(w01, wz0), fmul(w01, tz_),
                             fmul(w10, wz0), fmul(w10, tz_), fmul(w11, wz0), fmul(w11, tz_)};
-        long long sum = 0;
+        // w * 2^24 is exact in float, so rounding it to an integer in float
+        // is the quantisation itself; GB300's FP64 rate is no place for it.
+        int sum = 0;
         int big = 0;
         for (int k = 0; k < 8; k++) {
-          const long long qk = __double2ll_rn((double)w[k] * kQ);
+          const int qk = __float2int_rn(fmul(w[k], 16777216.0f));
           q[k] = (unsigned long long)qk;
           sum += qk;
           if (w[k] > w[big]) big = k;
         }
-        q[big] += (unsigned long long)((long long)kQ - sum);
+        q[big] += (unsigned long long)(long long)(16777216 - sum);
         cell = ((cx - ox) * TS + (cy - oy)) * TS + (cz - oz);
       }
       // Lanes bound for the same base cell add their eight corners together
@@ -213,7 +214,7 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
       const bool interior = a >= 1 && a < ex && b >= 1 && b < ey && c >= 1 && c < ez;
       if (interior) {
         grid[((uint64_t)gx * g.n + gy) * g.n + gz] =
-            fmul((float)((double)v * (1.0 / kQ)), inv_cell_vol);
+            fmul(fmul(__ull2float_rn(v), 1.0f / 16777216.0f), inv_cell_vol);
       } else if (v != 0ull) {
         atomicAdd(face_slot(faces, gx, gy, gz, g), v);
       }
@@ -251,7 +252,7 @@ __global__ void face_fixup_kernel(CicGeom g, float inv_cell_vol, float* __restri
       if (gz >= n || gx % TB == 0 || gy % TB == 0) continue;
       v = faces.fz[j];
     }
-    grid[(gx * n + gy) * n + gz] = fmul((float)((double)v * (1.0 / kQ)), inv_cell_vol);
+    grid[(gx * n + gy) * n + gz] = fmul(fmul(__ull2float_rn(v), 1.0f / 16777216.0f), inv_cell_vol);
   }
 }
 
