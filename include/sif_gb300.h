@@ -326,6 +326,21 @@ uint64_t sifg_launch_count(void);
 uint64_t sifg_stream(void);
 /* The resolve window (bins per pass) the sphere growth uses; default 8. */
 void sifg_set_window(int bins);
+/* The chain-mesh build of sifg_mesh_device, for callers that cannot let the
+ * library allocate device memory: a process whose framework reserves the
+ * GPU's memory in its own pool, a latency-bound pipeline that cannot afford
+ * cudaFree's device-wide wait, a host that enforces its own memory budget.
+ * It has no counterpart in the reference. Its scratch is a static device
+ * array of the library (about 17 MB, held on every GPU that loads the
+ * library until the process exits), which limits it to 1,048,576 particles
+ * and 262,144 mesh cells; larger inputs fail with SIF_ERR_RANGE. It calls no
+ * cudaMalloc, cudaFree or allocating library routine. The first call on a
+ * device looks up the array's device address; make that first call before
+ * any stream capture. Every call shares the one array, so calls that overlap
+ * on the GPU race; the library runs them on its one stream, in order. */
+int sifg_mesh_device_noalloc(const float* x, const float* y, const float* z, uint64_t n,
+                             uint32_t n_cells, float box, float* mx, float* my, float* mz,
+                             uint32_t* offsets, uint32_t* orig);
 /* The replay of the reference's candidate order on host data, for tests:
  * rank[k] = sorted position of delta[k]. */
 void sifg_candidate_ranks(const float* delta, uint32_t m, uint32_t* rank);

@@ -41,6 +41,7 @@ EXPORTED = [
     "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
     "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
     "sifg_set_window", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
+    "sifg_mesh_device_noalloc",
 ]
 
 
@@ -69,6 +70,7 @@ def load():
         "sifg_set_window": (None, [i32]),
         "sifg_stream": (u64, []),
         "sifg_launch_count": (u64, []),
+        "sifg_mesh_device_noalloc": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]),
         "sifg_candidate_ranks": (None, [vp, u32, vp]),
     }
     for name, (res, args) in sigs.items():

@@ -196,6 +196,19 @@ static void record_timings(RunTimings& t) {
   g_timings.growth_cells = t.growth_cells;
 }
 
+// The library's stream and device, under the API lock; false (with the error
+// set) before sif_system_init().
+bool api_stream(cudaStream_t* st, int* device) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_init || !g_engine) {
+    set_error(SIF_ERR_UNINITIALISED, "sif_system_init() has not been called");
+    return false;
+  }
+  *st = g_engine->stream();
+  *device = g_engine->device();
+  return true;
+}
+
 }  // namespace sifg
 
 using namespace sifg;

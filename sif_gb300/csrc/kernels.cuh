@@ -37,8 +37,12 @@ struct DevBuf {
 };
 
 // --- scan.cu ---
-// In-place exclusive prefix sum of n uint32 values (n < 2^31).
-void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st);
+// In-place exclusive prefix sum of n uint32 values (n < 2^31). The chunk
+// totals go to `sums_scratch` (scan_sums_needed(n) entries) when given, else
+// to a buffer the scan keeps.
+uint32_t scan_sums_needed(uint32_t n);
+void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st,
+                        uint32_t* sums_scratch = nullptr);
 
 // --- cic.cu ---
 size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n);
@@ -60,7 +64,10 @@ struct DeviceMesh {
 };
 size_t mesh_scratch_bytes(uint64_t n_particles, uint32_t n_cells);
 // Builds into caller buffers (x, y, z, offsets, orig sized for the mesh).
+// scratch: mesh_scratch_bytes(); scan_sums: NULL, or scan_sums_needed(cells
+// + 1) entries the scan uses instead of a buffer of its own.
 void mesh_build(const float* x, const float* y, const float* z, uint64_t n_particles,
-                DeviceMesh& m, void* scratch, cudaStream_t st, KernelTimer* timer);
+                DeviceMesh& m, void* scratch, cudaStream_t st, KernelTimer* timer,
+                uint32_t* scan_sums = nullptr);
 
 }  // namespace sifg

@@ -131,7 +131,8 @@ size_t mesh_scratch_bytes(uint64_t n_particles, uint32_t n_cells) {
 }
 
 void mesh_build(const float* x, const float* y, const float* z, uint64_t n_particles,
-                DeviceMesh& m, void* scratch, cudaStream_t st, KernelTimer* timer) {
+                DeviceMesh& m, void* scratch, cudaStream_t st, KernelTimer* timer,
+                uint32_t* scan_sums) {
   MeshGeom g;
   g.n = m.n_cells;
   g.box = m.box_length;
@@ -145,7 +146,7 @@ void mesh_build(const float* x, const float* y, const float* z, uint64_t n_parti
   if (timer) timer->begin(st);
   cell_count_kernel<<<grd, 256, 0, st>>>(x, y, z, n_particles, g, m.offsets);
   SIFG_LAUNCH_CHECK();
-  exclusive_scan_u32(m.offsets, (uint32_t)(cells + 1), st);
+  exclusive_scan_u32(m.offsets, (uint32_t)(cells + 1), st, scan_sums);
   SIFG_CUDA(cudaMemcpyAsync(cursor, m.offsets, cells * sizeof(uint32_t),
                             cudaMemcpyDeviceToDevice, st));
   cell_scatter_kernel<<<grd, 256, 0, st>>>(x, y, z, n_particles, g, cursor, tmp);
