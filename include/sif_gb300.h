@@ -263,6 +263,12 @@ typedef struct {
   uint64_t rounds;
   uint64_t n_rescale_fail;
   uint64_t n_overflow;
+  /* Host wall time of the rung's phases, milliseconds: the whole rung, the
+   * wait for the candidate count, the candidate sort, the commit rounds. */
+  double rung_ms;
+  double count_wait_ms;
+  double sort_ms;
+  double commit_ms;
 } sifg_rung_stat_t;
 
 /* Kernel timings of the last run, CUDA events on the launching stream. */

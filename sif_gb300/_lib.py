@@ -17,7 +17,9 @@ class RungStat(C.Structure):
     _fields_ = [("radius", C.c_float), ("r_search", C.c_float),
                 ("n_candidates", C.c_uint64), ("n_survivors", C.c_uint64),
                 ("n_accepted", C.c_uint64), ("rounds", C.c_uint64),
-                ("n_rescale_fail", C.c_uint64), ("n_overflow", C.c_uint64)]
+                ("n_rescale_fail", C.c_uint64), ("n_overflow", C.c_uint64),
+                ("rung_ms", C.c_double), ("count_wait_ms", C.c_double),
+                ("sort_ms", C.c_double), ("commit_ms", C.c_double)]
 
 
 class Timings(C.Structure):

@@ -91,35 +91,23 @@ static ApiBufs& bufs() {
 }
 
 // sif__field_check_in_box (src/structures/field.c:889-935): every coordinate
-// in [0, L), or within 4 float epsilons of L of a face (folded later).
+// in [0, L), or within 4 float epsilons of L of a face (folded later). The
+// reference compares in double against -tol and L + tol; a float v passes
+// those exactly when it passes the float bounds lo and hi found on the host
+// (the nearest floats inside them), so the kernel compares floats only.
 __global__ void box_check_kernel(const float* __restrict__ x, const float* __restrict__ y,
-                                 const float* __restrict__ z, uint64_t n, float box, double tol,
-                                 unsigned long long* __restrict__ out) {
-  unsigned long long bad = 0, edge = 0;
+                                 const float* __restrict__ z, uint64_t n, float box, float lo,
+                                 float hi, unsigned long long* __restrict__ out) {
+  unsigned long long bad = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const float v[3] = {x[i], y[i], z[i]};
-    bool inside = true, accepted = true;
-    for (int a = 0; a < 3; a++) {
-      inside = inside && v[a] >= 0.0f && v[a] < box;
-      const double d = (double)v[a];
-      accepted = accepted && d >= -tol && d <= (double)box + tol;
-    }
-    if (!inside) {
-      if (accepted)
-        edge++;
-      else
-        bad++;
-    }
+    bool ok = true;
+    for (int a = 0; a < 3; a++) ok = ok && v[a] >= lo && v[a] <= hi;  // false for NaN
+    bad += ok ? 0u : 1u;
   }
-  for (int d = 16; d > 0; d >>= 1) {
-    bad += __shfl_down_sync(0xffffffffu, bad, d);
-    edge += __shfl_down_sync(0xffffffffu, edge, d);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (bad) atomicAdd(out, bad);
-    if (edge) atomicAdd(out + 1, edge);
-  }
+  for (int d = 16; d > 0; d >>= 1) bad += __shfl_down_sync(0xffffffffu, bad, d);
+  if ((threadIdx.x & 31) == 0 && bad) atomicAdd(out, bad);
 }
 
 static int check_in_box(const float* dx, const float* dy, const float* dz, uint64_t n, float box,
@@ -127,7 +115,10 @@ static int check_in_box(const float* dx, const float* dy, const float* dz, uint6
   unsigned long long* d = (unsigned long long*)bufs().bad.ensure(16);
   SIFG_CUDA(cudaMemsetAsync(d, 0, 16, st));
   const double tol = (double)box * 4.0 * (double)FLT_EPSILON;
-  box_check_kernel<<<grid_for(n, 256), 256, 0, st>>>(dx, dy, dz, n, box, tol, d);
+  float lo = (float)(-tol), hi = (float)((double)box + tol);
+  if ((double)lo < -tol) lo = std::nextafter(lo, 0.0f);
+  if ((double)hi > (double)box + tol) hi = std::nextafter(hi, 0.0f);
+  box_check_kernel<<<grid_for(n, 256), 256, 0, st>>>(dx, dy, dz, n, box, lo, hi, d);
   SIFG_LAUNCH_CHECK();
   unsigned long long h[2];
   SIFG_CUDA(cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, st));
@@ -898,7 +889,8 @@ uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
   for (uint32_t i = 0; i < n && i < max_rungs; i++) {
     const RungStat& s = g_stats[i];
     out[i] = sifg_rung_stat_t{s.radius, s.r_search, s.n_candidates, s.n_survivors, s.n_accepted,
-                              s.rounds, s.n_rescale_fail, s.n_overflow};
+                              s.rounds, s.n_rescale_fail, s.n_overflow, s.rung_ms,
+                              s.count_wait_ms, s.sort_ms, s.commit_ms};
   }
   return n;
 }

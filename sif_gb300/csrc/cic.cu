@@ -16,9 +16,9 @@
 //   2. exclusive scan of the tile counts;
 //   3. tile_scatter: positions copied into tile order (one atomic per group
 //                    of lanes bound for the same tile);
-//   4. tile_deposit: one CTA per tile accumulates a 17^3 int64 tile in shared
-//                    memory, lanes bound for the same cell first reduced
-//                    across the warp; the 15^3 cells no other tile touches
+//   4. tile_deposit: one CTA per tile accumulates a 17^3 tile of 64-bit sums
+//                    (32-bit words plus carries) in shared memory with one
+//                    shared atomic per corner; the 15^3 cells no other tile touches
 //                    are written straight to the grid as float density, the
 //                    faces shared with neighbouring tiles go to int64 face
 //                    buffers with global atomics;
@@ -142,14 +142,19 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
     const float* __restrict__ sx, const float* __restrict__ sy, const float* __restrict__ sz,
     const uint32_t* __restrict__ offsets, CicGeom g, float inv_cell_vol,
     float* __restrict__ grid, FaceBufs faces) {
-  extern __shared__ unsigned long long acc[];  // TS^3
+  // The tile's sums as 32-bit words and their carries: a 32-bit shared atomic
+  // add is one instruction, a 64-bit one a compare-and-swap loop. A word that
+  // wraps past 2^32 counts the wrap in its carry (each add is below 2^32, so
+  // it wraps at most once), and the pair is the exact 64-bit sum whatever the
+  // order of the adds.
+  extern __shared__ uint32_t acc_lo[];  // TS^3 words, then TS^3 carries
+  uint32_t* acc_hi = acc_lo + TS * TS * TS;
   const uint32_t nt = g.nt;
   const uint32_t n_tiles = nt * nt * nt;
-  const unsigned lane = threadIdx.x & 31u;
   for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const uint32_t tx = tile / (nt * nt), ty = (tile / nt) % nt, tz = tile % nt;
     const uint32_t ox = tx * TB, oy = ty * TB, oz = tz * TB;
-    for (int i = threadIdx.x; i < TS * TS * TS; i += blockDim.x) acc[i] = 0ull;
+    for (int i = threadIdx.x; i < 2 * TS * TS * TS; i += blockDim.x) acc_lo[i] = 0u;
     __syncthreads();
 
     const uint32_t s = offsets[tile], e = offsets[tile + 1];
@@ -157,7 +162,7 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
       const uint32_t p = base + threadIdx.x;
       const bool valid = p < e;
       uint32_t cell = 0xffffffffu;
-      unsigned long long q[8];
+      uint32_t q[8];
       if (valid) {
         uint32_t cx, cy, cz;
         float tx_, ty_, tz_;
@@ -176,25 +181,26 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
         int big = 0;
         for (int k = 0; k < 8; k++) {
           const int qk = __float2int_rn(fmul(w[k], 16777216.0f));
-          q[k] = (unsigned long long)qk;
+          q[k] = (uint32_t)qk;
           sum += qk;
           if (w[k] > w[big]) big = k;
         }
-        q[big] += (unsigned long long)(long long)(16777216 - sum);
+        q[big] = (uint32_t)((int)q[big] + (16777216 - sum));
         cell = ((cx - ox) * TS + (cy - oy)) * TS + (cz - oz);
       }
-      // Lanes bound for the same base cell add their eight corners together
-      // first (a corner's quanta, at most 2^24 + 4, sum over a warp within 32
-      // bits); then one shared atomic per corner per group.
-      const unsigned peers = __match_any_sync(0xffffffffu, cell);
-      const bool leader = lane == (unsigned)(__ffs(peers) - 1);
+      // One shared atomic per corner. (Reducing lanes bound for the same cell
+      // first with __reduce_add_sync over each lane group's own mask costs a
+      // serialised pass per distinct group: eight per corner per cell in the
+      // warp, far more than the atomics it saves.)
+      if (valid) {
 #pragma unroll
-      for (int k = 0; k < 8; k++) {
-        const unsigned v = __reduce_add_sync(peers, valid ? (unsigned)q[k] : 0u);
-        if (valid && leader) {
+        for (int k = 0; k < 8; k++) {
+          const uint32_t v = q[k];
+          if (v == 0u) continue;
           const uint32_t c =
               cell + (uint32_t)(((k >> 2) & 1) * TS * TS + ((k >> 1) & 1) * TS + (k & 1));
-          atomicAdd(acc + c, (unsigned long long)v);
+          const uint32_t old = atomicAdd(acc_lo + c, v);
+          if (old + v < old) atomicAdd(acc_hi + c, 1u);
         }
       }
     }
@@ -207,7 +213,7 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
     for (int i = threadIdx.x; i < TS * TS * TS; i += blockDim.x) {
       const uint32_t a = i / (TS * TS), b = (i / TS) % TS, c = i % TS;
       if (a > ex || b > ey || c > ez) continue;
-      const unsigned long long v = acc[i];
+      const unsigned long long v = ((unsigned long long)acc_hi[i] << 32) | acc_lo[i];
       const uint32_t gx = ox + a == g.n ? 0u : ox + a;
       const uint32_t gy = oy + b == g.n ? 0u : oy + b;
       const uint32_t gz = oz + c == g.n ? 0u : oz + c;
@@ -358,7 +364,7 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   SIFG_LAUNCH_CHECK();
   const float cl = box / (float)n;
   const float inv_cell_vol = 1.0f / (float)(cl * cl * cl);
-  const size_t smem = (size_t)TS * TS * TS * sizeof(unsigned long long);
+  const size_t smem = (size_t)2 * TS * TS * TS * sizeof(uint32_t);
   static bool attr = false;
   if (!attr) {
     SIFG_CUDA(cudaFuncSetAttribute(tile_deposit_kernel,

@@ -41,8 +41,16 @@ static constexpr uint32_t kGrowCap = 1u << 15;  // overflow window, floats per C
 
 Engine::Engine(int device) : device_(device) {
   SIFG_CUDA(cudaSetDevice(device));
-  SIFG_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+  int lo_prio = 0, hi_prio = 0;  // numerically, lo_prio >= hi_prio
+  SIFG_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+  SIFG_CUDA(cudaStreamCreateWithPriority(&st_, cudaStreamNonBlocking, hi_prio));
+  SIFG_CUDA(cudaStreamCreateWithPriority(&st_fft_, cudaStreamNonBlocking, lo_prio));
   SIFG_CUDA(cudaEventCreateWithFlags(&ev_cand_, cudaEventDisableTiming));
+  SIFG_CUDA(cudaEventCreateWithFlags(&ev_start_, cudaEventDisableTiming));
+  for (int k = 0; k < 2; k++) {
+    SIFG_CUDA(cudaEventCreateWithFlags(&ev_smoothed_[k], cudaEventDisableTiming));
+    SIFG_CUDA(cudaEventCreateWithFlags(&ev_scanned_[k], cudaEventDisableTiming));
+  }
   SIFG_CUDA(cudaMallocHost(&h_counters_, 16 * sizeof(uint32_t)));
 }
 
@@ -52,6 +60,9 @@ Engine::~Engine() {
   cudaFreeHost(h_rank_);
   cudaFreeHost(h_counters_);
   if (ev_cand_) cudaEventDestroy(ev_cand_);
+  for (cudaEvent_t ev : {ev_start_, ev_smoothed_[0], ev_smoothed_[1], ev_scanned_[0], ev_scanned_[1]})
+    if (ev) cudaEventDestroy(ev);
+  if (st_fft_) cudaStreamDestroy(st_fft_);
   if (st_) cudaStreamDestroy(st_);
 }
 
@@ -116,7 +127,12 @@ void qsort_serial(Rec* a, int64_t lo, int64_t hi) {
   }
 }
 
-constexpr int64_t kTaskCutoff = 65536;  // SIF_QUICKSORT_TASK_CUTOFF, sort.h:104
+// The two sides of a partition are disjoint, so sorting them in any order, on
+// any threads, leaves the serial sort's permutation: tasks are spawned down
+// to a few thousand elements, well below the reference's task cutoff
+// (SIF_QUICKSORT_TASK_CUTOFF, include/sif/utils/sort.h:104), which only
+// bounds its task overhead.
+constexpr int64_t kTaskCutoff = 4096;
 
 void qsort_tasks(Rec* a, int64_t lo, int64_t hi) {
   if (hi - lo < kTaskCutoff) {
@@ -135,7 +151,7 @@ void qsort_tasks(Rec* a, int64_t lo, int64_t hi) {
 void candidate_ranks(const float* delta, uint32_t m, uint32_t* rank, int threads) {
   std::vector<Rec> a(m);
   for (uint32_t k = 0; k < m; k++) a[k] = Rec{delta[k], k};
-  if (m > (uint32_t)kTaskCutoff && threads != 1) {
+  if (m > 8 * (uint32_t)kTaskCutoff && threads != 1) {
     const int t = threads > 0 ? threads : omp_get_max_threads();
 #pragma omp parallel num_threads(t)
 #pragma omp single nowait
@@ -222,12 +238,29 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   std::vector<float> radii = p.radii;
   std::sort(radii.begin(), radii.end(), [](float a, float b) { return a > b; });
 
-  float* field = grow_to<float>(field_, cells);
+  float* fields[2] = {grow_to<float>(field_[0], cells), grow_to<float>(field_[1], cells)};
   uint32_t* mask = grow_to<uint32_t>(mask_, (cells + 31) / 32);
   SIFG_CUDA(cudaMemsetAsync(mask, 0, ((cells + 31) / 32) * sizeof(uint32_t), st_));
+  // The smoothing stream starts after everything queued on the run's stream
+  // (the density contrast among it); rung ri's field is fields[ri % 2].
+  SIFG_CUDA(cudaEventRecord(ev_start_, st_));
+  SIFG_CUDA(cudaStreamWaitEvent(st_fft_, ev_start_, 0));
+  for (int k = 0; k < 2; k++) SIFG_CUDA(cudaEventRecord(ev_scanned_[k], st_));
+  auto smooth_rung = [&](uint32_t ri) {
+    SIFG_CUDA(cudaStreamWaitEvent(st_fft_, ev_scanned_[ri % 2], 0));
+    smoother.smooth(kFilterTopHat, radii[ri], 0.0f, fields[ri % 2], tm ? &tm->filter : nullptr);
+    SIFG_CUDA(cudaEventRecord(ev_smoothed_[ri % 2], st_fft_));
+  };
+  // On every way out, nothing of the run is left in flight on the smoothing
+  // stream.
+  struct FftDrain {
+    cudaStream_t s;
+    ~FftDrain() { cudaStreamSynchronize(s); }
+  } drain{st_fft_};
   if (!p.inject) {
-    smoother.setup(N, box, window_mode, st_);
+    smoother.setup(N, box, window_mode, st_fft_);
     smoother.forward(d_delta);
+    if (!radii.empty()) smooth_rung(0);
   }
 
   // Loop invariants, exodus_finder.c:1629-1632.
@@ -272,24 +305,34 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   MeshView mv{mesh.x, mesh.y, mesh.z, mesh.offsets, (int32_t)mesh.n_cells, mesh.box_length,
               1.0f / mesh.cell_length};
 
+  using clk = std::chrono::steady_clock;
+  auto ms_since = [](clk::time_point t0) {
+    return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+  };
   for (uint32_t ri = 0; ri < radii.size(); ri++) {
+    const auto t_rung = clk::now();
     RungStat rs;
     const float radius = radii[ri];
     rs.radius = radius;
 
-    // 1. The rung's field.
+    // 1. The rung's field; the next rung's smoothing queued behind this
+    //    rung's last read of the buffer it overwrites.
+    float* field = fields[ri % 2];
     if (p.inject) {
       SIFG_CUDA(cudaMemcpyAsync(field, p.inject + (uint64_t)ri * cells, cells * sizeof(float),
                                 p.inject_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                 st_));
     } else {
-      smoother.smooth(kFilterTopHat, radius, 0.0f, field, tm ? &tm->filter : nullptr);
+      if (ri + 1 < radii.size()) smooth_rung(ri + 1);
+      SIFG_CUDA(cudaStreamWaitEvent(st_, ev_smoothed_[ri % 2], 0));
     }
 
     // 2. Candidates, in flat order.
     scan_count_pass(field, mask, cells, threshold, blocks, dcount, st_);
     SIFG_CUDA(cudaMemcpyAsync(h_counters_, dcount, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
+    const auto t_wait = clk::now();
     SIFG_CUDA(cudaStreamSynchronize(st_));
+    rs.count_wait_ms = ms_since(t_wait);
     const uint32_t m = h_counters_[0];
     rs.n_candidates = m;
 
@@ -300,6 +343,8 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     if (ri > 0 && radii[ri - 1] > r_search) r_search = radii[ri - 1];
     rs.r_search = r_search;
     if (m == 0) {
+      SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
+      rs.rung_ms = ms_since(t_rung);
       if (stats) stats->push_back(rs);
       continue;
     }
@@ -307,6 +352,7 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     float* cdelta = grow_to<float>(cand_delta_, m);
     uint32_t* cflat = grow_to<uint32_t>(cand_flat_, m);
     scan_write_pass(field, mask, cells, threshold, blocks, cdelta, cflat, st_);
+    SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
     ensure_host(m);
     SIFG_CUDA(cudaMemcpyAsync(h_delta_, cdelta, m * sizeof(float), cudaMemcpyDeviceToHost, st_));
     SIFG_CUDA(cudaEventRecord(ev_cand_, st_));
@@ -391,12 +437,15 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     }
 
     // 5. The order, on the host while the GPU grows spheres.
+    const auto t_sort = clk::now();
     SIFG_CUDA(cudaEventSynchronize(ev_cand_));
     candidate_ranks(h_delta_, m, h_rank_, host_threads);
+    rs.sort_ms = ms_since(t_sort);
     uint32_t* rank = grow_to<uint32_t>(rank_, m);
     SIFG_CUDA(cudaMemcpyAsync(rank, h_rank_, m * sizeof(uint32_t), cudaMemcpyHostToDevice, st_));
 
     // 6. The commit, in rounds.
+    const auto t_commit = clk::now();
     const float reach = 2.0f * scale * r_search + 2.0f * cell;
     int32_t ng = (int32_t)std::floor(box / reach);
     if (ng < 3) ng = 1;
@@ -412,23 +461,28 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     uint32_t* acc = grow_to<uint32_t>(acc_, m);
     SIFG_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(uint32_t), st_));
     commit_init(sv, sa, counters, m, st_);
+    // Rounds are issued a few at a time between reads of the undecided
+    // count: a round after the last one decides nothing and paints nothing.
     uint64_t rounds = 0;
-    for (;;) {
-      SIFG_CUDA(cudaMemcpyAsync(counters + 2, counters, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st_));
-      SIFG_CUDA(cudaMemsetAsync(counters + 1, 0, sizeof(uint32_t), st_));
-      commit_round(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters, m, st_);
-      paint_new(sv, acc, counters, mask, rc, m, st_);
-      std::swap(sa, sb);
-      rounds++;
+    for (uint32_t batch = 3;; batch = 4) {
+      for (uint32_t b = 0; b < batch; b++) {
+        SIFG_CUDA(cudaMemcpyAsync(counters + 2, counters, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st_));
+        SIFG_CUDA(cudaMemsetAsync(counters + 1, 0, sizeof(uint32_t), st_));
+        commit_round(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters, m, st_);
+        paint_new(sv, acc, counters, mask, rc, m, st_);
+        std::swap(sa, sb);
+        rounds++;
+      }
       SIFG_CUDA(cudaMemcpyAsync(h_counters_, counters, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
       SIFG_CUDA(cudaMemcpyAsync(h_counters_ + 8, dcount + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
       SIFG_CUDA(cudaStreamSynchronize(st_));
       if (h_counters_[1] == 0) break;
-      if (rounds > (uint64_t)m + 2) {
+      if (rounds > (uint64_t)m + 8) {
         set_error(kErrInvalid, "commit: no progress");
         return kErrInvalid;
       }
     }
+    rs.commit_ms = ms_since(t_commit);
     const uint32_t n_acc = h_counters_[0];
     rs.n_survivors = h_counters_[8];
     rs.n_accepted = n_acc;
@@ -446,11 +500,13 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
       build_void_index(cat_x_.as<float>(), cat_y_.as<float>(), cat_z_.as<float>(), n_voids, box,
                        vstart, vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
     }
+    rs.rung_ms = ms_since(t_rung);
     if (stats) stats->push_back(rs);
   }
 
   if (p.consume_out) {
-    SIFG_CUDA(cudaMemcpyAsync(p.consume_out, field, cells * sizeof(float), cudaMemcpyDeviceToDevice, st_));
+    const float* last = fields[(radii.size() + 1) % 2];
+    SIFG_CUDA(cudaMemcpyAsync(p.consume_out, last, cells * sizeof(float), cudaMemcpyDeviceToDevice, st_));
   }
   const size_t base = out.cx.size();
   out.cx.resize(base + n_voids);

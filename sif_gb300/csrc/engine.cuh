@@ -32,6 +32,7 @@ struct RungStat {
   float radius = 0.f, r_search = 0.f;
   uint64_t n_candidates = 0, n_survivors = 0, n_accepted = 0, rounds = 0;
   uint64_t n_rescale_fail = 0, n_overflow = 0;
+  double rung_ms = 0, count_wait_ms = 0, sort_ms = 0, commit_ms = 0;  // host wall time
 };
 
 struct RunTimings {
@@ -72,7 +73,7 @@ class Engine {
  private:
   int device_;
   cudaStream_t st_ = 0;
-  DevBuf field_, mask_, cand_delta_, cand_flat_, blocks_, rank_, rank_slots_, alive_;
+  DevBuf field_[2], mask_, cand_delta_, cand_flat_, blocks_, rank_, rank_slots_, alive_;
   DevBuf surv_cand_, surv_flat_, scx_, scy_, scz_, sr_, sreason_, state_a_, state_b_, acc_;
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
@@ -83,6 +84,11 @@ class Engine {
   uint32_t* h_counters_ = nullptr;
   size_t h_cap_ = 0;
   cudaEvent_t ev_cand_ = nullptr;
+  // The smoothing runs on its own, lower-priority stream into two field
+  // buffers: rung i+1's transform overlaps rung i's growth and commit.
+  cudaStream_t st_fft_ = 0;
+  cudaEvent_t ev_start_ = nullptr, ev_smoothed_[2] = {nullptr, nullptr},
+              ev_scanned_[2] = {nullptr, nullptr};
   void ensure_host(size_t m);
 };
 

@@ -27,15 +27,59 @@ namespace sifg {
 // ---------------------------------------------------------------------------
 // Candidate scan
 // ---------------------------------------------------------------------------
+// Each thread takes 4 consecutive cells per round with one 16-byte load (the
+// field is 256-byte aligned, cells 4k..4k+3 never straddle it) and their 4
+// mask bits from one word; a block covers kScanChunk cells.
 constexpr int kScanT = 256;
-constexpr int kScanRounds = 16;
-constexpr uint64_t kScanChunk = (uint64_t)kScanT * kScanRounds;
+constexpr int kScanRounds = 8;
+constexpr uint64_t kScanChunk = (uint64_t)kScanT * 4 * kScanRounds;
 
 uint32_t scan_blocks(uint64_t n_cells) { return (uint32_t)((n_cells + kScanChunk - 1) / kScanChunk); }
 
-__device__ __forceinline__ bool is_candidate(const float* f, const uint32_t* mask, uint64_t i,
-                                             uint64_t n, float thr) {
-  return i < n && f[i] <= thr && !mask_get(mask, i);
+// The candidate bits of cells c0..c0+3 (bit j for c0 + j), and their depths.
+__device__ __forceinline__ uint32_t quad_candidates(const float* __restrict__ f,
+                                                    const uint32_t* __restrict__ mask,
+                                                    uint64_t c0, uint64_t n, float thr,
+                                                    float4& v) {
+  if (c0 + 3 < n) {
+    v = __ldg(reinterpret_cast<const float4*>(f + c0));
+  } else {
+    v.x = c0 < n ? f[c0] : 1.0f;
+    v.y = c0 + 1 < n ? f[c0 + 1] : 1.0f;
+    v.z = c0 + 2 < n ? f[c0 + 2] : 1.0f;
+    v.w = c0 + 3 < n ? f[c0 + 3] : 1.0f;
+  }
+  if (c0 >= n) return 0u;
+  const uint32_t m = __ldg(mask + (c0 >> 5)) >> (c0 & 31);
+  uint32_t bits = 0;
+  bits |= (v.x <= thr && !(m & 1u) && c0 < n) ? 1u : 0u;
+  bits |= (v.y <= thr && !(m & 2u) && c0 + 1 < n) ? 2u : 0u;
+  bits |= (v.z <= thr && !(m & 4u) && c0 + 2 < n) ? 4u : 0u;
+  bits |= (v.w <= thr && !(m & 8u) && c0 + 3 < n) ? 8u : 0u;
+  return bits;
+}
+
+// Exclusive scan of one value per thread across the block; *total the sum.
+__device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* ws, uint32_t* total) {
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= (unsigned)d) x += y;
+  }
+  if (lane == 31) ws[warp] = x;
+  __syncthreads();
+  uint32_t before = 0, t = 0;
+#pragma unroll
+  for (int w = 0; w < kScanT / 32; w++) {
+    const uint32_t s = ws[w];
+    before += (w < (int)warp) ? s : 0u;
+    t += s;
+  }
+  __syncthreads();
+  *total = t;
+  return before + x - v;
 }
 
 __global__ void __launch_bounds__(kScanT) scan_count_kernel(const float* __restrict__ f,
@@ -45,7 +89,11 @@ __global__ void __launch_bounds__(kScanT) scan_count_kernel(const float* __restr
   __shared__ uint32_t ws[kScanT / 32];
   const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
   uint32_t c = 0;
-  for (int j = 0; j < kScanRounds; j++) c += is_candidate(f, mask, base + j * kScanT + threadIdx.x, n, thr);
+#pragma unroll
+  for (int j = 0; j < kScanRounds; j++) {
+    float4 v;
+    c += __popc(quad_candidates(f, mask, base + ((uint64_t)j * kScanT + threadIdx.x) * 4, n, thr, v));
+  }
   c = __reduce_add_sync(0xffffffffu, c);
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
   __syncthreads();
@@ -59,29 +107,25 @@ __global__ void __launch_bounds__(kScanT) scan_count_kernel(const float* __restr
 __global__ void __launch_bounds__(kScanT) scan_write_kernel(
     const float* __restrict__ f, const uint32_t* __restrict__ mask, uint64_t n, float thr,
     const uint32_t* __restrict__ offsets, float* __restrict__ cdelta, uint32_t* __restrict__ cflat) {
-  __shared__ uint32_t wsum[kScanT / 32];
+  __shared__ uint32_t ws[kScanT / 32];
   const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
-  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   uint32_t out = offsets[blockIdx.x];
   for (int j = 0; j < kScanRounds; j++) {
-    const uint64_t i = base + j * kScanT + threadIdx.x;
-    const bool p = is_candidate(f, mask, i, n, thr);
-    const unsigned bal = __ballot_sync(0xffffffffu, p);
-    if (lane == 0) wsum[warp] = __popc(bal);
-    __syncthreads();
-    uint32_t before = 0, total = 0;
-    for (int w = 0; w < kScanT / 32; w++) {
-      const uint32_t v = wsum[w];
-      before += (w < (int)warp) ? v : 0u;
-      total += v;
-    }
-    if (p) {
-      const uint32_t pos = out + before + __popc(bal & ((1u << lane) - 1u));
-      cdelta[pos] = f[i];
-      cflat[pos] = (uint32_t)i;
+    const uint64_t c0 = base + ((uint64_t)j * kScanT + threadIdx.x) * 4;
+    float4 v;
+    const uint32_t bits = quad_candidates(f, mask, c0, n, thr, v);
+    uint32_t total;
+    uint32_t pos = out + block_scan_excl(__popc(bits), ws, &total);
+    const float d[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (bits & (1u << k)) {
+        cdelta[pos] = d[k];
+        cflat[pos] = (uint32_t)(c0 + k);
+        pos++;
+      }
     }
     out += total;
-    __syncthreads();
   }
 }
 
@@ -308,12 +352,21 @@ void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, Void
 // ---------------------------------------------------------------------------
 // Sphere growth
 // ---------------------------------------------------------------------------
+// One CTA per survivor. A warp takes the template 32 cells at a time: each
+// lane looks up one cell's particle range and periodic image at once, then
+// the warp walks the cells that need distances with every lane on a particle.
+// The reference's three stages (exodus_rescale.c:738-1007) in two passes over
+// the particles: pass 1 reads only the cells that cross a boundary of the
+// annulus -- enough for the early refusal, and binning the annulus particles
+// they hold on the way; pass 2, for a survivor not refused, bins the cells
+// wholly inside the annulus. The counts and the histogram are the reference's
+// exactly: the same distances, the same bin_of, the same classification.
 constexpr int kGrowT = 256;
 constexpr int kGrowWarps = kGrowT / 32;
 constexpr uint32_t kMaxBins = 2048;
-constexpr uint32_t kSmemBuf = 4096;
+constexpr uint32_t kSmemBuf = 2048;
 
-unsigned growth_grid() { return 152u * 4u; }
+unsigned growth_grid() { return 152u * 6u; }
 
 struct CellRange {
   uint32_t s, e;
@@ -388,16 +441,67 @@ __device__ void bitonic_sort(float* buf, uint32_t p) {
   }
 }
 
+// The cells of the template a warp walks, 32 at a time: `want(type, i)` says
+// whether a cell's range is looked up, `whole(type, count)` is then called on
+// the lane holding it (for counts), `particles(type)` whether its particles
+// are read, and `each(type, d2, p)` runs per particle read. `visited` and
+// `read` count the lookups and the particles.
+template <class Want, class Whole, class Particles, class Each>
+__device__ __forceinline__ void walk_cells(const MeshView& mesh, const TemplateView& tpl,
+                                           int32_t ci, int32_t cj, int32_t ck, float cx, float cy,
+                                           float cz, Want want, Whole whole, Particles particles,
+                                           Each each, unsigned long long& visited,
+                                           unsigned long long& read) {
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (uint32_t c0 = warp * 32; c0 < tpl.count; c0 += kGrowWarps * 32) {
+    const uint32_t i = c0 + lane;
+    CellRange c{0, 0, 0.f, 0.f, 0.f};
+    uint8_t type = 0;
+    bool need = false;
+    if (i < tpl.count) {
+      type = __ldg(tpl.type + i);
+      if (want(type, i)) {
+        c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
+        whole(type, c.e - c.s);
+        need = c.e > c.s && particles(type);
+        visited++;
+      }
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, need);
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const uint32_t s = __shfl_sync(0xffffffffu, c.s, src);
+      const uint32_t e = __shfl_sync(0xffffffffu, c.e, src);
+      const float ex = __shfl_sync(0xffffffffu, c.ex, src);
+      const float ey = __shfl_sync(0xffffffffu, c.ey, src);
+      const float ez = __shfl_sync(0xffffffffu, c.ez, src);
+      const uint8_t t = (uint8_t)__shfl_sync(0xffffffffu, (int)type, src);
+      if (lane == 0) read += e - s;
+      uint32_t p = s + lane;
+      // Two particles per lane in flight.
+      for (; p + 32 < e; p += 64) {
+        const float x0 = __ldg(mesh.x + p), y0 = __ldg(mesh.y + p), z0 = __ldg(mesh.z + p);
+        const float x1 = __ldg(mesh.x + p + 32), y1 = __ldg(mesh.y + p + 32),
+                    z1 = __ldg(mesh.z + p + 32);
+        each(t, dist2(x0, y0, z0, ex, ey, ez), p);
+        each(t, dist2(x1, y1, z1, ex, ey, ez), p + 32);
+      }
+      if (p < e) each(t, dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), ex, ey, ez), p);
+    }
+  }
+}
+
 // traffic[0] counts the particles whose positions a pass read (12 bytes
 // each), traffic[1] the template cells a pass visited (a range lookup, 8
 // bytes, plus the template entry, 8 bytes): the gathered bytes of the
 // sphere growth.
-__global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateView tpl,
-                                                        RungConsts rc, Survivors sv,
-                                                        float* __restrict__ gbuf, uint32_t gcap,
-                                                        unsigned long long* __restrict__ traffic) {
+__global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, TemplateView tpl,
+                                                           RungConsts rc, Survivors sv,
+                                                           float* __restrict__ gbuf, uint32_t gcap,
+                                                           unsigned long long* __restrict__ traffic) {
   __shared__ uint32_t bins[kMaxBins];
-  __shared__ unsigned long long below[kMaxBins];  // particles inside bin b's lower edge
+  __shared__ uint32_t below[kMaxBins];  // particles inside bin b's lower edge
   __shared__ float sbuf[kSmemBuf];
   __shared__ unsigned long long red64[kGrowWarps];
   __shared__ int redi[kGrowWarps];
@@ -413,22 +517,38 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
                   ck = (int32_t)fmul(cz, mesh.inv_l);
     uint8_t reason = kRescaleOk;
     float radius = -1.0f;
+    unsigned long long read = 0, visited = 0;
 
-    // 1. The early refusal (exodus_rescale.c:738-782): whole core and shell
-    //    cells by their counts, the rest particle by particle.
-    unsigned long long within = 0, read = 0, visited = 0;
-    for (uint32_t i = warp; i < tpl.count; i += kGrowWarps) {
-      const CellRange c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
-      const uint8_t type = __ldg(tpl.type + i);
-      if (lane == 0) visited++;
-      if (type == kCellCore || type == kCellShell) {
-        if (lane == 0) within += c.e - c.s;
-      } else {
-        if (lane == 0) read += c.e - c.s;
-        for (uint32_t p = c.s + lane; p < c.e; p += 32)
-          within += dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez) <= rc.rs2;
-      }
-    }
+    for (uint32_t b = threadIdx.x; b < rc.nb; b += kGrowT) bins[b] = 0;
+    __syncthreads();
+
+    // 1. Every cell: core and shell cells by their counts, the boundary
+    //    cells particle by particle -- the early refusal's count
+    //    (exodus_rescale.c:738-782) and their share of the histogram
+    //    (794-865) from the same distances.
+    unsigned long long within = 0, n_core = 0, n_shell = 0;
+    walk_cells(
+        mesh, tpl, ci, cj, ck, cx, cy, cz, [](uint8_t, uint32_t) { return true; },
+        [&](uint8_t type, uint32_t cnt) {
+          if (type == kCellCore) {
+            within += cnt;
+            n_core += cnt;
+          } else if (type == kCellShell) {
+            within += cnt;
+            n_shell += cnt;
+          }
+        },
+        [](uint8_t type) { return type == kCellStraddle || type == kCellEdge; },
+        [&](uint8_t, float d2, uint32_t) {
+          if (d2 <= rc.rs2) within++;
+          if (d2 <= rc.rc2) {
+            n_core++;
+          } else if (d2 <= rc.rs2) {
+            atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
+            n_shell++;
+          }
+        },
+        visited, read);
     within = block_sum_u64(within, red64);
     if (within == 0) {
       reason = kRescaleEmpty;
@@ -437,37 +557,15 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
     }
 
     if (reason == kRescaleOk) {
-      // 2. The d^2 histogram (exodus_rescale.c:794-865).
-      for (uint32_t b = threadIdx.x; b < rc.nb; b += kGrowT) bins[b] = 0;
-      __syncthreads();
-      unsigned long long n_core = 0, n_shell = 0;
-      for (uint32_t i = warp; i < tpl.count; i += kGrowWarps) {
-        const CellRange c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
-        const uint8_t type = __ldg(tpl.type + i);
-        if (lane == 0) {
-          visited++;
-          if (type != kCellCore) read += c.e - c.s;
-        }
-        if (type == kCellCore) {
-          if (lane == 0) n_core += c.e - c.s;
-        } else if (type == kCellShell) {
-          for (uint32_t p = c.s + lane; p < c.e; p += 32) {
-            const float d2 = dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez);
+      // 2. The cells wholly inside the annulus, every particle binned.
+      walk_cells(
+          mesh, tpl, ci, cj, ck, cx, cy, cz,
+          [](uint8_t type, uint32_t) { return type == kCellShell; }, [](uint8_t, uint32_t) {},
+          [](uint8_t) { return true; },
+          [&](uint8_t, float d2, uint32_t) {
             atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
-          }
-          if (lane == 0) n_shell += c.e - c.s;
-        } else {
-          for (uint32_t p = c.s + lane; p < c.e; p += 32) {
-            const float d2 = dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez);
-            if (d2 <= rc.rc2) {
-              n_core++;
-            } else if (d2 <= rc.rs2) {
-              atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
-              n_shell++;
-            }
-          }
-        }
-      }
+          },
+          visited, read);
       n_core = block_sum_u64(n_core, red64);
       n_shell = block_sum_u64(n_shell, red64);
       const unsigned long long total = n_core + n_shell;
@@ -479,13 +577,13 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
       if (reason == kRescaleOk) {
         // below[b] = core + bins < b: the interior count of bin b's skip test.
         if (warp == 0) {
-          unsigned long long carry = n_core;
+          uint32_t carry = (uint32_t)n_core;
           for (uint32_t b0 = 0; b0 < rc.nb; b0 += 32) {
             const uint32_t b = b0 + lane;
-            const unsigned long long v = b < rc.nb ? bins[b] : 0ull;
-            unsigned long long x = v;
+            const uint32_t v = b < rc.nb ? bins[b] : 0u;
+            uint32_t x = v;
             for (int d = 1; d < 32; d <<= 1) {
-              const unsigned long long y = __shfl_up_sync(0xffffffffu, x, d);
+              const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
               if (lane >= (unsigned)d) x += y;
             }
             if (b < rc.nb) below[b] = carry + x - v;
@@ -494,17 +592,16 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
         }
         __syncthreads();
 
-        // 3. The walk (exodus_rescale.c:914-1007): the highest bin not ruled
-        //    out by its skip test, resolved with the bins below it.
+        // 3. The walk (exodus_rescale.c:914-1007): the highest bin its skip
+        //    test does not rule out, resolved with the bins below it.
         int32_t cursor = (int32_t)rc.nb - 1;
         reason = kRescaleBelowRung;
         while (cursor >= 0) {
           int best = -1;
           for (int32_t b = threadIdx.x; b <= cursor; b += kGrowT) {
-            const uint32_t cnt = bins[b];
-            if (cnt == 0) continue;
+            if (bins[b] == 0) continue;
             const float hi = bin_hi(rc, b);
-            const float nm = __ull2float_rn(below[b]);
+            const float nm = __uint2float_rn(below[b]);
             if (!(fmul(nm, nm) > fmul(fmul(fmul(rc.K2, hi), hi), hi))) best = max(best, b);
           }
           best = block_max_int(best, redi);
@@ -512,9 +609,9 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
           const int32_t b_hi = best;
           int32_t b_lo = b_hi - (int32_t)rc.window + 1;
           if (b_lo < 0) b_lo = 0;
-          const unsigned long long top = below[b_hi] + bins[b_hi];
+          const uint32_t top = below[b_hi] + bins[b_hi];
           while (b_lo < b_hi && top - below[b_lo] > kSmemBuf) b_lo++;
-          const uint32_t want = (uint32_t)(top - below[b_lo]);
+          const uint32_t want = top - below[b_lo];
           float* buf = sbuf;
           uint32_t cap = kSmemBuf;
           if (want > kSmemBuf) {
@@ -529,23 +626,21 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
           const float hi = bin_hi(rc, b_hi);
           if (threadIdx.x == 0) collected = 0;
           __syncthreads();
-          for (uint32_t i = warp; i < tpl.count; i += kGrowWarps) {
-            const uint8_t type = __ldg(tpl.type + i);
-            if (type == kCellCore || __ldg(tpl.max_d2 + i) < lo || __ldg(tpl.min_d2 + i) > hi) continue;
-            const CellRange c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
-            if (lane == 0) {
-              visited++;
-              read += c.e - c.s;
-            }
-            for (uint32_t p = c.s + lane; p < c.e; p += 32) {
-              const float d2 = dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), c.ex, c.ey, c.ez);
-              if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) continue;
-              const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
-              if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) continue;
-              const uint32_t slot = atomicAdd(&collected, 1u);
-              if (slot < cap) buf[slot] = d2;
-            }
-          }
+          walk_cells(
+              mesh, tpl, ci, cj, ck, cx, cy, cz,
+              [&](uint8_t type, uint32_t i) {
+                return type != kCellCore && !(__ldg(tpl.max_d2 + i) < lo) &&
+                       !(__ldg(tpl.min_d2 + i) > hi);
+              },
+              [](uint8_t, uint32_t) {}, [](uint8_t) { return true; },
+              [&](uint8_t type, float d2, uint32_t) {
+                if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) return;
+                const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
+                if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) return;
+                const uint32_t slot = atomicAdd(&collected, 1u);
+                if (slot < cap) buf[slot] = d2;
+              },
+              visited, read);
           __syncthreads();
           const uint32_t m = collected < cap ? collected : cap;
           uint32_t p2 = 1;
@@ -558,7 +653,7 @@ __global__ void __launch_bounds__(kGrowT) growth_kernel(MeshView mesh, TemplateV
           for (uint32_t k = threadIdx.x; k < m; k += kGrowT) {
             const float d2 = buf[k];
             if (d2 == 0.0f) continue;
-            const float rn = __ull2float_rn(top - m + k);
+            const float rn = __uint2float_rn(top - m + k);
             const float d2c = fmul(fmul(d2, d2), d2);
             if (fmul(rn, rn) <= fmul(rc.K2, d2c)) found = max(found, (int)k);
           }

@@ -32,24 +32,49 @@ namespace sifg {
     if (r_ != CUFFT_SUCCESS) throw ::sifg::CudaError{cudaErrorUnknown, #call};  \
   } while (0)
 
-__global__ void filter_kernel(const float2* __restrict__ spec, float2* __restrict__ out,
+__device__ __forceinline__ float filter_factor(uint32_t ix, uint32_t iy, uint32_t iz, uint32_t n,
+                                               const float* __restrict__ lut,
+                                               const float* __restrict__ win, float norm) {
+  const uint32_t h = n >> 1;
+  const int32_t kx = ix > h ? (int32_t)ix - (int32_t)n : (int32_t)ix;
+  const int32_t ky = iy > h ? (int32_t)iy - (int32_t)n : (int32_t)iy;
+  const uint32_t k2 = (uint32_t)(kx * kx + ky * ky) + iz * iz;
+  float s = __ldg(lut + k2) * norm;
+  if (win) s = s * __ldg(win + ix) * __ldg(win + iy) * __ldg(win + iz);
+  return s;
+}
+
+// Two modes per thread, one 16-byte load and store (an odd grid's last mode
+// on its own); Index is 32-bit whenever the count allows, the index
+// arithmetic being most of the kernel's instructions.
+template <class Index>
+__global__ void filter_kernel(const float4* __restrict__ spec, float4* __restrict__ out,
                               uint32_t n, const float* __restrict__ lut,
                               const float* __restrict__ win, float norm) {
   const uint32_t zd = n / 2 + 1;
-  const uint32_t h = n >> 1;
-  const uint64_t total = (uint64_t)n * n * zd;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
-    const uint32_t iz = (uint32_t)(i % zd);
-    const uint64_t row = i / zd;
+  const Index pairs = (Index)n * n * zd / 2;
+  const Index stride = (Index)gridDim.x * blockDim.x;
+  for (Index j = (Index)blockIdx.x * blockDim.x + threadIdx.x; j < pairs; j += stride) {
+    const Index i = 2 * j;
+    const Index row = i / zd;
+    const uint32_t iz = (uint32_t)(i - row * zd);
     const uint32_t iy = (uint32_t)(row % n), ix = (uint32_t)(row / n);
-    const int32_t kx = ix > h ? (int32_t)ix - (int32_t)n : (int32_t)ix;
-    const int32_t ky = iy > h ? (int32_t)iy - (int32_t)n : (int32_t)iy;
-    const uint32_t k2 = (uint32_t)(kx * kx + ky * ky) + iz * iz;
-    float s = __ldg(lut + k2) * norm;
-    if (win) s = s * __ldg(win + ix) * __ldg(win + iy) * __ldg(win + iz);
-    const float2 v = spec[i];
-    out[i] = make_float2(v.x * s, v.y * s);
+    const float s0 = filter_factor(ix, iy, iz, n, lut, win, norm);
+    float s1;
+    if (iz + 1 < zd) {
+      s1 = filter_factor(ix, iy, iz + 1, n, lut, win, norm);
+    } else {
+      const uint32_t iy1 = iy + 1 == n ? 0u : iy + 1;
+      s1 = filter_factor(iy1 == 0 ? ix + 1 : ix, iy1, 0, n, lut, win, norm);
+    }
+    const float4 v = spec[j];
+    out[j] = make_float4(v.x * s0, v.y * s0, v.z * s1, v.w * s1);
+  }
+  const Index total = (Index)n * n * zd;
+  if ((total & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const float s = filter_factor(n - 1, n - 1, zd - 1, n, lut, win, norm);
+    const float2 v = ((const float2*)spec)[total - 1];
+    ((float2*)out)[total - 1] = make_float2(v.x * s, v.y * s);
   }
 }
 
@@ -85,14 +110,18 @@ void Smoother::release() {
 }
 
 void Smoother::setup(uint32_t n_, float box_, int window_mode_, cudaStream_t st) {
-  if (n_ != n || st != stream) {
+  if (n_ != n) {
     release();
     n = n_;
-    stream = st;
     SIFG_CUFFT(cufftPlan3d(&plan_r2c, (int)n, (int)n, (int)n, CUFFT_R2C));
     SIFG_CUFFT(cufftPlan3d(&plan_c2r, (int)n, (int)n, (int)n, CUFFT_C2R));
     SIFG_CUFFT(cufftSetStream(plan_r2c, st));
     SIFG_CUFFT(cufftSetStream(plan_c2r, st));
+    stream = st;
+  } else if (st != stream) {
+    SIFG_CUFFT(cufftSetStream(plan_r2c, st));
+    SIFG_CUFFT(cufftSetStream(plan_c2r, st));
+    stream = st;
   }
   box = box_;
   window_mode = window_mode_;
@@ -135,9 +164,14 @@ void Smoother::smooth(int filter, float r, float sigma, float* out, KernelTimer*
   const uint64_t modes = (uint64_t)n * n * (n / 2 + 1);
   const float norm = (float)(1.0 / ((double)n * n * n));
   if (timer) timer->begin(stream);
-  filter_kernel<<<grid_for(modes, 256, 152u * 8u), 256, 0, stream>>>(
-      spectrum.as<float2>(), work.as<float2>(), n, lut.as<float>(),
-      (window_mode && filter != kFilterNone) ? win.as<float>() : nullptr, norm);
+  const float* w = (window_mode && filter != kFilterNone) ? win.as<float>() : nullptr;
+  const unsigned grd = grid_for(modes / 2 + 1, 256, 152u * 8u);
+  if (modes < (1ull << 32))
+    filter_kernel<uint32_t><<<grd, 256, 0, stream>>>(spectrum.as<float4>(), work.as<float4>(), n,
+                                                     lut.as<float>(), w, norm);
+  else
+    filter_kernel<uint64_t><<<grd, 256, 0, stream>>>(spectrum.as<float4>(), work.as<float4>(), n,
+                                                     lut.as<float>(), w, norm);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(stream);
   SIFG_CUFFT(cufftExecC2R(plan_c2r, (cufftComplex*)work.ptr, (cufftReal*)out));

@@ -55,20 +55,36 @@ def test_struct_sizes_match_the_reference_layout():
     assert abi.sif_catalogue_t.n_voids.offset == 88
 
 
+def _host_ranks_vs_oracle(lib, oracle, d):
+    m = len(d)
+    rank = np.empty(m, np.uint32)
+    if m:
+        lib.sifg_candidate_ranks(d.ctypes.data, m, rank.ctypes.data)
+    rec = np.zeros(m, oracle.CANDIDATE_DTYPE)
+    rec["delta"] = d
+    rec["flat"] = np.arange(m)
+    s = oracle.sort_candidates(rec)
+    want = np.empty(m, np.int64)
+    want[s["flat"].astype(np.int64)] = np.arange(m)
+    assert np.array_equal(rank.astype(np.int64), want), m
+
+
 def test_host_rank_replay_matches_oracle_sort(lib, oracle):
     rng = np.random.default_rng(9)
-    for m in [0, 1, 7, 4096, 70000, 200000]:
+    for m in [0, 1, 7, 4095, 4096, 4097, 32769, 70000, 200000]:
         d = (rng.integers(0, 64, m) * np.float32(-0.002) - np.float32(0.8)).astype(np.float32)
-        rank = np.empty(m, np.uint32)
-        if m:
-            lib.sifg_candidate_ranks(d.ctypes.data, m, rank.ctypes.data)
-        rec = np.zeros(m, oracle.CANDIDATE_DTYPE)
-        rec["delta"] = d
-        rec["flat"] = np.arange(m)
-        s = oracle.sort_candidates(rec)
-        want = np.empty(m, np.int64)
-        want[s["flat"].astype(np.int64)] = np.arange(m)
-        assert np.array_equal(rank.astype(np.int64), want)
+        _host_ranks_vs_oracle(lib, oracle, d)
+
+
+def test_host_rank_replay_shapes(lib, oracle):
+    """Continuous keys with scattered ties, already ordered and reversed
+    inputs, one key throughout, and a million keys over a few hundred values."""
+    rng = np.random.default_rng(10)
+    d = rng.uniform(-1.0, -0.8, 150000).astype(np.float32)
+    d[rng.integers(0, len(d), 20000)] = d[rng.integers(0, len(d), 20000)]
+    for case in [d, np.sort(d), np.sort(d)[::-1].copy(), np.full(50000, -0.9, np.float32),
+                 (rng.integers(0, 300, 1000000) * np.float32(-0.0005)).astype(np.float32)]:
+        _host_ranks_vs_oracle(lib, oracle, np.ascontiguousarray(case))
 
 
 def test_variants_and_argument_errors_without_a_gpu(lib):

@@ -123,6 +123,20 @@ def test_smoothing_against_fp64(dev, oracle, golden_box32, window):
         assert l2 <= FIELD_L2_TOL and mx <= FIELD_MAX_TOL, (r, l2, mx)
 
 
+@pytest.mark.parametrize("n", [27, 30])
+def test_smoothing_odd_and_non_power_grids(dev, oracle, n):
+    """Grids whose mode count n^2 (n/2+1) is odd (27) or not a power of two (30)."""
+    rng = np.random.default_rng(n)
+    delta = rng.standard_normal(n ** 3).astype(np.float32)
+    box = 3.0 * n
+    want = oracle.smooth(delta, n, box, [5.0, 9.0], mode=0, want="f64")
+    (d,) = _cuda(delta)
+    for i, r in enumerate([5.0, 9.0]):
+        got = dev.smooth(d, n, box, r).cpu().numpy()
+        l2, mx = _rel(got, want[i])
+        assert l2 <= FIELD_L2_TOL and mx <= FIELD_MAX_TOL, (n, r, l2, mx)
+
+
 def test_gaussian_smoothing_against_fp64(dev, oracle, golden_box32):
     g = golden_box32
     n, box = int(g["params"][0]), float(g["params"][1])
