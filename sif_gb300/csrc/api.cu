@@ -83,7 +83,7 @@ static Engine* engine() {
 // --- device scratch for the C API's copies -------------------------------
 
 struct ApiBufs {
-  DevBuf px, py, pz, grid, mx, my, mz, offs, orig, bad;
+  DevBuf px, py, pz, grid, mx, my, mz, offs, orig, bad, wide;
 };
 static ApiBufs& bufs() {
   static ApiBufs b;
@@ -140,6 +140,28 @@ static int check_field(const sif_field_t* field, const char* tag) {
   return SIF_OK;
 }
 
+__global__ void widen_kernel(const uint32_t* __restrict__ in, uint64_t* __restrict__ out, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = in[i];
+}
+
+__global__ void narrow_kernel(const uint64_t* __restrict__ in, uint32_t* __restrict__ out, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = (uint32_t)in[i];
+}
+
+static void widen(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t st) {
+  widen_kernel<<<grid_for(n, 256), 256, 0, st>>>(in, out, n);
+  SIFG_LAUNCH_CHECK();
+}
+
+static void narrow(const uint64_t* in, uint32_t* out, uint64_t n, cudaStream_t st) {
+  narrow_kernel<<<grid_for(n, 256), 256, 0, st>>>(in, out, n);
+  SIFG_LAUNCH_CHECK();
+}
+
 static void upload_positions(const sif_field_t* f, cudaStream_t st) {
   const size_t b = f->n_particles * sizeof(float);
   SIFG_CUDA(cudaMemcpyAsync(bufs().px.ensure(b), f->x, b, cudaMemcpyHostToDevice, st));
@@ -152,7 +174,7 @@ static sif_catalogue_t* make_catalogue(const HostCatalogue& c) {
   sif_catalogue_t* cat = (sif_catalogue_t*)calloc(1, sizeof(sif_catalogue_t));
   if (!cat) return nullptr;
   const uint64_t cap = n ? n : 1;
-  cat->_block = (float*)malloc(4 * cap * sizeof(float));
+  cat->_block = (float*)host_block_get(4 * cap * sizeof(float));
   if (!cat->_block) {
     free(cat);
     return nullptr;
@@ -247,6 +269,7 @@ int sif_system_init(sif_config_t* config) {
 void sif_system_finalise(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_engine.reset();
+  host_pool_trim();
   g_init = false;
   g_log_level = SIF_LOG_LEVEL_INFO;
 }
@@ -272,7 +295,7 @@ sif_field_t* sif_field_alloc(uint64_t n_particles) {
 
 void sif_field_free(sif_field_t* f) {
   if (!f) return;
-  free(f->_position_block);
+  host_block_put(f->_position_block);
   free(f->_velocity_block);
   free(f->weights);
   free(f->original_indices);
@@ -284,7 +307,7 @@ int sif_field_assign_positions(sif_field_t* f, const sif_real* x, const sif_real
   if (!f || !x || !y || !z) return fail(SIF_ERR_INVALID, "field: NULL argument");
   const uint64_t n = f->n_particles;
   if (!f->_position_block) {
-    f->_position_block = (float*)malloc(3 * (n ? n : 1) * sizeof(float));
+    f->_position_block = (float*)host_block_get(3 * (n ? n : 1) * sizeof(float));
     if (!f->_position_block) return fail(SIF_ERR_ALLOC, "field: cannot allocate positions");
     f->x = f->_position_block;
     f->y = f->_position_block + n;
@@ -321,7 +344,8 @@ sif_grid_t* sif_grid_alloc(uint32_t n_cells, sif_real box_length) {
   g->p2_shift = g->p2_mask ? (uint32_t)__builtin_ctz(n_cells) : 0;
   g->content = SIF_GRID_EMPTY;
   g->assignment = SIF_ASSIGNMENT_UNKNOWN;
-  g->values = (float*)calloc(g->total_cells, sizeof(float));
+  g->values = (float*)host_block_get(g->total_cells * sizeof(float));
+  if (g->values) memset(g->values, 0, g->total_cells * sizeof(float));
   if (!g->values) {
     free(g);
     fail(SIF_ERR_ALLOC, fmt("grid: cannot allocate %u^3 cells", n_cells));
@@ -332,13 +356,13 @@ sif_grid_t* sif_grid_alloc(uint32_t n_cells, sif_real box_length) {
 
 void sif_grid_free(sif_grid_t* g) {
   if (!g) return;
-  free(g->values);
+  host_block_put(g->values);
   free(g);
 }
 
 void sif_catalogue_free(sif_catalogue_t* c) {
   if (!c) return;
-  free(c->_block);
+  host_block_put(c->_block);
   free(c->_footprint_block);
   free(c);
 }
@@ -452,29 +476,33 @@ static sif_chain_mesh_t* mesh_alloc(uint32_t n_cells, sif_real box, sif_field_t*
   mesh->cell_length = m.cell_length;
   mesh->n_particles = n;
   mesh->total_weight = (double)n;
-  mesh->_position_block = (float*)malloc(3 * (n ? n : 1) * sizeof(float));
+  mesh->_position_block = (float*)host_block_get(3 * (n ? n : 1) * sizeof(float));
   mesh->x = mesh->_position_block;
   mesh->y = mesh->_position_block + n;
   mesh->z = mesh->_position_block + 2 * n;
-  mesh->cell_offsets = (uint64_t*)malloc((cells + 1) * sizeof(uint64_t));
-  std::vector<uint32_t> offs32(cells + 1);
+  mesh->cell_offsets = (uint64_t*)host_block_get((cells + 1) * sizeof(uint64_t));
+  if (keep_idx) mesh->original_indices = (uint64_t*)host_block_get(n * sizeof(uint64_t));
+  if (!mesh->_position_block || !mesh->cell_offsets || (keep_idx && !mesh->original_indices)) {
+    sif_chain_mesh_free(mesh);
+    fail(SIF_ERR_ALLOC, "mesh: cannot allocate host arrays");
+    return nullptr;
+  }
   SIFG_CUDA(cudaMemcpyAsync(mesh->x, m.x, n * 4, cudaMemcpyDeviceToHost, s));
   SIFG_CUDA(cudaMemcpyAsync(mesh->y, m.y, n * 4, cudaMemcpyDeviceToHost, s));
   SIFG_CUDA(cudaMemcpyAsync(mesh->z, m.z, n * 4, cudaMemcpyDeviceToHost, s));
-  SIFG_CUDA(cudaMemcpyAsync(offs32.data(), m.offsets, (cells + 1) * 4, cudaMemcpyDeviceToHost, s));
-  std::vector<uint32_t> orig32;
+  // The 64-bit offsets and indices of the reference's struct, widened on the
+  // device and copied straight into the struct's arrays.
+  uint64_t* wide = (uint64_t*)bufs().wide.ensure((keep_idx ? std::max<uint64_t>(n, cells + 1) : cells + 1) * 8);
+  widen(m.offsets, wide, cells + 1, s);
+  SIFG_CUDA(cudaMemcpyAsync(mesh->cell_offsets, wide, (cells + 1) * 8, cudaMemcpyDeviceToHost, s));
   if (keep_idx) {
-    orig32.resize(n);
-    SIFG_CUDA(cudaMemcpyAsync(orig32.data(), m.orig, n * 4, cudaMemcpyDeviceToHost, s));
+    SIFG_CUDA(cudaStreamSynchronize(s));
+    widen(m.orig, wide, n, s);
+    SIFG_CUDA(cudaMemcpyAsync(mesh->original_indices, wide, n * 8, cudaMemcpyDeviceToHost, s));
   }
   SIFG_CUDA(cudaStreamSynchronize(s));
-  for (uint64_t c = 0; c <= cells; c++) mesh->cell_offsets[c] = offs32[c];
-  if (keep_idx) {
-    mesh->original_indices = (uint64_t*)malloc(n * sizeof(uint64_t));
-    for (uint64_t i = 0; i < n; i++) mesh->original_indices[i] = orig32[i];
-  }
   if (consume) {
-    free(field->_position_block);
+    host_block_put(field->_position_block);
     field->_position_block = nullptr;
     field->x = field->y = field->z = nullptr;
     field->n_particles = 0;
@@ -495,12 +523,12 @@ sif_chain_mesh_t* sif_chain_mesh_alloc_consume(uint32_t n_cells, sif_real box_le
 
 void sif_chain_mesh_free(sif_chain_mesh_t* m) {
   if (!m) return;
-  free(m->_position_block);
+  host_block_put(m->_position_block);
   free(m->_velocity_block);
   free(m->weights);
   free(m->cell_weights);
-  free(m->original_indices);
-  free(m->cell_offsets);
+  host_block_put(m->original_indices);
+  host_block_put(m->cell_offsets);
   free(m);
 }
 
@@ -629,16 +657,28 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   m.box_length = mesh->box_length;
   m.cell_length = mesh->cell_length;
   m.n_particles = n;
+  // The mesh goes up on the copy stream while the first rungs are smoothed;
+  // the run waits for it before its first sphere growth.
+  cudaStream_t cs = e->copy_stream();
+  SIFG_CUDA(cudaEventRecord(e->ev_copy_start(), s));
+  SIFG_CUDA(cudaStreamWaitEvent(cs, e->ev_copy_start(), 0));
   m.x = (float*)bufs().mx.ensure(n * 4);
   m.y = (float*)bufs().my.ensure(n * 4);
   m.z = (float*)bufs().mz.ensure(n * 4);
-  SIFG_CUDA(cudaMemcpyAsync(m.x, mesh->x, n * 4, cudaMemcpyHostToDevice, s));
-  SIFG_CUDA(cudaMemcpyAsync(m.y, mesh->y, n * 4, cudaMemcpyHostToDevice, s));
-  SIFG_CUDA(cudaMemcpyAsync(m.z, mesh->z, n * 4, cudaMemcpyHostToDevice, s));
-  std::vector<uint32_t> offs32(mcells + 1);
-  for (uint64_t c = 0; c <= mcells; c++) offs32[c] = (uint32_t)mesh->cell_offsets[c];
   m.offsets = (uint32_t*)bufs().offs.ensure((mcells + 1) * 4);
-  SIFG_CUDA(cudaMemcpyAsync(m.offsets, offs32.data(), (mcells + 1) * 4, cudaMemcpyHostToDevice, s));
+  uint64_t* wide = (uint64_t*)bufs().wide.ensure((mcells + 1) * 8);
+  SIFG_CUDA(cudaMemcpyAsync(wide, mesh->cell_offsets, (mcells + 1) * 8, cudaMemcpyHostToDevice, cs));
+  narrow(wide, m.offsets, mcells + 1, cs);
+  SIFG_CUDA(cudaMemcpyAsync(m.x, mesh->x, n * 4, cudaMemcpyHostToDevice, cs));
+  SIFG_CUDA(cudaMemcpyAsync(m.y, mesh->y, n * 4, cudaMemcpyHostToDevice, cs));
+  SIFG_CUDA(cudaMemcpyAsync(m.z, mesh->z, n * 4, cudaMemcpyHostToDevice, cs));
+  SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
+  // Whatever the run's outcome, the copies out of the caller's mesh end
+  // before this call returns.
+  struct CopyDrain {
+    cudaStream_t s;
+    ~CopyDrain() { cudaStreamSynchronize(s); }
+  } drain{cs};
 
   RunParams p;
   p.grid_n = grid->n_cells;
@@ -648,6 +688,7 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   p.options = opt;
   p.radii.assign(radii, radii + n_radii);
   p.window = g_window;
+  p.mesh_ready = e->ev_mesh_ready();
   float* consume = nullptr;
   if (opt & SIF_FINDER_CONSUME_GRID) consume = (float*)bufs().px.ensure(gb);
   p.consume_out = consume;

@@ -45,6 +45,9 @@ Engine::Engine(int device) : device_(device) {
   SIFG_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
   SIFG_CUDA(cudaStreamCreateWithPriority(&st_, cudaStreamNonBlocking, hi_prio));
   SIFG_CUDA(cudaStreamCreateWithPriority(&st_fft_, cudaStreamNonBlocking, lo_prio));
+  SIFG_CUDA(cudaStreamCreateWithFlags(&st_copy_, cudaStreamNonBlocking));
+  SIFG_CUDA(cudaEventCreateWithFlags(&ev_copy_start_, cudaEventDisableTiming));
+  SIFG_CUDA(cudaEventCreateWithFlags(&ev_mesh_ready_, cudaEventDisableTiming));
   SIFG_CUDA(cudaEventCreateWithFlags(&ev_cand_, cudaEventDisableTiming));
   SIFG_CUDA(cudaEventCreateWithFlags(&ev_start_, cudaEventDisableTiming));
   for (int k = 0; k < 2; k++) {
@@ -60,9 +63,11 @@ Engine::~Engine() {
   cudaFreeHost(h_rank_);
   cudaFreeHost(h_counters_);
   if (ev_cand_) cudaEventDestroy(ev_cand_);
-  for (cudaEvent_t ev : {ev_start_, ev_smoothed_[0], ev_smoothed_[1], ev_scanned_[0], ev_scanned_[1]})
+  for (cudaEvent_t ev : {ev_start_, ev_smoothed_[0], ev_smoothed_[1], ev_scanned_[0], ev_scanned_[1],
+                         ev_copy_start_, ev_mesh_ready_})
     if (ev) cudaEventDestroy(ev);
   if (st_fft_) cudaStreamDestroy(st_fft_);
+  if (st_copy_) cudaStreamDestroy(st_copy_);
   if (st_) cudaStreamDestroy(st_);
 }
 
@@ -305,6 +310,7 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   MeshView mv{mesh.x, mesh.y, mesh.z, mesh.offsets, (int32_t)mesh.n_cells, mesh.box_length,
               1.0f / mesh.cell_length};
 
+  bool mesh_waited = false;
   using clk = std::chrono::steady_clock;
   auto ms_since = [](clk::time_point t0) {
     return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
@@ -433,6 +439,10 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
       SIFG_CUDA(cudaMemcpyAsync(sr, neg.data(), m * sizeof(float), cudaMemcpyHostToDevice, st_));
       SIFG_CUDA(cudaMemsetAsync(sreason, kRescaleDegenerate, m, st_));
     } else {
+      if (p.mesh_ready && !mesh_waited) {
+        SIFG_CUDA(cudaStreamWaitEvent(st_, p.mesh_ready, 0));
+        mesh_waited = true;
+      }
       grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic, st_, tm ? &tm->growth : nullptr);
     }
 

@@ -26,6 +26,9 @@ struct RunParams {
   bool inject_on_device = false;
   // Where the last rung's field goes under SIF_FINDER_CONSUME_GRID (device).
   float* consume_out = nullptr;
+  // Recorded once the mesh is on the device, if it is still being copied
+  // when the run starts: the first sphere growth waits for it.
+  cudaEvent_t mesh_ready = nullptr;
 };
 
 struct RungStat {
@@ -59,6 +62,10 @@ class Engine {
   ~Engine();
 
   cudaStream_t stream() const { return st_; }
+  // A stream for uploads that overlap the run, and two events for them.
+  cudaStream_t copy_stream() const { return st_copy_; }
+  cudaEvent_t ev_copy_start() const { return ev_copy_start_; }
+  cudaEvent_t ev_mesh_ready() const { return ev_mesh_ready_; }
   int device() const { return device_; }
 
   // The finder on a density contrast on the device and a device mesh.
@@ -86,7 +93,8 @@ class Engine {
   cudaEvent_t ev_cand_ = nullptr;
   // The smoothing runs on its own, lower-priority stream into two field
   // buffers: rung i+1's transform overlaps rung i's growth and commit.
-  cudaStream_t st_fft_ = 0;
+  cudaStream_t st_fft_ = 0, st_copy_ = 0;
+  cudaEvent_t ev_copy_start_ = nullptr, ev_mesh_ready_ = nullptr;
   cudaEvent_t ev_start_ = nullptr, ev_smoothed_[2] = {nullptr, nullptr},
               ev_scanned_[2] = {nullptr, nullptr};
   void ensure_host(size_t m);

@@ -36,6 +36,14 @@ struct DevBuf {
   T* as() const { return (T*)ptr; }
 };
 
+// --- hostpool.cu ---
+// Host blocks for the library's structs: page-locked where possible, reused
+// after host_block_put. host_block_put of a pointer the pool did not hand
+// out frees it with free().
+void* host_block_get(size_t bytes);
+void host_block_put(void* ptr);
+void host_pool_trim();
+
 // --- scan.cu ---
 // In-place exclusive prefix sum of n uint32 values (n < 2^31). The chunk
 // totals go to `sums_scratch` (scan_sums_needed(n) entries) when given, else

@@ -44,31 +44,51 @@ __device__ __forceinline__ float filter_factor(uint32_t ix, uint32_t iy, uint32_
   return s;
 }
 
-// Two modes per thread, one 16-byte load and store (an odd grid's last mode
-// on its own); Index is 32-bit whenever the count allows, the index
-// arithmetic being most of the kernel's instructions.
+// Two modes per 16-byte load and store (an odd grid's last mode on its own),
+// four loads in flight per thread before any is used: the kernel is bound by
+// the latency of its loads. Index is 32-bit whenever the count allows.
 template <class Index>
-__global__ void filter_kernel(const float4* __restrict__ spec, float4* __restrict__ out,
-                              uint32_t n, const float* __restrict__ lut,
-                              const float* __restrict__ win, float norm) {
+__device__ __forceinline__ float4 filter_pair(float4 v, Index j, uint32_t n, uint32_t zd,
+                                              const float* __restrict__ lut,
+                                              const float* __restrict__ win, float norm) {
+  const Index i = 2 * j;
+  const Index row = i / zd;
+  const uint32_t iz = (uint32_t)(i - row * zd);
+  const uint32_t iy = (uint32_t)(row % n), ix = (uint32_t)(row / n);
+  const float s0 = filter_factor(ix, iy, iz, n, lut, win, norm);
+  float s1;
+  if (iz + 1 < zd) {
+    s1 = filter_factor(ix, iy, iz + 1, n, lut, win, norm);
+  } else {
+    const uint32_t iy1 = iy + 1 == n ? 0u : iy + 1;
+    s1 = filter_factor(iy1 == 0 ? ix + 1 : ix, iy1, 0, n, lut, win, norm);
+  }
+  return make_float4(v.x * s0, v.y * s0, v.z * s1, v.w * s1);
+}
+
+constexpr int kFilterUnroll = 4;
+
+template <class Index>
+__global__ void __launch_bounds__(256) filter_kernel(const float4* __restrict__ spec,
+                                                     float4* __restrict__ out, uint32_t n,
+                                                     const float* __restrict__ lut,
+                                                     const float* __restrict__ win, float norm) {
   const uint32_t zd = n / 2 + 1;
   const Index pairs = (Index)n * n * zd / 2;
   const Index stride = (Index)gridDim.x * blockDim.x;
-  for (Index j = (Index)blockIdx.x * blockDim.x + threadIdx.x; j < pairs; j += stride) {
-    const Index i = 2 * j;
-    const Index row = i / zd;
-    const uint32_t iz = (uint32_t)(i - row * zd);
-    const uint32_t iy = (uint32_t)(row % n), ix = (uint32_t)(row / n);
-    const float s0 = filter_factor(ix, iy, iz, n, lut, win, norm);
-    float s1;
-    if (iz + 1 < zd) {
-      s1 = filter_factor(ix, iy, iz + 1, n, lut, win, norm);
-    } else {
-      const uint32_t iy1 = iy + 1 == n ? 0u : iy + 1;
-      s1 = filter_factor(iy1 == 0 ? ix + 1 : ix, iy1, 0, n, lut, win, norm);
+  for (Index j0 = (Index)blockIdx.x * blockDim.x + threadIdx.x; j0 < pairs;
+       j0 += kFilterUnroll * stride) {
+    float4 v[kFilterUnroll];
+#pragma unroll
+    for (int u = 0; u < kFilterUnroll; u++) {
+      const Index j = j0 + u * stride;
+      if (j < pairs) v[u] = __ldg(spec + j);
     }
-    const float4 v = spec[j];
-    out[j] = make_float4(v.x * s0, v.y * s0, v.z * s1, v.w * s1);
+#pragma unroll
+    for (int u = 0; u < kFilterUnroll; u++) {
+      const Index j = j0 + u * stride;
+      if (j < pairs) out[j] = filter_pair(v[u], j, n, zd, lut, win, norm);
+    }
   }
   const Index total = (Index)n * n * zd;
   if ((total & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
