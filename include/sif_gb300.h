@@ -269,6 +269,9 @@ typedef struct {
   double count_wait_ms;
   double sort_ms;
   double commit_ms;
+  /* Particles read and template cells visited by the rung's sphere growth. */
+  uint64_t growth_particles;
+  uint64_t growth_cells;
 } sifg_rung_stat_t;
 
 /* Kernel timings of the last run, CUDA events on the launching stream. */

@@ -19,7 +19,8 @@ class RungStat(C.Structure):
                 ("n_accepted", C.c_uint64), ("rounds", C.c_uint64),
                 ("n_rescale_fail", C.c_uint64), ("n_overflow", C.c_uint64),
                 ("rung_ms", C.c_double), ("count_wait_ms", C.c_double),
-                ("sort_ms", C.c_double), ("commit_ms", C.c_double)]
+                ("sort_ms", C.c_double), ("commit_ms", C.c_double),
+                ("growth_particles", C.c_uint64), ("growth_cells", C.c_uint64)]
 
 
 class Timings(C.Structure):

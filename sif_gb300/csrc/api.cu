@@ -83,7 +83,7 @@ static Engine* engine() {
 // --- device scratch for the C API's copies -------------------------------
 
 struct ApiBufs {
-  DevBuf px, py, pz, grid, mx, my, mz, offs, orig, bad, wide;
+  DevBuf px, py, pz, grid, mx, my, mz, offs, orig, bad, wide, mesh_sums;
 };
 static ApiBufs& bufs() {
   static ApiBufs b;
@@ -831,7 +831,8 @@ int sifg_smooth_device(const float* delta, uint32_t n_grid, float box, float r, 
 static int run_device(Engine* e, const float* delta, uint32_t n_grid, float box, DeviceMesh& m,
                       const float* radii, uint32_t n_radii, float threshold, float overlap,
                       uint32_t opt, const float* inject, float* cx, float* cy, float* cz, float* r,
-                      uint64_t capacity, uint64_t* n_voids, RunTimings& tm) {
+                      uint64_t capacity, uint64_t* n_voids, RunTimings& tm,
+                      cudaEvent_t mesh_ready = nullptr) {
   if (check_args(radii, n_radii, threshold, overlap) != SIF_OK) return g_status;
   RunParams p;
   p.grid_n = n_grid;
@@ -843,6 +844,7 @@ static int run_device(Engine* e, const float* delta, uint32_t n_grid, float box,
   p.window = g_window;
   p.inject = inject;
   p.inject_on_device = true;
+  p.mesh_ready = mesh_ready;
   HostCatalogue cat;
   g_stats.clear();
   const int st = e->exodus(delta, m, p, cat, &g_stats, &tm);
@@ -905,8 +907,16 @@ int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, 
   RunTimings tm;
   e->scratch.ensure(std::max(cic_scratch_bytes(n, n_grid), mesh_scratch_bytes(n, mesh_cells)));
   cic_deposit(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic);
-  double* cscratch = (double*)bufs().bad.ensure(density_contrast_scratch_bytes() + 64);
-  density_contrast(dg, cells, cscratch, s);
+  // The mesh is built on the copy stream (its own scan scratch) while the
+  // contrast is taken and the first rungs are smoothed; the run waits for it
+  // before its first sphere growth.
+  cudaStream_t cs = e->copy_stream();
+  SIFG_CUDA(cudaEventRecord(e->ev_copy_start(), s));
+  SIFG_CUDA(cudaStreamWaitEvent(cs, e->ev_copy_start(), 0));
+  struct CopyDrain {
+    cudaStream_t s;
+    ~CopyDrain() { cudaStreamSynchronize(s); }
+  } drain{cs};
   DeviceMesh m;
   m.n_cells = mesh_cells;
   m.box_length = box;
@@ -916,9 +926,14 @@ int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, 
   m.z = (float*)bufs().mz.ensure(n * 4);
   m.offsets = (uint32_t*)bufs().offs.ensure((mcells + 1) * 4);
   m.orig = nullptr;
-  mesh_build(x, y, z, n, m, e->scratch.ptr, s, &tm.mesh);
+  uint32_t* sums = (uint32_t*)bufs().mesh_sums.ensure(
+      (size_t)scan_sums_needed((uint32_t)(mcells + 1)) * sizeof(uint32_t));
+  mesh_build(x, y, z, n, m, e->scratch.ptr, cs, &tm.mesh, sums);
+  SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
+  double* cscratch = (double*)bufs().bad.ensure(density_contrast_scratch_bytes() + 64);
+  density_contrast(dg, cells, cscratch, s);
   st = run_device(e, dg, n_grid, box, m, radii, n_radii, threshold, overlap, opt, nullptr, cx, cy,
-                  cz, r, capacity, n_voids, tm);
+                  cz, r, capacity, n_voids, tm, e->ev_mesh_ready());
   tm.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   record_timings(tm);
   return st;
@@ -931,7 +946,8 @@ uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
     const RungStat& s = g_stats[i];
     out[i] = sifg_rung_stat_t{s.radius, s.r_search, s.n_candidates, s.n_survivors, s.n_accepted,
                               s.rounds, s.n_rescale_fail, s.n_overflow, s.rung_ms,
-                              s.count_wait_ms, s.sort_ms, s.commit_ms};
+                              s.count_wait_ms, s.sort_ms, s.commit_ms, s.growth_particles,
+                              s.growth_cells};
   }
   return n;
 }

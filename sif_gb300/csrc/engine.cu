@@ -301,8 +301,10 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   float max_r = 0.0f;
   float* gbuf = grow_to<float>(gbuf_, (size_t)growth_grid() * kGrowCap);
   uint32_t* dcount = grow_to<uint32_t>(dcount_, 16);
-  unsigned long long* traffic = (unsigned long long*)grow_to<uint64_t>(traffic_, 2);
-  SIFG_CUDA(cudaMemsetAsync(traffic, 0, 2 * sizeof(uint64_t), st_));
+  // Gathered particles and visited cells of each rung's sphere growth.
+  const size_t n_rungs = radii.size();
+  unsigned long long* traffic = (unsigned long long*)grow_to<uint64_t>(traffic_, 2 * n_rungs + 2);
+  SIFG_CUDA(cudaMemsetAsync(traffic, 0, (2 * n_rungs + 2) * sizeof(uint64_t), st_));
   uint32_t* counters = grow_to<uint32_t>(counters_, 16);
   const uint32_t nb_scan = scan_blocks(cells);
   uint32_t* blocks = grow_to<uint32_t>(blocks_, (size_t)std::max<uint64_t>(nb_scan + 1, 1024));
@@ -443,7 +445,7 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
         SIFG_CUDA(cudaStreamWaitEvent(st_, p.mesh_ready, 0));
         mesh_waited = true;
       }
-      grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic, st_, tm ? &tm->growth : nullptr);
+      grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_, tm ? &tm->growth : nullptr);
     }
 
     // 5. The order, on the host while the GPU grows spheres.
@@ -529,12 +531,19 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     SIFG_CUDA(cudaMemcpyAsync(out.cz.data() + base, cat_z_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
     SIFG_CUDA(cudaMemcpyAsync(out.r.data() + base, cat_r_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
   }
-  uint64_t h_traffic[2] = {0, 0};
-  SIFG_CUDA(cudaMemcpyAsync(h_traffic, traffic, sizeof h_traffic, cudaMemcpyDeviceToHost, st_));
+  std::vector<uint64_t> h_traffic(2 * n_rungs + 2, 0);
+  SIFG_CUDA(cudaMemcpyAsync(h_traffic.data(), traffic, h_traffic.size() * sizeof(uint64_t),
+                            cudaMemcpyDeviceToHost, st_));
   SIFG_CUDA(cudaStreamSynchronize(st_));
-  if (tm) {
-    tm->growth_particles += h_traffic[0];
-    tm->growth_cells += h_traffic[1];
+  for (size_t ri = 0; ri < n_rungs; ri++) {
+    if (tm) {
+      tm->growth_particles += h_traffic[2 * ri];
+      tm->growth_cells += h_traffic[2 * ri + 1];
+    }
+    if (stats && ri < stats->size()) {
+      (*stats)[stats->size() - n_rungs + ri].growth_particles = h_traffic[2 * ri];
+      (*stats)[stats->size() - n_rungs + ri].growth_cells = h_traffic[2 * ri + 1];
+    }
   }
   if (tm)
     tm->wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start)

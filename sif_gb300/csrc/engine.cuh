@@ -36,6 +36,7 @@ struct RungStat {
   uint64_t n_candidates = 0, n_survivors = 0, n_accepted = 0, rounds = 0;
   uint64_t n_rescale_fail = 0, n_overflow = 0;
   double rung_ms = 0, count_wait_ms = 0, sort_ms = 0, commit_ms = 0;  // host wall time
+  uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the rung's sphere growth
 };
 
 struct RunTimings {
