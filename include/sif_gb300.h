@@ -324,6 +324,31 @@ int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, 
                     float box, uint32_t mesh_cells, const float* radii, uint32_t n_radii,
                     float threshold, float overlap, uint32_t opt, float* cx, float* cy,
                     float* cz, float* r, uint64_t capacity, uint64_t* n_voids);
+/* The FP64 form: the calls above with every value in double, computing what
+ * the reference's SIF_USE_DOUBLE build computes (sif_real = double; its
+ * catalogue, on the same smoothed fields, bit for bit). The deposit sums each
+ * particle's weights as multiples of 2^-40 (exact, order-independent). These
+ * have no counterpart in the reference's float build, whose ABI they do not
+ * change; they are the form the float path is measured against. */
+int sifg_cic_device_f64(const double* x, const double* y, const double* z, uint64_t n,
+                        uint32_t n_grid, double box, double* grid);
+int sifg_contrast_device_f64(double* grid, uint64_t total_cells, double* mean_out);
+int sifg_mesh_device_f64(const double* x, const double* y, const double* z, uint64_t n,
+                         uint32_t n_cells, double box, double* mx, double* my, double* mz,
+                         uint32_t* offsets, uint32_t* orig);
+int sifg_smooth_device_f64(const double* delta, uint32_t n_grid, double box, double r,
+                           int filter, int window_mode, double* out);
+int sifg_exodus_device_f64(const double* delta, uint32_t n_grid, double box, const double* mx,
+                           const double* my, const double* mz, const uint32_t* offsets,
+                           uint64_t n_particles, uint32_t mesh_cells, const double* radii,
+                           uint32_t n_radii, double threshold, double overlap, uint32_t opt,
+                           const double* inject, double* cx, double* cy, double* cz, double* r,
+                           uint64_t capacity, uint64_t* n_voids);
+int sifg_box_device_f64(const double* x, const double* y, const double* z, uint64_t n,
+                        uint32_t n_grid, double box, uint32_t mesh_cells, const double* radii,
+                        uint32_t n_radii, double threshold, double overlap, uint32_t opt,
+                        double* cx, double* cy, double* cz, double* r, uint64_t capacity,
+                        uint64_t* n_voids);
 /* Statistics and timings of the last run (up to max_rungs entries). */
 uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs);
 void sifg_last_timings(sifg_timings_t* out);

@@ -37,15 +37,18 @@ def load(variant="strict", n_threads=0, log_level=abi.SIF_LOG_LEVEL_ERROR):
         return _LIBS[variant]
     path = os.path.join(HERE, "_ref", VARIANTS[variant])
     lib = C.CDLL(path, mode=C.RTLD_LOCAL)
-    abi.bind_sif_api(lib)
+    abi.bind_sif_api(lib, real_of(variant))
+    field_t, grid_t, mesh_t, _, extras_t = (
+        abi.STRUCTS_F64 if variant == "f64" else
+        (abi.sif_field_t, abi.sif_grid_t, abi.sif_chain_mesh_t, abi.sif_catalogue_t,
+         abi.sif_finder_exodus_extras_t))
     lib.sif_finder_exodus_raw.argtypes = [
-        C.POINTER(abi.sif_grid_t), C.POINTER(abi.sif_chain_mesh_t), C.c_void_p,
-        C.c_uint32, real_of(variant), real_of(variant), C.c_uint32,
-        C.POINTER(abi.sif_finder_exodus_extras_t)]
+        C.POINTER(grid_t), C.POINTER(mesh_t), C.c_void_p,
+        C.c_uint32, real_of(variant), real_of(variant), C.c_uint32, C.POINTER(extras_t)]
     lib.sif_grid_alloc.argtypes = [C.c_uint32, real_of(variant)]
     lib.sif_chain_mesh_alloc.argtypes = [C.c_uint32, real_of(variant),
-                                         C.POINTER(abi.sif_field_t), C.c_uint32]
-    lib.sif_field_assign_positions.argtypes = [C.POINTER(abi.sif_field_t),
+                                         C.POINTER(field_t), C.c_uint32]
+    lib.sif_field_assign_positions.argtypes = [C.POINTER(field_t),
                                                C.c_void_p, C.c_void_p, C.c_void_p]
     lib.orc_hook_inject.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32]
     lib.orc_hook_capture.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32]

@@ -45,6 +45,9 @@ EXPORTED = [
     "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
     "sifg_set_window", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
     "sifg_mesh_device_noalloc",
+    # the FP64 form
+    "sifg_cic_device_f64", "sifg_contrast_device_f64", "sifg_mesh_device_f64",
+    "sifg_smooth_device_f64", "sifg_exodus_device_f64", "sifg_box_device_f64",
 ]
 
 
@@ -59,6 +62,7 @@ def load():
     lib = C.CDLL(LIB_PATH)
     abi.bind_sif_api(lib)
     vp, u32, u64, f32, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_int
+    f64 = C.c_double
     sigs = {
         "sifg_cic_device": (i32, [vp, vp, vp, u64, u32, f32, vp]),
         "sifg_contrast_device": (i32, [vp, u64, C.POINTER(C.c_double)]),
@@ -75,6 +79,14 @@ def load():
         "sifg_launch_count": (u64, []),
         "sifg_mesh_device_noalloc": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]),
         "sifg_candidate_ranks": (None, [vp, u32, vp]),
+        "sifg_cic_device_f64": (i32, [vp, vp, vp, u64, u32, f64, vp]),
+        "sifg_contrast_device_f64": (i32, [vp, u64, C.POINTER(C.c_double)]),
+        "sifg_mesh_device_f64": (i32, [vp, vp, vp, u64, u32, f64, vp, vp, vp, vp, vp]),
+        "sifg_smooth_device_f64": (i32, [vp, u32, f64, f64, i32, i32, vp]),
+        "sifg_exodus_device_f64": (i32, [vp, u32, f64, vp, vp, vp, vp, u64, u32, vp, u32, f64,
+                                         f64, u32, vp, vp, vp, vp, vp, u64, C.POINTER(u64)]),
+        "sifg_box_device_f64": (i32, [vp, vp, vp, u64, u32, f64, u32, vp, u32, f64, f64, u32,
+                                      vp, vp, vp, vp, u64, C.POINTER(u64)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

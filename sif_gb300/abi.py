@@ -73,73 +73,6 @@ SIF_LOG_LEVEL_ERROR = 4
 SIF_LOG_LEVEL_NONE = 5
 
 
-class sif_field_t(C.Structure):
-    _fields_ = [
-        ("_position_block", P_real),
-        ("_velocity_block", P_real),
-        ("x", P_real), ("y", P_real), ("z", P_real),
-        ("vx", P_real), ("vy", P_real), ("vz", P_real),
-        ("weights", P_real),
-        ("original_indices", P_u64),
-        ("min_p", sif_real * 3),
-        ("max_p", sif_real * 3),
-        ("centre", sif_real * 3),
-        ("half_span", sif_real),
-        ("state_flags", C.c_uint32),
-        ("n_particles", C.c_uint64),
-        ("units", C.c_int),
-    ]
-
-
-class sif_grid_t(C.Structure):
-    _fields_ = [
-        ("values", P_real),
-        ("content", C.c_int),
-        ("assignment", C.c_int),
-        ("interlaced", C.c_uint32),
-        ("n_cells", C.c_uint32),
-        ("total_cells", C.c_uint64),
-        ("box_length", sif_real),
-        ("cell_length", sif_real),
-        ("p2_mask", C.c_uint32),
-        ("p2_shift", C.c_uint32),
-    ]
-
-
-class sif_chain_mesh_t(C.Structure):
-    _fields_ = [
-        ("n_cells", C.c_uint32),
-        ("total_cells", C.c_uint64),
-        ("box_length", sif_real),
-        ("cell_length", sif_real),
-        ("_position_block", P_real),
-        ("_velocity_block", P_real),
-        ("x", P_real), ("y", P_real), ("z", P_real),
-        ("vx", P_real), ("vy", P_real), ("vz", P_real),
-        ("weights", P_real),
-        ("total_weight", C.c_double),
-        ("cell_weights", P_real),
-        ("original_indices", P_u64),
-        ("n_particles", C.c_uint64),
-        ("cell_offsets", P_u64),
-    ]
-
-
-class sif_catalogue_t(C.Structure):
-    _fields_ = [
-        ("_block", P_real),
-        ("cx", P_real), ("cy", P_real), ("cz", P_real), ("radii", P_real),
-        ("_footprint_block", P_real),
-        ("footprint", P_real),
-        ("footprint_shell", P_real),
-        ("units", C.c_int),
-        ("_meta", C.c_void_p),
-        ("_n_meta", C.c_uint32),
-        ("n_voids", C.c_uint64),
-        ("capacity", C.c_uint64),
-    ]
-
-
 class sif_fft_config_t(C.Structure):
     _fields_ = [("skip_tuning", C.c_bool)]
 
@@ -162,25 +95,111 @@ class sif_config_t(C.Structure):
     ]
 
 
-class sif_finder_exodus_extras_t(C.Structure):
-    _fields_ = [
-        ("checkpoint", C.c_char_p),
-        ("prior", C.POINTER(sif_catalogue_t)),
-        ("keep_checkpoint", C.c_int),
-        ("save_memory", C.c_int),
-    ]
+def make_structs(real):
+    """The reference's public structs with sif_real = `real` (C.c_float for
+    the float build, C.c_double for its SIF_USE_DOUBLE build, whose struct
+    layouts differ where a sif_real field sits before a pointer)."""
+    sif_real = real
+    P_real = C.POINTER(real)
+
+    class sif_field_t(C.Structure):
+        _fields_ = [
+            ("_position_block", P_real),
+            ("_velocity_block", P_real),
+            ("x", P_real), ("y", P_real), ("z", P_real),
+            ("vx", P_real), ("vy", P_real), ("vz", P_real),
+            ("weights", P_real),
+            ("original_indices", P_u64),
+            ("min_p", sif_real * 3),
+            ("max_p", sif_real * 3),
+            ("centre", sif_real * 3),
+            ("half_span", sif_real),
+            ("state_flags", C.c_uint32),
+            ("n_particles", C.c_uint64),
+            ("units", C.c_int),
+        ]
 
 
-def bind_sif_api(lib):
+    class sif_grid_t(C.Structure):
+        _fields_ = [
+            ("values", P_real),
+            ("content", C.c_int),
+            ("assignment", C.c_int),
+            ("interlaced", C.c_uint32),
+            ("n_cells", C.c_uint32),
+            ("total_cells", C.c_uint64),
+            ("box_length", sif_real),
+            ("cell_length", sif_real),
+            ("p2_mask", C.c_uint32),
+            ("p2_shift", C.c_uint32),
+        ]
+
+
+    class sif_chain_mesh_t(C.Structure):
+        _fields_ = [
+            ("n_cells", C.c_uint32),
+            ("total_cells", C.c_uint64),
+            ("box_length", sif_real),
+            ("cell_length", sif_real),
+            ("_position_block", P_real),
+            ("_velocity_block", P_real),
+            ("x", P_real), ("y", P_real), ("z", P_real),
+            ("vx", P_real), ("vy", P_real), ("vz", P_real),
+            ("weights", P_real),
+            ("total_weight", C.c_double),
+            ("cell_weights", P_real),
+            ("original_indices", P_u64),
+            ("n_particles", C.c_uint64),
+            ("cell_offsets", P_u64),
+        ]
+
+
+    class sif_catalogue_t(C.Structure):
+        _fields_ = [
+            ("_block", P_real),
+            ("cx", P_real), ("cy", P_real), ("cz", P_real), ("radii", P_real),
+            ("_footprint_block", P_real),
+            ("footprint", P_real),
+            ("footprint_shell", P_real),
+            ("units", C.c_int),
+            ("_meta", C.c_void_p),
+            ("_n_meta", C.c_uint32),
+            ("n_voids", C.c_uint64),
+            ("capacity", C.c_uint64),
+        ]
+
+
+    class sif_finder_exodus_extras_t(C.Structure):
+        _fields_ = [
+            ("checkpoint", C.c_char_p),
+            ("prior", C.POINTER(sif_catalogue_t)),
+            ("keep_checkpoint", C.c_int),
+            ("save_memory", C.c_int),
+        ]
+
+    return sif_field_t, sif_grid_t, sif_chain_mesh_t, sif_catalogue_t, sif_finder_exodus_extras_t
+
+
+(sif_field_t, sif_grid_t, sif_chain_mesh_t, sif_catalogue_t,
+ sif_finder_exodus_extras_t) = make_structs(C.c_float)
+STRUCTS_F64 = make_structs(C.c_double)
+
+
+def bind_sif_api(lib, real=C.c_float):
     """Declares the signatures of sif's public C API on a loaded library.
 
     Used for both the reference build and the GB300 library, which export the
-    same entry points.
+    same entry points; real = C.c_double for the reference's double build.
     """
-    P_field = C.POINTER(sif_field_t)
-    P_grid = C.POINTER(sif_grid_t)
-    P_mesh = C.POINTER(sif_chain_mesh_t)
-    P_cat = C.POINTER(sif_catalogue_t)
+    field_t, grid_t, mesh_t, cat_t, extras_t = (
+        (sif_field_t, sif_grid_t, sif_chain_mesh_t, sif_catalogue_t, sif_finder_exodus_extras_t)
+        if real is C.c_float else STRUCTS_F64)
+    sif_real = real
+    P_real = C.POINTER(real)
+    P_field = C.POINTER(field_t)
+    P_grid = C.POINTER(grid_t)
+    P_mesh = C.POINTER(mesh_t)
+    P_cat = C.POINTER(cat_t)
     sigs = {
         "sif_system_init": (C.c_int, [C.POINTER(sif_config_t)]),
         "sif_system_finalise": (None, []),
@@ -198,10 +217,9 @@ def bind_sif_api(lib):
         "sif_chain_mesh_free": (None, [P_mesh]),
         "sif_catalogue_free": (None, [P_cat]),
         "sif_finder_exodus": (P_cat, [P_grid, P_mesh, P_real, C.c_uint32, sif_real,
-                                      C.c_int, C.POINTER(sif_finder_exodus_extras_t)]),
+                                      C.c_int, C.POINTER(extras_t)]),
         "sif_finder_exodus_raw": (P_cat, [P_grid, P_mesh, P_real, C.c_uint32, sif_real,
-                                          sif_real, C.c_uint32,
-                                          C.POINTER(sif_finder_exodus_extras_t)]),
+                                          sif_real, C.c_uint32, C.POINTER(extras_t)]),
         "sif_finder_exodus_preset": (C.c_int, [C.c_int, P_real, C.POINTER(C.c_uint32)]),
         "sif_finder_exodus_variant_name": (C.c_char_p, [C.c_int]),
         "sif_finder_exodus_variant_from_name": (C.c_int, [C.c_char_p, C.POINTER(C.c_int)]),

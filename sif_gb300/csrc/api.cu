@@ -83,7 +83,7 @@ static Engine* engine() {
 // --- device scratch for the C API's copies -------------------------------
 
 struct ApiBufs {
-  DevBuf px, py, pz, grid, mx, my, mz, offs, orig, bad, wide, mesh_sums;
+  DevBuf px, py, pz, grid, grid64, mx, my, mz, offs, orig, bad, wide, mesh_sums;
 };
 static ApiBufs& bufs() {
   static ApiBufs b;
@@ -95,13 +95,14 @@ static ApiBufs& bufs() {
 // reference compares in double against -tol and L + tol; a float v passes
 // those exactly when it passes the float bounds lo and hi found on the host
 // (the nearest floats inside them), so the kernel compares floats only.
-__global__ void box_check_kernel(const float* __restrict__ x, const float* __restrict__ y,
-                                 const float* __restrict__ z, uint64_t n, float box, float lo,
-                                 float hi, unsigned long long* __restrict__ out) {
+template <class R>
+__global__ void box_check_kernel(const R* __restrict__ x, const R* __restrict__ y,
+                                 const R* __restrict__ z, uint64_t n, R lo, R hi,
+                                 unsigned long long* __restrict__ out) {
   unsigned long long bad = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    const float v[3] = {x[i], y[i], z[i]};
+    const R v[3] = {x[i], y[i], z[i]};
     bool ok = true;
     for (int a = 0; a < 3; a++) ok = ok && v[a] >= lo && v[a] <= hi;  // false for NaN
     bad += ok ? 0u : 1u;
@@ -110,15 +111,30 @@ __global__ void box_check_kernel(const float* __restrict__ x, const float* __res
   if ((threadIdx.x & 31) == 0 && bad) atomicAdd(out, bad);
 }
 
-static int check_in_box(const float* dx, const float* dy, const float* dz, uint64_t n, float box,
+// The bounds: in the float form the nearest floats inside [-tol, L + tol];
+// in the FP64 form the double bounds themselves (tol of 4 DBL_EPSILON, the
+// SIF_USE_DOUBLE build's SIF__REAL_EPSILON).
+static void box_bounds(float box, float* lo, float* hi) {
+  const double tol = (double)box * 4.0 * (double)FLT_EPSILON;
+  *lo = (float)(-tol);
+  *hi = (float)((double)box + tol);
+  if ((double)*lo < -tol) *lo = std::nextafter(*lo, 0.0f);
+  if ((double)*hi > (double)box + tol) *hi = std::nextafter(*hi, 0.0f);
+}
+static void box_bounds(double box, double* lo, double* hi) {
+  const double tol = box * 4.0 * DBL_EPSILON;
+  *lo = -tol;
+  *hi = box + tol;
+}
+
+template <class R>
+static int check_in_box(const R* dx, const R* dy, const R* dz, uint64_t n, R box,
                         const char* name, cudaStream_t st) {
   unsigned long long* d = (unsigned long long*)bufs().bad.ensure(16);
   SIFG_CUDA(cudaMemsetAsync(d, 0, 16, st));
-  const double tol = (double)box * 4.0 * (double)FLT_EPSILON;
-  float lo = (float)(-tol), hi = (float)((double)box + tol);
-  if ((double)lo < -tol) lo = std::nextafter(lo, 0.0f);
-  if ((double)hi > (double)box + tol) hi = std::nextafter(hi, 0.0f);
-  box_check_kernel<<<grid_for(n, 256), 256, 0, st>>>(dx, dy, dz, n, box, lo, hi, d);
+  R lo, hi;
+  box_bounds(box, &lo, &hi);
+  box_check_kernel<R><<<grid_for(n, 256), 256, 0, st>>>(dx, dy, dz, n, lo, hi, d);
   SIFG_LAUNCH_CHECK();
   unsigned long long h[2];
   SIFG_CUDA(cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, st));
@@ -575,8 +591,11 @@ int sif_finder_exodus_variant_from_name(const char* name, sif_exodus_variant_t* 
 // The finder
 // ---------------------------------------------------------------------------
 
+}  // extern "C"
+
 // sif__finder_check_args, src/finder/utils.c:33-57.
-static int check_args(const sif_real* radii, uint32_t n_radii, sif_real threshold, sif_real f) {
+template <class R>
+static int check_args(const R* radii, uint32_t n_radii, R threshold, R f) {
   if (!radii || n_radii == 0) return fail(SIF_ERR_INVALID, "radii: none given");
   for (uint32_t i = 0; i < n_radii; i++)
     if (!(radii[i] > 0.0f) || !std::isfinite(radii[i]))
@@ -589,6 +608,8 @@ static int check_args(const sif_real* radii, uint32_t n_radii, sif_real threshol
     return fail(SIF_ERR_INVALID, fmt("overlap_fraction %g: not in [0, 1]", (double)f));
   return SIF_OK;
 }
+
+extern "C" {
 
 sif_catalogue_t* sif_finder_exodus(sif_grid_t* grid, const sif_chain_mesh_t* mesh,
                                    const sif_real* radii, uint32_t n_radii, sif_real threshold,
@@ -744,29 +765,38 @@ uint32_t sif_finder_grid_cells_from_size(uint64_t n_particles, sif_real box_leng
 // Part 2: device-resident entry points
 // ---------------------------------------------------------------------------
 
-int sifg_cic_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
-                    float box, float* grid) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  API_GUARD_BEGIN
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Device entry points, one template per stage for the float form and the
+// FP64 form (the reference's SIF_USE_DOUBLE build).
+// ---------------------------------------------------------------------------
+
+template <class R>
+static int cic_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n_grid, R box,
+                      R* grid) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   if (n_grid < 4) return fail(SIF_ERR_INVALID, "n_grid: expected at least 4");
   cudaStream_t s = e->stream();
   const int st = check_in_box(x, y, z, n, box, "field", s);
   if (st != SIF_OK) return st;
-  e->scratch.ensure(cic_scratch_bytes(n, n_grid));
   RunTimings tm;
-  cic_deposit(x, y, z, n, n_grid, box, grid, e->scratch.ptr, s, &tm.cic);
+  if constexpr (sizeof(R) == 4) {
+    e->scratch.ensure(cic_scratch_bytes(n, n_grid));
+    cic_deposit(x, y, z, n, n_grid, box, grid, e->scratch.ptr, s, &tm.cic);
+  } else {
+    e->scratch.ensure(cic_f64_scratch_bytes(n_grid));
+    cic_deposit_f64(x, y, z, n, n_grid, box, grid, e->scratch.ptr, s, &tm.cic);
+  }
   SIFG_CUDA(cudaStreamSynchronize(s));
   g_timings.cic_ms = tm.cic.total_ms();
   g_timings.cic_launches = tm.cic.launches();
   return SIF_OK;
-  API_GUARD_END(SIF_ERR_INVALID)
 }
 
-int sifg_contrast_device(float* grid, uint64_t total_cells, double* mean_out) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  API_GUARD_BEGIN
+template <class R>
+static int contrast_device(R* grid, uint64_t total_cells, double* mean_out) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   cudaStream_t s = e->stream();
@@ -777,64 +807,59 @@ int sifg_contrast_device(float* grid, uint64_t total_cells, double* mean_out) {
   if (!(mean > 0.0)) return fail(SIF_ERR_RANGE, fmt("grid: mean density %g (expected > 0)", mean));
   SIFG_CUDA(cudaStreamSynchronize(s));
   return SIF_OK;
-  API_GUARD_END(SIF_ERR_INVALID)
 }
 
-int sifg_mesh_device(const float* x, const float* y, const float* z, uint64_t n,
-                     uint32_t n_cells, float box, float* mx, float* my, float* mz,
-                     uint32_t* offsets, uint32_t* orig) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  API_GUARD_BEGIN
+template <class R>
+static int mesh_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n_cells, R box,
+                       R* mx, R* my, R* mz, uint32_t* offsets, uint32_t* orig) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   if (n_cells == 0 || !(box > 0.0f)) return fail(SIF_ERR_INVALID, "mesh: bad geometry");
   cudaStream_t s = e->stream();
   const int st = check_in_box(x, y, z, n, box, "field", s);
   if (st != SIF_OK) return st;
-  DeviceMesh m;
+  DeviceMeshT<R> m;
   m.n_cells = n_cells;
   m.box_length = box;
-  m.cell_length = box / (float)n_cells;
+  m.cell_length = box / (R)n_cells;
   m.x = mx;
   m.y = my;
   m.z = mz;
   m.offsets = offsets;
   m.orig = orig;
-  e->scratch.ensure(mesh_scratch_bytes(n, n_cells));
+  e->scratch.ensure(mesh_scratch_bytes(n, n_cells) * sizeof(R) / sizeof(float));
   RunTimings tm;
   mesh_build(x, y, z, n, m, e->scratch.ptr, s, &tm.mesh);
   SIFG_CUDA(cudaStreamSynchronize(s));
   g_timings.mesh_ms = tm.mesh.total_ms();
   g_timings.mesh_launches = tm.mesh.launches();
   return SIF_OK;
-  API_GUARD_END(SIF_ERR_INVALID)
 }
 
-int sifg_smooth_device(const float* delta, uint32_t n_grid, float box, float r, int filter,
-                       int window_mode, float* out) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  API_GUARD_BEGIN
+template <class R>
+static int smooth_device(const R* delta, uint32_t n_grid, R box, R r, int filter,
+                         int window_mode, R* out) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   cudaStream_t s = e->stream();
-  e->smoother.setup(n_grid, box, window_mode, s);
-  e->smoother.forward(delta);
+  SmootherT<R>& sm = e->smoother_for<R>();
+  sm.setup(n_grid, box, window_mode, s);
+  sm.forward(delta);
   RunTimings tm;
-  e->smoother.smooth(filter, r, 0.0f, out, &tm.filter);
+  sm.smooth(filter, r, R(0), out, &tm.filter);
   SIFG_CUDA(cudaStreamSynchronize(s));
   g_timings.filter_ms = tm.filter.total_ms();
   g_timings.filter_launches = tm.filter.launches();
   return SIF_OK;
-  API_GUARD_END(SIF_ERR_INVALID)
 }
 
-static int run_device(Engine* e, const float* delta, uint32_t n_grid, float box, DeviceMesh& m,
-                      const float* radii, uint32_t n_radii, float threshold, float overlap,
-                      uint32_t opt, const float* inject, float* cx, float* cy, float* cz, float* r,
-                      uint64_t capacity, uint64_t* n_voids, RunTimings& tm,
-                      cudaEvent_t mesh_ready = nullptr) {
+template <class R>
+static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceMeshT<R>& m,
+                      const R* radii, uint32_t n_radii, R threshold, R overlap, uint32_t opt,
+                      const R* inject, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
+                      uint64_t* n_voids, RunTimings& tm, cudaEvent_t mesh_ready = nullptr) {
   if (check_args(radii, n_radii, threshold, overlap) != SIF_OK) return g_status;
-  RunParams p;
+  RunParamsT<R> p;
   p.grid_n = n_grid;
   p.box = box;
   p.threshold = threshold;
@@ -845,7 +870,7 @@ static int run_device(Engine* e, const float* delta, uint32_t n_grid, float box,
   p.inject = inject;
   p.inject_on_device = true;
   p.mesh_ready = mesh_ready;
-  HostCatalogue cat;
+  HostCatalogueT<R> cat;
   g_stats.clear();
   const int st = e->exodus(delta, m, p, cat, &g_stats, &tm);
   if (st != SIF_OK) return st;
@@ -853,47 +878,43 @@ static int run_device(Engine* e, const float* delta, uint32_t n_grid, float box,
   if (n_voids) *n_voids = nv;
   const uint64_t w = nv < capacity ? nv : capacity;
   if (w) {
-    memcpy(cx, cat.cx.data(), w * 4);
-    memcpy(cy, cat.cy.data(), w * 4);
-    memcpy(cz, cat.cz.data(), w * 4);
-    memcpy(r, cat.r.data(), w * 4);
+    memcpy(cx, cat.cx.data(), w * sizeof(R));
+    memcpy(cy, cat.cy.data(), w * sizeof(R));
+    memcpy(cz, cat.cz.data(), w * sizeof(R));
+    memcpy(r, cat.r.data(), w * sizeof(R));
   }
   return SIF_OK;
 }
 
-int sifg_exodus_device(const float* delta, uint32_t n_grid, float box, const float* mx,
-                       const float* my, const float* mz, const uint32_t* offsets,
-                       uint64_t n_particles, uint32_t mesh_cells, const float* radii,
-                       uint32_t n_radii, float threshold, float overlap, uint32_t opt,
-                       const float* inject, float* cx, float* cy, float* cz, float* r,
-                       uint64_t capacity, uint64_t* n_voids) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  API_GUARD_BEGIN
+template <class R>
+static int exodus_device(const R* delta, uint32_t n_grid, R box, const R* mx, const R* my,
+                         const R* mz, const uint32_t* offsets, uint64_t n_particles,
+                         uint32_t mesh_cells, const R* radii, uint32_t n_radii, R threshold,
+                         R overlap, uint32_t opt, const R* inject, R* cx, R* cy, R* cz, R* r,
+                         uint64_t capacity, uint64_t* n_voids) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
-  DeviceMesh m;
+  DeviceMeshT<R> m;
   m.n_cells = mesh_cells;
   m.box_length = box;
-  m.cell_length = box / (float)mesh_cells;
+  m.cell_length = box / (R)mesh_cells;
   m.n_particles = n_particles;
-  m.x = const_cast<float*>(mx);
-  m.y = const_cast<float*>(my);
-  m.z = const_cast<float*>(mz);
+  m.x = const_cast<R*>(mx);
+  m.y = const_cast<R*>(my);
+  m.z = const_cast<R*>(mz);
   m.offsets = const_cast<uint32_t*>(offsets);
   RunTimings tm;
   const int st = run_device(e, delta, n_grid, box, m, radii, n_radii, threshold, overlap, opt,
                             inject, cx, cy, cz, r, capacity, n_voids, tm);
   record_timings(tm);
   return st;
-  API_GUARD_END(SIF_ERR_INVALID)
 }
 
-int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
-                    float box, uint32_t mesh_cells, const float* radii, uint32_t n_radii,
-                    float threshold, float overlap, uint32_t opt, float* cx, float* cy,
-                    float* cz, float* r, uint64_t capacity, uint64_t* n_voids) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  API_GUARD_BEGIN
+template <class R>
+static int box_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n_grid, R box,
+                      uint32_t mesh_cells, const R* radii, uint32_t n_radii, R threshold,
+                      R overlap, uint32_t opt, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
+                      uint64_t* n_voids) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   if (n_grid < 4 || mesh_cells == 0) return fail(SIF_ERR_INVALID, "grid or mesh: bad size");
@@ -903,10 +924,16 @@ int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, 
   if (st != SIF_OK) return st;
   const uint64_t cells = (uint64_t)n_grid * n_grid * n_grid;
   const uint64_t mcells = (uint64_t)mesh_cells * mesh_cells * mesh_cells;
-  float* dg = (float*)bufs().grid.ensure(cells * 4);
+  R* dg = (R*)(sizeof(R) == 4 ? bufs().grid : bufs().grid64).ensure(cells * sizeof(R));
   RunTimings tm;
-  e->scratch.ensure(std::max(cic_scratch_bytes(n, n_grid), mesh_scratch_bytes(n, mesh_cells)));
-  cic_deposit(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic);
+  const size_t mesh_scratch = mesh_scratch_bytes(n, mesh_cells) * sizeof(R) / sizeof(float);
+  if constexpr (sizeof(R) == 4) {
+    e->scratch.ensure(std::max(cic_scratch_bytes(n, n_grid), mesh_scratch));
+    cic_deposit(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic);
+  } else {
+    e->scratch.ensure(std::max(cic_f64_scratch_bytes(n_grid), mesh_scratch));
+    cic_deposit_f64(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic);
+  }
   // The mesh is built on the copy stream (its own scan scratch) while the
   // contrast is taken and the first rungs are smoothed; the run waits for it
   // before its first sphere growth.
@@ -917,13 +944,13 @@ int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, 
     cudaStream_t s;
     ~CopyDrain() { cudaStreamSynchronize(s); }
   } drain{cs};
-  DeviceMesh m;
+  DeviceMeshT<R> m;
   m.n_cells = mesh_cells;
   m.box_length = box;
-  m.cell_length = box / (float)mesh_cells;
-  m.x = (float*)bufs().mx.ensure(n * 4);
-  m.y = (float*)bufs().my.ensure(n * 4);
-  m.z = (float*)bufs().mz.ensure(n * 4);
+  m.cell_length = box / (R)mesh_cells;
+  m.x = (R*)bufs().mx.ensure(n * sizeof(R));
+  m.y = (R*)bufs().my.ensure(n * sizeof(R));
+  m.z = (R*)bufs().mz.ensure(n * sizeof(R));
   m.offsets = (uint32_t*)bufs().offs.ensure((mcells + 1) * 4);
   m.orig = nullptr;
   uint32_t* sums = (uint32_t*)bufs().mesh_sums.ensure(
@@ -932,12 +959,87 @@ int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, 
   SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
   double* cscratch = (double*)bufs().bad.ensure(density_contrast_scratch_bytes() + 64);
   density_contrast(dg, cells, cscratch, s);
-  st = run_device(e, dg, n_grid, box, m, radii, n_radii, threshold, overlap, opt, nullptr, cx, cy,
-                  cz, r, capacity, n_voids, tm, e->ev_mesh_ready());
+  st = run_device(e, dg, n_grid, box, m, radii, n_radii, threshold, overlap, opt, (const R*)nullptr,
+                  cx, cy, cz, r, capacity, n_voids, tm, e->ev_mesh_ready());
   tm.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   record_timings(tm);
   return st;
+}
+
+extern "C" {
+
+#define SIFG_LOCKED(call)               \
+  std::lock_guard<std::mutex> lk(g_mu); \
+  API_GUARD_BEGIN                       \
+  return call;                          \
   API_GUARD_END(SIF_ERR_INVALID)
+
+int sifg_cic_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
+                    float box, float* grid) {
+  SIFG_LOCKED(cic_device(x, y, z, n, n_grid, box, grid))
+}
+int sifg_cic_device_f64(const double* x, const double* y, const double* z, uint64_t n,
+                        uint32_t n_grid, double box, double* grid) {
+  SIFG_LOCKED(cic_device(x, y, z, n, n_grid, box, grid))
+}
+int sifg_contrast_device(float* grid, uint64_t total_cells, double* mean_out) {
+  SIFG_LOCKED(contrast_device(grid, total_cells, mean_out))
+}
+int sifg_contrast_device_f64(double* grid, uint64_t total_cells, double* mean_out) {
+  SIFG_LOCKED(contrast_device(grid, total_cells, mean_out))
+}
+int sifg_mesh_device(const float* x, const float* y, const float* z, uint64_t n,
+                     uint32_t n_cells, float box, float* mx, float* my, float* mz,
+                     uint32_t* offsets, uint32_t* orig) {
+  SIFG_LOCKED(mesh_device(x, y, z, n, n_cells, box, mx, my, mz, offsets, orig))
+}
+int sifg_mesh_device_f64(const double* x, const double* y, const double* z, uint64_t n,
+                         uint32_t n_cells, double box, double* mx, double* my, double* mz,
+                         uint32_t* offsets, uint32_t* orig) {
+  SIFG_LOCKED(mesh_device(x, y, z, n, n_cells, box, mx, my, mz, offsets, orig))
+}
+int sifg_smooth_device(const float* delta, uint32_t n_grid, float box, float r, int filter,
+                       int window_mode, float* out) {
+  SIFG_LOCKED(smooth_device(delta, n_grid, box, r, filter, window_mode, out))
+}
+int sifg_smooth_device_f64(const double* delta, uint32_t n_grid, double box, double r,
+                           int filter, int window_mode, double* out) {
+  SIFG_LOCKED(smooth_device(delta, n_grid, box, r, filter, window_mode, out))
+}
+int sifg_exodus_device(const float* delta, uint32_t n_grid, float box, const float* mx,
+                       const float* my, const float* mz, const uint32_t* offsets,
+                       uint64_t n_particles, uint32_t mesh_cells, const float* radii,
+                       uint32_t n_radii, float threshold, float overlap, uint32_t opt,
+                       const float* inject, float* cx, float* cy, float* cz, float* r,
+                       uint64_t capacity, uint64_t* n_voids) {
+  SIFG_LOCKED(exodus_device(delta, n_grid, box, mx, my, mz, offsets, n_particles, mesh_cells,
+                            radii, n_radii, threshold, overlap, opt, inject, cx, cy, cz, r,
+                            capacity, n_voids))
+}
+int sifg_exodus_device_f64(const double* delta, uint32_t n_grid, double box, const double* mx,
+                           const double* my, const double* mz, const uint32_t* offsets,
+                           uint64_t n_particles, uint32_t mesh_cells, const double* radii,
+                           uint32_t n_radii, double threshold, double overlap, uint32_t opt,
+                           const double* inject, double* cx, double* cy, double* cz, double* r,
+                           uint64_t capacity, uint64_t* n_voids) {
+  SIFG_LOCKED(exodus_device(delta, n_grid, box, mx, my, mz, offsets, n_particles, mesh_cells,
+                            radii, n_radii, threshold, overlap, opt, inject, cx, cy, cz, r,
+                            capacity, n_voids))
+}
+int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
+                    float box, uint32_t mesh_cells, const float* radii, uint32_t n_radii,
+                    float threshold, float overlap, uint32_t opt, float* cx, float* cy,
+                    float* cz, float* r, uint64_t capacity, uint64_t* n_voids) {
+  SIFG_LOCKED(box_device(x, y, z, n, n_grid, box, mesh_cells, radii, n_radii, threshold, overlap,
+                         opt, cx, cy, cz, r, capacity, n_voids))
+}
+int sifg_box_device_f64(const double* x, const double* y, const double* z, uint64_t n,
+                        uint32_t n_grid, double box, uint32_t mesh_cells, const double* radii,
+                        uint32_t n_radii, double threshold, double overlap, uint32_t opt,
+                        double* cx, double* cy, double* cz, double* r, uint64_t capacity,
+                        uint64_t* n_voids) {
+  SIFG_LOCKED(box_device(x, y, z, n, n_grid, box, mesh_cells, radii, n_radii, threshold, overlap,
+                         opt, cx, cy, cz, r, capacity, n_voids))
 }
 
 uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {

@@ -263,13 +263,98 @@ __global__ void face_fixup_kernel(CicGeom g, float inv_cell_vol, float* __restri
 }
 
 // ---------------------------------------------------------------------------
+// The FP64 form's deposit (the reference's SIF_USE_DOUBLE build): the cell
+// coordinate u = fold(x) * (N / L), its base cell and fraction, and the eight
+// weights in double as grid.c:585-650 computes them. Each weight is rounded to
+// a multiple of 2^-40 of a particle (the remainder to the largest, so the
+// eight sum to exactly one particle) and summed as int64 with global atomics:
+// the grid is exact to 2^-40 per particle and independent of the order the
+// additions land in. One thread per particle, no tiling: this is the plain
+// form the float path is measured against.
+// ---------------------------------------------------------------------------
+constexpr double kQ64 = 1099511627776.0;  // 2^40
+
+__device__ __forceinline__ void cic_axis_f64(double v, uint32_t n, double box, double idx,
+                                             uint32_t& c0, uint32_t& c1, double& t) {
+  const double u = fmul(box_fold(v, box), idx);
+  const uint32_t raw = (uint32_t)u;
+  c0 = raw >= n ? 0u : raw;
+  c1 = c0 + 1 == n ? 0u : c0 + 1;
+  t = fsub(u, (double)raw);
+}
+
+__global__ void cic_f64_kernel(const double* __restrict__ x, const double* __restrict__ y,
+                               const double* __restrict__ z, uint64_t np, uint32_t n, double box,
+                               double idx, unsigned long long* __restrict__ acc) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    uint32_t x0, x1, y0, y1, z0, z1;
+    double tx, ty, tz;
+    cic_axis_f64(x[p], n, box, idx, x0, x1, tx);
+    cic_axis_f64(y[p], n, box, idx, y0, y1, ty);
+    cic_axis_f64(z[p], n, box, idx, z0, z1, tz);
+    const double wx0 = fsub(1.0, tx), wy0 = fsub(1.0, ty), wz0 = fsub(1.0, tz);
+    const double w00 = fmul(wx0, wy0), w01 = fmul(wx0, ty), w10 = fmul(tx, wy0),
+                 w11 = fmul(tx, ty);
+    const double w[8] = {fmul(w00, wz0), fmul(w00, tz), fmul(w01, wz0), fmul(w01, tz),
+                         fmul(w10, wz0), fmul(w10, tz), fmul(w11, wz0), fmul(w11, tz)};
+    long long q[8];
+    long long sum = 0;
+    int big = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      q[k] = __double2ll_rn(fmul(w[k], kQ64));
+      sum += q[k];
+      if (w[k] > w[big]) big = k;
+    }
+    const long long fix = (long long)kQ64 - sum;
+    const uint32_t xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const long long v = q[k] + (k == big ? fix : 0);
+      if (v == 0) continue;
+      const uint64_t c = ((uint64_t)xs[k >> 2] * n + ys[(k >> 1) & 1]) * n + zs[k & 1];
+      atomicAdd(acc + c, (unsigned long long)v);
+    }
+  }
+}
+
+__global__ void cic_f64_finish_kernel(const unsigned long long* __restrict__ acc, uint64_t cells,
+                                      double inv_cell_vol, double* __restrict__ grid) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cells; i += stride)
+    grid[i] = fmul(fmul(__ull2double_rn(acc[i]), 1.0 / kQ64), inv_cell_vol);
+}
+
+size_t cic_f64_scratch_bytes(uint32_t n) { return (size_t)n * n * n * sizeof(unsigned long long) + 256; }
+
+void cic_deposit_f64(const double* x, const double* y, const double* z, uint64_t n_particles,
+                     uint32_t n, double box, double* grid, void* scratch, cudaStream_t st,
+                     KernelTimer* timer) {
+  const uint64_t cells = (uint64_t)n * n * n;
+  unsigned long long* acc = (unsigned long long*)scratch;
+  SIFG_CUDA(cudaMemsetAsync(acc, 0, cells * sizeof(unsigned long long), st));
+  // grid.c:684 and 735-737 in double.
+  const double idx = (double)n / box;
+  const double cl = box / (double)n;
+  const double inv_cell_vol = 1.0f / (double)(cl * cl * cl);
+  if (timer) timer->begin(st);
+  cic_f64_kernel<<<grid_for(n_particles, 256), 256, 0, st>>>(x, y, z, n_particles, n, box, idx, acc);
+  SIFG_LAUNCH_CHECK();
+  if (timer) timer->end(st);
+  cic_f64_finish_kernel<<<grid_for(cells, 256), 256, 0, st>>>(acc, cells, inv_cell_vol, grid);
+  SIFG_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
 // Density contrast: the mean in double over fixed blocks (a fixed launch, so
 // the summation order and the result never change), then v * inv - 1.
 // ---------------------------------------------------------------------------
 constexpr int kMeanBlocks = 1024;
 constexpr int kMeanThreads = 256;
 
-__global__ void __launch_bounds__(kMeanThreads) mean_partial_kernel(const float* __restrict__ v,
+template <class R>
+__global__ void __launch_bounds__(kMeanThreads) mean_partial_kernel(const R* __restrict__ v,
                                                                     uint64_t n,
                                                                     double* __restrict__ partial) {
   __shared__ double s[kMeanThreads];
@@ -296,13 +381,13 @@ __global__ void mean_final_kernel(const double* __restrict__ partial, uint64_t n
   }
 }
 
-__global__ void contrast_kernel(float* __restrict__ v, uint64_t n,
-                                const double* __restrict__ mean) {
+template <class R>
+__global__ void contrast_kernel(R* __restrict__ v, uint64_t n, const double* __restrict__ mean) {
   const double m = mean[0];
-  const float inv = (float)(1.0 / m);
+  const R inv = (R)(1.0 / m);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    v[i] = fsub(fmul(v[i], inv), 1.0f);
+    v[i] = fsub(fmul(v[i], inv), R(1.0f));
 }
 
 // ---------------------------------------------------------------------------
@@ -381,15 +466,18 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   SIFG_LAUNCH_CHECK();
 }
 
-void density_contrast(float* v, uint64_t n, double* d_scratch, cudaStream_t st) {
+template <class R>
+void density_contrast(R* v, uint64_t n, double* d_scratch, cudaStream_t st) {
   // d_scratch: kMeanBlocks + 1 doubles.
-  mean_partial_kernel<<<kMeanBlocks, kMeanThreads, 0, st>>>(v, n, d_scratch);
+  mean_partial_kernel<R><<<kMeanBlocks, kMeanThreads, 0, st>>>(v, n, d_scratch);
   SIFG_LAUNCH_CHECK();
   mean_final_kernel<<<1, 32, 0, st>>>(d_scratch, n, d_scratch + kMeanBlocks);
   SIFG_LAUNCH_CHECK();
-  contrast_kernel<<<grid_for(n, 256), 256, 0, st>>>(v, n, d_scratch + kMeanBlocks);
+  contrast_kernel<R><<<grid_for(n, 256), 256, 0, st>>>(v, n, d_scratch + kMeanBlocks);
   SIFG_LAUNCH_CHECK();
 }
+template void density_contrast<float>(float*, uint64_t, double*, cudaStream_t);
+template void density_contrast<double>(double*, uint64_t, double*, cudaStream_t);
 
 size_t density_contrast_scratch_bytes() { return (kMeanBlocks + 1) * sizeof(double); }
 

@@ -29,7 +29,9 @@
 
 namespace sifg {
 
-static constexpr float kPiF = (float)3.14159265358979323846;
+// SIF_PI, include/sif/core/macros.h:542.
+template <class R>
+static constexpr R kPi = (R)3.14159265358979323846;
 static constexpr uint32_t kOptSeedsMinima = 1u << 9;
 static constexpr uint32_t kOptKeepWindow = 1u << 14;
 static constexpr uint32_t kOptAliasing = 1u << 8;
@@ -77,7 +79,7 @@ void Engine::ensure_host(size_t m) {
   cudaFreeHost(h_flat_);
   cudaFreeHost(h_rank_);
   const size_t cap = m + m / 4 + 1024;
-  SIFG_CUDA(cudaMallocHost(&h_delta_, cap * sizeof(float)));
+  SIFG_CUDA(cudaMallocHost(&h_delta_, cap * sizeof(double)));
   SIFG_CUDA(cudaMallocHost(&h_flat_, cap * sizeof(uint32_t)));
   SIFG_CUDA(cudaMallocHost(&h_rank_, cap * sizeof(uint32_t)));
   h_cap_ = cap;
@@ -89,8 +91,9 @@ void Engine::ensure_host(size_t m) {
 
 namespace {
 
+template <class K>
 struct Rec {
-  float d;
+  K d;
   uint32_t i;
 };
 
@@ -98,11 +101,12 @@ struct Rec {
 // middle element's key; scanning from the left, a smaller key is exchanged to
 // the low end, a larger one with the high end (and examined again), an equal
 // one is passed over.
-inline void partition3(Rec* a, int64_t lo, int64_t hi, int64_t* lt_out, int64_t* gt_out) {
-  const float pivot = a[lo + (hi - lo) / 2].d;
+template <class K>
+inline void partition3(Rec<K>* a, int64_t lo, int64_t hi, int64_t* lt_out, int64_t* gt_out) {
+  const K pivot = a[lo + (hi - lo) / 2].d;
   int64_t lt = lo, i = lo, gt = hi;
   while (i <= gt) {
-    const float v = a[i].d;
+    const K v = a[i].d;
     if (v < pivot) {
       std::swap(a[lt], a[i]);
       lt++;
@@ -118,7 +122,8 @@ inline void partition3(Rec* a, int64_t lo, int64_t hi, int64_t* lt_out, int64_t*
   *gt_out = gt;
 }
 
-void qsort_serial(Rec* a, int64_t lo, int64_t hi) {
+template <class K>
+void qsort_serial(Rec<K>* a, int64_t lo, int64_t hi) {
   std::vector<std::pair<int64_t, int64_t>> stack;
   stack.emplace_back(lo, hi);
   while (!stack.empty()) {
@@ -139,7 +144,8 @@ void qsort_serial(Rec* a, int64_t lo, int64_t hi) {
 // bounds its task overhead.
 constexpr int64_t kTaskCutoff = 4096;
 
-void qsort_tasks(Rec* a, int64_t lo, int64_t hi) {
+template <class K>
+void qsort_tasks(Rec<K>* a, int64_t lo, int64_t hi) {
   if (hi - lo < kTaskCutoff) {
     qsort_serial(a, lo, hi);
     return;
@@ -153,9 +159,10 @@ void qsort_tasks(Rec* a, int64_t lo, int64_t hi) {
 
 }  // namespace
 
-void candidate_ranks(const float* delta, uint32_t m, uint32_t* rank, int threads) {
-  std::vector<Rec> a(m);
-  for (uint32_t k = 0; k < m; k++) a[k] = Rec{delta[k], k};
+template <class K>
+void candidate_ranks(const K* delta, uint32_t m, uint32_t* rank, int threads) {
+  std::vector<Rec<K>> a(m);
+  for (uint32_t k = 0; k < m; k++) a[k] = Rec<K>{delta[k], k};
   if (m > 8 * (uint32_t)kTaskCutoff && threads != 1) {
     const int t = threads > 0 ? threads : omp_get_max_threads();
 #pragma omp parallel num_threads(t)
@@ -167,29 +174,32 @@ void candidate_ranks(const float* delta, uint32_t m, uint32_t* rank, int threads
   for (uint32_t k = 0; k < m; k++) rank[a[k].i] = k;
 }
 
+template void candidate_ranks<float>(const float*, uint32_t, uint32_t*, int);
+template void candidate_ranks<double>(const double*, uint32_t, uint32_t*, int);
+
 // ---------------------------------------------------------------------------
 // The template
 // ---------------------------------------------------------------------------
 
-int build_template(HostTemplate& t, uint32_t mesh_n, float cell_length, float rmin,
-                   float r_search) {
-  t = HostTemplate();
+template <class R>
+int build_template(HostTemplateT<R>& t, uint32_t mesh_n, R cell_length, R rmin, R r_search) {
+  t = HostTemplateT<R>();
   const int32_t cr = (int32_t)(r_search / cell_length) + 1;
   if (cr >= (int32_t)mesh_n) return kErrRange;
-  const float rs2 = r_search * r_search;
-  const float rc2 = rmin * rmin;
+  const R rs2 = r_search * r_search;
+  const R rc2 = rmin * rmin;
   for (int32_t dx = -cr; dx <= cr; dx++)
     for (int32_t dy = -cr; dy <= cr; dy++)
       for (int32_t dz = -cr; dz <= cr; dz++) {
-        const float mnx = dx == 0 ? 0.0f : (std::fabs((float)dx) - 1.0f) * cell_length;
-        const float mny = dy == 0 ? 0.0f : (std::fabs((float)dy) - 1.0f) * cell_length;
-        const float mnz = dz == 0 ? 0.0f : (std::fabs((float)dz) - 1.0f) * cell_length;
-        const float mn = mnx * mnx + mny * mny + mnz * mnz;
+        const R mnx = dx == 0 ? 0.0f : (std::fabs((R)dx) - 1.0f) * cell_length;
+        const R mny = dy == 0 ? 0.0f : (std::fabs((R)dy) - 1.0f) * cell_length;
+        const R mnz = dz == 0 ? 0.0f : (std::fabs((R)dz) - 1.0f) * cell_length;
+        const R mn = mnx * mnx + mny * mny + mnz * mnz;
         if (mn > rs2) continue;
-        const float mxx = (std::fabs((float)dx) + 1.0f) * cell_length;
-        const float mxy = (std::fabs((float)dy) + 1.0f) * cell_length;
-        const float mxz = (std::fabs((float)dz) + 1.0f) * cell_length;
-        const float mx = mxx * mxx + mxy * mxy + mxz * mxz;
+        const R mxx = (std::fabs((R)dx) + 1.0f) * cell_length;
+        const R mxy = (std::fabs((R)dy) + 1.0f) * cell_length;
+        const R mxz = (std::fabs((R)dz) + 1.0f) * cell_length;
+        const R mx = mxx * mxx + mxy * mxy + mxz * mxz;
         t.dx.push_back(dx);
         t.dy.push_back(dy);
         t.dz.push_back(dz);
@@ -207,6 +217,9 @@ int build_template(HostTemplate& t, uint32_t mesh_n, float cell_length, float rm
   return kOk;
 }
 
+template int build_template<float>(HostTemplateT<float>&, uint32_t, float, float, float);
+template int build_template<double>(HostTemplateT<double>&, uint32_t, double, double, double);
+
 // ---------------------------------------------------------------------------
 // The run
 // ---------------------------------------------------------------------------
@@ -216,14 +229,16 @@ static T* grow_to(DevBuf& b, size_t n) {
   return (T*)b.ensure(n * sizeof(T));
 }
 
-int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams& p,
-                   HostCatalogue& out, std::vector<RungStat>* stats, RunTimings* tm) {
+template <class R>
+int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParamsT<R>& p,
+                   HostCatalogueT<R>& out, std::vector<RungStat>* stats, RunTimings* tm) {
+  SmootherT<R>& smoother = smoother_for<R>();
   const auto t_start = std::chrono::steady_clock::now();
   const uint32_t N = p.grid_n;
   const uint64_t cells = (uint64_t)N * N * N;
-  const float box = p.box;
-  const float cell = box / (float)N;
-  const float threshold = p.threshold, f = p.overlap;
+  const R box = p.box;
+  const R cell = box / (R)N;
+  const R threshold = p.threshold, f = p.overlap;
   const uint32_t opt = p.options;
   if (opt & (kOptSeedsMinima | kOptRefineMask | kOptExtendReach | kOptDisplace)) {
     set_error(kErrUnsupported,
@@ -235,15 +250,15 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     set_error(kErrRange, "grid: more than 2^32 cells");
     return kErrRange;
   }
-  const float scale = (opt & kOptLagrangian) ? (float)std::cbrt(1.0 + (double)threshold) : 1.0f;
-  static const float factors[4] = {1.5f, 1.25f, 1.75f, 2.0f};
-  const float search_factor = factors[(opt >> 12) & 3u];
+  const R scale = (opt & kOptLagrangian) ? (R)std::cbrt(1.0 + (double)threshold) : 1.0f;
+  static const R factors[4] = {1.5f, 1.25f, 1.75f, 2.0f};
+  const R search_factor = factors[(opt >> 12) & 3u];
   const int window_mode = (opt & kOptKeepWindow) ? 0 : ((opt & kOptAliasing) ? 2 : 1);
 
-  std::vector<float> radii = p.radii;
-  std::sort(radii.begin(), radii.end(), [](float a, float b) { return a > b; });
+  std::vector<R> radii = p.radii;
+  std::sort(radii.begin(), radii.end(), [](R a, R b) { return a > b; });
 
-  float* fields[2] = {grow_to<float>(field_[0], cells), grow_to<float>(field_[1], cells)};
+  R* fields[2] = {grow_to<R>(field_[0], cells), grow_to<R>(field_[1], cells)};
   uint32_t* mask = grow_to<uint32_t>(mask_, (cells + 31) / 32);
   SIFG_CUDA(cudaMemsetAsync(mask, 0, ((cells + 31) / 32) * sizeof(uint32_t), st_));
   // The smoothing stream starts after everything queued on the run's stream
@@ -269,9 +284,9 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   }
 
   // Loop invariants, exodus_finder.c:1629-1632.
-  const float box_volume = box * box * box;
-  const float mean_density = (float)mesh.n_particles / box_volume;
-  const float vol_factor = (4.0f / 3.0f) * kPiF * mean_density;
+  const R box_volume = box * box * box;
+  const R mean_density = (R)mesh.n_particles / box_volume;
+  const R vol_factor = (4.0f / 3.0f) * kPi<R> * mean_density;
 
   uint32_t n_voids = 0;
   size_t cat_cap = 0;
@@ -281,13 +296,13 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     DevBuf* bufs[4] = {&cat_x_, &cat_y_, &cat_z_, &cat_r_};
     for (DevBuf* b : bufs) {
       void* fresh = nullptr;
-      SIFG_CUDA(cudaMalloc(&fresh, cap * sizeof(float)));
+      SIFG_CUDA(cudaMalloc(&fresh, cap * sizeof(R)));
       if (n_voids)
-        SIFG_CUDA(cudaMemcpyAsync(fresh, b->ptr, n_voids * sizeof(float), cudaMemcpyDeviceToDevice, st_));
+        SIFG_CUDA(cudaMemcpyAsync(fresh, b->ptr, n_voids * sizeof(R), cudaMemcpyDeviceToDevice, st_));
       SIFG_CUDA(cudaStreamSynchronize(st_));
       b->release();
       b->ptr = fresh;
-      b->bytes = cap * sizeof(float);
+      b->bytes = cap * sizeof(R);
     }
     vids_.ensure(cap * sizeof(uint32_t));
     vcell_.ensure(cap * sizeof(uint32_t));
@@ -296,10 +311,10 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   ensure_cat(1 << 16);
   const uint32_t vcells = kVoidCells * kVoidCells * kVoidCells;
   uint32_t* vstart = grow_to<uint32_t>(vstart_, vcells + 1);
-  build_void_index(cat_x_.as<float>(), cat_y_.as<float>(), cat_z_.as<float>(), 0, box, vstart,
+  build_void_index(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), 0, box, vstart,
                    vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
-  float max_r = 0.0f;
-  float* gbuf = grow_to<float>(gbuf_, (size_t)growth_grid() * kGrowCap);
+  R max_r = 0.0f;
+  R* gbuf = grow_to<R>(gbuf_, (size_t)growth_grid() * kGrowCap);
   uint32_t* dcount = grow_to<uint32_t>(dcount_, 16);
   // Gathered particles and visited cells of each rung's sphere growth.
   const size_t n_rungs = radii.size();
@@ -309,7 +324,7 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   const uint32_t nb_scan = scan_blocks(cells);
   uint32_t* blocks = grow_to<uint32_t>(blocks_, (size_t)std::max<uint64_t>(nb_scan + 1, 1024));
 
-  MeshView mv{mesh.x, mesh.y, mesh.z, mesh.offsets, (int32_t)mesh.n_cells, mesh.box_length,
+  MeshViewT<R> mv{mesh.x, mesh.y, mesh.z, mesh.offsets, (int32_t)mesh.n_cells, mesh.box_length,
               1.0f / mesh.cell_length};
 
   bool mesh_waited = false;
@@ -320,14 +335,14 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   for (uint32_t ri = 0; ri < radii.size(); ri++) {
     const auto t_rung = clk::now();
     RungStat rs;
-    const float radius = radii[ri];
+    const R radius = radii[ri];
     rs.radius = radius;
 
     // 1. The rung's field; the next rung's smoothing queued behind this
     //    rung's last read of the buffer it overwrites.
-    float* field = fields[ri % 2];
+    R* field = fields[ri % 2];
     if (p.inject) {
-      SIFG_CUDA(cudaMemcpyAsync(field, p.inject + (uint64_t)ri * cells, cells * sizeof(float),
+      SIFG_CUDA(cudaMemcpyAsync(field, p.inject + (uint64_t)ri * cells, cells * sizeof(R),
                                 p.inject_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                 st_));
     } else {
@@ -346,8 +361,8 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
 
     // The reach and the rescaling's constants (exodus_finder.c:1771-1817,
     // exodus_rescale.c:681-720, 894-908).
-    const float rmin = 1.0f * radius;
-    float r_search = radius + std::fmax((search_factor - 1.0f) * radius, 3.0f * cell);
+    const R rmin = 1.0f * radius;
+    R r_search = radius + std::fmax((search_factor - 1.0f) * radius, 3.0f * cell);
     if (ri > 0 && radii[ri - 1] > r_search) r_search = radii[ri - 1];
     rs.r_search = r_search;
     if (m == 0) {
@@ -357,35 +372,35 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
       continue;
     }
 
-    float* cdelta = grow_to<float>(cand_delta_, m);
+    R* cdelta = grow_to<R>(cand_delta_, m);
     uint32_t* cflat = grow_to<uint32_t>(cand_flat_, m);
     scan_write_pass(field, mask, cells, threshold, blocks, cdelta, cflat, st_);
     SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
     ensure_host(m);
-    SIFG_CUDA(cudaMemcpyAsync(h_delta_, cdelta, m * sizeof(float), cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaMemcpyAsync(h_delta_, cdelta, m * sizeof(R), cudaMemcpyDeviceToHost, st_));
     SIFG_CUDA(cudaEventRecord(ev_cand_, st_));
 
-    RungConsts rc;
+    RungConstsT<R> rc;
     rc.radius = radius;
     rc.r_search = r_search;
     rc.rmin = rmin;
     rc.rs2 = r_search * r_search;
     rc.rc2 = rmin * rmin;
-    const float span = rc.rs2 - rc.rc2;
+    const R span = rc.rs2 - rc.rc2;
     uint32_t nb = 2048u;
     {
-      const float expected_shell =
+      const R expected_shell =
           vol_factor * (r_search * r_search * r_search - rmin * rmin * rmin);
-      const float want = expected_shell / 16.0f;
+      const R want = expected_shell / 16.0f;
       if (!(want >= 64.0f))
         nb = 64u;
       else if (want < 2048.0f)
         nb = (uint32_t)want;
     }
     rc.nb = nb;
-    rc.inv_w = (float)nb / span;
-    rc.bin_w = span / (float)nb;
-    const float K = (threshold + 1.0f) * vol_factor;
+    rc.inv_w = (R)nb / span;
+    rc.bin_w = span / (R)nb;
+    const R K = (threshold + 1.0f) * vol_factor;
     rc.K2 = K * K;
     rc.expected = vol_factor * r_search * r_search * r_search;
     rc.threshold = threshold;
@@ -395,10 +410,10 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     rc.cell = cell;
     rc.grid_n = N;
     rc.box = box;
-    rc.gbox = (float)N * cell;
+    rc.gbox = (R)N * cell;
     rc.window = (uint32_t)std::max(1, p.window);
 
-    HostTemplate ht;
+    HostTemplateT<R> ht;
     if (build_template(ht, mesh.n_cells, mesh.cell_length, rmin, r_search) != kOk) {
       set_error(kErrRange, "search sphere of " + std::to_string(r_search) +
                                " wider than the mesh; use a finer mesh or smaller radii");
@@ -409,36 +424,36 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     int32_t* tdy = grow_to<int32_t>(tdy_, tcount);
     int32_t* tdz = grow_to<int32_t>(tdz_, tcount);
     uint8_t* ttype = grow_to<uint8_t>(ttype_, tcount);
-    float* tmin = grow_to<float>(tmin_, tcount);
-    float* tmax = grow_to<float>(tmax_, tcount);
+    R* tmin = grow_to<R>(tmin_, tcount);
+    R* tmax = grow_to<R>(tmax_, tcount);
     SIFG_CUDA(cudaMemcpyAsync(tdx, ht.dx.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
     SIFG_CUDA(cudaMemcpyAsync(tdy, ht.dy.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
     SIFG_CUDA(cudaMemcpyAsync(tdz, ht.dz.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
     SIFG_CUDA(cudaMemcpyAsync(ttype, ht.type.data(), tcount, cudaMemcpyHostToDevice, st_));
-    SIFG_CUDA(cudaMemcpyAsync(tmin, ht.min_d2.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
-    SIFG_CUDA(cudaMemcpyAsync(tmax, ht.max_d2.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
-    TemplateView tv{tdx, tdy, tdz, ttype, tmin, tmax, tcount};
+    SIFG_CUDA(cudaMemcpyAsync(tmin, ht.min_d2.data(), tcount * sizeof(R), cudaMemcpyHostToDevice, st_));
+    SIFG_CUDA(cudaMemcpyAsync(tmax, ht.max_d2.data(), tcount * sizeof(R), cudaMemcpyHostToDevice, st_));
+    TemplateViewT<R> tv{tdx, tdy, tdz, ttype, tmin, tmax, tcount};
 
     // 3. Pre-filter at the rung, against the catalogue as the rung begins.
-    VoidView vv{cat_x_.as<float>(), cat_y_.as<float>(), cat_z_.as<float>(), cat_r_.as<float>(),
-                vstart, vids_.as<uint32_t>(), (float)kVoidCells / box, max_r, n_voids};
+    VoidViewT<R> vv{cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), cat_r_.as<R>(),
+                vstart, vids_.as<uint32_t>(), (R)kVoidCells / box, max_r, n_voids};
     uint8_t* alive = grow_to<uint8_t>(alive_, m);
     uint32_t* scand = grow_to<uint32_t>(surv_cand_, m);
     uint32_t* sflat = grow_to<uint32_t>(surv_flat_, m);
-    float* scx = grow_to<float>(scx_, m);
-    float* scy = grow_to<float>(scy_, m);
-    float* scz = grow_to<float>(scz_, m);
-    float* sr = grow_to<float>(sr_, m);
+    R* scx = grow_to<R>(scx_, m);
+    R* scy = grow_to<R>(scy_, m);
+    R* scz = grow_to<R>(scz_, m);
+    R* sr = grow_to<R>(sr_, m);
     uint8_t* sreason = grow_to<uint8_t>(sreason_, m);
     uint32_t* blocks2 = grow_to<uint32_t>(rank_slots_, (size_t)m + 2048);
     prefilter(cflat, m, mask, vv, rc, alive, blocks2, scand, sflat, scx, scy, scz, dcount + 1, st_);
-    Survivors sv{scand, sflat, scx, scy, scz, sr, sreason, dcount + 1};
+    SurvivorsT<R> sv{scand, sflat, scx, scy, scz, sr, sreason, dcount + 1};
 
     // 4. Sphere growth of every survivor.
     if (!(span > 0.0f)) {
       // RESCALE_DEGENERATE for every candidate: no annulus.
-      std::vector<float> neg(m, -1.0f);
-      SIFG_CUDA(cudaMemcpyAsync(sr, neg.data(), m * sizeof(float), cudaMemcpyHostToDevice, st_));
+      std::vector<R> neg(m, -1.0f);
+      SIFG_CUDA(cudaMemcpyAsync(sr, neg.data(), m * sizeof(R), cudaMemcpyHostToDevice, st_));
       SIFG_CUDA(cudaMemsetAsync(sreason, kRescaleDegenerate, m, st_));
     } else {
       if (p.mesh_ready && !mesh_waited) {
@@ -451,14 +466,14 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     // 5. The order, on the host while the GPU grows spheres.
     const auto t_sort = clk::now();
     SIFG_CUDA(cudaEventSynchronize(ev_cand_));
-    candidate_ranks(h_delta_, m, h_rank_, host_threads);
+    candidate_ranks((const R*)h_delta_, m, h_rank_, host_threads);
     rs.sort_ms = ms_since(t_sort);
     uint32_t* rank = grow_to<uint32_t>(rank_, m);
     SIFG_CUDA(cudaMemcpyAsync(rank, h_rank_, m * sizeof(uint32_t), cudaMemcpyHostToDevice, st_));
 
     // 6. The commit, in rounds.
     const auto t_commit = clk::now();
-    const float reach = 2.0f * scale * r_search + 2.0f * cell;
+    const R reach = 2.0f * scale * r_search + 2.0f * cell;
     int32_t ng = (int32_t)std::floor(box / reach);
     if (ng < 3) ng = 1;
     if (ng > 256) ng = 256;
@@ -467,7 +482,7 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     uint32_t* sg_ids = grow_to<uint32_t>(sgrid_ids_, m);
     uint32_t* sg_cell = grow_to<uint32_t>(sgrid_cellof_, m);
     build_survivor_grid(scx, scy, scz, dcount + 1, m, ng, box, sg_start, sg_ids, sg_cell, st_);
-    SurvivorGrid sg{sg_start, sg_ids, ng, (float)ng / box};
+    SurvivorGridT<R> sg{sg_start, sg_ids, ng, (R)ng / box};
     uint8_t* sa = grow_to<uint8_t>(state_a_, m);
     uint8_t* sb = grow_to<uint8_t>(state_b_, m);
     uint32_t* acc = grow_to<uint32_t>(acc_, m);
@@ -502,14 +517,14 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
     rs.n_rescale_fail = h_counters_[4];
     rs.n_overflow = h_counters_[5];
     if (n_acc) {
-      float rmax;
-      std::memcpy(&rmax, &h_counters_[3], sizeof(float));
+      R rmax;
+      std::memcpy(&rmax, sizeof(R) == 4 ? (void*)&h_counters_[3] : (void*)&h_counters_[6], sizeof(R));
       if (rmax > max_r) max_r = rmax;
       ensure_cat(n_voids + n_acc);
-      append_accepted(sv, rank, acc, counters, m, blocks2, cat_x_.as<float>(), cat_y_.as<float>(),
-                      cat_z_.as<float>(), cat_r_.as<float>(), n_voids, m, st_);
+      append_accepted(sv, rank, acc, counters, m, blocks2, cat_x_.as<R>(), cat_y_.as<R>(),
+                      cat_z_.as<R>(), cat_r_.as<R>(), n_voids, m, st_);
       n_voids += n_acc;
-      build_void_index(cat_x_.as<float>(), cat_y_.as<float>(), cat_z_.as<float>(), n_voids, box,
+      build_void_index(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), n_voids, box,
                        vstart, vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
     }
     rs.rung_ms = ms_since(t_rung);
@@ -517,8 +532,8 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   }
 
   if (p.consume_out) {
-    const float* last = fields[(radii.size() + 1) % 2];
-    SIFG_CUDA(cudaMemcpyAsync(p.consume_out, last, cells * sizeof(float), cudaMemcpyDeviceToDevice, st_));
+    const R* last = fields[(radii.size() + 1) % 2];
+    SIFG_CUDA(cudaMemcpyAsync(p.consume_out, last, cells * sizeof(R), cudaMemcpyDeviceToDevice, st_));
   }
   const size_t base = out.cx.size();
   out.cx.resize(base + n_voids);
@@ -526,10 +541,10 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
   out.cz.resize(base + n_voids);
   out.r.resize(base + n_voids);
   if (n_voids) {
-    SIFG_CUDA(cudaMemcpyAsync(out.cx.data() + base, cat_x_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
-    SIFG_CUDA(cudaMemcpyAsync(out.cy.data() + base, cat_y_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
-    SIFG_CUDA(cudaMemcpyAsync(out.cz.data() + base, cat_z_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
-    SIFG_CUDA(cudaMemcpyAsync(out.r.data() + base, cat_r_.ptr, n_voids * 4, cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaMemcpyAsync(out.cx.data() + base, cat_x_.ptr, n_voids * sizeof(R), cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaMemcpyAsync(out.cy.data() + base, cat_y_.ptr, n_voids * sizeof(R), cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaMemcpyAsync(out.cz.data() + base, cat_z_.ptr, n_voids * sizeof(R), cudaMemcpyDeviceToHost, st_));
+    SIFG_CUDA(cudaMemcpyAsync(out.r.data() + base, cat_r_.ptr, n_voids * sizeof(R), cudaMemcpyDeviceToHost, st_));
   }
   std::vector<uint64_t> h_traffic(2 * n_rungs + 2, 0);
   SIFG_CUDA(cudaMemcpyAsync(h_traffic.data(), traffic, h_traffic.size() * sizeof(uint64_t),
@@ -550,5 +565,11 @@ int Engine::exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams
                        .count();
   return kOk;
 }
+
+template int Engine::exodus<float>(const float*, const DeviceMeshT<float>&, const RunParamsT<float>&,
+                                  HostCatalogueT<float>&, std::vector<RungStat>*, RunTimings*);
+template int Engine::exodus<double>(const double*, const DeviceMeshT<double>&,
+                                   const RunParamsT<double>&, HostCatalogueT<double>&,
+                                   std::vector<RungStat>*, RunTimings*);
 
 }  // namespace sifg

@@ -12,24 +12,28 @@
 
 namespace sifg {
 
-struct RunParams {
+// A run's parameters, in the precision of its form (sif_real of the float
+// build, or of the SIF_USE_DOUBLE build).
+template <class R>
+struct RunParamsT {
   uint32_t grid_n = 0;
-  float box = 0.f;
-  float threshold = -0.8f;
-  float overlap = 0.f;
+  R box = 0;
+  R threshold = R(-0.8f);
+  R overlap = 0;
   uint32_t options = 0;
-  std::vector<float> radii;  // any order
-  int window = 8;            // bins resolved per pass
+  std::vector<R> radii;  // any order
+  int window = 8;        // bins resolved per pass
   // Fields that replace the smoothing, rung by rung (largest radius first),
-  // n_radii * grid_n^3 floats; host or device memory as inject_on_device says.
-  const float* inject = nullptr;
+  // n_radii * grid_n^3 values; host or device memory as inject_on_device says.
+  const R* inject = nullptr;
   bool inject_on_device = false;
   // Where the last rung's field goes under SIF_FINDER_CONSUME_GRID (device).
-  float* consume_out = nullptr;
+  R* consume_out = nullptr;
   // Recorded once the mesh is on the device, if it is still being copied
   // when the run starts: the first sphere growth waits for it.
   cudaEvent_t mesh_ready = nullptr;
 };
+using RunParams = RunParamsT<float>;
 
 struct RungStat {
   float radius = 0.f, r_search = 0.f;
@@ -53,9 +57,11 @@ struct RunTimings {
   }
 };
 
-struct HostCatalogue {
-  std::vector<float> cx, cy, cz, r;
+template <class R>
+struct HostCatalogueT {
+  std::vector<R> cx, cy, cz, r;
 };
+using HostCatalogue = HostCatalogueT<float>;
 
 class Engine {
  public:
@@ -71,11 +77,15 @@ class Engine {
 
   // The finder on a density contrast on the device and a device mesh.
   // Returns a sif status; the catalogue is appended to `out`.
-  int exodus(const float* d_delta, const DeviceMesh& mesh, const RunParams& p, HostCatalogue& out,
-             std::vector<RungStat>* stats, RunTimings* timings);
+  template <class R>
+  int exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParamsT<R>& p,
+             HostCatalogueT<R>& out, std::vector<RungStat>* stats, RunTimings* timings);
 
   DevBuf scratch;  // shared scratch for CIC / mesh builds
-  Smoother smoother;
+  Smoother smoother;        // the float form's
+  SmootherT<double> smoother64;  // the FP64 form's
+  template <class R>
+  SmootherT<R>& smoother_for();
   int host_threads = 0;
 
  private:
@@ -86,7 +96,7 @@ class Engine {
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
   DevBuf tdx_, tdy_, tdz_, ttype_, tmin_, tmax_, gbuf_, traffic_;
-  float* h_delta_ = nullptr;
+  void* h_delta_ = nullptr;  // candidate depths, float or double
   uint32_t* h_flat_ = nullptr;
   uint32_t* h_rank_ = nullptr;
   uint32_t* h_counters_ = nullptr;
@@ -104,14 +114,22 @@ class Engine {
 // The reference's candidate order (include/sif/utils/sort.h:56-145 over
 // src/finder/utils.c:24): rank[k] is the position of candidate k, given in
 // flat order, once sorted by depth with the three-way quicksort.
-void candidate_ranks(const float* delta, uint32_t m, uint32_t* rank, int threads);
+template <class K>
+void candidate_ranks(const K* delta, uint32_t m, uint32_t* rank, int threads);
 
 // Template of the rescaling (src/finder/exodus_rescale.c:175-283).
-struct HostTemplate {
+template <class R>
+struct HostTemplateT {
   std::vector<int32_t> dx, dy, dz;
   std::vector<uint8_t> type;
-  std::vector<float> min_d2, max_d2;
+  std::vector<R> min_d2, max_d2;
 };
-int build_template(HostTemplate& t, uint32_t mesh_n, float cell_length, float rmin, float r_search);
+template <class R>
+int build_template(HostTemplateT<R>& t, uint32_t mesh_n, R cell_length, R rmin, R r_search);
+
+template <>
+inline SmootherT<float>& Engine::smoother_for<float>() { return smoother; }
+template <>
+inline SmootherT<double>& Engine::smoother_for<double>() { return smoother64; }
 
 }  // namespace sifg

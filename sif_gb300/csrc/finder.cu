@@ -14,7 +14,7 @@
 //                  before it that it could interact with is decided.
 // paint_new        sif__mark_sphere (src/finder/utils.c:965-1033).
 //
-// Every float expression that decides a candidate is written with _rn
+// Every R expression that decides a candidate is written with _rn
 // intrinsics in the reference's order, so it rounds as the strict CPU build.
 #include <cuda_runtime.h>
 #include <math_constants.h>
@@ -36,26 +36,39 @@ constexpr uint64_t kScanChunk = (uint64_t)kScanT * 4 * kScanRounds;
 
 uint32_t scan_blocks(uint64_t n_cells) { return (uint32_t)((n_cells + kScanChunk - 1) / kScanChunk); }
 
+// Four consecutive cells in one 16-byte load (two for double).
+__device__ __forceinline__ void load4(const float* __restrict__ f, uint64_t c0, float* v) {
+  const float4 q = __ldg(reinterpret_cast<const float4*>(f + c0));
+  v[0] = q.x;
+  v[1] = q.y;
+  v[2] = q.z;
+  v[3] = q.w;
+}
+__device__ __forceinline__ void load4(const double* __restrict__ f, uint64_t c0, double* v) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(f + c0));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(f + c0 + 2));
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = b.x;
+  v[3] = b.y;
+}
+
 // The candidate bits of cells c0..c0+3 (bit j for c0 + j), and their depths.
-__device__ __forceinline__ uint32_t quad_candidates(const float* __restrict__ f,
+template <class R>
+__device__ __forceinline__ uint32_t quad_candidates(const R* __restrict__ f,
                                                     const uint32_t* __restrict__ mask,
-                                                    uint64_t c0, uint64_t n, float thr,
-                                                    float4& v) {
+                                                    uint64_t c0, uint64_t n, R thr, R* v) {
   if (c0 + 3 < n) {
-    v = __ldg(reinterpret_cast<const float4*>(f + c0));
+    load4(f, c0, v);
   } else {
-    v.x = c0 < n ? f[c0] : 1.0f;
-    v.y = c0 + 1 < n ? f[c0 + 1] : 1.0f;
-    v.z = c0 + 2 < n ? f[c0 + 2] : 1.0f;
-    v.w = c0 + 3 < n ? f[c0 + 3] : 1.0f;
+    for (int k = 0; k < 4; k++) v[k] = c0 + k < n ? f[c0 + k] : R(1);
   }
   if (c0 >= n) return 0u;
   const uint32_t m = __ldg(mask + (c0 >> 5)) >> (c0 & 31);
   uint32_t bits = 0;
-  bits |= (v.x <= thr && !(m & 1u) && c0 < n) ? 1u : 0u;
-  bits |= (v.y <= thr && !(m & 2u) && c0 + 1 < n) ? 2u : 0u;
-  bits |= (v.z <= thr && !(m & 4u) && c0 + 2 < n) ? 4u : 0u;
-  bits |= (v.w <= thr && !(m & 8u) && c0 + 3 < n) ? 8u : 0u;
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    bits |= (v[k] <= thr && !(m & (1u << k)) && c0 + k < n) ? (1u << k) : 0u;
   return bits;
 }
 
@@ -82,16 +95,17 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* ws, ui
   return before + x - v;
 }
 
-__global__ void __launch_bounds__(kScanT) scan_count_kernel(const float* __restrict__ f,
+template <class R>
+__global__ void __launch_bounds__(kScanT) scan_count_kernel(const R* __restrict__ f,
                                                             const uint32_t* __restrict__ mask,
-                                                            uint64_t n, float thr,
+                                                            uint64_t n, R thr,
                                                             uint32_t* __restrict__ counts) {
   __shared__ uint32_t ws[kScanT / 32];
   const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
   uint32_t c = 0;
 #pragma unroll
   for (int j = 0; j < kScanRounds; j++) {
-    float4 v;
+    R v[4];
     c += __popc(quad_candidates(f, mask, base + ((uint64_t)j * kScanT + threadIdx.x) * 4, n, thr, v));
   }
   c = __reduce_add_sync(0xffffffffu, c);
@@ -104,23 +118,23 @@ __global__ void __launch_bounds__(kScanT) scan_count_kernel(const float* __restr
   }
 }
 
+template <class R>
 __global__ void __launch_bounds__(kScanT) scan_write_kernel(
-    const float* __restrict__ f, const uint32_t* __restrict__ mask, uint64_t n, float thr,
-    const uint32_t* __restrict__ offsets, float* __restrict__ cdelta, uint32_t* __restrict__ cflat) {
+    const R* __restrict__ f, const uint32_t* __restrict__ mask, uint64_t n, R thr,
+    const uint32_t* __restrict__ offsets, R* __restrict__ cdelta, uint32_t* __restrict__ cflat) {
   __shared__ uint32_t ws[kScanT / 32];
   const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
   uint32_t out = offsets[blockIdx.x];
   for (int j = 0; j < kScanRounds; j++) {
     const uint64_t c0 = base + ((uint64_t)j * kScanT + threadIdx.x) * 4;
-    float4 v;
+    R v[4];
     const uint32_t bits = quad_candidates(f, mask, c0, n, thr, v);
     uint32_t total;
     uint32_t pos = out + block_scan_excl(__popc(bits), ws, &total);
-    const float d[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       if (bits & (1u << k)) {
-        cdelta[pos] = d[k];
+        cdelta[pos] = v[k];
         cflat[pos] = (uint32_t)(c0 + k);
         pos++;
       }
@@ -134,7 +148,8 @@ __global__ void store_total_kernel(const uint32_t* __restrict__ offsets, uint32_
   d_count[0] = offsets[nb];
 }
 
-void scan_count_pass(const float* field, const uint32_t* mask, uint64_t n_cells, float threshold,
+template <class R>
+void scan_count_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
                      uint32_t* block_counts, uint32_t* d_count, cudaStream_t st) {
   const uint32_t nb = scan_blocks(n_cells);
   scan_count_kernel<<<nb, kScanT, 0, st>>>(field, mask, n_cells, threshold, block_counts);
@@ -145,8 +160,9 @@ void scan_count_pass(const float* field, const uint32_t* mask, uint64_t n_cells,
   SIFG_LAUNCH_CHECK();
 }
 
-void scan_write_pass(const float* field, const uint32_t* mask, uint64_t n_cells, float threshold,
-                     const uint32_t* block_counts, float* cand_delta, uint32_t* cand_flat,
+template <class R>
+void scan_write_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
+                     const uint32_t* block_counts, R* cand_delta, uint32_t* cand_flat,
                      cudaStream_t st) {
   scan_write_kernel<<<scan_blocks(n_cells), kScanT, 0, st>>>(field, mask, n_cells, threshold,
                                                              block_counts, cand_delta, cand_flat);
@@ -173,52 +189,56 @@ __device__ bool overlap_quick(const uint32_t* mask, uint32_t n, uint32_t ix, uin
 // The pair test of sif__overlap_exact (src/finder/utils.c:904-955): the
 // interior form when the query's search box lies inside the box, the
 // minimum-image form otherwise.
-__device__ __forceinline__ bool collide(float cx, float cy, float cz, float r, float vx, float vy,
-                                        float vz, float rj, float f, float scale, float box,
-                                        float half, bool interior) {
-  const float mn = r < rj ? r : rj;
-  const float tot = fmul(scale, fsub(fadd(r, rj), fmul(f, mn)));
-  const float tot2 = fmul(tot, tot);
+template <class R>
+__device__ __forceinline__ bool collide(R cx, R cy, R cz, R r, R vx, R vy,
+                                        R vz, R rj, R f, R scale, R box,
+                                        R half, bool interior) {
+  const R mn = r < rj ? r : rj;
+  const R tot = fmul(scale, fsub(fadd(r, rj), fmul(f, mn)));
+  const R tot2 = fmul(tot, tot);
   if (interior) {
-    const float dx = fsub(cx, vx), dy = fsub(cy, vy), dz = fsub(cz, vz);
+    const R dx = fsub(cx, vx), dy = fsub(cy, vy), dz = fsub(cz, vz);
     return fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)) < tot2;
   }
-  float dx = fabsf(fsub(cx, vx));
+  R dx = fabs_(fsub(cx, vx));
   dx = dx > half ? fsub(box, dx) : dx;
-  const float dx2 = fmul(dx, dx);
+  const R dx2 = fmul(dx, dx);
   if (dx2 >= tot2) return false;
-  float dy = fabsf(fsub(cy, vy));
+  R dy = fabs_(fsub(cy, vy));
   dy = dy > half ? fsub(box, dy) : dy;
-  const float dy2 = fmul(dy, dy);
-  const float dxy2 = fadd(dx2, dy2);
+  const R dy2 = fmul(dy, dy);
+  const R dxy2 = fadd(dx2, dy2);
   if (dxy2 >= tot2) return false;
-  float dz = fabsf(fsub(cz, vz));
+  R dz = fabs_(fsub(cz, vz));
   dz = dz > half ? fsub(box, dz) : dz;
   return fadd(dxy2, fmul(dz, dz)) < tot2;
 }
 
-__device__ __forceinline__ float search_radius(float r, float max_r, float f, float scale) {
-  const float mn = r < max_r ? r : max_r;
+template <class R>
+__device__ __forceinline__ R search_radius(R r, R max_r, R f, R scale) {
+  const R mn = r < max_r ? r : max_r;
   return fmul(scale, fsub(fadd(r, max_r), fmul(f, mn)));
 }
 
-__device__ __forceinline__ bool is_interior(float cx, float cy, float cz, float s, float box) {
+template <class R>
+__device__ __forceinline__ bool is_interior(R cx, R cy, R cz, R s, R box) {
   return fsub(cx, s) >= 0.0f && fadd(cx, s) < box && fsub(cy, s) >= 0.0f && fadd(cy, s) < box &&
          fsub(cz, s) >= 0.0f && fadd(cz, s) < box;
 }
 
 // sif__overlap_exact (src/finder/utils.c:850-960) over the void index.
-__device__ bool overlap_exact(const VoidView& v, float cx, float cy, float cz, float r, float f,
-                              float scale, float box) {
+template <class R>
+__device__ bool overlap_exact(const VoidViewT<R>& v, R cx, R cy, R cz, R r, R f,
+                              R scale, R box) {
   if (v.n == 0) return false;
-  const float half = fmul(box, 0.5f);
-  const float s = search_radius(r, v.max_r, f, scale);
-  const int32_t x0 = (int32_t)floorf(fmul(fsub(cx, s), v.inv_cell));
-  const int32_t x1 = (int32_t)floorf(fmul(fadd(cx, s), v.inv_cell));
-  const int32_t y0 = (int32_t)floorf(fmul(fsub(cy, s), v.inv_cell));
-  const int32_t y1 = (int32_t)floorf(fmul(fadd(cy, s), v.inv_cell));
-  const int32_t z0 = (int32_t)floorf(fmul(fsub(cz, s), v.inv_cell));
-  const int32_t z1 = (int32_t)floorf(fmul(fadd(cz, s), v.inv_cell));
+  const R half = fmul(box, R(0.5f));
+  const R s = search_radius(r, v.max_r, f, scale);
+  const int32_t x0 = (int32_t)ffloor(fmul(fsub(cx, s), v.inv_cell));
+  const int32_t x1 = (int32_t)ffloor(fmul(fadd(cx, s), v.inv_cell));
+  const int32_t y0 = (int32_t)ffloor(fmul(fsub(cy, s), v.inv_cell));
+  const int32_t y1 = (int32_t)ffloor(fmul(fadd(cy, s), v.inv_cell));
+  const int32_t z0 = (int32_t)ffloor(fmul(fsub(cz, s), v.inv_cell));
+  const int32_t z1 = (int32_t)ffloor(fmul(fadd(cz, s), v.inv_cell));
   const bool interior = is_interior(cx, cy, cz, s, box);
   for (int32_t ix = x0; ix <= x1; ix++) {
     const uint32_t wx = (uint32_t)ix & (kVoidCells - 1);
@@ -243,8 +263,9 @@ __device__ bool overlap_exact(const VoidView& v, float cx, float cy, float cz, f
 // Pre-filter
 // ---------------------------------------------------------------------------
 
+template <class R>
 __global__ void prefilter_kernel(const uint32_t* __restrict__ cflat, uint32_t m,
-                                 const uint32_t* __restrict__ mask, VoidView voids, RungConsts rc,
+                                 const uint32_t* __restrict__ mask, VoidViewT<R> voids, RungConstsT<R> rc,
                                  uint8_t* __restrict__ alive) {
   const uint32_t n = rc.grid_n;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
@@ -257,8 +278,8 @@ __global__ void prefilter_kernel(const uint32_t* __restrict__ cflat, uint32_t m,
       if (rc.proxy_pole > 0 && overlap_quick(mask, n, ix, iy, iz, (uint32_t)rc.proxy_pole)) {
         ok = 0;
       } else {
-        const float cx = fmul((float)ix, rc.cell), cy = fmul((float)iy, rc.cell),
-                    cz = fmul((float)iz, rc.cell);
+        const R cx = fmul((R)ix, rc.cell), cy = fmul((R)iy, rc.cell),
+                    cz = fmul((R)iz, rc.cell);
         if (overlap_exact(voids, cx, cy, cz, rc.radius, rc.f, rc.scale, rc.box)) ok = 0;
       }
     }
@@ -290,11 +311,12 @@ __global__ void __launch_bounds__(kCompactT) flag_count_kernel(const uint8_t* __
   }
 }
 
+template <class R>
 __global__ void __launch_bounds__(kCompactT) survivor_write_kernel(
     const uint8_t* __restrict__ flags, uint32_t m, const uint32_t* __restrict__ offsets,
-    const uint32_t* __restrict__ cflat, RungConsts rc, uint32_t* __restrict__ surv_cand,
-    uint32_t* __restrict__ sflat, float* __restrict__ scx, float* __restrict__ scy,
-    float* __restrict__ scz) {
+    const uint32_t* __restrict__ cflat, RungConstsT<R> rc, uint32_t* __restrict__ surv_cand,
+    uint32_t* __restrict__ sflat, R* __restrict__ scx, R* __restrict__ scy,
+    R* __restrict__ scz) {
   __shared__ uint32_t wsum[kCompactT / 32];
   const uint32_t base = blockIdx.x * kCompactChunk;
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -318,18 +340,19 @@ __global__ void __launch_bounds__(kCompactT) survivor_write_kernel(
       surv_cand[pos] = i;
       sflat[pos] = flat;
       // candidate_centre (exodus_finder.c:366-388) on its node.
-      scx[pos] = fmul((float)(flat / (n * n)), rc.cell);
-      scy[pos] = fmul((float)((flat / n) % n), rc.cell);
-      scz[pos] = fmul((float)(flat % n), rc.cell);
+      scx[pos] = fmul((R)(flat / (n * n)), rc.cell);
+      scy[pos] = fmul((R)((flat / n) % n), rc.cell);
+      scz[pos] = fmul((R)(flat % n), rc.cell);
     }
     out += total;
     __syncthreads();
   }
 }
 
-void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, VoidView voids,
-               RungConsts rc, uint8_t* alive, uint32_t* block_counts, uint32_t* surv_cand,
-               uint32_t* surv_flat, float* scx, float* scy, float* scz, uint32_t* d_surv_count,
+template <class R>
+void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, VoidViewT<R> voids,
+               RungConstsT<R> rc, uint8_t* alive, uint32_t* block_counts, uint32_t* surv_cand,
+               uint32_t* surv_flat, R* scx, R* scy, R* scz, uint32_t* d_surv_count,
                cudaStream_t st) {
   if (m == 0) {
     SIFG_CUDA(cudaMemsetAsync(d_surv_count, 0, sizeof(uint32_t), st));
@@ -368,18 +391,20 @@ constexpr uint32_t kSmemBuf = 2048;
 
 unsigned growth_grid() { return 152u * 6u; }
 
+template <class R>
 struct CellRange {
   uint32_t s, e;
-  float ex, ey, ez;
+  R ex, ey, ez;
 };
 
 // query_cell, src/finder/exodus_rescale.c:295-342.
-__device__ __forceinline__ CellRange query_cell(const MeshView& m, const TemplateView& t,
+template <class R>
+__device__ __forceinline__ CellRange<R> query_cell(const MeshViewT<R>& m, const TemplateViewT<R>& t,
                                                 uint32_t i, int32_t ci, int32_t cj, int32_t ck,
-                                                float cx, float cy, float cz) {
+                                                R cx, R cy, R cz) {
   const int32_t N = m.n;
   int32_t ix = ci + __ldg(t.dx + i), iy = cj + __ldg(t.dy + i), iz = ck + __ldg(t.dz + i);
-  CellRange r;
+  CellRange<R> r;
   r.ex = cx;
   r.ey = cy;
   r.ez = cz;
@@ -416,19 +441,21 @@ __device__ __forceinline__ int block_max_int(int v, int* red) {
 }
 
 // Top edge of bin b (exodus_rescale.c:905-913).
-__device__ __forceinline__ float bin_hi(const RungConsts& rc, int32_t b) {
-  if (b == (int32_t)rc.nb - 1) return fmul(rc.rs2, 1.0f + 1e-6f);
-  return fadd(rc.rc2, fmul((float)(b + 1), rc.bin_w));
+template <class R>
+__device__ __forceinline__ R bin_hi(const RungConstsT<R>& rc, int32_t b) {
+  if (b == (int32_t)rc.nb - 1) return fmul(rc.rs2, R(1.0f + 1e-6f));
+  return fadd(rc.rc2, fmul((R)(b + 1), rc.bin_w));
 }
 
 // Ascending bitonic sort of buf[0, p), p a power of two.
-__device__ void bitonic_sort(float* buf, uint32_t p) {
+template <class R>
+__device__ void bitonic_sort(R* buf, uint32_t p) {
   for (uint32_t k = 2; k <= p; k <<= 1) {
     for (uint32_t j = k >> 1; j > 0; j >>= 1) {
       for (uint32_t i = threadIdx.x; i < p; i += kGrowT) {
         const uint32_t l = i ^ j;
         if (l > i) {
-          const float a = buf[i], b = buf[l];
+          const R a = buf[i], b = buf[l];
           const bool up = (i & k) == 0;
           if ((a > b) == up) {
             buf[i] = b;
@@ -446,16 +473,16 @@ __device__ void bitonic_sort(float* buf, uint32_t p) {
 // the lane holding it (for counts), `particles(type)` whether its particles
 // are read, and `each(type, d2, p)` runs per particle read. `visited` and
 // `read` count the lookups and the particles.
-template <class Want, class Whole, class Particles, class Each>
-__device__ __forceinline__ void walk_cells(const MeshView& mesh, const TemplateView& tpl,
-                                           int32_t ci, int32_t cj, int32_t ck, float cx, float cy,
-                                           float cz, Want want, Whole whole, Particles particles,
+template <class R, class Want, class Whole, class Particles, class Each>
+__device__ __forceinline__ void walk_cells(const MeshViewT<R>& mesh, const TemplateViewT<R>& tpl,
+                                           int32_t ci, int32_t cj, int32_t ck, R cx, R cy,
+                                           R cz, Want want, Whole whole, Particles particles,
                                            Each each, unsigned long long& visited,
                                            unsigned long long& read) {
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   for (uint32_t c0 = warp * 32; c0 < tpl.count; c0 += kGrowWarps * 32) {
     const uint32_t i = c0 + lane;
-    CellRange c{0, 0, 0.f, 0.f, 0.f};
+    CellRange<R> c{0, 0, 0.f, 0.f, 0.f};
     uint8_t type = 0;
     bool need = false;
     if (i < tpl.count) {
@@ -473,16 +500,16 @@ __device__ __forceinline__ void walk_cells(const MeshView& mesh, const TemplateV
       todo &= todo - 1;
       const uint32_t s = __shfl_sync(0xffffffffu, c.s, src);
       const uint32_t e = __shfl_sync(0xffffffffu, c.e, src);
-      const float ex = __shfl_sync(0xffffffffu, c.ex, src);
-      const float ey = __shfl_sync(0xffffffffu, c.ey, src);
-      const float ez = __shfl_sync(0xffffffffu, c.ez, src);
+      const R ex = __shfl_sync(0xffffffffu, c.ex, src);
+      const R ey = __shfl_sync(0xffffffffu, c.ey, src);
+      const R ez = __shfl_sync(0xffffffffu, c.ez, src);
       const uint8_t t = (uint8_t)__shfl_sync(0xffffffffu, (int)type, src);
       if (lane == 0) read += e - s;
       uint32_t p = s + lane;
       // Two particles per lane in flight.
       for (; p + 32 < e; p += 64) {
-        const float x0 = __ldg(mesh.x + p), y0 = __ldg(mesh.y + p), z0 = __ldg(mesh.z + p);
-        const float x1 = __ldg(mesh.x + p + 32), y1 = __ldg(mesh.y + p + 32),
+        const R x0 = __ldg(mesh.x + p), y0 = __ldg(mesh.y + p), z0 = __ldg(mesh.z + p);
+        const R x1 = __ldg(mesh.x + p + 32), y1 = __ldg(mesh.y + p + 32),
                     z1 = __ldg(mesh.z + p + 32);
         each(t, dist2(x0, y0, z0, ex, ey, ez), p);
         each(t, dist2(x1, y1, z1, ex, ey, ez), p + 32);
@@ -496,27 +523,28 @@ __device__ __forceinline__ void walk_cells(const MeshView& mesh, const TemplateV
 // each), traffic[1] the template cells a pass visited (a range lookup, 8
 // bytes, plus the template entry, 8 bytes): the gathered bytes of the
 // sphere growth.
-__global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, TemplateView tpl,
-                                                           RungConsts rc, Survivors sv,
-                                                           float* __restrict__ gbuf, uint32_t gcap,
+template <class R>
+__global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshViewT<R> mesh, TemplateViewT<R> tpl,
+                                                           RungConstsT<R> rc, SurvivorsT<R> sv,
+                                                           R* __restrict__ gbuf, uint32_t gcap,
                                                            unsigned long long* __restrict__ traffic) {
   __shared__ uint32_t bins[kMaxBins];
   __shared__ uint32_t below[kMaxBins];  // particles inside bin b's lower edge
-  __shared__ float sbuf[kSmemBuf];
+  __shared__ R sbuf[kSmemBuf];
   __shared__ unsigned long long red64[kGrowWarps];
   __shared__ int redi[kGrowWarps];
   __shared__ uint32_t collected;
 
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t n_surv = *sv.count;
-  float* my_gbuf = gbuf + (uint64_t)blockIdx.x * gcap;
+  R* my_gbuf = gbuf + (uint64_t)blockIdx.x * gcap;
 
   for (uint32_t s = blockIdx.x; s < n_surv; s += gridDim.x) {
-    const float cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
+    const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
                   ck = (int32_t)fmul(cz, mesh.inv_l);
     uint8_t reason = kRescaleOk;
-    float radius = -1.0f;
+    R radius = -1.0f;
     unsigned long long read = 0, visited = 0;
 
     for (uint32_t b = threadIdx.x; b < rc.nb; b += kGrowT) bins[b] = 0;
@@ -539,7 +567,7 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
           }
         },
         [](uint8_t type) { return type == kCellStraddle || type == kCellEdge; },
-        [&](uint8_t, float d2, uint32_t) {
+        [&](uint8_t, R d2, uint32_t) {
           if (d2 <= rc.rs2) within++;
           if (d2 <= rc.rc2) {
             n_core++;
@@ -552,7 +580,7 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
     within = block_sum_u64(within, red64);
     if (within == 0) {
       reason = kRescaleEmpty;
-    } else if (fsub(__fdiv_rn(__ull2float_rn(within), rc.expected), 1.0f) <= rc.threshold) {
+    } else if (fsub(fdiv(from_u64<R>(within), rc.expected), R(1.0f)) <= rc.threshold) {
       reason = kRescaleBeyondSearch;
     }
 
@@ -562,7 +590,7 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
           mesh, tpl, ci, cj, ck, cx, cy, cz,
           [](uint8_t type, uint32_t) { return type == kCellShell; }, [](uint8_t, uint32_t) {},
           [](uint8_t) { return true; },
-          [&](uint8_t, float d2, uint32_t) {
+          [&](uint8_t, R d2, uint32_t) {
             atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
           },
           visited, read);
@@ -571,7 +599,7 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
       const unsigned long long total = n_core + n_shell;
       if (total == 0) {
         reason = kRescaleEmpty;
-      } else if (fsub(__fdiv_rn(__ull2float_rn(total), rc.expected), 1.0f) <= rc.threshold) {
+      } else if (fsub(fdiv(from_u64<R>(total), rc.expected), R(1.0f)) <= rc.threshold) {
         reason = kRescaleBeyondSearch;
       }
       if (reason == kRescaleOk) {
@@ -600,8 +628,8 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
           int best = -1;
           for (int32_t b = threadIdx.x; b <= cursor; b += kGrowT) {
             if (bins[b] == 0) continue;
-            const float hi = bin_hi(rc, b);
-            const float nm = __uint2float_rn(below[b]);
+            const R hi = bin_hi(rc, b);
+            const R nm = from_u32<R>(below[b]);
             if (!(fmul(nm, nm) > fmul(fmul(fmul(rc.K2, hi), hi), hi))) best = max(best, b);
           }
           best = block_max_int(best, redi);
@@ -612,7 +640,7 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
           const uint32_t top = below[b_hi] + bins[b_hi];
           while (b_lo < b_hi && top - below[b_lo] > kSmemBuf) b_lo++;
           const uint32_t want = top - below[b_lo];
-          float* buf = sbuf;
+          R* buf = sbuf;
           uint32_t cap = kSmemBuf;
           if (want > kSmemBuf) {
             buf = my_gbuf;
@@ -622,8 +650,8 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
             reason = kRescaleOverflow;
             break;
           }
-          const float lo = fadd(rc.rc2, fmul((float)b_lo, rc.bin_w));
-          const float hi = bin_hi(rc, b_hi);
+          const R lo = fadd(rc.rc2, fmul((R)b_lo, rc.bin_w));
+          const R hi = bin_hi(rc, b_hi);
           if (threadIdx.x == 0) collected = 0;
           __syncthreads();
           walk_cells(
@@ -633,7 +661,7 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
                        !(__ldg(tpl.min_d2 + i) > hi);
               },
               [](uint8_t, uint32_t) {}, [](uint8_t) { return true; },
-              [&](uint8_t type, float d2, uint32_t) {
+              [&](uint8_t type, R d2, uint32_t) {
                 if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) return;
                 const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
                 if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) return;
@@ -645,21 +673,21 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
           const uint32_t m = collected < cap ? collected : cap;
           uint32_t p2 = 1;
           while (p2 < m) p2 <<= 1;
-          for (uint32_t i = m + threadIdx.x; i < p2; i += kGrowT) buf[i] = CUDART_INF_F;
+          for (uint32_t i = m + threadIdx.x; i < p2; i += kGrowT) buf[i] = real_inf<R>();
           __syncthreads();
           bitonic_sort(buf, p2);
           // Outside-in: the k-th smallest encloses top - m + k particles.
           int found = -1;
           for (uint32_t k = threadIdx.x; k < m; k += kGrowT) {
-            const float d2 = buf[k];
+            const R d2 = buf[k];
             if (d2 == 0.0f) continue;
-            const float rn = __uint2float_rn(top - m + k);
-            const float d2c = fmul(fmul(d2, d2), d2);
+            const R rn = from_u32<R>(top - m + k);
+            const R d2c = fmul(fmul(d2, d2), d2);
             if (fmul(rn, rn) <= fmul(rc.K2, d2c)) found = max(found, (int)k);
           }
           found = block_max_int(found, redi);
           if (found >= 0) {
-            radius = __fsqrt_rn(buf[found]);
+            radius = fsqrt(buf[found]);
             reason = kRescaleOk;
             break;
           }
@@ -684,8 +712,9 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshView mesh, Templa
   }
 }
 
-void grow(MeshView mesh, TemplateView tpl, RungConsts rc, Survivors s, uint32_t max_survivors,
-          float* gbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
+template <class R>
+void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s, uint32_t max_survivors,
+          R* gbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
           KernelTimer* timer) {
   if (max_survivors == 0) return;
   const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
@@ -699,14 +728,16 @@ void grow(MeshView mesh, TemplateView tpl, RungConsts rc, Survivors s, uint32_t 
 // Survivor hash
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ int32_t hash_axis(float c, float inv, int32_t ng) {
+template <class R>
+__device__ __forceinline__ int32_t hash_axis(R c, R inv, int32_t ng) {
   int32_t i = (int32_t)fmul(c, inv);
   return i < 0 ? 0 : (i >= ng ? ng - 1 : i);
 }
 
-__global__ void sgrid_count_kernel(const float* __restrict__ x, const float* __restrict__ y,
-                                   const float* __restrict__ z, const uint32_t* __restrict__ cnt,
-                                   int32_t ng, float inv, uint32_t* __restrict__ counts,
+template <class R>
+__global__ void sgrid_count_kernel(const R* __restrict__ x, const R* __restrict__ y,
+                                   const R* __restrict__ z, const uint32_t* __restrict__ cnt,
+                                   int32_t ng, R inv, uint32_t* __restrict__ counts,
                                    uint32_t* __restrict__ cell_of) {
   const uint32_t n = *cnt;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -725,13 +756,14 @@ __global__ void scatter_ids_kernel(const uint32_t* __restrict__ cell_of, const u
     ids[atomicAdd(cursor + cell_of[i], 1u)] = i;
 }
 
-void build_survivor_grid(const float* scx, const float* scy, const float* scz,
-                         const uint32_t* d_count, uint32_t max_survivors, int32_t ng, float box,
+template <class R>
+void build_survivor_grid(const R* scx, const R* scy, const R* scz,
+                         const uint32_t* d_count, uint32_t max_survivors, int32_t ng, R box,
                          uint32_t* start, uint32_t* ids, uint32_t* cell_of, cudaStream_t st) {
   const uint32_t cells = (uint32_t)(ng * ng * ng);
   SIFG_CUDA(cudaMemsetAsync(start, 0, (cells + 1) * sizeof(uint32_t), st));
   if (max_survivors == 0) return;
-  const float inv = (float)ng / box;
+  const R inv = (R)ng / box;
   sgrid_count_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(scx, scy, scz, d_count, ng, inv,
                                                                    start, cell_of);
   SIFG_LAUNCH_CHECK();
@@ -747,37 +779,47 @@ void build_survivor_grid(const float* scx, const float* scy, const float* scz,
 // Commit rounds
 // ---------------------------------------------------------------------------
 
+// The largest accepted radius: positive values order as their bit patterns.
+__device__ __forceinline__ void store_rmax(uint32_t* counters, float r) {
+  atomicMax((int*)(counters + 3), __float_as_int(r));
+}
+__device__ __forceinline__ void store_rmax(uint32_t* counters, double r) {
+  atomicMax((unsigned long long*)(counters + 6), (unsigned long long)__double_as_longlong(r));
+}
+
 // Two survivors can interact -- one's acceptance change the other's fate --
 // only if their centres are closer than the largest distance any of the
 // commit's tests reaches: the mask and pole probes reach scale * (r_i + r_j)
 // plus a cell, the overlap scale * (r_i + r_j); two cells of slack cover
 // every rounding.
-__device__ __forceinline__ bool interacts(float ax, float ay, float az, float ar, float bx,
-                                          float by, float bz, float br, const RungConsts& rc) {
-  const float half = 0.5f * rc.box;
-  float dx = fabsf(ax - bx), dy = fabsf(ay - by), dz = fabsf(az - bz);
+template <class R>
+__device__ __forceinline__ bool interacts(R ax, R ay, R az, R ar, R bx,
+                                          R by, R bz, R br, const RungConstsT<R>& rc) {
+  const R half = 0.5f * rc.box;
+  R dx = fabs_(ax - bx), dy = fabs_(ay - by), dz = fabs_(az - bz);
   dx = dx > half ? rc.box - dx : dx;
   dy = dy > half ? rc.box - dy : dy;
   dz = dz > half ? rc.box - dz : dz;
-  const float reach = rc.scale * (ar + br) + 2.0f * rc.cell;
+  const R reach = rc.scale * (ar + br) + 2.0f * rc.cell;
   return dx * dx + dy * dy + dz * dz < reach * reach;
 }
 
-__global__ void commit_round_kernel(Survivors sv, const uint32_t* __restrict__ rank,
-                                    SurvivorGrid g, VoidView voids, const uint32_t* __restrict__ mask,
-                                    RungConsts rc, const uint8_t* __restrict__ st_in,
+template <class R>
+__global__ void commit_round_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ rank,
+                                    SurvivorGridT<R> g, VoidViewT<R> voids, const uint32_t* __restrict__ mask,
+                                    RungConstsT<R> rc, const uint8_t* __restrict__ st_in,
                                     uint8_t* __restrict__ st_out, uint32_t* __restrict__ acc,
                                     uint32_t* __restrict__ counters) {
   const uint32_t n = *sv.count;
   const uint32_t nn = rc.grid_n;
-  const float half = fmul(rc.box, 0.5f);
+  const R half = fmul(rc.box, R(0.5f));
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint8_t s0 = st_in[i];
     if (s0 != kUndecided) {
       st_out[i] = s0;
       continue;
     }
-    const float cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i], r = sv.r[i];
+    const R cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i], r = sv.r[i];
     const uint32_t node = sv.flat[i];
     const uint32_t ix = node / (nn * nn), iy = (node / nn) % nn, iz = node % nn;
     // The commit's re-checks (exodus_finder.c:2286-2317), against every void
@@ -785,7 +827,7 @@ __global__ void commit_round_kernel(Survivors sv, const uint32_t* __restrict__ r
     // the exact overlap.
     bool reject = mask_get_rw(mask, node);
     if (!reject) {
-      const int32_t pole = (int32_t)(__fdiv_rn(fmul(fmul(rc.scale, r), fsub(1.0f, rc.f)), rc.cell)) - 1;
+      const int32_t pole = (int32_t)(fdiv(fmul(fmul(rc.scale, r), fsub(R(1.0f), rc.f)), rc.cell)) - 1;
       if (pole > 0 && overlap_quick(mask, nn, ix, iy, iz, (uint32_t)pole)) reject = true;
     }
     if (!reject && overlap_exact(voids, cx, cy, cz, r, rc.f, rc.scale, rc.box)) reject = true;
@@ -809,7 +851,7 @@ __global__ void commit_round_kernel(Survivors sv, const uint32_t* __restrict__ r
               if (j == i) continue;
               const uint8_t sj = st_in[j];
               if (sj == kRejected) continue;
-              const float jx = sv.cx[j], jy = sv.cy[j], jz = sv.cz[j], rj = sv.r[j];
+              const R jx = sv.cx[j], jy = sv.cy[j], jz = sv.cz[j], rj = sv.r[j];
               if (sj == kAccepted) {
                 // A same-rung void: the exact pair test (its search box is
                 // the reference's at the rung's largest radius; the minimum
@@ -833,7 +875,7 @@ __global__ void commit_round_kernel(Survivors sv, const uint32_t* __restrict__ r
     } else if (ready) {
       out = kAccepted;
       acc[atomicAdd(counters, 1u)] = i;
-      atomicMax((int*)(counters + 3), __float_as_int(r));  // r > 0: int order is float order
+      store_rmax(counters, r);
     } else {
       atomicAdd(counters + 1, 1u);
     }
@@ -841,7 +883,8 @@ __global__ void commit_round_kernel(Survivors sv, const uint32_t* __restrict__ r
   }
 }
 
-__global__ void commit_init_kernel(Survivors sv, uint8_t* __restrict__ state,
+template <class R>
+__global__ void commit_init_kernel(SurvivorsT<R> sv, uint8_t* __restrict__ state,
                                    uint32_t* __restrict__ counters) {
   const uint32_t n = *sv.count;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -852,15 +895,17 @@ __global__ void commit_init_kernel(Survivors sv, uint8_t* __restrict__ state,
   }
 }
 
-void commit_init(Survivors s, uint8_t* state, uint32_t* counters, uint32_t max_survivors,
+template <class R>
+void commit_init(SurvivorsT<R> s, uint8_t* state, uint32_t* counters, uint32_t max_survivors,
                  cudaStream_t st) {
   if (max_survivors == 0) return;
   commit_init_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(s, state, counters);
   SIFG_LAUNCH_CHECK();
 }
 
-void commit_round(Survivors s, const uint32_t* rank, SurvivorGrid g, VoidView voids,
-                  const uint32_t* mask, RungConsts rc, const uint8_t* state_in, uint8_t* state_out,
+template <class R>
+void commit_round(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, VoidViewT<R> voids,
+                  const uint32_t* mask, RungConstsT<R> rc, const uint8_t* state_in, uint8_t* state_out,
                   uint32_t* acc, uint32_t* counters, uint32_t max_survivors, cudaStream_t st) {
   commit_round_kernel<<<grid_for(max_survivors, 128), 128, 0, st>>>(s, rank, g, voids, mask, rc,
                                                                      state_in, state_out, acc,
@@ -871,37 +916,38 @@ void commit_round(Survivors s, const uint32_t* rank, SurvivorGrid g, VoidView vo
 // paint_sphere with set = 1 (src/finder/utils.c:965-1027), one warp per void:
 // every node whose centre lies within scale * r, measured as the reference
 // measures it.
-__global__ void paint_kernel(Survivors sv, const uint32_t* __restrict__ acc,
+template <class R>
+__global__ void paint_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ acc,
                              const uint32_t* __restrict__ counters, uint32_t* __restrict__ mask,
-                             RungConsts rc) {
+                             RungConstsT<R> rc) {
   const uint32_t lo = counters[2], hi = counters[0];
   const unsigned lane = threadIdx.x & 31u;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   const uint32_t n = rc.grid_n;
   for (uint32_t a = lo + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); a < hi; a += warps) {
     const uint32_t i = acc[a];
-    const float cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i];
-    const float rt = fmul(rc.scale, sv.r[i]);
-    const float r2 = fmul(rt, rt);
-    const float inv = __fdiv_rn(1.0f, rc.cell);
-    const float half = fmul(rc.gbox, 0.5f);
+    const R cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i];
+    const R rt = fmul(rc.scale, sv.r[i]);
+    const R r2 = fmul(rt, rt);
+    const R inv = fdiv(R(1.0f), rc.cell);
+    const R half = fmul(rc.gbox, R(0.5f));
     const int32_t cr = (int32_t)fmul(rt, inv) + 1;
     const int32_t ci = (int32_t)fmul(cx, inv), cj = (int32_t)fmul(cy, inv), ck = (int32_t)fmul(cz, inv);
     const int32_t side = 2 * cr + 1;
     for (int32_t q = lane; q < side * side; q += 32) {
       const int32_t gx = ci + q / side - cr, gy = cj + q % side - cr;
-      float ddx = fabsf(fsub(fmul((float)gx, rc.cell), cx));
+      R ddx = fabs_(fsub(fmul((R)gx, rc.cell), cx));
       ddx = ddx > half ? fsub(rc.gbox, ddx) : ddx;
-      const float dx2 = fmul(ddx, ddx);
+      const R dx2 = fmul(ddx, ddx);
       if (dx2 > r2) continue;
-      float ddy = fabsf(fsub(fmul((float)gy, rc.cell), cy));
+      R ddy = fabs_(fsub(fmul((R)gy, rc.cell), cy));
       ddy = ddy > half ? fsub(rc.gbox, ddy) : ddy;
-      const float dxy2 = fadd(dx2, fmul(ddy, ddy));
+      const R dxy2 = fadd(dx2, fmul(ddy, ddy));
       if (dxy2 > r2) continue;
       const uint64_t row = ((uint64_t)wrap_pbc(gx, n) * n + wrap_pbc(gy, n)) * n;
       for (int32_t dz = -cr; dz <= cr; dz++) {
         const int32_t gz = ck + dz;
-        float ddz = fabsf(fsub(fmul((float)gz, rc.cell), cz));
+        R ddz = fabs_(fsub(fmul((R)gz, rc.cell), cz));
         ddz = ddz > half ? fsub(rc.gbox, ddz) : ddz;
         if (fadd(dxy2, fmul(ddz, ddz)) <= r2) {
           const uint64_t cell = row + wrap_pbc(gz, n);
@@ -912,8 +958,9 @@ __global__ void paint_kernel(Survivors sv, const uint32_t* __restrict__ acc,
   }
 }
 
-void paint_new(Survivors s, const uint32_t* acc, const uint32_t* counters, uint32_t* mask,
-               RungConsts rc, uint32_t max_survivors, cudaStream_t st) {
+template <class R>
+void paint_new(SurvivorsT<R> s, const uint32_t* acc, const uint32_t* counters, uint32_t* mask,
+               RungConstsT<R> rc, uint32_t max_survivors, cudaStream_t st) {
   const uint32_t warps = max_survivors < 152u * 16u ? (max_survivors ? max_survivors : 1) : 152u * 16u;
   paint_kernel<<<(warps + 3) / 4, 128, 0, st>>>(s, acc, counters, mask, rc);
   SIFG_LAUNCH_CHECK();
@@ -923,7 +970,8 @@ void paint_new(Survivors s, const uint32_t* acc, const uint32_t* counters, uint3
 // Appending the rung's voids in rank order
 // ---------------------------------------------------------------------------
 
-__global__ void mark_ranks_kernel(Survivors sv, const uint32_t* __restrict__ rank,
+template <class R>
+__global__ void mark_ranks_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ rank,
                                   const uint32_t* __restrict__ acc, const uint32_t* __restrict__ counters,
                                   uint32_t* __restrict__ slots) {
   const uint32_t n = counters[0];
@@ -931,12 +979,13 @@ __global__ void mark_ranks_kernel(Survivors sv, const uint32_t* __restrict__ ran
     slots[rank[sv.cand[acc[a]]]] = 1;
 }
 
-__global__ void write_voids_kernel(Survivors sv, const uint32_t* __restrict__ rank,
+template <class R>
+__global__ void write_voids_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ rank,
                                    const uint32_t* __restrict__ acc,
                                    const uint32_t* __restrict__ counters,
-                                   const uint32_t* __restrict__ pos, float* __restrict__ cx,
-                                   float* __restrict__ cy, float* __restrict__ cz,
-                                   float* __restrict__ cr, uint32_t base) {
+                                   const uint32_t* __restrict__ pos, R* __restrict__ cx,
+                                   R* __restrict__ cy, R* __restrict__ cz,
+                                   R* __restrict__ cr, uint32_t base) {
   const uint32_t n = counters[0];
   for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
     const uint32_t i = acc[a];
@@ -948,9 +997,10 @@ __global__ void write_voids_kernel(Survivors sv, const uint32_t* __restrict__ ra
   }
 }
 
-void append_accepted(Survivors s, const uint32_t* rank, const uint32_t* acc,
+template <class R>
+void append_accepted(SurvivorsT<R> s, const uint32_t* rank, const uint32_t* acc,
                      const uint32_t* counters, uint32_t m_candidates, uint32_t* rank_slots,
-                     float* cat_x, float* cat_y, float* cat_z, float* cat_r, uint32_t n_voids,
+                     R* cat_x, R* cat_y, R* cat_z, R* cat_r, uint32_t n_voids,
                      uint32_t max_survivors, cudaStream_t st) {
   SIFG_CUDA(cudaMemsetAsync(rank_slots, 0, (m_candidates + 1) * sizeof(uint32_t), st));
   mark_ranks_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(s, rank, acc, counters, rank_slots);
@@ -966,15 +1016,17 @@ void append_accepted(Survivors s, const uint32_t* rank, const uint32_t* acc,
 // ---------------------------------------------------------------------------
 
 // cll_axis_index, src/structures/cell_linked_list.c:40-58 (periodic).
-__device__ __forceinline__ uint32_t void_axis(float c, float inv) {
-  int32_t i = (int32_t)floorf(fmul(c, inv));
+template <class R>
+__device__ __forceinline__ uint32_t void_axis(R c, R inv) {
+  int32_t i = (int32_t)ffloor(fmul(c, inv));
   i %= (int32_t)kVoidCells;
   if (i < 0) i += kVoidCells;
   return (uint32_t)i;
 }
 
-__global__ void void_count_kernel(const float* __restrict__ x, const float* __restrict__ y,
-                                  const float* __restrict__ z, uint32_t n, float inv,
+template <class R>
+__global__ void void_count_kernel(const R* __restrict__ x, const R* __restrict__ y,
+                                  const R* __restrict__ z, uint32_t n, R inv,
                                   uint32_t* __restrict__ counts, uint32_t* __restrict__ cell_of) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t c = (void_axis(x[i], inv) * kVoidCells + void_axis(y[i], inv)) * kVoidCells +
@@ -984,12 +1036,13 @@ __global__ void void_count_kernel(const float* __restrict__ x, const float* __re
   }
 }
 
-void build_void_index(const float* cx, const float* cy, const float* cz, uint32_t n, float box,
+template <class R>
+void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
                       uint32_t* start, uint32_t* ids, uint32_t* cell_of, cudaStream_t st) {
   const uint32_t cells = kVoidCells * kVoidCells * kVoidCells;
   SIFG_CUDA(cudaMemsetAsync(start, 0, (cells + 1) * sizeof(uint32_t), st));
   if (n == 0) return;
-  const float inv = (float)kVoidCells / box;
+  const R inv = (R)kVoidCells / box;
   void_count_kernel<<<grid_for(n, 256), 256, 0, st>>>(cx, cy, cz, n, inv, start, cell_of);
   SIFG_LAUNCH_CHECK();
   exclusive_scan_u32(start, cells + 1, st);
@@ -999,5 +1052,35 @@ void build_void_index(const float* cx, const float* cy, const float* cz, uint32_
   scatter_ids_kernel<<<grid_for(n, 256), 256, 0, st>>>(cell_of, nullptr, n, cur, ids);
   SIFG_LAUNCH_CHECK();
 }
+
+// ---------------------------------------------------------------------------
+// The two forms: the reference's float build and its SIF_USE_DOUBLE build.
+// ---------------------------------------------------------------------------
+#define SIFG_FINDER_FORM(R)                                                                        \
+  template void scan_count_pass<R>(const R*, const uint32_t*, uint64_t, R, uint32_t*, uint32_t*,   \
+                                   cudaStream_t);                                                  \
+  template void scan_write_pass<R>(const R*, const uint32_t*, uint64_t, R, const uint32_t*, R*,    \
+                                   uint32_t*, cudaStream_t);                                       \
+  template void prefilter<R>(const uint32_t*, uint32_t, const uint32_t*, VoidViewT<R>,             \
+                             RungConstsT<R>, uint8_t*, uint32_t*, uint32_t*, uint32_t*, R*, R*,    \
+                             R*, uint32_t*, cudaStream_t);                                         \
+  template void grow<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>, uint32_t,   \
+                        R*, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*);            \
+  template void build_survivor_grid<R>(const R*, const R*, const R*, const uint32_t*, uint32_t,    \
+                                       int32_t, R, uint32_t*, uint32_t*, uint32_t*, cudaStream_t); \
+  template void commit_init<R>(SurvivorsT<R>, uint8_t*, uint32_t*, uint32_t, cudaStream_t);        \
+  template void commit_round<R>(SurvivorsT<R>, const uint32_t*, SurvivorGridT<R>, VoidViewT<R>,    \
+                                const uint32_t*, RungConstsT<R>, const uint8_t*, uint8_t*,         \
+                                uint32_t*, uint32_t*, uint32_t, cudaStream_t);                     \
+  template void paint_new<R>(SurvivorsT<R>, const uint32_t*, const uint32_t*, uint32_t*,           \
+                             RungConstsT<R>, uint32_t, cudaStream_t);                              \
+  template void append_accepted<R>(SurvivorsT<R>, const uint32_t*, const uint32_t*,                \
+                                   const uint32_t*, uint32_t, uint32_t*, R*, R*, R*, R*, uint32_t, \
+                                   uint32_t, cudaStream_t);                                        \
+  template void build_void_index<R>(const R*, const R*, const R*, uint32_t, R, uint32_t*,          \
+                                    uint32_t*, uint32_t*, cudaStream_t);
+
+SIFG_FINDER_FORM(float)
+SIFG_FINDER_FORM(double)
 
 }  // namespace sifg

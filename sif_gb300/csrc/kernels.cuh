@@ -57,25 +57,34 @@ size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n);
 void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_particles,
                  uint32_t n, float box, float* grid, void* scratch, cudaStream_t st,
                  KernelTimer* timer);
+// The FP64 form's deposit: scratch is cic_f64_scratch_bytes(n).
+size_t cic_f64_scratch_bytes(uint32_t n);
+void cic_deposit_f64(const double* x, const double* y, const double* z, uint64_t n_particles,
+                     uint32_t n, double box, double* grid, void* scratch, cudaStream_t st,
+                     KernelTimer* timer);
 size_t density_contrast_scratch_bytes();
-void density_contrast(float* v, uint64_t n, double* d_scratch, cudaStream_t st);
+template <class R>
+void density_contrast(R* v, uint64_t n, double* d_scratch, cudaStream_t st);
 double read_mean(const double* d_scratch);
 
 // --- mesh.cu ---
-struct DeviceMesh {
+template <class R>
+struct DeviceMeshT {
   uint32_t n_cells = 0;
-  float box_length = 0.f, cell_length = 0.f;
+  R box_length = 0, cell_length = 0;
   uint64_t n_particles = 0;
-  float *x = nullptr, *y = nullptr, *z = nullptr;
+  R *x = nullptr, *y = nullptr, *z = nullptr;
   uint32_t* offsets = nullptr;  // n_cells^3 + 1
   uint32_t* orig = nullptr;     // source index of each entry
 };
+using DeviceMesh = DeviceMeshT<float>;
+// Scratch bytes of a mesh build in either form (the larger records).
 size_t mesh_scratch_bytes(uint64_t n_particles, uint32_t n_cells);
 // Builds into caller buffers (x, y, z, offsets, orig sized for the mesh).
 // scratch: mesh_scratch_bytes(); scan_sums: NULL, or scan_sums_needed(cells
 // + 1) entries the scan uses instead of a buffer of its own.
-void mesh_build(const float* x, const float* y, const float* z, uint64_t n_particles,
-                DeviceMesh& m, void* scratch, cudaStream_t st, KernelTimer* timer,
-                uint32_t* scan_sums = nullptr);
+template <class R>
+void mesh_build(const R* x, const R* y, const R* z, uint64_t n_particles, DeviceMeshT<R>& m,
+                void* scratch, cudaStream_t st, KernelTimer* timer, uint32_t* scan_sums = nullptr);
 
 }  // namespace sifg

@@ -21,13 +21,24 @@
 
 namespace sifg {
 
+template <class R>
 struct MeshGeom {
   uint32_t n;
-  float box;
-  float inv_l;  // 1.0f / cell_length
+  R box;
+  R inv_l;  // 1 / cell_length
 };
 
-__device__ __forceinline__ uint32_t mesh_cell(float x, float y, float z, const MeshGeom& g) {
+// A scatter record: source index and folded position.
+template <class R>
+struct alignas(16) MeshRec {
+  uint32_t i;
+  R x, y, z;
+};
+static_assert(sizeof(MeshRec<float>) == 16, "float records are 16 bytes");
+static_assert(sizeof(MeshRec<double>) == 32, "double records are 32 bytes");
+
+template <class R>
+__device__ __forceinline__ uint32_t mesh_cell(R x, R y, R z, const MeshGeom<R>& g) {
   int32_t ix = (int32_t)fmul(box_fold(x, g.box), g.inv_l);
   int32_t iy = (int32_t)fmul(box_fold(y, g.box), g.inv_l);
   int32_t iz = (int32_t)fmul(box_fold(z, g.box), g.inv_l);
@@ -38,8 +49,9 @@ __device__ __forceinline__ uint32_t mesh_cell(float x, float y, float z, const M
   return ((uint32_t)ix * g.n + (uint32_t)iy) * g.n + (uint32_t)iz;
 }
 
-__global__ void cell_count_kernel(const float* __restrict__ x, const float* __restrict__ y,
-                                  const float* __restrict__ z, uint64_t n, MeshGeom g,
+template <class R>
+__global__ void cell_count_kernel(const R* __restrict__ x, const R* __restrict__ y,
+                                  const R* __restrict__ z, uint64_t n, MeshGeom<R> g,
                                   uint32_t* __restrict__ counts) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -52,15 +64,16 @@ __global__ void cell_count_kernel(const float* __restrict__ x, const float* __re
   }
 }
 
-__global__ void cell_scatter_kernel(const float* __restrict__ x, const float* __restrict__ y,
-                                    const float* __restrict__ z, uint64_t n, MeshGeom g,
-                                    uint32_t* __restrict__ cursor, uint4* __restrict__ tmp) {
+template <class R>
+__global__ void cell_scatter_kernel(const R* __restrict__ x, const R* __restrict__ y,
+                                    const R* __restrict__ z, uint64_t n, MeshGeom<R> g,
+                                    uint32_t* __restrict__ cursor, MeshRec<R>* __restrict__ tmp) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const unsigned lane = threadIdx.x & 31u;
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
     const uint64_t p = base + threadIdx.x;
     const bool valid = p < n;
-    float px = 0.f, py = 0.f, pz = 0.f;
+    R px = 0, py = 0, pz = 0;
     uint32_t c = 0xffffffffu;
     if (valid) {
       px = box_fold(x[p], g.box);
@@ -75,8 +88,12 @@ __global__ void cell_scatter_kernel(const float* __restrict__ x, const float* __
     slot0 = __shfl_sync(0xffffffffu, slot0, leader);
     if (valid) {
       const uint32_t slot = slot0 + __popc(peers & ((1u << lane) - 1u));
-      tmp[slot] = make_uint4((uint32_t)p, __float_as_uint(px), __float_as_uint(py),
-                             __float_as_uint(pz));
+      MeshRec<R> rec;
+      rec.i = (uint32_t)p;
+      rec.x = px;
+      rec.y = py;
+      rec.z = pz;
+      tmp[slot] = rec;
     }
   }
 }
@@ -86,9 +103,10 @@ constexpr int kCanonSmem = 2048;  // entries a CTA ranks in shared memory
 
 // One warp per cell. A cell of up to kCanonSmem/4 entries per warp is ranked
 // from shared memory; a larger one is ranked straight from global memory.
+template <class R>
 __global__ void __launch_bounds__(kCanonThreads) cell_canon_kernel(
-    const uint4* __restrict__ tmp, const uint32_t* __restrict__ offsets, uint32_t n_cells_total,
-    float* __restrict__ ox, float* __restrict__ oy, float* __restrict__ oz,
+    const MeshRec<R>* __restrict__ tmp, const uint32_t* __restrict__ offsets,
+    uint32_t n_cells_total, R* __restrict__ ox, R* __restrict__ oy, R* __restrict__ oz,
     uint32_t* __restrict__ orig) {
   __shared__ uint32_t keys[kCanonSmem];
   const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -101,24 +119,26 @@ __global__ void __launch_bounds__(kCanonThreads) cell_canon_kernel(
     if (cnt == 0) continue;
     const bool in_smem = cnt <= per_warp;
     if (in_smem) {
-      for (uint32_t i = lane; i < cnt; i += 32) wk[i] = tmp[s + i].x;
+      for (uint32_t i = lane; i < cnt; i += 32) wk[i] = tmp[s + i].i;
       __syncwarp();
     }
     for (uint32_t i = lane; i < cnt + (32 - cnt % 32) % 32; i += 32) {
       const bool mine = i < cnt;
-      const uint4 v = mine ? tmp[s + i] : make_uint4(0, 0, 0, 0);
+      MeshRec<R> v;
+      v.i = 0;
+      if (mine) v = tmp[s + i];
       uint32_t rank = 0;
       if (in_smem) {
-        for (uint32_t j = 0; j < cnt; j++) rank += wk[j] < v.x;
+        for (uint32_t j = 0; j < cnt; j++) rank += wk[j] < v.i;
       } else {
-        for (uint32_t j = 0; j < cnt; j++) rank += tmp[s + j].x < v.x;
+        for (uint32_t j = 0; j < cnt; j++) rank += tmp[s + j].i < v.i;
       }
       if (mine) {
         const uint32_t dst = s + rank;
-        ox[dst] = __uint_as_float(v.y);
-        oy[dst] = __uint_as_float(v.z);
-        oz[dst] = __uint_as_float(v.w);
-        if (orig) orig[dst] = v.x;
+        ox[dst] = v.x;
+        oy[dst] = v.y;
+        oz[dst] = v.z;
+        if (orig) orig[dst] = v.i;
       }
     }
     __syncwarp();
@@ -127,36 +147,42 @@ __global__ void __launch_bounds__(kCanonThreads) cell_canon_kernel(
 
 size_t mesh_scratch_bytes(uint64_t n_particles, uint32_t n_cells) {
   const uint64_t cells = (uint64_t)n_cells * n_cells * n_cells;
-  return n_particles * sizeof(uint4) + (cells + 1) * sizeof(uint32_t) + 1024;
+  return n_particles * sizeof(MeshRec<float>) + (cells + 1) * sizeof(uint32_t) + 1024;
 }
 
-void mesh_build(const float* x, const float* y, const float* z, uint64_t n_particles,
-                DeviceMesh& m, void* scratch, cudaStream_t st, KernelTimer* timer,
-                uint32_t* scan_sums) {
-  MeshGeom g;
+template <class R>
+void mesh_build(const R* x, const R* y, const R* z, uint64_t n_particles, DeviceMeshT<R>& m,
+                void* scratch, cudaStream_t st, KernelTimer* timer, uint32_t* scan_sums) {
+  MeshGeom<R> g;
   g.n = m.n_cells;
   g.box = m.box_length;
-  g.inv_l = 1.0f / m.cell_length;
+  g.inv_l = R(1.0f) / m.cell_length;
   const uint64_t cells = (uint64_t)m.n_cells * m.n_cells * m.n_cells;
-  uint4* tmp = (uint4*)scratch;
-  uint32_t* cursor =
-      (uint32_t*)((char*)scratch + ((n_particles * sizeof(uint4) + 255) & ~(size_t)255));
+  MeshRec<R>* tmp = (MeshRec<R>*)scratch;
+  uint32_t* cursor = (uint32_t*)((char*)scratch +
+                                 ((n_particles * sizeof(MeshRec<R>) + 255) & ~(size_t)255));
   SIFG_CUDA(cudaMemsetAsync(m.offsets, 0, (cells + 1) * sizeof(uint32_t), st));
   const unsigned grd = grid_for(n_particles, 256, 152u * 16u);
   if (timer) timer->begin(st);
-  cell_count_kernel<<<grd, 256, 0, st>>>(x, y, z, n_particles, g, m.offsets);
+  cell_count_kernel<R><<<grd, 256, 0, st>>>(x, y, z, n_particles, g, m.offsets);
   SIFG_LAUNCH_CHECK();
   exclusive_scan_u32(m.offsets, (uint32_t)(cells + 1), st, scan_sums);
   SIFG_CUDA(cudaMemcpyAsync(cursor, m.offsets, cells * sizeof(uint32_t),
                             cudaMemcpyDeviceToDevice, st));
-  cell_scatter_kernel<<<grd, 256, 0, st>>>(x, y, z, n_particles, g, cursor, tmp);
+  cell_scatter_kernel<R><<<grd, 256, 0, st>>>(x, y, z, n_particles, g, cursor, tmp);
   SIFG_LAUNCH_CHECK();
   const unsigned cgrid = grid_for(cells, kCanonThreads / 32 * 1, 152u * 16u);
-  cell_canon_kernel<<<cgrid, kCanonThreads, 0, st>>>(tmp, m.offsets, (uint32_t)cells, m.x, m.y,
-                                                     m.z, m.orig);
+  cell_canon_kernel<R><<<cgrid, kCanonThreads, 0, st>>>(tmp, m.offsets, (uint32_t)cells, m.x, m.y,
+                                                        m.z, m.orig);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(st);
   m.n_particles = n_particles;
 }
+
+template void mesh_build<float>(const float*, const float*, const float*, uint64_t,
+                                DeviceMeshT<float>&, void*, cudaStream_t, KernelTimer*, uint32_t*);
+template void mesh_build<double>(const double*, const double*, const double*, uint64_t,
+                                 DeviceMeshT<double>&, void*, cudaStream_t, KernelTimer*,
+                                 uint32_t*);
 
 }  // namespace sifg

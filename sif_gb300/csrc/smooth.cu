@@ -98,9 +98,42 @@ __global__ void __launch_bounds__(256) filter_kernel(const float4* __restrict__ 
   }
 }
 
+// The FP64 form's filter: one mode per 16-byte load, four in flight.
+__global__ void __launch_bounds__(256) filter_kernel_f64(const double2* __restrict__ spec,
+                                                         double2* __restrict__ out, uint32_t n,
+                                                         const double* __restrict__ lut,
+                                                         const double* __restrict__ win,
+                                                         double norm) {
+  const uint32_t zd = n / 2 + 1, h = n >> 1;
+  const uint64_t total = (uint64_t)n * n * zd;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < total;
+       i0 += kFilterUnroll * stride) {
+    double2 v[kFilterUnroll];
+#pragma unroll
+    for (int u = 0; u < kFilterUnroll; u++)
+      if (i0 + u * stride < total) v[u] = __ldg(spec + i0 + u * stride);
+#pragma unroll
+    for (int u = 0; u < kFilterUnroll; u++) {
+      const uint64_t i = i0 + u * stride;
+      if (i >= total) continue;
+      const uint64_t row = i / zd;
+      const uint32_t iz = (uint32_t)(i - row * zd);
+      const uint32_t iy = (uint32_t)(row % n), ix = (uint32_t)(row / n);
+      const int32_t kx = ix > h ? (int32_t)ix - (int32_t)n : (int32_t)ix;
+      const int32_t ky = iy > h ? (int32_t)iy - (int32_t)n : (int32_t)iy;
+      const uint32_t k2 = (uint32_t)(kx * kx + ky * ky) + iz * iz;
+      double s = __ldg(lut + k2) * norm;
+      if (win) s = s * __ldg(win + ix) * __ldg(win + iy) * __ldg(win + iz);
+      out[i] = make_double2(v[u].x * s, v[u].y * s);
+    }
+  }
+}
+
 // fft_build_filter_lut, src/math/fft.c:521-568: the radial factor by integer
 // |k|^2, computed in double.
-__global__ void lut_kernel(float* __restrict__ lut, uint32_t max_k2, int filter, double factor,
+template <class R>
+__global__ void lut_kernel(R* __restrict__ lut, uint32_t max_k2, int filter, double factor,
                            double gfactor) {
   for (uint32_t k2 = blockIdx.x * blockDim.x + threadIdx.x; k2 <= max_k2;
        k2 += gridDim.x * blockDim.x) {
@@ -116,25 +149,31 @@ __global__ void lut_kernel(float* __restrict__ lut, uint32_t max_k2, int filter,
       v = 1.0;
     }
     if (gfactor > 0.0 && k2 > 0) v *= exp(-0.5 * gfactor * gfactor * (double)k2);
-    lut[k2] = (float)v;
+    lut[k2] = (R)v;
   }
 }
 
-Smoother::~Smoother() { release(); }
+template <class R>
+SmootherT<R>::~SmootherT() {
+  release();
+}
 
-void Smoother::release() {
+template <class R>
+void SmootherT<R>::release() {
   if (plan_r2c) cufftDestroy(plan_r2c);
   if (plan_c2r) cufftDestroy(plan_c2r);
   plan_r2c = plan_c2r = 0;
   n = 0;
 }
 
-void Smoother::setup(uint32_t n_, float box_, int window_mode_, cudaStream_t st) {
+template <class R>
+void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st) {
+  constexpr bool dbl = sizeof(R) == 8;
   if (n_ != n) {
     release();
     n = n_;
-    SIFG_CUFFT(cufftPlan3d(&plan_r2c, (int)n, (int)n, (int)n, CUFFT_R2C));
-    SIFG_CUFFT(cufftPlan3d(&plan_c2r, (int)n, (int)n, (int)n, CUFFT_C2R));
+    SIFG_CUFFT(cufftPlan3d(&plan_r2c, (int)n, (int)n, (int)n, dbl ? CUFFT_D2Z : CUFFT_R2C));
+    SIFG_CUFFT(cufftPlan3d(&plan_c2r, (int)n, (int)n, (int)n, dbl ? CUFFT_Z2D : CUFFT_C2R));
     SIFG_CUFFT(cufftSetStream(plan_r2c, st));
     SIFG_CUFFT(cufftSetStream(plan_c2r, st));
     stream = st;
@@ -146,57 +185,82 @@ void Smoother::setup(uint32_t n_, float box_, int window_mode_, cudaStream_t st)
   box = box_;
   window_mode = window_mode_;
   const uint64_t modes = (uint64_t)n * n * (n / 2 + 1);
-  spectrum.ensure(modes * sizeof(float2));
-  work.ensure(modes * sizeof(float2));
+  spectrum.ensure(modes * 2 * sizeof(R));
+  work.ensure(modes * 2 * sizeof(R));
   const uint32_t h = n >> 1;
   const uint32_t max_k2 = 3 * h * h;
-  lut.ensure(((size_t)max_k2 + 1) * sizeof(float));
-  win.ensure((size_t)n * sizeof(float));
+  lut.ensure(((size_t)max_k2 + 1) * sizeof(R));
+  win.ensure((size_t)n * sizeof(R));
   if (window_mode) {
     // fft_build_window_axis, src/math/fft.c:958-975, CIC (order 2): 1/W full,
     // W/S aliasing-aware, W = sinc^2(pi k / N), S = 1 - 2 sin^2/3.
-    std::vector<float> w(n);
+    std::vector<R> w(n);
     for (uint32_t i = 0; i < n; i++) {
       const int32_t k = i > h ? (int32_t)i - (int32_t)n : (int32_t)i;
       const double x = M_PI * (double)k / (double)n;
       const double s = (x < 1e-9 && x > -1e-9) ? 1.0 : std::sin(x) / x;
       const double W = s * s;
-      w[i] = (float)(window_mode == 2 ? W / (1.0 - 2.0 * std::sin(x) * std::sin(x) / 3.0)
-                                      : 1.0 / W);
+      w[i] = (R)(window_mode == 2 ? W / (1.0 - 2.0 * std::sin(x) * std::sin(x) / 3.0) : 1.0 / W);
     }
-    SIFG_CUDA(cudaMemcpyAsync(win.ptr, w.data(), n * sizeof(float), cudaMemcpyHostToDevice, st));
+    SIFG_CUDA(cudaMemcpyAsync(win.ptr, w.data(), n * sizeof(R), cudaMemcpyHostToDevice, st));
     SIFG_CUDA(cudaStreamSynchronize(st));
   }
 }
 
-void Smoother::forward(const float* grid) {
+template <>
+void SmootherT<float>::forward(const float* grid) {
   SIFG_CUFFT(cufftExecR2C(plan_r2c, (cufftReal*)grid, (cufftComplex*)spectrum.ptr));
 }
+template <>
+void SmootherT<double>::forward(const double* grid) {
+  SIFG_CUFFT(cufftExecD2Z(plan_r2c, (cufftDoubleReal*)grid, (cufftDoubleComplex*)spectrum.ptr));
+}
 
-void Smoother::smooth(int filter, float r, float sigma, float* out, KernelTimer* timer) {
+static void launch_filter(const SmootherT<float>& s, int filter, float norm) {
+  const uint64_t modes = (uint64_t)s.n * s.n * (s.n / 2 + 1);
+  const float* w = (s.window_mode && filter != kFilterNone) ? s.win.as<float>() : nullptr;
+  const unsigned grd = grid_for(modes / 2 + 1, 256, 152u * 8u);
+  if (modes < (1ull << 32))
+    filter_kernel<uint32_t><<<grd, 256, 0, s.stream>>>(s.spectrum.as<float4>(), s.work.as<float4>(),
+                                                       s.n, s.lut.as<float>(), w, norm);
+  else
+    filter_kernel<uint64_t><<<grd, 256, 0, s.stream>>>(s.spectrum.as<float4>(), s.work.as<float4>(),
+                                                       s.n, s.lut.as<float>(), w, norm);
+}
+
+static void launch_filter(const SmootherT<double>& s, int filter, double norm) {
+  const uint64_t modes = (uint64_t)s.n * s.n * (s.n / 2 + 1);
+  const double* w = (s.window_mode && filter != kFilterNone) ? s.win.as<double>() : nullptr;
+  filter_kernel_f64<<<grid_for(modes, 256, 152u * 8u), 256, 0, s.stream>>>(
+      s.spectrum.as<double2>(), s.work.as<double2>(), s.n, s.lut.as<double>(), w, norm);
+}
+
+template <class R>
+void SmootherT<R>::smooth(int filter, R r, R sigma, R* out, KernelTimer* timer) {
   const uint32_t h = n >> 1;
   const uint32_t max_k2 = 3 * h * h;
   const double factor = (double)r * 2.0 * M_PI / (double)box;
-  const double gfactor = sigma > 0.0f ? (double)sigma * 2.0 * M_PI / (double)box : 0.0;
-  lut_kernel<<<grid_for((uint64_t)max_k2 + 1, 256), 256, 0, stream>>>(lut.as<float>(), max_k2,
-                                                                        filter, factor, gfactor);
+  const double gfactor = sigma > R(0) ? (double)sigma * 2.0 * M_PI / (double)box : 0.0;
+  lut_kernel<R><<<grid_for((uint64_t)max_k2 + 1, 256), 256, 0, stream>>>(lut.as<R>(), max_k2, filter,
+                                                                         factor, gfactor);
   SIFG_LAUNCH_CHECK();
-  const uint64_t modes = (uint64_t)n * n * (n / 2 + 1);
-  const float norm = (float)(1.0 / ((double)n * n * n));
+  const R norm = (R)(1.0 / ((double)n * n * n));
   if (timer) timer->begin(stream);
-  const float* w = (window_mode && filter != kFilterNone) ? win.as<float>() : nullptr;
-  const unsigned grd = grid_for(modes / 2 + 1, 256, 152u * 8u);
-  if (modes < (1ull << 32))
-    filter_kernel<uint32_t><<<grd, 256, 0, stream>>>(spectrum.as<float4>(), work.as<float4>(), n,
-                                                     lut.as<float>(), w, norm);
-  else
-    filter_kernel<uint64_t><<<grd, 256, 0, stream>>>(spectrum.as<float4>(), work.as<float4>(), n,
-                                                     lut.as<float>(), w, norm);
+  launch_filter(*this, filter, norm);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(stream);
-  SIFG_CUFFT(cufftExecC2R(plan_c2r, (cufftComplex*)work.ptr, (cufftReal*)out));
+  if (sizeof(R) == 8)
+    SIFG_CUFFT(cufftExecZ2D(plan_c2r, (cufftDoubleComplex*)work.ptr, (cufftDoubleReal*)out));
+  else
+    SIFG_CUFFT(cufftExecC2R(plan_c2r, (cufftComplex*)work.ptr, (cufftReal*)out));
 }
 
-void Smoother::restore(float* out) { smooth(kFilterNone, 0.f, 0.f, out, nullptr); }
+template <class R>
+void SmootherT<R>::restore(R* out) {
+  smooth(kFilterNone, R(0), R(0), out, nullptr);
+}
+
+template struct SmootherT<float>;
+template struct SmootherT<double>;
 
 }  // namespace sifg

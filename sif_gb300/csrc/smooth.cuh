@@ -14,23 +14,26 @@ constexpr int kFilterTopHat = 1;
 constexpr int kFilterGaussian = 2;
 
 // Window modes: 0 none (SIF_FINDER_KEEP_CIC_WINDOW), 1 full CIC deconvolution,
-// 2 aliasing-aware (SIF_FINDER_ALIASING_WINDOW).
-struct Smoother {
+// 2 aliasing-aware (SIF_FINDER_ALIASING_WINDOW). R is the form's precision:
+// float (cuFFT R2C/C2R) or double (D2Z/Z2D).
+template <class R>
+struct SmootherT {
   uint32_t n = 0;
-  float box = 0.f;
+  R box = 0;
   int window_mode = 1;
   cudaStream_t stream = 0;
   cufftHandle plan_r2c = 0, plan_c2r = 0;
   DevBuf spectrum, work, lut, win;
 
-  void setup(uint32_t n, float box, int window_mode, cudaStream_t st);
-  void forward(const float* grid);  // grid: n^3 floats on the device
+  void setup(uint32_t n, R box, int window_mode, cudaStream_t st);
+  void forward(const R* grid);  // grid: n^3 values on the device
   // Writes the grid smoothed at r (and, with sigma > 0, a Gaussian of sigma
-  // on top) into out (n^3 floats), asynchronously on the stream.
-  void smooth(int filter, float r, float sigma, float* out, KernelTimer* timer);
-  void restore(float* out);
+  // on top) into out (n^3 values), asynchronously on the stream.
+  void smooth(int filter, R r, R sigma, R* out, KernelTimer* timer);
+  void restore(R* out);
   void release();
-  ~Smoother();
+  ~SmootherT();
 };
+using Smoother = SmootherT<float>;
 
 }  // namespace sifg

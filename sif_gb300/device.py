@@ -2,6 +2,8 @@
 
 torch only allocates and holds the device memory here; every stage is a call
 into libsif_gb300.so (include/sif_gb300.h, part 2) with raw device pointers.
+float64 inputs select the FP64 form (the `_f64` entry points, the reference's
+SIF_USE_DOUBLE arithmetic); float32 inputs the float form.
 """
 import ctypes as C
 
@@ -17,6 +19,20 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
+def _form(t):
+    """(entry-point suffix, torch dtype, numpy dtype) of a tensor's form."""
+    import torch
+
+    if t.dtype == torch.float64:
+        return "_f64", torch.float64, np.float64
+    assert t.dtype == torch.float32, f"expected float32 or float64, got {t.dtype}"
+    return "", torch.float32, np.float32
+
+
+def _fn(name, t):
+    return getattr(_lib.load(), name + _form(t)[0])
+
+
 def _check(status, what):
     if status != abi.SIF_OK:
         raise _lib.status_error(_lib.load(), status, what)
@@ -25,15 +41,15 @@ def _check(status, what):
 def cic(x, y, z, n_grid, box):
     import torch
 
-    grid = torch.empty(n_grid ** 3, dtype=torch.float32, device=x.device)
-    _check(_lib.load().sifg_cic_device(_ptr(x), _ptr(y), _ptr(z), x.numel(), n_grid, box,
-                                       _ptr(grid)), "cic")
+    grid = torch.empty(n_grid ** 3, dtype=_form(x)[1], device=x.device)
+    _check(_fn("sifg_cic_device", x)(_ptr(x), _ptr(y), _ptr(z), x.numel(), n_grid, box,
+                                     _ptr(grid)), "cic")
     return grid
 
 
 def density_contrast(grid):
     mean = C.c_double(0.0)
-    _check(_lib.load().sifg_contrast_device(_ptr(grid), grid.numel(), C.byref(mean)), "contrast")
+    _check(_fn("sifg_contrast_device", grid)(_ptr(grid), grid.numel(), C.byref(mean)), "contrast")
     return mean.value
 
 
@@ -42,40 +58,40 @@ def chain_mesh(x, y, z, n_cells, box, with_indices=True):
 
     n = x.numel()
     dev = x.device
-    mx = torch.empty(n, dtype=torch.float32, device=dev)
+    mx = torch.empty(n, dtype=_form(x)[1], device=dev)
     my = torch.empty_like(mx)
     mz = torch.empty_like(mx)
     offs = torch.empty(n_cells ** 3 + 1, dtype=torch.int32, device=dev)
     orig = torch.empty(n, dtype=torch.int32, device=dev) if with_indices else None
-    _check(_lib.load().sifg_mesh_device(_ptr(x), _ptr(y), _ptr(z), n, n_cells, box, _ptr(mx),
-                                        _ptr(my), _ptr(mz), _ptr(offs), _ptr(orig)), "chain_mesh")
+    _check(_fn("sifg_mesh_device", x)(_ptr(x), _ptr(y), _ptr(z), n, n_cells, box, _ptr(mx),
+                                      _ptr(my), _ptr(mz), _ptr(offs), _ptr(orig)), "chain_mesh")
     return mx, my, mz, offs, orig
 
 
 def smooth(delta, n_grid, box, radius, filter="top-hat", window="full"):
     import torch
 
-    out = torch.empty(n_grid ** 3, dtype=torch.float32, device=delta.device)
+    out = torch.empty(n_grid ** 3, dtype=_form(delta)[1], device=delta.device)
     f = {"top-hat": 1, "gaussian": 2}[filter]
     w = {"none": 0, "full": 1, "aliasing": 2}[window]
-    _check(_lib.load().sifg_smooth_device(_ptr(delta), n_grid, box, radius, f, w, _ptr(out)),
+    _check(_fn("sifg_smooth_device", delta)(_ptr(delta), n_grid, box, radius, f, w, _ptr(out)),
            "smooth")
     return out
 
 
-def _catalogue_arrays(cap):
-    return [np.empty(cap, np.float32) for _ in range(4)]
+def _catalogue_arrays(cap, dtype=np.float32):
+    return [np.empty(cap, dtype) for _ in range(4)]
 
 
 def exodus(delta, n_grid, box, mesh, mesh_cells, radii, threshold, overlap=0.0, options=0,
            inject=None, capacity=1 << 22):
     """The finder on device data. mesh = (mx, my, mz, offsets, ...)."""
-    lib = _lib.load()
-    radii = np.ascontiguousarray(radii, dtype=np.float32)
-    cols = _catalogue_arrays(capacity)
+    _, _, nt = _form(delta)
+    radii = np.ascontiguousarray(radii, dtype=nt)
+    cols = _catalogue_arrays(capacity, nt)
     n = C.c_uint64(0)
     mx, my, mz, offs = mesh[:4]
-    st = lib.sifg_exodus_device(_ptr(delta), n_grid, box, _ptr(mx), _ptr(my), _ptr(mz),
+    st = _fn("sifg_exodus_device", delta)(_ptr(delta), n_grid, box, _ptr(mx), _ptr(my), _ptr(mz),
                                 _ptr(offs), mx.numel(), mesh_cells,
                                 radii.ctypes.data_as(C.c_void_p), len(radii), threshold, overlap,
                                 options, _ptr(inject), *[c.ctypes.data_as(C.c_void_p) for c in cols],
@@ -87,11 +103,11 @@ def exodus(delta, n_grid, box, mesh, mesh_cells, radii, threshold, overlap=0.0, 
 def box(x, y, z, n_grid, box_length, mesh_cells, radii, threshold, overlap=0.0, options=0,
         capacity=1 << 22):
     """The whole path on device particles: CIC, contrast, mesh, finder."""
-    lib = _lib.load()
-    radii = np.ascontiguousarray(radii, dtype=np.float32)
-    cols = _catalogue_arrays(capacity)
+    _, _, nt = _form(x)
+    radii = np.ascontiguousarray(radii, dtype=nt)
+    cols = _catalogue_arrays(capacity, nt)
     n = C.c_uint64(0)
-    st = lib.sifg_box_device(_ptr(x), _ptr(y), _ptr(z), x.numel(), n_grid, box_length, mesh_cells,
+    st = _fn("sifg_box_device", x)(_ptr(x), _ptr(y), _ptr(z), x.numel(), n_grid, box_length, mesh_cells,
                              radii.ctypes.data_as(C.c_void_p), len(radii), threshold, overlap,
                              options, *[c.ctypes.data_as(C.c_void_p) for c in cols], capacity,
                              C.byref(n))

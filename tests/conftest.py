@@ -30,6 +30,12 @@ def golden_box32():
 
 
 @pytest.fixture(scope="session")
+def golden_box32_f64():
+    """The same box through the reference's SIF_USE_DOUBLE build."""
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32_f64.npz")))
+
+
+@pytest.fixture(scope="session")
 def gpu_lib():
     """The built GB300 library, initialised on the GPU."""
     import torch
@@ -51,3 +57,13 @@ def same_bits(a, b):
 
 def same_catalogue(c1, c2):
     return all(same_bits(a, b) for a, b in zip(c1, c2))
+
+
+def same_bits64(a, b):
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def same_catalogue64(c1, c2):
+    return all(same_bits64(a, b) for a, b in zip(c1, c2))

@@ -11,6 +11,11 @@ golden_box32.npz -- a 32^3 Zel'dovich box (side 128, rms displacement 4,
   (positions, offsets, source indices); the 12 per-rung smoothed fields its
   own run produced (captured from sif__fft_grid_backward); and its catalogue
   for several option sets, each run on exactly those fields.
+
+golden_box32_f64.npz -- the same box through the reference's SIF_USE_DOUBLE
+  build (sif_real = double): the float positions moved by a seeded jitter of
+  up to 1e-4 so that they need double precision, and the same records in
+  double (density, contrast, mesh, 12 captured fields, catalogues).
 """
 import os
 import sys
@@ -71,5 +76,47 @@ def make_box32(path):
     print(f"{path}: {len(cat[0])} voids over {len(radii)} rungs")
 
 
+def make_box32_f64(path):
+    p = BOX32
+    x32, y32, z32 = synth.zeldovich(p["n"], p["box"], p["rms_disp"], p["seed"])
+    rng = np.random.default_rng(p["seed"] + 1000)
+
+    def jitter(a):
+        v = a.astype(np.float64) + rng.uniform(-1e-4, 1e-4, a.shape)
+        v = np.where(v < 0.0, v + p["box"], v)
+        return np.where(v >= p["box"], v - p["box"], v)
+
+    x, y, z = jitter(x32), jitter(y32), jitter(z32)
+    radii = synth.ladder(p["r0"], 3 * p["r0"], 0.1).astype(np.float64)
+    v = "f64"
+    lib = R.load(v, 4, abi.SIF_LOG_LEVEL_ERROR)
+    f = R.RefField(lib, x, y, z, variant=v)
+    g = R.RefGrid(lib, p["n"], p["box"], variant=v)
+    g.assign_cic(f)
+    density = g.values()
+    g.to_contrast()
+    delta = g.values()
+    m = R.RefMesh(lib, p["mesh"], p["box"], f)
+    mx, my, mz, offs, idx = m.arrays(variant=v)
+    fields = np.zeros((len(radii), p["n"] ** 3), np.float64)
+    cat = R.exodus_raw(lib, g, m, radii, p["threshold"], variant=v, capture=fields)
+    out = dict(x=x, y=y, z=z, radii=radii, density=density, delta=delta, mesh_x=mx, mesh_y=my,
+               mesh_z=mz, mesh_offsets=offs, mesh_index=idx, fields=fields,
+               params=np.array([p["n"], p["box"], p["rms_disp"], p["seed"], p["r0"],
+                                p["threshold"], p["mesh"]], np.float64))
+    for name, overlap, opt in OPTION_SETS:
+        c = R.exodus_raw(lib, g, m, radii, p["threshold"], overlap, opt, variant=v, inject=fields)
+        for k, col in zip(("cx", "cy", "cz", "r"), c):
+            out[f"cat_{name}_{k}"] = col
+        out[f"cat_{name}_opt"] = np.array([overlap, opt], np.float64)
+    assert all(np.array_equal(a, out[f"cat_default_{k}"]) for a, k in zip(cat, "cx cy cz r".split()))
+    m.free()
+    g.free()
+    f.free()
+    np.savez_compressed(path, **out)
+    print(f"{path}: {len(cat[0])} voids over {len(radii)} rungs")
+
+
 if __name__ == "__main__":
     make_box32(os.path.join(HERE, "golden_box32.npz"))
+    make_box32_f64(os.path.join(HERE, "golden_box32_f64.npz"))

@@ -174,3 +174,23 @@ def test_oracle_matches_reference_library_on_zeldovich(oracle):
     rm.free()
     g.free()
     f.free()
+
+
+def test_fp64_golden_mesh_is_the_double_cell_sort(golden_box32_f64):
+    """The SIF_USE_DOUBLE build's mesh (the FP64 form's bit-exact target) is
+    the double-precision cell of chain_mesh_flat_idx (src/structures/
+    chain_mesh.c:316-331, inv_l = 1 / cell_length in double) with each cell in
+    source order."""
+    g = golden_box32_f64
+    box, nm = float(g["params"][1]), int(g["params"][6])
+    inv_l = 1.0 / (box / nm)
+    cells = []
+    for a in (g["x"], g["y"], g["z"]):
+        v = np.where(a >= box, a - box, np.where(a < 0.0, a + box, a))
+        cells.append(np.clip((v * inv_l).astype(np.int64), 0, nm - 1))
+    key = (cells[0] * nm + cells[1]) * nm + cells[2]
+    order = np.argsort(key, kind="stable")
+    assert np.array_equal(g["mesh_index"].astype(np.int64), order)
+    assert np.array_equal(g["mesh_x"], g["x"][order])
+    offs = np.concatenate([[0], np.cumsum(np.bincount(key, minlength=nm ** 3))])
+    assert np.array_equal(g["mesh_offsets"].astype(np.int64), offs)
