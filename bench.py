@@ -13,6 +13,13 @@ catalogue on the host.
 - ``cpu_baseline``: the CPU restatement of the reference's path (oracle/)
   with all host cores, on a bounded sample of the same recipe.
 
+- ``fp64_form``: the same step in the FP64 form (sifg_box_device_f64: the
+  reference's SIF_USE_DOUBLE arithmetic), the form the float path is
+  measured against.
+- ``adjoint``: the differentiation workload (256^3 particles, box 500,
+  grid 256^3, Gaussian R = 5): forward (deposit + contrast + smoothing) and
+  backward (smoothing of the gradient + the deposit's adjoint) times.
+
 ``--impl reference`` times that CPU path alone (the reference arm).
 Under torchrun every rank runs its own replica (the path does not shard).
 """
@@ -216,6 +223,11 @@ def gpu_arm(args, rank, world):
     if not args.no_e2e:
         e2e = e2e_run(args, w, x, y, z, radii)
 
+    fp64 = adj = None
+    if not args.no_forms and not args.small:
+        fp64 = fp64_run(args, w, x, y, z, radii)
+        adj = adjoint_run(args)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_run(seconds=args.cpu_seconds)
@@ -236,6 +248,8 @@ def gpu_arm(args, rank, world):
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "e2e": e2e,
+        "fp64_form": fp64,
+        "adjoint": adj,
         "cpu_baseline": cpu,
         "stages_ms_last_step": {"growth": round(tm["growth_ms"], 3), "cic_deposit": round(tm["cic_ms"], 3),
                                 "mesh": round(tm["mesh_ms"], 3), "filter": round(tm["filter_ms"], 3),
@@ -243,6 +257,92 @@ def gpu_arm(args, rank, world):
         "rungs_last_step": device.last_rung_stats() if args.verbose else None,
     }
     return line
+
+
+def fp64_run(args, w, x, y, z, radii):
+    """The step in the FP64 form on the same particles (as double), device-resident."""
+    import torch
+
+    from sif_gb300 import device
+
+    xs = [torch.from_numpy(a.astype(np.float64)).cuda() for a in (x, y, z)]
+    r64 = radii.astype(np.float64)
+    stream = device.stream()
+
+    def step():
+        return device.box(*xs, w["grid"], w["box"], w["mesh"], r64, float(w["threshold"]))
+
+    for _ in range(2):
+        cat = step()
+    steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        step()
+    end.record(stream)
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / steps
+    del xs
+    torch.cuda.empty_cache()
+    return {"value": round(len(x) / (ms / 1e3) / 1e6, 2), "unit": UNIT, "ms_per_step": round(ms, 3),
+            "steps": steps, "n_voids": len(cat[0]), "dtype": "f64"}
+
+
+# The differentiation workload: 256^3 particles, box 500, grid 256^3, rms
+# displacement 4, seed 1005, Gaussian R = 5; the loss is the sum of the squared
+# smoothed contrast over the cells within 2R of the voids the finder returns
+# (ladder(5, 30, 0.10), threshold -0.8), centres held fixed.
+ADJOINT = dict(n=256, box=500.0, rms=4.0, seed=1005, grid=256, radius=5.0, mesh=62)
+
+
+def adjoint_run(args):
+    import torch
+
+    from sif_gb300 import autograd, device, synth
+
+    a = ADJOINT
+    x, y, z = synth.zeldovich(a["n"], a["box"], a["rms"], a["seed"], backend="torch")
+    xs = [torch.from_numpy(v).cuda() for v in (x, y, z)]
+    radii = synth.ladder(a["radius"], 6 * a["radius"], 0.10).astype(np.float32)
+    cx, cy, cz, _ = device.box(*xs, a["grid"], a["box"], a["mesh"], radii, -0.8)
+    n = a["grid"]
+    cell = a["box"] / n
+    reach = 2.0 * a["radius"]
+    span = int(reach / cell) + 1
+    off = torch.arange(-span, span + 1, device="cuda")
+    ox, oy, oz = torch.meshgrid(off, off, off, indexing="ij")
+    ox, oy, oz = ox.reshape(-1), oy.reshape(-1), oz.reshape(-1)
+    mask = torch.zeros(n ** 3, dtype=torch.bool, device="cuda")
+    cs = torch.from_numpy(np.stack([cx, cy, cz], 1).astype(np.float64)).cuda()
+    for chunk in torch.split(cs, 512):
+        base = torch.floor(chunk / cell).long()
+        idx = [(base[:, k, None] + o[None, :]) for k, o in enumerate((ox, oy, oz))]
+        d2 = sum(((i.double() * cell - chunk[:, k, None] + a["box"] / 2) % a["box"] - a["box"] / 2) ** 2
+                 for k, i in enumerate(idx))
+        flat = ((idx[0] % n) * n + (idx[1] % n)) * n + (idx[2] % n)
+        mask[flat[d2 <= reach * reach]] = True
+    stream = device.stream()
+    fwd, bwd = [], []
+    for it in range(3 + 5):
+        xg = [v.clone().requires_grad_(True) for v in xs]
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        torch.cuda.synchronize()
+        e0.record(stream)
+        s_field = autograd.smoothed_contrast(*xg, n, a["box"], a["radius"], filter="gaussian")
+        e1.record(stream)
+        loss = (s_field[mask] ** 2).sum()
+        loss.backward()
+        e2.record(stream)
+        torch.cuda.synchronize()
+        if it >= 3:
+            fwd.append(e0.elapsed_time(e1))
+            bwd.append(e1.elapsed_time(e2))
+    f, b = statistics.median(fwd), statistics.median(bwd)
+    return {"config": "256^3 particles, box 500 Mpc/h, grid 256^3, Gaussian R=5, loss over "
+                      f"{int(mask.sum())} cells within 2R of {len(cx)} void centres",
+            "forward_ms": round(f, 3), "adjoint_ms": round(b, 3), "ratio": round(b / f, 3),
+            "steps": len(fwd)}
 
 
 def e2e_run(args, w, x, y, z, radii):
@@ -351,6 +451,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="a 128^3 box, for quick checks")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the FP64-form and adjoint runs")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--verbose", action="store_true")

@@ -349,6 +349,19 @@ int sifg_box_device_f64(const double* x, const double* y, const double* z, uint6
                         uint32_t n_radii, double threshold, double overlap, uint32_t opt,
                         double* cx, double* cy, double* cz, double* r, uint64_t capacity,
                         uint64_t* n_voids);
+/* The adjoint of the CIC density contrast (sifg_cic_device followed by
+ * sifg_contrast_device) with respect to the positions: given g = dL/d(delta)
+ * on the n_grid^3 device grid, writes dL/dx, dL/dy, dL/dz of every particle
+ * (device arrays of n). The smoothing is self-adjoint, so the gradient of a
+ * loss on a smoothed field is this call on the smoothed incoming gradient.
+ * No counterpart in the reference (which has no gradients); it backs the
+ * torch.autograd.Function in sif_gb300.autograd. */
+int sifg_contrast_vjp_device(const float* x, const float* y, const float* z, uint64_t n,
+                             uint32_t n_grid, float box, const float* g, float* gx, float* gy,
+                             float* gz);
+int sifg_contrast_vjp_device_f64(const double* x, const double* y, const double* z, uint64_t n,
+                                 uint32_t n_grid, double box, const double* g, double* gx,
+                                 double* gy, double* gz);
 /* Statistics and timings of the last run (up to max_rungs entries). */
 uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs);
 void sifg_last_timings(sifg_timings_t* out);

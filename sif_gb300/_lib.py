@@ -48,6 +48,8 @@ EXPORTED = [
     # the FP64 form
     "sifg_cic_device_f64", "sifg_contrast_device_f64", "sifg_mesh_device_f64",
     "sifg_smooth_device_f64", "sifg_exodus_device_f64", "sifg_box_device_f64",
+    # the adjoint
+    "sifg_contrast_vjp_device", "sifg_contrast_vjp_device_f64",
 ]
 
 
@@ -87,6 +89,8 @@ def load():
                                          f64, u32, vp, vp, vp, vp, vp, u64, C.POINTER(u64)]),
         "sifg_box_device_f64": (i32, [vp, vp, vp, u64, u32, f64, u32, vp, u32, f64, f64, u32,
                                       vp, vp, vp, vp, u64, C.POINTER(u64)]),
+        "sifg_contrast_vjp_device": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp]),
+        "sifg_contrast_vjp_device_f64": (i32, [vp, vp, vp, u64, u32, f64, vp, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

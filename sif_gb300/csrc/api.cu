@@ -854,6 +854,18 @@ static int smooth_device(const R* delta, uint32_t n_grid, R box, R r, int filter
 }
 
 template <class R>
+static int contrast_vjp_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n_grid,
+                               R box, const R* g, R* gx, R* gy, R* gz) {
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  if (n_grid < 4 || n == 0) return fail(SIF_ERR_INVALID, "vjp: bad grid or no particles");
+  cudaStream_t s = e->stream();
+  cic_contrast_vjp(x, y, z, n, n_grid, box, g, gx, gy, gz, s);
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  return SIF_OK;
+}
+
+template <class R>
 static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceMeshT<R>& m,
                       const R* radii, uint32_t n_radii, R threshold, R overlap, uint32_t opt,
                       const R* inject, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
@@ -1005,6 +1017,16 @@ int sifg_smooth_device(const float* delta, uint32_t n_grid, float box, float r, 
 int sifg_smooth_device_f64(const double* delta, uint32_t n_grid, double box, double r,
                            int filter, int window_mode, double* out) {
   SIFG_LOCKED(smooth_device(delta, n_grid, box, r, filter, window_mode, out))
+}
+int sifg_contrast_vjp_device(const float* x, const float* y, const float* z, uint64_t n,
+                             uint32_t n_grid, float box, const float* g, float* gx, float* gy,
+                             float* gz) {
+  SIFG_LOCKED(contrast_vjp_device(x, y, z, n, n_grid, box, g, gx, gy, gz))
+}
+int sifg_contrast_vjp_device_f64(const double* x, const double* y, const double* z, uint64_t n,
+                                 uint32_t n_grid, double box, const double* g, double* gx,
+                                 double* gy, double* gz) {
+  SIFG_LOCKED(contrast_vjp_device(x, y, z, n, n_grid, box, g, gx, gy, gz))
 }
 int sifg_exodus_device(const float* delta, uint32_t n_grid, float box, const float* mx,
                        const float* my, const float* mz, const uint32_t* offsets,

@@ -67,6 +67,13 @@ template <class R>
 void density_contrast(R* v, uint64_t n, double* d_scratch, cudaStream_t st);
 double read_mean(const double* d_scratch);
 
+// --- adjoint.cu ---
+// dL/dx, dL/dy, dL/dz of every particle for g = dL/d(delta) on the grid,
+// delta the CIC density contrast of the particles (the deposit's transpose).
+template <class R>
+void cic_contrast_vjp(const R* x, const R* y, const R* z, uint64_t np, uint32_t n, R box,
+                      const R* g, R* gx, R* gy, R* gz, cudaStream_t st);
+
 // --- mesh.cu ---
 template <class R>
 struct DeviceMeshT {

@@ -68,6 +68,17 @@ def chain_mesh(x, y, z, n_cells, box, with_indices=True):
     return mx, my, mz, offs, orig
 
 
+def contrast_vjp(x, y, z, n_grid, box, g):
+    """dL/dx, dL/dy, dL/dz for g = dL/d(delta), delta the CIC density contrast."""
+    import torch
+
+    gx, gy, gz = (torch.empty_like(x) for _ in range(3))
+    _check(_fn("sifg_contrast_vjp_device", x)(_ptr(x), _ptr(y), _ptr(z), x.numel(), n_grid, box,
+                                              _ptr(g), _ptr(gx), _ptr(gy), _ptr(gz)),
+           "contrast_vjp")
+    return gx, gy, gz
+
+
 def smooth(delta, n_grid, box, radius, filter="top-hat", window="full"):
     import torch
 

@@ -190,3 +190,13 @@ def _exodus_raw(grid, mesh, radii, threshold, overlap_fraction=0.0, *, overlap_t
 
 
 finders = types.SimpleNamespace(exodus=_exodus, exodus_raw=_exodus_raw)
+
+
+def smoothed_contrast(x, y, z, n_grid, box, radius, filter="gaussian", window="full"):
+    """The CIC density contrast of torch CUDA positions smoothed at `radius`,
+    differentiable with respect to the positions (a torch.autograd.Function,
+    sif_gb300.autograd.SmoothedContrast). Not in the reference's pysif, which
+    has no gradients; an addition beside its names."""
+    from . import autograd
+
+    return autograd.smoothed_contrast(x, y, z, n_grid, box, radius, filter, window)
