@@ -16,6 +16,8 @@ catalogue on the host.
 - ``fp64_form``: the same step in the FP64 form (sifg_box_device_f64: the
   reference's SIF_USE_DOUBLE arithmetic), the form the float path is
   measured against.
+- ``batched_form``: 64 boxes of 64^3-256^3 particles through
+  sifg_box_batch_device (engines run concurrently, their count autotuned).
 - ``adjoint``: the differentiation workload (256^3 particles, box 500,
   grid 256^3, Gaussian R = 5): forward (deposit + contrast + smoothing) and
   backward (smoothing of the gradient + the deposit's adjoint) times.
@@ -223,10 +225,11 @@ def gpu_arm(args, rank, world):
     if not args.no_e2e:
         e2e = e2e_run(args, w, x, y, z, radii)
 
-    fp64 = adj = None
+    fp64 = adj = batch = None
     if not args.no_forms and not args.small:
         fp64 = fp64_run(args, w, x, y, z, radii)
         adj = adjoint_run(args)
+        batch = batch_run(args)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -250,6 +253,7 @@ def gpu_arm(args, rank, world):
         "e2e": e2e,
         "fp64_form": fp64,
         "adjoint": adj,
+        "batched_form": batch,
         "cpu_baseline": cpu,
         "stages_ms_last_step": {"growth": round(tm["growth_ms"], 3), "cic_deposit": round(tm["cic_ms"], 3),
                                 "mesh": round(tm["mesh_ms"], 3), "filter": round(tm["filter_ms"], 3),
@@ -343,6 +347,59 @@ def adjoint_run(args):
                       f"{int(mask.sum())} cells within 2R of {len(cx)} void centres",
             "forward_ms": round(f, 3), "adjoint_ms": round(b, 3), "ratio": round(b / f, 3),
             "steps": len(fwd)}
+
+
+# The batching workload: 64 independent boxes, particles per side drawn
+# log-uniform in [64, 256], box sides uniform in [200, 1000] Mpc/h, grid =
+# particles per side, rms displacement 4, seed 2000 + box; ladder(R, 6R, 0.10)
+# with R twice the mean separation; threshold -0.8; mesh from
+# sif_finder_suggest_mesh_cells.
+BATCH = dict(boxes=64, n_lo=64, n_hi=256, box_lo=200.0, box_hi=1000.0, rms=4.0, seed=2000)
+
+
+def batch_run(args):
+    import torch
+
+    from sif_gb300 import device, synth
+
+    b = BATCH
+    rng = np.random.default_rng(b["seed"])
+    boxes = []
+    total = 0
+    for k in range(b["boxes"]):
+        n = int(round(math.exp(rng.uniform(math.log(b["n_lo"]), math.log(b["n_hi"])))))
+        n += n % 2
+        L = float(rng.uniform(b["box_lo"], b["box_hi"]))
+        x, y, z = synth.zeldovich(n, L, b["rms"], b["seed"] + k, backend="torch")
+        r0 = 2.0 * L / n
+        boxes.append(dict(x=torch.from_numpy(x).cuda(), y=torch.from_numpy(y).cuda(),
+                          z=torch.from_numpy(z).cuda(), n_grid=n, box=L, mesh_cells=0,
+                          radii=synth.ladder(r0, 6 * r0, 0.10).astype(np.float32),
+                          threshold=-0.8))
+        total += n ** 3
+    stream = device.stream()
+
+    def timed(engines):
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        start.record(stream)
+        cats, used = device.box_batch(boxes, engines=engines)
+        end.record(stream)
+        torch.cuda.synchronize()
+        return start.elapsed_time(end), used, sum(len(c[0]) for c in cats)
+
+    timed(0)  # the autotuner's trial runs (and warm-up)
+    seq_ms, _, nv1 = timed(1)
+    ms, used, nv = timed(0)
+    assert nv == nv1, "catalogues depend on the engine count"
+    del boxes
+    torch.cuda.empty_cache()
+    return {"config": f"{b['boxes']} boxes, {b['n_lo']}^3-{b['n_hi']}^3 particles (log-uniform), "
+                      f"box {b['box_lo']:.0f}-{b['box_hi']:.0f} Mpc/h, grid = lattice, "
+                      "ladder(2 sep, 12 sep, 0.10), threshold -0.8, suggested mesh",
+            "value": round(total / (ms / 1e3) / 1e6, 2), "unit": UNIT, "ms": round(ms, 2),
+            "engines": used, "one_engine_ms": round(seq_ms, 2),
+            "speedup_vs_one_engine": round(seq_ms / ms, 3), "n_particles": total, "n_voids": nv}
 
 
 def e2e_run(args, w, x, y, z, radii):

@@ -16,6 +16,7 @@
 #ifndef SIF_GB300_H
 #define SIF_GB300_H
 
+#include <math.h>
 #include <stdbool.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -249,6 +250,36 @@ uint32_t sif_finder_grid_cells_from_size(uint64_t n_particles, sif_real box_leng
                                          sif_real cell_size, sif_finder_units_t units,
                                          sif_real volume);
 
+/* include/sif/finder/exodus_finder.h:595-683: a static inline function
+ * there, so it is one here too. The mesh resolution the finder runs fastest
+ * at: about SIF_FINDER_MESH_PARTICLES_PER_CELL tracers per cell at the
+ * tracers' density over the whole box, no coarser than the widest search
+ * sphere's stencil allows (the traversal wraps a cell index once), between 8
+ * and SIF_FINDER_MESH_MAX_CELLS cells per side. The catalogue does not depend
+ * on it. 0 for arguments it cannot size a mesh from. */
+#define SIF_FINDER_MESH_PARTICLES_PER_CELL 30.0
+#define SIF_FINDER_MESH_MAX_CELLS 1024u
+static inline uint32_t sif_finder_suggest_mesh_cells(uint64_t n_particles, sif_real box_length,
+                                                     sif_real max_radius, sif_real volume) {
+  if (n_particles == 0 || !(box_length > 0.0f) || !isfinite(box_length) || !(volume >= 0.0f) ||
+      !isfinite(volume))
+    return 0;
+  const double L = (double)box_length;
+  /* Tracers the whole box would hold at their density. */
+  const double whole = volume > 0.0f ? (double)n_particles * (L * L * L) / (double)volume
+                                     : (double)n_particles;
+  double cells = cbrt(whole / SIF_FINDER_MESH_PARTICLES_PER_CELL);
+  if (max_radius > 0.0f) {
+    const double reach = 2.0 * (double)max_radius;
+    if (reach >= L) return 0;
+    const double at_least = L / (L - reach) + 1.0;
+    if (cells < at_least) cells = at_least;
+  }
+  if (cells < 8.0) cells = 8.0;
+  if (cells > (double)SIF_FINDER_MESH_MAX_CELLS) cells = (double)SIF_FINDER_MESH_MAX_CELLS;
+  return (uint32_t)cells;
+}
+
 /* ---------------------------------------------------------------------- */
 /* Part 2: device-resident entry points (no counterpart in the reference)  */
 /* ---------------------------------------------------------------------- */
@@ -362,6 +393,41 @@ int sifg_contrast_vjp_device(const float* x, const float* y, const float* z, uin
 int sifg_contrast_vjp_device_f64(const double* x, const double* y, const double* z, uint64_t n,
                                  uint32_t n_grid, double box, const double* g, double* gx,
                                  double* gy, double* gz);
+/* The batched form: independent boxes (particles on the device), each
+ * run through the whole box path as sifg_box_device would run it alone --
+ * same catalogue bit for bit -- by a pool of n_engines engines working
+ * concurrently (each its own streams and buffers), largest box first.
+ * n_engines 0: the count sifg_box_batch_autotune found for batches of this
+ * size (tuned on the spot the first time). Each job's status and n_voids are
+ * written; the call returns the first failing job's status, or SIF_OK. No
+ * counterpart in the reference, which runs one box per call. */
+typedef struct {
+  const float* x; /* device, n_particles each */
+  const float* y;
+  const float* z;
+  uint64_t n_particles;
+  uint32_t n_grid;
+  float box;
+  uint32_t mesh_cells; /* 0: sif_finder_suggest_mesh_cells(n_particles, box, max radius, 0) */
+  const float* radii;  /* host */
+  uint32_t n_radii;
+  float threshold;
+  float overlap;
+  uint32_t options;
+  float* cx; /* host, capacity each */
+  float* cy;
+  float* cz;
+  float* r;
+  uint64_t capacity;
+  uint64_t n_voids; /* out */
+  int status;       /* out */
+} sifg_box_job_t;
+int sifg_box_batch_device(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines,
+                          uint32_t* n_engines_used);
+/* Times the batch at 1, 2, 4 and 8 engines, keeps the fastest for batches of
+ * this size (total particles and job count, to a factor of two) and returns
+ * it in *n_engines. The catalogues do not depend on the choice. */
+int sifg_box_batch_autotune(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t* n_engines);
 /* Statistics and timings of the last run (up to max_rungs entries). */
 uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs);
 void sifg_last_timings(sifg_timings_t* out);

@@ -50,7 +50,19 @@ EXPORTED = [
     "sifg_smooth_device_f64", "sifg_exodus_device_f64", "sifg_box_device_f64",
     # the adjoint
     "sifg_contrast_vjp_device", "sifg_contrast_vjp_device_f64",
+    # the batched form
+    "sifg_box_batch_device", "sifg_box_batch_autotune",
 ]
+
+
+class BoxJob(C.Structure):
+    """sifg_box_job_t (include/sif_gb300.h)."""
+    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("n_particles", C.c_uint64), ("n_grid", C.c_uint32), ("box", C.c_float),
+                ("mesh_cells", C.c_uint32), ("radii", C.c_void_p), ("n_radii", C.c_uint32),
+                ("threshold", C.c_float), ("overlap", C.c_float), ("options", C.c_uint32),
+                ("cx", C.c_void_p), ("cy", C.c_void_p), ("cz", C.c_void_p), ("r", C.c_void_p),
+                ("capacity", C.c_uint64), ("n_voids", C.c_uint64), ("status", C.c_int)]
 
 
 def load():
@@ -91,6 +103,8 @@ def load():
                                       vp, vp, vp, vp, u64, C.POINTER(u64)]),
         "sifg_contrast_vjp_device": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp]),
         "sifg_contrast_vjp_device_f64": (i32, [vp, vp, vp, u64, u32, f64, vp, vp, vp, vp]),
+        "sifg_box_batch_device": (i32, [C.POINTER(BoxJob), u32, u32, C.POINTER(u32)]),
+        "sifg_box_batch_autotune": (i32, [C.POINTER(BoxJob), u32, C.POINTER(u32)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

@@ -17,7 +17,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <map>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -53,7 +55,10 @@ std::string fmt(const char* f, ...) {
 }
 }  // namespace
 
+static std::mutex g_err_mu;  // set_error may be called from several batch workers
+
 void set_error(int status, const std::string& msg) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
   g_status = status;
   g_message = msg;
   log_msg(SIF_LOG_LEVEL_ERROR, "gb300", msg);
@@ -129,8 +134,8 @@ static void box_bounds(double box, double* lo, double* hi) {
 
 template <class R>
 static int check_in_box(const R* dx, const R* dy, const R* dz, uint64_t n, R box,
-                        const char* name, cudaStream_t st) {
-  unsigned long long* d = (unsigned long long*)bufs().bad.ensure(16);
+                        const char* name, cudaStream_t st, DevBuf& flag) {
+  unsigned long long* d = (unsigned long long*)flag.ensure(16);
   SIFG_CUDA(cudaMemsetAsync(d, 0, 16, st));
   R lo, hi;
   box_bounds(box, &lo, &hi);
@@ -398,7 +403,7 @@ int sif_grid_assign_cic(sif_grid_t* grid, const sif_field_t* field) {
   cudaStream_t s = e->stream();
   upload_positions(field, s);
   st = check_in_box(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(),
-                    field->n_particles, grid->box_length, "field", s);
+                    field->n_particles, grid->box_length, "field", s, bufs().bad);
   if (st != SIF_OK) return st;
   float* dg = (float*)bufs().grid.ensure(grid->total_cells * sizeof(float));
   e->scratch.ensure(cic_scratch_bytes(field->n_particles, grid->n_cells));
@@ -468,7 +473,7 @@ static sif_chain_mesh_t* mesh_alloc(uint32_t n_cells, sif_real box, sif_field_t*
   cudaStream_t s = e->stream();
   upload_positions(field, s);
   if (check_in_box(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(), n, box,
-                   "field", s) != SIF_OK)
+                   "field", s, bufs().bad) != SIF_OK)
     return nullptr;
   DeviceMesh m;
   m.n_cells = n_cells;
@@ -779,7 +784,7 @@ static int cic_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n
   if (!e) return SIF_ERR_UNINITIALISED;
   if (n_grid < 4) return fail(SIF_ERR_INVALID, "n_grid: expected at least 4");
   cudaStream_t s = e->stream();
-  const int st = check_in_box(x, y, z, n, box, "field", s);
+  const int st = check_in_box(x, y, z, n, box, "field", s, e->io.flag);
   if (st != SIF_OK) return st;
   RunTimings tm;
   if constexpr (sizeof(R) == 4) {
@@ -816,7 +821,7 @@ static int mesh_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t 
   if (!e) return SIF_ERR_UNINITIALISED;
   if (n_cells == 0 || !(box > 0.0f)) return fail(SIF_ERR_INVALID, "mesh: bad geometry");
   cudaStream_t s = e->stream();
-  const int st = check_in_box(x, y, z, n, box, "field", s);
+  const int st = check_in_box(x, y, z, n, box, "field", s, e->io.flag);
   if (st != SIF_OK) return st;
   DeviceMeshT<R> m;
   m.n_cells = n_cells;
@@ -869,8 +874,9 @@ template <class R>
 static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceMeshT<R>& m,
                       const R* radii, uint32_t n_radii, R threshold, R overlap, uint32_t opt,
                       const R* inject, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
-                      uint64_t* n_voids, RunTimings& tm, cudaEvent_t mesh_ready = nullptr) {
-  if (check_args(radii, n_radii, threshold, overlap) != SIF_OK) return g_status;
+                      uint64_t* n_voids, RunTimings& tm, cudaEvent_t mesh_ready = nullptr,
+                      std::vector<RungStat>* stats = &g_stats) {
+  if (check_args(radii, n_radii, threshold, overlap) != SIF_OK) return kErrInvalid;
   RunParamsT<R> p;
   p.grid_n = n_grid;
   p.box = box;
@@ -883,8 +889,8 @@ static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceM
   p.inject_on_device = true;
   p.mesh_ready = mesh_ready;
   HostCatalogueT<R> cat;
-  g_stats.clear();
-  const int st = e->exodus(delta, m, p, cat, &g_stats, &tm);
+  if (stats) stats->clear();
+  const int st = e->exodus(delta, m, p, cat, stats, &tm);
   if (st != SIF_OK) return st;
   const uint64_t nv = cat.cx.size();
   if (n_voids) *n_voids = nv;
@@ -922,22 +928,22 @@ static int exodus_device(const R* delta, uint32_t n_grid, R box, const R* mx, co
   return st;
 }
 
+// The whole box path on one engine, with the engine's own buffers: the
+// device entry point's body, and one job of a batch. stats NULL: no
+// per-rung record (a batch worker).
 template <class R>
-static int box_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n_grid, R box,
-                      uint32_t mesh_cells, const R* radii, uint32_t n_radii, R threshold,
-                      R overlap, uint32_t opt, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
-                      uint64_t* n_voids) {
-  Engine* e = engine();
-  if (!e) return SIF_ERR_UNINITIALISED;
+static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, uint32_t n_grid,
+                   R box, uint32_t mesh_cells, const R* radii, uint32_t n_radii, R threshold,
+                   R overlap, uint32_t opt, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
+                   uint64_t* n_voids, RunTimings& tm, std::vector<RungStat>* stats) {
   if (n_grid < 4 || mesh_cells == 0) return fail(SIF_ERR_INVALID, "grid or mesh: bad size");
+  BoxBufs& io = e->io;
   cudaStream_t s = e->stream();
-  const auto t0 = std::chrono::steady_clock::now();
-  int st = check_in_box(x, y, z, n, box, "field", s);
+  int st = check_in_box(x, y, z, n, box, "field", s, io.flag);
   if (st != SIF_OK) return st;
   const uint64_t cells = (uint64_t)n_grid * n_grid * n_grid;
   const uint64_t mcells = (uint64_t)mesh_cells * mesh_cells * mesh_cells;
-  R* dg = (R*)(sizeof(R) == 4 ? bufs().grid : bufs().grid64).ensure(cells * sizeof(R));
-  RunTimings tm;
+  R* dg = (R*)io.grid.ensure(cells * sizeof(R));
   const size_t mesh_scratch = mesh_scratch_bytes(n, mesh_cells) * sizeof(R) / sizeof(float);
   if constexpr (sizeof(R) == 4) {
     e->scratch.ensure(std::max(cic_scratch_bytes(n, n_grid), mesh_scratch));
@@ -960,22 +966,127 @@ static int box_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n
   m.n_cells = mesh_cells;
   m.box_length = box;
   m.cell_length = box / (R)mesh_cells;
-  m.x = (R*)bufs().mx.ensure(n * sizeof(R));
-  m.y = (R*)bufs().my.ensure(n * sizeof(R));
-  m.z = (R*)bufs().mz.ensure(n * sizeof(R));
-  m.offsets = (uint32_t*)bufs().offs.ensure((mcells + 1) * 4);
+  m.x = (R*)io.mx.ensure(n * sizeof(R));
+  m.y = (R*)io.my.ensure(n * sizeof(R));
+  m.z = (R*)io.mz.ensure(n * sizeof(R));
+  m.offsets = (uint32_t*)io.offs.ensure((mcells + 1) * 4);
   m.orig = nullptr;
-  uint32_t* sums = (uint32_t*)bufs().mesh_sums.ensure(
+  uint32_t* sums = (uint32_t*)io.mesh_sums.ensure(
       (size_t)scan_sums_needed((uint32_t)(mcells + 1)) * sizeof(uint32_t));
   mesh_build(x, y, z, n, m, e->scratch.ptr, cs, &tm.mesh, sums);
   SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
-  double* cscratch = (double*)bufs().bad.ensure(density_contrast_scratch_bytes() + 64);
+  double* cscratch = (double*)io.mean.ensure(density_contrast_scratch_bytes() + 64);
   density_contrast(dg, cells, cscratch, s);
   st = run_device(e, dg, n_grid, box, m, radii, n_radii, threshold, overlap, opt, (const R*)nullptr,
-                  cx, cy, cz, r, capacity, n_voids, tm, e->ev_mesh_ready());
+                  cx, cy, cz, r, capacity, n_voids, tm, e->ev_mesh_ready(), stats);
+  return st;
+}
+
+template <class R>
+static int box_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n_grid, R box,
+                      uint32_t mesh_cells, const R* radii, uint32_t n_radii, R threshold,
+                      R overlap, uint32_t opt, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
+                      uint64_t* n_voids) {
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  const auto t0 = std::chrono::steady_clock::now();
+  RunTimings tm;
+  const int st = box_run(e, x, y, z, n, n_grid, box, mesh_cells, radii, n_radii, threshold,
+                         overlap, opt, cx, cy, cz, r, capacity, n_voids, tm, &g_stats);
   tm.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   record_timings(tm);
   return st;
+}
+
+// ---------------------------------------------------------------------------
+// The batched form: many independent boxes, each the whole box path, run by a
+// pool of engines (each its own streams, buffers and host thread) that take
+// the boxes largest first. Every box's catalogue is what sifg_box_device
+// gives for it alone: boxes share nothing but the GPU. How many engines run at
+// once is the one tuned parameter (sifg_box_batch_autotune).
+// ---------------------------------------------------------------------------
+
+static std::vector<std::unique_ptr<Engine>> g_pool;
+static std::map<std::pair<int, int>, uint32_t> g_tuned;  // (log2 particles, log2 jobs) -> engines
+
+static std::pair<int, int> batch_key(const sifg_box_job_t* jobs, uint32_t n_jobs) {
+  uint64_t total = 0;
+  for (uint32_t k = 0; k < n_jobs; k++) total += jobs[k].n_particles;
+  return {(int)std::log2((double)std::max<uint64_t>(total, 1)),
+          (int)std::log2((double)std::max<uint32_t>(n_jobs, 1))};
+}
+
+static void batch_worker(Engine* e, sifg_box_job_t* jobs, const std::vector<uint32_t>* order,
+                         std::atomic<uint32_t>* next) {
+  cudaSetDevice(e->device());
+  for (;;) {
+    const uint32_t k = next->fetch_add(1);
+    if (k >= order->size()) break;
+    sifg_box_job_t& j = jobs[(*order)[k]];
+    j.n_voids = 0;
+    try {
+      uint32_t mc = j.mesh_cells;
+      if (mc == 0) {
+        float rmax = 0.0f;
+        for (uint32_t i = 0; i < j.n_radii; i++) rmax = std::max(rmax, j.radii[i]);
+        mc = sif_finder_suggest_mesh_cells(j.n_particles, j.box, rmax, 0.0f);
+      }
+      RunTimings tm;
+      j.status = box_run<float>(e, j.x, j.y, j.z, j.n_particles, j.n_grid, j.box, mc, j.radii,
+                                j.n_radii, j.threshold, j.overlap, j.options, j.cx, j.cy, j.cz,
+                                j.r, j.capacity, &j.n_voids, tm, nullptr);
+    } catch (const CudaError& err) {
+      j.status = cuda_fail(err);
+    } catch (const std::bad_alloc&) {
+      j.status = fail(SIF_ERR_ALLOC, "batch: out of host memory");
+    }
+  }
+}
+
+static int run_batch(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines) {
+  Engine* main = engine();
+  if (!main) return SIF_ERR_UNINITIALISED;
+  if (!jobs && n_jobs) return fail(SIF_ERR_INVALID, "batch: NULL jobs");
+  if (n_jobs == 0) return SIF_OK;
+  n_engines = std::max(1u, std::min(n_engines, n_jobs));
+  while (g_pool.size() < n_engines) g_pool.emplace_back(new Engine(main->device()));
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  for (uint32_t k = 0; k < n_engines; k++) g_pool[k]->host_threads = (int)std::max(1u, hw / n_engines);
+  std::vector<uint32_t> order(n_jobs);
+  for (uint32_t k = 0; k < n_jobs; k++) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+    return jobs[a].n_particles > jobs[b].n_particles;
+  });
+  std::atomic<uint32_t> next{0};
+  std::vector<std::thread> threads;
+  for (uint32_t k = 0; k < n_engines; k++)
+    threads.emplace_back(batch_worker, g_pool[k].get(), jobs, &order, &next);
+  for (auto& t : threads) t.join();
+  cudaSetDevice(main->device());
+  for (uint32_t k = 0; k < n_jobs; k++)
+    if (jobs[k].status != SIF_OK) return jobs[k].status;
+  return SIF_OK;
+}
+
+// Times the batch at 1, 2, 4 and 8 engines (capped by the job count) and
+// keeps the fastest for batches of this size.
+static int autotune_batch(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t* best_out) {
+  uint32_t best = 1;
+  double best_ms = 1e300;
+  for (uint32_t k : {1u, 2u, 4u, 8u}) {
+    if (k > n_jobs && k > 1) break;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int st = run_batch(jobs, n_jobs, k);
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (st != SIF_OK) return st;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = k;
+    }
+  }
+  g_tuned[batch_key(jobs, n_jobs)] = best;
+  if (best_out) *best_out = best;
+  return SIF_OK;
 }
 
 extern "C" {
@@ -1055,6 +1166,28 @@ int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, 
   SIFG_LOCKED(box_device(x, y, z, n, n_grid, box, mesh_cells, radii, n_radii, threshold, overlap,
                          opt, cx, cy, cz, r, capacity, n_voids))
 }
+int sifg_box_batch_device(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines,
+                          uint32_t* n_engines_used) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  if (n_engines == 0) {
+    auto it = g_tuned.find(batch_key(jobs, n_jobs));
+    if (it != g_tuned.end()) {
+      n_engines = it->second;
+    } else {
+      const int st = autotune_batch(jobs, n_jobs, &n_engines);
+      if (st != SIF_OK) return st;
+    }
+  }
+  if (n_engines_used) *n_engines_used = std::max(1u, std::min(n_engines, std::max(n_jobs, 1u)));
+  return run_batch(jobs, n_jobs, n_engines);
+  API_GUARD_END(SIF_ERR_INVALID)
+}
+
+int sifg_box_batch_autotune(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t* n_engines) {
+  SIFG_LOCKED(autotune_batch(jobs, n_jobs, n_engines))
+}
+
 int sifg_box_device_f64(const double* x, const double* y, const double* z, uint64_t n,
                         uint32_t n_grid, double box, uint32_t mesh_cells, const double* radii,
                         uint32_t n_radii, double threshold, double overlap, uint32_t opt,

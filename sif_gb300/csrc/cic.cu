@@ -450,7 +450,7 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   const float cl = box / (float)n;
   const float inv_cell_vol = 1.0f / (float)(cl * cl * cl);
   const size_t smem = (size_t)2 * TS * TS * TS * sizeof(uint32_t);
-  static bool attr = false;
+  thread_local bool attr = false;  // a per-thread flag: the attribute is set once per thread
   if (!attr) {
     SIFG_CUDA(cudaFuncSetAttribute(tile_deposit_kernel,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -63,6 +63,11 @@ struct HostCatalogueT {
 };
 using HostCatalogue = HostCatalogueT<float>;
 
+// Device buffers of one engine's box path (grid, mesh, flags).
+struct BoxBufs {
+  DevBuf grid, mx, my, mz, offs, mesh_sums, flag, mean;
+};
+
 class Engine {
  public:
   explicit Engine(int device);
@@ -82,6 +87,7 @@ class Engine {
              HostCatalogueT<R>& out, std::vector<RungStat>* stats, RunTimings* timings);
 
   DevBuf scratch;  // shared scratch for CIC / mesh builds
+  BoxBufs io;      // the box path's buffers
   Smoother smoother;        // the float form's
   SmootherT<double> smoother64;  // the FP64 form's
   template <class R>

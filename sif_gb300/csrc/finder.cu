@@ -768,7 +768,7 @@ void build_survivor_grid(const R* scx, const R* scy, const R* scz,
                                                                    start, cell_of);
   SIFG_LAUNCH_CHECK();
   exclusive_scan_u32(start, cells + 1, st);
-  static DevBuf cursor;
+  thread_local DevBuf cursor;  // one per host thread driving a stream
   uint32_t* cur = (uint32_t*)cursor.ensure((cells + 1) * sizeof(uint32_t));
   SIFG_CUDA(cudaMemcpyAsync(cur, start, (cells + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
   scatter_ids_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(cell_of, d_count, 0, cur, ids);
@@ -1046,7 +1046,7 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
   void_count_kernel<<<grid_for(n, 256), 256, 0, st>>>(cx, cy, cz, n, inv, start, cell_of);
   SIFG_LAUNCH_CHECK();
   exclusive_scan_u32(start, cells + 1, st);
-  static DevBuf cursor;
+  thread_local DevBuf cursor;  // one per host thread driving a stream
   uint32_t* cur = (uint32_t*)cursor.ensure((cells + 1) * sizeof(uint32_t));
   SIFG_CUDA(cudaMemcpyAsync(cur, start, (cells + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
   scatter_ids_kernel<<<grid_for(n, 256), 256, 0, st>>>(cell_of, nullptr, n, cur, ids);

@@ -101,7 +101,7 @@ uint32_t scan_sums_needed(uint32_t n) { return (n + kScanChunk - 1) / kScanChunk
 void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st, uint32_t* sums_scratch) {
   if (n == 0) return;
   const uint32_t blocks = (n + kScanChunk - 1) / kScanChunk;
-  static DevBuf sums;  // chunk totals; small
+  thread_local DevBuf sums;  // chunk totals; small; one per host thread driving a stream
   uint32_t* s = sums_scratch ? sums_scratch
                              : (uint32_t*)sums.ensure((size_t)blocks * sizeof(uint32_t));
   scan_reduce_kernel<<<blocks, kScanThreads, 0, st>>>(data, n, s);

@@ -152,3 +152,34 @@ def launch_count():
 
 def set_window(bins):
     _lib.load().sifg_set_window(int(bins))
+
+
+def box_batch(boxes, engines=0, capacity=1 << 20, check=True):
+    """The batched form: boxes = [dict(x, y, z, n_grid, box, radii, threshold,
+    mesh_cells=0, overlap=0.0, options=0)], particles as float32 CUDA tensors.
+    Returns (catalogues, engines used); each catalogue is what box() returns
+    for that box alone."""
+    lib = _lib.load()
+    jobs = (_lib.BoxJob * len(boxes))()
+    keep = []
+    for j, b in zip(jobs, boxes):
+        radii = np.ascontiguousarray(b["radii"], dtype=np.float32)
+        cols = _catalogue_arrays(capacity)
+        keep.append((radii, cols))
+        j.x, j.y, j.z = (b[k].data_ptr() for k in ("x", "y", "z"))
+        j.n_particles = b["x"].numel()
+        j.n_grid, j.box = b["n_grid"], b["box"]
+        j.mesh_cells = b.get("mesh_cells", 0)
+        j.radii, j.n_radii = radii.ctypes.data, len(radii)
+        j.threshold, j.overlap, j.options = b["threshold"], b.get("overlap", 0.0), b.get("options", 0)
+        j.cx, j.cy, j.cz, j.r = (c.ctypes.data for c in cols)
+        j.capacity = capacity
+    used = C.c_uint32(0)
+    st = lib.sifg_box_batch_device(jobs, len(boxes), engines, C.byref(used))
+    if check:
+        _check(st, "box_batch")
+    cats = [tuple(c[: min(j.n_voids, capacity)].copy() for c in cols)
+            for j, (_, cols) in zip(jobs, keep)]
+    if not check:
+        return cats, used.value, [j.status for j in jobs]
+    return cats, used.value

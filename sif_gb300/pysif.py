@@ -189,7 +189,26 @@ def _exodus_raw(grid, mesh, radii, threshold, overlap_fraction=0.0, *, overlap_t
     return _take_catalogue(lib, ptr, "exodus_raw")
 
 
-finders = types.SimpleNamespace(exodus=_exodus, exodus_raw=_exodus_raw)
+def _suggest_mesh_cells(n_particles, box_length, max_radius=0.0, volume=0.0):
+    """pysif.finders.suggest_mesh_cells: sif_finder_suggest_mesh_cells
+    (include/sif/finder/exodus_finder.h:653-683), the same rule: about 30
+    tracers per cell, no coarser than the widest search stencil, 8..1024."""
+    import math
+
+    if n_particles <= 0 or not (box_length > 0) or not math.isfinite(box_length) or \
+            not (volume >= 0) or not math.isfinite(volume):
+        return 0
+    whole = n_particles * box_length ** 3 / volume if volume > 0 else float(n_particles)
+    cells = (whole / 30.0) ** (1.0 / 3.0)
+    if max_radius > 0:
+        if 2.0 * max_radius >= box_length:
+            return 0
+        cells = max(cells, box_length / (box_length - 2.0 * max_radius) + 1.0)
+    return int(min(max(cells, 8.0), 1024.0))
+
+
+finders = types.SimpleNamespace(exodus=_exodus, exodus_raw=_exodus_raw,
+                                suggest_mesh_cells=_suggest_mesh_cells)
 
 
 def smoothed_contrast(x, y, z, n_grid, box, radius, filter="gaussian", window="full"):

@@ -19,9 +19,48 @@ def lib():
 
 
 def _declared():
+    """The header's functions the library must export (static inline ones,
+    which a caller compiles from the header, excepted)."""
     text = open(os.path.join(ROOT, "include", "sif_gb300.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b((?:sif|sifg)_[a-z0-9_]+)\s*\(", text)))
+    inline = set(re.findall(r"static inline [^(]*?\b((?:sif|sifg)_[a-z0-9_]+)\s*\(", text))
+    return sorted(set(re.findall(r"\b((?:sif|sifg)_[a-z0-9_]+)\s*\(", text)) - inline)
+
+
+def test_suggest_mesh_cells_is_the_reference_rule():
+    """sif_finder_suggest_mesh_cells (exodus_finder.h:653-683), compiled from
+    the header, against the rule restated here: 30 tracers per cell,
+    a floor from the widest stencil, clamped to [8, 1024]."""
+    import subprocess
+    import tempfile
+
+    src = ('#include "sif_gb300.h"\n#include <stdio.h>\nint main(void) {\n'
+           '  printf("%u %u %u %u %u %u\\n", sif_finder_suggest_mesh_cells(134217728ull, 1000.f, 24.f, 0.f),\n'
+           '         sif_finder_suggest_mesh_cells(2097152ull, 500.f, 30.f, 0.f),\n'
+           '         sif_finder_suggest_mesh_cells(1000ull, 100.f, 45.f, 0.f),\n'
+           '         sif_finder_suggest_mesh_cells(64ull * 64 * 64, 200.f, 8.f, 8e6f),\n'
+           '         sif_finder_suggest_mesh_cells(0ull, 100.f, 5.f, 0.f),\n'
+           '         sif_finder_suggest_mesh_cells(1ull << 40, 1000.f, 5.f, 0.f));\n  return 0;\n}\n')
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "t")
+        subprocess.run(["gcc", "-O2", "-I", os.path.join(ROOT, "include"), c, "-o", exe, "-lm"],
+                       check=True)
+        got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
+
+    def rule(n, L, rmax, vol):
+        whole = n * L ** 3 / vol if vol > 0 else n
+        cells = (whole / 30.0) ** (1 / 3)
+        if rmax > 0:
+            if 2 * rmax >= L:
+                return 0
+            cells = max(cells, L / (L - 2 * rmax) + 1)
+        return int(min(max(cells, 8.0), 1024.0)) if n else 0
+
+    want = [rule(134217728, 1000, 24, 0), rule(2097152, 500, 30, 0), rule(1000, 100, 45, 0),
+            rule(64 ** 3, 200, 8, 8e6), 0, rule(1 << 40, 1000, 5, 0)]
+    assert got == want, (got, want)
 
 
 def test_header_declares_the_reference_entry_points():
