@@ -289,15 +289,21 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const R vol_factor = (4.0f / 3.0f) * kPi<R> * mean_density;
 
   uint32_t n_voids = 0;
-  size_t cat_cap = 0;
+  // The catalogue's buffers keep their size from run to run (a cudaFree
+  // waits for the whole device, which would stall every other engine of a
+  // batch); they grow, keeping the voids so far, only when a run needs more.
   auto ensure_cat = [&](size_t want) {
-    if (want <= cat_cap) return;
+    const size_t have = cat_x_.bytes / sizeof(R);
+    if (want <= have && cat_r_.ptr && vids_.bytes >= want * sizeof(uint32_t) &&
+        vcell_.bytes >= want * sizeof(uint32_t))
+      return;
     size_t cap = std::max<size_t>(want + want / 2, 1 << 16);
     DevBuf* bufs[4] = {&cat_x_, &cat_y_, &cat_z_, &cat_r_};
     for (DevBuf* b : bufs) {
+      if (b->ptr && b->bytes >= cap * sizeof(R)) continue;
       void* fresh = nullptr;
       SIFG_CUDA(cudaMalloc(&fresh, cap * sizeof(R)));
-      if (n_voids)
+      if (n_voids && b->ptr)
         SIFG_CUDA(cudaMemcpyAsync(fresh, b->ptr, n_voids * sizeof(R), cudaMemcpyDeviceToDevice, st_));
       SIFG_CUDA(cudaStreamSynchronize(st_));
       b->release();
@@ -306,7 +312,6 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     }
     vids_.ensure(cap * sizeof(uint32_t));
     vcell_.ensure(cap * sizeof(uint32_t));
-    cat_cap = cap;
   };
   ensure_cat(1 << 16);
   const uint32_t vcells = kVoidCells * kVoidCells * kVoidCells;

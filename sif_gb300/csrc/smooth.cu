@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -160,8 +161,11 @@ SmootherT<R>::~SmootherT() {
 
 template <class R>
 void SmootherT<R>::release() {
-  if (plan_r2c) cufftDestroy(plan_r2c);
-  if (plan_c2r) cufftDestroy(plan_c2r);
+  for (const Plans& p : plans) {
+    cufftDestroy(p.r2c);
+    cufftDestroy(p.c2r);
+  }
+  plans.clear();
   plan_r2c = plan_c2r = 0;
   n = 0;
 }
@@ -169,15 +173,27 @@ void SmootherT<R>::release() {
 template <class R>
 void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st) {
   constexpr bool dbl = sizeof(R) == 8;
-  if (n_ != n) {
-    release();
+  bool rebind = false;
+  if (n_ != n || !plan_r2c) {
+    auto it = std::find_if(plans.begin(), plans.end(), [&](const Plans& p) { return p.n == n_; });
+    if (it == plans.end()) {
+      if ((int)plans.size() >= kPlanCache) {
+        cufftDestroy(plans.front().r2c);
+        cufftDestroy(plans.front().c2r);
+        plans.erase(plans.begin());
+      }
+      Plans p{n_, 0, 0};
+      SIFG_CUFFT(cufftPlan3d(&p.r2c, (int)n_, (int)n_, (int)n_, dbl ? CUFFT_D2Z : CUFFT_R2C));
+      SIFG_CUFFT(cufftPlan3d(&p.c2r, (int)n_, (int)n_, (int)n_, dbl ? CUFFT_Z2D : CUFFT_C2R));
+      plans.push_back(p);
+      it = plans.end() - 1;
+    }
     n = n_;
-    SIFG_CUFFT(cufftPlan3d(&plan_r2c, (int)n, (int)n, (int)n, dbl ? CUFFT_D2Z : CUFFT_R2C));
-    SIFG_CUFFT(cufftPlan3d(&plan_c2r, (int)n, (int)n, (int)n, dbl ? CUFFT_Z2D : CUFFT_C2R));
-    SIFG_CUFFT(cufftSetStream(plan_r2c, st));
-    SIFG_CUFFT(cufftSetStream(plan_c2r, st));
-    stream = st;
-  } else if (st != stream) {
+    plan_r2c = it->r2c;
+    plan_c2r = it->c2r;
+    rebind = true;  // a cached plan may be bound to another stream
+  }
+  if (rebind || st != stream) {
     SIFG_CUFFT(cufftSetStream(plan_r2c, st));
     SIFG_CUFFT(cufftSetStream(plan_c2r, st));
     stream = st;

@@ -22,8 +22,16 @@ struct SmootherT {
   R box = 0;
   int window_mode = 1;
   cudaStream_t stream = 0;
-  cufftHandle plan_r2c = 0, plan_c2r = 0;
+  cufftHandle plan_r2c = 0, plan_c2r = 0;  // the plans for n
   DevBuf spectrum, work, lut, win;
+  // Plans by grid size, kept between runs (destroying one frees its work
+  // area, a device-wide wait): at most kPlanCache sizes, oldest out.
+  static constexpr int kPlanCache = 8;
+  struct Plans {
+    uint32_t n;
+    cufftHandle r2c, c2r;
+  };
+  std::vector<Plans> plans;
 
   void setup(uint32_t n, R box, int window_mode, cudaStream_t st);
   void forward(const R* grid);  // grid: n^3 values on the device
