@@ -1076,8 +1076,31 @@ static int cmp_desc(const void* a, const void* b) {
   return (x < y) - (x > y);
 }
 
+/* is_minimum of src/finder/utils.c:243-259 over the 27-node stencil of
+ * load_stencil (utils.c:221-241): the node is strictly below every neighbour
+ * at a lower flat index and not above any at a higher one, so of a run of
+ * equal values exactly the lowest-indexed is a minimum. */
+static int is_minimum_node(const float* f, uint32_t n, uint64_t i) {
+  const uint32_t ix = (uint32_t)(i / ((uint64_t)n * n)), iy = (uint32_t)((i / n) % n),
+                 iz = (uint32_t)(i % n);
+  const uint32_t xs[3] = {(ix + n - 1) % n, ix, (ix + 1) % n};
+  const uint32_t ys[3] = {(iy + n - 1) % n, iy, (iy + 1) % n};
+  const uint32_t zs[3] = {(iz + n - 1) % n, iz, (iz + 1) % n};
+  const float v = f[i];
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++)
+      for (int c = 0; c < 3; c++) {
+        const uint64_t j = ((uint64_t)xs[a] * n + ys[b]) * n + zs[c];
+        if (a == 1 && b == 1 && c == 1)
+          continue;
+        if (j < i ? !(v < f[j]) : !(v <= f[j]))
+          return 0;
+      }
+  return 1;
+}
+
 /* The rung loop of sif__exodus_run (src/finder/exodus_finder.c:1585-2492)
- * for a box, unweighted, SIF_FINDER_SEEDS_CELLS on their nodes: per rung the
+ * for a box, unweighted, seeds on their nodes: per rung the
  * top-hat smoothing, the scan and sort, the reach, the template, the
  * pre-filter at the rung, then speculative batches -- phase 0 (masked skip),
  * phase 1 (pole probe, exact overlap, collision witness, rescaling; in
@@ -1096,8 +1119,13 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   if (!(threshold > -1.0f && threshold < 0.0f) || !(f >= 0.0f && f <= 1.0f) ||
       n_radii == 0 || mesh->box_length != box)
     return -2;
-  if (opt & ((1u << 9) | (3u << 19) | (1u << 21) | (1u << 22)))
-    return -5; /* minima, refinement, extended reach, displacement */
+  if (opt & ((3u << 19) | (1u << 21) | (1u << 22)))
+    return -5; /* refinement, extended reach, displacement */
+  /* SIF_FINDER_SEEDS_MINIMA without refinement: the candidates are the
+   * below-threshold, unmasked nodes that are local minima of the rung's field
+   * (sif__finder_scan_refined with minima_only, utils.c:406-552); nothing
+   * else of the run changes (exodus_finder.c:287-292). */
+  const int minima = (opt & (1u << 9)) != 0;
 
   float* radii = malloc(n_radii * sizeof(float));
   memcpy(radii, radii_in, n_radii * sizeof(float));
@@ -1140,14 +1168,14 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
     /* The scan, src/finder/utils.c:130-213: flat order, then the sort. */
     uint64_t nc = 0;
     for (uint64_t i = 0; i < total; i++)
-      nc += field[i] <= threshold && !mask_get(mask, i);
+      nc += field[i] <= threshold && !mask_get(mask, i) && (!minima || is_minimum_node(field, N, i));
     if (nc > cand_cap) {
       cand_cap = nc;
       cand = realloc(cand, cand_cap * sizeof(orc_candidate_t));
     }
     nc = 0;
     for (uint64_t i = 0; i < total; i++)
-      if (field[i] <= threshold && !mask_get(mask, i)) {
+      if (field[i] <= threshold && !mask_get(mask, i) && (!minima || is_minimum_node(field, N, i))) {
         cand[nc].delta = field[i];
         cand[nc].refined = 0;
         cand[nc].flat = i;

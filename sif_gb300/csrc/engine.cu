@@ -1,6 +1,6 @@
 // The exodus run on one GPU: the rung loop of sif__exodus_run
 // (src/finder/exodus_finder.c:1585-2492) for a periodic box, unweighted,
-// SIF_FINDER_SEEDS_CELLS on their nodes.
+// seeds (every cell, or the local minima) on their nodes.
 //
 // Per rung, on one stream:
 //   smooth (filter + C2R)  ->  candidate count  ->  [host: M]  ->  candidate
@@ -240,10 +240,10 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const R cell = box / (R)N;
   const R threshold = p.threshold, f = p.overlap;
   const uint32_t opt = p.options;
-  if (opt & (kOptSeedsMinima | kOptRefineMask | kOptExtendReach | kOptDisplace)) {
+  if (opt & (kOptRefineMask | kOptExtendReach | kOptDisplace)) {
     set_error(kErrUnsupported,
-              "options: minima seeds, centre refinement, extended reach and displacement are not "
-              "supported by the GPU finder");
+              "options: centre refinement, extended reach and displacement are not supported by "
+              "the GPU finder");
     return kErrUnsupported;
   }
   if (cells >= (1ull << 32)) {
@@ -254,6 +254,9 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   static const R factors[4] = {1.5f, 1.25f, 1.75f, 2.0f};
   const R search_factor = factors[(opt >> 12) & 3u];
   const int window_mode = (opt & kOptKeepWindow) ? 0 : ((opt & kOptAliasing) ? 2 : 1);
+  // SIF_FINDER_SEEDS_MINIMA without refinement changes the candidates alone:
+  // the local minima of the rung's field among them (exodus_finder.c:287-292).
+  const bool minima = (opt & kOptSeedsMinima) != 0;
 
   std::vector<R> radii = p.radii;
   std::sort(radii.begin(), radii.end(), [](R a, R b) { return a > b; });
@@ -356,7 +359,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     }
 
     // 2. Candidates, in flat order.
-    scan_count_pass(field, mask, cells, threshold, blocks, dcount, st_);
+    scan_count_pass(field, mask, cells, threshold, blocks, dcount, st_, N, minima);
     SIFG_CUDA(cudaMemcpyAsync(h_counters_, dcount, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
     const auto t_wait = clk::now();
     SIFG_CUDA(cudaStreamSynchronize(st_));
@@ -379,7 +382,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
 
     R* cdelta = grow_to<R>(cand_delta_, m);
     uint32_t* cflat = grow_to<uint32_t>(cand_flat_, m);
-    scan_write_pass(field, mask, cells, threshold, blocks, cdelta, cflat, st_);
+    scan_write_pass(field, mask, cells, threshold, blocks, cdelta, cflat, st_, N, minima);
     SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
     ensure_host(m);
     SIFG_CUDA(cudaMemcpyAsync(h_delta_, cdelta, m * sizeof(R), cudaMemcpyDeviceToHost, st_));

@@ -53,11 +53,38 @@ __device__ __forceinline__ void load4(const double* __restrict__ f, uint64_t c0,
   v[3] = b.y;
 }
 
+// is_minimum of src/finder/utils.c:243-259 on the 27-node stencil of
+// load_stencil (utils.c:221-241): strictly below every neighbour at a lower
+// flat index, not above any at a higher one, so of a run of equal values
+// exactly the lowest-indexed node is a minimum.
+template <class R>
+__device__ bool is_minimum(const R* __restrict__ f, uint32_t n, uint64_t i) {
+  const uint64_t nn = (uint64_t)n * n;
+  const uint32_t ix = (uint32_t)(i / nn), iy = (uint32_t)((i / n) % n), iz = (uint32_t)(i % n);
+  const uint32_t xs[3] = {(ix + n - 1) % n, ix, (ix + 1) % n};
+  const uint32_t ys[3] = {(iy + n - 1) % n, iy, (iy + 1) % n};
+  const uint32_t zs[3] = {(iz + n - 1) % n, iz, (iz + 1) % n};
+  const R v = __ldg(f + i);
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++)
+      for (int c = 0; c < 3; c++) {
+        if (a == 1 && b == 1 && c == 1) continue;
+        const uint64_t j = (uint64_t)xs[a] * nn + (uint64_t)ys[b] * n + zs[c];
+        const R w = __ldg(f + j);
+        if (j < i ? !(v < w) : !(v <= w)) return false;
+      }
+  return true;
+}
+
 // The candidate bits of cells c0..c0+3 (bit j for c0 + j), and their depths.
+// With `minima` (SIF_FINDER_SEEDS_MINIMA, no refinement) a cell must also be
+// a local minimum of the field (sif__finder_scan_refined with minima_only,
+// utils.c:406-552); grid_n is the grid's side.
 template <class R>
 __device__ __forceinline__ uint32_t quad_candidates(const R* __restrict__ f,
                                                     const uint32_t* __restrict__ mask,
-                                                    uint64_t c0, uint64_t n, R thr, R* v) {
+                                                    uint64_t c0, uint64_t n, R thr, R* v,
+                                                    uint32_t grid_n, bool minima) {
   if (c0 + 3 < n) {
     load4(f, c0, v);
   } else {
@@ -69,6 +96,11 @@ __device__ __forceinline__ uint32_t quad_candidates(const R* __restrict__ f,
 #pragma unroll
   for (int k = 0; k < 4; k++)
     bits |= (v[k] <= thr && !(m & (1u << k)) && c0 + k < n) ? (1u << k) : 0u;
+  if (minima)
+    for (uint32_t b = bits; b; b &= b - 1) {
+      const int k = __ffs(b) - 1;
+      if (!is_minimum(f, grid_n, c0 + k)) bits &= ~(1u << k);
+    }
   return bits;
 }
 
@@ -99,14 +131,16 @@ template <class R>
 __global__ void __launch_bounds__(kScanT) scan_count_kernel(const R* __restrict__ f,
                                                             const uint32_t* __restrict__ mask,
                                                             uint64_t n, R thr,
-                                                            uint32_t* __restrict__ counts) {
+                                                            uint32_t* __restrict__ counts,
+                                                            uint32_t grid_n, bool minima) {
   __shared__ uint32_t ws[kScanT / 32];
   const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
   uint32_t c = 0;
 #pragma unroll
   for (int j = 0; j < kScanRounds; j++) {
     R v[4];
-    c += __popc(quad_candidates(f, mask, base + ((uint64_t)j * kScanT + threadIdx.x) * 4, n, thr, v));
+    c += __popc(quad_candidates(f, mask, base + ((uint64_t)j * kScanT + threadIdx.x) * 4, n, thr, v,
+                                grid_n, minima));
   }
   c = __reduce_add_sync(0xffffffffu, c);
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
@@ -121,14 +155,15 @@ __global__ void __launch_bounds__(kScanT) scan_count_kernel(const R* __restrict_
 template <class R>
 __global__ void __launch_bounds__(kScanT) scan_write_kernel(
     const R* __restrict__ f, const uint32_t* __restrict__ mask, uint64_t n, R thr,
-    const uint32_t* __restrict__ offsets, R* __restrict__ cdelta, uint32_t* __restrict__ cflat) {
+    const uint32_t* __restrict__ offsets, R* __restrict__ cdelta, uint32_t* __restrict__ cflat,
+    uint32_t grid_n, bool minima) {
   __shared__ uint32_t ws[kScanT / 32];
   const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
   uint32_t out = offsets[blockIdx.x];
   for (int j = 0; j < kScanRounds; j++) {
     const uint64_t c0 = base + ((uint64_t)j * kScanT + threadIdx.x) * 4;
     R v[4];
-    const uint32_t bits = quad_candidates(f, mask, c0, n, thr, v);
+    const uint32_t bits = quad_candidates(f, mask, c0, n, thr, v, grid_n, minima);
     uint32_t total;
     uint32_t pos = out + block_scan_excl(__popc(bits), ws, &total);
 #pragma unroll
@@ -150,9 +185,11 @@ __global__ void store_total_kernel(const uint32_t* __restrict__ offsets, uint32_
 
 template <class R>
 void scan_count_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
-                     uint32_t* block_counts, uint32_t* d_count, cudaStream_t st) {
+                     uint32_t* block_counts, uint32_t* d_count, cudaStream_t st, uint32_t grid_n,
+                     bool minima) {
   const uint32_t nb = scan_blocks(n_cells);
-  scan_count_kernel<<<nb, kScanT, 0, st>>>(field, mask, n_cells, threshold, block_counts);
+  scan_count_kernel<<<nb, kScanT, 0, st>>>(field, mask, n_cells, threshold, block_counts, grid_n,
+                                           minima);
   SIFG_LAUNCH_CHECK();
   SIFG_CUDA(cudaMemsetAsync(block_counts + nb, 0, sizeof(uint32_t), st));
   exclusive_scan_u32(block_counts, nb + 1, st);
@@ -163,9 +200,10 @@ void scan_count_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R t
 template <class R>
 void scan_write_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
                      const uint32_t* block_counts, R* cand_delta, uint32_t* cand_flat,
-                     cudaStream_t st) {
+                     cudaStream_t st, uint32_t grid_n, bool minima) {
   scan_write_kernel<<<scan_blocks(n_cells), kScanT, 0, st>>>(field, mask, n_cells, threshold,
-                                                             block_counts, cand_delta, cand_flat);
+                                                             block_counts, cand_delta, cand_flat,
+                                                             grid_n, minima);
   SIFG_LAUNCH_CHECK();
 }
 
@@ -1058,9 +1096,9 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
 // ---------------------------------------------------------------------------
 #define SIFG_FINDER_FORM(R)                                                                        \
   template void scan_count_pass<R>(const R*, const uint32_t*, uint64_t, R, uint32_t*, uint32_t*,   \
-                                   cudaStream_t);                                                  \
+                                   cudaStream_t, uint32_t, bool);                                  \
   template void scan_write_pass<R>(const R*, const uint32_t*, uint64_t, R, const uint32_t*, R*,    \
-                                   uint32_t*, cudaStream_t);                                       \
+                                   uint32_t*, cudaStream_t, uint32_t, bool);                       \
   template void prefilter<R>(const uint32_t*, uint32_t, const uint32_t*, VoidViewT<R>,             \
                              RungConstsT<R>, uint8_t*, uint32_t*, uint32_t*, uint32_t*, R*, R*,    \
                              R*, uint32_t*, cudaStream_t);                                         \

@@ -116,17 +116,20 @@ using Survivors = SurvivorsT<float>;
 // --- host wrappers (finder.cu), instantiated for float and double ---
 
 // Candidate scan (src/finder/utils.c:130-213): cells with delta <= threshold
-// whose mask bit is clear, in flat order. The count pass leaves per-block
-// offsets in `block_counts` (scan_blocks(n) + 1 entries) and the total in
-// *d_count; the write pass fills the candidates.
+// whose mask bit is clear, in flat order; with `minima` only those that are
+// local minima of the field (SIF_FINDER_SEEDS_MINIMA, utils.c:406-552).
+// The count pass leaves per-block offsets in `block_counts`
+// (scan_blocks(n) + 1 entries) and the total in *d_count; the write pass
+// fills the candidates. grid_n: the grid's side.
 uint32_t scan_blocks(uint64_t n_cells);
 template <class R>
 void scan_count_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
-                     uint32_t* block_counts, uint32_t* d_count, cudaStream_t st);
+                     uint32_t* block_counts, uint32_t* d_count, cudaStream_t st, uint32_t grid_n,
+                     bool minima);
 template <class R>
 void scan_write_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
                      const uint32_t* block_counts, R* cand_delta, uint32_t* cand_flat,
-                     cudaStream_t st);
+                     cudaStream_t st, uint32_t grid_n, bool minima);
 
 // Pre-filter at the rung radius (prefilter_cells, exodus_finder.c:871-944)
 // and compaction of the survivors, candidate order kept.

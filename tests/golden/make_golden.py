@@ -10,7 +10,8 @@ golden_box32.npz -- a 32^3 Zel'dovich box (side 128, rms displacement 4,
   (sif_grid_assign_cic, sif_grid_to_density_contrast); its chain mesh
   (positions, offsets, source indices); the 12 per-rung smoothed fields its
   own run produced (captured from sif__fft_grid_backward); and its catalogue
-  for several option sets, each run on exactly those fields.
+  for several option sets (SIF_FINDER_SEEDS_MINIMA among them), each run on
+  exactly those fields.
 
 golden_box32_f64.npz -- the same box through the reference's SIF_USE_DOUBLE
   build (sif_real = double): the float positions moved by a seeded jitter of
@@ -38,6 +39,7 @@ OPTION_SETS = [
     ("search_1_25", 0.0, abi.SIF_FINDER_SEARCH_1_25),
     ("lagrangian", 0.0, abi.SIF_FINDER_LAGRANGIAN_OVERLAP),
     ("overlap_0_5", 0.5, 0),
+    ("minima", 0.0, abi.SIF_FINDER_SEEDS_MINIMA),
 ]
 
 BOX32 = dict(n=32, box=128.0, rms_disp=4.0, seed=11, r0=8.0, threshold=-0.7, mesh=8)

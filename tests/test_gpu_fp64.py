@@ -14,7 +14,7 @@ from sif_gb300 import synth
 
 pytestmark = pytest.mark.gpu
 
-NAMES = ["default", "search_2_00", "search_1_25", "lagrangian", "overlap_0_5"]
+NAMES = ["default", "search_2_00", "search_1_25", "lagrangian", "overlap_0_5", "minima"]
 
 
 def _cuda(*arrays):

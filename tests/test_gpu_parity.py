@@ -151,7 +151,7 @@ def _golden_mesh(g):
     return _cuda(g["mesh_x"], g["mesh_y"], g["mesh_z"], g["mesh_offsets"].astype(np.int32))
 
 
-@pytest.mark.parametrize("name", ["default", "search_2_00", "search_1_25", "lagrangian",
+@pytest.mark.parametrize("name", ["default", "search_2_00", "search_1_25", "lagrangian", "minima",
                                   "overlap_0_5"])
 def test_catalogue_matches_reference_golden(dev, golden_box32, name):
     """The reference's own catalogue, on the fields its own run smoothed."""

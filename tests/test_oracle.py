@@ -40,7 +40,7 @@ def test_oracle_cic_f64_close_to_reference_float_cic(oracle, golden_box32):
     assert abs(f64.sum() * cl ** 3 - len(g["x"])) < 1e-6 * len(g["x"])
 
 
-@pytest.mark.parametrize("name", ["default", "search_2_00", "search_1_25", "lagrangian",
+@pytest.mark.parametrize("name", ["default", "search_2_00", "search_1_25", "lagrangian", "minima",
                                   "overlap_0_5"])
 def test_oracle_catalogue_matches_golden(oracle, golden_box32, name):
     g = golden_box32
