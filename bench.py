@@ -231,6 +231,8 @@ def gpu_arm(args, rank, world):
         adj = adjoint_run(args)
         batch = batch_run(args)
 
+    precision = precision_run(args) if args.precision else None
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_run(seconds=args.cpu_seconds)
@@ -254,6 +256,7 @@ def gpu_arm(args, rank, world):
         "fp64_form": fp64,
         "adjoint": adj,
         "batched_form": batch,
+        "precision_1024": precision,
         "cpu_baseline": cpu,
         "stages_ms_last_step": {"growth": round(tm["growth_ms"], 3), "cic_deposit": round(tm["cic_ms"], 3),
                                 "mesh": round(tm["mesh_ms"], 3), "filter": round(tm["filter_ms"], 3),
@@ -402,6 +405,67 @@ def batch_run(args):
             "speedup_vs_one_engine": round(seq_ms / ms, 3), "n_particles": total, "n_voids": nv}
 
 
+# The precision workload: 1024^3 particles in a 2000 Mpc/h box (rms
+# displacement 4, seed 1003), grid 1024^3. The float form's CIC contrast and
+# smoothed fields against the FP64 form's on the same positions (top-hat
+# R = 4 with the CIC window correction, the finder's smoothing; Gaussian
+# R = 5), and the float finder on the whole box (ladder(4, 24, 0.10),
+# threshold -0.8, suggested mesh).
+PRECISION = dict(n=1024, box=2000.0, rms=4.0, seed=1003, grid=1024, r_tophat=4.0, r_gauss=5.0)
+
+
+def precision_run(args):
+    import torch
+
+    from sif_gb300 import device, pysif, synth
+
+    c = PRECISION
+    n = c["grid"]
+    x, y, z = synth.zeldovich(c["n"], c["box"], c["rms"], c["seed"], backend="torch")
+    xs = [torch.from_numpy(v).cuda() for v in (x, y, z)]
+    del x, y, z
+
+    def rel(a, b):
+        d = (a.double() - b)
+        rms = torch.sqrt((b * b).mean())
+        return float(torch.sqrt((d * d).mean()) / rms), float(d.abs().max() / rms)
+
+    g32 = device.cic(*xs, n, c["box"])
+    device.density_contrast(g32)
+    fields32 = {"tophat": device.smooth(g32, n, c["box"], c["r_tophat"]),
+                "gauss": device.smooth(g32, n, c["box"], c["r_gauss"], filter="gaussian")}
+    xs64 = [v.double() for v in xs]
+    g64 = device.cic(*xs64, n, c["box"])
+    del xs64
+    device.density_contrast(g64)
+    out = {"config": "1024^3 particles, box 2000 Mpc/h, grid 1024^3; float form against the FP64 "
+                     "form on the same positions",
+           "contrast_rel_l2": None, "tophat_r4_rel_l2": None, "gauss_r5_rel_l2": None}
+    out["contrast_rel_l2"], out["contrast_rel_max"] = rel(g32, g64)
+    del g32
+    f64 = device.smooth(g64, n, c["box"], c["r_tophat"])
+    out["tophat_r4_rel_l2"], out["tophat_r4_rel_max"] = rel(fields32["tophat"], f64)
+    del f64
+    f64 = device.smooth(g64, n, c["box"], c["r_gauss"], filter="gaussian")
+    out["gauss_r5_rel_l2"], out["gauss_r5_rel_max"] = rel(fields32["gauss"], f64)
+    del f64, g64, fields32
+    torch.cuda.empty_cache()
+    radii = synth.ladder(4.0, 24.0, 0.10).astype(np.float32)
+    mesh = pysif.finders.suggest_mesh_cells(c["n"] ** 3, c["box"], float(radii.max()))
+    stream = device.stream()
+    cat = device.box(*xs, n, c["box"], mesh, radii, -0.8)
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    cat = device.box(*xs, n, c["box"], mesh, radii, -0.8)
+    end.record(stream)
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    out.update({"finder_ms": round(ms, 2), "finder_mparticles_s": round(c["n"] ** 3 / ms / 1e3, 2),
+                "mesh_cells": mesh, "n_voids": len(cat[0])})
+    return out
+
+
 def e2e_run(args, w, x, y, z, radii):
     from sif_gb300 import _lib, abi
 
@@ -509,6 +573,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP64-form and adjoint runs")
+    ap.add_argument("--precision", action="store_true",
+                    help="also the 1024^3 float-vs-FP64 field error and the 1024^3 finder")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--verbose", action="store_true")
