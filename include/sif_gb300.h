@@ -303,6 +303,8 @@ typedef struct {
   /* Particles read and template cells visited by the rung's sphere growth. */
   uint64_t growth_particles;
   uint64_t growth_cells;
+  /* Host wait for the candidates' depths before the sort, milliseconds. */
+  double cand_wait_ms;
 } sifg_rung_stat_t;
 
 /* Kernel timings of the last run, CUDA events on the launching stream. */
@@ -421,6 +423,7 @@ typedef struct {
   uint64_t capacity;
   uint64_t n_voids; /* out */
   int status;       /* out */
+  double wall_ms;   /* out: host wall time of this box's run */
 } sifg_box_job_t;
 int sifg_box_batch_device(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines,
                           uint32_t* n_engines_used);

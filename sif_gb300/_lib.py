@@ -20,7 +20,8 @@ class RungStat(C.Structure):
                 ("n_rescale_fail", C.c_uint64), ("n_overflow", C.c_uint64),
                 ("rung_ms", C.c_double), ("count_wait_ms", C.c_double),
                 ("sort_ms", C.c_double), ("commit_ms", C.c_double),
-                ("growth_particles", C.c_uint64), ("growth_cells", C.c_uint64)]
+                ("growth_particles", C.c_uint64), ("growth_cells", C.c_uint64),
+                ("cand_wait_ms", C.c_double)]
 
 
 class Timings(C.Structure):
@@ -62,7 +63,8 @@ class BoxJob(C.Structure):
                 ("mesh_cells", C.c_uint32), ("radii", C.c_void_p), ("n_radii", C.c_uint32),
                 ("threshold", C.c_float), ("overlap", C.c_float), ("options", C.c_uint32),
                 ("cx", C.c_void_p), ("cy", C.c_void_p), ("cz", C.c_void_p), ("r", C.c_void_p),
-                ("capacity", C.c_uint64), ("n_voids", C.c_uint64), ("status", C.c_int)]
+                ("capacity", C.c_uint64), ("n_voids", C.c_uint64), ("status", C.c_int),
+                ("wall_ms", C.c_double)]
 
 
 def load():

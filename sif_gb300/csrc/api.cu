@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <condition_variable>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -1016,31 +1017,95 @@ static std::pair<int, int> batch_key(const sifg_box_job_t* jobs, uint32_t n_jobs
           (int)std::log2((double)std::max<uint32_t>(n_jobs, 1))};
 }
 
-static void batch_worker(Engine* e, sifg_box_job_t* jobs, const std::vector<uint32_t>* order,
-                         std::atomic<uint32_t>* next) {
-  cudaSetDevice(e->device());
-  for (;;) {
-    const uint32_t k = next->fetch_add(1);
-    if (k >= order->size()) break;
-    sifg_box_job_t& j = jobs[(*order)[k]];
-    j.n_voids = 0;
-    try {
-      uint32_t mc = j.mesh_cells;
-      if (mc == 0) {
-        float rmax = 0.0f;
-        for (uint32_t i = 0; i < j.n_radii; i++) rmax = std::max(rmax, j.radii[i]);
-        mc = sif_finder_suggest_mesh_cells(j.n_particles, j.box, rmax, 0.0f);
+// One job on one engine.
+static void batch_job(Engine* e, sifg_box_job_t& j) {
+  const auto t0 = std::chrono::steady_clock::now();
+  j.n_voids = 0;
+  try {
+    uint32_t mc = j.mesh_cells;
+    if (mc == 0) {
+      float rmax = 0.0f;
+      for (uint32_t i = 0; i < j.n_radii; i++) rmax = std::max(rmax, j.radii[i]);
+      mc = sif_finder_suggest_mesh_cells(j.n_particles, j.box, rmax, 0.0f);
+    }
+    RunTimings tm;
+    j.status = box_run<float>(e, j.x, j.y, j.z, j.n_particles, j.n_grid, j.box, mc, j.radii,
+                              j.n_radii, j.threshold, j.overlap, j.options, j.cx, j.cy, j.cz,
+                              j.r, j.capacity, &j.n_voids, tm, nullptr);
+  } catch (const CudaError& err) {
+    j.status = cuda_fail(err);
+  } catch (const std::bad_alloc&) {
+    j.status = fail(SIF_ERR_ALLOC, "batch: out of host memory");
+  }
+  j.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// The batch's host threads, one per engine, kept between calls (a thread's
+// scan scratch lives as long as it does). A call hands each worker the same
+// job list and a shared cursor, and waits until every worker is done.
+struct BatchPool {
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::vector<std::thread> threads;
+  uint64_t generation = 0;
+  uint32_t active = 0;  // workers taking part in the current call
+  uint32_t busy = 0;    // of them, still working
+  sifg_box_job_t* jobs = nullptr;
+  const std::vector<uint32_t>* order = nullptr;
+  std::atomic<uint32_t> next{0};
+  bool stop = false;
+
+  void worker(uint32_t id) {
+    uint64_t seen = 0;
+    for (;;) {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_work.wait(lk, [&] { return stop || generation != seen; });
+      if (stop) return;
+      seen = generation;
+      const bool mine = id < active;
+      lk.unlock();
+      if (mine) {
+        Engine* e = g_pool[id].get();
+        cudaSetDevice(e->device());
+        for (;;) {
+          const uint32_t k = next.fetch_add(1);
+          if (k >= order->size()) break;
+          batch_job(e, jobs[(*order)[k]]);
+        }
+        lk.lock();
+        if (--busy == 0) cv_done.notify_all();
       }
-      RunTimings tm;
-      j.status = box_run<float>(e, j.x, j.y, j.z, j.n_particles, j.n_grid, j.box, mc, j.radii,
-                                j.n_radii, j.threshold, j.overlap, j.options, j.cx, j.cy, j.cz,
-                                j.r, j.capacity, &j.n_voids, tm, nullptr);
-    } catch (const CudaError& err) {
-      j.status = cuda_fail(err);
-    } catch (const std::bad_alloc&) {
-      j.status = fail(SIF_ERR_ALLOC, "batch: out of host memory");
     }
   }
+
+  void run(uint32_t n_engines, sifg_box_job_t* j, const std::vector<uint32_t>* o) {
+    while (threads.size() < n_engines) {
+      const uint32_t id = (uint32_t)threads.size();
+      threads.emplace_back(&BatchPool::worker, this, id);
+    }
+    std::unique_lock<std::mutex> lk(mu);
+    jobs = j;
+    order = o;
+    next = 0;
+    active = busy = n_engines;
+    generation++;
+    cv_work.notify_all();
+    cv_done.wait(lk, [&] { return busy == 0; });
+  }
+
+  ~BatchPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      stop = true;
+    }
+    cv_work.notify_all();
+    for (auto& t : threads) t.join();
+  }
+};
+
+static BatchPool& batch_pool() {
+  static BatchPool p;
+  return p;
 }
 
 static int run_batch(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines) {
@@ -1057,11 +1122,7 @@ static int run_batch(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines) 
   std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
     return jobs[a].n_particles > jobs[b].n_particles;
   });
-  std::atomic<uint32_t> next{0};
-  std::vector<std::thread> threads;
-  for (uint32_t k = 0; k < n_engines; k++)
-    threads.emplace_back(batch_worker, g_pool[k].get(), jobs, &order, &next);
-  for (auto& t : threads) t.join();
+  batch_pool().run(n_engines, jobs, &order);
   cudaSetDevice(main->device());
   for (uint32_t k = 0; k < n_jobs; k++)
     if (jobs[k].status != SIF_OK) return jobs[k].status;
@@ -1204,7 +1265,7 @@ uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
     out[i] = sifg_rung_stat_t{s.radius, s.r_search, s.n_candidates, s.n_survivors, s.n_accepted,
                               s.rounds, s.n_rescale_fail, s.n_overflow, s.rung_ms,
                               s.count_wait_ms, s.sort_ms, s.commit_ms, s.growth_particles,
-                              s.growth_cells};
+                              s.growth_cells, s.cand_wait_ms};
   }
   return n;
 }

@@ -56,7 +56,7 @@ Engine::Engine(int device) : device_(device) {
     SIFG_CUDA(cudaEventCreateWithFlags(&ev_smoothed_[k], cudaEventDisableTiming));
     SIFG_CUDA(cudaEventCreateWithFlags(&ev_scanned_[k], cudaEventDisableTiming));
   }
-  SIFG_CUDA(cudaMallocHost(&h_counters_, 16 * sizeof(uint32_t)));
+  SIFG_CUDA(cudaMallocHost(&h_counters_, 2 * kCommitCounters * sizeof(uint32_t)));
 }
 
 Engine::~Engine() {
@@ -328,7 +328,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const size_t n_rungs = radii.size();
   unsigned long long* traffic = (unsigned long long*)grow_to<uint64_t>(traffic_, 2 * n_rungs + 2);
   SIFG_CUDA(cudaMemsetAsync(traffic, 0, (2 * n_rungs + 2) * sizeof(uint64_t), st_));
-  uint32_t* counters = grow_to<uint32_t>(counters_, 16);
+  uint32_t* counters = grow_to<uint32_t>(counters_, kCommitCounters);
   const uint32_t nb_scan = scan_blocks(cells);
   uint32_t* blocks = grow_to<uint32_t>(blocks_, (size_t)std::max<uint64_t>(nb_scan + 1, 1024));
 
@@ -427,19 +427,28 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
                                " wider than the mesh; use a finer mesh or smaller radii");
       return kErrRange;
     }
+    // The template in one upload: min and max d^2, the three offsets, the
+    // classes, packed in that order (each part aligned for its type).
     const uint32_t tcount = (uint32_t)ht.type.size();
-    int32_t* tdx = grow_to<int32_t>(tdx_, tcount);
-    int32_t* tdy = grow_to<int32_t>(tdy_, tcount);
-    int32_t* tdz = grow_to<int32_t>(tdz_, tcount);
-    uint8_t* ttype = grow_to<uint8_t>(ttype_, tcount);
-    R* tmin = grow_to<R>(tmin_, tcount);
-    R* tmax = grow_to<R>(tmax_, tcount);
-    SIFG_CUDA(cudaMemcpyAsync(tdx, ht.dx.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
-    SIFG_CUDA(cudaMemcpyAsync(tdy, ht.dy.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
-    SIFG_CUDA(cudaMemcpyAsync(tdz, ht.dz.data(), tcount * 4, cudaMemcpyHostToDevice, st_));
-    SIFG_CUDA(cudaMemcpyAsync(ttype, ht.type.data(), tcount, cudaMemcpyHostToDevice, st_));
-    SIFG_CUDA(cudaMemcpyAsync(tmin, ht.min_d2.data(), tcount * sizeof(R), cudaMemcpyHostToDevice, st_));
-    SIFG_CUDA(cudaMemcpyAsync(tmax, ht.max_d2.data(), tcount * sizeof(R), cudaMemcpyHostToDevice, st_));
+    const size_t t_real = ((size_t)tcount * sizeof(R) + 15) & ~(size_t)15;
+    const size_t t_int = ((size_t)tcount * sizeof(int32_t) + 15) & ~(size_t)15;
+    const size_t t_bytes = 2 * t_real + 3 * t_int + tcount;
+    if (h_tpl_.size() < t_bytes) h_tpl_.resize(t_bytes);
+    uint8_t* hp = h_tpl_.data();
+    std::memcpy(hp, ht.min_d2.data(), tcount * sizeof(R));
+    std::memcpy(hp + t_real, ht.max_d2.data(), tcount * sizeof(R));
+    std::memcpy(hp + 2 * t_real, ht.dx.data(), tcount * sizeof(int32_t));
+    std::memcpy(hp + 2 * t_real + t_int, ht.dy.data(), tcount * sizeof(int32_t));
+    std::memcpy(hp + 2 * t_real + 2 * t_int, ht.dz.data(), tcount * sizeof(int32_t));
+    std::memcpy(hp + 2 * t_real + 3 * t_int, ht.type.data(), tcount);
+    uint8_t* dp = grow_to<uint8_t>(tpl_, t_bytes);
+    SIFG_CUDA(cudaMemcpyAsync(dp, hp, t_bytes, cudaMemcpyHostToDevice, st_));
+    const R* tmin = (const R*)dp;
+    const R* tmax = (const R*)(dp + t_real);
+    const int32_t* tdx = (const int32_t*)(dp + 2 * t_real);
+    const int32_t* tdy = (const int32_t*)(dp + 2 * t_real + t_int);
+    const int32_t* tdz = (const int32_t*)(dp + 2 * t_real + 2 * t_int);
+    const uint8_t* ttype = dp + 2 * t_real + 3 * t_int;
     TemplateViewT<R> tv{tdx, tdy, tdz, ttype, tmin, tmax, tcount};
 
     // 3. Pre-filter at the rung, against the catalogue as the rung begins.
@@ -472,8 +481,10 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     }
 
     // 5. The order, on the host while the GPU grows spheres.
-    const auto t_sort = clk::now();
+    const auto t_wait_cand = clk::now();
     SIFG_CUDA(cudaEventSynchronize(ev_cand_));
+    rs.cand_wait_ms = ms_since(t_wait_cand);
+    const auto t_sort = clk::now();
     candidate_ranks((const R*)h_delta_, m, h_rank_, host_threads);
     rs.sort_ms = ms_since(t_sort);
     uint32_t* rank = grow_to<uint32_t>(rank_, m);
@@ -494,24 +505,25 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     uint8_t* sa = grow_to<uint8_t>(state_a_, m);
     uint8_t* sb = grow_to<uint8_t>(state_b_, m);
     uint32_t* acc = grow_to<uint32_t>(acc_, m);
-    SIFG_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(uint32_t), st_));
+    SIFG_CUDA(cudaMemsetAsync(counters, 0, kCommitCounters * sizeof(uint32_t), st_));
     commit_init(sv, sa, counters, m, st_);
     // Rounds are issued a few at a time between reads of the undecided
     // count: a round after the last one decides nothing and paints nothing.
     uint64_t rounds = 0;
+    uint32_t* h_count = h_counters_ + kCommitCounters;
     for (uint32_t batch = 3;; batch = 4) {
+      SIFG_CUDA(cudaMemsetAsync(counters + kRoundUndecided, 0, kRoundRing * sizeof(uint32_t), st_));
       for (uint32_t b = 0; b < batch; b++) {
-        SIFG_CUDA(cudaMemcpyAsync(counters + 2, counters, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st_));
-        SIFG_CUDA(cudaMemsetAsync(counters + 1, 0, sizeof(uint32_t), st_));
-        commit_round(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters, m, st_);
-        paint_new(sv, acc, counters, mask, rc, m, st_);
+        commit_round(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters, (uint32_t)rounds, m, st_);
+        paint_new(sv, acc, counters, (uint32_t)rounds, mask, rc, m, st_);
         std::swap(sa, sb);
         rounds++;
       }
-      SIFG_CUDA(cudaMemcpyAsync(h_counters_, counters, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
-      SIFG_CUDA(cudaMemcpyAsync(h_counters_ + 8, dcount + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
+      SIFG_CUDA(cudaMemcpyAsync(h_counters_, counters, kCommitCounters * sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, st_));
+      SIFG_CUDA(cudaMemcpyAsync(h_count, dcount + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
       SIFG_CUDA(cudaStreamSynchronize(st_));
-      if (h_counters_[1] == 0) break;
+      if (h_counters_[kRoundUndecided + (rounds - 1) % kRoundRing] == 0) break;
       if (rounds > (uint64_t)m + 8) {
         set_error(kErrInvalid, "commit: no progress");
         return kErrInvalid;
@@ -519,7 +531,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     }
     rs.commit_ms = ms_since(t_commit);
     const uint32_t n_acc = h_counters_[0];
-    rs.n_survivors = h_counters_[8];
+    rs.n_survivors = h_count[0];
     rs.n_accepted = n_acc;
     rs.rounds = rounds;
     rs.n_rescale_fail = h_counters_[4];

@@ -40,6 +40,7 @@ struct RungStat {
   uint64_t n_candidates = 0, n_survivors = 0, n_accepted = 0, rounds = 0;
   uint64_t n_rescale_fail = 0, n_overflow = 0;
   double rung_ms = 0, count_wait_ms = 0, sort_ms = 0, commit_ms = 0;  // host wall time
+  double cand_wait_ms = 0;  // waiting for the candidates' depths before the sort
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the rung's sphere growth
 };
 
@@ -101,7 +102,8 @@ class Engine {
   DevBuf surv_cand_, surv_flat_, scx_, scy_, scz_, sr_, sreason_, state_a_, state_b_, acc_;
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
-  DevBuf tdx_, tdy_, tdz_, ttype_, tmin_, tmax_, gbuf_, traffic_;
+  DevBuf tpl_, gbuf_, traffic_;
+  std::vector<uint8_t> h_tpl_;  // the packed template, staged for its upload
   void* h_delta_ = nullptr;  // candidate depths, float or double
   uint32_t* h_flat_ = nullptr;
   uint32_t* h_rank_ = nullptr;

@@ -847,7 +847,7 @@ __global__ void commit_round_kernel(SurvivorsT<R> sv, const uint32_t* __restrict
                                     SurvivorGridT<R> g, VoidViewT<R> voids, const uint32_t* __restrict__ mask,
                                     RungConstsT<R> rc, const uint8_t* __restrict__ st_in,
                                     uint8_t* __restrict__ st_out, uint32_t* __restrict__ acc,
-                                    uint32_t* __restrict__ counters) {
+                                    uint32_t* __restrict__ counters, uint32_t slot) {
   const uint32_t n = *sv.count;
   const uint32_t nn = rc.grid_n;
   const R half = fmul(rc.box, R(0.5f));
@@ -915,7 +915,7 @@ __global__ void commit_round_kernel(SurvivorsT<R> sv, const uint32_t* __restrict
       acc[atomicAdd(counters, 1u)] = i;
       store_rmax(counters, r);
     } else {
-      atomicAdd(counters + 1, 1u);
+      atomicAdd(counters + kRoundUndecided + slot, 1u);
     }
     st_out[i] = out;
   }
@@ -944,10 +944,11 @@ void commit_init(SurvivorsT<R> s, uint8_t* state, uint32_t* counters, uint32_t m
 template <class R>
 void commit_round(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, VoidViewT<R> voids,
                   const uint32_t* mask, RungConstsT<R> rc, const uint8_t* state_in, uint8_t* state_out,
-                  uint32_t* acc, uint32_t* counters, uint32_t max_survivors, cudaStream_t st) {
+                  uint32_t* acc, uint32_t* counters, uint32_t round, uint32_t max_survivors,
+                  cudaStream_t st) {
   commit_round_kernel<<<grid_for(max_survivors, 128), 128, 0, st>>>(s, rank, g, voids, mask, rc,
                                                                      state_in, state_out, acc,
-                                                                     counters);
+                                                                     counters, round % kRoundRing);
   SIFG_LAUNCH_CHECK();
 }
 
@@ -956,9 +957,11 @@ void commit_round(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Voi
 // measures it.
 template <class R>
 __global__ void paint_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ acc,
-                             const uint32_t* __restrict__ counters, uint32_t* __restrict__ mask,
-                             RungConstsT<R> rc) {
-  const uint32_t lo = counters[2], hi = counters[0];
+                             uint32_t* __restrict__ counters, uint32_t slot,
+                             uint32_t* __restrict__ mask, RungConstsT<R> rc) {
+  const uint32_t lo = counters[kRoundBegin + slot], hi = counters[0];
+  // No round accepts while a paint runs: hi is where the next round begins.
+  if (blockIdx.x == 0 && threadIdx.x == 0) counters[kRoundBegin + (slot + 1) % kRoundRing] = hi;
   const unsigned lane = threadIdx.x & 31u;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   const uint32_t n = rc.grid_n;
@@ -997,10 +1000,10 @@ __global__ void paint_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ acc,
 }
 
 template <class R>
-void paint_new(SurvivorsT<R> s, const uint32_t* acc, const uint32_t* counters, uint32_t* mask,
-               RungConstsT<R> rc, uint32_t max_survivors, cudaStream_t st) {
+void paint_new(SurvivorsT<R> s, const uint32_t* acc, uint32_t* counters, uint32_t round,
+               uint32_t* mask, RungConstsT<R> rc, uint32_t max_survivors, cudaStream_t st) {
   const uint32_t warps = max_survivors < 152u * 16u ? (max_survivors ? max_survivors : 1) : 152u * 16u;
-  paint_kernel<<<(warps + 3) / 4, 128, 0, st>>>(s, acc, counters, mask, rc);
+  paint_kernel<<<(warps + 3) / 4, 128, 0, st>>>(s, acc, counters, round % kRoundRing, mask, rc);
   SIFG_LAUNCH_CHECK();
 }
 
@@ -1109,8 +1112,8 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
   template void commit_init<R>(SurvivorsT<R>, uint8_t*, uint32_t*, uint32_t, cudaStream_t);        \
   template void commit_round<R>(SurvivorsT<R>, const uint32_t*, SurvivorGridT<R>, VoidViewT<R>,    \
                                 const uint32_t*, RungConstsT<R>, const uint8_t*, uint8_t*,         \
-                                uint32_t*, uint32_t*, uint32_t, cudaStream_t);                     \
-  template void paint_new<R>(SurvivorsT<R>, const uint32_t*, const uint32_t*, uint32_t*,           \
+                                uint32_t*, uint32_t*, uint32_t, uint32_t, cudaStream_t);           \
+  template void paint_new<R>(SurvivorsT<R>, const uint32_t*, uint32_t*, uint32_t, uint32_t*,       \
                              RungConstsT<R>, uint32_t, cudaStream_t);                              \
   template void append_accepted<R>(SurvivorsT<R>, const uint32_t*, const uint32_t*,                \
                                    const uint32_t*, uint32_t, uint32_t*, R*, R*, R*, R*, uint32_t, \

@@ -161,18 +161,28 @@ template <class R>
 void commit_init(SurvivorsT<R> s, uint8_t* state, uint32_t* counters, uint32_t max_survivors,
                  cudaStream_t st);
 
-// One commit round: sweep, readiness, acceptance. counters[0] accepted so
-// far (appended to acc), counters[1] left undecided, counters[2] the
-// accepted count when the round began; the largest accepted radius as the
-// bits of a float in counters[3], of a double in counters[6..7].
+// The commit's counters: [0] accepted so far (appended to acc); the largest
+// accepted radius as the bits of a float in [3], of a double in [6..7]; [4]
+// rescaling failures, [5] resolve overflows; then two rings of kRoundRing
+// slots indexed by round % kRoundRing: the accepted count when the round
+// began (written by the previous round's paint), and the survivors the round
+// left undecided (zeroed by the host before each batch of rounds).
+constexpr uint32_t kRoundRing = 64;
+constexpr uint32_t kRoundBegin = 16;
+constexpr uint32_t kRoundUndecided = kRoundBegin + kRoundRing;
+constexpr uint32_t kCommitCounters = kRoundUndecided + kRoundRing;
+
+// One commit round: sweep, readiness, acceptance.
 template <class R>
 void commit_round(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, VoidViewT<R> voids,
                   const uint32_t* mask, RungConstsT<R> rc, const uint8_t* state_in,
-                  uint8_t* state_out, uint32_t* acc, uint32_t* counters, uint32_t max_survivors,
-                  cudaStream_t st);
+                  uint8_t* state_out, uint32_t* acc, uint32_t* counters, uint32_t round,
+                  uint32_t max_survivors, cudaStream_t st);
+// Paints the voids round `round` accepted and records where the next round's
+// acceptances begin.
 template <class R>
-void paint_new(SurvivorsT<R> s, const uint32_t* acc, const uint32_t* counters, uint32_t* mask,
-               RungConstsT<R> rc, uint32_t max_survivors, cudaStream_t st);
+void paint_new(SurvivorsT<R> s, const uint32_t* acc, uint32_t* counters, uint32_t round,
+               uint32_t* mask, RungConstsT<R> rc, uint32_t max_survivors, cudaStream_t st);
 
 // Appends the rung's accepted voids to the catalogue in candidate-rank order.
 template <class R>

@@ -1,7 +1,9 @@
 // Exclusive prefix sums, and the small host helpers of kernels.cuh.
 //
 // The scan is the usual three phases: every CTA reduces its chunk, one CTA
-// scans the chunk totals, every CTA rescans its chunk from its total.
+// scans the chunk totals, every CTA rescans its chunk from its total. Up to
+// kSmallChunks chunks (most of the path's scans: block totals, cell indexes)
+// it is one CTA walking the chunks with a carry: one launch instead of three.
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
@@ -96,11 +98,44 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(uint32_t* __re
   }
 }
 
+constexpr uint32_t kSmallChunks = 8;
+
+__global__ void __launch_bounds__(kScanThreads) scan_small_kernel(uint32_t* __restrict__ d,
+                                                                  uint32_t n) {
+  __shared__ uint32_t ws[32];
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < n; base += kScanChunk) {
+    const uint32_t first = base + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      const uint32_t i = first + k;
+      v[k] = i < n ? d[i] : 0u;
+      acc += v[k];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(acc, ws, total) + carry;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      const uint32_t i = first + k;
+      if (i < n) d[i] = run;
+      run += v[k];
+    }
+    carry += total;
+  }
+}
+
 uint32_t scan_sums_needed(uint32_t n) { return (n + kScanChunk - 1) / kScanChunk; }
 
 void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st, uint32_t* sums_scratch) {
   if (n == 0) return;
   const uint32_t blocks = (n + kScanChunk - 1) / kScanChunk;
+  if (blocks <= kSmallChunks) {
+    scan_small_kernel<<<1, kScanThreads, 0, st>>>(data, n);
+    SIFG_LAUNCH_CHECK();
+    return;
+  }
   thread_local DevBuf sums;  // chunk totals; small; one per host thread driving a stream
   uint32_t* s = sums_scratch ? sums_scratch
                              : (uint32_t*)sums.ensure((size_t)blocks * sizeof(uint32_t));
