@@ -159,15 +159,197 @@ void qsort_tasks(Rec<K>* a, int64_t lo, int64_t hi) {
 
 }  // namespace
 
+// One Dijkstra partition of a[lo..hi] on t threads, with the same result as
+// partition3. The sequential scan consumes the segment from two ends: from
+// the left while it meets smaller or equal keys, and, after each larger key,
+// from the right until it meets one that is not larger. So with K keys not
+// larger than the pivot, the left end consumes positions [0, s) -- s = K, or
+// K + 1 when position K holds a larger key -- and the right end the rest,
+// last to first; the j-th larger key from the left is followed by the right
+// end's run up to its j-th not-larger key. Every key's place follows from
+// counts in the two streams:
+//   smaller keys go to the front in the order examined, larger keys to the
+//   back in reverse order examined, and equal keys fill the middle as a queue
+//   that each later smaller key rotates by one (its exchange with the low
+//   end moves the first equal key to the back).
+// Returns false (nothing moved) when more than kMaxEqualQueue keys equal the
+// pivot: the caller then partitions sequentially.
+constexpr int64_t kParallelPartition = 32768;
+constexpr int64_t kMaxEqualQueue = 2048;
+
+template <class K>
+bool partition3_parallel(Rec<K>* a, int64_t lo, int64_t hi, int t, int64_t* lt_out,
+                         int64_t* gt_out) {
+  const int64_t n = hi - lo + 1;
+  Rec<K>* seg = a + lo;
+  const K pivot = a[lo + (hi - lo) / 2].d;
+  auto cls = [&](int64_t p) -> int { return seg[p].d < pivot ? 0 : (pivot < seg[p].d ? 2 : 1); };
+  // Counts of smaller (L), equal (E) and larger (G) keys.
+  std::vector<int64_t> cnt(3 * (size_t)t, 0);
+  auto chunk = [&](int64_t len, int c) { return len * c / t; };
+#pragma omp parallel for num_threads(t) schedule(static, 1)
+  for (int c = 0; c < t; c++) {
+    int64_t k3[3] = {0, 0, 0};  // counted in registers: the array is shared by every thread
+    for (int64_t p = chunk(n, c); p < chunk(n, c + 1); p++) k3[cls(p)]++;
+    for (int k = 0; k < 3; k++) cnt[3 * c + k] = k3[k];
+  }
+  int64_t nl = 0, ne = 0;
+  for (int c = 0; c < t; c++) {
+    nl += cnt[3 * c];
+    ne += cnt[3 * c + 1];
+  }
+  if (ne > kMaxEqualQueue) return false;
+  const int64_t k_ng = nl + ne;
+  const int64_t s = k_ng + ((k_ng < n && cls(k_ng) == 2) ? 1 : 0);
+  const int64_t nr = n - s;  // the right stream: r = 0..nr-1 is position n-1-r
+  // Per-chunk counts over each stream (L, G, not-G), then exclusive prefixes.
+  std::vector<int64_t> lc(3 * (size_t)(t + 1), 0), rc(3 * (size_t)(t + 1), 0);
+#pragma omp parallel for num_threads(t) schedule(static, 1)
+  for (int c = 0; c < t; c++) {
+    int64_t l = 0, g = 0, ng = 0;
+    for (int64_t p = chunk(s, c); p < chunk(s, c + 1); p++) {
+      const int k = cls(p);
+      l += k == 0;
+      g += k == 2;
+      ng += k != 2;
+    }
+    lc[3 * (c + 1)] = l;
+    lc[3 * (c + 1) + 1] = g;
+    lc[3 * (c + 1) + 2] = ng;
+    l = g = ng = 0;
+    for (int64_t r = chunk(nr, c); r < chunk(nr, c + 1); r++) {
+      const int k = cls(n - 1 - r);
+      l += k == 0;
+      g += k == 2;
+      ng += k != 2;
+    }
+    rc[3 * (c + 1)] = l;
+    rc[3 * (c + 1) + 1] = g;
+    rc[3 * (c + 1) + 2] = ng;
+  }
+  for (int c = 1; c <= t; c++)
+    for (int k = 0; k < 3; k++) {
+      lc[3 * c + k] += lc[3 * (c - 1) + k];
+      rc[3 * c + k] += rc[3 * (c - 1) + k];
+    }
+  // The j-th larger key of the left stream (1-based): the smaller and the
+  // not-larger keys before it (pa, pb). The right stream's j-th not-larger
+  // key: the smaller keys up to and including it (ra) and its index (rb).
+  std::vector<int64_t> pa(n + 2), pb(n + 2), ra(n + 2), rb(n + 2);
+#pragma omp parallel for num_threads(t) schedule(static, 1)
+  for (int c = 0; c < t; c++) {
+    int64_t l = lc[3 * c], g = lc[3 * c + 1], ng = lc[3 * c + 2];
+    for (int64_t p = chunk(s, c); p < chunk(s, c + 1); p++) {
+      const int k = cls(p);
+      if (k == 2) {
+        pa[g + 1] = l;
+        pb[g + 1] = ng;
+      }
+      l += k == 0;
+      g += k == 2;
+      ng += k != 2;
+    }
+    l = rc[3 * c];
+    g = rc[3 * c + 1];
+    ng = rc[3 * c + 2];
+    for (int64_t r = chunk(nr, c); r < chunk(nr, c + 1); r++) {
+      const int k = cls(n - 1 - r);
+      if (k != 2) {
+        ra[ng + 1] = l + (k == 0);
+        rb[ng + 1] = r;
+      }
+      l += k == 0;
+      g += k == 2;
+      ng += k != 2;
+    }
+  }
+  // Destinations; the equal keys with their place among the not-larger keys
+  // in the order examined.
+  std::vector<Rec<K>> out(n);
+  std::vector<std::vector<std::pair<int64_t, Rec<K>>>> eq(t);
+#pragma omp parallel for num_threads(t) schedule(static, 1)
+  for (int c = 0; c < t; c++) {
+    int64_t l = lc[3 * c], g = lc[3 * c + 1], ng = lc[3 * c + 2];
+    for (int64_t p = chunk(s, c); p < chunk(s, c + 1); p++) {
+      const int k = cls(p);
+      if (k == 0)
+        out[l + (g ? ra[g] : 0)] = seg[p];
+      else if (k == 2)
+        out[n - 1 - (g + (g ? rb[g] + 1 - g : 0))] = seg[p];
+      else
+        eq[c].emplace_back(ng + g, seg[p]);
+      l += k == 0;
+      g += k == 2;
+      ng += k != 2;
+    }
+    l = rc[3 * c];
+    g = rc[3 * c + 1];
+    ng = rc[3 * c + 2];
+    for (int64_t r = chunk(nr, c); r < chunk(nr, c + 1); r++) {
+      const int64_t p = n - 1 - r;
+      const int k = cls(p);
+      const int64_t j = ng + 1;
+      if (k == 2)
+        out[n - 1 - (j + g)] = seg[p];
+      else if (k == 0)
+        out[pa[j] + l] = seg[p];
+      else
+        eq[c].emplace_back(pb[j] + (j - 1), seg[p]);
+      l += k == 0;
+      g += k == 2;
+      ng += k != 2;
+    }
+  }
+  // The equal keys: in the order examined, each joins the back of the queue;
+  // each smaller key examined between two of them moves the front to the back.
+  std::vector<std::pair<int64_t, Rec<K>>> e;
+  for (auto& v : eq) e.insert(e.end(), v.begin(), v.end());
+  std::sort(e.begin(), e.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+  std::vector<Rec<K>> q;
+  q.reserve(e.size());
+  size_t head = 0;
+  for (size_t i = 0; i < e.size(); i++) {
+    q.insert(q.begin() + (ptrdiff_t)head, e[i].second);  // the back of the queue
+    head = (head + 1) % q.size();
+    const int64_t next_t = i + 1 < e.size() ? e[i + 1].first : k_ng;
+    const int64_t smaller = next_t - e[i].first - 1;  // not-larger keys between: all smaller
+    head = (size_t)((head + (uint64_t)smaller) % q.size());
+  }
+  for (size_t i = 0; i < q.size(); i++) out[nl + (int64_t)i] = q[(head + i) % q.size()];
+#pragma omp parallel for num_threads(t) schedule(static)
+  for (int64_t p = 0; p < n; p++) seg[p] = out[p];
+  *lt_out = lo + nl;
+  *gt_out = lo + nl + ne - 1;
+  return true;
+}
+
 template <class K>
 void candidate_ranks(const K* delta, uint32_t m, uint32_t* rank, int threads) {
   std::vector<Rec<K>> a(m);
   for (uint32_t k = 0; k < m; k++) a[k] = Rec<K>{delta[k], k};
-  if (m > 8 * (uint32_t)kTaskCutoff && threads != 1) {
-    const int t = threads > 0 ? threads : omp_get_max_threads();
+  const int t = threads > 0 ? threads : omp_get_max_threads();
+  if (m > 2 * (uint32_t)kTaskCutoff && t > 1) {
+    // The large segments partitioned one at a time on every thread, the
+    // rest as tasks; disjoint segments, so the permutation is the serial one.
+    std::vector<std::pair<int64_t, int64_t>> big{{0, (int64_t)m - 1}}, small;
+    while (!big.empty()) {
+      const auto [l, h] = big.back();
+      big.pop_back();
+      if (h - l + 1 < kParallelPartition) {
+        small.emplace_back(l, h);
+        continue;
+      }
+      int64_t lt, gt;
+      if (!partition3_parallel(a.data(), l, h, t, &lt, &gt)) partition3(a.data(), l, h, &lt, &gt);
+      big.emplace_back(l, lt - 1);
+      big.emplace_back(gt + 1, h);
+    }
 #pragma omp parallel num_threads(t)
 #pragma omp single nowait
-    qsort_tasks(a.data(), 0, (int64_t)m - 1);
+    for (const auto& [l, h] : small) {
+#pragma omp task firstprivate(l, h)
+      qsort_tasks(a.data(), l, h);
+    }
   } else if (m > 1) {
     qsort_serial(a.data(), 0, (int64_t)m - 1);
   }
@@ -359,7 +541,13 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     }
 
     // 2. Candidates, in flat order.
-    scan_count_pass(field, mask, cells, threshold, blocks, dcount, st_, N, minima);
+    const uint64_t slots = scan_region_slots(cells);
+    R* region_delta = grow_to<R>(region_delta_, slots);
+    uint32_t* region_flat = grow_to<uint32_t>(region_flat_, slots);
+    scan_fused_pass(field, mask, cells, threshold, blocks, dcount, region_delta, region_flat, st_, N,
+                    minima);
+    // The field's last reader: the next rung but one may smooth into it.
+    SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
     SIFG_CUDA(cudaMemcpyAsync(h_counters_, dcount, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
     const auto t_wait = clk::now();
     SIFG_CUDA(cudaStreamSynchronize(st_));
@@ -374,7 +562,6 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     if (ri > 0 && radii[ri - 1] > r_search) r_search = radii[ri - 1];
     rs.r_search = r_search;
     if (m == 0) {
-      SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
       rs.rung_ms = ms_since(t_rung);
       if (stats) stats->push_back(rs);
       continue;
@@ -382,8 +569,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
 
     R* cdelta = grow_to<R>(cand_delta_, m);
     uint32_t* cflat = grow_to<uint32_t>(cand_flat_, m);
-    scan_write_pass(field, mask, cells, threshold, blocks, cdelta, cflat, st_, N, minima);
-    SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
+    scan_compact(blocks, cells, region_delta, region_flat, cdelta, cflat, st_);
     ensure_host(m);
     SIFG_CUDA(cudaMemcpyAsync(h_delta_, cdelta, m * sizeof(R), cudaMemcpyDeviceToHost, st_));
     SIFG_CUDA(cudaEventRecord(ev_cand_, st_));

@@ -102,7 +102,7 @@ class Engine {
   DevBuf surv_cand_, surv_flat_, scx_, scy_, scz_, sr_, sreason_, state_a_, state_b_, acc_;
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
-  DevBuf tpl_, gbuf_, traffic_;
+  DevBuf tpl_, gbuf_, traffic_, region_delta_, region_flat_;
   std::vector<uint8_t> h_tpl_;  // the packed template, staged for its upload
   void* h_delta_ = nullptr;  // candidate depths, float or double
   uint32_t* h_flat_ = nullptr;

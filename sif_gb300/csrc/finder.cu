@@ -183,6 +183,80 @@ __global__ void store_total_kernel(const uint32_t* __restrict__ offsets, uint32_
   d_count[0] = offsets[nb];
 }
 
+// One pass over the field: each CTA writes its candidates, in flat order, to
+// the start of its own region of kScanChunk slots and its count to
+// counts[block]; the compaction then moves only the candidates.
+template <class R>
+__global__ void __launch_bounds__(kScanT) scan_regions_kernel(
+    const R* __restrict__ f, const uint32_t* __restrict__ mask, uint64_t n, R thr,
+    uint32_t* __restrict__ counts, R* __restrict__ rdelta, uint32_t* __restrict__ rflat,
+    uint32_t grid_n, bool minima) {
+  __shared__ uint32_t ws[kScanT / 32];
+  const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
+  uint32_t out = 0;
+  for (int j = 0; j < kScanRounds; j++) {
+    const uint64_t c0 = base + ((uint64_t)j * kScanT + threadIdx.x) * 4;
+    R v[4];
+    const uint32_t bits = quad_candidates(f, mask, c0, n, thr, v, grid_n, minima);
+    uint32_t total;
+    uint32_t pos = out + block_scan_excl(__popc(bits), ws, &total);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (bits & (1u << k)) {
+        rdelta[base + pos] = v[k];
+        rflat[base + pos] = (uint32_t)(c0 + k);
+        pos++;
+      }
+    }
+    out += total;
+  }
+  if (threadIdx.x == 0) counts[blockIdx.x] = out;
+}
+
+// A warp per region: its candidates to their place in the compacted list.
+template <class R>
+__global__ void scan_compact_kernel(const uint32_t* __restrict__ offsets, uint32_t nb,
+                                    const R* __restrict__ rdelta, const uint32_t* __restrict__ rflat,
+                                    R* __restrict__ cdelta, uint32_t* __restrict__ cflat) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < nb; b += warps) {
+    const uint32_t o = offsets[b], cnt = offsets[b + 1] - o;
+    const uint64_t src = (uint64_t)b * kScanChunk;
+    for (uint32_t i = lane; i < cnt; i += 32) {
+      cdelta[o + i] = rdelta[src + i];
+      cflat[o + i] = rflat[src + i];
+    }
+  }
+}
+
+uint64_t scan_region_slots(uint64_t n_cells) { return (uint64_t)scan_blocks(n_cells) * kScanChunk; }
+
+template <class R>
+void scan_fused_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
+                     uint32_t* block_counts, uint32_t* d_count, R* region_delta,
+                     uint32_t* region_flat, cudaStream_t st, uint32_t grid_n, bool minima) {
+  const uint32_t nb = scan_blocks(n_cells);
+  scan_regions_kernel<R><<<nb, kScanT, 0, st>>>(field, mask, n_cells, threshold, block_counts,
+                                                region_delta, region_flat, grid_n, minima);
+  SIFG_LAUNCH_CHECK();
+  SIFG_CUDA(cudaMemsetAsync(block_counts + nb, 0, sizeof(uint32_t), st));
+  exclusive_scan_u32(block_counts, nb + 1, st);
+  store_total_kernel<<<1, 1, 0, st>>>(block_counts, nb, d_count);
+  SIFG_LAUNCH_CHECK();
+}
+
+template <class R>
+void scan_compact(const uint32_t* block_counts, uint64_t n_cells, const R* region_delta,
+                  const uint32_t* region_flat, R* cand_delta, uint32_t* cand_flat,
+                  cudaStream_t st) {
+  const uint32_t nb = scan_blocks(n_cells);
+  const uint32_t warps = nb < 152u * 64u ? nb : 152u * 64u;
+  scan_compact_kernel<R><<<(warps + 7) / 8, 256, 0, st>>>(block_counts, nb, region_delta,
+                                                           region_flat, cand_delta, cand_flat);
+  SIFG_LAUNCH_CHECK();
+}
+
 template <class R>
 void scan_count_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
                      uint32_t* block_counts, uint32_t* d_count, cudaStream_t st, uint32_t grid_n,
@@ -1102,6 +1176,10 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
                                    cudaStream_t, uint32_t, bool);                                  \
   template void scan_write_pass<R>(const R*, const uint32_t*, uint64_t, R, const uint32_t*, R*,    \
                                    uint32_t*, cudaStream_t, uint32_t, bool);                       \
+  template void scan_fused_pass<R>(const R*, const uint32_t*, uint64_t, R, uint32_t*, uint32_t*,   \
+                                   R*, uint32_t*, cudaStream_t, uint32_t, bool);                   \
+  template void scan_compact<R>(const uint32_t*, uint64_t, const R*, const uint32_t*, R*,          \
+                                uint32_t*, cudaStream_t);                                          \
   template void prefilter<R>(const uint32_t*, uint32_t, const uint32_t*, VoidViewT<R>,             \
                              RungConstsT<R>, uint8_t*, uint32_t*, uint32_t*, uint32_t*, R*, R*,    \
                              R*, uint32_t*, cudaStream_t);                                         \

@@ -130,6 +130,18 @@ template <class R>
 void scan_write_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
                      const uint32_t* block_counts, R* cand_delta, uint32_t* cand_flat,
                      cudaStream_t st, uint32_t grid_n, bool minima);
+// The same candidates from one pass over the field: each block's go to its
+// own region (scan_region_slots(n) slots in all) with the count and offsets
+// as scan_count_pass leaves them; scan_compact then gathers them in order.
+uint64_t scan_region_slots(uint64_t n_cells);
+template <class R>
+void scan_fused_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
+                     uint32_t* block_counts, uint32_t* d_count, R* region_delta,
+                     uint32_t* region_flat, cudaStream_t st, uint32_t grid_n, bool minima);
+template <class R>
+void scan_compact(const uint32_t* block_counts, uint64_t n_cells, const R* region_delta,
+                  const uint32_t* region_flat, R* cand_delta, uint32_t* cand_flat,
+                  cudaStream_t st);
 
 // Pre-filter at the rung radius (prefilter_cells, exodus_finder.c:871-944)
 // and compaction of the survivors, candidate order kept.
