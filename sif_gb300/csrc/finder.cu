@@ -500,8 +500,9 @@ constexpr int kGrowT = 256;
 constexpr int kGrowWarps = kGrowT / 32;
 constexpr uint32_t kMaxBins = 2048;
 constexpr uint32_t kSmemBuf = 2048;
+constexpr int kWalkUnroll = 4;  // particle loads in flight per lane
 
-unsigned growth_grid() { return 152u * 6u; }
+unsigned growth_grid() { return 152u * 4u; }
 
 template <class R>
 struct CellRange {
@@ -539,6 +540,66 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
   for (int w = 0; w < kGrowWarps; w++) t += red[w];
   __syncthreads();
   return t;
+}
+
+// Two sums at once: one set of barriers instead of two.
+__device__ __forceinline__ void block_sum2_u64(unsigned long long& a, unsigned long long& b,
+                                               unsigned long long* red) {
+  for (int d = 16; d > 0; d >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, d);
+    b += __shfl_down_sync(0xffffffffu, b, d);
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5] = a;
+    red[kGrowWarps + (threadIdx.x >> 5)] = b;
+  }
+  __syncthreads();
+  unsigned long long ta = 0, tb = 0;
+  for (int w = 0; w < kGrowWarps; w++) {
+    ta += red[w];
+    tb += red[kGrowWarps + w];
+  }
+  __syncthreads();
+  a = ta;
+  b = tb;
+}
+
+// Ascending sort of 256 values held by one warp, v[j] at index j * 32 + lane:
+// a bitonic network, partners in other lanes through shuffles, in other
+// registers of the same lane directly. No block barrier.
+template <class R>
+__device__ __forceinline__ void warp_sort256(R (&v)[8]) {
+  const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+  for (int k = 2; k <= 256; k <<= 1) {
+#pragma unroll
+    for (int d = k >> 1; d > 0; d >>= 1) {
+      if (d >= 32) {
+        const int dj = d >> 5;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          if (j & dj) continue;
+          const int jj = j | dj;
+          const bool up = (((j << 5) | (int)lane) & k) == 0;
+          const R a = v[j], b = v[jj];
+          if ((a > b) == up) {
+            v[j] = b;
+            v[jj] = a;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const R o = __shfl_xor_sync(0xffffffffu, v[j], d);
+          const bool up = (((j << 5) | (int)lane) & k) == 0;
+          const bool lower = (lane & (unsigned)d) == 0;
+          const R lo = v[j] < o ? v[j] : o, hi = v[j] < o ? o : v[j];
+          v[j] = (lower == up) ? lo : hi;
+        }
+      }
+    }
+  }
 }
 
 __device__ __forceinline__ int block_max_int(int v, int* red) {
@@ -606,27 +667,56 @@ __device__ __forceinline__ void walk_cells(const MeshViewT<R>& mesh, const Templ
         visited++;
       }
     }
-    unsigned todo = __ballot_sync(0xffffffffu, need);
-    while (todo) {
-      const int src = __ffs(todo) - 1;
-      todo &= todo - 1;
-      const uint32_t s = __shfl_sync(0xffffffffu, c.s, src);
-      const uint32_t e = __shfl_sync(0xffffffffu, c.e, src);
-      const R ex = __shfl_sync(0xffffffffu, c.ex, src);
-      const R ey = __shfl_sync(0xffffffffu, c.ey, src);
-      const R ez = __shfl_sync(0xffffffffu, c.ez, src);
-      const uint8_t t = (uint8_t)__shfl_sync(0xffffffffu, (int)type, src);
-      if (lane == 0) read += e - s;
-      uint32_t p = s + lane;
-      // Two particles per lane in flight.
-      for (; p + 32 < e; p += 64) {
-        const R x0 = __ldg(mesh.x + p), y0 = __ldg(mesh.y + p), z0 = __ldg(mesh.z + p);
-        const R x1 = __ldg(mesh.x + p + 32), y1 = __ldg(mesh.y + p + 32),
-                    z1 = __ldg(mesh.z + p + 32);
-        each(t, dist2(x0, y0, z0, ex, ey, ez), p);
-        each(t, dist2(x1, y1, z1, ex, ey, ez), p + 32);
+    // The chunk's particles as one stream: each lane takes every 32nd item,
+    // finds the cell it falls in by a binary search over the cells' starts
+    // (shuffles), and keeps kWalkUnroll items' loads in flight.
+    const uint32_t cnt = need ? c.e - c.s : 0u;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= (unsigned)d) incl += y;
+    }
+    const uint32_t start = incl - cnt;  // this lane's cell's first item
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane == 0) read += total;
+    for (uint32_t base = 0; base < total; base += 32 * kWalkUnroll) {
+      uint32_t pp[kWalkUnroll];
+      int own[kWalkUnroll];
+#pragma unroll
+      for (int u = 0; u < kWalkUnroll; u++) {
+        const uint32_t idx = base + (uint32_t)u * 32 + lane;
+        // The last cell (lane) whose start is <= idx owns item idx (cells
+        // without items share a start with the next one).
+        int j = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+          const uint32_t st = __shfl_sync(0xffffffffu, start, j + step);
+          if (st <= idx) j += step;
+        }
+        const uint32_t s_j = __shfl_sync(0xffffffffu, c.s, j);
+        const uint32_t st_j = __shfl_sync(0xffffffffu, start, j);
+        own[u] = j;
+        pp[u] = idx < total ? s_j + (idx - st_j) : 0xffffffffu;
       }
-      if (p < e) each(t, dist2(__ldg(mesh.x + p), __ldg(mesh.y + p), __ldg(mesh.z + p), ex, ey, ez), p);
+      R px[kWalkUnroll], py[kWalkUnroll], pz[kWalkUnroll];
+#pragma unroll
+      for (int u = 0; u < kWalkUnroll; u++) {
+        // Past the stream's end a lane loads particle 0 (there is one: the
+        // stream is not empty) and drops it.
+        const uint32_t q = pp[u] != 0xffffffffu ? pp[u] : 0u;
+        px[u] = __ldg(mesh.x + q);
+        py[u] = __ldg(mesh.y + q);
+        pz[u] = __ldg(mesh.z + q);
+      }
+#pragma unroll
+      for (int u = 0; u < kWalkUnroll; u++) {
+        const R qx = __shfl_sync(0xffffffffu, c.ex, own[u]);
+        const R qy = __shfl_sync(0xffffffffu, c.ey, own[u]);
+        const R qz = __shfl_sync(0xffffffffu, c.ez, own[u]);
+        const uint8_t t = (uint8_t)__shfl_sync(0xffffffffu, (int)type, own[u]);
+        if (pp[u] != 0xffffffffu) each(t, dist2(px[u], py[u], pz[u], qx, qy, qz), pp[u]);
+      }
     }
   }
 }
@@ -636,14 +726,16 @@ __device__ __forceinline__ void walk_cells(const MeshViewT<R>& mesh, const Templ
 // bytes, plus the template entry, 8 bytes): the gathered bytes of the
 // sphere growth.
 template <class R>
-__global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshViewT<R> mesh, TemplateViewT<R> tpl,
+__global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, TemplateViewT<R> tpl,
                                                            RungConstsT<R> rc, SurvivorsT<R> sv,
                                                            R* __restrict__ gbuf, uint32_t gcap,
                                                            unsigned long long* __restrict__ traffic) {
   __shared__ uint32_t bins[kMaxBins];
   __shared__ uint32_t below[kMaxBins];  // particles inside bin b's lower edge
   __shared__ R sbuf[kSmemBuf];
-  __shared__ unsigned long long red64[kGrowWarps];
+  __shared__ unsigned long long red64[2 * kGrowWarps];
+  __shared__ R found_d2;
+  __shared__ int found_k;
   __shared__ int redi[kGrowWarps];
   __shared__ uint32_t collected;
 
@@ -706,8 +798,7 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshViewT<R> mesh, Te
             atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
           },
           visited, read);
-      n_core = block_sum_u64(n_core, red64);
-      n_shell = block_sum_u64(n_shell, red64);
+      block_sum2_u64(n_core, n_shell, red64);
       const unsigned long long total = n_core + n_shell;
       if (total == 0) {
         reason = kRescaleEmpty;
@@ -783,23 +874,63 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshViewT<R> mesh, Te
               visited, read);
           __syncthreads();
           const uint32_t m = collected < cap ? collected : cap;
-          uint32_t p2 = 1;
-          while (p2 < m) p2 <<= 1;
-          for (uint32_t i = m + threadIdx.x; i < p2; i += kGrowT) buf[i] = real_inf<R>();
-          __syncthreads();
-          bitonic_sort(buf, p2);
-          // Outside-in: the k-th smallest encloses top - m + k particles.
+          // Outside-in: the k-th smallest encloses top - m + k particles;
+          // the answer is the largest k that passes (exodus_rescale.c:405-438).
           int found = -1;
-          for (uint32_t k = threadIdx.x; k < m; k += kGrowT) {
-            const R d2 = buf[k];
-            if (d2 == 0.0f) continue;
-            const R rn = from_u32<R>(top - m + k);
-            const R d2c = fmul(fmul(d2, d2), d2);
-            if (fmul(rn, rn) <= fmul(rc.K2, d2c)) found = max(found, (int)k);
+          R found_val = 0;
+          if (m <= 256) {
+            // One warp sorts and tests the window in registers.
+            if (warp == 0) {
+              R v[8];
+#pragma unroll
+              for (int j = 0; j < 8; j++) {
+                const uint32_t i = (uint32_t)j * 32 + lane;
+                v[j] = i < m ? buf[i] : real_inf<R>();
+              }
+              warp_sort256(v);
+              int f = -1;
+              R fv = 0;
+#pragma unroll
+              for (int j = 0; j < 8; j++) {
+                const uint32_t k = (uint32_t)j * 32 + lane;
+                const R d2 = v[j];
+                if (k < m && d2 != R(0)) {
+                  const R rn = from_u32<R>(top - m + k);
+                  const R d2c = fmul(fmul(d2, d2), d2);
+                  if (fmul(rn, rn) <= fmul(rc.K2, d2c)) {
+                    f = (int)k;
+                    fv = d2;
+                  }
+                }
+              }
+              const int best_k = __reduce_max_sync(0xffffffffu, f + 1) - 1;
+              if (best_k >= 0 && f == best_k) {
+                found_k = best_k;
+                found_d2 = fv;
+              }
+              if (lane == 0 && best_k < 0) found_k = -1;
+            }
+            __syncthreads();
+            found = found_k;
+            found_val = found_d2;
+          } else {
+            uint32_t p2 = 1;
+            while (p2 < m) p2 <<= 1;
+            for (uint32_t i = m + threadIdx.x; i < p2; i += kGrowT) buf[i] = real_inf<R>();
+            __syncthreads();
+            bitonic_sort(buf, p2);
+            for (uint32_t k = threadIdx.x; k < m; k += kGrowT) {
+              const R d2 = buf[k];
+              if (d2 == 0.0f) continue;
+              const R rn = from_u32<R>(top - m + k);
+              const R d2c = fmul(fmul(d2, d2), d2);
+              if (fmul(rn, rn) <= fmul(rc.K2, d2c)) found = max(found, (int)k);
+            }
+            found = block_max_int(found, redi);
+            if (found >= 0) found_val = buf[found];
           }
-          found = block_max_int(found, redi);
           if (found >= 0) {
-            radius = fsqrt(buf[found]);
+            radius = fsqrt(found_val);
             reason = kRescaleOk;
             break;
           }
@@ -809,11 +940,11 @@ __global__ void __launch_bounds__(kGrowT, 6) growth_kernel(MeshViewT<R> mesh, Te
       }
     }
     if (traffic) {
-      read = block_sum_u64(read, red64);
-      visited = block_sum_u64(visited, red64);
-      if (threadIdx.x == 0) {
-        atomicAdd(traffic, read);
-        atomicAdd(traffic + 1, visited);
+      // walk_cells counts particles on lane 0 and the cells each lane looked up.
+      const unsigned long long v = __reduce_add_sync(0xffffffffu, (unsigned)visited);
+      if (lane == 0) {
+        if (read) atomicAdd(traffic, read);
+        if (v) atomicAdd(traffic + 1, v);
       }
     }
     if (threadIdx.x == 0) {
