@@ -1287,6 +1287,8 @@ uint64_t sifg_stream(void) {
   }
 }
 
+void sifg_set_growth_mode(int mode) { set_growth_mode(mode < 0 || mode > 2 ? 0 : mode); }
+
 void sifg_set_window(int bins) { g_window = bins < 1 ? 1 : (bins > 64 ? 64 : bins); }
 
 void sifg_candidate_ranks(const float* delta, uint32_t m, uint32_t* rank) {

@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "finder.cuh"
 
@@ -651,9 +653,12 @@ __device__ __forceinline__ void walk_cells(const MeshViewT<R>& mesh, const Templ
                                            int32_t ci, int32_t cj, int32_t ck, R cx, R cy,
                                            R cz, Want want, Whole whole, Particles particles,
                                            Each each, unsigned long long& visited,
-                                           unsigned long long& read) {
+                                           unsigned long long& read, bool whole_warp = false) {
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  for (uint32_t c0 = warp * 32; c0 < tpl.count; c0 += kGrowWarps * 32) {
+  // A CTA's warps share the template's chunks; a warp on its own takes all.
+  const uint32_t first = whole_warp ? 0u : warp * 32;
+  const uint32_t step = whole_warp ? 32u : kGrowWarps * 32;
+  for (uint32_t c0 = first; c0 < tpl.count; c0 += step) {
     const uint32_t i = c0 + lane;
     CellRange<R> c{0, 0, 0.f, 0.f, 0.f};
     uint8_t type = 0;
@@ -729,7 +734,8 @@ template <class R>
 __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, TemplateViewT<R> tpl,
                                                            RungConstsT<R> rc, SurvivorsT<R> sv,
                                                            R* __restrict__ gbuf, uint32_t gcap,
-                                                           unsigned long long* __restrict__ traffic) {
+                                                           unsigned long long* __restrict__ traffic,
+                                                           bool only_pending) {
   __shared__ uint32_t bins[kMaxBins];
   __shared__ uint32_t below[kMaxBins];  // particles inside bin b's lower edge
   __shared__ R sbuf[kSmemBuf];
@@ -744,6 +750,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
   R* my_gbuf = gbuf + (uint64_t)blockIdx.x * gcap;
 
   for (uint32_t s = blockIdx.x; s < n_surv; s += gridDim.x) {
+    if (only_pending && sv.reason[s] != kRescalePending) continue;
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
                   ck = (int32_t)fmul(cz, mesh.inv_l);
@@ -955,15 +962,234 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
   }
 }
 
+// The same growth with a warp per survivor and no block barrier: the warp
+// walks the whole template, keeps the survivor's histogram and prefix in its
+// own slice of shared memory, and resolves windows of up to 256 distances in
+// registers. A survivor whose window is wider is left kRescalePending for the
+// per-CTA kernel. Every count, bin and test is the per-CTA kernel's, so the
+// radius is the same bits.
+constexpr int kWarpSort = 256;
+
+template <class R>
+__global__ void __launch_bounds__(kGrowT) growth_warp_kernel(MeshViewT<R> mesh,
+                                                             TemplateViewT<R> tpl,
+                                                             RungConstsT<R> rc, SurvivorsT<R> sv,
+                                                             uint32_t nb_stride,
+                                                             unsigned long long* __restrict__ traffic) {
+  extern __shared__ unsigned char warp_smem[];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  // Per warp: bins[nb_stride], below[nb_stride], the window's distances, its count.
+  const size_t per_warp = 2 * (size_t)nb_stride * sizeof(uint32_t) + kWarpSort * sizeof(R) + 16;
+  unsigned char* base = warp_smem + warp * per_warp;
+  uint32_t* bins = (uint32_t*)base;
+  uint32_t* below = bins + nb_stride;
+  R* wbuf = (R*)(below + nb_stride);
+  uint32_t* collected = (uint32_t*)(wbuf + kWarpSort);
+  const uint32_t n_surv = *sv.count;
+  const uint32_t warps = gridDim.x * kGrowWarps;
+  for (uint32_t s = blockIdx.x * kGrowWarps + warp; s < n_surv; s += warps) {
+    const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
+    const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
+                  ck = (int32_t)fmul(cz, mesh.inv_l);
+    uint8_t reason = kRescaleOk;
+    R radius = -1.0f;
+    unsigned long long read = 0, visited = 0;
+    for (uint32_t b = lane; b < rc.nb; b += 32) bins[b] = 0;
+    __syncwarp();
+    // 1. Early refusal and the boundary cells' share of the histogram.
+    unsigned long long within = 0, n_core = 0, n_shell = 0;
+    walk_cells(
+        mesh, tpl, ci, cj, ck, cx, cy, cz, [](uint8_t, uint32_t) { return true; },
+        [&](uint8_t type, uint32_t cnt) {
+          if (type == kCellCore) {
+            within += cnt;
+            n_core += cnt;
+          } else if (type == kCellShell) {
+            within += cnt;
+            n_shell += cnt;
+          }
+        },
+        [](uint8_t type) { return type == kCellStraddle || type == kCellEdge; },
+        [&](uint8_t, R d2, uint32_t) {
+          if (d2 <= rc.rs2) within++;
+          if (d2 <= rc.rc2) {
+            n_core++;
+          } else if (d2 <= rc.rs2) {
+            atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
+            n_shell++;
+          }
+        },
+        visited, read, true);
+    within = __reduce_add_sync(0xffffffffu, (unsigned)within);
+    if (within == 0) {
+      reason = kRescaleEmpty;
+    } else if (fsub(fdiv(from_u64<R>(within), rc.expected), R(1.0f)) <= rc.threshold) {
+      reason = kRescaleBeyondSearch;
+    }
+    if (reason == kRescaleOk) {
+      // 2. The shell cells.
+      walk_cells(
+          mesh, tpl, ci, cj, ck, cx, cy, cz,
+          [](uint8_t type, uint32_t) { return type == kCellShell; }, [](uint8_t, uint32_t) {},
+          [](uint8_t) { return true; },
+          [&](uint8_t, R d2, uint32_t) {
+            atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
+          },
+          visited, read, true);
+      n_core = __reduce_add_sync(0xffffffffu, (unsigned)n_core);
+      n_shell = __reduce_add_sync(0xffffffffu, (unsigned)n_shell);
+      const unsigned long long total = n_core + n_shell;
+      if (total == 0) {
+        reason = kRescaleEmpty;
+      } else if (fsub(fdiv(from_u64<R>(total), rc.expected), R(1.0f)) <= rc.threshold) {
+        reason = kRescaleBeyondSearch;
+      }
+      if (reason == kRescaleOk) {
+        __syncwarp();
+        uint32_t carry = (uint32_t)n_core;
+        for (uint32_t b0 = 0; b0 < rc.nb; b0 += 32) {
+          const uint32_t b = b0 + lane;
+          const uint32_t v = b < rc.nb ? bins[b] : 0u;
+          uint32_t x = v;
+          for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= (unsigned)d) x += y;
+          }
+          if (b < rc.nb) below[b] = carry + x - v;
+          carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+        __syncwarp();
+        // 3. The walk and the resolution.
+        int32_t cursor = (int32_t)rc.nb - 1;
+        reason = kRescaleBelowRung;
+        while (cursor >= 0) {
+          int best = -1;
+          for (int32_t b = lane; b <= cursor; b += 32) {
+            if (bins[b] == 0) continue;
+            const R hi = bin_hi(rc, b);
+            const R nm = from_u32<R>(below[b]);
+            if (!(fmul(nm, nm) > fmul(fmul(fmul(rc.K2, hi), hi), hi))) best = max(best, b);
+          }
+          best = __reduce_max_sync(0xffffffffu, best + 1) - 1;
+          if (best < 0) break;
+          const int32_t b_hi = best;
+          int32_t b_lo = b_hi - (int32_t)rc.window + 1;
+          if (b_lo < 0) b_lo = 0;
+          const uint32_t top = below[b_hi] + bins[b_hi];
+          while (b_lo < b_hi && top - below[b_lo] > (uint32_t)kWarpSort) b_lo++;
+          if (top - below[b_lo] > (uint32_t)kWarpSort) {
+            reason = kRescalePending;  // one bin wider than the registers hold
+            break;
+          }
+          const R lo = fadd(rc.rc2, fmul((R)b_lo, rc.bin_w));
+          const R hi = bin_hi(rc, b_hi);
+          if (lane == 0) *collected = 0;
+          __syncwarp();
+          walk_cells(
+              mesh, tpl, ci, cj, ck, cx, cy, cz,
+              [&](uint8_t type, uint32_t i) {
+                return type != kCellCore && !(__ldg(tpl.max_d2 + i) < lo) &&
+                       !(__ldg(tpl.min_d2 + i) > hi);
+              },
+              [](uint8_t, uint32_t) {}, [](uint8_t) { return true; },
+              [&](uint8_t type, R d2, uint32_t) {
+                if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) return;
+                const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
+                if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) return;
+                const uint32_t slot = atomicAdd(collected, 1u);
+                if (slot < (uint32_t)kWarpSort) wbuf[slot] = d2;
+              },
+              visited, read, true);
+          __syncwarp();
+          const uint32_t m = *collected;  // = top - below[b_lo] <= kWarpSort
+          R v[8];
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            const uint32_t i = (uint32_t)j * 32 + lane;
+            v[j] = i < m ? wbuf[i] : real_inf<R>();
+          }
+          warp_sort256(v);
+          int f = -1;
+          R fv = 0;
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            const uint32_t k = (uint32_t)j * 32 + lane;
+            const R d2 = v[j];
+            if (k < m && d2 != R(0)) {
+              const R rn = from_u32<R>(top - m + k);
+              const R d2c = fmul(fmul(d2, d2), d2);
+              if (fmul(rn, rn) <= fmul(rc.K2, d2c)) {
+                f = (int)k;
+                fv = d2;
+              }
+            }
+          }
+          const int best_k = __reduce_max_sync(0xffffffffu, f + 1) - 1;
+          if (best_k >= 0) {
+            const int owner = best_k & 31;
+            radius = fsqrt(__shfl_sync(0xffffffffu, fv, owner));
+            reason = kRescaleOk;
+            break;
+          }
+          cursor = b_lo - 1;
+          __syncwarp();
+        }
+      }
+    }
+    if (traffic) {
+      const unsigned long long v = __reduce_add_sync(0xffffffffu, (unsigned)visited);
+      if (lane == 0) {
+        if (read) atomicAdd(traffic, read);
+        if (v) atomicAdd(traffic + 1, v);
+      }
+    }
+    if (lane == 0) {
+      sv.r[s] = reason == kRescaleOk ? radius : -1.0f;
+      sv.reason[s] = reason;
+    }
+    __syncwarp();
+  }
+}
+
+static int g_growth_mode = 0;
+void set_growth_mode(int mode) { g_growth_mode = mode; }
+
+// A warp per survivor pays once survivors outnumber the CTAs the per-CTA
+// kernel keeps resident several times over.
+constexpr uint32_t kWarpGrowthMin = 2048;
+
 template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s, uint32_t max_survivors,
           R* gbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
           KernelTimer* timer) {
   if (max_survivors == 0) return;
+  const bool by_warp = g_growth_mode == 2 || (g_growth_mode == 0 && max_survivors >= kWarpGrowthMin);
   const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
   if (timer) timer->begin(st);
-  growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic);
-  SIFG_LAUNCH_CHECK();
+  if (by_warp) {
+    const uint32_t nb_stride = (rc.nb + 31) & ~31u;
+    const size_t per_warp = 2 * (size_t)nb_stride * sizeof(uint32_t) + kWarpSort * sizeof(R) + 16;
+    const size_t smem = per_warp * kGrowWarps;
+    thread_local size_t attr_bytes = 0;  // the attribute is per thread's view of the function
+    if (smem > attr_bytes) {
+      SIFG_CUDA(cudaFuncSetAttribute(growth_warp_kernel<R>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr_bytes = smem;
+    }
+    int per_sm = 0;
+    SIFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, growth_warp_kernel<R>, kGrowT, smem));
+    const uint32_t warps_needed = (max_survivors + kGrowWarps - 1) / kGrowWarps;
+    const uint32_t cap = 152u * (uint32_t)std::max(per_sm, 1);
+    growth_warp_kernel<R><<<std::min(warps_needed, cap), kGrowT, smem, st>>>(mesh, tpl, rc, s,
+                                                                            nb_stride, traffic);
+    SIFG_LAUNCH_CHECK();
+    // The survivors whose windows were too wide for a warp.
+    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, true);
+    SIFG_LAUNCH_CHECK();
+  } else {
+    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, false);
+    SIFG_LAUNCH_CHECK();
+  }
   if (timer) timer->end(st);
 }
 

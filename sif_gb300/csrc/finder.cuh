@@ -24,6 +24,7 @@ enum : uint8_t {
   kRescaleBelowRung,
   kRescaleDegenerate,
   kRescaleOverflow,
+  kRescalePending,  // left by the warp-per-survivor growth for the per-CTA one
 };
 
 // Commit states.
@@ -160,6 +161,10 @@ template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
           uint32_t max_survivors, R* gbuf, uint32_t gcap, unsigned long long* traffic,
           cudaStream_t st, KernelTimer* timer);
+// Which growth kernel runs: 0 by the survivor count (a CTA per survivor for
+// few, a warp per survivor for many), 1 always a CTA, 2 always a warp. The
+// radii are the same either way (tests run both).
+void set_growth_mode(int mode);
 
 // The survivor hash for the commit.
 template <class R>

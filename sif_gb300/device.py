@@ -150,6 +150,11 @@ def launch_count():
     return int(_lib.load().sifg_launch_count())
 
 
+def set_growth_mode(mode):
+    """0 by survivor count, 1 a CTA per survivor, 2 a warp per survivor."""
+    _lib.load().sifg_set_growth_mode(int(mode))
+
+
 def set_window(bins):
     _lib.load().sifg_set_window(int(bins))
 

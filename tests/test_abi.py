@@ -126,6 +126,25 @@ def test_host_rank_replay_shapes(lib, oracle):
         _host_ranks_vs_oracle(lib, oracle, np.ascontiguousarray(case))
 
 
+def test_host_rank_replay_with_ties_on_the_pivot(lib, oracle):
+    """Segments large enough to be partitioned on every thread, with keys
+    equal to the first pivot (the middle element) scattered through them:
+    the queue of equal keys, rotated by the smaller keys examined between
+    them, must come out as the sequential partition leaves it."""
+    rng = np.random.default_rng(12)
+    for m, copies in [(100000, 2), (100000, 50), (120001, 2000), (70000, 300)]:
+        d = rng.uniform(-1.0, -0.8, m).astype(np.float32)
+        piv = d[(m - 1) // 2]
+        d[rng.choice(m, copies, replace=False)] = piv
+        d[rng.integers(0, m, 3000)] = d[rng.integers(0, m, 3000)]  # ties elsewhere too
+        _host_ranks_vs_oracle(lib, oracle, d)
+        # The pivot's twins bunched at either end.
+        e = d.copy()
+        e[:copies // 2] = piv
+        e[-(copies - copies // 2):] = piv
+        _host_ranks_vs_oracle(lib, oracle, e)
+
+
 def test_variants_and_argument_errors_without_a_gpu(lib):
     from sif_gb300 import abi
 

@@ -89,6 +89,16 @@ def test_fp64_catalogue_matches_reference(dev, golden_box32_f64, name):
     assert len(got[0]) == len(want[0]) and same_catalogue64(got, want), (len(got[0]), len(want[0]))
 
 
+@pytest.mark.parametrize("mode", [1, 2], ids=["cta", "warp"])
+def test_fp64_catalogue_either_growth_kernel(dev, golden_box32_f64, mode):
+    dev.set_growth_mode(mode)
+    try:
+        for name in ("default", "minima"):
+            test_fp64_catalogue_matches_reference(dev, golden_box32_f64, name)
+    finally:
+        dev.set_growth_mode(0)
+
+
 @pytest.mark.parametrize("window", ["full", "aliasing", "none"])
 def test_fp64_smoothing_against_oracle(dev, oracle, golden_box32_f64, window):
     g = golden_box32_f64

@@ -166,6 +166,20 @@ def test_catalogue_matches_reference_golden(dev, golden_box32, name):
     assert same_catalogue(cat, want)
 
 
+@pytest.fixture(params=[1, 2], ids=["cta", "warp"])
+def growth_mode(request, dev):
+    """Each sphere-growth kernel forced in turn; back to automatic after."""
+    dev.set_growth_mode(request.param)
+    yield request.param
+    dev.set_growth_mode(0)
+
+
+@pytest.mark.parametrize("name", ["default", "search_2_00", "lagrangian", "minima", "overlap_0_5"])
+def test_catalogue_matches_reference_golden_either_growth_kernel(dev, golden_box32, growth_mode,
+                                                                 name):
+    test_catalogue_matches_reference_golden(dev, golden_box32, name)
+
+
 @pytest.mark.parametrize("window", [1, 5, 64])
 def test_catalogue_independent_of_resolve_window(dev, golden_box32, window):
     g = golden_box32
@@ -213,6 +227,14 @@ def test_catalogue_matches_oracle_on_shared_fields(dev, oracle, case):
     # The GPU's own run (smoothing inside the finder) is the same run.
     own = dev.exodus(grid, ng, box, mesh, nm, radii, thr, ov, opt)
     assert same_catalogue(own, want)
+    # And so is each sphere-growth kernel forced.
+    for mode in (1, 2):
+        dev.set_growth_mode(mode)
+        try:
+            forced = dev.exodus(grid, ng, box, mesh, nm, radii, thr, ov, opt, inject=fields.reshape(-1))
+        finally:
+            dev.set_growth_mode(0)
+        assert same_catalogue(forced, want), mode
 
 
 def test_four_holes_and_brute_force_radii(gpu_lib, oracle):
