@@ -971,7 +971,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
 constexpr int kWarpSort = 256;
 
 template <class R>
-__global__ void __launch_bounds__(kGrowT) growth_warp_kernel(MeshViewT<R> mesh,
+__global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mesh,
                                                              TemplateViewT<R> tpl,
                                                              RungConstsT<R> rc, SurvivorsT<R> sv,
                                                              uint32_t nb_stride,
