@@ -1,5 +1,7 @@
 // The per-rung smoothing: cuFFT R2C of the density contrast once, then per
-// radius one fused filter kernel and a cuFFT C2R.
+// radius one fused filter kernel and a cuFFT C2R -- or, for the float form on
+// a 512^3 grid, three passes of its own that fuse the filter into the first
+// (below).
 //
 // Replaces sif__fft_grid_forward, fft_build_filter_lut,
 // sif__fft_apply_filter_smoothed and sif__fft_grid_backward
@@ -131,6 +133,312 @@ __global__ void __launch_bounds__(256) filter_kernel_f64(const double2* __restri
   }
 }
 
+// ---------------------------------------------------------------------------
+// The float form's inverse transform at n = 512, in three passes of its own
+// in place of the filter kernel and cuFFT's C2R:
+//   (1) filter + inverse FFT along kx (spectrum -> work),
+//   (2) inverse FFT along ky (work, in place),
+//   (3) C2R along kz (work -> the real grid).
+// A 512-point transform belongs to one warp, 16 values per lane: a 16-point
+// DFT in registers over the lane's stride-32 values, a twiddle, an exchange
+// through shared memory, a second 16-point DFT and a radix-2 step between
+// lane pairs by shuffles (512 = 16 x 32, 32 = 16 x 2). Passes (1) and (2)
+// give a CTA 16 neighbouring kz columns of one line (128 contiguous bytes
+// per row of the line); pass (3) gives each 257-mode kz row to a half-warp
+// as a 256-point complex transform of the packed even and odd samples.
+// Twiddles come from tables computed in double; the three passes read and
+// write the transform's data once each.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul_i(float2 a) { return make_float2(-a.y, a.x); }  // a * i
+
+// Asynchronous global -> shared copies (LDGSTS): a CTA's whole tile is in
+// flight at once, with no registers held for it.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// e^{+2 pi i k/32}, k < 16, rounded to float.
+__constant__ float2 kW32[16] = {
+    {1.0f, 0.0f},
+    {0.9807852506637573f, 0.19509032368659973f},
+    {0.9238795042037964f, 0.3826834261417389f},
+    {0.8314695954322815f, 0.5555702447891235f},
+    {0.7071067690849304f, 0.7071067690849304f},
+    {0.5555702447891235f, 0.8314695954322815f},
+    {0.3826834261417389f, 0.9238795042037964f},
+    {0.19509032368659973f, 0.9807852506637573f},
+    {0.0f, 1.0f},
+    {-0.19509032368659973f, 0.9807852506637573f},
+    {-0.3826834261417389f, 0.9238795042037964f},
+    {-0.5555702447891235f, 0.8314695954322815f},
+    {-0.7071067690849304f, 0.7071067690849304f},
+    {-0.8314695954322815f, 0.5555702447891235f},
+    {-0.9238795042037964f, 0.3826834261417389f},
+    {-0.9807852506637573f, 0.19509032368659973f},
+};
+
+// Inverse (e^{+2 pi i jk/R}) DFTs of 4, 8 and 16 points, in place, natural order.
+__device__ __forceinline__ void dft_inv(float2 (&v)[4]) {
+  const float2 c0 = cadd(v[0], v[2]), c2 = csub(v[0], v[2]);
+  const float2 c1 = cadd(v[1], v[3]), d = cmul_i(csub(v[1], v[3]));
+  v[0] = cadd(c0, c1);
+  v[2] = csub(c0, c1);
+  v[1] = cadd(c2, d);
+  v[3] = csub(c2, d);
+}
+__device__ __forceinline__ void dft_inv(float2 (&v)[8]) {
+  const float h = 0.70710678118654752440f;  // cos(pi/4)
+  float2 a[4], b[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    a[j] = cadd(v[j], v[j + 4]);
+    b[j] = csub(v[j], v[j + 4]);
+  }
+  // b[j] *= w^j, w = e^{+i pi/4}
+  b[1] = make_float2(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y));
+  b[2] = cmul_i(b[2]);
+  b[3] = make_float2(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y));
+  dft_inv(a);
+  dft_inv(b);
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    v[2 * m] = a[m];
+    v[2 * m + 1] = b[m];
+  }
+}
+__device__ __forceinline__ void dft_inv(float2 (&v)[16]) {
+  float2 e[8], o[8];
+#pragma unroll
+  for (int m = 0; m < 8; m++) {
+    e[m] = v[2 * m];
+    o[m] = v[2 * m + 1];
+  }
+  dft_inv(e);
+  dft_inv(o);
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    float2 t;
+    if (k == 0)
+      t = o[0];
+    else if (k == 4)
+      t = cmul_i(o[4]);
+    else
+      t = cmul(o[k], kW32[2 * k]);
+    v[k] = cadd(e[k], t);
+    v[k + 8] = csub(e[k], t);
+  }
+}
+
+// A column of 512 in shared memory: element i at col_slot(i), columns
+// kColStride slots apart (odd). The stage-to-stage exchange uses rows of
+// kColSpan slots. With these, every shared access of the transform, and the
+// 16-column row loads and stores, is free of bank conflicts.
+__host__ __device__ constexpr int col_slot(int i) { return i + (i >> 4) + 8 * (i >> 8); }
+constexpr int kColCols = 16;
+constexpr int kColWarps = 8;  // each warp transforms kColCols / kColWarps columns
+constexpr int kColSpan = 34;
+constexpr int kColStride = 551;
+static_assert(kColStride > col_slot(511) && kColStride >= 16 * kColSpan && (kColStride & 1),
+              "column layout");
+
+// Twiddle tables of the n = 512 transform, one device block:
+//   [0, 512):    W512^(j k), at k * 32 + j (j < 32, k < 16), the column pass
+//   [512, 768):  W256^(j k), at k * 16 + j (j, k < 16), the row pass
+//   [768, 1024): W512^k, k < 256, the row pass's even/odd packing
+constexpr int kTw512 = 1024;
+
+// The filter of one kx column at (ky, kz): mode kx is scaled by
+// lut[k^2] * norm * win[kx] * win[ky] * win[kz] (win optional), the factor
+// and the order of its products as the per-mode filter kernel has them.
+struct ColumnFilter {
+  const float* lut;
+  const float* win;
+  float norm, wy, wz;
+  uint32_t q;  // ky'^2 + kz^2
+};
+
+// One warp's inverse DFT of the 512 values in `col`, in place; with kFilter
+// each value is first scaled by its filter factor.
+template <bool kFilter>
+__device__ __forceinline__ void ifft512_column(float2* col, const float2* __restrict__ tw,
+                                               unsigned lane, const ColumnFilter& f) {
+  float2 v[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) v[r] = col[col_slot((int)lane + 32 * r)];
+  if (kFilter) {
+    // The factor is even in kx (the window table is built from |k|): a lane
+    // reads it for its kx < 256 and takes kx > 256 from the lane holding
+    // 512 - kx, half the table reads. Lane 0 holds both kx = 32 r and
+    // 512 - 32 r itself, and alone reads kx = 256.
+    float lo[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      const uint32_t kx = lane + 32u * r;
+      lo[r] = __ldg(f.lut + kx * kx + f.q) * f.norm;
+      if (f.win) lo[r] = lo[r] * __ldg(f.win + kx) * f.wy * f.wz;
+    }
+    float nyq = 0.f;
+    if (lane == 0) {
+      nyq = __ldg(f.lut + 256u * 256u + f.q) * f.norm;
+      if (f.win) nyq = nyq * __ldg(f.win + 256) * f.wy * f.wz;
+    }
+    const unsigned partner = (32u - lane) & 31u;
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+      float s;
+      if (r < 8) {
+        s = lo[r];
+      } else {
+        s = __shfl_sync(0xffffffffu, lo[15 - r], partner);
+        if (lane == 0) s = r == 8 ? nyq : lo[(16 - r) & 7];
+      }
+      v[r] = make_float2(v[r].x * s, v[r].y * s);
+    }
+  }
+  dft_inv(v);
+#pragma unroll
+  for (int k = 1; k < 16; k++) v[k] = cmul(v[k], __ldg(tw + k * 32 + lane));
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 16; k++) col[kColSpan * k + lane] = v[k];
+  __syncwarp();
+  const unsigned k1 = lane >> 1, q = lane & 1u;
+#pragma unroll
+  for (int m = 0; m < 16; m++) v[m] = col[kColSpan * k1 + q + 2 * m];
+  dft_inv(v);
+#pragma unroll
+  for (int k = 1; k < 16; k++) v[k] = cmul(v[k], q ? kW32[k] : make_float2(1.f, 0.f));
+#pragma unroll
+  for (int k = 0; k < 16; k++) {
+    const float2 o = make_float2(__shfl_xor_sync(0xffffffffu, v[k].x, 1),
+                                 __shfl_xor_sync(0xffffffffu, v[k].y, 1));
+    v[k] = q ? csub(o, v[k]) : cadd(v[k], o);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 16; k++) col[col_slot((int)k1 + 16 * (k + 16 * (int)q))] = v[k];
+  __syncwarp();
+}
+
+// Passes (1) and (2). Line `blockIdx.y` starts at line * line_stride; its
+// element a of column kz at a * elem_stride + kz. The tile arrives by
+// asynchronous copies; pass (1) scales each mode by its filter factor as the
+// transform first reads it (line = ky); pass (2) works in place. Columns past
+// kz = 256 (in the last CTA of a line) are neither read, transformed nor
+// written.
+template <bool kFilter>
+__global__ void __launch_bounds__(32 * kColWarps, 3)
+    colfft512_kernel(const float2* src, float2* dst, uint32_t line_stride, uint32_t elem_stride,
+                     const float* __restrict__ lut, const float* __restrict__ win, float norm,
+                     const float2* __restrict__ tw) {
+  extern __shared__ float2 cols[];  // kColCols columns of kColStride slots
+  constexpr uint32_t zd = 257;
+  constexpr uint32_t kRowStep = 32 * kColWarps / kColCols;  // rows a pass of the CTA covers
+  const uint32_t kz0 = blockIdx.x * kColCols, line = blockIdx.y;
+  const uint32_t c = threadIdx.x % kColCols, row0 = threadIdx.x / kColCols;
+  const bool live = kz0 + c < zd;
+  const size_t base = (size_t)line * line_stride + kz0 + c;
+  if (live) {
+    const float2* p = src + base + (size_t)row0 * elem_stride;
+    const size_t step = (size_t)kRowStep * elem_stride;
+#pragma unroll 8
+    for (uint32_t i = 0; i < 512 / kRowStep; i++, p += step)
+      cp_async8(cols + c * kColStride + col_slot((int)(row0 + kRowStep * i)), p);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+#pragma unroll 1
+  for (uint32_t w = warp; w < kColCols && kz0 + w < zd; w += kColWarps) {
+    ColumnFilter f{};
+    if (kFilter) {
+      const uint32_t kz = kz0 + w;
+      const int32_t ks = line > 256 ? (int32_t)line - 512 : (int32_t)line;
+      f = ColumnFilter{lut, win, norm, win ? __ldg(win + line) : 1.f, win ? __ldg(win + kz) : 1.f,
+                       (uint32_t)(ks * ks) + kz * kz};
+    }
+    ifft512_column<kFilter>(cols + w * kColStride, tw, lane, f);
+  }
+  __syncthreads();
+  if (live) {
+    float2* p = dst + base + (size_t)row0 * elem_stride;
+    const size_t step = (size_t)kRowStep * elem_stride;
+#pragma unroll 8
+    for (uint32_t i = 0; i < 512 / kRowStep; i++, p += step)
+      *p = cols[c * kColStride + col_slot((int)(row0 + kRowStep * i))];
+  }
+}
+
+// Pass (3): 16 rows of 257 modes per CTA, a half-warp per row. With Z the
+// row's modes (the imaginary parts of Z[0] and Z[256] taken as zero, as a
+// C2R does), c[k] = Fe[k] + i Fo[k] for k < 256, Fe = Z[k] + conj Z[256-k],
+// Fo = (Z[k] - conj Z[256-k]) W512^k, and its 256-point inverse DFT y gives
+// the real samples x[2m] = Re y[m], x[2m+1] = Im y[m]. The CTA's rows are one
+// contiguous, 16-byte aligned block, copied in whole by asynchronous copies;
+// the stage exchange swizzles slots (k1, j) -> 16 k1 + (j ^ k1) within the
+// row's own 257 slots.
+constexpr int kRowsPerCta = 16;
+__global__ void __launch_bounds__(16 * kRowsPerCta)
+    c2r512_rows_kernel(const float2* __restrict__ spec, float* __restrict__ out,
+                       const float2* __restrict__ tw) {
+  constexpr uint32_t zd = 257;
+  __shared__ __align__(16) float2 buf[kRowsPerCta * zd];
+  const size_t row0 = (size_t)blockIdx.x * kRowsPerCta;
+  const float4* src = reinterpret_cast<const float4*>(spec + row0 * zd);
+  for (uint32_t f = threadIdx.x; f < kRowsPerCta * zd / 2; f += blockDim.x)
+    cp_async16(buf + 2 * f, src + f);
+  cp_async_wait_all();
+  __syncthreads();
+  const unsigned j = threadIdx.x & 15u;
+  float2* row = buf + (threadIdx.x >> 4) * zd;
+  const float2* twb = tw + 512;
+  const float2* wpre = tw + 768;
+  float2 v[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    const unsigned k = j + 16u * r;
+    float2 z = row[k], zc = row[256 - k];
+    if (r == 0 && j == 0) z.y = zc.y = 0.f;
+    zc.y = -zc.y;
+    const float2 fe = cadd(z, zc), fo = cmul(csub(z, zc), __ldg(wpre + k));
+    v[r] = make_float2(fe.x - fo.y, fe.y + fo.x);
+  }
+  dft_inv(v);
+#pragma unroll
+  for (int k = 1; k < 16; k++) v[k] = cmul(v[k], __ldg(twb + k * 16 + j));
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 16; k++) row[16 * k + (j ^ k)] = v[k];
+  __syncwarp();
+#pragma unroll
+  for (int m = 0; m < 16; m++) v[m] = row[16 * j + (m ^ j)];
+  dft_inv(v);
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 16; k++) row[j + 16 * k] = v[k];
+  __syncthreads();
+  float2* dst = reinterpret_cast<float2*>(out + row0 * 512);
+  for (uint32_t f = threadIdx.x; f < kRowsPerCta * 256; f += blockDim.x)
+    dst[f] = buf[(f >> 8) * zd + (f & 255u)];
+}
+
+static bool own_inverse(uint32_t n) { return n == 512; }
+
 // fft_build_filter_lut, src/math/fft.c:521-568: the radial factor by integer
 // |k|^2, computed in double.
 template <class R>
@@ -160,13 +468,18 @@ SmootherT<R>::~SmootherT() {
 }
 
 template <class R>
+static void destroy_plans(typename SmootherT<R>::Plans& p) {
+  cufftDestroy(p.r2c);
+  if (p.c2r) cufftDestroy(p.c2r);
+  if (p.twiddles) cudaFree(p.twiddles);
+}
+
+template <class R>
 void SmootherT<R>::release() {
-  for (const Plans& p : plans) {
-    cufftDestroy(p.r2c);
-    cufftDestroy(p.c2r);
-  }
+  for (auto& p : plans) destroy_plans<R>(p);
   plans.clear();
   plan_r2c = plan_c2r = 0;
+  twiddles = nullptr;
   n = 0;
 }
 
@@ -178,24 +491,40 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
     auto it = std::find_if(plans.begin(), plans.end(), [&](const Plans& p) { return p.n == n_; });
     if (it == plans.end()) {
       if ((int)plans.size() >= kPlanCache) {
-        cufftDestroy(plans.front().r2c);
-        cufftDestroy(plans.front().c2r);
+        destroy_plans<R>(plans.front());
         plans.erase(plans.begin());
       }
       Plans p{n_, 0, 0};
       SIFG_CUFFT(cufftPlan3d(&p.r2c, (int)n_, (int)n_, (int)n_, dbl ? CUFFT_D2Z : CUFFT_R2C));
-      SIFG_CUFFT(cufftPlan3d(&p.c2r, (int)n_, (int)n_, (int)n_, dbl ? CUFFT_Z2D : CUFFT_C2R));
+      if (!dbl && own_inverse(n_)) {
+        // The tables of the three-pass inverse, computed in double.
+        std::vector<float2> tw(kTw512);
+        auto root = [](double num, double den) {
+          const double a = 2.0 * M_PI * num / den;
+          return make_float2((float)std::cos(a), (float)std::sin(a));
+        };
+        for (int k = 0; k < 16; k++)
+          for (int j = 0; j < 32; j++) tw[k * 32 + j] = root((double)(j * k), 512.0);
+        for (int k = 0; k < 16; k++)
+          for (int j = 0; j < 16; j++) tw[512 + k * 16 + j] = root((double)(j * k), 256.0);
+        for (int k = 0; k < 256; k++) tw[768 + k] = root((double)k, 512.0);
+        SIFG_CUDA(cudaMalloc(&p.twiddles, kTw512 * sizeof(float2)));
+        SIFG_CUDA(cudaMemcpy(p.twiddles, tw.data(), kTw512 * sizeof(float2), cudaMemcpyHostToDevice));
+      } else {
+        SIFG_CUFFT(cufftPlan3d(&p.c2r, (int)n_, (int)n_, (int)n_, dbl ? CUFFT_Z2D : CUFFT_C2R));
+      }
       plans.push_back(p);
       it = plans.end() - 1;
     }
     n = n_;
     plan_r2c = it->r2c;
     plan_c2r = it->c2r;
+    twiddles = it->twiddles;
     rebind = true;  // a cached plan may be bound to another stream
   }
   if (rebind || st != stream) {
     SIFG_CUFFT(cufftSetStream(plan_r2c, st));
-    SIFG_CUFFT(cufftSetStream(plan_c2r, st));
+    if (plan_c2r) SIFG_CUFFT(cufftSetStream(plan_c2r, st));
     stream = st;
   }
   box = box_;
@@ -212,7 +541,7 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
     // W/S aliasing-aware, W = sinc^2(pi k / N), S = 1 - 2 sin^2/3.
     std::vector<R> w(n);
     for (uint32_t i = 0; i < n; i++) {
-      const int32_t k = i > h ? (int32_t)i - (int32_t)n : (int32_t)i;
+      const int32_t k = i > h ? (int32_t)n - (int32_t)i : (int32_t)i;  // |k|: an even table
       const double x = M_PI * (double)k / (double)n;
       const double s = (x < 1e-9 && x > -1e-9) ? 1.0 : std::sin(x) / x;
       const double W = s * s;
@@ -244,6 +573,32 @@ static void launch_filter(const SmootherT<float>& s, int filter, float norm) {
                                                        s.n, s.lut.as<float>(), w, norm);
 }
 
+// The three passes of the n = 512 inverse transform, on the smoother's stream.
+static void launch_inverse512(const SmootherT<float>& s, int filter, float norm, float* out) {
+  constexpr uint32_t N = 512, zd = 257;
+  const float* w = (s.window_mode && filter != kFilterNone) ? s.win.as<float>() : nullptr;
+  const size_t smem = (size_t)kColCols * kColStride * sizeof(float2);
+  thread_local bool attr = false;  // set once per thread
+  if (!attr) {
+    SIFG_CUDA(cudaFuncSetAttribute(colfft512_kernel<true>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SIFG_CUDA(cudaFuncSetAttribute(colfft512_kernel<false>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  const float2* tw = (const float2*)s.twiddles;
+  const dim3 grid((zd + kColCols - 1) / kColCols, N);
+  colfft512_kernel<true><<<grid, 32 * kColWarps, smem, s.stream>>>(
+      s.spectrum.as<float2>(), s.work.as<float2>(), zd, N * zd, s.lut.as<float>(), w, norm, tw);
+  SIFG_LAUNCH_CHECK();
+  colfft512_kernel<false><<<grid, 32 * kColWarps, smem, s.stream>>>(
+      s.work.as<float2>(), s.work.as<float2>(), N * zd, zd, nullptr, nullptr, 1.f, tw);
+  SIFG_LAUNCH_CHECK();
+  c2r512_rows_kernel<<<N * N / kRowsPerCta, 16 * kRowsPerCta, 0, s.stream>>>(s.work.as<float2>(),
+                                                                           out, tw);
+}
+static void launch_inverse512(const SmootherT<double>&, int, double, double*) {}
+
 static void launch_filter(const SmootherT<double>& s, int filter, double norm) {
   const uint64_t modes = (uint64_t)s.n * s.n * (s.n / 2 + 1);
   const double* w = (s.window_mode && filter != kFilterNone) ? s.win.as<double>() : nullptr;
@@ -262,6 +617,11 @@ void SmootherT<R>::smooth(int filter, R r, R sigma, R* out, KernelTimer* timer) 
   SIFG_LAUNCH_CHECK();
   const R norm = (R)(1.0 / ((double)n * n * n));
   if (timer) timer->begin(stream);
+  if (twiddles) {
+    launch_inverse512(*this, filter, norm, out);
+    if (timer) timer->end(stream);
+    return;
+  }
   launch_filter(*this, filter, norm);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(stream);

@@ -30,7 +30,9 @@ struct SmootherT {
   struct Plans {
     uint32_t n;
     cufftHandle r2c, c2r;
+    void* twiddles = nullptr;  // the float form's own inverse at n = 512: its tables (c2r unset)
   };
+  const void* twiddles = nullptr;
   std::vector<Plans> plans;
 
   void setup(uint32_t n, R box, int window_mode, cudaStream_t st);

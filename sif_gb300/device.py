@@ -4,6 +4,10 @@ torch only allocates and holds the device memory here; every stage is a call
 into libsif_gb300.so (include/sif_gb300.h, part 2) with raw device pointers.
 float64 inputs select the FP64 form (the `_f64` entry points, the reference's
 SIF_USE_DOUBLE arithmetic); float32 inputs the float form.
+
+The library runs on its own streams and returns once its results are
+complete; before each call the torch stream that produced the inputs is
+drained, since nothing else orders the library's reads after torch's writes.
 """
 import ctypes as C
 
@@ -30,6 +34,11 @@ def _form(t):
 
 
 def _fn(name, t):
+    """The entry point for t's form, once torch's work on t's device is done."""
+    import torch
+
+    if t.is_cuda:
+        torch.cuda.current_stream(t.device).synchronize()
     return getattr(_lib.load(), name + _form(t)[0])
 
 
@@ -164,7 +173,11 @@ def box_batch(boxes, engines=0, capacity=1 << 20, check=True):
     mesh_cells=0, overlap=0.0, options=0)], particles as float32 CUDA tensors.
     Returns (catalogues, engines used); each catalogue is what box() returns
     for that box alone."""
+    import torch
+
     lib = _lib.load()
+    if boxes and boxes[0]["x"].is_cuda:
+        torch.cuda.current_stream(boxes[0]["x"].device).synchronize()
     jobs = (_lib.BoxJob * len(boxes))()
     keep = []
     for j, b in zip(jobs, boxes):
