@@ -272,15 +272,14 @@ struct ColumnFilter {
   uint32_t q;  // ky'^2 + kz^2
 };
 
-// One warp's inverse DFT of the 512 values in `col`, in place; with kFilter
-// each value is first scaled by its filter factor.
-template <bool kFilter>
+// One warp's inverse DFT of the 512 values in `col`, in place; with a filter
+// (f.lut set) each value is first scaled by its filter factor.
 __device__ __forceinline__ void ifft512_column(float2* col, const float2* __restrict__ tw,
                                                unsigned lane, const ColumnFilter& f) {
   float2 v[16];
 #pragma unroll
   for (int r = 0; r < 16; r++) v[r] = col[col_slot((int)lane + 32 * r)];
-  if (kFilter) {
+  if (f.lut) {
     // The factor is even in kx (the window table is built from |k|): a lane
     // reads it for its kx < 256 and takes kx > 256 from the lane holding
     // 512 - kx, half the table reads. Lane 0 holds both kx = 32 r and
@@ -320,28 +319,38 @@ __device__ __forceinline__ void ifft512_column(float2* col, const float2* __rest
   const unsigned k1 = lane >> 1, q = lane & 1u;
 #pragma unroll
   for (int m = 0; m < 16; m++) v[m] = col[kColSpan * k1 + q + 2 * m];
-  dft_inv(v);
+  dft_inv(v);  // E_q[k], k < 16
+  // The radix-2 step between the pair: X[k1 + 16 k] = E_0[k] + W32^k E_1[k],
+  // X[k1 + 16 (k + 16)] = E_0[k] - W32^k E_1[k]. Lane q = 0 finishes k < 8,
+  // lane q = 1 k >= 8; each sends the half of its E it does not keep, and
+  // W32^(8 + i) = i W32^i leaves one twiddle per register for both lanes.
 #pragma unroll
-  for (int k = 1; k < 16; k++) v[k] = cmul(v[k], q ? kW32[k] : make_float2(1.f, 0.f));
-#pragma unroll
-  for (int k = 0; k < 16; k++) {
-    const float2 o = make_float2(__shfl_xor_sync(0xffffffffu, v[k].x, 1),
-                                 __shfl_xor_sync(0xffffffffu, v[k].y, 1));
-    v[k] = q ? csub(o, v[k]) : cadd(v[k], o);
+  for (int i = 0; i < 8; i++) {
+    const float2 send = q ? v[i] : v[8 + i];
+    const float2 got = make_float2(__shfl_xor_sync(0xffffffffu, send.x, 1),
+                                   __shfl_xor_sync(0xffffffffu, send.y, 1));
+    const float2 a = q ? got : v[i];          // E_0[8 q + i]
+    const float2 b = q ? cmul_i(v[8 + i]) : got;  // E_1[8 q + i] (times i for q = 1)
+    const float2 t = i == 0 ? b : cmul(b, kW32[i]);
+    v[i] = cadd(a, t);
+    v[8 + i] = csub(a, t);
   }
   __syncwarp();
 #pragma unroll
-  for (int k = 0; k < 16; k++) col[col_slot((int)k1 + 16 * (k + 16 * (int)q))] = v[k];
+  for (int i = 0; i < 8; i++) {
+    const int x = (int)k1 + 16 * (8 * (int)q + i);
+    col[col_slot(x)] = v[i];
+    col[col_slot(x + 256)] = v[8 + i];
+  }
   __syncwarp();
 }
 
 // Passes (1) and (2). Line `blockIdx.y` starts at line * line_stride; its
 // element a of column kz at a * elem_stride + kz. The tile arrives by
-// asynchronous copies; pass (1) scales each mode by its filter factor as the
-// transform first reads it (line = ky); pass (2) works in place. Columns past
-// kz = 256 (in the last CTA of a line) are neither read, transformed nor
-// written.
-template <bool kFilter>
+// asynchronous copies; pass (1) (lut set) scales each mode by its filter
+// factor as the transform first reads it (line = ky); pass (2) works in
+// place. Columns past kz = 256 (in the last CTA of a line) are neither read,
+// transformed nor written.
 __global__ void __launch_bounds__(32 * kColWarps, 3)
     colfft512_kernel(const float2* src, float2* dst, uint32_t line_stride, uint32_t elem_stride,
                      const float* __restrict__ lut, const float* __restrict__ win, float norm,
@@ -366,13 +375,13 @@ __global__ void __launch_bounds__(32 * kColWarps, 3)
 #pragma unroll 1
   for (uint32_t w = warp; w < kColCols && kz0 + w < zd; w += kColWarps) {
     ColumnFilter f{};
-    if (kFilter) {
+    if (lut) {
       const uint32_t kz = kz0 + w;
       const int32_t ks = line > 256 ? (int32_t)line - 512 : (int32_t)line;
       f = ColumnFilter{lut, win, norm, win ? __ldg(win + line) : 1.f, win ? __ldg(win + kz) : 1.f,
                        (uint32_t)(ks * ks) + kz * kz};
     }
-    ifft512_column<kFilter>(cols + w * kColStride, tw, lane, f);
+    ifft512_column(cols + w * kColStride, tw, lane, f);
   }
   __syncthreads();
   if (live) {
@@ -574,30 +583,31 @@ static void launch_filter(const SmootherT<float>& s, int filter, float norm) {
 }
 
 // The three passes of the n = 512 inverse transform, on the smoother's stream.
-static void launch_inverse512(const SmootherT<float>& s, int filter, float norm, float* out) {
+// The timer, begun by the caller, ends after pass (1): the filter's kernel.
+static void launch_inverse512(const SmootherT<float>& s, int filter, float norm, float* out,
+                              KernelTimer* timer) {
   constexpr uint32_t N = 512, zd = 257;
   const float* w = (s.window_mode && filter != kFilterNone) ? s.win.as<float>() : nullptr;
   const size_t smem = (size_t)kColCols * kColStride * sizeof(float2);
   thread_local bool attr = false;  // set once per thread
   if (!attr) {
-    SIFG_CUDA(cudaFuncSetAttribute(colfft512_kernel<true>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    SIFG_CUDA(cudaFuncSetAttribute(colfft512_kernel<false>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SIFG_CUDA(cudaFuncSetAttribute(colfft512_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
     attr = true;
   }
   const float2* tw = (const float2*)s.twiddles;
   const dim3 grid((zd + kColCols - 1) / kColCols, N);
-  colfft512_kernel<true><<<grid, 32 * kColWarps, smem, s.stream>>>(
+  colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
       s.spectrum.as<float2>(), s.work.as<float2>(), zd, N * zd, s.lut.as<float>(), w, norm, tw);
   SIFG_LAUNCH_CHECK();
-  colfft512_kernel<false><<<grid, 32 * kColWarps, smem, s.stream>>>(
+  if (timer) timer->end(s.stream);
+  colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
       s.work.as<float2>(), s.work.as<float2>(), N * zd, zd, nullptr, nullptr, 1.f, tw);
   SIFG_LAUNCH_CHECK();
   c2r512_rows_kernel<<<N * N / kRowsPerCta, 16 * kRowsPerCta, 0, s.stream>>>(s.work.as<float2>(),
                                                                            out, tw);
 }
-static void launch_inverse512(const SmootherT<double>&, int, double, double*) {}
+static void launch_inverse512(const SmootherT<double>&, int, double, double*, KernelTimer*) {}
 
 static void launch_filter(const SmootherT<double>& s, int filter, double norm) {
   const uint64_t modes = (uint64_t)s.n * s.n * (s.n / 2 + 1);
@@ -618,8 +628,7 @@ void SmootherT<R>::smooth(int filter, R r, R sigma, R* out, KernelTimer* timer) 
   const R norm = (R)(1.0 / ((double)n * n * n));
   if (timer) timer->begin(stream);
   if (twiddles) {
-    launch_inverse512(*this, filter, norm, out);
-    if (timer) timer->end(stream);
+    launch_inverse512(*this, filter, norm, out, timer);
     return;
   }
   launch_filter(*this, filter, norm);
