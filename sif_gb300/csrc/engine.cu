@@ -45,9 +45,13 @@ Engine::Engine(int device) : device_(device) {
   SIFG_CUDA(cudaSetDevice(device));
   int lo_prio = 0, hi_prio = 0;  // numerically, lo_prio >= hi_prio
   SIFG_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+  // The run's stream first; then the smoothing, which the early rungs wait on;
+  // the chain-mesh build last: it is needed only at the first sphere growth
+  // and takes what bandwidth the smoothing leaves.
+  const int mid_prio = hi_prio < lo_prio ? hi_prio + 1 : lo_prio;
   SIFG_CUDA(cudaStreamCreateWithPriority(&st_, cudaStreamNonBlocking, hi_prio));
-  SIFG_CUDA(cudaStreamCreateWithPriority(&st_fft_, cudaStreamNonBlocking, lo_prio));
-  SIFG_CUDA(cudaStreamCreateWithFlags(&st_copy_, cudaStreamNonBlocking));
+  SIFG_CUDA(cudaStreamCreateWithPriority(&st_fft_, cudaStreamNonBlocking, mid_prio));
+  SIFG_CUDA(cudaStreamCreateWithPriority(&st_copy_, cudaStreamNonBlocking, lo_prio));
   SIFG_CUDA(cudaEventCreateWithFlags(&ev_copy_start_, cudaEventDisableTiming));
   SIFG_CUDA(cudaEventCreateWithFlags(&ev_mesh_ready_, cudaEventDisableTiming));
   SIFG_CUDA(cudaEventCreateWithFlags(&ev_cand_, cudaEventDisableTiming));
@@ -235,7 +239,19 @@ bool partition3_parallel(Rec<K>* a, int64_t lo, int64_t hi, int t, int64_t* lt_o
   // The j-th larger key of the left stream (1-based): the smaller and the
   // not-larger keys before it (pa, pb). The right stream's j-th not-larger
   // key: the smaller keys up to and including it (ra) and its index (rb).
-  std::vector<int64_t> pa(n + 2), pb(n + 2), ra(n + 2), rb(n + 2);
+  // Scratch kept by the calling thread between calls (fresh multi-megabyte
+  // vectors cost a page fault per page on every partition), reached from
+  // the team through plain pointers: a thread_local named inside the
+  // parallel regions would be each worker's own.
+  thread_local std::vector<int64_t> scratch;
+  thread_local std::vector<Rec<K>> out_buf;
+  if (scratch.size() < 4 * ((size_t)n + 2)) scratch.resize(4 * ((size_t)n + 2));
+  if (out_buf.size() < (size_t)n) out_buf.resize(n);
+  int64_t* const pa = scratch.data();
+  int64_t* const pb = pa + (n + 2);
+  int64_t* const ra = pb + (n + 2);
+  int64_t* const rb = ra + (n + 2);
+  Rec<K>* const out = out_buf.data();
 #pragma omp parallel for num_threads(t) schedule(static, 1)
   for (int c = 0; c < t; c++) {
     int64_t l = lc[3 * c], g = lc[3 * c + 1], ng = lc[3 * c + 2];
@@ -265,7 +281,6 @@ bool partition3_parallel(Rec<K>* a, int64_t lo, int64_t hi, int t, int64_t* lt_o
   }
   // Destinations; the equal keys with their place among the not-larger keys
   // in the order examined.
-  std::vector<Rec<K>> out(n);
   std::vector<std::vector<std::pair<int64_t, Rec<K>>>> eq(t);
 #pragma omp parallel for num_threads(t) schedule(static, 1)
   for (int c = 0; c < t; c++) {
@@ -325,7 +340,9 @@ bool partition3_parallel(Rec<K>* a, int64_t lo, int64_t hi, int t, int64_t* lt_o
 
 template <class K>
 void candidate_ranks(const K* delta, uint32_t m, uint32_t* rank, int threads) {
-  std::vector<Rec<K>> a(m);
+  thread_local std::vector<Rec<K>> keep;  // kept between calls, as the partition's scratch
+  if (keep.size() < m) keep.resize(m);
+  Rec<K>* const a = keep.data();  // the tasks reach it through this pointer
   for (uint32_t k = 0; k < m; k++) a[k] = Rec<K>{delta[k], k};
   const int t = threads > 0 ? threads : omp_get_max_threads();
   if (m > 2 * (uint32_t)kTaskCutoff && t > 1) {
@@ -340,7 +357,7 @@ void candidate_ranks(const K* delta, uint32_t m, uint32_t* rank, int threads) {
         continue;
       }
       int64_t lt, gt;
-      if (!partition3_parallel(a.data(), l, h, t, &lt, &gt)) partition3(a.data(), l, h, &lt, &gt);
+      if (!partition3_parallel(a, l, h, t, &lt, &gt)) partition3(a, l, h, &lt, &gt);
       big.emplace_back(l, lt - 1);
       big.emplace_back(gt + 1, h);
     }
@@ -348,10 +365,10 @@ void candidate_ranks(const K* delta, uint32_t m, uint32_t* rank, int threads) {
 #pragma omp single nowait
     for (const auto& [l, h] : small) {
 #pragma omp task firstprivate(l, h)
-      qsort_tasks(a.data(), l, h);
+      qsort_tasks(a, l, h);
     }
   } else if (m > 1) {
-    qsort_serial(a.data(), 0, (int64_t)m - 1);
+    qsort_serial(a, 0, (int64_t)m - 1);
   }
   for (uint32_t k = 0; k < m; k++) rank[a[k].i] = k;
 }
