@@ -940,29 +940,39 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
   if (n_grid < 4 || mesh_cells == 0) return fail(SIF_ERR_INVALID, "grid or mesh: bad size");
   BoxBufs& io = e->io;
   cudaStream_t s = e->stream();
-  int st = check_in_box(x, y, z, n, box, "field", s, io.flag);
-  if (st != SIF_OK) return st;
   const uint64_t cells = (uint64_t)n_grid * n_grid * n_grid;
   const uint64_t mcells = (uint64_t)mesh_cells * mesh_cells * mesh_cells;
   R* dg = (R*)io.grid.ensure(cells * sizeof(R));
-  const size_t mesh_scratch = mesh_scratch_bytes(n, mesh_cells) * sizeof(R) / sizeof(float);
-  if constexpr (sizeof(R) == 4) {
-    e->scratch.ensure(std::max(cic_scratch_bytes(n, n_grid), mesh_scratch));
-    cic_deposit(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic);
-  } else {
-    e->scratch.ensure(std::max(cic_f64_scratch_bytes(n_grid), mesh_scratch));
-    cic_deposit_f64(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic);
-  }
-  // The mesh is built on the copy stream (its own scan scratch) while the
-  // contrast is taken and the first rungs are smoothed; the run waits for it
-  // before its first sphere growth.
+  // The box check (sif__field_check_in_box) is counted on the device and read
+  // when the run ends, not waited for: every stage indexes safely whatever
+  // the positions, and a run over positions outside the box returns the
+  // range error and no catalogue.
+  unsigned long long* outside = (unsigned long long*)io.flag.ensure(16);
+  SIFG_CUDA(cudaMemsetAsync(outside, 0, 16, s));
+  R bounds[2];
+  box_bounds(box, &bounds[0], &bounds[1]);
+  // The mesh is built on the copy stream with its own scratch, beside the
+  // deposit proper (bound by shared-memory atomics, not by HBM: it starts
+  // once the deposit's tile sort has streamed the particles) and the first
+  // smoothings; the run waits for it before its first sphere growth.
   cudaStream_t cs = e->copy_stream();
-  SIFG_CUDA(cudaEventRecord(e->ev_copy_start(), s));
-  SIFG_CUDA(cudaStreamWaitEvent(cs, e->ev_copy_start(), 0));
   struct CopyDrain {
     cudaStream_t s;
     ~CopyDrain() { cudaStreamSynchronize(s); }
   } drain{cs};
+  io.mesh_scratch.ensure(mesh_scratch_bytes(n, mesh_cells) * sizeof(R) / sizeof(float));
+  if constexpr (sizeof(R) == 4) {
+    e->scratch.ensure(cic_scratch_bytes(n, n_grid));
+    cic_deposit(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic, bounds, outside,
+                e->ev_copy_start());
+  } else {
+    box_check_kernel<R><<<grid_for(n, 256), 256, 0, s>>>(x, y, z, n, bounds[0], bounds[1], outside);
+    SIFG_LAUNCH_CHECK();
+    SIFG_CUDA(cudaEventRecord(e->ev_copy_start(), s));
+    e->scratch.ensure(cic_f64_scratch_bytes(n_grid));
+    cic_deposit_f64(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic);
+  }
+  SIFG_CUDA(cudaStreamWaitEvent(cs, e->ev_copy_start(), 0));
   DeviceMeshT<R> m;
   m.n_cells = mesh_cells;
   m.box_length = box;
@@ -974,12 +984,21 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
   m.orig = nullptr;
   uint32_t* sums = (uint32_t*)io.mesh_sums.ensure(
       (size_t)scan_sums_needed((uint32_t)(mcells + 1)) * sizeof(uint32_t));
-  mesh_build(x, y, z, n, m, e->scratch.ptr, cs, &tm.mesh, sums);
+  mesh_build(x, y, z, n, m, io.mesh_scratch.ptr, cs, &tm.mesh, sums);
   SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
   double* cscratch = (double*)io.mean.ensure(density_contrast_scratch_bytes() + 64);
   density_contrast(dg, cells, cscratch, s);
-  st = run_device(e, dg, n_grid, box, m, radii, n_radii, threshold, overlap, opt, (const R*)nullptr,
-                  cx, cy, cz, r, capacity, n_voids, tm, e->ev_mesh_ready(), stats);
+  int st = run_device(e, dg, n_grid, box, m, radii, n_radii, threshold, overlap, opt,
+                      (const R*)nullptr, cx, cy, cz, r, capacity, n_voids, tm, e->ev_mesh_ready(),
+                      stats);
+  unsigned long long h_outside = 0;
+  SIFG_CUDA(cudaMemcpyAsync(&h_outside, outside, sizeof(h_outside), cudaMemcpyDeviceToHost, s));
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  if (h_outside) {
+    *n_voids = 0;
+    return fail(SIF_ERR_RANGE, fmt("field: %llu of %llu particles outside the box [0, %g)",
+                                   h_outside, (unsigned long long)n, (double)box));
+  }
   return st;
 }
 

@@ -63,7 +63,9 @@ __device__ __forceinline__ void cic_axis(float v, const CicGeom& g, uint32_t& ce
   int32_t c = (int32_t)r;
   if (c < 0) c += (int32_t)g.n;
   if (c >= (int32_t)g.n) c -= (int32_t)g.n;
-  cell = (uint32_t)c;
+  // In range for every position in the box; the clamp only keeps a position
+  // far outside it (which the box check reports) from indexing past the grid.
+  cell = min((uint32_t)c, g.n - 1);
   t = f;
 }
 
@@ -76,17 +78,30 @@ __device__ __forceinline__ uint32_t tile_of(float x, float y, float z, const Cic
   return ((cx / TB) * g.nt + cy / TB) * g.nt + cz / TB;
 }
 
+// With `outside` set, also counts the particles outside [lo, hi] on any axis
+// (NaN included): the box check, from the same reads.
 __global__ void tile_count_kernel(const float* __restrict__ x, const float* __restrict__ y,
                                   const float* __restrict__ z, uint64_t n, CicGeom g,
-                                  uint32_t* __restrict__ counts) {
+                                  uint32_t* __restrict__ counts, float lo, float hi,
+                                  unsigned long long* __restrict__ outside) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  unsigned long long bad = 0;
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
     const uint64_t p = base + threadIdx.x;
     const bool valid = p < n;
-    const uint32_t tile = valid ? tile_of(x[p], y[p], z[p], g) : 0xffffffffu;
+    uint32_t tile = 0xffffffffu;
+    if (valid) {
+      const float px = x[p], py = y[p], pz = z[p];
+      tile = tile_of(px, py, pz, g);
+      bad += (px >= lo && px <= hi && py >= lo && py <= hi && pz >= lo && pz <= hi) ? 0u : 1u;
+    }
     const unsigned peers = __match_any_sync(0xffffffffu, tile);
     if (valid && (threadIdx.x & 31u) == (unsigned)(__ffs(peers) - 1))
       atomicAdd(counts + tile, (uint32_t)__popc(peers));
+  }
+  if (outside) {
+    for (int d = 16; d > 0; d >>= 1) bad += __shfl_down_sync(0xffffffffu, bad, d);
+    if ((threadIdx.x & 31u) == 0 && bad) atomicAdd(outside, bad);
   }
 }
 
@@ -414,7 +429,8 @@ size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n) {
 
 void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_particles,
                  uint32_t n, float box, float* grid, void* scratch, cudaStream_t st,
-                 KernelTimer* timer) {
+                 KernelTimer* timer, const float* bounds, unsigned long long* outside,
+                 cudaEvent_t sorted) {
   const CicGeom g = make_geom(n, box);
   const uint64_t nt = g.nt, tiles = nt * nt * nt;
   char* p = (char*)scratch;
@@ -440,13 +456,16 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   SIFG_CUDA(cudaMemsetAsync(faces.fz, 0, face_elems * 8, st));
   const unsigned blk = 256;
   const unsigned grd = grid_for(n_particles, blk, 152u * 16u);
-  tile_count_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, counts);
+  tile_count_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, counts,
+                                         bounds ? bounds[0] : 0.f, bounds ? bounds[1] : 0.f,
+                                         bounds ? outside : nullptr);
   SIFG_LAUNCH_CHECK();
   exclusive_scan_u32(counts, (uint32_t)(tiles + 1), st);
   SIFG_CUDA(cudaMemcpyAsync(cursor, counts, (tiles + 1) * sizeof(uint32_t),
                             cudaMemcpyDeviceToDevice, st));
   tile_scatter_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, cursor, sx, sy, sz);
   SIFG_LAUNCH_CHECK();
+  if (sorted) SIFG_CUDA(cudaEventRecord(sorted, st));
   const float cl = box / (float)n;
   const float inv_cell_vol = 1.0f / (float)(cl * cl * cl);
   const size_t smem = (size_t)2 * TS * TS * TS * sizeof(uint32_t);

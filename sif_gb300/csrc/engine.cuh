@@ -67,6 +67,7 @@ using HostCatalogue = HostCatalogueT<float>;
 // Device buffers of one engine's box path (grid, mesh, flags).
 struct BoxBufs {
   DevBuf grid, mx, my, mz, offs, mesh_sums, flag, mean;
+  DevBuf mesh_scratch;  // the mesh build's own, so that it runs beside the deposit
 };
 
 class Engine {

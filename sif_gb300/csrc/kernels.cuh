@@ -54,9 +54,14 @@ void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st,
 
 // --- cic.cu ---
 size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n);
+// bounds (lo, hi) and outside, when given: the deposit also adds to
+// *outside the particles outside [lo, hi] (the box check from its own reads).
+// sorted, when given, is recorded once the particles are in tile order: what
+// follows (the deposit proper) is bound by shared-memory atomics, not by HBM.
 void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_particles,
                  uint32_t n, float box, float* grid, void* scratch, cudaStream_t st,
-                 KernelTimer* timer);
+                 KernelTimer* timer, const float* bounds = nullptr,
+                 unsigned long long* outside = nullptr, cudaEvent_t sorted = nullptr);
 // The FP64 form's deposit: scratch is cic_f64_scratch_bytes(n).
 size_t cic_f64_scratch_bytes(uint32_t n);
 void cic_deposit_f64(const double* x, const double* y, const double* z, uint64_t n_particles,
