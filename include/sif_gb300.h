@@ -445,6 +445,10 @@ void sifg_set_window(int bins);
 /* Which sphere-growth kernel runs: 0 (default) by the survivor count, 1 a
  * CTA per survivor, 2 a warp per survivor. The radii do not depend on it. */
 void sifg_set_growth_mode(int mode);
+/* How the commit's rounds run: 0 (default) all in one cooperative launch
+ * where the device allows it, 1 a kernel launch per round. The catalogue
+ * does not depend on it. */
+void sifg_set_commit_mode(int mode);
 /* The chain-mesh build of sifg_mesh_device, for callers that cannot let the
  * library allocate device memory: a process whose framework reserves the
  * GPU's memory in its own pool, a latency-bound pipeline that cannot afford

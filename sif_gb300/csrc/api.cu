@@ -1307,6 +1307,7 @@ uint64_t sifg_stream(void) {
 }
 
 void sifg_set_growth_mode(int mode) { set_growth_mode(mode < 0 || mode > 2 ? 0 : mode); }
+void sifg_set_commit_mode(int mode) { set_commit_mode(mode == 1 ? 1 : 0); }
 
 void sifg_set_window(int bins) { g_window = bins < 1 ? 1 : (bins > 64 ? 64 : bins); }
 

@@ -124,8 +124,10 @@ __device__ __forceinline__ bool mask_get(const uint32_t* m, uint64_t i) {
 // The mask is also read with plain loads by kernels that run after writers
 // in the same stream; __ldg is only used where the mask is read-only for the
 // whole kernel.
+// Read past L1: the mask is written (atomicOr) while kernels that read it
+// run, by other SMs within one cooperative launch.
 __device__ __forceinline__ bool mask_get_rw(const uint32_t* m, uint64_t i) {
-  return (m[i >> 5] >> (i & 31)) & 1u;
+  return (__ldcg(m + (i >> 5)) >> (i & 31)) & 1u;
 }
 
 }  // namespace sifg

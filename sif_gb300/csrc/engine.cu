@@ -710,22 +710,41 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     uint32_t* acc = grow_to<uint32_t>(acc_, m);
     SIFG_CUDA(cudaMemsetAsync(counters, 0, kCommitCounters * sizeof(uint32_t), st_));
     commit_init(sv, sa, counters, m, st_);
-    // Rounds are issued a few at a time between reads of the undecided
-    // count: a round after the last one decides nothing and paints nothing.
+    // The rounds run in one cooperative launch, to the round that leaves no
+    // survivor undecided (or a ring's worth, then another launch); where
+    // the device cannot, a few rounds are issued at a time between reads of
+    // the undecided count (a round after the last one decides nothing and
+    // paints nothing).
     uint64_t rounds = 0;
     uint32_t* h_count = h_counters_ + kCommitCounters;
+    uint32_t* h_bar = h_count + 1;  // the cooperative launch's report: bar[2] error, bar[3] rounds
+    unsigned* bar = grow_to<unsigned>(commit_bar_, 4);
     for (uint32_t batch = 3;; batch = 4) {
       SIFG_CUDA(cudaMemsetAsync(counters + kRoundUndecided, 0, kRoundRing * sizeof(uint32_t), st_));
-      for (uint32_t b = 0; b < batch; b++) {
-        commit_round(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters, (uint32_t)rounds, m, st_);
-        paint_new(sv, acc, counters, (uint32_t)rounds, mask, rc, m, st_);
-        std::swap(sa, sb);
-        rounds++;
+      const bool one_launch = commit_rounds(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters,
+                                            (uint32_t)rounds, kRoundRing, bar, st_);
+      if (one_launch) {
+        SIFG_CUDA(cudaMemcpyAsync(h_bar, bar, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, st_));
+      } else {
+        for (uint32_t b = 0; b < batch; b++) {
+          commit_round(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters, (uint32_t)rounds, m, st_);
+          paint_new(sv, acc, counters, (uint32_t)rounds, mask, rc, m, st_);
+          std::swap(sa, sb);
+          rounds++;
+        }
       }
       SIFG_CUDA(cudaMemcpyAsync(h_counters_, counters, kCommitCounters * sizeof(uint32_t),
                                 cudaMemcpyDeviceToHost, st_));
       SIFG_CUDA(cudaMemcpyAsync(h_count, dcount + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
       SIFG_CUDA(cudaStreamSynchronize(st_));
+      if (one_launch) {
+        if (h_bar[2] || h_bar[3] == 0) {
+          set_error(kErrInvalid, "commit: a grid barrier of the cooperative commit timed out");
+          return kErrInvalid;
+        }
+        if (h_bar[3] & 1u) std::swap(sa, sb);
+        rounds += h_bar[3];
+      }
       if (h_counters_[kRoundUndecided + (rounds - 1) % kRoundRing] == 0) break;
       if (rounds > (uint64_t)m + 8) {
         set_error(kErrInvalid, "commit: no progress");

@@ -101,6 +101,7 @@ class Engine {
   cudaStream_t st_ = 0;
   DevBuf field_[2], mask_, cand_delta_, cand_flat_, blocks_, rank_, rank_slots_, alive_;
   DevBuf surv_cand_, surv_flat_, scx_, scy_, scz_, sr_, sreason_, state_a_, state_b_, acc_;
+  DevBuf commit_bar_;  // the cooperative commit's grid barrier and its report
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
   DevBuf tpl_, gbuf_, traffic_, region_delta_, region_flat_;

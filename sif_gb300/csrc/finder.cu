@@ -1273,17 +1273,21 @@ __device__ __forceinline__ bool interacts(R ax, R ay, R az, R ar, R bx,
   return dx * dx + dy * dy + dz * dz < reach * reach;
 }
 
+// One round of the commit over every survivor: state st_in -> st_out. The
+// states, the acceptance list, the counters and the mask are read past L1
+// (__ldcg): the persistent form runs rounds in one kernel, where another SM
+// wrote them since the last barrier.
 template <class R>
-__global__ void commit_round_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ rank,
-                                    SurvivorGridT<R> g, VoidViewT<R> voids, const uint32_t* __restrict__ mask,
-                                    RungConstsT<R> rc, const uint8_t* __restrict__ st_in,
-                                    uint8_t* __restrict__ st_out, uint32_t* __restrict__ acc,
-                                    uint32_t* __restrict__ counters, uint32_t slot) {
+__device__ __forceinline__ void commit_pass(const SurvivorsT<R>& sv, const uint32_t* __restrict__ rank,
+                                            const SurvivorGridT<R>& g, const VoidViewT<R>& voids,
+                                            const uint32_t* mask, const RungConstsT<R>& rc,
+                                            const uint8_t* st_in, uint8_t* st_out, uint32_t* acc,
+                                            uint32_t* counters, uint32_t slot) {
   const uint32_t n = *sv.count;
   const uint32_t nn = rc.grid_n;
   const R half = fmul(rc.box, R(0.5f));
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint8_t s0 = st_in[i];
+    const uint8_t s0 = __ldcg(st_in + i);
     if (s0 != kUndecided) {
       st_out[i] = s0;
       continue;
@@ -1318,7 +1322,7 @@ __global__ void commit_round_kernel(SurvivorsT<R> sv, const uint32_t* __restrict
             for (uint32_t k = g.start[c]; k < e; k++) {
               const uint32_t j = g.ids[k];
               if (j == i) continue;
-              const uint8_t sj = st_in[j];
+              const uint8_t sj = __ldcg(st_in + j);
               if (sj == kRejected) continue;
               const R jx = sv.cx[j], jy = sv.cy[j], jz = sv.cz[j], rj = sv.r[j];
               if (sj == kAccepted) {
@@ -1350,6 +1354,14 @@ __global__ void commit_round_kernel(SurvivorsT<R> sv, const uint32_t* __restrict
     }
     st_out[i] = out;
   }
+}
+
+template <class R>
+__global__ void commit_round_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ rank,
+                                    SurvivorGridT<R> g, VoidViewT<R> voids, const uint32_t* mask,
+                                    RungConstsT<R> rc, const uint8_t* st_in, uint8_t* st_out,
+                                    uint32_t* acc, uint32_t* counters, uint32_t slot) {
+  commit_pass(sv, rank, g, voids, mask, rc, st_in, st_out, acc, counters, slot);
 }
 
 template <class R>
@@ -1387,17 +1399,17 @@ void commit_round(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Voi
 // every node whose centre lies within scale * r, measured as the reference
 // measures it.
 template <class R>
-__global__ void paint_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ acc,
-                             uint32_t* __restrict__ counters, uint32_t slot,
-                             uint32_t* __restrict__ mask, RungConstsT<R> rc) {
-  const uint32_t lo = counters[kRoundBegin + slot], hi = counters[0];
+__device__ __forceinline__ void paint_pass(const SurvivorsT<R>& sv, const uint32_t* acc,
+                                           uint32_t* counters, uint32_t slot, uint32_t* mask,
+                                           const RungConstsT<R>& rc) {
+  const uint32_t lo = __ldcg(counters + kRoundBegin + slot), hi = __ldcg(counters);
   // No round accepts while a paint runs: hi is where the next round begins.
   if (blockIdx.x == 0 && threadIdx.x == 0) counters[kRoundBegin + (slot + 1) % kRoundRing] = hi;
   const unsigned lane = threadIdx.x & 31u;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   const uint32_t n = rc.grid_n;
   for (uint32_t a = lo + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); a < hi; a += warps) {
-    const uint32_t i = acc[a];
+    const uint32_t i = __ldcg(acc + a);
     const R cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i];
     const R rt = fmul(rc.scale, sv.r[i]);
     const R r2 = fmul(rt, rt);
@@ -1430,12 +1442,109 @@ __global__ void paint_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ acc,
   }
 }
 
+// paint_sphere with set = 1 (src/finder/utils.c:965-1027), one warp per void:
+// every node whose centre lies within scale * r, measured as the reference
+// measures it.
+template <class R>
+__global__ void paint_kernel(SurvivorsT<R> sv, const uint32_t* acc, uint32_t* counters,
+                             uint32_t slot, uint32_t* mask, RungConstsT<R> rc) {
+  paint_pass(sv, acc, counters, slot, mask, rc);
+}
+
 template <class R>
 void paint_new(SurvivorsT<R> s, const uint32_t* acc, uint32_t* counters, uint32_t round,
                uint32_t* mask, RungConstsT<R> rc, uint32_t max_survivors, cudaStream_t st) {
   const uint32_t warps = max_survivors < 152u * 16u ? (max_survivors ? max_survivors : 1) : 152u * 16u;
   paint_kernel<<<(warps + 3) / 4, 128, 0, st>>>(s, acc, counters, round % kRoundRing, mask, rc);
   SIFG_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// The commit's rounds in one cooperative launch
+// ---------------------------------------------------------------------------
+
+// A grid-wide barrier for a cooperative launch (every block resident):
+// bar[0] counts arrivals, bar[1] is the generation, bar[2] the error flag.
+// A wait that outlasts kBarrierSpins naps (about a second) sets the flag; a
+// block that sees it returns false and the kernel ends.
+constexpr unsigned kBarrierSpins = 1u << 22;
+constexpr int kCommitT = 256;
+__device__ __forceinline__ bool grid_barrier(unsigned* bar) {
+  __shared__ bool ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = true;
+    volatile unsigned* vgen = bar + 1;
+    const unsigned gen = *vgen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned spins = 0;
+      while (*vgen == gen) {
+        if (++spins > kBarrierSpins) {
+          atomicExch(bar + 2, 1u);
+          break;
+        }
+        __nanosleep(256);
+      }
+    }
+    __threadfence();
+    if (*(volatile unsigned*)(bar + 2)) ok = false;
+  }
+  __syncthreads();
+  return ok;
+}
+
+// Rounds round0, round0 + 1, ... until one leaves no survivor undecided or
+// max_rounds have run: each a commit pass, a barrier, the paint of what it
+// accepted, a barrier. Round k reads the states from sa (k even) or sb and
+// writes the other. bar[3]: the rounds run.
+template <class R>
+__global__ void __launch_bounds__(kCommitT) commit_loop_kernel(
+    SurvivorsT<R> sv, const uint32_t* __restrict__ rank, SurvivorGridT<R> g, VoidViewT<R> voids,
+    uint32_t* mask, RungConstsT<R> rc, uint8_t* sa, uint8_t* sb, uint32_t* acc, uint32_t* counters,
+    uint32_t round0, uint32_t max_rounds, unsigned* bar) {
+  for (uint32_t k = 0; k < max_rounds; k++) {
+    const uint32_t slot = (round0 + k) % kRoundRing;
+    commit_pass(sv, rank, g, voids, mask, rc, (k & 1) ? sb : sa, (k & 1) ? sa : sb, acc, counters,
+                slot);
+    if (!grid_barrier(bar)) return;
+    paint_pass(sv, acc, counters, slot, mask, rc);
+    if (!grid_barrier(bar)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) bar[3] = k + 1;
+    if (__ldcg(counters + kRoundUndecided + slot) == 0) return;
+  }
+}
+
+static int g_commit_mode = 0;
+void set_commit_mode(int mode) { g_commit_mode = mode; }
+
+template <class R>
+bool commit_rounds(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, VoidViewT<R> voids,
+                   uint32_t* mask, RungConstsT<R> rc, uint8_t* sa, uint8_t* sb, uint32_t* acc,
+                   uint32_t* counters, uint32_t round0, uint32_t max_rounds, unsigned* bar,
+                   cudaStream_t st) {
+  if (g_commit_mode != 0) return false;
+  thread_local int blocks = -1;  // co-resident blocks of the device, found once per thread
+  if (blocks < 0) {
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    SIFG_CUDA(cudaGetDevice(&dev));
+    SIFG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SIFG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    SIFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, commit_loop_kernel<R>, kCommitT, 0));
+    blocks = coop && per_sm > 0 ? sms : 0;  // one block per SM
+  }
+  if (blocks == 0) return false;
+  SIFG_CUDA(cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned), st));
+  void* args[] = {&s, (void*)&rank, &g, &voids, &mask, &rc, &sa, &sb, &acc, &counters, &round0,
+                  &max_rounds, &bar};
+  SIFG_CUDA(cudaLaunchCooperativeKernel((const void*)commit_loop_kernel<R>, dim3(blocks),
+                                        dim3(kCommitT), args, 0, st));
+  SIFG_LAUNCH_CHECK();
+  return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -1550,6 +1659,9 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
                                 uint32_t*, uint32_t*, uint32_t, uint32_t, cudaStream_t);           \
   template void paint_new<R>(SurvivorsT<R>, const uint32_t*, uint32_t*, uint32_t, uint32_t*,       \
                              RungConstsT<R>, uint32_t, cudaStream_t);                              \
+  template bool commit_rounds<R>(SurvivorsT<R>, const uint32_t*, SurvivorGridT<R>, VoidViewT<R>,   \
+                                 uint32_t*, RungConstsT<R>, uint8_t*, uint8_t*, uint32_t*,         \
+                                 uint32_t*, uint32_t, uint32_t, unsigned*, cudaStream_t);          \
   template void append_accepted<R>(SurvivorsT<R>, const uint32_t*, const uint32_t*,                \
                                    const uint32_t*, uint32_t, uint32_t*, R*, R*, R*, R*, uint32_t, \
                                    uint32_t, cudaStream_t);                                        \

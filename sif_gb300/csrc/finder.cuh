@@ -195,6 +195,23 @@ void commit_round(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Voi
                   const uint32_t* mask, RungConstsT<R> rc, const uint8_t* state_in,
                   uint8_t* state_out, uint32_t* acc, uint32_t* counters, uint32_t round,
                   uint32_t max_survivors, cudaStream_t st);
+// The rounds from `round0` on in one cooperative launch, until a round leaves
+// no survivor undecided or max_rounds (at most kRoundRing) have run; round k
+// reads states from sa (k even) or sb and writes the other. bar: four
+// words, reset by the call; bar[3] ends up holding the rounds run and
+// bar[2] is set if a grid barrier timed out. Returns false, launching
+// nothing, where the device cannot run it (or set_commit_mode(1) asked for
+// a kernel launch per round): the caller then runs commit_round and
+// paint_new per round.
+template <class R>
+bool commit_rounds(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, VoidViewT<R> voids,
+                   uint32_t* mask, RungConstsT<R> rc, uint8_t* sa, uint8_t* sb, uint32_t* acc,
+                   uint32_t* counters, uint32_t round0, uint32_t max_rounds, unsigned* bar,
+                   cudaStream_t st);
+// 0 (default): the commit's rounds in one cooperative launch where the device
+// allows it; 1: a launch per round. The catalogue does not depend on it.
+void set_commit_mode(int mode);
+
 // Paints the voids round `round` accepted and records where the next round's
 // acceptances begin.
 template <class R>

@@ -164,6 +164,11 @@ def set_growth_mode(mode):
     _lib.load().sifg_set_growth_mode(int(mode))
 
 
+def set_commit_mode(mode):
+    """0 the commit's rounds in one cooperative launch, 1 a launch per round."""
+    _lib.load().sifg_set_commit_mode(int(mode))
+
+
 def set_window(bins):
     _lib.load().sifg_set_window(int(bins))
 

@@ -203,6 +203,20 @@ def test_catalogue_matches_reference_golden_either_growth_kernel(dev, golden_box
     test_catalogue_matches_reference_golden(dev, golden_box32, name)
 
 
+@pytest.fixture(params=[0, 1], ids=["one_launch", "launch_per_round"])
+def commit_mode(request, dev):
+    """The commit's rounds in one cooperative launch, then a launch per round."""
+    dev.set_commit_mode(request.param)
+    yield request.param
+    dev.set_commit_mode(0)
+
+
+@pytest.mark.parametrize("name", ["default", "lagrangian", "minima", "overlap_0_5"])
+def test_catalogue_matches_reference_golden_either_commit_form(dev, golden_box32, commit_mode,
+                                                               name):
+    test_catalogue_matches_reference_golden(dev, golden_box32, name)
+
+
 @pytest.mark.parametrize("window", [1, 5, 64])
 def test_catalogue_independent_of_resolve_window(dev, golden_box32, window):
     g = golden_box32
@@ -250,7 +264,7 @@ def test_catalogue_matches_oracle_on_shared_fields(dev, oracle, case):
     # The GPU's own run (smoothing inside the finder) is the same run.
     own = dev.exodus(grid, ng, box, mesh, nm, radii, thr, ov, opt)
     assert same_catalogue(own, want)
-    # And so is each sphere-growth kernel forced.
+    # And so is each sphere-growth kernel forced, and the commit a launch per round.
     for mode in (1, 2):
         dev.set_growth_mode(mode)
         try:
@@ -258,6 +272,12 @@ def test_catalogue_matches_oracle_on_shared_fields(dev, oracle, case):
         finally:
             dev.set_growth_mode(0)
         assert same_catalogue(forced, want), mode
+    dev.set_commit_mode(1)
+    try:
+        per_round = dev.exodus(grid, ng, box, mesh, nm, radii, thr, ov, opt, inject=fields.reshape(-1))
+    finally:
+        dev.set_commit_mode(0)
+    assert same_catalogue(per_round, want)
 
 
 def test_four_holes_and_brute_force_radii(gpu_lib, oracle):
