@@ -345,26 +345,42 @@ __device__ __forceinline__ void ifft512_column(float2* col, const float2* __rest
   __syncwarp();
 }
 
-// Passes (1) and (2). Line `blockIdx.y` starts at line * line_stride; its
-// element a of column kz at a * elem_stride + kz. The tile arrives by
-// asynchronous copies; pass (1) (lut set) scales each mode by its filter
-// factor as the transform first reads it (line = ky); pass (2) works in
+// The work buffer between the passes holds the half spectrum in tiles of 16
+// kz columns by 512: tile (x, kb) holds kz = 16 kb .. 16 kb + 15 for every
+// ky, at ((x * kKzBlocks + kb) * 512 + ky) * 16 + kz % 16. Pass (2) reads
+// and writes each tile as one contiguous 64 KB block, pass (3) reads each
+// row's modes as 16-row, 2 KB blocks. kz past 256 are never written or read.
+constexpr uint32_t kKzBlocks = 17;
+constexpr size_t kTileWorkElems = (size_t)512 * kKzBlocks * 512 * 16;
+
+// Where passes (1) and (2) find their columns: line `blockIdx.y`, kz block
+// `blockIdx.x`; element a of the block's column c at
+// line * line + kb * kblock + a * elem + c.
+struct ColumnLayout {
+  uint32_t line, kblock, elem;
+};
+
+// Passes (1) and (2): the inverse FFT along one axis of 16 neighbouring kz
+// columns of one line. The tile arrives by asynchronous copies; pass (1)
+// (lut set) reads the spectrum (line = ky, kx along the column), scales each
+// mode by its filter factor as the transform first reads it, and writes the
+// tiles; pass (2) (line = x, ky along the column) works on the tiles in
 // place. Columns past kz = 256 (in the last CTA of a line) are neither read,
 // transformed nor written.
 __global__ void __launch_bounds__(32 * kColWarps, 3)
-    colfft512_kernel(const float2* src, float2* dst, uint32_t line_stride, uint32_t elem_stride,
+    colfft512_kernel(const float2* src, float2* dst, ColumnLayout in, ColumnLayout out,
                      const float* __restrict__ lut, const float* __restrict__ win, float norm,
                      const float2* __restrict__ tw) {
   extern __shared__ float2 cols[];  // kColCols columns of kColStride slots
   constexpr uint32_t zd = 257;
   constexpr uint32_t kRowStep = 32 * kColWarps / kColCols;  // rows a pass of the CTA covers
-  const uint32_t kz0 = blockIdx.x * kColCols, line = blockIdx.y;
+  const uint32_t kb = blockIdx.x, kz0 = kb * kColCols, line = blockIdx.y;
   const uint32_t c = threadIdx.x % kColCols, row0 = threadIdx.x / kColCols;
   const bool live = kz0 + c < zd;
-  const size_t base = (size_t)line * line_stride + kz0 + c;
   if (live) {
-    const float2* p = src + base + (size_t)row0 * elem_stride;
-    const size_t step = (size_t)kRowStep * elem_stride;
+    const float2* p = src + (size_t)line * in.line + (size_t)kb * in.kblock + c +
+                      (size_t)row0 * in.elem;
+    const size_t step = (size_t)kRowStep * in.elem;
 #pragma unroll 8
     for (uint32_t i = 0; i < 512 / kRowStep; i++, p += step)
       cp_async8(cols + c * kColStride + col_slot((int)(row0 + kRowStep * i)), p);
@@ -385,8 +401,9 @@ __global__ void __launch_bounds__(32 * kColWarps, 3)
   }
   __syncthreads();
   if (live) {
-    float2* p = dst + base + (size_t)row0 * elem_stride;
-    const size_t step = (size_t)kRowStep * elem_stride;
+    float2* p = dst + (size_t)line * out.line + (size_t)kb * out.kblock + c +
+                (size_t)row0 * out.elem;
+    const size_t step = (size_t)kRowStep * out.elem;
 #pragma unroll 8
     for (uint32_t i = 0; i < 512 / kRowStep; i++, p += step)
       *p = cols[c * kColStride + col_slot((int)(row0 + kRowStep * i))];
@@ -397,24 +414,33 @@ __global__ void __launch_bounds__(32 * kColWarps, 3)
 // row's modes (the imaginary parts of Z[0] and Z[256] taken as zero, as a
 // C2R does), c[k] = Fe[k] + i Fo[k] for k < 256, Fe = Z[k] + conj Z[256-k],
 // Fo = (Z[k] - conj Z[256-k]) W512^k, and its 256-point inverse DFT y gives
-// the real samples x[2m] = Re y[m], x[2m+1] = Im y[m]. The CTA's rows are one
-// contiguous, 16-byte aligned block, copied in whole by asynchronous copies;
-// the stage exchange swizzles slots (k1, j) -> 16 k1 + (j ^ k1) within the
-// row's own 257 slots.
+// the real samples x[2m] = Re y[m], x[2m+1] = Im y[m]. The CTA's 16 rows
+// (x, y0 .. y0 + 15) come from the tiles in 16 contiguous 2 KB blocks (kz <
+// 256, by 16-byte asynchronous copies) and one mode each for kz = 256; a row
+// has kRowSlots slots in shared memory (even, for the 16-byte copies); the
+// stage exchange swizzles slots (k1, j) -> 16 k1 + (j ^ k1) within the row.
 constexpr int kRowsPerCta = 16;
+constexpr uint32_t kRowSlots = 258;
 __global__ void __launch_bounds__(16 * kRowsPerCta)
-    c2r512_rows_kernel(const float2* __restrict__ spec, float* __restrict__ out,
+    c2r512_rows_kernel(const float2* __restrict__ work, float* __restrict__ out,
                        const float2* __restrict__ tw) {
-  constexpr uint32_t zd = 257;
-  __shared__ __align__(16) float2 buf[kRowsPerCta * zd];
-  const size_t row0 = (size_t)blockIdx.x * kRowsPerCta;
-  const float4* src = reinterpret_cast<const float4*>(spec + row0 * zd);
-  for (uint32_t f = threadIdx.x; f < kRowsPerCta * zd / 2; f += blockDim.x)
-    cp_async16(buf + 2 * f, src + f);
+  __shared__ __align__(16) float2 buf[kRowsPerCta * kRowSlots];
+  const uint32_t x = blockIdx.x / (512 / kRowsPerCta);
+  const uint32_t y0 = (blockIdx.x % (512 / kRowsPerCta)) * kRowsPerCta;
+  const float2* tiles = work + ((size_t)x * kKzBlocks * 512 + y0) * 16;  // kz block 0
+  constexpr size_t kBlock = (size_t)512 * 16;                            // one kz block further
+  for (uint32_t f = threadIdx.x; f < 16 * kRowsPerCta * 8; f += blockDim.x) {
+    const uint32_t kb = f / (kRowsPerCta * 8), e = f % (kRowsPerCta * 8);
+    const uint32_t r = e / 8, jj = e % 8;
+    cp_async16(buf + r * kRowSlots + 16 * kb + 2 * jj,
+               reinterpret_cast<const float4*>(tiles + kb * kBlock) + e);
+  }
+  if (threadIdx.x < kRowsPerCta)
+    cp_async8(buf + threadIdx.x * kRowSlots + 256, tiles + 16 * kBlock + threadIdx.x * 16);
   cp_async_wait_all();
   __syncthreads();
   const unsigned j = threadIdx.x & 15u;
-  float2* row = buf + (threadIdx.x >> 4) * zd;
+  float2* row = buf + (threadIdx.x >> 4) * kRowSlots;
   const float2* twb = tw + 512;
   const float2* wpre = tw + 768;
   float2 v[16];
@@ -441,9 +467,9 @@ __global__ void __launch_bounds__(16 * kRowsPerCta)
 #pragma unroll
   for (int k = 0; k < 16; k++) row[j + 16 * k] = v[k];
   __syncthreads();
-  float2* dst = reinterpret_cast<float2*>(out + row0 * 512);
+  float2* dst = reinterpret_cast<float2*>(out + ((size_t)x * 512 + y0) * 512);
   for (uint32_t f = threadIdx.x; f < kRowsPerCta * 256; f += blockDim.x)
-    dst[f] = buf[(f >> 8) * zd + (f & 255u)];
+    dst[f] = buf[(f >> 8) * kRowSlots + (f & 255u)];
 }
 
 static bool own_inverse(uint32_t n) { return n == 512; }
@@ -540,7 +566,7 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
   window_mode = window_mode_;
   const uint64_t modes = (uint64_t)n * n * (n / 2 + 1);
   spectrum.ensure(modes * 2 * sizeof(R));
-  work.ensure(modes * 2 * sizeof(R));
+  work.ensure(twiddles ? kTileWorkElems * sizeof(float2) : modes * 2 * sizeof(R));
   const uint32_t h = n >> 1;
   const uint32_t max_k2 = 3 * h * h;
   lut.ensure(((size_t)max_k2 + 1) * sizeof(R));
@@ -596,13 +622,18 @@ static void launch_inverse512(const SmootherT<float>& s, int filter, float norm,
     attr = true;
   }
   const float2* tw = (const float2*)s.twiddles;
-  const dim3 grid((zd + kColCols - 1) / kColCols, N);
+  const dim3 grid(kKzBlocks, N);
+  // The spectrum: (kx * N + ky) * zd + kz; the tiles: ((x * kKzBlocks + kb) * N + ky) * 16 + kz % 16.
+  const ColumnLayout spectrum{zd, kColCols, N * zd};
+  const ColumnLayout tiles_by_ky{kColCols, N * kColCols, kKzBlocks * N * kColCols};
+  const ColumnLayout tiles_by_x{kKzBlocks * N * kColCols, N * kColCols, kColCols};
   colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
-      s.spectrum.as<float2>(), s.work.as<float2>(), zd, N * zd, s.lut.as<float>(), w, norm, tw);
+      s.spectrum.as<float2>(), s.work.as<float2>(), spectrum, tiles_by_ky, s.lut.as<float>(), w,
+      norm, tw);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(s.stream);
   colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
-      s.work.as<float2>(), s.work.as<float2>(), N * zd, zd, nullptr, nullptr, 1.f, tw);
+      s.work.as<float2>(), s.work.as<float2>(), tiles_by_x, tiles_by_x, nullptr, nullptr, 1.f, tw);
   SIFG_LAUNCH_CHECK();
   c2r512_rows_kernel<<<N * N / kRowsPerCta, 16 * kRowsPerCta, 0, s.stream>>>(s.work.as<float2>(),
                                                                            out, tw);
