@@ -274,11 +274,17 @@ struct ColumnFilter {
 
 // One warp's inverse DFT of the 512 values in `col`, in place; with a filter
 // (f.lut set) each value is first scaled by its filter factor.
+// With `forward` the forward DFT instead (e^{-2 pi i jk/512}), as the
+// conjugate of the inverse DFT of the conjugate.
 __device__ __forceinline__ void ifft512_column(float2* col, const float2* __restrict__ tw,
-                                               unsigned lane, const ColumnFilter& f) {
+                                               unsigned lane, const ColumnFilter& f,
+                                               bool forward) {
   float2 v[16];
 #pragma unroll
-  for (int r = 0; r < 16; r++) v[r] = col[col_slot((int)lane + 32 * r)];
+  for (int r = 0; r < 16; r++) {
+    v[r] = col[col_slot((int)lane + 32 * r)];
+    if (forward) v[r].y = -v[r].y;
+  }
   if (f.lut) {
     // The factor is even in kx (the window table is built from |k|): a lane
     // reads it for its kx < 256 and takes kx > 256 from the lane holding
@@ -339,8 +345,8 @@ __device__ __forceinline__ void ifft512_column(float2* col, const float2* __rest
 #pragma unroll
   for (int i = 0; i < 8; i++) {
     const int x = (int)k1 + 16 * (8 * (int)q + i);
-    col[col_slot(x)] = v[i];
-    col[col_slot(x + 256)] = v[8 + i];
+    col[col_slot(x)] = forward ? make_float2(v[i].x, -v[i].y) : v[i];
+    col[col_slot(x + 256)] = forward ? make_float2(v[8 + i].x, -v[8 + i].y) : v[8 + i];
   }
   __syncwarp();
 }
@@ -370,7 +376,7 @@ struct ColumnLayout {
 __global__ void __launch_bounds__(32 * kColWarps, 3)
     colfft512_kernel(const float2* src, float2* dst, ColumnLayout in, ColumnLayout out,
                      const float* __restrict__ lut, const float* __restrict__ win, float norm,
-                     const float2* __restrict__ tw) {
+                     const float2* __restrict__ tw, bool forward) {
   extern __shared__ float2 cols[];  // kColCols columns of kColStride slots
   constexpr uint32_t zd = 257;
   constexpr uint32_t kRowStep = 32 * kColWarps / kColCols;  // rows a pass of the CTA covers
@@ -397,7 +403,7 @@ __global__ void __launch_bounds__(32 * kColWarps, 3)
       f = ColumnFilter{lut, win, norm, win ? __ldg(win + line) : 1.f, win ? __ldg(win + kz) : 1.f,
                        (uint32_t)(ks * ks) + kz * kz};
     }
-    ifft512_column(cols + w * kColStride, tw, lane, f);
+    ifft512_column(cols + w * kColStride, tw, lane, f, forward);
   }
   __syncthreads();
   if (live) {
@@ -470,6 +476,78 @@ __global__ void __launch_bounds__(16 * kRowsPerCta)
   float2* dst = reinterpret_cast<float2*>(out + ((size_t)x * 512 + y0) * 512);
   for (uint32_t f = threadIdx.x; f < kRowsPerCta * 256; f += blockDim.x)
     dst[f] = buf[(f >> 8) * kRowSlots + (f & 255u)];
+}
+
+// The forward transform's first pass, the R2C along z: 16 rows of 512 reals
+// per CTA (one contiguous 32 KB block), a half-warp per row. The row read
+// as 256 complex values c[m] = x[2m] + i x[2m+1] is transformed forward (the
+// conjugate of the inverse of the conjugate); then, with C[-k] taken mod 256,
+// E[k] = (C[k] + conj C[-k]) / 2, O[k] = (C[k] - conj C[-k]) / 2i and
+// X[k] = E[k] + W512^-k O[k] for k < 256, X[256] = E[0] - O[0]. The 257 modes
+// go to the tiles (16 rows by 16 kz, 2 KB blocks).
+__global__ void __launch_bounds__(16 * kRowsPerCta)
+    r2c512_rows_kernel(const float* __restrict__ grid, float2* __restrict__ work,
+                       const float2* __restrict__ tw) {
+  __shared__ __align__(16) float2 buf[kRowsPerCta * kRowSlots];
+  const uint32_t x = blockIdx.x / (512 / kRowsPerCta);
+  const uint32_t y0 = (blockIdx.x % (512 / kRowsPerCta)) * kRowsPerCta;
+  const float4* src = reinterpret_cast<const float4*>(grid + ((size_t)x * 512 + y0) * 512);
+  for (uint32_t f = threadIdx.x; f < kRowsPerCta * 128; f += blockDim.x)
+    cp_async16(buf + (f >> 7) * kRowSlots + 2 * (f & 127u), src + f);
+  cp_async_wait_all();
+  __syncthreads();
+  const unsigned j = threadIdx.x & 15u;
+  float2* row = buf + (threadIdx.x >> 4) * kRowSlots;
+  const float2* twb = tw + 512;
+  const float2* wpre = tw + 768;
+  float2 v[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    v[r] = row[j + 16u * r];
+    v[r].y = -v[r].y;
+  }
+  dft_inv(v);
+#pragma unroll
+  for (int k = 1; k < 16; k++) v[k] = cmul(v[k], __ldg(twb + k * 16 + j));
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 16; k++) row[16 * k + (j ^ k)] = v[k];
+  __syncwarp();
+#pragma unroll
+  for (int m = 0; m < 16; m++) v[m] = row[16 * j + (m ^ j)];
+  dft_inv(v);
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 16; k++) row[j + 16 * k] = make_float2(v[k].x, -v[k].y);  // C
+  __syncwarp();
+  float2 out[16];
+  float2 nyq = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    const unsigned k = j + 16u * r;
+    const float2 c = row[k], m = row[(256u - k) & 255u];
+    const float2 e = make_float2(0.5f * (c.x + m.x), 0.5f * (c.y - m.y));  // (C + conj C[-k]) / 2
+    const float2 d = make_float2(c.x - m.x, c.y + m.y);                    // C - conj C[-k]
+    const float2 o = make_float2(0.5f * d.y, -0.5f * d.x);                 // d / 2i
+    const float2 w = __ldg(wpre + k);
+    out[r] = cadd(e, cmul(o, make_float2(w.x, -w.y)));
+    if (r == 0 && j == 0) nyq = make_float2(e.x - o.x, e.y - o.y);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 16; r++) row[j + 16u * r] = out[r];
+  if (j == 0) row[256] = nyq;
+  __syncthreads();
+  float2* tiles = work + ((size_t)x * kKzBlocks * 512 + y0) * 16;
+  constexpr size_t kBlock = (size_t)512 * 16;
+  for (uint32_t f = threadIdx.x; f < 16 * kRowsPerCta * 8; f += blockDim.x) {
+    const uint32_t kb = f / (kRowsPerCta * 8), e = f % (kRowsPerCta * 8);
+    const uint32_t r = e / 8, jj = e % 8;
+    reinterpret_cast<float4*>(tiles + kb * kBlock)[e] =
+        *reinterpret_cast<const float4*>(buf + r * kRowSlots + 16 * kb + 2 * jj);
+  }
+  if (threadIdx.x < kRowsPerCta)
+    tiles[16 * kBlock + threadIdx.x * 16] = buf[threadIdx.x * kRowSlots + 256];
 }
 
 static bool own_inverse(uint32_t n) { return n == 512; }
@@ -565,7 +643,7 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
   box = box_;
   window_mode = window_mode_;
   const uint64_t modes = (uint64_t)n * n * (n / 2 + 1);
-  spectrum.ensure(modes * 2 * sizeof(R));
+  spectrum.ensure(twiddles ? kTileWorkElems * sizeof(float2) : modes * 2 * sizeof(R));
   work.ensure(twiddles ? kTileWorkElems * sizeof(float2) : modes * 2 * sizeof(R));
   const uint32_t h = n >> 1;
   const uint32_t max_k2 = 3 * h * h;
@@ -587,9 +665,14 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
   }
 }
 
+static void launch_forward512(const SmootherT<float>& s, const float* grid);
+
 template <>
 void SmootherT<float>::forward(const float* grid) {
-  SIFG_CUFFT(cufftExecR2C(plan_r2c, (cufftReal*)grid, (cufftComplex*)spectrum.ptr));
+  if (twiddles)
+    launch_forward512(*this, grid);
+  else
+    SIFG_CUFFT(cufftExecR2C(plan_r2c, (cufftReal*)grid, (cufftComplex*)spectrum.ptr));
 }
 template <>
 void SmootherT<double>::forward(const double* grid) {
@@ -609,31 +692,60 @@ static void launch_filter(const SmootherT<float>& s, int filter, float norm) {
 }
 
 // The three passes of the n = 512 inverse transform, on the smoother's stream.
-// The timer, begun by the caller, ends after pass (1): the filter's kernel.
-static void launch_inverse512(const SmootherT<float>& s, int filter, float norm, float* out,
-                              KernelTimer* timer) {
-  constexpr uint32_t N = 512, zd = 257;
-  const float* w = (s.window_mode && filter != kFilterNone) ? s.win.as<float>() : nullptr;
-  const size_t smem = (size_t)kColCols * kColStride * sizeof(float2);
+// Tiles ((u * kKzBlocks + kb) * N + v) * 16 + kz % 16 read as columns along v
+// with line u, or along u with line v. The forward leaves the spectrum as
+// tiles of line ky along kx; the inverse's pass (1) writes the work buffer as
+// tiles of line x along ky (read along x by nothing, along ky by pass (2)).
+constexpr ColumnLayout kTilesByLine{kKzBlocks * 512 * kColCols, 512 * kColCols, kColCols};
+constexpr ColumnLayout kTilesByRow{kColCols, 512 * kColCols, kKzBlocks * 512 * kColCols};
+
+static void set_column_smem() {
   thread_local bool attr = false;  // set once per thread
   if (!attr) {
     SIFG_CUDA(cudaFuncSetAttribute(colfft512_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
+                                   (int)(kColCols * kColStride * sizeof(float2))));
     attr = true;
   }
+}
+
+// The float form's forward transform at n = 512: the R2C along z into the
+// work tiles, the forward ky FFT in place, the forward kx FFT into the
+// spectrum's tiles.
+static void launch_forward512(const SmootherT<float>& s, const float* grid) {
+  constexpr uint32_t N = 512;
+  set_column_smem();
+  const size_t smem = (size_t)kColCols * kColStride * sizeof(float2);
+  const float2* tw = (const float2*)s.twiddles;
+  r2c512_rows_kernel<<<N * N / kRowsPerCta, 16 * kRowsPerCta, 0, s.stream>>>(
+      grid, s.work.as<float2>(), tw);
+  SIFG_LAUNCH_CHECK();
+  colfft512_kernel<<<dim3(kKzBlocks, N), 32 * kColWarps, smem, s.stream>>>(
+      s.work.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByLine, nullptr, nullptr, 1.f,
+      tw, true);
+  SIFG_LAUNCH_CHECK();
+  colfft512_kernel<<<dim3(kKzBlocks, N), 32 * kColWarps, smem, s.stream>>>(
+      s.work.as<float2>(), s.spectrum.as<float2>(), kTilesByRow, kTilesByLine, nullptr, nullptr,
+      1.f, tw, true);
+  SIFG_LAUNCH_CHECK();
+}
+
+// The timer, begun by the caller, ends after pass (1): the filter's kernel.
+static void launch_inverse512(const SmootherT<float>& s, int filter, float norm, float* out,
+                              KernelTimer* timer) {
+  constexpr uint32_t N = 512;
+  const float* w = (s.window_mode && filter != kFilterNone) ? s.win.as<float>() : nullptr;
+  const size_t smem = (size_t)kColCols * kColStride * sizeof(float2);
+  set_column_smem();
   const float2* tw = (const float2*)s.twiddles;
   const dim3 grid(kKzBlocks, N);
-  // The spectrum: (kx * N + ky) * zd + kz; the tiles: ((x * kKzBlocks + kb) * N + ky) * 16 + kz % 16.
-  const ColumnLayout spectrum{zd, kColCols, N * zd};
-  const ColumnLayout tiles_by_ky{kColCols, N * kColCols, kKzBlocks * N * kColCols};
-  const ColumnLayout tiles_by_x{kKzBlocks * N * kColCols, N * kColCols, kColCols};
   colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
-      s.spectrum.as<float2>(), s.work.as<float2>(), spectrum, tiles_by_ky, s.lut.as<float>(), w,
-      norm, tw);
+      s.spectrum.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByRow, s.lut.as<float>(), w,
+      norm, tw, false);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(s.stream);
   colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
-      s.work.as<float2>(), s.work.as<float2>(), tiles_by_x, tiles_by_x, nullptr, nullptr, 1.f, tw);
+      s.work.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByLine, nullptr, nullptr, 1.f,
+      tw, false);
   SIFG_LAUNCH_CHECK();
   c2r512_rows_kernel<<<N * N / kRowsPerCta, 16 * kRowsPerCta, 0, s.stream>>>(s.work.as<float2>(),
                                                                            out, tw);
