@@ -977,14 +977,20 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
   m.n_cells = mesh_cells;
   m.box_length = box;
   m.cell_length = box / (R)mesh_cells;
-  m.x = (R*)io.mx.ensure(n * sizeof(R));
-  m.y = (R*)io.my.ensure(n * sizeof(R));
-  m.z = (R*)io.mz.ensure(n * sizeof(R));
+  if constexpr (sizeof(R) == 4) {
+    m.xyzw = (float4*)io.mx.ensure(n * sizeof(float4));
+  } else {
+    m.x = (R*)io.mx.ensure(n * sizeof(R));
+    m.y = (R*)io.my.ensure(n * sizeof(R));
+    m.z = (R*)io.mz.ensure(n * sizeof(R));
+  }
   m.offsets = (uint32_t*)io.offs.ensure((mcells + 1) * 4);
   m.orig = nullptr;
   uint32_t* sums = (uint32_t*)io.mesh_sums.ensure(
       (size_t)scan_sums_needed((uint32_t)(mcells + 1)) * sizeof(uint32_t));
-  mesh_build(x, y, z, n, m, io.mesh_scratch.ptr, cs, &tm.mesh, sums);
+  // Only the sphere growth reads this mesh: its cells need not be in the
+  // canonical order (a radius does not depend on the order within a cell).
+  mesh_build(x, y, z, n, m, io.mesh_scratch.ptr, cs, &tm.mesh, sums, false);
   SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
   double* cscratch = (double*)io.mean.ensure(density_contrast_scratch_bytes() + 64);
   density_contrast(dg, cells, cscratch, s);

@@ -531,8 +531,9 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const uint32_t nb_scan = scan_blocks(cells);
   uint32_t* blocks = grow_to<uint32_t>(blocks_, (size_t)std::max<uint64_t>(nb_scan + 1, 1024));
 
-  MeshViewT<R> mv{mesh.x, mesh.y, mesh.z, mesh.offsets, (int32_t)mesh.n_cells, mesh.box_length,
-              1.0f / mesh.cell_length};
+  MeshViewT<R> mv{mesh.x,          mesh.y,          mesh.z,
+                  mesh.offsets,    (int32_t)mesh.n_cells, mesh.box_length,
+                  1.0f / mesh.cell_length, mesh.xyzw};
 
   bool mesh_waited = false;
   using clk = std::chrono::steady_clock;

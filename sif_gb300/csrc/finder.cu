@@ -710,6 +710,15 @@ __device__ __forceinline__ void walk_cells(const MeshViewT<R>& mesh, const Templ
         // Past the stream's end a lane loads particle 0 (there is one: the
         // stream is not empty) and drops it.
         const uint32_t q = pp[u] != 0xffffffffu ? pp[u] : 0u;
+        if constexpr (sizeof(R) == 4) {
+          if (mesh.xyzw) {
+            const float4 v = __ldg(mesh.xyzw + q);
+            px[u] = v.x;
+            py[u] = v.y;
+            pz[u] = v.z;
+            continue;
+          }
+        }
         px[u] = __ldg(mesh.x + q);
         py[u] = __ldg(mesh.y + q);
         pz[u] = __ldg(mesh.z + q);

@@ -41,6 +41,7 @@ struct MeshViewT {
   int32_t n;
   R box;
   R inv_l;  // 1 / cell_length
+  const float4* xyzw;  // the float form's 16-byte position records, or NULL (x, y, z)
 };
 
 template <class R>

@@ -88,15 +88,23 @@ struct DeviceMeshT {
   R *x = nullptr, *y = nullptr, *z = nullptr;
   uint32_t* offsets = nullptr;  // n_cells^3 + 1
   uint32_t* orig = nullptr;     // source index of each entry
+  // The float form's positions as 16-byte records (x, y, z, unused), one
+  // load per particle, in place of x, y, z: the unordered build writes them.
+  float4* xyzw = nullptr;
 };
 using DeviceMesh = DeviceMeshT<float>;
 // Scratch bytes of a mesh build in either form (the larger records).
 size_t mesh_scratch_bytes(uint64_t n_particles, uint32_t n_cells);
 // Builds into caller buffers (x, y, z, offsets, orig sized for the mesh).
 // scratch: mesh_scratch_bytes(); scan_sums: NULL, or scan_sums_needed(cells
-// + 1) entries the scan uses instead of a buffer of its own.
+// + 1) entries the scan uses instead of a buffer of its own. With
+// canonical false the cells' entries are left in the order the scatter
+// placed them (no orig) and, in the float form, the positions go to m.xyzw:
+// the same cells and counts, for a mesh only the sphere growth reads -- a
+// radius depends on which particles a cell holds, not on their order.
 template <class R>
 void mesh_build(const R* x, const R* y, const R* z, uint64_t n_particles, DeviceMeshT<R>& m,
-                void* scratch, cudaStream_t st, KernelTimer* timer, uint32_t* scan_sums = nullptr);
+                void* scratch, cudaStream_t st, KernelTimer* timer, uint32_t* scan_sums = nullptr,
+                bool canonical = true);
 
 }  // namespace sifg

@@ -98,6 +98,69 @@ __global__ void cell_scatter_kernel(const R* __restrict__ x, const R* __restrict
   }
 }
 
+// The float form's scatter straight into 16-byte position records, for a
+// build that leaves each cell in scatter order.
+__global__ void cell_scatter_xyzw_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                         const float* __restrict__ z, uint64_t n,
+                                         MeshGeom<float> g, uint32_t* __restrict__ cursor,
+                                         float4* __restrict__ out) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint64_t p = base + threadIdx.x;
+    const bool valid = p < n;
+    float px = 0, py = 0, pz = 0;
+    uint32_t c = 0xffffffffu;
+    if (valid) {
+      px = x[p];
+      py = y[p];
+      pz = z[p];
+      c = mesh_cell(px, py, pz, g);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    const unsigned leader = __ffs(peers) - 1;
+    uint32_t slot0 = 0;
+    if (valid && lane == leader) slot0 = atomicAdd(cursor + c, (uint32_t)__popc(peers));
+    slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+    if (valid)
+      out[slot0 + __popc(peers & ((1u << lane) - 1u))] =
+          make_float4(box_fold(px, g.box), box_fold(py, g.box), box_fold(pz, g.box), 0.f);
+  }
+}
+
+// The FP64 form's: straight into the mesh's position arrays.
+template <class R>
+__global__ void cell_scatter_soa_kernel(const R* __restrict__ x, const R* __restrict__ y,
+                                        const R* __restrict__ z, uint64_t n, MeshGeom<R> g,
+                                        uint32_t* __restrict__ cursor, R* __restrict__ ox,
+                                        R* __restrict__ oy, R* __restrict__ oz) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint64_t p = base + threadIdx.x;
+    const bool valid = p < n;
+    R px = 0, py = 0, pz = 0;
+    uint32_t c = 0xffffffffu;
+    if (valid) {
+      px = x[p];
+      py = y[p];
+      pz = z[p];
+      c = mesh_cell(px, py, pz, g);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    const unsigned leader = __ffs(peers) - 1;
+    uint32_t slot0 = 0;
+    if (valid && lane == leader) slot0 = atomicAdd(cursor + c, (uint32_t)__popc(peers));
+    slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+    if (valid) {
+      const uint32_t slot = slot0 + __popc(peers & ((1u << lane) - 1u));
+      ox[slot] = box_fold(px, g.box);
+      oy[slot] = box_fold(py, g.box);
+      oz[slot] = box_fold(pz, g.box);
+    }
+  }
+}
+
 constexpr int kCanonThreads = 128;
 constexpr int kCanonSmem = 2048;  // entries a CTA ranks in shared memory
 
@@ -152,7 +215,8 @@ size_t mesh_scratch_bytes(uint64_t n_particles, uint32_t n_cells) {
 
 template <class R>
 void mesh_build(const R* x, const R* y, const R* z, uint64_t n_particles, DeviceMeshT<R>& m,
-                void* scratch, cudaStream_t st, KernelTimer* timer, uint32_t* scan_sums) {
+                void* scratch, cudaStream_t st, KernelTimer* timer, uint32_t* scan_sums,
+                bool canonical) {
   MeshGeom<R> g;
   g.n = m.n_cells;
   g.box = m.box_length;
@@ -169,6 +233,17 @@ void mesh_build(const R* x, const R* y, const R* z, uint64_t n_particles, Device
   exclusive_scan_u32(m.offsets, (uint32_t)(cells + 1), st, scan_sums);
   SIFG_CUDA(cudaMemcpyAsync(cursor, m.offsets, cells * sizeof(uint32_t),
                             cudaMemcpyDeviceToDevice, st));
+  if (!canonical) {
+    if constexpr (sizeof(R) == 4)
+      cell_scatter_xyzw_kernel<<<grd, 256, 0, st>>>(x, y, z, n_particles, g, cursor, m.xyzw);
+    else
+      cell_scatter_soa_kernel<R><<<grd, 256, 0, st>>>(x, y, z, n_particles, g, cursor, m.x, m.y,
+                                                      m.z);
+    SIFG_LAUNCH_CHECK();
+    if (timer) timer->end(st);
+    m.n_particles = n_particles;
+    return;
+  }
   cell_scatter_kernel<R><<<grd, 256, 0, st>>>(x, y, z, n_particles, g, cursor, tmp);
   SIFG_LAUNCH_CHECK();
   const unsigned cgrid = grid_for(cells, kCanonThreads / 32 * 1, 152u * 16u);
@@ -180,9 +255,10 @@ void mesh_build(const R* x, const R* y, const R* z, uint64_t n_particles, Device
 }
 
 template void mesh_build<float>(const float*, const float*, const float*, uint64_t,
-                                DeviceMeshT<float>&, void*, cudaStream_t, KernelTimer*, uint32_t*);
+                                DeviceMeshT<float>&, void*, cudaStream_t, KernelTimer*, uint32_t*,
+                                bool);
 template void mesh_build<double>(const double*, const double*, const double*, uint64_t,
                                  DeviceMeshT<double>&, void*, cudaStream_t, KernelTimer*,
-                                 uint32_t*);
+                                 uint32_t*, bool);
 
 }  // namespace sifg
