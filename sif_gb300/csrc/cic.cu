@@ -166,11 +166,12 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
   uint32_t* acc_hi = acc_lo + TS * TS * TS;
   const uint32_t nt = g.nt;
   const uint32_t n_tiles = nt * nt * nt;
+  // Cleared once; each flush leaves the cells it reads cleared for the next tile.
+  for (int i = threadIdx.x; i < 2 * TS * TS * TS; i += blockDim.x) acc_lo[i] = 0u;
+  __syncthreads();
   for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const uint32_t tx = tile / (nt * nt), ty = (tile / nt) % nt, tz = tile % nt;
     const uint32_t ox = tx * TB, oy = ty * TB, oz = tz * TB;
-    for (int i = threadIdx.x; i < 2 * TS * TS * TS; i += blockDim.x) acc_lo[i] = 0u;
-    __syncthreads();
 
     const uint32_t s = offsets[tile], e = offsets[tile + 1];
     for (uint32_t base = s; base < e; base += blockDim.x) {
@@ -194,13 +195,20 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
         // is the quantisation itself; GB300's FP64 rate is no place for it.
         int sum = 0;
         int big = 0;
+        float wbig = w[0];
+#pragma unroll
         for (int k = 0; k < 8; k++) {
           const int qk = __float2int_rn(fmul(w[k], 16777216.0f));
           q[k] = (uint32_t)qk;
           sum += qk;
-          if (w[k] > w[big]) big = k;
+          if (w[k] > wbig) {  // the first largest, as a scan from corner 0 finds it
+            wbig = w[k];
+            big = k;
+          }
         }
-        q[big] = (uint32_t)((int)q[big] + (16777216 - sum));
+        const int fix = 16777216 - sum;
+#pragma unroll
+        for (int k = 0; k < 8; k++) q[k] = (uint32_t)((int)q[k] + (k == big ? fix : 0));
         cell = ((cx - ox) * TS + (cy - oy)) * TS + (cz - oz);
       }
       // One shared atomic per corner. (Reducing lanes bound for the same cell
@@ -211,7 +219,6 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
 #pragma unroll
         for (int k = 0; k < 8; k++) {
           const uint32_t v = q[k];
-          if (v == 0u) continue;
           const uint32_t c =
               cell + (uint32_t)(((k >> 2) & 1) * TS * TS + ((k >> 1) & 1) * TS + (k & 1));
           const uint32_t old = atomicAdd(acc_lo + c, v);
@@ -229,6 +236,8 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
       const uint32_t a = i / (TS * TS), b = (i / TS) % TS, c = i % TS;
       if (a > ex || b > ey || c > ez) continue;
       const unsigned long long v = ((unsigned long long)acc_hi[i] << 32) | acc_lo[i];
+      acc_lo[i] = 0u;
+      acc_hi[i] = 0u;
       const uint32_t gx = ox + a == g.n ? 0u : ox + a;
       const uint32_t gy = oy + b == g.n ? 0u : oy + b;
       const uint32_t gz = oz + c == g.n ? 0u : oz + c;
