@@ -876,7 +876,8 @@ static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceM
                       const R* radii, uint32_t n_radii, R threshold, R overlap, uint32_t opt,
                       const R* inject, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
                       uint64_t* n_voids, RunTimings& tm, cudaEvent_t mesh_ready = nullptr,
-                      std::vector<RungStat>* stats = &g_stats) {
+                      std::vector<RungStat>* stats = &g_stats,
+                      const double* contrast_mean = nullptr) {
   if (check_args(radii, n_radii, threshold, overlap) != SIF_OK) return kErrInvalid;
   RunParamsT<R> p;
   p.grid_n = n_grid;
@@ -889,6 +890,7 @@ static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceM
   p.inject = inject;
   p.inject_on_device = true;
   p.mesh_ready = mesh_ready;
+  p.contrast_mean = contrast_mean;
   HostCatalogueT<R> cat;
   if (stats) stats->clear();
   const int st = e->exodus(delta, m, p, cat, stats, &tm);
@@ -992,11 +994,13 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
   // canonical order (a radius does not depend on the order within a cell).
   mesh_build(x, y, z, n, m, io.mesh_scratch.ptr, cs, &tm.mesh, sums, false);
   SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
+  // The mean only: the contrast is taken by the run's forward transform as it
+  // reads the density (the grid is used for nothing else).
   double* cscratch = (double*)io.mean.ensure(density_contrast_scratch_bytes() + 64);
-  density_contrast(dg, cells, cscratch, s);
+  density_contrast(dg, cells, cscratch, s, true);
   int st = run_device(e, dg, n_grid, box, m, radii, n_radii, threshold, overlap, opt,
                       (const R*)nullptr, cx, cy, cz, r, capacity, n_voids, tm, e->ev_mesh_ready(),
-                      stats);
+                      stats, contrast_mean(cscratch));
   unsigned long long h_outside = 0;
   SIFG_CUDA(cudaMemcpyAsync(&h_outside, outside, sizeof(h_outside), cudaMemcpyDeviceToHost, s));
   SIFG_CUDA(cudaStreamSynchronize(s));

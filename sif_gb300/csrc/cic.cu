@@ -386,7 +386,17 @@ __global__ void __launch_bounds__(kMeanThreads) mean_partial_kernel(const R* __r
   const uint64_t lo = (uint64_t)blockIdx.x * chunk;
   const uint64_t hi = lo + chunk < n ? lo + chunk : n;
   double acc = 0.0;
-  for (uint64_t i = lo + threadIdx.x; i < hi; i += kMeanThreads) acc += (double)v[i];
+  // Four loads in flight, added in the same order as one at a time.
+  uint64_t i = lo + threadIdx.x;
+  for (; i + 3 * kMeanThreads < hi; i += 4 * kMeanThreads) {
+    const R a = v[i], b = v[i + kMeanThreads], c = v[i + 2 * kMeanThreads],
+            d = v[i + 3 * kMeanThreads];
+    acc += (double)a;
+    acc += (double)b;
+    acc += (double)c;
+    acc += (double)d;
+  }
+  for (; i < hi; i += kMeanThreads) acc += (double)v[i];
   s[threadIdx.x] = acc;
   __syncthreads();
   for (int w = kMeanThreads / 2; w > 0; w >>= 1) {
@@ -495,17 +505,26 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
 }
 
 template <class R>
-void density_contrast(R* v, uint64_t n, double* d_scratch, cudaStream_t st) {
+void density_contrast(R* v, uint64_t n, double* d_scratch, cudaStream_t st, bool mean_only) {
   // d_scratch: kMeanBlocks + 1 doubles.
   mean_partial_kernel<R><<<kMeanBlocks, kMeanThreads, 0, st>>>(v, n, d_scratch);
   SIFG_LAUNCH_CHECK();
   mean_final_kernel<<<1, 32, 0, st>>>(d_scratch, n, d_scratch + kMeanBlocks);
   SIFG_LAUNCH_CHECK();
-  contrast_kernel<R><<<grid_for(n, 256), 256, 0, st>>>(v, n, d_scratch + kMeanBlocks);
+  if (!mean_only) apply_contrast(v, n, d_scratch + kMeanBlocks, st);
+}
+template void density_contrast<float>(float*, uint64_t, double*, cudaStream_t, bool);
+template void density_contrast<double>(double*, uint64_t, double*, cudaStream_t, bool);
+
+template <class R>
+void apply_contrast(R* v, uint64_t n, const double* mean, cudaStream_t st) {
+  contrast_kernel<R><<<grid_for(n, 256), 256, 0, st>>>(v, n, mean);
   SIFG_LAUNCH_CHECK();
 }
-template void density_contrast<float>(float*, uint64_t, double*, cudaStream_t);
-template void density_contrast<double>(double*, uint64_t, double*, cudaStream_t);
+template void apply_contrast<float>(float*, uint64_t, const double*, cudaStream_t);
+template void apply_contrast<double>(double*, uint64_t, const double*, cudaStream_t);
+
+const double* contrast_mean(const double* d_scratch) { return d_scratch + kMeanBlocks; }
 
 size_t density_contrast_scratch_bytes() { return (kMeanBlocks + 1) * sizeof(double); }
 

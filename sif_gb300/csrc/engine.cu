@@ -481,7 +481,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   } drain{st_fft_};
   if (!p.inject) {
     smoother.setup(N, box, window_mode, st_fft_);
-    smoother.forward(d_delta);
+    smoother.forward(d_delta, p.contrast_mean);
     if (!radii.empty()) smooth_rung(0);
   }
 

@@ -29,6 +29,9 @@ struct RunParamsT {
   bool inject_on_device = false;
   // Where the last rung's field goes under SIF_FINDER_CONSUME_GRID (device).
   R* consume_out = nullptr;
+  // When set, the grid handed to the run is the density itself and this the
+  // device-side mean: the forward transform takes the contrast as it reads.
+  const double* contrast_mean = nullptr;
   // Recorded once the mesh is on the device, if it is still being copied
   // when the run starts: the first sphere growth waits for it.
   cudaEvent_t mesh_ready = nullptr;

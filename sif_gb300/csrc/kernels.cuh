@@ -68,8 +68,13 @@ void cic_deposit_f64(const double* x, const double* y, const double* z, uint64_t
                      uint32_t n, double box, double* grid, void* scratch, cudaStream_t st,
                      KernelTimer* timer);
 size_t density_contrast_scratch_bytes();
+// The mean (a fixed summation order) into d_scratch, then v * (1 / mean) - 1
+// in place unless mean_only; contrast_mean() is where the mean sits.
 template <class R>
-void density_contrast(R* v, uint64_t n, double* d_scratch, cudaStream_t st);
+void density_contrast(R* v, uint64_t n, double* d_scratch, cudaStream_t st, bool mean_only = false);
+template <class R>
+void apply_contrast(R* v, uint64_t n, const double* mean, cudaStream_t st);
+const double* contrast_mean(const double* d_scratch);
 double read_mean(const double* d_scratch);
 
 // --- adjoint.cu ---

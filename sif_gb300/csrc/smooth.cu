@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(16 * kRowsPerCta)
 // go to the tiles (16 rows by 16 kz, 2 KB blocks).
 __global__ void __launch_bounds__(16 * kRowsPerCta)
     r2c512_rows_kernel(const float* __restrict__ grid, float2* __restrict__ work,
-                       const float2* __restrict__ tw) {
+                       const float2* __restrict__ tw, const double* __restrict__ mean) {
   __shared__ __align__(16) float2 buf[kRowsPerCta * kRowSlots];
   const uint32_t x = blockIdx.x / (512 / kRowsPerCta);
   const uint32_t y0 = (blockIdx.x % (512 / kRowsPerCta)) * kRowsPerCta;
@@ -501,9 +501,14 @@ __global__ void __launch_bounds__(16 * kRowsPerCta)
   const float2* twb = tw + 512;
   const float2* wpre = tw + 768;
   float2 v[16];
+  // With the mean, the rows are the density: its contrast, as the contrast
+  // kernel computes it (inv rounded from the double 1 / mean).
+  const float inv = mean ? (float)(1.0 / __ldg(mean)) : 0.f;
 #pragma unroll
   for (int r = 0; r < 16; r++) {
     v[r] = row[j + 16u * r];
+    if (mean) v[r] = make_float2(__fsub_rn(__fmul_rn(v[r].x, inv), 1.0f),
+                                 __fsub_rn(__fmul_rn(v[r].y, inv), 1.0f));
     v[r].y = -v[r].y;
   }
   dft_inv(v);
@@ -665,17 +670,20 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
   }
 }
 
-static void launch_forward512(const SmootherT<float>& s, const float* grid);
+static void launch_forward512(const SmootherT<float>& s, const float* grid, const double* mean);
 
 template <>
-void SmootherT<float>::forward(const float* grid) {
-  if (twiddles)
-    launch_forward512(*this, grid);
-  else
-    SIFG_CUFFT(cufftExecR2C(plan_r2c, (cufftReal*)grid, (cufftComplex*)spectrum.ptr));
+void SmootherT<float>::forward(const float* grid, const double* mean) {
+  if (twiddles) {
+    launch_forward512(*this, grid, mean);
+    return;
+  }
+  if (mean) apply_contrast(const_cast<float*>(grid), (uint64_t)n * n * n, mean, stream);
+  SIFG_CUFFT(cufftExecR2C(plan_r2c, (cufftReal*)grid, (cufftComplex*)spectrum.ptr));
 }
 template <>
-void SmootherT<double>::forward(const double* grid) {
+void SmootherT<double>::forward(const double* grid, const double* mean) {
+  if (mean) apply_contrast(const_cast<double*>(grid), (uint64_t)n * n * n, mean, stream);
   SIFG_CUFFT(cufftExecD2Z(plan_r2c, (cufftDoubleReal*)grid, (cufftDoubleComplex*)spectrum.ptr));
 }
 
@@ -711,13 +719,13 @@ static void set_column_smem() {
 // The float form's forward transform at n = 512: the R2C along z into the
 // work tiles, the forward ky FFT in place, the forward kx FFT into the
 // spectrum's tiles.
-static void launch_forward512(const SmootherT<float>& s, const float* grid) {
+static void launch_forward512(const SmootherT<float>& s, const float* grid, const double* mean) {
   constexpr uint32_t N = 512;
   set_column_smem();
   const size_t smem = (size_t)kColCols * kColStride * sizeof(float2);
   const float2* tw = (const float2*)s.twiddles;
   r2c512_rows_kernel<<<N * N / kRowsPerCta, 16 * kRowsPerCta, 0, s.stream>>>(
-      grid, s.work.as<float2>(), tw);
+      grid, s.work.as<float2>(), tw, mean);
   SIFG_LAUNCH_CHECK();
   colfft512_kernel<<<dim3(kKzBlocks, N), 32 * kColWarps, smem, s.stream>>>(
       s.work.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByLine, nullptr, nullptr, 1.f,

@@ -36,7 +36,10 @@ struct SmootherT {
   std::vector<Plans> plans;
 
   void setup(uint32_t n, R box, int window_mode, cudaStream_t st);
-  void forward(const R* grid);  // grid: n^3 values on the device
+  // grid: n^3 values on the device; with mean set, the density, whose
+  // contrast v * (1 / mean) - 1 is transformed (taken as the transform reads
+  // it where it can, else in place first).
+  void forward(const R* grid, const double* mean = nullptr);
   // Writes the grid smoothed at r (and, with sigma > 0, a Gaussian of sigma
   // on top) into out (n^3 values), asynchronously on the stream.
   void smooth(int filter, R r, R sigma, R* out, KernelTimer* timer);
