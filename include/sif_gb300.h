@@ -305,6 +305,7 @@ typedef struct {
   uint64_t growth_cells;
   /* Host wait for the candidates' depths before the sort, milliseconds. */
   double cand_wait_ms;
+  uint64_t from_list;      /* 1: the candidates came from the smoothing's below-threshold list */
 } sifg_rung_stat_t;
 
 /* Kernel timings of the last run, CUDA events on the launching stream. */
@@ -449,6 +450,11 @@ void sifg_set_growth_mode(int mode);
  * where the device allows it, 1 a kernel launch per round. The catalogue
  * does not depend on it. */
 void sifg_set_commit_mode(int mode);
+/* How a rung's candidates are found under the cell seeds: 0 (default) from
+ * the list of cells at or below the threshold that the smoothing writes as
+ * it goes, where it can (the float form at a 512^3 grid), less the masked
+ * cells; 1 a scan of the whole field. The catalogue does not depend on it. */
+void sifg_set_scan_mode(int mode);
 /* The chain-mesh build of sifg_mesh_device, for callers that cannot let the
  * library allocate device memory: a process whose framework reserves the
  * GPU's memory in its own pool, a latency-bound pipeline that cannot afford

@@ -1294,7 +1294,7 @@ uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
     out[i] = sifg_rung_stat_t{s.radius, s.r_search, s.n_candidates, s.n_survivors, s.n_accepted,
                               s.rounds, s.n_rescale_fail, s.n_overflow, s.rung_ms,
                               s.count_wait_ms, s.sort_ms, s.commit_ms, s.growth_particles,
-                              s.growth_cells, s.cand_wait_ms};
+                              s.growth_cells, s.cand_wait_ms, s.from_list};
   }
   return n;
 }
@@ -1318,6 +1318,7 @@ uint64_t sifg_stream(void) {
 
 void sifg_set_growth_mode(int mode) { set_growth_mode(mode < 0 || mode > 2 ? 0 : mode); }
 void sifg_set_commit_mode(int mode) { set_commit_mode(mode == 1 ? 1 : 0); }
+void sifg_set_scan_mode(int mode) { set_scan_mode(mode == 1 ? 1 : 0); }
 
 void sifg_set_window(int bins) { g_window = bins < 1 ? 1 : (bins > 64 ? 64 : bins); }
 

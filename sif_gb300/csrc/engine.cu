@@ -423,6 +423,9 @@ template int build_template<double>(HostTemplateT<double>&, uint32_t, double, do
 // The run
 // ---------------------------------------------------------------------------
 
+static int g_scan_mode = 0;
+void set_scan_mode(int mode) { g_scan_mode = mode; }
+
 template <class T>
 static T* grow_to(DevBuf& b, size_t n) {
   return (T*)b.ensure(n * sizeof(T));
@@ -468,9 +471,15 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   SIFG_CUDA(cudaEventRecord(ev_start_, st_));
   SIFG_CUDA(cudaStreamWaitEvent(st_fft_, ev_start_, 0));
   for (int k = 0; k < 2; k++) SIFG_CUDA(cudaEventRecord(ev_scanned_[k], st_));
+  // Under the cell seeds, where the smoothing can list the cells at or below
+  // the threshold as it writes them (the float form's own transform), the
+  // scan is a mask filter over that list; two lists alternate with the fields.
+  BelowList below[2];
+  bool listed = false;
   auto smooth_rung = [&](uint32_t ri) {
     SIFG_CUDA(cudaStreamWaitEvent(st_fft_, ev_scanned_[ri % 2], 0));
-    smoother.smooth(kFilterTopHat, radii[ri], 0.0f, fields[ri % 2], tm ? &tm->filter : nullptr);
+    smoother.smooth(kFilterTopHat, radii[ri], 0.0f, fields[ri % 2], tm ? &tm->filter : nullptr,
+                    listed ? &below[ri % 2] : nullptr);
     SIFG_CUDA(cudaEventRecord(ev_smoothed_[ri % 2], st_fft_));
   };
   // On every way out, nothing of the run is left in flight on the smoothing
@@ -479,8 +488,18 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     cudaStream_t s;
     ~FftDrain() { cudaStreamSynchronize(s); }
   } drain{st_fft_};
+  const uint32_t nb_below = (uint32_t)((cells + kBelowBlock - 1) / kBelowBlock);
   if (!p.inject) {
     smoother.setup(N, box, window_mode, st_fft_);
+    listed = g_scan_mode == 0 && sizeof(R) == 4 && !minima && smoother.lists_below() &&
+             cells % kBelowBlock == 0;
+    if (listed)
+      for (int k = 0; k < 2; k++) {
+        below[k].thr = (float)threshold;
+        below[k].counts = grow_to<uint32_t>(below_counts_[k], nb_below);
+        below[k].delta = grow_to<float>(below_delta_[k], cells);
+        below[k].flat = grow_to<uint32_t>(below_flat_[k], cells);
+      }
     smoother.forward(d_delta, p.contrast_mean);
     if (!radii.empty()) smooth_rung(0);
   }
@@ -529,7 +548,8 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   SIFG_CUDA(cudaMemsetAsync(traffic, 0, (2 * n_rungs + 2) * sizeof(uint64_t), st_));
   uint32_t* counters = grow_to<uint32_t>(counters_, kCommitCounters);
   const uint32_t nb_scan = scan_blocks(cells);
-  uint32_t* blocks = grow_to<uint32_t>(blocks_, (size_t)std::max<uint64_t>(nb_scan + 1, 1024));
+  uint32_t* blocks = grow_to<uint32_t>(
+      blocks_, (size_t)std::max<uint64_t>(std::max<uint64_t>(nb_scan, nb_below) + 1, 1024));
 
   MeshViewT<R> mv{mesh.x,          mesh.y,          mesh.z,
                   mesh.offsets,    (int32_t)mesh.n_cells, mesh.box_length,
@@ -559,13 +579,21 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     }
 
     // 2. Candidates, in flat order.
-    const uint64_t slots = scan_region_slots(cells);
-    R* region_delta = grow_to<R>(region_delta_, slots);
-    uint32_t* region_flat = grow_to<uint32_t>(region_flat_, slots);
-    scan_fused_pass(field, mask, cells, threshold, blocks, dcount, region_delta, region_flat, st_, N,
-                    minima);
-    // The field's last reader: the next rung but one may smooth into it.
-    SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
+    R* region_delta = nullptr;
+    uint32_t* region_flat = nullptr;
+    const BelowList& bl = below[ri % 2];
+    rs.from_list = listed ? 1u : 0u;
+    if (listed) {
+      below_count_pass(bl.counts, bl.flat, nb_below, kBelowBlock, mask, blocks, dcount, st_);
+    } else {
+      const uint64_t slots = scan_region_slots(cells);
+      region_delta = grow_to<R>(region_delta_, slots);
+      region_flat = grow_to<uint32_t>(region_flat_, slots);
+      scan_fused_pass(field, mask, cells, threshold, blocks, dcount, region_delta, region_flat, st_,
+                      N, minima);
+      // The field's last reader: the next rung but one may smooth into it.
+      SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
+    }
     SIFG_CUDA(cudaMemcpyAsync(h_counters_, dcount, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
     const auto t_wait = clk::now();
     SIFG_CUDA(cudaStreamSynchronize(st_));
@@ -580,6 +608,8 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     if (ri > 0 && radii[ri - 1] > r_search) r_search = radii[ri - 1];
     rs.r_search = r_search;
     if (m == 0) {
+      // The list's last reader was its count pass.
+      if (listed) SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
       rs.rung_ms = ms_since(t_rung);
       if (stats) stats->push_back(rs);
       continue;
@@ -587,7 +617,15 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
 
     R* cdelta = grow_to<R>(cand_delta_, m);
     uint32_t* cflat = grow_to<uint32_t>(cand_flat_, m);
-    scan_compact(blocks, cells, region_delta, region_flat, cdelta, cflat, st_);
+    if (listed) {
+      if constexpr (sizeof(R) == 4)
+        below_write_pass(bl.counts, bl.delta, bl.flat, nb_below, kBelowBlock, mask, blocks, cdelta,
+                         cflat, st_);
+      // The list's last reader: the next rung but one may smooth into it.
+      SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
+    } else {
+      scan_compact(blocks, cells, region_delta, region_flat, cdelta, cflat, st_);
+    }
     ensure_host(m);
     SIFG_CUDA(cudaMemcpyAsync(h_delta_, cdelta, m * sizeof(R), cudaMemcpyDeviceToHost, st_));
     SIFG_CUDA(cudaEventRecord(ev_cand_, st_));

@@ -44,6 +44,7 @@ struct RungStat {
   uint64_t n_rescale_fail = 0, n_overflow = 0;
   double rung_ms = 0, count_wait_ms = 0, sort_ms = 0, commit_ms = 0;  // host wall time
   double cand_wait_ms = 0;  // waiting for the candidates' depths before the sort
+  uint64_t from_list = 0;   // 1: candidates from the smoothing's below-threshold list
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the rung's sphere growth
 };
 
@@ -108,6 +109,7 @@ class Engine {
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
   DevBuf tpl_, gbuf_, traffic_, region_delta_, region_flat_;
+  DevBuf below_counts_[2], below_delta_[2], below_flat_[2];  // the smoothing's below-threshold lists
   std::vector<uint8_t> h_tpl_;  // the packed template, staged for its upload
   void* h_delta_ = nullptr;  // candidate depths, float or double
   uint32_t* h_flat_ = nullptr;
@@ -127,6 +129,12 @@ class Engine {
 // The reference's candidate order (include/sif/utils/sort.h:56-145 over
 // src/finder/utils.c:24): rank[k] is the position of candidate k, given in
 // flat order, once sorted by depth with the three-way quicksort.
+// 0 (default): under the cell seeds, where the smoothing lists the cells at
+// or below the threshold as it writes them, the candidates are that list
+// less the masked cells; 1: a scan of the whole field every rung. The
+// catalogue does not depend on it.
+void set_scan_mode(int mode);
+
 template <class K>
 void candidate_ranks(const K* delta, uint32_t m, uint32_t* rank, int threads);
 

@@ -234,6 +234,76 @@ __global__ void scan_compact_kernel(const uint32_t* __restrict__ offsets, uint32
 
 uint64_t scan_region_slots(uint64_t n_cells) { return (uint64_t)scan_blocks(n_cells) * kScanChunk; }
 
+// The candidates from a below-threshold list made by the smoothing (blocks
+// of `block` cells, block b's entries at the start of its region): the
+// listed cells whose mask bit is clear, in the list's order. A warp per block.
+__global__ void below_count_kernel(const uint32_t* __restrict__ counts,
+                                   const uint32_t* __restrict__ flat, uint32_t nb, uint32_t block,
+                                   const uint32_t* mask, uint32_t* __restrict__ kept) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < nb; b += warps) {
+    const uint32_t cnt = counts[b];
+    const uint32_t* f = flat + (uint64_t)b * block;
+    uint32_t k = 0;
+    for (uint32_t i = lane; i < cnt; i += 32) k += mask_get_rw(mask, f[i]) ? 0u : 1u;
+    k = __reduce_add_sync(0xffffffffu, k);
+    if (lane == 0) kept[b] = k;
+  }
+}
+
+__global__ void below_write_kernel(const uint32_t* __restrict__ counts,
+                                   const float* __restrict__ delta,
+                                   const uint32_t* __restrict__ flat, uint32_t nb, uint32_t block,
+                                   const uint32_t* mask, const uint32_t* __restrict__ offsets,
+                                   float* __restrict__ cdelta, uint32_t* __restrict__ cflat) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < nb; b += warps) {
+    const uint32_t cnt = counts[b];
+    const uint64_t src = (uint64_t)b * block;
+    uint32_t out = offsets[b];
+    for (uint32_t i0 = 0; i0 < cnt; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      uint32_t c = 0;
+      bool keep = false;
+      if (i < cnt) {
+        c = flat[src + i];
+        keep = !mask_get_rw(mask, c);
+      }
+      const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+      if (keep) {
+        const uint32_t pos = out + __popc(ballot & ((1u << lane) - 1u));
+        cdelta[pos] = delta[src + i];
+        cflat[pos] = c;
+      }
+      out += __popc(ballot);
+    }
+  }
+}
+
+void below_count_pass(const uint32_t* counts, const uint32_t* flat, uint32_t nb, uint32_t block,
+                      const uint32_t* mask, uint32_t* block_counts, uint32_t* d_count,
+                      cudaStream_t st) {
+  const uint32_t warps = nb < 152u * 64u ? nb : 152u * 64u;
+  below_count_kernel<<<(warps + 7) / 8, 256, 0, st>>>(counts, flat, nb, block, mask, block_counts);
+  SIFG_LAUNCH_CHECK();
+  SIFG_CUDA(cudaMemsetAsync(block_counts + nb, 0, sizeof(uint32_t), st));
+  exclusive_scan_u32(block_counts, nb + 1, st);
+  store_total_kernel<<<1, 1, 0, st>>>(block_counts, nb, d_count);
+  SIFG_LAUNCH_CHECK();
+}
+
+void below_write_pass(const uint32_t* counts, const float* delta, const uint32_t* flat,
+                      uint32_t nb, uint32_t block, const uint32_t* mask,
+                      const uint32_t* block_offsets, float* cand_delta, uint32_t* cand_flat,
+                      cudaStream_t st) {
+  const uint32_t warps = nb < 152u * 64u ? nb : 152u * 64u;
+  below_write_kernel<<<(warps + 7) / 8, 256, 0, st>>>(counts, delta, flat, nb, block, mask,
+                                                      block_offsets, cand_delta, cand_flat);
+  SIFG_LAUNCH_CHECK();
+}
+
 template <class R>
 void scan_fused_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R threshold,
                      uint32_t* block_counts, uint32_t* d_count, R* region_delta,

@@ -145,6 +145,20 @@ void scan_compact(const uint32_t* block_counts, uint64_t n_cells, const R* regio
                   const uint32_t* region_flat, R* cand_delta, uint32_t* cand_flat,
                   cudaStream_t st);
 
+// The candidates (cells mode) from the below-threshold list a smoothing made
+// (blocks of `block` cells, counts per block, block b's entries at the start
+// of its region of delta and flat): the listed cells whose mask bit is
+// clear, in flat order. The count pass leaves the per-block offsets in
+// block_counts (nb + 1 entries) and the total in *d_count, as
+// scan_count_pass does; the write pass fills the candidates.
+void below_count_pass(const uint32_t* counts, const uint32_t* flat, uint32_t nb, uint32_t block,
+                      const uint32_t* mask, uint32_t* block_counts, uint32_t* d_count,
+                      cudaStream_t st);
+void below_write_pass(const uint32_t* counts, const float* delta, const uint32_t* flat,
+                      uint32_t nb, uint32_t block, const uint32_t* mask,
+                      const uint32_t* block_offsets, float* cand_delta, uint32_t* cand_flat,
+                      cudaStream_t st);
+
 // Pre-filter at the rung radius (prefilter_cells, exodus_finder.c:871-944)
 // and compaction of the survivors, candidate order kept.
 template <class R>

@@ -425,11 +425,18 @@ __global__ void __launch_bounds__(32 * kColWarps, 3)
 // 256, by 16-byte asynchronous copies) and one mode each for kz = 256; a row
 // has kRowSlots slots in shared memory (even, for the 16-byte copies); the
 // stage exchange swizzles slots (k1, j) -> 16 k1 + (j ^ k1) within the row.
+//
+// With `below` set the pass also lists, in flat order, the cells it writes
+// whose value is at most below.thr: the CTA's 8192 cells are one contiguous
+// flat range, and their entries go to the start of the CTA's own region of
+// 8192 slots, their number to below.counts[CTA] (the candidate scan's
+// threshold test, from the values in hand).
 constexpr int kRowsPerCta = 16;
 constexpr uint32_t kRowSlots = 258;
+static_assert(kRowsPerCta * 512 == kBelowBlock, "a CTA's cells are one below-list block");
 __global__ void __launch_bounds__(16 * kRowsPerCta)
     c2r512_rows_kernel(const float2* __restrict__ work, float* __restrict__ out,
-                       const float2* __restrict__ tw) {
+                       const float2* __restrict__ tw, BelowList below) {
   __shared__ __align__(16) float2 buf[kRowsPerCta * kRowSlots];
   const uint32_t x = blockIdx.x / (512 / kRowsPerCta);
   const uint32_t y0 = (blockIdx.x % (512 / kRowsPerCta)) * kRowsPerCta;
@@ -474,8 +481,51 @@ __global__ void __launch_bounds__(16 * kRowsPerCta)
   for (int k = 0; k < 16; k++) row[j + 16 * k] = v[k];
   __syncthreads();
   float2* dst = reinterpret_cast<float2*>(out + ((size_t)x * 512 + y0) * 512);
-  for (uint32_t f = threadIdx.x; f < kRowsPerCta * 256; f += blockDim.x)
-    dst[f] = buf[(f >> 8) * kRowSlots + (f & 255u)];
+  if (!below.counts) {
+    for (uint32_t f = threadIdx.x; f < kRowsPerCta * 256; f += blockDim.x)
+      dst[f] = buf[(f >> 8) * kRowSlots + (f & 255u)];
+    return;
+  }
+  __shared__ uint32_t ws[16 * kRowsPerCta / 32];
+  const uint32_t cell0 = (x * 512 + y0) * 512;
+  const size_t region = (size_t)blockIdx.x * (kRowsPerCta * 512);
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t n_out = 0;
+  for (uint32_t f0 = 0; f0 < kRowsPerCta * 256; f0 += blockDim.x) {
+    const uint32_t f = f0 + threadIdx.x;
+    const float2 v = buf[(f >> 8) * kRowSlots + (f & 255u)];
+    dst[f] = v;
+    const uint32_t bits = (v.x <= below.thr ? 1u : 0u) | (v.y <= below.thr ? 2u : 0u);
+    // The block's exclusive scan of the counts, in thread order (flat order).
+    const uint32_t c = __popc(bits);
+    uint32_t incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= (unsigned)d) incl += y;
+    }
+    if (lane == 31) ws[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < 16 * kRowsPerCta / 32; w++) {
+      before += w < (int)warp ? ws[w] : 0u;
+      total += ws[w];
+    }
+    __syncthreads();
+    uint32_t pos = n_out + before + incl - c;
+    if (bits & 1u) {
+      below.delta[region + pos] = v.x;
+      below.flat[region + pos] = cell0 + 2 * f;
+      pos++;
+    }
+    if (bits & 2u) {
+      below.delta[region + pos] = v.y;
+      below.flat[region + pos] = cell0 + 2 * f + 1;
+    }
+    n_out += total;
+  }
+  if (threadIdx.x == 0) below.counts[blockIdx.x] = n_out;
 }
 
 // The forward transform's first pass, the R2C along z: 16 rows of 512 reals
@@ -739,7 +789,7 @@ static void launch_forward512(const SmootherT<float>& s, const float* grid, cons
 
 // The timer, begun by the caller, ends after pass (1): the filter's kernel.
 static void launch_inverse512(const SmootherT<float>& s, int filter, float norm, float* out,
-                              KernelTimer* timer) {
+                              KernelTimer* timer, const BelowList& below) {
   constexpr uint32_t N = 512;
   const float* w = (s.window_mode && filter != kFilterNone) ? s.win.as<float>() : nullptr;
   const size_t smem = (size_t)kColCols * kColStride * sizeof(float2);
@@ -756,9 +806,11 @@ static void launch_inverse512(const SmootherT<float>& s, int filter, float norm,
       tw, false);
   SIFG_LAUNCH_CHECK();
   c2r512_rows_kernel<<<N * N / kRowsPerCta, 16 * kRowsPerCta, 0, s.stream>>>(s.work.as<float2>(),
-                                                                           out, tw);
+                                                                           out, tw, below);
+  SIFG_LAUNCH_CHECK();
 }
-static void launch_inverse512(const SmootherT<double>&, int, double, double*, KernelTimer*) {}
+static void launch_inverse512(const SmootherT<double>&, int, double, double*, KernelTimer*,
+                              const BelowList&) {}
 
 static void launch_filter(const SmootherT<double>& s, int filter, double norm) {
   const uint64_t modes = (uint64_t)s.n * s.n * (s.n / 2 + 1);
@@ -768,7 +820,8 @@ static void launch_filter(const SmootherT<double>& s, int filter, double norm) {
 }
 
 template <class R>
-void SmootherT<R>::smooth(int filter, R r, R sigma, R* out, KernelTimer* timer) {
+void SmootherT<R>::smooth(int filter, R r, R sigma, R* out, KernelTimer* timer,
+                          const BelowList* below) {
   const uint32_t h = n >> 1;
   const uint32_t max_k2 = 3 * h * h;
   const double factor = (double)r * 2.0 * M_PI / (double)box;
@@ -779,7 +832,7 @@ void SmootherT<R>::smooth(int filter, R r, R sigma, R* out, KernelTimer* timer) 
   const R norm = (R)(1.0 / ((double)n * n * n));
   if (timer) timer->begin(stream);
   if (twiddles) {
-    launch_inverse512(*this, filter, norm, out, timer);
+    launch_inverse512(*this, filter, norm, out, timer, below ? *below : BelowList{});
     return;
   }
   launch_filter(*this, filter, norm);

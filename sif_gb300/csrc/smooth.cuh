@@ -13,6 +13,18 @@ constexpr int kFilterNone = 0;
 constexpr int kFilterTopHat = 1;
 constexpr int kFilterGaussian = 2;
 
+// Where a smoothing can list the cells it writes at or below a threshold, in
+// flat order, by blocks of kBelowBlock cells: block b's entries at the start
+// of its region [b * kBelowBlock, (b + 1) * kBelowBlock) of delta and flat,
+// their number in counts[b]. counts NULL: no list.
+constexpr uint32_t kBelowBlock = 8192;
+struct BelowList {
+  float thr = 0.f;
+  uint32_t* counts = nullptr;  // cells / kBelowBlock
+  float* delta = nullptr;      // cells slots
+  uint32_t* flat = nullptr;    // cells slots
+};
+
 // Window modes: 0 none (SIF_FINDER_KEEP_CIC_WINDOW), 1 full CIC deconvolution,
 // 2 aliasing-aware (SIF_FINDER_ALIASING_WINDOW). R is the form's precision:
 // float (cuFFT R2C/C2R) or double (D2Z/Z2D).
@@ -42,7 +54,11 @@ struct SmootherT {
   void forward(const R* grid, const double* mean = nullptr);
   // Writes the grid smoothed at r (and, with sigma > 0, a Gaussian of sigma
   // on top) into out (n^3 values), asynchronously on the stream.
-  void smooth(int filter, R r, R sigma, R* out, KernelTimer* timer);
+  // below (float form): the cells at or below below->thr listed as the
+  // transform writes them, where lists_below() -- else the caller scans.
+  void smooth(int filter, R r, R sigma, R* out, KernelTimer* timer,
+              const BelowList* below = nullptr);
+  bool lists_below() const { return sizeof(R) == 4 && twiddles != nullptr; }
   void restore(R* out);
   void release();
   ~SmootherT();

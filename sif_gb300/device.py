@@ -169,6 +169,12 @@ def set_commit_mode(mode):
     _lib.load().sifg_set_commit_mode(int(mode))
 
 
+def set_scan_mode(mode):
+    """0 the candidates from the smoothing's below-threshold list where it
+    makes one, 1 a scan of the whole field every rung."""
+    _lib.load().sifg_set_scan_mode(int(mode))
+
+
 def set_window(bins):
     _lib.load().sifg_set_window(int(bins))
 

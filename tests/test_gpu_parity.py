@@ -345,3 +345,28 @@ def test_c_api_end_to_end_and_errors(gpu_lib, oracle):
     g2.to_density_contrast()
     pysif.finders.exodus_raw(g2, m, radii, -0.75, consume_grid=True)
     assert not same_bits(g2.values, g.values)
+
+
+@pytest.mark.parametrize("options,overlap", [(0, 0.0), (abi.SIF_FINDER_LAGRANGIAN_OVERLAP, 0.0),
+                                             (0, 0.5)], ids=["default", "lagrangian", "overlap_0_5"])
+def test_box_candidates_from_the_smoothing_list(dev, options, overlap):
+    """At a 512^3 grid the float form's smoothing lists the cells at or below
+    the threshold as it writes the field, and the rung's candidates are that
+    list less the masked cells: the same catalogue, bit for bit, as a scan of
+    the whole field every rung (which the oracle tests pin)."""
+    import torch
+
+    x, y, z = synth.zeldovich(256, 500.0, 5.0, 1205, backend="torch")
+    xs = [torch.from_numpy(a).cuda() for a in (x, y, z)]
+    radii = synth.ladder(4.0, 16.0, 0.1).astype(np.float32)
+    cats, listed = [], []
+    for mode in (0, 1):
+        dev.set_scan_mode(mode)
+        try:
+            cats.append(dev.box(*xs, 512, 500.0, 62, radii, -0.8, overlap, options))
+            listed.append([r["from_list"] for r in dev.last_rung_stats()])
+        finally:
+            dev.set_scan_mode(0)
+    assert all(listed[0]) and not any(listed[1])
+    assert len(cats[0][0]) > 100
+    assert len(cats[0][0]) == len(cats[1][0]) and same_catalogue(cats[0], cats[1])
