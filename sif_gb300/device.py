@@ -10,6 +10,7 @@ complete; before each call the torch stream that produced the inputs is
 drained, since nothing else orders the library's reads after torch's writes.
 """
 import ctypes as C
+import threading
 
 import numpy as np
 
@@ -99,8 +100,19 @@ def smooth(delta, n_grid, box, radius, filter="top-hat", window="full"):
     return out
 
 
+_scratch = threading.local()
+
+
 def _catalogue_arrays(cap, dtype=np.float32):
-    return [np.empty(cap, dtype) for _ in range(4)]
+    """Four output columns for the library to fill; kept per thread between
+    calls (callers get copies): fresh arrays of this size cost more in page
+    faults than the run's own host work."""
+    key = (cap, np.dtype(dtype).str)
+    cols = getattr(_scratch, "cols", {}).get(key)
+    if cols is None:
+        cols = [np.empty(cap, dtype) for _ in range(4)]
+        _scratch.cols = {key: cols}
+    return cols
 
 
 def exodus(delta, n_grid, box, mesh, mesh_cells, radii, threshold, overlap=0.0, options=0,
@@ -193,7 +205,7 @@ def box_batch(boxes, engines=0, capacity=1 << 20, check=True):
     keep = []
     for j, b in zip(jobs, boxes):
         radii = np.ascontiguousarray(b["radii"], dtype=np.float32)
-        cols = _catalogue_arrays(capacity)
+        cols = [np.empty(capacity, np.float32) for _ in range(4)]  # one set per job
         keep.append((radii, cols))
         j.x, j.y, j.z = (b[k].data_ptr() for k in ("x", "y", "z"))
         j.n_particles = b["x"].numel()
