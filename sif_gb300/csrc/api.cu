@@ -891,7 +891,13 @@ static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceM
   p.inject_on_device = true;
   p.mesh_ready = mesh_ready;
   p.contrast_mean = contrast_mean;
-  HostCatalogueT<R> cat;
+  // Kept per thread between runs (cleared, capacity kept): fresh vectors would
+  // take their page faults on every run.
+  thread_local HostCatalogueT<R> cat;
+  cat.cx.clear();
+  cat.cy.clear();
+  cat.cz.clear();
+  cat.r.clear();
   if (stats) stats->clear();
   const int st = e->exodus(delta, m, p, cat, stats, &tm);
   if (st != SIF_OK) return st;
