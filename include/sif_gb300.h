@@ -428,9 +428,10 @@ typedef struct {
 } sifg_box_job_t;
 int sifg_box_batch_device(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines,
                           uint32_t* n_engines_used);
-/* Times the batch at 1, 2, 4 and 8 engines, keeps the fastest for batches of
- * this size (total particles and job count, to a factor of two) and returns
- * it in *n_engines. The catalogues do not depend on the choice. */
+/* Times the batch at 1, 2, 4 and 8 engines (each count run twice, the second
+ * run timed), keeps the fastest for batches of this size (total particles and
+ * job count, to a factor of two) and returns it in *n_engines. The catalogues
+ * do not depend on the choice. */
 int sifg_box_batch_autotune(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t* n_engines);
 /* Statistics and timings of the last run (up to max_rungs entries). */
 uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs);

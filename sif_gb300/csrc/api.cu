@@ -1165,14 +1165,18 @@ static int run_batch(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines) 
 }
 
 // Times the batch at 1, 2, 4 and 8 engines (capped by the job count) and
-// keeps the fastest for batches of this size.
+// keeps the fastest for batches of this size. Each count runs twice and the
+// second run is timed: an engine's first boxes of a size make its transform
+// plans, a cost that later batches do not pay.
 static int autotune_batch(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t* best_out) {
   uint32_t best = 1;
   double best_ms = 1e300;
   for (uint32_t k : {1u, 2u, 4u, 8u}) {
     if (k > n_jobs && k > 1) break;
+    int st = run_batch(jobs, n_jobs, k);
+    if (st != SIF_OK) return st;
     const auto t0 = std::chrono::steady_clock::now();
-    const int st = run_batch(jobs, n_jobs, k);
+    st = run_batch(jobs, n_jobs, k);
     const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (st != SIF_OK) return st;
     if (ms < best_ms) {

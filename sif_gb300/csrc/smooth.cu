@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(32 * kColWarps, 3)
 constexpr int kRowsPerCta = 16;
 constexpr uint32_t kRowSlots = 258;
 static_assert(kRowsPerCta * 512 == kBelowBlock, "a CTA's cells are one below-list block");
-__global__ void __launch_bounds__(16 * kRowsPerCta)
+__global__ void __launch_bounds__(16 * kRowsPerCta, 4)
     c2r512_rows_kernel(const float2* __restrict__ work, float* __restrict__ out,
                        const float2* __restrict__ tw, BelowList below) {
   __shared__ __align__(16) float2 buf[kRowsPerCta * kRowSlots];
@@ -486,46 +486,59 @@ __global__ void __launch_bounds__(16 * kRowsPerCta)
       dst[f] = buf[(f >> 8) * kRowSlots + (f & 255u)];
     return;
   }
-  __shared__ uint32_t ws[16 * kRowsPerCta / 32];
-  const uint32_t cell0 = (x * 512 + y0) * 512;
-  const size_t region = (size_t)blockIdx.x * (kRowsPerCta * 512);
+  // Each warp takes 512 consecutive pairs (two rows), 32 at a time: it writes
+  // them out and keeps its lanes' threshold bits (two per pair) in `bits`;
+  // the warps' totals place each warp's entries, and a second walk over the
+  // pairs with set bits writes the entries in flat order.
+  constexpr uint32_t kWarps = 16 * kRowsPerCta / 32;
+  constexpr uint32_t kWarpPairs = kRowsPerCta * 256 / kWarps;
+  static_assert(kWarpPairs == 32 * 16, "16 pairs a lane, two bits each in one word");
+  __shared__ uint32_t ws[kWarps];
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  uint32_t n_out = 0;
-  for (uint32_t f0 = 0; f0 < kRowsPerCta * 256; f0 += blockDim.x) {
-    const uint32_t f = f0 + threadIdx.x;
+  const uint32_t base = warp * kWarpPairs;
+  uint32_t bits = 0;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    const uint32_t f = base + 32u * i + lane;
     const float2 v = buf[(f >> 8) * kRowSlots + (f & 255u)];
     dst[f] = v;
-    const uint32_t bits = (v.x <= below.thr ? 1u : 0u) | (v.y <= below.thr ? 2u : 0u);
-    // The block's exclusive scan of the counts, in thread order (flat order).
-    const uint32_t c = __popc(bits);
-    uint32_t incl = c;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-      if (lane >= (unsigned)d) incl += y;
-    }
-    if (lane == 31) ws[warp] = incl;
-    __syncthreads();
-    uint32_t before = 0, total = 0;
-#pragma unroll
-    for (int w = 0; w < 16 * kRowsPerCta / 32; w++) {
-      before += w < (int)warp ? ws[w] : 0u;
-      total += ws[w];
-    }
-    __syncthreads();
-    uint32_t pos = n_out + before + incl - c;
-    if (bits & 1u) {
-      below.delta[region + pos] = v.x;
-      below.flat[region + pos] = cell0 + 2 * f;
-      pos++;
-    }
-    if (bits & 2u) {
-      below.delta[region + pos] = v.y;
-      below.flat[region + pos] = cell0 + 2 * f + 1;
-    }
-    n_out += total;
+    bits |= ((v.x <= below.thr ? 1u : 0u) | (v.y <= below.thr ? 2u : 0u)) << (2 * i);
   }
-  if (threadIdx.x == 0) below.counts[blockIdx.x] = n_out;
+  const uint32_t n_warp = __reduce_add_sync(0xffffffffu, (unsigned)__popc(bits));
+  if (lane == 0) ws[warp] = n_warp;
+  __syncthreads();
+  uint32_t pos = 0, total = 0;
+#pragma unroll
+  for (uint32_t w = 0; w < kWarps; w++) {
+    pos += w < warp ? ws[w] : 0u;
+    total += ws[w];
+  }
+  if (threadIdx.x == 0) below.counts[blockIdx.x] = total;
+  if (n_warp == 0) return;
+  const uint32_t cell0 = (x * 512 + y0) * 512;
+  const size_t region = (size_t)blockIdx.x * (kRowsPerCta * 512);
+  const uint32_t lower = (1u << lane) - 1u;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    const uint32_t b = (bits >> (2 * i)) & 3u;
+    const uint32_t mx = __ballot_sync(0xffffffffu, b & 1u), my = __ballot_sync(0xffffffffu, b & 2u);
+    if ((mx | my) == 0u) continue;
+    if (b) {
+      const uint32_t f = base + 32u * i + lane;
+      const float2 v = buf[(f >> 8) * kRowSlots + (f & 255u)];
+      uint32_t p = pos + __popc(mx & lower) + __popc(my & lower);
+      if (b & 1u) {
+        below.delta[region + p] = v.x;
+        below.flat[region + p] = cell0 + 2 * f;
+        p++;
+      }
+      if (b & 2u) {
+        below.delta[region + p] = v.y;
+        below.flat[region + p] = cell0 + 2 * f + 1;
+      }
+    }
+    pos += __popc(mx) + __popc(my);
+  }
 }
 
 // The forward transform's first pass, the R2C along z: 16 rows of 512 reals
@@ -535,7 +548,7 @@ __global__ void __launch_bounds__(16 * kRowsPerCta)
 // E[k] = (C[k] + conj C[-k]) / 2, O[k] = (C[k] - conj C[-k]) / 2i and
 // X[k] = E[k] + W512^-k O[k] for k < 256, X[256] = E[0] - O[0]. The 257 modes
 // go to the tiles (16 rows by 16 kz, 2 KB blocks).
-__global__ void __launch_bounds__(16 * kRowsPerCta)
+__global__ void __launch_bounds__(16 * kRowsPerCta, 4)
     r2c512_rows_kernel(const float* __restrict__ grid, float2* __restrict__ work,
                        const float2* __restrict__ tw, const double* __restrict__ mean) {
   __shared__ __align__(16) float2 buf[kRowsPerCta * kRowSlots];
@@ -637,9 +650,25 @@ SmootherT<R>::~SmootherT() {
 
 template <class R>
 static void destroy_plans(typename SmootherT<R>::Plans& p) {
-  cufftDestroy(p.r2c);
+  if (p.r2c) cufftDestroy(p.r2c);
   if (p.c2r) cufftDestroy(p.c2r);
   if (p.twiddles) cudaFree(p.twiddles);
+}
+
+// A plan without a work area of its own (the smoother's shared one is set
+// before it runs); `need` grows to the area it asks for.
+static cufftHandle make_plan(uint32_t n, cufftType type, size_t* need) {
+  cufftHandle h = 0;
+  SIFG_CUFFT(cufftCreate(&h));
+  size_t ws = 0;
+  const cufftResult a = cufftSetAutoAllocation(h, 0);
+  const cufftResult m = a == CUFFT_SUCCESS ? cufftMakePlan3d(h, (int)n, (int)n, (int)n, type, &ws) : a;
+  if (m != CUFFT_SUCCESS) {
+    cufftDestroy(h);
+    throw CudaError{cudaErrorUnknown, "cufftMakePlan3d"};
+  }
+  if (ws > *need) *need = ws;
+  return h;
 }
 
 template <class R>
@@ -647,6 +676,7 @@ void SmootherT<R>::release() {
   for (auto& p : plans) destroy_plans<R>(p);
   plans.clear();
   plan_r2c = plan_c2r = 0;
+  plan_work = 0;
   twiddles = nullptr;
   n = 0;
 }
@@ -655,7 +685,7 @@ template <class R>
 void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st) {
   constexpr bool dbl = sizeof(R) == 8;
   bool rebind = false;
-  if (n_ != n || !plan_r2c) {
+  if (n_ != n) {
     auto it = std::find_if(plans.begin(), plans.end(), [&](const Plans& p) { return p.n == n_; });
     if (it == plans.end()) {
       if ((int)plans.size() >= kPlanCache) {
@@ -663,7 +693,6 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
         plans.erase(plans.begin());
       }
       Plans p{n_, 0, 0};
-      SIFG_CUFFT(cufftPlan3d(&p.r2c, (int)n_, (int)n_, (int)n_, dbl ? CUFFT_D2Z : CUFFT_R2C));
       if (!dbl && own_inverse(n_)) {
         // The tables of the three-pass inverse, computed in double.
         std::vector<float2> tw(kTw512);
@@ -679,7 +708,8 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
         SIFG_CUDA(cudaMalloc(&p.twiddles, kTw512 * sizeof(float2)));
         SIFG_CUDA(cudaMemcpy(p.twiddles, tw.data(), kTw512 * sizeof(float2), cudaMemcpyHostToDevice));
       } else {
-        SIFG_CUFFT(cufftPlan3d(&p.c2r, (int)n_, (int)n_, (int)n_, dbl ? CUFFT_Z2D : CUFFT_C2R));
+        p.r2c = make_plan(n_, dbl ? CUFFT_D2Z : CUFFT_R2C, &p.work);
+        p.c2r = make_plan(n_, dbl ? CUFFT_Z2D : CUFFT_C2R, &p.work);
       }
       plans.push_back(p);
       it = plans.end() - 1;
@@ -687,12 +717,20 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
     n = n_;
     plan_r2c = it->r2c;
     plan_c2r = it->c2r;
+    plan_work = it->work;
     twiddles = it->twiddles;
-    rebind = true;  // a cached plan may be bound to another stream
+    rebind = true;  // a cached plan may be bound to another stream and area
+  }
+  if (plan_work > area.bytes) {
+    area.ensure(plan_work);
+    rebind = true;
   }
   if (rebind || st != stream) {
-    SIFG_CUFFT(cufftSetStream(plan_r2c, st));
-    if (plan_c2r) SIFG_CUFFT(cufftSetStream(plan_c2r, st));
+    for (cufftHandle h : {plan_r2c, plan_c2r}) {
+      if (!h) continue;
+      SIFG_CUFFT(cufftSetStream(h, st));
+      if (plan_work) SIFG_CUFFT(cufftSetWorkArea(h, area.ptr));
+    }
     stream = st;
   }
   box = box_;

@@ -34,16 +34,22 @@ struct SmootherT {
   R box = 0;
   int window_mode = 1;
   cudaStream_t stream = 0;
-  cufftHandle plan_r2c = 0, plan_c2r = 0;  // the plans for n
+  cufftHandle plan_r2c = 0, plan_c2r = 0;  // the plans for n (unset on the own path at 512)
   DevBuf spectrum, work, lut, win;
-  // Plans by grid size, kept between runs (destroying one frees its work
-  // area, a device-wide wait): at most kPlanCache sizes, oldest out.
-  static constexpr int kPlanCache = 8;
+  // The plans' work area, one for all of them: they run on `stream`, one at a
+  // time. A plan made with its own area would allocate it, and destroying
+  // it free it, a device-wide wait that stalls every other engine.
+  DevBuf area;
+  // Plans by grid size, kept between runs: at most kPlanCache sizes, oldest
+  // out; a batch of boxes of many sizes keeps them all.
+  static constexpr int kPlanCache = 64;
   struct Plans {
     uint32_t n;
     cufftHandle r2c, c2r;
-    void* twiddles = nullptr;  // the float form's own inverse at n = 512: its tables (c2r unset)
+    size_t work = 0;           // bytes of work area the two need
+    void* twiddles = nullptr;  // the float form's own inverse at n = 512: its tables (no plans)
   };
+  size_t plan_work = 0;  // the current plans' need
   const void* twiddles = nullptr;
   std::vector<Plans> plans;
 
