@@ -14,7 +14,8 @@
 // correction 1/sinc^2 per axis (or the aliasing-aware W/S), and by the C2R's
 // 1/N^3, reading the spectrum once and writing the transform's input once.
 // The radial factor comes from a table indexed by the integer |k|^2, built in
-// double by a small kernel, as the reference tabulates it. The unfiltered
+// double by a small kernel, as the reference tabulates it (the own inverse at
+// 512 evaluates the same formulas in float as it applies them). The unfiltered
 // pass (the grid handed back at the end of a run) applies no window, as the
 // reference's SIF__FILTER_NONE copies the spectrum untouched.
 #include <cuda_runtime.h>
@@ -265,15 +266,76 @@ constexpr int kTw512 = 1024;
 // The filter of one kx column at (ky, kz): mode kx is scaled by
 // lut[k^2] * norm * win[kx] * win[ky] * win[kz] (win optional), the factor
 // and the order of its products as the per-mode filter kernel has them.
+// The radial factor of the filter pass, evaluated where it is applied: a
+// table by |k|^2 (as the other grids use) is a gather whose lanes fall in as
+// many cache lines, and it doubled the pass's time. These are the table's
+// formulas (fft_build_filter_lut, src/math/fft.c:521-568) in float: the
+// top-hat 3 (sin x - x cos x) / x^3 by its Taylor series below x = 2, where
+// the formula cancels, and by sincosf above; the Gaussian exp(-x^2 / 2); the
+// extra Gaussian of sigma on top of either. Above x = 2 the phase x = f |k|
+// carries its rounding error as a second float (f's low part, sqrt's
+// residual, the product's error by fma), and sin and cos are corrected to
+// first order in it: a float x alone is off by up to x ulp, as much as 4e-6
+// in the factor at x = 70; with the correction the factor is within about
+// 2 ulp of the table's double value.
+struct RadialFilter {
+  int kind;         // kFilterTopHat, kFilterGaussian, else 1
+  float x2;         // x^2 per unit |k|^2: f^2, f = R 2 pi / L
+  float g2;         // the extra Gaussian's exponent per unit |k|^2: (sigma 2 pi / L)^2 / 2; 0 for none
+  float f, f_lo;    // f as a float and its remainder
+};
+
+// The series sum_{n >= 1} (-1)^(n+1) 6n x^(2n-2) / (2n+1)! of the top-hat,
+// through n = 8: the first term left out is below 3e-11 for x < 2.
+__device__ __forceinline__ float tophat_series(float x2) {
+  float p = (float)(-48.0 / 355687428096000.0);
+  p = fmaf(p, x2, (float)(42.0 / 1307674368000.0));
+  p = fmaf(p, x2, (float)(-36.0 / 6227020800.0));
+  p = fmaf(p, x2, (float)(30.0 / 39916800.0));
+  p = fmaf(p, x2, (float)(-24.0 / 362880.0));
+  p = fmaf(p, x2, (float)(18.0 / 5040.0));
+  p = fmaf(p, x2, (float)(-12.0 / 120.0));
+  return fmaf(p, x2, 1.0f);
+}
+
+__device__ __forceinline__ float radial_factor(uint32_t k2, const RadialFilter& rf) {
+  if (k2 == 0) return 1.0f;
+  const float kk = (float)k2;  // exact: k2 <= 3 * 256^2
+  float v = 1.0f;
+  if (rf.kind == kFilterTopHat) {
+    const float x2 = rf.x2 * kk;
+    if (x2 < 4.0f) {
+      v = tophat_series(x2);
+    } else {
+      const float k = sqrtf(kk);
+      const float k_lo = __fdividef(fmaf(-k, k, kk), k + k);
+      const float x = rf.f * k;
+      const float x_lo = fmaf(rf.f, k, -x) + fmaf(rf.f, k_lo, rf.f_lo * k);
+      float s, c;
+      sincosf(x, &s, &c);
+      const float sl = fmaf(c, x_lo, s);   // sin(x + x_lo)
+      const float cl = fmaf(-s, x_lo, c);  // cos(x + x_lo)
+      v = 3.0f * fmaf(-x, cl, sl) / (x2 * x);
+    }
+  } else if (rf.kind == kFilterGaussian) {
+    v = expf(-0.5f * (rf.x2 * kk));
+  }
+  if (rf.g2 > 0.0f) v *= expf(-(rf.g2 * kk));
+  return v;
+}
+
+constexpr RadialFilter kNoFilter{-1, 0.0f, 0.0f, 0.0f, 0.0f};  // a pass that applies no filter
+
 struct ColumnFilter {
-  const float* lut;
+  bool on;
+  RadialFilter rf;
   const float* win;
   float norm, wy, wz;
   uint32_t q;  // ky'^2 + kz^2
 };
 
 // One warp's inverse DFT of the 512 values in `col`, in place; with a filter
-// (f.lut set) each value is first scaled by its filter factor.
+// (f.on) each value is first scaled by its filter factor.
 // With `forward` the forward DFT instead (e^{-2 pi i jk/512}), as the
 // conjugate of the inverse DFT of the conjugate.
 __device__ __forceinline__ void ifft512_column(float2* col, const float2* __restrict__ tw,
@@ -285,21 +347,21 @@ __device__ __forceinline__ void ifft512_column(float2* col, const float2* __rest
     v[r] = col[col_slot((int)lane + 32 * r)];
     if (forward) v[r].y = -v[r].y;
   }
-  if (f.lut) {
+  if (f.on) {
     // The factor is even in kx (the window table is built from |k|): a lane
-    // reads it for its kx < 256 and takes kx > 256 from the lane holding
-    // 512 - kx, half the table reads. Lane 0 holds both kx = 32 r and
-    // 512 - 32 r itself, and alone reads kx = 256.
+    // finds it for its kx < 256 and takes kx > 256 from the lane holding
+    // 512 - kx, half the evaluations. Lane 0 holds both kx = 32 r and
+    // 512 - 32 r itself, and alone finds kx = 256.
     float lo[8];
 #pragma unroll
     for (int r = 0; r < 8; r++) {
       const uint32_t kx = lane + 32u * r;
-      lo[r] = __ldg(f.lut + kx * kx + f.q) * f.norm;
+      lo[r] = radial_factor(kx * kx + f.q, f.rf) * f.norm;
       if (f.win) lo[r] = lo[r] * __ldg(f.win + kx) * f.wy * f.wz;
     }
     float nyq = 0.f;
     if (lane == 0) {
-      nyq = __ldg(f.lut + 256u * 256u + f.q) * f.norm;
+      nyq = radial_factor(256u * 256u + f.q, f.rf) * f.norm;
       if (f.win) nyq = nyq * __ldg(f.win + 256) * f.wy * f.wz;
     }
     const unsigned partner = (32u - lane) & 31u;
@@ -368,14 +430,14 @@ struct ColumnLayout {
 
 // Passes (1) and (2): the inverse FFT along one axis of 16 neighbouring kz
 // columns of one line. The tile arrives by asynchronous copies; pass (1)
-// (lut set) reads the spectrum (line = ky, kx along the column), scales each
+// (rf.kind >= 0) reads the spectrum (line = ky, kx along the column), scales each
 // mode by its filter factor as the transform first reads it, and writes the
 // tiles; pass (2) (line = x, ky along the column) works on the tiles in
 // place. Columns past kz = 256 (in the last CTA of a line) are neither read,
 // transformed nor written.
 __global__ void __launch_bounds__(32 * kColWarps, 3)
     colfft512_kernel(const float2* src, float2* dst, ColumnLayout in, ColumnLayout out,
-                     const float* __restrict__ lut, const float* __restrict__ win, float norm,
+                     RadialFilter rf, const float* __restrict__ win, float norm,
                      const float2* __restrict__ tw, bool forward) {
   extern __shared__ float2 cols[];  // kColCols columns of kColStride slots
   constexpr uint32_t zd = 257;
@@ -397,11 +459,11 @@ __global__ void __launch_bounds__(32 * kColWarps, 3)
 #pragma unroll 1
   for (uint32_t w = warp; w < kColCols && kz0 + w < zd; w += kColWarps) {
     ColumnFilter f{};
-    if (lut) {
+    if (rf.kind >= 0) {
       const uint32_t kz = kz0 + w;
       const int32_t ks = line > 256 ? (int32_t)line - 512 : (int32_t)line;
-      f = ColumnFilter{lut, win, norm, win ? __ldg(win + line) : 1.f, win ? __ldg(win + kz) : 1.f,
-                       (uint32_t)(ks * ks) + kz * kz};
+      f = ColumnFilter{true, rf, win, norm, win ? __ldg(win + line) : 1.f,
+                       win ? __ldg(win + kz) : 1.f, (uint32_t)(ks * ks) + kz * kz};
     }
     ifft512_column(cols + w * kColStride, tw, lane, f, forward);
   }
@@ -816,18 +878,18 @@ static void launch_forward512(const SmootherT<float>& s, const float* grid, cons
       grid, s.work.as<float2>(), tw, mean);
   SIFG_LAUNCH_CHECK();
   colfft512_kernel<<<dim3(kKzBlocks, N), 32 * kColWarps, smem, s.stream>>>(
-      s.work.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByLine, nullptr, nullptr, 1.f,
+      s.work.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByLine, kNoFilter, nullptr, 1.f,
       tw, true);
   SIFG_LAUNCH_CHECK();
   colfft512_kernel<<<dim3(kKzBlocks, N), 32 * kColWarps, smem, s.stream>>>(
-      s.work.as<float2>(), s.spectrum.as<float2>(), kTilesByRow, kTilesByLine, nullptr, nullptr,
+      s.work.as<float2>(), s.spectrum.as<float2>(), kTilesByRow, kTilesByLine, kNoFilter, nullptr,
       1.f, tw, true);
   SIFG_LAUNCH_CHECK();
 }
 
 // The timer, begun by the caller, ends after pass (1): the filter's kernel.
-static void launch_inverse512(const SmootherT<float>& s, int filter, float norm, float* out,
-                              KernelTimer* timer, const BelowList& below) {
+static void launch_inverse512(const SmootherT<float>& s, int filter, const RadialFilter& rf,
+                              float norm, float* out, KernelTimer* timer, const BelowList& below) {
   constexpr uint32_t N = 512;
   const float* w = (s.window_mode && filter != kFilterNone) ? s.win.as<float>() : nullptr;
   const size_t smem = (size_t)kColCols * kColStride * sizeof(float2);
@@ -835,20 +897,20 @@ static void launch_inverse512(const SmootherT<float>& s, int filter, float norm,
   const float2* tw = (const float2*)s.twiddles;
   const dim3 grid(kKzBlocks, N);
   colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
-      s.spectrum.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByRow, s.lut.as<float>(), w,
+      s.spectrum.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByRow, rf, w,
       norm, tw, false);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(s.stream);
   colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
-      s.work.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByLine, nullptr, nullptr, 1.f,
+      s.work.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByLine, kNoFilter, nullptr, 1.f,
       tw, false);
   SIFG_LAUNCH_CHECK();
   c2r512_rows_kernel<<<N * N / kRowsPerCta, 16 * kRowsPerCta, 0, s.stream>>>(s.work.as<float2>(),
                                                                            out, tw, below);
   SIFG_LAUNCH_CHECK();
 }
-static void launch_inverse512(const SmootherT<double>&, int, double, double*, KernelTimer*,
-                              const BelowList&) {}
+static void launch_inverse512(const SmootherT<double>&, int, const RadialFilter&, double, double*,
+                              KernelTimer*, const BelowList&) {}
 
 static void launch_filter(const SmootherT<double>& s, int filter, double norm) {
   const uint64_t modes = (uint64_t)s.n * s.n * (s.n / 2 + 1);
@@ -864,15 +926,21 @@ void SmootherT<R>::smooth(int filter, R r, R sigma, R* out, KernelTimer* timer,
   const uint32_t max_k2 = 3 * h * h;
   const double factor = (double)r * 2.0 * M_PI / (double)box;
   const double gfactor = sigma > R(0) ? (double)sigma * 2.0 * M_PI / (double)box : 0.0;
+  const R norm = (R)(1.0 / ((double)n * n * n));
+  if (twiddles) {
+    // The own inverse evaluates the radial factor as it applies it: no table.
+    const float f = (float)factor;
+    const RadialFilter rf{filter == kFilterTopHat || filter == kFilterGaussian ? filter : kFilterNone,
+                          (float)(factor * factor), (float)(0.5 * gfactor * gfactor), f,
+                          (float)(factor - (double)f)};
+    if (timer) timer->begin(stream);
+    launch_inverse512(*this, filter, rf, norm, out, timer, below ? *below : BelowList{});
+    return;
+  }
   lut_kernel<R><<<grid_for((uint64_t)max_k2 + 1, 256), 256, 0, stream>>>(lut.as<R>(), max_k2, filter,
                                                                          factor, gfactor);
   SIFG_LAUNCH_CHECK();
-  const R norm = (R)(1.0 / ((double)n * n * n));
   if (timer) timer->begin(stream);
-  if (twiddles) {
-    launch_inverse512(*this, filter, norm, out, timer, below ? *below : BelowList{});
-    return;
-  }
   launch_filter(*this, filter, norm);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(stream);
