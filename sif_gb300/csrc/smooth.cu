@@ -271,19 +271,52 @@ constexpr int kTw512 = 1024;
 // many cache lines, and it doubled the pass's time. These are the table's
 // formulas (fft_build_filter_lut, src/math/fft.c:521-568) in float: the
 // top-hat 3 (sin x - x cos x) / x^3 by its Taylor series below x = 2, where
-// the formula cancels, and by sincosf above; the Gaussian exp(-x^2 / 2); the
-// extra Gaussian of sigma on top of either. Above x = 2 the phase x = f |k|
-// carries its rounding error as a second float (f's low part, sqrt's
-// residual, the product's error by fma), and sin and cos are corrected to
-// first order in it: a float x alone is off by up to x ulp, as much as 4e-6
-// in the factor at x = 70; with the correction the factor is within about
-// 2 ulp of the table's double value.
+// the formula cancels, and through sin and cos above; the Gaussian
+// exp(-x^2 / 2); the extra Gaussian of sigma on top of either. Above x = 2
+// the phase x = f |k| carries its rounding error as a second float (f's low
+// part, the square root's residual, the product's error by fma): a float x
+// alone is off by up to x ulp, as much as 4e-6 in the factor at x = 70. sin
+// and cos of that pair come from a reduction by pi/2 (Cody and Waite: pi/2 in
+// three parts, the first two of 12 significant bits so that n times them is
+// exact, the pair's low part added to the remainder) and Taylor series on
+// [-pi/4, pi/4] (to x^9 and x^10: the first term left out is below 2e-10);
+// within 1.5 ulp. The factor is then within about 4 ulp of the table's
+// double value (2e-7 rms relative over the modes above x = 2).
 struct RadialFilter {
   int kind;         // kFilterTopHat, kFilterGaussian, else 1
   float x2;         // x^2 per unit |k|^2: f^2, f = R 2 pi / L
   float g2;         // the extra Gaussian's exponent per unit |k|^2: (sigma 2 pi / L)^2 / 2; 0 for none
   float f, f_lo;    // f as a float and its remainder
 };
+
+// sin and cos of x + x_lo (|x_lo| below an ulp of x, 0 < x < 4096 pi / 2).
+__device__ __forceinline__ void sincos_pair(float x, float x_lo, float& s, float& c) {
+  constexpr float kP1 = 1.57080078125f;             // pi/2 to 12 bits
+  constexpr float kP2 = -4.4535845518112183e-06f;   // the remainder to 12 bits
+  constexpr float kP3 = (float)(1.57079632679489661923 - 1.57080078125 + 4.4535845518112183e-06);
+  const float n = rintf(x * (float)(2.0 / 3.14159265358979323846));
+  float r = fmaf(-n, kP1, x);  // exact: n kP1 has 24 bits and lies within a factor 2 of x
+  r = fmaf(-n, kP2, r);
+  r = fmaf(-n, kP3, r) + x_lo;
+  const float r2 = r * r;
+  float ps = (float)(1.0 / 362880.0);
+  ps = fmaf(ps, r2, (float)(-1.0 / 5040.0));
+  ps = fmaf(ps, r2, (float)(1.0 / 120.0));
+  ps = fmaf(ps, r2, (float)(-1.0 / 6.0));
+  const float sr = fmaf(ps * r2, r, r);
+  float pc = (float)(-1.0 / 3628800.0);
+  pc = fmaf(pc, r2, (float)(1.0 / 40320.0));
+  pc = fmaf(pc, r2, (float)(-1.0 / 720.0));
+  pc = fmaf(pc, r2, (float)(1.0 / 24.0));
+  pc = fmaf(pc, r2, -0.5f);
+  const float cr = fmaf(pc, r2, 1.0f);
+  // x = n pi/2 + r: quadrant q of n turns (sin r, cos r) by q quarter turns.
+  const int q = (int)n & 3;
+  s = (q & 1) ? cr : sr;
+  c = (q & 1) ? sr : cr;
+  if (q & 2) s = -s;
+  if ((q + 1) & 2) c = -c;
+}
 
 // The series sum_{n >= 1} (-1)^(n+1) 6n x^(2n-2) / (2n+1)! of the top-hat,
 // through n = 8: the first term left out is below 3e-11 for x < 2.
@@ -307,15 +340,17 @@ __device__ __forceinline__ float radial_factor(uint32_t k2, const RadialFilter& 
     if (x2 < 4.0f) {
       v = tophat_series(x2);
     } else {
-      const float k = sqrtf(kk);
-      const float k_lo = __fdividef(fmaf(-k, k, kk), k + k);
+      // |k| as k + k_lo: a reciprocal square root, and the residual's
+      // first-order correction (exact to well below an ulp whatever the
+      // reciprocal's own error).
+      const float y = rsqrtf(kk);
+      const float k = kk * y;
+      const float k_lo = fmaf(-k, k, kk) * (0.5f * y);
       const float x = rf.f * k;
       const float x_lo = fmaf(rf.f, k, -x) + fmaf(rf.f, k_lo, rf.f_lo * k);
       float s, c;
-      sincosf(x, &s, &c);
-      const float sl = fmaf(c, x_lo, s);   // sin(x + x_lo)
-      const float cl = fmaf(-s, x_lo, c);  // cos(x + x_lo)
-      v = 3.0f * fmaf(-x, cl, sl) / (x2 * x);
+      sincos_pair(x, x_lo, s, c);
+      v = 3.0f * fmaf(-x, c, s) * __frcp_rn(x2 * x);
     }
   } else if (rf.kind == kFilterGaussian) {
     v = expf(-0.5f * (rf.x2 * kk));
