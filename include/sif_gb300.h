@@ -447,6 +447,13 @@ void sifg_set_window(int bins);
 /* Which sphere-growth kernel runs: 0 (default) by the survivor count, 1 a
  * CTA per survivor, 2 a warp per survivor. The radii do not depend on it. */
 void sifg_set_growth_mode(int mode);
+/* The warp-per-survivor growth keeps the distances its windows can collect
+ * in a list in shared memory, so that a window need not read the particles
+ * again: -1 (default) a list sized per rung from the shell's expected
+ * particle count (none for the large spheres of the early rungs), 0 no list,
+ * n > 0 a list of n entries (rounded up to 32, at most 512) on every rung.
+ * The radii do not depend on it. */
+void sifg_set_shell_list(int entries);
 /* How the commit's rounds run: 0 (default) all in one cooperative launch
  * where the device allows it, 1 a kernel launch per round. The catalogue
  * does not depend on it. */

@@ -44,7 +44,7 @@ EXPORTED = [
     # device-resident additions
     "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
     "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
-    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
+    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
     "sifg_mesh_device_noalloc",
     # the FP64 form
     "sifg_cic_device_f64", "sifg_contrast_device_f64", "sifg_mesh_device_f64",
@@ -92,6 +92,7 @@ def load():
         "sifg_last_timings": (None, [C.POINTER(Timings)]),
         "sifg_set_window": (None, [i32]),
         "sifg_set_growth_mode": (None, [i32]),
+        "sifg_set_shell_list": (None, [i32]),
         "sifg_set_commit_mode": (None, [i32]),
         "sifg_set_scan_mode": (None, [i32]),
         "sifg_stream": (u64, []),

@@ -1327,6 +1327,7 @@ uint64_t sifg_stream(void) {
 }
 
 void sifg_set_growth_mode(int mode) { set_growth_mode(mode < 0 || mode > 2 ? 0 : mode); }
+void sifg_set_shell_list(int entries) { set_shell_list(entries < 0 ? -1 : entries); }
 void sifg_set_commit_mode(int mode) { set_commit_mode(mode == 1 ? 1 : 0); }
 void sifg_set_scan_mode(int mode) { set_scan_mode(mode == 1 ? 1 : 0); }
 

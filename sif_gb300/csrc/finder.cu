@@ -716,8 +716,8 @@ __device__ void bitonic_sort(R* buf, uint32_t p) {
 // The cells of the template a warp walks, 32 at a time: `want(type, i)` says
 // whether a cell's range is looked up, `whole(type, count)` is then called on
 // the lane holding it (for counts), `particles(type)` whether its particles
-// are read, and `each(type, d2, p)` runs per particle read. `visited` and
-// `read` count the lookups and the particles.
+// are read, and `each(type, d2, p, i)` runs per particle read (i: its cell's
+// template index). `visited` and `read` count the lookups and the particles.
 template <class R, class Want, class Whole, class Particles, class Each>
 __device__ __forceinline__ void walk_cells(const MeshViewT<R>& mesh, const TemplateViewT<R>& tpl,
                                            int32_t ci, int32_t cj, int32_t ck, R cx, R cy,
@@ -799,7 +799,8 @@ __device__ __forceinline__ void walk_cells(const MeshViewT<R>& mesh, const Templ
         const R qy = __shfl_sync(0xffffffffu, c.ey, own[u]);
         const R qz = __shfl_sync(0xffffffffu, c.ez, own[u]);
         const uint8_t t = (uint8_t)__shfl_sync(0xffffffffu, (int)type, own[u]);
-        if (pp[u] != 0xffffffffu) each(t, dist2(px[u], py[u], pz[u], qx, qy, qz), pp[u]);
+        if (pp[u] != 0xffffffffu)
+          each(t, dist2(px[u], py[u], pz[u], qx, qy, qz), pp[u], c0 + (uint32_t)own[u]);
       }
     }
   }
@@ -857,7 +858,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
           }
         },
         [](uint8_t type) { return type == kCellStraddle || type == kCellEdge; },
-        [&](uint8_t, R d2, uint32_t) {
+        [&](uint8_t, R d2, uint32_t, uint32_t) {
           if (d2 <= rc.rs2) within++;
           if (d2 <= rc.rc2) {
             n_core++;
@@ -880,7 +881,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
           mesh, tpl, ci, cj, ck, cx, cy, cz,
           [](uint8_t type, uint32_t) { return type == kCellShell; }, [](uint8_t, uint32_t) {},
           [](uint8_t) { return true; },
-          [&](uint8_t, R d2, uint32_t) {
+          [&](uint8_t, R d2, uint32_t, uint32_t) {
             atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
           },
           visited, read);
@@ -950,7 +951,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
                        !(__ldg(tpl.min_d2 + i) > hi);
               },
               [](uint8_t, uint32_t) {}, [](uint8_t) { return true; },
-              [&](uint8_t type, R d2, uint32_t) {
+              [&](uint8_t type, R d2, uint32_t, uint32_t) {
                 if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) return;
                 const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
                 if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) return;
@@ -1047,23 +1048,50 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
 // registers. A survivor whose window is wider is left kRescalePending for the
 // per-CTA kernel. Every count, bin and test is the per-CTA kernel's, so the
 // radius is the same bits.
+//
+// With shell_cap > 0 the warp also keeps, as the first two walks meet them,
+// the distances of the particles the windows can collect -- the boundary
+// cells' particles inside the shell and every particle of the shell cells --
+// with their cells' template indices, up to shell_cap of them. A window then
+// takes its distances from that list, with the walk's own cell test (the
+// cell's bounds against the window) and bin test: the same distances as a
+// walk over the cells, without reading a particle again. A survivor with
+// more is resolved by walks, as without the list.
 constexpr int kWarpSort = 256;
+
+// Bytes of one warp's slice: bins, prefix, the window's distances, two
+// counters (and padding), the shell list's distances and template indices.
+template <class R>
+__host__ __device__ constexpr size_t warp_slice_bytes(uint32_t nb_stride, uint32_t shell_cap) {
+  return 2 * (size_t)nb_stride * sizeof(uint32_t) + kWarpSort * sizeof(R) + 16 +
+         (size_t)shell_cap * (sizeof(R) + sizeof(uint32_t));
+}
 
 template <class R>
 __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mesh,
                                                              TemplateViewT<R> tpl,
                                                              RungConstsT<R> rc, SurvivorsT<R> sv,
-                                                             uint32_t nb_stride,
+                                                             uint32_t nb_stride, uint32_t shell_cap,
                                                              unsigned long long* __restrict__ traffic) {
   extern __shared__ unsigned char warp_smem[];
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  // Per warp: bins[nb_stride], below[nb_stride], the window's distances, its count.
-  const size_t per_warp = 2 * (size_t)nb_stride * sizeof(uint32_t) + kWarpSort * sizeof(R) + 16;
-  unsigned char* base = warp_smem + warp * per_warp;
+  unsigned char* base = warp_smem + warp * warp_slice_bytes<R>(nb_stride, shell_cap);
   uint32_t* bins = (uint32_t*)base;
   uint32_t* below = bins + nb_stride;
   R* wbuf = (R*)(below + nb_stride);
   uint32_t* collected = (uint32_t*)(wbuf + kWarpSort);
+  uint32_t* listed = collected + 1;  // entries offered to the shell list (may pass shell_cap)
+  R* sd2 = (R*)(collected + 16 / sizeof(uint32_t));
+  uint32_t* scell = (uint32_t*)(sd2 + shell_cap);
+  // One entry of the shell list, for as long as there is room.
+  auto keep = [&](R d2, uint32_t cell) {
+    if (shell_cap == 0) return;
+    const uint32_t slot = atomicAdd(listed, 1u);
+    if (slot < shell_cap) {
+      sd2[slot] = d2;
+      scell[slot] = cell;
+    }
+  };
   const uint32_t n_surv = *sv.count;
   const uint32_t warps = gridDim.x * kGrowWarps;
   for (uint32_t s = blockIdx.x * kGrowWarps + warp; s < n_surv; s += warps) {
@@ -1074,6 +1102,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
     R radius = -1.0f;
     unsigned long long read = 0, visited = 0;
     for (uint32_t b = lane; b < rc.nb; b += 32) bins[b] = 0;
+    if (lane == 0) *listed = 0;
     __syncwarp();
     // 1. Early refusal and the boundary cells' share of the histogram.
     unsigned long long within = 0, n_core = 0, n_shell = 0;
@@ -1089,13 +1118,14 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
           }
         },
         [](uint8_t type) { return type == kCellStraddle || type == kCellEdge; },
-        [&](uint8_t, R d2, uint32_t) {
+        [&](uint8_t, R d2, uint32_t, uint32_t cell) {
           if (d2 <= rc.rs2) within++;
           if (d2 <= rc.rc2) {
             n_core++;
           } else if (d2 <= rc.rs2) {
             atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
             n_shell++;
+            keep(d2, cell);
           }
         },
         visited, read, true);
@@ -1111,8 +1141,9 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
           mesh, tpl, ci, cj, ck, cx, cy, cz,
           [](uint8_t type, uint32_t) { return type == kCellShell; }, [](uint8_t, uint32_t) {},
           [](uint8_t) { return true; },
-          [&](uint8_t, R d2, uint32_t) {
+          [&](uint8_t, R d2, uint32_t, uint32_t cell) {
             atomicAdd(bins + bin_of(d2, rc.rc2, rc.inv_w, rc.nb), 1u);
+            keep(d2, cell);
           },
           visited, read, true);
       n_core = __reduce_add_sync(0xffffffffu, (unsigned)n_core);
@@ -1164,21 +1195,37 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
           const R hi = bin_hi(rc, b_hi);
           if (lane == 0) *collected = 0;
           __syncwarp();
-          walk_cells(
-              mesh, tpl, ci, cj, ck, cx, cy, cz,
-              [&](uint8_t type, uint32_t i) {
-                return type != kCellCore && !(__ldg(tpl.max_d2 + i) < lo) &&
-                       !(__ldg(tpl.min_d2 + i) > hi);
-              },
-              [](uint8_t, uint32_t) {}, [](uint8_t) { return true; },
-              [&](uint8_t type, R d2, uint32_t) {
-                if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) return;
-                const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
-                if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) return;
-                const uint32_t slot = atomicAdd(collected, 1u);
-                if (slot < (uint32_t)kWarpSort) wbuf[slot] = d2;
-              },
-              visited, read, true);
+          const uint32_t n_listed = *listed;
+          if (shell_cap > 0 && n_listed <= shell_cap) {
+            // From the shell list: its entries are the particles the walk
+            // below reads and keeps (shell cells whole, the others' inside
+            // the shell), so the same cell and bin tests leave the same set.
+            for (uint32_t e = lane; e < n_listed; e += 32) {
+              const uint32_t i = scell[e];
+              if (__ldg(tpl.max_d2 + i) < lo || __ldg(tpl.min_d2 + i) > hi) continue;
+              const R d2 = sd2[e];
+              const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
+              if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) continue;
+              const uint32_t slot = atomicAdd(collected, 1u);
+              if (slot < (uint32_t)kWarpSort) wbuf[slot] = d2;
+            }
+          } else {
+            walk_cells(
+                mesh, tpl, ci, cj, ck, cx, cy, cz,
+                [&](uint8_t type, uint32_t i) {
+                  return type != kCellCore && !(__ldg(tpl.max_d2 + i) < lo) &&
+                         !(__ldg(tpl.min_d2 + i) > hi);
+                },
+                [](uint8_t, uint32_t) {}, [](uint8_t) { return true; },
+                [&](uint8_t type, R d2, uint32_t, uint32_t) {
+                  if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) return;
+                  const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
+                  if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) return;
+                  const uint32_t slot = atomicAdd(collected, 1u);
+                  if (slot < (uint32_t)kWarpSort) wbuf[slot] = d2;
+                },
+                visited, read, true);
+          }
           __syncwarp();
           const uint32_t m = *collected;  // = top - below[b_lo] <= kWarpSort
           R v[8];
@@ -1232,10 +1279,13 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
 
 static int g_growth_mode = 0;
 void set_growth_mode(int mode) { g_growth_mode = mode; }
+static int g_shell_list = -1;
+void set_shell_list(int entries) { g_shell_list = entries; }
 
 // A warp per survivor pays once survivors outnumber the CTAs the per-CTA
 // kernel keeps resident several times over.
 constexpr uint32_t kWarpGrowthMin = 2048;
+constexpr uint32_t kShellListMax = 512;  // entries of a warp's shell list, at most (4 CTAs an SM)
 
 template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s, uint32_t max_survivors,
@@ -1247,8 +1297,20 @@ void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT
   if (timer) timer->begin(st);
   if (by_warp) {
     const uint32_t nb_stride = (rc.nb + 31) & ~31u;
-    const size_t per_warp = 2 * (size_t)nb_stride * sizeof(uint32_t) + kWarpSort * sizeof(R) + 16;
-    const size_t smem = per_warp * kGrowWarps;
+    // The shell list: room for the particles a shell of the mean density
+    // holds (and 64), at most kShellListMax, where that shell holds at most
+    // twice kShellListMax -- survivors sit in voids, and most of their shells
+    // hold well under the mean; none for the larger spheres of the early
+    // rungs, whose lists would overflow and only cost occupancy.
+    const double rr = (double)rc.rc2 / (double)rc.rs2;
+    const double shell = (double)rc.expected * (1.0 - rr * std::sqrt(rr));
+    uint32_t shell_cap =
+        shell <= 2.0 * kShellListMax
+            ? std::min<uint32_t>(kShellListMax, ((uint32_t)shell + 64u + 31u) & ~31u)
+            : 0u;
+    if (g_shell_list >= 0)
+      shell_cap = std::min<uint32_t>(kShellListMax, ((uint32_t)g_shell_list + 31u) & ~31u);
+    const size_t smem = warp_slice_bytes<R>(nb_stride, shell_cap) * kGrowWarps;
     thread_local size_t attr_bytes = 0;  // the attribute is per thread's view of the function
     if (smem > attr_bytes) {
       SIFG_CUDA(cudaFuncSetAttribute(growth_warp_kernel<R>,
@@ -1260,7 +1322,8 @@ void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT
     const uint32_t warps_needed = (max_survivors + kGrowWarps - 1) / kGrowWarps;
     const uint32_t cap = 152u * (uint32_t)std::max(per_sm, 1);
     growth_warp_kernel<R><<<std::min(warps_needed, cap), kGrowT, smem, st>>>(mesh, tpl, rc, s,
-                                                                            nb_stride, traffic);
+                                                                            nb_stride, shell_cap,
+                                                                            traffic);
     SIFG_LAUNCH_CHECK();
     // The survivors whose windows were too wide for a warp.
     growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, true);

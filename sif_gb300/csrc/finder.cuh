@@ -180,6 +180,10 @@ void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT
 // few, a warp per survivor for many), 1 always a CTA, 2 always a warp. The
 // radii are the same either way (tests run both).
 void set_growth_mode(int mode);
+// The warp growth kernel's shell list: -1 sized per rung from the shell's
+// expected count (none for large spheres), 0 none, n > 0 that many entries
+// (rounded up to 32, at most 512) on every rung. The radii are the same.
+void set_shell_list(int entries);
 
 // The survivor hash for the commit.
 template <class R>

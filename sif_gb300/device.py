@@ -176,6 +176,11 @@ def set_growth_mode(mode):
     _lib.load().sifg_set_growth_mode(int(mode))
 
 
+def set_shell_list(entries):
+    """The warp growth's shell list: -1 sized per rung, 0 none, n entries."""
+    _lib.load().sifg_set_shell_list(int(entries))
+
+
 def set_commit_mode(mode):
     """0 the commit's rounds in one cooperative launch, 1 a launch per round."""
     _lib.load().sifg_set_commit_mode(int(mode))

@@ -203,6 +203,24 @@ def test_catalogue_matches_reference_golden_either_growth_kernel(dev, golden_box
     test_catalogue_matches_reference_golden(dev, golden_box32, name)
 
 
+@pytest.fixture(params=[-1, 0, 64, 512], ids=["list_auto", "list_none", "list_64", "list_512"])
+def shell_list(request, dev):
+    """The warp growth's shell list sized per rung, absent, small (most
+    survivors walk again), and at its largest; back to automatic after."""
+    dev.set_growth_mode(2)
+    dev.set_shell_list(request.param)
+    yield request.param
+    dev.set_shell_list(-1)
+    dev.set_growth_mode(0)
+
+
+@pytest.mark.parametrize("name", ["default", "search_2_00", "lagrangian", "overlap_0_5"])
+def test_catalogue_matches_reference_golden_any_shell_list(dev, golden_box32, shell_list, name):
+    """A window's distances from the shell list or from a walk over the
+    cells: the same catalogue, bit for bit."""
+    test_catalogue_matches_reference_golden(dev, golden_box32, name)
+
+
 @pytest.fixture(params=[0, 1], ids=["one_launch", "launch_per_round"])
 def commit_mode(request, dev):
     """The commit's rounds in one cooperative launch, then a launch per round."""
