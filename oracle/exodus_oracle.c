@@ -1119,8 +1119,12 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   if (!(threshold > -1.0f && threshold < 0.0f) || !(f >= 0.0f && f <= 1.0f) ||
       n_radii == 0 || mesh->box_length != box)
     return -2;
-  if (opt & ((3u << 19) | (1u << 21) | (1u << 22)))
-    return -5; /* refinement, extended reach, displacement */
+  if (opt & ((3u << 19) | (1u << 22)))
+    return -5; /* refinement, displacement */
+  /* SIF_FINDER_EXTEND_REACH (exodus_finder.c:1664-1702, 2060-2072): a
+   * crossing past the rung's reach is measured again at the levels of an
+   * extended reach, from the first level EXT_SLACK past the rung's own. */
+  const int extend_reach = (opt & (1u << 21)) != 0;
   /* SIF_FINDER_SEEDS_MINIMA without refinement: the candidates are the
    * below-threshold, unmasked nodes that are local minima of the rung's field
    * (sif__finder_scan_refined with minima_only, utils.c:406-552); nothing
@@ -1145,6 +1149,36 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   const float vol_factor = (4.0f / 3.0f) * PI_F * mean_density;
 
   int n_threads = p->n_threads > 0 ? p->n_threads : 1;
+
+  /* The extended reach's levels (exodus_finder.c:1675-1702, 242-244, 1342-
+   * 1353): from the top rung's reach down by EXT_GROWTH to below the bottom
+   * rung, level k measuring [ext_rmin[k], ext_reach[k]] with template etpl[k]. */
+  enum { EXT_MAX_LEVELS = 32 };
+  const float EXT_GROWTH = 1.5f, EXT_SLACK = 1.2f;
+  uint32_t n_ext = 0;
+  float ext_reach[EXT_MAX_LEVELS], ext_rmin[EXT_MAX_LEVELS];
+  orc_template_t etpl[EXT_MAX_LEVELS];
+  memset(etpl, 0, sizeof(etpl));
+  if (extend_reach) {
+    const float r_ext = radii[0] + fmaxf((search_factor - 1.0f) * radii[0], 3.0f * cell);
+    const float r_low = radii[n_radii - 1];
+    while (n_ext < EXT_MAX_LEVELS &&
+           (n_ext == 0 || r_ext / powf(EXT_GROWTH, (float)(n_ext - 1)) > r_low))
+      n_ext++;
+    for (uint32_t k = 0; k < n_ext; k++)
+      ext_reach[k] = r_ext / powf(EXT_GROWTH, (float)(n_ext - 1 - k));
+    for (uint32_t k = 0; k < n_ext; k++) {
+      ext_rmin[k] = (k ? ext_reach[k - 1] : ext_reach[0] / EXT_GROWTH) / EXT_SLACK;
+      if (orc_template_build(&etpl[k], mesh->n_cells, mesh->cell_length, ext_rmin[k],
+            ext_reach[k])) {
+        for (uint32_t j = 0; j < k; j++)
+          orc_template_free(&etpl[j]);
+        free(radii);
+        return -3;
+      }
+    }
+  }
+
   uint64_t* mask = calloc((total + 63) / 64, sizeof(uint64_t));
   float* field = malloc(total * sizeof(float));
   voids_t V;
@@ -1195,6 +1229,13 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
     }
     const int32_t proxy_pole = (int32_t)(scale * radius * (1.0f - f) / cell) - 1;
     const float rc2 = rmin * rmin;
+    /* The first level of the extended reach this rung enters (1826-1832). */
+    uint32_t ext0 = n_ext;
+    for (uint32_t e = 0; e < n_ext && ext0 == n_ext; e++)
+      if (ext_reach[e] >= EXT_SLACK * r_search)
+        ext0 = e;
+    if (ext0 == n_ext && n_ext > 0 && ext_reach[n_ext - 1] > r_search)
+      ext0 = n_ext - 1;
 
     /* prefilter_cells, src/finder/exodus_finder.c:871-944 (order kept). */
     {
@@ -1282,6 +1323,14 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
           vol_factor, rmin, window, &reason, &ss, &sc);
         span_sum += ss;
         span_count += sc;
+        for (uint32_t e = ext0; e < n_ext && r->r < 0.0f && reason == ORC_RESCALE_BEYOND_SEARCH;
+             e++) {
+          ss = sc = 0;
+          r->r = orc_find_radius(mesh, &etpl[e], r->cx, r->cy, r->cz, ext_reach[e], threshold,
+            vol_factor, ext_rmin[e], window, &reason, &ss, &sc);
+          span_sum += ss;
+          span_count += sc;
+        }
         r->status = r->r < 0.0f ? ST_RESCALE : ST_ACCEPTED;
       }
 
@@ -1351,6 +1400,8 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
       stats_out[ri] = st;
   }
 
+  for (uint32_t k = 0; k < n_ext; k++)
+    orc_template_free(&etpl[k]);
   free(bidx);
   free(res);
   free(cand);

@@ -36,6 +36,19 @@ def golden_box32_f64():
 
 
 @pytest.fixture(scope="session")
+def golden_box32_extend():
+    """The same positions at threshold -0.3 and ladder(4, 8): catalogues with
+    and without SIF_FINDER_EXTEND_REACH."""
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32_extend.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_box32_extend_f64():
+    """The extended-reach box through the reference's SIF_USE_DOUBLE build."""
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32_extend_f64.npz")))
+
+
+@pytest.fixture(scope="session")
 def gpu_lib():
     """The built GB300 library, initialised on the GPU."""
     import torch

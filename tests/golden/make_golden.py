@@ -17,6 +17,14 @@ golden_box32_f64.npz -- the same box through the reference's SIF_USE_DOUBLE
   build (sif_real = double): the float positions moved by a seeded jitter of
   up to 1e-4 so that they need double precision, and the same records in
   double (density, contrast, mesh, 12 captured fields, catalogues).
+
+golden_box32_extend.npz, golden_box32_extend_f64.npz -- the same positions
+  (the f64 file with the same jitter) at a shallow threshold, -0.3, and the
+  ladder(4, 8, 0.1) (8 rungs), where SIF_FINDER_EXTEND_REACH changes the
+  catalogue: with minima seeds and an overlap fraction of 1 (the
+  excursion-peak preset less its displacement) it changes 61 of 355 radii.
+  The contrast, the mesh, the 8 fields the reference's own run smoothed, and
+  its catalogues with and without the extended reach.
 """
 import os
 import sys
@@ -119,6 +127,63 @@ def make_box32_f64(path):
     print(f"{path}: {len(cat[0])} voids over {len(radii)} rungs")
 
 
+# The extended reach's box: BOX32's positions at a shallow threshold and a
+# short ladder, and the option sets that differ by SIF_FINDER_EXTEND_REACH.
+EXTEND = dict(BOX32, threshold=-0.3, r0=4.0, top=2.0)
+EXTEND_SETS = [
+    ("minima_f1", 1.0, abi.SIF_FINDER_SEEDS_MINIMA),
+    ("extend_minima_f1", 1.0, abi.SIF_FINDER_SEEDS_MINIMA | abi.SIF_FINDER_EXTEND_REACH),
+    ("extend_f1", 1.0, abi.SIF_FINDER_EXTEND_REACH),
+    ("extend", 0.0, abi.SIF_FINDER_EXTEND_REACH),
+]
+
+
+def make_box32_extend(path, v="strict"):
+    p = EXTEND
+    x, y, z = synth.zeldovich(p["n"], p["box"], p["rms_disp"], p["seed"])
+    real = np.float32
+    if v == "f64":
+        rng = np.random.default_rng(p["seed"] + 1000)  # BOX32's f64 jitter
+
+        def jitter(a):
+            w = a.astype(np.float64) + rng.uniform(-1e-4, 1e-4, a.shape)
+            w = np.where(w < 0.0, w + p["box"], w)
+            return np.where(w >= p["box"], w - p["box"], w)
+
+        x, y, z = jitter(x), jitter(y), jitter(z)
+        real = np.float64
+    radii = synth.ladder(p["r0"], p["top"] * p["r0"], 0.1).astype(real)
+    lib = R.load(v, 4, abi.SIF_LOG_LEVEL_ERROR)
+    kw = dict(variant=v) if v == "f64" else {}
+    f = R.RefField(lib, x, y, z, **kw)
+    g = R.RefGrid(lib, p["n"], p["box"], **kw)
+    g.assign_cic(f)
+    g.to_contrast()
+    delta = g.values()
+    m = R.RefMesh(lib, p["mesh"], p["box"], f)
+    mx, my, mz, offs, idx = m.arrays(**kw)
+    fields = np.zeros((len(radii), p["n"] ** 3), real)
+    R.exodus_raw(lib, g, m, radii, p["threshold"], capture=fields, **kw)
+    out = dict(x=x, y=y, z=z, radii=radii, delta=delta, mesh_x=mx, mesh_y=my, mesh_z=mz,
+               mesh_offsets=offs, mesh_index=idx, fields=fields,
+               params=np.array([p["n"], p["box"], p["rms_disp"], p["seed"], p["r0"],
+                                p["threshold"], p["mesh"]], np.float64))
+    for name, overlap, opt in EXTEND_SETS:
+        c = R.exodus_raw(lib, g, m, radii, p["threshold"], overlap, opt, inject=fields, **kw)
+        for k, col in zip(("cx", "cy", "cz", "r"), c):
+            out[f"cat_{name}_{k}"] = col
+        out[f"cat_{name}_opt"] = np.array([overlap, opt], np.float64)
+    a, b = out["cat_minima_f1_r"], out["cat_extend_minima_f1_r"]
+    assert len(a) != len(b) or not np.array_equal(a, b), "the extended reach changes nothing here"
+    m.free()
+    g.free()
+    f.free()
+    np.savez_compressed(path, **out)
+    print(f"{path}: " + ", ".join(f"{n} {len(out[f'cat_{n}_r'])}" for n, _, _ in EXTEND_SETS))
+
+
 if __name__ == "__main__":
     make_box32(os.path.join(HERE, "golden_box32.npz"))
     make_box32_f64(os.path.join(HERE, "golden_box32_f64.npz"))
+    make_box32_extend(os.path.join(HERE, "golden_box32_extend.npz"))
+    make_box32_extend(os.path.join(HERE, "golden_box32_extend_f64.npz"), "f64")

@@ -54,6 +54,24 @@ def test_oracle_catalogue_matches_golden(oracle, golden_box32, name):
     assert same_catalogue(cat, want)
 
 
+EXTEND_SETS = ["minima_f1", "extend_minima_f1", "extend_f1", "extend"]
+
+
+@pytest.mark.parametrize("name", EXTEND_SETS)
+def test_oracle_catalogue_matches_golden_extended_reach(oracle, golden_box32_extend, name):
+    """SIF_FINDER_EXTEND_REACH (src/finder/exodus_finder.c:1664-1702,
+    2060-2072): a crossing past the rung's reach measured at the levels of an
+    extended reach; the reference's catalogues on its own fields, with and
+    without it (they differ: the fixture is made where they do)."""
+    test_oracle_catalogue_matches_golden(oracle, golden_box32_extend, name)
+
+
+def test_extended_reach_golden_differs_from_the_plain_run(golden_box32_extend):
+    g = golden_box32_extend
+    a, b = g["cat_minima_f1_r"], g["cat_extend_minima_f1_r"]
+    assert len(a) != len(b) or not np.array_equal(a, b)
+
+
 @pytest.mark.parametrize("window", [1, 3, 64])
 def test_oracle_catalogue_window_invariant(oracle, golden_box32, window):
     """The resolve window changes how bins are grouped, never the answer
