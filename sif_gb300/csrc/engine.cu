@@ -442,12 +442,12 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const R cell = box / (R)N;
   const R threshold = p.threshold, f = p.overlap;
   const uint32_t opt = p.options;
-  if (opt & (kOptRefineMask | kOptExtendReach | kOptDisplace)) {
+  if (opt & (kOptRefineMask | kOptDisplace)) {
     set_error(kErrUnsupported,
-              "options: centre refinement, extended reach and displacement are not supported by "
-              "the GPU finder");
+              "options: centre refinement and displacement are not supported by the GPU finder");
     return kErrUnsupported;
   }
+  const bool extend = (opt & kOptExtendReach) != 0;
   if (cells >= (1ull << 32)) {
     set_error(kErrRange, "grid: more than 2^32 cells");
     return kErrRange;
@@ -555,6 +555,89 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
                   mesh.offsets,    (int32_t)mesh.n_cells, mesh.box_length,
                   1.0f / mesh.cell_length, mesh.xyzw};
 
+  // The sphere growth's constants for a search shell [rmin, r_search]
+  // (exodus_rescale.c:681-720, 894-908), on top of the rung's own.
+  auto shell_consts = [&](RungConstsT<R> rc, R rmin, R r_search) {
+    rc.r_search = r_search;
+    rc.rmin = rmin;
+    rc.rs2 = r_search * r_search;
+    rc.rc2 = rmin * rmin;
+    const R span = rc.rs2 - rc.rc2;
+    uint32_t nb = 2048u;
+    const R expected_shell = vol_factor * (r_search * r_search * r_search - rmin * rmin * rmin);
+    const R want = expected_shell / 16.0f;
+    if (!(want >= 64.0f))
+      nb = 64u;
+    else if (want < 2048.0f)
+      nb = (uint32_t)want;
+    rc.nb = nb;
+    rc.inv_w = (R)nb / span;
+    rc.bin_w = span / (R)nb;
+    const R K = (threshold + 1.0f) * vol_factor;
+    rc.K2 = K * K;
+    rc.expected = vol_factor * r_search * r_search * r_search;
+    rc.threshold = threshold;
+    rc.window = (uint32_t)std::max(1, p.window);
+    return rc;
+  };
+  // A template in one upload into `buf`: min and max d^2, the three offsets,
+  // the classes, packed in that order (each part aligned for its type).
+  auto upload_template = [&](const HostTemplateT<R>& ht, DevBuf& buf) {
+    const uint32_t tcount = (uint32_t)ht.type.size();
+    const size_t t_real = ((size_t)tcount * sizeof(R) + 15) & ~(size_t)15;
+    const size_t t_int = ((size_t)tcount * sizeof(int32_t) + 15) & ~(size_t)15;
+    const size_t t_bytes = 2 * t_real + 3 * t_int + tcount;
+    if (h_tpl_.size() < t_bytes) h_tpl_.resize(t_bytes);
+    uint8_t* hp = h_tpl_.data();
+    std::memcpy(hp, ht.min_d2.data(), tcount * sizeof(R));
+    std::memcpy(hp + t_real, ht.max_d2.data(), tcount * sizeof(R));
+    std::memcpy(hp + 2 * t_real, ht.dx.data(), tcount * sizeof(int32_t));
+    std::memcpy(hp + 2 * t_real + t_int, ht.dy.data(), tcount * sizeof(int32_t));
+    std::memcpy(hp + 2 * t_real + 2 * t_int, ht.dz.data(), tcount * sizeof(int32_t));
+    std::memcpy(hp + 2 * t_real + 3 * t_int, ht.type.data(), tcount);
+    uint8_t* dp = grow_to<uint8_t>(buf, t_bytes);
+    // Pageable source: the copy is staged before the call returns, so the
+    // staging vector is free for the next template at once.
+    SIFG_CUDA(cudaMemcpyAsync(dp, hp, t_bytes, cudaMemcpyHostToDevice, st_));
+    return TemplateViewT<R>{(const int32_t*)(dp + 2 * t_real),
+                            (const int32_t*)(dp + 2 * t_real + t_int),
+                            (const int32_t*)(dp + 2 * t_real + 2 * t_int),
+                            dp + 2 * t_real + 3 * t_int,
+                            (const R*)dp,
+                            (const R*)(dp + t_real),
+                            tcount};
+  };
+
+  // SIF_FINDER_EXTEND_REACH (exodus_finder.c:1664-1702, 242-244, 1342-1353):
+  // a crossing past a rung's reach is measured again at the levels of an
+  // extended reach, from the top rung's reach down by EXT_GROWTH to below the
+  // bottom rung; level k measures [ext_rmin[k], ext_reach[k]]. The levels are
+  // the same for every rung and built once.
+  const R kExtGrowth = 1.5f, kExtSlack = 1.2f;
+  uint32_t n_ext = 0;
+  R ext_reach[kExtMaxLevels], ext_rmin[kExtMaxLevels];
+  TemplateViewT<R> ext_tv[kExtMaxLevels];
+  if (extend && !radii.empty()) {
+    const R r_top = radii.front();
+    const R r_ext = r_top + std::fmax((search_factor - 1.0f) * r_top, 3.0f * cell);
+    const R r_low = radii.back();
+    while (n_ext < kExtMaxLevels &&
+           (n_ext == 0 || r_ext / std::pow(kExtGrowth, (R)(n_ext - 1)) > r_low))
+      n_ext++;
+    for (uint32_t k = 0; k < n_ext; k++)
+      ext_reach[k] = r_ext / std::pow(kExtGrowth, (R)(n_ext - 1 - k));
+    for (uint32_t k = 0; k < n_ext; k++) {
+      ext_rmin[k] = (k ? ext_reach[k - 1] : ext_reach[0] / kExtGrowth) / kExtSlack;
+      HostTemplateT<R> ht;
+      if (build_template(ht, mesh.n_cells, mesh.cell_length, ext_rmin[k], ext_reach[k]) != kOk) {
+        set_error(kErrRange, "extended reach of " + std::to_string(ext_reach[k]) +
+                                 " wider than the mesh; use a finer mesh or smaller radii");
+        return kErrRange;
+      }
+      ext_tv[k] = upload_template(ht, ext_tpl_[k]);
+    }
+  }
+
   bool mesh_waited = false;
   using clk = std::chrono::steady_clock;
   auto ms_since = [](clk::time_point t0) {
@@ -630,38 +713,17 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     SIFG_CUDA(cudaMemcpyAsync(h_delta_, cdelta, m * sizeof(R), cudaMemcpyDeviceToHost, st_));
     SIFG_CUDA(cudaEventRecord(ev_cand_, st_));
 
-    RungConstsT<R> rc;
-    rc.radius = radius;
-    rc.r_search = r_search;
-    rc.rmin = rmin;
-    rc.rs2 = r_search * r_search;
-    rc.rc2 = rmin * rmin;
+    RungConstsT<R> rc0{};
+    rc0.radius = radius;
+    rc0.proxy_pole = (int32_t)(scale * radius * (1.0f - f) / cell) - 1;
+    rc0.scale = scale;
+    rc0.f = f;
+    rc0.cell = cell;
+    rc0.grid_n = N;
+    rc0.box = box;
+    rc0.gbox = (R)N * cell;
+    const RungConstsT<R> rc = shell_consts(rc0, rmin, r_search);
     const R span = rc.rs2 - rc.rc2;
-    uint32_t nb = 2048u;
-    {
-      const R expected_shell =
-          vol_factor * (r_search * r_search * r_search - rmin * rmin * rmin);
-      const R want = expected_shell / 16.0f;
-      if (!(want >= 64.0f))
-        nb = 64u;
-      else if (want < 2048.0f)
-        nb = (uint32_t)want;
-    }
-    rc.nb = nb;
-    rc.inv_w = (R)nb / span;
-    rc.bin_w = span / (R)nb;
-    const R K = (threshold + 1.0f) * vol_factor;
-    rc.K2 = K * K;
-    rc.expected = vol_factor * r_search * r_search * r_search;
-    rc.threshold = threshold;
-    rc.proxy_pole = (int32_t)(scale * radius * (1.0f - f) / cell) - 1;
-    rc.scale = scale;
-    rc.f = f;
-    rc.cell = cell;
-    rc.grid_n = N;
-    rc.box = box;
-    rc.gbox = (R)N * cell;
-    rc.window = (uint32_t)std::max(1, p.window);
 
     HostTemplateT<R> ht;
     if (build_template(ht, mesh.n_cells, mesh.cell_length, rmin, r_search) != kOk) {
@@ -669,29 +731,14 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
                                " wider than the mesh; use a finer mesh or smaller radii");
       return kErrRange;
     }
-    // The template in one upload: min and max d^2, the three offsets, the
-    // classes, packed in that order (each part aligned for its type).
-    const uint32_t tcount = (uint32_t)ht.type.size();
-    const size_t t_real = ((size_t)tcount * sizeof(R) + 15) & ~(size_t)15;
-    const size_t t_int = ((size_t)tcount * sizeof(int32_t) + 15) & ~(size_t)15;
-    const size_t t_bytes = 2 * t_real + 3 * t_int + tcount;
-    if (h_tpl_.size() < t_bytes) h_tpl_.resize(t_bytes);
-    uint8_t* hp = h_tpl_.data();
-    std::memcpy(hp, ht.min_d2.data(), tcount * sizeof(R));
-    std::memcpy(hp + t_real, ht.max_d2.data(), tcount * sizeof(R));
-    std::memcpy(hp + 2 * t_real, ht.dx.data(), tcount * sizeof(int32_t));
-    std::memcpy(hp + 2 * t_real + t_int, ht.dy.data(), tcount * sizeof(int32_t));
-    std::memcpy(hp + 2 * t_real + 2 * t_int, ht.dz.data(), tcount * sizeof(int32_t));
-    std::memcpy(hp + 2 * t_real + 3 * t_int, ht.type.data(), tcount);
-    uint8_t* dp = grow_to<uint8_t>(tpl_, t_bytes);
-    SIFG_CUDA(cudaMemcpyAsync(dp, hp, t_bytes, cudaMemcpyHostToDevice, st_));
-    const R* tmin = (const R*)dp;
-    const R* tmax = (const R*)(dp + t_real);
-    const int32_t* tdx = (const int32_t*)(dp + 2 * t_real);
-    const int32_t* tdy = (const int32_t*)(dp + 2 * t_real + t_int);
-    const int32_t* tdz = (const int32_t*)(dp + 2 * t_real + 2 * t_int);
-    const uint8_t* ttype = dp + 2 * t_real + 3 * t_int;
-    TemplateViewT<R> tv{tdx, tdy, tdz, ttype, tmin, tmax, tcount};
+    const TemplateViewT<R> tv = upload_template(ht, tpl_);
+    // The first level of the extended reach this rung enters: the lowest
+    // EXT_SLACK past its own reach, or the top if none is
+    // (exodus_finder.c:1826-1832).
+    uint32_t ext0 = n_ext;
+    for (uint32_t k = 0; k < n_ext && ext0 == n_ext; k++)
+      if (ext_reach[k] >= kExtSlack * r_search) ext0 = k;
+    if (ext0 == n_ext && n_ext > 0 && ext_reach[n_ext - 1] > r_search) ext0 = n_ext - 1;
 
     // 3. Pre-filter at the rung, against the catalogue as the rung begins.
     VoidViewT<R> vv{cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), cat_r_.as<R>(),
@@ -720,6 +767,11 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
         mesh_waited = true;
       }
       grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_, tm ? &tm->growth : nullptr);
+      // Each level of the extended reach, for the survivors whose crossing
+      // still lies past the reach (exodus_finder.c:2060-2072).
+      for (uint32_t e = ext0; e < n_ext; e++)
+        grow(mv, ext_tv[e], shell_consts(rc, ext_rmin[e], ext_reach[e]), sv, m, gbuf, kGrowCap,
+             traffic + 2 * ri, st_, tm ? &tm->growth : nullptr, kRescaleBeyondSearch);
     }
 
     // 5. The order, on the host while the GPU grows spheres.
@@ -734,7 +786,9 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
 
     // 6. The commit, in rounds.
     const auto t_commit = clk::now();
-    const R reach = 2.0f * scale * r_search + 2.0f * cell;
+    // Radii reach the top level's reach where the rung enters the extended one.
+    const R r_max = ext0 < n_ext ? std::max(r_search, ext_reach[n_ext - 1]) : r_search;
+    const R reach = 2.0f * scale * r_max + 2.0f * cell;
     int32_t ng = (int32_t)std::floor(box / reach);
     if (ng < 3) ng = 1;
     if (ng > 256) ng = 256;

@@ -109,6 +109,8 @@ class Engine {
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
   DevBuf tpl_, gbuf_, traffic_, region_delta_, region_flat_;
+  static constexpr uint32_t kExtMaxLevels = 32;  // EXT_MAX_LEVELS, exodus_finder.c:244
+  DevBuf ext_tpl_[kExtMaxLevels];  // the extended reach's templates, one per level
   DevBuf below_counts_[2], below_delta_[2], below_flat_[2];  // the smoothing's below-threshold lists
   std::vector<uint8_t> h_tpl_;  // the packed template, staged for its upload
   void* h_delta_ = nullptr;  // candidate depths, float or double

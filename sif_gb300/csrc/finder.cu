@@ -815,7 +815,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
                                                            RungConstsT<R> rc, SurvivorsT<R> sv,
                                                            R* __restrict__ gbuf, uint32_t gcap,
                                                            unsigned long long* __restrict__ traffic,
-                                                           bool only_pending) {
+                                                           uint8_t only) {
   __shared__ uint32_t bins[kMaxBins];
   __shared__ uint32_t below[kMaxBins];  // particles inside bin b's lower edge
   __shared__ R sbuf[kSmemBuf];
@@ -830,7 +830,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
   R* my_gbuf = gbuf + (uint64_t)blockIdx.x * gcap;
 
   for (uint32_t s = blockIdx.x; s < n_surv; s += gridDim.x) {
-    if (only_pending && sv.reason[s] != kRescalePending) continue;
+    if (only != kAllSurvivors && sv.reason[s] != only) continue;
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
                   ck = (int32_t)fmul(cz, mesh.inv_l);
@@ -1072,6 +1072,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
                                                              TemplateViewT<R> tpl,
                                                              RungConstsT<R> rc, SurvivorsT<R> sv,
                                                              uint32_t nb_stride, uint32_t shell_cap,
+                                                             uint8_t only,
                                                              unsigned long long* __restrict__ traffic) {
   extern __shared__ unsigned char warp_smem[];
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -1095,6 +1096,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
   const uint32_t n_surv = *sv.count;
   const uint32_t warps = gridDim.x * kGrowWarps;
   for (uint32_t s = blockIdx.x * kGrowWarps + warp; s < n_surv; s += warps) {
+    if (only != kAllSurvivors && sv.reason[s] != only) continue;
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
                   ck = (int32_t)fmul(cz, mesh.inv_l);
@@ -1290,7 +1292,7 @@ constexpr uint32_t kShellListMax = 512;  // entries of a warp's shell list, at m
 template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s, uint32_t max_survivors,
           R* gbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
-          KernelTimer* timer) {
+          KernelTimer* timer, uint8_t only) {
   if (max_survivors == 0) return;
   const bool by_warp = g_growth_mode == 2 || (g_growth_mode == 0 && max_survivors >= kWarpGrowthMin);
   const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
@@ -1323,13 +1325,13 @@ void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT
     const uint32_t cap = 152u * (uint32_t)std::max(per_sm, 1);
     growth_warp_kernel<R><<<std::min(warps_needed, cap), kGrowT, smem, st>>>(mesh, tpl, rc, s,
                                                                             nb_stride, shell_cap,
-                                                                            traffic);
+                                                                            only, traffic);
     SIFG_LAUNCH_CHECK();
     // The survivors whose windows were too wide for a warp.
-    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, true);
+    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, kRescalePending);
     SIFG_LAUNCH_CHECK();
   } else {
-    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, false);
+    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, only);
     SIFG_LAUNCH_CHECK();
   }
   if (timer) timer->end(st);
@@ -1792,7 +1794,7 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
                              RungConstsT<R>, uint8_t*, uint32_t*, uint32_t*, uint32_t*, R*, R*,    \
                              R*, uint32_t*, cudaStream_t);                                         \
   template void grow<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>, uint32_t,   \
-                        R*, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*);            \
+                        R*, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*, uint8_t);   \
   template void build_survivor_grid<R>(const R*, const R*, const R*, const uint32_t*, uint32_t,    \
                                        int32_t, R, uint32_t*, uint32_t*, uint32_t*, cudaStream_t); \
   template void commit_init<R>(SurvivorsT<R>, uint8_t*, uint32_t*, uint32_t, cudaStream_t);        \

@@ -167,15 +167,17 @@ void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, Void
                uint32_t* surv_flat, R* scx, R* scy, R* scz, uint32_t* d_surv_count,
                cudaStream_t st);
 
-// Sphere growth of every survivor. gbuf: a global overflow scratch of
-// grid * gcap values.
+// Sphere growth of every survivor, or (only != kAllSurvivors) of those whose
+// rescale outcome is `only`. gbuf: a global overflow scratch of grid * gcap
+// values.
+constexpr uint8_t kAllSurvivors = 0xff;
 unsigned growth_grid();
 // traffic (may be NULL): two counters the kernel adds to -- particles read
 // and template cells visited.
 template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
           uint32_t max_survivors, R* gbuf, uint32_t gcap, unsigned long long* traffic,
-          cudaStream_t st, KernelTimer* timer);
+          cudaStream_t st, KernelTimer* timer, uint8_t only = kAllSurvivors);
 // Which growth kernel runs: 0 by the survivor count (a CTA per survivor for
 // few, a warp per survivor for many), 1 always a CTA, 2 always a warp. The
 // radii are the same either way (tests run both).

@@ -99,6 +99,18 @@ def test_fp64_catalogue_either_growth_kernel(dev, golden_box32_f64, mode):
         dev.set_growth_mode(0)
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["auto", "cta", "warp"])
+@pytest.mark.parametrize("name", ["minima_f1", "extend_minima_f1", "extend_f1", "extend"])
+def test_fp64_catalogue_extended_reach(dev, golden_box32_extend_f64, name, mode):
+    """SIF_FINDER_EXTEND_REACH in the FP64 form: the reference's
+    SIF_USE_DOUBLE catalogues, with and without it, on its own fields."""
+    dev.set_growth_mode(mode)
+    try:
+        test_fp64_catalogue_matches_reference(dev, golden_box32_extend_f64, name)
+    finally:
+        dev.set_growth_mode(0)
+
+
 @pytest.mark.parametrize("window", ["full", "aliasing", "none"])
 def test_fp64_smoothing_against_oracle(dev, oracle, golden_box32_f64, window):
     g = golden_box32_f64

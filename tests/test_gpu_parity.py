@@ -189,6 +189,22 @@ def test_catalogue_matches_reference_golden(dev, golden_box32, name):
     assert same_catalogue(cat, want)
 
 
+EXTEND_SETS = ["minima_f1", "extend_minima_f1", "extend_f1", "extend"]
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["auto", "cta", "warp"])
+@pytest.mark.parametrize("name", EXTEND_SETS)
+def test_catalogue_matches_reference_golden_extended_reach(dev, golden_box32_extend, name, mode):
+    """SIF_FINDER_EXTEND_REACH: a crossing past the rung's reach measured at
+    the levels of an extended reach, by each growth kernel; the reference's
+    catalogues, with and without it, on its own fields."""
+    dev.set_growth_mode(mode)
+    try:
+        test_catalogue_matches_reference_golden(dev, golden_box32_extend, name)
+    finally:
+        dev.set_growth_mode(0)
+
+
 @pytest.fixture(params=[1, 2], ids=["cta", "warp"])
 def growth_mode(request, dev):
     """Each sphere-growth kernel forced in turn; back to automatic after."""
