@@ -14,8 +14,9 @@
 //   1. tile_count:   each particle's tile (16^3 base cells), histogram with
 //                    warp-aggregated atomics;
 //   2. exclusive scan of the tile counts;
-//   3. tile_scatter: positions copied into tile order (one atomic per group
-//                    of lanes bound for the same tile);
+//   3. tile_scatter: each particle's base cell and fractions, found once, as
+//                    a 16-byte record in tile order (one atomic per group of
+//                    lanes bound for the same tile);
 //   4. tile_deposit: one CTA per tile accumulates a 17^3 tile of 64-bit sums
 //                    (32-bit words plus carries) in shared memory with one
 //                    shared atomic per corner; the 15^3 cells no other tile touches
@@ -105,34 +106,34 @@ __global__ void tile_count_kernel(const float* __restrict__ x, const float* __re
   }
 }
 
+// A particle's deposit record: its fractions along x, y, z and, in the
+// fourth word's bits, its base cell within its tile (x << 8 | y << 4 | z).
+static_assert(TB == 16, "4 bits per axis of the cell within its tile");
+
 __global__ void tile_scatter_kernel(const float* __restrict__ x, const float* __restrict__ y,
                                     const float* __restrict__ z, uint64_t n, CicGeom g,
-                                    uint32_t* __restrict__ cursor, float* __restrict__ sx,
-                                    float* __restrict__ sy, float* __restrict__ sz) {
+                                    uint32_t* __restrict__ cursor, float4* __restrict__ rec) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const unsigned lane = threadIdx.x & 31u;
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
     const uint64_t p = base + threadIdx.x;
     const bool valid = p < n;
-    float px = 0.f, py = 0.f, pz = 0.f;
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
     uint32_t tile = 0xffffffffu;
     if (valid) {
-      px = x[p];
-      py = y[p];
-      pz = z[p];
-      tile = tile_of(px, py, pz, g);
+      uint32_t cx, cy, cz;
+      cic_axis(x[p], g, cx, r.x);
+      cic_axis(y[p], g, cy, r.y);
+      cic_axis(z[p], g, cz, r.z);
+      tile = ((cx / TB) * g.nt + cy / TB) * g.nt + cz / TB;
+      r.w = __uint_as_float((cx % TB) << 8 | (cy % TB) << 4 | (cz % TB));
     }
     const unsigned peers = __match_any_sync(0xffffffffu, tile);
     const unsigned leader = __ffs(peers) - 1;
     uint32_t slot0 = 0;
     if (valid && lane == leader) slot0 = atomicAdd(cursor + tile, (uint32_t)__popc(peers));
     slot0 = __shfl_sync(0xffffffffu, slot0, leader);
-    if (valid) {
-      const uint32_t slot = slot0 + __popc(peers & ((1u << lane) - 1u));
-      sx[slot] = px;
-      sy[slot] = py;
-      sz[slot] = pz;
-    }
+    if (valid) rec[slot0 + __popc(peers & ((1u << lane) - 1u))] = r;
   }
 }
 
@@ -154,9 +155,8 @@ __device__ __forceinline__ unsigned long long* face_slot(const FaceBufs& f, uint
 }
 
 __global__ void __launch_bounds__(256) tile_deposit_kernel(
-    const float* __restrict__ sx, const float* __restrict__ sy, const float* __restrict__ sz,
-    const uint32_t* __restrict__ offsets, CicGeom g, float inv_cell_vol,
-    float* __restrict__ grid, FaceBufs faces) {
+    const float4* __restrict__ rec, const uint32_t* __restrict__ offsets, CicGeom g,
+    float inv_cell_vol, float* __restrict__ grid, FaceBufs faces) {
   // The tile's sums as 32-bit words and their carries: a 32-bit shared atomic
   // add is one instruction, a 64-bit one a compare-and-swap loop. A word that
   // wraps past 2^32 counts the wrap in its carry (each add is below 2^32, so
@@ -180,11 +180,9 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
       uint32_t cell = 0xffffffffu;
       uint32_t q[8];
       if (valid) {
-        uint32_t cx, cy, cz;
-        float tx_, ty_, tz_;
-        cic_axis(sx[p], g, cx, tx_);
-        cic_axis(sy[p], g, cy, ty_);
-        cic_axis(sz[p], g, cz, tz_);
+        const float4 r = __ldg(rec + p);
+        const float tx_ = r.x, ty_ = r.y, tz_ = r.z;
+        const uint32_t local = __float_as_uint(r.w);
         const float wx0 = fsub(1.0f, tx_), wy0 = fsub(1.0f, ty_), wz0 = fsub(1.0f, tz_);
         // The reference's eight products (grid.c:627-650): (x,y) pairs times z.
         const float w00 = fmul(wx0, wy0), w01 = fmul(wx0, ty_);
@@ -209,7 +207,7 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
         const int fix = 16777216 - sum;
 #pragma unroll
         for (int k = 0; k < 8; k++) q[k] = (uint32_t)((int)q[k] + (k == big ? fix : 0));
-        cell = ((cx - ox) * TS + (cy - oy)) * TS + (cz - oz);
+        cell = ((local >> 8) * TS + ((local >> 4) & 15u)) * TS + (local & 15u);
       }
       // One shared atomic per corner. (Reducing lanes bound for the same cell
       // first with __reduce_add_sync over each lane group's own mask costs a
@@ -443,7 +441,7 @@ size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n) {
   const uint64_t nt = (n + TB - 1) / TB;
   const uint64_t tiles = nt * nt * nt;
   const uint64_t face = 3 * nt * (uint64_t)n * n * sizeof(unsigned long long);
-  return 3 * n_particles * sizeof(float) + (2 * tiles + 2) * sizeof(uint32_t) + face + 16 * 256;
+  return n_particles * sizeof(float4) + (2 * tiles + 2) * sizeof(uint32_t) + face + 16 * 256;
 }
 
 void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_particles,
@@ -458,9 +456,7 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
     p += (bytes + 255) & ~(size_t)255;
     return (void*)r;
   };
-  float* sx = (float*)take(n_particles * sizeof(float));
-  float* sy = (float*)take(n_particles * sizeof(float));
-  float* sz = (float*)take(n_particles * sizeof(float));
+  float4* rec = (float4*)take(n_particles * sizeof(float4));
   uint32_t* counts = (uint32_t*)take((tiles + 1) * sizeof(uint32_t));
   uint32_t* cursor = (uint32_t*)take((tiles + 1) * sizeof(uint32_t));
   const size_t face_elems = nt * (uint64_t)n * n;
@@ -482,7 +478,7 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   exclusive_scan_u32(counts, (uint32_t)(tiles + 1), st);
   SIFG_CUDA(cudaMemcpyAsync(cursor, counts, (tiles + 1) * sizeof(uint32_t),
                             cudaMemcpyDeviceToDevice, st));
-  tile_scatter_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, cursor, sx, sy, sz);
+  tile_scatter_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, cursor, rec);
   SIFG_LAUNCH_CHECK();
   if (sorted) SIFG_CUDA(cudaEventRecord(sorted, st));
   const float cl = box / (float)n;
@@ -496,8 +492,7 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   }
   const unsigned dgrid = (unsigned)(tiles < 152u * 5u ? tiles : 152u * 5u);
   if (timer) timer->begin(st);
-  tile_deposit_kernel<<<dgrid, 256, smem, st>>>(sx, sy, sz, counts, g, inv_cell_vol, grid,
-                                                faces);
+  tile_deposit_kernel<<<dgrid, 256, smem, st>>>(rec, counts, g, inv_cell_vol, grid, faces);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(st);
   face_fixup_kernel<<<grid_for(3 * face_elems, 256), 256, 0, st>>>(g, inv_cell_vol, grid, faces);
