@@ -404,6 +404,46 @@ __global__ void __launch_bounds__(kMeanThreads) mean_partial_kernel(const R* __r
   if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
 }
 
+// The float form's partial sums without a double operation per value: this
+// GPU's FP64 rate would bound the pass (a conversion and an add per cell),
+// not its 4 bytes a cell. Each thread keeps its running sum as a float pair
+// by Knuth's TwoSum (the rounding error of every add kept in the low part),
+// at least as exact as a double chain over the same values, in the same
+// fixed order; the block's 256 pairs are then added in double as above.
+template <>
+__global__ void __launch_bounds__(kMeanThreads) mean_partial_kernel<float>(
+    const float* __restrict__ v, uint64_t n, double* __restrict__ partial) {
+  __shared__ double s[kMeanThreads];
+  const uint64_t chunk = (n + kMeanBlocks - 1) / kMeanBlocks;
+  const uint64_t lo = (uint64_t)blockIdx.x * chunk;
+  const uint64_t hi = lo + chunk < n ? lo + chunk : n;
+  float sh = 0.0f, sl = 0.0f;
+  auto add = [&](float x) {
+    const float t = __fadd_rn(sh, x);
+    const float b = __fsub_rn(t, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, b)), __fsub_rn(x, b));
+    sh = t;
+    sl = __fadd_rn(sl, e);
+  };
+  uint64_t i = lo + threadIdx.x;
+  for (; i + 3 * kMeanThreads < hi; i += 4 * kMeanThreads) {
+    const float a = v[i], b = v[i + kMeanThreads], c = v[i + 2 * kMeanThreads],
+                d = v[i + 3 * kMeanThreads];
+    add(a);
+    add(b);
+    add(c);
+    add(d);
+  }
+  for (; i < hi; i += kMeanThreads) add(v[i]);
+  s[threadIdx.x] = (double)sh + (double)sl;
+  __syncthreads();
+  for (int w = kMeanThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+}
+
 __global__ void mean_final_kernel(const double* __restrict__ partial, uint64_t n,
                                   double* __restrict__ mean_out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
