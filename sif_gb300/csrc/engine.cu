@@ -815,7 +815,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     for (uint32_t batch = 3;; batch = 4) {
       SIFG_CUDA(cudaMemsetAsync(counters + kRoundUndecided, 0, kRoundRing * sizeof(uint32_t), st_));
       const bool one_launch = commit_rounds(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters,
-                                            (uint32_t)rounds, kRoundRing, bar, st_);
+                                            (uint32_t)rounds, kRoundRing, bar, m, st_);
       if (one_launch) {
         SIFG_CUDA(cudaMemcpyAsync(h_bar, bar, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, st_));
       } else {

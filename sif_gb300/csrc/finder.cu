@@ -1670,7 +1670,7 @@ template <class R>
 bool commit_rounds(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, VoidViewT<R> voids,
                    uint32_t* mask, RungConstsT<R> rc, uint8_t* sa, uint8_t* sb, uint32_t* acc,
                    uint32_t* counters, uint32_t round0, uint32_t max_rounds, unsigned* bar,
-                   cudaStream_t st) {
+                   uint32_t max_survivors, cudaStream_t st) {
   if (g_commit_mode != 0) return false;
   thread_local int blocks = -1;  // co-resident blocks of the device, found once per thread
   if (blocks < 0) {
@@ -1682,10 +1682,15 @@ bool commit_rounds(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Vo
     blocks = coop && per_sm > 0 ? sms : 0;  // one block per SM
   }
   if (blocks == 0) return false;
+  // A block per kCommitT survivors: a small rung's grid barriers gather few
+  // blocks, and its launch finds room beside other engines' kernels (all of
+  // a cooperative launch's blocks must be resident at once).
+  const unsigned want = (unsigned)std::max<uint64_t>(1, ((uint64_t)max_survivors + kCommitT - 1) / kCommitT);
+  const unsigned grid = std::min<unsigned>((unsigned)blocks, want);
   SIFG_CUDA(cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned), st));
   void* args[] = {&s, (void*)&rank, &g, &voids, &mask, &rc, &sa, &sb, &acc, &counters, &round0,
                   &max_rounds, &bar};
-  SIFG_CUDA(cudaLaunchCooperativeKernel((const void*)commit_loop_kernel<R>, dim3(blocks),
+  SIFG_CUDA(cudaLaunchCooperativeKernel((const void*)commit_loop_kernel<R>, dim3(grid),
                                         dim3(kCommitT), args, 0, st));
   SIFG_LAUNCH_CHECK();
   return true;
@@ -1805,7 +1810,7 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
                              RungConstsT<R>, uint32_t, cudaStream_t);                              \
   template bool commit_rounds<R>(SurvivorsT<R>, const uint32_t*, SurvivorGridT<R>, VoidViewT<R>,   \
                                  uint32_t*, RungConstsT<R>, uint8_t*, uint8_t*, uint32_t*,         \
-                                 uint32_t*, uint32_t, uint32_t, unsigned*, cudaStream_t);          \
+                                 uint32_t*, uint32_t, uint32_t, unsigned*, uint32_t, cudaStream_t);\
   template void append_accepted<R>(SurvivorsT<R>, const uint32_t*, const uint32_t*,                \
                                    const uint32_t*, uint32_t, uint32_t*, R*, R*, R*, R*, uint32_t, \
                                    uint32_t, cudaStream_t);                                        \

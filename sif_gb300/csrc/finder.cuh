@@ -223,12 +223,13 @@ void commit_round(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Voi
 // bar[2] is set if a grid barrier timed out. Returns false, launching
 // nothing, where the device cannot run it (or set_commit_mode(1) asked for
 // a kernel launch per round): the caller then runs commit_round and
-// paint_new per round.
+// paint_new per round. max_survivors bounds the survivors: the launch takes
+// a block per kCommitT of them, at most one per SM.
 template <class R>
 bool commit_rounds(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, VoidViewT<R> voids,
                    uint32_t* mask, RungConstsT<R> rc, uint8_t* sa, uint8_t* sb, uint32_t* acc,
                    uint32_t* counters, uint32_t round0, uint32_t max_rounds, unsigned* bar,
-                   cudaStream_t st);
+                   uint32_t max_survivors, cudaStream_t st);
 // 0 (default): the commit's rounds in one cooperative launch where the device
 // allows it; 1: a launch per round. The catalogue does not depend on it.
 void set_commit_mode(int mode);
