@@ -344,15 +344,17 @@ int sifg_smooth_device(const float* delta, uint32_t n_grid, float box, float r, 
                        int window_mode, float* out);
 /* The exodus finder on a device density contrast and a device mesh. radii in
  * host memory. inject: NULL, or n_radii device grids that replace the
- * smoothing, largest radius first. The catalogue is written to the host
- * arrays (capacity entries each); *n_voids receives the count (which may
- * exceed capacity: then only capacity are written). */
+ * smoothing, largest radius first. prior: NULL, or n_prior voids to start
+ * from in host memory, as four columns one after another (cx, cy, cz, r),
+ * checked and used as sif_finder_exodus_extras_t::prior is. The catalogue is
+ * written to the host arrays (capacity entries each); *n_voids receives the
+ * count (which may exceed capacity: then only capacity are written). */
 int sifg_exodus_device(const float* delta, uint32_t n_grid, float box, const float* mx,
                        const float* my, const float* mz, const uint32_t* offsets,
                        uint64_t n_particles, uint32_t mesh_cells, const float* radii,
                        uint32_t n_radii, float threshold, float overlap, uint32_t opt,
-                       const float* inject, float* cx, float* cy, float* cz, float* r,
-                       uint64_t capacity, uint64_t* n_voids);
+                       const float* inject, const float* prior, uint64_t n_prior, float* cx,
+                       float* cy, float* cz, float* r, uint64_t capacity, uint64_t* n_voids);
 /* The whole box path on device particles: CIC, contrast, mesh, exodus. */
 int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
                     float box, uint32_t mesh_cells, const float* radii, uint32_t n_radii,
@@ -376,8 +378,9 @@ int sifg_exodus_device_f64(const double* delta, uint32_t n_grid, double box, con
                            const double* my, const double* mz, const uint32_t* offsets,
                            uint64_t n_particles, uint32_t mesh_cells, const double* radii,
                            uint32_t n_radii, double threshold, double overlap, uint32_t opt,
-                           const double* inject, double* cx, double* cy, double* cz, double* r,
-                           uint64_t capacity, uint64_t* n_voids);
+                           const double* inject, const double* prior, uint64_t n_prior,
+                           double* cx, double* cy, double* cz, double* r, uint64_t capacity,
+                           uint64_t* n_voids);
 int sifg_box_device_f64(const double* x, const double* y, const double* z, uint64_t n,
                         uint32_t n_grid, double box, uint32_t mesh_cells, const double* radii,
                         uint32_t n_radii, double threshold, double overlap, uint32_t opt,

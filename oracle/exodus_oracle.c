@@ -1184,6 +1184,16 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   voids_t V;
   voids_init(&V, box);
   float max_acc = 0.0f;
+  /* The prior voids, put back as accept_void() puts a void in
+   * (exodus_finder.c:1614-1622, 656-683): the catalogue, the mask at
+   * scale * r, the largest radius. */
+  for (uint64_t v = 0; v < p->n_prior; v++) {
+    voids_add(&V, p->prior_cx[v], p->prior_cy[v], p->prior_cz[v], p->prior_r[v]);
+    mark_sphere(mask, p->prior_cx[v], p->prior_cy[v], p->prior_cz[v], scale * p->prior_r[v], N,
+      cell);
+    if (p->prior_r[v] > max_acc)
+      max_acc = p->prior_r[v];
+  }
   orc_candidate_t* cand = NULL;
   uint64_t cand_cap = 0;
   result_t* res = malloc(2 * BATCH_MAX * sizeof(result_t));

@@ -127,6 +127,13 @@ typedef struct {
   int window;         /* 0: the reference's adaptive window; >0: fixed */
   int smoothing_mode; /* as orc_spectrum_new when no fields are injected */
   const float* inject; /* NULL, or n_radii fields of grid_n^3, largest rung first */
+  /* Voids to start from (sif_finder_exodus_extras_t::prior): accepted before
+   * the first rung and returned first. NULL when n_prior is 0. */
+  const float* prior_cx;
+  const float* prior_cy;
+  const float* prior_cz;
+  const float* prior_r;
+  uint64_t n_prior;
 } orc_exodus_params_t;
 
 typedef struct {

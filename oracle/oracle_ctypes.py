@@ -48,7 +48,9 @@ class Params(C.Structure):
     _fields_ = [("grid_n", C.c_uint32), ("box_length", C.c_float),
                 ("threshold", C.c_float), ("overlap_fraction", C.c_float),
                 ("options", C.c_uint32), ("n_threads", C.c_int), ("window", C.c_int),
-                ("smoothing_mode", C.c_int), ("inject", C.c_void_p)]
+                ("smoothing_mode", C.c_int), ("inject", C.c_void_p),
+                ("prior_cx", C.c_void_p), ("prior_cy", C.c_void_p), ("prior_cz", C.c_void_p),
+                ("prior_r", C.c_void_p), ("n_prior", C.c_uint64)]
 
 
 class Catalogue(C.Structure):
@@ -195,16 +197,19 @@ def brute_force_radius(x, y, z, box, c, rung, r_search, threshold):
 
 
 def exodus(delta, mesh, radii, n_grid, box, threshold, overlap=0.0, options=0, n_threads=1,
-           window=0, smoothing_mode=1, inject=None, with_stats=False):
-    """The oracle finder; returns (cx, cy, cz, r) float32 arrays."""
+           window=0, smoothing_mode=1, inject=None, with_stats=False, prior=None):
+    """The oracle finder; returns (cx, cy, cz, r) float32 arrays. prior:
+    (cx, cy, cz, r), voids to start from."""
     d = np.ascontiguousarray(delta, dtype=np.float32)
     radii = np.ascontiguousarray(radii, dtype=np.float32)
     inj = None
     if inject is not None:
         inj = np.ascontiguousarray(inject, dtype=np.float32)
         assert inj.shape == (len(radii), n_grid ** 3)
+    pri = [np.ascontiguousarray(c, dtype=np.float32) for c in prior] if prior is not None else None
     p = Params(n_grid, box, threshold, overlap, options, n_threads, window, smoothing_mode,
-               _p(inj) if inj is not None else None)
+               _p(inj) if inj is not None else None,
+               *([_p(c) for c in pri] if pri else [None] * 4), len(pri[0]) if pri else 0)
     cat = Catalogue()
     stats = (RungStats * len(radii))()
     st = lib().orc_exodus(_p(d), C.byref(mesh.struct), _p(radii), len(radii), C.byref(p),

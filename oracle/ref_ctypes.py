@@ -173,17 +173,32 @@ def catalogue_arrays(lib, cat_ptr, variant="strict"):
 
 
 def exodus_raw(lib, grid, mesh, radii, threshold, overlap=0.0, opt=0, variant="strict",
-               inject=None, capture=None):
+               inject=None, capture=None, prior=None):
     """Runs sif_finder_exodus_raw; returns (cx, cy, cz, r).
 
     inject: (n_rungs, cells) array of smoothed fields that replace the
     reference's own, rung by rung; capture: an array of the same shape that
-    receives the fields the reference computed.
+    receives the fields the reference computed; prior: (cx, cy, cz, r), the
+    voids to start from (sif_finder_exodus_extras_t::prior).
     """
     t = np_real(variant)
     radii = np.ascontiguousarray(radii, dtype=t)
     cells = grid.ptr.contents.total_cells
     keep = []
+    extras = None
+    if prior is not None:
+        Cat, Extras = ((abi.STRUCTS_F64[3], abi.STRUCTS_F64[4]) if variant == "f64" else
+                       (abi.sif_catalogue_t, abi.sif_finder_exodus_extras_t))
+        cols = [np.ascontiguousarray(c, dtype=t) for c in prior]
+        keep.extend(cols)
+        P = C.POINTER(real_of(variant))
+        cat = Cat()
+        cat.cx, cat.cy, cat.cz, cat.radii = (c.ctypes.data_as(P) for c in cols)
+        cat.units = 0
+        cat.n_voids = cat.capacity = len(cols[0])
+        keep.append(cat)
+        extras = Extras(None, C.pointer(cat), 0, 0)
+        keep.append(extras)
     if inject is not None:
         inj = np.ascontiguousarray(inject, dtype=t)
         keep.append(inj)
@@ -194,7 +209,7 @@ def exodus_raw(lib, grid, mesh, radii, threshold, overlap=0.0, opt=0, variant="s
     try:
         cat = lib.sif_finder_exodus_raw(grid.ptr, mesh.ptr, _ptr(radii), len(radii),
                                         threshold, overlap, opt | abi.SIF_FINDER_NO_CHECKPOINT,
-                                        None)
+                                        C.byref(extras) if extras is not None else None)
     finally:
         lib.orc_hook_inject(None, 0, 0)
         lib.orc_hook_capture(None, 0, 0)

@@ -85,7 +85,7 @@ def load():
         "sifg_mesh_device": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]),
         "sifg_smooth_device": (i32, [vp, u32, f32, f32, i32, i32, vp]),
         "sifg_exodus_device": (i32, [vp, u32, f32, vp, vp, vp, vp, u64, u32, vp, u32, f32, f32,
-                                     u32, vp, vp, vp, vp, vp, u64, C.POINTER(u64)]),
+                                     u32, vp, vp, u64, vp, vp, vp, vp, u64, C.POINTER(u64)]),
         "sifg_box_device": (i32, [vp, vp, vp, u64, u32, f32, u32, vp, u32, f32, f32, u32,
                                   vp, vp, vp, vp, u64, C.POINTER(u64)]),
         "sifg_last_rung_stats": (u32, [C.POINTER(RungStat), u32]),
@@ -104,7 +104,7 @@ def load():
         "sifg_mesh_device_f64": (i32, [vp, vp, vp, u64, u32, f64, vp, vp, vp, vp, vp]),
         "sifg_smooth_device_f64": (i32, [vp, u32, f64, f64, i32, i32, vp]),
         "sifg_exodus_device_f64": (i32, [vp, u32, f64, vp, vp, vp, vp, u64, u32, vp, u32, f64,
-                                         f64, u32, vp, vp, vp, vp, vp, u64, C.POINTER(u64)]),
+                                         f64, u32, vp, vp, u64, vp, vp, vp, vp, u64, C.POINTER(u64)]),
         "sifg_box_device_f64": (i32, [vp, vp, vp, u64, u32, f64, u32, vp, u32, f64, f64, u32,
                                       vp, vp, vp, vp, u64, C.POINTER(u64)]),
         "sifg_contrast_vjp_device": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp]),

@@ -615,6 +615,25 @@ static int check_args(const R* radii, uint32_t n_radii, R threshold, R f) {
   return SIF_OK;
 }
 
+// The prior voids sif__exodus_check_extras accepts (src/finder/exodus_finder.c:
+// 1163-1197): radii positive and finite, centres inside [0, box).
+template <class R>
+static int check_prior(const R* cx, const R* cy, const R* cz, const R* r, uint64_t n, R box) {
+  for (uint64_t i = 0; i < n; i++) {
+    if (!(r[i] > R(0)) || !std::isfinite(r[i]))
+      return fail(SIF_ERR_INVALID, fmt("prior: void %llu: radius %g (expected positive and finite)",
+                                       (unsigned long long)i, (double)r[i]));
+    const R c[3] = {cx[i], cy[i], cz[i]};
+    for (int k = 0; k < 3; k++)
+      if (!(c[k] >= R(0) && c[k] < box))
+        return fail(SIF_ERR_INVALID,
+                    fmt("prior: void %llu: centre (%g, %g, %g) outside the box [0, %g)",
+                        (unsigned long long)i, (double)c[0], (double)c[1], (double)c[2],
+                        (double)box));
+  }
+  return SIF_OK;
+}
+
 extern "C" {
 
 sif_catalogue_t* sif_finder_exodus(sif_grid_t* grid, const sif_chain_mesh_t* mesh,
@@ -654,15 +673,29 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
     fail(SIF_ERR_UNSUPPORTED, "mesh: weighted meshes are not supported by the GPU finder");
     return nullptr;
   }
+  // sif__exodus_check_extras, src/finder/exodus_finder.c:1145-1200: a prior
+  // catalogue the finder can place, and no checkpoint path beside the
+  // option that turns checkpoints off.
+  const sif_catalogue_t* prior = extras ? extras->prior : nullptr;
   if (extras) {
     if (extras->checkpoint && (opt & SIF_FINDER_NO_CHECKPOINT)) {
       fail(SIF_ERR_INVALID, fmt("checkpoint: %s, with SIF_FINDER_NO_CHECKPOINT set", extras->checkpoint));
       return nullptr;
     }
-    if (extras->checkpoint || (extras->prior && extras->prior->n_voids) || extras->save_memory) {
-      fail(SIF_ERR_UNSUPPORTED,
-           "extras: checkpoints, prior catalogues and save_memory are not supported by the GPU finder");
+    if (extras->checkpoint) {
+      fail(SIF_ERR_UNSUPPORTED, "extras: checkpoints are not supported by the GPU finder");
       return nullptr;
+    }
+    // save_memory changes where the reference keeps the grid's transform, and
+    // nothing of the run; the GPU run keeps its own in device memory.
+    if (prior) {
+      if (prior->units != SIF_COORDINATES_CARTESIAN) {
+        fail(SIF_ERR_INVALID, "prior: centres on the sky (expected Cartesian coordinates)");
+        return nullptr;
+      }
+      if (check_prior(prior->cx, prior->cy, prior->cz, prior->radii, prior->n_voids,
+                      grid->box_length) != SIF_OK)
+        return nullptr;
     }
   }
   if (mesh->n_particles >= 0xffffffffull) {
@@ -716,6 +749,13 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   p.radii.assign(radii, radii + n_radii);
   p.window = g_window;
   p.mesh_ready = e->ev_mesh_ready();
+  if (prior && prior->n_voids) {
+    p.prior_cx = prior->cx;
+    p.prior_cy = prior->cy;
+    p.prior_cz = prior->cz;
+    p.prior_r = prior->radii;
+    p.n_prior = prior->n_voids;
+  }
   float* consume = nullptr;
   if (opt & SIF_FINDER_CONSUME_GRID) consume = (float*)bufs().px.ensure(gb);
   p.consume_out = consume;
@@ -877,7 +917,8 @@ static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceM
                       const R* inject, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
                       uint64_t* n_voids, RunTimings& tm, cudaEvent_t mesh_ready = nullptr,
                       std::vector<RungStat>* stats = &g_stats,
-                      const double* contrast_mean = nullptr) {
+                      const double* contrast_mean = nullptr, const R* prior = nullptr,
+                      uint64_t n_prior = 0) {
   if (check_args(radii, n_radii, threshold, overlap) != SIF_OK) return kErrInvalid;
   RunParamsT<R> p;
   p.grid_n = n_grid;
@@ -891,6 +932,13 @@ static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceM
   p.inject_on_device = true;
   p.mesh_ready = mesh_ready;
   p.contrast_mean = contrast_mean;
+  if (n_prior) {
+    p.prior_cx = prior;
+    p.prior_cy = prior + n_prior;
+    p.prior_cz = prior + 2 * n_prior;
+    p.prior_r = prior + 3 * n_prior;
+    p.n_prior = n_prior;
+  }
   // Kept per thread between runs (cleared, capacity kept): fresh vectors would
   // take their page faults on every run.
   thread_local HostCatalogueT<R> cat;
@@ -917,10 +965,17 @@ template <class R>
 static int exodus_device(const R* delta, uint32_t n_grid, R box, const R* mx, const R* my,
                          const R* mz, const uint32_t* offsets, uint64_t n_particles,
                          uint32_t mesh_cells, const R* radii, uint32_t n_radii, R threshold,
-                         R overlap, uint32_t opt, const R* inject, R* cx, R* cy, R* cz, R* r,
-                         uint64_t capacity, uint64_t* n_voids) {
+                         R overlap, uint32_t opt, const R* inject, const R* prior,
+                         uint64_t n_prior, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
+                         uint64_t* n_voids) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
+  if (n_prior && !prior) return fail(SIF_ERR_INVALID, "prior: NULL with voids to start from");
+  if (n_prior) {
+    const int st = check_prior(prior, prior + n_prior, prior + 2 * n_prior, prior + 3 * n_prior,
+                               n_prior, box);
+    if (st != SIF_OK) return st;
+  }
   DeviceMeshT<R> m;
   m.n_cells = mesh_cells;
   m.box_length = box;
@@ -932,7 +987,8 @@ static int exodus_device(const R* delta, uint32_t n_grid, R box, const R* mx, co
   m.offsets = const_cast<uint32_t*>(offsets);
   RunTimings tm;
   const int st = run_device(e, delta, n_grid, box, m, radii, n_radii, threshold, overlap, opt,
-                            inject, cx, cy, cz, r, capacity, n_voids, tm);
+                            inject, cx, cy, cz, r, capacity, n_voids, tm, nullptr, &g_stats,
+                            nullptr, n_prior ? prior : nullptr, n_prior);
   record_timings(tm);
   return st;
 }
@@ -1243,21 +1299,22 @@ int sifg_exodus_device(const float* delta, uint32_t n_grid, float box, const flo
                        const float* my, const float* mz, const uint32_t* offsets,
                        uint64_t n_particles, uint32_t mesh_cells, const float* radii,
                        uint32_t n_radii, float threshold, float overlap, uint32_t opt,
-                       const float* inject, float* cx, float* cy, float* cz, float* r,
-                       uint64_t capacity, uint64_t* n_voids) {
+                       const float* inject, const float* prior, uint64_t n_prior, float* cx,
+                       float* cy, float* cz, float* r, uint64_t capacity, uint64_t* n_voids) {
   SIFG_LOCKED(exodus_device(delta, n_grid, box, mx, my, mz, offsets, n_particles, mesh_cells,
-                            radii, n_radii, threshold, overlap, opt, inject, cx, cy, cz, r,
-                            capacity, n_voids))
+                            radii, n_radii, threshold, overlap, opt, inject, prior, n_prior, cx,
+                            cy, cz, r, capacity, n_voids))
 }
 int sifg_exodus_device_f64(const double* delta, uint32_t n_grid, double box, const double* mx,
                            const double* my, const double* mz, const uint32_t* offsets,
                            uint64_t n_particles, uint32_t mesh_cells, const double* radii,
                            uint32_t n_radii, double threshold, double overlap, uint32_t opt,
-                           const double* inject, double* cx, double* cy, double* cz, double* r,
-                           uint64_t capacity, uint64_t* n_voids) {
+                           const double* inject, const double* prior, uint64_t n_prior,
+                           double* cx, double* cy, double* cz, double* r, uint64_t capacity,
+                           uint64_t* n_voids) {
   SIFG_LOCKED(exodus_device(delta, n_grid, box, mx, my, mz, offsets, n_particles, mesh_cells,
-                            radii, n_radii, threshold, overlap, opt, inject, cx, cy, cz, r,
-                            capacity, n_voids))
+                            radii, n_radii, threshold, overlap, opt, inject, prior, n_prior, cx,
+                            cy, cz, r, capacity, n_voids))
 }
 int sifg_box_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
                     float box, uint32_t mesh_cells, const float* radii, uint32_t n_radii,

@@ -540,6 +540,32 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   build_void_index(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), 0, box, vstart,
                    vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
   R max_r = 0.0f;
+  if (p.n_prior) {
+    // The prior voids, as though earlier rungs had accepted them: the
+    // catalogue, the overlap mask at scale * r, the void index and the
+    // largest radius (accept_void, exodus_finder.c:656-683).
+    if (p.n_prior >= (1ull << 31)) {
+      set_error(kErrRange, "prior: 2^31 voids or more");
+      return kErrRange;
+    }
+    const uint32_t np = (uint32_t)p.n_prior;
+    ensure_cat(np);
+    const R* cols[4] = {p.prior_cx, p.prior_cy, p.prior_cz, p.prior_r};
+    DevBuf* dst[4] = {&cat_x_, &cat_y_, &cat_z_, &cat_r_};
+    for (int k = 0; k < 4; k++)
+      SIFG_CUDA(cudaMemcpyAsync(dst[k]->ptr, cols[k], np * sizeof(R), cudaMemcpyHostToDevice, st_));
+    for (uint32_t v = 0; v < np; v++)
+      if (p.prior_r[v] > max_r) max_r = p.prior_r[v];
+    RungConstsT<R> pc{};
+    pc.scale = scale;
+    pc.cell = cell;
+    pc.gbox = (R)N * cell;
+    pc.grid_n = N;
+    paint_voids(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), cat_r_.as<R>(), np, mask, pc, st_);
+    n_voids = np;
+    build_void_index(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), n_voids, box, vstart,
+                     vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
+  }
   R* gbuf = grow_to<R>(gbuf_, (size_t)growth_grid() * kGrowCap);
   uint32_t* dcount = grow_to<uint32_t>(dcount_, 16);
   // Gathered particles and visited cells of each rung's sphere growth.

@@ -35,6 +35,14 @@ struct RunParamsT {
   // Recorded once the mesh is on the device, if it is still being copied
   // when the run starts: the first sphere growth waits for it.
   cudaEvent_t mesh_ready = nullptr;
+  // Voids to start from (sif_finder_exodus_extras_t::prior), host memory:
+  // accepted before the first rung and returned first (exodus_finder.c:
+  // 1614-1622, 656-683).
+  const R* prior_cx = nullptr;
+  const R* prior_cy = nullptr;
+  const R* prior_cz = nullptr;
+  const R* prior_r = nullptr;
+  uint64_t n_prior = 0;
 };
 using RunParams = RunParamsT<float>;
 

@@ -1539,23 +1539,15 @@ void commit_round(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Voi
   SIFG_LAUNCH_CHECK();
 }
 
-// paint_sphere with set = 1 (src/finder/utils.c:965-1027), one warp per void:
-// every node whose centre lies within scale * r, measured as the reference
+// paint_sphere with set = 1 (src/finder/utils.c:965-1027) by one warp: every
+// node whose centre lies within scale * r, measured as the reference
 // measures it.
 template <class R>
-__device__ __forceinline__ void paint_pass(const SurvivorsT<R>& sv, const uint32_t* acc,
-                                           uint32_t* counters, uint32_t slot, uint32_t* mask,
-                                           const RungConstsT<R>& rc) {
-  const uint32_t lo = __ldcg(counters + kRoundBegin + slot), hi = __ldcg(counters);
-  // No round accepts while a paint runs: hi is where the next round begins.
-  if (blockIdx.x == 0 && threadIdx.x == 0) counters[kRoundBegin + (slot + 1) % kRoundRing] = hi;
-  const unsigned lane = threadIdx.x & 31u;
-  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+__device__ __forceinline__ void paint_one(R cx, R cy, R cz, R r, uint32_t* mask,
+                                          const RungConstsT<R>& rc, unsigned lane) {
   const uint32_t n = rc.grid_n;
-  for (uint32_t a = lo + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); a < hi; a += warps) {
-    const uint32_t i = __ldcg(acc + a);
-    const R cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i];
-    const R rt = fmul(rc.scale, sv.r[i]);
+  {
+    const R rt = fmul(rc.scale, r);
     const R r2 = fmul(rt, rt);
     const R inv = fdiv(R(1.0f), rc.cell);
     const R half = fmul(rc.gbox, R(0.5f));
@@ -1584,6 +1576,41 @@ __device__ __forceinline__ void paint_pass(const SurvivorsT<R>& sv, const uint32
       }
     }
   }
+}
+
+// The voids the rounds accepted, one warp each.
+template <class R>
+__device__ __forceinline__ void paint_pass(const SurvivorsT<R>& sv, const uint32_t* acc,
+                                           uint32_t* counters, uint32_t slot, uint32_t* mask,
+                                           const RungConstsT<R>& rc) {
+  const uint32_t lo = __ldcg(counters + kRoundBegin + slot), hi = __ldcg(counters);
+  // No round accepts while a paint runs: hi is where the next round begins.
+  if (blockIdx.x == 0 && threadIdx.x == 0) counters[kRoundBegin + (slot + 1) % kRoundRing] = hi;
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t a = lo + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); a < hi; a += warps) {
+    const uint32_t i = __ldcg(acc + a);
+    paint_one(sv.cx[i], sv.cy[i], sv.cz[i], sv.r[i], mask, rc, lane);
+  }
+}
+
+// Voids given before the first rung (a prior catalogue), one warp each.
+template <class R>
+__global__ void paint_voids_kernel(const R* __restrict__ cx, const R* __restrict__ cy,
+                                   const R* __restrict__ cz, const R* __restrict__ r, uint32_t n_voids,
+                                   uint32_t* mask, RungConstsT<R> rc) {
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); v < n_voids; v += warps)
+    paint_one(cx[v], cy[v], cz[v], r[v], mask, rc, threadIdx.x & 31u);
+}
+
+template <class R>
+void paint_voids(const R* cx, const R* cy, const R* cz, const R* r, uint32_t n_voids,
+                 uint32_t* mask, RungConstsT<R> rc, cudaStream_t st) {
+  if (n_voids == 0) return;
+  paint_voids_kernel<R><<<grid_for((uint64_t)n_voids * 32, 256), 256, 0, st>>>(cx, cy, cz, r, n_voids,
+                                                                              mask, rc);
+  SIFG_LAUNCH_CHECK();
 }
 
 // paint_sphere with set = 1 (src/finder/utils.c:965-1027), one warp per void:
@@ -1808,6 +1835,8 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
                                 uint32_t*, uint32_t*, uint32_t, uint32_t, cudaStream_t);           \
   template void paint_new<R>(SurvivorsT<R>, const uint32_t*, uint32_t*, uint32_t, uint32_t*,       \
                              RungConstsT<R>, uint32_t, cudaStream_t);                              \
+  template void paint_voids<R>(const R*, const R*, const R*, const R*, uint32_t, uint32_t*,        \
+                               RungConstsT<R>, cudaStream_t);                                      \
   template bool commit_rounds<R>(SurvivorsT<R>, const uint32_t*, SurvivorGridT<R>, VoidViewT<R>,   \
                                  uint32_t*, RungConstsT<R>, uint8_t*, uint8_t*, uint32_t*,         \
                                  uint32_t*, uint32_t, uint32_t, unsigned*, uint32_t, cudaStream_t);\

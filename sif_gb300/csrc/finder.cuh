@@ -234,6 +234,11 @@ bool commit_rounds(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Vo
 // allows it; 1: a launch per round. The catalogue does not depend on it.
 void set_commit_mode(int mode);
 
+// Paints n_voids given voids (a prior catalogue) into the mask at scale * r
+// (rc: scale, cell, gbox, grid_n), as the commit paints the ones it accepts.
+template <class R>
+void paint_voids(const R* cx, const R* cy, const R* cz, const R* r, uint32_t n_voids,
+                 uint32_t* mask, RungConstsT<R> rc, cudaStream_t st);
 // Paints the voids round `round` accepted and records where the next round's
 // acceptances begin.
 template <class R>

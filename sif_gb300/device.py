@@ -116,17 +116,23 @@ def _catalogue_arrays(cap, dtype=np.float32):
 
 
 def exodus(delta, n_grid, box, mesh, mesh_cells, radii, threshold, overlap=0.0, options=0,
-           inject=None, capacity=1 << 22):
-    """The finder on device data. mesh = (mx, my, mz, offsets, ...)."""
+           inject=None, capacity=1 << 22, prior=None):
+    """The finder on device data. mesh = (mx, my, mz, offsets, ...);
+    prior: (cx, cy, cz, r) host arrays, voids to start from."""
     _, _, nt = _form(delta)
     radii = np.ascontiguousarray(radii, dtype=nt)
     cols = _catalogue_arrays(capacity, nt)
     n = C.c_uint64(0)
     mx, my, mz, offs = mesh[:4]
+    packed = np.ascontiguousarray(np.concatenate([np.asarray(c, nt) for c in prior])) \
+        if prior is not None else None
+    n_prior = len(prior[0]) if prior is not None else 0
     st = _fn("sifg_exodus_device", delta)(_ptr(delta), n_grid, box, _ptr(mx), _ptr(my), _ptr(mz),
                                 _ptr(offs), mx.numel(), mesh_cells,
                                 radii.ctypes.data_as(C.c_void_p), len(radii), threshold, overlap,
-                                options, _ptr(inject), *[c.ctypes.data_as(C.c_void_p) for c in cols],
+                                options, _ptr(inject),
+                                packed.ctypes.data_as(C.c_void_p) if packed is not None else None,
+                                n_prior, *[c.ctypes.data_as(C.c_void_p) for c in cols],
                                 capacity, C.byref(n))
     _check(st, "exodus")
     return tuple(c[: n.value].copy() for c in cols)

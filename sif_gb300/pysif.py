@@ -162,11 +162,24 @@ def _exodus(grid, mesh, radii, threshold, variant="excursion-set", *, checkpoint
     if variant not in _VARIANTS:
         raise ValueError(f"variant: {variant!r}")
     radii = np.ascontiguousarray(radii, dtype=np.float32)
-    extras = None
-    if checkpoint or prior is not None or save_memory:
-        raise NotImplementedError("checkpoints, prior catalogues and save_memory")
+    if checkpoint:
+        raise NotImplementedError("checkpoints")
+    extras, keep = None, []
+    if prior is not None or save_memory:
+        cat = None
+        if prior is not None:
+            cols = [np.ascontiguousarray(c, dtype=np.float32) for c in
+                    (prior.as_tuple() if isinstance(prior, Catalogue) else prior)]
+            keep.extend(cols)
+            cat = abi.sif_catalogue_t()
+            cat.cx, cat.cy, cat.cz, cat.radii = (_P(c) for c in cols)
+            cat.units = 0
+            cat.n_voids = cat.capacity = len(cols[0])
+            keep.append(cat)
+        extras = abi.sif_finder_exodus_extras_t(None, C.pointer(cat) if cat is not None else None,
+                                                int(keep_checkpoint), int(bool(save_memory)))
     ptr = lib.sif_finder_exodus(grid._ptr, mesh._ptr, _P(radii), len(radii), threshold,
-                                _VARIANTS[variant], extras)
+                                _VARIANTS[variant], C.byref(extras) if extras is not None else None)
     return _take_catalogue(lib, ptr, "exodus")
 
 

@@ -79,11 +79,20 @@ def make_box32(path):
         out[f"cat_{name}_opt"] = np.array([overlap, opt], np.float64)
     # The default run on its own fields is the run that captured them.
     assert all(np.array_equal(a, out[f"cat_default_{k}"]) for a, k in zip(cat, "cx cy cz r".split()))
+    # A prior catalogue (sif_finder_exodus_extras_t::prior): the ten largest
+    # voids of the search-2.0 run, given to a default run, which returns them
+    # first and adds what respects them.
+    order = np.argsort(-out["cat_search_2_00_r"], kind="stable")[:10]
+    prior = tuple(out[f"cat_search_2_00_{k}"][order] for k in ("cx", "cy", "cz", "r"))
+    c = R.exodus_raw(lib, g, m, radii, p["threshold"], inject=fields, prior=prior)
+    for k, col, pc in zip(("cx", "cy", "cz", "r"), c, prior):
+        out[f"prior_{k}"] = pc
+        out[f"cat_prior_{k}"] = col
     m.free()
     g.free()
     f.free()
     np.savez_compressed(path, **out)
-    print(f"{path}: {len(cat[0])} voids over {len(radii)} rungs")
+    print(f"{path}: {len(cat[0])} voids over {len(radii)} rungs; with the prior {len(c[0])}")
 
 
 def make_box32_f64(path):

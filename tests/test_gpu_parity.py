@@ -189,6 +189,67 @@ def test_catalogue_matches_reference_golden(dev, golden_box32, name):
     assert same_catalogue(cat, want)
 
 
+@pytest.mark.parametrize("mode", [1, 2], ids=["cta", "warp"])
+def test_catalogue_with_prior_matches_reference_golden(dev, golden_box32, mode):
+    """Ten voids to start from (sif_finder_exodus_extras_t::prior): accepted
+    before the first rung, returned first, and respected by every rung after;
+    the reference's catalogue on its own fields, by each growth kernel."""
+    g = golden_box32
+    n, box, thr, n_mesh = int(g["params"][0]), float(g["params"][1]), float(g["params"][5]), int(g["params"][6])
+    delta, fields = _cuda(g["delta"], g["fields"].reshape(-1))
+    prior = tuple(g[f"prior_{k}"] for k in ("cx", "cy", "cz", "r"))
+    dev.set_growth_mode(mode)
+    try:
+        cat = dev.exodus(delta, n, box, _golden_mesh(g), n_mesh, g["radii"], thr, inject=fields,
+                         prior=prior)
+    finally:
+        dev.set_growth_mode(0)
+    want = tuple(g[f"cat_prior_{k}"] for k in ("cx", "cy", "cz", "r"))
+    assert len(cat[0]) == len(want[0])
+    assert same_catalogue(cat, want)
+
+
+@pytest.mark.parametrize("bad", ["radius_zero", "radius_nan", "centre_outside", "centre_negative"])
+def test_prior_checked_as_the_reference_checks_it(dev, golden_box32, bad):
+    """sif__exodus_check_extras (src/finder/exodus_finder.c:1163-1197): a radius
+    that is not positive and finite, or a centre outside [0, box), is refused."""
+    g = golden_box32
+    n, box, thr, n_mesh = int(g["params"][0]), float(g["params"][1]), float(g["params"][5]), int(g["params"][6])
+    delta, fields = _cuda(g["delta"], g["fields"].reshape(-1))
+    cx, cy, cz, r = (g[f"prior_{k}"].copy() for k in ("cx", "cy", "cz", "r"))
+    if bad == "radius_zero":
+        r[3] = 0.0
+    elif bad == "radius_nan":
+        r[3] = np.nan
+    elif bad == "centre_outside":
+        cy[2] = box
+    else:
+        cz[1] = -1e-3
+    with pytest.raises(Exception, match="prior"):
+        dev.exodus(delta, n, box, _golden_mesh(g), n_mesh, g["radii"], thr, inject=fields,
+                   prior=(cx, cy, cz, r))
+
+
+def test_pysif_exodus_with_prior_and_save_memory(gpu_lib):
+    """finders.exodus(prior=..., save_memory=True) through sif's C API: the
+    prior voids come back first and unchanged; save_memory changes nothing."""
+    from test_oracle import _holes_field
+
+    pysif = gpu_lib
+    x, y, z, holes = _holes_field()
+    f = pysif.Field(x, y, z)
+    g = pysif.Grid(32, 200.0)
+    g.assign_cic(f)
+    g.to_density_contrast()
+    m = pysif.ChainMesh(8, 200.0, f, drop_indices=True)
+    radii = np.array([30, 25, 20, 16, 13, 10], np.float32)
+    plain = pysif.finders.exodus(g, m, radii, -0.7).as_tuple()
+    prior = tuple(np.asarray(c[:2], np.float32) for c in plain)
+    cat = pysif.finders.exodus(g, m, radii, -0.7, prior=prior, save_memory=True).as_tuple()
+    assert all(np.array_equal(a[:2], b) for a, b in zip(cat, prior))
+    assert same_catalogue(pysif.finders.exodus(g, m, radii, -0.7, save_memory=True).as_tuple(), plain)
+
+
 EXTEND_SETS = ["minima_f1", "extend_minima_f1", "extend_f1", "extend"]
 
 

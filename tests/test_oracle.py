@@ -54,6 +54,21 @@ def test_oracle_catalogue_matches_golden(oracle, golden_box32, name):
     assert same_catalogue(cat, want)
 
 
+def test_oracle_catalogue_with_prior_matches_golden(oracle, golden_box32):
+    """sif_finder_exodus_extras_t::prior (src/finder/exodus_finder.c:1614-1622):
+    the voids to start from, accepted before the first rung and returned first;
+    the reference's catalogue with ten of them, on its own fields."""
+    g = golden_box32
+    n, box, thr, n_mesh = int(g["params"][0]), float(g["params"][1]), float(g["params"][5]), int(g["params"][6])
+    m = oracle.OracleMesh(g["x"], g["y"], g["z"], n_mesh, box)
+    prior = tuple(g[f"prior_{k}"] for k in ("cx", "cy", "cz", "r"))
+    cat = oracle.exodus(g["delta"], m, g["radii"], n, box, thr, n_threads=2, inject=g["fields"],
+                        prior=prior)
+    want = tuple(g[f"cat_prior_{k}"] for k in ("cx", "cy", "cz", "r"))
+    assert same_catalogue(cat, want)
+    assert all(np.array_equal(a[:10], b) for a, b in zip(want, prior))
+
+
 EXTEND_SETS = ["minima_f1", "extend_minima_f1", "extend_f1", "extend"]
 
 
