@@ -431,7 +431,7 @@ typedef struct {
 } sifg_box_job_t;
 int sifg_box_batch_device(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines,
                           uint32_t* n_engines_used);
-/* Times the batch at 1, 2, 4 and 8 engines (each count run twice, the second
+/* Times the batch at 1, 2, 3, 4, 6 and 8 engines (each count run twice, the second
  * run timed), keeps the fastest for batches of this size (total particles and
  * job count, to a factor of two) and returns it in *n_engines. The catalogues
  * do not depend on the choice. */

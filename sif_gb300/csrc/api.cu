@@ -1220,14 +1220,14 @@ static int run_batch(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engines) 
   return SIF_OK;
 }
 
-// Times the batch at 1, 2, 4 and 8 engines (capped by the job count) and
+// Times the batch at 1, 2, 3, 4, 6 and 8 engines (capped by the job count) and
 // keeps the fastest for batches of this size. Each count runs twice and the
 // second run is timed: an engine's first boxes of a size make its transform
 // plans, a cost that later batches do not pay.
 static int autotune_batch(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t* best_out) {
   uint32_t best = 1;
   double best_ms = 1e300;
-  for (uint32_t k : {1u, 2u, 4u, 8u}) {
+  for (uint32_t k : {1u, 2u, 3u, 4u, 6u, 8u}) {
     if (k > n_jobs && k > 1) break;
     int st = run_batch(jobs, n_jobs, k);
     if (st != SIF_OK) return st;
