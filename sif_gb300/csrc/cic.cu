@@ -455,8 +455,11 @@ __global__ void mean_final_kernel(const double* __restrict__ partial, uint64_t n
 
 template <class R>
 __global__ void contrast_kernel(R* __restrict__ v, uint64_t n, const double* __restrict__ mean) {
-  const double m = mean[0];
-  const R inv = (R)(1.0 / m);
+  // The double division once a block (this GPU's FP64 rate is low).
+  __shared__ R inv_s;
+  if (threadIdx.x == 0) inv_s = (R)(1.0 / mean[0]);
+  __syncthreads();
+  const R inv = inv_s;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     v[i] = fsub(fmul(v[i], inv), R(1.0f));

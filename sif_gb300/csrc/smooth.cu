@@ -654,6 +654,11 @@ __global__ void __launch_bounds__(16 * kRowsPerCta, 4)
   const float4* src = reinterpret_cast<const float4*>(grid + ((size_t)x * 512 + y0) * 512);
   for (uint32_t f = threadIdx.x; f < kRowsPerCta * 128; f += blockDim.x)
     cp_async16(buf + (f >> 7) * kRowSlots + 2 * (f & 127u), src + f);
+  // With the mean, the rows are the density: its contrast, as the contrast
+  // kernel computes it (inv rounded from the double 1 / mean), the double
+  // division done once for the CTA while its copies land.
+  __shared__ float inv_s;
+  if (mean && threadIdx.x == 0) inv_s = (float)(1.0 / __ldg(mean));
   cp_async_wait_all();
   __syncthreads();
   const unsigned j = threadIdx.x & 15u;
@@ -661,9 +666,7 @@ __global__ void __launch_bounds__(16 * kRowsPerCta, 4)
   const float2* twb = tw + 512;
   const float2* wpre = tw + 768;
   float2 v[16];
-  // With the mean, the rows are the density: its contrast, as the contrast
-  // kernel computes it (inv rounded from the double 1 / mean).
-  const float inv = mean ? (float)(1.0 / __ldg(mean)) : 0.f;
+  const float inv = mean ? inv_s : 0.f;
 #pragma unroll
   for (int r = 0; r < 16; r++) {
     v[r] = row[j + 16u * r];
