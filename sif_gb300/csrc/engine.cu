@@ -143,10 +143,11 @@ void qsort_serial(Rec<K>* a, int64_t lo, int64_t hi) {
 
 // The two sides of a partition are disjoint, so sorting them in any order, on
 // any threads, leaves the serial sort's permutation: tasks are spawned down
-// to a few thousand elements, well below the reference's task cutoff
+// to about a thousand elements, well below the reference's task cutoff
 // (SIF_QUICKSORT_TASK_CUTOFF, include/sif/utils/sort.h:104), which only
-// bounds its task overhead.
-constexpr int64_t kTaskCutoff = 4096;
+// bounds its task overhead. (On 16 Grace cores, 100k candidates: 1.05 ms at
+// 1024, 1.22 at 4096, 1.55 at 256, 1.71 at 16384.)
+constexpr int64_t kTaskCutoff = 1024;
 
 template <class K>
 void qsort_tasks(Rec<K>* a, int64_t lo, int64_t hi) {
