@@ -473,11 +473,16 @@ void sifg_set_scan_mode(int mode);
  * It has no counterpart in the reference. Its scratch is a static device
  * array of the library (about 17 MB, held on every GPU that loads the
  * library until the process exits), which limits it to 1,048,576 particles
- * and 262,144 mesh cells; larger inputs fail with SIF_ERR_RANGE. It calls no
- * cudaMalloc, cudaFree or allocating library routine. The first call on a
- * device looks up the array's device address; make that first call before
- * any stream capture. Every call shares the one array, so calls that overlap
- * on the GPU race; the library runs them on its one stream, in order. */
+ * and 64^3 = 262,144 mesh cells; larger inputs fail with SIF_ERR_RANGE. It
+ * calls no cudaMalloc, cudaFree or allocating library routine. The first call
+ * on a device after sif_system_init() looks up the array's device address.
+ * Every call synchronises the library's stream before it returns (it reads
+ * the box check's count back), so it must not be made while a stream capture
+ * is in progress. Every call shares the one array, so calls that overlap on
+ * the GPU would race; the library holds its API lock for the whole call and
+ * runs it on its one stream, so calls from several host threads run one after
+ * another. A caller that resets the device calls sif_system_finalise() and
+ * sif_system_init() again before the next call. */
 int sifg_mesh_device_noalloc(const float* x, const float* y, const float* z, uint64_t n,
                              uint32_t n_cells, float box, float* mx, float* my, float* mz,
                              uint32_t* offsets, uint32_t* orig);

@@ -29,6 +29,8 @@
 
 namespace sifg {
 
+void noalloc_forget();  // noalloc.cu
+
 namespace {
 std::mutex g_mu;
 std::unique_ptr<Engine> g_engine;
@@ -231,10 +233,13 @@ static void record_timings(RunTimings& t) {
   g_timings.growth_cells = t.growth_cells;
 }
 
-// The library's stream and device, under the API lock; false (with the error
-// set) before sif_system_init().
+// The API lock, for entry points outside this file that hold it for a whole
+// call (every entry point here does).
+std::mutex& api_mutex() { return g_mu; }
+
+// The library's stream and device; false (with the error set) before
+// sif_system_init(). The caller holds api_mutex().
 bool api_stream(cudaStream_t* st, int* device) {
-  std::lock_guard<std::mutex> lk(g_mu);
   if (!g_init || !g_engine) {
     set_error(SIF_ERR_UNINITIALISED, "sif_system_init() has not been called");
     return false;
@@ -290,6 +295,7 @@ int sif_system_init(sif_config_t* config) {
 
 void sif_system_finalise(void) {
   std::lock_guard<std::mutex> lk(g_mu);
+  noalloc_forget();
   g_engine.reset();
   host_pool_trim();
   g_init = false;
@@ -452,6 +458,11 @@ static sif_chain_mesh_t* mesh_alloc(uint32_t n_cells, sif_real box, sif_field_t*
   if (check_field(field, "mesh") != SIF_OK) return nullptr;
   if (n_cells == 0) {
     fail(SIF_ERR_INVALID, "n_cells: 0 (expected > 0)");
+    return nullptr;
+  }
+  if (n_cells > kMaxMeshSide) {
+    fail(SIF_ERR_RANGE, fmt("n_cells: %u (the GPU mesh holds at most %u^3 cells)", n_cells,
+                            kMaxMeshSide));
     return nullptr;
   }
   if (!(box > 0.0f)) {
@@ -673,6 +684,11 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
     fail(SIF_ERR_UNSUPPORTED, "mesh: weighted meshes are not supported by the GPU finder");
     return nullptr;
   }
+  if (mesh->n_cells == 0 || mesh->n_cells > kMaxMeshSide) {
+    fail(SIF_ERR_RANGE, fmt("mesh: %u cells a side (the GPU mesh holds 1 to %u)", mesh->n_cells,
+                            kMaxMeshSide));
+    return nullptr;
+  }
   // sif__exodus_check_extras, src/finder/exodus_finder.c:1145-1200: a prior
   // catalogue the finder can place, and no checkpoint path beside the
   // option that turns checkpoints off.
@@ -861,6 +877,8 @@ static int mesh_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t 
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   if (n_cells == 0 || !(box > 0.0f)) return fail(SIF_ERR_INVALID, "mesh: bad geometry");
+  if (n_cells > kMaxMeshSide)
+    return fail(SIF_ERR_RANGE, fmt("mesh: %u cells a side (at most %u)", n_cells, kMaxMeshSide));
   cudaStream_t s = e->stream();
   const int st = check_in_box(x, y, z, n, box, "field", s, e->io.flag);
   if (st != SIF_OK) return st;
@@ -971,6 +989,9 @@ static int exodus_device(const R* delta, uint32_t n_grid, R box, const R* mx, co
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   if (n_prior && !prior) return fail(SIF_ERR_INVALID, "prior: NULL with voids to start from");
+  if (mesh_cells == 0 || mesh_cells > kMaxMeshSide)
+    return fail(SIF_ERR_RANGE, fmt("mesh: %u cells a side (the GPU mesh holds 1 to %u)", mesh_cells,
+                                   kMaxMeshSide));
   if (n_prior) {
     const int st = check_prior(prior, prior + n_prior, prior + 2 * n_prior, prior + 3 * n_prior,
                                n_prior, box);
@@ -1002,6 +1023,8 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
                    R overlap, uint32_t opt, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
                    uint64_t* n_voids, RunTimings& tm, std::vector<RungStat>* stats) {
   if (n_grid < 4 || mesh_cells == 0) return fail(SIF_ERR_INVALID, "grid or mesh: bad size");
+  if (mesh_cells > kMaxMeshSide)
+    return fail(SIF_ERR_RANGE, fmt("mesh: %u cells a side (at most %u)", mesh_cells, kMaxMeshSide));
   BoxBufs& io = e->io;
   cudaStream_t s = e->stream();
   const uint64_t cells = (uint64_t)n_grid * n_grid * n_grid;

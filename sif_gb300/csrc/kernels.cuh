@@ -13,6 +13,12 @@ namespace sifg {
 
 constexpr int kCicTile = 16;  // CIC tile side, in grid cells
 
+// The largest chain mesh side the GPU builds and reads: its cell ids and
+// offsets are 32-bit, and 1625^3 + 1 is the last cube (plus the end offset)
+// below 2^32. The reference's 64-bit offsets have no such bound; a larger
+// mesh is refused with SIF_ERR_RANGE before anything is cubed.
+constexpr uint32_t kMaxMeshSide = 1625;
+
 // Times a kernel with events on the stream it is launched on; accumulates.
 struct KernelTimer {
   std::vector<cudaEvent_t> starts, stops;

@@ -13,8 +13,8 @@
 //
 // The scratch holds what sifg_mesh_device's scratch holds: the (source index,
 // x, y, z) records of the scatter, the per-cell cursors and the scan's chunk
-// totals, plus two counters of the box check. Its size fixes the limits:
-// at most kNoAllocMaxParticles particles and kNoAllocMaxCells mesh cells.
+// totals, plus the box check's counter. Its size fixes the limits: at most
+// kNoAllocMaxParticles particles and kNoAllocMaxSide^3 mesh cells.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -26,13 +26,16 @@
 
 namespace sifg {
 
+std::mutex& api_mutex();
 bool api_stream(cudaStream_t* st, int* device);
 
 constexpr uint64_t kNoAllocMaxParticles = 1ull << 20;  // 1,048,576 particles
-constexpr uint64_t kNoAllocMaxCells = 1ull << 18;      // 262,144 mesh cells (64^3)
+constexpr uint32_t kNoAllocMaxSide = 64;               // mesh cells a side
+constexpr uint64_t kNoAllocMaxCells = (uint64_t)kNoAllocMaxSide * kNoAllocMaxSide * kNoAllocMaxSide;
 
 // Layout: the build's scratch (records, then cursors: mesh_scratch_bytes()
-// at the limits), the scan's chunk totals, two counters.
+// at the limits), the scan's chunk totals, the box check's counter (in a
+// 256-byte slot).
 constexpr size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 constexpr size_t kMeshScratchBytes =
     a256(kNoAllocMaxParticles * 16 + (kNoAllocMaxCells + 1) * 4 + 1024);
@@ -45,9 +48,18 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 // The array's device address, per device. In host code g_noalloc_scratch
 // names a host-side stand-in, not device memory, so the address comes from
-// cudaGetSymbolAddress, with that device current.
+// cudaGetSymbolAddress, with that device current. It is looked up by the
+// first call on a device after sif_system_init() and forgotten by
+// sif_system_finalise(): a caller that resets the device (cudaDeviceReset,
+// which also ends the library's streams) finalises and initialises the
+// library again, and the next call looks the address up anew.
 static std::mutex g_setup_mu;
 static void* g_scratch_addr[64] = {};
+
+void noalloc_forget() {
+  std::lock_guard<std::mutex> lk(g_setup_mu);
+  for (void*& p : g_scratch_addr) p = nullptr;
+}
 
 static int scratch_address(int device, void** out) {
   if (device < 0 || device >= 64) return SIF_ERR_RANGE;
@@ -66,9 +78,10 @@ static int scratch_address(int device, void** out) {
   return SIF_OK;
 }
 
-// sif__field_check_in_box (src/structures/field.c:889-935) into two counters
-// of the static scratch: coordinates outside the box beyond 4 float epsilons
-// of it, and those within (folded by the build).
+// sif__field_check_in_box (src/structures/field.c:889-935) into a counter of
+// the static scratch: the particles with a coordinate outside the box by more
+// than 4 float epsilons of it, or not a number. Those within that tolerance
+// are folded by the build, as the reference folds them.
 __global__ void noalloc_box_check_kernel(const float* __restrict__ x, const float* __restrict__ y,
                                          const float* __restrict__ z, uint64_t n, float box,
                                          double tol, unsigned long long* __restrict__ out) {
@@ -96,6 +109,10 @@ extern "C" int sifg_mesh_device_noalloc(const float* x, const float* y, const fl
                                         uint64_t n, uint32_t n_cells, float box, float* mx,
                                         float* my, float* mz, uint32_t* offsets,
                                         uint32_t* orig) {
+  // The whole call under the API lock: its enqueues on the library's stream
+  // do not interleave with another host thread's call, and the stream
+  // outlives it (sif_system_finalise waits for the lock).
+  std::lock_guard<std::mutex> lk(api_mutex());
   cudaStream_t st;
   int device;
   if (!api_stream(&st, &device)) return SIF_ERR_UNINITIALISED;
@@ -103,13 +120,14 @@ extern "C" int sifg_mesh_device_noalloc(const float* x, const float* y, const fl
     set_error(SIF_ERR_INVALID, "allocation-free mesh: n_cells must be positive and box > 0");
     return SIF_ERR_INVALID;
   }
-  const uint64_t cells = (uint64_t)n_cells * n_cells * n_cells;
-  if (n > kNoAllocMaxParticles || cells > kNoAllocMaxCells) {
+  // The side is bounded before it is cubed: a cube of a large side would
+  // wrap around 64 bits and pass a bound on the cube.
+  if (n > kNoAllocMaxParticles || n_cells > kNoAllocMaxSide) {
     set_error(SIF_ERR_RANGE,
               "allocation-free mesh: " + std::to_string(n) + " particles in " +
-                  std::to_string(cells) + " cells exceeds its fixed scratch (at most " +
+                  std::to_string(n_cells) + "^3 cells exceeds its fixed scratch (at most " +
                   std::to_string(kNoAllocMaxParticles) + " particles and " +
-                  std::to_string(kNoAllocMaxCells) + " cells); use sifg_mesh_device");
+                  std::to_string(kNoAllocMaxSide) + "^3 cells); use sifg_mesh_device");
     return SIF_ERR_RANGE;
   }
   try {
@@ -120,7 +138,7 @@ extern "C" int sifg_mesh_device_noalloc(const float* x, const float* y, const fl
     uint32_t* scan_sums = (uint32_t*)((char*)scratch + kMeshScratchBytes);
     unsigned long long* counters =
         (unsigned long long*)((char*)scratch + kMeshScratchBytes + kScanSumsBytes);
-    SIFG_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), st));
+    SIFG_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long), st));
     if (n) {
       noalloc_box_check_kernel<<<grid_for(n, 256), 256, 0, st>>>(
           x, y, z, n, box, (double)box * 4.0 * (double)FLT_EPSILON, counters);

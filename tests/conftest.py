@@ -11,6 +11,16 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
+def reference_dir():
+    """The reference's source checkout, where one is present: the directory
+    SIF_REFERENCE_DIR names, else a checkout named `reference` beside this
+    repository; None where there is neither (the GPU machines)."""
+    for cand in (os.environ.get("SIF_REFERENCE_DIR"), os.path.join(ROOT, "..", "reference")):
+        if cand and os.path.isfile(os.path.join(cand, "include", "sif", "finder", "exodus_finder.h")):
+            return os.path.abspath(cand)
+    return None
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
     config.addinivalue_line("markers", "slow: a full-size workload")

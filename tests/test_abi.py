@@ -79,19 +79,78 @@ def test_library_exports_every_declared_symbol(lib):
     assert set(_declared()) == set(_lib.EXPORTED)
 
 
-def test_struct_sizes_match_the_reference_layout():
+_PROBE_HEADERS = {
+    "reference": ["sif/structures/field.h", "sif/structures/grid.h", "sif/structures/chain_mesh.h",
+                  "sif/structures/catalogue.h", "sif/finder/exodus_finder.h", "sif/core/system.h"],
+    "gb300": ["sif_gb300.h"],
+}
+
+
+def _layout_probe(include_dir, headers, structs, defines=()):
+    """Compiles a C program against `headers` that prints sizeof of each
+    struct and offsetof of each of its fields (the ctypes field names), and
+    returns {struct: [size, offset, ...]}."""
+    import subprocess
+    import tempfile
+
+    lines = ["#include <stddef.h>", "#include <stdio.h>"]
+    lines += [f'#include "{h}"' for h in headers]
+    lines.append("int main(void) {")
+    for name, cls in structs.items():
+        args = [f"sizeof({name})"] + [f"offsetof({name}, {f})" for f, _ in cls._fields_]
+        lines.append(f'  printf("{name}' + " %zu" * len(args) + '\\n", ' + ", ".join(args) + ");")
+    lines.append("  return 0;\n}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "probe.c")
+        open(c, "w").write("\n".join(lines) + "\n")
+        exe = os.path.join(d, "probe")
+        subprocess.run(["gcc", "-std=gnu99", "-I", include_dir, *[f"-D{x}" for x in defines], c,
+                        "-o", exe, "-lm"], check=True, capture_output=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    return {ln.split()[0]: [int(v) for v in ln.split()[1:]] for ln in out.strip().splitlines()}
+
+
+def _ctypes_layout(structs):
+    return {name: [C.sizeof(cls)] + [getattr(cls, f).offset for f, _ in cls._fields_]
+            for name, cls in structs.items()}
+
+
+def _structs(real):
     from sif_gb300 import abi
 
-    # LP64 sizes of the reference's structs (float build), as its own headers
-    # compile them.
-    assert C.sizeof(abi.sif_grid_t) == 48
-    assert C.sizeof(abi.sif_chain_mesh_t) == 136
-    assert C.sizeof(abi.sif_catalogue_t) == 104
-    assert C.sizeof(abi.sif_field_t) == 144
-    assert C.sizeof(abi.sif_finder_exodus_extras_t) == 24
-    assert C.sizeof(abi.sif_config_t) == 40
-    assert abi.sif_chain_mesh_t.cell_offsets.offset == 128
-    assert abi.sif_catalogue_t.n_voids.offset == 88
+    field, grid, mesh, cat, extras = (
+        (abi.sif_field_t, abi.sif_grid_t, abi.sif_chain_mesh_t, abi.sif_catalogue_t,
+         abi.sif_finder_exodus_extras_t) if real == "float" else abi.STRUCTS_F64)
+    return {"sif_field_t": field, "sif_grid_t": grid, "sif_chain_mesh_t": mesh,
+            "sif_catalogue_t": cat, "sif_finder_exodus_extras_t": extras,
+            "sif_config_t": abi.sif_config_t}
+
+
+def test_header_struct_layouts_match_the_ctypes_mirror():
+    """include/sif_gb300.h compiled: every struct's size and every field's
+    offset equal the ctypes structs pysif's mirror and the tests use."""
+    structs = _structs("float")
+    got = _layout_probe(os.path.join(ROOT, "include"), _PROBE_HEADERS["gb300"], structs)
+    assert got == _ctypes_layout(structs)
+
+
+@pytest.mark.parametrize("real", ["float", "double"])
+def test_struct_layouts_match_the_reference_headers(real):
+    """The reference's own headers compiled (its float build, and its
+    SIF_USE_DOUBLE build whose layouts the _f64 entry points' callers use):
+    sizeof and offsetof of every field of the boundary's structs equal the
+    ctypes mirror, and, for the float build, this library's header."""
+    from conftest import reference_dir
+
+    ref = reference_dir()
+    if ref is None:
+        pytest.skip("no reference checkout (SIF_REFERENCE_DIR)")
+    structs = _structs(real)
+    want = _layout_probe(os.path.join(ref, "include"), _PROBE_HEADERS["reference"], structs,
+                         ("SIF_USE_DOUBLE",) if real == "double" else ())
+    assert _ctypes_layout(structs) == want
+    if real == "float":
+        assert _layout_probe(os.path.join(ROOT, "include"), _PROBE_HEADERS["gb300"], structs) == want
 
 
 def _host_ranks_vs_oracle(lib, oracle, d):

@@ -109,6 +109,26 @@ def test_mesh_matches_oracle(dev, oracle, n_cells):
     assert np.array_equal(orig.cpu().numpy().astype(np.uint64), m.orig)
 
 
+@pytest.mark.parametrize("n_cells", [1626, 1 << 22])
+def test_mesh_refuses_a_side_past_32_bit_offsets(gpu_lib, n_cells):
+    """The GPU mesh keeps 32-bit cell ids and offsets: a side whose cube
+    (plus the end offset) passes 2^32, or whose cube wraps in 64 bits, is
+    refused with SIF_ERR_RANGE before anything is cubed or allocated."""
+    import ctypes as C
+
+    import torch
+
+    from sif_gb300 import _lib
+
+    lib = _lib.load()
+    xs = [torch.zeros(16, dtype=torch.float32, device="cuda") for _ in range(3)]
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    st = lib.sifg_mesh_device(p(xs[0]), p(xs[1]), p(xs[2]), 16, n_cells, 100.0, p(xs[0]),
+                              p(xs[1]), p(xs[2]), p(xs[0]), p(xs[1]))
+    assert st == abi.SIF_ERR_RANGE
+    assert b"cells a side" in lib.sif_error_message()
+
+
 @pytest.mark.parametrize("window", ["full", "aliasing", "none"])
 def test_smoothing_against_fp64(dev, oracle, golden_box32, window):
     g = golden_box32
