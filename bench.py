@@ -10,8 +10,9 @@ catalogue on the host.
 - ``e2e``: the same step through sif's C API with host buffers
   (sif_grid_assign_cic, sif_grid_to_density_contrast, sif_chain_mesh_alloc,
   sif_finder_exodus_raw), every host<->device copy inside the timed region.
-- ``cpu_baseline``: the CPU restatement of the reference's path (oracle/)
-  with all host cores, on a bounded sample of the same recipe.
+- ``cpu_baseline``: the CPU restatement of the reference's path (oracle/,
+  its release-flags build) with all host cores, on the same 512^3 workload:
+  one whole-path run, and the same with the FFT stage taken out.
 
 - ``fp64_form``: the same step in the FP64 form (sifg_box_device_f64: the
   reference's SIF_USE_DOUBLE arithmetic), the form the float path is
@@ -22,7 +23,8 @@ catalogue on the host.
   grid 256^3, Gaussian R = 5): forward (deposit + contrast + smoothing) and
   backward (smoothing of the gradient + the deposit's adjoint) times.
 
-``--impl reference`` times that CPU path alone (the reference arm).
+``--impl reference`` times that CPU path alone (the reference arm), on the
+same workload.
 Under torchrun every rank runs its own replica (the path does not shard).
 """
 import argparse
@@ -49,10 +51,10 @@ UNIT = "Mparticles/s"
 # threshold -0.8; excursion-set variant.
 WORKLOAD = dict(name="B", n=512, box=1000.0, rms=5.0, seed=1002, grid=512, mesh=125, r0=4.0,
                 threshold=-0.8)
-# The CPU sample: the same recipe (density, grid spacing, mesh cell, ladder,
-# displacement) on a periodic box of 1/64 the volume.
-CPU_SAMPLE = dict(n=128, box=250.0, rms=5.0, seed=1102, grid=128, mesh=31, r0=4.0,
-                  threshold=-0.8)
+
+
+WORKLOAD_NAME = ("512^3 particles, box 1000 Mpc/h, grid 512^3, mesh 125^3 (8 Mpc/h), "
+                 "ladder(4, 24, 0.10) 19 rungs, threshold -0.8, excursion-set")
 
 
 def radii_of(w):
@@ -245,17 +247,16 @@ def gpu_arm(args, rank, world):
     precision = precision_run(args) if args.precision else None
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
-        cpu = cpu_run(seconds=args.cpu_seconds)
+    if rank == 0 and not args.no_cpu and not args.small:
+        cpu = cpu_run(x, y, z, w, radii, steps=1, warmup=0)
 
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic Zel'dovich lattice (seeded), no dataset",
-        "config": {"workload": ("512^3 particles, box 1000 Mpc/h, grid 512^3, mesh 125^3 (8 Mpc/h),"
-                                " ladder(4, 24, 0.10) 19 rungs, threshold -0.8, excursion-set")
-                   if not args.small else "128^3 particles, box 500, grid 128^3, mesh 50^3",
+        "config": {"workload": WORKLOAD_NAME if not args.small
+                   else "128^3 particles, box 500, grid 128^3, mesh 50^3",
                    "n_particles": n, "n_voids": n_voids, "l2": "inputs larger than L2 (1.6 GB of particles)",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "window_bins": 8},
@@ -522,53 +523,75 @@ def e2e_run(args, w, x, y, z, radii):
 # the CPU path (the oracle port of the reference)
 # --------------------------------------------------------------------------
 
-def cpu_pipeline(O, x, y, z, w, radii, threads):
-    """The whole path through the CPU restatement: CIC, contrast, mesh,
-    finder (its own smoothing)."""
-    d = O.density_contrast(O.cic_f64(x, y, z, w["grid"], w["box"]).astype(np.float32))
-    m = O.OracleMesh(x, y, z, w["mesh"], w["box"])
-    return O.exodus(d, m, radii, w["grid"], w["box"], w["threshold"], n_threads=threads)
+def cpu_step(O, x, y, z, w, radii, threads):
+    """One whole path through the port's release-flags build, as the
+    reference's caller runs it: float CIC, contrast, chain mesh, the finder
+    with its own smoothing (and the restore of the grid). Returns the seconds
+    per stage and the voids found."""
+    cat, t = O.pipeline(x, y, z, w["grid"], w["box"], w["mesh"], radii, w["threshold"], threads,
+                        fast=True)
+    return t, len(cat[0])
 
 
-def cpu_run(seconds=20.0, steps=None, warmup=1):
+def cpu_run(x, y, z, w, radii, steps=1, warmup=0, budget_s=150.0):
+    """The CPU baseline on the workload itself: `warmup` untimed runs, then up
+    to `steps` timed ones (at least one; no more once budget_s has gone by);
+    the median, and the same with the finder's FFT stage (its transforms,
+    timed alone on the same contrast) taken out."""
     import oracle_ctypes as O
-
-    from sif_gb300 import synth
 
     O.build()
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    w = CPU_SAMPLE
-    radii = radii_of(w)
-    x, y, z = synth.zeldovich(w["n"], w["box"], w["rms"], w["seed"])
     for _ in range(warmup):
-        cpu_pipeline(O, x, y, z, w, radii, threads)
-    times = []
+        cpu_step(O, x, y, z, w, radii, threads)
+    runs = []
     t_start = time.perf_counter()
-    while True:
-        t0 = time.perf_counter()
-        cpu_pipeline(O, x, y, z, w, radii, threads)
-        times.append(time.perf_counter() - t0)
-        if steps is not None and len(times) >= steps:
+    nv = 0
+    while len(runs) < max(1, steps):
+        t, nv = cpu_step(O, x, y, z, w, radii, threads)
+        runs.append(t)
+        if time.perf_counter() - t_start >= budget_s:
             break
-        if steps is None and time.perf_counter() - t_start >= seconds:
-            break
-    dt = statistics.median(times)
-    sample = (f"the same recipe on a {w['n']}^3-particle periodic box of {w['box']} Mpc/h (1/64 "
-              f"of the volume: same density, grid spacing, mesh cell, ladder), whole path, "
-              f"median of {len(times)} runs")
-    return {"value": round(len(x) / dt / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": sample, "ms_per_step": round(dt * 1e3, 1)}
+    total = statistics.median(sum(t.values()) for t in runs)
+    stages = {k: round(statistics.median(t[k] for t in runs) * 1e3, 1) for k in runs[0]}
+    delta = O.density_contrast(O.cic_float(x, y, z, w["grid"], w["box"]))
+    fft = O.smoothing_seconds(delta, w["grid"], w["box"], radii, fast=True)
+    n = len(x)
+    sample = (f"the whole workload ({w['n']}^3 particles, box {w['box']:.0f}, grid {w['grid']}^3, "
+              f"mesh {w['mesh']}^3, {len(radii)} rungs), the port's release-flags build, median of "
+              f"{len(runs)} run(s)")
+    return {"value": round(n / total / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": sample, "ms_per_step": round(total * 1e3, 1), "stages_ms": stages,
+            "fft_stage_ms": round(fft * 1e3, 1),
+            "value_excluding_fft": round(n / max(total - fft, 1e-9) / 1e6, 3),
+            "n_voids": nv, "steps": len(runs)}
 
 
 def reference_arm(args):
-    cpu = cpu_run(steps=args.steps, warmup=args.warmup)
+    """The reference's path on the host cores (the port: the reference
+    sources are not on the GPU machines), on the GPU arm's own workload and
+    inputs: W untimed runs (at most 1), then up to K timed ones within a few
+    minutes."""
+    from sif_gb300 import synth
+
+    w = WORKLOAD
+    try:
+        import torch
+
+        backend = "torch" if torch.cuda.is_available() else "numpy"
+    except ImportError:
+        backend = "numpy"
+    x, y, z = synth.zeldovich(w["n"], w["box"], w["rms"], w["seed"], backend=backend)
+    cpu = cpu_run(x, y, z, w, radii_of(w), steps=args.steps, warmup=min(args.warmup, 1),
+                  budget_s=150.0)
     return {
         "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cpu["ms_per_step"],
+        "steps": cpu["steps"], "warmup": min(args.warmup, 1), "ms_per_step": cpu["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic Zel'dovich lattice (seeded), no dataset",
-        "config": {"workload": "512^3 recipe, timed on " + cpu["sample"]},
+        "config": {"workload": WORKLOAD_NAME, "n_particles": len(x),
+                   "timed_on": f"{cpu['cores']} host cores"},
         "cpu_baseline": cpu,
         "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -587,7 +610,6 @@ def main():
     ap.add_argument("--precision", action="store_true",
                     help="also the 1024^3 float-vs-FP64 field error and the 1024^3 finder")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

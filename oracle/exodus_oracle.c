@@ -49,10 +49,25 @@ static inline uint64_t mesh_cell_of(
 }
 
 /* The mesh of chain_mesh_create + chain_mesh_canonicalise
- * (src/structures/chain_mesh.c:680-832, 420-542): counts per cell, offsets,
- * and each cell in ascending source index -- which a stable counting sort
- * gives directly. The box check of chain_mesh_new (field.c:889-935) is the
- * caller's; coordinates are folded as the scatter folds them. */
+ * (src/structures/chain_mesh.c:680-832, 420-542), with their parallel
+ * structure: counts per cell by run-length-batched atomic adds over one
+ * chunk of particles per thread, a serial prefix, a scatter that claims each
+ * run's slots with one atomic, then every cell put in ascending source index
+ * (a sort of (index, slot) records, insertion sort up to 32 entries), which
+ * makes the result independent of the threads: each cell in source order.
+ * The box check of chain_mesh_new (field.c:889-935) is the caller's;
+ * coordinates are folded as the scatter folds them. */
+#define CANON_INSERTION_MAX 32u
+
+typedef struct {
+  uint64_t key, slot;
+} canon_t;
+
+static int canon_cmp(const void* a, const void* b) {
+  const uint64_t x = ((const canon_t*)a)->key, y = ((const canon_t*)b)->key;
+  return (x > y) - (x < y);
+}
+
 int orc_chain_mesh(const float* x, const float* y, const float* z, uint64_t n,
   uint32_t n_cells, float box, float* ox, float* oy, float* oz,
   uint64_t* offsets, uint64_t* orig) {
@@ -61,32 +76,123 @@ int orc_chain_mesh(const float* x, const float* y, const float* z, uint64_t n,
   const uint64_t total = (uint64_t)n_cells * n_cells * n_cells;
   const float cell_length = box / (float)n_cells;
   const float inv_l = 1.0f / cell_length;
-  uint64_t* cell = malloc(n * sizeof(uint64_t));
-  if (!cell)
-    return -1;
-  memset(offsets, 0, (total + 1) * sizeof(uint64_t));
-  for (uint64_t i = 0; i < n; i++) {
-    cell[i] = mesh_cell_of(x[i], y[i], z[i], inv_l, n_cells, box);
-    offsets[cell[i] + 1]++;
-  }
-  for (uint64_t c = 0; c < total; c++)
-    offsets[c + 1] += offsets[c];
+  uint64_t* idx = orig ? orig : malloc(n * sizeof(uint64_t));
   uint64_t* cursor = malloc(total * sizeof(uint64_t));
-  if (!cursor) {
-    free(cell);
+  if (!idx || !cursor) {
+    if (!orig)
+      free(idx);
+    free(cursor);
     return -1;
   }
-  memcpy(cursor, offsets, total * sizeof(uint64_t));
-  for (uint64_t i = 0; i < n; i++) {
-    const uint64_t pos = cursor[cell[i]]++;
-    ox[pos] = box_fold(x[i], box);
-    oy[pos] = box_fold(y[i], box);
-    oz[pos] = box_fold(z[i], box);
-    if (orig)
-      orig[pos] = i;
+#pragma omp parallel for schedule(static)
+  for (uint64_t c = 0; c <= total; c++)
+    offsets[c] = 0;
+#pragma omp parallel
+  {
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    const uint64_t chunk = n / (uint64_t)nt;
+    const uint64_t a = (uint64_t)t * chunk, e = t == nt - 1 ? n : a + chunk;
+    uint64_t i = a;
+    while (i < e) {
+      const uint64_t c = mesh_cell_of(x[i], y[i], z[i], inv_l, n_cells, box);
+      uint64_t run = 1;
+      while (i + run < e && mesh_cell_of(x[i + run], y[i + run], z[i + run], inv_l, n_cells,
+                              box) == c)
+        run++;
+#pragma omp atomic
+      offsets[c] += run;
+      i += run;
+    }
+  }
+  uint64_t acc = 0;
+  for (uint64_t c = 0; c < total; c++) {
+    const uint64_t v = offsets[c];
+    offsets[c] = acc;
+    acc += v;
+  }
+  offsets[total] = acc;
+#pragma omp parallel for schedule(static)
+  for (uint64_t c = 0; c < total; c++)
+    cursor[c] = offsets[c];
+#pragma omp parallel
+  {
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    const uint64_t chunk = n / (uint64_t)nt;
+    const uint64_t a = (uint64_t)t * chunk, e = t == nt - 1 ? n : a + chunk;
+    uint64_t i = a;
+    while (i < e) {
+      const uint64_t c = mesh_cell_of(x[i], y[i], z[i], inv_l, n_cells, box);
+      uint64_t run = 1;
+      while (i + run < e && mesh_cell_of(x[i + run], y[i + run], z[i + run], inv_l, n_cells,
+                              box) == c)
+        run++;
+      uint64_t base;
+#pragma omp atomic capture
+      {
+        base = cursor[c];
+        cursor[c] += run;
+      }
+      for (uint64_t j = 0; j < run; j++) {
+        idx[base + j] = i + j;
+        ox[base + j] = box_fold(x[i + j], box);
+        oy[base + j] = box_fold(y[i + j], box);
+        oz[base + j] = box_fold(z[i + j], box);
+      }
+      i += run;
+    }
   }
   free(cursor);
-  free(cell);
+#pragma omp parallel
+  {
+    canon_t* order = NULL;
+    float* tmp = NULL;
+    uint64_t cap = 0;
+#pragma omp for schedule(dynamic, 64)
+    for (uint64_t c = 0; c < total; c++) {
+      const uint64_t lo = offsets[c], hi = offsets[c + 1], m = hi - lo;
+      if (m < 2)
+        continue;
+      uint64_t run = 1;
+      while (run < m && idx[lo + run - 1] < idx[lo + run])
+        run++;
+      if (run == m)
+        continue;
+      if (m > cap) {
+        cap = m + (m >> 1) + 8;
+        order = realloc(order, cap * sizeof(canon_t));
+        tmp = realloc(tmp, cap * sizeof(float));
+      }
+      for (uint64_t i = 0; i < m; i++) {
+        order[i].key = idx[lo + i];
+        order[i].slot = i;
+      }
+      if (m <= CANON_INSERTION_MAX) {
+        for (uint64_t i = 1; i < m; i++) {
+          const canon_t v = order[i];
+          uint64_t j = i;
+          while (j > 0 && order[j - 1].key > v.key) {
+            order[j] = order[j - 1];
+            j--;
+          }
+          order[j] = v;
+        }
+      } else {
+        qsort(order, (size_t)m, sizeof(canon_t), canon_cmp);
+      }
+      float* cols[3] = {ox, oy, oz};
+      for (int k = 0; k < 3; k++) {
+        for (uint64_t i = 0; i < m; i++)
+          tmp[i] = cols[k][lo + order[i].slot];
+        memcpy(cols[k] + lo, tmp, m * sizeof(float));
+      }
+      for (uint64_t i = 0; i < m; i++)
+        idx[lo + i] = order[i].key;
+    }
+    free(order);
+    free(tmp);
+  }
+  if (!orig)
+    free(idx);
   return 0;
 }
 
@@ -97,39 +203,244 @@ int orc_chain_mesh(const float* x, const float* y, const float* z, uint64_t n,
 /* The CIC deposit of grid_compute_cic (src/structures/grid.c:455-746) in
  * double: base cell (uint32)(fold(x) * N/L) with the >= N fallback to 0,
  * weights (1 - t, t), periodic upper neighbours, divided by the cell volume.
- */
+ * The particles are bucketed by their base x plane; a plane's bucket writes
+ * planes x and x + 1 only, so the even planes' buckets run in parallel, then
+ * the odd ones' (and, for an odd N, the last plane, which wraps onto plane 0,
+ * alone). The sums are double: their order moves only the last bits. */
+static void cic_f64_base(float v, float box, double idx, uint32_t N, uint32_t* i0,
+  uint32_t* i1, double* w0, double* w1) {
+  const double u = (double)box_fold(v, box) * idx;
+  const uint32_t raw = (uint32_t)u;
+  *i0 = raw >= N ? 0u : raw;
+  *i1 = *i0 + 1 == N ? 0u : *i0 + 1;
+  const double t = u - (double)raw;
+  *w0 = 1.0 - t;
+  *w1 = t;
+}
+
 void orc_cic_f64(const float* x, const float* y, const float* z, uint64_t n,
   uint32_t N, float box, double* out) {
   const uint64_t total = (uint64_t)N * N * N;
-  memset(out, 0, total * sizeof(double));
+  const uint64_t plane = (uint64_t)N * N;
   const double idx = (double)N / (double)box;
-  for (uint64_t p = 0; p < n; p++) {
-    const double u[3] = {(double)box_fold(x[p], box) * idx,
-      (double)box_fold(y[p], box) * idx, (double)box_fold(z[p], box) * idx};
-    uint32_t i0[3], i1[3];
-    double w0[3], w1[3];
-    for (int a = 0; a < 3; a++) {
-      const uint32_t raw = (uint32_t)u[a];
-      i0[a] = raw >= N ? 0u : raw;
-      i1[a] = i0[a] + 1 == N ? 0u : i0[a] + 1;
-      const double t = u[a] - (double)raw;
-      w0[a] = 1.0 - t;
-      w1[a] = t;
-    }
-    for (int a = 0; a < 2; a++)
-      for (int b = 0; b < 2; b++)
-        for (int c = 0; c < 2; c++) {
-          const uint64_t cell =
-            ((uint64_t)(a ? i1[0] : i0[0]) * N + (b ? i1[1] : i0[1])) * N +
-            (c ? i1[2] : i0[2]);
-          out[cell] += (a ? w1[0] : w0[0]) * (b ? w1[1] : w0[1]) *
-                       (c ? w1[2] : w0[2]);
-        }
+#pragma omp parallel for schedule(static)
+  for (uint64_t i = 0; i < total; i++)
+    out[i] = 0.0;
+  uint64_t* start = calloc((size_t)N + 1, sizeof(uint64_t));
+  uint32_t* base = malloc(n * sizeof(uint32_t));
+  uint64_t* order = malloc(n * sizeof(uint64_t));
+  if (!start || !base || !order) {
+    free(start);
+    free(base);
+    free(order);
+    return;
   }
+#pragma omp parallel for schedule(static)
+  for (uint64_t p = 0; p < n; p++) {
+    uint32_t a, b;
+    double w0, w1;
+    cic_f64_base(x[p], box, idx, N, &a, &b, &w0, &w1);
+    base[p] = a;
+  }
+  for (uint64_t p = 0; p < n; p++)
+    start[base[p] + 1]++;
+  for (uint32_t i = 0; i < N; i++)
+    start[i + 1] += start[i];
+  {
+    uint64_t* cur = malloc((size_t)N * sizeof(uint64_t));
+    memcpy(cur, start, (size_t)N * sizeof(uint64_t));
+    for (uint64_t p = 0; p < n; p++)
+      order[cur[base[p]]++] = p;
+    free(cur);
+  }
+  free(base);
+  for (int phase = 0; phase < 3; phase++) {
+    /* Phase 0: even planes, 1: odd planes, 2: an odd N's last plane. */
+    const uint32_t last = (N & 1u) ? N - 1 : N;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (uint32_t ix = 0; ix < N; ix++) {
+      const int mine = phase == 2 ? ix == last : (ix != last && (int)(ix & 1u) == phase);
+      if (!mine)
+        continue;
+      for (uint64_t q = start[ix]; q < start[ix + 1]; q++) {
+        const uint64_t p = order[q];
+        uint32_t i0[3], i1[3];
+        double w0[3], w1[3];
+        cic_f64_base(x[p], box, idx, N, &i0[0], &i1[0], &w0[0], &w1[0]);
+        cic_f64_base(y[p], box, idx, N, &i0[1], &i1[1], &w0[1], &w1[1]);
+        cic_f64_base(z[p], box, idx, N, &i0[2], &i1[2], &w0[2], &w1[2]);
+        for (int a = 0; a < 2; a++)
+          for (int b = 0; b < 2; b++)
+            for (int c = 0; c < 2; c++) {
+              const uint64_t cell = (uint64_t)(a ? i1[0] : i0[0]) * plane +
+                                    (uint64_t)(b ? i1[1] : i0[1]) * N + (c ? i1[2] : i0[2]);
+              out[cell] += (a ? w1[0] : w0[0]) * (b ? w1[1] : w0[1]) * (c ? w1[2] : w0[2]);
+            }
+      }
+    }
+  }
+  free(order);
+  free(start);
   const double cl = (double)box / (double)N;
   const double inv_vol = 1.0 / (cl * cl * cl);
+#pragma omp parallel for schedule(static)
   for (uint64_t i = 0; i < total; i++)
     out[i] *= inv_vol;
+}
+
+/* The reference's own float CIC deposit, grid_compute_cic with
+ * grid_cic_deposit_tile for SIF_ASSIGNMENT_CIC (src/structures/grid.c:
+ * 180-345, 455-746): slabs of N/16 planes' width (the last takes the rest),
+ * each with one ghost plane above; the particles taken in tiles of 64Mi
+ * (the cic_tile_particles default), each tile counting-sorted by slab over
+ * 256 fixed chunks (counts per chunk and slab, offsets slab-major, a scatter
+ * of indices) and deposited a slab per thread in that order; the ghost planes
+ * folded into the next slab serially; the slabs copied out times the
+ * inverse cell volume. The order of every float addition is the reference's,
+ * so the density is its bit for bit. */
+#define CIC_CHUNKS 256
+#define CIC_SLAB_WIDTH 16u
+#define CIC_TILE_PARTICLES 67108864ull
+
+void orc_cic_float(const float* xs, const float* ys, const float* zs, uint64_t n,
+  uint32_t N, float box, float* grid) {
+  const float idx = (float)N / (float)box;
+  int32_t n_slabs = (int32_t)(N / CIC_SLAB_WIDTH);
+  if (n_slabs < 1)
+    n_slabs = 1;
+  const uint64_t plane = (uint64_t)N * N;
+  uint64_t* slab_off = malloc(((size_t)n_slabs + 1) * sizeof(uint64_t));
+  uint32_t* slab_x0 = malloc((size_t)n_slabs * sizeof(uint32_t));
+  uint32_t* slab_w = malloc((size_t)n_slabs * sizeof(uint32_t));
+  slab_off[0] = 0;
+  for (int t = 0; t < n_slabs; t++) {
+    slab_x0[t] = (uint32_t)t * (N / (uint32_t)n_slabs);
+    const uint32_t end = t == n_slabs - 1 ? N : (uint32_t)(t + 1) * (N / (uint32_t)n_slabs);
+    slab_w[t] = end - slab_x0[t];
+    uint64_t cells = (uint64_t)(slab_w[t] + 1) * plane;
+    cells = (cells + 15) & ~(uint64_t)15; /* a 64-byte line of floats */
+    slab_off[t + 1] = slab_off[t] + cells;
+  }
+  float* arena = calloc(slab_off[n_slabs], sizeof(float));
+  const uint32_t base_width = N / (uint32_t)n_slabs;
+  uint64_t tile_n = CIC_TILE_PARTICLES < n ? CIC_TILE_PARTICLES : n;
+  if (tile_n == 0)
+    tile_n = 1;
+  uint64_t* counts = malloc((size_t)CIC_CHUNKS * n_slabs * sizeof(uint64_t));
+  uint64_t* sorted = malloc(tile_n * sizeof(uint64_t));
+  for (uint64_t lo = 0; lo < n; lo += tile_n) {
+    const uint64_t hi = lo + tile_n > n ? n : lo + tile_n;
+    const uint64_t chunk = (hi - lo + CIC_CHUNKS - 1) / CIC_CHUNKS;
+    memset(counts, 0, (size_t)CIC_CHUNKS * n_slabs * sizeof(uint64_t));
+#pragma omp parallel for schedule(static, 1)
+    for (int c = 0; c < CIC_CHUNKS; c++) {
+      const uint64_t a = lo + (uint64_t)c * chunk, e = a + chunk > hi ? hi : a + chunk;
+      for (uint64_t p = a; p < e; p++) {
+        uint32_t ix = (uint32_t)(box_fold(xs[p], box) * idx);
+        ix = ix >= N ? ix - N : ix;
+        const uint32_t sl = ix / base_width < (uint32_t)(n_slabs - 1) ? ix / base_width
+                                                                      : (uint32_t)(n_slabs - 1);
+        counts[(uint64_t)c * n_slabs + sl]++;
+      }
+    }
+    uint64_t run = 0;
+    for (int32_t sl = 0; sl < n_slabs; sl++)
+      for (int c = 0; c < CIC_CHUNKS; c++) {
+        const uint64_t k = (uint64_t)c * n_slabs + sl, v = counts[k];
+        counts[k] = run;
+        run += v;
+      }
+#pragma omp parallel for schedule(static, 1)
+    for (int c = 0; c < CIC_CHUNKS; c++) {
+      const uint64_t a = lo + (uint64_t)c * chunk, e = a + chunk > hi ? hi : a + chunk;
+      for (uint64_t p = a; p < e; p++) {
+        uint32_t ix = (uint32_t)(box_fold(xs[p], box) * idx);
+        ix = ix >= N ? ix - N : ix;
+        const uint32_t sl = ix / base_width < (uint32_t)(n_slabs - 1) ? ix / base_width
+                                                                      : (uint32_t)(n_slabs - 1);
+        sorted[counts[(uint64_t)c * n_slabs + sl]++] = p;
+      }
+    }
+#pragma omp parallel for schedule(static, 1)
+    for (int32_t sl = 0; sl < n_slabs; sl++) {
+      const uint64_t s0 = sl == 0 ? 0 : counts[(uint64_t)(CIC_CHUNKS - 1) * n_slabs + sl - 1];
+      const uint64_t s1 = counts[(uint64_t)(CIC_CHUNKS - 1) * n_slabs + sl];
+      float* v = arena + slab_off[sl];
+      const uint32_t x0 = slab_x0[sl];
+      for (uint64_t q = s0; q < s1; q++) {
+        const uint64_t p = sorted[q];
+        const float cx = box_fold(xs[p], box) * idx;
+        const float cy = box_fold(ys[p], box) * idx;
+        const float cz = box_fold(zs[p], box) * idx;
+        const uint32_t rx = (uint32_t)cx, ry = (uint32_t)cy, rz = (uint32_t)cz;
+        const uint32_t ix = rx >= N ? 0 : rx, iy = ry >= N ? 0 : ry, iz = rz >= N ? 0 : rz;
+        const uint32_t iy1 = iy + 1 == N ? 0 : iy + 1, iz1 = iz + 1 == N ? 0 : iz + 1;
+        const uint64_t l0 = (uint64_t)(ix - x0) * plane, l1 = l0 + plane;
+        const float tx = cx - (float)rx, ty = cy - (float)ry, tz = cz - (float)rz;
+        const float wx0 = 1.0f - tx, wx1 = tx, wy0 = 1.0f - ty, wy1 = ty;
+        const float wz0 = 1.0f - tz, wz1 = tz;
+        const float w00 = wx0 * wy0, w01 = wx0 * wy1, w10 = wx1 * wy0, w11 = wx1 * wy1;
+        const float mz0 = 1.0f * wz0, mz1 = 1.0f * wz1;
+        v[l0 + (uint64_t)iy * N + iz] += w00 * mz0;
+        v[l0 + (uint64_t)iy * N + iz1] += w00 * mz1;
+        v[l0 + (uint64_t)iy1 * N + iz] += w01 * mz0;
+        v[l0 + (uint64_t)iy1 * N + iz1] += w01 * mz1;
+        v[l1 + (uint64_t)iy * N + iz] += w10 * mz0;
+        v[l1 + (uint64_t)iy * N + iz1] += w10 * mz1;
+        v[l1 + (uint64_t)iy1 * N + iz] += w11 * mz0;
+        v[l1 + (uint64_t)iy1 * N + iz1] += w11 * mz1;
+      }
+    }
+  }
+  /* grid_cic_reduce_ghost_cells: slab t's ghost plane into slab t+1's first. */
+  for (int32_t t = 0; t < n_slabs; t++) {
+    const float* ghost = arena + slab_off[t] + (uint64_t)slab_w[t] * plane;
+    float* first = arena + slab_off[(t + 1) % n_slabs];
+    for (uint64_t i = 0; i < plane; i++)
+      first[i] += ghost[i];
+  }
+  const float cl = box / (float)N;
+  const float inv_vol = 1.0f / (float)(cl * cl * cl);
+#pragma omp parallel for schedule(static)
+  for (int32_t t = 0; t < n_slabs; t++) {
+    const float* v = arena + slab_off[t];
+    float* out = grid + (uint64_t)slab_x0[t] * plane;
+    for (uint64_t i = 0; i < (uint64_t)slab_w[t] * plane; i++)
+      out[i] = v[i] * inv_vol;
+  }
+  free(sorted);
+  free(counts);
+  free(arena);
+  free(slab_w);
+  free(slab_x0);
+  free(slab_off);
+}
+
+/* The density contrast of an FP64 density, all in double: the mean by the
+ * same 64 fixed blocks, then v / mean - 1. */
+int orc_density_contrast_f64(double* v, uint64_t n) {
+  const int blocks = 64;
+  const uint64_t block = (n + blocks - 1) / blocks;
+  double part[64];
+#pragma omp parallel for schedule(static, 1)
+  for (int b = 0; b < blocks; b++) {
+    const uint64_t s = (uint64_t)b * block;
+    const uint64_t e = s + block < n ? s + block : n;
+    double sum = 0.0;
+    for (uint64_t i = s; i < e; i++)
+      sum += v[i];
+    part[b] = sum;
+  }
+  double total = 0.0;
+  for (int b = 0; b < blocks; b++)
+    total += part[b];
+  const double mean = total / (double)n;
+  if (!(mean > 0.0))
+    return -3;
+#pragma omp parallel for schedule(static)
+  for (uint64_t i = 0; i < n; i++)
+    v[i] = v[i] / mean - 1.0;
+  return 0;
 }
 
 /* sif_grid_to_density_contrast, src/structures/grid.c:1177-1244: the mean in
@@ -137,19 +448,24 @@ void orc_cic_f64(const float* x, const float* y, const float* z, uint64_t n,
 int orc_density_contrast(float* v, uint64_t n) {
   const int blocks = 64;
   const uint64_t block = (n + blocks - 1) / blocks;
-  double total = 0.0;
+  double part[64];
+#pragma omp parallel for schedule(static, 1)
   for (int b = 0; b < blocks; b++) {
     const uint64_t s = (uint64_t)b * block;
     const uint64_t e = s + block < n ? s + block : n;
     double sum = 0.0;
     for (uint64_t i = s; i < e; i++)
       sum += (double)v[i];
-    total += sum;
+    part[b] = sum;
   }
+  double total = 0.0;
+  for (int b = 0; b < blocks; b++)
+    total += part[b];
   const double mean = total / (double)n;
   if (!(mean > 0.0))
     return -3;
   const float inv = (float)(1.0 / mean);
+#pragma omp parallel for schedule(static)
   for (uint64_t i = 0; i < n; i++)
     v[i] = v[i] * inv - 1.0f;
   return 0;
@@ -163,9 +479,92 @@ struct orc_spectrum {
   uint32_t n;
   float box;
   int mode;
-  fftw_complex* spec; /* n * n * (n/2+1) */
-  double* window;     /* per-axis factor, or NULL */
+  fftw_complex* spec;   /* mode 0: n * n * (n/2+1), double */
+  fftwf_complex* specf; /* mode 1: the same modes in float, plane-major */
+  double* window;       /* per-axis factor, or NULL */
 };
+
+/* The float mode's transforms are laid out as the reference lays out its own
+ * (src/math/fft.c:269-434, 790-888): a 2-D transform of every x plane and a
+ * 1-D transform along x of every (y, kz) pencil, FFT_PENCIL_BLOCK pencils at
+ * a time, each through one single-threaded plan, in parallel over the planes
+ * and the pencil blocks. Through the same FFTW-API calls on the same plans
+ * the spectrum and the smoothed fields are the reference's bit for bit. */
+#define PENCIL_BLOCK 16
+
+static uint64_t plane_modes(uint32_t n) { return (uint64_t)n * (n / 2 + 1); }
+
+/* fft_pencils, src/math/fft.c:378-434. */
+static void pencils_f(fftwf_complex* c, uint32_t n, int sign) {
+  const int len[1] = {(int)n};
+  const uint64_t n_pencils = plane_modes(n);
+  const uint64_t n_blocks = (n_pencils + PENCIL_BLOCK - 1) / PENCIL_BLOCK;
+  fftwf_complex* scratch = fftwf_malloc((size_t)n * PENCIL_BLOCK * sizeof(fftwf_complex));
+  fftwf_plan plan = fftwf_plan_many_dft(1, len, PENCIL_BLOCK, scratch, NULL, PENCIL_BLOCK, 1,
+    scratch, NULL, PENCIL_BLOCK, 1, sign, FFTW_ESTIMATE);
+  fftwf_free(scratch);
+#pragma omp parallel
+  {
+    fftwf_complex* g = fftwf_malloc((size_t)n * PENCIL_BLOCK * sizeof(fftwf_complex));
+#pragma omp for schedule(static)
+    for (uint64_t b = 0; b < n_blocks; b++) {
+      const uint64_t j0 = b * PENCIL_BLOCK;
+      const uint64_t w = n_pencils - j0 < PENCIL_BLOCK ? n_pencils - j0 : PENCIL_BLOCK;
+      for (uint32_t x = 0; x < n; x++) {
+        fftwf_complex* row = g + (uint64_t)x * PENCIL_BLOCK;
+        memcpy(row, c + x * n_pencils + j0, w * sizeof(fftwf_complex));
+        if (w < PENCIL_BLOCK)
+          memset(row + w, 0, (PENCIL_BLOCK - w) * sizeof(fftwf_complex));
+      }
+      fftwf_execute_dft(plan, g, g);
+      for (uint32_t x = 0; x < n; x++)
+        memcpy(c + x * n_pencils + j0, g + (uint64_t)x * PENCIL_BLOCK, w * sizeof(fftwf_complex));
+    }
+    fftwf_free(g);
+  }
+  fftwf_destroy_plan(plan);
+}
+
+/* sif__fft_grid_forward, src/math/fft.c:790-818. */
+static void forward_f(const float* in, fftwf_complex* spec, uint32_t n) {
+  const uint64_t reals = (uint64_t)n * n, modes = plane_modes(n);
+  float* pr = fftwf_malloc(reals * sizeof(float));
+  fftwf_complex* pc = fftwf_malloc(modes * sizeof(fftwf_complex));
+  fftwf_plan plane = fftwf_plan_dft_r2c_2d((int)n, (int)n, pr, pc, FFTW_ESTIMATE);
+  fftwf_free(pr);
+  fftwf_free(pc);
+#pragma omp parallel for schedule(static)
+  for (uint32_t x = 0; x < n; x++)
+    fftwf_execute_dft_r2c(plane, (float*)in + x * reals, spec + x * modes);
+  fftwf_destroy_plan(plane);
+  pencils_f(spec, n, FFTW_FORWARD);
+}
+
+/* sif__fft_grid_backward, src/math/fft.c:820-888: the pencils in place, then
+ * each plane's C2R, times 1/N^3 in float, into out. */
+static void backward_f(fftwf_complex* c, float* out, uint32_t n) {
+  pencils_f(c, n, FFTW_BACKWARD);
+  const uint64_t reals = (uint64_t)n * n, modes = plane_modes(n);
+  const float norm = 1.0f / (float)((uint64_t)n * n * n);
+  float* pr = fftwf_malloc(reals * sizeof(float));
+  fftwf_complex* pc = fftwf_malloc(modes * sizeof(fftwf_complex));
+  fftwf_plan plane = fftwf_plan_dft_c2r_2d((int)n, (int)n, pc, pr, FFTW_ESTIMATE);
+  fftwf_free(pr);
+  fftwf_free(pc);
+#pragma omp parallel
+  {
+    float* buf = fftwf_malloc(reals * sizeof(float));
+#pragma omp for schedule(static)
+    for (uint32_t x = 0; x < n; x++) {
+      fftwf_execute_dft_c2r(plane, c + x * modes, buf);
+      float* o = out + x * reals;
+      for (uint64_t i = 0; i < reals; i++)
+        o[i] = buf[i] * norm;
+    }
+    fftwf_free(buf);
+  }
+  fftwf_destroy_plan(plane);
+}
 
 /* x = pi k / N for index i (src/math/fft.c:939-943), with the reference's
  * float pi in the float mode. */
@@ -176,28 +575,27 @@ static double axis_x(uint32_t i, uint32_t n, int mode) {
   return pi * (double)k / (double)n;
 }
 
-orc_spectrum_t* orc_spectrum_new(
-  const float* delta, uint32_t n, float box, int window_mode, int mode) {
+static orc_spectrum_t* spectrum_new(const float* delta_f, const double* delta_d, uint32_t n,
+  float box, int window_mode, int mode) {
   orc_spectrum_t* s = calloc(1, sizeof(*s));
   s->n = n;
   s->box = box;
   s->mode = mode;
   const uint64_t total = (uint64_t)n * n * n;
   const uint64_t modes = (uint64_t)n * n * (n / 2 + 1);
-  double* in = malloc(total * sizeof(double));
-  for (uint64_t i = 0; i < total; i++)
-    in[i] = (double)delta[i];
-  s->spec = fftw_malloc(modes * sizeof(fftw_complex));
-  fftw_plan p = fftw_plan_dft_r2c_3d(n, n, n, in, s->spec, FFTW_ESTIMATE);
-  fftw_execute(p);
-  fftw_destroy_plan(p);
-  free(in);
   if (mode) {
-    /* The forward transform of a float grid comes back in float. */
-    for (uint64_t i = 0; i < modes; i++) {
-      s->spec[i][0] = (double)(float)s->spec[i][0];
-      s->spec[i][1] = (double)(float)s->spec[i][1];
-    }
+    s->specf = fftwf_malloc(modes * sizeof(fftwf_complex));
+    forward_f(delta_f, s->specf, n);
+  } else {
+    double* in = malloc(total * sizeof(double));
+#pragma omp parallel for schedule(static)
+    for (uint64_t i = 0; i < total; i++)
+      in[i] = delta_d ? delta_d[i] : (double)delta_f[i];
+    s->spec = fftw_malloc(modes * sizeof(fftw_complex));
+    fftw_plan p = fftw_plan_dft_r2c_3d(n, n, n, in, s->spec, FFTW_ESTIMATE);
+    fftw_execute(p);
+    fftw_destroy_plan(p);
+    free(in);
   }
   if (window_mode) {
     /* fft_build_window_axis, src/math/fft.c:958-975, order 2 (CIC):
@@ -220,8 +618,20 @@ orc_spectrum_t* orc_spectrum_new(
   return s;
 }
 
+orc_spectrum_t* orc_spectrum_new(
+  const float* delta, uint32_t n, float box, int window_mode, int mode) {
+  return spectrum_new(delta, NULL, n, box, window_mode, mode);
+}
+
+orc_spectrum_t* orc_spectrum_new_f64(
+  const double* delta, uint32_t n, float box, int window_mode) {
+  return spectrum_new(NULL, delta, n, box, window_mode, 0);
+}
+
 /* fft_build_filter_lut + sif__fft_apply_filter_smoothed + the backward
- * transform's 1/N^3 (src/math/fft.c:521-568, 703-788, 820-888). */
+ * transform's 1/N^3 (src/math/fft.c:521-568, 703-788, 820-888). filter 0 is
+ * SIF__FILTER_NONE: the spectrum as it is, no window (the reference's restore
+ * of the grid at the end of a run, exodus_finder.c:2430-2453). */
 void orc_spectrum_smooth(orc_spectrum_t* s, int filter, float r, float sigma,
   float* out_f, double* out_d) {
   const uint32_t n = s->n;
@@ -236,6 +646,7 @@ void orc_spectrum_smooth(orc_spectrum_t* s, int filter, float r, float sigma,
     const float factor2 = factor * factor;
     const float gfactor = (float)((double)sigma * 2.0 * (double)PI_F / (double)s->box);
     const float gfactor2 = gfactor * gfactor;
+#pragma omp parallel for schedule(static)
     for (uint32_t k2 = 0; k2 <= max_k2; k2++) {
       float v;
       if (k2 == 0) {
@@ -253,6 +664,7 @@ void orc_spectrum_smooth(orc_spectrum_t* s, int filter, float r, float sigma,
   } else {
     const double factor = (double)r * 2.0 * M_PI / (double)s->box;
     const double gfactor = (double)sigma * 2.0 * M_PI / (double)s->box;
+#pragma omp parallel for schedule(static)
     for (uint32_t k2 = 0; k2 <= max_k2; k2++) {
       double v;
       if (k2 == 0) {
@@ -268,8 +680,47 @@ void orc_spectrum_smooth(orc_spectrum_t* s, int filter, float r, float sigma,
       lut[k2] = v;
     }
   }
+  const double* win = filter ? s->window : NULL;
+  if (s->mode) {
+    fftwf_complex* work = fftwf_malloc(modes * sizeof(fftwf_complex));
+    const fftwf_complex* spec = s->specf;
+#pragma omp parallel for schedule(static)
+    for (uint32_t ix = 0; ix < n; ix++) {
+      const int32_t kx = ix > h ? (int32_t)ix - (int32_t)n : (int32_t)ix;
+      const uint32_t kx2 = (uint32_t)(kx * kx);
+      const double cx = win ? win[ix] : 1.0;
+      for (uint32_t iy = 0; iy < n; iy++) {
+        const int32_t ky = iy > h ? (int32_t)iy - (int32_t)n : (int32_t)iy;
+        const uint32_t kxy2 = kx2 + (uint32_t)(ky * ky);
+        const double cxy = cx * (win ? win[iy] : 1.0);
+        for (uint32_t iz = 0; iz < zd; iz++) {
+          const uint64_t i = ((uint64_t)ix * n + iy) * zd + iz;
+          if (!filter) {
+            work[i][0] = spec[i][0];
+            work[i][1] = spec[i][1];
+            continue;
+          }
+          float smf = (float)lut[kxy2 + iz * iz];
+          if (win)
+            smf = (float)((double)smf * cxy * win[iz]);
+          work[i][0] = spec[i][0] * smf;
+          work[i][1] = spec[i][1] * smf;
+        }
+      }
+    }
+    free(lut);
+    float* f = out_f ? out_f : malloc(total * sizeof(float));
+    backward_f(work, f, n);
+    fftwf_free(work);
+    if (out_d)
+#pragma omp parallel for schedule(static)
+      for (uint64_t i = 0; i < total; i++)
+        out_d[i] = (double)f[i];
+    if (!out_f)
+      free(f);
+    return;
+  }
   fftw_complex* work = fftw_malloc(modes * sizeof(fftw_complex));
-  const double* win = s->window;
 #pragma omp parallel for schedule(static)
   for (uint32_t ix = 0; ix < n; ix++) {
     const int32_t kx = ix > h ? (int32_t)ix - (int32_t)n : (int32_t)ix;
@@ -282,16 +733,7 @@ void orc_spectrum_smooth(orc_spectrum_t* s, int filter, float r, float sigma,
       for (uint32_t iz = 0; iz < zd; iz++) {
         const uint32_t k2 = kxy2 + iz * iz;
         const uint64_t i = ((uint64_t)ix * n + iy) * zd + iz;
-        double sm;
-        if (s->mode) {
-          float smf = (float)lut[k2];
-          if (win)
-            smf = (float)((double)smf * cxy * win[iz]);
-          work[i][0] = (double)((float)s->spec[i][0] * smf);
-          work[i][1] = (double)((float)s->spec[i][1] * smf);
-          continue;
-        }
-        sm = lut[k2];
+        double sm = filter ? lut[k2] : 1.0;
         if (win)
           sm = sm * cxy * win[iz];
         work[i][0] = s->spec[i][0] * sm;
@@ -306,12 +748,12 @@ void orc_spectrum_smooth(orc_spectrum_t* s, int filter, float r, float sigma,
   fftw_destroy_plan(p);
   fftw_free(work);
   const double norm = 1.0 / (double)total;
-  const float normf = 1.0f / (float)total;
+#pragma omp parallel for schedule(static)
   for (uint64_t i = 0; i < total; i++) {
     if (out_d)
       out_d[i] = real[i] * norm;
     if (out_f)
-      out_f[i] = s->mode ? (float)real[i] * normf : (float)(real[i] * norm);
+      out_f[i] = (float)(real[i] * norm);
   }
   free(real);
 }
@@ -320,6 +762,7 @@ void orc_spectrum_free(orc_spectrum_t* s) {
   if (!s)
     return;
   fftw_free(s->spec);
+  fftwf_free(s->specf);
   free(s->window);
   free(s);
 }
@@ -336,7 +779,61 @@ void orc_spectrum_free(orc_spectrum_t* s) {
  * the low end, a larger one is exchanged with the high end and re-examined,
  * an equal one stays. Ranges are kept on an explicit stack; the two sides of a
  * partition are disjoint, so the order they are processed in is immaterial. */
+static void partition3_cand(orc_candidate_t* a, int64_t lo, int64_t hi, int64_t* lt_out,
+  int64_t* gt_out) {
+  const float pivot = a[lo + (hi - lo) / 2].delta;
+  int64_t lt = lo, i = lo, gt = hi;
+  while (i <= gt) {
+    const float v = a[i].delta;
+    if (v < pivot) {
+      const orc_candidate_t t = a[lt];
+      a[lt] = a[i];
+      a[i] = t;
+      lt++;
+      i++;
+    } else if (pivot < v) {
+      const orc_candidate_t t = a[i];
+      a[i] = a[gt];
+      a[gt] = t;
+      gt--;
+    } else {
+      i++;
+    }
+  }
+  *lt_out = lt;
+  *gt_out = gt;
+}
+
+static void sort_serial(orc_candidate_t* a, uint64_t count);
+
+/* SIF_DEFINE_QUICKSORT_PARALLEL (include/sif/utils/sort.h:100-145): the two
+ * sides of a partition of more than SIF_QUICKSORT_TASK_CUTOFF (65536)
+ * elements sorted as OpenMP tasks; the same permutation as the serial sort. */
+#define SORT_TASK_CUTOFF 65536
+static void sort_tasks(orc_candidate_t* a, int64_t lo, int64_t hi) {
+  if (hi - lo < SORT_TASK_CUTOFF) {
+    if (hi > lo)
+      sort_serial(a + lo, (uint64_t)(hi - lo + 1));
+    return;
+  }
+  int64_t lt, gt;
+  partition3_cand(a, lo, hi, &lt, &gt);
+#pragma omp task untied
+  sort_tasks(a, lo, lt - 1);
+  sort_tasks(a, gt + 1, hi);
+}
+
 void orc_sort_candidates(orc_candidate_t* a, uint64_t count) {
+  if (count <= SORT_TASK_CUTOFF) {
+    sort_serial(a, count);
+    return;
+  }
+#pragma omp parallel
+#pragma omp single nowait
+  sort_tasks(a, 0, (int64_t)count - 1);
+}
+
+static void sort_serial(orc_candidate_t* a, uint64_t count) {
   if (count < 2)
     return;
   int64_t* stack = malloc(sizeof(int64_t) * 2 * 128);
@@ -1209,22 +1706,42 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
     else
       orc_spectrum_smooth(spec, 1, radius, 0.0f, field, NULL);
 
-    /* The scan, src/finder/utils.c:130-213: flat order, then the sort. */
+    /* The scan, src/finder/utils.c:130-213: 256 fixed chunks counted, their
+     * offsets, each chunk written in flat order; then the sort. */
+    enum { SCAN_CHUNKS = 256 };
+    uint64_t chunk_off[SCAN_CHUNKS];
+    const uint64_t scan_chunk = total / SCAN_CHUNKS;
+#pragma omp parallel for schedule(static, 1) num_threads(n_threads)
+    for (int c = 0; c < SCAN_CHUNKS; c++) {
+      const uint64_t a = (uint64_t)c * scan_chunk, e = c == SCAN_CHUNKS - 1 ? total : a + scan_chunk;
+      uint64_t k = 0;
+      for (uint64_t i = a; i < e; i++)
+        k += field[i] <= threshold && !mask_get(mask, i) && (!minima || is_minimum_node(field, N, i));
+      chunk_off[c] = k;
+    }
     uint64_t nc = 0;
-    for (uint64_t i = 0; i < total; i++)
-      nc += field[i] <= threshold && !mask_get(mask, i) && (!minima || is_minimum_node(field, N, i));
+    for (int c = 0; c < SCAN_CHUNKS; c++) {
+      const uint64_t k = chunk_off[c];
+      chunk_off[c] = nc;
+      nc += k;
+    }
     if (nc > cand_cap) {
       cand_cap = nc;
       cand = realloc(cand, cand_cap * sizeof(orc_candidate_t));
     }
-    nc = 0;
-    for (uint64_t i = 0; i < total; i++)
-      if (field[i] <= threshold && !mask_get(mask, i) && (!minima || is_minimum_node(field, N, i))) {
-        cand[nc].delta = field[i];
-        cand[nc].refined = 0;
-        cand[nc].flat = i;
-        nc++;
-      }
+#pragma omp parallel for schedule(static, 1) num_threads(n_threads)
+    for (int c = 0; c < SCAN_CHUNKS; c++) {
+      const uint64_t a = (uint64_t)c * scan_chunk, e = c == SCAN_CHUNKS - 1 ? total : a + scan_chunk;
+      uint64_t w = chunk_off[c];
+      for (uint64_t i = a; i < e; i++)
+        if (field[i] <= threshold && !mask_get(mask, i) &&
+            (!minima || is_minimum_node(field, N, i))) {
+          cand[w].delta = field[i];
+          cand[w].refined = 0;
+          cand[w].flat = i;
+          w++;
+        }
+    }
     orc_sort_candidates(cand, nc);
     st.n_candidates = nc;
 
@@ -1247,29 +1764,52 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
     if (ext0 == n_ext && n_ext > 0 && ext_reach[n_ext - 1] > r_search)
       ext0 = n_ext - 1;
 
-    /* prefilter_cells, src/finder/exodus_finder.c:871-944 (order kept). */
-    {
-      uint64_t w = 0;
-      for (uint64_t k = 0; k < nc; k++) {
-        const uint64_t flat = cand[k].flat;
-        if (mask_get(mask, flat)) {
-          st.rejected_masked++;
-          continue;
+    /* prefilter_cells, src/finder/exodus_finder.c:871-944: 16 chunks a
+     * thread, each compacted by one thread, then closed up in order. */
+    if (nc > 0) {
+      uint64_t n_chunks = 16u * (uint64_t)n_threads;
+      if (n_chunks > nc)
+        n_chunks = nc;
+      uint64_t* kept = malloc(n_chunks * sizeof(uint64_t));
+      uint64_t n_masked = 0, n_proxy = 0, n_overlap = 0;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads) \
+  reduction(+ : n_masked, n_proxy, n_overlap)
+      for (uint64_t c = 0; c < n_chunks; c++) {
+        const uint64_t lo = nc * c / n_chunks, hi = nc * (c + 1) / n_chunks;
+        uint64_t w = lo;
+        for (uint64_t k = lo; k < hi; k++) {
+          const uint64_t flat = cand[k].flat;
+          if (mask_get(mask, flat)) {
+            n_masked++;
+            continue;
+          }
+          const uint32_t ix = (uint32_t)(flat / ((uint64_t)N * N)),
+                         iy = (uint32_t)((flat / N) % N), iz = (uint32_t)(flat % N);
+          if (proxy_pole > 0 && overlap_quick(mask, N, ix, iy, iz, (uint32_t)proxy_pole)) {
+            n_proxy++;
+            continue;
+          }
+          if (overlap_exact(&V, (float)ix * cell, (float)iy * cell, (float)iz * cell,
+                radius, max_acc, box, f, scale)) {
+            n_overlap++;
+            continue;
+          }
+          cand[w++] = cand[k];
         }
-        const uint32_t ix = (uint32_t)(flat / ((uint64_t)N * N)),
-                       iy = (uint32_t)((flat / N) % N), iz = (uint32_t)(flat % N);
-        if (proxy_pole > 0 && overlap_quick(mask, N, ix, iy, iz, (uint32_t)proxy_pole)) {
-          st.rejected_proxy++;
-          continue;
-        }
-        if (overlap_exact(&V, (float)ix * cell, (float)iy * cell, (float)iz * cell,
-              radius, max_acc, box, f, scale)) {
-          st.rejected_overlap++;
-          continue;
-        }
-        cand[w++] = cand[k];
+        kept[c] = w - lo;
       }
+      uint64_t w = 0;
+      for (uint64_t c = 0; c < n_chunks; c++) {
+        const uint64_t lo = nc * c / n_chunks;
+        if (lo != w && kept[c] > 0)
+          memmove(&cand[w], &cand[lo], kept[c] * sizeof(orc_candidate_t));
+        w += kept[c];
+      }
+      free(kept);
       nc = w;
+      st.rejected_masked += n_masked;
+      st.rejected_proxy += n_proxy;
+      st.rejected_overlap += n_overlap;
     }
 
     uint64_t floor_ = (uint64_t)BATCH_PER_THREAD * (uint64_t)n_threads;
@@ -1410,6 +1950,12 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
       stats_out[ri] = st;
   }
 
+  /* The grid handed back restored: an unfiltered backward transform of its
+   * spectrum, as the reference runs one unless SIF_FINDER_CONSUME_GRID
+   * (exodus_finder.c:2430-2453); here the values are discarded, since the
+   * oracle never changes the caller's contrast. */
+  if (spec && status == 0)
+    orc_spectrum_smooth(spec, 0, 0.0f, 0.0f, field, NULL);
   for (uint32_t k = 0; k < n_ext; k++)
     orc_template_free(&etpl[k]);
   free(bidx);

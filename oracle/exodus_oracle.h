@@ -41,6 +41,15 @@ int orc_chain_mesh(const float* x, const float* y, const float* z, uint64_t n,
 void orc_cic_f64(const float* x, const float* y, const float* z, uint64_t n,
   uint32_t grid_n, float box, double* out);
 
+/* The reference's float CIC (src/structures/grid.c:455-746): density per
+ * unit volume, its slab and chunk order, so its bits. */
+void orc_cic_float(const float* x, const float* y, const float* z, uint64_t n,
+  uint32_t grid_n, float box, float* out);
+
+/* The density contrast of an FP64 density in double: 0, or -3 if the mean
+ * is not positive. */
+int orc_density_contrast_f64(double* v, uint64_t n);
+
 /* sif_grid_to_density_contrast in place: 0, or -3 if the mean is not
  * positive. */
 int orc_density_contrast(float* v, uint64_t n);
@@ -52,6 +61,9 @@ int orc_density_contrast(float* v, uint64_t n);
 typedef struct orc_spectrum orc_spectrum_t;
 orc_spectrum_t* orc_spectrum_new(const float* delta, uint32_t n, float box,
   int window_mode /* 0 none, 1 full CIC, 2 aliasing-aware CIC */, int mode);
+/* The FP64 spectrum (mode 0) of a double contrast: the whole chain in double. */
+orc_spectrum_t* orc_spectrum_new_f64(const double* delta, uint32_t n, float box,
+  int window_mode);
 void orc_spectrum_smooth(orc_spectrum_t* s, int filter, float r, float sigma,
   float* out_f, double* out_d);
 void orc_spectrum_free(orc_spectrum_t* s);

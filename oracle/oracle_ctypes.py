@@ -14,8 +14,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+FAST_PATH = os.path.join(HERE, "liboracle_fast.so")
 
 _lib = None
+_fast = None
 
 
 def build(quiet=True):
@@ -59,35 +61,50 @@ class Catalogue(C.Structure):
                 ("n_voids", C.c_uint64)]
 
 
-def lib():
-    global _lib
+def lib(fast=False):
+    """The strict build (the checker), or with fast=True the release-flags
+    build the CPU baseline is timed with."""
+    global _lib, _fast
+    if fast:
+        if _fast is None:
+            if not os.path.exists(FAST_PATH):
+                build()
+            _fast = _declare(C.CDLL(FAST_PATH))
+        return _fast
     if _lib is None:
         if not os.path.exists(LIB_PATH):
             build()
-        L = C.CDLL(LIB_PATH)
-        vp, u64, u32, f32 = C.c_void_p, C.c_uint64, C.c_uint32, C.c_float
-        L.orc_chain_mesh.argtypes = [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]
-        L.orc_cic_f64.argtypes = [vp, vp, vp, u64, u32, f32, vp]
-        L.orc_density_contrast.argtypes = [vp, u64]
-        L.orc_spectrum_new.argtypes = [vp, u32, f32, C.c_int, C.c_int]
-        L.orc_spectrum_new.restype = vp
-        L.orc_spectrum_smooth.argtypes = [vp, C.c_int, f32, f32, vp, vp]
-        L.orc_spectrum_free.argtypes = [vp]
-        L.orc_sort_candidates.argtypes = [vp, u64]
-        L.orc_template_build.argtypes = [C.POINTER(Template), u32, f32, f32, f32]
-        L.orc_template_free.argtypes = [C.POINTER(Template)]
-        L.orc_find_radius.argtypes = [C.POINTER(Mesh), C.POINTER(Template), f32, f32, f32,
-                                      f32, f32, f32, f32, u32, C.POINTER(C.c_uint8),
-                                      C.POINTER(u64), C.POINTER(u64)]
-        L.orc_find_radius.restype = f32
-        L.orc_brute_force_radius.argtypes = [vp, vp, vp, u64, f32, C.c_double, C.c_double,
-                                             C.c_double, C.c_double, C.c_double, C.c_double]
-        L.orc_brute_force_radius.restype = C.c_double
-        L.orc_exodus.argtypes = [vp, C.POINTER(Mesh), vp, u32, C.POINTER(Params),
-                                 C.POINTER(Catalogue), vp]
-        L.orc_catalogue_free.argtypes = [C.POINTER(Catalogue)]
-        _lib = L
+        _lib = _declare(C.CDLL(LIB_PATH))
     return _lib
+
+
+def _declare(L):
+    vp, u64, u32, f32 = C.c_void_p, C.c_uint64, C.c_uint32, C.c_float
+    L.orc_chain_mesh.argtypes = [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]
+    L.orc_cic_f64.argtypes = [vp, vp, vp, u64, u32, f32, vp]
+    L.orc_cic_float.argtypes = [vp, vp, vp, u64, u32, f32, vp]
+    L.orc_density_contrast.argtypes = [vp, u64]
+    L.orc_density_contrast_f64.argtypes = [vp, u64]
+    L.orc_spectrum_new_f64.argtypes = [vp, u32, f32, C.c_int]
+    L.orc_spectrum_new_f64.restype = vp
+    L.orc_spectrum_new.argtypes = [vp, u32, f32, C.c_int, C.c_int]
+    L.orc_spectrum_new.restype = vp
+    L.orc_spectrum_smooth.argtypes = [vp, C.c_int, f32, f32, vp, vp]
+    L.orc_spectrum_free.argtypes = [vp]
+    L.orc_sort_candidates.argtypes = [vp, u64]
+    L.orc_template_build.argtypes = [C.POINTER(Template), u32, f32, f32, f32]
+    L.orc_template_free.argtypes = [C.POINTER(Template)]
+    L.orc_find_radius.argtypes = [C.POINTER(Mesh), C.POINTER(Template), f32, f32, f32,
+                                  f32, f32, f32, f32, u32, C.POINTER(C.c_uint8),
+                                  C.POINTER(u64), C.POINTER(u64)]
+    L.orc_find_radius.restype = f32
+    L.orc_brute_force_radius.argtypes = [vp, vp, vp, u64, f32, C.c_double, C.c_double,
+                                         C.c_double, C.c_double, C.c_double, C.c_double]
+    L.orc_brute_force_radius.restype = C.c_double
+    L.orc_exodus.argtypes = [vp, C.POINTER(Mesh), vp, u32, C.POINTER(Params),
+                             C.POINTER(Catalogue), vp]
+    L.orc_catalogue_free.argtypes = [C.POINTER(Catalogue)]
+    return L
 
 
 def _p(a):
@@ -140,6 +157,14 @@ def cic_f64(x, y, z, n_grid, box):
     return out
 
 
+def cic_float(x, y, z, n_grid, box):
+    """The reference's float CIC deposit (its slab and chunk order)."""
+    out = np.empty(n_grid ** 3, np.float32)
+    xs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
+    lib().orc_cic_float(_p(xs[0]), _p(xs[1]), _p(xs[2]), len(xs[0]), n_grid, box, _p(out))
+    return out
+
+
 def density_contrast(v):
     v = np.ascontiguousarray(v, dtype=np.float32).copy()
     st = lib().orc_density_contrast(_p(v), v.size)
@@ -148,11 +173,25 @@ def density_contrast(v):
     return v
 
 
+def density_contrast_f64(v):
+    """The contrast of an FP64 density, in double."""
+    v = np.ascontiguousarray(v, dtype=np.float64).copy()
+    st = lib().orc_density_contrast_f64(_p(v), v.size)
+    if st != 0:
+        raise ValueError(f"orc_density_contrast_f64: {st}")
+    return v
+
+
 def smooth(delta, n_grid, box, radii, filter=1, sigma=0.0, window_mode=1, mode=0,
            want="f32"):
-    """Per-radius smoothed fields, (len(radii), n^3), float32 or float64."""
-    d = np.ascontiguousarray(delta, dtype=np.float32)
-    s = lib().orc_spectrum_new(_p(d), n_grid, box, window_mode, mode)
+    """Per-radius smoothed fields, (len(radii), n^3), float32 or float64. A
+    float64 delta takes the whole chain in double (mode 0)."""
+    if np.asarray(delta).dtype == np.float64:
+        d = np.ascontiguousarray(delta)
+        s = lib().orc_spectrum_new_f64(_p(d), n_grid, box, window_mode)
+    else:
+        d = np.ascontiguousarray(delta, dtype=np.float32)
+        s = lib().orc_spectrum_new(_p(d), n_grid, box, window_mode, mode)
     try:
         out = np.empty((len(radii), n_grid ** 3), np.float64 if want == "f64" else np.float32)
         for i, r in enumerate(radii):
@@ -223,3 +262,65 @@ def exodus(delta, mesh, radii, n_grid, box, threshold, overlap=0.0, options=0, n
     if with_stats:
         return out, [{k: getattr(s, k) for k, _ in RungStats._fields_} for s in stats]
     return out
+
+
+def pipeline(x, y, z, n_grid, box, mesh_cells, radii, threshold, n_threads, fast=False):
+    """The whole path through the restatement, as the reference's caller runs
+    it (sif_grid_assign_cic, sif_grid_to_density_contrast,
+    sif_chain_mesh_alloc, sif_finder_exodus_raw with its own smoothing and
+    the final restore of the grid): (catalogue, seconds per stage). fast: the
+    release-flags build, for timing."""
+    import time
+
+    L = lib(fast)
+    xs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
+    n = len(xs[0])
+    t = {}
+    t0 = time.perf_counter()
+    grid = np.empty(n_grid ** 3, np.float32)
+    L.orc_cic_float(_p(xs[0]), _p(xs[1]), _p(xs[2]), n, n_grid, box, _p(grid))
+    t["cic"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    if L.orc_density_contrast(_p(grid), grid.size) != 0:
+        raise ValueError("orc_density_contrast")
+    t["contrast"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mx, my, mz = (np.empty(n, np.float32) for _ in range(3))
+    offs = np.empty(mesh_cells ** 3 + 1, np.uint64)
+    if L.orc_chain_mesh(_p(xs[0]), _p(xs[1]), _p(xs[2]), n, mesh_cells, box, _p(mx), _p(my),
+                        _p(mz), _p(offs), None) != 0:
+        raise ValueError("orc_chain_mesh")
+    t["mesh"] = time.perf_counter() - t0
+    mesh = Mesh(_p(mx), _p(my), _p(mz), _p(offs), n, mesh_cells, float(np.float32(box)),
+                float(np.float32(np.float32(box) / np.float32(mesh_cells))))
+    r = np.ascontiguousarray(radii, dtype=np.float32)
+    p = Params(n_grid, box, threshold, 0.0, 0, n_threads, 0, 1, None, None, None, None, None, 0)
+    cat = Catalogue()
+    t0 = time.perf_counter()
+    st = L.orc_exodus(_p(grid), C.byref(mesh), _p(r), len(r), C.byref(p), C.byref(cat), None)
+    t["finder"] = time.perf_counter() - t0
+    if st != 0:
+        raise ValueError(f"orc_exodus: {st}")
+    nv = cat.n_voids
+    out = tuple(np.ctypeslib.as_array(getattr(cat, k), shape=(nv,)).copy() if nv else
+                np.zeros(0, np.float32) for k in ("cx", "cy", "cz", "r"))
+    L.orc_catalogue_free(C.byref(cat))
+    return out, t
+
+
+def smoothing_seconds(delta, n_grid, box, radii, fast=False):
+    """The transforms the finder runs on its own (the forward once, the
+    filter and backward per rung, the unfiltered restore), timed alone: the
+    part of the finder's time that is the FFT stage."""
+    import time
+
+    L = lib(fast)
+    d = np.ascontiguousarray(delta, dtype=np.float32)
+    out = np.empty(n_grid ** 3, np.float32)
+    t0 = time.perf_counter()
+    s = L.orc_spectrum_new(_p(d), n_grid, box, 1, 1)
+    for r in radii:
+        L.orc_spectrum_smooth(s, 1, float(r), 0.0, _p(out), None)
+    L.orc_spectrum_smooth(s, 0, 0.0, 0.0, _p(out), None)
+    L.orc_spectrum_free(s)
+    return time.perf_counter() - t0

@@ -18,6 +18,14 @@ golden_box32_f64.npz -- the same box through the reference's SIF_USE_DOUBLE
   up to 1e-4 so that they need double precision, and the same records in
   double (density, contrast, mesh, 12 captured fields, catalogues).
 
+golden_workload_a.npz -- workload A itself: 128^3 particles (synth.workload_particles
+  ("A"): box 500, rms displacement 4, seed 1001), grid 128^3, mesh 50^3,
+  ladder(5, 30, 0.10) (19 rungs), threshold -0.8. The reference's whole path
+  on its own (CIC in float, contrast, mesh, the shim's FFT), and its
+  catalogue; the positions are not stored (25 MB), only the SHA-256 of their
+  float32 bytes, so that a test regenerating them on another machine fails
+  loudly where the generator does not give the same bits there.
+
 golden_box32_extend.npz, golden_box32_extend_f64.npz -- the same positions
   (the f64 file with the same jitter) at a shallow threshold, -0.3, and the
   ladder(4, 8, 0.1) (8 rungs), where SIF_FINDER_EXTEND_REACH changes the
@@ -191,8 +199,35 @@ def make_box32_extend(path, v="strict"):
     print(f"{path}: " + ", ".join(f"{n} {len(out[f'cat_{n}_r'])}" for n, _, _ in EXTEND_SETS))
 
 
+def positions_sha256(x, y, z):
+    import hashlib
+
+    h = hashlib.sha256()
+    for a in (x, y, z):
+        h.update(np.ascontiguousarray(a, np.float32).tobytes())
+    return h.hexdigest()
+
+
+def make_workload_a(path):
+    w = synth.WORKLOADS["A"]
+    x, y, z = synth.workload_particles("A")
+    radii = synth.workload_radii("A")
+    mesh = int(round(w["box"] / w["mesh_cell"]))
+    cat = R.pipeline(x, y, z, w["n"], w["box"], mesh, radii, w["threshold"], n_threads=0)
+    out = {f"cat_{k}": c for k, c in zip(("cx", "cy", "cz", "r"), cat)}
+    out.update(radii=radii, positions_sha256=np.array(positions_sha256(x, y, z)),
+               params=np.array([w["n"], w["box"], w["rms_disp"], w["seed"], w["n"], mesh,
+                                w["threshold"]], np.float64))
+    np.savez_compressed(path, **out)
+    print(f"{path}: {len(cat[0])} voids over {len(radii)} rungs")
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 1 and sys.argv[1] == "workload_a":
+        make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))
+        sys.exit(0)
     make_box32(os.path.join(HERE, "golden_box32.npz"))
     make_box32_f64(os.path.join(HERE, "golden_box32_f64.npz"))
     make_box32_extend(os.path.join(HERE, "golden_box32_extend.npz"))
     make_box32_extend(os.path.join(HERE, "golden_box32_extend_f64.npz"), "f64")
+    make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))

@@ -29,6 +29,82 @@ def test_oracle_contrast_matches_golden(oracle, golden_box32):
     assert same_bits(d, golden_box32["delta"])
 
 
+def test_port_float_cic_is_the_reference_deposit(oracle, golden_box32):
+    """The port's float CIC (grid_compute_cic's slabs, tiles, chunks and
+    ghost fold, src/structures/grid.c:455-746): the reference's density, bit
+    for bit."""
+    g = golden_box32
+    d = oracle.cic_float(g["x"], g["y"], g["z"], int(g["params"][0]), float(g["params"][1]))
+    assert same_bits(d, g["density"])
+
+
+def test_port_float_smoothing_is_the_reference_transform(oracle, golden_box32):
+    """The oracle's float smoothing (the reference's planes and pencils
+    through the same FFTW-API calls, src/math/fft.c:378-434, 790-888, with its
+    float filter table and window): the fields the reference's own run
+    smoothed, bit for bit."""
+    g = golden_box32
+    radii = np.sort(g["radii"])[::-1]
+    f = oracle.smooth(g["delta"], int(g["params"][0]), float(g["params"][1]), radii, mode=1)
+    assert same_bits(f, g["fields"])
+
+
+def test_port_pipeline_reproduces_the_reference_run_on_workload_a(oracle):
+    """Workload A (128^3 particles, box 500, grid 128^3, mesh 50^3, 19 rungs,
+    threshold -0.8) through the whole port -- float CIC, contrast, mesh, the
+    finder with its own smoothing -- gives the reference's own end-to-end
+    catalogue bit for bit (tests/golden/golden_workload_a.npz, made from the
+    reference's strict build)."""
+    import hashlib
+    import os
+
+    from conftest import GOLDEN
+
+    g = dict(np.load(os.path.join(GOLDEN, "golden_workload_a.npz")))
+    x, y, z = synth.workload_particles("A")
+    h = hashlib.sha256()
+    for a in (x, y, z):
+        h.update(np.ascontiguousarray(a, np.float32).tobytes())
+    assert h.hexdigest() == str(g["positions_sha256"])
+    cat, _ = oracle.pipeline(x, y, z, 128, 500.0, 50, g["radii"], -0.8, n_threads=4)
+    want = tuple(g[f"cat_{k}"] for k in ("cx", "cy", "cz", "r"))
+    assert len(cat[0]) == len(want[0]) and same_catalogue(cat, want)
+
+
+@pytest.mark.skipif("not __import__('ref_ctypes').available('fast')")
+def test_port_runs_at_the_reference_release_build_speed(oracle):
+    """The timed CPU baseline is the port's release-flags build: on workload A
+    it takes about what the reference's own release build takes on the same
+    cores (median of three whole-path runs each; printed). A bound of 1.5x
+    leaves room for a loaded machine."""
+    import os
+    import time
+
+    import ref_ctypes as R
+
+    x, y, z = synth.workload_particles("A")
+    radii = synth.workload_radii("A")
+    threads = os.cpu_count() or 1
+
+    def ref_run():
+        t0 = time.perf_counter()
+        R.pipeline(x, y, z, 128, 500.0, 50, radii, -0.8, variant="fast", n_threads=0)
+        return time.perf_counter() - t0
+
+    def port_run():
+        t0 = time.perf_counter()
+        oracle.pipeline(x, y, z, 128, 500.0, 50, radii, -0.8, threads, fast=True)
+        return time.perf_counter() - t0
+
+    ref_run()
+    port_run()
+    t_ref = sorted(ref_run() for _ in range(3))[1]
+    t_port = sorted(port_run() for _ in range(3))[1]
+    print(f"workload A on {threads} threads: port {t_port * 1e3:.1f} ms, reference release "
+          f"build {t_ref * 1e3:.1f} ms, ratio {t_port / t_ref:.3f}")
+    assert t_port <= 1.5 * t_ref
+
+
 def test_oracle_cic_f64_close_to_reference_float_cic(oracle, golden_box32):
     g = golden_box32
     n, box = int(g["params"][0]), float(g["params"][1])
@@ -180,6 +256,16 @@ def test_oracle_four_holes_and_brute_force_radius(oracle, holes_field):
             assert want > 0 and abs(c[3][i] - want) <= 1e-5 * want
 
 
+def _ref_density(lib, field):
+    import ref_ctypes as R
+
+    g = R.RefGrid(lib, 48, 200.0)
+    g.assign_cic(field)
+    d = g.values()
+    g.free()
+    return d
+
+
 @pytest.mark.skipif("not __import__('ref_ctypes').available()")
 def test_oracle_matches_reference_library_on_zeldovich(oracle):
     """Against the reference compiled from its own sources: its own CIC,
@@ -200,10 +286,10 @@ def test_oracle_matches_reference_library_on_zeldovich(oracle):
     m = oracle.OracleMesh(x, y, z, 12, 200.0)
     got = oracle.exodus(delta, m, radii, 48, 200.0, -0.75, n_threads=3, inject=fields)
     assert len(want[0]) > 5 and same_catalogue(got, want)
-    # The oracle's own float smoothing reproduces the reference's to rounding.
+    # The oracle's own float smoothing and CIC are the reference's, bit for bit.
     own = oracle.smooth(delta, 48, 200.0, np.sort(radii)[::-1], mode=1)
-    rms = np.sqrt((fields ** 2).mean())
-    assert np.abs(own - fields).max() <= 1e-5 * rms
+    assert same_bits(own, fields)
+    assert same_bits(oracle.cic_float(x, y, z, 48, 200.0), _ref_density(lib, f))
     rm.free()
     g.free()
     f.free()
