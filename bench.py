@@ -244,7 +244,7 @@ def gpu_arm(args, rank, world):
         adj = adjoint_run(args)
         batch = batch_run(args)
 
-    precision = precision_run(args) if args.precision else None
+    precision = precision_run(args) if not (args.no_precision or args.small) else None
 
     cpu = None
     if rank == 0 and not args.no_cpu and not args.small:
@@ -418,12 +418,41 @@ def batch_run(args):
 
 
 # The precision workload: 1024^3 particles in a 2000 Mpc/h box (rms
-# displacement 4, seed 1003), grid 1024^3. The float form's CIC contrast and
-# smoothed fields against the FP64 form's on the same positions (top-hat
-# R = 4 with the CIC window correction, the finder's smoothing; Gaussian
-# R = 5), and the float finder on the whole box (ladder(4, 24, 0.10),
+# displacement 4, seed 1003), grid 1024^3. The float form's smoothed fields
+# (top-hat R = 4 with the CIC window correction, the finder's smoothing;
+# Gaussian R = 5), from its own CIC and contrast, against the whole chain in
+# FP64 on the CPU (the oracle: FP64 CIC, contrast, transforms) and against the
+# GPU's FP64 form; then the float finder on the whole box (ladder(4, 24, 0.10),
 # threshold -0.8, suggested mesh).
 PRECISION = dict(n=1024, box=2000.0, rms=4.0, seed=1003, grid=1024, r_tophat=4.0, r_gauss=5.0)
+# Host memory the CPU FP64 chain at 1024^3 needs at its peak (positions,
+# density, spectrum, a filtered copy, a field, the two float fields).
+PRECISION_HOST_GB = 64.0
+
+
+def host_available_gb():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) / 2 ** 20
+    except OSError:
+        pass
+    return 0.0
+
+
+def rel_err(got, want, chunk=1 << 26):
+    """Relative L2 and max-norm (both over the rms of want) of two n^3
+    arrays, in chunks (no full-size temporaries)."""
+    se = sw = mx = 0.0
+    for a in range(0, len(want), chunk):
+        g = np.asarray(got[a:a + chunk], np.float64)
+        w = np.asarray(want[a:a + chunk], np.float64)
+        d = g - w
+        se += float(np.dot(d, d))
+        sw += float(np.dot(w, w))
+        mx = max(mx, float(np.abs(d).max()))
+    rms = math.sqrt(sw / len(want))
+    return math.sqrt(se / len(want)) / rms, mx / rms
 
 
 def precision_run(args):
@@ -435,7 +464,6 @@ def precision_run(args):
     n = c["grid"]
     x, y, z = synth.zeldovich(c["n"], c["box"], c["rms"], c["seed"], backend="torch")
     xs = [torch.from_numpy(v).cuda() for v in (x, y, z)]
-    del x, y, z
 
     def rel(a, b):
         d = (a.double() - b)
@@ -446,22 +474,55 @@ def precision_run(args):
     device.density_contrast(g32)
     fields32 = {"tophat": device.smooth(g32, n, c["box"], c["r_tophat"]),
                 "gauss": device.smooth(g32, n, c["box"], c["r_gauss"], filter="gaussian")}
+    out = {"config": "1024^3 particles, box 2000 Mpc/h, grid 1024^3; the float form's fields "
+                     "(its CIC, contrast, top-hat R=4 and Gaussian R=5 smoothing) against the "
+                     "whole chain in FP64"}
+    # Against the GPU's FP64 form on the same positions.
     xs64 = [v.double() for v in xs]
     g64 = device.cic(*xs64, n, c["box"])
     del xs64
     device.density_contrast(g64)
-    out = {"config": "1024^3 particles, box 2000 Mpc/h, grid 1024^3; float form against the FP64 "
-                     "form on the same positions",
-           "contrast_rel_l2": None, "tophat_r4_rel_l2": None, "gauss_r5_rel_l2": None}
-    out["contrast_rel_l2"], out["contrast_rel_max"] = rel(g32, g64)
-    del g32
-    f64 = device.smooth(g64, n, c["box"], c["r_tophat"])
-    out["tophat_r4_rel_l2"], out["tophat_r4_rel_max"] = rel(fields32["tophat"], f64)
-    del f64
-    f64 = device.smooth(g64, n, c["box"], c["r_gauss"], filter="gaussian")
-    out["gauss_r5_rel_l2"], out["gauss_r5_rel_max"] = rel(fields32["gauss"], f64)
-    del f64, g64, fields32
+    out["fp64_form"] = {}
+    out["fp64_form"]["contrast_rel_l2"], out["fp64_form"]["contrast_rel_max"] = rel(g32, g64)
+    for key, r, filt in (("tophat_r4", c["r_tophat"], "top-hat"), ("gauss_r5", c["r_gauss"], "gaussian")):
+        f64 = device.smooth(g64, n, c["box"], r, filter=filt)
+        out["fp64_form"][f"{key}_rel_l2"], out["fp64_form"][f"{key}_rel_max"] = rel(
+            fields32["tophat" if key.startswith("top") else "gauss"], f64)
+        del f64
+    del g64, g32
+    host32 = {k: v.cpu().numpy() for k, v in fields32.items()}
+    del fields32
     torch.cuda.empty_cache()
+    # Against the CPU FP64 oracle, where the host has the memory for it.
+    avail = host_available_gb()
+    if avail >= PRECISION_HOST_GB:
+        import oracle_ctypes as O
+
+        O.build()
+        t0 = time.perf_counter()
+        d64 = O.cic_f64(x, y, z, n, c["box"])
+        O.density_contrast_f64(d64, inplace=True)
+        spec = O.Spectrum(d64, n, c["box"])
+        del d64
+        oracle = {}
+        for key, r, code in (("tophat_r4", c["r_tophat"], 1), ("gauss_r5", c["r_gauss"], 2)):
+            f64 = spec.smooth(r, code)
+            oracle[f"{key}_rel_l2"], oracle[f"{key}_rel_max"] = rel_err(
+                host32["tophat" if code == 1 else "gauss"], f64)
+            del f64
+        spec.free()
+        oracle["cpu_s"] = round(time.perf_counter() - t0, 1)
+        out["fp64_oracle"] = oracle
+        out["tophat_r4_rel_l2"] = oracle["tophat_r4_rel_l2"]
+        out["gauss_r5_rel_l2"] = oracle["gauss_r5_rel_l2"]
+        out["reference"] = "FP64 oracle (CPU)"
+    else:
+        out["fp64_oracle"] = (f"not run: {avail:.0f} GB of host memory available, the CPU FP64 "
+                              f"chain at 1024^3 needs about {PRECISION_HOST_GB:.0f}")
+        out["tophat_r4_rel_l2"] = out["fp64_form"]["tophat_r4_rel_l2"]
+        out["gauss_r5_rel_l2"] = out["fp64_form"]["gauss_r5_rel_l2"]
+        out["reference"] = "the GPU's FP64 form"
+    del host32, x, y, z
     radii = synth.ladder(4.0, 24.0, 0.10).astype(np.float32)
     mesh = pysif.finders.suggest_mesh_cells(c["n"] ** 3, c["box"], float(radii.max()))
     stream = device.stream()
@@ -475,6 +536,8 @@ def precision_run(args):
     ms = start.elapsed_time(end)
     out.update({"finder_ms": round(ms, 2), "finder_mparticles_s": round(c["n"] ** 3 / ms / 1e3, 2),
                 "mesh_cells": mesh, "n_voids": len(cat[0])})
+    del xs
+    torch.cuda.empty_cache()
     return out
 
 
@@ -607,8 +670,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP64-form and adjoint runs")
-    ap.add_argument("--precision", action="store_true",
-                    help="also the 1024^3 float-vs-FP64 field error and the 1024^3 finder")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the 1024^3 float-vs-FP64 field error and the 1024^3 finder")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()

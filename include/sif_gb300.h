@@ -306,6 +306,7 @@ typedef struct {
   /* Host wait for the candidates' depths before the sort, milliseconds. */
   double cand_wait_ms;
   uint64_t from_list;      /* 1: the candidates came from the smoothing's below-threshold list */
+  uint64_t n_witness;      /* survivors the collision witness refused before any growth */
 } sifg_rung_stat_t;
 
 /* Kernel timings of the last run, CUDA events on the launching stream. */
@@ -319,10 +320,14 @@ typedef struct {
   int cic_launches;
   double mesh_ms;
   int mesh_launches;
-  /* What the sphere growth gathered: particle positions read (12 bytes
-   * each) and template cells visited (16 bytes each). */
+  /* What the sphere growth and the collision witness gathered: particle
+   * positions read (12 bytes each) and template cells visited (16 bytes
+   * each). */
   uint64_t growth_particles;
   uint64_t growth_cells;
+  /* The collision witness, run ahead of each rung's growth. */
+  double witness_ms;
+  int witness_launches;
 } sifg_timings_t;
 
 /* The CIC density (per unit volume, float) of n device-resident particles
@@ -466,6 +471,12 @@ void sifg_set_commit_mode(int mode);
  * it goes, where it can (the float form at a 512^3 grid), less the masked
  * cells; 1 a scan of the whole field. The catalogue does not depend on it. */
 void sifg_set_scan_mode(int mode);
+/* The collision witness (exodus_finder.c:780-845, exodus_rescale.c:
+ * 1074-1167): 1 (default) survivors whose sphere is certain to collide with
+ * a void of an earlier rung at any radius they could return are refused
+ * before growth, as the reference refuses them; 0 every survivor is grown
+ * and the commit refuses them. The catalogue does not depend on it. */
+void sifg_set_witness(int on);
 /* The chain-mesh build of sifg_mesh_device, for callers that cannot let the
  * library allocate device memory: a process whose framework reserves the
  * GPU's memory in its own pool, a latency-bound pipeline that cannot afford

@@ -226,34 +226,52 @@ void orc_cic_f64(const float* x, const float* y, const float* z, uint64_t n,
 #pragma omp parallel for schedule(static)
   for (uint64_t i = 0; i < total; i++)
     out[i] = 0.0;
-  uint64_t* start = calloc((size_t)N + 1, sizeof(uint64_t));
-  uint32_t* base = malloc(n * sizeof(uint32_t));
-  uint64_t* order = malloc(n * sizeof(uint64_t));
-  if (!start || !base || !order) {
-    free(start);
-    free(base);
+  if (n == 0 || n >= (1ull << 32))
+    return;
+  /* Bucketed by base plane, counted per thread chunk and placed in order. */
+  const int nt = omp_get_max_threads();
+  uint64_t* counts = calloc((size_t)nt * N + 1, sizeof(uint64_t));
+  uint32_t* order = malloc(n * sizeof(uint32_t));
+  uint64_t* start = malloc(((size_t)N + 1) * sizeof(uint64_t));
+  if (!counts || !order || !start) {
+    free(counts);
     free(order);
+    free(start);
     return;
   }
-#pragma omp parallel for schedule(static)
-  for (uint64_t p = 0; p < n; p++) {
-    uint32_t a, b;
-    double w0, w1;
-    cic_f64_base(x[p], box, idx, N, &a, &b, &w0, &w1);
-    base[p] = a;
-  }
-  for (uint64_t p = 0; p < n; p++)
-    start[base[p] + 1]++;
-  for (uint32_t i = 0; i < N; i++)
-    start[i + 1] += start[i];
+#pragma omp parallel num_threads(nt)
   {
-    uint64_t* cur = malloc((size_t)N * sizeof(uint64_t));
-    memcpy(cur, start, (size_t)N * sizeof(uint64_t));
-    for (uint64_t p = 0; p < n; p++)
-      order[cur[base[p]]++] = p;
-    free(cur);
+    const int t = omp_get_thread_num();
+    const uint64_t a = n * (uint64_t)t / (uint64_t)nt, e = n * (uint64_t)(t + 1) / (uint64_t)nt;
+    uint64_t* c = counts + (uint64_t)t * N;
+    for (uint64_t p = a; p < e; p++) {
+      uint32_t i0, i1;
+      double w0, w1;
+      cic_f64_base(x[p], box, idx, N, &i0, &i1, &w0, &w1);
+      c[i0]++;
+    }
+#pragma omp barrier
+#pragma omp single
+    {
+      uint64_t run = 0;
+      for (uint32_t ix = 0; ix < N; ix++) {
+        start[ix] = run;
+        for (int u = 0; u < nt; u++) {
+          const uint64_t v = counts[(uint64_t)u * N + ix];
+          counts[(uint64_t)u * N + ix] = run;
+          run += v;
+        }
+      }
+      start[N] = run;
+    }
+    for (uint64_t p = a; p < e; p++) {
+      uint32_t i0, i1;
+      double w0, w1;
+      cic_f64_base(x[p], box, idx, N, &i0, &i1, &w0, &w1);
+      order[c[i0]++] = (uint32_t)p;
+    }
   }
-  free(base);
+  free(counts);
   for (int phase = 0; phase < 3; phase++) {
     /* Phase 0: even planes, 1: odd planes, 2: an odd N's last plane. */
     const uint32_t last = (N & 1u) ? N - 1 : N;
@@ -494,77 +512,83 @@ struct orc_spectrum {
 
 static uint64_t plane_modes(uint32_t n) { return (uint64_t)n * (n / 2 + 1); }
 
-/* fft_pencils, src/math/fft.c:378-434. */
-static void pencils_f(fftwf_complex* c, uint32_t n, int sign) {
-  const int len[1] = {(int)n};
-  const uint64_t n_pencils = plane_modes(n);
-  const uint64_t n_blocks = (n_pencils + PENCIL_BLOCK - 1) / PENCIL_BLOCK;
-  fftwf_complex* scratch = fftwf_malloc((size_t)n * PENCIL_BLOCK * sizeof(fftwf_complex));
-  fftwf_plan plan = fftwf_plan_many_dft(1, len, PENCIL_BLOCK, scratch, NULL, PENCIL_BLOCK, 1,
-    scratch, NULL, PENCIL_BLOCK, 1, sign, FFTW_ESTIMATE);
-  fftwf_free(scratch);
-#pragma omp parallel
-  {
-    fftwf_complex* g = fftwf_malloc((size_t)n * PENCIL_BLOCK * sizeof(fftwf_complex));
-#pragma omp for schedule(static)
-    for (uint64_t b = 0; b < n_blocks; b++) {
-      const uint64_t j0 = b * PENCIL_BLOCK;
-      const uint64_t w = n_pencils - j0 < PENCIL_BLOCK ? n_pencils - j0 : PENCIL_BLOCK;
-      for (uint32_t x = 0; x < n; x++) {
-        fftwf_complex* row = g + (uint64_t)x * PENCIL_BLOCK;
-        memcpy(row, c + x * n_pencils + j0, w * sizeof(fftwf_complex));
-        if (w < PENCIL_BLOCK)
-          memset(row + w, 0, (PENCIL_BLOCK - w) * sizeof(fftwf_complex));
-      }
-      fftwf_execute_dft(plan, g, g);
-      for (uint32_t x = 0; x < n; x++)
-        memcpy(c + x * n_pencils + j0, g + (uint64_t)x * PENCIL_BLOCK, w * sizeof(fftwf_complex));
-    }
-    fftwf_free(g);
+/* fft_pencils (src/math/fft.c:378-434), sif__fft_grid_forward (790-818) and
+ * sif__fft_grid_backward (820-888) for a precision: X the FFTW-API prefix,
+ * R its real type. The float pair is the reference's transform; the double
+ * pair runs the FP64 oracle's transforms the same way (plane by plane, pencil
+ * block by pencil block), which keeps them in cache at large grids. */
+#define ORC_TRANSFORMS(X, R, SUFFIX)                                              \
+  static void pencils_##SUFFIX(X##_complex* c, uint32_t n, int sign) {            \
+    const int len[1] = {(int)n};                                                  \
+    const uint64_t n_pencils = plane_modes(n);                                    \
+    const uint64_t n_blocks = (n_pencils + PENCIL_BLOCK - 1) / PENCIL_BLOCK;      \
+    X##_complex* scratch = X##_malloc((size_t)n * PENCIL_BLOCK * sizeof(X##_complex)); \
+    X##_plan plan = X##_plan_many_dft(1, len, PENCIL_BLOCK, scratch, NULL,        \
+      PENCIL_BLOCK, 1, scratch, NULL, PENCIL_BLOCK, 1, sign, FFTW_ESTIMATE);      \
+    X##_free(scratch);                                                            \
+    _Pragma("omp parallel")                                                       \
+    {                                                                             \
+      X##_complex* g = X##_malloc((size_t)n * PENCIL_BLOCK * sizeof(X##_complex)); \
+      _Pragma("omp for schedule(static)")                                         \
+      for (uint64_t b = 0; b < n_blocks; b++) {                                   \
+        const uint64_t j0 = b * PENCIL_BLOCK;                                     \
+        const uint64_t w = n_pencils - j0 < PENCIL_BLOCK ? n_pencils - j0 : PENCIL_BLOCK; \
+        for (uint32_t x = 0; x < n; x++) {                                        \
+          X##_complex* row = g + (uint64_t)x * PENCIL_BLOCK;                      \
+          memcpy(row, c + x * n_pencils + j0, w * sizeof(X##_complex));           \
+          if (w < PENCIL_BLOCK)                                                   \
+            memset(row + w, 0, (PENCIL_BLOCK - w) * sizeof(X##_complex));        \
+        }                                                                         \
+        X##_execute_dft(plan, g, g);                                              \
+        for (uint32_t x = 0; x < n; x++)                                          \
+          memcpy(c + x * n_pencils + j0, g + (uint64_t)x * PENCIL_BLOCK,          \
+            w * sizeof(X##_complex));                                             \
+      }                                                                           \
+      X##_free(g);                                                                \
+    }                                                                             \
+    X##_destroy_plan(plan);                                                       \
+  }                                                                               \
+                                                                                  \
+  static void forward_##SUFFIX(const R* in, X##_complex* spec, uint32_t n) {      \
+    const uint64_t reals = (uint64_t)n * n, modes = plane_modes(n);               \
+    R* pr = X##_malloc(reals * sizeof(R));                                        \
+    X##_complex* pc = X##_malloc(modes * sizeof(X##_complex));                    \
+    X##_plan plane = X##_plan_dft_r2c_2d((int)n, (int)n, pr, pc, FFTW_ESTIMATE);  \
+    X##_free(pr);                                                                 \
+    X##_free(pc);                                                                 \
+    _Pragma("omp parallel for schedule(static)")                                  \
+    for (uint32_t x = 0; x < n; x++)                                              \
+      X##_execute_dft_r2c(plane, (R*)in + x * reals, spec + x * modes);           \
+    X##_destroy_plan(plane);                                                      \
+    pencils_##SUFFIX(spec, n, FFTW_FORWARD);                                      \
+  }                                                                               \
+                                                                                  \
+  static void backward_##SUFFIX(X##_complex* c, R* out, uint32_t n) {             \
+    pencils_##SUFFIX(c, n, FFTW_BACKWARD);                                        \
+    const uint64_t reals = (uint64_t)n * n, modes = plane_modes(n);               \
+    const R norm = (R)1.0 / (R)((uint64_t)n * n * n);                             \
+    R* pr = X##_malloc(reals * sizeof(R));                                        \
+    X##_complex* pc = X##_malloc(modes * sizeof(X##_complex));                    \
+    X##_plan plane = X##_plan_dft_c2r_2d((int)n, (int)n, pc, pr, FFTW_ESTIMATE);  \
+    X##_free(pr);                                                                 \
+    X##_free(pc);                                                                 \
+    _Pragma("omp parallel")                                                       \
+    {                                                                             \
+      R* buf = X##_malloc(reals * sizeof(R));                                     \
+      _Pragma("omp for schedule(static)")                                         \
+      for (uint32_t x = 0; x < n; x++) {                                          \
+        X##_execute_dft_c2r(plane, c + x * modes, buf);                           \
+        R* o = out + x * reals;                                                   \
+        for (uint64_t i = 0; i < reals; i++)                                      \
+          o[i] = buf[i] * norm;                                                   \
+      }                                                                           \
+      X##_free(buf);                                                              \
+    }                                                                             \
+    X##_destroy_plan(plane);                                                      \
   }
-  fftwf_destroy_plan(plan);
-}
 
-/* sif__fft_grid_forward, src/math/fft.c:790-818. */
-static void forward_f(const float* in, fftwf_complex* spec, uint32_t n) {
-  const uint64_t reals = (uint64_t)n * n, modes = plane_modes(n);
-  float* pr = fftwf_malloc(reals * sizeof(float));
-  fftwf_complex* pc = fftwf_malloc(modes * sizeof(fftwf_complex));
-  fftwf_plan plane = fftwf_plan_dft_r2c_2d((int)n, (int)n, pr, pc, FFTW_ESTIMATE);
-  fftwf_free(pr);
-  fftwf_free(pc);
-#pragma omp parallel for schedule(static)
-  for (uint32_t x = 0; x < n; x++)
-    fftwf_execute_dft_r2c(plane, (float*)in + x * reals, spec + x * modes);
-  fftwf_destroy_plan(plane);
-  pencils_f(spec, n, FFTW_FORWARD);
-}
-
-/* sif__fft_grid_backward, src/math/fft.c:820-888: the pencils in place, then
- * each plane's C2R, times 1/N^3 in float, into out. */
-static void backward_f(fftwf_complex* c, float* out, uint32_t n) {
-  pencils_f(c, n, FFTW_BACKWARD);
-  const uint64_t reals = (uint64_t)n * n, modes = plane_modes(n);
-  const float norm = 1.0f / (float)((uint64_t)n * n * n);
-  float* pr = fftwf_malloc(reals * sizeof(float));
-  fftwf_complex* pc = fftwf_malloc(modes * sizeof(fftwf_complex));
-  fftwf_plan plane = fftwf_plan_dft_c2r_2d((int)n, (int)n, pc, pr, FFTW_ESTIMATE);
-  fftwf_free(pr);
-  fftwf_free(pc);
-#pragma omp parallel
-  {
-    float* buf = fftwf_malloc(reals * sizeof(float));
-#pragma omp for schedule(static)
-    for (uint32_t x = 0; x < n; x++) {
-      fftwf_execute_dft_c2r(plane, c + x * modes, buf);
-      float* o = out + x * reals;
-      for (uint64_t i = 0; i < reals; i++)
-        o[i] = buf[i] * norm;
-    }
-    fftwf_free(buf);
-  }
-  fftwf_destroy_plan(plane);
-}
+ORC_TRANSFORMS(fftwf, float, f)
+ORC_TRANSFORMS(fftw, double, d)
 
 /* x = pi k / N for index i (src/math/fft.c:939-943), with the reference's
  * float pi in the float mode. */
@@ -587,15 +611,17 @@ static orc_spectrum_t* spectrum_new(const float* delta_f, const double* delta_d,
     s->specf = fftwf_malloc(modes * sizeof(fftwf_complex));
     forward_f(delta_f, s->specf, n);
   } else {
-    double* in = malloc(total * sizeof(double));
-#pragma omp parallel for schedule(static)
-    for (uint64_t i = 0; i < total; i++)
-      in[i] = delta_d ? delta_d[i] : (double)delta_f[i];
     s->spec = fftw_malloc(modes * sizeof(fftw_complex));
-    fftw_plan p = fftw_plan_dft_r2c_3d(n, n, n, in, s->spec, FFTW_ESTIMATE);
-    fftw_execute(p);
-    fftw_destroy_plan(p);
-    free(in);
+    if (delta_d) {
+      forward_d(delta_d, s->spec, n);
+    } else {
+      double* in = malloc(total * sizeof(double));
+#pragma omp parallel for schedule(static)
+      for (uint64_t i = 0; i < total; i++)
+        in[i] = (double)delta_f[i];
+      forward_d(in, s->spec, n);
+      free(in);
+    }
   }
   if (window_mode) {
     /* fft_build_window_axis, src/math/fft.c:958-975, order 2 (CIC):
@@ -742,20 +768,15 @@ void orc_spectrum_smooth(orc_spectrum_t* s, int filter, float r, float sigma,
     }
   }
   free(lut);
-  double* real = malloc(total * sizeof(double));
-  fftw_plan p = fftw_plan_dft_c2r_3d(n, n, n, work, real, FFTW_ESTIMATE);
-  fftw_execute(p);
-  fftw_destroy_plan(p);
+  double* real = out_d ? out_d : malloc(total * sizeof(double));
+  backward_d(work, real, n);
   fftw_free(work);
-  const double norm = 1.0 / (double)total;
+  if (out_f)
 #pragma omp parallel for schedule(static)
-  for (uint64_t i = 0; i < total; i++) {
-    if (out_d)
-      out_d[i] = real[i] * norm;
-    if (out_f)
-      out_f[i] = (float)(real[i] * norm);
-  }
-  free(real);
+    for (uint64_t i = 0; i < total; i++)
+      out_f[i] = (float)real[i];
+  if (!out_d)
+    free(real);
 }
 
 void orc_spectrum_free(orc_spectrum_t* s) {

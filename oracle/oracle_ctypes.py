@@ -173,9 +173,10 @@ def density_contrast(v):
     return v
 
 
-def density_contrast_f64(v):
-    """The contrast of an FP64 density, in double."""
-    v = np.ascontiguousarray(v, dtype=np.float64).copy()
+def density_contrast_f64(v, inplace=False):
+    """The contrast of an FP64 density, in double (in v itself with inplace,
+    for a contiguous float64 v)."""
+    v = v if inplace else np.ascontiguousarray(v, dtype=np.float64).copy()
     st = lib().orc_density_contrast_f64(_p(v), v.size)
     if st != 0:
         raise ValueError(f"orc_density_contrast_f64: {st}")
@@ -324,3 +325,23 @@ def smoothing_seconds(delta, n_grid, box, radii, fast=False):
     L.orc_spectrum_smooth(s, 0, 0.0, 0.0, _p(out), None)
     L.orc_spectrum_free(s)
     return time.perf_counter() - t0
+
+
+class Spectrum:
+    """An FP64 spectrum of a double contrast, kept to smooth at several radii
+    one at a time (each smoothing returns one n^3 float64 field)."""
+
+    def __init__(self, delta64, n_grid, box, window_mode=1):
+        d = np.ascontiguousarray(delta64, dtype=np.float64)
+        self.n = n_grid
+        self.ptr = lib().orc_spectrum_new_f64(_p(d), n_grid, box, window_mode)
+
+    def smooth(self, r, filter=1):
+        out = np.empty(self.n ** 3, np.float64)
+        lib().orc_spectrum_smooth(self.ptr, filter, float(r), 0.0, None, _p(out))
+        return out
+
+    def free(self):
+        if self.ptr:
+            lib().orc_spectrum_free(self.ptr)
+            self.ptr = None

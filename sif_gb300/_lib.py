@@ -21,7 +21,8 @@ class RungStat(C.Structure):
                 ("rung_ms", C.c_double), ("count_wait_ms", C.c_double),
                 ("sort_ms", C.c_double), ("commit_ms", C.c_double),
                 ("growth_particles", C.c_uint64), ("growth_cells", C.c_uint64),
-                ("cand_wait_ms", C.c_double), ("from_list", C.c_uint64)]
+                ("cand_wait_ms", C.c_double), ("from_list", C.c_uint64),
+                ("n_witness", C.c_uint64)]
 
 
 class Timings(C.Structure):
@@ -29,7 +30,8 @@ class Timings(C.Structure):
                 ("filter_ms", C.c_double), ("filter_launches", C.c_int),
                 ("cic_ms", C.c_double), ("cic_launches", C.c_int),
                 ("mesh_ms", C.c_double), ("mesh_launches", C.c_int),
-                ("growth_particles", C.c_uint64), ("growth_cells", C.c_uint64)]
+                ("growth_particles", C.c_uint64), ("growth_cells", C.c_uint64),
+                ("witness_ms", C.c_double), ("witness_launches", C.c_int)]
 
 
 EXPORTED = [
@@ -44,7 +46,7 @@ EXPORTED = [
     # device-resident additions
     "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
     "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
-    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
+    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_set_witness", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
     "sifg_mesh_device_noalloc",
     # the FP64 form
     "sifg_cic_device_f64", "sifg_contrast_device_f64", "sifg_mesh_device_f64",
@@ -95,6 +97,7 @@ def load():
         "sifg_set_shell_list": (None, [i32]),
         "sifg_set_commit_mode": (None, [i32]),
         "sifg_set_scan_mode": (None, [i32]),
+        "sifg_set_witness": (None, [i32]),
         "sifg_stream": (u64, []),
         "sifg_launch_count": (u64, []),
         "sifg_mesh_device_noalloc": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]),

@@ -231,6 +231,8 @@ static void record_timings(RunTimings& t) {
   g_timings.mesh_launches = t.mesh.launches();
   g_timings.growth_particles = t.growth_particles;
   g_timings.growth_cells = t.growth_cells;
+  g_timings.witness_ms = t.witness.total_ms();
+  g_timings.witness_launches = t.witness.launches();
 }
 
 // The API lock, for entry points outside this file that hold it for a whole
@@ -1384,7 +1386,7 @@ uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
     out[i] = sifg_rung_stat_t{s.radius, s.r_search, s.n_candidates, s.n_survivors, s.n_accepted,
                               s.rounds, s.n_rescale_fail, s.n_overflow, s.rung_ms,
                               s.count_wait_ms, s.sort_ms, s.commit_ms, s.growth_particles,
-                              s.growth_cells, s.cand_wait_ms, s.from_list};
+                              s.growth_cells, s.cand_wait_ms, s.from_list, s.n_witness};
   }
   return n;
 }
@@ -1410,6 +1412,8 @@ void sifg_set_growth_mode(int mode) { set_growth_mode(mode < 0 || mode > 2 ? 0 :
 void sifg_set_shell_list(int entries) { set_shell_list(entries < 0 ? -1 : entries); }
 void sifg_set_commit_mode(int mode) { set_commit_mode(mode == 1 ? 1 : 0); }
 void sifg_set_scan_mode(int mode) { set_scan_mode(mode == 1 ? 1 : 0); }
+
+void sifg_set_witness(int on) { set_witness(on); }
 
 void sifg_set_window(int bins) { g_window = bins < 1 ? 1 : (bins > 64 ? 64 : bins); }
 

@@ -793,6 +793,9 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
         SIFG_CUDA(cudaStreamWaitEvent(st_, p.mesh_ready, 0));
         mesh_waited = true;
       }
+      // The collision witness against the catalogue as the rung begins
+      // (exodus_finder.c:2019-2030), then the growth of the rest.
+      witness(mv, tv, rc, sv, vv, m, traffic + 2 * ri, st_, tm ? &tm->witness : nullptr);
       grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_, tm ? &tm->growth : nullptr);
       // Each level of the extended reach, for the survivors whose crossing
       // still lies past the reach (exodus_finder.c:2060-2072).
@@ -878,6 +881,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     rs.rounds = rounds;
     rs.n_rescale_fail = h_counters_[4];
     rs.n_overflow = h_counters_[5];
+    rs.n_witness = h_counters_[8];
     if (n_acc) {
       R rmax;
       std::memcpy(&rmax, sizeof(R) == 4 ? (void*)&h_counters_[3] : (void*)&h_counters_[6], sizeof(R));

@@ -54,15 +54,17 @@ struct RungStat {
   double cand_wait_ms = 0;  // waiting for the candidates' depths before the sort
   uint64_t from_list = 0;   // 1: candidates from the smoothing's below-threshold list
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the rung's sphere growth
+  uint64_t n_witness = 0;  // survivors the collision witness refused before growth
 };
 
 struct RunTimings {
-  KernelTimer growth, filter, cic, mesh;
+  KernelTimer growth, filter, cic, mesh, witness;
   double wall_ms = 0.0;
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the sphere growth
   void reset() {
     growth_particles = growth_cells = 0;
     growth.reset();
+    witness.reset();
     filter.reset();
     cic.reset();
     mesh.reset();

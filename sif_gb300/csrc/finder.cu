@@ -830,7 +830,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
   R* my_gbuf = gbuf + (uint64_t)blockIdx.x * gcap;
 
   for (uint32_t s = blockIdx.x; s < n_surv; s += gridDim.x) {
-    if (only != kAllSurvivors && sv.reason[s] != only) continue;
+    if (only != kAllSurvivors ? sv.reason[s] != only : sv.reason[s] == kRescaleWitness) continue;
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
                   ck = (int32_t)fmul(cz, mesh.inv_l);
@@ -1096,7 +1096,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
   const uint32_t n_surv = *sv.count;
   const uint32_t warps = gridDim.x * kGrowWarps;
   for (uint32_t s = blockIdx.x * kGrowWarps + warp; s < n_surv; s += warps) {
-    if (only != kAllSurvivors && sv.reason[s] != only) continue;
+    if (only != kAllSurvivors ? sv.reason[s] != only : sv.reason[s] == kRescaleWitness) continue;
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
                   ck = (int32_t)fmul(cz, mesh.inv_l);
@@ -1277,6 +1277,182 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
     }
     __syncwarp();
   }
+}
+
+// ---------------------------------------------------------------------------
+// The collision witness
+// ---------------------------------------------------------------------------
+// One warp per survivor. First the collision radius rho: over the void-index
+// cells within scale * (r_search + largest radius) of the centre, the
+// smallest radius past which the survivor's sphere is certain to collide
+// with an accepted void, in IEEE double as collision_radius computes it
+// (exodus_finder.c:780-845; the separation padded by 1e-5 of the lengths).
+// Then, where rho < r_search, the witness (exodus_rescale.c:1074-1167): the
+// particles at or inside rho^2 (whole cells counted where their bounds clear
+// rho^2 by the 1e-5 slack, the rest by distance) must satisfy the crossing
+// test already, n^2 <= K^2 rho^6 (1 - 1e-5), with a particle beyond rho^2 in
+// the search shell: the crossing then lies past rho and the commit would
+// refuse the void. The reference walks the cells in order and stops early
+// (past n_cap inside, or skipping cells wholly beyond rho^2 once one
+// particle is); the warp counts every cell, which gives the same answer: n
+// only grows, and a cell whose bound lies beyond rho^2 by the slack holds no
+// particle at or inside it. Cells wholly beyond rho^2 are read only while no
+// non-empty shell cell beyond it has been seen.
+constexpr double kCollisionSlack = 1e-5;
+
+template <class R>
+__device__ __forceinline__ double collision_radius_warp(const VoidViewT<R>& v, R cx, R cy, R cz,
+                                                         R r_hi, R f, R scale, R box) {
+  const unsigned lane = threadIdx.x & 31u;
+  if (v.n == 0) return CUDART_INF;
+  const double L = (double)box, half = __dmul_rn(0.5, L), ff = (double)f, sc = (double)scale;
+  const R reach = fmul(scale, fadd(r_hi, v.max_r));
+  const R xs[3] = {cx, cy, cz};
+  int32_t lo[3], span[3];
+  for (int a = 0; a < 3; a++) {
+    lo[a] = (int32_t)ffloor(fmul(fsub(xs[a], reach), v.inv_cell));
+    int32_t hi = (int32_t)ffloor(fmul(fadd(xs[a], reach), v.inv_cell));
+    if (hi - lo[a] >= (int32_t)kVoidCells) {
+      lo[a] = 0;
+      hi = (int32_t)kVoidCells - 1;
+    }
+    span[a] = hi - lo[a] + 1;
+  }
+  const uint32_t cells = (uint32_t)(span[0] * span[1] * span[2]);
+  double best = CUDART_INF;
+  for (uint32_t k = lane; k < cells; k += 32) {
+    const int32_t a = lo[0] + (int32_t)(k / (uint32_t)(span[1] * span[2]));
+    const int32_t b = lo[1] + (int32_t)((k / (uint32_t)span[2]) % (uint32_t)span[1]);
+    const int32_t c = lo[2] + (int32_t)(k % (uint32_t)span[2]);
+    const int32_t n = (int32_t)kVoidCells;
+    const uint32_t cell = (uint32_t)(((((a % n) + n) % n) * n + (((b % n) + n) % n)) * n +
+                                     (((c % n) + n) % n));
+    for (uint32_t q = __ldg(v.start + cell); q < __ldg(v.start + cell + 1); q++) {
+      const uint32_t i = __ldg(v.ids + q);
+      const double rj = (double)v.r[i];
+      double dx = fabs(__dsub_rn((double)cx, (double)v.cx[i]));
+      double dy = fabs(__dsub_rn((double)cy, (double)v.cy[i]));
+      double dz = fabs(__dsub_rn((double)cz, (double)v.cz[i]));
+      dx = dx > half ? __dsub_rn(L, dx) : dx;
+      dy = dy > half ? __dsub_rn(L, dy) : dy;
+      dz = dz > half ? __dsub_rn(L, dz) : dz;
+      const double d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                            __dmul_rn(dz, dz)));
+      const double pad = __dmul_rn(kCollisionSlack, __dadd_rn(__dadd_rn(L, (double)r_hi), rj));
+      const double D = __ddiv_rn(__dadd_rn(d, pad), sc);
+      double r_star;
+      if (D <= rj)
+        r_star = 0.0;
+      else if (D <= __dmul_rn(__dsub_rn(2.0, ff), rj))
+        r_star = __ddiv_rn(__dsub_rn(D, rj), __dsub_rn(1.0, ff));
+      else
+        r_star = __dsub_rn(D, __dmul_rn(__dsub_rn(1.0, ff), rj));
+      best = r_star < best ? r_star : best;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double other = __shfl_xor_sync(0xffffffffu, best, o);
+    best = other < best ? other : best;
+  }
+  return best;
+}
+
+template <class R>
+__global__ void __launch_bounds__(kGrowT) witness_kernel(MeshViewT<R> mesh, TemplateViewT<R> tpl,
+                                                         RungConstsT<R> rc, SurvivorsT<R> sv,
+                                                         VoidViewT<R> voids,
+                                                         unsigned long long* __restrict__ traffic) {
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t n_surv = *sv.count;
+  const uint32_t warps = gridDim.x * kGrowWarps;
+  const R slack_lo = R(1.0f - 1e-5f), slack_hi = R(1.0f + 1e-5f);
+  for (uint32_t s = blockIdx.x * kGrowWarps + warp; s < n_surv; s += warps) {
+    const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
+    bool refused = false;
+    unsigned long long read = 0, visited = 0;
+    const double rho = collision_radius_warp(voids, cx, cy, cz, rc.r_search, rc.f, rc.scale, rc.box);
+    if (rho < (double)rc.r_search) {
+      R rho2 = (R)__dmul_rn(__dmul_rn(rho, rho), 1.0 + kCollisionSlack);
+      if (rho2 < rc.rc2) rho2 = rc.rc2;
+      if (rho2 < rc.rs2) {
+        const R bound = fmul(fmul(rc.K2, fmul(fmul(rho2, rho2), rho2)), slack_lo);
+        const double n_cap = __dadd_rn(__dsqrt_rn((double)bound), 2.0);
+        const R whole_in = fmul(rho2, slack_lo), whole_out = fmul(rho2, slack_hi);
+        const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
+                      ck = (int32_t)fmul(cz, mesh.inv_l);
+        // Whole cells: inside rho^2, or non-empty shell cells beyond it.
+        unsigned long long n = 0;
+        bool beyond = false;
+        for (uint32_t i = lane; i < tpl.count; i += 32) {
+          const uint8_t type = __ldg(tpl.type + i);
+          const bool in = type == kCellCore || !(__ldg(tpl.max_d2 + i) > whole_in);
+          const bool out = type == kCellShell && __ldg(tpl.min_d2 + i) > whole_out;
+          if (!in && !out) continue;
+          const CellRange<R> c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
+          visited++;
+          if (in)
+            n += c.e - c.s;
+          else if (c.e > c.s)
+            beyond = true;
+        }
+        beyond = __any_sync(0xffffffffu, beyond);
+        // The cells that need distances.
+        walk_cells(
+            mesh, tpl, ci, cj, ck, cx, cy, cz,
+            [&](uint8_t type, uint32_t i) {
+              if (type == kCellCore || !(__ldg(tpl.max_d2 + i) > whole_in)) return false;
+              const bool far = __ldg(tpl.min_d2 + i) > whole_out;
+              if (type == kCellShell && far) return false;
+              return !(beyond && far);  // such a cell can only show what is already shown
+            },
+            [](uint8_t, uint32_t) {}, [](uint8_t) { return true; },
+            [&](uint8_t type, R d2, uint32_t, uint32_t) {
+              if (!(d2 > rho2))
+                n++;
+              else if (type == kCellShell || !(d2 > rc.rs2))
+                beyond = true;
+            },
+            visited, read, true);
+        n = __reduce_add_sync(0xffffffffu, (unsigned)n);
+        beyond = __any_sync(0xffffffffu, beyond);
+        const R rn = from_u64<R>(n);
+        refused = beyond && !((double)n > n_cap) && !(fmul(rn, rn) > bound);
+      }
+    }
+    if (traffic) {
+      const unsigned long long v = __reduce_add_sync(0xffffffffu, (unsigned)visited);
+      if (lane == 0) {
+        if (read) atomicAdd(traffic, read);
+        if (v) atomicAdd(traffic + 1, v);
+      }
+    }
+    if (lane == 0) {
+      sv.reason[s] = refused ? kRescaleWitness : kRescaleOk;
+      if (refused) sv.r[s] = -1.0f;
+    }
+    __syncwarp();
+  }
+}
+
+static int g_witness = 1;
+void set_witness(int on) { g_witness = on; }
+
+template <class R>
+void witness(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
+             VoidViewT<R> voids, uint32_t max_survivors, unsigned long long* traffic,
+             cudaStream_t st, KernelTimer* timer) {
+  if (max_survivors == 0) return;
+  if (!g_witness) {
+    // Every survivor to be grown (kRescaleOk is 0).
+    SIFG_CUDA(cudaMemsetAsync(s.reason, 0, max_survivors, st));
+    return;
+  }
+  const uint32_t warps_needed = (max_survivors + kGrowWarps - 1) / kGrowWarps;
+  if (timer) timer->begin(st);
+  witness_kernel<R><<<std::min<uint32_t>(warps_needed, 152u * 8u), kGrowT, 0, st>>>(
+      mesh, tpl, rc, s, voids, traffic);
+  SIFG_LAUNCH_CHECK();
+  if (timer) timer->end(st);
 }
 
 static int g_growth_mode = 0;
@@ -1517,6 +1693,7 @@ __global__ void commit_init_kernel(SurvivorsT<R> sv, uint8_t* __restrict__ state
     state[i] = ok ? kUndecided : kRejected;
     if (!ok) atomicAdd(counters + 4, 1u);
     if (sv.reason[i] == kRescaleOverflow) atomicAdd(counters + 5, 1u);
+    if (sv.reason[i] == kRescaleWitness) atomicAdd(counters + 8, 1u);
   }
 }
 
@@ -1825,6 +2002,8 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
   template void prefilter<R>(const uint32_t*, uint32_t, const uint32_t*, VoidViewT<R>,             \
                              RungConstsT<R>, uint8_t*, uint32_t*, uint32_t*, uint32_t*, R*, R*,    \
                              R*, uint32_t*, cudaStream_t);                                         \
+  template void witness<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>,         \
+                           VoidViewT<R>, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*);\
   template void grow<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>, uint32_t,   \
                         R*, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*, uint8_t);   \
   template void build_survivor_grid<R>(const R*, const R*, const R*, const uint32_t*, uint32_t,    \

@@ -25,6 +25,7 @@ enum : uint8_t {
   kRescaleDegenerate,
   kRescaleOverflow,
   kRescalePending,  // left by the warp-per-survivor growth for the per-CTA one
+  kRescaleWitness,  // refused by the collision witness before any growth
 };
 
 // Commit states.
@@ -167,9 +168,26 @@ void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, Void
                uint32_t* surv_flat, R* scx, R* scy, R* scz, uint32_t* d_surv_count,
                cudaStream_t st);
 
+// The collision witness (collision_radius, src/finder/exodus_finder.c:
+// 780-845, and sif__exodus_witness, src/finder/exodus_rescale.c:1074-1167):
+// a survivor whose crossing is certain to lie past the radius at which it
+// collides with a void of `voids` (the catalogue as the rung begins) is
+// refused before any growth, as the reference refuses it -- the commit would
+// refuse it at any radius it could return. Writes every survivor's outcome:
+// kRescaleWitness (radius -1) or kRescaleOk (to be grown). traffic as grow's.
+template <class R>
+void witness(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
+             VoidViewT<R> voids, uint32_t max_survivors, unsigned long long* traffic,
+             cudaStream_t st, KernelTimer* timer);
+
+// 1 (default): the witness runs; 0: every survivor is grown. The catalogue
+// does not depend on it (tests run both).
+void set_witness(int on);
+
 // Sphere growth of every survivor, or (only != kAllSurvivors) of those whose
-// rescale outcome is `only`. gbuf: a global overflow scratch of grid * gcap
-// values.
+// rescale outcome is `only`; with only == kAllSurvivors, survivors the
+// witness refused are left as they are. gbuf: a global overflow scratch of
+// grid * gcap values.
 constexpr uint8_t kAllSurvivors = 0xff;
 unsigned growth_grid();
 // traffic (may be NULL): two counters the kernel adds to -- particles read
@@ -194,7 +212,8 @@ void build_survivor_grid(const R* scx, const R* scy, const R* scz, const uint32_
                          uint32_t* ids, uint32_t* cell_of, cudaStream_t st);
 
 // Survivors whose rescaling failed start rejected, the rest undecided;
-// counters[4] counts the failures, counters[5] the resolve overflows.
+// counters[4] counts the failures, counters[5] the resolve overflows,
+// counters[8] the witness's refusals (among the failures).
 template <class R>
 void commit_init(SurvivorsT<R> s, uint8_t* state, uint32_t* counters, uint32_t max_survivors,
                  cudaStream_t st);

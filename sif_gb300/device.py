@@ -198,6 +198,12 @@ def set_scan_mode(mode):
     _lib.load().sifg_set_scan_mode(int(mode))
 
 
+def set_witness(on):
+    """1 the collision witness refuses doomed survivors before growth, 0 every
+    survivor is grown; the catalogue is the same."""
+    _lib.load().sifg_set_witness(int(on))
+
+
 def set_window(bins):
     _lib.load().sifg_set_window(int(bins))
 

@@ -318,6 +318,26 @@ def test_catalogue_matches_reference_golden_any_shell_list(dev, golden_box32, sh
     test_catalogue_matches_reference_golden(dev, golden_box32, name)
 
 
+@pytest.mark.parametrize("name", ["default", "search_2_00", "lagrangian", "minima", "overlap_0_5"])
+def test_catalogue_matches_reference_golden_without_the_witness(dev, golden_box32, name):
+    """The collision witness only refuses survivors the commit would refuse:
+    switched off, the reference's catalogue all the same."""
+    dev.set_witness(0)
+    try:
+        test_catalogue_matches_reference_golden(dev, golden_box32, name)
+    finally:
+        dev.set_witness(1)
+
+
+@pytest.mark.parametrize("name", EXTEND_SETS)
+def test_extended_reach_golden_without_the_witness(dev, golden_box32_extend, name):
+    dev.set_witness(0)
+    try:
+        test_catalogue_matches_reference_golden(dev, golden_box32_extend, name)
+    finally:
+        dev.set_witness(1)
+
+
 @pytest.fixture(params=[0, 1], ids=["one_launch", "launch_per_round"])
 def commit_mode(request, dev):
     """The commit's rounds in one cooperative launch, then a launch per round."""
