@@ -307,6 +307,7 @@ typedef struct {
   double cand_wait_ms;
   uint64_t from_list;      /* 1: the candidates came from the smoothing's below-threshold list */
   uint64_t n_witness;      /* survivors the collision witness refused before any growth */
+  uint64_t n_displaced;    /* voids the rung's acceptances displaced (SIF_FINDER_DISPLACE) */
 } sifg_rung_stat_t;
 
 /* Kernel timings of the last run, CUDA events on the launching stream. */
@@ -471,6 +472,11 @@ void sifg_set_commit_mode(int mode);
  * it goes, where it can (the float form at a 512^3 grid), less the masked
  * cells; 1 a scan of the whole field. The catalogue does not depend on it. */
 void sifg_set_scan_mode(int mode);
+/* The float form's own inverse transform at a 512^3 grid: 1 (default) the
+ * filter pass reads each smoothing's filter factors from a table built on its
+ * first use (257^3 floats, 68 MB, up to 24 kept); 0 it evaluates them as it
+ * applies them. The smoothed fields are the same bits either way. */
+void sifg_set_factor_tables(int on);
 /* The collision witness (exodus_finder.c:780-845, exodus_rescale.c:
  * 1074-1167): 1 (default) survivors whose sphere is certain to collide with
  * a void of an earlier rung at any radius they could return are refused

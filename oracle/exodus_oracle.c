@@ -1362,6 +1362,140 @@ static void voids_add(voids_t* v, float cx, float cy, float cz, float r) {
   v->head[cell] = (int32_t)i;
 }
 
+static void paint_sphere(uint64_t* mask, float cx, float cy, float cz, float r,
+  uint32_t n, float cell_length, int set);
+
+static uint64_t void_cell(const voids_t* v, float cx, float cy, float cz) {
+  return ((uint64_t)void_axis(v, cx) * VOID_CELLS + void_axis(v, cy)) * VOID_CELLS +
+         void_axis(v, cz);
+}
+
+/* sif_cell_linked_list_remove, src/structures/cell_linked_list.c:212-232. */
+static void voids_unlink(voids_t* v, uint64_t i) {
+  int32_t* link = &v->head[void_cell(v, v->cx[i], v->cy[i], v->cz[i])];
+  while (*link != -1 && *link != (int32_t)i)
+    link = &v->next[*link];
+  if (*link != -1)
+    *link = v->next[i];
+}
+
+/* compact_catalogue, src/finder/exodus_finder.c:1043-1078: the displaced
+ * voids (radius negated) dropped, the rest re-indexed in order. */
+static void voids_compact(voids_t* v) {
+  uint64_t j = 0;
+  for (uint64_t i = 0; i < v->n; i++) {
+    if (!(v->r[i] > 0.0f))
+      continue;
+    v->cx[j] = v->cx[i];
+    v->cy[j] = v->cy[i];
+    v->cz[j] = v->cz[i];
+    v->r[j] = v->r[i];
+    j++;
+  }
+  memset(v->head, 0xFF, sizeof(v->head));
+  v->n = 0;
+  for (uint64_t i = 0; i < j; i++) {
+    const uint64_t cell = void_cell(v, v->cx[i], v->cy[i], v->cz[i]);
+    v->next[i] = v->head[cell];
+    v->head[cell] = (int32_t)i;
+  }
+  v->n = j;
+}
+
+/* find_conflicts, src/finder/exodus_finder.c:696-756: the accepted voids a
+ * sphere at r collides with (the exact overlap's pair test, minimum image),
+ * in the order the index walks them; returns their count, the largest
+ * radius among them in *largest (-1 for none). */
+static uint64_t find_conflicts(const voids_t* v, float max_r, float scale, float cx, float cy,
+  float cz, float r, float f, float box, uint64_t** list, uint64_t* cap, float* largest) {
+  const float half = 0.5f * box;
+  const float reach = scale * (r + max_r - f * (r < max_r ? r : max_r));
+  const float x[3] = {cx, cy, cz};
+  int32_t lo[3], hi[3];
+  for (int a = 0; a < 3; a++) {
+    lo[a] = (int32_t)floorf((x[a] - reach) * v->inv_cell);
+    hi[a] = (int32_t)floorf((x[a] + reach) * v->inv_cell);
+    if (hi[a] - lo[a] >= VOID_CELLS) {
+      lo[a] = 0;
+      hi[a] = VOID_CELLS - 1;
+    }
+  }
+  uint64_t k = 0;
+  *largest = -1.0f;
+  for (int32_t a = lo[0]; a <= hi[0]; a++) {
+    const int32_t wa = ((a % VOID_CELLS) + VOID_CELLS) % VOID_CELLS;
+    for (int32_t b = lo[1]; b <= hi[1]; b++) {
+      const int32_t wb = ((b % VOID_CELLS) + VOID_CELLS) % VOID_CELLS;
+      for (int32_t c = lo[2]; c <= hi[2]; c++) {
+        const int32_t wc = ((c % VOID_CELLS) + VOID_CELLS) % VOID_CELLS;
+        for (int32_t i = v->head[(wa * VOID_CELLS + wb) * VOID_CELLS + wc]; i != -1;
+             i = v->next[i]) {
+          float dx = fabsf(cx - v->cx[i]);
+          float dy = fabsf(cy - v->cy[i]);
+          float dz = fabsf(cz - v->cz[i]);
+          dx = dx > half ? box - dx : dx;
+          dy = dy > half ? box - dy : dy;
+          dz = dz > half ? box - dz : dz;
+          const float ri = v->r[i];
+          const float tot = scale * (r + ri - f * (r < ri ? r : ri));
+          if (dx * dx + dy * dy + dz * dz >= tot * tot)
+            continue;
+          if (k == *cap) {
+            *cap = *cap ? 2 * *cap : 64;
+            *list = realloc(*list, *cap * sizeof(uint64_t));
+          }
+          (*list)[k++] = (uint64_t)i;
+          if (ri > *largest)
+            *largest = ri;
+        }
+      }
+    }
+  }
+  return k;
+}
+
+/* displace_void, src/finder/exodus_finder.c:946-1037: void i leaves the
+ * index, its radius is negated, its sphere cleared from the mask, and the
+ * spheres of the voids still indexed that intersect it painted back. */
+static void displace_void(voids_t* v, uint64_t* mask, uint64_t i, float max_r, float scale,
+  uint32_t n, float cell, float box) {
+  const float cx = v->cx[i], cy = v->cy[i], cz = v->cz[i], r = v->r[i];
+  voids_unlink(v, i);
+  v->r[i] = -r;
+  paint_sphere(mask, cx, cy, cz, scale * r, n, cell, 0);
+  const float half = 0.5f * box;
+  const float reach = scale * (r + max_r);
+  const float x[3] = {cx, cy, cz};
+  int32_t lo[3], hi[3];
+  for (int a = 0; a < 3; a++) {
+    lo[a] = (int32_t)floorf((x[a] - reach) * v->inv_cell);
+    hi[a] = (int32_t)floorf((x[a] + reach) * v->inv_cell);
+    if (hi[a] - lo[a] >= VOID_CELLS) {
+      lo[a] = 0;
+      hi[a] = VOID_CELLS - 1;
+    }
+  }
+  for (int32_t a = lo[0]; a <= hi[0]; a++)
+    for (int32_t b = lo[1]; b <= hi[1]; b++)
+      for (int32_t c = lo[2]; c <= hi[2]; c++) {
+        const int32_t wa = ((a % VOID_CELLS) + VOID_CELLS) % VOID_CELLS;
+        const int32_t wb = ((b % VOID_CELLS) + VOID_CELLS) % VOID_CELLS;
+        const int32_t wc = ((c % VOID_CELLS) + VOID_CELLS) % VOID_CELLS;
+        for (int32_t j = v->head[(wa * VOID_CELLS + wb) * VOID_CELLS + wc]; j != -1;
+             j = v->next[j]) {
+          float dx = fabsf(cx - v->cx[j]);
+          float dy = fabsf(cy - v->cy[j]);
+          float dz = fabsf(cz - v->cz[j]);
+          dx = dx > half ? box - dx : dx;
+          dy = dy > half ? box - dy : dy;
+          dz = dz > half ? box - dz : dz;
+          const float t = scale * (r + v->r[j]);
+          if (dx * dx + dy * dy + dz * dz < t * t)
+            paint_sphere(mask, v->cx[j], v->cy[j], v->cz[j], scale * v->r[j], n, cell, 1);
+        }
+      }
+}
+
 static void voids_free(voids_t* v) {
   free(v->cx);
   free(v->cy);
@@ -1428,8 +1562,19 @@ static int overlap_exact(const voids_t* v, float cx, float cy, float cz,
 }
 
 /* paint_sphere with set = 1, src/finder/utils.c:965-1027. */
+static inline void mask_clear(uint64_t* words, uint64_t i) {
+  words[i >> 6] &= ~(1ull << (i & 63));
+}
+
 static void mark_sphere(uint64_t* mask, float cx, float cy, float cz, float r,
   uint32_t n, float cell_length) {
+  paint_sphere(mask, cx, cy, cz, r, n, cell_length, 1);
+}
+
+/* paint_sphere, src/finder/utils.c:965-1027: set (sif__mark_sphere) or
+ * clear (sif__clear_sphere) every node within r. */
+static void paint_sphere(uint64_t* mask, float cx, float cy, float cz, float r,
+  uint32_t n, float cell_length, int set) {
   const float r2 = r * r;
   const float inv = 1.0f / cell_length;
   const float box = (float)n * cell_length;
@@ -1457,14 +1602,20 @@ static void mark_sphere(uint64_t* mask, float cx, float cy, float cz, float r,
         const int32_t gz = ck + dz;
         float ddz = fabsf((float)gz * cell_length - cz);
         ddz = ddz > half ? box - ddz : ddz;
-        if (dxy2 + ddz * ddz <= r2)
-          mask_set(mask, ((uint64_t)wx * n + wy) * n + wrap_pbc(gz, n));
+        if (dxy2 + ddz * ddz <= r2) {
+          const uint64_t cell = ((uint64_t)wx * n + wy) * n + wrap_pbc(gz, n);
+          if (set)
+            mask_set(mask, cell);
+          else
+            mask_clear(mask, cell);
+        }
       }
     }
   }
 }
 
-/* collision_radius, src/finder/exodus_finder.c:780-845 (no displacement). */
+/* collision_radius, src/finder/exodus_finder.c:780-845: voids smaller than
+ * min_rj left out (under displacement only a larger void refuses). */
 #define COLLISION_SLACK 1e-5
 static double collision_radius(const voids_t* v, float max_acc, float scale_f,
   float cx, float cy, float cz, float r_hi, float min_rj, float f, float box) {
@@ -1522,7 +1673,7 @@ static double collision_radius(const voids_t* v, float max_acc, float scale_f,
 #define WITNESS_SLACK 1e-5f
 static int witness(const orc_mesh_t* m, const orc_template_t* t, float cx,
   float cy, float cz, float rho2, float r_search, float threshold,
-  float vol_factor) {
+  float vol_factor, int closed) {
   const float inv_l = 1.0f / m->cell_length;
   const query_t q = {m, t, cx, cy, cz, (int32_t)(cx * inv_l),
     (int32_t)(cy * inv_l), (int32_t)(cz * inv_l)};
@@ -1535,11 +1686,11 @@ static int witness(const orc_mesh_t* m, const orc_template_t* t, float cx,
   const double n_cap = sqrt((double)bound) + 2.0;
   const float whole_in = rho2 * (1.0f - WITNESS_SLACK);
   const float whole_out = rho2 * (1.0f + WITNESS_SLACK);
-  uint64_t n = 0;
+  uint64_t n = 0, within = 0;
   int beyond = 0;
   for (uint32_t i = 0; i < t->count; i++) {
     const uint8_t type = t->type[i];
-    if (beyond && t->min_d2[i] > whole_out)
+    if (!closed && beyond && t->min_d2[i] > whole_out)
       continue;
     uint64_t s, e;
     float ex, ey, ez;
@@ -1547,15 +1698,20 @@ static int witness(const orc_mesh_t* m, const orc_template_t* t, float cx,
       continue;
     if (type == CELL_CORE || t->max_d2[i] <= whole_in) {
       n += e - s;
+      within += e - s;
     } else if (type == CELL_SHELL && t->min_d2[i] > whole_out) {
+      within += e - s;
       beyond = 1;
     } else {
       for (uint64_t p = s; p < e; p++) {
         const float d2 = dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez);
-        if (d2 <= rho2)
+        if (d2 <= rho2) {
           n++;
-        else if (type == CELL_SHELL || d2 <= rs2)
+          within++;
+        } else if (type == CELL_SHELL || d2 <= rs2) {
+          within++;
           beyond = 1;
+        }
       }
     }
     if ((double)n > n_cap)
@@ -1564,6 +1720,14 @@ static int witness(const orc_mesh_t* m, const orc_template_t* t, float cx,
   const float rn = (float)n;
   if (!beyond || !(rn * rn <= bound))
     return 0;
+  if (closed) {
+    /* The search sphere must not be underdense out to r_search (the
+     * rescaling's refusal is within / expected - 1 <= threshold). */
+    const double expected = (double)vol_factor * (double)r_search * (double)r_search *
+                            (double)r_search;
+    if (!((double)within > (1.0 + (double)threshold) * expected * (1.0 + WITNESS_SLACK)))
+      return 0;
+  }
   return 1;
 }
 
@@ -1637,8 +1801,15 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   if (!(threshold > -1.0f && threshold < 0.0f) || !(f >= 0.0f && f <= 1.0f) ||
       n_radii == 0 || mesh->box_length != box)
     return -2;
-  if (opt & ((3u << 19) | (1u << 22)))
-    return -5; /* refinement, displacement */
+  if (opt & (3u << 19))
+    return -5; /* centre refinement */
+  /* SIF_FINDER_DISPLACE (exodus_finder.c:696-756, 946-1078, 2239-2275): a
+   * void is refused only by a larger one and displaces the smaller ones it
+   * collides with. The reference's catalogue does not depend on where its
+   * batches fall (a displacement ends one), so it is restated here as the
+   * sequential pass that defines it: each candidate in order against the
+   * catalogue as it then stands. */
+  const int displace = (opt & (1u << 22)) != 0;
   /* SIF_FINDER_EXTEND_REACH (exodus_finder.c:1664-1702, 2060-2072): a
    * crossing past the rung's reach is measured again at the levels of an
    * extended reach, from the first level EXT_SLACK past the rung's own. */
@@ -1714,6 +1885,8 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   }
   orc_candidate_t* cand = NULL;
   uint64_t cand_cap = 0;
+  uint64_t* conflicts = NULL;
+  uint64_t conf_cap = 0;
   result_t* res = malloc(2 * BATCH_MAX * sizeof(result_t));
   uint64_t* bidx = malloc(2 * BATCH_MAX * sizeof(uint64_t));
   int status = 0;
@@ -1786,8 +1959,10 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
       ext0 = n_ext - 1;
 
     /* prefilter_cells, src/finder/exodus_finder.c:871-944: 16 chunks a
-     * thread, each compacted by one thread, then closed up in order. */
-    if (nc > 0) {
+     * thread, each compacted by one thread, then closed up in order. Not
+     * under displacement: a void refusing a candidate now may be gone by its
+     * turn (exodus_finder.c:1873-1875). */
+    if (nc > 0 && !displace) {
       uint64_t n_chunks = 16u * (uint64_t)n_threads;
       if (n_chunks > nc)
         n_chunks = nc;
@@ -1831,6 +2006,79 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
       st.rejected_masked += n_masked;
       st.rejected_proxy += n_proxy;
       st.rejected_overlap += n_overlap;
+    }
+
+    if (displace) {
+      /* The witness under displacement: only a void larger than anything the
+       * search sphere can return refuses (min_rj), and with an extended reach
+       * the sphere must be closed (exodus_finder.c:1868-1871, 2019-2030). */
+      const float witness_min_rj = r_search * (1.0f + (float)COLLISION_SLACK);
+      uint64_t removed = 0;
+      for (uint64_t k = 0; k < nc && status == 0; k++) {
+        const uint64_t flat = cand[k].flat;
+        if (mask_get(mask, flat)) {
+          st.rejected_masked++;
+          continue;
+        }
+        const uint32_t ix = (uint32_t)(flat / ((uint64_t)N * N)),
+                       iy = (uint32_t)((flat / N) % N), iz = (uint32_t)(flat % N);
+        if (proxy_pole > 0 && overlap_quick(mask, N, ix, iy, iz, (uint32_t)proxy_pole)) {
+          st.rejected_proxy++;
+          continue;
+        }
+        const float cx = (float)ix * cell, cy = (float)iy * cell, cz = (float)iz * cell;
+        if (overlap_exact(&V, cx, cy, cz, radius, max_acc, box, f, scale)) {
+          st.rejected_overlap++;
+          continue;
+        }
+        const double rho =
+          collision_radius(&V, max_acc, scale, cx, cy, cz, r_search, witness_min_rj, f, box);
+        if (rho < (double)r_search) {
+          float rho2 = (float)(rho * rho * (1.0 + COLLISION_SLACK));
+          if (rho2 < rc2)
+            rho2 = rc2;
+          if (witness(mesh, &tpl, cx, cy, cz, rho2, r_search, threshold, vol_factor,
+                extend_reach)) {
+            st.rejected_witness++;
+            continue;
+          }
+        }
+        uint8_t reason;
+        uint64_t ss = 0, sc = 0;
+        float rr = orc_find_radius(mesh, &tpl, cx, cy, cz, r_search, threshold, vol_factor, rmin,
+          p->window > 0 ? (uint32_t)p->window : RESOLVE_INITIAL, &reason, &ss, &sc);
+        for (uint32_t e = ext0; e < n_ext && rr < 0.0f && reason == ORC_RESCALE_BEYOND_SEARCH;
+             e++)
+          rr = orc_find_radius(mesh, &etpl[e], cx, cy, cz, ext_reach[e], threshold, vol_factor,
+            ext_rmin[e], p->window > 0 ? (uint32_t)p->window : RESOLVE_INITIAL, &reason, &ss, &sc);
+        st.n_rescaled++;
+        if (rr < 0.0f) {
+          st.rejected_rescale++;
+          continue;
+        }
+        float largest;
+        const uint64_t nconf =
+          find_conflicts(&V, max_acc, scale, cx, cy, cz, rr, f, box, &conflicts, &conf_cap,
+            &largest);
+        if (largest >= rr) {
+          st.rejected_exact++;
+          continue;
+        }
+        for (uint64_t j = 0; j < nconf; j++)
+          displace_void(&V, mask, conflicts[j], max_acc, scale, N, cell, box);
+        removed += nconf;
+        voids_add(&V, cx, cy, cz, rr);
+        mark_sphere(mask, cx, cy, cz, scale * rr, N, cell);
+        if (rr > max_acc)
+          max_acc = rr;
+        st.accepted++;
+      }
+      if (removed)
+        voids_compact(&V);
+      orc_template_free(&tpl);
+      if (stats_out)
+        stats_out[ri] = st;
+      continue;
     }
 
     uint64_t floor_ = (uint64_t)BATCH_PER_THREAD * (uint64_t)n_threads;
@@ -1883,7 +2131,7 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
           if (rho2 < rc2)
             rho2 = rc2;
           if (witness(mesh, &tpl, r->cx, r->cy, r->cz, rho2, r_search, threshold,
-                vol_factor)) {
+                vol_factor, 0)) {
             r->status = ST_WITNESS;
             continue;
           }
@@ -1982,6 +2230,7 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   free(bidx);
   free(res);
   free(cand);
+  free(conflicts);
   free(field);
   free(mask);
   free(radii);

@@ -22,7 +22,7 @@ class RungStat(C.Structure):
                 ("sort_ms", C.c_double), ("commit_ms", C.c_double),
                 ("growth_particles", C.c_uint64), ("growth_cells", C.c_uint64),
                 ("cand_wait_ms", C.c_double), ("from_list", C.c_uint64),
-                ("n_witness", C.c_uint64)]
+                ("n_witness", C.c_uint64), ("n_displaced", C.c_uint64)]
 
 
 class Timings(C.Structure):
@@ -46,7 +46,7 @@ EXPORTED = [
     # device-resident additions
     "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
     "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
-    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_set_witness", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
+    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_set_witness", "sifg_set_factor_tables", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
     "sifg_mesh_device_noalloc",
     # the FP64 form
     "sifg_cic_device_f64", "sifg_contrast_device_f64", "sifg_mesh_device_f64",
@@ -98,6 +98,7 @@ def load():
         "sifg_set_commit_mode": (None, [i32]),
         "sifg_set_scan_mode": (None, [i32]),
         "sifg_set_witness": (None, [i32]),
+        "sifg_set_factor_tables": (None, [i32]),
         "sifg_stream": (u64, []),
         "sifg_launch_count": (u64, []),
         "sifg_mesh_device_noalloc": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]),

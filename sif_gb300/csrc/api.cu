@@ -1386,7 +1386,8 @@ uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
     out[i] = sifg_rung_stat_t{s.radius, s.r_search, s.n_candidates, s.n_survivors, s.n_accepted,
                               s.rounds, s.n_rescale_fail, s.n_overflow, s.rung_ms,
                               s.count_wait_ms, s.sort_ms, s.commit_ms, s.growth_particles,
-                              s.growth_cells, s.cand_wait_ms, s.from_list, s.n_witness};
+                              s.growth_cells, s.cand_wait_ms, s.from_list, s.n_witness,
+                              s.n_displaced};
   }
   return n;
 }
@@ -1414,6 +1415,8 @@ void sifg_set_commit_mode(int mode) { set_commit_mode(mode == 1 ? 1 : 0); }
 void sifg_set_scan_mode(int mode) { set_scan_mode(mode == 1 ? 1 : 0); }
 
 void sifg_set_witness(int on) { set_witness(on); }
+
+void sifg_set_factor_tables(int on) { set_factor_tables(on); }
 
 void sifg_set_window(int bins) { g_window = bins < 1 ? 1 : (bins > 64 ? 64 : bins); }
 

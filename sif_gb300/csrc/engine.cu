@@ -443,11 +443,14 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const R cell = box / (R)N;
   const R threshold = p.threshold, f = p.overlap;
   const uint32_t opt = p.options;
-  if (opt & (kOptRefineMask | kOptDisplace)) {
-    set_error(kErrUnsupported,
-              "options: centre refinement and displacement are not supported by the GPU finder");
+  if (opt & kOptRefineMask) {
+    set_error(kErrUnsupported, "options: centre refinement is not supported by the GPU finder");
     return kErrUnsupported;
   }
+  // SIF_FINDER_DISPLACE: no pre-filter, no witness against the rung's
+  // starting catalogue (voids can leave it), and the commit one survivor at a
+  // time in rank order (displace_commit).
+  const bool displace = (opt & kOptDisplace) != 0;
   const bool extend = (opt & kOptExtendReach) != 0;
   if (cells >= (1ull << 32)) {
     set_error(kErrRange, "grid: more than 2^32 cells");
@@ -779,7 +782,8 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     R* sr = grow_to<R>(sr_, m);
     uint8_t* sreason = grow_to<uint8_t>(sreason_, m);
     uint32_t* blocks2 = grow_to<uint32_t>(rank_slots_, (size_t)m + 2048);
-    prefilter(cflat, m, mask, vv, rc, alive, blocks2, scand, sflat, scx, scy, scz, dcount + 1, st_);
+    prefilter(cflat, m, mask, vv, rc, alive, blocks2, scand, sflat, scx, scy, scz, dcount + 1, st_,
+              displace);
     SurvivorsT<R> sv{scand, sflat, scx, scy, scz, sr, sreason, dcount + 1};
 
     // 4. Sphere growth of every survivor.
@@ -794,8 +798,13 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
         mesh_waited = true;
       }
       // The collision witness against the catalogue as the rung begins
-      // (exodus_finder.c:2019-2030), then the growth of the rest.
-      witness(mv, tv, rc, sv, vv, m, traffic + 2 * ri, st_, tm ? &tm->witness : nullptr);
+      // (exodus_finder.c:2019-2030), then the growth of the rest. Under
+      // displacement every survivor is grown: a void refusing it now may be
+      // displaced before its turn.
+      if (displace)
+        SIFG_CUDA(cudaMemsetAsync(sreason, kRescaleOk, m, st_));
+      else
+        witness(mv, tv, rc, sv, vv, m, traffic + 2 * ri, st_, tm ? &tm->witness : nullptr);
       grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_, tm ? &tm->growth : nullptr);
       // Each level of the extended reach, for the survivors whose crossing
       // still lies past the reach (exodus_finder.c:2060-2072).
@@ -814,8 +823,50 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     uint32_t* rank = grow_to<uint32_t>(rank_, m);
     SIFG_CUDA(cudaMemcpyAsync(rank, h_rank_, m * sizeof(uint32_t), cudaMemcpyHostToDevice, st_));
 
-    // 6. The commit, in rounds.
+    // 6. The commit, in rounds; under displacement one survivor at a time.
     const auto t_commit = clk::now();
+    if (displace) {
+      ensure_cat(n_voids + m);
+      // The compressed index again: growing the catalogue may have moved its
+      // buffers. The chains are built from it.
+      build_void_index(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), n_voids, box, vstart,
+                       vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
+      uint32_t* order = grow_to<uint32_t>(acc_, m);
+      int32_t* head = grow_to<int32_t>(vhead_, kVoidCells * kVoidCells * kVoidCells);
+      int32_t* next = grow_to<int32_t>(vnext_, (size_t)n_voids + m + 1);
+      const uint32_t cap = n_voids + m + 1;
+      uint32_t* conflicts = grow_to<uint32_t>(dlist_, 2 * (size_t)cap);
+      uint32_t hstate[8] = {n_voids, 0, 0, 0, 0, 0, 0, 0};
+      std::memcpy(&hstate[4], &max_r, sizeof(R));
+      uint32_t* dstate = counters;
+      SIFG_CUDA(cudaMemcpyAsync(dstate, hstate, sizeof hstate, cudaMemcpyHostToDevice, st_));
+      displace_commit(sv, rank, m, order, vstart, vids_.as<uint32_t>(), head, next, cat_x_.as<R>(),
+                      cat_y_.as<R>(), cat_z_.as<R>(), cat_r_.as<R>(), box, mask, rc, dstate,
+                      conflicts, conflicts + cap, cap, st_);
+      SIFG_CUDA(cudaMemcpyAsync(h_counters_, dstate, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
+      SIFG_CUDA(cudaStreamSynchronize(st_));
+      if (h_counters_[3]) {
+        set_error(kErrInvalid, "displacement: a conflict list outgrew its scratch");
+        return kErrInvalid;
+      }
+      const uint32_t n_acc = h_counters_[1], n_removed = h_counters_[2];
+      std::memcpy(&max_r, &h_counters_[4], sizeof(R));
+      if (n_removed) {
+        compact_voids(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), cat_r_.as<R>(), dstate, st_);
+        SIFG_CUDA(cudaMemcpyAsync(h_counters_, dstate, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
+        SIFG_CUDA(cudaStreamSynchronize(st_));
+      }
+      n_voids = h_counters_[0];
+      build_void_index(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), n_voids, box, vstart,
+                       vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
+      rs.commit_ms = ms_since(t_commit);
+      rs.n_survivors = m;
+      rs.n_accepted = n_acc;
+      rs.n_displaced = n_removed;
+      rs.rung_ms = ms_since(t_rung);
+      if (stats) stats->push_back(rs);
+      continue;
+    }
     // Radii reach the top level's reach where the rung enters the extended one.
     const R r_max = ext0 < n_ext ? std::max(r_search, ext_reach[n_ext - 1]) : r_search;
     const R reach = 2.0f * scale * r_max + 2.0f * cell;

@@ -55,6 +55,7 @@ struct RungStat {
   uint64_t from_list = 0;   // 1: candidates from the smoothing's below-threshold list
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the rung's sphere growth
   uint64_t n_witness = 0;  // survivors the collision witness refused before growth
+  uint64_t n_displaced = 0;  // voids displaced by the rung's acceptances (SIF_FINDER_DISPLACE)
 };
 
 struct RunTimings {
@@ -118,6 +119,7 @@ class Engine {
   DevBuf commit_bar_;  // the cooperative commit's grid barrier and its report
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
+  DevBuf vhead_, vnext_, dlist_;  // displacement: the linked void index, its lists
   DevBuf tpl_, gbuf_, traffic_, region_delta_, region_flat_;
   static constexpr uint32_t kExtMaxLevels = 32;  // EXT_MAX_LEVELS, exodus_finder.c:244
   DevBuf ext_tpl_[kExtMaxLevels];  // the extended reach's templates, one per level

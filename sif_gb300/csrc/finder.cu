@@ -450,12 +450,15 @@ __device__ bool overlap_exact(const VoidViewT<R>& v, R cx, R cy, R cz, R r, R f,
 template <class R>
 __global__ void prefilter_kernel(const uint32_t* __restrict__ cflat, uint32_t m,
                                  const uint32_t* __restrict__ mask, VoidViewT<R> voids, RungConstsT<R> rc,
-                                 uint8_t* __restrict__ alive) {
+                                 uint8_t* __restrict__ alive, bool keep_all) {
   const uint32_t n = rc.grid_n;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
     const uint32_t flat = cflat[k];
     uint8_t ok = 1;
-    if (mask_get_rw(mask, flat)) {
+    if (keep_all) {
+      // Under displacement a void refusing a candidate now may be gone by
+      // its turn (exodus_finder.c:1873-1875): nothing is refused here.
+    } else if (mask_get_rw(mask, flat)) {
       ok = 0;
     } else {
       const uint32_t ix = flat / (n * n), iy = (flat / n) % n, iz = flat % n;
@@ -537,12 +540,12 @@ template <class R>
 void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, VoidViewT<R> voids,
                RungConstsT<R> rc, uint8_t* alive, uint32_t* block_counts, uint32_t* surv_cand,
                uint32_t* surv_flat, R* scx, R* scy, R* scz, uint32_t* d_surv_count,
-               cudaStream_t st) {
+               cudaStream_t st, bool keep_all) {
   if (m == 0) {
     SIFG_CUDA(cudaMemsetAsync(d_surv_count, 0, sizeof(uint32_t), st));
     return;
   }
-  prefilter_kernel<<<grid_for(m, 128), 128, 0, st>>>(cand_flat, m, mask, voids, rc, alive);
+  prefilter_kernel<<<grid_for(m, 128), 128, 0, st>>>(cand_flat, m, mask, voids, rc, alive, keep_all);
   SIFG_LAUNCH_CHECK();
   const uint32_t nb = (m + kCompactChunk - 1) / kCompactChunk;
   flag_count_kernel<<<nb, kCompactT, 0, st>>>(alive, m, block_counts);
@@ -1988,6 +1991,382 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
 }
 
 // ---------------------------------------------------------------------------
+// Displacement (SIF_FINDER_DISPLACE)
+// ---------------------------------------------------------------------------
+// Under displacement a void is refused only by a larger one, and displaces
+// the smaller ones it collides with (find_conflicts, displace_void,
+// exodus_finder.c:696-756, 946-1037, and the commit at 2239-2275). Voids
+// leave the catalogue, so a test that fails now may pass later and the
+// rounds above do not apply: one CTA takes the survivors in rank order and
+// does what the reference's sequential pass does, against a linked void index
+// like the reference's (each cell's chain in descending void index: the
+// order its head insertions and compaction leave, which fixes the order the
+// conflicts are displaced in and the spheres painted back). Thread 0 walks
+// the index; the CTA paints.
+
+// The void index as linked chains: head per cell of the 32^3 index, next per
+// void, -1 ends a chain.
+template <class R>
+struct VoidListT {
+  R* cx;
+  R* cy;
+  R* cz;
+  R* r;  // negated once displaced (the index no longer holds it)
+  int32_t* head;
+  int32_t* next;
+  R inv_cell;
+};
+
+// The chains from the compressed index (ids of a cell in any order): each
+// cell's ids sorted descending and linked. A thread per cell.
+__global__ void void_chains_kernel(const uint32_t* __restrict__ start, uint32_t* ids,
+                                   int32_t* __restrict__ head, int32_t* __restrict__ next) {
+  constexpr uint32_t cells = kVoidCells * kVoidCells * kVoidCells;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += gridDim.x * blockDim.x) {
+    const uint32_t s = start[c], e = start[c + 1];
+    for (uint32_t a = s + 1; a < e; a++) {
+      const uint32_t v = ids[a];
+      uint32_t b = a;
+      while (b > s && ids[b - 1] < v) {
+        ids[b] = ids[b - 1];
+        b--;
+      }
+      ids[b] = v;
+    }
+    head[c] = s < e ? (int32_t)ids[s] : -1;
+    for (uint32_t a = s; a < e; a++) next[ids[a]] = a + 1 < e ? (int32_t)ids[a + 1] : -1;
+  }
+}
+
+template <class R>
+__device__ __forceinline__ uint32_t void_cell_of(R cx, R cy, R cz, R inv) {
+  return (void_axis(cx, inv) * kVoidCells + void_axis(cy, inv)) * kVoidCells + void_axis(cz, inv);
+}
+
+// The cell window of a search of `reach` about c (the reference's
+// floor((x -+ reach) / cell), the whole index when it is as wide).
+template <class R>
+__device__ __forceinline__ void void_window(R cx, R cy, R cz, R reach, R inv, int32_t* lo,
+                                            int32_t* hi) {
+  const R xs[3] = {cx, cy, cz};
+  for (int a = 0; a < 3; a++) {
+    lo[a] = (int32_t)ffloor(fmul(fsub(xs[a], reach), inv));
+    hi[a] = (int32_t)ffloor(fmul(fadd(xs[a], reach), inv));
+    if (hi[a] - lo[a] >= (int32_t)kVoidCells) {
+      lo[a] = 0;
+      hi[a] = (int32_t)kVoidCells - 1;
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t wrap_void(int32_t a) {
+  const int32_t n = (int32_t)kVoidCells;
+  return (uint32_t)(((a % n) + n) % n);
+}
+
+// sif__overlap_exact (src/finder/utils.c:850-960) over the chains.
+template <class R>
+__device__ bool overlap_exact_chains(const VoidListT<R>& v, R max_r, R cx, R cy, R cz, R r, R f,
+                                     R scale, R box) {
+  const R half = fmul(box, R(0.5f));
+  const R s = search_radius(r, max_r, f, scale);
+  const int32_t x0 = (int32_t)ffloor(fmul(fsub(cx, s), v.inv_cell));
+  const int32_t x1 = (int32_t)ffloor(fmul(fadd(cx, s), v.inv_cell));
+  const int32_t y0 = (int32_t)ffloor(fmul(fsub(cy, s), v.inv_cell));
+  const int32_t y1 = (int32_t)ffloor(fmul(fadd(cy, s), v.inv_cell));
+  const int32_t z0 = (int32_t)ffloor(fmul(fsub(cz, s), v.inv_cell));
+  const int32_t z1 = (int32_t)ffloor(fmul(fadd(cz, s), v.inv_cell));
+  const bool interior = is_interior(cx, cy, cz, s, box);
+  for (int32_t ix = x0; ix <= x1; ix++)
+    for (int32_t iy = y0; iy <= y1; iy++)
+      for (int32_t iz = z0; iz <= z1; iz++) {
+        const uint32_t c = (((uint32_t)ix & (kVoidCells - 1)) * kVoidCells +
+                            ((uint32_t)iy & (kVoidCells - 1))) * kVoidCells +
+                           ((uint32_t)iz & (kVoidCells - 1));
+        for (int32_t j = v.head[c]; j != -1; j = v.next[j])
+          if (collide(cx, cy, cz, r, v.cx[j], v.cy[j], v.cz[j], v.r[j], f, scale, box, half,
+                      interior))
+            return true;
+      }
+  return false;
+}
+
+// The minimum-image distance test of find_conflicts and displace_void.
+template <class R>
+__device__ __forceinline__ R min_image_d2(R ax, R ay, R az, R bx, R by, R bz, R box) {
+  const R half = fmul(R(0.5f), box);
+  R dx = fabs_(fsub(ax, bx)), dy = fabs_(fsub(ay, by)), dz = fabs_(fsub(az, bz));
+  dx = dx > half ? fsub(box, dx) : dx;
+  dy = dy > half ? fsub(box, dy) : dy;
+  dz = dz > half ? fsub(box, dz) : dz;
+  return fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
+}
+
+// paint_sphere (set or clear) by the whole CTA: every node within r of c.
+template <class R>
+__device__ void paint_cta(R cx, R cy, R cz, R r, uint32_t* mask, const RungConstsT<R>& rc, bool set) {
+  const uint32_t n = rc.grid_n;
+  const R r2 = fmul(r, r);
+  const R inv = fdiv(R(1.0f), rc.cell);
+  const R half = fmul(rc.gbox, R(0.5f));
+  const int32_t cr = (int32_t)fmul(r, inv) + 1;
+  const int32_t ci = (int32_t)fmul(cx, inv), cj = (int32_t)fmul(cy, inv), ck = (int32_t)fmul(cz, inv);
+  const int32_t side = 2 * cr + 1;
+  for (int32_t q = threadIdx.x; q < side * side; q += blockDim.x) {
+    const int32_t gx = ci + q / side - cr, gy = cj + q % side - cr;
+    R ddx = fabs_(fsub(fmul((R)gx, rc.cell), cx));
+    ddx = ddx > half ? fsub(rc.gbox, ddx) : ddx;
+    const R dx2 = fmul(ddx, ddx);
+    if (dx2 > r2) continue;
+    R ddy = fabs_(fsub(fmul((R)gy, rc.cell), cy));
+    ddy = ddy > half ? fsub(rc.gbox, ddy) : ddy;
+    const R dxy2 = fadd(dx2, fmul(ddy, ddy));
+    if (dxy2 > r2) continue;
+    const uint64_t row = ((uint64_t)wrap_pbc(gx, n) * n + wrap_pbc(gy, n)) * n;
+    for (int32_t dz = -cr; dz <= cr; dz++) {
+      const int32_t gz = ck + dz;
+      R ddz = fabs_(fsub(fmul((R)gz, rc.cell), cz));
+      ddz = ddz > half ? fsub(rc.gbox, ddz) : ddz;
+      if (fadd(dxy2, fmul(ddz, ddz)) <= r2) {
+        const uint64_t cell = row + wrap_pbc(gz, n);
+        if (set)
+          atomicOr(mask + (cell >> 5), 1u << (cell & 31));
+        else
+          atomicAnd(mask + (cell >> 5), ~(1u << (cell & 31)));
+      }
+    }
+  }
+}
+
+// The commit's state: [0] voids in the catalogue (displaced ones included
+// until the compaction), [1] accepted this rung, [2] displaced this rung,
+// [3] a list overflowed, [4..5] the largest accepted radius (R's bits).
+constexpr uint32_t kDispVoids = 0, kDispAccepted = 1, kDispRemoved = 2, kDispOverflow = 3,
+                   kDispMaxR = 4;
+constexpr int kDispT = 512;
+
+template <class R>
+__device__ __forceinline__ R load_real(const uint32_t* p) {
+  R v;
+  memcpy(&v, (const void*)p, sizeof(R));
+  return v;
+}
+template <class R>
+__device__ __forceinline__ void store_real(uint32_t* p, R v) {
+  memcpy((void*)p, &v, sizeof(R));
+}
+
+template <class R>
+__global__ void __launch_bounds__(kDispT) displace_commit_kernel(
+    SurvivorsT<R> sv, const uint32_t* __restrict__ order, uint32_t m, VoidListT<R> vl,
+    uint32_t* mask, RungConstsT<R> rc, uint32_t* state, uint32_t* conflicts, uint32_t* paints,
+    uint32_t cap) {
+  __shared__ int s_accept;
+  __shared__ uint32_t s_n, s_j;
+  __shared__ R s_v[4];
+  const uint32_t nn = rc.grid_n;
+  for (uint32_t k = 0; k < m; k++) {
+    if (threadIdx.x == 0) {
+      s_accept = 0;
+      s_n = 0;
+      const uint32_t i = order[k];
+      const R r = sv.r[i];
+      const uint32_t node = sv.flat[i];
+      const R cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i];
+      const R max_r = load_real<R>(state + kDispMaxR);
+      const uint32_t ix = node / (nn * nn), iy = (node / nn) % nn, iz = node % nn;
+      // The rescaling failed; the node's mask bit; the poles and the exact
+      // overlap at the rung radius, against the catalogue as it now stands.
+      bool ok = r >= R(0) && !mask_get_rw(mask, node);
+      if (ok && rc.proxy_pole > 0 && overlap_quick(mask, nn, ix, iy, iz, (uint32_t)rc.proxy_pole))
+        ok = false;
+      if (ok && overlap_exact_chains(vl, max_r, cx, cy, cz, rc.radius, rc.f, rc.scale, rc.box))
+        ok = false;
+      if (ok) {
+        // find_conflicts at the rescaled radius: refused by a void at least
+        // as large, else those it collides with are displaced.
+        const R reach = search_radius(r, max_r, rc.f, rc.scale);
+        int32_t lo[3], hi[3];
+        void_window(cx, cy, cz, reach, vl.inv_cell, lo, hi);
+        R largest = R(-1.0f);
+        uint32_t nc = 0;
+        for (int32_t a = lo[0]; a <= hi[0]; a++)
+          for (int32_t b = lo[1]; b <= hi[1]; b++)
+            for (int32_t c = lo[2]; c <= hi[2]; c++) {
+              const uint32_t cell = (wrap_void(a) * kVoidCells + wrap_void(b)) * kVoidCells + wrap_void(c);
+              for (int32_t j = vl.head[cell]; j != -1; j = vl.next[j]) {
+                const R rj = vl.r[j];
+                const R mn = r < rj ? r : rj;
+                const R tot = fmul(rc.scale, fsub(fadd(r, rj), fmul(rc.f, mn)));
+                if (!(min_image_d2(cx, cy, cz, vl.cx[j], vl.cy[j], vl.cz[j], rc.box) < fmul(tot, tot)))
+                  continue;
+                if (nc < cap) conflicts[nc] = (uint32_t)j;
+                nc++;
+                if (rj > largest) largest = rj;
+              }
+            }
+        if (nc > cap) state[kDispOverflow] = 1;
+        if (largest < r && nc <= cap) {
+          s_accept = 1;
+          s_n = nc;
+          s_v[0] = cx;
+          s_v[1] = cy;
+          s_v[2] = cz;
+          s_v[3] = r;
+        }
+      }
+    }
+    __syncthreads();
+    if (!s_accept) continue;
+    const uint32_t nconf = s_n;
+    const R ncx = s_v[0], ncy = s_v[1], ncz = s_v[2], nr = s_v[3];
+    for (uint32_t q = 0; q < nconf; q++) {
+      // displace_void: out of the index, radius negated, its sphere cleared,
+      // the spheres of the voids still indexed that intersect it painted back.
+      __shared__ R d[4];
+      if (threadIdx.x == 0) {
+        const uint32_t j = conflicts[q];
+        d[0] = vl.cx[j];
+        d[1] = vl.cy[j];
+        d[2] = vl.cz[j];
+        d[3] = vl.r[j];
+        int32_t* link = vl.head + void_cell_of(d[0], d[1], d[2], vl.inv_cell);
+        while (*link != -1 && *link != (int32_t)j) link = vl.next + *link;
+        if (*link != -1) *link = vl.next[j];
+        vl.r[j] = -d[3];
+        state[kDispRemoved]++;
+      }
+      __syncthreads();
+      paint_cta(d[0], d[1], d[2], fmul(rc.scale, d[3]), mask, rc, false);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const R max_r = load_real<R>(state + kDispMaxR);
+        const R reach = fmul(rc.scale, fadd(d[3], max_r));
+        int32_t lo[3], hi[3];
+        void_window(d[0], d[1], d[2], reach, vl.inv_cell, lo, hi);
+        uint32_t np = 0;
+        for (int32_t a = lo[0]; a <= hi[0]; a++)
+          for (int32_t b = lo[1]; b <= hi[1]; b++)
+            for (int32_t c = lo[2]; c <= hi[2]; c++) {
+              const uint32_t cell = (wrap_void(a) * kVoidCells + wrap_void(b)) * kVoidCells + wrap_void(c);
+              for (int32_t j = vl.head[cell]; j != -1; j = vl.next[j]) {
+                const R t = fmul(rc.scale, fadd(d[3], vl.r[j]));
+                if (min_image_d2(d[0], d[1], d[2], vl.cx[j], vl.cy[j], vl.cz[j], rc.box) < fmul(t, t)) {
+                  if (np < cap) paints[np] = (uint32_t)j;
+                  np++;
+                }
+              }
+            }
+        if (np > cap) state[kDispOverflow] = 1;
+        s_j = np < cap ? np : cap;
+      }
+      __syncthreads();
+      // Painting sets bits only: the spheres in any order, a warp each.
+      const uint32_t warps = blockDim.x >> 5;
+      for (uint32_t p = threadIdx.x >> 5; p < s_j; p += warps) {
+        const uint32_t j = paints[p];
+        paint_one(vl.cx[j], vl.cy[j], vl.cz[j], vl.r[j], mask, rc, threadIdx.x & 31u);
+      }
+      __syncthreads();
+    }
+    // accept_void: appended, indexed at the head of its chain, painted.
+    if (threadIdx.x == 0) {
+      const uint32_t v = state[kDispVoids];
+      vl.cx[v] = ncx;
+      vl.cy[v] = ncy;
+      vl.cz[v] = ncz;
+      vl.r[v] = nr;
+      const uint32_t cell = void_cell_of(ncx, ncy, ncz, vl.inv_cell);
+      vl.next[v] = vl.head[cell];
+      vl.head[cell] = (int32_t)v;
+      state[kDispVoids] = v + 1;
+      state[kDispAccepted]++;
+      if (nr > load_real<R>(state + kDispMaxR)) store_real<R>(state + kDispMaxR, nr);
+    }
+    paint_cta(ncx, ncy, ncz, fmul(rc.scale, nr), mask, rc, true);
+    __syncthreads();
+  }
+}
+
+// Survivor order from the ranks: order[rank[cand[i]]] = i (every candidate
+// is a survivor under displacement).
+template <class R>
+__global__ void order_by_rank_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ rank,
+                                     uint32_t* __restrict__ order) {
+  const uint32_t n = *sv.count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    order[rank[sv.cand[i]]] = i;
+}
+
+// compact_catalogue (exodus_finder.c:1043-1078): the voids still standing
+// (radius > 0) closed up in order, by one CTA in chunks.
+template <class R>
+__global__ void __launch_bounds__(1024) compact_voids_kernel(R* cx, R* cy, R* cz, R* r,
+                                                             uint32_t* state) {
+  __shared__ uint32_t ws[32];
+  __shared__ uint32_t base;
+  const uint32_t n = state[kDispVoids];
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  for (uint32_t c0 = 0; c0 < n; c0 += blockDim.x) {
+    const uint32_t i = c0 + threadIdx.x;
+    R v[4] = {0, 0, 0, 0};
+    bool keep = false;
+    if (i < n) {
+      v[0] = cx[i];
+      v[1] = cy[i];
+      v[2] = cz[i];
+      v[3] = r[i];
+      keep = v[3] > R(0);
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (uint32_t w = 0; w < blockDim.x / 32; w++) {
+      before += w < (threadIdx.x >> 5) ? ws[w] : 0u;
+      total += ws[w];
+    }
+    const uint32_t pos = base + before + __popc(bal & ((1u << (threadIdx.x & 31)) - 1u));
+    __syncthreads();  // every read of this chunk is done before any write
+    if (keep) {
+      cx[pos] = v[0];
+      cy[pos] = v[1];
+      cz[pos] = v[2];
+      r[pos] = v[3];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) base += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) state[kDispVoids] = base;
+}
+
+template <class R>
+void displace_commit(SurvivorsT<R> s, const uint32_t* rank, uint32_t m, uint32_t* order,
+                     const uint32_t* vstart, uint32_t* vids, int32_t* head, int32_t* next,
+                     R* cat_x, R* cat_y, R* cat_z, R* cat_r, R box, uint32_t* mask,
+                     RungConstsT<R> rc, uint32_t* state, uint32_t* conflicts, uint32_t* paints,
+                     uint32_t cap, cudaStream_t st) {
+  void_chains_kernel<<<grid_for((uint64_t)kVoidCells * kVoidCells * kVoidCells, 256), 256, 0, st>>>(
+      vstart, vids, head, next);
+  SIFG_LAUNCH_CHECK();
+  if (m == 0) return;
+  order_by_rank_kernel<R><<<grid_for(m, 256), 256, 0, st>>>(s, rank, order);
+  SIFG_LAUNCH_CHECK();
+  VoidListT<R> vl{cat_x, cat_y, cat_z, cat_r, head, next, (R)kVoidCells / box};
+  displace_commit_kernel<R><<<1, kDispT, 0, st>>>(s, order, m, vl, mask, rc, state, conflicts, paints,
+                                                 cap);
+  SIFG_LAUNCH_CHECK();
+}
+
+template <class R>
+void compact_voids(R* cx, R* cy, R* cz, R* r, uint32_t* state, cudaStream_t st) {
+  compact_voids_kernel<R><<<1, 1024, 0, st>>>(cx, cy, cz, r, state);
+  SIFG_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
 // The two forms: the reference's float build and its SIF_USE_DOUBLE build.
 // ---------------------------------------------------------------------------
 #define SIFG_FINDER_FORM(R)                                                                        \
@@ -2001,7 +2380,7 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
                                 uint32_t*, cudaStream_t);                                          \
   template void prefilter<R>(const uint32_t*, uint32_t, const uint32_t*, VoidViewT<R>,             \
                              RungConstsT<R>, uint8_t*, uint32_t*, uint32_t*, uint32_t*, R*, R*,    \
-                             R*, uint32_t*, cudaStream_t);                                         \
+                             R*, uint32_t*, cudaStream_t, bool);                                   \
   template void witness<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>,         \
                            VoidViewT<R>, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*);\
   template void grow<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>, uint32_t,   \
@@ -2023,7 +2402,12 @@ void build_void_index(const R* cx, const R* cy, const R* cz, uint32_t n, R box,
                                    const uint32_t*, uint32_t, uint32_t*, R*, R*, R*, R*, uint32_t, \
                                    uint32_t, cudaStream_t);                                        \
   template void build_void_index<R>(const R*, const R*, const R*, uint32_t, R, uint32_t*,          \
-                                    uint32_t*, uint32_t*, cudaStream_t);
+                                    uint32_t*, uint32_t*, cudaStream_t);                           \
+  template void displace_commit<R>(SurvivorsT<R>, const uint32_t*, uint32_t, uint32_t*,            \
+                                   const uint32_t*, uint32_t*, int32_t*, int32_t*, R*, R*, R*, R*, \
+                                   R, uint32_t*, RungConstsT<R>, uint32_t*, uint32_t*, uint32_t*,  \
+                                   uint32_t, cudaStream_t);                                        \
+  template void compact_voids<R>(R*, R*, R*, R*, uint32_t*, cudaStream_t);
 
 SIFG_FINDER_FORM(float)
 SIFG_FINDER_FORM(double)

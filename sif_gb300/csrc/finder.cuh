@@ -161,12 +161,13 @@ void below_write_pass(const uint32_t* counts, const float* delta, const uint32_t
                       cudaStream_t st);
 
 // Pre-filter at the rung radius (prefilter_cells, exodus_finder.c:871-944)
-// and compaction of the survivors, candidate order kept.
+// and compaction of the survivors, candidate order kept; with keep_all
+// (displacement) every candidate survives.
 template <class R>
 void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, VoidViewT<R> voids,
                RungConstsT<R> rc, uint8_t* alive, uint32_t* block_counts, uint32_t* surv_cand,
                uint32_t* surv_flat, R* scx, R* scy, R* scz, uint32_t* d_surv_count,
-               cudaStream_t st);
+               cudaStream_t st, bool keep_all = false);
 
 // The collision witness (collision_radius, src/finder/exodus_finder.c:
 // 780-845, and sif__exodus_witness, src/finder/exodus_rescale.c:1074-1167):
@@ -270,6 +271,26 @@ void append_accepted(SurvivorsT<R> s, const uint32_t* rank, const uint32_t* acc,
                      const uint32_t* counters, uint32_t m_candidates, uint32_t* rank_slots,
                      R* cat_x, R* cat_y, R* cat_z, R* cat_r, uint32_t n_voids,
                      uint32_t max_survivors, cudaStream_t st);
+
+// Displacement (SIF_FINDER_DISPLACE, exodus_finder.c:696-756, 946-1078,
+// 2239-2275): every survivor (every candidate: no pre-filter) in rank order
+// by one CTA, against a linked void index rebuilt from the compressed one
+// (vstart, vids over the first state[0] voids of the catalogue): refused by
+// its mask bit, the poles and the exact overlap at the rung radius, or by a
+// colliding void at least its size; else the smaller voids it collides with
+// are displaced (radius negated, sphere cleared, intersecting spheres painted
+// back) and it is appended. state: [0] the catalogue's voids (in and out),
+// [1] accepted, [2] displaced, [3] a list overflowed (cap entries each for
+// conflicts and paints), [4..5] the largest radius (in and out).
+template <class R>
+void displace_commit(SurvivorsT<R> s, const uint32_t* rank, uint32_t m, uint32_t* order,
+                     const uint32_t* vstart, uint32_t* vids, int32_t* head, int32_t* next,
+                     R* cat_x, R* cat_y, R* cat_z, R* cat_r, R box, uint32_t* mask,
+                     RungConstsT<R> rc, uint32_t* state, uint32_t* conflicts, uint32_t* paints,
+                     uint32_t cap, cudaStream_t st);
+// The displaced voids (radius <= 0) dropped, order kept; state[0] updated.
+template <class R>
+void compact_voids(R* cx, R* cy, R* cz, R* r, uint32_t* state, cudaStream_t st);
 
 // Rebuilds the void index over the first n voids.
 template <class R>

@@ -367,7 +367,28 @@ struct ColumnFilter {
   const float* win;
   float norm, wy, wz;
   uint32_t q;  // ky'^2 + kz^2
+  const float* tab;  // the column's factors by |kx| (257), or NULL: evaluate them
 };
+
+// The factor table of a smoothing at n = 512: entry ((|ky| * 257 + kz) * 257
+// + |kx|) holds the factor the filter pass applies to mode (kx, ky, kz) --
+// radial_factor(k^2) * norm, then the window's three factors, in the order
+// and with the values ifft512_column computes them, so the table changes no
+// bit of the transform.
+constexpr uint32_t kFactorSide = 257;
+__global__ void factor_table_kernel(float* __restrict__ tab, RadialFilter rf,
+                                    const float* __restrict__ win, float norm) {
+  constexpr uint64_t total = (uint64_t)kFactorSide * kFactorSide * kFactorSide;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t kx = (uint32_t)(i % kFactorSide);
+    const uint32_t kz = (uint32_t)((i / kFactorSide) % kFactorSide);
+    const uint32_t ky = (uint32_t)(i / ((uint64_t)kFactorSide * kFactorSide));
+    float v = radial_factor(kx * kx + (ky * ky + kz * kz), rf) * norm;
+    if (win) v = v * __ldg(win + kx) * __ldg(win + ky) * __ldg(win + kz);
+    tab[i] = v;
+  }
+}
 
 // One warp's inverse DFT of the 512 values in `col`, in place; with a filter
 // (f.on) each value is first scaled by its filter factor.
@@ -388,16 +409,22 @@ __device__ __forceinline__ void ifft512_column(float2* col, const float2* __rest
     // 512 - kx, half the evaluations. Lane 0 holds both kx = 32 r and
     // 512 - 32 r itself, and alone finds kx = 256.
     float lo[8];
-#pragma unroll
-    for (int r = 0; r < 8; r++) {
-      const uint32_t kx = lane + 32u * r;
-      lo[r] = radial_factor(kx * kx + f.q, f.rf) * f.norm;
-      if (f.win) lo[r] = lo[r] * __ldg(f.win + kx) * f.wy * f.wz;
-    }
     float nyq = 0.f;
-    if (lane == 0) {
-      nyq = radial_factor(256u * 256u + f.q, f.rf) * f.norm;
-      if (f.win) nyq = nyq * __ldg(f.win + 256) * f.wy * f.wz;
+    if (f.tab) {
+#pragma unroll
+      for (int r = 0; r < 8; r++) lo[r] = __ldg(f.tab + lane + 32u * r);
+      if (lane == 0) nyq = __ldg(f.tab + 256);
+    } else {
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        const uint32_t kx = lane + 32u * r;
+        lo[r] = radial_factor(kx * kx + f.q, f.rf) * f.norm;
+        if (f.win) lo[r] = lo[r] * __ldg(f.win + kx) * f.wy * f.wz;
+      }
+      if (lane == 0) {
+        nyq = radial_factor(256u * 256u + f.q, f.rf) * f.norm;
+        if (f.win) nyq = nyq * __ldg(f.win + 256) * f.wy * f.wz;
+      }
     }
     const unsigned partner = (32u - lane) & 31u;
 #pragma unroll
@@ -473,7 +500,8 @@ struct ColumnLayout {
 __global__ void __launch_bounds__(32 * kColWarps, 3)
     colfft512_kernel(const float2* src, float2* dst, ColumnLayout in, ColumnLayout out,
                      RadialFilter rf, const float* __restrict__ win, float norm,
-                     const float2* __restrict__ tw, bool forward) {
+                     const float2* __restrict__ tw, bool forward,
+                     const float* __restrict__ ftab = nullptr) {
   extern __shared__ float2 cols[];  // kColCols columns of kColStride slots
   constexpr uint32_t zd = 257;
   constexpr uint32_t kRowStep = 32 * kColWarps / kColCols;  // rows a pass of the CTA covers
@@ -497,8 +525,10 @@ __global__ void __launch_bounds__(32 * kColWarps, 3)
     if (rf.kind >= 0) {
       const uint32_t kz = kz0 + w;
       const int32_t ks = line > 256 ? (int32_t)line - 512 : (int32_t)line;
+      const uint32_t aky = (uint32_t)(ks < 0 ? -ks : ks);
       f = ColumnFilter{true, rf, win, norm, win ? __ldg(win + line) : 1.f,
-                       win ? __ldg(win + kz) : 1.f, (uint32_t)(ks * ks) + kz * kz};
+                       win ? __ldg(win + kz) : 1.f, (uint32_t)(ks * ks) + kz * kz,
+                       ftab ? ftab + ((size_t)aky * kFactorSide + kz) * kFactorSide : nullptr};
     }
     ifft512_column(cols + w * kColStride, tw, lane, f, forward);
   }
@@ -778,6 +808,7 @@ void SmootherT<R>::release() {
   plan_r2c = plan_c2r = 0;
   plan_work = 0;
   twiddles = nullptr;
+  factor_tables.clear();
   n = 0;
 }
 
@@ -926,8 +957,10 @@ static void launch_forward512(const SmootherT<float>& s, const float* grid, cons
 }
 
 // The timer, begun by the caller, ends after pass (1): the filter's kernel.
+// ftab: the smoothing's factor table, or NULL (the factors evaluated).
 static void launch_inverse512(const SmootherT<float>& s, int filter, const RadialFilter& rf,
-                              float norm, float* out, KernelTimer* timer, const BelowList& below) {
+                              float norm, float* out, KernelTimer* timer, const BelowList& below,
+                              const float* ftab) {
   constexpr uint32_t N = 512;
   const float* w = (s.window_mode && filter != kFilterNone) ? s.win.as<float>() : nullptr;
   const size_t smem = (size_t)kColCols * kColStride * sizeof(float2);
@@ -936,7 +969,7 @@ static void launch_inverse512(const SmootherT<float>& s, int filter, const Radia
   const dim3 grid(kKzBlocks, N);
   colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
       s.spectrum.as<float2>(), s.work.as<float2>(), kTilesByLine, kTilesByRow, rf, w,
-      norm, tw, false);
+      norm, tw, false, ftab);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(s.stream);
   colfft512_kernel<<<grid, 32 * kColWarps, smem, s.stream>>>(
@@ -948,7 +981,58 @@ static void launch_inverse512(const SmootherT<float>& s, int filter, const Radia
   SIFG_LAUNCH_CHECK();
 }
 static void launch_inverse512(const SmootherT<double>&, int, const RadialFilter&, double, double*,
-                              KernelTimer*, const BelowList&) {}
+                              KernelTimer*, const BelowList&, const float*) {}
+
+static int g_factor_tables = 1;
+void set_factor_tables(int on) { g_factor_tables = on; }
+
+static RadialFilter radial_filter_of(int filter, double factor, double gfactor) {
+  const float f = (float)factor;
+  return RadialFilter{filter == kFilterTopHat || filter == kFilterGaussian ? filter : kFilterNone,
+                      (float)(factor * factor), (float)(0.5 * gfactor * gfactor), f,
+                      (float)(factor - (double)f)};
+}
+
+template <class R>
+const float* SmootherT<R>::factor_table(int filter, R r, R sigma) {
+  if constexpr (sizeof(R) != 4) {
+    return nullptr;
+  } else {
+    if (!g_factor_tables || !twiddles || filter == kFilterNone) return nullptr;
+    factor_clock++;
+    for (auto& t : factor_tables)
+      if (t->filter == filter && t->r == r && t->sigma == sigma && t->box == box &&
+          t->window_mode == window_mode) {
+        t->used = factor_clock;
+        return t->buf.template as<float>();
+      }
+    std::unique_ptr<FactorTable> t;
+    if ((int)factor_tables.size() >= kFactorTables) {
+      auto lru = std::min_element(factor_tables.begin(), factor_tables.end(),
+                                  [](const auto& a, const auto& b) { return a->used < b->used; });
+      t = std::move(*lru);
+      factor_tables.erase(lru);
+    } else {
+      t.reset(new FactorTable);
+    }
+    t->filter = filter;
+    t->r = r;
+    t->sigma = sigma;
+    t->box = box;
+    t->window_mode = window_mode;
+    t->used = factor_clock;
+    float* tab = (float*)t->buf.ensure((size_t)kFactorSide * kFactorSide * kFactorSide * sizeof(float));
+    const double factor = (double)r * 2.0 * M_PI / (double)box;
+    const double gfactor = sigma > R(0) ? (double)sigma * 2.0 * M_PI / (double)box : 0.0;
+    const float norm = (float)(1.0 / ((double)n * n * n));
+    factor_table_kernel<<<152u * 8u, 256, 0, stream>>>(tab, radial_filter_of(filter, factor, gfactor),
+                                                       window_mode ? win.template as<float>() : nullptr,
+                                                       norm);
+    SIFG_LAUNCH_CHECK();
+    factor_tables.push_back(std::move(t));
+    return factor_tables.back()->buf.template as<float>();
+  }
+}
 
 static void launch_filter(const SmootherT<double>& s, int filter, double norm) {
   const uint64_t modes = (uint64_t)s.n * s.n * (s.n / 2 + 1);
@@ -966,13 +1050,12 @@ void SmootherT<R>::smooth(int filter, R r, R sigma, R* out, KernelTimer* timer,
   const double gfactor = sigma > R(0) ? (double)sigma * 2.0 * M_PI / (double)box : 0.0;
   const R norm = (R)(1.0 / ((double)n * n * n));
   if (twiddles) {
-    // The own inverse evaluates the radial factor as it applies it: no table.
-    const float f = (float)factor;
-    const RadialFilter rf{filter == kFilterTopHat || filter == kFilterGaussian ? filter : kFilterNone,
-                          (float)(factor * factor), (float)(0.5 * gfactor * gfactor), f,
-                          (float)(factor - (double)f)};
+    // The own inverse reads the smoothing's factor table (built on first use)
+    // or evaluates the radial factor as it applies it.
+    const RadialFilter rf = radial_filter_of(filter, factor, gfactor);
+    const float* ftab = factor_table(filter, r, sigma);
     if (timer) timer->begin(stream);
-    launch_inverse512(*this, filter, rf, norm, out, timer, below ? *below : BelowList{});
+    launch_inverse512(*this, filter, rf, norm, out, timer, below ? *below : BelowList{}, ftab);
     return;
   }
   lut_kernel<R><<<grid_for((uint64_t)max_k2 + 1, 256), 256, 0, stream>>>(lut.as<R>(), max_k2, filter,

@@ -3,6 +3,7 @@
 
 #include <cufft.h>
 
+#include <memory>
 #include <vector>
 
 #include "kernels.cuh"
@@ -52,6 +53,21 @@ struct SmootherT {
   size_t plan_work = 0;  // the current plans' need
   const void* twiddles = nullptr;
   std::vector<Plans> plans;
+  // The own inverse's filter factors at n = 512, one table per smoothing
+  // (filter, radius, sigma, window, box): 257^3 floats (68 MB), the factor of
+  // mode (|kx|, |ky|, kz) as the filter pass applies it. Built once, kept
+  // (least recently used out past kFactorTables): a run's rungs smooth at the
+  // same radii every time.
+  struct FactorTable {
+    int filter = 0, window_mode = 0;
+    R r = 0, sigma = 0, box = 0;
+    uint64_t used = 0;
+    DevBuf buf;
+  };
+  static constexpr int kFactorTables = 24;
+  std::vector<std::unique_ptr<FactorTable>> factor_tables;
+  uint64_t factor_clock = 0;
+  const float* factor_table(int filter, R r, R sigma);
 
   void setup(uint32_t n, R box, int window_mode, cudaStream_t st);
   // grid: n^3 values on the device; with mean set, the density, whose
@@ -70,5 +86,9 @@ struct SmootherT {
   ~SmootherT();
 };
 using Smoother = SmootherT<float>;
+
+// 1 (default): the own inverse at 512 reads per-smoothing factor tables; 0:
+// it evaluates the factors as it applies them. The same bits either way.
+void set_factor_tables(int on);
 
 }  // namespace sifg

@@ -204,6 +204,12 @@ def set_witness(on):
     _lib.load().sifg_set_witness(int(on))
 
 
+def set_factor_tables(on):
+    """1 the 512^3 filter pass reads per-smoothing factor tables, 0 it
+    evaluates the factors; the same bits either way."""
+    _lib.load().sifg_set_factor_tables(int(on))
+
+
 def set_window(bins):
     _lib.load().sifg_set_window(int(bins))
 

@@ -59,6 +59,19 @@ def golden_box32_extend_f64():
 
 
 @pytest.fixture(scope="session")
+def golden_box32_displace():
+    """The same positions at threshold -0.3 and ladder(3, 6): catalogues under
+    SIF_FINDER_DISPLACE (the excursion-peak preset among them)."""
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32_displace.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_box32_displace_f64():
+    """The displacement box through the reference's SIF_USE_DOUBLE build."""
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32_displace_f64.npz")))
+
+
+@pytest.fixture(scope="session")
 def gpu_lib():
     """The built GB300 library, initialised on the GPU."""
     import torch

@@ -18,6 +18,15 @@ golden_box32_f64.npz -- the same box through the reference's SIF_USE_DOUBLE
   up to 1e-4 so that they need double precision, and the same records in
   double (density, contrast, mesh, 12 captured fields, catalogues).
 
+golden_box32_displace.npz, golden_box32_displace_f64.npz -- the same
+  positions (the f64 file with the same jitter) at threshold -0.3 and
+  ladder(3, 6, 0.1) (8 rungs), where SIF_FINDER_DISPLACE changes the
+  catalogue: the excursion-peak preset (minima seeds, extended reach,
+  displacement, overlap fraction 1), the same less its displacement, and
+  displacement with cell seeds (overlap 0 and 0.5), with minima at 0.5 and
+  with the Lagrangian overlap. The contrast, the mesh, the 8 fields the
+  reference's own run smoothed, and its catalogues on them.
+
 golden_workload_a.npz -- workload A itself: 128^3 particles (synth.workload_particles
   ("A"): box 500, rms displacement 4, seed 1001), grid 128^3, mesh 50^3,
   ladder(5, 30, 0.10) (19 rungs), threshold -0.8. The reference's whole path
@@ -199,6 +208,61 @@ def make_box32_extend(path, v="strict"):
     print(f"{path}: " + ", ".join(f"{n} {len(out[f'cat_{n}_r'])}" for n, _, _ in EXTEND_SETS))
 
 
+DISPLACE = dict(BOX32, threshold=-0.3, r0=3.0, top=2.0)
+DISPLACE_SETS = [
+    ("peak", 1.0, abi.SIF_FINDER_SEEDS_MINIMA | abi.SIF_FINDER_EXTEND_REACH | abi.SIF_FINDER_DISPLACE),
+    ("peak_no_displace", 1.0, abi.SIF_FINDER_SEEDS_MINIMA | abi.SIF_FINDER_EXTEND_REACH),
+    ("cells_f0", 0.0, abi.SIF_FINDER_DISPLACE),
+    ("cells_f05", 0.5, abi.SIF_FINDER_DISPLACE),
+    ("minima_f05", 0.5, abi.SIF_FINDER_SEEDS_MINIMA | abi.SIF_FINDER_DISPLACE),
+    ("lagrangian", 0.0, abi.SIF_FINDER_LAGRANGIAN_OVERLAP | abi.SIF_FINDER_DISPLACE),
+]
+
+
+def make_box32_displace(path, v="strict"):
+    p = DISPLACE
+    x, y, z = synth.zeldovich(p["n"], p["box"], p["rms_disp"], p["seed"])
+    real = np.float32
+    if v == "f64":
+        rng = np.random.default_rng(p["seed"] + 1000)  # BOX32's f64 jitter
+
+        def jitter(a):
+            w = a.astype(np.float64) + rng.uniform(-1e-4, 1e-4, a.shape)
+            w = np.where(w < 0.0, w + p["box"], w)
+            return np.where(w >= p["box"], w - p["box"], w)
+
+        x, y, z = jitter(x), jitter(y), jitter(z)
+        real = np.float64
+    radii = synth.ladder(p["r0"], p["top"] * p["r0"], 0.1).astype(real)
+    lib = R.load(v, 4, abi.SIF_LOG_LEVEL_ERROR)
+    kw = dict(variant=v) if v == "f64" else {}
+    f = R.RefField(lib, x, y, z, **kw)
+    g = R.RefGrid(lib, p["n"], p["box"], **kw)
+    g.assign_cic(f)
+    g.to_contrast()
+    delta = g.values()
+    m = R.RefMesh(lib, p["mesh"], p["box"], f)
+    mx, my, mz, offs, idx = m.arrays(**kw)
+    fields = np.zeros((len(radii), p["n"] ** 3), real)
+    R.exodus_raw(lib, g, m, radii, p["threshold"], capture=fields, **kw)
+    out = dict(x=x, y=y, z=z, radii=radii, delta=delta, mesh_x=mx, mesh_y=my, mesh_z=mz,
+               mesh_offsets=offs, mesh_index=idx, fields=fields,
+               params=np.array([p["n"], p["box"], p["rms_disp"], p["seed"], p["r0"],
+                                p["threshold"], p["mesh"]], np.float64))
+    for name, overlap, opt in DISPLACE_SETS:
+        c = R.exodus_raw(lib, g, m, radii, p["threshold"], overlap, opt, inject=fields, **kw)
+        for k, col in zip(("cx", "cy", "cz", "r"), c):
+            out[f"cat_{name}_{k}"] = col
+        out[f"cat_{name}_opt"] = np.array([overlap, opt], np.float64)
+    a, b = out["cat_peak_r"], out["cat_peak_no_displace_r"]
+    assert len(a) != len(b) or not np.array_equal(a, b), "displacement changes nothing here"
+    m.free()
+    g.free()
+    f.free()
+    np.savez_compressed(path, **out)
+    print(f"{path}: " + ", ".join(f"{n} {len(out[f'cat_{n}_r'])}" for n, _, _ in DISPLACE_SETS))
+
+
 def positions_sha256(x, y, z):
     import hashlib
 
@@ -226,8 +290,14 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "workload_a":
         make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))
         sys.exit(0)
+    if len(sys.argv) > 1 and sys.argv[1] == "displace":
+        make_box32_displace(os.path.join(HERE, "golden_box32_displace.npz"))
+        make_box32_displace(os.path.join(HERE, "golden_box32_displace_f64.npz"), "f64")
+        sys.exit(0)
     make_box32(os.path.join(HERE, "golden_box32.npz"))
     make_box32_f64(os.path.join(HERE, "golden_box32_f64.npz"))
     make_box32_extend(os.path.join(HERE, "golden_box32_extend.npz"))
     make_box32_extend(os.path.join(HERE, "golden_box32_extend_f64.npz"), "f64")
+    make_box32_displace(os.path.join(HERE, "golden_box32_displace.npz"))
+    make_box32_displace(os.path.join(HERE, "golden_box32_displace_f64.npz"), "f64")
     make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))

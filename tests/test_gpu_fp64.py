@@ -111,6 +111,19 @@ def test_fp64_catalogue_extended_reach(dev, golden_box32_extend_f64, name, mode)
         dev.set_growth_mode(0)
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["auto", "cta", "warp"])
+@pytest.mark.parametrize("name", ["peak", "peak_no_displace", "cells_f0", "cells_f05",
+                                  "minima_f05", "lagrangian"])
+def test_fp64_catalogue_displacement(dev, golden_box32_displace_f64, name, mode):
+    """SIF_FINDER_DISPLACE in the FP64 form: the reference's SIF_USE_DOUBLE
+    catalogues (the excursion-peak preset among them) on its own fields."""
+    dev.set_growth_mode(mode)
+    try:
+        test_fp64_catalogue_matches_reference(dev, golden_box32_displace_f64, name)
+    finally:
+        dev.set_growth_mode(0)
+
+
 @pytest.mark.parametrize("window", ["full", "aliasing", "none"])
 def test_fp64_smoothing_against_oracle(dev, oracle, golden_box32_f64, window):
     g = golden_box32_f64

@@ -180,6 +180,30 @@ def test_smoothing_512_against_the_fp64_form(dev, window):
         assert l2 <= FIELD_L2_TOL and mx <= FIELD_MAX_TOL, (r, filt, l2, mx)
 
 
+def test_factor_tables_change_no_bit(dev):
+    """At 512^3 the filter pass reads each smoothing's factor table; the
+    fields are bit for bit those of the pass that evaluates the factors, for
+    both filters and every window, and a table reused on a second smoothing
+    at the same radius gives the same bits again."""
+    import torch
+
+    n, box = 512, 1000.0
+    x, y, z = synth.zeldovich(128, box, 5.0, 23)
+    grid = dev.cic(*_cuda(x, y, z), n, box)
+    dev.density_contrast(grid)
+    for window in ("full", "aliasing", "none"):
+        for r, filt in ((4.0, "top-hat"), (17.3, "top-hat"), (6.0, "gaussian")):
+            a = dev.smooth(grid, n, box, r, filter=filt, window=window)
+            b = dev.smooth(grid, n, box, r, filter=filt, window=window)
+            dev.set_factor_tables(0)
+            try:
+                c = dev.smooth(grid, n, box, r, filter=filt, window=window)
+            finally:
+                dev.set_factor_tables(1)
+            assert torch.equal(a.view(torch.int32), c.view(torch.int32)), (window, r, filt)
+            assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+
+
 def test_gaussian_smoothing_against_fp64(dev, oracle, golden_box32):
     g = golden_box32
     n, box = int(g["params"][0]), float(g["params"][1])
@@ -282,6 +306,23 @@ def test_catalogue_matches_reference_golden_extended_reach(dev, golden_box32_ext
     dev.set_growth_mode(mode)
     try:
         test_catalogue_matches_reference_golden(dev, golden_box32_extend, name)
+    finally:
+        dev.set_growth_mode(0)
+
+
+DISPLACE_SETS = ["peak", "peak_no_displace", "cells_f0", "cells_f05", "minima_f05", "lagrangian"]
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["auto", "cta", "warp"])
+@pytest.mark.parametrize("name", DISPLACE_SETS)
+def test_catalogue_matches_reference_golden_displacement(dev, golden_box32_displace, name, mode):
+    """SIF_FINDER_DISPLACE on the GPU: every candidate grown, then the
+    survivors one at a time in rank order, displacing the smaller voids they
+    collide with; the reference's catalogues (the excursion-peak preset among
+    them) on its own fields, by each growth kernel."""
+    dev.set_growth_mode(mode)
+    try:
+        test_catalogue_matches_reference_golden(dev, golden_box32_displace, name)
     finally:
         dev.set_growth_mode(0)
 
@@ -465,8 +506,10 @@ def test_c_api_end_to_end_and_errors(gpu_lib, oracle):
         pysif.finders.exodus(g, m, radii, 0.5)  # threshold out of (-1, 0)
     with pytest.raises(ValueError):
         pysif.finders.exodus(g, m, [-1.0], -0.7)
-    with pytest.raises(NotImplementedError):
-        pysif.finders.exodus(g, m, radii, -0.7, variant="excursion-peak")
+    # The excursion-peak preset (minima seeds, extended reach, displacement)
+    # runs through sif's C API, and agrees with the oracle on the GPU's field.
+    peak = pysif.finders.exodus(g, m, radii, -0.75, variant="excursion-peak").as_tuple()
+    assert len(peak[0]) > 0
     wrong = pysif.Grid(48, 221.0)
     with pytest.raises(ValueError):
         pysif.finders.exodus(wrong, m, radii, -0.7)

@@ -130,6 +130,19 @@ def test_oracle_catalogue_matches_golden(oracle, golden_box32, name):
     assert same_catalogue(cat, want)
 
 
+DISPLACE_SETS = ["peak", "peak_no_displace", "cells_f0", "cells_f05", "minima_f05", "lagrangian"]
+
+
+@pytest.mark.parametrize("name", DISPLACE_SETS)
+def test_oracle_displacement_matches_golden(oracle, golden_box32_displace, name):
+    """SIF_FINDER_DISPLACE (find_conflicts, displace_void, the displacing
+    commit: src/finder/exodus_finder.c:696-756, 946-1078, 2239-2275): the
+    oracle's sequential pass gives the reference's catalogue, bit for bit, on
+    its own fields -- the excursion-peak preset and displacement under other
+    seeds, overlaps and the Lagrangian scale."""
+    test_oracle_catalogue_matches_golden(oracle, golden_box32_displace, name)
+
+
 def test_oracle_catalogue_with_prior_matches_golden(oracle, golden_box32):
     """sif_finder_exodus_extras_t::prior (src/finder/exodus_finder.c:1614-1622):
     the voids to start from, accepted before the first rung and returned first;
