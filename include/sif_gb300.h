@@ -185,6 +185,40 @@ typedef struct {
   int save_memory;
 } sif_finder_exodus_extras_t;
 
+/* include/sif/finder/exodus_finder.h:409-507: the exodus checkpoint's fixed
+ * 192-byte header. The file is this header, then the ladder largest first
+ * (n_radii sif_real), then the voids as four columns of n_voids sif_real
+ * (every x, then every y, z, radius), in host byte order. */
+#define SIF_FINDER_CHECKPOINT_MAGIC "XCKP"
+#define SIF_FINDER_CHECKPOINT_VERSION 3
+typedef struct {
+  char magic[4];
+  uint32_t version;
+  uint32_t byte_order; /* 0x01020304 as written */
+  uint32_t is_double;
+  uint32_t is_survey;
+  uint32_t is_weighted;
+  uint32_t options;    /* the options that change the catalogue */
+  uint32_t n_radii;
+  uint32_t next_rung;  /* rungs done */
+  uint32_t grid_n_cells;
+  double box_length;
+  double threshold;
+  double overlap_fraction;
+  uint64_t n_particles;
+  double total_weight;
+  uint64_t random_n_particles;
+  double random_total_weight;
+  double offset[3];
+  uint64_t n_prior;
+  uint32_t prior_crc32;
+  uint32_t crc32;
+  uint64_t n_voids;
+  uint64_t n_mismatched;
+  uint32_t assignment;
+  char reserved[36];
+} sif_finder_exodus_checkpoint_t;
+
 /* include/sif/finder/exodus_finder.h:124-133 */
 typedef enum {
   SIF_EXODUS_EXCURSION_SET = 0,
@@ -227,6 +261,11 @@ void sif_chain_mesh_free(sif_chain_mesh_t* mesh);
 
 /* include/sif/structures/catalogue.h:116 */
 void sif_catalogue_free(sif_catalogue_t* catalogue);
+
+/* include/sif/finder/exodus_finder.h:547: a checkpoint's voids (and its
+ * header, when asked), read and checked as a resume reads it. */
+sif_catalogue_t* sif_finder_exodus_checkpoint_read(const char* filepath,
+                                                   sif_finder_exodus_checkpoint_t* header);
 
 /* include/sif/finder/exodus_finder.h:147, 155, 163 */
 int sif_finder_exodus_preset(sif_exodus_variant_t variant, sif_real* overlap_fraction,
@@ -477,6 +516,11 @@ void sifg_set_scan_mode(int mode);
  * first use (257^3 floats, 68 MB, up to 24 kept); 0 it evaluates them as it
  * applies them. The smoothed fields are the same bits either way. */
 void sifg_set_factor_tables(int on);
+/* A test hook, as the reference's sif__exodus_halt_after_set
+ * (src/finder/exodus_checkpoint.h): the finder runs that follow stop after
+ * n_rungs rungs of their ladder, checkpoint written, and fail as a job killed
+ * there would; 0 lets them finish. */
+void sifg_set_halt_after(uint32_t n_rungs);
 /* The collision witness (exodus_finder.c:780-845, exodus_rescale.c:
  * 1074-1167): 1 (default) survivors whose sphere is certain to collide with
  * a void of an earlier rung at any radius they could return are refused

@@ -42,11 +42,11 @@ EXPORTED = [
     "sif_chain_mesh_alloc", "sif_chain_mesh_alloc_consume", "sif_chain_mesh_free",
     "sif_catalogue_free", "sif_finder_exodus_preset", "sif_finder_exodus_variant_name",
     "sif_finder_exodus_variant_from_name", "sif_finder_exodus", "sif_finder_exodus_raw",
-    "sif_finder_grid_cells_from_size",
+    "sif_finder_grid_cells_from_size", "sif_finder_exodus_checkpoint_read",
     # device-resident additions
     "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
     "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
-    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_set_witness", "sifg_set_factor_tables", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
+    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_set_witness", "sifg_set_factor_tables", "sifg_set_halt_after", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
     "sifg_mesh_device_noalloc",
     # the FP64 form
     "sifg_cic_device_f64", "sifg_contrast_device_f64", "sifg_mesh_device_f64",
@@ -99,6 +99,7 @@ def load():
         "sifg_set_scan_mode": (None, [i32]),
         "sifg_set_witness": (None, [i32]),
         "sifg_set_factor_tables": (None, [i32]),
+        "sifg_set_halt_after": (None, [u32]),
         "sifg_stream": (u64, []),
         "sifg_launch_count": (u64, []),
         "sifg_mesh_device_noalloc": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]),

@@ -95,6 +95,23 @@ class sif_config_t(C.Structure):
     ]
 
 
+class sif_finder_exodus_checkpoint_t(C.Structure):
+    """The exodus checkpoint's 192-byte header (include/sif/finder/
+    exodus_finder.h:427-507)."""
+    _fields_ = [
+        ("magic", C.c_char * 4), ("version", C.c_uint32), ("byte_order", C.c_uint32),
+        ("is_double", C.c_uint32), ("is_survey", C.c_uint32), ("is_weighted", C.c_uint32),
+        ("options", C.c_uint32), ("n_radii", C.c_uint32), ("next_rung", C.c_uint32),
+        ("grid_n_cells", C.c_uint32), ("box_length", C.c_double), ("threshold", C.c_double),
+        ("overlap_fraction", C.c_double), ("n_particles", C.c_uint64),
+        ("total_weight", C.c_double), ("random_n_particles", C.c_uint64),
+        ("random_total_weight", C.c_double), ("offset", C.c_double * 3),
+        ("n_prior", C.c_uint64), ("prior_crc32", C.c_uint32), ("crc32", C.c_uint32),
+        ("n_voids", C.c_uint64), ("n_mismatched", C.c_uint64), ("assignment", C.c_uint32),
+        ("reserved", C.c_char * 36),
+    ]
+
+
 def make_structs(real):
     """The reference's public structs with sif_real = `real` (C.c_float for
     the float build, C.c_double for its SIF_USE_DOUBLE build, whose struct
@@ -225,6 +242,8 @@ def bind_sif_api(lib, real=C.c_float):
         "sif_finder_exodus_variant_from_name": (C.c_int, [C.c_char_p, C.POINTER(C.c_int)]),
         "sif_finder_grid_cells_from_size": (C.c_uint32, [C.c_uint64, sif_real, sif_real,
                                                          C.c_int, sif_real]),
+        "sif_finder_exodus_checkpoint_read": (P_cat, [C.c_char_p,
+                                                      C.POINTER(sif_finder_exodus_checkpoint_t)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

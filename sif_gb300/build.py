@@ -14,7 +14,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsif_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-UNITS = ["scan", "cic", "mesh", "smooth", "finder", "engine", "api", "noalloc", "hostpool", "adjoint"]
+UNITS = ["scan", "cic", "mesh", "smooth", "finder", "engine", "api", "noalloc", "hostpool", "adjoint",
+         "checkpoint"]
 
 
 def nvcc():

@@ -24,7 +24,10 @@
 #include <string>
 #include <vector>
 
+#include <unistd.h>
+
 #include "../../include/sif_gb300.h"
+#include "checkpoint.cuh"
 #include "engine.cuh"
 
 namespace sifg {
@@ -647,7 +650,174 @@ static int check_prior(const R* cx, const R* cy, const R* cz, const R* r, uint64
   return SIF_OK;
 }
 
+static uint32_t g_halt_after = 0;  // sifg_set_halt_after
+
+// A run's checkpoint and where it stands (checkpoint_t and run_start,
+// checkpoint_rung, checkpoint_finish of exodus_finder.c:1384-1574).
+struct RunCheckpoint {
+  bool active = false;    // written after every rung
+  bool on_disk = false;   // written or resumed by this run
+  bool progress = false;  // the one on disk holds a finished rung
+  bool keep = false;      // left in place on success
+  std::string path;
+  sif_finder_exodus_checkpoint_t header{};
+  std::vector<float> sorted;    // the ladder, largest first
+  std::vector<float> voids[4];  // where the run starts: prior or resumed voids
+  uint32_t first_rung = 0;
+  std::vector<float> host[4];   // a rung's catalogue, copied back to write
+
+  int start(const sif_grid_t* grid, const sif_chain_mesh_t* mesh, const float* radii,
+            uint32_t n_radii, float threshold, float f, sif_option opt,
+            const sif_finder_exodus_extras_t* extras) {
+    const sif_catalogue_t* prior = extras ? extras->prior : nullptr;
+    const char* named = extras ? extras->checkpoint : nullptr;
+    keep = extras && extras->keep_checkpoint;
+    auto take_prior = [&]() {
+      const uint64_t np = prior ? prior->n_voids : 0;
+      const float* cols[4] = {np ? prior->cx : nullptr, np ? prior->cy : nullptr,
+                              np ? prior->cz : nullptr, np ? prior->radii : nullptr};
+      for (int k = 0; k < 4; k++) voids[k].assign(cols[k], cols[k] + np);
+    };
+    if (opt & SIF_FINDER_NO_CHECKPOINT) {
+      take_prior();
+      return SIF_OK;
+    }
+    sorted.assign(radii, radii + n_radii);
+    std::sort(sorted.begin(), sorted.end(), [](float a, float b) { return a > b; });
+    sif_finder_exodus_checkpoint_t& h = header;
+    h = sif_finder_exodus_checkpoint_t{};
+    h.is_survey = 0;
+    h.is_weighted = mesh->weights != nullptr;
+    h.options = opt & (SIF_FINDER_SEARCH_2_00 | SIF_FINDER_KEEP_CIC_WINDOW | SIF_FINDER_SEEDS_MINIMA |
+                       SIF_FINDER_REFINE_HILL | SIF_FINDER_EXTEND_REACH | SIF_FINDER_DISPLACE |
+                       SIF_FINDER_ALIASING_WINDOW | SIF_FINDER_LAGRANGIAN_OVERLAP);
+    h.n_radii = n_radii;
+    h.grid_n_cells = grid->n_cells;
+    // The window order of the grid's assignment (CIC for an unknown one) and
+    // the interlacing bit (sif__fft_grid_window_order, src/math/fft.c).
+    const uint32_t order = (grid->assignment >= SIF_ASSIGNMENT_NGP && grid->assignment <= SIF_ASSIGNMENT_PCS)
+                               ? (uint32_t)grid->assignment
+                               : (uint32_t)SIF_ASSIGNMENT_CIC;
+    h.assignment = (order & 0xffu) | ((grid->interlaced ? 1u : 0u) << 8);
+    h.box_length = (double)grid->box_length;
+    h.threshold = (double)threshold;
+    h.overlap_fraction = (double)f;
+    h.n_particles = mesh->n_particles;
+    h.total_weight = mesh->total_weight;
+    if (prior && prior->n_voids) {
+      h.n_prior = prior->n_voids;
+      h.prior_crc32 = catalogue_crc(prior->cx, prior->cy, prior->cz, prior->radii, prior->n_voids);
+    }
+    path = named ? std::string(named) : checkpoint_default_name();
+    std::string msg;
+    if (named && access(named, F_OK) == 0) {
+      sif_finder_exodus_checkpoint_t got;
+      std::vector<float> got_radii;
+      int st = checkpoint_load(path, got, got_radii, voids, &msg);
+      if (st == SIF_OK) st = checkpoint_match(path, h, sorted.data(), got, got_radii.data(), &msg);
+      if (st != SIF_OK) {
+        for (auto& v : voids) v.clear();
+        return fail(st, "checkpoint: " + msg);
+      }
+      first_rung = got.next_rung;
+      header.n_mismatched = got.n_mismatched;
+      active = on_disk = progress = true;
+      log_msg(SIF_LOG_LEVEL_INFO, "finder.exodus",
+              fmt("checkpoint: %s: resuming with %u of %u rungs done, %llu voids", named,
+                  got.next_rung, n_radii, (unsigned long long)got.n_voids));
+      return SIF_OK;
+    }
+    take_prior();
+    const int st = checkpoint_write(path, h, sorted.data(), voids[0].data(), voids[1].data(),
+                                    voids[2].data(), voids[3].data(), voids[0].size(),
+                                    named ? nullptr : "running without a checkpoint", &msg);
+    if (st == SIF_OK) {
+      active = on_disk = true;
+      log_msg(SIF_LOG_LEVEL_INFO, "finder.exodus", "checkpoint: " + path);
+      return SIF_OK;
+    }
+    // Only a checkpoint the caller asked for by name is worth failing over.
+    if (named) return fail(st, "checkpoint: " + msg);
+    log_msg(SIF_LOG_LEVEL_WARNING, "finder.exodus", "checkpoint: " + msg);
+    return SIF_OK;
+  }
+
+  // After a rung: the catalogue so far, copied back, and the rungs it covers;
+  // a failure leaves the previous checkpoint. Then the halt hook.
+  int rung(uint32_t done, const float* cx, const float* cy, const float* cz, const float* r,
+           uint32_t nv, uint64_t mismatched, cudaStream_t st) {
+    const float* cols[4] = {cx, cy, cz, r};
+    for (int k = 0; k < 4; k++) {
+      host[k].resize(nv);
+      if (nv)
+        SIFG_CUDA(cudaMemcpyAsync(host[k].data(), cols[k], nv * sizeof(float), cudaMemcpyDeviceToHost, st));
+    }
+    SIFG_CUDA(cudaStreamSynchronize(st));
+    header.next_rung = done;
+    header.n_mismatched += mismatched;
+    std::string msg;
+    if (checkpoint_write(path, header, sorted.data(), host[0].data(), host[1].data(), host[2].data(),
+                         host[3].data(), nv, "checkpoint not updated, the previous one stands",
+                         &msg) == SIF_OK)
+      progress = true;
+    else
+      log_msg(SIF_LOG_LEVEL_WARNING, "finder.exodus", "checkpoint: " + msg);
+    if (g_halt_after && g_halt_after == done) {
+      set_error(SIF_ERR_INVALID, fmt("halted after rung %u of %u (test hook)", done, header.n_radii));
+      return SIF_ERR_INVALID;
+    }
+    return SIF_OK;
+  }
+
+  // A finished run removes its checkpoint unless kept; one that failed keeps
+  // it if it holds a finished rung.
+  void finish(int status) {
+    if (!on_disk) return;
+    if (status != SIF_OK && progress) {
+      log_msg(SIF_LOG_LEVEL_INFO, "finder.exodus",
+              "checkpoint: " + path + ": kept, resume the run from it");
+      return;
+    }
+    if (status == SIF_OK && keep) return;
+    if (unlink(path.c_str()) != 0)
+      log_msg(SIF_LOG_LEVEL_WARNING, "finder.exodus",
+              "checkpoint: " + path + ": cannot remove: " + strerror(errno));
+  }
+};
+
 extern "C" {
+
+void sifg_set_halt_after(uint32_t n_rungs) { g_halt_after = n_rungs; }
+
+// sif_finder_exodus_checkpoint_read (src/finder/exodus_checkpoint.c:451-488):
+// a box's voids as saved (no survey frame to move them back from).
+sif_catalogue_t* sif_finder_exodus_checkpoint_read(const char* filepath,
+                                                   sif_finder_exodus_checkpoint_t* header) {
+  if (!filepath) {
+    fail(SIF_ERR_INVALID, "filepath: NULL");
+    return nullptr;
+  }
+  sif_finder_exodus_checkpoint_t h;
+  std::vector<float> radii, cols[4];
+  std::string msg;
+  const int st = checkpoint_load(filepath, h, radii, cols, &msg);
+  if (st != SIF_OK) {
+    fail(st, "checkpoint: " + msg);
+    return nullptr;
+  }
+  HostCatalogue c;
+  c.cx = std::move(cols[0]);
+  c.cy = std::move(cols[1]);
+  c.cz = std::move(cols[2]);
+  c.r = std::move(cols[3]);
+  sif_catalogue_t* cat = make_catalogue(c);
+  if (!cat) {
+    fail(SIF_ERR_ALLOC, "catalogue: cannot allocate");
+    return nullptr;
+  }
+  if (header) *header = h;
+  return cat;
+}
 
 sif_catalogue_t* sif_finder_exodus(sif_grid_t* grid, const sif_chain_mesh_t* mesh,
                                    const sif_real* radii, uint32_t n_radii, sif_real threshold,
@@ -700,10 +870,6 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
       fail(SIF_ERR_INVALID, fmt("checkpoint: %s, with SIF_FINDER_NO_CHECKPOINT set", extras->checkpoint));
       return nullptr;
     }
-    if (extras->checkpoint) {
-      fail(SIF_ERR_UNSUPPORTED, "extras: checkpoints are not supported by the GPU finder");
-      return nullptr;
-    }
     // save_memory changes where the reference keeps the grid's transform, and
     // nothing of the run; the GPU run keeps its own in device memory.
     if (prior) {
@@ -720,6 +886,12 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
     fail(SIF_ERR_RANGE, "mesh: 2^32 particles or more");
     return nullptr;
   }
+  // Where the run starts (run_start, exodus_finder.c:1437-1540): a
+  // checkpoint the caller named and that exists is resumed -- its header must
+  // describe this run -- else the run starts from the prior voids and writes
+  // its first checkpoint now, unless SIF_FINDER_NO_CHECKPOINT.
+  RunCheckpoint ck;
+  if (ck.start(grid, mesh, radii, n_radii, threshold, f, opt, extras) != SIF_OK) return nullptr;
   std::lock_guard<std::mutex> lk(g_mu);
   API_GUARD_BEGIN
   Engine* e = engine();
@@ -767,13 +939,19 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   p.radii.assign(radii, radii + n_radii);
   p.window = g_window;
   p.mesh_ready = e->ev_mesh_ready();
-  if (prior && prior->n_voids) {
-    p.prior_cx = prior->cx;
-    p.prior_cy = prior->cy;
-    p.prior_cz = prior->cz;
-    p.prior_r = prior->radii;
-    p.n_prior = prior->n_voids;
+  if (!ck.voids[0].empty()) {
+    p.prior_cx = ck.voids[0].data();
+    p.prior_cy = ck.voids[1].data();
+    p.prior_cz = ck.voids[2].data();
+    p.prior_r = ck.voids[3].data();
+    p.n_prior = ck.voids[0].size();
   }
+  p.first_rung = ck.first_rung;
+  if (ck.active)
+    p.after_rung = [&](uint32_t done, const float* cx, const float* cy, const float* cz,
+                       const float* r, uint32_t nv, uint64_t mismatched) {
+      return ck.rung(done, cx, cy, cz, r, nv, mismatched, s);
+    };
   float* consume = nullptr;
   if (opt & SIF_FINDER_CONSUME_GRID) consume = (float*)bufs().px.ensure(gb);
   p.consume_out = consume;
@@ -782,6 +960,7 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   g_stats.clear();
   const int st = e->exodus(dg, m, p, cat, &g_stats, &tm);
   record_timings(tm);
+  ck.finish(st);
   if (st != SIF_OK) return nullptr;
   // The grid handed back: untouched, which restores it exactly; under
   // SIF_FINDER_CONSUME_GRID it holds the last rung's smoothing, as the

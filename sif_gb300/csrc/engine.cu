@@ -505,7 +505,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
         below[k].flat = grow_to<uint32_t>(below_flat_[k], cells);
       }
     smoother.forward(d_delta, p.contrast_mean);
-    if (!radii.empty()) smooth_rung(0);
+    if (p.first_rung < radii.size()) smooth_rung(p.first_rung);
   }
 
   // Loop invariants, exodus_finder.c:1629-1632.
@@ -673,7 +673,13 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   auto ms_since = [](clk::time_point t0) {
     return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
   };
-  for (uint32_t ri = 0; ri < radii.size(); ri++) {
+  // Called at each rung's end (after the commit's voids are in the catalogue).
+  auto rung_done = [&](uint32_t done, uint64_t mismatched) -> int {
+    if (!p.after_rung) return kOk;
+    return p.after_rung(done, cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), cat_r_.as<R>(),
+                        n_voids, mismatched);
+  };
+  for (uint32_t ri = p.first_rung; ri < radii.size(); ri++) {
     const auto t_rung = clk::now();
     RungStat rs;
     const R radius = radii[ri];
@@ -725,6 +731,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       if (listed) SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
       rs.rung_ms = ms_since(t_rung);
       if (stats) stats->push_back(rs);
+      if (const int hs = rung_done(ri + 1, 0); hs != kOk) return hs;
       continue;
     }
 
@@ -850,6 +857,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
         return kErrInvalid;
       }
       const uint32_t n_acc = h_counters_[1], n_removed = h_counters_[2];
+      rs.n_mismatched = h_counters_[6];
       std::memcpy(&max_r, &h_counters_[4], sizeof(R));
       if (n_removed) {
         compact_voids(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), cat_r_.as<R>(), dstate, st_);
@@ -865,6 +873,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       rs.n_displaced = n_removed;
       rs.rung_ms = ms_since(t_rung);
       if (stats) stats->push_back(rs);
+      if (const int hs = rung_done(ri + 1, rs.n_mismatched); hs != kOk) return hs;
       continue;
     }
     // Radii reach the top level's reach where the rung enters the extended one.
@@ -933,6 +942,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     rs.n_rescale_fail = h_counters_[4];
     rs.n_overflow = h_counters_[5];
     rs.n_witness = h_counters_[8];
+    rs.n_mismatched = h_counters_[9];
     if (n_acc) {
       R rmax;
       std::memcpy(&rmax, sizeof(R) == 4 ? (void*)&h_counters_[3] : (void*)&h_counters_[6], sizeof(R));
@@ -946,6 +956,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     }
     rs.rung_ms = ms_since(t_rung);
     if (stats) stats->push_back(rs);
+    if (const int hs = rung_done(ri + 1, rs.n_mismatched); hs != kOk) return hs;
   }
 
   if (p.consume_out) {

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <vector>
 
 #include "finder.cuh"
@@ -43,6 +44,16 @@ struct RunParamsT {
   const R* prior_cz = nullptr;
   const R* prior_r = nullptr;
   uint64_t n_prior = 0;
+  // A resumed run: the rungs before this one (largest first) are done, and
+  // their voids are the prior ones. The ladder stays whole: the reach and
+  // the extended reach's levels come from it.
+  uint32_t first_rung = 0;
+  // Called after each rung with the rungs done, the catalogue on the device
+  // (its n_voids voids) and the rung's acceptances at more than twice its
+  // radius, e.g. to write a checkpoint; a status other than SIF_OK ends the
+  // run with that status.
+  std::function<int(uint32_t, const R*, const R*, const R*, const R*, uint32_t, uint64_t)>
+      after_rung;
 };
 using RunParams = RunParamsT<float>;
 
@@ -56,6 +67,7 @@ struct RungStat {
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the rung's sphere growth
   uint64_t n_witness = 0;  // survivors the collision witness refused before growth
   uint64_t n_displaced = 0;  // voids displaced by the rung's acceptances (SIF_FINDER_DISPLACE)
+  uint64_t n_mismatched = 0;  // acceptances at more than twice the rung's radius
 };
 
 struct RunTimings {

@@ -1672,6 +1672,9 @@ __device__ __forceinline__ void commit_pass(const SurvivorsT<R>& sv, const uint3
       out = kAccepted;
       acc[atomicAdd(counters, 1u)] = i;
       store_rmax(counters, r);
+      // More than MISMATCH_RATIO (2) times the rung (exodus_finder.c:233,
+      // 2324-2328): counted for the checkpoint and the run's warning.
+      if (fdiv(r, rc.radius) > R(2.0f)) atomicAdd(counters + 9, 1u);
     } else {
       atomicAdd(counters + kRoundUndecided + slot, 1u);
     }
@@ -2140,9 +2143,10 @@ __device__ void paint_cta(R cx, R cy, R cz, R r, uint32_t* mask, const RungConst
 
 // The commit's state: [0] voids in the catalogue (displaced ones included
 // until the compaction), [1] accepted this rung, [2] displaced this rung,
-// [3] a list overflowed, [4..5] the largest accepted radius (R's bits).
+// [3] a list overflowed, [4..5] the largest accepted radius (R's bits), [6]
+// accepted at more than twice the rung.
 constexpr uint32_t kDispVoids = 0, kDispAccepted = 1, kDispRemoved = 2, kDispOverflow = 3,
-                   kDispMaxR = 4;
+                   kDispMaxR = 4, kDispMismatched = 6;
 constexpr int kDispT = 512;
 
 template <class R>
@@ -2281,6 +2285,7 @@ __global__ void __launch_bounds__(kDispT) displace_commit_kernel(
       vl.head[cell] = (int32_t)v;
       state[kDispVoids] = v + 1;
       state[kDispAccepted]++;
+      if (fdiv(nr, rc.radius) > R(2.0f)) state[kDispMismatched]++;
       if (nr > load_real<R>(state + kDispMaxR)) store_real<R>(state + kDispMaxR, nr);
     }
     paint_cta(ncx, ncy, ncz, fmul(rc.scale, nr), mask, rc, true);

@@ -221,7 +221,8 @@ void commit_init(SurvivorsT<R> s, uint8_t* state, uint32_t* counters, uint32_t m
 
 // The commit's counters: [0] accepted so far (appended to acc); the largest
 // accepted radius as the bits of a float in [3], of a double in [6..7]; [4]
-// rescaling failures, [5] resolve overflows; then two rings of kRoundRing
+// rescaling failures, [5] resolve overflows, [8] witness refusals, [9]
+// acceptances at more than twice the rung's radius; then two rings of kRoundRing
 // slots indexed by round % kRoundRing: the accepted count when the round
 // began (written by the previous round's paint), and the survivors the round
 // left undecided (zeroed by the host before each batch of rounds).
@@ -281,7 +282,8 @@ void append_accepted(SurvivorsT<R> s, const uint32_t* rank, const uint32_t* acc,
 // are displaced (radius negated, sphere cleared, intersecting spheres painted
 // back) and it is appended. state: [0] the catalogue's voids (in and out),
 // [1] accepted, [2] displaced, [3] a list overflowed (cap entries each for
-// conflicts and paints), [4..5] the largest radius (in and out).
+// conflicts and paints), [4..5] the largest radius (in and out), [6]
+// acceptances at more than twice the rung's radius.
 template <class R>
 void displace_commit(SurvivorsT<R> s, const uint32_t* rank, uint32_t m, uint32_t* order,
                      const uint32_t* vstart, uint32_t* vids, int32_t* head, int32_t* next,

@@ -155,40 +155,68 @@ _SEARCH = {1.5: abi.SIF_FINDER_SEARCH_1_50, 1.25: abi.SIF_FINDER_SEARCH_1_25,
            1.75: abi.SIF_FINDER_SEARCH_1_75, 2.0: abi.SIF_FINDER_SEARCH_2_00}
 
 
+def _extras(checkpoint, prior, keep_checkpoint, save_memory, raw):
+    """exodus_extras (python/src/finders/py_finders.c:222-270): checkpoint=
+    None for a name of the run's own, a path, or False for none (the raw
+    entry point only; a variant always checkpoints). Returns (extras or None,
+    extra option bits, objects to keep alive)."""
+    import os
+
+    keep, opt, path = [], 0, None
+    if checkpoint is False and raw:
+        opt = abi.SIF_FINDER_NO_CHECKPOINT
+    elif checkpoint is False:
+        raise ValueError("checkpoint: False (expected a path, or None for a name of the run's "
+                         "own: a variant always checkpoints; exodus_raw() runs without)")
+    elif checkpoint is True:
+        raise ValueError("checkpoint: True (expected a path, None for a name of the run's own, "
+                         "or False for none)")
+    elif checkpoint is not None:
+        path = os.fsencode(checkpoint)
+        keep.append(path)
+    cat = None
+    if prior is not None:
+        cols = [np.ascontiguousarray(c, dtype=np.float32) for c in
+                (prior.as_tuple() if isinstance(prior, Catalogue) else prior)]
+        keep.extend(cols)
+        cat = abi.sif_catalogue_t()
+        cat.cx, cat.cy, cat.cz, cat.radii = (_P(c) for c in cols)
+        cat.units = 0
+        cat.n_voids = cat.capacity = len(cols[0])
+        keep.append(cat)
+    if path is None and cat is None and not keep_checkpoint and not save_memory:
+        return None, opt, keep
+    extras = abi.sif_finder_exodus_extras_t(path, C.pointer(cat) if cat is not None else None,
+                                            int(bool(keep_checkpoint)), int(bool(save_memory)))
+    return extras, opt, keep
+
+
 def _exodus(grid, mesh, radii, threshold, variant="excursion-set", *, checkpoint=None,
             prior=None, keep_checkpoint=False, save_memory=False):
-    """finders.exodus (python/pysif/finders.pyi:37-140)."""
+    """finders.exodus (python/pysif/finders.pyi:37-140): a variant, which
+    checkpoints after every rung (to the named file, which it resumes if it
+    exists, or to a name of its own, removed when the run succeeds)."""
     lib = _lib.load()
     if variant not in _VARIANTS:
         raise ValueError(f"variant: {variant!r}")
     radii = np.ascontiguousarray(radii, dtype=np.float32)
-    if checkpoint:
-        raise NotImplementedError("checkpoints")
-    extras, keep = None, []
-    if prior is not None or save_memory:
-        cat = None
-        if prior is not None:
-            cols = [np.ascontiguousarray(c, dtype=np.float32) for c in
-                    (prior.as_tuple() if isinstance(prior, Catalogue) else prior)]
-            keep.extend(cols)
-            cat = abi.sif_catalogue_t()
-            cat.cx, cat.cy, cat.cz, cat.radii = (_P(c) for c in cols)
-            cat.units = 0
-            cat.n_voids = cat.capacity = len(cols[0])
-            keep.append(cat)
-        extras = abi.sif_finder_exodus_extras_t(None, C.pointer(cat) if cat is not None else None,
-                                                int(keep_checkpoint), int(bool(save_memory)))
+    extras, _, keep = _extras(checkpoint, prior, keep_checkpoint, save_memory, raw=False)
     ptr = lib.sif_finder_exodus(grid._ptr, mesh._ptr, _P(radii), len(radii), threshold,
                                 _VARIANTS[variant], C.byref(extras) if extras is not None else None)
+    del keep
     return _take_catalogue(lib, ptr, "exodus")
 
 
 def _exodus_raw(grid, mesh, radii, threshold, overlap_fraction=0.0, *, overlap_type="eulerian",
-                search_factor=1.5, deconvolution="full", consume_grid=False, checkpoint=False):
-    """finders.exodus_raw, for the options the GPU finder runs."""
+                search_factor=1.5, deconvolution="full", consume_grid=False, seeds="cells",
+                extend_reach=False, displace=False, checkpoint=False, prior=None,
+                keep_checkpoint=False, save_memory=False):
+    """finders.exodus_raw, for the options the GPU finder runs; checkpoint=
+    False (the default here) runs without one."""
     lib = _lib.load()
     radii = np.ascontiguousarray(radii, dtype=np.float32)
-    opt = _SEARCH[float(search_factor)] | abi.SIF_FINDER_NO_CHECKPOINT
+    extras, opt, keep = _extras(checkpoint, prior, keep_checkpoint, save_memory, raw=True)
+    opt |= _SEARCH[float(search_factor)]
     if overlap_type == "lagrangian":
         opt |= abi.SIF_FINDER_LAGRANGIAN_OVERLAP
     if deconvolution == "none":
@@ -197,9 +225,31 @@ def _exodus_raw(grid, mesh, radii, threshold, overlap_fraction=0.0, *, overlap_t
         opt |= abi.SIF_FINDER_ALIASING_WINDOW
     if consume_grid:
         opt |= abi.SIF_FINDER_CONSUME_GRID
+    if seeds == "minima":
+        opt |= abi.SIF_FINDER_SEEDS_MINIMA
+    elif seeds != "cells":
+        raise ValueError(f"seeds must be 'cells' or 'minima', not {seeds!r}")
+    if extend_reach:
+        opt |= abi.SIF_FINDER_EXTEND_REACH
+    if displace:
+        opt |= abi.SIF_FINDER_DISPLACE
     ptr = lib.sif_finder_exodus_raw(grid._ptr, mesh._ptr, _P(radii), len(radii), threshold,
-                                    overlap_fraction, opt, None)
+                                    overlap_fraction, opt,
+                                    C.byref(extras) if extras is not None else None)
+    del keep
     return _take_catalogue(lib, ptr, "exodus_raw")
+
+
+def checkpoint_read(path):
+    """sif_finder_exodus_checkpoint_read: (Catalogue, header fields as a dict)."""
+    import os
+
+    lib = _lib.load()
+    h = abi.sif_finder_exodus_checkpoint_t()
+    ptr = lib.sif_finder_exodus_checkpoint_read(os.fsencode(path), C.byref(h))
+    cat = _take_catalogue(lib, ptr, "checkpoint_read")
+    return cat, {f: getattr(h, f) for f, _ in abi.sif_finder_exodus_checkpoint_t._fields_
+                 if f not in ("magic", "reserved", "offset")}
 
 
 def _suggest_mesh_cells(n_particles, box_length, max_radius=0.0, volume=0.0):
@@ -221,7 +271,8 @@ def _suggest_mesh_cells(n_particles, box_length, max_radius=0.0, volume=0.0):
 
 
 finders = types.SimpleNamespace(exodus=_exodus, exodus_raw=_exodus_raw,
-                                suggest_mesh_cells=_suggest_mesh_cells)
+                                suggest_mesh_cells=_suggest_mesh_cells,
+                                checkpoint_read=checkpoint_read)
 
 
 def smoothed_contrast(x, y, z, n_grid, box, radius, filter="gaussian", window="full"):

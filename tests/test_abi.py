@@ -232,3 +232,81 @@ def test_init_without_a_gpu_fails_loudly(lib):
     cfg = abi.sif_config_t(None, None, abi.SIF_LOG_LEVEL_NONE, None, 0)
     assert lib.sif_system_init(C.byref(cfg)) == abi.SIF_ERR_UNSUPPORTED
     assert b"GPU" in lib.sif_error_message()
+
+
+def _ref_checkpoint(tmp_path, halt=9):
+    """A checkpoint the reference writes: the golden box's run stopped after
+    `halt` rungs by its own test hook (sif__exodus_halt_after_set)."""
+    import numpy as np
+
+    import ref_ctypes as R
+    from sif_gb300 import synth
+
+    lib = R.load("strict", 4, abi_mod().SIF_LOG_LEVEL_NONE)
+    x, y, z = synth.zeldovich(32, 128.0, 4.0, 11)
+    f = R.RefField(lib, x, y, z)
+    g = R.RefGrid(lib, 32, 128.0)
+    g.assign_cic(f)
+    g.to_contrast()
+    m = R.RefMesh(lib, 8, 128.0, f)
+    radii = synth.ladder(8.0, 24.0, 0.1).astype(np.float32)
+    path = str(tmp_path / "ref.ckpt")
+    extras = abi_mod().sif_finder_exodus_extras_t(path.encode(), None, 1, 0)
+    lib.sif__exodus_halt_after_set.argtypes = [C.c_uint32]
+    lib.sif__exodus_halt_after_set(halt)
+    try:
+        cat = lib.sif_finder_exodus_raw(g.ptr, m.ptr, radii.ctypes.data, len(radii), -0.7, 0.0, 0,
+                                        C.byref(extras))
+    finally:
+        lib.sif__exodus_halt_after_set(0)
+    assert not cat  # halted: the run fails, the checkpoint stays
+    h = abi_mod().sif_finder_exodus_checkpoint_t()
+    want = lib.sif_finder_exodus_checkpoint_read(path.encode(), C.byref(h))
+    assert want
+    cols = R.catalogue_arrays(lib, want)
+    m.free()
+    g.free()
+    f.free()
+    return path, h, cols
+
+
+def abi_mod():
+    from sif_gb300 import abi
+
+    return abi
+
+
+@pytest.mark.skipif("not __import__('ref_ctypes').available()")
+def test_reads_the_reference_checkpoint(lib, tmp_path):
+    """The XCKP v3 file (include/sif/finder/exodus_finder.h:409-507) the
+    reference writes is read by this library as the reference reads it: the
+    same header, the same voids; its CRC-32 is zlib's; a corrupted byte or a
+    truncated file is refused."""
+    import zlib
+
+    import numpy as np
+
+    from sif_gb300 import abi
+
+    path, want_h, want = _ref_checkpoint(tmp_path)
+    h = abi.sif_finder_exodus_checkpoint_t()
+    got = lib.sif_finder_exodus_checkpoint_read(path.encode(), C.byref(h))
+    assert got
+    c = got.contents
+    cols = [np.ctypeslib.as_array(p, shape=(c.n_voids,)).copy() for p in (c.cx, c.cy, c.cz, c.radii)]
+    lib.sif_catalogue_free(got)
+    assert bytes(h) == bytes(want_h)
+    assert h.next_rung == 9 and h.n_voids == len(want[0]) > 0
+    assert all(np.array_equal(a, b) for a, b in zip(cols, want))
+    raw = bytearray(open(path, "rb").read())
+    body = bytearray(raw)
+    body[132:136] = b"\0\0\0\0"  # the header's crc32 field, zeroed
+    assert zlib.crc32(bytes(body)) == h.crc32
+    bad = tmp_path / "bad.ckpt"
+    raw[-3] ^= 0x40
+    bad.write_bytes(bytes(raw))
+    assert not lib.sif_finder_exodus_checkpoint_read(str(bad).encode(), None)
+    assert b"checksum" in lib.sif_error_message()
+    bad.write_bytes(bytes(raw[:-4]))
+    assert not lib.sif_finder_exodus_checkpoint_read(str(bad).encode(), None)
+    assert b"bytes" in lib.sif_error_message()
