@@ -245,6 +245,13 @@ sif_field_t* sif_field_alloc(uint64_t n_particles);
 void sif_field_free(sif_field_t* field);
 int sif_field_assign_positions(sif_field_t* field, const sif_real* x, const sif_real* y,
                                const sif_real* z);
+/* include/sif/structures/field.h:188, 231: the weight column (uninitialised,
+ * or copied from the caller's array in the field's particle order). A
+ * weighted field deposits its weights (sif_grid_assign_cic) and gives a
+ * weighted mesh (weights in mesh order, cell_weights, total_weight), which
+ * the finder measures against the mean weight density. */
+int sif_field_reserve_weights(sif_field_t* field);
+int sif_field_assign_weights(sif_field_t* field, const sif_real* weights);
 
 /* include/sif/structures/grid.h:140, 147, 212, 233 */
 sif_grid_t* sif_grid_alloc(uint32_t n_cells, sif_real box_length);
@@ -431,6 +438,45 @@ int sifg_box_device_f64(const double* x, const double* y, const double* z, uint6
                         uint32_t n_radii, double threshold, double overlap, uint32_t opt,
                         double* cx, double* cy, double* cz, double* r, uint64_t capacity,
                         uint64_t* n_voids);
+/* Weighted meshes on the device (the reference's sif_field_assign_weights
+ * path, for device data; float and FP64 forms). sifg_cic_weighted_device: the
+ * CIC density of weighted particles (w: one weight each, device).
+ * sifg_mesh_weights_device: a mesh's weight columns from the field's
+ * weights (source order) and the mesh's offsets and source indices (from
+ * sifg_mesh_device with orig): w (mesh order), cell_w (n_cells^3 per-cell
+ * sums), *total_weight (host). sifg_exodus_weighted_device: sifg_exodus_device
+ * on a weighted mesh (its w, cell_w and total_weight added after offsets):
+ * the weights must be finite and non-negative (SIF_ERR_INVALID otherwise),
+ * the density tests measure against the mean weight density. */
+int sifg_cic_weighted_device(const float* x, const float* y, const float* z, const float* w,
+                             uint64_t n, uint32_t n_grid, float box, float* grid);
+int sifg_cic_weighted_device_f64(const double* x, const double* y, const double* z,
+                                 const double* w, uint64_t n, uint32_t n_grid, double box,
+                                 double* grid);
+int sifg_mesh_weights_device(const float* field_w, const uint32_t* orig, uint64_t n,
+                             const uint32_t* offsets, uint32_t n_cells, float* w, float* cell_w,
+                             double* total_weight);
+int sifg_mesh_weights_device_f64(const double* field_w, const uint32_t* orig, uint64_t n,
+                                 const uint32_t* offsets, uint32_t n_cells, double* w,
+                                 double* cell_w, double* total_weight);
+int sifg_exodus_weighted_device(const float* delta, uint32_t n_grid, float box, const float* mx,
+                                const float* my, const float* mz, const uint32_t* offsets,
+                                const float* w, const float* cell_w, double total_weight,
+                                uint64_t n_particles, uint32_t mesh_cells, const float* radii,
+                                uint32_t n_radii, float threshold, float overlap, uint32_t opt,
+                                const float* inject, const float* prior, uint64_t n_prior,
+                                float* cx, float* cy, float* cz, float* r, uint64_t capacity,
+                                uint64_t* n_voids);
+int sifg_exodus_weighted_device_f64(const double* delta, uint32_t n_grid, double box,
+                                    const double* mx, const double* my, const double* mz,
+                                    const uint32_t* offsets, const double* w,
+                                    const double* cell_w, double total_weight,
+                                    uint64_t n_particles, uint32_t mesh_cells,
+                                    const double* radii, uint32_t n_radii, double threshold,
+                                    double overlap, uint32_t opt, const double* inject,
+                                    const double* prior, uint64_t n_prior, double* cx,
+                                    double* cy, double* cz, double* r, uint64_t capacity,
+                                    uint64_t* n_voids);
 /* The adjoint of the CIC density contrast (sifg_cic_device followed by
  * sifg_contrast_device) with respect to the positions: given g = dL/d(delta)
  * on the n_grid^3 device grid, writes dL/dx, dL/dy, dL/dz of every particle

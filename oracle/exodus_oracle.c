@@ -196,6 +196,40 @@ int orc_chain_mesh(const float* x, const float* y, const float* z, uint64_t n,
   return 0;
 }
 
+/* The mesh's weight columns, chain_mesh.c:800-801 (a tracer's weight moves
+ * with it, so in mesh order it is the field's at the source index) and
+ * chain_mesh_sum_weights, 624-672: per cell a double sum in mesh order,
+ * stored as float; the total over 64 fixed blocks of cells, each a serial
+ * double sum of its cells', added in block order. */
+void orc_mesh_weights(const float* field_w, const uint64_t* orig, uint64_t n,
+  const uint64_t* offsets, uint32_t n_cells, float* out_w, float* out_cell_w,
+  double* total) {
+  for (uint64_t p = 0; p < n; p++)
+    out_w[p] = field_w[orig[p]];
+  enum { WEIGHT_BLOCKS = 64 };
+  const uint64_t cells = (uint64_t)n_cells * n_cells * n_cells;
+  const uint64_t block = (cells + WEIGHT_BLOCKS - 1) / WEIGHT_BLOCKS;
+  double bt[WEIGHT_BLOCKS];
+#pragma omp parallel for schedule(static, 1)
+  for (int b = 0; b < WEIGHT_BLOCKS; b++) {
+    const uint64_t c0 = (uint64_t)b * block;
+    const uint64_t c1 = c0 + block < cells ? c0 + block : cells;
+    double sum = 0.0;
+    for (uint64_t c = c0; c < c1; c++) {
+      double cell = 0.0;
+      for (uint64_t p = offsets[c]; p < offsets[c + 1]; p++)
+        cell += (double)out_w[p];
+      out_cell_w[c] = (float)cell;
+      sum += cell;
+    }
+    bt[b] = sum;
+  }
+  double t = 0.0;
+  for (int b = 0; b < WEIGHT_BLOCKS; b++)
+    t += bt[b];
+  *total = t;
+}
+
 /* ------------------------------------------------------------------------ */
 /* CIC and the density contrast                                             */
 /* ------------------------------------------------------------------------ */
@@ -220,6 +254,11 @@ static void cic_f64_base(float v, float box, double idx, uint32_t N, uint32_t* i
 
 void orc_cic_f64(const float* x, const float* y, const float* z, uint64_t n,
   uint32_t N, float box, double* out) {
+  orc_cic_f64_w(x, y, z, NULL, n, N, box, out);
+}
+
+void orc_cic_f64_w(const float* x, const float* y, const float* z, const float* ws,
+  uint64_t n, uint32_t N, float box, double* out) {
   const uint64_t total = (uint64_t)N * N * N;
   const uint64_t plane = (uint64_t)N * N;
   const double idx = (double)N / (double)box;
@@ -292,7 +331,8 @@ void orc_cic_f64(const float* x, const float* y, const float* z, uint64_t n,
             for (int c = 0; c < 2; c++) {
               const uint64_t cell = (uint64_t)(a ? i1[0] : i0[0]) * plane +
                                     (uint64_t)(b ? i1[1] : i0[1]) * N + (c ? i1[2] : i0[2]);
-              out[cell] += (a ? w1[0] : w0[0]) * (b ? w1[1] : w0[1]) * (c ? w1[2] : w0[2]);
+              out[cell] += (a ? w1[0] : w0[0]) * (b ? w1[1] : w0[1]) * (c ? w1[2] : w0[2]) *
+                           (ws ? (double)ws[p] : 1.0);
             }
       }
     }
@@ -322,6 +362,14 @@ void orc_cic_f64(const float* x, const float* y, const float* z, uint64_t n,
 
 void orc_cic_float(const float* xs, const float* ys, const float* zs, uint64_t n,
   uint32_t N, float box, float* grid) {
+  orc_cic_float_w(xs, ys, zs, NULL, n, N, box, grid);
+}
+
+/* The same with per-particle weights (NULL: 1 each), which enter as the
+ * reference's do (grid.c:635-639): the weight times each z factor, then the
+ * (x, y) products times those. */
+void orc_cic_float_w(const float* xs, const float* ys, const float* zs, const float* ws,
+  uint64_t n, uint32_t N, float box, float* grid) {
   const float idx = (float)N / (float)box;
   int32_t n_slabs = (int32_t)(N / CIC_SLAB_WIDTH);
   if (n_slabs < 1)
@@ -398,7 +446,8 @@ void orc_cic_float(const float* xs, const float* ys, const float* zs, uint64_t n
         const float wx0 = 1.0f - tx, wx1 = tx, wy0 = 1.0f - ty, wy1 = ty;
         const float wz0 = 1.0f - tz, wz1 = tz;
         const float w00 = wx0 * wy0, w01 = wx0 * wy1, w10 = wx1 * wy0, w11 = wx1 * wy1;
-        const float mz0 = 1.0f * wz0, mz1 = 1.0f * wz1;
+        const float pw = ws ? ws[p] : 1.0f;
+        const float mz0 = pw * wz0, mz1 = pw * wz1;
         v[l0 + (uint64_t)iy * N + iz] += w00 * mz0;
         v[l0 + (uint64_t)iy * N + iz1] += w00 * mz1;
         v[l0 + (uint64_t)iy1 * N + iz] += w01 * mz0;
@@ -1013,6 +1062,15 @@ static inline int query_cell(const query_t* q, uint32_t i, uint64_t* s,
   return *e > *s;
 }
 
+/* The flat index of the cell query_cell() wraps template entry i into. */
+static inline uint64_t query_flat(const query_t* q, uint32_t i) {
+  const int32_t N = (int32_t)q->m->n_cells;
+  int32_t a[3] = {q->ix + q->t->dx[i], q->iy + q->t->dy[i], q->iz + q->t->dz[i]};
+  for (int k = 0; k < 3; k++)
+    a[k] = a[k] < 0 ? a[k] + N : (a[k] >= N ? a[k] - N : a[k]);
+  return (uint64_t)a[0] * N * N + (uint64_t)a[1] * N + (uint64_t)a[2];
+}
+
 /* dist2, src/finder/exodus_rescale.c:349-355. */
 static inline float dist2(float px, float py, float pz, float cx, float cy, float cz) {
   const float dx = px - cx;
@@ -1036,13 +1094,58 @@ static int cmp_float(const void* a, const void* b) {
   return (x > y) - (x < y);
 }
 
-/* resolve_bin, src/finder/exodus_rescale.c:391-507 (unweighted). The
+/* A weighted refinement entry (exodus_internal.h:84-88) and the reference's
+ * three-way quicksort over them by d2 ascending (sort_pairs_asc,
+ * exodus_rescale.c:29, the SIF_DEFINE_QUICKSORT of include/sif/utils/
+ * sort.h:56-98): middle pivot, the same swaps, so ties of d2 come out in the
+ * reference's order and the double walk subtracts their weights in its order. */
+typedef struct {
+  float d2;
+  float w;
+} pair_t;
+
+static void pairs_partition(pair_t* a, int64_t lo, int64_t hi, int64_t* lt_out,
+  int64_t* gt_out) {
+  int64_t lt = lo, gt = hi, i = lo;
+  const pair_t pivot = a[lo + (hi - lo) / 2];
+  while (i <= gt) {
+    if (a[i].d2 < pivot.d2) {
+      const pair_t t = a[lt];
+      a[lt] = a[i];
+      a[i] = t;
+      lt++;
+      i++;
+    } else if (pivot.d2 < a[i].d2) {
+      const pair_t t = a[i];
+      a[i] = a[gt];
+      a[gt] = t;
+      gt--;
+    } else {
+      i++;
+    }
+  }
+  *lt_out = lt;
+  *gt_out = gt;
+}
+
+static void pairs_sort(pair_t* a, int64_t lo, int64_t hi) {
+  if (lo >= hi)
+    return;
+  int64_t lt, gt;
+  pairs_partition(a, lo, hi, &lt, &gt);
+  pairs_sort(a, lo, lt - 1);
+  pairs_sort(a, gt + 1, hi);
+}
+
+/* resolve_bin, src/finder/exodus_rescale.c:391-507. Unweighted, the
  * collected distances are equal values wherever they tie, so any ascending
- * sort gives the reference's sequence. */
+ * sort gives the reference's sequence; weighted, the pairs are sorted as the
+ * reference sorts them. cur_w is the weight at or below the window's top. */
 static int resolve(const query_t* q, uint32_t blo, uint32_t bhi, float lo,
   float hi, float rc2, float rs2, float inv_w, uint32_t nb, uint64_t cur_n,
-  float K2, float* out, float** buf, uint64_t* cap) {
+  double cur_w, float K2, float* out, void** buf, uint64_t* cap, int weighted) {
   const orc_template_t* t = q->t;
+  const size_t esz = weighted ? sizeof(pair_t) : sizeof(float);
   uint64_t count = 0;
   for (uint32_t i = 0; i < t->count; i++) {
     const uint8_t type = t->type[i];
@@ -1055,7 +1158,7 @@ static int resolve(const query_t* q, uint32_t blo, uint32_t bhi, float lo,
     if (count + (e - s) > *cap) {
       while (count + (e - s) > *cap)
         *cap *= 2;
-      *buf = realloc(*buf, *cap * sizeof(float));
+      *buf = realloc(*buf, *cap * esz);
     }
     for (uint64_t p = s; p < e; p++) {
       const float d2 = dist2(q->m->x[p], q->m->y[p], q->m->z[p], ex, ey, ez);
@@ -1064,13 +1167,38 @@ static int resolve(const query_t* q, uint32_t blo, uint32_t bhi, float lo,
       const uint32_t bi = bin_of(d2, rc2, inv_w, nb);
       if (bi < blo || bi > bhi)
         continue;
-      (*buf)[count++] = d2;
+      if (weighted)
+        ((pair_t*)*buf)[count++] = (pair_t){d2, q->m->w[p]};
+      else
+        ((float*)*buf)[count++] = d2;
     }
   }
+  if (weighted) {
+    pair_t* pr = (pair_t*)*buf;
+    if (count > 1)
+      pairs_sort(pr, 0, (int64_t)count - 1);
+    for (int64_t k = (int64_t)count - 1; k >= 0; k--) {
+      const float d2 = pr[k].d2;
+      const double wt = (double)pr[k].w;
+      if (d2 == 0.0f) {
+        cur_w -= wt;
+        continue;
+      }
+      const float w_in = (float)(cur_w - wt);
+      const float d2c = d2 * d2 * d2;
+      if (w_in * w_in <= K2 * d2c) {
+        *out = sqrtf(d2);
+        return 1;
+      }
+      cur_w -= wt;
+    }
+    return 0;
+  }
+  float* fb = (float*)*buf;
   if (count > 1)
-    qsort(*buf, count, sizeof(float), cmp_float);
+    qsort(fb, count, sizeof(float), cmp_float);
   for (int64_t k = (int64_t)count - 1; k >= 0; k--) {
-    const float d2 = (*buf)[k];
+    const float d2 = fb[k];
     if (d2 == 0.0f) {
       cur_n--;
       continue;
@@ -1087,18 +1215,23 @@ static int resolve(const query_t* q, uint32_t blo, uint32_t bhi, float lo,
   return 0;
 }
 
-/* find_exact_radius_impl, src/finder/exodus_rescale.c:642-1012, unweighted
- * (mass_factor = vol_factor). */
-float orc_find_radius(const orc_mesh_t* m, const orc_template_t* t, float cx,
-  float cy, float cz, float r_search, float threshold, float vol_factor,
-  float rmin, uint32_t window, uint8_t* reason, uint64_t* span_sum,
-  uint64_t* span_count) {
+/* find_exact_radius_impl, src/finder/exodus_rescale.c:642-1012. Weighted
+ * (the mesh's w set), every count is a double sum of weights taken in the
+ * reference's order -- whole cells from cell_w, the rest tracer by tracer --
+ * and the density tests use mass_factor; vol_factor still sizes the
+ * histogram. */
+static float find_radius_impl(const orc_mesh_t* m, const orc_template_t* t, float cx,
+  float cy, float cz, float r_search, float threshold, float vol_factor, float mass_factor,
+  float rmin, uint32_t window, uint8_t* reason, uint64_t* span_sum, uint64_t* span_count,
+  int weighted) {
   *reason = ORC_RESCALE_OK;
   const float inv_l = 1.0f / m->cell_length;
   const query_t q = {m, t, cx, cy, cz, (int32_t)(cx * inv_l),
     (int32_t)(cy * inv_l), (int32_t)(cz * inv_l)};
   const float rs2 = r_search * r_search;
   const float rc2 = rmin * rmin;
+  const float* mw = m->w;
+  const float* cw = m->cell_w;
 
   const float span = rs2 - rc2;
   uint32_t nb = 2048u;
@@ -1118,8 +1251,9 @@ float orc_find_radius(const orc_mesh_t* m, const orc_template_t* t, float cx,
 
   /* The early refusal, 738-782. */
   {
-    const float expected = vol_factor * r_search * r_search * r_search;
+    const float expected = mass_factor * r_search * r_search * r_search;
     uint64_t within = 0;
+    double w_within = 0.0;
     for (uint32_t i = 0; i < t->count; i++) {
       const uint8_t type = t->type[i];
       uint64_t s, e;
@@ -1127,17 +1261,28 @@ float orc_find_radius(const orc_mesh_t* m, const orc_template_t* t, float cx,
       if (!query_cell(&q, i, &s, &e, &ex, &ey, &ez))
         continue;
       if (type == CELL_CORE || type == CELL_SHELL) {
-        within += e - s;
+        if (weighted) {
+          w_within += (double)cw[query_flat(&q, i)];
+        } else {
+          within += e - s;
+        }
         continue;
       }
-      for (uint64_t p = s; p < e; p++)
-        within += dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez) <= rs2;
+      if (weighted) {
+        for (uint64_t p = s; p < e; p++)
+          if (dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez) <= rs2)
+            w_within += (double)mw[p];
+      } else {
+        for (uint64_t p = s; p < e; p++)
+          within += dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez) <= rs2;
+      }
     }
-    if (within == 0) {
+    if (weighted ? !(w_within > 0.0) : within == 0) {
       *reason = ORC_RESCALE_EMPTY;
       return -1.0f;
     }
-    if (((float)within / expected) - 1.0f <= threshold) {
+    const float wf = weighted ? (float)w_within : (float)within;
+    if ((wf / expected) - 1.0f <= threshold) {
       *reason = ORC_RESCALE_BEYOND_SEARCH;
       return -1.0f;
     }
@@ -1146,7 +1291,9 @@ float orc_find_radius(const orc_mesh_t* m, const orc_template_t* t, float cx,
   const float inv_w = (float)nb / span;
   const float bin_w = span / (float)nb;
   uint32_t* bins = calloc(nb, sizeof(uint32_t));
+  double* wbins = calloc(nb, sizeof(double));
   uint64_t n_core = 0, n_shell = 0;
+  double w_core = 0.0, w_shell = 0.0;
   for (uint32_t i = 0; i < t->count; i++) {
     const uint8_t type = t->type[i];
     uint64_t s, e;
@@ -1154,56 +1301,88 @@ float orc_find_radius(const orc_mesh_t* m, const orc_template_t* t, float cx,
     if (!query_cell(&q, i, &s, &e, &ex, &ey, &ez))
       continue;
     if (type == CELL_CORE) {
-      n_core += e - s;
+      if (weighted) {
+        w_core += (double)cw[query_flat(&q, i)];
+      } else {
+        n_core += e - s;
+      }
     } else if (type == CELL_SHELL) {
-      for (uint64_t p = s; p < e; p++)
-        bins[bin_of(dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez), rc2, inv_w, nb)]++;
-      n_shell += e - s;
+      for (uint64_t p = s; p < e; p++) {
+        const uint32_t b = bin_of(dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez), rc2, inv_w, nb);
+        if (weighted) {
+          wbins[b] += (double)mw[p];
+          w_shell += (double)mw[p];
+        } else {
+          bins[b]++;
+        }
+      }
+      if (!weighted)
+        n_shell += e - s;
     } else {
       for (uint64_t p = s; p < e; p++) {
         const float d2 = dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez);
-        n_core += d2 <= rc2;
-        if (d2 > rc2 && d2 <= rs2) {
-          bins[bin_of(d2, rc2, inv_w, nb)]++;
-          n_shell++;
+        if (weighted) {
+          const double wt = (double)mw[p];
+          if (d2 <= rc2) {
+            w_core += wt;
+          } else if (d2 <= rs2) {
+            wbins[bin_of(d2, rc2, inv_w, nb)] += wt;
+            w_shell += wt;
+          }
+        } else {
+          n_core += d2 <= rc2;
+          if (d2 > rc2 && d2 <= rs2) {
+            bins[bin_of(d2, rc2, inv_w, nb)]++;
+            n_shell++;
+          }
         }
       }
     }
   }
 
   const uint64_t total = n_core + n_shell;
-  if (total == 0) {
+  const double total_w = w_core + w_shell;
+  if (weighted ? !(total_w > 0.0) : total == 0) {
     free(bins);
+    free(wbins);
     *reason = ORC_RESCALE_EMPTY;
     return -1.0f;
   }
   {
-    const float expected = vol_factor * r_search * r_search * r_search;
-    if (((float)total / expected) - 1.0f <= threshold) {
+    const float expected = mass_factor * r_search * r_search * r_search;
+    const float tf = weighted ? (float)total_w : (float)total;
+    if ((tf / expected) - 1.0f <= threshold) {
       free(bins);
+      free(wbins);
       *reason = ORC_RESCALE_BEYOND_SEARCH;
       return -1.0f;
     }
   }
 
-  const float K = (threshold + 1.0f) * vol_factor;
+  const float K = (threshold + 1.0f) * mass_factor;
   const float K2 = K * K;
   uint64_t above = 0;
+  double above_w = 0.0;
   int32_t b_first = -1;
   uint64_t cap = 4096;
-  float* buf = malloc(cap * sizeof(float));
+  void* buf = malloc(cap * (weighted ? sizeof(pair_t) : sizeof(float)));
   float result = -1.0f;
   *reason = ORC_RESCALE_BELOW_RUNG;
   for (int32_t b = (int32_t)nb - 1; b >= 0; b--) {
-    const uint32_t count = bins[b];
-    if (count == 0)
+    const uint32_t count = weighted ? 0u : bins[b];
+    const double count_w = weighted ? wbins[b] : 0.0;
+    if (weighted ? !(count_w > 0.0) : count == 0)
       continue;
     float hi = rc2 + (float)(b + 1) * bin_w;
     if (b == (int32_t)nb - 1)
       hi = rs2 * (1.0f + 1e-6f);
-    const float n_in_min = (float)(total - above - count);
+    const float n_in_min =
+      weighted ? (float)(total_w - above_w - count_w) : (float)(total - above - count);
     if (n_in_min * n_in_min > K2 * hi * hi * hi) {
-      above += count;
+      if (weighted)
+        above_w += count_w;
+      else
+        above += count;
       continue;
     }
     if (b_first < 0)
@@ -1212,12 +1391,17 @@ float orc_find_radius(const orc_mesh_t* m, const orc_template_t* t, float cx,
     if (b_lo < 0)
       b_lo = 0;
     uint64_t wcount = 0;
-    for (int32_t bb = b_lo; bb <= b; bb++)
-      wcount += bins[bb];
+    double wsum = 0.0;
+    for (int32_t bb = b_lo; bb <= b; bb++) {
+      if (weighted)
+        wsum += wbins[bb];
+      else
+        wcount += bins[bb];
+    }
     const float win_lo = rc2 + (float)b_lo * bin_w;
     float r = -1.0f;
     if (resolve(&q, (uint32_t)b_lo, (uint32_t)b, win_lo, hi, rc2, rs2, inv_w, nb,
-          total - above, K2, &r, &buf, &cap)) {
+          total - above, total_w - above_w, K2, &r, &buf, &cap, weighted)) {
       const int32_t b_found = (int32_t)bin_of(r * r, rc2, inv_w, nb);
       int32_t reached = b_first - b_found + 1;
       if (reached < 1)
@@ -1230,12 +1414,32 @@ float orc_find_radius(const orc_mesh_t* m, const orc_template_t* t, float cx,
       *reason = ORC_RESCALE_OK;
       break;
     }
-    above += wcount;
+    if (weighted)
+      above_w += wsum;
+    else
+      above += wcount;
     b = b_lo;
   }
   free(buf);
   free(bins);
+  free(wbins);
   return result;
+}
+
+float orc_find_radius(const orc_mesh_t* m, const orc_template_t* t, float cx,
+  float cy, float cz, float r_search, float threshold, float vol_factor,
+  float rmin, uint32_t window, uint8_t* reason, uint64_t* span_sum,
+  uint64_t* span_count) {
+  return find_radius_impl(m, t, cx, cy, cz, r_search, threshold, vol_factor, vol_factor,
+    rmin, window, reason, span_sum, span_count, 0);
+}
+
+float orc_find_radius_weighted(const orc_mesh_t* m, const orc_template_t* t, float cx,
+  float cy, float cz, float r_search, float threshold, float vol_factor,
+  float mass_factor, float rmin, uint32_t window, uint8_t* reason, uint64_t* span_sum,
+  uint64_t* span_count) {
+  return find_radius_impl(m, t, cx, cy, cz, r_search, threshold, vol_factor, mass_factor,
+    rmin, window, reason, span_sum, span_count, 1);
 }
 
 static int cmp_double(const void* a, const void* b) {
@@ -1788,6 +1992,15 @@ static int is_minimum_node(const float* f, uint32_t n, uint64_t i) {
  * phase 1 (pole probe, exact overlap, collision witness, rescaling; in
  * parallel), phase 2 (the sequential commit with its re-checks at the
  * rescaled radius) -- and the batch and window retuning between them. */
+/* The rescaling a run calls for a candidate (exodus_finder.c:2046-2072):
+ * weighted on a weighted mesh. */
+static float grow_one(const orc_mesh_t* m, const orc_template_t* t, float cx, float cy,
+  float cz, float r_search, float threshold, float vol_factor, float mass_factor, float rmin,
+  uint32_t window, uint8_t* reason, uint64_t* span_sum, uint64_t* span_count) {
+  return find_radius_impl(m, t, cx, cy, cz, r_search, threshold, vol_factor, mass_factor,
+    rmin, window, reason, span_sum, span_count, m->w != NULL);
+}
+
 int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in,
   uint32_t n_radii, const orc_exodus_params_t* p, orc_catalogue_t* out,
   orc_rung_stats_t* stats_out) {
@@ -1829,6 +2042,30 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   const float search_factor = factors[(opt >> 12) & 3u];
   const int window_mode = (opt & (1u << 14)) ? 0 : ((opt & (1u << 8)) ? 2 : 1);
 
+  /* A weighted mesh (exodus_finder.c:1316-1319, 1076-1106, 1634-1642): its
+   * weights finite and non-negative (by their bits; a negative zero passes),
+   * their total positive, and the density tests against the mean weight
+   * density. No collision witness on it (1868). */
+  const int weighted = mesh->w != NULL;
+  if (weighted) {
+    if (!mesh->cell_w) {
+      free(radii);
+      return -2;
+    }
+    for (uint64_t i = 0; i < mesh->n_particles; i++) {
+      uint32_t b;
+      memcpy(&b, &mesh->w[i], 4);
+      if (((b >> 23) & 0xFFu) == 0xFFu || ((b >> 31) && (b << 1))) {
+        free(radii);
+        return -2;
+      }
+    }
+    if (!(mesh->total_weight > 0.0)) {
+      free(radii);
+      return -2;
+    }
+  }
+
   orc_spectrum_t* spec = NULL;
   if (!p->inject)
     spec = orc_spectrum_new(delta, N, box, window_mode, p->smoothing_mode);
@@ -1836,6 +2073,8 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   const float box_volume = box * box * box;
   const float mean_density = (float)mesh->n_particles / box_volume;
   const float vol_factor = (4.0f / 3.0f) * PI_F * mean_density;
+  const float mass_factor =
+    weighted ? (4.0f / 3.0f) * PI_F * ((float)mesh->total_weight / box_volume) : vol_factor;
 
   int n_threads = p->n_threads > 0 ? p->n_threads : 1;
 
@@ -2033,7 +2272,7 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
         }
         const double rho =
           collision_radius(&V, max_acc, scale, cx, cy, cz, r_search, witness_min_rj, f, box);
-        if (rho < (double)r_search) {
+        if (!weighted && rho < (double)r_search) {
           float rho2 = (float)(rho * rho * (1.0 + COLLISION_SLACK));
           if (rho2 < rc2)
             rho2 = rc2;
@@ -2045,11 +2284,11 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
         }
         uint8_t reason;
         uint64_t ss = 0, sc = 0;
-        float rr = orc_find_radius(mesh, &tpl, cx, cy, cz, r_search, threshold, vol_factor, rmin,
+        float rr = grow_one(mesh, &tpl, cx, cy, cz, r_search, threshold, vol_factor, mass_factor, rmin,
           p->window > 0 ? (uint32_t)p->window : RESOLVE_INITIAL, &reason, &ss, &sc);
         for (uint32_t e = ext0; e < n_ext && rr < 0.0f && reason == ORC_RESCALE_BEYOND_SEARCH;
              e++)
-          rr = orc_find_radius(mesh, &etpl[e], cx, cy, cz, ext_reach[e], threshold, vol_factor,
+          rr = grow_one(mesh, &etpl[e], cx, cy, cz, ext_reach[e], threshold, vol_factor, mass_factor,
             ext_rmin[e], p->window > 0 ? (uint32_t)p->window : RESOLVE_INITIAL, &reason, &ss, &sc);
         st.n_rescaled++;
         if (rr < 0.0f) {
@@ -2126,7 +2365,7 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
         }
         const double rho = collision_radius(&V, max_acc_frozen, scale, r->cx, r->cy,
           r->cz, r_search, 0.0f, f, box);
-        if (rho < (double)r_search) {
+        if (!weighted && rho < (double)r_search) {
           float rho2 = (float)(rho * rho * (1.0 + COLLISION_SLACK));
           if (rho2 < rc2)
             rho2 = rc2;
@@ -2138,15 +2377,15 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
         }
         uint8_t reason;
         uint64_t ss = 0, sc = 0;
-        r->r = orc_find_radius(mesh, &tpl, r->cx, r->cy, r->cz, r_search, threshold,
-          vol_factor, rmin, window, &reason, &ss, &sc);
+        r->r = grow_one(mesh, &tpl, r->cx, r->cy, r->cz, r_search, threshold,
+          vol_factor, mass_factor, rmin, window, &reason, &ss, &sc);
         span_sum += ss;
         span_count += sc;
         for (uint32_t e = ext0; e < n_ext && r->r < 0.0f && reason == ORC_RESCALE_BEYOND_SEARCH;
              e++) {
           ss = sc = 0;
-          r->r = orc_find_radius(mesh, &etpl[e], r->cx, r->cy, r->cz, ext_reach[e], threshold,
-            vol_factor, ext_rmin[e], window, &reason, &ss, &sc);
+          r->r = grow_one(mesh, &etpl[e], r->cx, r->cy, r->cz, ext_reach[e], threshold,
+            vol_factor, mass_factor, ext_rmin[e], window, &reason, &ss, &sc);
           span_sum += ss;
           span_count += sc;
         }

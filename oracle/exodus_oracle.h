@@ -29,7 +29,20 @@ typedef struct {
   uint32_t n_cells;
   float box_length;
   float cell_length;
+  /* A weighted mesh (sif_chain_mesh_t::weights, cell_weights, total_weight,
+   * include/sif/structures/chain_mesh.h:60-89): per-particle weights in mesh
+   * order, their per-cell sums and their total; w NULL when unweighted. */
+  const float* w;
+  const float* cell_w;
+  double total_weight;
 } orc_mesh_t;
+
+/* The mesh's weight columns (chain_mesh.c:624-672, 800-801): the field's
+ * weights in mesh order through the source-index map, each cell's sum in
+ * double rounded to float, and the total over 64 fixed blocks of cells. */
+void orc_mesh_weights(const float* field_w, const uint64_t* orig, uint64_t n,
+  const uint64_t* offsets, uint32_t n_cells, float* out_w, float* out_cell_w,
+  double* total);
 
 /* Builds a mesh into caller storage (n entries per column, n_cells^3 + 1
  * offsets, optional source-index map). 0, or -2 for invalid input. */
@@ -45,6 +58,11 @@ void orc_cic_f64(const float* x, const float* y, const float* z, uint64_t n,
  * unit volume, its slab and chunk order, so its bits. */
 void orc_cic_float(const float* x, const float* y, const float* z, uint64_t n,
   uint32_t grid_n, float box, float* out);
+/* Both with per-particle weights (NULL: every weight 1), grid.c:635-639. */
+void orc_cic_float_w(const float* x, const float* y, const float* z, const float* w,
+  uint64_t n, uint32_t grid_n, float box, float* out);
+void orc_cic_f64_w(const float* x, const float* y, const float* z, const float* w,
+  uint64_t n, uint32_t grid_n, float box, double* out);
 
 /* The density contrast of an FP64 density in double: 0, or -3 if the mean
  * is not positive. */
@@ -107,6 +125,14 @@ enum {
 float orc_find_radius(const orc_mesh_t* m, const orc_template_t* tpl, float cx,
   float cy, float cz, float r_search, float threshold, float vol_factor,
   float rmin, uint32_t window, uint8_t* reason, uint64_t* span_sum,
+  uint64_t* span_count);
+
+/* sif__exodus_find_radius_weighted (exodus_rescale.c:642-1037 with the
+ * weighted flag): the mesh's weights in every sum, double accumulators in the
+ * reference's order, mass_factor in the density tests. */
+float orc_find_radius_weighted(const orc_mesh_t* m, const orc_template_t* tpl, float cx,
+  float cy, float cz, float r_search, float threshold, float vol_factor,
+  float mass_factor, float rmin, uint32_t window, uint8_t* reason, uint64_t* span_sum,
   uint64_t* span_count);
 
 /* Double-precision brute force over every particle (the definition the

@@ -30,7 +30,8 @@ class Mesh(C.Structure):
     _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
                 ("offsets", C.c_void_p), ("n_particles", C.c_uint64),
                 ("n_cells", C.c_uint32), ("box_length", C.c_float),
-                ("cell_length", C.c_float)]
+                ("cell_length", C.c_float), ("w", C.c_void_p), ("cell_w", C.c_void_p),
+                ("total_weight", C.c_double)]
 
 
 class Template(C.Structure):
@@ -83,6 +84,9 @@ def _declare(L):
     L.orc_chain_mesh.argtypes = [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]
     L.orc_cic_f64.argtypes = [vp, vp, vp, u64, u32, f32, vp]
     L.orc_cic_float.argtypes = [vp, vp, vp, u64, u32, f32, vp]
+    L.orc_cic_f64_w.argtypes = [vp, vp, vp, vp, u64, u32, f32, vp]
+    L.orc_cic_float_w.argtypes = [vp, vp, vp, vp, u64, u32, f32, vp]
+    L.orc_mesh_weights.argtypes = [vp, vp, u64, vp, u32, vp, vp, C.POINTER(C.c_double)]
     L.orc_density_contrast.argtypes = [vp, u64]
     L.orc_density_contrast_f64.argtypes = [vp, u64]
     L.orc_spectrum_new_f64.argtypes = [vp, u32, f32, C.c_int]
@@ -98,6 +102,10 @@ def _declare(L):
                                   f32, f32, f32, f32, u32, C.POINTER(C.c_uint8),
                                   C.POINTER(u64), C.POINTER(u64)]
     L.orc_find_radius.restype = f32
+    L.orc_find_radius_weighted.argtypes = [C.POINTER(Mesh), C.POINTER(Template), f32, f32, f32,
+                                           f32, f32, f32, f32, f32, u32, C.POINTER(C.c_uint8),
+                                           C.POINTER(u64), C.POINTER(u64)]
+    L.orc_find_radius_weighted.restype = f32
     L.orc_brute_force_radius.argtypes = [vp, vp, vp, u64, f32, C.c_double, C.c_double,
                                          C.c_double, C.c_double, C.c_double, C.c_double]
     L.orc_brute_force_radius.restype = C.c_double
@@ -115,9 +123,10 @@ CANDIDATE_DTYPE = np.dtype([("delta", np.float32), ("refined", np.uint32), ("fla
 
 
 class OracleMesh:
-    """A chain mesh built by the oracle; keeps its arrays alive."""
+    """A chain mesh built by the oracle; keeps its arrays alive. weights:
+    per-particle weights in the field's order (a weighted mesh), or None."""
 
-    def __init__(self, x, y, z, n_cells, box):
+    def __init__(self, x, y, z, n_cells, box, weights=None):
         n = len(x)
         self.x = np.empty(n, np.float32)
         self.y = np.empty(n, np.float32)
@@ -133,11 +142,30 @@ class OracleMesh:
         self.n_cells = n_cells
         self.box = np.float32(box)
         self.cell_length = np.float32(np.float32(box) / np.float32(n_cells))
-        self.struct = Mesh(_p(self.x), _p(self.y), _p(self.z), _p(self.offsets), n,
-                           n_cells, float(self.box), float(self.cell_length))
+        self.w = self.cell_w = None
+        self.total_weight = float(n)
+        if weights is not None:
+            fw = np.ascontiguousarray(weights, np.float32)
+            assert fw.shape == (n,)
+            self.w = np.empty(n, np.float32)
+            self.cell_w = np.empty(n_cells ** 3, np.float32)
+            tot = C.c_double()
+            lib().orc_mesh_weights(_p(fw), _p(self.orig), n, _p(self.offsets), n_cells,
+                                   _p(self.w), _p(self.cell_w), C.byref(tot))
+            self.total_weight = tot.value
+        self._make_struct()
+
+    def _make_struct(self):
+        self.struct = Mesh(_p(self.x), _p(self.y), _p(self.z), _p(self.offsets), len(self.x),
+                           self.n_cells, float(self.box), float(self.cell_length),
+                           _p(self.w) if self.w is not None else None,
+                           _p(self.cell_w) if self.cell_w is not None else None,
+                           self.total_weight)
 
     @classmethod
-    def from_arrays(cls, x, y, z, offsets, n_cells, box):
+    def from_arrays(cls, x, y, z, offsets, n_cells, box, w=None, cell_w=None, total_weight=None):
+        """A mesh from its columns (another build's), weighted when w is given
+        (with the per-cell sums and the total)."""
         self = cls.__new__(cls)
         self.x, self.y, self.z = (np.ascontiguousarray(a, np.float32) for a in (x, y, z))
         self.offsets = np.ascontiguousarray(offsets, np.uint64)
@@ -145,23 +173,35 @@ class OracleMesh:
         self.n_cells = n_cells
         self.box = np.float32(box)
         self.cell_length = np.float32(np.float32(box) / np.float32(n_cells))
-        self.struct = Mesh(_p(self.x), _p(self.y), _p(self.z), _p(self.offsets), len(self.x),
-                           n_cells, float(self.box), float(self.cell_length))
+        self.w = None if w is None else np.ascontiguousarray(w, np.float32)
+        self.cell_w = None if cell_w is None else np.ascontiguousarray(cell_w, np.float32)
+        self.total_weight = float(len(self.x)) if total_weight is None else float(total_weight)
+        self._make_struct()
         return self
 
 
-def cic_f64(x, y, z, n_grid, box):
+def _weights_arg(w, n):
+    if w is None:
+        return None, None
+    a = np.ascontiguousarray(w, dtype=np.float32)
+    assert a.shape == (n,)
+    return a, _p(a)
+
+
+def cic_f64(x, y, z, n_grid, box, weights=None):
     out = np.empty(n_grid ** 3, np.float64)
     xs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
-    lib().orc_cic_f64(_p(xs[0]), _p(xs[1]), _p(xs[2]), len(xs[0]), n_grid, box, _p(out))
+    keep, wp = _weights_arg(weights, len(xs[0]))
+    lib().orc_cic_f64_w(_p(xs[0]), _p(xs[1]), _p(xs[2]), wp, len(xs[0]), n_grid, box, _p(out))
     return out
 
 
-def cic_float(x, y, z, n_grid, box):
+def cic_float(x, y, z, n_grid, box, weights=None):
     """The reference's float CIC deposit (its slab and chunk order)."""
     out = np.empty(n_grid ** 3, np.float32)
     xs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
-    lib().orc_cic_float(_p(xs[0]), _p(xs[1]), _p(xs[2]), len(xs[0]), n_grid, box, _p(out))
+    keep, wp = _weights_arg(weights, len(xs[0]))
+    lib().orc_cic_float_w(_p(xs[0]), _p(xs[1]), _p(xs[2]), wp, len(xs[0]), n_grid, box, _p(out))
     return out
 
 

@@ -50,6 +50,7 @@ def load(variant="strict", n_threads=0, log_level=abi.SIF_LOG_LEVEL_ERROR):
                                          C.POINTER(field_t), C.c_uint32]
     lib.sif_field_assign_positions.argtypes = [C.POINTER(field_t),
                                                C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.sif_field_assign_weights.argtypes = [C.POINTER(field_t), C.c_void_p]
     lib.orc_hook_inject.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32]
     lib.orc_hook_capture.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32]
     lib.orc_hook_calls.restype = C.c_uint32
@@ -82,7 +83,7 @@ def _check(lib, ok, what):
 
 
 class RefField:
-    def __init__(self, lib, x, y, z, variant="strict"):
+    def __init__(self, lib, x, y, z, variant="strict", weights=None):
         t = np_real(variant)
         self.lib = lib
         self.x, self.y, self.z = (np.ascontiguousarray(a, dtype=t) for a in (x, y, z))
@@ -90,6 +91,10 @@ class RefField:
         _check(lib, bool(self.ptr), "sif_field_alloc")
         st = lib.sif_field_assign_positions(self.ptr, _ptr(self.x), _ptr(self.y), _ptr(self.z))
         _check(lib, st == 0, "sif_field_assign_positions")
+        if weights is not None:
+            self.w = np.ascontiguousarray(weights, dtype=t)
+            st = lib.sif_field_assign_weights(self.ptr, _ptr(self.w))
+            _check(lib, st == 0, "sif_field_assign_weights")
 
     def free(self):
         if self.ptr:
@@ -151,6 +156,17 @@ class RefMesh:
         if m.original_indices:
             idx = np.ctypeslib.as_array(m.original_indices, shape=(n,)).copy()
         return col(m.x), col(m.y), col(m.z), offs, idx
+
+    def weights(self, variant="strict"):
+        """(weights in mesh order, per-cell sums, total), or None unweighted."""
+        m = self.ptr.contents
+        if not m.weights:
+            return None
+        ct = C.c_double if variant == "f64" else C.c_float
+        w = np.ctypeslib.as_array(C.cast(m.weights, C.POINTER(ct)), shape=(m.n_particles,)).copy()
+        cw = np.ctypeslib.as_array(C.cast(m.cell_weights, C.POINTER(ct)),
+                                   shape=(m.total_cells,)).copy()
+        return w, cw, float(m.total_weight)
 
     def free(self):
         if self.ptr:

@@ -38,6 +38,7 @@ EXPORTED = [
     # sif's API
     "sif_system_init", "sif_system_finalise", "sif_error_message", "sif_error_status",
     "sif_field_alloc", "sif_field_free", "sif_field_assign_positions",
+    "sif_field_assign_weights", "sif_field_reserve_weights",
     "sif_grid_alloc", "sif_grid_free", "sif_grid_assign_cic", "sif_grid_to_density_contrast",
     "sif_chain_mesh_alloc", "sif_chain_mesh_alloc_consume", "sif_chain_mesh_free",
     "sif_catalogue_free", "sif_finder_exodus_preset", "sif_finder_exodus_variant_name",
@@ -51,6 +52,10 @@ EXPORTED = [
     # the FP64 form
     "sifg_cic_device_f64", "sifg_contrast_device_f64", "sifg_mesh_device_f64",
     "sifg_smooth_device_f64", "sifg_exodus_device_f64", "sifg_box_device_f64",
+    # weighted meshes
+    "sifg_cic_weighted_device", "sifg_cic_weighted_device_f64", "sifg_mesh_weights_device",
+    "sifg_mesh_weights_device_f64", "sifg_exodus_weighted_device",
+    "sifg_exodus_weighted_device_f64",
     # the adjoint
     "sifg_contrast_vjp_device", "sifg_contrast_vjp_device_f64",
     # the batched form
@@ -112,6 +117,16 @@ def load():
                                          f64, u32, vp, vp, u64, vp, vp, vp, vp, u64, C.POINTER(u64)]),
         "sifg_box_device_f64": (i32, [vp, vp, vp, u64, u32, f64, u32, vp, u32, f64, f64, u32,
                                       vp, vp, vp, vp, u64, C.POINTER(u64)]),
+        "sifg_cic_weighted_device": (i32, [vp, vp, vp, vp, u64, u32, f32, vp]),
+        "sifg_cic_weighted_device_f64": (i32, [vp, vp, vp, vp, u64, u32, f64, vp]),
+        "sifg_mesh_weights_device": (i32, [vp, vp, u64, vp, u32, vp, vp, C.POINTER(f64)]),
+        "sifg_mesh_weights_device_f64": (i32, [vp, vp, u64, vp, u32, vp, vp, C.POINTER(f64)]),
+        "sifg_exodus_weighted_device": (i32, [vp, u32, f32, vp, vp, vp, vp, vp, vp, f64, u64, u32,
+                                              vp, u32, f32, f32, u32, vp, vp, u64, vp, vp, vp,
+                                              vp, u64, C.POINTER(u64)]),
+        "sifg_exodus_weighted_device_f64": (i32, [vp, u32, f64, vp, vp, vp, vp, vp, vp, f64, u64,
+                                                  u32, vp, u32, f64, f64, u32, vp, vp, u64, vp,
+                                                  vp, vp, vp, u64, C.POINTER(u64)]),
         "sifg_contrast_vjp_device": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp]),
         "sifg_contrast_vjp_device_f64": (i32, [vp, vp, vp, u64, u32, f64, vp, vp, vp, vp]),
         "sifg_box_batch_device": (i32, [C.POINTER(BoxJob), u32, u32, C.POINTER(u32)]),

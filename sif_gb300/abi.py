@@ -225,6 +225,8 @@ def bind_sif_api(lib, real=C.c_float):
         "sif_field_alloc": (P_field, [C.c_uint64]),
         "sif_field_free": (None, [P_field]),
         "sif_field_assign_positions": (C.c_int, [P_field, P_real, P_real, P_real]),
+        "sif_field_assign_weights": (C.c_int, [P_field, P_real]),
+        "sif_field_reserve_weights": (C.c_int, [P_field]),
         "sif_grid_alloc": (P_grid, [C.c_uint32, sif_real]),
         "sif_grid_free": (None, [P_grid]),
         "sif_grid_assign_cic": (C.c_int, [P_grid, P_field]),

@@ -95,6 +95,7 @@ static Engine* engine() {
 
 struct ApiBufs {
   DevBuf px, py, pz, grid, grid64, mx, my, mz, offs, orig, bad, wide, mesh_sums;
+  DevBuf pw, mw, mcw, wtotal;  // a weighted field's weights; a weighted mesh's columns, total
 };
 static ApiBufs& bufs() {
   static ApiBufs b;
@@ -330,7 +331,7 @@ void sif_field_free(sif_field_t* f) {
   if (!f) return;
   host_block_put(f->_position_block);
   free(f->_velocity_block);
-  free(f->weights);
+  host_block_put(f->weights);
   free(f->original_indices);
   free(f);
 }
@@ -352,6 +353,27 @@ int sif_field_assign_positions(sif_field_t* f, const sif_real* x, const sif_real
   free(f->original_indices);
   f->original_indices = nullptr;
   f->state_flags = 0;
+  return SIF_OK;
+}
+
+// sif_field_reserve_weights / sif_field_assign_weights (src/structures/
+// field.c:171-182, 292-321): the weight column, in the field's order (this
+// library never reorders a field, so the caller's order is the field's).
+int sif_field_reserve_weights(sif_field_t* f) {
+  if (!f) return fail(SIF_ERR_INVALID, "field: NULL");
+  if (f->n_particles == 0) return fail(SIF_ERR_INVALID, "field: no particles");
+  if (f->weights) return SIF_OK;
+  f->weights = (float*)host_block_get(f->n_particles * sizeof(float));
+  return f->weights ? SIF_OK : fail(SIF_ERR_ALLOC, "field: cannot allocate weights");
+}
+
+int sif_field_assign_weights(sif_field_t* f, const sif_real* weights) {
+  if (!f) return fail(SIF_ERR_INVALID, "field: NULL");
+  if (f->n_particles == 0) return fail(SIF_ERR_INVALID, "field: no particles");
+  if (!weights) return fail(SIF_ERR_INVALID, "weights: NULL");
+  const int st = sif_field_reserve_weights(f);
+  if (st != SIF_OK) return st;
+  memcpy(f->weights, weights, f->n_particles * sizeof(float));
   return SIF_OK;
 }
 
@@ -418,9 +440,17 @@ int sif_grid_assign_cic(sif_grid_t* grid, const sif_field_t* field) {
                     field->n_particles, grid->box_length, "field", s, bufs().bad);
   if (st != SIF_OK) return st;
   float* dg = (float*)bufs().grid.ensure(grid->total_cells * sizeof(float));
-  e->scratch.ensure(cic_scratch_bytes(field->n_particles, grid->n_cells));
+  // Weighted (grid.c:635-639): the weights go up beside the positions.
+  const float* dw = nullptr;
+  if (field->weights) {
+    const size_t wb = field->n_particles * sizeof(float);
+    dw = (const float*)bufs().pw.ensure(wb);
+    SIFG_CUDA(cudaMemcpyAsync((void*)dw, field->weights, wb, cudaMemcpyHostToDevice, s));
+  }
+  e->scratch.ensure(cic_scratch_bytes(field->n_particles, grid->n_cells, dw != nullptr));
   cic_deposit(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(),
-              field->n_particles, grid->n_cells, grid->box_length, dg, e->scratch.ptr, s, nullptr);
+              field->n_particles, grid->n_cells, grid->box_length, dg, e->scratch.ptr, s, nullptr,
+              nullptr, nullptr, nullptr, dw);
   SIFG_CUDA(cudaMemcpyAsync(grid->values, dg, grid->total_cells * sizeof(float),
                             cudaMemcpyDeviceToHost, s));
   SIFG_CUDA(cudaStreamSynchronize(s));
@@ -474,8 +504,8 @@ static sif_chain_mesh_t* mesh_alloc(uint32_t n_cells, sif_real box, sif_field_t*
     fail(SIF_ERR_INVALID, fmt("box_length: %g (expected > 0)", (double)box));
     return nullptr;
   }
-  if (field->weights || field->vx) {
-    fail(SIF_ERR_UNSUPPORTED, "mesh: weighted or velocity-carrying fields are not supported on the GPU");
+  if (field->vx) {
+    fail(SIF_ERR_UNSUPPORTED, "mesh: velocity-carrying fields are not supported on the GPU");
     return nullptr;
   }
   const uint64_t n = field->n_particles;
@@ -502,10 +532,25 @@ static sif_chain_mesh_t* mesh_alloc(uint32_t n_cells, sif_real box, sif_field_t*
   m.z = (float*)bufs().mz.ensure(n * 4);
   m.offsets = (uint32_t*)bufs().offs.ensure((cells + 1) * 4);
   const bool keep_idx = !(opt & SIF_MESH_DROP_INDICES);
-  m.orig = keep_idx ? (uint32_t*)bufs().orig.ensure(n * 4) : nullptr;
-  e->scratch.ensure(mesh_scratch_bytes(n, n_cells));
+  const bool weighted = field->weights != nullptr;
+  // A weighted mesh takes its weights through the source indices, kept on
+  // the device whether or not the caller keeps them.
+  m.orig = (keep_idx || weighted) ? (uint32_t*)bufs().orig.ensure(n * 4) : nullptr;
+  e->scratch.ensure(std::max(mesh_scratch_bytes(n, n_cells),
+                             weighted ? mesh_weights_scratch_bytes(n_cells) : (size_t)0));
   mesh_build(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(), n, m,
              e->scratch.ptr, s, nullptr);
+  double* d_total = nullptr;
+  if (weighted) {
+    // chain_mesh.c:800-801, 624-672: the weights in mesh order, each cell's
+    // sum, the total.
+    float* fw = (float*)bufs().pw.ensure(n * 4);
+    SIFG_CUDA(cudaMemcpyAsync(fw, field->weights, n * 4, cudaMemcpyHostToDevice, s));
+    m.w = (float*)bufs().mw.ensure(n * 4);
+    m.cell_w = (float*)bufs().mcw.ensure(cells * 4);
+    d_total = (double*)bufs().wtotal.ensure(sizeof(double));
+    mesh_weights(fw, m, e->scratch.ptr, d_total, s);
+  }
 
   sif_chain_mesh_t* mesh = (sif_chain_mesh_t*)calloc(1, sizeof(sif_chain_mesh_t));
   mesh->n_cells = n_cells;
@@ -514,6 +559,18 @@ static sif_chain_mesh_t* mesh_alloc(uint32_t n_cells, sif_real box, sif_field_t*
   mesh->cell_length = m.cell_length;
   mesh->n_particles = n;
   mesh->total_weight = (double)n;
+  if (weighted) {
+    mesh->weights = (float*)host_block_get(n * sizeof(float));
+    mesh->cell_weights = (float*)host_block_get(cells * sizeof(float));
+    if (!mesh->weights || !mesh->cell_weights) {
+      sif_chain_mesh_free(mesh);
+      fail(SIF_ERR_ALLOC, "mesh: cannot allocate the weight columns");
+      return nullptr;
+    }
+    SIFG_CUDA(cudaMemcpyAsync(mesh->weights, m.w, n * 4, cudaMemcpyDeviceToHost, s));
+    SIFG_CUDA(cudaMemcpyAsync(mesh->cell_weights, m.cell_w, cells * 4, cudaMemcpyDeviceToHost, s));
+    SIFG_CUDA(cudaMemcpyAsync(&mesh->total_weight, d_total, 8, cudaMemcpyDeviceToHost, s));
+  }
   mesh->_position_block = (float*)host_block_get(3 * (n ? n : 1) * sizeof(float));
   mesh->x = mesh->_position_block;
   mesh->y = mesh->_position_block + n;
@@ -563,8 +620,8 @@ void sif_chain_mesh_free(sif_chain_mesh_t* m) {
   if (!m) return;
   host_block_put(m->_position_block);
   free(m->_velocity_block);
-  free(m->weights);
-  free(m->cell_weights);
+  host_block_put(m->weights);
+  host_block_put(m->cell_weights);
   host_block_put(m->original_indices);
   host_block_put(m->cell_offsets);
   free(m);
@@ -852,9 +909,34 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
                               (double)mesh->box_length, (double)grid->box_length));
     return nullptr;
   }
+  // sif__exodus_check_weights (exodus_finder.c:1076-1106), before the run
+  // starts or writes a checkpoint: by the bits, a negative zero passing.
   if (mesh->weights) {
-    fail(SIF_ERR_UNSUPPORTED, "mesh: weighted meshes are not supported by the GPU finder");
-    return nullptr;
+    if (!mesh->cell_weights) {
+      fail(SIF_ERR_INVALID, "mesh: weights but no per-cell weight table");
+      return nullptr;
+    }
+    uint64_t neg = 0, bad = 0;
+    const uint64_t nw = mesh->n_particles;
+#pragma omp parallel for schedule(static) reduction(+ : neg, bad)
+    for (uint64_t i = 0; i < nw; i++) {
+      uint32_t b;
+      memcpy(&b, mesh->weights + i, 4);
+      const bool nonfinite = ((b >> 23) & 0xffu) == 0xffu;
+      bad += nonfinite;
+      neg += !nonfinite && (b >> 31) && (b << 1);
+    }
+    if (neg || bad) {
+      fail(SIF_ERR_INVALID, fmt("mesh: weights must be finite and non-negative (%llu negative, "
+                                "%llu not finite, of %llu)",
+                                (unsigned long long)neg, (unsigned long long)bad,
+                                (unsigned long long)nw));
+      return nullptr;
+    }
+    if (!(mesh->total_weight > 0.0)) {
+      fail(SIF_ERR_INVALID, "mesh: weights sum to zero (no mean density)");
+      return nullptr;
+    }
   }
   if (mesh->n_cells == 0 || mesh->n_cells > kMaxMeshSide) {
     fail(SIF_ERR_RANGE, fmt("mesh: %u cells a side (the GPU mesh holds 1 to %u)", mesh->n_cells,
@@ -922,6 +1004,13 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   SIFG_CUDA(cudaMemcpyAsync(m.x, mesh->x, n * 4, cudaMemcpyHostToDevice, cs));
   SIFG_CUDA(cudaMemcpyAsync(m.y, mesh->y, n * 4, cudaMemcpyHostToDevice, cs));
   SIFG_CUDA(cudaMemcpyAsync(m.z, mesh->z, n * 4, cudaMemcpyHostToDevice, cs));
+  if (mesh->weights) {
+    m.w = (float*)bufs().mw.ensure(n * 4);
+    m.cell_w = (float*)bufs().mcw.ensure(mcells * 4);
+    m.total_weight = mesh->total_weight;
+    SIFG_CUDA(cudaMemcpyAsync(m.w, mesh->weights, n * 4, cudaMemcpyHostToDevice, cs));
+    SIFG_CUDA(cudaMemcpyAsync(m.cell_w, mesh->cell_weights, mcells * 4, cudaMemcpyHostToDevice, cs));
+  }
   SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
   // Whatever the run's outcome, the copies out of the caller's mesh end
   // before this call returns.
@@ -939,6 +1028,7 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   p.radii.assign(radii, radii + n_radii);
   p.window = g_window;
   p.mesh_ready = e->ev_mesh_ready();
+  p.weights_checked = true;  // above, on the host copy
   if (!ck.voids[0].empty()) {
     p.prior_cx = ck.voids[0].data();
     p.prior_cy = ck.voids[1].data();
@@ -1017,7 +1107,7 @@ uint32_t sif_finder_grid_cells_from_size(uint64_t n_particles, sif_real box_leng
 
 template <class R>
 static int cic_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n_grid, R box,
-                      R* grid) {
+                      R* grid, const R* w = nullptr) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   if (n_grid < 4) return fail(SIF_ERR_INVALID, "n_grid: expected at least 4");
@@ -1026,11 +1116,12 @@ static int cic_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n
   if (st != SIF_OK) return st;
   RunTimings tm;
   if constexpr (sizeof(R) == 4) {
-    e->scratch.ensure(cic_scratch_bytes(n, n_grid));
-    cic_deposit(x, y, z, n, n_grid, box, grid, e->scratch.ptr, s, &tm.cic);
+    e->scratch.ensure(cic_scratch_bytes(n, n_grid, w != nullptr));
+    cic_deposit(x, y, z, n, n_grid, box, grid, e->scratch.ptr, s, &tm.cic, nullptr, nullptr,
+                nullptr, w);
   } else {
     e->scratch.ensure(cic_f64_scratch_bytes(n_grid));
-    cic_deposit_f64(x, y, z, n, n_grid, box, grid, e->scratch.ptr, s, &tm.cic);
+    cic_deposit_f64(x, y, z, n, n_grid, box, grid, e->scratch.ptr, s, &tm.cic, w);
   }
   SIFG_CUDA(cudaStreamSynchronize(s));
   g_timings.cic_ms = tm.cic.total_ms();
@@ -1160,13 +1251,44 @@ static int run_device(Engine* e, const R* delta, uint32_t n_grid, R box, DeviceM
   return SIF_OK;
 }
 
+// A weighted device mesh's columns from the field's weights and the mesh's
+// source indices (chain_mesh.c:624-672, 800-801); *total_out (host) gets the
+// total weight.
+template <class R>
+static int mesh_weights_device(const R* field_w, const uint32_t* orig, uint64_t n,
+                               const uint32_t* offsets, uint32_t n_cells, R* w_out, R* cell_w_out,
+                               double* total_out) {
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  if (!field_w || !orig || !offsets || !w_out || !cell_w_out || !total_out)
+    return fail(SIF_ERR_INVALID, "mesh weights: NULL argument");
+  if (n_cells == 0 || n_cells > kMaxMeshSide)
+    return fail(SIF_ERR_RANGE, fmt("mesh: %u cells a side (the GPU mesh holds 1 to %u)", n_cells,
+                                   kMaxMeshSide));
+  cudaStream_t s = e->stream();
+  DeviceMeshT<R> m;
+  m.n_cells = n_cells;
+  m.n_particles = n;
+  m.orig = const_cast<uint32_t*>(orig);
+  m.offsets = const_cast<uint32_t*>(offsets);
+  m.w = w_out;
+  m.cell_w = cell_w_out;
+  e->scratch.ensure(mesh_weights_scratch_bytes(n_cells) + 64);
+  double* d_total = (double*)((char*)e->scratch.ptr + mesh_weights_scratch_bytes(n_cells));
+  mesh_weights(field_w, m, e->scratch.ptr, d_total, s);
+  SIFG_CUDA(cudaMemcpyAsync(total_out, d_total, sizeof(double), cudaMemcpyDeviceToHost, s));
+  SIFG_CUDA(cudaStreamSynchronize(s));
+  return SIF_OK;
+}
+
 template <class R>
 static int exodus_device(const R* delta, uint32_t n_grid, R box, const R* mx, const R* my,
                          const R* mz, const uint32_t* offsets, uint64_t n_particles,
                          uint32_t mesh_cells, const R* radii, uint32_t n_radii, R threshold,
                          R overlap, uint32_t opt, const R* inject, const R* prior,
                          uint64_t n_prior, R* cx, R* cy, R* cz, R* r, uint64_t capacity,
-                         uint64_t* n_voids) {
+                         uint64_t* n_voids, const R* mw = nullptr, const R* mcw = nullptr,
+                         double total_weight = 0.0) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   if (n_prior && !prior) return fail(SIF_ERR_INVALID, "prior: NULL with voids to start from");
@@ -1187,6 +1309,9 @@ static int exodus_device(const R* delta, uint32_t n_grid, R box, const R* mx, co
   m.y = const_cast<R*>(my);
   m.z = const_cast<R*>(mz);
   m.offsets = const_cast<uint32_t*>(offsets);
+  m.w = const_cast<R*>(mw);
+  m.cell_w = const_cast<R*>(mcw);
+  m.total_weight = total_weight;
   RunTimings tm;
   const int st = run_device(e, delta, n_grid, box, m, radii, n_radii, threshold, overlap, opt,
                             inject, cx, cy, cz, r, capacity, n_voids, tm, nullptr, &g_stats,
@@ -1508,6 +1633,55 @@ int sifg_exodus_device(const float* delta, uint32_t n_grid, float box, const flo
   SIFG_LOCKED(exodus_device(delta, n_grid, box, mx, my, mz, offsets, n_particles, mesh_cells,
                             radii, n_radii, threshold, overlap, opt, inject, prior, n_prior, cx,
                             cy, cz, r, capacity, n_voids))
+}
+int sifg_cic_weighted_device(const float* x, const float* y, const float* z, const float* w,
+                             uint64_t n, uint32_t n_grid, float box, float* grid) {
+  if (!w) return fail(SIF_ERR_INVALID, "weights: NULL");
+  SIFG_LOCKED(cic_device(x, y, z, n, n_grid, box, grid, w))
+}
+int sifg_cic_weighted_device_f64(const double* x, const double* y, const double* z,
+                                 const double* w, uint64_t n, uint32_t n_grid, double box,
+                                 double* grid) {
+  if (!w) return fail(SIF_ERR_INVALID, "weights: NULL");
+  SIFG_LOCKED(cic_device(x, y, z, n, n_grid, box, grid, w))
+}
+int sifg_mesh_weights_device(const float* field_w, const uint32_t* orig, uint64_t n,
+                             const uint32_t* offsets, uint32_t n_cells, float* w, float* cell_w,
+                             double* total_weight) {
+  SIFG_LOCKED(mesh_weights_device(field_w, orig, n, offsets, n_cells, w, cell_w, total_weight))
+}
+int sifg_mesh_weights_device_f64(const double* field_w, const uint32_t* orig, uint64_t n,
+                                 const uint32_t* offsets, uint32_t n_cells, double* w,
+                                 double* cell_w, double* total_weight) {
+  SIFG_LOCKED(mesh_weights_device(field_w, orig, n, offsets, n_cells, w, cell_w, total_weight))
+}
+int sifg_exodus_weighted_device(const float* delta, uint32_t n_grid, float box, const float* mx,
+                                const float* my, const float* mz, const uint32_t* offsets,
+                                const float* w, const float* cell_w, double total_weight,
+                                uint64_t n_particles, uint32_t mesh_cells, const float* radii,
+                                uint32_t n_radii, float threshold, float overlap, uint32_t opt,
+                                const float* inject, const float* prior, uint64_t n_prior,
+                                float* cx, float* cy, float* cz, float* r, uint64_t capacity,
+                                uint64_t* n_voids) {
+  if (!w || !cell_w) return fail(SIF_ERR_INVALID, "mesh weights: NULL");
+  SIFG_LOCKED(exodus_device(delta, n_grid, box, mx, my, mz, offsets, n_particles, mesh_cells,
+                            radii, n_radii, threshold, overlap, opt, inject, prior, n_prior, cx,
+                            cy, cz, r, capacity, n_voids, w, cell_w, total_weight))
+}
+int sifg_exodus_weighted_device_f64(const double* delta, uint32_t n_grid, double box,
+                                    const double* mx, const double* my, const double* mz,
+                                    const uint32_t* offsets, const double* w,
+                                    const double* cell_w, double total_weight,
+                                    uint64_t n_particles, uint32_t mesh_cells,
+                                    const double* radii, uint32_t n_radii, double threshold,
+                                    double overlap, uint32_t opt, const double* inject,
+                                    const double* prior, uint64_t n_prior, double* cx,
+                                    double* cy, double* cz, double* r, uint64_t capacity,
+                                    uint64_t* n_voids) {
+  if (!w || !cell_w) return fail(SIF_ERR_INVALID, "mesh weights: NULL");
+  SIFG_LOCKED(exodus_device(delta, n_grid, box, mx, my, mz, offsets, n_particles, mesh_cells,
+                            radii, n_radii, threshold, overlap, opt, inject, prior, n_prior, cx,
+                            cy, cz, r, capacity, n_voids, w, cell_w, total_weight))
 }
 int sifg_exodus_device_f64(const double* delta, uint32_t n_grid, double box, const double* mx,
                            const double* my, const double* mz, const uint32_t* offsets,

@@ -24,6 +24,16 @@
 //                    faces shared with neighbouring tiles go to int64 face
 //                    buffers with global atomics;
 //   5. face_fixup:   the face buffers converted to float density.
+//
+// Weighted (sif_field_t::weights), a particle's corners carry its weight as
+// the reference's products do (grid.c:635-639: the weight times each z
+// factor, then the (x, y) products times those), quantised to 2^-24 of the
+// binade of the largest weight magnitude: the same integers as unweighted
+// when every weight is that power of two, so weights of 1 or 4 give the
+// unweighted density times the weight, bit for bit. Negative weights sum as
+// two's complement; a non-finite weight deposits nothing in the sums and
+// its products are added to its eight cells afterwards, so those cells go
+// non-finite as the reference's do.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -112,7 +122,8 @@ static_assert(TB == 16, "4 bits per axis of the cell within its tile");
 
 __global__ void tile_scatter_kernel(const float* __restrict__ x, const float* __restrict__ y,
                                     const float* __restrict__ z, uint64_t n, CicGeom g,
-                                    uint32_t* __restrict__ cursor, float4* __restrict__ rec) {
+                                    uint32_t* __restrict__ cursor, float4* __restrict__ rec,
+                                    const float* __restrict__ w, float* __restrict__ wrec) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const unsigned lane = threadIdx.x & 31u;
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -133,7 +144,71 @@ __global__ void tile_scatter_kernel(const float* __restrict__ x, const float* __
     uint32_t slot0 = 0;
     if (valid && lane == leader) slot0 = atomicAdd(cursor + tile, (uint32_t)__popc(peers));
     slot0 = __shfl_sync(0xffffffffu, slot0, leader);
-    if (valid) rec[slot0 + __popc(peers & ((1u << lane) - 1u))] = r;
+    if (valid) {
+      const uint32_t slot = slot0 + __popc(peers & ((1u << lane) - 1u));
+      rec[slot] = r;
+      if (w) wrec[slot] = w[p];
+    }
+  }
+}
+
+// The largest finite weight magnitude, as its bits (which order as the
+// magnitudes do), and the count of non-finite weights.
+__global__ void weight_max_kernel(const float* __restrict__ w, uint64_t n,
+                                  unsigned* __restrict__ out) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  unsigned m = 0, bad = 0;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+    const unsigned b = __float_as_uint(w[p]) & 0x7fffffffu;
+    if (b >= 0x7f800000u)
+      bad++;
+    else
+      m = max(m, b);
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  bad = __reduce_add_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31u) == 0) {
+    if (m) atomicMax(out, m);
+    if (bad) atomicAdd(out + 1, bad);
+  }
+}
+
+// The weighted quantum from the largest weight's binade [2^E, 2^(E+1)):
+// corners quantised at 2^(E-24) (scale 2^(24-E)), clamped to keep both the
+// scale and its inverse normal floats.
+__device__ __forceinline__ int weight_scale_exp(const unsigned* wmax) {
+  const int e = (int)(*wmax >> 23) - 127;
+  return min(100, max(-100, 24 - e));
+}
+
+// Each non-finite weight's eight products, added to its cells after the
+// deposit (the reference's float sums carry them into those cells).
+__global__ void nonfinite_weights_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                         const float* __restrict__ z,
+                                         const float* __restrict__ w, uint64_t n, CicGeom g,
+                                         const unsigned* __restrict__ wmax,
+                                         float* __restrict__ grid) {
+  if (wmax[1] == 0) return;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+    const float pw = w[p];
+    if ((__float_as_uint(pw) & 0x7fffffffu) < 0x7f800000u) continue;
+    uint32_t c[3];
+    float t[3];
+    cic_axis(x[p], g, c[0], t[0]);
+    cic_axis(y[p], g, c[1], t[1]);
+    cic_axis(z[p], g, c[2], t[2]);
+    for (int k = 0; k < 8; k++) {
+      uint32_t q[3];
+      float f = 1.0f;
+      for (int a = 0; a < 3; a++) {
+        const int up = (k >> (2 - a)) & 1;
+        q[a] = up ? (c[a] + 1 == g.n ? 0u : c[a] + 1) : c[a];
+        f = fmul(f, up ? t[a] : fsub(1.0f, t[a]));
+      }
+      float* cell = grid + ((uint64_t)q[0] * g.n + q[1]) * g.n + q[2];
+      *cell = fadd(*cell, fmul(pw, f));
+    }
   }
 }
 
@@ -156,7 +231,8 @@ __device__ __forceinline__ unsigned long long* face_slot(const FaceBufs& f, uint
 
 __global__ void __launch_bounds__(256) tile_deposit_kernel(
     const float4* __restrict__ rec, const uint32_t* __restrict__ offsets, CicGeom g,
-    float inv_cell_vol, float* __restrict__ grid, FaceBufs faces) {
+    float inv_cell_vol, float* __restrict__ grid, FaceBufs faces,
+    const float* __restrict__ wrec, const unsigned* __restrict__ wmax) {
   // The tile's sums as 32-bit words and their carries: a 32-bit shared atomic
   // add is one instruction, a 64-bit one a compare-and-swap loop. A word that
   // wraps past 2^32 counts the wrap in its carry (each add is below 2^32, so
@@ -166,6 +242,13 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
   uint32_t* acc_hi = acc_lo + TS * TS * TS;
   const uint32_t nt = g.nt;
   const uint32_t n_tiles = nt * nt * nt;
+  // The quantum: 2^-24 of a particle, or of the largest weight's binade.
+  float qscale = 16777216.0f, qinv = 1.0f / 16777216.0f;
+  if (wrec) {
+    const int e = weight_scale_exp(wmax);
+    qscale = __uint_as_float((uint32_t)(127 + e) << 23);
+    qinv = __uint_as_float((uint32_t)(127 - e) << 23);
+  }
   // Cleared once; each flush leaves the cells it reads cleared for the next tile.
   for (int i = threadIdx.x; i < 2 * TS * TS * TS; i += blockDim.x) acc_lo[i] = 0u;
   __syncthreads();
@@ -183,28 +266,40 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
         const float4 r = __ldg(rec + p);
         const float tx_ = r.x, ty_ = r.y, tz_ = r.z;
         const uint32_t local = __float_as_uint(r.w);
-        const float wx0 = fsub(1.0f, tx_), wy0 = fsub(1.0f, ty_), wz0 = fsub(1.0f, tz_);
-        // The reference's eight products (grid.c:627-650): (x,y) pairs times z.
+        float wz0 = fsub(1.0f, tz_), wz1 = tz_;
+        float pw = 1.0f;
+        if (wrec) {
+          // A non-finite weight is added afterwards, outside the sums.
+          pw = __ldg(wrec + p);
+          if ((__float_as_uint(pw) & 0x7fffffffu) >= 0x7f800000u) pw = 0.0f;
+          wz0 = fmul(pw, wz0);
+          wz1 = fmul(pw, wz1);
+        }
+        const float wx0 = fsub(1.0f, tx_), wy0 = fsub(1.0f, ty_);
+        // The reference's eight products (grid.c:627-650): (x,y) pairs times
+        // z (times the weight).
         const float w00 = fmul(wx0, wy0), w01 = fmul(wx0, ty_);
         const float w10 = fmul(tx_, wy0), w11 = fmul(tx_, ty_);
-        const float w[8] = {fmul(w00, wz0), fmul(w00, tz_), fmul(w01, wz0), fmul(w01, tz_),
-                            fmul(w10, wz0), fmul(w10, tz_), fmul(w11, wz0), fmul(w11, tz_)};
-        // w * 2^24 is exact in float, so rounding it to an integer in float
-        // is the quantisation itself; GB300's FP64 rate is no place for it.
+        const float w[8] = {fmul(w00, wz0), fmul(w00, wz1), fmul(w01, wz0), fmul(w01, wz1),
+                            fmul(w10, wz0), fmul(w10, wz1), fmul(w11, wz0), fmul(w11, wz1)};
+        // w times a power of two is exact in float, so rounding it to an
+        // integer in float is the quantisation itself; GB300's FP64 rate is
+        // no place for it.
         int sum = 0;
         int big = 0;
-        float wbig = w[0];
+        float wbig = fabsf(w[0]);
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-          const int qk = __float2int_rn(fmul(w[k], 16777216.0f));
+          const int qk = __float2int_rn(fmul(w[k], qscale));
           q[k] = (uint32_t)qk;
           sum += qk;
-          if (w[k] > wbig) {  // the first largest, as a scan from corner 0 finds it
-            wbig = w[k];
+          if (fabsf(w[k]) > wbig) {  // the first largest, as a scan from corner 0 finds it
+            wbig = fabsf(w[k]);
             big = k;
           }
         }
-        const int fix = 16777216 - sum;
+        // The eight sum to the particle's own quantised weight.
+        const int fix = (wrec ? __float2int_rn(fmul(pw, qscale)) : 16777216) - sum;
 #pragma unroll
         for (int k = 0; k < 8; k++) q[k] = (uint32_t)((int)q[k] + (k == big ? fix : 0));
         cell = ((local >> 8) * TS + ((local >> 4) & 15u)) * TS + (local & 15u);
@@ -220,7 +315,9 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
           const uint32_t c =
               cell + (uint32_t)(((k >> 2) & 1) * TS * TS + ((k >> 1) & 1) * TS + (k & 1));
           const uint32_t old = atomicAdd(acc_lo + c, v);
-          if (old + v < old) atomicAdd(acc_hi + c, 1u);
+          // The carry, and for a negative value its sign extension.
+          const uint32_t hi = (old + v < old ? 1u : 0u) + ((int)v < 0 ? 0xffffffffu : 0u);
+          if (hi) atomicAdd(acc_hi + c, hi);
         }
       }
     }
@@ -242,7 +339,7 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
       const bool interior = a >= 1 && a < ex && b >= 1 && b < ey && c >= 1 && c < ez;
       if (interior) {
         grid[((uint64_t)gx * g.n + gy) * g.n + gz] =
-            fmul(fmul(__ull2float_rn(v), 1.0f / 16777216.0f), inv_cell_vol);
+            fmul(fmul(__ll2float_rn((long long)v), qinv), inv_cell_vol);
       } else if (v != 0ull) {
         atomicAdd(face_slot(faces, gx, gy, gz, g), v);
       }
@@ -252,7 +349,9 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
 }
 
 __global__ void face_fixup_kernel(CicGeom g, float inv_cell_vol, float* __restrict__ grid,
-                                  FaceBufs faces) {
+                                  FaceBufs faces, const unsigned* __restrict__ wmax) {
+  float qinv = 1.0f / 16777216.0f;
+  if (wmax) qinv = __uint_as_float((uint32_t)(127 - weight_scale_exp(wmax)) << 23);
   const uint64_t n = g.n, nt = g.nt;
   const uint64_t nfx = nt * n * n;
   const uint64_t total = 3 * nfx;
@@ -280,7 +379,7 @@ __global__ void face_fixup_kernel(CicGeom g, float inv_cell_vol, float* __restri
       if (gz >= n || gx % TB == 0 || gy % TB == 0) continue;
       v = faces.fz[j];
     }
-    grid[(gx * n + gy) * n + gz] = fmul(fmul(__ull2float_rn(v), 1.0f / 16777216.0f), inv_cell_vol);
+    grid[(gx * n + gy) * n + gz] = fmul(fmul(__ll2float_rn((long long)v), qinv), inv_cell_vol);
   }
 }
 
@@ -305,31 +404,76 @@ __device__ __forceinline__ void cic_axis_f64(double v, uint32_t n, double box, d
   t = fsub(u, (double)raw);
 }
 
+// Weighted: the largest finite weight magnitude's bits and the count of
+// non-finite weights, as weight_max_kernel in float.
+__global__ void weight_max_f64_kernel(const double* __restrict__ w, uint64_t n,
+                                      unsigned long long* __restrict__ out) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  unsigned long long m = 0, bad = 0;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(w[p]) & 0x7fffffffffffffffull;
+    if (b >= 0x7ff0000000000000ull)
+      bad++;
+    else
+      m = b > m ? b : m;
+  }
+  for (int d = 16; d > 0; d >>= 1) {
+    const unsigned long long o = __shfl_down_sync(0xffffffffu, m, d);
+    m = o > m ? o : m;
+    bad += __shfl_down_sync(0xffffffffu, bad, d);
+  }
+  if ((threadIdx.x & 31u) == 0) {
+    if (m) atomicMax(out, m);
+    if (bad) atomicAdd(out + 1, bad);
+  }
+}
+
+// The FP64 quantum: 2^-40 of a particle, or of the largest weight's binade
+// (clamped to keep the scale and its inverse normal).
+__device__ __forceinline__ int weight_scale_exp_f64(const unsigned long long* wmax) {
+  const int e = (int)(wmax[0] >> 52) - 1023;
+  return min(900, max(-900, 40 - e));
+}
+
 __global__ void cic_f64_kernel(const double* __restrict__ x, const double* __restrict__ y,
                                const double* __restrict__ z, uint64_t np, uint32_t n, double box,
-                               double idx, unsigned long long* __restrict__ acc) {
+                               double idx, unsigned long long* __restrict__ acc,
+                               const double* __restrict__ wts,
+                               const unsigned long long* __restrict__ wmax) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  double qs = kQ64;
+  if (wts) qs = __longlong_as_double((long long)(1023 + weight_scale_exp_f64(wmax)) << 52);
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
     uint32_t x0, x1, y0, y1, z0, z1;
     double tx, ty, tz;
     cic_axis_f64(x[p], n, box, idx, x0, x1, tx);
     cic_axis_f64(y[p], n, box, idx, y0, y1, ty);
     cic_axis_f64(z[p], n, box, idx, z0, z1, tz);
-    const double wx0 = fsub(1.0, tx), wy0 = fsub(1.0, ty), wz0 = fsub(1.0, tz);
+    double wz0 = fsub(1.0, tz), wz1 = tz, pw = 1.0;
+    if (wts) {
+      pw = wts[p];
+      // A non-finite weight is added afterwards, outside the sums.
+      if (((unsigned long long)__double_as_longlong(pw) & 0x7fffffffffffffffull) >=
+          0x7ff0000000000000ull)
+        continue;
+      wz0 = fmul(pw, wz0);
+      wz1 = fmul(pw, wz1);
+    }
+    const double wx0 = fsub(1.0, tx), wy0 = fsub(1.0, ty);
     const double w00 = fmul(wx0, wy0), w01 = fmul(wx0, ty), w10 = fmul(tx, wy0),
                  w11 = fmul(tx, ty);
-    const double w[8] = {fmul(w00, wz0), fmul(w00, tz), fmul(w01, wz0), fmul(w01, tz),
-                         fmul(w10, wz0), fmul(w10, tz), fmul(w11, wz0), fmul(w11, tz)};
+    const double w[8] = {fmul(w00, wz0), fmul(w00, wz1), fmul(w01, wz0), fmul(w01, wz1),
+                         fmul(w10, wz0), fmul(w10, wz1), fmul(w11, wz0), fmul(w11, wz1)};
     long long q[8];
     long long sum = 0;
     int big = 0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      q[k] = __double2ll_rn(fmul(w[k], kQ64));
+      q[k] = __double2ll_rn(fmul(w[k], qs));
       sum += q[k];
-      if (w[k] > w[big]) big = k;
+      if (fabs(w[k]) > fabs(w[big])) big = k;
     }
-    const long long fix = (long long)kQ64 - sum;
+    const long long fix = (wts ? __double2ll_rn(fmul(pw, qs)) : (long long)kQ64) - sum;
     const uint32_t xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -342,30 +486,80 @@ __global__ void cic_f64_kernel(const double* __restrict__ x, const double* __res
 }
 
 __global__ void cic_f64_finish_kernel(const unsigned long long* __restrict__ acc, uint64_t cells,
-                                      double inv_cell_vol, double* __restrict__ grid) {
+                                      double inv_cell_vol, double* __restrict__ grid,
+                                      const unsigned long long* __restrict__ wmax) {
+  double qinv = 1.0 / kQ64;
+  if (wmax) qinv = __longlong_as_double((long long)(1023 - weight_scale_exp_f64(wmax)) << 52);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cells; i += stride)
-    grid[i] = fmul(fmul(__ull2double_rn(acc[i]), 1.0 / kQ64), inv_cell_vol);
+    grid[i] = fmul(fmul(__ll2double_rn((long long)acc[i]), qinv), inv_cell_vol);
 }
 
-size_t cic_f64_scratch_bytes(uint32_t n) { return (size_t)n * n * n * sizeof(unsigned long long) + 256; }
+// Each non-finite weight's eight products added to its cells (see the float
+// form's nonfinite_weights_kernel).
+__global__ void nonfinite_weights_f64_kernel(const double* __restrict__ x,
+                                             const double* __restrict__ y,
+                                             const double* __restrict__ z,
+                                             const double* __restrict__ w, uint64_t np, uint32_t n,
+                                             double box, double idx,
+                                             const unsigned long long* __restrict__ wmax,
+                                             double* __restrict__ grid) {
+  if (wmax[1] == 0) return;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    const double pw = w[p];
+    if (((unsigned long long)__double_as_longlong(pw) & 0x7fffffffffffffffull) <
+        0x7ff0000000000000ull)
+      continue;
+    uint32_t c0[3], c1[3];
+    double t[3];
+    cic_axis_f64(x[p], n, box, idx, c0[0], c1[0], t[0]);
+    cic_axis_f64(y[p], n, box, idx, c0[1], c1[1], t[1]);
+    cic_axis_f64(z[p], n, box, idx, c0[2], c1[2], t[2]);
+    for (int k = 0; k < 8; k++) {
+      uint32_t q[3];
+      double f = 1.0;
+      for (int a = 0; a < 3; a++) {
+        const int up = (k >> (2 - a)) & 1;
+        q[a] = up ? c1[a] : c0[a];
+        f = fmul(f, up ? t[a] : fsub(1.0, t[a]));
+      }
+      double* cell = grid + ((uint64_t)q[0] * n + q[1]) * n + q[2];
+      *cell = fadd(*cell, fmul(pw, f));
+    }
+  }
+}
+
+size_t cic_f64_scratch_bytes(uint32_t n) { return (size_t)n * n * n * sizeof(unsigned long long) + 512; }
 
 void cic_deposit_f64(const double* x, const double* y, const double* z, uint64_t n_particles,
                      uint32_t n, double box, double* grid, void* scratch, cudaStream_t st,
-                     KernelTimer* timer) {
+                     KernelTimer* timer, const double* w) {
   const uint64_t cells = (uint64_t)n * n * n;
   unsigned long long* acc = (unsigned long long*)scratch;
-  SIFG_CUDA(cudaMemsetAsync(acc, 0, cells * sizeof(unsigned long long), st));
+  unsigned long long* wmax = w ? acc + cells : nullptr;
+  SIFG_CUDA(cudaMemsetAsync(acc, 0, (cells + (w ? 2 : 0)) * sizeof(unsigned long long), st));
   // grid.c:684 and 735-737 in double.
   const double idx = (double)n / box;
   const double cl = box / (double)n;
   const double inv_cell_vol = 1.0f / (double)(cl * cl * cl);
+  if (w) {
+    weight_max_f64_kernel<<<grid_for(n_particles, 256, 152u * 16u), 256, 0, st>>>(w, n_particles,
+                                                                                  wmax);
+    SIFG_LAUNCH_CHECK();
+  }
   if (timer) timer->begin(st);
-  cic_f64_kernel<<<grid_for(n_particles, 256), 256, 0, st>>>(x, y, z, n_particles, n, box, idx, acc);
+  cic_f64_kernel<<<grid_for(n_particles, 256), 256, 0, st>>>(x, y, z, n_particles, n, box, idx, acc,
+                                                             w, wmax);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(st);
-  cic_f64_finish_kernel<<<grid_for(cells, 256), 256, 0, st>>>(acc, cells, inv_cell_vol, grid);
+  cic_f64_finish_kernel<<<grid_for(cells, 256), 256, 0, st>>>(acc, cells, inv_cell_vol, grid, wmax);
   SIFG_LAUNCH_CHECK();
+  if (w) {
+    nonfinite_weights_f64_kernel<<<grid_for(n_particles, 256, 152u * 16u), 256, 0, st>>>(
+        x, y, z, w, n_particles, n, box, idx, wmax, grid);
+    SIFG_LAUNCH_CHECK();
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -480,17 +674,18 @@ static CicGeom make_geom(uint32_t n, float box) {
   return g;
 }
 
-size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n) {
+size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n, bool weighted) {
   const uint64_t nt = (n + TB - 1) / TB;
   const uint64_t tiles = nt * nt * nt;
   const uint64_t face = 3 * nt * (uint64_t)n * n * sizeof(unsigned long long);
-  return n_particles * sizeof(float4) + (2 * tiles + 2) * sizeof(uint32_t) + face + 16 * 256;
+  return n_particles * (sizeof(float4) + (weighted ? sizeof(float) : 0)) +
+         (2 * tiles + 2) * sizeof(uint32_t) + face + 16 * 256 + 512;
 }
 
 void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_particles,
                  uint32_t n, float box, float* grid, void* scratch, cudaStream_t st,
                  KernelTimer* timer, const float* bounds, unsigned long long* outside,
-                 cudaEvent_t sorted) {
+                 cudaEvent_t sorted, const float* w) {
   const CicGeom g = make_geom(n, box);
   const uint64_t nt = g.nt, tiles = nt * nt * nt;
   char* p = (char*)scratch;
@@ -507,6 +702,8 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   faces.fx = (unsigned long long*)take(face_elems * 8);
   faces.fy = (unsigned long long*)take(face_elems * 8);
   faces.fz = (unsigned long long*)take(face_elems * 8);
+  float* wrec = w ? (float*)take(n_particles * sizeof(float)) : nullptr;
+  unsigned* wmax = w ? (unsigned*)take(2 * sizeof(unsigned)) : nullptr;
 
   SIFG_CUDA(cudaMemsetAsync(counts, 0, (tiles + 1) * sizeof(uint32_t), st));
   SIFG_CUDA(cudaMemsetAsync(faces.fx, 0, face_elems * 8, st));
@@ -514,6 +711,11 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   SIFG_CUDA(cudaMemsetAsync(faces.fz, 0, face_elems * 8, st));
   const unsigned blk = 256;
   const unsigned grd = grid_for(n_particles, blk, 152u * 16u);
+  if (w) {
+    SIFG_CUDA(cudaMemsetAsync(wmax, 0, 2 * sizeof(unsigned), st));
+    weight_max_kernel<<<grd, blk, 0, st>>>(w, n_particles, wmax);
+    SIFG_LAUNCH_CHECK();
+  }
   tile_count_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, counts,
                                          bounds ? bounds[0] : 0.f, bounds ? bounds[1] : 0.f,
                                          bounds ? outside : nullptr);
@@ -521,7 +723,7 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   exclusive_scan_u32(counts, (uint32_t)(tiles + 1), st);
   SIFG_CUDA(cudaMemcpyAsync(cursor, counts, (tiles + 1) * sizeof(uint32_t),
                             cudaMemcpyDeviceToDevice, st));
-  tile_scatter_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, cursor, rec);
+  tile_scatter_kernel<<<grd, blk, 0, st>>>(x, y, z, n_particles, g, cursor, rec, w, wrec);
   SIFG_LAUNCH_CHECK();
   if (sorted) SIFG_CUDA(cudaEventRecord(sorted, st));
   const float cl = box / (float)n;
@@ -535,11 +737,17 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   }
   const unsigned dgrid = (unsigned)(tiles < 152u * 5u ? tiles : 152u * 5u);
   if (timer) timer->begin(st);
-  tile_deposit_kernel<<<dgrid, 256, smem, st>>>(rec, counts, g, inv_cell_vol, grid, faces);
+  tile_deposit_kernel<<<dgrid, 256, smem, st>>>(rec, counts, g, inv_cell_vol, grid, faces,
+                                                 wrec, wmax);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(st);
-  face_fixup_kernel<<<grid_for(3 * face_elems, 256), 256, 0, st>>>(g, inv_cell_vol, grid, faces);
+  face_fixup_kernel<<<grid_for(3 * face_elems, 256), 256, 0, st>>>(g, inv_cell_vol, grid, faces,
+                                                                  wmax);
   SIFG_LAUNCH_CHECK();
+  if (w) {
+    nonfinite_weights_kernel<<<grd, blk, 0, st>>>(x, y, z, w, n_particles, g, wmax, grid);
+    SIFG_LAUNCH_CHECK();
+  }
 }
 
 template <class R>

@@ -456,6 +456,34 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     set_error(kErrRange, "grid: more than 2^32 cells");
     return kErrRange;
   }
+  // A weighted mesh (exodus_finder.c:1316-1319, 1076-1106): its weights
+  // finite and non-negative, their total positive, before anything runs.
+  const bool weighted = mesh.w != nullptr;
+  if (weighted) {
+    if (!mesh.cell_w) {
+      set_error(kErrInvalid, "mesh: weights but no per-cell weight table");
+      return kErrInvalid;
+    }
+    unsigned long long h_wc[2] = {0, 0};
+    if (!p.weights_checked) {
+      unsigned long long* wc = (unsigned long long*)grow_to<uint64_t>(wcheck_, 2);
+      if (p.mesh_ready) SIFG_CUDA(cudaStreamWaitEvent(st_, p.mesh_ready, 0));
+      check_weights(mesh.w, mesh.n_particles, wc, st_);
+      SIFG_CUDA(cudaMemcpyAsync(h_wc, wc, sizeof(h_wc), cudaMemcpyDeviceToHost, st_));
+      SIFG_CUDA(cudaStreamSynchronize(st_));
+    }
+    if (h_wc[0] || h_wc[1]) {
+      set_error(kErrInvalid, "mesh: weights must be finite and non-negative (" +
+                                 std::to_string(h_wc[0]) + " negative, " +
+                                 std::to_string(h_wc[1]) + " not finite, of " +
+                                 std::to_string(mesh.n_particles) + ")");
+      return kErrInvalid;
+    }
+    if (!(mesh.total_weight > 0.0)) {
+      set_error(kErrInvalid, "mesh: weights sum to zero (no mean density)");
+      return kErrInvalid;
+    }
+  }
   const R scale = (opt & kOptLagrangian) ? (R)std::cbrt(1.0 + (double)threshold) : 1.0f;
   static const R factors[4] = {1.5f, 1.25f, 1.75f, 2.0f};
   const R search_factor = factors[(opt >> 12) & 3u];
@@ -512,6 +540,11 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const R box_volume = box * box * box;
   const R mean_density = (R)mesh.n_particles / box_volume;
   const R vol_factor = (4.0f / 3.0f) * kPi<R> * mean_density;
+  // What the density tests measure against (1634-1642): on a weighted mesh
+  // the mean weight density, rounded and divided as the count is; the
+  // histogram is still sized by the tracer count.
+  const R mass_factor =
+      weighted ? (4.0f / 3.0f) * kPi<R> * ((R)mesh.total_weight / box_volume) : vol_factor;
 
   uint32_t n_voids = 0;
   // The catalogue's buffers keep their size from run to run (a cudaFree
@@ -584,6 +617,23 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   MeshViewT<R> mv{mesh.x,          mesh.y,          mesh.z,
                   mesh.offsets,    (int32_t)mesh.n_cells, mesh.box_length,
                   1.0f / mesh.cell_length, mesh.xyzw};
+  long long* gwbuf = nullptr;
+  if (weighted) {
+    // The fixed point of the weight sums: no sum exceeds the total weight
+    // times the times a search's template can meet one cell (its side over
+    // the mesh's, cubed; the top rung's reach is the widest).
+    const R r_top = radii.front();
+    const R reach = r_top + std::fmax((search_factor - 1.0f) * r_top, 3.0f * cell);
+    const double side = 2.0 * ((double)(int64_t)(reach / mesh.cell_length) + 2.0) + 1.0;
+    const double rep = std::pow(std::ceil(side / (double)mesh.n_cells), 3.0);
+    double ws = 0, wi = 0;
+    weight_fixed_point(mesh.total_weight * rep, &ws, &wi);
+    mv.w = mesh.w;
+    mv.cell_w = mesh.cell_w;
+    mv.wscale = (R)ws;
+    mv.winv = wi;
+    gwbuf = grow_to<long long>(gwbuf_, (size_t)growth_grid() * kGrowCap);
+  }
 
   // The sphere growth's constants for a search shell [rmin, r_search]
   // (exodus_rescale.c:681-720, 894-908), on top of the rung's own.
@@ -603,9 +653,9 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     rc.nb = nb;
     rc.inv_w = (R)nb / span;
     rc.bin_w = span / (R)nb;
-    const R K = (threshold + 1.0f) * vol_factor;
+    const R K = (threshold + 1.0f) * mass_factor;
     rc.K2 = K * K;
-    rc.expected = vol_factor * r_search * r_search * r_search;
+    rc.expected = mass_factor * r_search * r_search * r_search;
     rc.threshold = threshold;
     rc.window = (uint32_t)std::max(1, p.window);
     return rc;
@@ -808,16 +858,27 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       // (exodus_finder.c:2019-2030), then the growth of the rest. Under
       // displacement every survivor is grown: a void refusing it now may be
       // displaced before its turn.
-      if (displace)
+      // No witness on a weighted mesh either (1865-1868).
+      if (displace || weighted)
         SIFG_CUDA(cudaMemsetAsync(sreason, kRescaleOk, m, st_));
       else
         witness(mv, tv, rc, sv, vv, m, traffic + 2 * ri, st_, tm ? &tm->witness : nullptr);
-      grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_, tm ? &tm->growth : nullptr);
+      if (weighted)
+        grow_weighted(mv, tv, rc, sv, m, gbuf, gwbuf, kGrowCap, traffic + 2 * ri, st_,
+                      tm ? &tm->growth : nullptr);
+      else
+        grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_, tm ? &tm->growth : nullptr);
       // Each level of the extended reach, for the survivors whose crossing
       // still lies past the reach (exodus_finder.c:2060-2072).
-      for (uint32_t e = ext0; e < n_ext; e++)
-        grow(mv, ext_tv[e], shell_consts(rc, ext_rmin[e], ext_reach[e]), sv, m, gbuf, kGrowCap,
-             traffic + 2 * ri, st_, tm ? &tm->growth : nullptr, kRescaleBeyondSearch);
+      for (uint32_t e = ext0; e < n_ext; e++) {
+        const RungConstsT<R> ec = shell_consts(rc, ext_rmin[e], ext_reach[e]);
+        if (weighted)
+          grow_weighted(mv, ext_tv[e], ec, sv, m, gbuf, gwbuf, kGrowCap, traffic + 2 * ri, st_,
+                        tm ? &tm->growth : nullptr, kRescaleBeyondSearch);
+        else
+          grow(mv, ext_tv[e], ec, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_,
+               tm ? &tm->growth : nullptr, kRescaleBeyondSearch);
+      }
     }
 
     // 5. The order, on the host while the GPU grows spheres.

@@ -36,6 +36,9 @@ struct RunParamsT {
   // Recorded once the mesh is on the device, if it is still being copied
   // when the run starts: the first sphere growth waits for it.
   cudaEvent_t mesh_ready = nullptr;
+  // A weighted mesh's weights already checked (finite, non-negative) by the
+  // caller; else the run checks them on the device before it starts.
+  bool weights_checked = false;
   // Voids to start from (sif_finder_exodus_extras_t::prior), host memory:
   // accepted before the first rung and returned first (exodus_finder.c:
   // 1614-1622, 656-683).
@@ -132,6 +135,7 @@ class Engine {
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
   DevBuf vhead_, vnext_, dlist_;  // displacement: the linked void index, its lists
+  DevBuf gwbuf_, wcheck_;  // a weighted mesh: the wide windows' weights, the weight check
   DevBuf tpl_, gbuf_, traffic_, region_delta_, region_flat_;
   static constexpr uint32_t kExtMaxLevels = 32;  // EXT_MAX_LEVELS, exodus_finder.c:244
   DevBuf ext_tpl_[kExtMaxLevels];  // the extended reach's templates, one per level

@@ -20,6 +20,8 @@
 #include <math_constants.h>
 
 #include <algorithm>
+#include <cmath>
+#include <type_traits>
 
 #include "common.cuh"
 #include "finder.cuh"
@@ -583,6 +585,7 @@ template <class R>
 struct CellRange {
   uint32_t s, e;
   R ex, ey, ez;
+  uint32_t flat;  // the wrapped cell's flat index
 };
 
 // query_cell, src/finder/exodus_rescale.c:295-342.
@@ -602,6 +605,7 @@ __device__ __forceinline__ CellRange<R> query_cell(const MeshViewT<R>& m, const 
   const uint64_t flat = ((uint64_t)ix * N + iy) * N + iz;
   r.s = __ldg(m.offsets + flat);
   r.e = __ldg(m.offsets + flat + 1);
+  r.flat = (uint32_t)flat;
   return r;
 }
 
@@ -717,8 +721,9 @@ __device__ void bitonic_sort(R* buf, uint32_t p) {
 }
 
 // The cells of the template a warp walks, 32 at a time: `want(type, i)` says
-// whether a cell's range is looked up, `whole(type, count)` is then called on
-// the lane holding it (for counts), `particles(type)` whether its particles
+// whether a cell's range is looked up, `whole(type, count)` (or
+// `whole(type, count, flat)`, for a per-cell table) is then called on the
+// lane holding it (for counts), `particles(type)` whether its particles
 // are read, and `each(type, d2, p, i)` runs per particle read (i: its cell's
 // template index). `visited` and `read` count the lookups and the particles.
 template <class R, class Want, class Whole, class Particles, class Each>
@@ -733,14 +738,17 @@ __device__ __forceinline__ void walk_cells(const MeshViewT<R>& mesh, const Templ
   const uint32_t step = whole_warp ? 32u : kGrowWarps * 32;
   for (uint32_t c0 = first; c0 < tpl.count; c0 += step) {
     const uint32_t i = c0 + lane;
-    CellRange<R> c{0, 0, 0.f, 0.f, 0.f};
+    CellRange<R> c{0, 0, 0.f, 0.f, 0.f, 0};
     uint8_t type = 0;
     bool need = false;
     if (i < tpl.count) {
       type = __ldg(tpl.type + i);
       if (want(type, i)) {
         c = query_cell(mesh, tpl, i, ci, cj, ck, cx, cy, cz);
-        whole(type, c.e - c.s);
+        if constexpr (std::is_invocable_v<Whole, uint8_t, uint32_t, uint32_t>)
+          whole(type, c.e - c.s, c.flat);
+        else
+          whole(type, c.e - c.s);
         need = c.e > c.s && particles(type);
         visited++;
       }
@@ -1322,6 +1330,15 @@ __device__ __forceinline__ double collision_radius_warp(const VoidViewT<R>& v, R
     span[a] = hi - lo[a] + 1;
   }
   const uint32_t cells = (uint32_t)(span[0] * span[1] * span[2]);
+  // Only a void whose r* is below r_hi can decide anything (the caller
+  // compares the result with r_hi), and r* grows with the separation: it
+  // reaches r_hi at D0 = tot(r_hi) = r_hi + rj - f min(r_hi, rj), and D is at
+  // least d / scale. A float separation past scale * D0 by 1e-4 of it and
+  // 1e-5 of the box (far more than float rounding, of the positions too)
+  // rules the void out before any double arithmetic;
+  // the minimum over the rest is the same double whenever it is below r_hi.
+  const float halff = 0.5f * (float)box, boxf = (float)box, rhf = (float)r_hi, ff32 = (float)f;
+  const float scf = (float)scale;
   double best = CUDART_INF;
   for (uint32_t k = lane; k < cells; k += 32) {
     const int32_t a = lo[0] + (int32_t)(k / (uint32_t)(span[1] * span[2]));
@@ -1332,6 +1349,16 @@ __device__ __forceinline__ double collision_radius_warp(const VoidViewT<R>& v, R
                                      (((c % n) + n) % n));
     for (uint32_t q = __ldg(v.start + cell); q < __ldg(v.start + cell + 1); q++) {
       const uint32_t i = __ldg(v.ids + q);
+      {
+        float ex = fabsf((float)cx - (float)v.cx[i]), ey = fabsf((float)cy - (float)v.cy[i]),
+              ez = fabsf((float)cz - (float)v.cz[i]);
+        ex = ex > halff ? boxf - ex : ex;
+        ey = ey > halff ? boxf - ey : ey;
+        ez = ez > halff ? boxf - ez : ez;
+        const float rjf = (float)v.r[i];
+        const float d0 = (rhf + rjf - ff32 * fminf(rhf, rjf)) * scf * 1.0001f + 1e-5f * boxf;
+        if (ex * ex + ey * ey + ez * ez > d0 * d0) continue;
+      }
       const double rj = (double)v.r[i];
       double dx = fabs(__dsub_rn((double)cx, (double)v.cx[i]));
       double dy = fabs(__dsub_rn((double)cy, (double)v.cy[i]));
@@ -1515,6 +1542,415 @@ void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT
   }
   if (timer) timer->end(st);
 }
+
+// ---------------------------------------------------------------------------
+// Weighted sphere growth (sif__exodus_find_radius_weighted,
+// exodus_rescale.c:642-1037 with weighted set; resolve_bin 391-507).
+//
+// The same three stages as growth_kernel with every count a sum of weights:
+// whole core and shell cells from the mesh's per-cell sums in the early
+// refusal, whole core cells from them in the histogram, every other tracer by
+// its own weight; the density tests against mass_factor (rc.expected and
+// rc.K2 are built from it). The reference accumulates in double; here every
+// weight is a fixed-point integer (MeshViewT::wscale), so each sum is exact
+// and independent of the order the CTA adds in. Where the reference's double
+// sums are exact -- its weights' smallest unit times 2^53 above the total,
+// which the 63-bit sums here cover with room to spare -- the two agree bit
+// for bit; only a mesh whose weights span more than that could differ, and
+// then in the last bit of a sum. A window's tracers are sorted by distance
+// with their weights and tested outside-in through suffix sums of the
+// weights: the tracer at k encloses the window's top weight less everything
+// from k up, as the reference's walk has it when it reaches k. Tracers at the
+// same distance may sort in another order than the reference's quicksort
+// puts them; the radius is the same (the group passes where its last tracer
+// would, whose enclosed weight does not depend on the order).
+// ---------------------------------------------------------------------------
+constexpr uint32_t kWBuf = 1024;  // a window's pairs held in shared memory
+
+template <class R>
+__device__ __forceinline__ long long wfix(R w, R scale) {
+  if constexpr (sizeof(R) == 4)
+    return __float2ll_rn(__fmul_rn(w, scale));
+  else
+    return __double2ll_rn(__dmul_rn(w, scale));
+}
+
+// A weight sum as the reference's double accumulator holds it (exactly,
+// while that sum is exact), then rounded to the form's precision as its
+// (sif_real) casts do.
+template <class R>
+__device__ __forceinline__ R wreal(long long q, double winv) {
+  return (R)__dmul_rn(__ll2double_rn(q), winv);
+}
+
+// Ascending bitonic sort of key[0, p) carrying val, p a power of two.
+template <class R>
+__device__ void bitonic_sort_pairs(R* key, long long* val, uint32_t p) {
+  for (uint32_t k = 2; k <= p; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < p; i += kGrowT) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const R a = key[i], b = key[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            key[i] = b;
+            key[l] = a;
+            const long long t = val[i];
+            val[i] = val[l];
+            val[l] = t;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// v[k] = v[k] + v[k + 1] + ... + v[p - 1], in place, by the block: a
+// contiguous chunk per thread, the chunks' totals combined by warp 0.
+__device__ void suffix_sums(long long* v, uint32_t p, long long* tsum) {
+  static_assert(kGrowT == 256, "warp 0 combines 8 chunk totals per lane");
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t per = (p + kGrowT - 1) / kGrowT;
+  const uint32_t a = min(p, threadIdx.x * per), e = min(p, a + per);
+  long long t = 0;
+  for (uint32_t k = a; k < e; k++) t += v[k];
+  tsum[threadIdx.x] = t;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    long long loc[8], ls = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      loc[j] = tsum[threadIdx.x * 8 + j];
+      ls += loc[j];
+    }
+    long long incl = ls;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const long long y = __shfl_down_sync(0xffffffffu, incl, d);
+      if (lane + d < 32) incl += y;
+    }
+    long long after = incl - ls;
+#pragma unroll
+    for (int j = 7; j >= 0; j--) {
+      tsum[threadIdx.x * 8 + j] = after;
+      after += loc[j];
+    }
+  }
+  __syncthreads();
+  long long run = tsum[threadIdx.x];  // everything past this thread's chunk
+  for (uint32_t k = e; k > a; k--) {
+    run += v[k - 1];
+    v[k - 1] = run;
+  }
+  __syncthreads();
+}
+
+template <class R>
+constexpr size_t weighted_smem_bytes() {
+  return (2 * (size_t)kMaxBins + kWBuf) * sizeof(long long) + 2 * (size_t)kMaxBins * sizeof(uint32_t) +
+         kWBuf * sizeof(R);
+}
+
+template <class R>
+__global__ void __launch_bounds__(kGrowT) growth_weighted_kernel(
+    MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> sv,
+    R* __restrict__ gbuf, long long* __restrict__ gwbuf, uint32_t gcap,
+    unsigned long long* __restrict__ traffic, uint8_t only) {
+  extern __shared__ __align__(16) unsigned char wsm[];
+  long long* bw = (long long*)wsm;           // weight per bin
+  long long* belw = bw + kMaxBins;           // weight inside bin b's lower edge
+  long long* pwv = belw + kMaxBins;          // a window's weights (then their suffix sums)
+  uint32_t* bn = (uint32_t*)(pwv + kWBuf);   // tracers per bin (sizes the windows)
+  uint32_t* beln = bn + kMaxBins;            // tracers in the bins below b
+  R* pd2 = (R*)(beln + kMaxBins);            // a window's distances
+  __shared__ unsigned long long red64[2 * kGrowWarps];
+  __shared__ long long tsum[kGrowT];
+  __shared__ int redi[kGrowWarps];
+  __shared__ uint32_t collected;
+
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t n_surv = *sv.count;
+  const R ws = mesh.wscale;
+  const double winv = mesh.winv;
+
+  for (uint32_t s = blockIdx.x; s < n_surv; s += gridDim.x) {
+    if (only != kAllSurvivors ? sv.reason[s] != only : sv.reason[s] == kRescaleWitness) continue;
+    const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
+    const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
+                  ck = (int32_t)fmul(cz, mesh.inv_l);
+    uint8_t reason = kRescaleOk;
+    R radius = -1.0f;
+    unsigned long long read = 0, visited = 0;
+
+    for (uint32_t b = threadIdx.x; b < rc.nb; b += kGrowT) {
+      bw[b] = 0;
+      bn[b] = 0;
+    }
+    __syncthreads();
+
+    // 1. The early refusal's weight (exodus_rescale.c:738-782) and the
+    //    boundary cells' share of the histogram (794-865), from the same
+    //    distances; whole core and shell cells from the per-cell sums.
+    long long within = 0, core = 0, shell = 0;
+    walk_cells(
+        mesh, tpl, ci, cj, ck, cx, cy, cz, [](uint8_t, uint32_t) { return true; },
+        [&](uint8_t type, uint32_t cnt, uint32_t flat) {
+          if (cnt == 0) return;  // an empty cell is skipped (query_cell)
+          if (type == kCellCore) {
+            const long long q = wfix(__ldg(mesh.cell_w + flat), ws);
+            within += q;
+            core += q;
+          } else if (type == kCellShell) {
+            within += wfix(__ldg(mesh.cell_w + flat), ws);
+          }
+        },
+        [](uint8_t type) { return type == kCellStraddle || type == kCellEdge; },
+        [&](uint8_t, R d2, uint32_t p, uint32_t) {
+          const long long q = wfix(__ldg(mesh.w + p), ws);
+          if (d2 <= rc.rs2) within += q;
+          if (d2 <= rc.rc2) {
+            core += q;
+          } else if (d2 <= rc.rs2) {
+            const uint32_t b = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
+            atomicAdd((unsigned long long*)(bw + b), (unsigned long long)q);
+            atomicAdd(bn + b, 1u);
+            shell += q;
+          }
+        },
+        visited, read);
+    within = (long long)block_sum_u64((unsigned long long)within, red64);
+    if (!(within > 0)) {
+      reason = kRescaleEmpty;
+    } else if (fsub(fdiv(wreal<R>(within, winv), rc.expected), R(1.0f)) <= rc.threshold) {
+      reason = kRescaleBeyondSearch;
+    }
+
+    if (reason == kRescaleOk) {
+      // 2. The shell cells, tracer by tracer.
+      walk_cells(
+          mesh, tpl, ci, cj, ck, cx, cy, cz,
+          [](uint8_t type, uint32_t) { return type == kCellShell; }, [](uint8_t, uint32_t) {},
+          [](uint8_t) { return true; },
+          [&](uint8_t, R d2, uint32_t p, uint32_t) {
+            const long long q = wfix(__ldg(mesh.w + p), ws);
+            const uint32_t b = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
+            atomicAdd((unsigned long long*)(bw + b), (unsigned long long)q);
+            atomicAdd(bn + b, 1u);
+            shell += q;
+          },
+          visited, read);
+      unsigned long long uc = (unsigned long long)core, us = (unsigned long long)shell;
+      block_sum2_u64(uc, us, red64);
+      const long long total = (long long)uc + (long long)us;
+      if (!(total > 0)) {
+        reason = kRescaleEmpty;
+      } else if (fsub(fdiv(wreal<R>(total, winv), rc.expected), R(1.0f)) <= rc.threshold) {
+        reason = kRescaleBeyondSearch;
+      }
+      if (reason == kRescaleOk) {
+        // belw[b]: the core and the bins below b -- total less the bins from
+        // b up, the weight the skip test measures (914-957).
+        if (warp == 0) {
+          long long carry = (long long)uc;
+          uint32_t carry_n = 0;
+          for (uint32_t b0 = 0; b0 < rc.nb; b0 += 32) {
+            const uint32_t b = b0 + lane;
+            const long long v = b < rc.nb ? bw[b] : 0;
+            const uint32_t vn = b < rc.nb ? bn[b] : 0u;
+            long long x = v;
+            uint32_t xn = vn;
+            for (int d = 1; d < 32; d <<= 1) {
+              const long long y = __shfl_up_sync(0xffffffffu, x, d);
+              const uint32_t yn = __shfl_up_sync(0xffffffffu, xn, d);
+              if (lane >= (unsigned)d) {
+                x += y;
+                xn += yn;
+              }
+            }
+            if (b < rc.nb) {
+              belw[b] = carry + x - v;
+              beln[b] = carry_n + xn - vn;
+            }
+            carry += __shfl_sync(0xffffffffu, x, 31);
+            carry_n += __shfl_sync(0xffffffffu, xn, 31);
+          }
+        }
+        __syncthreads();
+
+        // 3. The walk: the highest bin with weight that the skip test does
+        //    not rule out, resolved with the bins below it.
+        int32_t cursor = (int32_t)rc.nb - 1;
+        reason = kRescaleBelowRung;
+        while (cursor >= 0) {
+          int best = -1;
+          for (int32_t b = threadIdx.x; b <= cursor; b += kGrowT) {
+            if (!(bw[b] > 0)) continue;  // no weight: skipped like an empty bin
+            const R hi = bin_hi(rc, b);
+            const R nm = wreal<R>(belw[b], winv);
+            if (!(fmul(nm, nm) > fmul(fmul(fmul(rc.K2, hi), hi), hi))) best = max(best, b);
+          }
+          best = block_max_int(best, redi);
+          if (best < 0) break;
+          const int32_t b_hi = best;
+          int32_t b_lo = b_hi - (int32_t)rc.window + 1;
+          if (b_lo < 0) b_lo = 0;
+          const uint32_t top_n = beln[b_hi] + bn[b_hi];
+          while (b_lo < b_hi && top_n - beln[b_lo] > kWBuf) b_lo++;
+          const uint32_t want = top_n - beln[b_lo];
+          R* kb = pd2;
+          long long* vb = pwv;
+          uint32_t cap = kWBuf;
+          if (want > kWBuf) {
+            kb = gbuf + (uint64_t)blockIdx.x * gcap;
+            vb = gwbuf + (uint64_t)blockIdx.x * gcap;
+            cap = gcap;
+          }
+          if (want > cap) {
+            reason = kRescaleOverflow;
+            break;
+          }
+          const R lo = fadd(rc.rc2, fmul((R)b_lo, rc.bin_w));
+          const R hi = bin_hi(rc, b_hi);
+          if (threadIdx.x == 0) collected = 0;
+          __syncthreads();
+          walk_cells(
+              mesh, tpl, ci, cj, ck, cx, cy, cz,
+              [&](uint8_t type, uint32_t i) {
+                return type != kCellCore && !(__ldg(tpl.max_d2 + i) < lo) &&
+                       !(__ldg(tpl.min_d2 + i) > hi);
+              },
+              [](uint8_t, uint32_t) {}, [](uint8_t) { return true; },
+              [&](uint8_t type, R d2, uint32_t p, uint32_t) {
+                if (type != kCellShell && !(d2 > rc.rc2 && d2 <= rc.rs2)) return;
+                const uint32_t bi = bin_of(d2, rc.rc2, rc.inv_w, rc.nb);
+                if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) return;
+                const uint32_t slot = atomicAdd(&collected, 1u);
+                if (slot < cap) {
+                  kb[slot] = d2;
+                  vb[slot] = wfix(__ldg(mesh.w + p), ws);
+                }
+              },
+              visited, read);
+          __syncthreads();
+          const uint32_t m = collected < cap ? collected : cap;
+          uint32_t p2 = 1;
+          while (p2 < m) p2 <<= 1;
+          for (uint32_t i = m + threadIdx.x; i < p2; i += kGrowT) {
+            kb[i] = real_inf<R>();
+            vb[i] = 0;
+          }
+          __syncthreads();
+          bitonic_sort_pairs(kb, vb, p2);
+          suffix_sums(vb, p2, tsum);
+          // Outside-in (405-438): the tracer at k encloses the window's top
+          // weight less its own and everything beyond it.
+          const long long top_w = belw[b_hi] + bw[b_hi];
+          int found = -1;
+          for (uint32_t k = threadIdx.x; k < m; k += kGrowT) {
+            const R d2 = kb[k];
+            if (d2 == R(0)) continue;
+            const R wi = wreal<R>(top_w - vb[k], winv);
+            const R d2c = fmul(fmul(d2, d2), d2);
+            if (fmul(wi, wi) <= fmul(rc.K2, d2c)) found = max(found, (int)k);
+          }
+          found = block_max_int(found, redi);
+          if (found >= 0) {
+            radius = fsqrt(kb[found]);
+            reason = kRescaleOk;
+            break;
+          }
+          cursor = b_lo - 1;
+          __syncthreads();
+        }
+      }
+    }
+    if (traffic) {
+      const unsigned long long v = __reduce_add_sync(0xffffffffu, (unsigned)visited);
+      if (lane == 0) {
+        if (read) atomicAdd(traffic, read);
+        if (v) atomicAdd(traffic + 1, v);
+      }
+    }
+    if (threadIdx.x == 0) {
+      sv.r[s] = reason == kRescaleOk ? radius : -1.0f;
+      sv.reason[s] = reason;
+    }
+    __syncthreads();
+  }
+}
+
+template <class R>
+void grow_weighted(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
+                   uint32_t max_survivors, R* gbuf, long long* gwbuf, uint32_t gcap,
+                   unsigned long long* traffic, cudaStream_t st, KernelTimer* timer, uint8_t only) {
+  if (max_survivors == 0) return;
+  constexpr size_t smem = weighted_smem_bytes<R>();
+  thread_local bool attr = false;  // the attribute is per thread's view of the function
+  if (!attr) {
+    SIFG_CUDA(cudaFuncSetAttribute(growth_weighted_kernel<R>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
+  if (timer) timer->begin(st);
+  growth_weighted_kernel<R><<<g, kGrowT, smem, st>>>(mesh, tpl, rc, s, gbuf, gwbuf, gcap, traffic,
+                                                    only);
+  SIFG_LAUNCH_CHECK();
+  if (timer) timer->end(st);
+}
+
+// sif__exodus_check_weights (exodus_finder.c:1039-1106): by the bits, so a
+// NaN or an infinity is caught whatever the compiler assumes; a negative
+// zero is a zero.
+template <class R>
+__global__ void check_weights_kernel(const R* __restrict__ w, uint64_t n,
+                                     unsigned long long* __restrict__ counts) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  unsigned neg = 0, bad = 0;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+    if constexpr (sizeof(R) == 4) {
+      const uint32_t b = __float_as_uint(w[p]);
+      bad += ((b >> 23) & 0xffu) == 0xffu;
+      neg += ((b >> 23) & 0xffu) != 0xffu && (b >> 31) && (b << 1);
+    } else {
+      const uint64_t b = (uint64_t)__double_as_longlong(w[p]);
+      bad += ((b >> 52) & 0x7ffu) == 0x7ffu;
+      neg += ((b >> 52) & 0x7ffu) != 0x7ffu && (b >> 63) && (b << 1);
+    }
+  }
+  neg = __reduce_add_sync(0xffffffffu, neg);
+  bad = __reduce_add_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31u) == 0) {
+    if (neg) atomicAdd(counts, (unsigned long long)neg);
+    if (bad) atomicAdd(counts + 1, (unsigned long long)bad);
+  }
+}
+
+template <class R>
+void check_weights(const R* w, uint64_t n, unsigned long long* counts, cudaStream_t st) {
+  SIFG_CUDA(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), st));
+  check_weights_kernel<R><<<grid_for(n, 256, 152u * 16u), 256, 0, st>>>(w, n, counts);
+  SIFG_LAUNCH_CHECK();
+}
+
+void weight_fixed_point(double bound, double* wscale, double* winv) {
+  int e = 0;
+  std::frexp(bound > 0.0 ? bound : 1.0, &e);  // bound < 2^e
+  const int s = std::min(100, std::max(-100, 58 - e));
+  *wscale = std::ldexp(1.0, s);
+  *winv = std::ldexp(1.0, -s);
+}
+
+template void grow_weighted<float>(MeshViewT<float>, TemplateViewT<float>, RungConstsT<float>,
+                                   SurvivorsT<float>, uint32_t, float*, long long*, uint32_t,
+                                   unsigned long long*, cudaStream_t, KernelTimer*, uint8_t);
+template void grow_weighted<double>(MeshViewT<double>, TemplateViewT<double>, RungConstsT<double>,
+                                    SurvivorsT<double>, uint32_t, double*, long long*, uint32_t,
+                                    unsigned long long*, cudaStream_t, KernelTimer*, uint8_t);
+template void check_weights<float>(const float*, uint64_t, unsigned long long*, cudaStream_t);
+template void check_weights<double>(const double*, uint64_t, unsigned long long*, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Survivor hash

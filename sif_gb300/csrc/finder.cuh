@@ -43,6 +43,14 @@ struct MeshViewT {
   R box;
   R inv_l;  // 1 / cell_length
   const float4* xyzw;  // the float form's 16-byte position records, or NULL (x, y, z)
+  // A weighted mesh: weights in mesh order and per-cell sums (NULL when
+  // unweighted), and the fixed point every sum of them is taken in -- a
+  // weight w counts llrint(w * wscale) units of winv -- so that the sums are
+  // exact and do not depend on the order the GPU adds in.
+  const R* w = nullptr;
+  const R* cell_w = nullptr;
+  R wscale = 0;
+  double winv = 0;
 };
 
 template <class R>
@@ -197,6 +205,24 @@ template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
           uint32_t max_survivors, R* gbuf, uint32_t gcap, unsigned long long* traffic,
           cudaStream_t st, KernelTimer* timer, uint8_t only = kAllSurvivors);
+// The weighted sphere growth (sif__exodus_find_radius_weighted,
+// exodus_rescale.c:642-1037 with the weighted flag): mesh.w set. A CTA per
+// survivor; gbuf and gwbuf (gcap entries per CTA each) hold the windows too
+// wide for shared memory.
+template <class R>
+void grow_weighted(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
+                   uint32_t max_survivors, R* gbuf, long long* gwbuf, uint32_t gcap,
+                   unsigned long long* traffic, cudaStream_t st, KernelTimer* timer,
+                   uint8_t only = kAllSurvivors);
+// Counts a weighted mesh's negative (below zero; a negative zero is not)
+// and non-finite weights into counts[0], counts[1] (device, zeroed here).
+template <class R>
+void check_weights(const R* w, uint64_t n, unsigned long long* counts, cudaStream_t st);
+// The fixed-point scale of a weighted mesh's sums (MeshViewT::wscale and
+// winv): 2^s with s chosen so that `bound` (the most weight any one sum can
+// reach) stays below 2^58 units.
+void weight_fixed_point(double bound, double* wscale, double* winv);
+
 // Which growth kernel runs: 0 by the survivor count (a CTA per survivor for
 // few, a warp per survivor for many), 1 always a CTA, 2 always a warp. The
 // radii are the same either way (tests run both).

@@ -59,20 +59,23 @@ void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st,
                         uint32_t* sums_scratch = nullptr);
 
 // --- cic.cu ---
-size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n);
+size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n, bool weighted = false);
 // bounds (lo, hi) and outside, when given: the deposit also adds to
 // *outside the particles outside [lo, hi] (the box check from its own reads).
 // sorted, when given, is recorded once the particles are in tile order: what
 // follows (the deposit proper) is bound by shared-memory atomics, not by HBM.
+// w: per-particle weights (device), or NULL for 1 each; the scratch is then
+// cic_scratch_bytes(n_particles, n, true).
 void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_particles,
                  uint32_t n, float box, float* grid, void* scratch, cudaStream_t st,
                  KernelTimer* timer, const float* bounds = nullptr,
-                 unsigned long long* outside = nullptr, cudaEvent_t sorted = nullptr);
+                 unsigned long long* outside = nullptr, cudaEvent_t sorted = nullptr,
+                 const float* w = nullptr);
 // The FP64 form's deposit: scratch is cic_f64_scratch_bytes(n).
 size_t cic_f64_scratch_bytes(uint32_t n);
 void cic_deposit_f64(const double* x, const double* y, const double* z, uint64_t n_particles,
                      uint32_t n, double box, double* grid, void* scratch, cudaStream_t st,
-                     KernelTimer* timer);
+                     KernelTimer* timer, const double* w = nullptr);
 size_t density_contrast_scratch_bytes();
 // The mean (a fixed summation order) into d_scratch, then v * (1 / mean) - 1
 // in place unless mean_only; contrast_mean() is where the mean sits.
@@ -102,6 +105,11 @@ struct DeviceMeshT {
   // The float form's positions as 16-byte records (x, y, z, unused), one
   // load per particle, in place of x, y, z: the unordered build writes them.
   float4* xyzw = nullptr;
+  // A weighted mesh (sif_chain_mesh_t::weights, cell_weights, total_weight):
+  // weights in mesh order, per-cell sums; w NULL when unweighted.
+  R* w = nullptr;
+  R* cell_w = nullptr;
+  double total_weight = 0.0;
 };
 using DeviceMesh = DeviceMeshT<float>;
 // Scratch bytes of a mesh build in either form (the larger records).
@@ -117,5 +125,12 @@ template <class R>
 void mesh_build(const R* x, const R* y, const R* z, uint64_t n_particles, DeviceMeshT<R>& m,
                 void* scratch, cudaStream_t st, KernelTimer* timer, uint32_t* scan_sums = nullptr,
                 bool canonical = true);
+// A canonical mesh's weight columns from the field's weights (device, source
+// order): m.w (n_particles) and m.cell_w (n_cells^3) written, the total to
+// *d_total (device). scratch: mesh_weights_scratch_bytes(n_cells).
+size_t mesh_weights_scratch_bytes(uint32_t n_cells);
+template <class R>
+void mesh_weights(const R* field_w, DeviceMeshT<R>& m, void* scratch, double* d_total,
+                  cudaStream_t st);
 
 }  // namespace sifg

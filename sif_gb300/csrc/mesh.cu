@@ -254,6 +254,76 @@ void mesh_build(const R* x, const R* y, const R* z, uint64_t n_particles, Device
   m.n_particles = n_particles;
 }
 
+// ---------------------------------------------------------------------------
+// A weighted mesh's columns (chain_mesh.c:800-801, 624-672): each entry's
+// weight is the field's at its source index; each cell's weights summed in
+// double in mesh order and stored in the form's precision; the total over 64
+// fixed blocks of cells, each block's cell sums added in order, the blocks
+// then added in order. Every sum in the reference's order, so every bit is
+// the reference's.
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void gather_weights_kernel(const R* __restrict__ fw, const uint32_t* __restrict__ orig,
+                                      uint64_t n, R* __restrict__ out) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride)
+    out[p] = fw[orig[p]];
+}
+
+template <class R>
+__global__ void cell_weight_kernel(const uint32_t* __restrict__ offsets, const R* __restrict__ w,
+                                   uint64_t cells, double* __restrict__ csum, R* __restrict__ cw) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += stride) {
+    double s = 0.0;
+    for (uint32_t p = offsets[c]; p < offsets[c + 1]; p++) s = __dadd_rn(s, (double)w[p]);
+    csum[c] = s;
+    cw[c] = (R)s;
+  }
+}
+
+constexpr int kWeightBlocks = 64;  // WEIGHT_BLOCKS, chain_mesh.c:642
+
+__global__ void weight_total_kernel(const double* __restrict__ csum, uint64_t cells,
+                                    double* __restrict__ total) {
+  __shared__ double bt[kWeightBlocks];
+  const uint64_t block = (cells + kWeightBlocks - 1) / kWeightBlocks;
+  const uint64_t c0 = (uint64_t)threadIdx.x * block;
+  const uint64_t c1 = c0 + block < cells ? c0 + block : cells;
+  double s = 0.0;
+  for (uint64_t c = c0; c < c1; c++) s = __dadd_rn(s, csum[c]);
+  bt[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int b = 0; b < kWeightBlocks; b++) t = __dadd_rn(t, bt[b]);
+    *total = t;
+  }
+}
+
+size_t mesh_weights_scratch_bytes(uint32_t n_cells) {
+  return (size_t)n_cells * n_cells * n_cells * sizeof(double) + 256;
+}
+
+template <class R>
+void mesh_weights(const R* field_w, DeviceMeshT<R>& m, void* scratch, double* d_total,
+                  cudaStream_t st) {
+  const uint64_t cells = (uint64_t)m.n_cells * m.n_cells * m.n_cells;
+  gather_weights_kernel<R><<<grid_for(m.n_particles, 256, 152u * 16u), 256, 0, st>>>(
+      field_w, m.orig, m.n_particles, m.w);
+  SIFG_LAUNCH_CHECK();
+  double* csum = (double*)scratch;
+  cell_weight_kernel<R><<<grid_for(cells, 128, 152u * 32u), 128, 0, st>>>(m.offsets, m.w, cells,
+                                                                         csum, m.cell_w);
+  SIFG_LAUNCH_CHECK();
+  weight_total_kernel<<<1, kWeightBlocks, 0, st>>>(csum, cells, d_total);
+  SIFG_LAUNCH_CHECK();
+}
+
+template void mesh_weights<float>(const float*, DeviceMeshT<float>&, void*, double*, cudaStream_t);
+template void mesh_weights<double>(const double*, DeviceMeshT<double>&, void*, double*,
+                                   cudaStream_t);
+
 template void mesh_build<float>(const float*, const float*, const float*, uint64_t,
                                 DeviceMeshT<float>&, void*, cudaStream_t, KernelTimer*, uint32_t*,
                                 bool);

@@ -78,6 +78,31 @@ def chain_mesh(x, y, z, n_cells, box, with_indices=True):
     return mx, my, mz, offs, orig
 
 
+def cic_weighted(x, y, z, w, n_grid, box):
+    """The CIC density of weighted device particles (one weight each)."""
+    import torch
+
+    grid = torch.empty(n_grid ** 3, dtype=_form(x)[1], device=x.device)
+    _check(_fn("sifg_cic_weighted_device", x)(_ptr(x), _ptr(y), _ptr(z), _ptr(w), x.numel(),
+                                              n_grid, box, _ptr(grid)), "cic_weighted")
+    return grid
+
+
+def mesh_weights(field_w, mesh, n_cells):
+    """A mesh's weight columns from the field's weights: (w in mesh order,
+    per-cell sums, total). mesh = chain_mesh(..., with_indices=True)."""
+    import torch
+
+    offs, orig = mesh[3], mesh[4]
+    w = torch.empty_like(field_w)
+    cw = torch.empty(n_cells ** 3, dtype=field_w.dtype, device=field_w.device)
+    tot = C.c_double(0.0)
+    _check(_fn("sifg_mesh_weights_device", field_w)(_ptr(field_w), _ptr(orig), field_w.numel(),
+                                                    _ptr(offs), n_cells, _ptr(w), _ptr(cw),
+                                                    C.byref(tot)), "mesh_weights")
+    return w, cw, tot.value
+
+
 def contrast_vjp(x, y, z, n_grid, box, g):
     """dL/dx, dL/dy, dL/dz for g = dL/d(delta), delta the CIC density contrast."""
     import torch
@@ -116,9 +141,10 @@ def _catalogue_arrays(cap, dtype=np.float32):
 
 
 def exodus(delta, n_grid, box, mesh, mesh_cells, radii, threshold, overlap=0.0, options=0,
-           inject=None, capacity=1 << 22, prior=None):
+           inject=None, capacity=1 << 22, prior=None, weights=None):
     """The finder on device data. mesh = (mx, my, mz, offsets, ...);
-    prior: (cx, cy, cz, r) host arrays, voids to start from."""
+    prior: (cx, cy, cz, r) host arrays, voids to start from; weights: a
+    weighted mesh's (w, cell_w, total_weight), as mesh_weights gives them."""
     _, _, nt = _form(delta)
     radii = np.ascontiguousarray(radii, dtype=nt)
     cols = _catalogue_arrays(capacity, nt)
@@ -127,13 +153,17 @@ def exodus(delta, n_grid, box, mesh, mesh_cells, radii, threshold, overlap=0.0, 
     packed = np.ascontiguousarray(np.concatenate([np.asarray(c, nt) for c in prior])) \
         if prior is not None else None
     n_prior = len(prior[0]) if prior is not None else 0
-    st = _fn("sifg_exodus_device", delta)(_ptr(delta), n_grid, box, _ptr(mx), _ptr(my), _ptr(mz),
-                                _ptr(offs), mx.numel(), mesh_cells,
-                                radii.ctypes.data_as(C.c_void_p), len(radii), threshold, overlap,
-                                options, _ptr(inject),
-                                packed.ctypes.data_as(C.c_void_p) if packed is not None else None,
-                                n_prior, *[c.ctypes.data_as(C.c_void_p) for c in cols],
-                                capacity, C.byref(n))
+    tail = (radii.ctypes.data_as(C.c_void_p), len(radii), threshold, overlap, options,
+            _ptr(inject), packed.ctypes.data_as(C.c_void_p) if packed is not None else None,
+            n_prior, *[c.ctypes.data_as(C.c_void_p) for c in cols], capacity, C.byref(n))
+    if weights is None:
+        st = _fn("sifg_exodus_device", delta)(_ptr(delta), n_grid, box, _ptr(mx), _ptr(my),
+                                              _ptr(mz), _ptr(offs), mx.numel(), mesh_cells, *tail)
+    else:
+        w, cw, tot = weights
+        st = _fn("sifg_exodus_weighted_device", delta)(
+            _ptr(delta), n_grid, box, _ptr(mx), _ptr(my), _ptr(mz), _ptr(offs), _ptr(w), _ptr(cw),
+            float(tot), mx.numel(), mesh_cells, *tail)
     _check(st, "exodus")
     return tuple(c[: n.value].copy() for c in cols)
 

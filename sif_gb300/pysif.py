@@ -40,9 +40,11 @@ def system_finalise():
 
 
 class Field:
-    """Particle positions (float32, in [0, box))."""
+    """Particle positions (float32, in [0, box)) and, optionally, per-particle
+    weights (a mass, a luminosity, a selection weight; None: every particle
+    counts 1), which the CIC deposit, the mesh and the finder all use."""
 
-    def __init__(self, x, y, z):
+    def __init__(self, x, y, z, weights=None):
         lib = _lib.load()
         x, y, z = (np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z))
         if not (len(x) == len(y) == len(z)):
@@ -51,15 +53,38 @@ class Field:
         if not self._ptr:
             raise MemoryError("field")
         _check(lib.sif_field_assign_positions(self._ptr, _P(x), _P(y), _P(z)), "Field")
+        if weights is not None:
+            w = np.ascontiguousarray(weights, dtype=np.float32)
+            if w.shape != x.shape:
+                raise ValueError("weights: not one per particle")
+            _check(lib.sif_field_assign_weights(self._ptr, _P(w)), "Field")
 
     @property
     def n_particles(self):
         return self._ptr.contents.n_particles if self._ptr else 0
 
+    @property
+    def has_weights(self):
+        return bool(self._ptr and self._ptr.contents.weights)
+
+    @property
+    def weights(self):
+        """The weights (a copy), or None for an unweighted field."""
+        if not self.has_weights:
+            return None
+        f = self._ptr.contents
+        return np.ctypeslib.as_array(f.weights, shape=(f.n_particles,)).copy()
+
     def __del__(self):
         if getattr(self, "_ptr", None):
             _lib.load().sif_field_free(self._ptr)
             self._ptr = None
+
+
+def field_from_numpy(x, y, z, *, weights=None):
+    """pysif.field_from_numpy for Cartesian positions: a new Field with its
+    particles (and weights, if given) copied out of the arrays."""
+    return Field(x, y, z, weights=weights)
 
 
 class Grid:
@@ -119,6 +144,25 @@ class ChainMesh:
         idx = np.ctypeslib.as_array(m.original_indices, shape=(n,)).copy() \
             if m.original_indices else None
         return col(m.x), col(m.y), col(m.z), offs, idx
+
+    @property
+    def weights(self):
+        """Per-particle weights in mesh order (a copy), or None unweighted."""
+        m = self._ptr.contents
+        return (np.ctypeslib.as_array(m.weights, shape=(m.n_particles,)).copy()
+                if m.weights else None)
+
+    @property
+    def cell_weights(self):
+        """Each cell's total weight (a copy), or None unweighted."""
+        m = self._ptr.contents
+        return (np.ctypeslib.as_array(m.cell_weights, shape=(m.total_cells,)).copy()
+                if m.cell_weights else None)
+
+    @property
+    def total_weight(self):
+        """The mesh's total weight (its tracer count when unweighted)."""
+        return float(self._ptr.contents.total_weight)
 
     def __del__(self):
         if getattr(self, "_ptr", None):

@@ -66,6 +66,20 @@ def golden_box32_displace():
 
 
 @pytest.fixture(scope="session")
+def golden_box32_weighted():
+    """Weighted meshes through the reference: the "rand" and "holes" sets
+    (positions, weights, weighted contrast, mesh with its weight columns,
+    captured fields, catalogues)."""
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32_weighted.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_box32_weighted_f64():
+    """The "rand" weighted set through the reference's SIF_USE_DOUBLE build."""
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32_weighted_f64.npz")))
+
+
+@pytest.fixture(scope="session")
 def golden_box32_displace_f64():
     """The displacement box through the reference's SIF_USE_DOUBLE build."""
     return dict(np.load(os.path.join(GOLDEN, "golden_box32_displace_f64.npz")))

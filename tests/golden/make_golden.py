@@ -42,6 +42,19 @@ golden_box32_extend.npz, golden_box32_extend_f64.npz -- the same positions
   excursion-peak preset less its displacement) it changes 61 of 355 radii.
   The contrast, the mesh, the 8 fields the reference's own run smoothed, and
   its catalogues with and without the extended reach.
+golden_box32_weighted.npz, golden_box32_weighted_f64.npz -- weighted meshes
+  (sif_field_assign_weights on both the grid's field and the mesh's). Two
+  sets, each through the reference's whole path at threshold -0.7 and
+  ladder(8, 24, 0.15) (8 rungs): "rand", BOX32's positions (the f64 file
+  with its jitter) with seeded weights, a fifth of them 0 and the rest
+  uniform in [0.5, 1.5) as float32; "holes" (float file only), 32^3
+  uniform positions whose weights are 0 inside three spheres and 1
+  elsewhere, so that the voids exist only in the weights. Per set: the
+  positions and weights, the weighted contrast, the mesh with its weight
+  columns (weights in mesh order, per-cell sums, total), the 8 fields the
+  reference's own run smoothed, and its catalogues for several option sets
+  on them. The generator also checks that weights of 1 and of 4 give the
+  unweighted catalogue bit for bit, as the reference's own test does.
 """
 import os
 import sys
@@ -263,6 +276,102 @@ def make_box32_displace(path, v="strict"):
     print(f"{path}: " + ", ".join(f"{n} {len(out[f'cat_{n}_r'])}" for n, _, _ in DISPLACE_SETS))
 
 
+WEIGHTED = dict(BOX32, r0=8.0, top=3.0, step=0.15)
+WEIGHTED_SETS = [
+    ("default", 0.0, 0),
+    ("minima", 0.0, abi.SIF_FINDER_SEEDS_MINIMA),
+    ("extend_minima_f1", 1.0, abi.SIF_FINDER_SEEDS_MINIMA | abi.SIF_FINDER_EXTEND_REACH),
+    ("peak", 1.0, abi.SIF_FINDER_SEEDS_MINIMA | abi.SIF_FINDER_EXTEND_REACH | abi.SIF_FINDER_DISPLACE),
+    ("lagrangian", 0.0, abi.SIF_FINDER_LAGRANGIAN_OVERLAP),
+]
+HOLES = [((32.0, 32.0, 32.0), 18.0), ((90.0, 70.0, 40.0), 14.0), ((60.0, 100.0, 96.0), 20.0)]
+
+
+def weighted_inputs(name, v="strict"):
+    """Positions and weights of a weighted set (see the module docstring)."""
+    p = WEIGHTED
+    n3 = p["n"] ** 3
+    if name == "rand":
+        x, y, z = synth.zeldovich(p["n"], p["box"], p["rms_disp"], p["seed"])
+        rng = np.random.default_rng(p["seed"] + 2000)
+        w = rng.uniform(0.5, 1.5, n3).astype(np.float32)
+        w[rng.random(n3) < 0.2] = 0.0
+        if v == "f64":
+            jr = np.random.default_rng(p["seed"] + 1000)  # BOX32's f64 jitter
+
+            def jitter(a):
+                u = a.astype(np.float64) + jr.uniform(-1e-4, 1e-4, a.shape)
+                u = np.where(u < 0.0, u + p["box"], u)
+                return np.where(u >= p["box"], u - p["box"], u)
+
+            x, y, z = jitter(x), jitter(y), jitter(z)
+        return x, y, z, w
+    rng = np.random.default_rng(p["seed"] + 3000)
+    pos = (rng.random((3, n3)) * p["box"]).astype(np.float32)
+    pos = np.where(pos >= np.float32(p["box"]), np.float32(0.0), pos)
+    w = np.ones(n3, np.float32)
+    for c, r in HOLES:
+        d = pos.astype(np.float64) - np.array(c)[:, None]
+        d -= p["box"] * np.round(d / p["box"])
+        w[(d ** 2).sum(0) < r * r] = 0.0
+    return pos[0], pos[1], pos[2], w
+
+
+def _ref_run(lib, x, y, z, w, radii, kw):
+    p = WEIGHTED
+    f = R.RefField(lib, x, y, z, weights=w, **kw)
+    g = R.RefGrid(lib, p["n"], p["box"], **kw)
+    g.assign_cic(f)
+    g.to_contrast()
+    m = R.RefMesh(lib, p["mesh"], p["box"], f)
+    return f, g, m
+
+
+def make_box32_weighted(path, v="strict"):
+    p = WEIGHTED
+    real = np.float64 if v == "f64" else np.float32
+    kw = dict(variant=v) if v == "f64" else {}
+    radii = synth.ladder(p["r0"], p["top"] * p["r0"], p["step"]).astype(real)
+    lib = R.load(v, 4, abi.SIF_LOG_LEVEL_ERROR)
+    out = dict(radii=radii, params=np.array([p["n"], p["box"], p["rms_disp"], p["seed"], p["r0"],
+                                             p["threshold"], p["mesh"]], np.float64))
+    for name in (("rand", "holes") if v == "strict" else ("rand",)):
+        x, y, z, w = weighted_inputs(name, v)
+        f, g, m = _ref_run(lib, x, y, z, w, radii, kw)
+        mx, my, mz, offs, idx = m.arrays(**kw)
+        mw, cw, tot = m.weights(**kw)
+        delta = g.values()  # before the run smooths the grid in place and restores it
+        fields = np.zeros((len(radii), p["n"] ** 3), real)
+        R.exodus_raw(lib, g, m, radii, p["threshold"], capture=fields, **kw)
+        out.update({f"{name}_{k}": a for k, a in dict(
+            x=x, y=y, z=z, w=w, delta=delta, mesh_x=mx, mesh_y=my, mesh_z=mz,
+            mesh_offsets=offs, mesh_index=idx, mesh_w=mw, mesh_cell_w=cw, fields=fields).items()})
+        out[f"{name}_total_weight"] = np.array(tot)
+        for oname, overlap, opt in WEIGHTED_SETS:
+            c = R.exodus_raw(lib, g, m, radii, p["threshold"], overlap, opt, inject=fields, **kw)
+            for k, col in zip(("cx", "cy", "cz", "r"), c):
+                out[f"{name}_cat_{oname}_{k}"] = col
+            out[f"{name}_cat_{oname}_opt"] = np.array([overlap, opt], np.float64)
+        m.free()
+        g.free()
+        f.free()
+        print(f"{path} {name}: " + ", ".join(
+            f"{o} {len(out[f'{name}_cat_{o}_r'])}" for o, _, _ in WEIGHTED_SETS))
+    # Weights of 1 and of 4 change nothing, bit for bit (the grid through the
+    # CIC deposit, the rescaling through the mesh).
+    x, y, z, _ = weighted_inputs("rand", v)
+    cats = []
+    for w in (None, np.ones(len(x), np.float32), np.full(len(x), 4.0, np.float32)):
+        f, g, m = _ref_run(lib, x, y, z, w, radii, kw)
+        cats.append(R.exodus_raw(lib, g, m, radii, p["threshold"], **kw))
+        m.free()
+        g.free()
+        f.free()
+    for c in cats[1:]:
+        assert all(np.array_equal(a, b) for a, b in zip(c, cats[0])), "uniform weights changed the run"
+    np.savez_compressed(path, **out)
+
+
 def positions_sha256(x, y, z):
     import hashlib
 
@@ -290,6 +399,10 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "workload_a":
         make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))
         sys.exit(0)
+    if len(sys.argv) > 1 and sys.argv[1] == "weighted":
+        make_box32_weighted(os.path.join(HERE, "golden_box32_weighted.npz"))
+        make_box32_weighted(os.path.join(HERE, "golden_box32_weighted_f64.npz"), "f64")
+        sys.exit(0)
     if len(sys.argv) > 1 and sys.argv[1] == "displace":
         make_box32_displace(os.path.join(HERE, "golden_box32_displace.npz"))
         make_box32_displace(os.path.join(HERE, "golden_box32_displace_f64.npz"), "f64")
@@ -300,4 +413,6 @@ if __name__ == "__main__":
     make_box32_extend(os.path.join(HERE, "golden_box32_extend_f64.npz"), "f64")
     make_box32_displace(os.path.join(HERE, "golden_box32_displace.npz"))
     make_box32_displace(os.path.join(HERE, "golden_box32_displace_f64.npz"), "f64")
+    make_box32_weighted(os.path.join(HERE, "golden_box32_weighted.npz"))
+    make_box32_weighted(os.path.join(HERE, "golden_box32_weighted_f64.npz"), "f64")
     make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))

@@ -326,3 +326,69 @@ def test_fp64_golden_mesh_is_the_double_cell_sort(golden_box32_f64):
     assert np.array_equal(g["mesh_x"], g["x"][order])
     offs = np.concatenate([[0], np.cumsum(np.bincount(key, minlength=nm ** 3))])
     assert np.array_equal(g["mesh_offsets"].astype(np.int64), offs)
+
+
+WEIGHTED_SETS = ["default", "minima", "extend_minima_f1", "peak", "lagrangian"]
+
+
+@pytest.mark.parametrize("which", ["rand", "holes"])
+def test_oracle_weighted_mesh_and_contrast_match_golden(oracle, golden_box32_weighted, which):
+    """A weighted field's mesh columns (chain_mesh.c:624-672, 800-801: the
+    weights in mesh order, the per-cell double sums as float, the total over
+    64 blocks) and its weighted float CIC (grid.c:635-639) then contrast: the
+    reference's, bit for bit."""
+    g = golden_box32_weighted
+    n, box, n_mesh = int(g["params"][0]), float(g["params"][1]), int(g["params"][6])
+    x, y, z, w = (g[f"{which}_{k}"] for k in "xyzw")
+    m = oracle.OracleMesh(x, y, z, n_mesh, box, weights=w)
+    assert np.array_equal(m.orig, g[f"{which}_mesh_index"])
+    assert same_bits(m.w, g[f"{which}_mesh_w"]) and same_bits(m.cell_w, g[f"{which}_mesh_cell_w"])
+    assert m.total_weight == float(g[f"{which}_total_weight"])
+    d = oracle.density_contrast(oracle.cic_float(x, y, z, n, box, weights=w))
+    assert same_bits(d, g[f"{which}_delta"])
+
+
+@pytest.mark.parametrize("which,name", [("rand", s) for s in WEIGHTED_SETS] + [("holes", "default")])
+def test_oracle_weighted_catalogue_matches_golden(oracle, golden_box32_weighted, which, name):
+    """sif__exodus_find_radius_weighted (exodus_rescale.c:642-1037): double
+    sums of weights in the reference's order, the refinement's pairs in its
+    quicksort order, mass_factor in every density test, no collision witness
+    -- the reference's catalogue bit for bit, under every option set recorded
+    (the excursion-peak preset's displacement among them); on "holes" the
+    three voids that exist only in the weights."""
+    g = golden_box32_weighted
+    n, box, thr, n_mesh = (int(g["params"][0]), float(g["params"][1]), float(g["params"][5]),
+                           int(g["params"][6]))
+    overlap, opt = g[f"{which}_cat_{name}_opt"]
+    m = oracle.OracleMesh.from_arrays(
+        g[f"{which}_mesh_x"], g[f"{which}_mesh_y"], g[f"{which}_mesh_z"],
+        g[f"{which}_mesh_offsets"], n_mesh, box, w=g[f"{which}_mesh_w"],
+        cell_w=g[f"{which}_mesh_cell_w"], total_weight=float(g[f"{which}_total_weight"]))
+    cat = oracle.exodus(g[f"{which}_delta"], m, g["radii"], n, box, thr, float(overlap), int(opt),
+                        n_threads=2, inject=g[f"{which}_fields"])
+    want = tuple(g[f"{which}_cat_{name}_{k}"] for k in ("cx", "cy", "cz", "r"))
+    assert len(cat[0]) == len(want[0])
+    assert same_catalogue(cat, want)
+    if which == "holes":
+        assert len(want[0]) == 3
+
+
+def test_oracle_refuses_negative_or_nonfinite_weights(oracle, golden_box32_weighted):
+    """exodus_finder.c:1076-1106: a negative or non-finite weight, or no total
+    weight, is refused before any rung runs; a negative zero passes."""
+    g = golden_box32_weighted
+    n, box, thr, n_mesh = (int(g["params"][0]), float(g["params"][1]), float(g["params"][5]),
+                           int(g["params"][6]))
+    base = g["rand_mesh_w"]
+    cols = [g[f"rand_mesh_{k}"] for k in ("x", "y", "z", "offsets")]
+    for bad, ok in ((-1.0, False), (np.nan, False), (np.inf, False), (-0.0, True)):
+        w = base.copy()
+        w[len(w) // 2] = bad
+        m = oracle.OracleMesh.from_arrays(*cols, n_mesh, box, w=w, cell_w=g["rand_mesh_cell_w"],
+                                          total_weight=float(g["rand_total_weight"]))
+        if ok:
+            oracle.exodus(g["rand_delta"], m, g["radii"][:2], n, box, thr, inject=g["rand_fields"][:2])
+        else:
+            with pytest.raises(ValueError):
+                oracle.exodus(g["rand_delta"], m, g["radii"][:2], n, box, thr,
+                              inject=g["rand_fields"][:2])
