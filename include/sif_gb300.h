@@ -395,8 +395,11 @@ int sifg_mesh_device(const float* x, const float* y, const float* z, uint64_t n,
 int sifg_smooth_device(const float* delta, uint32_t n_grid, float box, float r, int filter,
                        int window_mode, float* out);
 /* The exodus finder on a device density contrast and a device mesh. radii in
- * host memory. inject: NULL, or n_radii device grids that replace the
- * smoothing, largest radius first. prior: NULL, or n_prior voids to start
+ * host memory. inject: NULL, or device grids that replace the smoothing, in
+ * the order the run's transforms return them: per rung (largest radius
+ * first) its top-hat and, under SIF_FINDER_REFINE_GAUSSIAN for a rung with
+ * candidates, the top-hat times the Gaussian of 0.15 of the rung the minima
+ * are found on (2 * n_radii grids cover any run). prior: NULL, or n_prior voids to start
  * from in host memory, as four columns one after another (cx, cy, cz, r),
  * checked and used as sif_finder_exodus_extras_t::prior is. The catalogue is
  * written to the host arrays (capacity entries each); *n_voids receives the

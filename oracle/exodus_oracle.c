@@ -1985,6 +1985,101 @@ static int is_minimum_node(const float* f, uint32_t n, uint64_t i) {
   return 1;
 }
 
+/* A refined candidate's offset off its node, in cells (sif_offset_t,
+ * src/finder/utils.h:164-172). */
+typedef struct {
+  float dx, dy, dz;
+} orc_offset_t;
+
+/* newton_step, src/finder/utils.c:261-313: gradient and Hessian by central
+ * differences on the 27-node stencil (cross terms included), d = -H^-1 g by
+ * cofactors, in double; 0 unless H is positive definite (Sylvester's leading
+ * minors) and the step is within MINIMUM_MAX_STEP (one cell) on every axis.
+ * s[(a+1)*9 + (b+1)*3 + (c+1)] holds the value at offset (a, b, c). */
+static int newton_step(const float s[27], double d[3], double* depth) {
+#define S(a, b, c) ((double)s[((a) + 1) * 9 + ((b) + 1) * 3 + ((c) + 1)])
+  const double c0 = S(0, 0, 0);
+  const double g0 = 0.5 * (S(1, 0, 0) - S(-1, 0, 0));
+  const double g1 = 0.5 * (S(0, 1, 0) - S(0, -1, 0));
+  const double g2 = 0.5 * (S(0, 0, 1) - S(0, 0, -1));
+  const double h00 = S(1, 0, 0) - 2.0 * c0 + S(-1, 0, 0);
+  const double h11 = S(0, 1, 0) - 2.0 * c0 + S(0, -1, 0);
+  const double h22 = S(0, 0, 1) - 2.0 * c0 + S(0, 0, -1);
+  const double h01 = 0.25 * (S(1, 1, 0) - S(1, -1, 0) - S(-1, 1, 0) + S(-1, -1, 0));
+  const double h02 = 0.25 * (S(1, 0, 1) - S(1, 0, -1) - S(-1, 0, 1) + S(-1, 0, -1));
+  const double h12 = 0.25 * (S(0, 1, 1) - S(0, 1, -1) - S(0, -1, 1) + S(0, -1, -1));
+#undef S
+  const double k00 = h11 * h22 - h12 * h12;
+  const double k01 = h02 * h12 - h01 * h22;
+  const double k02 = h01 * h12 - h02 * h11;
+  const double k11 = h00 * h22 - h02 * h02;
+  const double k12 = h01 * h02 - h00 * h12;
+  const double k22 = h00 * h11 - h01 * h01;
+  const double det = h00 * k00 + h01 * k01 + h02 * k02;
+  if (!(h00 > 0.0 && k22 > 0.0 && det > 0.0))
+    return 0;
+  d[0] = -(k00 * g0 + k01 * g1 + k02 * g2) / det;
+  d[1] = -(k01 * g0 + k11 * g1 + k12 * g2) / det;
+  d[2] = -(k02 * g0 + k12 * g1 + k22 * g2) / det;
+  if (!(fabs(d[0]) <= 1.0 && fabs(d[1]) <= 1.0 && fabs(d[2]) <= 1.0))
+    return 0;
+  *depth = c0 + 0.5 * (g0 * d[0] + g1 * d[1] + g2 * d[2]);
+  return 1;
+}
+
+/* The 27 values around node i (load_stencil, utils.c:227-241). */
+static void load_stencil27(const float* f, uint32_t n, uint64_t i, float s[27]) {
+  const uint32_t ix = (uint32_t)(i / ((uint64_t)n * n)), iy = (uint32_t)((i / n) % n),
+                 iz = (uint32_t)(i % n);
+  const uint32_t xs[3] = {(ix + n - 1) % n, ix, (ix + 1) % n};
+  const uint32_t ys[3] = {(iy + n - 1) % n, iy, (iy + 1) % n};
+  const uint32_t zs[3] = {(iz + n - 1) % n, iz, (iz + 1) % n};
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++)
+      for (int c = 0; c < 3; c++)
+        s[a * 9 + b * 3 + c] = f[((uint64_t)xs[a] * n + ys[b]) * n + zs[c]];
+}
+
+/* step_cells, utils.c:317-319: a step of exactly half a cell stays. */
+static int32_t step_cells(double d) { return d > 0.5 ? 1 : (d < -0.5 ? -1 : 0); }
+
+/* candidate_centre, exodus_finder.c:371-393: node plus offset, in cells,
+ * times the cell length, wrapped into the box. */
+static void cand_centre(const orc_candidate_t* c, const orc_offset_t* offs, uint32_t N,
+  float cell, float box, float out[3]) {
+  const uint32_t node[3] = {(uint32_t)(c->flat / ((uint64_t)N * N)),
+    (uint32_t)((c->flat / N) % N), (uint32_t)(c->flat % N)};
+  float off[3] = {0.0f, 0.0f, 0.0f};
+  if (c->refined) {
+    const orc_offset_t* o = &offs[c->refined - 1];
+    off[0] = o->dx;
+    off[1] = o->dy;
+    off[2] = o->dz;
+  }
+  for (int a = 0; a < 3; a++) {
+    float x = ((float)node[a] + off[a]) * cell;
+    if (x < 0.0f)
+      x += box;
+    if (x >= box)
+      x -= box;
+    out[a] = x;
+  }
+}
+
+/* masked_overlap, exodus_finder.c:440-452: the node's mask bit; for a
+ * centre refined off its node, only while the offset is within
+ * scale * r * (1 - f). */
+static int cand_masked(const uint64_t* mask, const orc_candidate_t* c, const orc_offset_t* offs,
+  float r, float f, float scale, float cell) {
+  if (!mask_get(mask, c->flat))
+    return 0;
+  if (!c->refined)
+    return 1;
+  const orc_offset_t* o = &offs[c->refined - 1];
+  const float off = sqrtf(o->dx * o->dx + o->dy * o->dy + o->dz * o->dz) * cell;
+  return off < scale * r * (1.0f - f);
+}
+
 /* The rung loop of sif__exodus_run (src/finder/exodus_finder.c:1585-2492)
  * for a box, unweighted, seeds on their nodes: per rung the
  * top-hat smoothing, the scan and sort, the reach, the template, the
@@ -2014,8 +2109,15 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   if (!(threshold > -1.0f && threshold < 0.0f) || !(f >= 0.0f && f <= 1.0f) ||
       n_radii == 0 || mesh->box_length != box)
     return -2;
-  if (opt & (3u << 19))
-    return -5; /* centre refinement */
+  /* SIF_FINDER_REFINE_GAUSSIAN (utils.c:406-552, exodus_finder.c:1362-1380,
+   * 1740-1760): the minima found on the rung's top-hat times a Gaussian of
+   * 0.15 of the rung (one more transform), placed between the nodes by a
+   * Newton step; the candidates ordered on that field; the threshold still
+   * tested on the top-hat. The tracer and hill refinements are not here. */
+  const uint32_t refine = opt & (3u << 19);
+  if (refine && refine != (1u << 19))
+    return -5;
+  const int gaussian = refine == (1u << 19);
   /* SIF_FINDER_DISPLACE (exodus_finder.c:696-756, 946-1078, 2239-2275): a
    * void is refused only by a larger one and displaces the smaller ones it
    * collides with. The reference's catalogue does not depend on where its
@@ -2109,6 +2211,12 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
 
   uint64_t* mask = calloc((total + 63) / 64, sizeof(uint64_t));
   float* field = malloc(total * sizeof(float));
+  /* The field the minima are found and the candidates ordered on: the
+   * refinement's own smoothing, or the top-hat itself. */
+  float* fmin = gaussian ? malloc(total * sizeof(float)) : field;
+  orc_offset_t* offs = NULL;
+  uint64_t offs_cap = 0;
+  uint64_t inj_k = 0;  /* the next injected field */
   voids_t V;
   voids_init(&V, box);
   float max_acc = 0.0f;
@@ -2134,46 +2242,115 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
     const float radius = radii[ri];
     orc_rung_stats_t st;
     memset(&st, 0, sizeof(st));
+    /* Injected fields are taken in the order the run's transforms return
+     * them (each backward transform the next field): the rung's top-hat,
+     * then, refined, the top-hat times the Gaussian -- which the reference
+     * runs only for a rung with cells to refine (utils.c:441-453). */
     if (p->inject)
-      memcpy(field, p->inject + (uint64_t)ri * total, total * sizeof(float));
+      memcpy(field, p->inject + inj_k++ * total, total * sizeof(float));
     else
       orc_spectrum_smooth(spec, 1, radius, 0.0f, field, NULL);
 
     /* The scan, src/finder/utils.c:130-213: 256 fixed chunks counted, their
      * offsets, each chunk written in flat order; then the sort. */
-    enum { SCAN_CHUNKS = 256 };
-    uint64_t chunk_off[SCAN_CHUNKS];
-    const uint64_t scan_chunk = total / SCAN_CHUNKS;
-#pragma omp parallel for schedule(static, 1) num_threads(n_threads)
-    for (int c = 0; c < SCAN_CHUNKS; c++) {
-      const uint64_t a = (uint64_t)c * scan_chunk, e = c == SCAN_CHUNKS - 1 ? total : a + scan_chunk;
-      uint64_t k = 0;
-      for (uint64_t i = a; i < e; i++)
-        k += field[i] <= threshold && !mask_get(mask, i) && (!minima || is_minimum_node(field, N, i));
-      chunk_off[c] = k;
-    }
     uint64_t nc = 0;
-    for (int c = 0; c < SCAN_CHUNKS; c++) {
-      const uint64_t k = chunk_off[c];
-      chunk_off[c] = nc;
-      nc += k;
-    }
-    if (nc > cand_cap) {
-      cand_cap = nc;
-      cand = realloc(cand, cand_cap * sizeof(orc_candidate_t));
-    }
-#pragma omp parallel for schedule(static, 1) num_threads(n_threads)
-    for (int c = 0; c < SCAN_CHUNKS; c++) {
-      const uint64_t a = (uint64_t)c * scan_chunk, e = c == SCAN_CHUNKS - 1 ? total : a + scan_chunk;
-      uint64_t w = chunk_off[c];
-      for (uint64_t i = a; i < e; i++)
-        if (field[i] <= threshold && !mask_get(mask, i) &&
-            (!minima || is_minimum_node(field, N, i))) {
-          cand[w].delta = field[i];
-          cand[w].refined = 0;
-          cand[w].flat = i;
-          w++;
+    if (gaussian) {
+      /* sif__finder_scan_refined, utils.c:406-552: the cells at or below the
+       * threshold on the top-hat and unmasked, in flat order; each one's
+       * stencil on the refinement's field; a minimum (its own test, ties to
+       * the lower index) gets a Newton step and, if that lands on a node
+       * that is itself a candidate, moves there at the step's depth with the
+       * rest of the step as its offset (place_candidate, 331-365); every
+       * candidate goes by its depth on the refinement's field. A minimum
+       * takes the next offset slot whether or not it moves. */
+      uint64_t count = 0, n_min = 0;
+      for (uint64_t i = 0; i < total; i++)
+        count += field[i] <= threshold && !mask_get(mask, i);
+      if (count > 0) {
+        if (p->inject)
+          memcpy(fmin, p->inject + inj_k++ * total, total * sizeof(float));
+        else
+          orc_spectrum_smooth(spec, 1, radius, 0.15f * radius, fmin, NULL);
+        for (uint64_t i = 0; i < total; i++)
+          n_min += field[i] <= threshold && !mask_get(mask, i) && is_minimum_node(fmin, N, i);
+      }
+      if (count > cand_cap) {
+        cand_cap = count;
+        cand = realloc(cand, cand_cap * sizeof(orc_candidate_t));
+      }
+      if (n_min > offs_cap) {
+        offs_cap = n_min;
+        offs = realloc(offs, offs_cap * sizeof(orc_offset_t));
+      }
+      uint64_t slot = 0;
+      for (uint64_t i = 0; i < total; i++) {
+        if (!(field[i] <= threshold && !mask_get(mask, i)))
+          continue;
+        const int minimum = is_minimum_node(fmin, N, i);
+        if (minima && !minimum)
+          continue;
+        orc_candidate_t* c = &cand[nc++];
+        c->delta = fmin[i];
+        c->refined = 0;
+        c->flat = i;
+        if (minimum) {
+          float s27[27];
+          double d[3], depth;
+          load_stencil27(fmin, N, i, s27);
+          if (newton_step(s27, d, &depth)) {
+            const int32_t sx = step_cells(d[0]), sy = step_cells(d[1]), sz = step_cells(d[2]);
+            const uint32_t ix = (uint32_t)(i / ((uint64_t)N * N)), iy = (uint32_t)((i / N) % N),
+                           iz = (uint32_t)(i % N);
+            const uint32_t jx = (uint32_t)(((int64_t)ix + sx + N) % N);
+            const uint32_t jy = (uint32_t)(((int64_t)iy + sy + N) % N);
+            const uint32_t jz = (uint32_t)(((int64_t)iz + sz + N) % N);
+            const uint64_t j = ((uint64_t)jx * N + jy) * N + jz;
+            if (field[j] <= threshold && !mask_get(mask, j)) {
+              c->delta = (float)depth;
+              c->flat = j;
+              c->refined = (uint32_t)(slot + 1);
+              offs[slot].dx = (float)(d[0] - sx);
+              offs[slot].dy = (float)(d[1] - sy);
+              offs[slot].dz = (float)(d[2] - sz);
+            }
+          }
+          slot++;
         }
+      }
+    } else {
+      enum { SCAN_CHUNKS = 256 };
+      uint64_t chunk_off[SCAN_CHUNKS];
+      const uint64_t scan_chunk = total / SCAN_CHUNKS;
+#pragma omp parallel for schedule(static, 1) num_threads(n_threads)
+      for (int c = 0; c < SCAN_CHUNKS; c++) {
+        const uint64_t a = (uint64_t)c * scan_chunk, e = c == SCAN_CHUNKS - 1 ? total : a + scan_chunk;
+        uint64_t k = 0;
+        for (uint64_t i = a; i < e; i++)
+          k += field[i] <= threshold && !mask_get(mask, i) && (!minima || is_minimum_node(field, N, i));
+        chunk_off[c] = k;
+      }
+      for (int c = 0; c < SCAN_CHUNKS; c++) {
+        const uint64_t k = chunk_off[c];
+        chunk_off[c] = nc;
+        nc += k;
+      }
+      if (nc > cand_cap) {
+        cand_cap = nc;
+        cand = realloc(cand, cand_cap * sizeof(orc_candidate_t));
+      }
+#pragma omp parallel for schedule(static, 1) num_threads(n_threads)
+      for (int c = 0; c < SCAN_CHUNKS; c++) {
+        const uint64_t a = (uint64_t)c * scan_chunk, e = c == SCAN_CHUNKS - 1 ? total : a + scan_chunk;
+        uint64_t w = chunk_off[c];
+        for (uint64_t i = a; i < e; i++)
+          if (field[i] <= threshold && !mask_get(mask, i) &&
+              (!minima || is_minimum_node(field, N, i))) {
+            cand[w].delta = field[i];
+            cand[w].refined = 0;
+            cand[w].flat = i;
+            w++;
+          }
+      }
     }
     orc_sort_candidates(cand, nc);
     st.n_candidates = nc;
@@ -2214,7 +2391,7 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
         uint64_t w = lo;
         for (uint64_t k = lo; k < hi; k++) {
           const uint64_t flat = cand[k].flat;
-          if (mask_get(mask, flat)) {
+          if (cand_masked(mask, &cand[k], offs, radius, f, scale, cell)) {
             n_masked++;
             continue;
           }
@@ -2224,8 +2401,9 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
             n_proxy++;
             continue;
           }
-          if (overlap_exact(&V, (float)ix * cell, (float)iy * cell, (float)iz * cell,
-                radius, max_acc, box, f, scale)) {
+          float cc[3];
+          cand_centre(&cand[k], offs, N, cell, box, cc);
+          if (overlap_exact(&V, cc[0], cc[1], cc[2], radius, max_acc, box, f, scale)) {
             n_overlap++;
             continue;
           }
@@ -2255,7 +2433,7 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
       uint64_t removed = 0;
       for (uint64_t k = 0; k < nc && status == 0; k++) {
         const uint64_t flat = cand[k].flat;
-        if (mask_get(mask, flat)) {
+        if (cand_masked(mask, &cand[k], offs, radius, f, scale, cell)) {
           st.rejected_masked++;
           continue;
         }
@@ -2265,7 +2443,9 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
           st.rejected_proxy++;
           continue;
         }
-        const float cx = (float)ix * cell, cy = (float)iy * cell, cz = (float)iz * cell;
+        float cc[3];
+        cand_centre(&cand[k], offs, N, cell, box, cc);
+        const float cx = cc[0], cy = cc[1], cz = cc[2];
         if (overlap_exact(&V, cx, cy, cz, radius, max_acc, box, f, scale)) {
           st.rejected_overlap++;
           continue;
@@ -2332,7 +2512,7 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
     while (k < nc && status == 0) {
       uint64_t nb = 0;
       while (k < nc && nb < batch_cap) {
-        if (mask_get(mask, cand[k].flat))
+        if (cand_masked(mask, &cand[k], offs, radius, f, scale, cell))
           st.rejected_masked++;
         else
           bidx[nb++] = k;
@@ -2355,9 +2535,11 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
           r->status = ST_PROXY;
           continue;
         }
-        r->cx = (float)r->ix * cell;
-        r->cy = (float)r->iy * cell;
-        r->cz = (float)r->iz * cell;
+        float cc[3];
+        cand_centre(&cand[bidx[b]], offs, N, cell, box, cc);
+        r->cx = cc[0];
+        r->cy = cc[1];
+        r->cz = cc[2];
         if (overlap_exact(&V, r->cx, r->cy, r->cz, radius, max_acc_frozen, box, f,
               scale)) {
           r->status = ST_MESH;
@@ -2413,7 +2595,7 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
           continue;
         }
         st.n_rescaled++;
-        if (mask_get(mask, cand[bidx[b]].flat)) {
+        if (cand_masked(mask, &cand[bidx[b]], offs, r->r, f, scale, cell)) {
           st.rejected_masked++;
           continue;
         }
@@ -2469,7 +2651,10 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
   free(bidx);
   free(res);
   free(cand);
+  free(offs);
   free(conflicts);
+  if (fmin != field)
+    free(fmin);
   free(field);
   free(mask);
   free(radii);

@@ -164,7 +164,11 @@ typedef struct {
   int n_threads;      /* the team, which also sets the batch floor */
   int window;         /* 0: the reference's adaptive window; >0: fixed */
   int smoothing_mode; /* as orc_spectrum_new when no fields are injected */
-  const float* inject; /* NULL, or n_radii fields of grid_n^3, largest rung first */
+  /* NULL, or fields of grid_n^3 taken in the order the run's transforms
+   * return them: per rung (largest first) the top-hat and, under
+   * SIF_FINDER_REFINE_GAUSSIAN for a rung with candidates, the top-hat times
+   * the Gaussian the minima are found on. */
+  const float* inject;
   /* Voids to start from (sif_finder_exodus_extras_t::prior): accepted before
    * the first rung and returned first. NULL when n_prior is 0. */
   const float* prior_cx;

@@ -284,8 +284,13 @@ def exodus(delta, mesh, radii, n_grid, box, threshold, overlap=0.0, options=0, n
     radii = np.ascontiguousarray(radii, dtype=np.float32)
     inj = None
     if inject is not None:
-        inj = np.ascontiguousarray(inject, dtype=np.float32)
-        assert inj.shape == (len(radii), n_grid ** 3)
+        # As the run's transforms return them; under the Gaussian refinement
+        # up to two a rung (padded, so a short list is never read past).
+        inj = np.ascontiguousarray(inject, dtype=np.float32).reshape(-1, n_grid ** 3)
+        assert inj.shape[0] >= len(radii)
+        want = 2 * len(radii) if options & (3 << 19) else len(radii)
+        if inj.shape[0] < want:
+            inj = np.concatenate([inj, np.zeros((want - inj.shape[0], n_grid ** 3), np.float32)])
     pri = [np.ascontiguousarray(c, dtype=np.float32) for c in prior] if prior is not None else None
     p = Params(n_grid, box, threshold, overlap, options, n_threads, window, smoothing_mode,
                _p(inj) if inj is not None else None,

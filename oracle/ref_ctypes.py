@@ -189,13 +189,14 @@ def catalogue_arrays(lib, cat_ptr, variant="strict"):
 
 
 def exodus_raw(lib, grid, mesh, radii, threshold, overlap=0.0, opt=0, variant="strict",
-               inject=None, capture=None, prior=None):
+               inject=None, capture=None, prior=None, calls=None):
     """Runs sif_finder_exodus_raw; returns (cx, cy, cz, r).
 
     inject: (n_rungs, cells) array of smoothed fields that replace the
     reference's own, rung by rung; capture: an array of the same shape that
     receives the fields the reference computed; prior: (cx, cy, cz, r), the
-    voids to start from (sif_finder_exodus_extras_t::prior).
+    voids to start from (sif_finder_exodus_extras_t::prior); calls: a list
+    that receives the number of backward transforms the run made.
     """
     t = np_real(variant)
     radii = np.ascontiguousarray(radii, dtype=t)
@@ -227,6 +228,8 @@ def exodus_raw(lib, grid, mesh, radii, threshold, overlap=0.0, opt=0, variant="s
                                         threshold, overlap, opt | abi.SIF_FINDER_NO_CHECKPOINT,
                                         C.byref(extras) if extras is not None else None)
     finally:
+        if calls is not None:
+            calls.append(lib.orc_hook_calls())
         lib.orc_hook_inject(None, 0, 0)
         lib.orc_hook_capture(None, 0, 0)
     _check(lib, bool(cat), "sif_finder_exodus_raw")

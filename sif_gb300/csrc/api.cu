@@ -477,7 +477,7 @@ int sif_grid_to_density_contrast(sif_grid_t* grid) {
   SIFG_CUDA(cudaMemcpyAsync(dg, grid->values, b, cudaMemcpyHostToDevice, s));
   double* scratch = (double*)e->scratch.ensure(density_contrast_scratch_bytes());
   density_contrast(dg, grid->total_cells, scratch, s);
-  const double mean = read_mean(scratch);
+  const double mean = read_mean(scratch, s);
   if (!(mean > 0.0))
     return fail(SIF_ERR_RANGE, fmt("grid: mean density %g (expected > 0)", mean));
   SIFG_CUDA(cudaMemcpyAsync(grid->values, dg, b, cudaMemcpyDeviceToHost, s));
@@ -1136,7 +1136,7 @@ static int contrast_device(R* grid, uint64_t total_cells, double* mean_out) {
   cudaStream_t s = e->stream();
   double* scratch = (double*)e->scratch.ensure(density_contrast_scratch_bytes());
   density_contrast(grid, total_cells, scratch, s);
-  const double mean = read_mean(scratch);
+  const double mean = read_mean(scratch, s);
   if (mean_out) *mean_out = mean;
   if (!(mean > 0.0)) return fail(SIF_ERR_RANGE, fmt("grid: mean density %g (expected > 0)", mean));
   SIFG_CUDA(cudaStreamSynchronize(s));

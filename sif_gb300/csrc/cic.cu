@@ -774,9 +774,12 @@ const double* contrast_mean(const double* d_scratch) { return d_scratch + kMeanB
 
 size_t density_contrast_scratch_bytes() { return (kMeanBlocks + 1) * sizeof(double); }
 
-double read_mean(const double* d_scratch) {
+double read_mean(const double* d_scratch, cudaStream_t st) {
+  // On the stream that computed it: the library's streams do not wait for
+  // the legacy default stream, nor it for them.
   double m = 0.0;
-  SIFG_CUDA(cudaMemcpy(&m, d_scratch + kMeanBlocks, sizeof(double), cudaMemcpyDeviceToHost));
+  SIFG_CUDA(cudaMemcpyAsync(&m, d_scratch + kMeanBlocks, sizeof(double), cudaMemcpyDeviceToHost, st));
+  SIFG_CUDA(cudaStreamSynchronize(st));
   return m;
 }
 

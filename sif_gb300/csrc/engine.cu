@@ -37,6 +37,7 @@ static constexpr uint32_t kOptKeepWindow = 1u << 14;
 static constexpr uint32_t kOptAliasing = 1u << 8;
 static constexpr uint32_t kOptLagrangian = 1u << 18;
 static constexpr uint32_t kOptRefineMask = 3u << 19;
+static constexpr uint32_t kOptRefineGaussian = 1u << 19;
 static constexpr uint32_t kOptExtendReach = 1u << 21;
 static constexpr uint32_t kOptDisplace = 1u << 22;
 static constexpr uint32_t kGrowCap = 1u << 15;  // overflow window, floats per CTA
@@ -443,8 +444,16 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const R cell = box / (R)N;
   const R threshold = p.threshold, f = p.overlap;
   const uint32_t opt = p.options;
-  if (opt & kOptRefineMask) {
-    set_error(kErrUnsupported, "options: centre refinement is not supported by the GPU finder");
+  // SIF_FINDER_REFINE_GAUSSIAN (exodus_finder.c:1362-1380, 1740-1760;
+  // utils.c:406-552): the minima found on the top-hat times a Gaussian of
+  // 0.15 of the rung, placed between the nodes by a Newton step, and every
+  // candidate ordered on that field. The tracer and hill refinements are
+  // not run here.
+  const bool gaussian = (opt & kOptRefineMask) == kOptRefineGaussian;
+  if ((opt & kOptRefineMask) && !gaussian) {
+    set_error(kErrUnsupported,
+              "options: SIF_FINDER_REFINE_TRACERS and SIF_FINDER_REFINE_HILL are not supported by "
+              "the GPU finder");
     return kErrUnsupported;
   }
   // SIF_FINDER_DISPLACE: no pre-filter, no witness against the rung's
@@ -496,6 +505,14 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   std::sort(radii.begin(), radii.end(), [](R a, R b) { return a > b; });
 
   R* fields[2] = {grow_to<R>(field_[0], cells), grow_to<R>(field_[1], cells)};
+  // The refinement's own fields (the top-hat times the Gaussian), alongside.
+  R* gfields[2] = {nullptr, nullptr};
+  if (gaussian)
+    for (int k = 0; k < 2; k++) gfields[k] = grow_to<R>(gfield_[k], cells);
+  // Injected fields are consumed in the order the run's transforms return
+  // them: per rung the top-hat and, refined, for a rung with candidates, the
+  // refinement's field (the reference runs that transform only then).
+  uint64_t inj_k = 0;
   uint32_t* mask = grow_to<uint32_t>(mask_, (cells + 31) / 32);
   SIFG_CUDA(cudaMemsetAsync(mask, 0, ((cells + 31) / 32) * sizeof(uint32_t), st_));
   // The smoothing stream starts after everything queued on the run's stream
@@ -512,6 +529,11 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     SIFG_CUDA(cudaStreamWaitEvent(st_fft_, ev_scanned_[ri % 2], 0));
     smoother.smooth(kFilterTopHat, radii[ri], 0.0f, fields[ri % 2], tm ? &tm->filter : nullptr,
                     listed ? &below[ri % 2] : nullptr);
+    // RUNG_MINIMA_SIGMA (exodus_finder.c:1362-1365) of the rung on top of
+    // the top-hat, for every rung: a rung without candidates never reads it.
+    if (gaussian)
+      smoother.smooth(kFilterTopHat, radii[ri], R(0.15f) * radii[ri], gfields[ri % 2],
+                      tm ? &tm->filter : nullptr);
     SIFG_CUDA(cudaEventRecord(ev_smoothed_[ri % 2], st_fft_));
   };
   // On every way out, nothing of the run is left in flight on the smoothing
@@ -523,8 +545,8 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const uint32_t nb_below = (uint32_t)((cells + kBelowBlock - 1) / kBelowBlock);
   if (!p.inject) {
     smoother.setup(N, box, window_mode, st_fft_);
-    listed = g_scan_mode == 0 && sizeof(R) == 4 && !minima && smoother.lists_below() &&
-             cells % kBelowBlock == 0;
+    listed = g_scan_mode == 0 && sizeof(R) == 4 && !minima && !gaussian &&
+             smoother.lists_below() && cells % kBelowBlock == 0;
     if (listed)
       for (int k = 0; k < 2; k++) {
         below[k].thr = (float)threshold;
@@ -738,10 +760,10 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     // 1. The rung's field; the next rung's smoothing queued behind this
     //    rung's last read of the buffer it overwrites.
     R* field = fields[ri % 2];
+    const cudaMemcpyKind inj_kind =
+        p.inject_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (p.inject) {
-      SIFG_CUDA(cudaMemcpyAsync(field, p.inject + (uint64_t)ri * cells, cells * sizeof(R),
-                                p.inject_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                                st_));
+      SIFG_CUDA(cudaMemcpyAsync(field, p.inject + inj_k++ * cells, cells * sizeof(R), inj_kind, st_));
     } else {
       if (ri + 1 < radii.size()) smooth_rung(ri + 1);
       SIFG_CUDA(cudaStreamWaitEvent(st_, ev_smoothed_[ri % 2], 0));
@@ -758,17 +780,45 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       const uint64_t slots = scan_region_slots(cells);
       region_delta = grow_to<R>(region_delta_, slots);
       region_flat = grow_to<uint32_t>(region_flat_, slots);
+      // Refined, the candidates are every cell at or below the threshold
+      // (the minima are found on the refinement's field, below).
       scan_fused_pass(field, mask, cells, threshold, blocks, dcount, region_delta, region_flat, st_,
-                      N, minima);
-      // The field's last reader: the next rung but one may smooth into it.
-      SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
+                      N, minima && !gaussian);
+      // The field's last reader: the next rung but one may smooth into it
+      // (refined, the placing reads it again: recorded after that).
+      if (!gaussian) SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
     }
     SIFG_CUDA(cudaMemcpyAsync(h_counters_, dcount, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
     const auto t_wait = clk::now();
     SIFG_CUDA(cudaStreamSynchronize(st_));
     rs.count_wait_ms = ms_since(t_wait);
-    const uint32_t m = h_counters_[0];
+    uint32_t m = h_counters_[0];
     rs.n_candidates = m;
+    R* cdelta = nullptr;
+    uint32_t* cflat = nullptr;
+    const CandOffT<R>* coff = nullptr;
+    if (gaussian) {
+      if (m > 0) {
+        // The cells to place, then the refinement's field: the next injected
+        // one, or the smoothing's.
+        cdelta = grow_to<R>(cand_delta_, m);
+        cflat = grow_to<uint32_t>(cand_flat_, m);
+        scan_compact(blocks, cells, region_delta, region_flat, cdelta, cflat, st_);
+        R* gf = gfields[ri % 2];
+        if (p.inject)
+          SIFG_CUDA(cudaMemcpyAsync(gf, p.inject + inj_k++ * cells, cells * sizeof(R), inj_kind, st_));
+        CandOffT<R>* ocoff = nullptr;
+        m = refine_candidates(field, gf, mask, threshold, N, cell, m, minima, cdelta, cflat,
+                              grow_to<R>(cand_delta2_, m), grow_to<uint32_t>(cand_flat2_, m),
+                              grow_to<CandOffT<R>>(cand_off2_, m), ocoff,
+                              grow_to<CandOffT<R>>(cand_off_, m), grow_to<uint32_t>(keep_, m + 1),
+                              h_counters_ + 1, st_);
+        coff = ocoff;
+      }
+      // Both fields' last reader was the placing.
+      SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
+      rs.n_candidates = m;
+    }
 
     // The reach and the rescaling's constants (exodus_finder.c:1771-1817,
     // exodus_rescale.c:681-720, 894-908).
@@ -785,15 +835,19 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       continue;
     }
 
-    R* cdelta = grow_to<R>(cand_delta_, m);
-    uint32_t* cflat = grow_to<uint32_t>(cand_flat_, m);
-    if (listed) {
+    if (gaussian) {
+      // placed above
+    } else if (listed) {
+      cdelta = grow_to<R>(cand_delta_, m);
+      cflat = grow_to<uint32_t>(cand_flat_, m);
       if constexpr (sizeof(R) == 4)
         below_write_pass(bl.counts, bl.delta, bl.flat, nb_below, kBelowBlock, mask, blocks, cdelta,
                          cflat, st_);
       // The list's last reader: the next rung but one may smooth into it.
       SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
     } else {
+      cdelta = grow_to<R>(cand_delta_, m);
+      cflat = grow_to<uint32_t>(cand_flat_, m);
       scan_compact(blocks, cells, region_delta, region_flat, cdelta, cflat, st_);
     }
     ensure_host(m);
@@ -839,9 +893,10 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     R* sr = grow_to<R>(sr_, m);
     uint8_t* sreason = grow_to<uint8_t>(sreason_, m);
     uint32_t* blocks2 = grow_to<uint32_t>(rank_slots_, (size_t)m + 2048);
+    R* soff = coff ? grow_to<R>(soff_, m) : nullptr;
     prefilter(cflat, m, mask, vv, rc, alive, blocks2, scand, sflat, scx, scy, scz, dcount + 1, st_,
-              displace);
-    SurvivorsT<R> sv{scand, sflat, scx, scy, scz, sr, sreason, dcount + 1};
+              displace, coff, soff);
+    SurvivorsT<R> sv{scand, sflat, scx, scy, scz, sr, sreason, dcount + 1, soff};
 
     // 4. Sphere growth of every survivor.
     if (!(span > 0.0f)) {

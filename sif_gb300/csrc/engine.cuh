@@ -24,8 +24,11 @@ struct RunParamsT {
   uint32_t options = 0;
   std::vector<R> radii;  // any order
   int window = 8;        // bins resolved per pass
-  // Fields that replace the smoothing, rung by rung (largest radius first),
-  // n_radii * grid_n^3 values; host or device memory as inject_on_device says.
+  // Fields that replace the smoothing, in the order the run's transforms
+  // return them (largest rung first): each rung's top-hat and, under
+  // SIF_FINDER_REFINE_GAUSSIAN for a rung with candidates, the refinement's
+  // field; grid_n^3 values each, host or device memory as inject_on_device
+  // says.
   const R* inject = nullptr;
   bool inject_on_device = false;
   // Where the last rung's field goes under SIF_FINDER_CONSUME_GRID (device).
@@ -136,6 +139,10 @@ class Engine {
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
   DevBuf vhead_, vnext_, dlist_;  // displacement: the linked void index, its lists
   DevBuf gwbuf_, wcheck_;  // a weighted mesh: the wide windows' weights, the weight check
+  // SIF_FINDER_REFINE_GAUSSIAN: the refinement's fields, the placed
+  // candidates and their offsets, the minima's keep flags, the survivors'
+  // offset lengths.
+  DevBuf gfield_[2], cand_delta2_, cand_flat2_, cand_off_, cand_off2_, keep_, soff_;
   DevBuf tpl_, gbuf_, traffic_, region_delta_, region_flat_;
   static constexpr uint32_t kExtMaxLevels = 32;  // EXT_MAX_LEVELS, exodus_finder.c:244
   DevBuf ext_tpl_[kExtMaxLevels];  // the extended reach's templates, one per level

@@ -446,29 +446,199 @@ __device__ bool overlap_exact(const VoidViewT<R>& v, R cx, R cy, R cz, R r, R f,
 }
 
 // ---------------------------------------------------------------------------
+// SIF_FINDER_REFINE_GAUSSIAN: the candidates' placing (sif__finder_scan_refined,
+// src/finder/utils.c:406-552; place_candidate 331-365; newton_step 261-313)
+// ---------------------------------------------------------------------------
+
+// One Newton step from the node on the stencil of the refinement's field,
+// in double and in the reference's operation order: the gradient and the
+// Hessian by central differences, d = -H^-1 g by cofactors; false unless H
+// is positive definite and the step stays within a cell on every axis.
+template <class R>
+__device__ bool newton_step(const R (&s)[27], double (&d)[3], double& depth) {
+  auto S = [&](int a, int b, int c) { return (double)s[(a + 1) * 9 + (b + 1) * 3 + (c + 1)]; };
+  const double c0 = S(0, 0, 0);
+  const double g0 = __dmul_rn(0.5, __dsub_rn(S(1, 0, 0), S(-1, 0, 0)));
+  const double g1 = __dmul_rn(0.5, __dsub_rn(S(0, 1, 0), S(0, -1, 0)));
+  const double g2 = __dmul_rn(0.5, __dsub_rn(S(0, 0, 1), S(0, 0, -1)));
+  const double two_c0 = __dmul_rn(2.0, c0);
+  const double h00 = __dadd_rn(__dsub_rn(S(1, 0, 0), two_c0), S(-1, 0, 0));
+  const double h11 = __dadd_rn(__dsub_rn(S(0, 1, 0), two_c0), S(0, -1, 0));
+  const double h22 = __dadd_rn(__dsub_rn(S(0, 0, 1), two_c0), S(0, 0, -1));
+  const double h01 = __dmul_rn(
+      0.25, __dadd_rn(__dsub_rn(__dsub_rn(S(1, 1, 0), S(1, -1, 0)), S(-1, 1, 0)), S(-1, -1, 0)));
+  const double h02 = __dmul_rn(
+      0.25, __dadd_rn(__dsub_rn(__dsub_rn(S(1, 0, 1), S(1, 0, -1)), S(-1, 0, 1)), S(-1, 0, -1)));
+  const double h12 = __dmul_rn(
+      0.25, __dadd_rn(__dsub_rn(__dsub_rn(S(0, 1, 1), S(0, 1, -1)), S(0, -1, 1)), S(0, -1, -1)));
+  const double k00 = __dsub_rn(__dmul_rn(h11, h22), __dmul_rn(h12, h12));
+  const double k01 = __dsub_rn(__dmul_rn(h02, h12), __dmul_rn(h01, h22));
+  const double k02 = __dsub_rn(__dmul_rn(h01, h12), __dmul_rn(h02, h11));
+  const double k11 = __dsub_rn(__dmul_rn(h00, h22), __dmul_rn(h02, h02));
+  const double k12 = __dsub_rn(__dmul_rn(h01, h02), __dmul_rn(h00, h12));
+  const double k22 = __dsub_rn(__dmul_rn(h00, h11), __dmul_rn(h01, h01));
+  const double det =
+      __dadd_rn(__dadd_rn(__dmul_rn(h00, k00), __dmul_rn(h01, k01)), __dmul_rn(h02, k02));
+  if (!(h00 > 0.0 && k22 > 0.0 && det > 0.0)) return false;
+  d[0] = __ddiv_rn(-__dadd_rn(__dadd_rn(__dmul_rn(k00, g0), __dmul_rn(k01, g1)), __dmul_rn(k02, g2)),
+                   det);
+  d[1] = __ddiv_rn(-__dadd_rn(__dadd_rn(__dmul_rn(k01, g0), __dmul_rn(k11, g1)), __dmul_rn(k12, g2)),
+                   det);
+  d[2] = __ddiv_rn(-__dadd_rn(__dadd_rn(__dmul_rn(k02, g0), __dmul_rn(k12, g1)), __dmul_rn(k22, g2)),
+                   det);
+  if (!(fabs(d[0]) <= 1.0 && fabs(d[1]) <= 1.0 && fabs(d[2]) <= 1.0)) return false;
+  depth = __dadd_rn(c0, __dmul_rn(0.5, __dadd_rn(__dadd_rn(__dmul_rn(g0, d[0]), __dmul_rn(g1, d[1])),
+                                                __dmul_rn(g2, d[2]))));
+  return true;
+}
+
+__device__ __forceinline__ int32_t step_cells(double d) { return d > 0.5 ? 1 : (d < -0.5 ? -1 : 0); }
+
+// Each candidate (a cell at or below the threshold on the top-hat fa, not
+// masked, in flat order) placed on the refinement's field fb: its depth
+// there; a minimum of fb moved by its Newton step to the node it lands on,
+// if that node is a candidate too, at the step's depth and with the rest of
+// the step as its offset. keep[k]: whether it stays a candidate (all, or
+// under SIF_FINDER_SEEDS_MINIMA the minima).
+template <class R>
+__global__ void refine_kernel(const R* __restrict__ fa, const R* __restrict__ fb,
+                              const uint32_t* __restrict__ mask, R thr, uint32_t n, R cell,
+                              const uint32_t* __restrict__ cflat, uint32_t m, bool minima_only,
+                              R* __restrict__ d_out, uint32_t* __restrict__ f_out,
+                              CandOffT<R>* __restrict__ o_out, uint32_t* __restrict__ keep) {
+  const uint64_t nn = (uint64_t)n * n;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const uint32_t i = cflat[k];
+    const bool minimum = is_minimum(fb, n, i);
+    keep[k] = (!minima_only || minimum) ? 1u : 0u;
+    R delta = __ldg(fb + i);
+    uint32_t flat = i;
+    CandOffT<R> o{R(0), R(0), R(0), R(-1.0f)};
+    if (minimum) {
+      const uint32_t ix = (uint32_t)(i / nn), iy = (uint32_t)((i / n) % n), iz = (uint32_t)(i % n);
+      const uint32_t xs[3] = {(ix + n - 1) % n, ix, (ix + 1) % n};
+      const uint32_t ys[3] = {(iy + n - 1) % n, iy, (iy + 1) % n};
+      const uint32_t zs[3] = {(iz + n - 1) % n, iz, (iz + 1) % n};
+      R st[27];
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+#pragma unroll
+          for (int c = 0; c < 3; c++) st[a * 9 + b * 3 + c] = __ldg(fb + xs[a] * nn + (uint64_t)ys[b] * n + zs[c]);
+      double d[3], depth;
+      if (newton_step(st, d, depth)) {
+        const int32_t sx = step_cells(d[0]), sy = step_cells(d[1]), sz = step_cells(d[2]);
+        const uint32_t jx = (uint32_t)(((int64_t)ix + sx + n) % n);
+        const uint32_t jy = (uint32_t)(((int64_t)iy + sy + n) % n);
+        const uint32_t jz = (uint32_t)(((int64_t)iz + sz + n) % n);
+        const uint32_t j = (uint32_t)(((uint64_t)jx * n + jy) * n + jz);
+        if (__ldg(fa + j) <= thr && !mask_get(mask, j)) {
+          delta = (R)depth;
+          flat = j;
+          o.dx = (R)__dsub_rn(d[0], (double)sx);
+          o.dy = (R)__dsub_rn(d[1], (double)sy);
+          o.dz = (R)__dsub_rn(d[2], (double)sz);
+          // masked_overlap's off (exodus_finder.c:449-451).
+          o.len = fmul(fsqrt(fadd(fadd(fmul(o.dx, o.dx), fmul(o.dy, o.dy)), fmul(o.dz, o.dz))), cell);
+        }
+      }
+    }
+    d_out[k] = delta;
+    f_out[k] = flat;
+    o_out[k] = o;
+  }
+}
+
+// The kept entries in order; pos the exclusive scan of keep (m + 1 entries).
+template <class R>
+__global__ void refine_compact_kernel(const uint32_t* __restrict__ pos, uint32_t m,
+                                      const R* __restrict__ d_in, const uint32_t* __restrict__ f_in,
+                                      const CandOffT<R>* __restrict__ o_in, R* __restrict__ d_out,
+                                      uint32_t* __restrict__ f_out, CandOffT<R>* __restrict__ o_out) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const uint32_t p = pos[k];
+    if (pos[k + 1] == p) continue;
+    d_out[p] = d_in[k];
+    f_out[p] = f_in[k];
+    o_out[p] = o_in[k];
+  }
+}
+
+template <class R>
+uint32_t refine_candidates(const R* fa, const R* fb, const uint32_t* mask, R thr, uint32_t n,
+                           R cell, uint32_t m, bool minima_only, R*& cdelta, uint32_t*& cflat,
+                           R* d_tmp, uint32_t* f_tmp, CandOffT<R>* o_tmp, CandOffT<R>*& coff,
+                           CandOffT<R>* o_out, uint32_t* keep, uint32_t* h_count,
+                           cudaStream_t st) {
+  if (m == 0) return 0;
+  refine_kernel<R><<<grid_for(m, 128), 128, 0, st>>>(fa, fb, mask, thr, n, cell, cflat, m,
+                                                      minima_only, d_tmp, f_tmp, o_tmp, keep);
+  SIFG_LAUNCH_CHECK();
+  if (!minima_only) {
+    // Every candidate stays, in order: the placed arrays are the list.
+    std::swap(cdelta, d_tmp);
+    std::swap(cflat, f_tmp);
+    coff = o_tmp;
+    return m;
+  }
+  SIFG_CUDA(cudaMemsetAsync(keep + m, 0, sizeof(uint32_t), st));
+  exclusive_scan_u32(keep, m + 1, st);
+  refine_compact_kernel<R><<<grid_for(m, 256), 256, 0, st>>>(keep, m, d_tmp, f_tmp, o_tmp, cdelta,
+                                                              cflat, o_out);
+  SIFG_LAUNCH_CHECK();
+  coff = o_out;
+  SIFG_CUDA(cudaMemcpyAsync(h_count, keep + m, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  SIFG_CUDA(cudaStreamSynchronize(st));
+  return *h_count;
+}
+
+// candidate_centre (exodus_finder.c:371-393): node plus offset, times the
+// cell length, wrapped into the box; on its node, node times the cell.
+template <class R>
+__device__ __forceinline__ R cand_axis(uint32_t node, R off, const RungConstsT<R>& rc) {
+  R x = fmul(fadd((R)node, off), rc.cell);
+  if (x < R(0)) x = fadd(x, rc.box);
+  if (x >= rc.box) x = fsub(x, rc.box);
+  return x;
+}
+
+// masked_overlap (exodus_finder.c:440-452): the node's mask bit; a centre
+// off its node (len >= 0) only while len < scale * r * (1 - f).
+template <class R>
+__device__ __forceinline__ bool cand_masked(const uint32_t* mask, uint32_t node, R len, R r,
+                                            const RungConstsT<R>& rc) {
+  if (!mask_get_rw(mask, node)) return false;
+  if (len < R(0)) return true;
+  return len < fmul(fmul(rc.scale, r), fsub(R(1.0f), rc.f));
+}
+
+// ---------------------------------------------------------------------------
 // Pre-filter
 // ---------------------------------------------------------------------------
 
 template <class R>
 __global__ void prefilter_kernel(const uint32_t* __restrict__ cflat, uint32_t m,
                                  const uint32_t* __restrict__ mask, VoidViewT<R> voids, RungConstsT<R> rc,
-                                 uint8_t* __restrict__ alive, bool keep_all) {
+                                 uint8_t* __restrict__ alive, bool keep_all,
+                                 const CandOffT<R>* __restrict__ coff) {
   const uint32_t n = rc.grid_n;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
     const uint32_t flat = cflat[k];
+    const CandOffT<R> o = coff ? coff[k] : CandOffT<R>{R(0), R(0), R(0), R(-1.0f)};
     uint8_t ok = 1;
     if (keep_all) {
       // Under displacement a void refusing a candidate now may be gone by
       // its turn (exodus_finder.c:1873-1875): nothing is refused here.
-    } else if (mask_get_rw(mask, flat)) {
+    } else if (cand_masked(mask, flat, o.len, rc.radius, rc)) {
       ok = 0;
     } else {
       const uint32_t ix = flat / (n * n), iy = (flat / n) % n, iz = flat % n;
       if (rc.proxy_pole > 0 && overlap_quick(mask, n, ix, iy, iz, (uint32_t)rc.proxy_pole)) {
         ok = 0;
       } else {
-        const R cx = fmul((R)ix, rc.cell), cy = fmul((R)iy, rc.cell),
-                    cz = fmul((R)iz, rc.cell);
+        const R cx = cand_axis(ix, o.dx, rc), cy = cand_axis(iy, o.dy, rc),
+                cz = cand_axis(iz, o.dz, rc);
         if (overlap_exact(voids, cx, cy, cz, rc.radius, rc.f, rc.scale, rc.box)) ok = 0;
       }
     }
@@ -505,7 +675,7 @@ __global__ void __launch_bounds__(kCompactT) survivor_write_kernel(
     const uint8_t* __restrict__ flags, uint32_t m, const uint32_t* __restrict__ offsets,
     const uint32_t* __restrict__ cflat, RungConstsT<R> rc, uint32_t* __restrict__ surv_cand,
     uint32_t* __restrict__ sflat, R* __restrict__ scx, R* __restrict__ scy,
-    R* __restrict__ scz) {
+    R* __restrict__ scz, const CandOffT<R>* __restrict__ coff, R* __restrict__ soff) {
   __shared__ uint32_t wsum[kCompactT / 32];
   const uint32_t base = blockIdx.x * kCompactChunk;
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -528,10 +698,13 @@ __global__ void __launch_bounds__(kCompactT) survivor_write_kernel(
       const uint32_t flat = cflat[i];
       surv_cand[pos] = i;
       sflat[pos] = flat;
-      // candidate_centre (exodus_finder.c:366-388) on its node.
-      scx[pos] = fmul((R)(flat / (n * n)), rc.cell);
-      scy[pos] = fmul((R)((flat / n) % n), rc.cell);
-      scz[pos] = fmul((R)(flat % n), rc.cell);
+      // candidate_centre (exodus_finder.c:366-388): its node, and its
+      // offset off the node where the refinement moved it.
+      const CandOffT<R> o = coff ? coff[i] : CandOffT<R>{R(0), R(0), R(0), R(-1.0f)};
+      scx[pos] = cand_axis(flat / (n * n), o.dx, rc);
+      scy[pos] = cand_axis((flat / n) % n, o.dy, rc);
+      scz[pos] = cand_axis(flat % n, o.dz, rc);
+      if (soff) soff[pos] = o.len;
     }
     out += total;
     __syncthreads();
@@ -542,12 +715,13 @@ template <class R>
 void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, VoidViewT<R> voids,
                RungConstsT<R> rc, uint8_t* alive, uint32_t* block_counts, uint32_t* surv_cand,
                uint32_t* surv_flat, R* scx, R* scy, R* scz, uint32_t* d_surv_count,
-               cudaStream_t st, bool keep_all) {
+               cudaStream_t st, bool keep_all, const CandOffT<R>* coff, R* soff) {
   if (m == 0) {
     SIFG_CUDA(cudaMemsetAsync(d_surv_count, 0, sizeof(uint32_t), st));
     return;
   }
-  prefilter_kernel<<<grid_for(m, 128), 128, 0, st>>>(cand_flat, m, mask, voids, rc, alive, keep_all);
+  prefilter_kernel<<<grid_for(m, 128), 128, 0, st>>>(cand_flat, m, mask, voids, rc, alive, keep_all,
+                                                      coff);
   SIFG_LAUNCH_CHECK();
   const uint32_t nb = (m + kCompactChunk - 1) / kCompactChunk;
   flag_count_kernel<<<nb, kCompactT, 0, st>>>(alive, m, block_counts);
@@ -557,7 +731,7 @@ void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, Void
   store_total_kernel<<<1, 1, 0, st>>>(block_counts, nb, d_surv_count);
   SIFG_LAUNCH_CHECK();
   survivor_write_kernel<<<nb, kCompactT, 0, st>>>(alive, m, block_counts, cand_flat, rc,
-                                                  surv_cand, surv_flat, scx, scy, scz);
+                                                  surv_cand, surv_flat, scx, scy, scz, coff, soff);
   SIFG_LAUNCH_CHECK();
 }
 
@@ -2057,7 +2231,7 @@ __device__ __forceinline__ void commit_pass(const SurvivorsT<R>& sv, const uint3
     // The commit's re-checks (exodus_finder.c:2286-2317), against every void
     // accepted so far: the node's mask bit, the poles at the rescaled radius,
     // the exact overlap.
-    bool reject = mask_get_rw(mask, node);
+    bool reject = cand_masked(mask, node, sv.off ? sv.off[i] : R(-1.0f), r, rc);
     if (!reject) {
       const int32_t pole = (int32_t)(fdiv(fmul(fmul(rc.scale, r), fsub(R(1.0f), rc.f)), rc.cell)) - 1;
       if (pole > 0 && overlap_quick(mask, nn, ix, iy, iz, (uint32_t)pole)) reject = true;
@@ -2617,7 +2791,7 @@ __global__ void __launch_bounds__(kDispT) displace_commit_kernel(
       const uint32_t ix = node / (nn * nn), iy = (node / nn) % nn, iz = node % nn;
       // The rescaling failed; the node's mask bit; the poles and the exact
       // overlap at the rung radius, against the catalogue as it now stands.
-      bool ok = r >= R(0) && !mask_get_rw(mask, node);
+      bool ok = r >= R(0) && !cand_masked(mask, node, sv.off ? sv.off[i] : R(-1.0f), rc.radius, rc);
       if (ok && rc.proxy_pole > 0 && overlap_quick(mask, nn, ix, iy, iz, (uint32_t)rc.proxy_pole))
         ok = false;
       if (ok && overlap_exact_chains(vl, max_r, cx, cy, cz, rc.radius, rc.f, rc.scale, rc.box))
@@ -2821,7 +2995,11 @@ void compact_voids(R* cx, R* cy, R* cz, R* r, uint32_t* state, cudaStream_t st) 
                                 uint32_t*, cudaStream_t);                                          \
   template void prefilter<R>(const uint32_t*, uint32_t, const uint32_t*, VoidViewT<R>,             \
                              RungConstsT<R>, uint8_t*, uint32_t*, uint32_t*, uint32_t*, R*, R*,    \
-                             R*, uint32_t*, cudaStream_t, bool);                                   \
+                             R*, uint32_t*, cudaStream_t, bool, const CandOffT<R>*, R*);          \
+  template uint32_t refine_candidates<R>(const R*, const R*, const uint32_t*, R, uint32_t, R,      \
+                                         uint32_t, bool, R*&, uint32_t*&, R*, uint32_t*,           \
+                                         CandOffT<R>*, CandOffT<R>*&, CandOffT<R>*, uint32_t*,     \
+                                         uint32_t*, cudaStream_t);                                 \
   template void witness<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>,         \
                            VoidViewT<R>, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*);\
   template void grow<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>, uint32_t,   \

@@ -115,6 +115,17 @@ struct SurvivorsT {
   R* r;             // rescaled radius, or -1
   uint8_t* reason;  // rescale outcome
   const uint32_t* count;  // device-side survivor count
+  // Under SIF_FINDER_REFINE_GAUSSIAN: each survivor's centre's distance off
+  // its node (|offset| * cell), or -1 on the node; NULL: all on their nodes.
+  const R* off = nullptr;
+};
+
+// A candidate's centre off its node (sif_offset_t, src/finder/utils.h:
+// 164-172), in cells, and len = |offset| * cell as masked_overlap takes it
+// (exodus_finder.c:440-452); len -1 for a candidate on its node.
+template <class R>
+struct CandOffT {
+  R dx, dy, dz, len;
 };
 
 using MeshView = MeshViewT<float>;
@@ -171,11 +182,31 @@ void below_write_pass(const uint32_t* counts, const float* delta, const uint32_t
 // Pre-filter at the rung radius (prefilter_cells, exodus_finder.c:871-944)
 // and compaction of the survivors, candidate order kept; with keep_all
 // (displacement) every candidate survives.
+// coff: the candidates' offsets (SIF_FINDER_REFINE_GAUSSIAN), or NULL when
+// every candidate sits on its node; soff then receives each survivor's
+// offset length (or is NULL).
 template <class R>
 void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, VoidViewT<R> voids,
                RungConstsT<R> rc, uint8_t* alive, uint32_t* block_counts, uint32_t* surv_cand,
                uint32_t* surv_flat, R* scx, R* scy, R* scz, uint32_t* d_surv_count,
-               cudaStream_t st, bool keep_all = false);
+               cudaStream_t st, bool keep_all = false, const CandOffT<R>* coff = nullptr,
+               R* soff = nullptr);
+
+// SIF_FINDER_REFINE_GAUSSIAN's placing (sif__finder_scan_refined, src/finder/
+// utils.c:406-552): the m candidates (cdelta, cflat: the cells at or below
+// thr on the top-hat fa, unmasked, flat order) placed on the refinement's
+// field fb -- depth from fb, minima moved by a Newton step -- and, under
+// minima_only, reduced to the minima. On return cdelta and cflat point at
+// the placed list (the tmp buffers or the originals, swapped as needed),
+// coff at its offsets (o_tmp or o_out); keep holds m + 1 entries; h_count is
+// pinned host memory. Returns the candidates left (a host sync under
+// minima_only).
+template <class R>
+uint32_t refine_candidates(const R* fa, const R* fb, const uint32_t* mask, R thr, uint32_t n,
+                           R cell, uint32_t m, bool minima_only, R*& cdelta, uint32_t*& cflat,
+                           R* d_tmp, uint32_t* f_tmp, CandOffT<R>* o_tmp, CandOffT<R>*& coff,
+                           CandOffT<R>* o_out, uint32_t* keep, uint32_t* h_count,
+                           cudaStream_t st);
 
 // The collision witness (collision_radius, src/finder/exodus_finder.c:
 // 780-845, and sif__exodus_witness, src/finder/exodus_rescale.c:1074-1167):

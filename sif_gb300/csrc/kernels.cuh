@@ -84,7 +84,7 @@ void density_contrast(R* v, uint64_t n, double* d_scratch, cudaStream_t st, bool
 template <class R>
 void apply_contrast(R* v, uint64_t n, const double* mean, cudaStream_t st);
 const double* contrast_mean(const double* d_scratch);
-double read_mean(const double* d_scratch);
+double read_mean(const double* d_scratch, cudaStream_t st);
 
 // --- adjoint.cu ---
 // dL/dx, dL/dy, dL/dz of every particle for g = dL/d(delta) on the grid,

@@ -837,7 +837,13 @@ void SmootherT<R>::setup(uint32_t n_, R box_, int window_mode_, cudaStream_t st)
           for (int j = 0; j < 16; j++) tw[512 + k * 16 + j] = root((double)(j * k), 256.0);
         for (int k = 0; k < 256; k++) tw[768 + k] = root((double)k, 512.0);
         SIFG_CUDA(cudaMalloc(&p.twiddles, kTw512 * sizeof(float2)));
-        SIFG_CUDA(cudaMemcpy(p.twiddles, tw.data(), kTw512 * sizeof(float2), cudaMemcpyHostToDevice));
+        // On the smoothing stream, which every use of the tables follows (a
+        // plain cudaMemcpy runs on the legacy stream, which the library's
+        // non-blocking streams do not wait for), and finished before the
+        // staging vector goes.
+        SIFG_CUDA(cudaMemcpyAsync(p.twiddles, tw.data(), kTw512 * sizeof(float2),
+                                  cudaMemcpyHostToDevice, st));
+        SIFG_CUDA(cudaStreamSynchronize(st));
       } else {
         p.r2c = make_plan(n_, dbl ? CUFFT_D2Z : CUFFT_R2C, &p.work);
         p.c2r = make_plan(n_, dbl ? CUFFT_Z2D : CUFFT_C2R, &p.work);

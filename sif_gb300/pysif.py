@@ -253,8 +253,8 @@ def _exodus(grid, mesh, radii, threshold, variant="excursion-set", *, checkpoint
 
 def _exodus_raw(grid, mesh, radii, threshold, overlap_fraction=0.0, *, overlap_type="eulerian",
                 search_factor=1.5, deconvolution="full", consume_grid=False, seeds="cells",
-                extend_reach=False, displace=False, checkpoint=False, prior=None,
-                keep_checkpoint=False, save_memory=False):
+                refine_centres="none", extend_reach=False, displace=False, checkpoint=False,
+                prior=None, keep_checkpoint=False, save_memory=False):
     """finders.exodus_raw, for the options the GPU finder runs; checkpoint=
     False (the default here) runs without one."""
     lib = _lib.load()
@@ -273,6 +273,12 @@ def _exodus_raw(grid, mesh, radii, threshold, overlap_fraction=0.0, *, overlap_t
         opt |= abi.SIF_FINDER_SEEDS_MINIMA
     elif seeds != "cells":
         raise ValueError(f"seeds must be 'cells' or 'minima', not {seeds!r}")
+    refine = {None: 0, "none": 0, "gaussian": abi.SIF_FINDER_REFINE_GAUSSIAN,
+              "tracers": abi.SIF_FINDER_REFINE_TRACERS, "hill": abi.SIF_FINDER_REFINE_HILL}
+    if refine_centres not in refine:
+        raise ValueError("refine_centres must be 'none', 'gaussian', 'tracers' or 'hill', "
+                         f"not {refine_centres!r}")
+    opt |= refine[refine_centres]
     if extend_reach:
         opt |= abi.SIF_FINDER_EXTEND_REACH
     if displace:

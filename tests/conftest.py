@@ -80,6 +80,32 @@ def golden_box32_weighted_f64():
 
 
 @pytest.fixture(scope="session")
+def golden_box32_refine():
+    """SIF_FINDER_REFINE_GAUSSIAN through the reference: the rungs' top-hat
+    and refinement fields, and per option set the rungs refined and the
+    catalogue."""
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32_refine.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_box32_refine_f64():
+    """The refinement through the reference's SIF_USE_DOUBLE build."""
+    return dict(np.load(os.path.join(GOLDEN, "golden_box32_refine_f64.npz")))
+
+
+def refine_fields(g, name):
+    """The fields a refined run's transforms returned, in order: per rung the
+    top-hat and, where the rung ran it, the refinement's own."""
+    where = {int(r): k for k, r in enumerate(g["gauss_rungs"])}
+    seq = []
+    for i, th in enumerate(g["tophat"]):
+        seq.append(th)
+        if g[f"{name}_refined_rungs"][i]:
+            seq.append(g["gauss"][where[i]])
+    return np.stack(seq)
+
+
+@pytest.fixture(scope="session")
 def golden_box32_displace_f64():
     """The displacement box through the reference's SIF_USE_DOUBLE build."""
     return dict(np.load(os.path.join(GOLDEN, "golden_box32_displace_f64.npz")))

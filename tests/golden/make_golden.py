@@ -55,6 +55,13 @@ golden_box32_weighted.npz, golden_box32_weighted_f64.npz -- weighted meshes
   reference's own run smoothed, and its catalogues for several option sets
   on them. The generator also checks that weights of 1 and of 4 give the
   unweighted catalogue bit for bit, as the reference's own test does.
+golden_box32_refine.npz, golden_box32_refine_f64.npz -- SIF_FINDER_REFINE_GAUSSIAN
+  on BOX32's positions (the f64 file with its jitter), threshold -0.7 and
+  ladder(8, 24, 0.1) (12 rungs): the rungs' top-hat fields and the
+  refinement's fields (the top-hat times a Gaussian of 0.15 of the rung) the
+  reference's own runs returned, and for each option set the refinement
+  takes (three in the f64 file) which rungs ran the refinement's transform
+  (those with candidates) and its catalogue on those fields.
 """
 import os
 import sys
@@ -372,6 +379,95 @@ def make_box32_weighted(path, v="strict"):
     np.savez_compressed(path, **out)
 
 
+REFINE = dict(BOX32)
+REFINE_SETS = [
+    ("cells", 0.0, abi.SIF_FINDER_REFINE_GAUSSIAN),
+    ("minima", 0.0, abi.SIF_FINDER_SEEDS_MINIMA | abi.SIF_FINDER_REFINE_GAUSSIAN),
+    ("minima_f05", 0.5, abi.SIF_FINDER_SEEDS_MINIMA | abi.SIF_FINDER_REFINE_GAUSSIAN),
+    ("peak", 1.0, abi.SIF_FINDER_SEEDS_MINIMA | abi.SIF_FINDER_REFINE_GAUSSIAN |
+     abi.SIF_FINDER_EXTEND_REACH | abi.SIF_FINDER_DISPLACE),
+    ("lagrangian", 0.0, abi.SIF_FINDER_REFINE_GAUSSIAN | abi.SIF_FINDER_LAGRANGIAN_OVERLAP),
+]
+
+
+def make_box32_refine(path, v="strict"):
+    p = REFINE
+    x, y, z = synth.zeldovich(p["n"], p["box"], p["rms_disp"], p["seed"])
+    real = np.float32
+    kw = {}
+    if v == "f64":
+        rng = np.random.default_rng(p["seed"] + 1000)  # BOX32's f64 jitter
+
+        def jitter(a):
+            w = a.astype(np.float64) + rng.uniform(-1e-4, 1e-4, a.shape)
+            w = np.where(w < 0.0, w + p["box"], w)
+            return np.where(w >= p["box"], w - p["box"], w)
+
+        x, y, z = jitter(x), jitter(y), jitter(z)
+        real = np.float64
+        kw = dict(variant=v)
+    radii = synth.ladder(p["r0"], 3 * p["r0"], 0.1).astype(real)
+    lib = R.load(v, 4, abi.SIF_LOG_LEVEL_ERROR)
+    f = R.RefField(lib, x, y, z, **kw)
+    g = R.RefGrid(lib, p["n"], p["box"], **kw)
+    g.assign_cic(f)
+    g.to_contrast()
+    delta = g.values()
+    m = R.RefMesh(lib, p["mesh"], p["box"], f)
+    mx, my, mz, offs, idx = m.arrays(**kw)
+    out = dict(radii=radii, delta=delta, mesh_x=mx, mesh_y=my, mesh_z=mz, mesh_offsets=offs,
+               params=np.array([p["n"], p["box"], p["rms_disp"], p["seed"], p["r0"],
+                                p["threshold"], p["mesh"]], np.float64))
+    # The rungs' top-hat fields, from an unrefined run of the same contrast.
+    n_r = len(radii)
+    tophat = np.zeros((n_r + 1, p["n"] ** 3), real)
+    R.exodus_raw(lib, g, m, radii, p["threshold"], capture=tophat, **kw)
+    tophat = tophat[:n_r]
+    gauss = np.zeros((n_r, p["n"] ** 3), real)
+    have = np.zeros(n_r, bool)
+    sets = REFINE_SETS if v == "strict" else [s_ for s_ in REFINE_SETS if s_[0] in ("cells", "minima", "peak")]
+    for name, overlap, opt in sets:
+        # Each run from the same contrast (a run hands its grid back restored
+        # through a transform, not bit for bit).
+        g.set_values(delta)
+        cap = np.zeros((2 * n_r + 1, p["n"] ** 3), real)
+        calls = []
+        c0 = R.exodus_raw(lib, g, m, radii, p["threshold"], overlap, opt, capture=cap,
+                          calls=calls, **kw)
+        seq = cap[: calls[0] - 1]  # the last call is the grid's restore
+        # Which rungs ran the refinement's transform: after rung i's top-hat
+        # comes either rung i+1's top-hat or rung i's refinement field.
+        k, used = 0, np.zeros(n_r, bool)
+        for i in range(n_r):
+            assert np.array_equal(seq[k], tophat[i])
+            k += 1
+            if k < len(seq) and (i + 1 == n_r or not np.array_equal(seq[k], tophat[i + 1])):
+                assert not have[i] or np.array_equal(gauss[i], seq[k])
+                gauss[i], have[i], used[i] = seq[k], True, True
+                k += 1
+        assert k == len(seq)
+        g.set_values(delta)
+        c = R.exodus_raw(lib, g, m, radii, p["threshold"], overlap, opt, inject=seq, **kw)
+        # The run on its own fields is the run that returned them.
+        assert all(np.array_equal(a, b) for a, b in zip(c, c0))
+        out[f"{name}_refined_rungs"] = used
+        for k_, col in zip(("cx", "cy", "cz", "r"), c):
+            out[f"cat_{name}_{k_}"] = col
+        out[f"cat_{name}_opt"] = np.array([overlap, opt], np.float64)
+        g.set_values(delta)
+        base = R.exodus_raw(lib, g, m, radii, p["threshold"], overlap,
+                            opt & ~abi.SIF_FINDER_REFINE_GAUSSIAN, **kw)
+        print(f"{path} {name}: {len(c[0])} voids ({len(base[0])} unrefined), "
+              f"{int(used.sum())} rungs refined")
+    out["tophat"] = tophat
+    out["gauss_rungs"] = np.flatnonzero(have)
+    out["gauss"] = gauss[have]
+    m.free()
+    g.free()
+    f.free()
+    np.savez_compressed(path, **out)
+
+
 def positions_sha256(x, y, z):
     import hashlib
 
@@ -399,6 +495,10 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "workload_a":
         make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))
         sys.exit(0)
+    if len(sys.argv) > 1 and sys.argv[1] == "refine":
+        make_box32_refine(os.path.join(HERE, "golden_box32_refine.npz"))
+        make_box32_refine(os.path.join(HERE, "golden_box32_refine_f64.npz"), "f64")
+        sys.exit(0)
     if len(sys.argv) > 1 and sys.argv[1] == "weighted":
         make_box32_weighted(os.path.join(HERE, "golden_box32_weighted.npz"))
         make_box32_weighted(os.path.join(HERE, "golden_box32_weighted_f64.npz"), "f64")
@@ -415,4 +515,6 @@ if __name__ == "__main__":
     make_box32_displace(os.path.join(HERE, "golden_box32_displace_f64.npz"), "f64")
     make_box32_weighted(os.path.join(HERE, "golden_box32_weighted.npz"))
     make_box32_weighted(os.path.join(HERE, "golden_box32_weighted_f64.npz"), "f64")
+    make_box32_refine(os.path.join(HERE, "golden_box32_refine.npz"))
+    make_box32_refine(os.path.join(HERE, "golden_box32_refine_f64.npz"), "f64")
     make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))

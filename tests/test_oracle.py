@@ -392,3 +392,28 @@ def test_oracle_refuses_negative_or_nonfinite_weights(oracle, golden_box32_weigh
             with pytest.raises(ValueError):
                 oracle.exodus(g["rand_delta"], m, g["radii"][:2], n, box, thr,
                               inject=g["rand_fields"][:2])
+
+
+REFINE_SETS = ["cells", "minima", "minima_f05", "peak", "lagrangian"]
+
+
+@pytest.mark.parametrize("name", REFINE_SETS)
+def test_oracle_refinement_matches_golden(oracle, golden_box32_refine, name):
+    """SIF_FINDER_REFINE_GAUSSIAN (sif__finder_scan_refined, utils.c:406-552:
+    minima on the refinement's field, a Newton step on the 27-node stencil,
+    candidates ordered on that field; centres off their nodes in the overlap
+    tests, exodus_finder.c:371-452): the reference's catalogue bit for bit on
+    the fields its own run returned, under cell and minima seeds, an overlap
+    fraction, the excursion-peak preset and the Lagrangian scale."""
+    from conftest import refine_fields
+
+    g = golden_box32_refine
+    n, box, thr, n_mesh = int(g["params"][0]), float(g["params"][1]), float(g["params"][5]), int(g["params"][6])
+    overlap, opt = g[f"cat_{name}_opt"]
+    m = oracle.OracleMesh.from_arrays(g["mesh_x"], g["mesh_y"], g["mesh_z"], g["mesh_offsets"],
+                                      n_mesh, box)
+    cat = oracle.exodus(g["delta"], m, g["radii"], n, box, thr, float(overlap), int(opt),
+                        n_threads=2, inject=refine_fields(g, name))
+    want = tuple(g[f"cat_{name}_{k}"] for k in ("cx", "cy", "cz", "r"))
+    assert len(cat[0]) == len(want[0])
+    assert same_catalogue(cat, want)
