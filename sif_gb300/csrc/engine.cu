@@ -438,6 +438,8 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
                    HostCatalogueT<R>& out, std::vector<RungStat>* stats, RunTimings* tm) {
   SmootherT<R>& smoother = smoother_for<R>();
   const auto t_start = std::chrono::steady_clock::now();
+  // The run appends one entry to stats per rung it runs (from first_rung).
+  const size_t stats0 = stats ? stats->size() : 0;
   const uint32_t N = p.grid_n;
   const uint64_t cells = (uint64_t)N * N * N;
   const R box = p.box;
@@ -627,6 +629,8 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   }
   R* gbuf = grow_to<R>(gbuf_, (size_t)growth_grid() * kGrowCap);
   uint32_t* dcount = grow_to<uint32_t>(dcount_, 16);
+  // The growth and witness kernels' work counters (the survivors' queue).
+  uint32_t* work = grow_to<uint32_t>(work_, 4);
   // Gathered particles and visited cells of each rung's sphere growth.
   const size_t n_rungs = radii.size();
   unsigned long long* traffic = (unsigned long long*)grow_to<uint64_t>(traffic_, 2 * n_rungs + 2);
@@ -917,22 +921,23 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       if (displace || weighted)
         SIFG_CUDA(cudaMemsetAsync(sreason, kRescaleOk, m, st_));
       else
-        witness(mv, tv, rc, sv, vv, m, traffic + 2 * ri, st_, tm ? &tm->witness : nullptr);
+        witness(mv, tv, rc, sv, vv, m, traffic + 2 * ri, st_, tm ? &tm->witness : nullptr, work);
       if (weighted)
         grow_weighted(mv, tv, rc, sv, m, gbuf, gwbuf, kGrowCap, traffic + 2 * ri, st_,
-                      tm ? &tm->growth : nullptr);
+                      tm ? &tm->growth : nullptr, kAllSurvivors, work);
       else
-        grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_, tm ? &tm->growth : nullptr);
+        grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_, tm ? &tm->growth : nullptr,
+             kAllSurvivors, work);
       // Each level of the extended reach, for the survivors whose crossing
       // still lies past the reach (exodus_finder.c:2060-2072).
       for (uint32_t e = ext0; e < n_ext; e++) {
         const RungConstsT<R> ec = shell_consts(rc, ext_rmin[e], ext_reach[e]);
         if (weighted)
           grow_weighted(mv, ext_tv[e], ec, sv, m, gbuf, gwbuf, kGrowCap, traffic + 2 * ri, st_,
-                        tm ? &tm->growth : nullptr, kRescaleBeyondSearch);
+                        tm ? &tm->growth : nullptr, kRescaleBeyondSearch, work);
         else
           grow(mv, ext_tv[e], ec, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_,
-               tm ? &tm->growth : nullptr, kRescaleBeyondSearch);
+               tm ? &tm->growth : nullptr, kRescaleBeyondSearch, work);
       }
     }
 
@@ -1099,9 +1104,11 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       tm->growth_particles += h_traffic[2 * ri];
       tm->growth_cells += h_traffic[2 * ri + 1];
     }
-    if (stats && ri < stats->size()) {
-      (*stats)[stats->size() - n_rungs + ri].growth_particles = h_traffic[2 * ri];
-      (*stats)[stats->size() - n_rungs + ri].growth_cells = h_traffic[2 * ri + 1];
+    // Rung ri's entry: the rungs before first_rung (a resumed run) have none.
+    const size_t k = stats0 + (ri - p.first_rung);
+    if (stats && ri >= p.first_rung && k < stats->size()) {
+      (*stats)[k].growth_particles = h_traffic[2 * ri];
+      (*stats)[k].growth_cells = h_traffic[2 * ri + 1];
     }
   }
   if (tm)

@@ -138,6 +138,7 @@ class Engine {
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
   DevBuf vhead_, vnext_, dlist_;  // displacement: the linked void index, its lists
+  DevBuf work_;  // the sphere growth's and the witness's survivor queues
   DevBuf gwbuf_, wcheck_;  // a weighted mesh: the wide windows' weights, the weight check
   // SIF_FINDER_REFINE_GAUSSIAN: the refinement's fields, the placed
   // candidates and their offsets, the minima's keep flags, the survivors'

@@ -991,6 +991,25 @@ __device__ __forceinline__ void walk_cells(const MeshViewT<R>& mesh, const Templ
   }
 }
 
+// The next survivor for the calling warp (CTA) from a work counter zeroed
+// before the launch: survivors go to whichever warp (CTA) is free, so a
+// survivor that takes long delays only its own warp, not a fixed share of
+// survivors behind it. A survivor's result does not depend on which warp
+// takes it, or when.
+__device__ __forceinline__ uint32_t next_warp_item(uint32_t* work) {
+  uint32_t s = 0;
+  if ((threadIdx.x & 31u) == 0) s = atomicAdd(work, 1u);
+  return __shfl_sync(0xffffffffu, s, 0);
+}
+
+__device__ __forceinline__ uint32_t next_cta_item(uint32_t* work, uint32_t* slot) {
+  if (threadIdx.x == 0) *slot = atomicAdd(work, 1u);
+  __syncthreads();
+  const uint32_t s = *slot;
+  __syncthreads();
+  return s;
+}
+
 // traffic[0] counts the particles whose positions a pass read (12 bytes
 // each), traffic[1] the template cells a pass visited (a range lookup, 8
 // bytes, plus the template entry, 8 bytes): the gathered bytes of the
@@ -1000,7 +1019,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
                                                            RungConstsT<R> rc, SurvivorsT<R> sv,
                                                            R* __restrict__ gbuf, uint32_t gcap,
                                                            unsigned long long* __restrict__ traffic,
-                                                           uint8_t only) {
+                                                           uint8_t only, uint32_t* work) {
   __shared__ uint32_t bins[kMaxBins];
   __shared__ uint32_t below[kMaxBins];  // particles inside bin b's lower edge
   __shared__ R sbuf[kSmemBuf];
@@ -1013,8 +1032,9 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t n_surv = *sv.count;
   R* my_gbuf = gbuf + (uint64_t)blockIdx.x * gcap;
+  __shared__ uint32_t s_item;
 
-  for (uint32_t s = blockIdx.x; s < n_surv; s += gridDim.x) {
+  for (uint32_t s = next_cta_item(work, &s_item); s < n_surv; s = next_cta_item(work, &s_item)) {
     if (only != kAllSurvivors ? sv.reason[s] != only : sv.reason[s] == kRescaleWitness) continue;
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
@@ -1258,7 +1278,8 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
                                                              RungConstsT<R> rc, SurvivorsT<R> sv,
                                                              uint32_t nb_stride, uint32_t shell_cap,
                                                              uint8_t only,
-                                                             unsigned long long* __restrict__ traffic) {
+                                                             unsigned long long* __restrict__ traffic,
+                                                             uint32_t* work) {
   extern __shared__ unsigned char warp_smem[];
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   unsigned char* base = warp_smem + warp * warp_slice_bytes<R>(nb_stride, shell_cap);
@@ -1279,8 +1300,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
     }
   };
   const uint32_t n_surv = *sv.count;
-  const uint32_t warps = gridDim.x * kGrowWarps;
-  for (uint32_t s = blockIdx.x * kGrowWarps + warp; s < n_surv; s += warps) {
+  for (uint32_t s = next_warp_item(work); s < n_surv; s = next_warp_item(work)) {
     if (only != kAllSurvivors ? sv.reason[s] != only : sv.reason[s] == kRescaleWitness) continue;
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
@@ -1565,12 +1585,12 @@ template <class R>
 __global__ void __launch_bounds__(kGrowT) witness_kernel(MeshViewT<R> mesh, TemplateViewT<R> tpl,
                                                          RungConstsT<R> rc, SurvivorsT<R> sv,
                                                          VoidViewT<R> voids,
-                                                         unsigned long long* __restrict__ traffic) {
-  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+                                                         unsigned long long* __restrict__ traffic,
+                                                         uint32_t* work) {
+  const unsigned lane = threadIdx.x & 31u;
   const uint32_t n_surv = *sv.count;
-  const uint32_t warps = gridDim.x * kGrowWarps;
   const R slack_lo = R(1.0f - 1e-5f), slack_hi = R(1.0f + 1e-5f);
-  for (uint32_t s = blockIdx.x * kGrowWarps + warp; s < n_surv; s += warps) {
+  for (uint32_t s = next_warp_item(work); s < n_surv; s = next_warp_item(work)) {
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     bool refused = false;
     unsigned long long read = 0, visited = 0;
@@ -1644,17 +1664,20 @@ void set_witness(int on) { g_witness = on; }
 template <class R>
 void witness(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
              VoidViewT<R> voids, uint32_t max_survivors, unsigned long long* traffic,
-             cudaStream_t st, KernelTimer* timer) {
+             cudaStream_t st, KernelTimer* timer, uint32_t* work) {
   if (max_survivors == 0) return;
   if (!g_witness) {
     // Every survivor to be grown (kRescaleOk is 0).
     SIFG_CUDA(cudaMemsetAsync(s.reason, 0, max_survivors, st));
     return;
   }
-  const uint32_t warps_needed = (max_survivors + kGrowWarps - 1) / kGrowWarps;
+  // As many CTAs as the GPU keeps resident (four an SM at 64 registers),
+  // taking survivors from the counter.
+  const uint32_t ctas_needed = (max_survivors + kGrowWarps - 1) / kGrowWarps;
+  SIFG_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), st));
   if (timer) timer->begin(st);
-  witness_kernel<R><<<std::min<uint32_t>(warps_needed, 152u * 8u), kGrowT, 0, st>>>(
-      mesh, tpl, rc, s, voids, traffic);
+  witness_kernel<R><<<std::min<uint32_t>(ctas_needed, 152u * 4u), kGrowT, 0, st>>>(
+      mesh, tpl, rc, s, voids, traffic, work);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(st);
 }
@@ -1672,8 +1695,11 @@ constexpr uint32_t kShellListMax = 512;  // entries of a warp's shell list, at m
 template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s, uint32_t max_survivors,
           R* gbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
-          KernelTimer* timer, uint8_t only) {
+          KernelTimer* timer, uint8_t only, uint32_t* work) {
   if (max_survivors == 0) return;
+  // work[0] for the first launch, work[1] for the per-CTA pass after the
+  // warp kernel.
+  SIFG_CUDA(cudaMemsetAsync(work, 0, 2 * sizeof(uint32_t), st));
   const bool by_warp = g_growth_mode == 2 || (g_growth_mode == 0 && max_survivors >= kWarpGrowthMin);
   const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
   if (timer) timer->begin(st);
@@ -1705,13 +1731,14 @@ void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT
     const uint32_t cap = 152u * (uint32_t)std::max(per_sm, 1);
     growth_warp_kernel<R><<<std::min(warps_needed, cap), kGrowT, smem, st>>>(mesh, tpl, rc, s,
                                                                             nb_stride, shell_cap,
-                                                                            only, traffic);
+                                                                            only, traffic, work);
     SIFG_LAUNCH_CHECK();
     // The survivors whose windows were too wide for a warp.
-    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, kRescalePending);
+    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, kRescalePending,
+                                        work + 1);
     SIFG_LAUNCH_CHECK();
   } else {
-    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, only);
+    growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, only, work);
     SIFG_LAUNCH_CHECK();
   }
   if (timer) timer->end(st);
@@ -1831,7 +1858,7 @@ template <class R>
 __global__ void __launch_bounds__(kGrowT) growth_weighted_kernel(
     MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> sv,
     R* __restrict__ gbuf, long long* __restrict__ gwbuf, uint32_t gcap,
-    unsigned long long* __restrict__ traffic, uint8_t only) {
+    unsigned long long* __restrict__ traffic, uint8_t only, uint32_t* work) {
   extern __shared__ __align__(16) unsigned char wsm[];
   long long* bw = (long long*)wsm;           // weight per bin
   long long* belw = bw + kMaxBins;           // weight inside bin b's lower edge
@@ -1848,8 +1875,9 @@ __global__ void __launch_bounds__(kGrowT) growth_weighted_kernel(
   const uint32_t n_surv = *sv.count;
   const R ws = mesh.wscale;
   const double winv = mesh.winv;
+  __shared__ uint32_t s_item;
 
-  for (uint32_t s = blockIdx.x; s < n_surv; s += gridDim.x) {
+  for (uint32_t s = next_cta_item(work, &s_item); s < n_surv; s = next_cta_item(work, &s_item)) {
     if (only != kAllSurvivors ? sv.reason[s] != only : sv.reason[s] == kRescaleWitness) continue;
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
@@ -2058,8 +2086,10 @@ __global__ void __launch_bounds__(kGrowT) growth_weighted_kernel(
 template <class R>
 void grow_weighted(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
                    uint32_t max_survivors, R* gbuf, long long* gwbuf, uint32_t gcap,
-                   unsigned long long* traffic, cudaStream_t st, KernelTimer* timer, uint8_t only) {
+                   unsigned long long* traffic, cudaStream_t st, KernelTimer* timer, uint8_t only,
+                   uint32_t* work) {
   if (max_survivors == 0) return;
+  SIFG_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), st));
   constexpr size_t smem = weighted_smem_bytes<R>();
   thread_local bool attr = false;  // the attribute is per thread's view of the function
   if (!attr) {
@@ -2070,7 +2100,7 @@ void grow_weighted(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, S
   const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
   if (timer) timer->begin(st);
   growth_weighted_kernel<R><<<g, kGrowT, smem, st>>>(mesh, tpl, rc, s, gbuf, gwbuf, gcap, traffic,
-                                                    only);
+                                                    only, work);
   SIFG_LAUNCH_CHECK();
   if (timer) timer->end(st);
 }
@@ -2119,10 +2149,12 @@ void weight_fixed_point(double bound, double* wscale, double* winv) {
 
 template void grow_weighted<float>(MeshViewT<float>, TemplateViewT<float>, RungConstsT<float>,
                                    SurvivorsT<float>, uint32_t, float*, long long*, uint32_t,
-                                   unsigned long long*, cudaStream_t, KernelTimer*, uint8_t);
+                                   unsigned long long*, cudaStream_t, KernelTimer*, uint8_t,
+                                   uint32_t*);
 template void grow_weighted<double>(MeshViewT<double>, TemplateViewT<double>, RungConstsT<double>,
                                     SurvivorsT<double>, uint32_t, double*, long long*, uint32_t,
-                                    unsigned long long*, cudaStream_t, KernelTimer*, uint8_t);
+                                    unsigned long long*, cudaStream_t, KernelTimer*, uint8_t,
+                                    uint32_t*);
 template void check_weights<float>(const float*, uint64_t, unsigned long long*, cudaStream_t);
 template void check_weights<double>(const double*, uint64_t, unsigned long long*, cudaStream_t);
 
@@ -3001,9 +3033,11 @@ void compact_voids(R* cx, R* cy, R* cz, R* r, uint32_t* state, cudaStream_t st) 
                                          CandOffT<R>*, CandOffT<R>*&, CandOffT<R>*, uint32_t*,     \
                                          uint32_t*, cudaStream_t);                                 \
   template void witness<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>,         \
-                           VoidViewT<R>, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*);\
+                           VoidViewT<R>, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*, \
+                           uint32_t*);                                                              \
   template void grow<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>, uint32_t,   \
-                        R*, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*, uint8_t);   \
+                        R*, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*, uint8_t,    \
+                        uint32_t*);                                                                \
   template void build_survivor_grid<R>(const R*, const R*, const R*, const uint32_t*, uint32_t,    \
                                        int32_t, R, uint32_t*, uint32_t*, uint32_t*, cudaStream_t); \
   template void commit_init<R>(SurvivorsT<R>, uint8_t*, uint32_t*, uint32_t, cudaStream_t);        \

@@ -214,11 +214,12 @@ uint32_t refine_candidates(const R* fa, const R* fb, const uint32_t* mask, R thr
 // collides with a void of `voids` (the catalogue as the rung begins) is
 // refused before any growth, as the reference refuses it -- the commit would
 // refuse it at any radius it could return. Writes every survivor's outcome:
-// kRescaleWitness (radius -1) or kRescaleOk (to be grown). traffic as grow's.
+// kRescaleWitness (radius -1) or kRescaleOk (to be grown). traffic as grow's;
+// work: a device counter (zeroed here) from which the warps take survivors.
 template <class R>
 void witness(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
              VoidViewT<R> voids, uint32_t max_survivors, unsigned long long* traffic,
-             cudaStream_t st, KernelTimer* timer);
+             cudaStream_t st, KernelTimer* timer, uint32_t* work);
 
 // 1 (default): the witness runs; 0: every survivor is grown. The catalogue
 // does not depend on it (tests run both).
@@ -231,11 +232,12 @@ void set_witness(int on);
 constexpr uint8_t kAllSurvivors = 0xff;
 unsigned growth_grid();
 // traffic (may be NULL): two counters the kernel adds to -- particles read
-// and template cells visited.
+// and template cells visited. work: two device counters (zeroed here) from
+// which the warps or CTAs take survivors.
 template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
           uint32_t max_survivors, R* gbuf, uint32_t gcap, unsigned long long* traffic,
-          cudaStream_t st, KernelTimer* timer, uint8_t only = kAllSurvivors);
+          cudaStream_t st, KernelTimer* timer, uint8_t only, uint32_t* work);
 // The weighted sphere growth (sif__exodus_find_radius_weighted,
 // exodus_rescale.c:642-1037 with the weighted flag): mesh.w set. A CTA per
 // survivor; gbuf and gwbuf (gcap entries per CTA each) hold the windows too
@@ -244,7 +246,7 @@ template <class R>
 void grow_weighted(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
                    uint32_t max_survivors, R* gbuf, long long* gwbuf, uint32_t gcap,
                    unsigned long long* traffic, cudaStream_t st, KernelTimer* timer,
-                   uint8_t only = kAllSurvivors);
+                   uint8_t only, uint32_t* work);
 // Counts a weighted mesh's negative (below zero; a negative zero is not)
 // and non-finite weights into counts[0], counts[1] (device, zeroed here).
 template <class R>
