@@ -542,6 +542,20 @@ def precision_run(args):
 
 
 def e2e_run(args, w, x, y, z, radii):
+    """The step through sif's C API on host buffers: the positions live in a
+    sif_field_t (host memory), and each step runs sif_grid_assign_cic,
+    sif_grid_to_density_contrast, sif_chain_mesh_alloc and
+    sif_finder_exodus_raw, each returning its result in its struct's host
+    arrays. Timed on the host clock around the whole step.
+
+    With the library's host mirrors on (sifg_set_host_mirrors: a call reuses
+    the device copy an earlier call made of an array instead of copying it
+    up again), the step first declares the field's positions new
+    (sifg_host_modified), so they are copied up every step as a new input
+    would be; the grid and the mesh the step itself made are not copied back
+    up. The bytes each step copied are the library's own count
+    (sifg_copy_bytes). `copy_all` is the same step with mirrors off: every
+    call copies its inputs up and its results down."""
     from sif_gb300 import _lib, abi
 
     lib = _lib.load()
@@ -552,8 +566,10 @@ def e2e_run(args, w, x, y, z, radii):
     grid = lib.sif_grid_alloc(w["grid"], w["box"])
     r = np.ascontiguousarray(radii, np.float32)
     opt = abi.SIF_FINDER_NO_CHECKPOINT
+    positions = C.cast(field.contents.x, C.c_void_p)
 
     def step():
+        lib.sifg_host_modified(positions)  # this step's input
         grid.contents.content = abi.SIF_GRID_EMPTY
         assert lib.sif_grid_assign_cic(grid, field) == 0
         assert lib.sif_grid_to_density_contrast(grid) == 0
@@ -566,20 +582,36 @@ def e2e_run(args, w, x, y, z, radii):
         lib.sif_chain_mesh_free(mesh)
         return nv
 
-    steps = max(1, min(args.steps, args.e2e_steps))
-    for _ in range(max(1, min(args.warmup, 2))):
-        nv = step()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        nv = step()
-    dt = (time.perf_counter() - t0) / steps
+    def copied():
+        h2d, d2h = C.c_uint64(0), C.c_uint64(0)
+        lib.sifg_copy_bytes(C.byref(h2d), C.byref(d2h))
+        return h2d.value, d2h.value
+
+    def timed(mirrors):
+        lib.sifg_set_host_mirrors(1 if mirrors else 0)
+        steps = max(1, min(args.steps, args.e2e_steps))
+        for _ in range(max(1, min(args.warmup, 2))):
+            step()
+        b0 = copied()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            nv = step()
+        dt = (time.perf_counter() - t0) / steps
+        b1 = copied()
+        return {"value": round(n / dt / 1e6, 2), "unit": UNIT,
+                "h2d_bytes_per_step": (b1[0] - b0[0]) // steps,
+                "d2h_bytes_per_step": (b1[1] - b0[1]) // steps,
+                "ms_per_step": round(dt * 1e3, 2), "steps": steps, "n_voids": nv}
+
+    try:
+        out = timed(True)
+        out["host_mirrors"] = True
+        out["copy_all"] = timed(False)
+    finally:
+        lib.sifg_set_host_mirrors(0)
     lib.sif_grid_free(grid)
     lib.sif_field_free(field)
-    nc, mc = w["grid"] ** 3, w["mesh"] ** 3 + 1
-    h2d = 2 * 12 * n + 4 * nc + 4 * nc + 12 * n + 4 * mc
-    d2h = 4 * nc + 4 * nc + 12 * n + 4 * mc + 16 * nv
-    return {"value": round(n / dt / 1e6, 2), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "ms_per_step": round(dt * 1e3, 2), "steps": steps}
+    return out
 
 
 # --------------------------------------------------------------------------

@@ -565,6 +565,32 @@ void sifg_set_scan_mode(int mode);
  * first use (257^3 floats, 68 MB, up to 24 kept); 0 it evaluates them as it
  * applies them. The smoothed fields are the same bits either way. */
 void sifg_set_factor_tables(int on);
+/* Device mirrors of the structs' host arrays. Each C API call copies its
+ * inputs up from the structs' host arrays and its results down into them, so
+ * a pipeline (sif_grid_assign_cic, sif_grid_to_density_contrast,
+ * sif_chain_mesh_alloc, sif_finder_exodus) copies the positions up twice and
+ * the grid and the mesh up again right after copying them down. With mirrors
+ * on (1; or SIFG_HOST_MIRRORS=1 in the environment at sif_system_init), the
+ * device copy a call made of an array inside one of the library's own
+ * blocks (a field's positions and weights, a grid's values, a chain mesh's
+ * columns) is kept, and later calls that read the array use it instead of
+ * copying it again. A caller that writes such an array through the struct's
+ * pointer must then call sifg_host_modified with the array (or any address
+ * inside the block it lies in; NULL forgets every mirror) before the next
+ * call reads it. As a net for writes not declared, each mirror samples 1024
+ * evenly spaced words of its array when the two sides last agreed, and a call
+ * that finds any of them changed copies the array again; a write that misses
+ * every sampled word reads stale data. The library's own writes
+ * (sif_field_assign_positions, sif_field_assign_weights) and freed structs
+ * forget their mirrors themselves. 0 (default) copies every input on every
+ * call, as the reference's arrays behave. Mirrors hold at most 96 GB of
+ * device memory; an array past that is copied as without them. */
+void sifg_set_host_mirrors(int on);
+int sifg_host_mirrors(void);
+void sifg_host_modified(const void* ptr);
+/* The bytes the C API's calls have copied up from and down into the structs'
+ * host arrays (and the catalogues' columns) since the library was loaded. */
+void sifg_copy_bytes(uint64_t* h2d, uint64_t* d2h);
 /* A test hook, as the reference's sif__exodus_halt_after_set
  * (src/finder/exodus_checkpoint.h): the finder runs that follow stop after
  * n_rungs rungs of their ladder, checkpoint written, and fail as a job killed

@@ -47,7 +47,8 @@ EXPORTED = [
     # device-resident additions
     "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
     "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
-    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_set_witness", "sifg_set_factor_tables", "sifg_set_halt_after", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
+    "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_set_witness", "sifg_set_factor_tables", "sifg_set_halt_after",
+    "sifg_set_host_mirrors", "sifg_host_mirrors", "sifg_host_modified", "sifg_copy_bytes", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
     "sifg_mesh_device_noalloc",
     # the FP64 form
     "sifg_cic_device_f64", "sifg_contrast_device_f64", "sifg_mesh_device_f64",
@@ -105,6 +106,10 @@ def load():
         "sifg_set_witness": (None, [i32]),
         "sifg_set_factor_tables": (None, [i32]),
         "sifg_set_halt_after": (None, [u32]),
+        "sifg_set_host_mirrors": (None, [i32]),
+        "sifg_host_mirrors": (i32, []),
+        "sifg_host_modified": (None, [vp]),
+        "sifg_copy_bytes": (None, [C.POINTER(u64), C.POINTER(u64)]),
         "sifg_stream": (u64, []),
         "sifg_launch_count": (u64, []),
         "sifg_mesh_device_noalloc": (i32, [vp, vp, vp, u64, u32, f32, vp, vp, vp, vp, vp]),

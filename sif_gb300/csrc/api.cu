@@ -190,11 +190,37 @@ static void narrow(const uint64_t* in, uint32_t* out, uint64_t n, cudaStream_t s
   SIFG_LAUNCH_CHECK();
 }
 
-static void upload_positions(const sif_field_t* f, cudaStream_t st) {
+// The bytes the C API's calls copied between the structs' host arrays and
+// the device, since the library was loaded (sifg_copy_bytes).
+static uint64_t g_h2d_bytes = 0, g_d2h_bytes = 0;
+
+static void copy_up(void* d, const void* h, size_t b, cudaStream_t st) {
+  SIFG_CUDA(cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, st));
+  g_h2d_bytes += b;
+}
+
+static void copy_down(void* h, const void* d, size_t b, cudaStream_t st) {
+  SIFG_CUDA(cudaMemcpyAsync(h, d, b, cudaMemcpyDeviceToHost, st));
+  g_d2h_bytes += b;
+}
+
+// Host array h (b bytes) on the device for a call that only reads it: its
+// mirror where that stands, else copied up on st (into its mirror, or into
+// the API's scratch when mirrors are off).
+static const void* array_in(const void* h, size_t b, DevBuf& scratch, cudaStream_t st) {
+  bool holds = false;
+  void* d = mirror_acquire(h, b, b, scratch, &holds);
+  if (!holds) copy_up(d, h, b, st);
+  mirror_commit(h);
+  return d;
+}
+
+// The field's positions on the device, axis by axis.
+static void positions_in(const sif_field_t* f, cudaStream_t st, const float* d[3]) {
   const size_t b = f->n_particles * sizeof(float);
-  SIFG_CUDA(cudaMemcpyAsync(bufs().px.ensure(b), f->x, b, cudaMemcpyHostToDevice, st));
-  SIFG_CUDA(cudaMemcpyAsync(bufs().py.ensure(b), f->y, b, cudaMemcpyHostToDevice, st));
-  SIFG_CUDA(cudaMemcpyAsync(bufs().pz.ensure(b), f->z, b, cudaMemcpyHostToDevice, st));
+  d[0] = (const float*)array_in(f->x, b, bufs().px, st);
+  d[1] = (const float*)array_in(f->y, b, bufs().py, st);
+  d[2] = (const float*)array_in(f->z, b, bufs().pz, st);
 }
 
 static sif_catalogue_t* make_catalogue(const HostCatalogue& c) {
@@ -292,6 +318,7 @@ int sif_system_init(sif_config_t* config) {
   g_engine->host_threads =
       (config && config->omp_config && config->omp_config->n_threads) ? (int)config->omp_config->n_threads
                                                                       : omp_get_max_threads();
+  if (const char* v = getenv("SIFG_HOST_MIRRORS")) mirror_enable(atoi(v) != 0);
   g_init = true;
   g_status = SIF_OK;
   g_message.clear();
@@ -302,6 +329,7 @@ int sif_system_init(sif_config_t* config) {
 void sif_system_finalise(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   noalloc_forget();
+  mirror_clear();  // device memory goes with the engine; the switch stays
   g_engine.reset();
   host_pool_trim();
   g_init = false;
@@ -347,9 +375,19 @@ int sif_field_assign_positions(sif_field_t* f, const sif_real* x, const sif_real
     f->y = f->_position_block + n;
     f->z = f->_position_block + 2 * n;
   }
-  memcpy(f->x, x, n * sizeof(float));
-  memcpy(f->y, y, n * sizeof(float));
-  memcpy(f->z, z, n * sizeof(float));
+  // The three columns in slices over the host's threads (one thread's
+  // memcpy moves a gigabyte-sized field at a tenth of what the memory gives).
+  const float* src[3] = {x, y, z};
+  float* dst[3] = {f->x, f->y, f->z};
+  const int64_t slices = n >= (1u << 22) ? 64 : 1;
+#pragma omp parallel for schedule(static) if (slices > 1)
+  for (int64_t k = 0; k < 3 * slices; k++) {
+    const uint64_t a = n * (uint64_t)(k % slices) / slices, b = n * (uint64_t)(k % slices + 1) / slices;
+    memcpy(dst[k / slices] + a, src[k / slices] + a, (b - a) * sizeof(float));
+  }
+  mirror_forget(f->x);
+  mirror_forget(f->y);
+  mirror_forget(f->z);
   free(f->original_indices);
   f->original_indices = nullptr;
   f->state_flags = 0;
@@ -374,6 +412,7 @@ int sif_field_assign_weights(sif_field_t* f, const sif_real* weights) {
   const int st = sif_field_reserve_weights(f);
   if (st != SIF_OK) return st;
   memcpy(f->weights, weights, f->n_particles * sizeof(float));
+  mirror_forget(f->weights);
   return SIF_OK;
 }
 
@@ -435,25 +474,23 @@ int sif_grid_assign_cic(sif_grid_t* grid, const sif_field_t* field) {
   Engine* e = engine();
   if (!e) return SIF_ERR_UNINITIALISED;
   cudaStream_t s = e->stream();
-  upload_positions(field, s);
-  st = check_in_box(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(),
-                    field->n_particles, grid->box_length, "field", s, bufs().bad);
+  const float* dp[3];
+  positions_in(field, s, dp);
+  st = check_in_box(dp[0], dp[1], dp[2], field->n_particles, grid->box_length, "field", s, bufs().bad);
   if (st != SIF_OK) return st;
-  float* dg = (float*)bufs().grid.ensure(grid->total_cells * sizeof(float));
+  const size_t gb = grid->total_cells * sizeof(float);
+  bool holds = false;
+  float* dg = (float*)mirror_acquire(grid->values, gb, gb, bufs().grid, &holds);
   // Weighted (grid.c:635-639): the weights go up beside the positions.
   const float* dw = nullptr;
-  if (field->weights) {
-    const size_t wb = field->n_particles * sizeof(float);
-    dw = (const float*)bufs().pw.ensure(wb);
-    SIFG_CUDA(cudaMemcpyAsync((void*)dw, field->weights, wb, cudaMemcpyHostToDevice, s));
-  }
+  if (field->weights)
+    dw = (const float*)array_in(field->weights, field->n_particles * sizeof(float), bufs().pw, s);
   e->scratch.ensure(cic_scratch_bytes(field->n_particles, grid->n_cells, dw != nullptr));
-  cic_deposit(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(),
-              field->n_particles, grid->n_cells, grid->box_length, dg, e->scratch.ptr, s, nullptr,
-              nullptr, nullptr, nullptr, dw);
-  SIFG_CUDA(cudaMemcpyAsync(grid->values, dg, grid->total_cells * sizeof(float),
-                            cudaMemcpyDeviceToHost, s));
+  cic_deposit(dp[0], dp[1], dp[2], field->n_particles, grid->n_cells, grid->box_length, dg,
+              e->scratch.ptr, s, nullptr, nullptr, nullptr, nullptr, dw);
+  copy_down(grid->values, dg, gb, s);
   SIFG_CUDA(cudaStreamSynchronize(s));
+  mirror_commit(grid->values);
   grid->content = SIF_GRID_DENSITY;
   grid->assignment = SIF_ASSIGNMENT_CIC;
   grid->interlaced = 0;
@@ -473,15 +510,17 @@ int sif_grid_to_density_contrast(sif_grid_t* grid) {
   if (!e) return SIF_ERR_UNINITIALISED;
   cudaStream_t s = e->stream();
   const size_t b = grid->total_cells * sizeof(float);
-  float* dg = (float*)bufs().grid.ensure(b);
-  SIFG_CUDA(cudaMemcpyAsync(dg, grid->values, b, cudaMemcpyHostToDevice, s));
+  bool holds = false;
+  float* dg = (float*)mirror_acquire(grid->values, b, b, bufs().grid, &holds);
+  if (!holds) copy_up(dg, grid->values, b, s);
   double* scratch = (double*)e->scratch.ensure(density_contrast_scratch_bytes());
   density_contrast(dg, grid->total_cells, scratch, s);
   const double mean = read_mean(scratch, s);
   if (!(mean > 0.0))
     return fail(SIF_ERR_RANGE, fmt("grid: mean density %g (expected > 0)", mean));
-  SIFG_CUDA(cudaMemcpyAsync(grid->values, dg, b, cudaMemcpyDeviceToHost, s));
+  copy_down(grid->values, dg, b, s);
   SIFG_CUDA(cudaStreamSynchronize(s));
+  mirror_commit(grid->values);
   grid->content = SIF_GRID_DENSITY_CONTRAST;
   return SIF_OK;
   API_GUARD_END(SIF_ERR_INVALID)
@@ -518,84 +557,96 @@ static sif_chain_mesh_t* mesh_alloc(uint32_t n_cells, sif_real box, sif_field_t*
   Engine* e = engine();
   if (!e) return nullptr;
   cudaStream_t s = e->stream();
-  upload_positions(field, s);
-  if (check_in_box(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(), n, box,
-                   "field", s, bufs().bad) != SIF_OK)
+  const float* dp[3];
+  positions_in(field, s, dp);
+  if (check_in_box(dp[0], dp[1], dp[2], n, box, "field", s, bufs().bad) != SIF_OK) return nullptr;
+  const uint64_t cells = (uint64_t)n_cells * n_cells * n_cells;
+  const bool keep_idx = !(opt & SIF_MESH_DROP_INDICES);
+  const bool weighted = field->weights != nullptr;
+  // The struct and its host arrays first: the device buffers the build
+  // writes are their mirrors.
+  sif_chain_mesh_t* mesh = (sif_chain_mesh_t*)calloc(1, sizeof(sif_chain_mesh_t));
+  if (!mesh) {
+    fail(SIF_ERR_ALLOC, "mesh: cannot allocate");
     return nullptr;
+  }
+  struct Unwind {  // frees the half-built mesh on every early return
+    sif_chain_mesh_t* m;
+    ~Unwind() { sif_chain_mesh_free(m); }
+  } unwind{mesh};
+  mesh->n_cells = n_cells;
+  mesh->total_cells = cells;
+  mesh->box_length = box;
+  mesh->cell_length = box / (float)n_cells;
+  mesh->n_particles = n;
+  mesh->total_weight = (double)n;
+  mesh->_position_block = (float*)host_block_get(3 * (n ? n : 1) * sizeof(float));
+  mesh->cell_offsets = (uint64_t*)host_block_get((cells + 1) * sizeof(uint64_t));
+  if (keep_idx) mesh->original_indices = (uint64_t*)host_block_get(n * sizeof(uint64_t));
+  if (weighted) {
+    mesh->weights = (float*)host_block_get(n * sizeof(float));
+    mesh->cell_weights = (float*)host_block_get(cells * sizeof(float));
+  }
+  if (!mesh->_position_block || !mesh->cell_offsets || (keep_idx && !mesh->original_indices) ||
+      (weighted && (!mesh->weights || !mesh->cell_weights))) {
+    fail(SIF_ERR_ALLOC, "mesh: cannot allocate host arrays");
+    return nullptr;
+  }
+  mesh->x = mesh->_position_block;
+  mesh->y = mesh->_position_block + n;
+  mesh->z = mesh->_position_block + 2 * n;
+
   DeviceMesh m;
   m.n_cells = n_cells;
   m.box_length = box;
-  m.cell_length = box / (float)n_cells;
-  const uint64_t cells = (uint64_t)n_cells * n_cells * n_cells;
-  m.x = (float*)bufs().mx.ensure(n * 4);
-  m.y = (float*)bufs().my.ensure(n * 4);
-  m.z = (float*)bufs().mz.ensure(n * 4);
-  m.offsets = (uint32_t*)bufs().offs.ensure((cells + 1) * 4);
-  const bool keep_idx = !(opt & SIF_MESH_DROP_INDICES);
-  const bool weighted = field->weights != nullptr;
+  m.cell_length = mesh->cell_length;
+  bool holds = false;
+  m.x = (float*)mirror_acquire(mesh->x, n * 4, n * 4, bufs().mx, &holds);
+  m.y = (float*)mirror_acquire(mesh->y, n * 4, n * 4, bufs().my, &holds);
+  m.z = (float*)mirror_acquire(mesh->z, n * 4, n * 4, bufs().mz, &holds);
+  // The device keeps 32-bit offsets; the struct's are 64-bit.
+  m.offsets = (uint32_t*)mirror_acquire(mesh->cell_offsets, (cells + 1) * 8, (cells + 1) * 4,
+                                        bufs().offs, &holds);
   // A weighted mesh takes its weights through the source indices, kept on
   // the device whether or not the caller keeps them.
   m.orig = (keep_idx || weighted) ? (uint32_t*)bufs().orig.ensure(n * 4) : nullptr;
   e->scratch.ensure(std::max(mesh_scratch_bytes(n, n_cells),
                              weighted ? mesh_weights_scratch_bytes(n_cells) : (size_t)0));
-  mesh_build(bufs().px.as<float>(), bufs().py.as<float>(), bufs().pz.as<float>(), n, m,
-             e->scratch.ptr, s, nullptr);
-  double* d_total = nullptr;
+  mesh_build(dp[0], dp[1], dp[2], n, m, e->scratch.ptr, s, nullptr);
   if (weighted) {
     // chain_mesh.c:800-801, 624-672: the weights in mesh order, each cell's
     // sum, the total.
-    float* fw = (float*)bufs().pw.ensure(n * 4);
-    SIFG_CUDA(cudaMemcpyAsync(fw, field->weights, n * 4, cudaMemcpyHostToDevice, s));
-    m.w = (float*)bufs().mw.ensure(n * 4);
-    m.cell_w = (float*)bufs().mcw.ensure(cells * 4);
-    d_total = (double*)bufs().wtotal.ensure(sizeof(double));
+    const float* fw = (const float*)array_in(field->weights, n * 4, bufs().pw, s);
+    m.w = (float*)mirror_acquire(mesh->weights, n * 4, n * 4, bufs().mw, &holds);
+    m.cell_w = (float*)mirror_acquire(mesh->cell_weights, cells * 4, cells * 4, bufs().mcw, &holds);
+    double* d_total = (double*)bufs().wtotal.ensure(sizeof(double));
     mesh_weights(fw, m, e->scratch.ptr, d_total, s);
-  }
-
-  sif_chain_mesh_t* mesh = (sif_chain_mesh_t*)calloc(1, sizeof(sif_chain_mesh_t));
-  mesh->n_cells = n_cells;
-  mesh->total_cells = cells;
-  mesh->box_length = box;
-  mesh->cell_length = m.cell_length;
-  mesh->n_particles = n;
-  mesh->total_weight = (double)n;
-  if (weighted) {
-    mesh->weights = (float*)host_block_get(n * sizeof(float));
-    mesh->cell_weights = (float*)host_block_get(cells * sizeof(float));
-    if (!mesh->weights || !mesh->cell_weights) {
-      sif_chain_mesh_free(mesh);
-      fail(SIF_ERR_ALLOC, "mesh: cannot allocate the weight columns");
-      return nullptr;
-    }
-    SIFG_CUDA(cudaMemcpyAsync(mesh->weights, m.w, n * 4, cudaMemcpyDeviceToHost, s));
-    SIFG_CUDA(cudaMemcpyAsync(mesh->cell_weights, m.cell_w, cells * 4, cudaMemcpyDeviceToHost, s));
+    copy_down(mesh->weights, m.w, n * 4, s);
+    copy_down(mesh->cell_weights, m.cell_w, cells * 4, s);
     SIFG_CUDA(cudaMemcpyAsync(&mesh->total_weight, d_total, 8, cudaMemcpyDeviceToHost, s));
   }
-  mesh->_position_block = (float*)host_block_get(3 * (n ? n : 1) * sizeof(float));
-  mesh->x = mesh->_position_block;
-  mesh->y = mesh->_position_block + n;
-  mesh->z = mesh->_position_block + 2 * n;
-  mesh->cell_offsets = (uint64_t*)host_block_get((cells + 1) * sizeof(uint64_t));
-  if (keep_idx) mesh->original_indices = (uint64_t*)host_block_get(n * sizeof(uint64_t));
-  if (!mesh->_position_block || !mesh->cell_offsets || (keep_idx && !mesh->original_indices)) {
-    sif_chain_mesh_free(mesh);
-    fail(SIF_ERR_ALLOC, "mesh: cannot allocate host arrays");
-    return nullptr;
-  }
-  SIFG_CUDA(cudaMemcpyAsync(mesh->x, m.x, n * 4, cudaMemcpyDeviceToHost, s));
-  SIFG_CUDA(cudaMemcpyAsync(mesh->y, m.y, n * 4, cudaMemcpyDeviceToHost, s));
-  SIFG_CUDA(cudaMemcpyAsync(mesh->z, m.z, n * 4, cudaMemcpyDeviceToHost, s));
+  copy_down(mesh->x, m.x, n * 4, s);
+  copy_down(mesh->y, m.y, n * 4, s);
+  copy_down(mesh->z, m.z, n * 4, s);
   // The 64-bit offsets and indices of the reference's struct, widened on the
   // device and copied straight into the struct's arrays.
   uint64_t* wide = (uint64_t*)bufs().wide.ensure((keep_idx ? std::max<uint64_t>(n, cells + 1) : cells + 1) * 8);
   widen(m.offsets, wide, cells + 1, s);
-  SIFG_CUDA(cudaMemcpyAsync(mesh->cell_offsets, wide, (cells + 1) * 8, cudaMemcpyDeviceToHost, s));
+  copy_down(mesh->cell_offsets, wide, (cells + 1) * 8, s);
   if (keep_idx) {
     SIFG_CUDA(cudaStreamSynchronize(s));
     widen(m.orig, wide, n, s);
-    SIFG_CUDA(cudaMemcpyAsync(mesh->original_indices, wide, n * 8, cudaMemcpyDeviceToHost, s));
+    copy_down(mesh->original_indices, wide, n * 8, s);
   }
   SIFG_CUDA(cudaStreamSynchronize(s));
+  for (const void* h : {(const void*)mesh->x, (const void*)mesh->y, (const void*)mesh->z,
+                        (const void*)mesh->cell_offsets})
+    mirror_commit(h);
+  if (weighted) {
+    mirror_commit(mesh->weights);
+    mirror_commit(mesh->cell_weights);
+  }
+  unwind.m = nullptr;
   if (consume) {
     host_block_put(field->_position_block);
     field->_position_block = nullptr;
@@ -982,8 +1033,7 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   const uint64_t n = mesh->n_particles;
   const uint64_t mcells = mesh->total_cells;
   const size_t gb = grid->total_cells * sizeof(float);
-  float* dg = (float*)bufs().grid.ensure(gb);
-  SIFG_CUDA(cudaMemcpyAsync(dg, grid->values, gb, cudaMemcpyHostToDevice, s));
+  const float* dg = (const float*)array_in(grid->values, gb, bufs().grid, s);
   DeviceMesh m;
   m.n_cells = mesh->n_cells;
   m.box_length = mesh->box_length;
@@ -994,22 +1044,22 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   cudaStream_t cs = e->copy_stream();
   SIFG_CUDA(cudaEventRecord(e->ev_copy_start(), s));
   SIFG_CUDA(cudaStreamWaitEvent(cs, e->ev_copy_start(), 0));
-  m.x = (float*)bufs().mx.ensure(n * 4);
-  m.y = (float*)bufs().my.ensure(n * 4);
-  m.z = (float*)bufs().mz.ensure(n * 4);
-  m.offsets = (uint32_t*)bufs().offs.ensure((mcells + 1) * 4);
-  uint64_t* wide = (uint64_t*)bufs().wide.ensure((mcells + 1) * 8);
-  SIFG_CUDA(cudaMemcpyAsync(wide, mesh->cell_offsets, (mcells + 1) * 8, cudaMemcpyHostToDevice, cs));
-  narrow(wide, m.offsets, mcells + 1, cs);
-  SIFG_CUDA(cudaMemcpyAsync(m.x, mesh->x, n * 4, cudaMemcpyHostToDevice, cs));
-  SIFG_CUDA(cudaMemcpyAsync(m.y, mesh->y, n * 4, cudaMemcpyHostToDevice, cs));
-  SIFG_CUDA(cudaMemcpyAsync(m.z, mesh->z, n * 4, cudaMemcpyHostToDevice, cs));
+  bool holds = false;
+  m.offsets = (uint32_t*)mirror_acquire(mesh->cell_offsets, (mcells + 1) * 8, (mcells + 1) * 4,
+                                        bufs().offs, &holds);
+  if (!holds) {
+    uint64_t* wide = (uint64_t*)bufs().wide.ensure((mcells + 1) * 8);
+    copy_up(wide, mesh->cell_offsets, (mcells + 1) * 8, cs);
+    narrow(wide, m.offsets, mcells + 1, cs);
+  }
+  mirror_commit(mesh->cell_offsets);
+  m.x = (float*)array_in(mesh->x, n * 4, bufs().mx, cs);
+  m.y = (float*)array_in(mesh->y, n * 4, bufs().my, cs);
+  m.z = (float*)array_in(mesh->z, n * 4, bufs().mz, cs);
   if (mesh->weights) {
-    m.w = (float*)bufs().mw.ensure(n * 4);
-    m.cell_w = (float*)bufs().mcw.ensure(mcells * 4);
+    m.w = (float*)array_in(mesh->weights, n * 4, bufs().mw, cs);
+    m.cell_w = (float*)array_in(mesh->cell_weights, mcells * 4, bufs().mcw, cs);
     m.total_weight = mesh->total_weight;
-    SIFG_CUDA(cudaMemcpyAsync(m.w, mesh->weights, n * 4, cudaMemcpyHostToDevice, cs));
-    SIFG_CUDA(cudaMemcpyAsync(m.cell_w, mesh->cell_weights, mcells * 4, cudaMemcpyHostToDevice, cs));
   }
   SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
   // Whatever the run's outcome, the copies out of the caller's mesh end
@@ -1056,9 +1106,11 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   // SIF_FINDER_CONSUME_GRID it holds the last rung's smoothing, as the
   // reference leaves it (exodus_finder.c:2426-2453).
   if (consume) {
-    SIFG_CUDA(cudaMemcpyAsync(grid->values, consume, gb, cudaMemcpyDeviceToHost, s));
+    mirror_forget(grid->values);
+    copy_down(grid->values, consume, gb, s);
     SIFG_CUDA(cudaStreamSynchronize(s));
   }
+  g_d2h_bytes += 4 * sizeof(float) * (uint64_t)cat.cx.size();  // the catalogue's columns
   sif_catalogue_t* out = make_catalogue(cat);
   if (!out) fail(SIF_ERR_ALLOC, "catalogue: cannot allocate");
   return out;
@@ -1770,6 +1822,24 @@ void sifg_set_scan_mode(int mode) { set_scan_mode(mode == 1 ? 1 : 0); }
 void sifg_set_witness(int on) { set_witness(on); }
 
 void sifg_set_factor_tables(int on) { set_factor_tables(on); }
+
+void sifg_set_host_mirrors(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  mirror_enable(on != 0);
+}
+
+int sifg_host_mirrors(void) { return mirror_enabled() ? 1 : 0; }
+
+void sifg_host_modified(const void* ptr) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  mirror_forget(ptr);
+}
+
+void sifg_copy_bytes(uint64_t* h2d, uint64_t* d2h) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (h2d) *h2d = g_h2d_bytes;
+  if (d2h) *d2h = g_d2h_bytes;
+}
 
 void sifg_set_window(int bins) { g_window = bins < 1 ? 1 : (bins > 64 ? 64 : bins); }
 

@@ -94,6 +94,9 @@ void host_block_put(void* ptr) {
     return;
   }
   const Block b = it->second;
+  // The block's content is gone for whoever takes it next: its device
+  // mirrors with it (the registry's own lock, taken inside the pool's).
+  mirror_forget_block(ptr, b.bytes);
   p.live.erase(it);
   p.spare.emplace_back(ptr, b);
   p.spare_bytes += b.bytes;
@@ -102,6 +105,21 @@ void host_block_put(void* ptr) {
     p.spare_bytes -= p.spare.front().second.bytes;
     p.spare.pop_front();
   }
+}
+
+bool host_block_find(const void* p, const void** start, size_t* bytes) {
+  Pool& pl = pool();
+  std::lock_guard<std::mutex> lk(pl.mu);
+  const char* c = (const char*)p;
+  for (const auto& kv : pl.live) {
+    const char* s = (const char*)kv.first;
+    if (c >= s && c < s + kv.second.bytes) {
+      *start = kv.first;
+      *bytes = kv.second.bytes;
+      return true;
+    }
+  }
+  return false;
 }
 
 void host_pool_trim() {

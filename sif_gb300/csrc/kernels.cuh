@@ -49,6 +49,28 @@ struct DevBuf {
 void* host_block_get(size_t bytes);
 void host_block_put(void* ptr);
 void host_pool_trim();
+// The live block holding p (its start and size), if p lies in one.
+bool host_block_find(const void* p, const void** start, size_t* bytes);
+
+// --- mirror.cu ---
+// Device mirrors of host arrays inside the library's blocks (off until
+// mirror_enable(true)). mirror_acquire: the device buffer a call uses for host
+// array `host` (host_bytes on the host, dev_bytes in its device form) --
+// the array's mirror, or `scratch` when mirrors are off, the array is not in
+// a library block, or the mirrors' cap is reached -- and whether it already
+// holds the array's content (*holds). The mirror stands again only after
+// mirror_commit(host), called once the two sides agree (the copy either way
+// done or ordered before any later use). mirror_forget: the mirrors within
+// the live block holding p (every mirror for NULL); mirror_forget_block: those
+// within [start, start + bytes).
+void mirror_enable(bool on);
+bool mirror_enabled();
+void* mirror_acquire(const void* host, size_t host_bytes, size_t dev_bytes, DevBuf& scratch,
+                     bool* holds);
+void mirror_commit(const void* host);
+void mirror_forget(const void* p);
+void mirror_forget_block(const void* start, size_t bytes);
+void mirror_clear();
 
 // --- scan.cu ---
 // In-place exclusive prefix sum of n uint32 values (n < 2^31). The chunk

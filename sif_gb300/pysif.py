@@ -39,6 +39,39 @@ def system_finalise():
     _lib.load().sif_system_finalise()
 
 
+def set_host_mirrors(on):
+    """Keep device copies of the structs' host arrays between calls
+    (sifg_set_host_mirrors): a pipeline then copies each array up once. With
+    mirrors on, writes through a struct's arrays (Grid.values) must be
+    declared with host_modified before the next call reads them."""
+    _lib.load().sifg_set_host_mirrors(1 if on else 0)
+
+
+def host_modified(obj=None):
+    """Declares writes through a struct's host arrays (sifg_host_modified):
+    a Grid, a Field, a ChainMesh, or None for every mirror."""
+    lib = _lib.load()
+    if obj is None:
+        lib.sifg_host_modified(None)
+        return
+    c = obj._ptr.contents
+    ptr = c.values if isinstance(obj, Grid) else c.x
+    lib.sifg_host_modified(C.cast(ptr, C.c_void_p))
+    if isinstance(obj, (Field, ChainMesh)) and c.weights:
+        lib.sifg_host_modified(C.cast(c.weights, C.c_void_p))
+    if isinstance(obj, ChainMesh):
+        lib.sifg_host_modified(C.cast(c.cell_offsets, C.c_void_p))
+        if c.cell_weights:
+            lib.sifg_host_modified(C.cast(c.cell_weights, C.c_void_p))
+
+
+def copy_bytes():
+    """(host->device, device->host) bytes the C API has copied so far."""
+    h2d, d2h = C.c_uint64(0), C.c_uint64(0)
+    _lib.load().sifg_copy_bytes(C.byref(h2d), C.byref(d2h))
+    return h2d.value, d2h.value
+
+
 class Field:
     """Particle positions (float32, in [0, box)) and, optionally, per-particle
     weights (a mass, a luminosity, a selection weight; None: every particle

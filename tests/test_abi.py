@@ -310,3 +310,20 @@ def test_reads_the_reference_checkpoint(lib, tmp_path):
     bad.write_bytes(bytes(raw[:-4]))
     assert not lib.sif_finder_exodus_checkpoint_read(str(bad).encode(), None)
     assert b"bytes" in lib.sif_error_message()
+
+
+def test_host_mirror_switch_without_a_gpu(lib):
+    """The mirrors' switch and the copy counters answer without a device;
+    declaring a write to an address the library never mirrored is harmless."""
+    import ctypes as C
+
+    lib.sifg_set_host_mirrors(1)
+    assert lib.sifg_host_mirrors() == 1
+    buf = (C.c_float * 16)()
+    lib.sifg_host_modified(C.cast(buf, C.c_void_p))
+    lib.sifg_host_modified(None)
+    lib.sifg_set_host_mirrors(0)
+    assert lib.sifg_host_mirrors() == 0
+    h2d, d2h = C.c_uint64(1), C.c_uint64(1)
+    lib.sifg_copy_bytes(C.byref(h2d), C.byref(d2h))
+    assert h2d.value == 0 and d2h.value == 0
