@@ -597,10 +597,12 @@ void sifg_copy_bytes(uint64_t* h2d, uint64_t* d2h);
  * there would; 0 lets them finish. */
 void sifg_set_halt_after(uint32_t n_rungs);
 /* The collision witness (exodus_finder.c:780-845, exodus_rescale.c:
- * 1074-1167): 1 (default) survivors whose sphere is certain to collide with
- * a void of an earlier rung at any radius they could return are refused
- * before growth, as the reference refuses them; 0 every survivor is grown
- * and the commit refuses them. The catalogue does not depend on it. */
+ * 1074-1167): 1 survivors whose sphere is certain to collide with a void of
+ * an earlier rung at any radius they could return are refused before growth,
+ * as the reference refuses them; 0 (default) every survivor is grown and the
+ * commit refuses them. The catalogue does not depend on it. On the GPU the
+ * proof costs more than the growth it saves (at 512^3: 2.1 ms a step to
+ * refuse 1.5% of the survivors, 1.1 ms a step more in all). */
 void sifg_set_witness(int on);
 /* The chain-mesh build of sifg_mesh_device, for callers that cannot let the
  * library allocate device memory: a process whose framework reserves the

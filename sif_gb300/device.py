@@ -229,8 +229,8 @@ def set_scan_mode(mode):
 
 
 def set_witness(on):
-    """1 the collision witness refuses doomed survivors before growth, 0 every
-    survivor is grown; the catalogue is the same."""
+    """1 the collision witness refuses doomed survivors before growth, 0 (the
+    default) every survivor is grown; the catalogue is the same."""
     _lib.load().sifg_set_witness(int(on))
 
 

@@ -360,23 +360,23 @@ def test_catalogue_matches_reference_golden_any_shell_list(dev, golden_box32, sh
 
 
 @pytest.mark.parametrize("name", ["default", "search_2_00", "lagrangian", "minima", "overlap_0_5"])
-def test_catalogue_matches_reference_golden_without_the_witness(dev, golden_box32, name):
+def test_catalogue_matches_reference_golden_with_the_witness(dev, golden_box32, name):
     """The collision witness only refuses survivors the commit would refuse:
-    switched off, the reference's catalogue all the same."""
-    dev.set_witness(0)
+    switched on, the reference's catalogue all the same."""
+    dev.set_witness(1)
     try:
         test_catalogue_matches_reference_golden(dev, golden_box32, name)
     finally:
-        dev.set_witness(1)
+        dev.set_witness(0)
 
 
 @pytest.mark.parametrize("name", EXTEND_SETS)
-def test_extended_reach_golden_without_the_witness(dev, golden_box32_extend, name):
-    dev.set_witness(0)
+def test_extended_reach_golden_with_the_witness(dev, golden_box32_extend, name):
+    dev.set_witness(1)
     try:
         test_catalogue_matches_reference_golden(dev, golden_box32_extend, name)
     finally:
-        dev.set_witness(1)
+        dev.set_witness(0)
 
 
 @pytest.fixture(params=[0, 1], ids=["one_launch", "launch_per_round"])

@@ -82,17 +82,16 @@ def test_workload_a_box_path_matches_the_oracle(dev, oracle):
     want = _oracle_on_gpu_fields(dev, oracle, xs, grid, fields, n, box, nm, radii, thr)
     assert len(want[0]) > 500
     assert len(got[0]) == len(want[0]) and same_catalogue(got, want)
-    # The collision witness refused survivors before growth, and without it
-    # (every survivor grown, the commit refusing them) the catalogue is the
-    # same.
-    refused = sum(r["n_witness"] for r in dev.last_rung_stats())
-    assert refused > 0
-    dev.set_witness(0)
+    # Every survivor grown (the default), the commit refusing the doomed
+    # ones; with the collision witness refusing them before growth the
+    # catalogue is the same.
+    assert sum(r["n_witness"] for r in dev.last_rung_stats()) == 0
+    dev.set_witness(1)
     try:
         assert same_catalogue(dev.box(*xs, n, box, nm, radii, thr), want)
-        assert sum(r["n_witness"] for r in dev.last_rung_stats()) == 0
+        assert sum(r["n_witness"] for r in dev.last_rung_stats()) > 0
     finally:
-        dev.set_witness(1)
+        dev.set_witness(0)
     # Each sphere-growth kernel forced gives the same catalogue.
     for mode in (1, 2):
         dev.set_growth_mode(mode)
