@@ -2089,6 +2089,401 @@ static int cand_masked(const uint64_t* mask, const orc_candidate_t* c, const orc
  * rescaled radius) -- and the batch and window retuning between them. */
 /* The rescaling a run calls for a candidate (exodus_finder.c:2046-2072):
  * weighted on a weighted mesh. */
+/* ---------------------------------------------------------------------------
+ * Surveys: the footprint the randoms mark out, the field scanned against
+ * them, the radius grown against them, and how much of each void was
+ * observed (src/finder/exodus_survey.c; exodus_rescale.c:1944-2317).
+ * ------------------------------------------------------------------------- */
+
+/* SIF__FINDER_UNOBSERVED, src/finder/utils.h:161-166. */
+#define SURVEY_OUTSIDE 1e30f
+/* CLOSING_MIN_RANDOMS, CLOSING_MAX_RADIUS, exodus_survey.c:59-60. */
+#define CLOSING_MIN_RANDOMS 128.0
+#define CLOSING_MAX_RADIUS 4
+/* RESCALE_NO_RANDOMS, src/finder/exodus_internal.h:174. */
+#define ORC_RESCALE_NO_RANDOMS 6
+
+/* survey_node, exodus_survey.c:41-44: the node nearest a position. */
+static inline uint32_t survey_node(float p, float inv_l, uint32_t n) {
+  const uint32_t i = (uint32_t)(p * inv_l + 0.5f);
+  return i < n ? i : n - 1;
+}
+
+/* survey_randoms_per_node, exodus_survey.c:68-80: lambda from m = lambda /
+ * (1 - exp(-lambda)) by 64 bisections. */
+static double survey_randoms_per_node(double m) {
+  if (!(m > 1.0))
+    return 0.0;
+  double lo = 0.0, hi = m;
+  for (int i = 0; i < 64; i++) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid < m * (1.0 - exp(-mid)))
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+/* survey_close_pass, exodus_survey.c:89-120: along `axis`, a node is set when
+ * its window of 2k + 1 nodes (those past the faces unset) holds any set node
+ * (dilate) or only set nodes (erode). */
+static void survey_close_pass(const uint64_t* src, uint64_t* dst, uint32_t n, int axis,
+  int32_t k, int erode) {
+  const uint64_t n2 = (uint64_t)n * n;
+  const uint64_t stride = axis == 0 ? n2 : (axis == 1 ? n : 1);
+  const uint64_t step_a = axis == 0 ? n : n2;
+  const uint64_t step_b = axis == 2 ? n : 1;
+  const int32_t len = (int32_t)n, full = 2 * k + 1;
+  memset(dst, 0, ((n2 * n + 63) / 64) * sizeof(uint64_t));
+  for (uint64_t line = 0; line < n2; line++) {
+    const uint64_t base = (line / n) * step_a + (line % n) * step_b;
+    for (int32_t i = 0; i < len; i++) {
+      int32_t count = 0;
+      for (int32_t j = i - k; j <= i + k; j++)
+        if (j >= 0 && j < len)
+          count += mask_get(src, base + (uint64_t)j * stride);
+      if (erode ? count == full : count > 0)
+        mask_set(dst, base + (uint64_t)i * stride);
+    }
+  }
+}
+
+uint64_t orc_survey_occupancy(const orc_mesh_t* rm, uint32_t n, float box, uint64_t* occ,
+  int32_t* k_out) {
+  /* sif__exodus_survey_occupancy, exodus_survey.c:159-201: every node a
+   * random is nearest to, then closed (dilated, then eroded) over a box of
+   * 2k + 1 nodes, k the smallest that expects CLOSING_MIN_RANDOMS at the
+   * randoms' density over the marked nodes, at most CLOSING_MAX_RADIUS. */
+  const uint64_t total = (uint64_t)n * n * n;
+  const uint64_t words = (total + 63) / 64;
+  memset(occ, 0, words * sizeof(uint64_t));
+  const float cell = box / (float)n;
+  const float inv_l = 1.0f / cell;
+  for (uint64_t p = 0; p < rm->n_particles; p++) {
+    const uint64_t ix = survey_node(rm->x[p], inv_l, n), iy = survey_node(rm->y[p], inv_l, n),
+                   iz = survey_node(rm->z[p], inv_l, n);
+    mask_set(occ, (ix * n + iy) * n + iz);
+  }
+  uint64_t marked = 0;
+  for (uint64_t w = 0; w < words; w++)
+    marked += (uint64_t)__builtin_popcountll(occ[w]);
+  *k_out = 0;
+  if (marked == 0)
+    return 0;
+  const double lambda = survey_randoms_per_node((double)rm->n_particles / (double)marked);
+  int32_t k = 1;
+  while (k < CLOSING_MAX_RADIUS &&
+         lambda * (2 * k + 1) * (2 * k + 1) * (2 * k + 1) < CLOSING_MIN_RANDOMS)
+    k++;
+  *k_out = k;
+  uint64_t* tmp = malloc(words * sizeof(uint64_t));
+  survey_close_pass(occ, tmp, n, 0, k, 0);
+  survey_close_pass(tmp, occ, n, 1, k, 0);
+  survey_close_pass(occ, tmp, n, 2, k, 0);
+  survey_close_pass(tmp, occ, n, 0, k, 1);
+  survey_close_pass(occ, tmp, n, 1, k, 1);
+  survey_close_pass(tmp, occ, n, 2, k, 1);
+  free(tmp);
+  uint64_t observed = 0;
+  for (uint64_t w = 0; w < words; w++)
+    observed += (uint64_t)__builtin_popcountll(occ[w]);
+  return observed;
+}
+
+/* sif__exodus_survey_contrast, exodus_survey.c:215-227: the smoothed data
+ * over alpha times the smoothed randoms, less 1, on observed nodes with an
+ * expectation; SURVEY_OUTSIDE elsewhere. */
+static void survey_contrast(float* data, const float* randoms, const uint64_t* occ,
+  float alpha, uint64_t total) {
+  for (uint64_t c = 0; c < total; c++) {
+    const float expected = alpha * randoms[c];
+    data[c] = (mask_get(occ, c) && expected > 0.0f) ? data[c] / expected - 1.0f : SURVEY_OUTSIDE;
+  }
+}
+
+static inline double survey_w(const float* w, uint64_t p) { return w ? (double)w[p] : 1.0; }
+
+/* survey_sphere_total, exodus_rescale.c:1957-1993: the weight and the tracers
+ * within r_search, whole core and shell cells from the cell table (or their
+ * counts), the rest tracer by tracer. */
+static void survey_sphere_total(const query_t* q, float rs2, double* w_out, uint64_t* n_out) {
+  const orc_mesh_t* m = q->m;
+  double w = 0.0;
+  uint64_t n = 0;
+  for (uint32_t i = 0; i < q->t->count; i++) {
+    const uint8_t type = q->t->type[i];
+    uint64_t s, e;
+    float ex, ey, ez;
+    if (!query_cell(q, i, &s, &e, &ex, &ey, &ez))
+      continue;
+    if (type == CELL_CORE || type == CELL_SHELL) {
+      w += m->cell_w ? (double)m->cell_w[query_flat(q, i)] : (double)(e - s);
+      n += e - s;
+      continue;
+    }
+    for (uint64_t p = s; p < e; p++)
+      if (dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez) <= rs2) {
+        w += survey_w(m->w, p);
+        n++;
+      }
+  }
+  *w_out = w;
+  *n_out = n;
+}
+
+/* survey_histogram, exodus_rescale.c:2000-2056: one mesh's weight per bin of
+ * the annulus, in its core and in the annulus. */
+static void survey_histogram(const query_t* q, double* bins, uint32_t nb, float rc2, float rs2,
+  float inv_w, double* core_out, double* shell_out) {
+  const orc_mesh_t* m = q->m;
+  double core = 0.0, shell = 0.0;
+  memset(bins, 0, nb * sizeof(double));
+  for (uint32_t i = 0; i < q->t->count; i++) {
+    const uint8_t type = q->t->type[i];
+    uint64_t s, e;
+    float ex, ey, ez;
+    if (!query_cell(q, i, &s, &e, &ex, &ey, &ez))
+      continue;
+    if (type == CELL_CORE) {
+      core += m->cell_w ? (double)m->cell_w[query_flat(q, i)] : (double)(e - s);
+    } else if (type == CELL_SHELL) {
+      for (uint64_t p = s; p < e; p++) {
+        const float d2 = dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez);
+        const double w = survey_w(m->w, p);
+        bins[bin_of(d2, rc2, inv_w, nb)] += w;
+        shell += w;
+      }
+    } else {
+      for (uint64_t p = s; p < e; p++) {
+        const float d2 = dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez);
+        const double w = survey_w(m->w, p);
+        if (d2 <= rc2) {
+          core += w;
+        } else if (d2 <= rs2) {
+          bins[bin_of(d2, rc2, inv_w, nb)] += w;
+          shell += w;
+        }
+      }
+    }
+  }
+  *core_out = core;
+  *shell_out = shell;
+}
+
+/* survey_resolve, exodus_rescale.c:2058-2146: the data tracers in bins
+ * [blo, bhi], sorted (the reference's pair quicksort) and walked outside-in
+ * against the random weight interpolated at each one's distance. */
+static int survey_resolve(const query_t* dq, uint32_t blo, uint32_t bhi, float lo, float hi,
+  float rc2, float rs2, float inv_w, float bin_w, uint32_t nb, double d_top, double r_top,
+  const double* rbins, float K, float* out, pair_t** buf, uint64_t* cap) {
+  const orc_mesh_t* m = dq->m;
+  uint64_t count = 0;
+  for (uint32_t i = 0; i < dq->t->count; i++) {
+    const uint8_t type = dq->t->type[i];
+    if (type == CELL_CORE || dq->t->max_d2[i] < lo || dq->t->min_d2[i] > hi)
+      continue;
+    uint64_t s, e;
+    float ex, ey, ez;
+    if (!query_cell(dq, i, &s, &e, &ex, &ey, &ez))
+      continue;
+    if (count + (e - s) > *cap) {
+      while (count + (e - s) > *cap)
+        *cap *= 2;
+      *buf = realloc(*buf, *cap * sizeof(pair_t));
+    }
+    for (uint64_t p = s; p < e; p++) {
+      const float d2 = dist2(m->x[p], m->y[p], m->z[p], ex, ey, ez);
+      if (type != CELL_SHELL && !(d2 > rc2 && d2 <= rs2))
+        continue;
+      const uint32_t bi = bin_of(d2, rc2, inv_w, nb);
+      if (bi < blo || bi > bhi)
+        continue;
+      (*buf)[count++] = (pair_t){d2, (float)survey_w(m->w, p)};
+    }
+  }
+  pair_t* pr = *buf;
+  if (count > 1)
+    pairs_sort(pr, 0, (int64_t)count - 1);
+  uint32_t cur = bhi;
+  double r_below = r_top - rbins[bhi];
+  double d_cur = d_top;
+  for (int64_t k = (int64_t)count - 1; k >= 0; k--) {
+    const float d2 = pr[k].d2;
+    const double wt = (double)pr[k].w;
+    if (d2 == 0.0f) {
+      d_cur -= wt;
+      continue;
+    }
+    const uint32_t bi = bin_of(d2, rc2, inv_w, nb);
+    while (cur > bi) {
+      cur--;
+      r_below -= rbins[cur];
+    }
+    float frac = (d2 - (rc2 + (float)cur * bin_w)) * inv_w;
+    frac = frac < 0.0f ? 0.0f : (frac > 1.0f ? 1.0f : frac);
+    const float r_in = (float)(r_below + rbins[cur] * (double)frac);
+    const float d_in = (float)(d_cur - wt);
+    if (r_in > 0.0f && d_in <= K * r_in) {
+      *out = sqrtf(d2);
+      return 1;
+    }
+    d_cur -= wt;
+  }
+  return 0;
+}
+
+/* sif__exodus_find_radius_survey, exodus_rescale.c:2154-2317: the largest
+ * data distance at which D(<d) <= K R(<d), data and randoms each on its own
+ * mesh and template. */
+float orc_find_radius_survey(const orc_mesh_t* dm, const orc_template_t* dt,
+  const orc_mesh_t* rm, const orc_template_t* rt, float cx, float cy, float cz,
+  float r_search, float K, float rmin, uint32_t window, uint8_t* reason, uint64_t* span_sum,
+  uint64_t* span_count) {
+  *reason = ORC_RESCALE_OK;
+  const float dinv = 1.0f / dm->cell_length, rinv = 1.0f / rm->cell_length;
+  const query_t dq = {dm, dt, cx, cy, cz, (int32_t)(cx * dinv), (int32_t)(cy * dinv),
+    (int32_t)(cz * dinv)};
+  const query_t rq = {rm, rt, cx, cy, cz, (int32_t)(cx * rinv), (int32_t)(cy * rinv),
+    (int32_t)(cz * rinv)};
+  const float rs2 = r_search * r_search, rc2 = rmin * rmin, span = rs2 - rc2;
+  if (!(span > 0.0f)) {
+    *reason = ORC_RESCALE_DEGENERATE;
+    return -1.0f;
+  }
+  double d_within, r_within;
+  uint64_t n_d, n_r;
+  survey_sphere_total(&dq, rs2, &d_within, &n_d);
+  survey_sphere_total(&rq, rs2, &r_within, &n_r);
+  if (!(r_within > 0.0)) {
+    *reason = ORC_RESCALE_NO_RANDOMS;
+    return -1.0f;
+  }
+  if ((float)d_within <= K * (float)r_within) {
+    *reason = ORC_RESCALE_BEYOND_SEARCH;
+    return -1.0f;
+  }
+  uint32_t nb = 2048u;
+  {
+    const float core_fraction = (rmin * rmin * rmin) / (r_search * r_search * r_search);
+    const float want = (float)n_d * (1.0f - core_fraction) / 16.0f;
+    if (!(want >= 64.0f))
+      nb = 64u;
+    else if (want < 2048.0f)
+      nb = (uint32_t)want;
+  }
+  const float inv_w = (float)nb / span, bin_w = span / (float)nb;
+  double* dbins = malloc(nb * sizeof(double));
+  double* rbins = malloc(nb * sizeof(double));
+  double d_core, d_shell, r_core, r_shell;
+  survey_histogram(&dq, dbins, nb, rc2, rs2, inv_w, &d_core, &d_shell);
+  survey_histogram(&rq, rbins, nb, rc2, rs2, inv_w, &r_core, &r_shell);
+  const double d_total = d_core + d_shell, r_total = r_core + r_shell;
+  float result = -1.0f;
+  uint64_t cap = 4096;
+  pair_t* buf = malloc(cap * sizeof(pair_t));
+  if (!(r_total > 0.0)) {
+    *reason = ORC_RESCALE_NO_RANDOMS;
+  } else if ((float)d_total <= K * (float)r_total) {
+    *reason = ORC_RESCALE_BEYOND_SEARCH;
+  } else {
+    *reason = ORC_RESCALE_BELOW_RUNG;
+    double d_above = 0.0, r_above = 0.0;
+    int32_t b_first = -1;
+    for (int32_t b = (int32_t)nb - 1; b >= 0; b--) {
+      const double bd = dbins[b], br = rbins[b];
+      if (!(bd > 0.0)) {
+        r_above += br;
+        continue;
+      }
+      float hi = rc2 + (float)(b + 1) * bin_w;
+      if (b == (int32_t)nb - 1)
+        hi = rs2 * (1.0f + 1e-6f);
+      const float d_in_min = (float)(d_total - d_above - bd);
+      const float r_in_max = (float)(r_total - r_above);
+      if (!(r_in_max > 0.0f) || d_in_min > K * r_in_max) {
+        d_above += bd;
+        r_above += br;
+        continue;
+      }
+      if (b_first < 0)
+        b_first = b;
+      int32_t b_lo = b - (int32_t)(window - 1);
+      if (b_lo < 0)
+        b_lo = 0;
+      double win_d = 0.0, win_r = 0.0;
+      for (int32_t bb = b_lo; bb <= b; bb++) {
+        win_d += dbins[bb];
+        win_r += rbins[bb];
+      }
+      const float win_lo = rc2 + (float)b_lo * bin_w;
+      float radius = -1.0f;
+      if (survey_resolve(&dq, (uint32_t)b_lo, (uint32_t)b, win_lo, hi, rc2, rs2, inv_w, bin_w,
+            nb, d_total - d_above, r_total - r_above, rbins, K, &radius, &buf, &cap)) {
+        const int32_t b_found = (int32_t)bin_of(radius * radius, rc2, inv_w, nb);
+        int32_t reached = b_first - b_found + 1;
+        if (reached < 1)
+          reached = 1;
+        *span_sum += (uint64_t)reached;
+        (*span_count)++;
+        *reason = ORC_RESCALE_OK;
+        result = radius;
+        break;
+      }
+      d_above += win_d;
+      r_above += win_r;
+      b = b_lo;
+    }
+  }
+  free(buf);
+  free(dbins);
+  free(rbins);
+  return result;
+}
+
+/* survey_void_footprint, exodus_survey.c:240-296: the observed fraction of a
+ * lattice of points through the sphere and through the shell out to twice its
+ * radius, spaced a sixteenth of the diameter (half a cell at least). */
+static void survey_void_footprint(const uint64_t* occ, uint32_t n, float box, float cx,
+  float cy, float cz, float r, float* inside, float* shell) {
+  const float l = box / (float)n;
+  const float inv_l = 1.0f / l;
+  float h = 0.125f * r;
+  if (h < 0.5f * l)
+    h = 0.5f * l;
+  const int32_t half = (int32_t)(2.0f * r / h) + 1;
+  const float r2 = r * r, r2_out = 4.0f * r2;
+  uint64_t n_in = 0, occ_in = 0, n_sh = 0, occ_sh = 0;
+  for (int32_t a = -half; a < half; a++) {
+    const float dx = ((float)a + 0.5f) * h;
+    for (int32_t b = -half; b < half; b++) {
+      const float dy = ((float)b + 0.5f) * h;
+      for (int32_t c = -half; c < half; c++) {
+        const float dz = ((float)c + 0.5f) * h;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 > r2_out)
+          continue;
+        const float px = cx + dx, py = cy + dy, pz = cz + dz;
+        int o = 0;
+        if (px >= 0.0f && px < box && py >= 0.0f && py < box && pz >= 0.0f && pz < box) {
+          const uint64_t ix = survey_node(px, inv_l, n), iy = survey_node(py, inv_l, n),
+                         iz = survey_node(pz, inv_l, n);
+          o = mask_get(occ, (ix * n + iy) * n + iz);
+        }
+        if (d2 <= r2) {
+          n_in++;
+          occ_in += (uint64_t)o;
+        } else {
+          n_sh++;
+          occ_sh += (uint64_t)o;
+        }
+      }
+    }
+  }
+  *inside = n_in ? (float)((double)occ_in / (double)n_in) : 0.0f;
+  *shell = n_sh ? (float)((double)occ_sh / (double)n_sh) : 0.0f;
+}
+
 static float grow_one(const orc_mesh_t* m, const orc_template_t* t, float cx, float cy,
   float cz, float r_search, float threshold, float vol_factor, float mass_factor, float rmin,
   uint32_t window, uint8_t* reason, uint64_t* span_sum, uint64_t* span_count) {
@@ -2134,6 +2529,11 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
    * (sif__finder_scan_refined with minima_only, utils.c:406-552); nothing
    * else of the run changes (exodus_finder.c:287-292). */
   const int minima = (opt & (1u << 9)) != 0;
+  /* A survey (exodus_survey.c:401-545, exodus_finder.c:1114-1137): cell
+   * seeds on their nodes only. */
+  const int survey = p->random_mesh != NULL;
+  if (survey && (refine || displace || extend_reach || minima || !p->random_grid))
+    return -2;
 
   float* radii = malloc(n_radii * sizeof(float));
   memcpy(radii, radii_in, n_radii * sizeof(float));
@@ -2167,10 +2567,43 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
       return -2;
     }
   }
+  if (survey) {
+    const orc_mesh_t* rm = p->random_mesh;
+    for (uint64_t i = 0; rm->w && i < rm->n_particles; i++) {
+      uint32_t b;
+      memcpy(&b, &rm->w[i], 4);
+      if (((b >> 23) & 0xFFu) == 0xFFu || ((b >> 31) && (b << 1))) {
+        free(radii);
+        return -2;
+      }
+    }
+    if ((rm->w && !rm->cell_w) || !(rm->total_weight > 0.0) || !(mesh->total_weight > 0.0) ||
+        rm->box_length != box) {
+      free(radii);
+      return -2;
+    }
+  }
 
   orc_spectrum_t* spec = NULL;
-  if (!p->inject)
+  orc_spectrum_t* rspec = NULL;
+  if (!p->inject) {
     spec = orc_spectrum_new(delta, N, box, window_mode, p->smoothing_mode);
+    if (survey)
+      rspec = orc_spectrum_new(p->random_grid, N, box, window_mode, p->smoothing_mode);
+  }
+  /* The survey's footprint and normalisation (exodus_finder.c:630-644,
+   * 1649-1653): the observed nodes, how much data weight each unit of random
+   * weight stands for, and the rescaling's K. */
+  uint64_t* occ = NULL;
+  float survey_alpha = 0.0f, survey_K = 0.0f;
+  if (survey) {
+    int32_t k_close;
+    occ = calloc((total + 63) / 64, sizeof(uint64_t));
+    orc_survey_occupancy(p->random_mesh, N, box, occ, &k_close);
+    survey_alpha = (float)(mesh->total_weight / p->random_mesh->total_weight);
+    survey_K = (1.0f + threshold) * survey_alpha;
+  }
+  float* rfield = survey ? malloc(total * sizeof(float)) : NULL;
 
   const float box_volume = box * box * box;
   const float mean_density = (float)mesh->n_particles / box_volume;
@@ -2250,6 +2683,15 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
       memcpy(field, p->inject + inj_k++ * total, total * sizeof(float));
     else
       orc_spectrum_smooth(spec, 1, radius, 0.0f, field, NULL);
+    /* A survey's rung (exodus_finder.c:1729-1737): the randoms smoothed the
+     * same way, then the field scanned is the data against them. */
+    if (survey) {
+      if (p->inject)
+        memcpy(rfield, p->inject + inj_k++ * total, total * sizeof(float));
+      else
+        orc_spectrum_smooth(rspec, 1, radius, 0.0f, rfield, NULL);
+      survey_contrast(field, rfield, occ, survey_alpha, total);
+    }
 
     /* The scan, src/finder/utils.c:130-213: 256 fixed chunks counted, their
      * offsets, each chunk written in flat order; then the sort. */
@@ -2359,8 +2801,16 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
     float r_search = radius + fmaxf((search_factor - 1.0f) * radius, 3.0f * cell);
     if (ri > 0 && radii[ri - 1] > r_search)
       r_search = radii[ri - 1];
-    orc_template_t tpl;
+    orc_template_t tpl, rtpl;
+    memset(&rtpl, 0, sizeof(rtpl));
     if (orc_template_build(&tpl, mesh->n_cells, mesh->cell_length, rmin, r_search)) {
+      status = -3;
+      break;
+    }
+    /* The random mesh's own template (exodus_finder.c:1834-1845). */
+    if (survey && orc_template_build(&rtpl, p->random_mesh->n_cells,
+                    p->random_mesh->cell_length, rmin, r_search)) {
+      orc_template_free(&tpl);
       status = -3;
       break;
     }
@@ -2545,9 +2995,11 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
           r->status = ST_MESH;
           continue;
         }
-        const double rho = collision_radius(&V, max_acc_frozen, scale, r->cx, r->cy,
-          r->cz, r_search, 0.0f, f, box);
-        if (!weighted && rho < (double)r_search) {
+        /* No witness on a weighted mesh or a survey (1868). */
+        const double rho = (weighted || survey) ? INFINITY
+                                                : collision_radius(&V, max_acc_frozen, scale,
+                                                    r->cx, r->cy, r->cz, r_search, 0.0f, f, box);
+        if (rho < (double)r_search) {
           float rho2 = (float)(rho * rho * (1.0 + COLLISION_SLACK));
           if (rho2 < rc2)
             rho2 = rc2;
@@ -2559,8 +3011,12 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
         }
         uint8_t reason;
         uint64_t ss = 0, sc = 0;
-        r->r = grow_one(mesh, &tpl, r->cx, r->cy, r->cz, r_search, threshold,
-          vol_factor, mass_factor, rmin, window, &reason, &ss, &sc);
+        if (survey)
+          r->r = orc_find_radius_survey(mesh, &tpl, p->random_mesh, &rtpl, r->cx, r->cy, r->cz,
+            r_search, survey_K, rmin, window, &reason, &ss, &sc);
+        else
+          r->r = grow_one(mesh, &tpl, r->cx, r->cy, r->cz, r_search, threshold,
+            vol_factor, mass_factor, rmin, window, &reason, &ss, &sc);
         span_sum += ss;
         span_count += sc;
         for (uint32_t e = ext0; e < n_ext && r->r < 0.0f && reason == ORC_RESCALE_BEYOND_SEARCH;
@@ -2636,6 +3092,7 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
       }
     }
     orc_template_free(&tpl);
+    orc_template_free(&rtpl);
     if (stats_out)
       stats_out[ri] = st;
   }
@@ -2646,6 +3103,20 @@ int orc_exodus(const float* delta, const orc_mesh_t* mesh, const float* radii_in
    * oracle never changes the caller's contrast. */
   if (spec && status == 0)
     orc_spectrum_smooth(spec, 0, 0.0f, 0.0f, field, NULL);
+  if (rspec && status == 0)
+    orc_spectrum_smooth(rspec, 0, 0.0f, 0.0f, field, NULL);
+  /* The footprint of every void, once the catalogue is final
+   * (sif__exodus_survey_footprint, exodus_survey.c:299-311). */
+  if (survey && status == 0) {
+    out->footprint = malloc((V.n ? V.n : 1) * sizeof(float));
+    out->footprint_shell = malloc((V.n ? V.n : 1) * sizeof(float));
+    for (uint64_t v = 0; v < V.n; v++)
+      survey_void_footprint(occ, N, box, V.cx[v], V.cy[v], V.cz[v], V.r[v], &out->footprint[v],
+        &out->footprint_shell[v]);
+  }
+  free(occ);
+  free(rfield);
+  orc_spectrum_free(rspec);
   for (uint32_t k = 0; k < n_ext; k++)
     orc_template_free(&etpl[k]);
   free(bidx);
@@ -2677,5 +3148,7 @@ void orc_catalogue_free(orc_catalogue_t* c) {
   free(c->cy);
   free(c->cz);
   free(c->r);
+  free(c->footprint);
+  free(c->footprint_shell);
   memset(c, 0, sizeof(*c));
 }

@@ -176,6 +176,15 @@ typedef struct {
   const float* prior_cz;
   const float* prior_r;
   uint64_t n_prior;
+  /* A survey (sif_finder_exodus_survey_raw, src/finder/exodus_survey.c:
+   * 401-545): the randoms' mesh and their CIC density grid (grid_n^3), NULL
+   * for a periodic box. `delta` is then the data's CIC density, not a
+   * contrast; each rung scans the smoothed data over alpha times the smoothed
+   * randoms and grows every radius against the randoms; injected fields come
+   * two a rung, the data's top-hat, then the randoms'. Only cell seeds on
+   * their nodes; the catalogue gets its footprint columns. */
+  const orc_mesh_t* random_mesh;
+  const float* random_grid;
 } orc_exodus_params_t;
 
 typedef struct {
@@ -184,7 +193,24 @@ typedef struct {
   float* cz;
   float* r;
   uint64_t n_voids;
+  /* A survey run's observed fractions of each sphere and of the shell out to
+   * twice its radius (sif_catalogue_t::footprint, footprint_shell); NULL for
+   * a box. */
+  float* footprint;
+  float* footprint_shell;
 } orc_catalogue_t;
+
+/* The observed nodes of a survey's grid (sif__exodus_survey_occupancy,
+ * src/finder/exodus_survey.c:159-201) into occ, (n^3 + 63) / 64 words; the
+ * closing's k into *k_out. Returns the observed node count. */
+uint64_t orc_survey_occupancy(const orc_mesh_t* random_mesh, uint32_t n, float box,
+  uint64_t* occ, int32_t* k_out);
+
+/* sif__exodus_find_radius_survey (src/finder/exodus_rescale.c:2154-2317). */
+float orc_find_radius_survey(const orc_mesh_t* data_mesh, const orc_template_t* data_tpl,
+  const orc_mesh_t* random_mesh, const orc_template_t* random_tpl, float cx, float cy,
+  float cz, float r_search, float K, float rmin, uint32_t window, uint8_t* reason,
+  uint64_t* span_sum, uint64_t* span_count);
 
 /* sif_finder_exodus_raw on a periodic box (src/finder/exodus_finder.c:1272,
  * 1585-2492), for SIF_FINDER_SEEDS_CELLS on their nodes. `delta` is the

@@ -53,13 +53,15 @@ class Params(C.Structure):
                 ("options", C.c_uint32), ("n_threads", C.c_int), ("window", C.c_int),
                 ("smoothing_mode", C.c_int), ("inject", C.c_void_p),
                 ("prior_cx", C.c_void_p), ("prior_cy", C.c_void_p), ("prior_cz", C.c_void_p),
-                ("prior_r", C.c_void_p), ("n_prior", C.c_uint64)]
+                ("prior_r", C.c_void_p), ("n_prior", C.c_uint64),
+                ("random_mesh", C.c_void_p), ("random_grid", C.c_void_p)]
 
 
 class Catalogue(C.Structure):
     _fields_ = [("cx", C.POINTER(C.c_float)), ("cy", C.POINTER(C.c_float)),
                 ("cz", C.POINTER(C.c_float)), ("r", C.POINTER(C.c_float)),
-                ("n_voids", C.c_uint64)]
+                ("n_voids", C.c_uint64), ("footprint", C.POINTER(C.c_float)),
+                ("footprint_shell", C.POINTER(C.c_float))]
 
 
 def lib(fast=False):
@@ -112,6 +114,8 @@ def _declare(L):
     L.orc_exodus.argtypes = [vp, C.POINTER(Mesh), vp, u32, C.POINTER(Params),
                              C.POINTER(Catalogue), vp]
     L.orc_catalogue_free.argtypes = [C.POINTER(Catalogue)]
+    L.orc_survey_occupancy.argtypes = [C.POINTER(Mesh), u32, f32, vp, C.POINTER(C.c_int32)]
+    L.orc_survey_occupancy.restype = u64
     return L
 
 
@@ -277,24 +281,36 @@ def brute_force_radius(x, y, z, box, c, rung, r_search, threshold):
 
 
 def exodus(delta, mesh, radii, n_grid, box, threshold, overlap=0.0, options=0, n_threads=1,
-           window=0, smoothing_mode=1, inject=None, with_stats=False, prior=None):
+           window=0, smoothing_mode=1, inject=None, with_stats=False, prior=None,
+           survey=None):
     """The oracle finder; returns (cx, cy, cz, r) float32 arrays. prior:
-    (cx, cy, cz, r), voids to start from."""
+    (cx, cy, cz, r), voids to start from. survey: (random_mesh,
+    random_density) for a survey run -- delta is then the data's CIC density,
+    injected fields come two a rung (data, randoms), and the footprint columns
+    follow the four (cx, cy, cz, r, footprint, footprint_shell)."""
     d = np.ascontiguousarray(delta, dtype=np.float32)
     radii = np.ascontiguousarray(radii, dtype=np.float32)
     inj = None
     if inject is not None:
         # As the run's transforms return them; under the Gaussian refinement
-        # up to two a rung (padded, so a short list is never read past).
+        # up to two a rung (padded, so a short list is never read past), in a
+        # survey two a rung.
         inj = np.ascontiguousarray(inject, dtype=np.float32).reshape(-1, n_grid ** 3)
         assert inj.shape[0] >= len(radii)
-        want = 2 * len(radii) if options & (3 << 19) else len(radii)
+        want = 2 * len(radii) if (options & (3 << 19) or survey is not None) else len(radii)
         if inj.shape[0] < want:
+            assert survey is None, "a survey takes both fields of every rung"
             inj = np.concatenate([inj, np.zeros((want - inj.shape[0], n_grid ** 3), np.float32)])
     pri = [np.ascontiguousarray(c, dtype=np.float32) for c in prior] if prior is not None else None
+    rmesh = rgrid = None
+    if survey is not None:
+        rmesh = survey[0]
+        rgrid = np.ascontiguousarray(survey[1], dtype=np.float32)
     p = Params(n_grid, box, threshold, overlap, options, n_threads, window, smoothing_mode,
                _p(inj) if inj is not None else None,
-               *([_p(c) for c in pri] if pri else [None] * 4), len(pri[0]) if pri else 0)
+               *([_p(c) for c in pri] if pri else [None] * 4), len(pri[0]) if pri else 0,
+               C.cast(C.pointer(rmesh.struct), C.c_void_p) if rmesh is not None else None,
+               _p(rgrid) if rgrid is not None else None)
     cat = Catalogue()
     stats = (RungStats * len(radii))()
     st = lib().orc_exodus(_p(d), C.byref(mesh.struct), _p(radii), len(radii), C.byref(p),
@@ -302,8 +318,9 @@ def exodus(delta, mesh, radii, n_grid, box, threshold, overlap=0.0, options=0, n
     if st != 0:
         raise ValueError(f"orc_exodus: {st}")
     n = cat.n_voids
+    cols = ("cx", "cy", "cz", "r") + (("footprint", "footprint_shell") if survey is not None else ())
     out = tuple(np.ctypeslib.as_array(getattr(cat, k), shape=(n,)).copy() if n else
-                np.zeros(0, np.float32) for k in ("cx", "cy", "cz", "r"))
+                np.zeros(0, np.float32) for k in cols)
     lib().orc_catalogue_free(C.byref(cat))
     if with_stats:
         return out, [{k: getattr(s, k) for k, _ in RungStats._fields_} for s in stats]
@@ -340,7 +357,8 @@ def pipeline(x, y, z, n_grid, box, mesh_cells, radii, threshold, n_threads, fast
     mesh = Mesh(_p(mx), _p(my), _p(mz), _p(offs), n, mesh_cells, float(np.float32(box)),
                 float(np.float32(np.float32(box) / np.float32(mesh_cells))))
     r = np.ascontiguousarray(radii, dtype=np.float32)
-    p = Params(n_grid, box, threshold, 0.0, 0, n_threads, 0, 1, None, None, None, None, None, 0)
+    p = Params(n_grid, box, threshold, 0.0, 0, n_threads, 0, 1, None, None, None, None, None, 0,
+               None, None)
     cat = Catalogue()
     t0 = time.perf_counter()
     st = L.orc_exodus(_p(grid), C.byref(mesh), _p(r), len(r), C.byref(p), C.byref(cat), None)
@@ -390,3 +408,13 @@ class Spectrum:
         if self.ptr:
             lib().orc_spectrum_free(self.ptr)
             self.ptr = None
+
+
+def survey_occupancy(random_mesh, n_grid, box):
+    """The observed nodes of a survey's grid, as a bool array (n^3,), and the
+    closing's k."""
+    words = np.zeros((n_grid ** 3 + 63) // 64, np.uint64)
+    k = C.c_int32(0)
+    lib().orc_survey_occupancy(C.byref(random_mesh.struct), n_grid, box, _p(words), C.byref(k))
+    bits = np.unpackbits(words.view(np.uint8), bitorder="little")[: n_grid ** 3]
+    return bits.astype(bool), k.value

@@ -256,3 +256,70 @@ def pipeline(x, y, z, n_grid, box, mesh_cells, radii, threshold, overlap=0.0, op
         g.free()
         f.free()
     return (cat, grid_vals) if want_grid else cat
+
+
+def _bind_survey(lib, variant):
+    if getattr(lib, "_survey_bound", False):
+        return
+    field_t, grid_t, mesh_t, cat_t, extras_t = (
+        abi.STRUCTS_F64 if variant == "f64" else
+        (abi.sif_field_t, abi.sif_grid_t, abi.sif_chain_mesh_t, abi.sif_catalogue_t,
+         abi.sif_finder_exodus_extras_t))
+    real = real_of(variant)
+    lib.sif_finder_exodus_survey_raw.argtypes = [
+        C.POINTER(grid_t), C.POINTER(grid_t), C.POINTER(mesh_t), C.POINTER(mesh_t), C.c_void_p,
+        C.c_void_p, C.c_uint32, real, real, C.c_uint32, C.POINTER(extras_t)]
+    lib.sif_finder_exodus_survey_raw.restype = C.POINTER(cat_t)
+    lib.sif_finder_exodus_survey_box.argtypes = [
+        C.POINTER(field_t), C.POINTER(field_t), C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+        C.POINTER(real)]
+    lib.sif_finder_exodus_survey_box.restype = C.c_int
+    lib._survey_bound = True
+
+
+def survey_box(lib, data, randoms, radii, opt=0, variant="strict"):
+    """sif_finder_exodus_survey_box: (offset (3,), box length)."""
+    _bind_survey(lib, variant)
+    t = np_real(variant)
+    r = np.ascontiguousarray(radii, dtype=t)
+    off = np.zeros(3, t)
+    L = real_of(variant)(0)
+    st = lib.sif_finder_exodus_survey_box(data.ptr, randoms.ptr, _ptr(r), len(r), opt, _ptr(off),
+                                          C.byref(L))
+    _check(lib, st == 0, "sif_finder_exodus_survey_box")
+    return off, float(L.value)
+
+
+def exodus_survey_raw(lib, dgrid, rgrid, dmesh, rmesh, radii, threshold, overlap=0.0, opt=0,
+                      offset=None, variant="strict", capture=None, calls=None):
+    """Runs sif_finder_exodus_survey_raw on CIC density grids (as
+    sif_grid_assign_cic leaves them) and the two meshes; returns (cx, cy, cz,
+    r, footprint, footprint_shell). capture: (2 n_radii + 2, cells) receives
+    the fields the run's backward transforms return, in order (per rung the
+    data's top-hat, then the randoms'; the two restores last)."""
+    _bind_survey(lib, variant)
+    t = np_real(variant)
+    radii = np.ascontiguousarray(radii, dtype=t)
+    cells = dgrid.ptr.contents.total_cells
+    off = None if offset is None else np.ascontiguousarray(offset, dtype=t)
+    if capture is not None:
+        assert capture.dtype == t and capture.flags.c_contiguous
+        lib.orc_hook_capture(_ptr(capture), cells, capture.shape[0])
+    try:
+        cat = lib.sif_finder_exodus_survey_raw(
+            dgrid.ptr, rgrid.ptr, dmesh.ptr, rmesh.ptr, _ptr(off) if off is not None else None,
+            _ptr(radii), len(radii), threshold, overlap, opt | abi.SIF_FINDER_NO_CHECKPOINT, None)
+    finally:
+        if calls is not None:
+            calls.append(lib.orc_hook_calls())
+        lib.orc_hook_capture(None, 0, 0)
+    _check(lib, bool(cat), "sif_finder_exodus_survey_raw")
+    c = cat.contents
+    n = c.n_voids
+    ct = C.c_double if variant == "f64" else C.c_float
+    cols = []
+    for p in (c.cx, c.cy, c.cz, c.radii, c.footprint, c.footprint_shell):
+        cols.append(np.ctypeslib.as_array(C.cast(p, C.POINTER(ct)), shape=(n,)).copy() if n and p
+                    else np.zeros(0, t))
+    lib.sif_catalogue_free(cat)
+    return tuple(cols)

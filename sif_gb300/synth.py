@@ -135,3 +135,50 @@ def batch_boxes(n_boxes=64, seed=2000, n_lo=64, n_hi=256):
         box = float(rng.uniform(200.0, 1000.0))
         out.append(dict(n=n, box=box, rms_disp=4.0, seed=2000 + b))
     return out
+
+
+# A synthetic survey: a spherical footprint inside a padded box, less a
+# stripe through it; data and randoms over it under a selection that falls
+# along z; holes carved into the data (three inside, one cut by the edge).
+SURVEY = dict(box=400.0, centre=(200.0, 200.0, 200.0), radius=140.0,
+              stripe=((200.0, 260.0), 12.0),
+              holes=((160.0, 160.0, 160.0, 26.0), (240.0, 160.0, 240.0, 22.0),
+                     (150.0, 240.0, 220.0, 20.0), (200.0, 200.0, 325.0, 25.0)),
+              kept_in_hole=0.03)
+
+
+def _in_survey(p, s):
+    c = np.asarray(s["centre"])
+    inside = ((p - c) ** 2).sum(axis=1) <= s["radius"] ** 2
+    (sx, sy), half = s["stripe"]
+    stripe = (np.abs(p[:, 0] - sx) < half) & (np.abs(p[:, 1] - sy) < half)
+    return inside & ~stripe
+
+
+def survey(n_data, n_randoms, seed, selection=False, spec=SURVEY):
+    """(data, randoms): each (x, y, z) float32 arrays inside the footprint,
+    drawn uniformly (times a selection falling linearly from 1 at the bottom
+    of the footprint to 0.4 at its top, when asked); the data thinned to
+    ``kept_in_hole`` inside each hole."""
+    rng = np.random.default_rng(seed)
+    c = np.asarray(spec["centre"])
+    R = spec["radius"]
+
+    def draw(n, carve):
+        out = np.empty((0, 3))
+        while len(out) < n:
+            p = c + (2.0 * rng.random((2 * n, 3)) - 1.0) * R
+            p = p[_in_survey(p, spec)]
+            if selection:
+                keep = 1.0 - 0.6 * (p[:, 2] - (c[2] - R)) / (2.0 * R)
+                p = p[rng.random(len(p)) <= keep]
+            if carve:
+                holes = np.zeros(len(p), bool)
+                for hx, hy, hz, hr in spec["holes"]:
+                    holes |= ((p - (hx, hy, hz)) ** 2).sum(axis=1) < hr * hr
+                p = p[~holes | (rng.random(len(p)) <= spec["kept_in_hole"])]
+            out = np.concatenate([out, p])
+        out = out[:n].astype(np.float32)
+        return out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy()
+
+    return draw(n_data, True), draw(n_randoms, False)

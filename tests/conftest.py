@@ -80,6 +80,11 @@ def golden_box32_weighted_f64():
 
 
 @pytest.fixture(scope="session")
+def golden_survey():
+    return np.load(os.path.join(GOLDEN, "golden_survey.npz"))
+
+
+@pytest.fixture(scope="session")
 def golden_box32_refine():
     """SIF_FINDER_REFINE_GAUSSIAN through the reference: the rungs' top-hat
     and refinement fields, and per option set the rungs refined and the

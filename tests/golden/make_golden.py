@@ -62,6 +62,19 @@ golden_box32_refine.npz, golden_box32_refine_f64.npz -- SIF_FINDER_REFINE_GAUSSI
   reference's own runs returned, and for each option set the refinement
   takes (three in the f64 file) which rungs ran the refinement's transform
   (those with candidates) and its catalogue on those fields.
+golden_survey.npz -- the survey finder (sif_finder_exodus_survey_raw) on
+  synth.survey's footprint (a ball of radius 140 inside a box of 400, less a
+  stripe, four holes carved into the data, one cut by the edge): 60,000 data
+  and 600,000 randoms (180,000 in "sparse", whose footprint needs its chance
+  holes closed), under a selection falling along z ("flat": none), grid 64^3,
+  meshes of 20^3. Cases by threshold and ladder: [30, 24, 19, 15] at -0.8;
+  ladder(10, 30, 0.1) at -0.5 (also weighted -- data weights uniform in
+  [0.5, 1.5), a fifth 0, randoms 2 each -- and with the Lagrangian overlap);
+  ladder(8, 24, 0.1) at -0.3; and "offset", the survey moved to its own frame
+  and placed by sif_finder_exodus_survey_box (grid 64^3 over the box it
+  gives). Per case the reference's catalogue with its footprint columns,
+  from its whole path (float CIC of both sets, the shim's transforms); the
+  positions are not stored, only the SHA-256 of their float32 bytes.
 """
 import os
 import sys
@@ -76,6 +89,10 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 from sif_gb300 import abi, synth  # noqa: E402
 
 import ref_ctypes as R  # noqa: E402
+
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+from survey_cases import (SURVEY_CASES, SURVEY_GRID, SURVEY_MESH, survey_inputs,  # noqa: E402
+                          survey_sha256)
 
 # Option sets the catalogue is recorded for: (name, overlap_fraction, options).
 OPTION_SETS = [
@@ -491,7 +508,45 @@ def make_workload_a(path):
     print(f"{path}: {len(cat[0])} voids over {len(radii)} rungs")
 
 
+def make_survey(path):
+    lib = R.load()
+    out = {}
+    for case in SURVEY_CASES:
+        name, sel, n_r, thr, lad, weighted, opt, moved = case
+        data, rand, wd, wr, radii = survey_inputs(case)
+        fd = R.RefField(lib, *data, weights=wd)
+        fr = R.RefField(lib, *rand, weights=wr)
+        offset = None
+        box = synth.SURVEY["box"]
+        if moved:
+            offset, box = R.survey_box(lib, fd, fr, radii, opt)
+            fd.free()
+            fr.free()
+            data = tuple(np.float32(a + o) for a, o in zip(data, offset))
+            rand = tuple(np.float32(a + o) for a, o in zip(rand, offset))
+            fd = R.RefField(lib, *data, weights=wd)
+            fr = R.RefField(lib, *rand, weights=wr)
+        gd, gr = R.RefGrid(lib, SURVEY_GRID, box), R.RefGrid(lib, SURVEY_GRID, box)
+        gd.assign_cic(fd)
+        gr.assign_cic(fr)
+        md = R.RefMesh(lib, SURVEY_MESH, box, fd, abi.SIF_MESH_DROP_INDICES)
+        mr = R.RefMesh(lib, SURVEY_MESH, box, fr, abi.SIF_MESH_DROP_INDICES)
+        cat = R.exodus_survey_raw(lib, gd, gr, md, mr, radii, thr, 0.0, opt, offset=offset)
+        for k, c in zip(("cx", "cy", "cz", "r", "foot", "shell"), cat):
+            out[f"{name}_{k}"] = c
+        out[f"{name}_sha256"] = np.array(survey_sha256(*survey_inputs(case)[:4]))
+        out[f"{name}_box"] = np.array([box] + (list(offset) if moved else [0.0, 0.0, 0.0]),
+                                      np.float32)
+        print(f"{path}: {name}: {len(cat[0])} voids over {len(radii)} rungs")
+        for o in (md, mr, gd, gr, fd, fr):
+            o.free()
+    np.savez_compressed(path, **out)
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 1 and sys.argv[1] == "survey":
+        make_survey(os.path.join(HERE, "golden_survey.npz"))
+        sys.exit(0)
     if len(sys.argv) > 1 and sys.argv[1] == "workload_a":
         make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))
         sys.exit(0)
@@ -518,3 +573,4 @@ if __name__ == "__main__":
     make_box32_refine(os.path.join(HERE, "golden_box32_refine.npz"))
     make_box32_refine(os.path.join(HERE, "golden_box32_refine_f64.npz"), "f64")
     make_workload_a(os.path.join(HERE, "golden_workload_a.npz"))
+    make_survey(os.path.join(HERE, "golden_survey.npz"))

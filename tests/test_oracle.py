@@ -417,3 +417,63 @@ def test_oracle_refinement_matches_golden(oracle, golden_box32_refine, name):
     want = tuple(g[f"cat_{name}_{k}"] for k in ("cx", "cy", "cz", "r"))
     assert len(cat[0]) == len(want[0])
     assert same_catalogue(cat, want)
+
+
+@pytest.mark.parametrize("case", [c[0] for c in __import__("survey_cases").SURVEY_CASES])
+def test_oracle_survey_matches_golden(oracle, golden_survey, case):
+    """The survey restatement (exodus_survey.c; exodus_rescale.c:1944-2317)
+    through the whole path as the reference's caller runs it -- the float
+    CIC of data and randoms, their meshes, the run with its own smoothing of
+    both -- against the reference's catalogue and footprint columns, bit for
+    bit: selection, sparse randoms, weights, the Lagrangian overlap, many
+    voids, and a survey moved into the box sif_finder_exodus_survey_box
+    gives (the voids translated back by the oracle's caller here, as the
+    survey entry point does)."""
+    import survey_cases as S
+
+    spec = next(c for c in S.SURVEY_CASES if c[0] == case)
+    g = golden_survey
+    data, rand, wd, wr, radii = S.survey_inputs(spec)
+    assert S.survey_sha256(data, rand, wd, wr) == str(g[f"{case}_sha256"])
+    box = float(g[f"{case}_box"][0])
+    offset = g[f"{case}_box"][1:]
+    if spec[7]:
+        data = tuple(np.float32(a + o) for a, o in zip(data, offset))
+        rand = tuple(np.float32(a + o) for a, o in zip(rand, offset))
+    n = S.SURVEY_GRID
+    dm = oracle.OracleMesh(*data, S.SURVEY_MESH, box, weights=wd)
+    rm = oracle.OracleMesh(*rand, S.SURVEY_MESH, box, weights=wr)
+    dd = oracle.cic_float(*data, n, box, weights=wd)
+    rd = oracle.cic_float(*rand, n, box, weights=wr)
+    got = oracle.exodus(dd, dm, radii, n, box, spec[3], 0.0, spec[6], n_threads=4,
+                        survey=(rm, rd))
+    got = list(got)
+    if spec[7]:
+        for k in range(3):
+            got[k] = np.float32(got[k] - np.float32(offset[k]))
+    want = [g[f"{case}_{k}"] for k in ("cx", "cy", "cz", "r", "foot", "shell")]
+    assert len(got[0]) == len(want[0]) > 0
+    assert all(same_bits(a, b) for a, b in zip(got, want))
+
+
+def test_oracle_survey_occupancy_closes_chance_holes(oracle):
+    """sif__exodus_survey_occupancy's closing: with randoms three times the
+    data a 64^3 grid's footprint has nodes no random reached; closed, every
+    node well inside the ball is observed, and nothing outside the ball
+    (past the closing's reach) is."""
+    import survey_cases as S
+
+    _, rand = synth.survey(S.SURVEY_DATA, 180000, S.SURVEY_SEED)
+    box, n = synth.SURVEY["box"], S.SURVEY_GRID
+    rm = oracle.OracleMesh(*rand, S.SURVEY_MESH, box)
+    occ, k = oracle.survey_occupancy(rm, n, box)
+    assert k > 1
+    cell = box / n
+    idx = np.arange(n ** 3)
+    pos = np.stack([idx // (n * n), (idx // n) % n, idx % n], axis=1) * cell
+    r = np.sqrt(((pos - np.asarray(synth.SURVEY["centre"])) ** 2).sum(axis=1))
+    (sx, sy), half = synth.SURVEY["stripe"]
+    stripe = (np.abs(pos[:, 0] - sx) < half + 2 * k * cell) & (np.abs(pos[:, 1] - sy) < half + 2 * k * cell)
+    deep = (r < synth.SURVEY["radius"] - 2 * k * cell) & ~stripe
+    assert occ[deep].all()
+    assert not occ[r > synth.SURVEY["radius"] + 2 * k * cell].any()
