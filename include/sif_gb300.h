@@ -291,6 +291,44 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
                                        sif_real threshold, sif_real overlap_fraction,
                                        sif_option opt, const sif_finder_exodus_extras_t* extras);
 
+/* include/sif/finder/exodus_finder.h:296-310, 312-413: the finder on a
+ * survey -- any geometry, described by a random catalogue -- inside a box
+ * padded so that nothing wraps (every tracer at least max(r_search,
+ * (r_search + mesh cell) / 2) + a grid cell from every face; r_search the
+ * largest rung's reach), sif_finder_exodus_survey_box sizing it. The grids
+ * hold the CIC densities of data and randoms (sif_grid_assign_cic, not
+ * converted to a contrast), on the same n_cells and box; each mesh may
+ * carry weights. Each rung scans the smoothed data over alpha times the
+ * smoothed randoms on the observed nodes (those the randoms reach, their
+ * chance holes closed; alpha the data's total weight over the randoms') and
+ * grows each radius against the randoms. `offset` is what the survey was
+ * moved into the box by (NULL: not moved); the voids come back less it, with
+ * the footprint columns (the observed fraction of each sphere and of its
+ * shell to twice the radius). Cell seeds on their nodes only: the
+ * excursion-peak preset and SIF_FINDER_SEEDS_MINIMA, REFINE_*, EXTEND_REACH
+ * and DISPLACE fail with SIF_ERR_INVALID. */
+sif_catalogue_t* sif_finder_exodus_survey(sif_grid_t* data_grid, sif_grid_t* random_grid,
+                                          const sif_chain_mesh_t* data_mesh,
+                                          const sif_chain_mesh_t* random_mesh,
+                                          const sif_real offset[3], const sif_real* radii,
+                                          uint32_t n_radii, sif_real threshold,
+                                          sif_exodus_variant_t variant,
+                                          const sif_finder_exodus_extras_t* extras);
+sif_catalogue_t* sif_finder_exodus_survey_raw(sif_grid_t* data_grid, sif_grid_t* random_grid,
+                                              const sif_chain_mesh_t* data_mesh,
+                                              const sif_chain_mesh_t* random_mesh,
+                                              const sif_real offset[3], const sif_real* radii,
+                                              uint32_t n_radii, sif_real threshold,
+                                              sif_real overlap_fraction, sif_option options,
+                                              const sif_finder_exodus_extras_t* extras);
+/* include/sif/finder/exodus_finder.h:551-606: the box a survey is searched
+ * in (its data and randoms' extent, plus the margin above at the largest grid
+ * cell the smallest radius allows, 1% over) and the offset that centres the
+ * survey in it. */
+int sif_finder_exodus_survey_box(const sif_field_t* data, const sif_field_t* randoms,
+                                 const sif_real* radii, uint32_t n_radii, sif_option opt,
+                                 sif_real offset[3], sif_real* box_length);
+
 /* include/sif/finder/exodus_finder.h:721-723 */
 uint32_t sif_finder_grid_cells_from_size(uint64_t n_particles, sif_real box_length,
                                          sif_real cell_size, sif_finder_units_t units,
@@ -480,6 +518,37 @@ int sifg_exodus_weighted_device_f64(const double* delta, uint32_t n_grid, double
                                     const double* prior, uint64_t n_prior, double* cx,
                                     double* cy, double* cz, double* r, uint64_t capacity,
                                     uint64_t* n_voids);
+/* A chain mesh on the device, for the survey entry point: positions in mesh
+ * order, n_cells^3 + 1 offsets, and optionally its weight columns (w in mesh
+ * order and cell_w per cell, both or neither) with their total; total_weight
+ * is the tracer count for a mesh without weights. */
+typedef struct {
+  const float* x;
+  const float* y;
+  const float* z;
+  const uint32_t* offsets;
+  const float* w;
+  const float* cell_w;
+  double total_weight;
+  uint64_t n_particles;
+  uint32_t n_cells;
+} sifg_device_mesh_t;
+/* The survey finder on device arrays (sif_finder_exodus_survey_raw's run,
+ * src/finder/exodus_survey.c:401-545, without its margin check and offset):
+ * the data's and the randoms' CIC densities (n_grid^3 each) and meshes in the
+ * box's frame, the voids (prior ones in the same frame, prior[4 * n_prior]
+ * as cx.., cy.., cz.., r..) and their footprint columns written to the host
+ * arrays cx .. footprint_shell (capacity entries each; *n_voids is the
+ * count). inject: NULL, or 2 n_radii device fields in the order the run's
+ * transforms return them (per rung, largest first, the data's top-hat then
+ * the randoms'), replacing the smoothing. */
+int sifg_exodus_survey_device(const float* data_density, const float* random_density,
+                              uint32_t n_grid, float box, const sifg_device_mesh_t* data,
+                              const sifg_device_mesh_t* randoms, const float* radii,
+                              uint32_t n_radii, float threshold, float overlap, uint32_t opt,
+                              const float* inject, const float* prior, uint64_t n_prior,
+                              float* cx, float* cy, float* cz, float* r, float* footprint,
+                              float* footprint_shell, uint64_t capacity, uint64_t* n_voids);
 /* The adjoint of the CIC density contrast (sifg_cic_device followed by
  * sifg_contrast_device) with respect to the positions: given g = dL/d(delta)
  * on the n_grid^3 device grid, writes dL/dx, dL/dy, dL/dz of every particle

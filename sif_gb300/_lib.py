@@ -10,6 +10,14 @@ from . import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libsif_gb300.so")
 
+class DeviceMesh(C.Structure):
+    """sifg_device_mesh_t: a chain mesh's device columns."""
+    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("offsets", C.c_void_p), ("w", C.c_void_p), ("cell_w", C.c_void_p),
+                ("total_weight", C.c_double), ("n_particles", C.c_uint64),
+                ("n_cells", C.c_uint32)]
+
+
 _lib = None
 
 
@@ -44,6 +52,8 @@ EXPORTED = [
     "sif_catalogue_free", "sif_finder_exodus_preset", "sif_finder_exodus_variant_name",
     "sif_finder_exodus_variant_from_name", "sif_finder_exodus", "sif_finder_exodus_raw",
     "sif_finder_grid_cells_from_size", "sif_finder_exodus_checkpoint_read",
+    "sif_finder_exodus_survey", "sif_finder_exodus_survey_raw", "sif_finder_exodus_survey_box",
+    "sifg_exodus_survey_device",
     # device-resident additions
     "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
     "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
@@ -106,6 +116,10 @@ def load():
         "sifg_set_witness": (None, [i32]),
         "sifg_set_factor_tables": (None, [i32]),
         "sifg_set_halt_after": (None, [u32]),
+        "sifg_exodus_survey_device": (i32, [vp, vp, u32, f32, C.POINTER(DeviceMesh),
+                                            C.POINTER(DeviceMesh), vp, u32, f32, f32, u32, vp,
+                                            vp, u64, vp, vp, vp, vp, vp, vp, u64,
+                                            C.POINTER(u64)]),
         "sifg_set_host_mirrors": (None, [i32]),
         "sifg_host_mirrors": (i32, []),
         "sifg_host_modified": (None, [vp]),

@@ -246,6 +246,14 @@ def bind_sif_api(lib, real=C.c_float):
                                                          C.c_int, sif_real]),
         "sif_finder_exodus_checkpoint_read": (P_cat, [C.c_char_p,
                                                       C.POINTER(sif_finder_exodus_checkpoint_t)]),
+        "sif_finder_exodus_survey": (P_cat, [P_grid, P_grid, P_mesh, P_mesh, P_real, P_real,
+                                             C.c_uint32, sif_real, C.c_int,
+                                             C.POINTER(extras_t)]),
+        "sif_finder_exodus_survey_raw": (P_cat, [P_grid, P_grid, P_mesh, P_mesh, P_real, P_real,
+                                                 C.c_uint32, sif_real, sif_real, C.c_uint32,
+                                                 C.POINTER(extras_t)]),
+        "sif_finder_exodus_survey_box": (C.c_int, [P_field, P_field, P_real, C.c_uint32,
+                                                   C.c_uint32, P_real, P_real]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

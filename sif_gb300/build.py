@@ -15,7 +15,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsif_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 UNITS = ["scan", "cic", "mesh", "smooth", "finder", "engine", "api", "noalloc", "hostpool", "adjoint",
-         "checkpoint", "mirror"]
+         "checkpoint", "mirror", "survey"]
 
 
 def nvcc():

@@ -223,7 +223,9 @@ static void positions_in(const sif_field_t* f, cudaStream_t st, const float* d[3
   d[2] = (const float*)array_in(f->z, b, bufs().pz, st);
 }
 
-static sif_catalogue_t* make_catalogue(const HostCatalogue& c) {
+// A catalogue of c's voids; with footprint, its footprint columns too
+// (sif_catalogue_reserve_footprint, src/structures/catalogue.c), from c's.
+static sif_catalogue_t* make_catalogue(const HostCatalogue& c, bool footprint = false) {
   const uint64_t n = c.cx.size();
   sif_catalogue_t* cat = (sif_catalogue_t*)calloc(1, sizeof(sif_catalogue_t));
   if (!cat) return nullptr;
@@ -232,6 +234,20 @@ static sif_catalogue_t* make_catalogue(const HostCatalogue& c) {
   if (!cat->_block) {
     free(cat);
     return nullptr;
+  }
+  if (footprint) {
+    cat->_footprint_block = (float*)malloc(2 * cap * sizeof(float));
+    if (!cat->_footprint_block) {
+      host_block_put(cat->_block);
+      free(cat);
+      return nullptr;
+    }
+    cat->footprint = cat->_footprint_block;
+    cat->footprint_shell = cat->_footprint_block + cap;
+    if (n) {
+      memcpy(cat->footprint, c.foot.data(), n * 4);
+      memcpy(cat->footprint_shell, c.shell.data(), n * 4);
+    }
   }
   cat->cx = cat->_block;
   cat->cy = cat->_block + cap;
@@ -774,9 +790,13 @@ struct RunCheckpoint {
   uint32_t first_rung = 0;
   std::vector<float> host[4];   // a rung's catalogue, copied back to write
 
+  // random_mesh and offset: a survey's randoms and what it was moved into
+  // the box by (NULL for none), for the header; the prior voids are moved by
+  // it (prior_in_box, exodus_finder.c:1404-1423).
   int start(const sif_grid_t* grid, const sif_chain_mesh_t* mesh, const float* radii,
             uint32_t n_radii, float threshold, float f, sif_option opt,
-            const sif_finder_exodus_extras_t* extras) {
+            const sif_finder_exodus_extras_t* extras,
+            const sif_chain_mesh_t* random_mesh = nullptr, const float* offset = nullptr) {
     const sif_catalogue_t* prior = extras ? extras->prior : nullptr;
     const char* named = extras ? extras->checkpoint : nullptr;
     keep = extras && extras->keep_checkpoint;
@@ -785,6 +805,8 @@ struct RunCheckpoint {
       const float* cols[4] = {np ? prior->cx : nullptr, np ? prior->cy : nullptr,
                               np ? prior->cz : nullptr, np ? prior->radii : nullptr};
       for (int k = 0; k < 4; k++) voids[k].assign(cols[k], cols[k] + np);
+      for (int k = 0; offset && k < 3; k++)
+        for (float& v : voids[k]) v = v + offset[k];
     };
     if (opt & SIF_FINDER_NO_CHECKPOINT) {
       take_prior();
@@ -794,7 +816,7 @@ struct RunCheckpoint {
     std::sort(sorted.begin(), sorted.end(), [](float a, float b) { return a > b; });
     sif_finder_exodus_checkpoint_t& h = header;
     h = sif_finder_exodus_checkpoint_t{};
-    h.is_survey = 0;
+    h.is_survey = random_mesh != nullptr;
     h.is_weighted = mesh->weights != nullptr;
     h.options = opt & (SIF_FINDER_SEARCH_2_00 | SIF_FINDER_KEEP_CIC_WINDOW | SIF_FINDER_SEEDS_MINIMA |
                        SIF_FINDER_REFINE_HILL | SIF_FINDER_EXTEND_REACH | SIF_FINDER_DISPLACE |
@@ -812,6 +834,11 @@ struct RunCheckpoint {
     h.overlap_fraction = (double)f;
     h.n_particles = mesh->n_particles;
     h.total_weight = mesh->total_weight;
+    if (random_mesh) {
+      h.random_n_particles = random_mesh->n_particles;
+      h.random_total_weight = random_mesh->total_weight;
+      for (int k = 0; offset && k < 3; k++) h.offset[k] = (double)offset[k];
+    }
     if (prior && prior->n_voids) {
       h.n_prior = prior->n_voids;
       h.prior_crc32 = catalogue_crc(prior->cx, prior->cy, prior->cz, prior->radii, prior->n_voids);
@@ -898,7 +925,8 @@ extern "C" {
 void sifg_set_halt_after(uint32_t n_rungs) { g_halt_after = n_rungs; }
 
 // sif_finder_exodus_checkpoint_read (src/finder/exodus_checkpoint.c:451-488):
-// a box's voids as saved (no survey frame to move them back from).
+// the voids as saved; a survey's moved back to the caller's frame by the
+// offset the run recorded.
 sif_catalogue_t* sif_finder_exodus_checkpoint_read(const char* filepath,
                                                    sif_finder_exodus_checkpoint_t* header) {
   if (!filepath) {
@@ -918,6 +946,12 @@ sif_catalogue_t* sif_finder_exodus_checkpoint_read(const char* filepath,
   c.cy = std::move(cols[1]);
   c.cz = std::move(cols[2]);
   c.r = std::move(cols[3]);
+  if (h.is_survey && (h.offset[0] != 0.0 || h.offset[1] != 0.0 || h.offset[2] != 0.0)) {
+    const float back[3] = {(float)-h.offset[0], (float)-h.offset[1], (float)-h.offset[2]};
+    std::vector<float>* cc[3] = {&c.cx, &c.cy, &c.cz};
+    for (int k = 0; k < 3; k++)
+      for (float& v : *cc[k]) v = v + back[k];
+  }
   sif_catalogue_t* cat = make_catalogue(c);
   if (!cat) {
     fail(SIF_ERR_ALLOC, "catalogue: cannot allocate");
@@ -1115,6 +1149,376 @@ sif_catalogue_t* sif_finder_exodus_raw(sif_grid_t* grid, const sif_chain_mesh_t*
   if (!out) fail(SIF_ERR_ALLOC, "catalogue: cannot allocate");
   return out;
   API_GUARD_END(nullptr)
+}
+
+// sif__exodus_check_weights (exodus_finder.c:1076-1106) on a mesh's host
+// column: by the bits, a negative zero passing.
+static int host_weights_ok(const sif_chain_mesh_t* mesh, const char* which) {
+  if (!mesh->weights) return SIF_OK;
+  if (!mesh->cell_weights)
+    return fail(SIF_ERR_INVALID, fmt("%s: weights but no per-cell weight table", which));
+  uint64_t neg = 0, bad = 0;
+  const uint64_t nw = mesh->n_particles;
+#pragma omp parallel for schedule(static) reduction(+ : neg, bad)
+  for (uint64_t i = 0; i < nw; i++) {
+    uint32_t b;
+    memcpy(&b, mesh->weights + i, 4);
+    const bool nonfinite = ((b >> 23) & 0xffu) == 0xffu;
+    bad += nonfinite;
+    neg += !nonfinite && (b >> 31) && (b << 1);
+  }
+  if (neg || bad)
+    return fail(SIF_ERR_INVALID,
+                fmt("%s: weights must be finite and non-negative (%llu negative, %llu not finite, "
+                    "of %llu)",
+                    which, (unsigned long long)neg, (unsigned long long)bad,
+                    (unsigned long long)nw));
+  return SIF_OK;
+}
+
+static float search_factor_of(sif_option opt) {
+  static const float factors[4] = {1.5f, 1.25f, 1.75f, 2.0f};
+  return factors[(opt >> 12) & 3u];
+}
+
+// sif_finder_exodus_survey_raw, src/finder/exodus_survey.c:401-545: the
+// finder on a survey -- any geometry, described by its randoms -- inside a
+// box padded so that nothing wraps (see the margin below). The grids are the
+// CIC densities of data and randoms as sif_grid_assign_cic leaves them; each
+// rung scans the smoothed data over alpha times the smoothed randoms and
+// grows each radius against the randoms; the catalogue comes back in the
+// caller's frame (less `offset`), with its footprint columns.
+sif_catalogue_t* sif_finder_exodus_survey_raw(sif_grid_t* data_grid, sif_grid_t* random_grid,
+                                              const sif_chain_mesh_t* data_mesh,
+                                              const sif_chain_mesh_t* random_mesh,
+                                              const sif_real offset[3], const sif_real* radii,
+                                              uint32_t n_radii, sif_real threshold,
+                                              sif_real f, sif_option opt,
+                                              const sif_finder_exodus_extras_t* extras) {
+  const char* missing = !data_grid                              ? "data grid: NULL"
+                        : !data_grid->values                    ? "data grid: no values"
+                        : !random_grid                          ? "random grid: NULL"
+                        : !random_grid->values                  ? "random grid: no values"
+                        : !data_mesh                            ? "data mesh: NULL"
+                        : !random_mesh                          ? "random mesh: NULL"
+                        : !data_mesh->x || !data_mesh->n_particles ? "data mesh: no particles"
+                        : !random_mesh->x || !random_mesh->n_particles
+                            ? "random mesh: no particles"
+                            : nullptr;
+  if (missing) {
+    fail(SIF_ERR_INVALID, missing);
+    return nullptr;
+  }
+  if (check_args(radii, n_radii, threshold, f) != SIF_OK) return nullptr;
+  // sif__exodus_check_seeds (exodus_finder.c:1114-1137): cell seeds on their
+  // nodes only, in a survey.
+  const sif_option refine = opt & (3u << 19);
+  const char* box_only = (opt & SIF_FINDER_SEEDS_MINIMA)   ? "SIF_FINDER_SEEDS_MINIMA"
+                         : refine == (1u << 19)             ? "SIF_FINDER_REFINE_GAUSSIAN"
+                         : refine == (2u << 19)             ? "SIF_FINDER_REFINE_TRACERS"
+                         : refine                           ? "SIF_FINDER_REFINE_HILL"
+                         : (opt & SIF_FINDER_EXTEND_REACH) ? "SIF_FINDER_EXTEND_REACH"
+                         : (opt & SIF_FINDER_DISPLACE)     ? "SIF_FINDER_DISPLACE"
+                                                            : nullptr;
+  if (box_only) {
+    fail(SIF_ERR_INVALID,
+         fmt("options: %s: a survey (expected SIF_FINDER_SEEDS_CELLS on their nodes, for now)",
+             box_only));
+    return nullptr;
+  }
+  for (int k = 0; offset && k < 3; k++)
+    if (!std::isfinite(offset[k])) {
+      fail(SIF_ERR_INVALID, fmt("offset[%d]: %g, expected finite", k, (double)offset[k]));
+      return nullptr;
+    }
+  // The contrast is formed against the randoms: a grid already turned into
+  // one against the box mean is the wrong input.
+  if (data_grid->content == SIF_GRID_DENSITY_CONTRAST ||
+      random_grid->content == SIF_GRID_DENSITY_CONTRAST) {
+    fail(SIF_ERR_INVALID,
+         fmt("%s grid: holds a density contrast; a survey takes the CIC densities as assign_cic "
+             "leaves them",
+             data_grid->content == SIF_GRID_DENSITY_CONTRAST ? "data" : "random"));
+    return nullptr;
+  }
+  if (data_grid->n_cells != random_grid->n_cells || data_grid->box_length != random_grid->box_length) {
+    fail(SIF_ERR_INVALID, fmt("data grid: %u cells over %g, random grid: %u over %g (must match)",
+                              data_grid->n_cells, (double)data_grid->box_length,
+                              random_grid->n_cells, (double)random_grid->box_length));
+    return nullptr;
+  }
+  if (data_mesh->box_length != data_grid->box_length ||
+      random_mesh->box_length != data_grid->box_length) {
+    fail(SIF_ERR_INVALID, fmt("meshes: boxes of %g (data) and %g (randoms), grids: %g (must match)",
+                              (double)data_mesh->box_length, (double)random_mesh->box_length,
+                              (double)data_grid->box_length));
+    return nullptr;
+  }
+  if (host_weights_ok(data_mesh, "data mesh") != SIF_OK ||
+      host_weights_ok(random_mesh, "random mesh") != SIF_OK)
+    return nullptr;
+  if (!(data_mesh->total_weight > 0.0) || !(random_mesh->total_weight > 0.0)) {
+    fail(SIF_ERR_INVALID, fmt("%s mesh: total weight is zero",
+                              data_mesh->total_weight > 0.0 ? "random" : "data"));
+    return nullptr;
+  }
+  for (const sif_chain_mesh_t* m : {data_mesh, random_mesh})
+    if (m->n_cells == 0 || m->n_cells > kMaxMeshSide || m->n_particles >= 0xffffffffull) {
+      fail(SIF_ERR_RANGE, fmt("mesh: %u cells a side and %llu tracers (the GPU mesh holds 1 to %u "
+                              "cells a side, fewer than 2^32 tracers)",
+                              m->n_cells, (unsigned long long)m->n_particles, kMaxMeshSide));
+      return nullptr;
+    }
+  const sif_catalogue_t* prior = extras ? extras->prior : nullptr;
+  if (extras) {
+    if (extras->checkpoint && (opt & SIF_FINDER_NO_CHECKPOINT)) {
+      fail(SIF_ERR_INVALID, fmt("checkpoint: %s, with SIF_FINDER_NO_CHECKPOINT set", extras->checkpoint));
+      return nullptr;
+    }
+    // sif__exodus_check_extras (1145-1200): the prior voids placed in the
+    // box once moved by the offset.
+    if (prior && prior->n_voids) {
+      if (prior->units != SIF_COORDINATES_CARTESIAN) {
+        fail(SIF_ERR_INVALID, "prior: centres on the sky (expected Cartesian coordinates)");
+        return nullptr;
+      }
+      std::vector<float> moved[3];
+      for (int k = 0; k < 3; k++) {
+        const float* c = k == 0 ? prior->cx : (k == 1 ? prior->cy : prior->cz);
+        moved[k].assign(c, c + prior->n_voids);
+        for (float& v : moved[k]) v = v + (offset ? offset[k] : 0.0f);
+      }
+      if (check_prior(moved[0].data(), moved[1].data(), moved[2].data(), prior->radii,
+                      prior->n_voids, data_grid->box_length) != SIF_OK)
+        return nullptr;
+    }
+  }
+  RunCheckpoint ck;
+  if (ck.start(data_grid, data_mesh, radii, n_radii, threshold, f, opt, extras, random_mesh,
+               offset) != SIF_OK)
+    return nullptr;
+  std::lock_guard<std::mutex> lk(g_mu);
+  API_GUARD_BEGIN
+  Engine* e = engine();
+  if (!e) return nullptr;
+  cudaStream_t s = e->stream();
+  const size_t gb = data_grid->total_cells * sizeof(float);
+  const float* dg = (const float*)array_in(data_grid->values, gb, bufs().grid, s);
+  thread_local DevBuf rgrid_scratch;
+  const float* rg = (const float*)array_in(random_grid->values, gb, rgrid_scratch, s);
+  // The meshes, each with its 32-bit offsets on the device.
+  thread_local ApiBufs rbufs;  // the randoms' columns, beside the data's
+  auto mesh_in = [&](const sif_chain_mesh_t* mesh, ApiBufs& b) {
+    DeviceMesh m;
+    const uint64_t n = mesh->n_particles, mc = mesh->total_cells;
+    m.n_cells = mesh->n_cells;
+    m.box_length = mesh->box_length;
+    m.cell_length = mesh->cell_length;
+    m.n_particles = n;
+    bool holds = false;
+    m.offsets = (uint32_t*)mirror_acquire(mesh->cell_offsets, (mc + 1) * 8, (mc + 1) * 4, b.offs,
+                                          &holds);
+    if (!holds) {
+      uint64_t* wide = (uint64_t*)b.wide.ensure((mc + 1) * 8);
+      copy_up(wide, mesh->cell_offsets, (mc + 1) * 8, s);
+      narrow(wide, m.offsets, mc + 1, s);
+    }
+    mirror_commit(mesh->cell_offsets);
+    m.x = (float*)array_in(mesh->x, n * 4, b.mx, s);
+    m.y = (float*)array_in(mesh->y, n * 4, b.my, s);
+    m.z = (float*)array_in(mesh->z, n * 4, b.mz, s);
+    m.total_weight = mesh->total_weight;
+    if (mesh->weights) {
+      m.w = (float*)array_in(mesh->weights, n * 4, b.mw, s);
+      m.cell_w = (float*)array_in(mesh->cell_weights, mc * 4, b.mcw, s);
+    }
+    return m;
+  };
+  DeviceMesh dm = mesh_in(data_mesh, bufs());
+  DeviceMesh rm = mesh_in(random_mesh, rbufs);
+  // survey_check_margin (exodus_survey.c:350-372): every tracer at least the
+  // margin from every face, so that nothing downstream -- the transforms,
+  // the mesh walks, the overlap tests, all periodic -- sees the wrap.
+  {
+    float r_max = radii[0], r_min = radii[0];
+    for (uint32_t i = 1; i < n_radii; i++) {
+      r_max = std::max(r_max, radii[i]);
+      r_min = std::min(r_min, radii[i]);
+    }
+    const float cell = data_grid->cell_length;
+    const float r_search = r_max + std::fmax((search_factor_of(opt) - 1.0f) * r_max, 3.0f * cell);
+    const float mesh_cell = std::fmax(data_mesh->cell_length, random_mesh->cell_length);
+    const float margin = std::fmax(r_search, 0.5f * (r_search + mesh_cell)) + cell;
+    const std::string hint =
+        cell > r_min ? fmt("; survey_box allows for grid cells up to the smallest radius, %g, and "
+                           "these are %g",
+                           (double)r_min, (double)cell)
+                     : std::string(", as survey_box sizes it");
+    const struct {
+      const DeviceMesh* m;
+      const char* what;
+    } sets[2] = {{&rm, "randoms"}, {&dm, "data"}};
+    for (const auto& set : sets) {
+      float lo[3], hi[3];
+      extent(set.m->x, set.m->y, set.m->z, set.m->n_particles, lo, hi, s);
+      const float L = set.m->box_length;
+      for (int k = 0; k < 3; k++)
+        if (lo[k] < margin || hi[k] > L - margin) {
+          fail(SIF_ERR_INVALID,
+               fmt("%s: span [%g, %g] on axis %d of a box of %g, %g from its face (needs %g of "
+                   "padding on every side%s)",
+                   set.what, (double)lo[k], (double)hi[k], k, (double)L,
+                   (double)std::min(lo[k], L - hi[k]), (double)margin, hint.c_str()));
+          return nullptr;
+        }
+    }
+  }
+  RunParams p;
+  p.grid_n = data_grid->n_cells;
+  p.box = data_grid->box_length;
+  p.threshold = threshold;
+  p.overlap = f;
+  p.options = opt;
+  p.radii.assign(radii, radii + n_radii);
+  p.window = g_window;
+  p.weights_checked = true;  // above, on the host columns
+  p.random_mesh = &rm;
+  p.random_density = rg;
+  // exodus_finder.c:1649-1653: how much data weight a unit of random weight
+  // stands for.
+  p.survey_alpha = (float)(data_mesh->total_weight / random_mesh->total_weight);
+  if (!ck.voids[0].empty()) {
+    p.prior_cx = ck.voids[0].data();
+    p.prior_cy = ck.voids[1].data();
+    p.prior_cz = ck.voids[2].data();
+    p.prior_r = ck.voids[3].data();
+    p.n_prior = ck.voids[0].size();
+  }
+  p.first_rung = ck.first_rung;
+  if (ck.active)
+    p.after_rung = [&](uint32_t done, const float* cx, const float* cy, const float* cz,
+                       const float* r, uint32_t nv, uint64_t mismatched) {
+      return ck.rung(done, cx, cy, cz, r, nv, mismatched, s);
+    };
+  HostCatalogue cat;
+  RunTimings tm;
+  g_stats.clear();
+  const int st = e->exodus(dg, dm, p, cat, &g_stats, &tm);
+  record_timings(tm);
+  ck.finish(st);
+  if (st != SIF_OK) return nullptr;
+  // Back to the caller's frame (sif_catalogue_translate by -offset); the
+  // prior voids, the caller's own, as given.
+  if (offset) {
+    const float back[3] = {-offset[0], -offset[1], -offset[2]};
+    std::vector<float>* cc[3] = {&cat.cx, &cat.cy, &cat.cz};
+    for (int k = 0; k < 3; k++)
+      for (float& v : *cc[k]) v = v + back[k];
+    const uint64_t np = prior ? prior->n_voids : 0;
+    if (np && cat.cx.size() >= np) {
+      std::copy(prior->cx, prior->cx + np, cat.cx.begin());
+      std::copy(prior->cy, prior->cy + np, cat.cy.begin());
+      std::copy(prior->cz, prior->cz + np, cat.cz.begin());
+    }
+  }
+  g_d2h_bytes += 6 * sizeof(float) * (uint64_t)cat.cx.size();
+  sif_catalogue_t* out = make_catalogue(cat, true);
+  if (!out) fail(SIF_ERR_ALLOC, "catalogue: cannot allocate");
+  return out;
+  API_GUARD_END(nullptr)
+}
+
+sif_catalogue_t* sif_finder_exodus_survey(sif_grid_t* data_grid, sif_grid_t* random_grid,
+                                          const sif_chain_mesh_t* data_mesh,
+                                          const sif_chain_mesh_t* random_mesh,
+                                          const sif_real offset[3], const sif_real* radii,
+                                          uint32_t n_radii, sif_real threshold,
+                                          sif_exodus_variant_t variant,
+                                          const sif_finder_exodus_extras_t* extras) {
+  sif_real f;
+  sif_option opt;
+  if (sif_finder_exodus_preset(variant, &f, &opt) != SIF_OK) return nullptr;
+  return sif_finder_exodus_survey_raw(data_grid, random_grid, data_mesh, random_mesh, offset,
+                                      radii, n_radii, threshold, f, opt, extras);
+}
+
+// sif_finder_exodus_survey_box, src/finder/exodus_survey.c:590-703: the box
+// a survey is searched in -- its extent (data and randoms) plus, on every
+// side, the margin survey_raw checks for at the largest grid cell the
+// ladder's smallest radius allows, times 1.01 -- and the offset that centres
+// the survey in it.
+int sif_finder_exodus_survey_box(const sif_field_t* data, const sif_field_t* randoms,
+                                 const sif_real* radii, uint32_t n_radii, sif_option opt,
+                                 sif_real offset[3], sif_real* box_length) {
+  const char* names[2] = {"data", "randoms"};
+  const sif_field_t* given[2] = {data, randoms};
+  for (int i = 0; i < 2; i++) {
+    const sif_field_t* fl = given[i];
+    if (!fl || !fl->x || !fl->y || !fl->z || fl->n_particles == 0)
+      return fail(SIF_ERR_INVALID, fmt("%s: %s", names[i],
+                                       !fl ? "NULL" : (fl->n_particles == 0 ? "no particles"
+                                                                            : "no positions")));
+    if (fl->units != SIF_COORDINATES_CARTESIAN)
+      return fail(SIF_ERR_INVALID,
+                  fmt("%s: sky coordinates (expected Cartesian; convert them first)", names[i]));
+  }
+  if (!radii || n_radii == 0 || !offset || !box_length)
+    return fail(SIF_ERR_INVALID, !radii || n_radii == 0 ? "radii: none given"
+                                                        : "offset, box_length: NULL");
+  for (uint32_t i = 0; i < n_radii; i++)
+    if (!(radii[i] > 0.0f) || !std::isfinite(radii[i]))
+      return fail(SIF_ERR_INVALID, fmt("radii[%u] = %g: not a positive radius", i, (double)radii[i]));
+  // survey_field_extent (595-628): the bounding box grown by a field, a
+  // coordinate that is not finite counted and refused.
+  auto grow = [&](const sif_field_t* fl, const char* what, float lo[3], float hi[3]) {
+    float x0 = lo[0], y0 = lo[1], z0 = lo[2], x1 = hi[0], y1 = hi[1], z1 = hi[2];
+    uint64_t bad = 0;
+    const uint64_t n = fl->n_particles;
+#pragma omp parallel for schedule(static) reduction(min : x0, y0, z0) reduction(max : x1, y1, z1) \
+    reduction(+ : bad)
+    for (uint64_t p = 0; p < n; p++) {
+      const float x = fl->x[p], y = fl->y[p], z = fl->z[p];
+      bad += !(std::isfinite(x) && std::isfinite(y) && std::isfinite(z));
+      x0 = std::fmin(x0, x);
+      y0 = std::fmin(y0, y);
+      z0 = std::fmin(z0, z);
+      x1 = std::fmax(x1, x);
+      y1 = std::fmax(y1, y);
+      z1 = std::fmax(z1, z);
+    }
+    if (bad)
+      return fail(SIF_ERR_INVALID, fmt("%s: %llu of %llu with a coordinate that is not finite", what,
+                                       (unsigned long long)bad, (unsigned long long)n));
+    lo[0] = x0, lo[1] = y0, lo[2] = z0;
+    hi[0] = x1, hi[1] = y1, hi[2] = z1;
+    return SIF_OK;
+  };
+  float lo[3] = {randoms->x[0], randoms->y[0], randoms->z[0]};
+  float hi[3] = {lo[0], lo[1], lo[2]};
+  if (grow(randoms, "randoms", lo, hi) != SIF_OK) return SIF_ERR_INVALID;
+  const float r_lo[3] = {lo[0], lo[1], lo[2]}, r_hi[3] = {hi[0], hi[1], hi[2]};
+  if (grow(data, "data", lo, hi) != SIF_OK) return SIF_ERR_INVALID;
+  float beyond = 0.0f;
+  for (int k = 0; k < 3; k++) beyond = std::fmax(beyond, std::fmax(r_lo[k] - lo[k], hi[k] - r_hi[k]));
+  if (beyond > 0.0f)
+    log_msg(SIF_LOG_LEVEL_WARNING, "finder.exodus",
+            fmt("the data reach %g past the randoms' bounding box; the box is sized around both, "
+                "but tracers outside the randoms are outside the footprint",
+                (double)beyond));
+  float extent_max = 0.0f;
+  for (int k = 0; k < 3; k++) extent_max = std::fmax(extent_max, hi[k] - lo[k]);
+  float r_min = radii[0], r_max = radii[0];
+  for (uint32_t i = 1; i < n_radii; i++) {
+    r_min = std::fmin(r_min, radii[i]);
+    r_max = std::fmax(r_max, radii[i]);
+  }
+  const float fs = search_factor_of(opt);
+  const float cell = r_min;
+  const float margin = r_max + std::fmax((fs - 1.0f) * r_max, 3.0f * cell) + cell;
+  const float L = extent_max + 2.0f * 1.01f * margin;  // SURVEY_BOX_SLACK, 573
+  for (int k = 0; k < 3; k++) offset[k] = 0.5f * L - 0.5f * (lo[k] + hi[k]);
+  *box_length = L;
+  return SIF_OK;
 }
 
 // sif_finder_grid_cells_from_size, src/finder/exodus_finder.c:2494-2560.
@@ -1370,6 +1774,74 @@ static int exodus_device(const R* delta, uint32_t n_grid, R box, const R* mx, co
                             nullptr, n_prior ? prior : nullptr, n_prior);
   record_timings(tm);
   return st;
+}
+
+static int survey_device(const float* dd, const float* rd, uint32_t n_grid, float box,
+                         const sifg_device_mesh_t* data, const sifg_device_mesh_t* randoms,
+                         const float* radii, uint32_t n_radii, float threshold, float overlap,
+                         uint32_t opt, const float* inject, const float* prior, uint64_t n_prior,
+                         float* cx, float* cy, float* cz, float* r, float* foot, float* shell,
+                         uint64_t capacity, uint64_t* n_voids) {
+  Engine* e = engine();
+  if (!e) return SIF_ERR_UNINITIALISED;
+  if (!dd || !rd || !data || !randoms) return fail(SIF_ERR_INVALID, "survey: NULL argument");
+  if (check_args(radii, n_radii, threshold, overlap) != SIF_OK) return SIF_ERR_INVALID;
+  if (n_prior && !prior) return fail(SIF_ERR_INVALID, "prior: NULL with voids to start from");
+  DeviceMesh m[2];
+  const sifg_device_mesh_t* src[2] = {data, randoms};
+  for (int k = 0; k < 2; k++) {
+    const sifg_device_mesh_t* d = src[k];
+    if (d->n_cells == 0 || d->n_cells > kMaxMeshSide || d->n_particles == 0 ||
+        d->n_particles >= 0xffffffffull || !d->x || !d->y || !d->z || !d->offsets ||
+        (!d->w) != (!d->cell_w) || !(d->total_weight > 0.0))
+      return fail(SIF_ERR_INVALID, fmt("%s mesh: bad description", k ? "random" : "data"));
+    m[k].n_cells = d->n_cells;
+    m[k].box_length = box;
+    m[k].cell_length = box / (float)d->n_cells;
+    m[k].n_particles = d->n_particles;
+    m[k].x = const_cast<float*>(d->x);
+    m[k].y = const_cast<float*>(d->y);
+    m[k].z = const_cast<float*>(d->z);
+    m[k].offsets = const_cast<uint32_t*>(d->offsets);
+    m[k].w = const_cast<float*>(d->w);
+    m[k].cell_w = const_cast<float*>(d->cell_w);
+    m[k].total_weight = d->total_weight;
+  }
+  RunParams p;
+  p.grid_n = n_grid;
+  p.box = box;
+  p.threshold = threshold;
+  p.overlap = overlap;
+  p.options = opt;
+  p.radii.assign(radii, radii + n_radii);
+  p.window = g_window;
+  p.inject = inject;
+  p.inject_on_device = true;
+  p.random_mesh = &m[1];
+  p.random_density = rd;
+  p.survey_alpha = (float)(data->total_weight / randoms->total_weight);
+  if (n_prior) {
+    p.prior_cx = prior;
+    p.prior_cy = prior + n_prior;
+    p.prior_cz = prior + 2 * n_prior;
+    p.prior_r = prior + 3 * n_prior;
+    p.n_prior = n_prior;
+  }
+  thread_local HostCatalogue cat;
+  for (auto* v : {&cat.cx, &cat.cy, &cat.cz, &cat.r, &cat.foot, &cat.shell}) v->clear();
+  g_stats.clear();
+  RunTimings tm;
+  const int st = e->exodus(dd, m[0], p, cat, &g_stats, &tm);
+  record_timings(tm);
+  if (st != SIF_OK) return st;
+  const uint64_t nv = cat.cx.size();
+  if (n_voids) *n_voids = nv;
+  const uint64_t w = nv < capacity ? nv : capacity;
+  float* dst[6] = {cx, cy, cz, r, foot, shell};
+  const std::vector<float>* col[6] = {&cat.cx, &cat.cy, &cat.cz, &cat.r, &cat.foot, &cat.shell};
+  for (int k = 0; k < 6 && w; k++)
+    if (dst[k]) memcpy(dst[k], col[k]->data(), w * sizeof(float));
+  return SIF_OK;
 }
 
 // The whole box path on one engine, with the engine's own buffers: the
@@ -1734,6 +2206,17 @@ int sifg_exodus_weighted_device_f64(const double* delta, uint32_t n_grid, double
   SIFG_LOCKED(exodus_device(delta, n_grid, box, mx, my, mz, offsets, n_particles, mesh_cells,
                             radii, n_radii, threshold, overlap, opt, inject, prior, n_prior, cx,
                             cy, cz, r, capacity, n_voids, w, cell_w, total_weight))
+}
+int sifg_exodus_survey_device(const float* data_density, const float* random_density,
+                              uint32_t n_grid, float box, const sifg_device_mesh_t* data,
+                              const sifg_device_mesh_t* randoms, const float* radii,
+                              uint32_t n_radii, float threshold, float overlap, uint32_t opt,
+                              const float* inject, const float* prior, uint64_t n_prior,
+                              float* cx, float* cy, float* cz, float* r, float* footprint,
+                              float* footprint_shell, uint64_t capacity, uint64_t* n_voids) {
+  SIFG_LOCKED(survey_device(data_density, random_density, n_grid, box, data, randoms, radii,
+                            n_radii, threshold, overlap, opt, inject, prior, n_prior, cx, cy, cz,
+                            r, footprint, footprint_shell, capacity, n_voids))
 }
 int sifg_exodus_device_f64(const double* delta, uint32_t n_grid, double box, const double* mx,
                            const double* my, const double* mz, const uint32_t* offsets,

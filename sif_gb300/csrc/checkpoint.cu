@@ -231,7 +231,9 @@ int checkpoint_match(const std::string& path, const sif_finder_exodus_checkpoint
     *message = path + ": not this run: " + what;
     return SIF_ERR_INVALID;
   };
-  if (got.is_survey != want.is_survey) return mismatch("saved from a survey (this run is a box)");
+  if (got.is_survey != want.is_survey)
+    return mismatch(got.is_survey ? "saved from a survey (this run is a box)"
+                                  : "saved from a box (this run is a survey)");
   if (got.is_weighted != want.is_weighted) return mismatch("tracer weighting differs");
   if (got.n_radii != want.n_radii) {
     snprintf(b, sizeof b, "ladder of %u radii (expected %u)", got.n_radii, want.n_radii);
@@ -279,6 +281,22 @@ int checkpoint_match(const std::string& path, const sif_finder_exodus_checkpoint
              (unsigned long long)got.n_particles, got.total_weight,
              (unsigned long long)want.n_particles, want.total_weight);
     return mismatch(b);
+  }
+  if (want.is_survey) {
+    const double rw = std::fabs(got.random_total_weight - want.random_total_weight);
+    if (got.random_n_particles != want.random_n_particles ||
+        rw > 1e-9 * std::fmax(std::fabs(got.random_total_weight),
+                              std::fabs(want.random_total_weight))) {
+      snprintf(b, sizeof b, "%llu randoms of total weight %.17g (expected %llu of %.17g)",
+               (unsigned long long)got.random_n_particles, got.random_total_weight,
+               (unsigned long long)want.random_n_particles, want.random_total_weight);
+      return mismatch(b);
+    }
+    for (int k = 0; k < 3; k++)
+      if (got.offset[k] != want.offset[k]) {
+        snprintf(b, sizeof b, "offset[%d] %g (expected %g)", k, got.offset[k], want.offset[k]);
+        return mismatch(b);
+      }
   }
   if (got.n_prior != want.n_prior || got.prior_crc32 != want.prior_crc32) {
     snprintf(b, sizeof b, "started from %llu prior voids, checksum %08x (this run's: %llu, %08x)",

@@ -463,6 +463,12 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   // time in rank order (displace_commit).
   const bool displace = (opt & kOptDisplace) != 0;
   const bool extend = (opt & kOptExtendReach) != 0;
+  // A survey (exodus_finder.c:1114-1137): cell seeds on their nodes only.
+  const bool survey = p.random_mesh != nullptr;
+  if (survey && (gaussian || displace || extend || (opt & kOptSeedsMinima) || !p.random_density)) {
+    set_error(kErrInvalid, "options: a survey (expected SIF_FINDER_SEEDS_CELLS on their nodes)");
+    return kErrInvalid;
+  }
   if (cells >= (1ull << 32)) {
     set_error(kErrRange, "grid: more than 2^32 cells");
     return kErrRange;
@@ -517,6 +523,30 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   uint64_t inj_k = 0;
   uint32_t* mask = grow_to<uint32_t>(mask_, (cells + 31) / 32);
   SIFG_CUDA(cudaMemsetAsync(mask, 0, ((cells + 31) / 32) * sizeof(uint32_t), st_));
+  // A survey's footprint, before any field is scanned
+  // (sif__exodus_survey_occupancy, exodus_survey.c:159-201): the nodes the
+  // randoms are nearest to, closed over the window that expects enough of
+  // them; and the randoms' two fields.
+  R* rfields[2] = {nullptr, nullptr};
+  uint32_t* occ = nullptr;
+  bool mesh_waited = false;
+  if (survey) {
+    for (int k = 0; k < 2; k++) rfields[k] = grow_to<R>(rfield_[k], cells);
+    const uint64_t words = (cells + 31) / 32;
+    occ = grow_to<uint32_t>(occ_, words);
+    if (p.mesh_ready) {
+      SIFG_CUDA(cudaStreamWaitEvent(st_, p.mesh_ready, 0));
+      mesh_waited = true;
+    }
+    const DeviceMeshT<R>& rmesh = *p.random_mesh;
+    const uint64_t marked =
+        survey_mark(rmesh.x, rmesh.y, rmesh.z, rmesh.n_particles, N, box, occ,
+                    (unsigned long long*)grow_to<uint64_t>(occ_count_, 1), st_);
+    if (marked)
+      survey_close(occ, grow_to<uint32_t>(occ_tmp_, words), N,
+                   survey_closing_k(rmesh.n_particles, marked), st_);
+  }
+  SmootherT<R>& rsmoother = rsmoother_for<R>();
   // The smoothing stream starts after everything queued on the run's stream
   // (the density contrast among it); rung ri's field is fields[ri % 2].
   SIFG_CUDA(cudaEventRecord(ev_start_, st_));
@@ -536,6 +566,12 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     if (gaussian)
       smoother.smooth(kFilterTopHat, radii[ri], R(0.15f) * radii[ri], gfields[ri % 2],
                       tm ? &tm->filter : nullptr);
+    // A survey's rung (exodus_finder.c:1729-1737): the randoms smoothed the
+    // same way, and the field scanned is the data against them.
+    if (survey) {
+      rsmoother.smooth(kFilterTopHat, radii[ri], 0.0f, rfields[ri % 2], nullptr);
+      survey_contrast(fields[ri % 2], (const R*)rfields[ri % 2], occ, p.survey_alpha, cells, st_fft_);
+    }
     SIFG_CUDA(cudaEventRecord(ev_smoothed_[ri % 2], st_fft_));
   };
   // On every way out, nothing of the run is left in flight on the smoothing
@@ -547,8 +583,12 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   const uint32_t nb_below = (uint32_t)((cells + kBelowBlock - 1) / kBelowBlock);
   if (!p.inject) {
     smoother.setup(N, box, window_mode, st_fft_);
-    listed = g_scan_mode == 0 && sizeof(R) == 4 && !minima && !gaussian &&
+    listed = g_scan_mode == 0 && sizeof(R) == 4 && !minima && !gaussian && !survey &&
              smoother.lists_below() && cells % kBelowBlock == 0;
+    if (survey) {
+      rsmoother.setup(N, box, window_mode, st_fft_);
+      rsmoother.forward(p.random_density, nullptr);
+    }
     if (listed)
       for (int k = 0; k < 2; k++) {
         below[k].thr = (float)threshold;
@@ -660,6 +700,36 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     mv.winv = wi;
     gwbuf = grow_to<long long>(gwbuf_, (size_t)growth_grid() * kGrowCap);
   }
+  // A survey weighs on both meshes: a mesh without weights counts each
+  // tracer 1 (a unit of 1); the randoms' weights in a fixed point of their own.
+  MeshViewT<R> rmv{};
+  R survey_K = 0;
+  if (survey) {
+    if (!weighted) {
+      mv.wscale = (R)1;
+      mv.winv = 1.0;
+    }
+    const DeviceMeshT<R>& rm = *p.random_mesh;
+    rmv = MeshViewT<R>{rm.x, rm.y, rm.z, rm.offsets, (int32_t)rm.n_cells, rm.box_length,
+                       1.0f / rm.cell_length, rm.xyzw};
+    rmv.wscale = (R)1;
+    rmv.winv = 1.0;
+    if (rm.w) {
+      const R r_top = radii.front();
+      const R reach = r_top + std::fmax((search_factor - 1.0f) * r_top, 3.0f * cell);
+      const double side = 2.0 * ((double)(int64_t)(reach / rm.cell_length) + 2.0) + 1.0;
+      const double rep = std::pow(std::ceil(side / (double)rm.n_cells), 3.0);
+      double ws = 0, wi = 0;
+      weight_fixed_point(rm.total_weight * rep, &ws, &wi);
+      rmv.w = rm.w;
+      rmv.cell_w = rm.cell_w;
+      rmv.wscale = (R)ws;
+      rmv.winv = wi;
+    }
+    // exodus_finder.c:1649-1653.
+    survey_K = (1.0f + threshold) * p.survey_alpha;
+    gwbuf = grow_to<long long>(gwbuf_, (size_t)growth_grid() * kGrowCap);
+  }
 
   // The sphere growth's constants for a search shell [rmin, r_search]
   // (exodus_rescale.c:681-720, 894-908), on top of the rung's own.
@@ -744,7 +814,6 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     }
   }
 
-  bool mesh_waited = false;
   using clk = std::chrono::steady_clock;
   auto ms_since = [](clk::time_point t0) {
     return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
@@ -768,6 +837,11 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
         p.inject_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (p.inject) {
       SIFG_CUDA(cudaMemcpyAsync(field, p.inject + inj_k++ * cells, cells * sizeof(R), inj_kind, st_));
+      if (survey) {
+        R* rf = rfields[ri % 2];
+        SIFG_CUDA(cudaMemcpyAsync(rf, p.inject + inj_k++ * cells, cells * sizeof(R), inj_kind, st_));
+        survey_contrast(field, (const R*)rf, occ, p.survey_alpha, cells, st_);
+      }
     } else {
       if (ri + 1 < radii.size()) smooth_rung(ri + 1);
       SIFG_CUDA(cudaStreamWaitEvent(st_, ev_smoothed_[ri % 2], 0));
@@ -877,6 +951,19 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       return kErrRange;
     }
     const TemplateViewT<R> tv = upload_template(ht, tpl_);
+    // The randoms' mesh is free to use cells of its own, so it gets its own
+    // template (exodus_finder.c:1834-1845).
+    TemplateViewT<R> rtv{};
+    if (survey) {
+      HostTemplateT<R> rht;
+      if (build_template(rht, p.random_mesh->n_cells, p.random_mesh->cell_length, rmin, r_search) !=
+          kOk) {
+        set_error(kErrRange, "search sphere of " + std::to_string(r_search) +
+                                 " wider than the random mesh; use a finer mesh or smaller radii");
+        return kErrRange;
+      }
+      rtv = upload_template(rht, rtpl_);
+    }
     // The first level of the extended reach this rung enters: the lowest
     // EXT_SLACK past its own reach, or the top if none is
     // (exodus_finder.c:1826-1832).
@@ -918,11 +1005,14 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       // displacement every survivor is grown: a void refusing it now may be
       // displaced before its turn.
       // No witness on a weighted mesh either (1865-1868).
-      if (displace || weighted)
+      if (displace || weighted || survey)
         SIFG_CUDA(cudaMemsetAsync(sreason, kRescaleOk, m, st_));
       else
         witness(mv, tv, rc, sv, vv, m, traffic + 2 * ri, st_, tm ? &tm->witness : nullptr, work);
-      if (weighted)
+      if (survey)
+        grow_survey(mv, tv, rmv, rtv, rc, survey_K, sv, m, gbuf, gwbuf, kGrowCap, traffic + 2 * ri,
+                    st_, tm ? &tm->growth : nullptr, work);
+      else if (weighted)
         grow_weighted(mv, tv, rc, sv, m, gbuf, gwbuf, kGrowCap, traffic + 2 * ri, st_,
                       tm ? &tm->growth : nullptr, kAllSurvivors, work);
       else
@@ -1089,6 +1179,22 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   out.cy.resize(base + n_voids);
   out.cz.resize(base + n_voids);
   out.r.resize(base + n_voids);
+  // A survey's footprints, once the catalogue is final
+  // (sif__exodus_survey_footprint, exodus_survey.c:299-311).
+  if (survey) {
+    out.foot.resize(base + n_voids);
+    out.shell.resize(base + n_voids);
+    if (n_voids) {
+      R* foot = grow_to<R>(foot_, n_voids);
+      R* shell = grow_to<R>(shell_, n_voids);
+      survey_footprint(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), cat_r_.as<R>(), n_voids, occ,
+                       N, box, foot, shell, st_);
+      SIFG_CUDA(cudaMemcpyAsync(out.foot.data() + base, foot, n_voids * sizeof(R),
+                                cudaMemcpyDeviceToHost, st_));
+      SIFG_CUDA(cudaMemcpyAsync(out.shell.data() + base, shell, n_voids * sizeof(R),
+                                cudaMemcpyDeviceToHost, st_));
+    }
+  }
   if (n_voids) {
     SIFG_CUDA(cudaMemcpyAsync(out.cx.data() + base, cat_x_.ptr, n_voids * sizeof(R), cudaMemcpyDeviceToHost, st_));
     SIFG_CUDA(cudaMemcpyAsync(out.cy.data() + base, cat_y_.ptr, n_voids * sizeof(R), cudaMemcpyDeviceToHost, st_));

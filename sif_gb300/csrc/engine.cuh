@@ -60,6 +60,17 @@ struct RunParamsT {
   // run with that status.
   std::function<int(uint32_t, const R*, const R*, const R*, const R*, uint32_t, uint64_t)>
       after_rung;
+  // A survey (sif_finder_exodus_survey_raw, src/finder/exodus_survey.c:
+  // 401-545; the survey branches of exodus_finder.c): the randoms' mesh and
+  // their CIC density grid on the device, NULL for a periodic box. The run's
+  // grid is then the data's CIC density (no contrast); each rung scans the
+  // smoothed data over survey_alpha times the smoothed randoms on the
+  // observed nodes, and grows every radius against the randoms; injected
+  // fields come two a rung, the data's top-hat then the randoms'. The
+  // catalogue gets its footprint columns. Cell seeds on their nodes only.
+  const DeviceMeshT<R>* random_mesh = nullptr;
+  const R* random_density = nullptr;
+  R survey_alpha = 0;  // the data's total weight over the randoms'
 };
 using RunParams = RunParamsT<float>;
 
@@ -94,6 +105,9 @@ struct RunTimings {
 template <class R>
 struct HostCatalogueT {
   std::vector<R> cx, cy, cz, r;
+  // A survey's observed fractions of each sphere and of its shell to twice
+  // the radius (sif_catalogue_t::footprint, footprint_shell); empty for a box.
+  std::vector<R> foot, shell;
 };
 using HostCatalogue = HostCatalogueT<float>;
 
@@ -125,8 +139,13 @@ class Engine {
   BoxBufs io;      // the box path's buffers
   Smoother smoother;        // the float form's
   SmootherT<double> smoother64;  // the FP64 form's
+  // A survey's randoms, smoothed beside the data (their own spectrum).
+  Smoother rsmoother;
+  SmootherT<double> rsmoother64;
   template <class R>
   SmootherT<R>& smoother_for();
+  template <class R>
+  SmootherT<R>& rsmoother_for();
   int host_threads = 0;
 
  private:
@@ -145,6 +164,10 @@ class Engine {
   // offset lengths.
   DevBuf gfield_[2], cand_delta2_, cand_flat2_, cand_off_, cand_off2_, keep_, soff_;
   DevBuf tpl_, gbuf_, traffic_, region_delta_, region_flat_;
+  // A survey: the randoms' smoothed fields, the footprint (and the closing's
+  // other mask, the marked count), the randoms' template, the voids' observed
+  // fractions.
+  DevBuf rfield_[2], occ_, occ_tmp_, occ_count_, rtpl_, foot_, shell_;
   static constexpr uint32_t kExtMaxLevels = 32;  // EXT_MAX_LEVELS, exodus_finder.c:244
   DevBuf ext_tpl_[kExtMaxLevels];  // the extended reach's templates, one per level
   DevBuf below_counts_[2], below_delta_[2], below_flat_[2];  // the smoothing's below-threshold lists
@@ -190,5 +213,9 @@ template <>
 inline SmootherT<float>& Engine::smoother_for<float>() { return smoother; }
 template <>
 inline SmootherT<double>& Engine::smoother_for<double>() { return smoother64; }
+template <>
+inline SmootherT<float>& Engine::rsmoother_for<float>() { return rsmoother; }
+template <>
+inline SmootherT<double>& Engine::rsmoother_for<double>() { return rsmoother64; }
 
 }  // namespace sifg

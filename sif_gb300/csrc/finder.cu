@@ -2119,6 +2119,353 @@ void grow_weighted(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, S
   if (timer) timer->end(st);
 }
 
+// ---------------------------------------------------------------------------
+// Survey sphere growth (sif__exodus_find_radius_survey, exodus_rescale.c:
+// 2154-2317; survey_sphere_total 1957-1993, survey_histogram 2000-2056,
+// survey_resolve 2058-2146).
+//
+// The largest data distance d at which the data weight inside d is at most K
+// times the random weight inside it, K = (1 + threshold) alpha: the data and
+// the randoms each on its own mesh and template, both in the fixed point of
+// the weighted growth (a mesh without weights counts each tracer 1). One CTA
+// per survivor: the two sphere totals (the cheap refusal), the bin count from
+// the data's tracers, the two histograms, then the walk down the bins with
+// the skip test, resolving a window of bins at a time: its data tracers
+// sorted by distance with their weights, each tested against the data weight
+// it encloses (the window's top less the suffix sum of the weights from it
+// up) and the random weight interpolated at its distance inside its bin, in
+// the reference's double expression. Every sum is exact, so the bins below
+// each edge stand for the reference's running r_below and d_current wherever
+// its double sums are exact.
+// ---------------------------------------------------------------------------
+template <class R>
+constexpr size_t survey_smem_bytes() {
+  return (4 * (size_t)kMaxBins + kWBuf) * sizeof(long long) + 2 * (size_t)kMaxBins * sizeof(uint32_t) +
+         kWBuf * sizeof(R);
+}
+
+// A tracer's or a whole cell's weight in the mesh's fixed point: its own
+// weight, or 1 a tracer where the mesh has none.
+template <class R>
+__device__ __forceinline__ long long tracer_w(const MeshViewT<R>& m, uint32_t p) {
+  return m.w ? wfix(__ldg(m.w + p), m.wscale) : 1ll;
+}
+template <class R>
+__device__ __forceinline__ long long cell_wt(const MeshViewT<R>& m, uint32_t flat, uint32_t cnt) {
+  return m.cell_w ? wfix(__ldg(m.cell_w + flat), m.wscale) : (long long)cnt;
+}
+
+template <class R>
+__global__ void __launch_bounds__(kGrowT) growth_survey_kernel(
+    MeshViewT<R> dm, TemplateViewT<R> dt, MeshViewT<R> rm, TemplateViewT<R> rt, RungConstsT<R> rc,
+    R K, SurvivorsT<R> sv, R* __restrict__ gbuf, long long* __restrict__ gwbuf, uint32_t gcap,
+    unsigned long long* __restrict__ traffic, uint32_t* work) {
+  extern __shared__ __align__(16) unsigned char ssm[];
+  long long* dbin = (long long*)ssm;       // data weight per bin
+  long long* rbin = dbin + kMaxBins;       // random weight per bin
+  long long* dbel = rbin + kMaxBins;       // data weight inside bin b's lower edge
+  long long* rbel = dbel + kMaxBins;       // random weight inside it
+  long long* pwv = rbel + kMaxBins;        // a window's weights (then their suffix sums)
+  uint32_t* bn = (uint32_t*)(pwv + kWBuf);  // data tracers per bin (sizes the windows)
+  uint32_t* beln = bn + kMaxBins;           // data tracers in the bins below b
+  R* pd2 = (R*)(beln + kMaxBins);           // a window's distances
+  __shared__ unsigned long long red64[2 * kGrowWarps];
+  __shared__ long long tsum[kGrowT];
+  __shared__ int redi[kGrowWarps];
+  __shared__ uint32_t collected;
+  __shared__ uint32_t s_item;
+
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t n_surv = *sv.count;
+  const double dinv = dm.winv, rinv = rm.winv;
+  const R rs2 = rc.rs2, rc2 = rc.rc2, span = fsub(rs2, rc2);
+  // exodus_rescale.c:2192-2204, the same for every survivor of the rung but
+  // its tracer count.
+  const R core_fraction = fdiv(fmul(fmul(rc.rmin, rc.rmin), rc.rmin),
+                               fmul(fmul(rc.r_search, rc.r_search), rc.r_search));
+
+  for (uint32_t s = next_cta_item(work, &s_item); s < n_surv; s = next_cta_item(work, &s_item)) {
+    const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
+    const int32_t di = (int32_t)fmul(cx, dm.inv_l), dj = (int32_t)fmul(cy, dm.inv_l),
+                  dk = (int32_t)fmul(cz, dm.inv_l);
+    const int32_t ri_ = (int32_t)fmul(cx, rm.inv_l), rj = (int32_t)fmul(cy, rm.inv_l),
+                  rk = (int32_t)fmul(cz, rm.inv_l);
+    uint8_t reason = kRescaleOk;
+    R radius = -1.0f;
+    unsigned long long read = 0, visited = 0;
+
+    // 1. The weight inside r_search on both meshes, and the data's tracers.
+    long long dw = 0, rw = 0;
+    unsigned long long dn = 0;
+    walk_cells(
+        dm, dt, di, dj, dk, cx, cy, cz, [](uint8_t, uint32_t) { return true; },
+        [&](uint8_t type, uint32_t cnt, uint32_t flat) {
+          if (cnt == 0 || !(type == kCellCore || type == kCellShell)) return;
+          dw += cell_wt(dm, flat, cnt);
+          dn += cnt;
+        },
+        [](uint8_t type) { return type == kCellStraddle || type == kCellEdge; },
+        [&](uint8_t, R d2, uint32_t p, uint32_t) {
+          if (d2 <= rs2) {
+            dw += tracer_w(dm, p);
+            dn++;
+          }
+        },
+        visited, read);
+    walk_cells(
+        rm, rt, ri_, rj, rk, cx, cy, cz, [](uint8_t, uint32_t) { return true; },
+        [&](uint8_t type, uint32_t cnt, uint32_t flat) {
+          if (cnt == 0 || !(type == kCellCore || type == kCellShell)) return;
+          rw += cell_wt(rm, flat, cnt);
+        },
+        [](uint8_t type) { return type == kCellStraddle || type == kCellEdge; },
+        [&](uint8_t, R d2, uint32_t p, uint32_t) {
+          if (d2 <= rs2) rw += tracer_w(rm, p);
+        },
+        visited, read);
+    unsigned long long udw = (unsigned long long)dw, urw = (unsigned long long)rw;
+    block_sum2_u64(udw, urw, red64);
+    dn = block_sum_u64(dn, red64);
+    if (!((long long)urw > 0)) {
+      reason = kRescaleNoRandoms;
+    } else if (wreal<R>((long long)udw, dinv) <= fmul(K, wreal<R>((long long)urw, rinv))) {
+      reason = kRescaleBeyondSearch;
+    }
+
+    if (reason == kRescaleOk) {
+      // 2. The bins, sized by the data's tracers, and both histograms.
+      uint32_t nb = kMaxBins;
+      {
+        const R want = fdiv(fmul((R)dn, fsub(R(1.0f), core_fraction)), R(16.0f));
+        if (!(want >= R(64.0f)))
+          nb = 64u;
+        else if (want < R(2048.0f))
+          nb = (uint32_t)want;
+      }
+      const R inv_w = fdiv((R)nb, span), bin_w = fdiv(span, (R)nb);
+      for (uint32_t b = threadIdx.x; b < nb; b += kGrowT) {
+        dbin[b] = 0;
+        rbin[b] = 0;
+        bn[b] = 0;
+      }
+      __syncthreads();
+      long long dcore = 0, dshell = 0, rcore = 0, rshell = 0;
+      walk_cells(
+          dm, dt, di, dj, dk, cx, cy, cz, [](uint8_t, uint32_t) { return true; },
+          [&](uint8_t type, uint32_t cnt, uint32_t flat) {
+            if (cnt && type == kCellCore) dcore += cell_wt(dm, flat, cnt);
+          },
+          [](uint8_t type) { return type != kCellCore; },
+          [&](uint8_t type, R d2, uint32_t p, uint32_t) {
+            const long long q = tracer_w(dm, p);
+            if (type != kCellShell && d2 <= rc2) {
+              dcore += q;
+            } else if (type == kCellShell || d2 <= rs2) {
+              const uint32_t b = bin_of(d2, rc2, inv_w, nb);
+              atomicAdd((unsigned long long*)(dbin + b), (unsigned long long)q);
+              atomicAdd(bn + b, 1u);
+              dshell += q;
+            }
+          },
+          visited, read);
+      walk_cells(
+          rm, rt, ri_, rj, rk, cx, cy, cz, [](uint8_t, uint32_t) { return true; },
+          [&](uint8_t type, uint32_t cnt, uint32_t flat) {
+            if (cnt && type == kCellCore) rcore += cell_wt(rm, flat, cnt);
+          },
+          [](uint8_t type) { return type != kCellCore; },
+          [&](uint8_t type, R d2, uint32_t p, uint32_t) {
+            const long long q = tracer_w(rm, p);
+            if (type != kCellShell && d2 <= rc2) {
+              rcore += q;
+            } else if (type == kCellShell || d2 <= rs2) {
+              atomicAdd((unsigned long long*)(rbin + bin_of(d2, rc2, inv_w, nb)),
+                        (unsigned long long)q);
+              rshell += q;
+            }
+          },
+          visited, read);
+      unsigned long long ua = (unsigned long long)dcore, ub = (unsigned long long)dshell;
+      block_sum2_u64(ua, ub, red64);
+      const long long d_core = (long long)ua, d_total = (long long)ua + (long long)ub;
+      ua = (unsigned long long)rcore;
+      ub = (unsigned long long)rshell;
+      block_sum2_u64(ua, ub, red64);
+      const long long r_core = (long long)ua, r_total = (long long)ua + (long long)ub;
+      // The backstops (2226-2237).
+      if (!(r_total > 0)) {
+        reason = kRescaleNoRandoms;
+      } else if (wreal<R>(d_total, dinv) <= fmul(K, wreal<R>(r_total, rinv))) {
+        reason = kRescaleBeyondSearch;
+      }
+      if (reason == kRescaleOk) {
+        // Below each bin's lower edge: the core and the bins under it.
+        if (warp == 0) {
+          long long cd = d_core, cr = r_core;
+          uint32_t cn = 0;
+          for (uint32_t b0 = 0; b0 < nb; b0 += 32) {
+            const uint32_t b = b0 + lane;
+            const long long vd = b < nb ? dbin[b] : 0, vr = b < nb ? rbin[b] : 0;
+            const uint32_t vn = b < nb ? bn[b] : 0u;
+            long long xd = vd, xr = vr;
+            uint32_t xn = vn;
+            for (int d = 1; d < 32; d <<= 1) {
+              const long long yd = __shfl_up_sync(0xffffffffu, xd, d);
+              const long long yr = __shfl_up_sync(0xffffffffu, xr, d);
+              const uint32_t yn = __shfl_up_sync(0xffffffffu, xn, d);
+              if (lane >= (unsigned)d) {
+                xd += yd;
+                xr += yr;
+                xn += yn;
+              }
+            }
+            if (b < nb) {
+              dbel[b] = cd + xd - vd;
+              rbel[b] = cr + xr - vr;
+              beln[b] = cn + xn - vn;
+            }
+            cd += __shfl_sync(0xffffffffu, xd, 31);
+            cr += __shfl_sync(0xffffffffu, xr, 31);
+            cn += __shfl_sync(0xffffffffu, xn, 31);
+          }
+        }
+        __syncthreads();
+
+        // 3. The walk (2239-2312): the highest bin with data weight whose
+        //    skip test fails -- the least data a tracer in it could enclose
+        //    against the most randoms, everything to the bin's top -- then
+        //    its window resolved.
+        int32_t cursor = (int32_t)nb - 1;
+        reason = kRescaleBelowRung;
+        while (cursor >= 0) {
+          int best = -1;
+          for (int32_t b = threadIdx.x; b <= cursor; b += kGrowT) {
+            if (!(dbin[b] > 0)) continue;
+            const R d_in_min = wreal<R>(dbel[b], dinv);
+            const R r_in_max = wreal<R>(rbel[b] + rbin[b], rinv);
+            if (!(r_in_max > R(0.0f)) || d_in_min > fmul(K, r_in_max)) continue;
+            best = max(best, b);
+          }
+          best = block_max_int(best, redi);
+          if (best < 0) break;
+          const int32_t b_hi = best;
+          int32_t b_lo = b_hi - (int32_t)rc.window + 1;
+          if (b_lo < 0) b_lo = 0;
+          const uint32_t top_n = beln[b_hi] + bn[b_hi];
+          while (b_lo < b_hi && top_n - beln[b_lo] > kWBuf) b_lo++;
+          const uint32_t want = top_n - beln[b_lo];
+          R* kb = pd2;
+          long long* vb = pwv;
+          uint32_t cap = kWBuf;
+          if (want > kWBuf) {
+            kb = gbuf + (uint64_t)blockIdx.x * gcap;
+            vb = gwbuf + (uint64_t)blockIdx.x * gcap;
+            cap = gcap;
+          }
+          if (want > cap) {
+            reason = kRescaleOverflow;
+            break;
+          }
+          const R lo = fadd(rc2, fmul((R)b_lo, bin_w));
+          const R hi = b_hi == (int32_t)nb - 1 ? fmul(rs2, R(1.0f + 1e-6f))
+                                               : fadd(rc2, fmul((R)(b_hi + 1), bin_w));
+          if (threadIdx.x == 0) collected = 0;
+          __syncthreads();
+          walk_cells(
+              dm, dt, di, dj, dk, cx, cy, cz,
+              [&](uint8_t type, uint32_t i) {
+                return type != kCellCore && !(__ldg(dt.max_d2 + i) < lo) &&
+                       !(__ldg(dt.min_d2 + i) > hi);
+              },
+              [](uint8_t, uint32_t) {}, [](uint8_t) { return true; },
+              [&](uint8_t type, R d2, uint32_t p, uint32_t) {
+                if (type != kCellShell && !(d2 > rc2 && d2 <= rs2)) return;
+                const uint32_t bi = bin_of(d2, rc2, inv_w, nb);
+                if (bi < (uint32_t)b_lo || bi > (uint32_t)b_hi) return;
+                const uint32_t slot = atomicAdd(&collected, 1u);
+                if (slot < cap) {
+                  kb[slot] = d2;
+                  vb[slot] = tracer_w(dm, p);
+                }
+              },
+              visited, read);
+          __syncthreads();
+          const uint32_t m = collected < cap ? collected : cap;
+          uint32_t p2 = 1;
+          while (p2 < m) p2 <<= 1;
+          for (uint32_t i = m + threadIdx.x; i < p2; i += kGrowT) {
+            kb[i] = real_inf<R>();
+            vb[i] = 0;
+          }
+          __syncthreads();
+          bitonic_sort_pairs(kb, vb, p2);
+          suffix_sums(vb, p2, tsum);
+          // Outside-in: the tracer at k encloses the data to the window's
+          // top less its own weight and everything beyond it, against the
+          // randoms below its bin's lower edge and the share of its bin's
+          // randoms up to it.
+          const long long d_top = dbel[b_hi] + dbin[b_hi];
+          int found = -1;
+          for (uint32_t k = threadIdx.x; k < m; k += kGrowT) {
+            const R d2 = kb[k];
+            if (d2 == R(0)) continue;
+            const uint32_t bi = bin_of(d2, rc2, inv_w, nb);
+            R frac = fmul(fsub(d2, fadd(rc2, fmul((R)bi, bin_w))), inv_w);
+            frac = frac < R(0.0f) ? R(0.0f) : (frac > R(1.0f) ? R(1.0f) : frac);
+            const double rb = __dmul_rn(__ll2double_rn(rbel[bi]), rinv);
+            const double rn = __dmul_rn(__ll2double_rn(rbin[bi]), rinv);
+            const R r_in = (R)__dadd_rn(rb, __dmul_rn(rn, (double)frac));
+            const R d_in = wreal<R>(d_top - vb[k], dinv);
+            if (r_in > R(0.0f) && d_in <= fmul(K, r_in)) found = max(found, (int)k);
+          }
+          found = block_max_int(found, redi);
+          if (found >= 0) {
+            radius = fsqrt(kb[found]);
+            reason = kRescaleOk;
+            break;
+          }
+          cursor = b_lo - 1;
+          __syncthreads();
+        }
+      }
+    }
+    if (traffic) {
+      const unsigned long long v = __reduce_add_sync(0xffffffffu, (unsigned)visited);
+      if (lane == 0) {
+        if (read) atomicAdd(traffic, read);
+        if (v) atomicAdd(traffic + 1, v);
+      }
+    }
+    if (threadIdx.x == 0) {
+      sv.r[s] = reason == kRescaleOk ? radius : -1.0f;
+      sv.reason[s] = reason;
+    }
+    __syncthreads();
+  }
+}
+
+template <class R>
+void grow_survey(MeshViewT<R> dm, TemplateViewT<R> dt, MeshViewT<R> rm, TemplateViewT<R> rt,
+                 RungConstsT<R> rc, R K, SurvivorsT<R> s, uint32_t max_survivors, R* gbuf,
+                 long long* gwbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
+                 KernelTimer* timer, uint32_t* work) {
+  if (max_survivors == 0) return;
+  SIFG_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), st));
+  constexpr size_t smem = survey_smem_bytes<R>();
+  thread_local bool attr = false;  // the attribute is per thread's view of the function
+  if (!attr) {
+    SIFG_CUDA(cudaFuncSetAttribute(growth_survey_kernel<R>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
+  if (timer) timer->begin(st);
+  growth_survey_kernel<R><<<g, kGrowT, smem, st>>>(dm, dt, rm, rt, rc, K, s, gbuf, gwbuf, gcap,
+                                                  traffic, work);
+  SIFG_LAUNCH_CHECK();
+  if (timer) timer->end(st);
+}
+
 // sif__exodus_check_weights (exodus_finder.c:1039-1106): by the bits, so a
 // NaN or an infinity is caught whatever the compiler assumes; a negative
 // zero is a zero.
@@ -2161,6 +2508,14 @@ void weight_fixed_point(double bound, double* wscale, double* winv) {
   *winv = std::ldexp(1.0, -s);
 }
 
+template void grow_survey<float>(MeshViewT<float>, TemplateViewT<float>, MeshViewT<float>,
+                                 TemplateViewT<float>, RungConstsT<float>, float, SurvivorsT<float>,
+                                 uint32_t, float*, long long*, uint32_t, unsigned long long*,
+                                 cudaStream_t, KernelTimer*, uint32_t*);
+template void grow_survey<double>(MeshViewT<double>, TemplateViewT<double>, MeshViewT<double>,
+                                  TemplateViewT<double>, RungConstsT<double>, double,
+                                  SurvivorsT<double>, uint32_t, double*, long long*, uint32_t,
+                                  unsigned long long*, cudaStream_t, KernelTimer*, uint32_t*);
 template void grow_weighted<float>(MeshViewT<float>, TemplateViewT<float>, RungConstsT<float>,
                                    SurvivorsT<float>, uint32_t, float*, long long*, uint32_t,
                                    unsigned long long*, cudaStream_t, KernelTimer*, uint8_t,

@@ -26,6 +26,7 @@ enum : uint8_t {
   kRescaleOverflow,
   kRescalePending,  // left by the warp-per-survivor growth for the per-CTA one
   kRescaleWitness,  // refused by the collision witness before any growth
+  kRescaleNoRandoms,  // a survey: no random weight inside r_search (RESCALE_NO_RANDOMS)
 };
 
 // Commit states.
@@ -247,6 +248,41 @@ void grow_weighted(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, S
                    uint32_t max_survivors, R* gbuf, long long* gwbuf, uint32_t gcap,
                    unsigned long long* traffic, cudaStream_t st, KernelTimer* timer,
                    uint8_t only, uint32_t* work);
+// A survey's sphere growth (sif__exodus_find_radius_survey, src/finder/
+// exodus_rescale.c:2154-2317): the largest data distance at which the data
+// weight inside is at most K times the random weight, data on dm with
+// template dt, randoms on rm with rt (each mesh's weights, or 1 a tracer,
+// in its own fixed point: wscale and winv set either way). Every survivor.
+template <class R>
+void grow_survey(MeshViewT<R> dm, TemplateViewT<R> dt, MeshViewT<R> rm, TemplateViewT<R> rt,
+                 RungConstsT<R> rc, R K, SurvivorsT<R> s, uint32_t max_survivors, R* gbuf,
+                 long long* gwbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
+                 KernelTimer* timer, uint32_t* work);
+// The survey's footprint and field (survey.cu; src/finder/exodus_survey.c).
+// The nodes nearest the randoms (n^3 bits, (n^3 + 31) / 32 words of occ),
+// and how many: survey_mark returns the marked count (synchronises st).
+template <class R>
+uint64_t survey_mark(const R* x, const R* y, const R* z, uint64_t n_randoms, uint32_t n, R box,
+                     uint32_t* occ, unsigned long long* d_count, cudaStream_t st);
+// The closing over 2k + 1 nodes (dilate then erode along each axis; tmp of
+// the same size as occ), the result back in occ.
+void survey_close(uint32_t* occ, uint32_t* tmp, uint32_t n, int32_t k, cudaStream_t st);
+// The closing's k for n_randoms over `marked` nodes (exodus_survey.c:181-188).
+int32_t survey_closing_k(uint64_t n_randoms, uint64_t marked);
+// The scanned field over the smoothed data: data / (alpha randoms) - 1 on
+// observed nodes with randoms, SIF__FINDER_UNOBSERVED elsewhere.
+template <class R>
+void survey_contrast(R* data, const R* randoms, const uint32_t* occ, R alpha, uint64_t cells,
+                     cudaStream_t st);
+// Each void's observed fractions of its sphere and of the shell to twice its
+// radius (survey_void_footprint, exodus_survey.c:240-296).
+template <class R>
+void survey_footprint(const R* cx, const R* cy, const R* cz, const R* r, uint32_t n_voids,
+                      const uint32_t* occ, uint32_t n, R box, R* inside, R* shell,
+                      cudaStream_t st);
+// The bounding box of n positions (lo[3], hi[3] on the host; synchronises).
+template <class R>
+void extent(const R* x, const R* y, const R* z, uint64_t n, R lo[3], R hi[3], cudaStream_t st);
 // Counts a weighted mesh's negative (below zero; a negative zero is not)
 // and non-finite weights into counts[0], counts[1] (device, zeroed here).
 template <class R>

@@ -168,6 +168,44 @@ def exodus(delta, n_grid, box, mesh, mesh_cells, radii, threshold, overlap=0.0, 
     return tuple(c[: n.value].copy() for c in cols)
 
 
+def exodus_survey(data_density, random_density, n_grid, box, data_mesh, random_mesh, radii,
+                  threshold, overlap=0.0, options=0, inject=None, capacity=1 << 20, prior=None):
+    """The survey finder on device data (sifg_exodus_survey_device), in the
+    box's frame. data_mesh / random_mesh: (mx, my, mz, offsets, mesh_cells,
+    total_weight) or with (w, cell_w) after them for a weighted mesh;
+    inject: 2 fields a rung (data, randoms). Returns (cx, cy, cz, r,
+    footprint, footprint_shell)."""
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    cols = tuple(_catalogue_arrays(capacity, np.float32)) + \
+        (np.empty(capacity, np.float32), np.empty(capacity, np.float32))
+    n = C.c_uint64(0)
+
+    def addr(t):
+        if t is None:
+            return None
+        assert t.is_cuda and t.is_contiguous(), "expected a contiguous CUDA tensor"
+        return t.data_ptr()
+
+    def dmesh(m):
+        mx, my, mz, offs, cells, tot = m[:6]
+        w = m[6] if len(m) > 6 else None
+        cw = m[7] if len(m) > 7 else None
+        return _lib.DeviceMesh(addr(mx), addr(my), addr(mz), addr(offs), addr(w), addr(cw),
+                               float(tot), mx.numel(), cells)
+
+    dm, rm = dmesh(data_mesh), dmesh(random_mesh)
+    packed = np.ascontiguousarray(np.concatenate([np.asarray(c, np.float32) for c in prior])) \
+        if prior is not None else None
+    st = _lib.load().sifg_exodus_survey_device(
+        _ptr(data_density), _ptr(random_density), n_grid, box, C.byref(dm), C.byref(rm),
+        radii.ctypes.data_as(C.c_void_p), len(radii), threshold, overlap, options, _ptr(inject),
+        packed.ctypes.data_as(C.c_void_p) if packed is not None else None,
+        len(prior[0]) if prior is not None else 0, *[c.ctypes.data_as(C.c_void_p) for c in cols],
+        capacity, C.byref(n))
+    _check(st, "exodus_survey")
+    return tuple(c[: n.value].copy() for c in cols)
+
+
 def box(x, y, z, n_grid, box_length, mesh_cells, radii, threshold, overlap=0.0, options=0,
         capacity=1 << 22):
     """The whole path on device particles: CIC, contrast, mesh, finder."""

@@ -204,10 +204,12 @@ class ChainMesh:
 
 
 class Catalogue:
-    """Void centres and radii (float32 arrays)."""
+    """Void centres and radii (float32 arrays); a survey's also the observed
+    fractions of each sphere and of its shell to twice the radius."""
 
-    def __init__(self, cx, cy, cz, radii):
+    def __init__(self, cx, cy, cz, radii, footprint=None, footprint_shell=None):
         self.cx, self.cy, self.cz, self.radii = cx, cy, cz, radii
+        self.footprint, self.footprint_shell = footprint, footprint_shell
 
     def __len__(self):
         return len(self.radii)
@@ -223,6 +225,9 @@ def _take_catalogue(lib, ptr, what):
     n = cat.n_voids
     cols = [np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0, np.float32)
             for p in (cat.cx, cat.cy, cat.cz, cat.radii)]
+    if cat.footprint:
+        cols += [np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0, np.float32)
+                 for p in (cat.footprint, cat.footprint_shell)]
     lib.sif_catalogue_free(ptr)
     return Catalogue(*cols)
 
@@ -353,8 +358,80 @@ def _suggest_mesh_cells(n_particles, box_length, max_radius=0.0, volume=0.0):
     return int(min(max(cells, 8.0), 1024.0))
 
 
+def _survey_opt(overlap_type, search_factor, deconvolution):
+    opt = _SEARCH[float(search_factor)]
+    if overlap_type == "lagrangian":
+        opt |= abi.SIF_FINDER_LAGRANGIAN_OVERLAP
+    if deconvolution == "none":
+        opt |= abi.SIF_FINDER_KEEP_CIC_WINDOW
+    elif deconvolution == "aliasing":
+        opt |= abi.SIF_FINDER_ALIASING_WINDOW
+    return opt
+
+
+def _offset_arg(offset):
+    if offset is None:
+        return None, None
+    o = np.ascontiguousarray(offset, dtype=np.float32)
+    assert o.shape == (3,)
+    return o, _P(o)
+
+
+def _exodus_survey_raw(data_grid, random_grid, data_mesh, random_mesh, radii, threshold,
+                       overlap_fraction=0.0, *, offset=None, overlap_type="eulerian",
+                       search_factor=1.5, deconvolution="full", checkpoint=False, prior=None,
+                       keep_checkpoint=False):
+    """finders.exodus_survey_raw (sif_finder_exodus_survey_raw): grids hold
+    the CIC densities of data and randoms; offset what the survey was moved
+    into the box by. The catalogue comes back in the caller's frame with its
+    footprint columns."""
+    lib = _lib.load()
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    extras, opt, keep = _extras(checkpoint, prior, keep_checkpoint, False, raw=True)
+    opt |= _survey_opt(overlap_type, search_factor, deconvolution)
+    o, op = _offset_arg(offset)
+    ptr = lib.sif_finder_exodus_survey_raw(data_grid._ptr, random_grid._ptr, data_mesh._ptr,
+                                           random_mesh._ptr, op, _P(radii), len(radii), threshold,
+                                           overlap_fraction, opt,
+                                           C.byref(extras) if extras is not None else None)
+    del keep, o
+    return _take_catalogue(lib, ptr, "exodus_survey_raw")
+
+
+def _exodus_survey(data_grid, random_grid, data_mesh, random_mesh, radii, threshold,
+                   variant="excursion-set", *, offset=None, checkpoint=None, prior=None,
+                   keep_checkpoint=False):
+    """finders.exodus_survey (sif_finder_exodus_survey): a variant."""
+    lib = _lib.load()
+    if variant not in _VARIANTS:
+        raise ValueError(f"variant: {variant!r}")
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    extras, _, keep = _extras(checkpoint, prior, keep_checkpoint, False, raw=False)
+    o, op = _offset_arg(offset)
+    ptr = lib.sif_finder_exodus_survey(data_grid._ptr, random_grid._ptr, data_mesh._ptr,
+                                       random_mesh._ptr, op, _P(radii), len(radii), threshold,
+                                       _VARIANTS[variant],
+                                       C.byref(extras) if extras is not None else None)
+    del keep, o
+    return _take_catalogue(lib, ptr, "exodus_survey")
+
+
+def _survey_box(data, randoms, radii, search_factor=1.5):
+    """finders.survey_box (sif_finder_exodus_survey_box): (offset, box_length)
+    for Fields in the survey's own frame."""
+    lib = _lib.load()
+    radii = np.ascontiguousarray(radii, dtype=np.float32)
+    off = np.zeros(3, np.float32)
+    L = C.c_float(0.0)
+    _check(lib.sif_finder_exodus_survey_box(data._ptr, randoms._ptr, _P(radii), len(radii),
+                                            _SEARCH[float(search_factor)], _P(off), C.byref(L)),
+           "survey_box")
+    return off, float(L.value)
+
+
 finders = types.SimpleNamespace(exodus=_exodus, exodus_raw=_exodus_raw,
-                                suggest_mesh_cells=_suggest_mesh_cells,
+                                exodus_survey=_exodus_survey, exodus_survey_raw=_exodus_survey_raw,
+                                survey_box=_survey_box, suggest_mesh_cells=_suggest_mesh_cells,
                                 checkpoint_read=checkpoint_read)
 
 
