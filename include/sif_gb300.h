@@ -413,6 +413,8 @@ typedef struct {
   /* The collision witness, run ahead of each rung's growth. */
   double witness_ms;
   int witness_launches;
+  double commit_ms; /* the commit's rounds, kernel time on the run's stream */
+  int commit_launches;
 } sifg_timings_t;
 
 /* The CIC density (per unit volume, float) of n device-resident particles

@@ -279,6 +279,8 @@ static void record_timings(RunTimings& t) {
   g_timings.growth_cells = t.growth_cells;
   g_timings.witness_ms = t.witness.total_ms();
   g_timings.witness_launches = t.witness.launches();
+  g_timings.commit_ms = t.commit.total_ms();
+  g_timings.commit_launches = t.commit.launches();
 }
 
 // The API lock, for entry points outside this file that hold it for a whole

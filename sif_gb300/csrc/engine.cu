@@ -1103,7 +1103,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     uint8_t* sb = grow_to<uint8_t>(state_b_, m);
     uint32_t* acc = grow_to<uint32_t>(acc_, m);
     SIFG_CUDA(cudaMemsetAsync(counters, 0, kCommitCounters * sizeof(uint32_t), st_));
-    commit_init(sv, sa, counters, m, st_);
+    commit_init(sv, vv, rc, sa, counters, m, st_);
     // The rounds run in one cooperative launch, to the round that leaves no
     // survivor undecided (or a ring's worth, then another launch); where
     // the device cannot, a few rounds are issued at a time between reads of
@@ -1114,6 +1114,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     uint32_t* h_bar = h_count + 1;  // the cooperative launch's report: bar[2] error, bar[3] rounds
     unsigned* bar = grow_to<unsigned>(commit_bar_, 4);
     for (uint32_t batch = 3;; batch = 4) {
+      if (tm) tm->commit.begin(st_);
       SIFG_CUDA(cudaMemsetAsync(counters + kRoundUndecided, 0, kRoundRing * sizeof(uint32_t), st_));
       const bool one_launch = commit_rounds(sv, rank, sg, vv, mask, rc, sa, sb, acc, counters,
                                             (uint32_t)rounds, kRoundRing, bar, m, st_);
@@ -1127,6 +1128,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
           rounds++;
         }
       }
+      if (tm) tm->commit.end(st_);
       SIFG_CUDA(cudaMemcpyAsync(h_counters_, counters, kCommitCounters * sizeof(uint32_t),
                                 cudaMemcpyDeviceToHost, st_));
       SIFG_CUDA(cudaMemcpyAsync(h_count, dcount + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));

@@ -88,13 +88,14 @@ struct RungStat {
 };
 
 struct RunTimings {
-  KernelTimer growth, filter, cic, mesh, witness;
+  KernelTimer growth, filter, cic, mesh, witness, commit;
   double wall_ms = 0.0;
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the sphere growth
   void reset() {
     growth_particles = growth_cells = 0;
     growth.reset();
     witness.reset();
+    commit.reset();
     filter.reset();
     cic.reset();
     mesh.reset();

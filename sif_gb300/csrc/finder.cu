@@ -445,6 +445,43 @@ __device__ bool overlap_exact(const VoidViewT<R>& v, R cx, R cy, R cz, R r, R f,
   return false;
 }
 
+// overlap_exact by a warp: the same cells and the same pair tests, the
+// lanes taking the cells 32 at a time (a thread alone walks them one load
+// after another). Every lane returns the answer.
+template <class R>
+__device__ bool overlap_exact_warp(const VoidViewT<R>& v, R cx, R cy, R cz, R r, R f, R scale,
+                                   R box) {
+  if (v.n == 0) return false;
+  const unsigned lane = threadIdx.x & 31u;
+  const R half = fmul(box, R(0.5f));
+  const R s = search_radius(r, v.max_r, f, scale);
+  const int32_t x0 = (int32_t)ffloor(fmul(fsub(cx, s), v.inv_cell));
+  const int32_t x1 = (int32_t)ffloor(fmul(fadd(cx, s), v.inv_cell));
+  const int32_t y0 = (int32_t)ffloor(fmul(fsub(cy, s), v.inv_cell));
+  const int32_t y1 = (int32_t)ffloor(fmul(fadd(cy, s), v.inv_cell));
+  const int32_t z0 = (int32_t)ffloor(fmul(fsub(cz, s), v.inv_cell));
+  const int32_t z1 = (int32_t)ffloor(fmul(fadd(cz, s), v.inv_cell));
+  const bool interior = is_interior(cx, cy, cz, s, box);
+  const uint32_t ny = (uint32_t)(y1 - y0 + 1), nz = (uint32_t)(z1 - z0 + 1);
+  const uint32_t cells = (uint32_t)(x1 - x0 + 1) * ny * nz;
+  for (uint32_t k0 = 0; k0 < cells; k0 += 32) {
+    bool hit = false;
+    const uint32_t k = k0 + lane;
+    if (k < cells) {
+      const uint32_t wx = (uint32_t)(x0 + (int32_t)(k / (ny * nz))) & (kVoidCells - 1);
+      const uint32_t wy = (uint32_t)(y0 + (int32_t)((k / nz) % ny)) & (kVoidCells - 1);
+      const uint32_t wz = (uint32_t)(z0 + (int32_t)(k % nz)) & (kVoidCells - 1);
+      const uint32_t c = (wx * kVoidCells + wy) * kVoidCells + wz;
+      for (uint32_t q = v.start[c]; q < v.start[c + 1] && !hit; q++) {
+        const uint32_t j = v.ids[q];
+        hit = collide(cx, cy, cz, r, v.cx[j], v.cy[j], v.cz[j], v.r[j], f, scale, box, half, interior);
+      }
+    }
+    if (__any_sync(0xffffffffu, hit)) return true;
+  }
+  return false;
+}
+
 // ---------------------------------------------------------------------------
 // SIF_FINDER_REFINE_GAUSSIAN: the candidates' placing (sif__finder_scan_refined,
 // src/finder/utils.c:406-552; place_candidate 331-365; newton_step 261-313)
@@ -2631,13 +2668,13 @@ __device__ __forceinline__ void commit_pass(const SurvivorsT<R>& sv, const uint3
     const uint32_t ix = node / (nn * nn), iy = (node / nn) % nn, iz = node % nn;
     // The commit's re-checks (exodus_finder.c:2286-2317), against every void
     // accepted so far: the node's mask bit, the poles at the rescaled radius,
-    // the exact overlap.
+    // the exact overlap -- with the catalogue as the rung began, once, before
+    // the rounds (commit_init); with the rung's own voids, below.
     bool reject = cand_masked(mask, node, sv.off ? sv.off[i] : R(-1.0f), r, rc);
     if (!reject) {
       const int32_t pole = (int32_t)(fdiv(fmul(fmul(rc.scale, r), fsub(R(1.0f), rc.f)), rc.cell)) - 1;
       if (pole > 0 && overlap_quick(mask, nn, ix, iy, iz, (uint32_t)pole)) reject = true;
     }
-    if (!reject && overlap_exact(voids, cx, cy, cz, r, rc.f, rc.scale, rc.box)) reject = true;
     // Voids accepted this rung, from the survivor hash.
     bool ready = true;
     if (!reject) {
@@ -2701,24 +2738,36 @@ __global__ void commit_round_kernel(SurvivorsT<R> sv, const uint32_t* __restrict
   commit_pass(sv, rank, g, voids, mask, rc, st_in, st_out, acc, counters, slot);
 }
 
+// Before the rounds: a survivor whose rescaling failed is rejected, and so
+// is one whose sphere at its rescaled radius overlaps a void of the
+// catalogue as the rung began (the re-check's exact overlap, whose answer no
+// round can change; a warp per survivor); the rest start undecided.
 template <class R>
-__global__ void commit_init_kernel(SurvivorsT<R> sv, uint8_t* __restrict__ state,
-                                   uint32_t* __restrict__ counters) {
+__global__ void commit_init_kernel(SurvivorsT<R> sv, VoidViewT<R> voids, RungConstsT<R> rc,
+                                   uint8_t* __restrict__ state, uint32_t* __restrict__ counters) {
   const uint32_t n = *sv.count;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const bool ok = sv.r[i] >= 0.0f;
-    state[i] = ok ? kUndecided : kRejected;
-    if (!ok) atomicAdd(counters + 4, 1u);
-    if (sv.reason[i] == kRescaleOverflow) atomicAdd(counters + 5, 1u);
-    if (sv.reason[i] == kRescaleWitness) atomicAdd(counters + 8, 1u);
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+    const R r = sv.r[i];
+    const bool ok = r >= 0.0f;
+    const bool overlaps =
+        ok && overlap_exact_warp(voids, sv.cx[i], sv.cy[i], sv.cz[i], r, rc.f, rc.scale, rc.box);
+    if (lane == 0) {
+      state[i] = ok && !overlaps ? kUndecided : kRejected;
+      if (!ok) atomicAdd(counters + 4, 1u);
+      if (sv.reason[i] == kRescaleOverflow) atomicAdd(counters + 5, 1u);
+      if (sv.reason[i] == kRescaleWitness) atomicAdd(counters + 8, 1u);
+    }
   }
 }
 
 template <class R>
-void commit_init(SurvivorsT<R> s, uint8_t* state, uint32_t* counters, uint32_t max_survivors,
-                 cudaStream_t st) {
+void commit_init(SurvivorsT<R> s, VoidViewT<R> voids, RungConstsT<R> rc, uint8_t* state,
+                 uint32_t* counters, uint32_t max_survivors, cudaStream_t st) {
   if (max_survivors == 0) return;
-  commit_init_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(s, state, counters);
+  commit_init_kernel<<<grid_for((uint64_t)max_survivors * 32, 256), 256, 0, st>>>(s, voids, rc, state,
+                                                                                counters);
   SIFG_LAUNCH_CHECK();
 }
 
@@ -2900,7 +2949,9 @@ bool commit_rounds(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Vo
     SIFG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SIFG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     SIFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, commit_loop_kernel<R>, kCommitT, 0));
-    blocks = coop && per_sm > 0 ? sms : 0;  // one block per SM
+    // As many blocks as the device keeps resident (its passes are chains of
+    // dependent loads: the more warps an SM holds, the more of them overlap).
+    blocks = coop && per_sm > 0 ? sms * per_sm : 0;
   }
   if (blocks == 0) return false;
   // A block per kCommitT survivors: a small rung's grid barriers gather few
@@ -3409,7 +3460,8 @@ void compact_voids(R* cx, R* cy, R* cz, R* r, uint32_t* state, cudaStream_t st) 
                         uint32_t*);                                                                \
   template void build_survivor_grid<R>(const R*, const R*, const R*, const uint32_t*, uint32_t,    \
                                        int32_t, R, uint32_t*, uint32_t*, uint32_t*, cudaStream_t); \
-  template void commit_init<R>(SurvivorsT<R>, uint8_t*, uint32_t*, uint32_t, cudaStream_t);        \
+  template void commit_init<R>(SurvivorsT<R>, VoidViewT<R>, RungConstsT<R>, uint8_t*, uint32_t*,     \
+                              uint32_t, cudaStream_t);                                              \
   template void commit_round<R>(SurvivorsT<R>, const uint32_t*, SurvivorGridT<R>, VoidViewT<R>,    \
                                 const uint32_t*, RungConstsT<R>, const uint8_t*, uint8_t*,         \
                                 uint32_t*, uint32_t*, uint32_t, uint32_t, cudaStream_t);           \

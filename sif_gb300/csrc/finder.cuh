@@ -307,12 +307,14 @@ void build_survivor_grid(const R* scx, const R* scy, const R* scz, const uint32_
                          uint32_t max_survivors, int32_t ng, R box, uint32_t* start,
                          uint32_t* ids, uint32_t* cell_of, cudaStream_t st);
 
-// Survivors whose rescaling failed start rejected, the rest undecided;
-// counters[4] counts the failures, counters[5] the resolve overflows,
-// counters[8] the witness's refusals (among the failures).
+// Survivors whose rescaling failed, or whose sphere at the rescaled radius
+// overlaps a void of the catalogue as the rung began (voids), start
+// rejected, the rest undecided; counters[4] counts the failures,
+// counters[5] the resolve overflows, counters[8] the witness's refusals
+// (among the failures).
 template <class R>
-void commit_init(SurvivorsT<R> s, uint8_t* state, uint32_t* counters, uint32_t max_survivors,
-                 cudaStream_t st);
+void commit_init(SurvivorsT<R> s, VoidViewT<R> voids, RungConstsT<R> rc, uint8_t* state,
+                 uint32_t* counters, uint32_t max_survivors, cudaStream_t st);
 
 // The commit's counters: [0] accepted so far (appended to acc); the largest
 // accepted radius as the bits of a float in [3], of a double in [6..7]; [4]
