@@ -1031,6 +1031,32 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       }
     }
 
+    // The commit's preparation, which needs the radii but not the order:
+    // queued now, so that it runs while the host sorts.
+    SurvivorGridT<R> sg{};
+    uint8_t* sa = nullptr;
+    uint8_t* sb = nullptr;
+    uint32_t* acc = nullptr;
+    if (!displace) {
+      // Radii reach the top level's reach where the rung enters the extended one.
+      const R r_max = ext0 < n_ext ? std::max(r_search, ext_reach[n_ext - 1]) : r_search;
+      const R reach = 2.0f * scale * r_max + 2.0f * cell;
+      int32_t ng = (int32_t)std::floor(box / reach);
+      if (ng < 3) ng = 1;
+      if (ng > 256) ng = 256;
+      const uint32_t sg_cells = (uint32_t)(ng * ng * ng);
+      uint32_t* sg_start = grow_to<uint32_t>(sgrid_start_, sg_cells + 1);
+      uint32_t* sg_ids = grow_to<uint32_t>(sgrid_ids_, m);
+      uint32_t* sg_cell = grow_to<uint32_t>(sgrid_cellof_, m);
+      build_survivor_grid(scx, scy, scz, dcount + 1, m, ng, box, sg_start, sg_ids, sg_cell, st_);
+      sg = SurvivorGridT<R>{sg_start, sg_ids, ng, (R)ng / box};
+      sa = grow_to<uint8_t>(state_a_, m);
+      sb = grow_to<uint8_t>(state_b_, m);
+      acc = grow_to<uint32_t>(acc_, m);
+      SIFG_CUDA(cudaMemsetAsync(counters, 0, kCommitCounters * sizeof(uint32_t), st_));
+      commit_init(sv, vv, rc, sa, counters, m, st_);
+    }
+
     // 5. The order, on the host while the GPU grows spheres.
     const auto t_wait_cand = clk::now();
     SIFG_CUDA(cudaEventSynchronize(ev_cand_));
@@ -1087,23 +1113,6 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       if (const int hs = rung_done(ri + 1, rs.n_mismatched); hs != kOk) return hs;
       continue;
     }
-    // Radii reach the top level's reach where the rung enters the extended one.
-    const R r_max = ext0 < n_ext ? std::max(r_search, ext_reach[n_ext - 1]) : r_search;
-    const R reach = 2.0f * scale * r_max + 2.0f * cell;
-    int32_t ng = (int32_t)std::floor(box / reach);
-    if (ng < 3) ng = 1;
-    if (ng > 256) ng = 256;
-    const uint32_t sg_cells = (uint32_t)(ng * ng * ng);
-    uint32_t* sg_start = grow_to<uint32_t>(sgrid_start_, sg_cells + 1);
-    uint32_t* sg_ids = grow_to<uint32_t>(sgrid_ids_, m);
-    uint32_t* sg_cell = grow_to<uint32_t>(sgrid_cellof_, m);
-    build_survivor_grid(scx, scy, scz, dcount + 1, m, ng, box, sg_start, sg_ids, sg_cell, st_);
-    SurvivorGridT<R> sg{sg_start, sg_ids, ng, (R)ng / box};
-    uint8_t* sa = grow_to<uint8_t>(state_a_, m);
-    uint8_t* sb = grow_to<uint8_t>(state_b_, m);
-    uint32_t* acc = grow_to<uint32_t>(acc_, m);
-    SIFG_CUDA(cudaMemsetAsync(counters, 0, kCommitCounters * sizeof(uint32_t), st_));
-    commit_init(sv, vv, rc, sa, counters, m, st_);
     // The rounds run in one cooperative launch, to the round that leaves no
     // survivor undecided (or a ring's worth, then another launch); where
     // the device cannot, a few rounds are issued at a time between reads of
