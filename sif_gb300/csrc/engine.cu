@@ -559,6 +559,9 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   bool listed = false;
   auto smooth_rung = [&](uint32_t ri) {
     SIFG_CUDA(cudaStreamWaitEvent(st_fft_, ev_scanned_[ri % 2], 0));
+    // With the list, the field's only other reader is SIF_FINDER_CONSUME_GRID
+    // (the last rung's): the other rungs' fields are not written.
+    if (listed) below[ri % 2].field = p.consume_out && ri + 1 == radii.size();
     smoother.smooth(kFilterTopHat, radii[ri], 0.0f, fields[ri % 2], tm ? &tm->filter : nullptr,
                     listed ? &below[ri % 2] : nullptr);
     // RUNG_MINIMA_SIGMA (exodus_finder.c:1362-1365) of the rung on top of

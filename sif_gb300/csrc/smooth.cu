@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(16 * kRowsPerCta, 4)
   for (int i = 0; i < 16; i++) {
     const uint32_t f = base + 32u * i + lane;
     const float2 v = buf[(f >> 8) * kRowSlots + (f & 255u)];
-    dst[f] = v;
+    if (below.field) dst[f] = v;
     bits |= ((v.x <= below.thr ? 1u : 0u) | (v.y <= below.thr ? 2u : 0u)) << (2 * i);
   }
   const uint32_t n_warp = __reduce_add_sync(0xffffffffu, (unsigned)__popc(bits));

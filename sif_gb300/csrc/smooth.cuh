@@ -24,6 +24,9 @@ struct BelowList {
   uint32_t* counts = nullptr;  // cells / kBelowBlock
   float* delta = nullptr;      // cells slots
   uint32_t* flat = nullptr;    // cells slots
+  // The field itself written too; false where the list is all its reader
+  // needs (a run's candidates, under the cell seeds).
+  bool field = true;
 };
 
 // Window modes: 0 none (SIF_FINDER_KEEP_CIC_WINDOW), 1 full CIC deconvolution,

@@ -525,6 +525,28 @@ def test_c_api_end_to_end_and_errors(gpu_lib, oracle):
     assert not same_bits(g2.values, g.values)
 
 
+def test_consumed_grid_at_512_is_the_last_smoothing(gpu_lib, dev):
+    """At a 512^3 grid the rungs' candidates come from the smoothing's lists
+    and the fields themselves are not written -- but the last rung's is, for
+    SIF_FINDER_CONSUME_GRID: the grid handed back is that rung's smoothing,
+    bit for bit the transform's own."""
+    import torch
+
+    pysif = gpu_lib
+    x, y, z = synth.zeldovich(128, 1000.0, 5.0, 31)
+    f = pysif.Field(x, y, z)
+    g = pysif.Grid(512, 1000.0)
+    g.assign_cic(f)
+    g.to_density_contrast()
+    contrast = torch.from_numpy(g.values.reshape(-1).copy()).cuda()
+    m = pysif.ChainMesh(50, 1000.0, f, drop_indices=True)
+    radii = synth.ladder(16.0, 40.0, 0.2).astype(np.float32)
+    cat = pysif.finders.exodus_raw(g, m, radii, -0.6, consume_grid=True)
+    assert len(cat) > 0
+    want = dev.smooth(contrast, 512, 1000.0, float(radii.min())).cpu().numpy()
+    assert same_bits(g.values.reshape(-1), want)
+
+
 @pytest.mark.parametrize("options,overlap", [(0, 0.0), (abi.SIF_FINDER_LAGRANGIAN_OVERLAP, 0.0),
                                              (0, 0.5)], ids=["default", "lagrangian", "overlap_0_5"])
 def test_box_candidates_from_the_smoothing_list(dev, options, overlap):
