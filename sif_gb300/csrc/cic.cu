@@ -233,10 +233,14 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
     const float4* __restrict__ rec, const uint32_t* __restrict__ offsets, CicGeom g,
     float inv_cell_vol, float* __restrict__ grid, FaceBufs faces,
     const float* __restrict__ wrec, const unsigned* __restrict__ wmax) {
-  // The tile's sums as 32-bit words and their carries: a 32-bit shared atomic
-  // add is one instruction, a 64-bit one a compare-and-swap loop. A word that
-  // wraps past 2^32 counts the wrap in its carry (each add is below 2^32, so
-  // it wraps at most once), and the pair is the exact 64-bit sum whatever the
+  // The tile's sums as two 32-bit words a cell: a 32-bit shared atomic add is
+  // one instruction, a 64-bit one a compare-and-swap loop. A tile with fewer
+  // than 2^16 particles adds each quantum's low 16 bits to the first word and
+  // its high bits (arithmetic shift) to the second, neither of which can wrap
+  // (a cell takes one add per particle), with adds that return nothing; a
+  // denser tile adds the whole quantum to the first word and counts its wraps
+  // in the second (each add is below 2^32, so it wraps at most once), which
+  // needs the old value back. Either pair is the exact 64-bit sum whatever the
   // order of the adds.
   extern __shared__ uint32_t acc_lo[];  // TS^3 words, then TS^3 carries
   uint32_t* acc_hi = acc_lo + TS * TS * TS;
@@ -257,6 +261,7 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
     const uint32_t ox = tx * TB, oy = ty * TB, oz = tz * TB;
 
     const uint32_t s = offsets[tile], e = offsets[tile + 1];
+    const bool split = e - s < (1u << 16);
     for (uint32_t base = s; base < e; base += blockDim.x) {
       const uint32_t p = base + threadIdx.x;
       const bool valid = p < e;
@@ -308,7 +313,16 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
       // first with __reduce_add_sync over each lane group's own mask costs a
       // serialised pass per distinct group: eight per corner per cell in the
       // warp, far more than the atomics it saves.)
-      if (valid) {
+      if (valid && split) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          const uint32_t c =
+              cell + (uint32_t)(((k >> 2) & 1) * TS * TS + ((k >> 1) & 1) * TS + (k & 1));
+          atomicAdd(acc_lo + c, q[k] & 0xffffu);
+          const int hi16 = (int)q[k] >> 16;
+          if (hi16) atomicAdd(acc_hi + c, (uint32_t)hi16);
+        }
+      } else if (valid) {
 #pragma unroll
         for (int k = 0; k < 8; k++) {
           const uint32_t v = q[k];
@@ -330,7 +344,9 @@ __global__ void __launch_bounds__(256) tile_deposit_kernel(
     for (int i = threadIdx.x; i < TS * TS * TS; i += blockDim.x) {
       const uint32_t a = i / (TS * TS), b = (i / TS) % TS, c = i % TS;
       if (a > ex || b > ey || c > ez) continue;
-      const unsigned long long v = ((unsigned long long)acc_hi[i] << 32) | acc_lo[i];
+      const unsigned long long v =
+          split ? (unsigned long long)((long long)(int)acc_hi[i] * 65536ll + (long long)acc_lo[i])
+                : ((unsigned long long)acc_hi[i] << 32) | acc_lo[i];
       acc_lo[i] = 0u;
       acc_hi[i] = 0u;
       const uint32_t gx = ox + a == g.n ? 0u : ox + a;

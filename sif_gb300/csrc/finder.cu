@@ -2949,9 +2949,7 @@ bool commit_rounds(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Vo
     SIFG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SIFG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     SIFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, commit_loop_kernel<R>, kCommitT, 0));
-    // As many blocks as the device keeps resident (its passes are chains of
-    // dependent loads: the more warps an SM holds, the more of them overlap).
-    blocks = coop && per_sm > 0 ? sms * per_sm : 0;
+    blocks = coop && per_sm > 0 ? sms : 0;  // one block per SM
   }
   if (blocks == 0) return false;
   // A block per kCommitT survivors: a small rung's grid barriers gather few
