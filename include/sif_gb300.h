@@ -417,6 +417,25 @@ typedef struct {
   int commit_launches;
 } sifg_timings_t;
 
+/* One span of the last run's timeline: a tracked launch (or stage) with its
+ * start and end in milliseconds after the run's first event, CUDA events on
+ * the stream it ran on. */
+typedef enum {
+  SIFG_TRACE_GROWTH = 0,    /* a sphere-growth launch (run's stream) */
+  SIFG_TRACE_FILTER = 1,    /* the filter pass of a smoothing (smoothing stream) */
+  SIFG_TRACE_CIC = 2,       /* the deposit kernel */
+  SIFG_TRACE_MESH = 3,      /* the chain mesh build (copy stream in the box path) */
+  SIFG_TRACE_WITNESS = 4,   /* a collision-witness launch */
+  SIFG_TRACE_COMMIT = 5,    /* a commit launch (its rounds) */
+  SIFG_TRACE_SMOOTHING = 6, /* a rung's whole smoothing (smoothing stream) */
+  SIFG_TRACE_RUNG = 7       /* a rung on the run's stream, from its field's arrival */
+} sifg_trace_kind_t;
+typedef struct {
+  int32_t kind; /* sifg_trace_kind_t */
+  float start_ms;
+  float end_ms;
+} sifg_trace_event_t;
+
 /* The CIC density (per unit volume, float) of n device-resident particles
  * on an n_grid^3 device grid. */
 int sifg_cic_device(const float* x, const float* y, const float* z, uint64_t n, uint32_t n_grid,
@@ -604,6 +623,9 @@ int sifg_box_batch_autotune(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t* n_e
 /* Statistics and timings of the last run (up to max_rungs entries). */
 uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs);
 void sifg_last_timings(sifg_timings_t* out);
+/* The last run's timeline: copies up to `capacity` spans (in the order
+ * recorded, kind by kind) and returns how many there are. */
+uint32_t sifg_last_trace(sifg_trace_event_t* out, uint32_t capacity);
 /* Kernels of this library launched so far in the process (cuFFT's own are
  * not counted). */
 uint64_t sifg_launch_count(void);

@@ -43,6 +43,11 @@ class Timings(C.Structure):
                 ("commit_ms", C.c_double), ("commit_launches", C.c_int)]
 
 
+class TraceEvent(C.Structure):
+    """sifg_trace_event_t: one span of the last run's timeline."""
+    _fields_ = [("kind", C.c_int32), ("start_ms", C.c_float), ("end_ms", C.c_float)]
+
+
 EXPORTED = [
     # sif's API
     "sif_system_init", "sif_system_finalise", "sif_error_message", "sif_error_status",
@@ -57,7 +62,7 @@ EXPORTED = [
     "sifg_exodus_survey_device",
     # device-resident additions
     "sifg_cic_device", "sifg_contrast_device", "sifg_mesh_device", "sifg_smooth_device",
-    "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings",
+    "sifg_exodus_device", "sifg_box_device", "sifg_last_rung_stats", "sifg_last_timings", "sifg_last_trace",
     "sifg_set_window", "sifg_set_growth_mode", "sifg_set_shell_list", "sifg_set_commit_mode", "sifg_set_scan_mode", "sifg_set_witness", "sifg_set_factor_tables", "sifg_set_halt_after",
     "sifg_set_host_mirrors", "sifg_host_mirrors", "sifg_host_modified", "sifg_copy_bytes", "sifg_candidate_ranks", "sifg_stream", "sifg_launch_count",
     "sifg_mesh_device_noalloc",
@@ -109,6 +114,7 @@ def load():
                                   vp, vp, vp, vp, u64, C.POINTER(u64)]),
         "sifg_last_rung_stats": (u32, [C.POINTER(RungStat), u32]),
         "sifg_last_timings": (None, [C.POINTER(Timings)]),
+        "sifg_last_trace": (u32, [C.POINTER(TraceEvent), u32]),
         "sifg_set_window": (None, [i32]),
         "sifg_set_growth_mode": (None, [i32]),
         "sifg_set_shell_list": (None, [i32]),

@@ -265,7 +265,35 @@ static sif_catalogue_t* make_catalogue(const HostCatalogue& c, bool footprint = 
   return cat;
 }
 
+// The last run's timeline (sifg_last_trace).
+static std::vector<sifg_trace_event_t> g_trace;
+
+static void append_trace(KernelTimer& k, int32_t kind, cudaEvent_t origin) {
+  for (size_t i = 0; i < k.stops.size() && i < k.starts.size(); i++) {
+    SIFG_CUDA(cudaEventSynchronize(k.stops[i]));
+    float a = 0.f, b = 0.f;
+    SIFG_CUDA(cudaEventElapsedTime(&a, origin, k.starts[i]));
+    SIFG_CUDA(cudaEventElapsedTime(&b, origin, k.stops[i]));
+    g_trace.push_back(sifg_trace_event_t{kind, a, b});
+  }
+}
+
+static void record_trace(RunTimings& t) {
+  g_trace.clear();
+  if (!t.origin) return;
+  SIFG_CUDA(cudaEventSynchronize(t.origin));
+  append_trace(t.cic, SIFG_TRACE_CIC, t.origin);
+  append_trace(t.mesh, SIFG_TRACE_MESH, t.origin);
+  append_trace(t.smoothing, SIFG_TRACE_SMOOTHING, t.origin);
+  append_trace(t.filter, SIFG_TRACE_FILTER, t.origin);
+  append_trace(t.rung, SIFG_TRACE_RUNG, t.origin);
+  append_trace(t.witness, SIFG_TRACE_WITNESS, t.origin);
+  append_trace(t.growth, SIFG_TRACE_GROWTH, t.origin);
+  append_trace(t.commit, SIFG_TRACE_COMMIT, t.origin);
+}
+
 static void record_timings(RunTimings& t) {
+  record_trace(t);
   g_timings.wall_ms = t.wall_ms;
   g_timings.growth_ms = t.growth.total_ms();
   g_timings.growth_launches = t.growth.launches();
@@ -1866,6 +1894,7 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
   // when the run ends, not waited for: every stage indexes safely whatever
   // the positions, and a run over positions outside the box returns the
   // range error and no catalogue.
+  tm.mark_origin(s);
   unsigned long long* outside = (unsigned long long*)io.flag.ensure(16);
   SIFG_CUDA(cudaMemsetAsync(outside, 0, 16, s));
   R bounds[2];
@@ -1873,7 +1902,9 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
   // The mesh is built on the copy stream with its own scratch, beside the
   // deposit proper (bound by shared-memory atomics, not by HBM: it starts
   // once the deposit's tile sort has streamed the particles) and the first
-  // smoothings; the run waits for it before its first sphere growth.
+  // smoothings; the run waits for it before its first sphere growth. (Queued
+  // after the forward transform instead, it took as much time from the first
+  // rungs' smoothing as it gave the transform.)
   cudaStream_t cs = e->copy_stream();
   struct CopyDrain {
     cudaStream_t s;
@@ -2284,6 +2315,14 @@ uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
 
 void sifg_last_timings(sifg_timings_t* out) {
   if (out) *out = g_timings;
+}
+
+uint32_t sifg_last_trace(sifg_trace_event_t* out, uint32_t capacity) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const uint32_t n = (uint32_t)g_trace.size();
+  if (out)
+    for (uint32_t i = 0; i < n && i < capacity; i++) out[i] = g_trace[i];
+  return n;
 }
 
 uint64_t sifg_launch_count(void) { return g_kernel_launches.load(); }

@@ -438,6 +438,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
                    HostCatalogueT<R>& out, std::vector<RungStat>* stats, RunTimings* tm) {
   SmootherT<R>& smoother = smoother_for<R>();
   const auto t_start = std::chrono::steady_clock::now();
+  if (tm) tm->mark_origin(st_);
   // The run appends one entry to stats per rung it runs (from first_rung).
   const size_t stats0 = stats ? stats->size() : 0;
   const uint32_t N = p.grid_n;
@@ -559,6 +560,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
   bool listed = false;
   auto smooth_rung = [&](uint32_t ri) {
     SIFG_CUDA(cudaStreamWaitEvent(st_fft_, ev_scanned_[ri % 2], 0));
+    if (tm) tm->smoothing.begin(st_fft_);
     // With the list, the field's only other reader is SIF_FINDER_CONSUME_GRID
     // (the last rung's): the other rungs' fields are not written.
     if (listed) below[ri % 2].field = p.consume_out && ri + 1 == radii.size();
@@ -575,6 +577,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       rsmoother.smooth(kFilterTopHat, radii[ri], 0.0f, rfields[ri % 2], nullptr);
       survey_contrast(fields[ri % 2], (const R*)rfields[ri % 2], occ, p.survey_alpha, cells, st_fft_);
     }
+    if (tm) tm->smoothing.end(st_fft_);
     SIFG_CUDA(cudaEventRecord(ev_smoothed_[ri % 2], st_fft_));
   };
   // On every way out, nothing of the run is left in flight on the smoothing
@@ -849,6 +852,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       if (ri + 1 < radii.size()) smooth_rung(ri + 1);
       SIFG_CUDA(cudaStreamWaitEvent(st_, ev_smoothed_[ri % 2], 0));
     }
+    if (tm) tm->rung.begin(st_);
 
     // 2. Candidates, in flat order.
     R* region_delta = nullptr;
@@ -910,6 +914,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     if (m == 0) {
       // The list's last reader was its count pass.
       if (listed) SIFG_CUDA(cudaEventRecord(ev_scanned_[ri % 2], st_));
+      if (tm) tm->rung.end(st_);
       rs.rung_ms = ms_since(t_rung);
       if (stats) stats->push_back(rs);
       if (const int hs = rung_done(ri + 1, 0); hs != kOk) return hs;
@@ -1107,6 +1112,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       n_voids = h_counters_[0];
       build_void_index(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), n_voids, box, vstart,
                        vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
+      if (tm) tm->rung.end(st_);
       rs.commit_ms = ms_since(t_commit);
       rs.n_survivors = m;
       rs.n_accepted = n_acc;
@@ -1179,6 +1185,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       build_void_index(cat_x_.as<R>(), cat_y_.as<R>(), cat_z_.as<R>(), n_voids, box,
                        vstart, vids_.as<uint32_t>(), vcell_.as<uint32_t>(), st_);
     }
+    if (tm) tm->rung.end(st_);
     rs.rung_ms = ms_since(t_rung);
     if (stats) stats->push_back(rs);
     if (const int hs = rung_done(ri + 1, rs.n_mismatched); hs != kOk) return hs;

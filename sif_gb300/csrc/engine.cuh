@@ -89,8 +89,17 @@ struct RungStat {
 
 struct RunTimings {
   KernelTimer growth, filter, cic, mesh, witness, commit;
+  KernelTimer smoothing, rung;  // the timeline's stage spans
+  cudaEvent_t origin = nullptr;  // the run's first event: the timeline's zero
   double wall_ms = 0.0;
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the sphere growth
+  void mark_origin(cudaStream_t st) {
+    if (origin) return;
+    if (cudaEventCreate(&origin) != cudaSuccess || cudaEventRecord(origin, st) != cudaSuccess) {
+      if (origin) cudaEventDestroy(origin);
+      origin = nullptr;
+    }
+  }
   void reset() {
     growth_particles = growth_cells = 0;
     growth.reset();
@@ -99,7 +108,17 @@ struct RunTimings {
     filter.reset();
     cic.reset();
     mesh.reset();
+    smoothing.reset();
+    rung.reset();
+    if (origin) cudaEventDestroy(origin);
+    origin = nullptr;
     wall_ms = 0.0;
+  }
+  RunTimings() = default;
+  RunTimings(const RunTimings&) = delete;
+  RunTimings& operator=(const RunTimings&) = delete;
+  ~RunTimings() {
+    if (origin) cudaEventDestroy(origin);
   }
 };
 

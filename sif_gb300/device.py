@@ -234,6 +234,19 @@ def last_timings():
     return {f: getattr(t, f) for f, _ in _lib.Timings._fields_}
 
 
+TRACE_KINDS = ("growth", "filter", "cic", "mesh", "witness", "commit", "smoothing", "rung")
+
+
+def last_trace():
+    """The last run's timeline (sifg_last_trace): (kind, start_ms, end_ms)
+    spans after the run's first event, kind by kind in the order recorded."""
+    lib = _lib.load()
+    n = lib.sifg_last_trace(None, 0)
+    buf = (_lib.TraceEvent * max(n, 1))()
+    n = min(n, lib.sifg_last_trace(buf, n))
+    return [(TRACE_KINDS[e.kind], e.start_ms, e.end_ms) for e in buf[:n]]
+
+
 def stream():
     """The library's CUDA stream as a torch stream, for events on it."""
     import torch

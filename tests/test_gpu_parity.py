@@ -570,3 +570,29 @@ def test_box_candidates_from_the_smoothing_list(dev, options, overlap):
     assert all(listed[0]) and not any(listed[1])
     assert len(cats[0][0]) > 100
     assert len(cats[0][0]) == len(cats[1][0]) and same_catalogue(cats[0], cats[1])
+
+
+def test_last_run_timeline(dev):
+    """sifg_last_trace after a box run: a span per rung on the run's stream,
+    in order and not overlapping, a smoothing span per rung, and as many
+    growth and commit spans as the run's timings count, each after its
+    rung's start."""
+    import torch
+
+    x, y, z = synth.zeldovich(64, 250.0, 4.0, 31, backend="torch")
+    xs = [torch.from_numpy(a).cuda() for a in (x, y, z)]
+    radii = synth.ladder(5.0, 20.0, 0.1).astype(np.float32)
+    cat = dev.box(*xs, 64, 250.0, 25, radii, -0.75)
+    assert len(cat[0]) > 0
+    trace = dev.last_trace()
+    tm = dev.last_timings()
+    by = {k: [(a, b) for kk, a, b in trace if kk == k] for k in dev.TRACE_KINDS}
+    assert all(0.0 <= a <= b for _, a, b in trace)
+    rungs = by["rung"]
+    assert len(rungs) == len(radii) == len(by["smoothing"])
+    assert all(b0 <= a1 for (_, b0), (a1, _) in zip(rungs, rungs[1:]))
+    assert len(by["growth"]) == tm["growth_launches"] > 0
+    assert len(by["commit"]) == tm["commit_launches"] > 0
+    assert len(by["cic"]) == 1 and len(by["mesh"]) == 1
+    assert by["cic"][0][1] <= rungs[0][0]
+    assert all(any(a >= r0 and b <= r1 for r0, r1 in rungs) for a, b in by["growth"])
