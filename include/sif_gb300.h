@@ -415,6 +415,9 @@ typedef struct {
   int witness_launches;
   double commit_ms; /* the commit's rounds, kernel time on the run's stream */
   int commit_launches;
+  /* The box path's whole deposit: the tile sort, the deposit kernel (cic_ms)
+   * and the faces' fix-up. */
+  double cic_stage_ms;
 } sifg_timings_t;
 
 /* One span of the last run's timeline: a tracked launch (or stage) with its
@@ -428,7 +431,8 @@ typedef enum {
   SIFG_TRACE_WITNESS = 4,   /* a collision-witness launch */
   SIFG_TRACE_COMMIT = 5,    /* a commit launch (its rounds) */
   SIFG_TRACE_SMOOTHING = 6, /* a rung's whole smoothing (smoothing stream) */
-  SIFG_TRACE_RUNG = 7       /* a rung on the run's stream, from its field's arrival */
+  SIFG_TRACE_RUNG = 7,      /* a rung on the run's stream, from its field's arrival */
+  SIFG_TRACE_CIC_STAGE = 8  /* the box path's whole deposit (tile sort, deposit, faces) */
 } sifg_trace_kind_t;
 typedef struct {
   int32_t kind; /* sifg_trace_kind_t */

@@ -40,7 +40,8 @@ class Timings(C.Structure):
                 ("mesh_ms", C.c_double), ("mesh_launches", C.c_int),
                 ("growth_particles", C.c_uint64), ("growth_cells", C.c_uint64),
                 ("witness_ms", C.c_double), ("witness_launches", C.c_int),
-                ("commit_ms", C.c_double), ("commit_launches", C.c_int)]
+                ("commit_ms", C.c_double), ("commit_launches", C.c_int),
+                ("cic_stage_ms", C.c_double)]
 
 
 class TraceEvent(C.Structure):

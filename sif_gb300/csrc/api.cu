@@ -290,6 +290,7 @@ static void record_trace(RunTimings& t) {
   append_trace(t.witness, SIFG_TRACE_WITNESS, t.origin);
   append_trace(t.growth, SIFG_TRACE_GROWTH, t.origin);
   append_trace(t.commit, SIFG_TRACE_COMMIT, t.origin);
+  append_trace(t.cic_stage, SIFG_TRACE_CIC_STAGE, t.origin);
 }
 
 static void record_timings(RunTimings& t) {
@@ -309,6 +310,7 @@ static void record_timings(RunTimings& t) {
   g_timings.witness_launches = t.witness.launches();
   g_timings.commit_ms = t.commit.total_ms();
   g_timings.commit_launches = t.commit.launches();
+  g_timings.cic_stage_ms = t.cic_stage.total_ms();
 }
 
 // The API lock, for entry points outside this file that hold it for a whole
@@ -1914,7 +1916,7 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
   if constexpr (sizeof(R) == 4) {
     e->scratch.ensure(cic_scratch_bytes(n, n_grid));
     cic_deposit(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic, bounds, outside,
-                e->ev_copy_start());
+                e->ev_copy_start(), nullptr, &tm.cic_stage);
   } else {
     box_check_kernel<R><<<grid_for(n, 256), 256, 0, s>>>(x, y, z, n, bounds[0], bounds[1], outside);
     SIFG_LAUNCH_CHECK();

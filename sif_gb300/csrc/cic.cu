@@ -701,7 +701,7 @@ size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n, bool weighted) {
 void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_particles,
                  uint32_t n, float box, float* grid, void* scratch, cudaStream_t st,
                  KernelTimer* timer, const float* bounds, unsigned long long* outside,
-                 cudaEvent_t sorted, const float* w) {
+                 cudaEvent_t sorted, const float* w, KernelTimer* stage) {
   const CicGeom g = make_geom(n, box);
   const uint64_t nt = g.nt, tiles = nt * nt * nt;
   char* p = (char*)scratch;
@@ -721,6 +721,8 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   float* wrec = w ? (float*)take(n_particles * sizeof(float)) : nullptr;
   unsigned* wmax = w ? (unsigned*)take(2 * sizeof(unsigned)) : nullptr;
 
+  // The stage: the tile sort, the deposit proper and the faces' fix-up.
+  if (stage) stage->begin(st);
   SIFG_CUDA(cudaMemsetAsync(counts, 0, (tiles + 1) * sizeof(uint32_t), st));
   SIFG_CUDA(cudaMemsetAsync(faces.fx, 0, face_elems * 8, st));
   SIFG_CUDA(cudaMemsetAsync(faces.fy, 0, face_elems * 8, st));
@@ -760,6 +762,7 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
   face_fixup_kernel<<<grid_for(3 * face_elems, 256), 256, 0, st>>>(g, inv_cell_vol, grid, faces,
                                                                   wmax);
   SIFG_LAUNCH_CHECK();
+  if (stage) stage->end(st);
   if (w) {
     nonfinite_weights_kernel<<<grd, blk, 0, st>>>(x, y, z, w, n_particles, g, wmax, grid);
     SIFG_LAUNCH_CHECK();

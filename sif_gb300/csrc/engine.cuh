@@ -90,6 +90,7 @@ struct RungStat {
 struct RunTimings {
   KernelTimer growth, filter, cic, mesh, witness, commit;
   KernelTimer smoothing, rung;  // the timeline's stage spans
+  KernelTimer cic_stage;        // the whole deposit: tile sort, deposit, faces
   cudaEvent_t origin = nullptr;  // the run's first event: the timeline's zero
   double wall_ms = 0.0;
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the sphere growth
@@ -110,6 +111,7 @@ struct RunTimings {
     mesh.reset();
     smoothing.reset();
     rung.reset();
+    cic_stage.reset();
     if (origin) cudaEventDestroy(origin);
     origin = nullptr;
     wall_ms = 0.0;

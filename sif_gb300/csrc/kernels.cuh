@@ -92,7 +92,7 @@ void cic_deposit(const float* x, const float* y, const float* z, uint64_t n_part
                  uint32_t n, float box, float* grid, void* scratch, cudaStream_t st,
                  KernelTimer* timer, const float* bounds = nullptr,
                  unsigned long long* outside = nullptr, cudaEvent_t sorted = nullptr,
-                 const float* w = nullptr);
+                 const float* w = nullptr, KernelTimer* stage = nullptr);
 // The FP64 form's deposit: scratch is cic_f64_scratch_bytes(n).
 size_t cic_f64_scratch_bytes(uint32_t n);
 void cic_deposit_f64(const double* x, const double* y, const double* z, uint64_t n_particles,

@@ -100,27 +100,33 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(uint32_t* __re
 
 constexpr uint32_t kSmallChunks = 8;
 
+// Every chunk is loaded before the first is scanned: the loads of all
+// kSmallChunks chunks are in flight at once (the scans of the path's block
+// totals sit between dependent launches, so this CTA's latency is theirs).
 __global__ void __launch_bounds__(kScanThreads) scan_small_kernel(uint32_t* __restrict__ d,
                                                                   uint32_t n) {
   __shared__ uint32_t ws[32];
+  uint32_t v[kSmallChunks][kScanItems];
+#pragma unroll
+  for (uint32_t c = 0; c < kSmallChunks; c++) {
+    const uint32_t first = c * kScanChunk + threadIdx.x * kScanItems;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) v[c][k] = first + k < n ? d[first + k] : 0u;
+  }
   uint32_t carry = 0;
-  for (uint32_t base = 0; base < n; base += kScanChunk) {
-    const uint32_t first = base + threadIdx.x * kScanItems;
-    uint32_t v[kScanItems];
+#pragma unroll
+  for (uint32_t c = 0; c < kSmallChunks; c++) {
+    if (c * kScanChunk >= n) break;  // uniform across the CTA
+    const uint32_t first = c * kScanChunk + threadIdx.x * kScanItems;
     uint32_t acc = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-      const uint32_t i = first + k;
-      v[k] = i < n ? d[i] : 0u;
-      acc += v[k];
-    }
+    for (int k = 0; k < kScanItems; k++) acc += v[c][k];
     uint32_t total;
     uint32_t run = block_exclusive_scan(acc, ws, total) + carry;
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) {
-      const uint32_t i = first + k;
-      if (i < n) d[i] = run;
-      run += v[k];
+      if (first + k < n) d[first + k] = run;
+      run += v[c][k];
     }
     carry += total;
   }

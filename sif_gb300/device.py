@@ -234,7 +234,8 @@ def last_timings():
     return {f: getattr(t, f) for f, _ in _lib.Timings._fields_}
 
 
-TRACE_KINDS = ("growth", "filter", "cic", "mesh", "witness", "commit", "smoothing", "rung")
+TRACE_KINDS = ("growth", "filter", "cic", "mesh", "witness", "commit", "smoothing", "rung",
+               "cic_stage")
 
 
 def last_trace():

@@ -593,6 +593,8 @@ def test_last_run_timeline(dev):
     assert all(b0 <= a1 for (_, b0), (a1, _) in zip(rungs, rungs[1:]))
     assert len(by["growth"]) == tm["growth_launches"] > 0
     assert len(by["commit"]) == tm["commit_launches"] > 0
-    assert len(by["cic"]) == 1 and len(by["mesh"]) == 1
-    assert by["cic"][0][1] <= rungs[0][0]
+    assert len(by["cic"]) == 1 and len(by["mesh"]) == 1 and len(by["cic_stage"]) == 1
+    stage = by["cic_stage"][0]
+    assert stage[0] <= by["cic"][0][0] and by["cic"][0][1] <= stage[1] <= rungs[0][0]
+    assert abs(tm["cic_stage_ms"] - (stage[1] - stage[0])) < 1e-3
     assert all(any(a >= r0 and b <= r1 for r0, r1 in rungs) for a, b in by["growth"])
