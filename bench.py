@@ -189,13 +189,14 @@ def gpu_arm(args, rank, world):
         start.record(stream)
         for _ in range(args.steps):
             step()
-            timings.append(device.last_timings())
         end.record(stream)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
     ms = start.elapsed_time(end) / args.steps
     launches = (device.launch_count() - launches0) // args.steps
+    # The last step's kernel timings, read after the timed region.
+    timings.append(device.last_timings())
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -252,7 +253,7 @@ def gpu_arm(args, rank, world):
 
     cpu = None
     if rank == 0 and not args.no_cpu and not args.small:
-        cpu = cpu_run(x, y, z, w, radii, steps=1, warmup=0)
+        cpu = cpu_run(x, y, z, w, radii, steps=3, warmup=1)
 
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,

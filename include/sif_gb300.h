@@ -624,7 +624,10 @@ int sifg_box_batch_device(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t n_engi
  * job count, to a factor of two) and returns it in *n_engines. The catalogues
  * do not depend on the choice. */
 int sifg_box_batch_autotune(sifg_box_job_t* jobs, uint32_t n_jobs, uint32_t* n_engines);
-/* Statistics and timings of the last run (up to max_rungs entries). */
+/* Statistics and timings of the last run (up to max_rungs entries). A run
+ * keeps its timing events; the first of sifg_last_timings and
+ * sifg_last_trace after it reads them (waiting for the run's last event),
+ * so that runs back to back pay nothing for timings nobody reads. */
 uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs);
 void sifg_last_timings(sifg_timings_t* out);
 /* The last run's timeline: copies up to `capacity` spans (in the order

@@ -293,9 +293,17 @@ static void record_trace(RunTimings& t) {
   append_trace(t.cic_stage, SIFG_TRACE_CIC_STAGE, t.origin);
 }
 
-static void record_timings(RunTimings& t) {
+// The last run's events, kept until its timings or its timeline are asked
+// for: reading them (a synchronize and an elapsed time per event) between
+// runs would leave the GPU idle meanwhile.
+static RunTimings g_last_run;
+static bool g_last_pending = false;
+
+static void resolve_timings() {
+  if (!g_last_pending) return;
+  g_last_pending = false;
+  RunTimings& t = g_last_run;
   record_trace(t);
-  g_timings.wall_ms = t.wall_ms;
   g_timings.growth_ms = t.growth.total_ms();
   g_timings.growth_launches = t.growth.launches();
   g_timings.filter_ms = t.filter.total_ms();
@@ -304,13 +312,31 @@ static void record_timings(RunTimings& t) {
   g_timings.cic_launches = t.cic.launches();
   g_timings.mesh_ms = t.mesh.total_ms();
   g_timings.mesh_launches = t.mesh.launches();
-  g_timings.growth_particles = t.growth_particles;
-  g_timings.growth_cells = t.growth_cells;
   g_timings.witness_ms = t.witness.total_ms();
   g_timings.witness_launches = t.witness.launches();
   g_timings.commit_ms = t.commit.total_ms();
   g_timings.commit_launches = t.commit.launches();
   g_timings.cic_stage_ms = t.cic_stage.total_ms();
+  t.reset();
+}
+
+// A stage timed and read at once (a single-stage call) supersedes a run's
+// timings that were not read.
+static void drop_pending_timings() {
+  if (!g_last_pending) return;
+  g_last_pending = false;
+  g_last_run.reset();
+  g_trace.clear();
+}
+
+static void record_timings(RunTimings& t) {
+  drop_pending_timings();
+  g_timings = sifg_timings_t{};
+  g_timings.wall_ms = t.wall_ms;
+  g_timings.growth_particles = t.growth_particles;
+  g_timings.growth_cells = t.growth_cells;
+  g_last_run.swap_events(t);
+  g_last_pending = true;
 }
 
 // The API lock, for entry points outside this file that hold it for a whole
@@ -377,6 +403,7 @@ int sif_system_init(sif_config_t* config) {
 void sif_system_finalise(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   noalloc_forget();
+  drop_pending_timings();
   mirror_clear();  // device memory goes with the engine; the switch stays
   g_engine.reset();
   host_pool_trim();
@@ -1612,6 +1639,7 @@ static int cic_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t n
     cic_deposit_f64(x, y, z, n, n_grid, box, grid, e->scratch.ptr, s, &tm.cic, w);
   }
   SIFG_CUDA(cudaStreamSynchronize(s));
+  drop_pending_timings();
   g_timings.cic_ms = tm.cic.total_ms();
   g_timings.cic_launches = tm.cic.launches();
   return SIF_OK;
@@ -1655,6 +1683,7 @@ static int mesh_device(const R* x, const R* y, const R* z, uint64_t n, uint32_t 
   RunTimings tm;
   mesh_build(x, y, z, n, m, e->scratch.ptr, s, &tm.mesh);
   SIFG_CUDA(cudaStreamSynchronize(s));
+  drop_pending_timings();
   g_timings.mesh_ms = tm.mesh.total_ms();
   g_timings.mesh_launches = tm.mesh.launches();
   return SIF_OK;
@@ -1672,6 +1701,7 @@ static int smooth_device(const R* delta, uint32_t n_grid, R box, R r, int filter
   RunTimings tm;
   sm.smooth(filter, r, R(0), out, &tm.filter);
   SIFG_CUDA(cudaStreamSynchronize(s));
+  drop_pending_timings();
   g_timings.filter_ms = tm.filter.total_ms();
   g_timings.filter_launches = tm.filter.launches();
   return SIF_OK;
@@ -2316,11 +2346,22 @@ uint32_t sifg_last_rung_stats(sifg_rung_stat_t* out, uint32_t max_rungs) {
 }
 
 void sifg_last_timings(sifg_timings_t* out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  try {
+    resolve_timings();
+  } catch (const CudaError&) {
+    g_last_run.reset();
+  }
   if (out) *out = g_timings;
 }
 
 uint32_t sifg_last_trace(sifg_trace_event_t* out, uint32_t capacity) {
   std::lock_guard<std::mutex> lk(g_mu);
+  try {
+    resolve_timings();
+  } catch (const CudaError&) {
+    g_last_run.reset();
+  }
   const uint32_t n = (uint32_t)g_trace.size();
   if (out)
     for (uint32_t i = 0; i < n && i < capacity; i++) out[i] = g_trace[i];

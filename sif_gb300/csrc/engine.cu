@@ -1056,8 +1056,11 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
       uint32_t* sg_start = grow_to<uint32_t>(sgrid_start_, sg_cells + 1);
       uint32_t* sg_ids = grow_to<uint32_t>(sgrid_ids_, m);
       uint32_t* sg_cell = grow_to<uint32_t>(sgrid_cellof_, m);
-      build_survivor_grid(scx, scy, scz, dcount + 1, m, ng, box, sg_start, sg_ids, sg_cell, st_);
-      sg = SurvivorGridT<R>{sg_start, sg_ids, ng, (R)ng / box};
+      SurvPackT<R>* sg_pack = grow_to<SurvPackT<R>>(sgrid_pack_, m);
+      build_survivor_grid(scx, scy, scz, (const R*)sr, dcount + 1, m, ng, box, sg_start, sg_ids,
+                          sg_cell, sg_pack, st_);
+      sg = SurvivorGridT<R>{sg_start, sg_ids, ng, (R)ng / box, sg_pack,
+                            grow_to<uint32_t>(sgrid_rank_, m)};
       sa = grow_to<uint8_t>(state_a_, m);
       sb = grow_to<uint8_t>(state_b_, m);
       acc = grow_to<uint32_t>(acc_, m);
@@ -1074,6 +1077,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
     rs.sort_ms = ms_since(t_sort);
     uint32_t* rank = grow_to<uint32_t>(rank_, m);
     SIFG_CUDA(cudaMemcpyAsync(rank, h_rank_, m * sizeof(uint32_t), cudaMemcpyHostToDevice, st_));
+    if (!displace) survivor_grid_ranks(sv, rank, sg.ids, (uint32_t*)sg.hrank, m, st_);
 
     // 6. The commit, in rounds; under displacement one survivor at a time.
     const auto t_commit = clk::now();

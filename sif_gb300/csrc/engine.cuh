@@ -116,6 +116,17 @@ struct RunTimings {
     origin = nullptr;
     wall_ms = 0.0;
   }
+  // Exchanges every timer's events and the origin with o's (the plain
+  // counts are not exchanged).
+  void swap_events(RunTimings& o) {
+    for (auto [a, b] : {std::pair<KernelTimer*, KernelTimer*>{&growth, &o.growth},
+                        {&filter, &o.filter}, {&cic, &o.cic}, {&mesh, &o.mesh},
+                        {&witness, &o.witness}, {&commit, &o.commit},
+                        {&smoothing, &o.smoothing}, {&rung, &o.rung},
+                        {&cic_stage, &o.cic_stage}})
+      a->swap(*b);
+    std::swap(origin, o.origin);
+  }
   RunTimings() = default;
   RunTimings(const RunTimings&) = delete;
   RunTimings& operator=(const RunTimings&) = delete;
@@ -176,7 +187,7 @@ class Engine {
   DevBuf field_[2], mask_, cand_delta_, cand_flat_, blocks_, rank_, rank_slots_, alive_;
   DevBuf surv_cand_, surv_flat_, scx_, scy_, scz_, sr_, sreason_, state_a_, state_b_, acc_;
   DevBuf commit_bar_;  // the cooperative commit's grid barrier and its report
-  DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_;
+  DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_, sgrid_pack_, sgrid_rank_;
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
   DevBuf vhead_, vnext_, dlist_;  // displacement: the linked void index, its lists
   DevBuf work_;  // the sphere growth's and the witness's survivor queues

@@ -2597,9 +2597,42 @@ __global__ void scatter_ids_kernel(const uint32_t* __restrict__ cell_of, const u
 }
 
 template <class R>
-void build_survivor_grid(const R* scx, const R* scy, const R* scz,
+__global__ void scatter_survivors_kernel(const uint32_t* __restrict__ cell_of,
+                                         const uint32_t* __restrict__ cnt,
+                                         uint32_t* __restrict__ cursor, uint32_t* __restrict__ ids,
+                                         const R* __restrict__ x, const R* __restrict__ y,
+                                         const R* __restrict__ z, const R* __restrict__ r,
+                                         SurvPackT<R>* __restrict__ pack) {
+  const uint32_t n = *cnt;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t k = atomicAdd(cursor + cell_of[i], 1u);
+    ids[k] = i;
+    pack[k] = SurvPackT<R>{x[i], y[i], z[i], r[i]};
+  }
+}
+
+template <class R>
+__global__ void survivor_ranks_kernel(SurvivorsT<R> sv, const uint32_t* __restrict__ rank,
+                                      const uint32_t* __restrict__ ids,
+                                      uint32_t* __restrict__ hrank) {
+  const uint32_t n = *sv.count;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    hrank[k] = rank[sv.cand[ids[k]]];
+}
+
+template <class R>
+void survivor_grid_ranks(SurvivorsT<R> s, const uint32_t* rank, const uint32_t* ids,
+                         uint32_t* hrank, uint32_t max_survivors, cudaStream_t st) {
+  if (max_survivors == 0) return;
+  survivor_ranks_kernel<R><<<grid_for(max_survivors, 256), 256, 0, st>>>(s, rank, ids, hrank);
+  SIFG_LAUNCH_CHECK();
+}
+
+template <class R>
+void build_survivor_grid(const R* scx, const R* scy, const R* scz, const R* sr,
                          const uint32_t* d_count, uint32_t max_survivors, int32_t ng, R box,
-                         uint32_t* start, uint32_t* ids, uint32_t* cell_of, cudaStream_t st) {
+                         uint32_t* start, uint32_t* ids, uint32_t* cell_of, SurvPackT<R>* pack,
+                         cudaStream_t st) {
   const uint32_t cells = (uint32_t)(ng * ng * ng);
   SIFG_CUDA(cudaMemsetAsync(start, 0, (cells + 1) * sizeof(uint32_t), st));
   if (max_survivors == 0) return;
@@ -2611,7 +2644,8 @@ void build_survivor_grid(const R* scx, const R* scy, const R* scz,
   thread_local DevBuf cursor;  // one per host thread driving a stream
   uint32_t* cur = (uint32_t*)cursor.ensure((cells + 1) * sizeof(uint32_t));
   SIFG_CUDA(cudaMemcpyAsync(cur, start, (cells + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
-  scatter_ids_kernel<<<grid_for(max_survivors, 256), 256, 0, st>>>(cell_of, d_count, 0, cur, ids);
+  scatter_survivors_kernel<R><<<grid_for(max_survivors, 256), 256, 0, st>>>(
+      cell_of, d_count, cur, ids, scx, scy, scz, sr, pack);
   SIFG_LAUNCH_CHECK();
 }
 
@@ -2675,7 +2709,10 @@ __device__ __forceinline__ void commit_pass(const SurvivorsT<R>& sv, const uint3
       const int32_t pole = (int32_t)(fdiv(fmul(fmul(rc.scale, r), fsub(R(1.0f), rc.f)), rc.cell)) - 1;
       if (pole > 0 && overlap_quick(mask, nn, ix, iy, iz, (uint32_t)pole)) reject = true;
     }
-    // Voids accepted this rung, from the survivor hash.
+    // Voids accepted this rung, from the survivor hash: the 27 cells' ranges
+    // loaded together first, then each neighbour's centre and radius (one
+    // load, in the hash's order); only a neighbour within reach -- the reach
+    // of every test, the exact overlap's included -- has its state read.
     bool ready = true;
     if (!reject) {
       const uint32_t my_rank = rank[sv.cand[i]];
@@ -2683,35 +2720,42 @@ __device__ __forceinline__ void commit_pass(const SurvivorsT<R>& sv, const uint3
       const int32_t ng = g.ng;
       const int32_t hx = hash_axis(cx, g.inv_cell, ng), hy = hash_axis(cy, g.inv_cell, ng),
                     hz = hash_axis(cz, g.inv_cell, ng);
-      const int32_t span = ng >= 3 ? 1 : 0;  // a hash coarser than 3 cells is one cell
-      for (int32_t ax = -span; ax <= span && !reject; ax++)
-        for (int32_t ay = -span; ay <= span && !reject; ay++)
-          for (int32_t az = -span; az <= span && !reject; az++) {
-            const uint32_t c = (uint32_t)(((hx + ax + ng) % ng) * ng + (hy + ay + ng) % ng) * ng +
-                               (uint32_t)((hz + az + ng) % ng);
-            const uint32_t e = g.start[c + 1];
-            for (uint32_t k = g.start[c]; k < e; k++) {
-              const uint32_t j = g.ids[k];
-              if (j == i) continue;
-              const uint8_t sj = __ldcg(st_in + j);
-              if (sj == kRejected) continue;
-              const R jx = sv.cx[j], jy = sv.cy[j], jz = sv.cz[j], rj = sv.r[j];
-              if (sj == kAccepted) {
-                // A same-rung void: the exact pair test (its search box is
-                // the reference's at the rung's largest radius; the minimum
-                // image form agrees with the interior one wherever it
-                // applies, since neither reaches half the box).
-                if (collide(cx, cy, cz, r, jx, jy, jz, rj, rc.f, rc.scale, rc.box, half,
-                            interior_all)) {
-                  reject = true;
-                  break;
-                }
-              } else if (ready && rank[sv.cand[j]] < my_rank &&
-                         interacts(cx, cy, cz, r, jx, jy, jz, rj, rc)) {
-                ready = false;
-              }
-            }
+      const bool one = ng < 3;  // a hash coarser than 3 cells is one cell
+      uint32_t lo[27], hi[27];
+#pragma unroll
+      for (int q = 0; q < 27; q++) {
+        lo[q] = hi[q] = 0;
+        if (one ? q == 13 : true) {
+          const int32_t ax = q / 9 - 1, ay = (q / 3) % 3 - 1, az = q % 3 - 1;
+          const uint32_t c = one ? 0u
+                                 : (uint32_t)(((hx + ax + ng) % ng) * ng + (hy + ay + ng) % ng) * ng +
+                                       (uint32_t)((hz + az + ng) % ng);
+          lo[q] = g.start[c];
+          hi[q] = g.start[c + 1];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 27; q++) {
+        for (uint32_t k = lo[q]; k < hi[q] && !reject; k++) {
+          const SurvPackT<R> p = g.pack[k];
+          if (!interacts(cx, cy, cz, r, p.x, p.y, p.z, p.r, rc)) continue;
+          const uint32_t j = g.ids[k];
+          if (j == i) continue;
+          const uint8_t sj = __ldcg(st_in + j);
+          if (sj == kRejected) continue;
+          if (sj == kAccepted) {
+            // A same-rung void: the exact pair test (its search box is the
+            // reference's at the rung's largest radius; the minimum image
+            // form agrees with the interior one wherever it applies, since
+            // neither reaches half the box).
+            if (collide(cx, cy, cz, r, p.x, p.y, p.z, p.r, rc.f, rc.scale, rc.box, half,
+                        interior_all))
+              reject = true;
+          } else if (ready && g.hrank[k] < my_rank) {
+            ready = false;
           }
+        }
+      }
     }
     uint8_t out = kUndecided;
     if (reject) {
@@ -3456,8 +3500,11 @@ void compact_voids(R* cx, R* cy, R* cz, R* r, uint32_t* state, cudaStream_t st) 
   template void grow<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>, uint32_t,   \
                         R*, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*, uint8_t,    \
                         uint32_t*);                                                                \
-  template void build_survivor_grid<R>(const R*, const R*, const R*, const uint32_t*, uint32_t,    \
-                                       int32_t, R, uint32_t*, uint32_t*, uint32_t*, cudaStream_t); \
+  template void build_survivor_grid<R>(const R*, const R*, const R*, const R*, const uint32_t*,    \
+                                       uint32_t, int32_t, R, uint32_t*, uint32_t*, uint32_t*,      \
+                                       SurvPackT<R>*, cudaStream_t);                               \
+  template void survivor_grid_ranks<R>(SurvivorsT<R>, const uint32_t*, const uint32_t*, uint32_t*, \
+                                       uint32_t, cudaStream_t);                                    \
   template void commit_init<R>(SurvivorsT<R>, VoidViewT<R>, RungConstsT<R>, uint8_t*, uint32_t*,     \
                               uint32_t, cudaStream_t);                                              \
   template void commit_round<R>(SurvivorsT<R>, const uint32_t*, SurvivorGridT<R>, VoidViewT<R>,    \

@@ -96,6 +96,13 @@ struct VoidViewT {
   uint32_t n;
 };
 
+// A survivor's centre and rescaled radius, as the commit's neighbour walk
+// reads them: one load a neighbour.
+template <class R>
+struct SurvPackT {
+  R x, y, z, r;
+};
+
 // Survivors of the pre-filter, hashed on a coarse grid for the commit's
 // neighbour queries.
 template <class R>
@@ -104,6 +111,8 @@ struct SurvivorGridT {
   const uint32_t* ids;
   int32_t ng;
   R inv_cell;  // ng / box
+  const SurvPackT<R>* pack;  // each slot's survivor's centre and radius, in the grid's order
+  const uint32_t* hrank;     // and its rank (survivor_grid_ranks, once the order is known)
 };
 
 template <class R>
@@ -301,11 +310,16 @@ void set_growth_mode(int mode);
 // (rounded up to 32, at most 512) on every rung. The radii are the same.
 void set_shell_list(int entries);
 
-// The survivor hash for the commit.
+// The survivor hash for the commit (after the growth: pack holds the radii).
 template <class R>
-void build_survivor_grid(const R* scx, const R* scy, const R* scz, const uint32_t* d_count,
-                         uint32_t max_survivors, int32_t ng, R box, uint32_t* start,
-                         uint32_t* ids, uint32_t* cell_of, cudaStream_t st);
+void build_survivor_grid(const R* scx, const R* scy, const R* scz, const R* sr,
+                         const uint32_t* d_count, uint32_t max_survivors, int32_t ng, R box,
+                         uint32_t* start, uint32_t* ids, uint32_t* cell_of, SurvPackT<R>* pack,
+                         cudaStream_t st);
+// hrank[k] = rank of the survivor in slot k of the hash (rank: the candidates').
+template <class R>
+void survivor_grid_ranks(SurvivorsT<R> s, const uint32_t* rank, const uint32_t* ids,
+                         uint32_t* hrank, uint32_t max_survivors, cudaStream_t st);
 
 // Survivors whose rescaling failed, or whose sphere at the rescaled radius
 // overlaps a void of the catalogue as the rung began (voids), start

@@ -28,6 +28,11 @@ struct KernelTimer {
   double total_ms();  // synchronises; sums every begin/end pair recorded
   int launches() const { return (int)stops.size(); }
   void reset();
+  void swap(KernelTimer& o) {
+    starts.swap(o.starts);
+    stops.swap(o.stops);
+    std::swap(open, o.open);
+  }
   ~KernelTimer();
 };
 
