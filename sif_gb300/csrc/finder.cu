@@ -2682,95 +2682,184 @@ __device__ __forceinline__ bool interacts(R ax, R ay, R az, R ar, R bx,
 // states, the acceptance list, the counters and the mask are read past L1
 // (__ldcg): the persistent form runs rounds in one kernel, where another SM
 // wrote them since the last barrier.
+// A survivor's outcome for the round: state, the accepted list, counters.
+template <class R>
+__device__ __forceinline__ void commit_outcome(uint32_t i, R r, bool reject, bool ready,
+                                               const RungConstsT<R>& rc, uint8_t* st_out,
+                                               uint32_t* acc, uint32_t* counters, uint32_t slot) {
+  uint8_t out = kUndecided;
+  if (reject) {
+    out = kRejected;
+  } else if (ready) {
+    out = kAccepted;
+    acc[atomicAdd(counters, 1u)] = i;
+    store_rmax(counters, r);
+    // More than MISMATCH_RATIO (2) times the rung (exodus_finder.c:233,
+    // 2324-2328): counted for the checkpoint and the run's warning.
+    if (fdiv(r, rc.radius) > R(2.0f)) atomicAdd(counters + 9, 1u);
+  } else {
+    atomicAdd(counters + kRoundUndecided + slot, 1u);
+  }
+  st_out[i] = out;
+}
+
+// The commit's re-checks (exodus_finder.c:2286-2317) that read the mask: the
+// node's bit, the poles at the rescaled radius. (The exact overlap with the
+// catalogue as the rung began is decided once, before the rounds, by
+// commit_init; with the rung's own voids, from the survivor hash.)
+template <class R>
+__device__ __forceinline__ bool commit_mask_reject(const SurvivorsT<R>& sv, uint32_t i, R r,
+                                                   const uint32_t* mask, const RungConstsT<R>& rc) {
+  const uint32_t nn = rc.grid_n;
+  const uint32_t node = sv.flat[i];
+  if (cand_masked(mask, node, sv.off ? sv.off[i] : R(-1.0f), r, rc)) return true;
+  const uint32_t ix = node / (nn * nn), iy = (node / nn) % nn, iz = node % nn;
+  const int32_t pole = (int32_t)(fdiv(fmul(fmul(rc.scale, r), fsub(R(1.0f), rc.f)), rc.cell)) - 1;
+  return pole > 0 && overlap_quick(mask, nn, ix, iy, iz, (uint32_t)pole);
+}
+
+// Cell q (0..26) of the 3^3 hash cells around (hx, hy, hz): its slots.
+template <class R>
+__device__ __forceinline__ void hash_range(const SurvivorGridT<R>& g, int32_t hx, int32_t hy,
+                                           int32_t hz, int q, uint32_t& lo, uint32_t& hi) {
+  const int32_t ng = g.ng;
+  lo = hi = 0;
+  const bool one = ng < 3;  // a hash coarser than 3 cells is one cell
+  if (one && q != 13) return;
+  const int32_t ax = q / 9 - 1, ay = (q / 3) % 3 - 1, az = q % 3 - 1;
+  const uint32_t c = one ? 0u
+                         : (uint32_t)(((hx + ax + ng) % ng) * ng + (hy + ay + ng) % ng) * ng +
+                               (uint32_t)((hz + az + ng) % ng);
+  lo = g.start[c];
+  hi = g.start[c + 1];
+}
+
+// Neighbour k of survivor i in the hash: sets reject on a collision with an
+// accepted void of this rung, clears ready on an undecided lower-ranked
+// survivor within reach. Only a neighbour within reach -- the reach of every
+// test, the exact overlap's included -- has its state read.
+template <class R>
+__device__ __forceinline__ void commit_neighbour(const SurvivorGridT<R>& g, const SurvPackT<R>& p,
+                                                 uint32_t k, uint32_t i, R cx, R cy, R cz, R r,
+                                                 uint32_t my_rank, R half, const RungConstsT<R>& rc,
+                                                 const uint8_t* st_in, bool& reject, bool& ready) {
+  if (!interacts(cx, cy, cz, r, p.x, p.y, p.z, p.r, rc)) return;
+  const uint32_t j = g.ids[k];
+  if (j == i) return;
+  const uint8_t sj = __ldcg(st_in + j);
+  if (sj == kRejected) return;
+  if (sj == kAccepted) {
+    // A same-rung void: the exact pair test (its search box is the
+    // reference's at the rung's largest radius; the minimum image form
+    // agrees with the interior one wherever it applies, since neither
+    // reaches half the box).
+    if (collide(cx, cy, cz, r, p.x, p.y, p.z, p.r, rc.f, rc.scale, rc.box, half, false))
+      reject = true;
+  } else if (ready && g.hrank[k] < my_rank) {
+    ready = false;
+  }
+}
+
+// One round over the undecided survivors: a thread each, reading the 27 hash
+// cells' ranges together and then the neighbours' records kBatch at a time.
+// A survivor inside a crowd (more than kCrowd records in its 27 cells) goes
+// to its block's queue instead, and after the block's pass a warp takes it,
+// the lanes sharing its records: one thread walking a long list held every
+// other block at the barrier that follows the pass. st_in / st_out: the
+// states before and after the round; states, acceptances and the mask are
+// read past L1, since other SMs wrote them since the last barrier.
+constexpr uint32_t kCrowd = 96;
+constexpr uint32_t kCrowdQueue = 512;
 template <class R>
 __device__ __forceinline__ void commit_pass(const SurvivorsT<R>& sv, const uint32_t* __restrict__ rank,
                                             const SurvivorGridT<R>& g, const VoidViewT<R>& voids,
                                             const uint32_t* mask, const RungConstsT<R>& rc,
                                             const uint8_t* st_in, uint8_t* st_out, uint32_t* acc,
                                             uint32_t* counters, uint32_t slot) {
+  __shared__ uint32_t crowd[kCrowdQueue];
+  __shared__ uint32_t n_crowd;
+  if (threadIdx.x == 0) n_crowd = 0;
+  __syncthreads();
   const uint32_t n = *sv.count;
-  const uint32_t nn = rc.grid_n;
   const R half = fmul(rc.box, R(0.5f));
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const unsigned lane = threadIdx.x & 31u;
+  // Warps take 32 consecutive survivors at a time from the round's counter
+  // (counters[kCommitWork], zeroed by the paint that ends each round):
+  // survivors next to one another in the list are next to one another in
+  // space, and a fixed share per block left the blocks over the crowded
+  // voids to finish the pass alone.
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(counters + kCommitWork, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    const uint32_t i = base + lane;
+    if (i >= n) continue;
     const uint8_t s0 = __ldcg(st_in + i);
     if (s0 != kUndecided) {
       st_out[i] = s0;
       continue;
     }
     const R cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i], r = sv.r[i];
-    const uint32_t node = sv.flat[i];
-    const uint32_t ix = node / (nn * nn), iy = (node / nn) % nn, iz = node % nn;
-    // The commit's re-checks (exodus_finder.c:2286-2317), against every void
-    // accepted so far: the node's mask bit, the poles at the rescaled radius,
-    // the exact overlap -- with the catalogue as the rung began, once, before
-    // the rounds (commit_init); with the rung's own voids, below.
-    bool reject = cand_masked(mask, node, sv.off ? sv.off[i] : R(-1.0f), r, rc);
-    if (!reject) {
-      const int32_t pole = (int32_t)(fdiv(fmul(fmul(rc.scale, r), fsub(R(1.0f), rc.f)), rc.cell)) - 1;
-      if (pole > 0 && overlap_quick(mask, nn, ix, iy, iz, (uint32_t)pole)) reject = true;
-    }
-    // Voids accepted this rung, from the survivor hash: the 27 cells' ranges
-    // loaded together first, then each neighbour's centre and radius (one
-    // load, in the hash's order); only a neighbour within reach -- the reach
-    // of every test, the exact overlap's included -- has its state read.
+    bool reject = commit_mask_reject(sv, i, r, mask, rc);
     bool ready = true;
     if (!reject) {
       const uint32_t my_rank = rank[sv.cand[i]];
-      const bool interior_all = false;
-      const int32_t ng = g.ng;
-      const int32_t hx = hash_axis(cx, g.inv_cell, ng), hy = hash_axis(cy, g.inv_cell, ng),
-                    hz = hash_axis(cz, g.inv_cell, ng);
-      const bool one = ng < 3;  // a hash coarser than 3 cells is one cell
-      uint32_t lo[27], hi[27];
+      const int32_t hx = hash_axis(cx, g.inv_cell, g.ng), hy = hash_axis(cy, g.inv_cell, g.ng),
+                    hz = hash_axis(cz, g.inv_cell, g.ng);
+      uint32_t lo[27], hi[27], total = 0;
 #pragma unroll
       for (int q = 0; q < 27; q++) {
-        lo[q] = hi[q] = 0;
-        if (one ? q == 13 : true) {
-          const int32_t ax = q / 9 - 1, ay = (q / 3) % 3 - 1, az = q % 3 - 1;
-          const uint32_t c = one ? 0u
-                                 : (uint32_t)(((hx + ax + ng) % ng) * ng + (hy + ay + ng) % ng) * ng +
-                                       (uint32_t)((hz + az + ng) % ng);
-          lo[q] = g.start[c];
-          hi[q] = g.start[c + 1];
+        hash_range(g, hx, hy, hz, q, lo[q], hi[q]);
+        total += hi[q] - lo[q];
+      }
+      if (total > kCrowd) {
+        const uint32_t at = atomicAdd(&n_crowd, 1u);
+        if (at < kCrowdQueue) {
+          crowd[at] = i;
+          continue;
         }
       }
+      constexpr uint32_t kBatch = 8;
+#pragma unroll 1
+      for (int q = 0; q < 27 && !reject; q++) {
+        const uint32_t e = hi[q];
+        for (uint32_t k0 = lo[q]; k0 < e && !reject; k0 += kBatch) {
+          SurvPackT<R> pb[kBatch];
 #pragma unroll
-      for (int q = 0; q < 27; q++) {
-        for (uint32_t k = lo[q]; k < hi[q] && !reject; k++) {
-          const SurvPackT<R> p = g.pack[k];
-          if (!interacts(cx, cy, cz, r, p.x, p.y, p.z, p.r, rc)) continue;
-          const uint32_t j = g.ids[k];
-          if (j == i) continue;
-          const uint8_t sj = __ldcg(st_in + j);
-          if (sj == kRejected) continue;
-          if (sj == kAccepted) {
-            // A same-rung void: the exact pair test (its search box is the
-            // reference's at the rung's largest radius; the minimum image
-            // form agrees with the interior one wherever it applies, since
-            // neither reaches half the box).
-            if (collide(cx, cy, cz, r, p.x, p.y, p.z, p.r, rc.f, rc.scale, rc.box, half,
-                        interior_all))
-              reject = true;
-          } else if (ready && g.hrank[k] < my_rank) {
-            ready = false;
+          for (uint32_t u = 0; u < kBatch; u++)
+            if (k0 + u < e) pb[u] = g.pack[k0 + u];
+#pragma unroll
+          for (uint32_t u = 0; u < kBatch; u++) {
+            if (k0 + u >= e || reject) break;
+            commit_neighbour(g, pb[u], k0 + u, i, cx, cy, cz, r, my_rank, half, rc, st_in, reject,
+                             ready);
           }
         }
       }
     }
-    uint8_t out = kUndecided;
-    if (reject) {
-      out = kRejected;
-    } else if (ready) {
-      out = kAccepted;
-      acc[atomicAdd(counters, 1u)] = i;
-      store_rmax(counters, r);
-      // More than MISMATCH_RATIO (2) times the rung (exodus_finder.c:233,
-      // 2324-2328): counted for the checkpoint and the run's warning.
-      if (fdiv(r, rc.radius) > R(2.0f)) atomicAdd(counters + 9, 1u);
-    } else {
-      atomicAdd(counters + kRoundUndecided + slot, 1u);
+    commit_outcome(i, r, reject, ready, rc, st_out, acc, counters, slot);
+  }
+  __syncthreads();
+  // The crowded survivors, a warp each.
+  const uint32_t queued = min(n_crowd, kCrowdQueue);
+  for (uint32_t w = threadIdx.x >> 5; w < queued; w += blockDim.x >> 5) {
+    const uint32_t i = crowd[w];
+    const R cx = sv.cx[i], cy = sv.cy[i], cz = sv.cz[i], r = sv.r[i];
+    const uint32_t my_rank = rank[sv.cand[i]];
+    const int32_t hx = hash_axis(cx, g.inv_cell, g.ng), hy = hash_axis(cy, g.inv_cell, g.ng),
+                  hz = hash_axis(cz, g.inv_cell, g.ng);
+    uint32_t lo = 0, hi = 0;
+    if (lane < 27) hash_range(g, hx, hy, hz, (int)lane, lo, hi);
+    bool reject = false, ready = true;
+    for (int q = 0; q < 27; q++) {
+      const uint32_t clo = __shfl_sync(0xffffffffu, lo, q), chi = __shfl_sync(0xffffffffu, hi, q);
+      for (uint32_t k = clo + lane; k < chi && !reject; k += 32)
+        commit_neighbour(g, g.pack[k], k, i, cx, cy, cz, r, my_rank, half, rc, st_in, reject, ready);
     }
-    st_out[i] = out;
+    const bool any_reject = __any_sync(0xffffffffu, reject);
+    const bool all_ready = __all_sync(0xffffffffu, ready);
+    if (lane == 0) commit_outcome(i, r, any_reject, all_ready, rc, st_out, acc, counters, slot);
   }
 }
 
@@ -2829,9 +2918,12 @@ void commit_round(SurvivorsT<R> s, const uint32_t* rank, SurvivorGridT<R> g, Voi
 // paint_sphere with set = 1 (src/finder/utils.c:965-1027) by one warp: every
 // node whose centre lies within scale * r, measured as the reference
 // measures it.
+// part / parts: the warp paints every parts-th 32 of the sphere's columns,
+// from the part-th (several warps share a large sphere).
 template <class R>
 __device__ __forceinline__ void paint_one(R cx, R cy, R cz, R r, uint32_t* mask,
-                                          const RungConstsT<R>& rc, unsigned lane) {
+                                          const RungConstsT<R>& rc, unsigned lane,
+                                          uint32_t part = 0, uint32_t parts = 1) {
   const uint32_t n = rc.grid_n;
   {
     const R rt = fmul(rc.scale, r);
@@ -2841,7 +2933,7 @@ __device__ __forceinline__ void paint_one(R cx, R cy, R cz, R r, uint32_t* mask,
     const int32_t cr = (int32_t)fmul(rt, inv) + 1;
     const int32_t ci = (int32_t)fmul(cx, inv), cj = (int32_t)fmul(cy, inv), ck = (int32_t)fmul(cz, inv);
     const int32_t side = 2 * cr + 1;
-    for (int32_t q = lane; q < side * side; q += 32) {
+    for (int32_t q = lane + 32 * (int32_t)part; q < side * side; q += 32 * (int32_t)parts) {
       const int32_t gx = ci + q / side - cr, gy = cj + q % side - cr;
       R ddx = fabs_(fsub(fmul((R)gx, rc.cell), cx));
       ddx = ddx > half ? fsub(rc.gbox, ddx) : ddx;
@@ -2871,13 +2963,24 @@ __device__ __forceinline__ void paint_pass(const SurvivorsT<R>& sv, const uint32
                                            uint32_t* counters, uint32_t slot, uint32_t* mask,
                                            const RungConstsT<R>& rc) {
   const uint32_t lo = __ldcg(counters + kRoundBegin + slot), hi = __ldcg(counters);
-  // No round accepts while a paint runs: hi is where the next round begins.
-  if (blockIdx.x == 0 && threadIdx.x == 0) counters[kRoundBegin + (slot + 1) % kRoundRing] = hi;
+  // No round accepts while a paint runs: hi is where the next round begins,
+  // and the next round's pass takes its survivors from a counter at zero.
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    counters[kRoundBegin + (slot + 1) % kRoundRing] = hi;
+    counters[kCommitWork] = 0;
+  }
   const unsigned lane = threadIdx.x & 31u;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t a = lo + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); a < hi; a += warps) {
-    const uint32_t i = __ldcg(acc + a);
-    paint_one(sv.cx[i], sv.cy[i], sv.cz[i], sv.r[i], mask, rc, lane);
+  const uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const uint32_t nv = hi - lo;
+  if (nv == 0) return;
+  // Fewer voids than warps: each void's columns shared by warps / nv warps
+  // (a large sphere painted by one warp held every other block at the
+  // barrier after the paint).
+  const uint32_t parts = nv < warps ? min(warps / nv, 64u) : 1u;
+  for (uint32_t item = w; item < nv * parts; item += warps) {
+    const uint32_t i = __ldcg(acc + lo + item / parts);
+    paint_one(sv.cx[i], sv.cy[i], sv.cz[i], sv.r[i], mask, rc, lane, item % parts, parts);
   }
 }
 

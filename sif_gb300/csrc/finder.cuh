@@ -337,6 +337,7 @@ void commit_init(SurvivorsT<R> s, VoidViewT<R> voids, RungConstsT<R> rc, uint8_t
 // slots indexed by round % kRoundRing: the accepted count when the round
 // began (written by the previous round's paint), and the survivors the round
 // left undecided (zeroed by the host before each batch of rounds).
+constexpr uint32_t kCommitWork = 15;  // counters[]: the round's pass's next survivor
 constexpr uint32_t kRoundRing = 64;
 constexpr uint32_t kRoundBegin = 16;
 constexpr uint32_t kRoundUndecided = kRoundBegin + kRoundRing;
