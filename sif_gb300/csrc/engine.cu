@@ -345,8 +345,11 @@ void candidate_ranks(const K* delta, uint32_t m, uint32_t* rank, int threads) {
   thread_local std::vector<Rec<K>> keep;  // kept between calls, as the partition's scratch
   if (keep.size() < m) keep.resize(m);
   Rec<K>* const a = keep.data();  // the tasks reach it through this pointer
-  for (uint32_t k = 0; k < m; k++) a[k] = Rec<K>{delta[k], k};
   const int t = threads > 0 ? threads : omp_get_max_threads();
+  // The records and, after the sort, the ranks: independent per entry.
+  const bool wide = m > 2 * (uint32_t)kTaskCutoff && t > 1;
+#pragma omp parallel for num_threads(t) schedule(static) if (wide)
+  for (int64_t k = 0; k < (int64_t)m; k++) a[k] = Rec<K>{delta[k], (uint32_t)k};
   if (m > 2 * (uint32_t)kTaskCutoff && t > 1) {
     // The large segments partitioned one at a time on every thread, the
     // rest as tasks; disjoint segments, so the permutation is the serial one.
@@ -372,7 +375,8 @@ void candidate_ranks(const K* delta, uint32_t m, uint32_t* rank, int threads) {
   } else if (m > 1) {
     qsort_serial(a, 0, (int64_t)m - 1);
   }
-  for (uint32_t k = 0; k < m; k++) rank[a[k].i] = k;
+#pragma omp parallel for num_threads(t) schedule(static) if (wide)
+  for (int64_t k = 0; k < (int64_t)m; k++) rank[a[k].i] = (uint32_t)k;
 }
 
 template void candidate_ranks<float>(const float*, uint32_t, uint32_t*, int);
