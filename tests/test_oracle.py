@@ -75,8 +75,9 @@ def test_port_pipeline_reproduces_the_reference_run_on_workload_a(oracle):
 def test_port_runs_at_the_reference_release_build_speed(oracle):
     """The timed CPU baseline is the port's release-flags build: on workload A
     it takes about what the reference's own release build takes on the same
-    cores (median of three whole-path runs each; printed). A bound of 1.5x
-    leaves room for a loaded machine."""
+    cores (the fastest of five whole-path runs each; printed). A bound of
+    1.5x, measured again once before failing, leaves room for a loaded
+    machine."""
     import os
     import time
 
@@ -98,10 +99,13 @@ def test_port_runs_at_the_reference_release_build_speed(oracle):
 
     ref_run()
     port_run()
-    t_ref = sorted(ref_run() for _ in range(3))[1]
-    t_port = sorted(port_run() for _ in range(3))[1]
-    print(f"workload A on {threads} threads: port {t_port * 1e3:.1f} ms, reference release "
-          f"build {t_ref * 1e3:.1f} ms, ratio {t_port / t_ref:.3f}")
+    for attempt in range(2):
+        t_ref = min(ref_run() for _ in range(5))
+        t_port = min(port_run() for _ in range(5))
+        print(f"workload A on {threads} threads: port {t_port * 1e3:.1f} ms, reference release "
+              f"build {t_ref * 1e3:.1f} ms, ratio {t_port / t_ref:.3f}")
+        if t_port <= 1.5 * t_ref:
+            break
     assert t_port <= 1.5 * t_ref
 
 
