@@ -1926,7 +1926,7 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
   // when the run ends, not waited for: every stage indexes safely whatever
   // the positions, and a run over positions outside the box returns the
   // range error and no catalogue.
-  tm.mark_origin(s);
+  if (tm.timed) tm.mark_origin(s);
   unsigned long long* outside = (unsigned long long*)io.flag.ensure(16);
   SIFG_CUDA(cudaMemsetAsync(outside, 0, 16, s));
   R bounds[2];
@@ -1945,14 +1945,14 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
   io.mesh_scratch.ensure(mesh_scratch_bytes(n, mesh_cells) * sizeof(R) / sizeof(float));
   if constexpr (sizeof(R) == 4) {
     e->scratch.ensure(cic_scratch_bytes(n, n_grid));
-    cic_deposit(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic, bounds, outside,
-                e->ev_copy_start(), nullptr, &tm.cic_stage);
+    cic_deposit(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, tm.timed ? &tm.cic : nullptr,
+                bounds, outside, e->ev_copy_start(), nullptr, tm.timed ? &tm.cic_stage : nullptr);
   } else {
     box_check_kernel<R><<<grid_for(n, 256), 256, 0, s>>>(x, y, z, n, bounds[0], bounds[1], outside);
     SIFG_LAUNCH_CHECK();
     SIFG_CUDA(cudaEventRecord(e->ev_copy_start(), s));
     e->scratch.ensure(cic_f64_scratch_bytes(n_grid));
-    cic_deposit_f64(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, &tm.cic);
+    cic_deposit_f64(x, y, z, n, n_grid, box, dg, e->scratch.ptr, s, tm.timed ? &tm.cic : nullptr);
   }
   SIFG_CUDA(cudaStreamWaitEvent(cs, e->ev_copy_start(), 0));
   DeviceMeshT<R> m;
@@ -1972,7 +1972,7 @@ static int box_run(Engine* e, const R* x, const R* y, const R* z, uint64_t n, ui
       (size_t)scan_sums_needed((uint32_t)(mcells + 1)) * sizeof(uint32_t));
   // Only the sphere growth reads this mesh: its cells need not be in the
   // canonical order (a radius does not depend on the order within a cell).
-  mesh_build(x, y, z, n, m, io.mesh_scratch.ptr, cs, &tm.mesh, sums, false);
+  mesh_build(x, y, z, n, m, io.mesh_scratch.ptr, cs, tm.timed ? &tm.mesh : nullptr, sums, false);
   SIFG_CUDA(cudaEventRecord(e->ev_mesh_ready(), cs));
   // The mean only: the contrast is taken by the run's forward transform as it
   // reads the density (the grid is used for nothing else).
@@ -2038,6 +2038,7 @@ static void batch_job(Engine* e, sifg_box_job_t& j) {
       mc = sif_finder_suggest_mesh_cells(j.n_particles, j.box, rmax, 0.0f);
     }
     RunTimings tm;
+    tm.timed = false;
     j.status = box_run<float>(e, j.x, j.y, j.z, j.n_particles, j.n_grid, j.box, mc, j.radii,
                               j.n_radii, j.threshold, j.overlap, j.options, j.cx, j.cy, j.cz,
                               j.r, j.capacity, &j.n_voids, tm, nullptr);

@@ -442,6 +442,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
                    HostCatalogueT<R>& out, std::vector<RungStat>* stats, RunTimings* tm) {
   SmootherT<R>& smoother = smoother_for<R>();
   const auto t_start = std::chrono::steady_clock::now();
+  if (tm && !tm->timed) tm = nullptr;
   if (tm) tm->mark_origin(st_);
   // The run appends one entry to stats per rung it runs (from first_rung).
   const size_t stats0 = stats ? stats->size() : 0;

@@ -92,6 +92,9 @@ struct RunTimings {
   KernelTimer smoothing, rung;  // the timeline's stage spans
   KernelTimer cic_stage;        // the whole deposit: tile sort, deposit, faces
   cudaEvent_t origin = nullptr;  // the run's first event: the timeline's zero
+  // False: nothing is timed and no event is made (a batch job: event creation
+  // from several host threads at once serialises them).
+  bool timed = true;
   double wall_ms = 0.0;
   uint64_t growth_particles = 0, growth_cells = 0;  // gathered by the sphere growth
   void mark_origin(cudaStream_t st) {

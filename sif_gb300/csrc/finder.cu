@@ -182,11 +182,6 @@ __global__ void __launch_bounds__(kScanT) scan_write_kernel(
   }
 }
 
-__global__ void store_total_kernel(const uint32_t* __restrict__ offsets, uint32_t nb,
-                                   uint32_t* __restrict__ d_count) {
-  d_count[0] = offsets[nb];
-}
-
 // One pass over the field: each CTA writes its candidates, in flat order, to
 // the start of its own region of kScanChunk slots and its count to
 // counts[block]; the compaction then moves only the candidates.
@@ -290,10 +285,7 @@ void below_count_pass(const uint32_t* counts, const uint32_t* flat, uint32_t nb,
   const uint32_t warps = nb < 152u * 64u ? nb : 152u * 64u;
   below_count_kernel<<<(warps + 7) / 8, 256, 0, st>>>(counts, flat, nb, block, mask, block_counts);
   SIFG_LAUNCH_CHECK();
-  SIFG_CUDA(cudaMemsetAsync(block_counts + nb, 0, sizeof(uint32_t), st));
-  exclusive_scan_u32(block_counts, nb + 1, st);
-  store_total_kernel<<<1, 1, 0, st>>>(block_counts, nb, d_count);
-  SIFG_LAUNCH_CHECK();
+  exclusive_scan_total(block_counts, nb, d_count, st);
 }
 
 void below_write_pass(const uint32_t* counts, const float* delta, const uint32_t* flat,
@@ -314,10 +306,7 @@ void scan_fused_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R t
   scan_regions_kernel<R><<<nb, kScanT, 0, st>>>(field, mask, n_cells, threshold, block_counts,
                                                 region_delta, region_flat, grid_n, minima);
   SIFG_LAUNCH_CHECK();
-  SIFG_CUDA(cudaMemsetAsync(block_counts + nb, 0, sizeof(uint32_t), st));
-  exclusive_scan_u32(block_counts, nb + 1, st);
-  store_total_kernel<<<1, 1, 0, st>>>(block_counts, nb, d_count);
-  SIFG_LAUNCH_CHECK();
+  exclusive_scan_total(block_counts, nb, d_count, st);
 }
 
 template <class R>
@@ -339,10 +328,7 @@ void scan_count_pass(const R* field, const uint32_t* mask, uint64_t n_cells, R t
   scan_count_kernel<<<nb, kScanT, 0, st>>>(field, mask, n_cells, threshold, block_counts, grid_n,
                                            minima);
   SIFG_LAUNCH_CHECK();
-  SIFG_CUDA(cudaMemsetAsync(block_counts + nb, 0, sizeof(uint32_t), st));
-  exclusive_scan_u32(block_counts, nb + 1, st);
-  store_total_kernel<<<1, 1, 0, st>>>(block_counts, nb, d_count);
-  SIFG_LAUNCH_CHECK();
+  exclusive_scan_total(block_counts, nb, d_count, st);
 }
 
 template <class R>
@@ -763,10 +749,7 @@ void prefilter(const uint32_t* cand_flat, uint32_t m, const uint32_t* mask, Void
   const uint32_t nb = (m + kCompactChunk - 1) / kCompactChunk;
   flag_count_kernel<<<nb, kCompactT, 0, st>>>(alive, m, block_counts);
   SIFG_LAUNCH_CHECK();
-  SIFG_CUDA(cudaMemsetAsync(block_counts + nb, 0, sizeof(uint32_t), st));
-  exclusive_scan_u32(block_counts, nb + 1, st);
-  store_total_kernel<<<1, 1, 0, st>>>(block_counts, nb, d_surv_count);
-  SIFG_LAUNCH_CHECK();
+  exclusive_scan_total(block_counts, nb, d_surv_count, st);
   survivor_write_kernel<<<nb, kCompactT, 0, st>>>(alive, m, block_counts, cand_flat, rc,
                                                   surv_cand, surv_flat, scx, scy, scz, coff, soff);
   SIFG_LAUNCH_CHECK();

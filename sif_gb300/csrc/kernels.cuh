@@ -84,6 +84,10 @@ void mirror_clear();
 uint32_t scan_sums_needed(uint32_t n);
 void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st,
                         uint32_t* sums_scratch = nullptr);
+// data[0..nb) scanned exclusively in place, data[nb] set to their total and
+// *total (device) too; data[nb] need not be initialised. One launch up to
+// 32,767 entries.
+void exclusive_scan_total(uint32_t* data, uint32_t nb, uint32_t* total, cudaStream_t st);
 
 // --- cic.cu ---
 size_t cic_scratch_bytes(uint64_t n_particles, uint32_t n, bool weighted = false);

@@ -103,15 +103,19 @@ constexpr uint32_t kSmallChunks = 8;
 // Every chunk is loaded before the first is scanned: the loads of all
 // kSmallChunks chunks are in flight at once (the scans of the path's block
 // totals sit between dependent launches, so this CTA's latency is theirs).
+// last_zero: d[n - 1] is taken as 0 (not read); total, when set, receives the
+// sum of all n.
 __global__ void __launch_bounds__(kScanThreads) scan_small_kernel(uint32_t* __restrict__ d,
-                                                                  uint32_t n) {
+                                                                  uint32_t n, bool last_zero,
+                                                                  uint32_t* __restrict__ total_out) {
   __shared__ uint32_t ws[32];
   uint32_t v[kSmallChunks][kScanItems];
 #pragma unroll
   for (uint32_t c = 0; c < kSmallChunks; c++) {
     const uint32_t first = c * kScanChunk + threadIdx.x * kScanItems;
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) v[c][k] = first + k < n ? d[first + k] : 0u;
+    for (int k = 0; k < kScanItems; k++)
+      v[c][k] = first + k < n && !(last_zero && first + k == n - 1) ? d[first + k] : 0u;
   }
   uint32_t carry = 0;
 #pragma unroll
@@ -130,6 +134,12 @@ __global__ void __launch_bounds__(kScanThreads) scan_small_kernel(uint32_t* __re
     }
     carry += total;
   }
+  if (total_out && threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void store_last_kernel(const uint32_t* __restrict__ d, uint32_t i,
+                                  uint32_t* __restrict__ out) {
+  *out = d[i];
 }
 
 uint32_t scan_sums_needed(uint32_t n) { return (n + kScanChunk - 1) / kScanChunk; }
@@ -138,7 +148,7 @@ void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st, uint32_t* s
   if (n == 0) return;
   const uint32_t blocks = (n + kScanChunk - 1) / kScanChunk;
   if (blocks <= kSmallChunks) {
-    scan_small_kernel<<<1, kScanThreads, 0, st>>>(data, n);
+    scan_small_kernel<<<1, kScanThreads, 0, st>>>(data, n, false, nullptr);
     SIFG_LAUNCH_CHECK();
     return;
   }
@@ -150,6 +160,20 @@ void exclusive_scan_u32(uint32_t* data, uint32_t n, cudaStream_t st, uint32_t* s
   scan_sums_kernel<<<1, kScanThreads, 0, st>>>(s, blocks);
   SIFG_LAUNCH_CHECK();
   scan_apply_kernel<<<blocks, kScanThreads, 0, st>>>(data, n, s);
+  SIFG_LAUNCH_CHECK();
+}
+
+void exclusive_scan_total(uint32_t* data, uint32_t nb, uint32_t* total, cudaStream_t st) {
+  const uint32_t n = nb + 1;
+  if ((n + kScanChunk - 1) / kScanChunk <= kSmallChunks) {
+    // One launch: data[nb] taken as zero, the total written as the scan ends.
+    scan_small_kernel<<<1, kScanThreads, 0, st>>>(data, n, true, total);
+    SIFG_LAUNCH_CHECK();
+    return;
+  }
+  SIFG_CUDA(cudaMemsetAsync(data + nb, 0, sizeof(uint32_t), st));
+  exclusive_scan_u32(data, n, st);
+  store_last_kernel<<<1, 1, 0, st>>>(data, nb, total);
   SIFG_LAUNCH_CHECK();
 }
 
