@@ -404,6 +404,7 @@ void sif_system_finalise(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   noalloc_forget();
   drop_pending_timings();
+  event_pool_clear();
   mirror_clear();  // device memory goes with the engine; the switch stays
   g_engine.reset();
   host_pool_trim();

@@ -19,7 +19,11 @@ constexpr int kCicTile = 16;  // CIC tile side, in grid cells
 // mesh is refused with SIF_ERR_RANGE before anything is cubed.
 constexpr uint32_t kMaxMeshSide = 1625;
 
+// Destroys the timing events kept for reuse (before a device reset).
+void event_pool_clear();
+
 // Times a kernel with events on the stream it is launched on; accumulates.
+// Its events come from, and go back to, a pool kept per device.
 struct KernelTimer {
   std::vector<cudaEvent_t> starts, stops;
   int open = -1;

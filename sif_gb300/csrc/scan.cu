@@ -6,6 +6,10 @@
 // it is one CTA walking the chunks with a carry: one launch instead of three.
 #include <cuda_runtime.h>
 
+#include <map>
+#include <mutex>
+#include <vector>
+
 #include "kernels.cuh"
 
 namespace sifg {
@@ -194,20 +198,65 @@ void DevBuf::release() {
   bytes = 0;
 }
 
-void KernelTimer::begin(cudaStream_t st) {
+// Timing events are kept for reuse, per device, instead of being created and
+// destroyed for every span (a run records a few hundred). The pool and its
+// lock are never destroyed: timers held by static objects return their
+// events at exit, in no fixed order with other files' statics.
+static std::mutex& event_mu() {
+  static std::mutex* m = new std::mutex;
+  return *m;
+}
+static std::map<int, std::vector<cudaEvent_t>>& event_pool() {
+  static auto* p = new std::map<int, std::vector<cudaEvent_t>>;
+  return *p;
+}
+
+static cudaEvent_t take_event() {
+  int dev = 0;
+  SIFG_CUDA(cudaGetDevice(&dev));
+  {
+    std::lock_guard<std::mutex> lk(event_mu());
+    auto& pool = event_pool()[dev];
+    if (!pool.empty()) {
+      const cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+  }
   cudaEvent_t e;
   SIFG_CUDA(cudaEventCreate(&e));
-  SIFG_CUDA(cudaEventRecord(e, st));
+  return e;
+}
+
+static void give_event(cudaEvent_t e) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaEventDestroy(e);
+    return;
+  }
+  std::lock_guard<std::mutex> lk(event_mu());
+  event_pool()[dev].push_back(e);
+}
+
+void event_pool_clear() {
+  std::lock_guard<std::mutex> lk(event_mu());
+  for (auto& [dev, pool] : event_pool())
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  event_pool().clear();
+}
+
+void KernelTimer::begin(cudaStream_t st) {
+  const cudaEvent_t e = take_event();
   starts.push_back(e);
   open = (int)starts.size() - 1;
+  SIFG_CUDA(cudaEventRecord(e, st));
 }
 
 void KernelTimer::end(cudaStream_t st) {
-  cudaEvent_t e;
-  SIFG_CUDA(cudaEventCreate(&e));
-  SIFG_CUDA(cudaEventRecord(e, st));
+  const cudaEvent_t e = take_event();
   stops.push_back(e);
   open = -1;
+  SIFG_CUDA(cudaEventRecord(e, st));
 }
 
 double KernelTimer::total_ms() {
@@ -222,8 +271,8 @@ double KernelTimer::total_ms() {
 }
 
 void KernelTimer::reset() {
-  for (auto e : starts) cudaEventDestroy(e);
-  for (auto e : stops) cudaEventDestroy(e);
+  for (auto e : starts) give_event(e);
+  for (auto e : stops) give_event(e);
   starts.clear();
   stops.clear();
   open = -1;
