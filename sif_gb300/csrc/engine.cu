@@ -1030,7 +1030,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
                       tm ? &tm->growth : nullptr, kAllSurvivors, work);
       else
         grow(mv, tv, rc, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_, tm ? &tm->growth : nullptr,
-             kAllSurvivors, work);
+             kAllSurvivors, work, grow_to<uint32_t>(pend_, m));
       // Each level of the extended reach, for the survivors whose crossing
       // still lies past the reach (exodus_finder.c:2060-2072).
       for (uint32_t e = ext0; e < n_ext; e++) {
@@ -1040,7 +1040,7 @@ int Engine::exodus(const R* d_delta, const DeviceMeshT<R>& mesh, const RunParams
                         tm ? &tm->growth : nullptr, kRescaleBeyondSearch, work);
         else
           grow(mv, ext_tv[e], ec, sv, m, gbuf, kGrowCap, traffic + 2 * ri, st_,
-               tm ? &tm->growth : nullptr, kRescaleBeyondSearch, work);
+               tm ? &tm->growth : nullptr, kRescaleBeyondSearch, work, grow_to<uint32_t>(pend_, m));
       }
     }
 

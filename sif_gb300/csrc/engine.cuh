@@ -191,6 +191,7 @@ class Engine {
   DevBuf surv_cand_, surv_flat_, scx_, scy_, scz_, sr_, sreason_, state_a_, state_b_, acc_;
   DevBuf commit_bar_;  // the cooperative commit's grid barrier and its report
   DevBuf counters_, dcount_, sgrid_start_, sgrid_ids_, sgrid_cellof_, sgrid_pack_, sgrid_rank_;
+  DevBuf pend_;  // the sphere growth's warp-kernel leftovers
   DevBuf cat_x_, cat_y_, cat_z_, cat_r_, vstart_, vids_, vcell_;
   DevBuf vhead_, vnext_, dlist_;  // displacement: the linked void index, its lists
   DevBuf work_;  // the sphere growth's and the witness's survivor queues

@@ -1039,7 +1039,9 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
                                                            RungConstsT<R> rc, SurvivorsT<R> sv,
                                                            R* __restrict__ gbuf, uint32_t gcap,
                                                            unsigned long long* __restrict__ traffic,
-                                                           uint8_t only, uint32_t* work) {
+                                                           uint8_t only, uint32_t* work,
+                                                           const uint32_t* __restrict__ list = nullptr,
+                                                           const uint32_t* __restrict__ list_count = nullptr) {
   __shared__ uint32_t bins[kMaxBins];
   __shared__ uint32_t below[kMaxBins];  // particles inside bin b's lower edge
   __shared__ R sbuf[kSmemBuf];
@@ -1054,7 +1056,10 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_kernel(MeshViewT<R> mesh, Te
   R* my_gbuf = gbuf + (uint64_t)blockIdx.x * gcap;
   __shared__ uint32_t s_item;
 
-  for (uint32_t s = next_cta_item(work, &s_item); s < n_surv; s = next_cta_item(work, &s_item)) {
+  // With a list, only the survivors it names (the warp kernel's leftovers).
+  const uint32_t n_items = list ? *list_count : n_surv;
+  for (uint32_t k = next_cta_item(work, &s_item); k < n_items; k = next_cta_item(work, &s_item)) {
+    const uint32_t s = list ? list[k] : k;
     if (only != kAllSurvivors ? sv.reason[s] != only : sv.reason[s] == kRescaleWitness) continue;
     const R cx = sv.cx[s], cy = sv.cy[s], cz = sv.cz[s];
     const int32_t ci = (int32_t)fmul(cx, mesh.inv_l), cj = (int32_t)fmul(cy, mesh.inv_l),
@@ -1299,7 +1304,7 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
                                                              uint32_t nb_stride, uint32_t shell_cap,
                                                              uint8_t only,
                                                              unsigned long long* __restrict__ traffic,
-                                                             uint32_t* work) {
+                                                             uint32_t* work, uint32_t* __restrict__ pend) {
   extern __shared__ unsigned char warp_smem[];
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   unsigned char* base = warp_smem + warp * warp_slice_bytes<R>(nb_stride, shell_cap);
@@ -1499,6 +1504,8 @@ __global__ void __launch_bounds__(kGrowT, 4) growth_warp_kernel(MeshViewT<R> mes
     if (lane == 0) {
       sv.r[s] = reason == kRescaleOk ? radius : -1.0f;
       sv.reason[s] = reason;
+      // A leftover for the per-CTA pass, listed (work[2] counts them).
+      if (reason == kRescalePending && pend) pend[atomicAdd(work + 2, 1u)] = s;
     }
     __syncwarp();
   }
@@ -1729,11 +1736,11 @@ constexpr uint32_t kShellListMax = 512;  // entries of a warp's shell list, at m
 template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s, uint32_t max_survivors,
           R* gbuf, uint32_t gcap, unsigned long long* traffic, cudaStream_t st,
-          KernelTimer* timer, uint8_t only, uint32_t* work) {
+          KernelTimer* timer, uint8_t only, uint32_t* work, uint32_t* pend) {
   if (max_survivors == 0) return;
   // work[0] for the first launch, work[1] for the per-CTA pass after the
-  // warp kernel.
-  SIFG_CUDA(cudaMemsetAsync(work, 0, 2 * sizeof(uint32_t), st));
+  // warp kernel, work[2] the warp kernel's leftovers listed in pend.
+  SIFG_CUDA(cudaMemsetAsync(work, 0, 3 * sizeof(uint32_t), st));
   const bool by_warp = g_growth_mode == 2 || (g_growth_mode == 0 && max_survivors >= kWarpGrowthMin);
   const unsigned g = max_survivors < growth_grid() ? max_survivors : growth_grid();
   if (timer) timer->begin(st);
@@ -1765,11 +1772,13 @@ void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT
     const uint32_t cap = 152u * (uint32_t)std::max(per_sm, 1);
     growth_warp_kernel<R><<<std::min(warps_needed, cap), kGrowT, smem, st>>>(mesh, tpl, rc, s,
                                                                             nb_stride, shell_cap,
-                                                                            only, traffic, work);
+                                                                            only, traffic, work, pend);
     SIFG_LAUNCH_CHECK();
-    // The survivors whose windows were too wide for a warp.
+    // The survivors whose windows were too wide for a warp: from the warp
+    // kernel's list when there is one (a CTA taking every survivor in turn
+    // to find the few left over cost a round trip each), else by their state.
     growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, kRescalePending,
-                                        work + 1);
+                                        work + 1, pend, pend ? work + 2 : nullptr);
     SIFG_LAUNCH_CHECK();
   } else {
     growth_kernel<<<g, kGrowT, 0, st>>>(mesh, tpl, rc, s, gbuf, gcap, traffic, only, work);
@@ -3585,7 +3594,7 @@ void compact_voids(R* cx, R* cy, R* cz, R* r, uint32_t* state, cudaStream_t st) 
                            uint32_t*);                                                              \
   template void grow<R>(MeshViewT<R>, TemplateViewT<R>, RungConstsT<R>, SurvivorsT<R>, uint32_t,   \
                         R*, uint32_t, unsigned long long*, cudaStream_t, KernelTimer*, uint8_t,    \
-                        uint32_t*);                                                                \
+                        uint32_t*, uint32_t*);                                                     \
   template void build_survivor_grid<R>(const R*, const R*, const R*, const R*, const uint32_t*,    \
                                        uint32_t, int32_t, R, uint32_t*, uint32_t*, uint32_t*,      \
                                        SurvPackT<R>*, cudaStream_t);                               \

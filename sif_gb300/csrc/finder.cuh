@@ -247,7 +247,8 @@ unsigned growth_grid();
 template <class R>
 void grow(MeshViewT<R> mesh, TemplateViewT<R> tpl, RungConstsT<R> rc, SurvivorsT<R> s,
           uint32_t max_survivors, R* gbuf, uint32_t gcap, unsigned long long* traffic,
-          cudaStream_t st, KernelTimer* timer, uint8_t only, uint32_t* work);
+          cudaStream_t st, KernelTimer* timer, uint8_t only, uint32_t* work,
+          uint32_t* pend = nullptr);
 // The weighted sphere growth (sif__exodus_find_radius_weighted,
 // exodus_rescale.c:642-1037 with the weighted flag): mesh.w set. A CTA per
 // survivor; gbuf and gwbuf (gcap entries per CTA each) hold the windows too
